@@ -1,0 +1,206 @@
+/*
+ * rich_gb300.h -- C ABI of the GB300 (sm_103a) hydro hot path of RICH.
+ *
+ * The library replaces, on one GPU, the per-step work that RICH's hdsim does
+ * through five plugin interfaces:
+ *
+ *   FluxCalculator        source/newtonian/two_dimensional/flux_calculator_2d.hpp:35-44
+ *     SimpleFluxCalculator   simple_flux_calculator.cpp:216-244  (order 1)
+ *     ModularFluxCalculator  modular_flux_calculator.cpp:39-71   (order 2)
+ *   SpatialReconstruction spatial_reconstruction.hpp:37-42
+ *     LinearGaussImproved    interpolations/LinearGaussImproved.cpp:536-635
+ *   RiemannSolver         source/newtonian/common/riemann_solver.hpp:22-23
+ *     Hllc (massflux=true)   source/newtonian/common/hllc.cpp:97-154
+ *   ExtensiveUpdater      extensive_updater.hpp:34-43
+ *     SimpleExtensiveUpdater simple_extensive_updater.cpp:11-35
+ *   CellUpdater           cell_updater_2d.hpp:34-41
+ *     SimpleCellUpdater      simple_cell_updater.cpp:85-106
+ *   TimeStepFunction      time_step_function.hpp:29-35
+ *     SimpleCFL              simple_cfl.cpp:58-71
+ *   EquationOfState       source/newtonian/common/equation_of_state.hpp:20-85
+ *     IdealGas               source/newtonian/common/ideal_gas.cpp:13-44
+ *
+ * Conventions
+ *  - Every function returns rg_status and never throws.  Physical failures
+ *    that the reference reports by throwing UniversalError are returned as
+ *    the matching RG_ERR_* code; rg_last_error() gives the cell or face index
+ *    and the offending value, as the reference's AddEntry diagnostics do.
+ *  - Host arrays passed in are borrowed for the duration of the call only.
+ *    Device memory is owned by the handle.
+ *  - A handle is not thread-safe (like the reference's const plugins, which
+ *    mutate mutable caches); use one handle per simulation.
+ *  - Cell records are 4 doubles {density, pressure, velocity.x, velocity.y}
+ *    (ComputationalCell order); extensive records are 4 doubles
+ *    {mass, energy, momentum.x, momentum.y} (Extensive order); face fluxes
+ *    use the extensive layout.
+ */
+#ifndef RICH_GB300_H
+#define RICH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum rg_status {
+  RG_OK = 0,
+  RG_ERR_INVALID_ARGUMENT = 1,
+  RG_ERR_CUDA = 2,
+  RG_ERR_NOT_READY = 3,          /* call order violated (e.g. flux before mesh) */
+  RG_ERR_OUT_OF_MEMORY = 4,
+  /* physical failures, same conditions as the reference's UniversalError */
+  RG_ERR_NEGATIVE_DENSITY = 10,  /* simple_cell_updater.cpp:33-34 "Negative density" */
+  RG_ERR_NEGATIVE_ENERGY = 11,   /* ideal_gas.cpp:20-21 "Negative thermal energy" */
+  RG_ERR_HLLC_NAN = 12,          /* hllc.cpp:102-103 "Hllc::Solved entered with nan" */
+  RG_ERR_HLLC_WAVE_SPEEDS = 13,  /* hllc.cpp:142-148 "Invalid wave speeds in hllc solver" */
+  RG_ERR_SINGULAR_MATRIX = 14,   /* LinearGaussImproved.cpp:111-119 "Singular matrix" */
+  RG_ERR_TOO_MANY_NEIGHBORS = 15 /* LinearGaussImproved.cpp:73-79 "Cell has too many neighbors" */
+} rg_status;
+
+/* First failure of the last call.  index is a cell index for density,
+ * energy, slope errors and a face (edge) index for HLLC errors; value is the
+ * offending quantity (density, thermal energy, determinant, ...). */
+typedef struct rg_error {
+  int32_t status;
+  int32_t phase;   /* 1 cfl, 2 slopes, 3 faces, 4 extensive update, 5 cell update, 6 geometry */
+  int64_t index;
+  double value;
+} rg_error;
+
+/* LinearGaussImproved's GhostPointGenerator (its `ghost_` member). */
+typedef enum rg_ghost_kind {
+  RG_GHOST_RIGID_WALL = 0, /* RigidWallGenerator.cpp:17-54 */
+  RG_GHOST_PERIODIC = 1    /* PeriodicGhostGenerator.cpp:3-24 */
+} rg_ghost_kind;
+
+typedef enum rg_precision {
+  RG_FP64 = 0,      /* plain FP64: every operation in the reference's order */
+  RG_FP32_MIXED = 1 /* reconstruction + HLLC in FP32; geometry, volumes,
+                       extensive accumulation and e = E/m - v^2/2 in FP64 */
+} rg_precision;
+
+typedef struct rg_config {
+  double gamma;          /* IdealGas adiabatic index (ideal_gas.cpp:5-6) */
+  double cfl;            /* SimpleCFL cfl number (simple_cfl.cpp:8) */
+  int32_t order;         /* 1: SimpleFluxCalculator; 2: ModularFluxCalculator(LinearGaussImproved, Hllc) */
+  int32_t ghost_kind;    /* rg_ghost_kind, used by order 2 */
+  int32_t slope_limiter; /* LinearGaussImproved slf (LinearGaussImproved.hpp:31-40), default 1 */
+  int32_t precision;     /* rg_precision */
+  double delta_v;        /* LinearGaussImproved shockratio_, default 0.2 */
+  double theta;          /* LinearGaussImproved diffusecoeff_, default 0.5 */
+  double delta_p;        /* LinearGaussImproved pressure_ratio_, default 0.7 */
+  int32_t device;        /* CUDA device ordinal */
+  int32_t reserved;
+} rg_config;
+
+/* Fills *cfg with the reference's constructor defaults: Hllc(), SimpleCFL(0.3),
+ * LinearGaussImproved(eos, ghost) defaults, IdealGas(5/3), order 2, FP64. */
+void rg_default_config(rg_config* cfg);
+
+/*
+ * A tessellation packed into flat arrays (what a Tessellation + CacheData
+ * give the hot path).  Point ids: real cells are 0..n_cells-1; ghost
+ * (mirror / periodic) points are n_cells..n_cells+n_ghosts-1.  The adapter
+ * in huji-rich_gb300/host/rich_pack.hpp builds this from a VoronoiMesh.
+ *
+ *   point_xy      (n_cells+n_ghosts)*2  Tessellation::GetMeshPoint
+ *   cm_xy         (n_cells+n_ghosts)*2  Tessellation::GetCellCM (ghost CMs are
+ *                                       the reflected / shifted ones, VoronoiMesh.cpp:355-398)
+ *   volume        n_cells   Tessellation::GetVolume (mesh-point fan, VoronoiMesh.cpp:420-434)
+ *   cd_volume     n_cells   CacheData::volumes = SlabSymmetry::calcVolume (physical_geometry.cpp:13-21)
+ *   ghost_source  n_ghosts  Tessellation::GetOriginalIndex of each ghost
+ *   ghost_face    n_ghosts  first face (ascending) touching the ghost, -1 if none
+ *                           (the entry RigidWallGenerator's flat_map keeps)
+ *   face_cells    n_faces*2 Edge::neighbors (first, second) as point ids
+ *   face_vertices n_faces*4 Edge::vertices (first.x, first.y, second.x, second.y)
+ *   cell_face_offset n_cells+1, cell_faces: Tessellation::GetCellEdges, which
+ *                 VoronoiMesh::build_v fills in ascending face order
+ */
+typedef struct rg_mesh_view {
+  int32_t n_cells;
+  int32_t n_ghosts;
+  int32_t n_faces;
+  int32_t reserved;
+  const double* point_xy;
+  const double* cm_xy;
+  const double* volume;
+  const double* cd_volume;
+  const int32_t* ghost_source;
+  const int32_t* ghost_face;
+  const int32_t* face_cells;
+  const double* face_vertices;
+  const int32_t* cell_face_offset;
+  const int32_t* cell_faces;
+} rg_mesh_view;
+
+/* Device addresses of the handle's state, for callers that keep data on the
+ * GPU (all valid until the next rg_upload_mesh or rg_destroy). */
+typedef struct rg_device_view {
+  double* cells;           /* n_cells*4 */
+  double* extensives;      /* n_cells*4 */
+  double* edge_velocities; /* n_faces*2 */
+  double* fluxes;          /* n_faces*4, last rg_flux result (unscaled) */
+  void* stream;            /* cudaStream_t all kernels of the handle run on */
+} rg_device_view;
+
+/* Upload flags */
+#define RG_MESH_STATIC 1u /* mesh will not change: later uploads may be skipped by the caller */
+
+typedef struct rg_handle rg_handle;
+
+/* Lifecycle ---------------------------------------------------------------- */
+rg_status rg_create(const rg_config* cfg, rg_handle** out);
+rg_status rg_destroy(rg_handle* h);
+const char* rg_status_string(rg_status s);
+rg_status rg_last_error(const rg_handle* h, rg_error* err);
+
+/* Mesh --------------------------------------------------------------------- */
+/* Copies the mesh to the device through pinned staging buffers on the upload
+ * stream and computes all geometry-only terms there (face normals, lengths,
+ * widths, gradient matrices).  Returns RG_ERR_SINGULAR_MATRIX /
+ * RG_ERR_TOO_MANY_NEIGHBORS only when the reconstruction would throw for it
+ * (order 2); the error is also returned by the next rg_flux, which is where
+ * the reference throws it. */
+rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* mesh, uint32_t flags);
+/* Milliseconds the last upload took (host->device copies + geometry pass). */
+rg_status rg_last_upload_ms(const rg_handle* h, double* ms);
+
+/* State -------------------------------------------------------------------- */
+rg_status rg_set_cells(rg_handle* h, const double* cells);
+rg_status rg_get_cells(rg_handle* h, double* cells);
+rg_status rg_set_extensives(rg_handle* h, const double* extensives);
+rg_status rg_get_extensives(rg_handle* h, double* extensives);
+rg_status rg_set_edge_velocities(rg_handle* h, const double* edge_velocities);
+rg_status rg_device_buffers(rg_handle* h, rg_device_view* view);
+/* hdsim's init_extensives (hdsim2d.cpp:41-67): extensives from cells and cd_volume. */
+rg_status rg_init_extensives(rg_handle* h);
+
+/* The five plugin operations ---------------------------------------------- */
+/* SimpleCFL::operator() on the current cells and edge velocities. */
+rg_status rg_cfl_dt(rg_handle* h, double* dt);
+/* FluxCalculator::operator(): per-face fluxes (unscaled, as the reference
+ * returns them).  fluxes_out (n_faces*4, host) may be NULL to keep them on
+ * the device only. */
+rg_status rg_flux(rg_handle* h, double dt, double* fluxes_out);
+/* Upload caller-provided fluxes (n_faces*4) in place of the last rg_flux. */
+rg_status rg_set_fluxes(rg_handle* h, const double* fluxes);
+/* SimpleExtensiveUpdater::operator(): extensives += gathered dt*area*flux,
+ * in ascending face order per cell (no atomics). */
+rg_status rg_extensive_update(rg_handle* h, double dt);
+/* SimpleCellUpdater::operator(): cells from extensives and cd_volume. */
+rg_status rg_cell_update(rg_handle* h);
+
+/* hdsim::TimeAdvance's hot path fused on the device (hdsim2d.cpp:149-241 with
+ * a fixed mesh): dt = SimpleCFL, fluxes, extensive update, cell update.  dt
+ * never leaves the device between the passes; *dt_out receives it. */
+rg_status rg_step(rg_handle* h, double* dt_out);
+/* n_steps rg_step calls without a host synchronisation between them; errors
+ * are checked once at the end.  dt_out (n_steps, host) may be NULL. */
+rg_status rg_run(rg_handle* h, int32_t n_steps, double* dt_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RICH_GB300_H */

@@ -1,0 +1,156 @@
+"""ctypes binding of the C parity oracle (rich_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg, as the checker.  Never used by the product.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+LIB = os.path.join(HERE, "liboracle.so")
+
+
+def build(force=False):
+    """Compile rich_oracle.c with gcc (no FMA contraction)."""
+    src = os.path.join(HERE, "rich_oracle.c")
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(
+            os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "rich_oracle.h"))):
+        return LIB
+    subprocess.check_call(["gcc", "-O2", "-std=c99", "-ffp-contract=off", "-fno-fast-math",
+                           "-fPIC", "-shared", "-Wall", "-I" + os.path.join(ROOT, "include"),
+                           src, "-o", LIB + ".tmp", "-lm"])
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+class RoError(C.Structure):
+    _fields_ = [("status", C.c_int32), ("phase", C.c_int32), ("index", C.c_int64),
+                ("value", C.c_double)]
+
+
+class RoLgiParams(C.Structure):
+    _fields_ = [("ghost_kind", C.c_int32), ("slf", C.c_int32), ("delta_v", C.c_double),
+                ("theta", C.c_double), ("delta_p", C.c_double)]
+
+
+class OracleError(RuntimeError):
+    def __init__(self, err):
+        self.status, self.phase, self.index, self.value = err.status, err.phase, err.index, err.value
+        super().__init__(f"oracle status {err.status} phase {err.phase} index {err.index} value {err.value}")
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = C.CDLL(LIB)
+    return _lib
+
+
+def _d(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _f64(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a if shape is None else a.reshape(shape)
+
+
+def _check(st, err):
+    if st:
+        raise OracleError(err)
+
+
+def lgi_params(ghost_kind=0, slf=1, delta_v=0.2, theta=0.5, delta_p=0.7):
+    return RoLgiParams(ghost_kind, slf, delta_v, theta, delta_p)
+
+
+def cfl(mesh, cells, ev, gamma, cfl_number=0.3):
+    cells, ev = _f64(cells), _f64(ev)
+    dt = C.c_double()
+    err = RoError()
+    _check(lib().ro_cfl(C.byref(mesh.view()), _d(cells), _d(ev), C.c_double(gamma),
+                        C.c_double(cfl_number), C.byref(dt), C.byref(err)), err)
+    return dt.value
+
+
+def simple_flux(mesh, cells, ev, gamma):
+    out = np.zeros((mesh.n_faces, 4))
+    err = RoError()
+    cells, ev = _f64(cells), _f64(ev)
+    _check(lib().ro_simple_flux(C.byref(mesh.view()), _d(cells), _d(ev), C.c_double(gamma),
+                                _d(out), C.byref(err)), err)
+    return out
+
+
+def lgi(mesh, cells, gamma, lp):
+    slopes = np.zeros((mesh.n_cells, 8))
+    interp = np.zeros((mesh.n_faces, 8))
+    err = RoError()
+    cells = _f64(cells)
+    _check(lib().ro_lgi(C.byref(mesh.view()), _d(cells), C.c_double(gamma), C.byref(lp),
+                        _d(slopes), _d(interp), C.byref(err)), err)
+    return slopes, interp
+
+
+def modular_flux(mesh, cells, ev, gamma, lp):
+    out = np.zeros((mesh.n_faces, 4))
+    err = RoError()
+    cells, ev = _f64(cells), _f64(ev)
+    _check(lib().ro_modular_flux(C.byref(mesh.view()), _d(cells), _d(ev), C.c_double(gamma),
+                                 C.byref(lp), _d(out), C.byref(err)), err)
+    return out
+
+
+def extensive_update(mesh, fluxes, dt, ext):
+    ext = _f64(ext).copy()
+    err = RoError()
+    fluxes = _f64(fluxes)
+    _check(lib().ro_extensive_update(C.byref(mesh.view()), _d(fluxes), C.c_double(dt), _d(ext),
+                                     C.byref(err)), err)
+    return ext
+
+
+def cell_update(mesh, ext, gamma):
+    out = np.zeros((mesh.n_cells, 4))
+    err = RoError()
+    ext = _f64(ext)
+    _check(lib().ro_cell_update(C.byref(mesh.view()), _d(ext), C.c_double(gamma), _d(out),
+                                C.byref(err)), err)
+    return out
+
+
+def init_extensives(mesh, cells, gamma):
+    out = np.zeros((mesh.n_cells, 4))
+    cells = _f64(cells)
+    lib().ro_init_extensives(C.byref(mesh.view()), _d(cells), C.c_double(gamma), _d(out))
+    return out
+
+
+def step(mesh, cells, ext, ev, gamma, cfl_number=0.3, order=2, lp=None):
+    """One fixed-mesh hot-path pass; returns (cells, ext, dt)."""
+    cells = _f64(cells).copy()
+    ext = _f64(ext).copy()
+    ev = _f64(ev)
+    lp = lp or lgi_params()
+    dt = C.c_double()
+    err = RoError()
+    _check(lib().ro_step(C.byref(mesh.view()), _d(cells), _d(ext), _d(ev), C.c_double(gamma),
+                         C.c_double(cfl_number), C.c_int(order), C.byref(lp), C.byref(dt),
+                         C.byref(err)), err)
+    return cells, ext, dt.value
+
+
+def run(mesh, cells, ext, ev, gamma, steps, cfl_number=0.3, order=2, lp=None):
+    dts = []
+    for _ in range(steps):
+        cells, ext, dt = step(mesh, cells, ext, ev, gamma, cfl_number, order, lp)
+        dts.append(dt)
+    return cells, ext, np.array(dts)

@@ -1,0 +1,343 @@
+// ref_dump.cpp -- runs the reference RICH hot path on a seeded case and
+// writes its inputs and outputs as .npy files, which
+// tests/golden/make_golden.py bundles into tests/golden/<case>.npz.
+//
+// Test infrastructure only: it links the reference sources built by
+// oracle/ref/Makefile and is never part of the product.
+//
+//   ref_dump <case> <outdir> <nx> <ny> <warm_steps> <run_steps>
+//
+// For every case it writes, for the state reached after <warm_steps>
+// hdsim::TimeAdvance steps (hdsim2d.cpp:149-241):
+//   mesh_*          the packed tessellation (huji-rich_gb300/host/rich_pack.hpp)
+//   cells0, ext0    ComputationalCell / Extensive state
+//   ev_cfl, dt      edge velocities given to SimpleCFL and its dt (hdsim2d.cpp:161-165)
+//   ev_flux         edge velocities after PointMotion::ApplyFix (hdsim2d.cpp:167-174)
+//   slopes, interp  LinearGaussImproved slopes and per-edge states (order 2)
+//   fluxes          FluxCalculator output (hdsim2d.cpp:176-184)
+//   ext1            after SimpleExtensiveUpdater (hdsim2d.cpp:188-195)
+//   cells1          SimpleCellUpdater on ext1 with the same mesh
+// and, when <run_steps> > 0, the state after that many further
+// hdsim::TimeAdvance steps (run_cells, run_ext, run_time, run_times).
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <random>
+#include <string>
+
+#include "rich_pack.hpp"
+#include "source/newtonian/common/hllc.hpp"
+#include "source/newtonian/common/ideal_gas.hpp"
+#include "source/newtonian/two_dimensional/geometric_outer_boundaries/PeriodicBox.hpp"
+#include "source/newtonian/two_dimensional/geometric_outer_boundaries/SquareBox.hpp"
+#include "source/newtonian/two_dimensional/ghost_point_generators/PeriodicGhostGenerator.hpp"
+#include "source/newtonian/two_dimensional/ghost_point_generators/RigidWallGenerator.hpp"
+#include "source/newtonian/two_dimensional/hdsim2d.hpp"
+#include "source/newtonian/two_dimensional/interpolations/LinearGaussImproved.hpp"
+#include "source/newtonian/two_dimensional/modular_flux_calculator.hpp"
+#include "source/newtonian/two_dimensional/periodic_edge_velocities.hpp"
+#include "source/newtonian/two_dimensional/point_motions/eulerian.hpp"
+#include "source/newtonian/two_dimensional/point_motions/lagrangian.hpp"
+#include "source/newtonian/two_dimensional/point_motions/round_cells.hpp"
+#include "source/newtonian/two_dimensional/simple_cell_updater.hpp"
+#include "source/newtonian/two_dimensional/simple_cfl.hpp"
+#include "source/newtonian/two_dimensional/simple_extensive_updater.hpp"
+#include "source/newtonian/two_dimensional/simple_flux_calculator.hpp"
+#include "source/newtonian/two_dimensional/source_terms/zero_force.hpp"
+#include "source/newtonian/two_dimensional/stationary_box.hpp"
+#include "source/tessellation/VoronoiMesh.hpp"
+
+namespace {
+
+std::string g_out;
+
+void write_npy(const std::string& name, const char* descr, size_t elem, const void* data,
+               size_t rows, size_t cols) {
+  std::string path = g_out + "/" + name + ".npy";
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (!f) throw std::runtime_error("cannot open " + path);
+  char shape[64];
+  if (cols == 0)
+    std::snprintf(shape, sizeof shape, "(%zu,)", rows);
+  else
+    std::snprintf(shape, sizeof shape, "(%zu, %zu)", rows, cols);
+  std::string hdr = std::string("{'descr': '") + descr + "', 'fortran_order': False, 'shape': " +
+                    shape + ", }";
+  while ((10 + hdr.size() + 1) % 64 != 0) hdr += ' ';
+  hdr += '\n';
+  const unsigned char magic[8] = {0x93, 'N', 'U', 'M', 'P', 'Y', 1, 0};
+  std::fwrite(magic, 1, 8, f);
+  const uint16_t hl = static_cast<uint16_t>(hdr.size());
+  std::fwrite(&hl, 2, 1, f);
+  std::fwrite(hdr.data(), 1, hdr.size(), f);
+  std::fwrite(data, elem, rows * (cols ? cols : 1), f);
+  std::fclose(f);
+}
+
+void dump_f64(const std::string& n, const std::vector<double>& v, size_t cols) {
+  write_npy(n, "<f8", 8, v.data(), cols ? v.size() / cols : v.size(), cols);
+}
+void dump_i32(const std::string& n, const std::vector<int32_t>& v, size_t cols) {
+  write_npy(n, "<i4", 4, v.data(), cols ? v.size() / cols : v.size(), cols);
+}
+void dump_scalar(const std::string& n, double x) { write_npy(n, "<f8", 8, &x, 1, 0); }
+
+std::vector<double> cells_flat(const std::vector<ComputationalCell>& c) {
+  std::vector<double> r;
+  for (const auto& x : c) {
+    r.push_back(x.density);
+    r.push_back(x.pressure);
+    r.push_back(x.velocity.x);
+    r.push_back(x.velocity.y);
+  }
+  return r;
+}
+std::vector<double> ext_flat(const std::vector<Extensive>& e) {
+  std::vector<double> r;
+  for (const auto& x : e) {
+    r.push_back(x.mass);
+    r.push_back(x.energy);
+    r.push_back(x.momentum.x);
+    r.push_back(x.momentum.y);
+  }
+  return r;
+}
+std::vector<double> vec_flat(const std::vector<Vector2D>& v) {
+  std::vector<double> r;
+  for (const auto& x : v) {
+    r.push_back(x.x);
+    r.push_back(x.y);
+  }
+  return r;
+}
+
+void dump_mesh(const std::string& prefix, const Tessellation& tess, const PhysicalGeometry& pg) {
+  CacheData cd(tess, pg);
+  rich_gb300::PackedMesh m;
+  rich_gb300::pack_tessellation(tess, cd, m);
+  dump_f64(prefix + "point_xy", m.point_xy, 2);
+  dump_f64(prefix + "cm_xy", m.cm_xy, 2);
+  dump_f64(prefix + "volume", m.volume, 0);
+  dump_f64(prefix + "cd_volume", m.cd_volume, 0);
+  dump_i32(prefix + "ghost_source", m.ghost_source, 0);
+  dump_i32(prefix + "ghost_face", m.ghost_face, 0);
+  dump_i32(prefix + "face_cells", m.face_cells, 2);
+  dump_f64(prefix + "face_vertices", m.face_vertices, 4);
+  dump_i32(prefix + "cell_face_offset", m.cell_face_offset, 0);
+  dump_i32(prefix + "cell_faces", m.cell_faces, 0);
+}
+
+std::vector<Vector2D> jittered_lattice(int nx, int ny, double x0, double x1, double y0, double y1,
+                                       unsigned seed, double jitter) {
+  std::mt19937_64 gen(seed);
+  std::uniform_real_distribution<double> u(-jitter, jitter);
+  std::vector<Vector2D> r;
+  const double dx = (x1 - x0) / nx, dy = (y1 - y0) / ny;
+  for (int i = 0; i < nx; ++i)
+    for (int j = 0; j < ny; ++j) {
+      const double ux = u(gen), uy = u(gen);
+      r.push_back(Vector2D(x0 + (i + 0.5 + ux) * dx, y0 + (j + 0.5 + uy) * dy));
+    }
+  return r;
+}
+
+// One hot-path pass on a fixed mesh, in hdsim::TimeAdvance's order.
+void dump_components(hdsim& sim, const PhysicalGeometry& pg, const EquationOfState& eos,
+                     const PointMotion& pm, const EdgeVelocityCalculator& evc,
+                     const TimeStepFunction& tsf, const FluxCalculator& fc,
+                     const ExtensiveUpdater& eu, const CellUpdater& cu,
+                     const LinearGaussImproved* lgi) {
+  const Tessellation& tess = sim.getTessellation();
+  const vector<ComputationalCell>& cells = sim.getAllCells();
+  const vector<Extensive>& ext = sim.getAllExtensives();
+  const TracerStickerNames& tsn = sim.GetTracerStickerNames();
+  const double t = sim.getTime();
+  dump_mesh("mesh_", tess, pg);
+  dump_f64("cells0", cells_flat(cells), 4);
+  dump_f64("ext0", ext_flat(ext), 4);
+  dump_scalar("time0", t);
+  vector<Vector2D> pv = pm(tess, cells, t, tsn);
+  vector<Vector2D> ev = evc(tess, pv);
+  const double dt = tsf(tess, cells, eos, ev, t, tsn);
+  dump_f64("ev_cfl", vec_flat(ev), 2);
+  dump_scalar("dt", dt);
+  pv = pm.ApplyFix(tess, cells, t, dt, pv, tsn);
+  ev = evc(tess, pv);
+  dump_f64("ev_flux", vec_flat(ev), 2);
+  CacheData cd(tess, pg);
+  if (lgi) {
+    vector<pair<ComputationalCell, ComputationalCell> > interp(
+        static_cast<size_t>(tess.GetTotalSidesNumber()),
+        pair<ComputationalCell, ComputationalCell>(cells[0], cells[0]));
+    (*lgi)(tess, cells, t, interp, tsn, cd);
+    std::vector<double> sl, ip;
+    for (const Slope& s : lgi->GetSlopes()) {
+      for (const ComputationalCell* c : {&s.xderivative, &s.yderivative}) {
+        sl.push_back(c->density);
+        sl.push_back(c->pressure);
+        sl.push_back(c->velocity.x);
+        sl.push_back(c->velocity.y);
+      }
+    }
+    for (const auto& pr : interp)
+      for (const ComputationalCell* c : {&pr.first, &pr.second}) {
+        ip.push_back(c->density);
+        ip.push_back(c->pressure);
+        ip.push_back(c->velocity.x);
+        ip.push_back(c->velocity.y);
+      }
+    dump_f64("slopes", sl, 8);
+    dump_f64("interp", ip, 8);
+  }
+  const vector<Extensive> fl = fc(tess, ev, cells, ext, cd, eos, t, dt, tsn);
+  dump_f64("fluxes", ext_flat(fl), 4);
+  vector<Extensive> ext1 = ext;
+  eu(fl, pg, tess, dt, cd, cells, ext1, t, tsn);
+  dump_f64("ext1", ext_flat(ext1), 4);
+  const vector<ComputationalCell> cells1 = cu(tess, pg, eos, ext1, cells, cd, tsn);
+  dump_f64("cells1", cells_flat(cells1), 4);
+}
+
+void run_and_dump(hdsim& sim, int steps) {
+  // hdsim keeps time_ += dt (hdsim2d.cpp:238); the sequence of times pins
+  // every dt without the rounding of a difference.
+  std::vector<double> times;
+  for (int s = 0; s < steps; ++s) {
+    sim.TimeAdvance();
+    times.push_back(sim.getTime());
+  }
+  dump_f64("run_cells", cells_flat(sim.getAllCells()), 4);
+  dump_f64("run_ext", ext_flat(sim.getAllExtensives()), 4);
+  dump_scalar("run_time", sim.getTime());
+  dump_f64("run_times", times, 0);
+  dump_mesh("runmesh_", sim.getTessellation(), SlabSymmetry());
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  if (argc < 7) {
+    std::fprintf(stderr, "usage: ref_dump <case> <outdir> <nx> <ny> <warm> <run>\n");
+    return 2;
+  }
+  const std::string which = argv[1];
+  g_out = argv[2];
+  const int nx = std::atoi(argv[3]), ny = std::atoi(argv[4]);
+  const int warm = std::atoi(argv[5]), run = std::atoi(argv[6]);
+  try {
+    SlabSymmetry pg;
+    Hllc rs;
+    ZeroForce force;
+    SimpleCFL tsf(0.3);
+    SimpleExtensiveUpdater eu;
+    SimpleCellUpdater cu;
+    if (which == "sod" || which == "sod_lagrangian") {
+      // 2D Sod tube: [0,1]x[0,0.2], reflective walls, piecewise-constant Hllc, gamma 1.4.
+      SquareBox outer(Vector2D(0, 0), Vector2D(1, 0.2));
+      VoronoiMesh tess(jittered_lattice(nx, ny, 0, 1, 0, 0.2, 1, 1e-3), outer);
+      IdealGas eos(1.4);
+      Eulerian eul;
+      Lagrangian lag;
+      const PointMotion& pm = which == "sod" ? static_cast<const PointMotion&>(eul)
+                                             : static_cast<const PointMotion&>(lag);
+      StationaryBox evc;
+      SimpleFluxCalculator fc(rs);
+      vector<ComputationalCell> ic(static_cast<size_t>(tess.GetPointNo()));
+      for (size_t i = 0; i < ic.size(); ++i) {
+        const bool left = tess.GetMeshPoint(static_cast<int>(i)).x < 0.5;
+        ic[i].density = left ? 1 : 0.125;
+        ic[i].pressure = left ? 1 : 0.1;
+      }
+      hdsim sim(tess, outer, pg, ic, eos, pm, evc, force, tsf, fc, eu, cu);
+      for (int s = 0; s < warm; ++s) sim.TimeAdvance();
+      dump_scalar("gamma", 1.4);
+      dump_scalar("order", 1);
+      dump_scalar("ghost_kind", 0);
+      dump_components(sim, pg, eos, pm, evc, tsf, fc, eu, cu, nullptr);
+      if (run > 0) run_and_dump(sim, run);
+    } else if (which == "sedov" || which == "sedov_eulerian") {
+      // Sedov-Taylor on [-1,1]^2, RoundCells(Lagrangian) (or Eulerian),
+      // LinearGaussImproved + rigid walls.
+      SquareBox outer(Vector2D(-1, -1), Vector2D(1, 1));
+      VoronoiMesh tess(jittered_lattice(nx, ny, -1, 1, -1, 1, 2, 1e-3), outer);
+      IdealGas eos(5. / 3.);
+      Lagrangian lag;
+      RoundCells round(lag, eos);
+      Eulerian eul;
+      const PointMotion& pm = which == "sedov" ? static_cast<const PointMotion&>(round)
+                                               : static_cast<const PointMotion&>(eul);
+      StationaryBox evc;
+      RigidWallGenerator gpg;
+      LinearGaussImproved sr(eos, gpg);
+      ModularFluxCalculator fc(sr, rs);
+      const double dx = 2.0 / nx;
+      const double rdep = std::max(0.02, 1.5 * dx);
+      double vin = 0;
+      for (int i = 0; i < tess.GetPointNo(); ++i)
+        if (abs(tess.GetMeshPoint(i)) < rdep) vin += tess.GetVolume(i);
+      vector<ComputationalCell> ic(static_cast<size_t>(tess.GetPointNo()));
+      for (size_t i = 0; i < ic.size(); ++i) {
+        ic[i].density = 1;
+        ic[i].pressure = abs(tess.GetMeshPoint(static_cast<int>(i))) < rdep ? (5. / 3. - 1) / vin : 1e-6;
+      }
+      hdsim sim(tess, outer, pg, ic, eos, pm, evc, force, tsf, fc, eu, cu);
+      for (int s = 0; s < warm; ++s) sim.TimeAdvance();
+      dump_scalar("gamma", 5. / 3.);
+      dump_scalar("order", 2);
+      dump_scalar("ghost_kind", 0);
+      dump_components(sim, pg, eos, pm, evc, tsf, fc, eu, cu, &sr);
+      if (run > 0) run_and_dump(sim, run);
+    } else if (which == "periodic" || which == "periodic_lagrangian") {
+      // Periodic [0,1]^2, LinearGaussImproved + PeriodicGhostGenerator, smooth bumps + velocity modes.
+      PeriodicBox outer(0, 1, 1, 0);
+      VoronoiMesh tess(jittered_lattice(nx, ny, 0, 1, 0, 1, 3, 1e-3), outer);
+      IdealGas eos(5. / 3.);
+      Eulerian eul;
+      Lagrangian lag;
+      const PointMotion& pm = which == "periodic" ? static_cast<const PointMotion&>(eul)
+                                                  : static_cast<const PointMotion&>(lag);
+      PeriodicEdgeVelocities evc;
+      PeriodicGhostGenerator gpg;
+      LinearGaussImproved sr(eos, gpg);
+      ModularFluxCalculator fc(sr, rs);
+      std::mt19937_64 gen(7);
+      std::uniform_real_distribution<double> u01(0, 1);
+      double bx[8], by[8], bw[8];
+      for (int k = 0; k < 8; ++k) {
+        bx[k] = u01(gen);
+        by[k] = u01(gen);
+        bw[k] = 0.02 + 0.08 * u01(gen);
+      }
+      vector<ComputationalCell> ic(static_cast<size_t>(tess.GetPointNo()));
+      const double pi2 = 2 * M_PI;
+      for (size_t i = 0; i < ic.size(); ++i) {
+        const Vector2D r = tess.GetMeshPoint(static_cast<int>(i));
+        double rho = 1;
+        for (int k = 0; k < 8; ++k) {
+          const double ddx = r.x - bx[k], ddy = r.y - by[k];
+          rho += 0.1 * std::exp(-(ddx * ddx + ddy * ddy) / (bw[k] * bw[k]));
+        }
+        ic[i].density = rho;
+        ic[i].pressure = 1;
+        ic[i].velocity = Vector2D(0.1 * std::sin(pi2 * (r.x + 2 * r.y)), 0.1 * std::cos(pi2 * (2 * r.x - r.y)));
+      }
+      hdsim sim(tess, outer, pg, ic, eos, pm, evc, force, tsf, fc, eu, cu);
+      for (int s = 0; s < warm; ++s) sim.TimeAdvance();
+      dump_scalar("gamma", 5. / 3.);
+      dump_scalar("order", 2);
+      dump_scalar("ghost_kind", 1);
+      dump_components(sim, pg, eos, pm, evc, tsf, fc, eu, cu, &sr);
+      if (run > 0) run_and_dump(sim, run);
+    } else {
+      std::fprintf(stderr, "unknown case %s\n", which.c_str());
+      return 2;
+    }
+  } catch (UniversalError const& eo) {
+    std::fprintf(stderr, "UniversalError: %s\n", eo.GetErrorMessage().c_str());
+    for (size_t i = 0; i < eo.GetFields().size(); ++i)
+      std::fprintf(stderr, "  %s = %.17g\n", eo.GetFields()[i].c_str(), eo.GetValues()[i]);
+    return 1;
+  }
+  return 0;
+}

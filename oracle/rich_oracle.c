@@ -1,0 +1,693 @@
+/*
+ * rich_oracle.c -- CPU restatement of RICH's hydro hot path (parity oracle).
+ *
+ * TEST INFRASTRUCTURE ONLY (see rich_oracle.h).  Build with
+ *   gcc -O2 -ffp-contract=off -fPIC -shared rich_oracle.c -lm
+ * so that no multiply-add is contracted; the reference fixtures are built
+ * the same way.
+ *
+ * Paths are relative to the RICH source root (source/...).  Each function
+ * follows the reference expression by expression; comments give the file and
+ * lines.  Vector2D / ComputationalCell arithmetic is expanded component-wise
+ * with the same operands in the same order (tessellation/geometry.cpp,
+ * two_dimensional/computational_cell_2d.cpp, common/hydrodynamic_variables.cpp).
+ */
+#include "rich_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* M_PI as <cmath> defines it for the reference (VoronoiMesh.cpp:412) */
+#define RO_PI 3.14159265358979323846
+
+typedef struct { double x, y; } v2;
+typedef struct { double d, p, vx, vy; } cc;           /* ComputationalCell (no tracers) */
+typedef struct { double d, p, vx, vy, e, c; } prim;   /* Primitive */
+typedef struct { double m, mx, my, en; } cons;        /* Conserved */
+
+/* std::min / std::max: min(a,b) = b<a ? b : a; max(a,b) = a<b ? b : a. */
+static double smin(double a, double b) { return b < a ? b : a; }
+static double smax(double a, double b) { return a < b ? b : a; }
+/* geometry.cpp:18-21 abs(Vector2D) */
+static double vabs(v2 v) { return sqrt(v.x * v.x + v.y * v.y); }
+/* geometry.cpp:100-105 ScalarProd */
+static double dot(v2 a, v2 b) { return a.x * b.x + a.y * b.y; }
+static v2 vsub(v2 a, v2 b) { v2 r = {a.x - b.x, a.y - b.y}; return r; }
+static v2 vadd(v2 a, v2 b) { v2 r = {a.x + b.x, a.y + b.y}; return r; }
+/* geometry.cpp:85-93 d*v and v*d both give (v.x*d, v.y*d) */
+static v2 vscale(v2 v, double d) { v2 r = {v.x * d, v.y * d}; return r; }
+/* geometry.cpp:95-98 */
+static v2 vdiv(v2 v, double d) { v2 r = {v.x / d, v.y / d}; return r; }
+
+static v2 point(const rg_mesh_view* m, int i) { v2 r = {m->point_xy[2 * i], m->point_xy[2 * i + 1]}; return r; }
+static v2 cmof(const rg_mesh_view* m, int i) { v2 r = {m->cm_xy[2 * i], m->cm_xy[2 * i + 1]}; return r; }
+static v2 vert0(const rg_mesh_view* m, int e) { v2 r = {m->face_vertices[4 * e], m->face_vertices[4 * e + 1]}; return r; }
+static v2 vert1(const rg_mesh_view* m, int e) { v2 r = {m->face_vertices[4 * e + 2], m->face_vertices[4 * e + 3]}; return r; }
+static int fc0(const rg_mesh_view* m, int e) { return m->face_cells[2 * e]; }
+static int fc1(const rg_mesh_view* m, int e) { return m->face_cells[2 * e + 1]; }
+/* VoronoiMesh.cpp:169-206 GetOriginalIndex */
+static int orig(const rg_mesh_view* m, int p) { return p < m->n_cells ? p : m->ghost_source[p - m->n_cells]; }
+static cc cell_at(const double* cells, int i) { cc r = {cells[4 * i], cells[4 * i + 1], cells[4 * i + 2], cells[4 * i + 3]}; return r; }
+
+static void set_err(ro_error* err, int status, int phase, int64_t index, double value) {
+  if (err && err->status == 0) {
+    err->status = status;
+    err->phase = phase;
+    err->index = index;
+    err->value = value;
+  }
+}
+
+/* spatial_reconstruction.cpp:3-6 CalcCentroid: 0.5*(first+second) */
+static v2 centroid(const rg_mesh_view* m, int e) { return vscale(vadd(vert0(m, e), vert1(m, e)), 0.5); }
+/* Edge.cpp:83-86 Parallel: second - first */
+static v2 parallel(const rg_mesh_view* m, int e) { return vsub(vert1(m, e), vert0(m, e)); }
+/* Edge.cpp GetLength: abs(second-first); physical_geometry.cpp:8-11 calcArea: abs(first-second) */
+static double edge_length(const rg_mesh_view* m, int e) { return vabs(vsub(vert1(m, e), vert0(m, e))); }
+static double edge_area(const rg_mesh_view* m, int e) { return vabs(vsub(vert0(m, e), vert1(m, e))); }
+/* VoronoiMesh.cpp:410-413 GetWidth */
+static double width(const rg_mesh_view* m, int i) { return sqrt(m->volume[i] / RO_PI); }
+
+/* ideal_gas.cpp:13-16 dp2e, :40-44 dp2c, :18-23 de2p */
+static double dp2e(double g, double d, double p) { return p / d / (g - 1); }
+static double dp2c(double g, double d, double p) { return sqrt(g * p / d); }
+
+/* simple_flux_calculator.cpp:9-15 convert_to_primitive */
+static prim to_prim(double g, cc c) {
+  prim r;
+  r.d = c.d;
+  r.p = c.p;
+  r.vx = c.vx;
+  r.vy = c.vy;
+  r.e = dp2e(g, c.d, c.p);
+  r.c = dp2c(g, c.d, c.p);
+  return r;
+}
+
+/* simple_flux_calculator.cpp:17-25 reflect, geometry.cpp:117-120 Reflect:
+ * 2*ScalarProd(v,axis)*axis/pow(abs(axis),2)-v (pow(x,2) folds to x*x). */
+static prim reflect(prim p, v2 axis) {
+  v2 v = {p.vx, p.vy};
+  const double s = 2 * dot(v, axis);
+  const double aa = vabs(axis);
+  const v2 t = vdiv(vscale(axis, s), aa * aa);
+  p.vx = t.x - v.x;
+  p.vy = t.y - v.y;
+  return p;
+}
+
+/* hydrodynamic_variables.cpp:261-265 TotalEnergyDensity: d*(0.5*pow(abs(v),2)+e) */
+static double ted(prim p) {
+  v2 v = {p.vx, p.vy};
+  const double s = vabs(v);
+  return p.d * (0.5 * (s * s) + p.e);
+}
+
+/* hydrodynamic_variables.cpp:267-272 Primitive2Conserved */
+static cons p2c(prim p) {
+  cons r;
+  r.m = p.d;
+  r.mx = p.vx * p.d;
+  r.my = p.vy * p.d;
+  r.en = ted(p);
+  return r;
+}
+
+/* hydrodynamic_variables.cpp:281-290 Primitive2Flux with n = (1,0) */
+static cons p2f_x(prim p) {
+  const v2 n = {1, 0};
+  const v2 nn = vdiv(n, vabs(n));
+  const v2 v = {p.vx, p.vy};
+  const double sp = dot(v, nn);
+  cons r;
+  r.m = p.d * sp;
+  const double dsp = p.d * sp;
+  r.mx = nn.x * p.p + v.x * dsp;
+  r.my = nn.y * p.p + v.y * dsp;
+  r.en = (ted(p) + p.p) * sp;
+  return r;
+}
+
+/* hllc.cpp:76-92 starred_state */
+static cons starred(prim s, double sk, double ss) {
+  const double dk = s.d, pk = s.p, uk = s.vx, vk = s.vy;
+  const double ds = dk * (sk - uk) / (sk - ss);
+  const double ek = ted(s);
+  cons r;
+  r.m = ds;
+  r.mx = ds * ss;
+  r.my = ds * vk;
+  r.en = ek * ds / dk + ds * (ss - uk) * (ss + pk / dk / (sk - uk));
+  return r;
+}
+
+/* hllc.cpp:97-154 Hllc::operator() with massflux_ = true */
+static int hllc(prim left, prim right, double velocity, cons* out, int64_t face, ro_error* err) {
+  if (isnan(right.vx)) {
+    set_err(err, RG_ERR_HLLC_NAN, 3, face, right.vx);
+    return RG_ERR_HLLC_NAN;
+  }
+  /* local.Velocity -= velocity*normaldir, normaldir = (1,0) */
+  const double bx = 1 * velocity, by = 0 * velocity;
+  left.vx -= bx;
+  left.vy -= by;
+  right.vx -= bx;
+  right.vy -= by;
+  /* hllc.cpp:27-43 estimate_wave_speeds */
+  const double dl = left.d, pl = left.p, vl = left.vx, cl = left.c;
+  const double dr = right.d, pr = right.p, vr = right.vx, cr = right.c;
+  const double sl = smin(vl - cl, vr - cr);
+  const double sr = smax(vl + cl, vr + cr);
+  const double ss = (pr - pl + dl * vl * (sl - vl) - dr * vr * (sr - vr)) / (dl * (sl - vl) - dr * (sr - vr));
+  const cons ul = p2c(left), ur = p2c(right);
+  const cons fl = p2f_x(left), fr = p2f_x(right);
+  const cons usl = starred(left, sl, ss), usr = starred(right, sr, ss);
+  cons f;
+  if (sl > 0)
+    f = fl;
+  else if (sl <= 0 && ss >= 0) {
+    f.m = fl.m + sl * (usl.m - ul.m);
+    f.mx = fl.mx + (usl.mx - ul.mx) * sl;
+    f.my = fl.my + (usl.my - ul.my) * sl;
+    f.en = fl.en + sl * (usl.en - ul.en);
+  } else if (ss < 0 && sr >= 0) {
+    f.m = fr.m + sr * (usr.m - ur.m);
+    f.mx = fr.mx + (usr.mx - ur.mx) * sr;
+    f.my = fr.my + (usr.my - ur.my) * sr;
+    f.en = fr.en + sr * (usr.en - ur.en);
+  } else if (sr < 0)
+    f = fr;
+  else {
+    set_err(err, RG_ERR_HLLC_WAVE_SPEEDS, 3, face, ss);
+    return RG_ERR_HLLC_WAVE_SPEEDS;
+  }
+  /* hllc.cpp:150-152 */
+  const v2 vn = {1 * velocity, 0 * velocity};
+  const v2 mom = {f.mx, f.my};
+  f.en += dot(mom, vn) + 0.5 * f.m * velocity * velocity;
+  const double vm = velocity * f.m;
+  f.mx += 1 * vm;
+  f.my += 0 * vm;
+  *out = f;
+  return 0;
+}
+
+/* simple_flux_calculator.cpp:130-140 rotate: (Projection(v,n), Projection(v,p)) */
+static prim rotate(prim s, v2 n, v2 p) {
+  const v2 v = {s.vx, s.vy};
+  s.vx = dot(v, n) / vabs(n);
+  s.vy = dot(v, p) / vabs(p);
+  return s;
+}
+
+/* simple_flux_calculator.cpp:142-165 rotate_back / rotate_solve_rotate_back */
+static int rotate_solve_rotate_back(prim left, prim right, double velocity, v2 n, v2 p, cons* out,
+                                    int64_t face, ro_error* err) {
+  cons c;
+  const int st = hllc(rotate(left, n, p), rotate(right, n, p), velocity, &c, face, err);
+  if (st) return st;
+  const v2 a = vdiv(vscale(n, c.mx), vabs(n));
+  const v2 b = vdiv(vscale(p, c.my), vabs(p));
+  out->m = c.m;
+  out->mx = a.x + b.x;
+  out->my = a.y + b.y;
+  out->en = c.en;
+  return 0;
+}
+
+static void put_flux(double* f, cons c) { f[0] = c.m; f[1] = c.en; f[2] = c.mx; f[3] = c.my; }
+
+/* State of a point (real cell or ghost) as SimpleFluxCalculator sees it:
+ * a ghost that is not a self-mirror takes its source cell's state (the
+ * reference indexes cells[] with the ghost id there, which only exists in
+ * MPI builds; the source cell is what that entry holds). */
+static cc point_state(const rg_mesh_view* m, const double* cells, int p) {
+  return cell_at(cells, orig(m, p));
+}
+
+/* simple_flux_calculator.cpp:80-126 riemann_reduce + :167-189 calcHydroFlux
+ * + :216-244 operator() */
+int ro_simple_flux(const rg_mesh_view* m, const double* cells, const double* ev, double g,
+                   double* fluxes, ro_error* err) {
+  const int N = m->n_cells;
+  for (int e = 0; e < m->n_faces; ++e) {
+    const int a = fc0(m, e), b = fc1(m, e);
+    const v2 p = parallel(m, e);
+    const v2 n = vsub(point(m, b), point(m, a));
+    const int va = a >= 0 && a < N, vb = b >= 0 && b < N;
+    prim left, right;
+    if (!va) {
+      right = to_prim(g, point_state(m, cells, b));
+      if (orig(m, b) == orig(m, a))
+        left = reflect(right, p);
+      else
+        left = to_prim(g, point_state(m, cells, a));
+    } else if (!vb) {
+      left = to_prim(g, point_state(m, cells, a));
+      if (orig(m, b) == orig(m, a))
+        right = reflect(left, p);
+      else
+        right = to_prim(g, point_state(m, cells, b));
+    } else {
+      left = to_prim(g, cell_at(cells, a));
+      right = to_prim(g, cell_at(cells, b));
+    }
+    const v2 w = {ev[2 * e], ev[2 * e + 1]};
+    const double velocity = dot(n, w) / vabs(n);
+    cons c;
+    const int st = rotate_solve_rotate_back(left, right, velocity, n, p, &c, e, err);
+    if (st) return st;
+    put_flux(fluxes + 4 * e, c);
+  }
+  return 0;
+}
+
+/* ---------------- LinearGaussImproved (interpolations/LinearGaussImproved.cpp) ---------- */
+
+/* computational_cell_2d.cpp:59-68 ComputationalCellAddMult */
+static void addmult(cc* r, cc o, double s) {
+  r->d += o.d * s;
+  r->p += o.p * s;
+  r->vx += o.vx * s;
+  r->vy += o.vy * s;
+}
+static cc ccsub(cc a, cc b) { cc r = {a.d - b.d, a.p - b.p, a.vx - b.vx, a.vy - b.vy}; return r; }
+static cc ccscale(cc a, double s) { cc r = {a.d * s, a.p * s, a.vx * s, a.vy * s}; return r; }
+static cc ccadd(cc a, cc b) { cc r = {a.d + b.d, a.p + b.p, a.vx + b.vx, a.vy + b.vy}; return r; }
+
+typedef struct { cc x, y; } slope;
+
+/* Ghost states: RigidWallGenerator.cpp:17-37 / PeriodicGhostGenerator.cpp:3-17.
+ * new_cells[ghost] for every ghost (LinearGaussImproved.cpp:543-550). */
+static void ghost_states(const rg_mesh_view* m, const double* cells, int ghost_kind, cc* gs) {
+  const int N = m->n_cells;
+  for (int g = 0; g < m->n_ghosts; ++g) {
+    const int e = m->ghost_face[g];
+    memset(&gs[g], 0, sizeof(cc));
+    if (e < 0) continue;
+    const int a = fc0(m, e), b = fc1(m, e);
+    if (ghost_kind == RG_GHOST_PERIODIC) {
+      gs[g] = cell_at(cells, m->ghost_source[g]);
+    } else {
+      /* index 1: ghost is neighbors.first; the real side is the other one */
+      const int ghost_first = a >= N;
+      const int real = ghost_first ? b : a;
+      cc c = cell_at(cells, real);
+      /* RigidWallGenerator.cpp:5-15 ReverseNormalVelocity */
+      v2 normal = ghost_first ? vsub(point(m, a), point(m, b)) : vsub(point(m, b), point(m, a));
+      normal = vdiv(normal, vabs(normal));
+      const v2 v = {c.vx, c.vy};
+      const v2 t = vscale(normal, 2 * dot(v, normal));
+      c.vx -= t.x;
+      c.vy -= t.y;
+      gs[g] = c;
+    }
+  }
+}
+
+static cc any_state(const rg_mesh_view* m, const double* cells, const cc* gs, int p) {
+  return p < m->n_cells ? cell_at(cells, p) : gs[p - m->n_cells];
+}
+
+/* :159-165 interp and :167-172 interp2 */
+static void interp2(cc* r, slope s, v2 target, v2 cm) {
+  addmult(r, s.x, target.x - cm.x);
+  addmult(r, s.y, target.y - cm.y);
+}
+
+/* :67-134 calc_naive_slope */
+static int naive_slope(const rg_mesh_view* m, int i, cc cell, v2 center, v2 cell_cm, double vol,
+                       const int* edges, int n, const cc* nb, const v2* nb_pt, const v2* nb_cm,
+                       slope* res, ro_error* err) {
+  if (n > 20) {
+    set_err(err, RG_ERR_TOO_MANY_NEIGHBORS, 2, i, n);
+    return RG_ERR_TOO_MANY_NEIGHBORS;
+  }
+  double mm[4] = {0, 0, 0, 0};
+  slope vc;
+  for (int k = 0; k < n; ++k) {
+    const int e = edges[k];
+    const v2 c_ij = vsub(centroid(m, e), vscale(vadd(nb_cm[k], cell_cm), 0.5));
+    const double e_length = edge_length(m, e);
+    const v2 dd = vsub(nb_pt[k], center);
+    const v2 r_ij = vscale(vdiv(dd, vabs(dd)), e_length);
+    mm[0] -= c_ij.x * r_ij.x;
+    mm[1] -= c_ij.y * r_ij.x;
+    mm[2] -= c_ij.x * r_ij.y;
+    mm[3] -= c_ij.y * r_ij.y;
+    if (k == 0) {
+      vc.x = ccscale(cell, r_ij.x * 0.5);
+      vc.y = ccscale(cell, r_ij.y * 0.5);
+    } else {
+      addmult(&vc.x, cell, r_ij.x * 0.5);
+      addmult(&vc.y, cell, r_ij.y * 0.5);
+    }
+    addmult(&vc.y, nb[k], r_ij.y * 0.5);
+    addmult(&vc.x, nb[k], r_ij.x * 0.5);
+  }
+  mm[0] += vol;
+  mm[3] += vol;
+  const double det = mm[0] * mm[3] - mm[1] * mm[2];
+  if (fabs(det) < 1e-10 * vol * vol) {
+    set_err(err, RG_ERR_SINGULAR_MATRIX, 2, i, det);
+    return RG_ERR_SINGULAR_MATRIX;
+  }
+  const double det_inv = 1.0 / det;
+  const double mi0 = mm[3] * det_inv, mi1 = -mm[1] * det_inv, mi2 = -mm[2] * det_inv, mi3 = mm[0] * det_inv;
+  res->x = ccscale(vc.x, mi0);
+  res->y = ccscale(vc.y, mi3);
+  addmult(&res->x, vc.y, mi1);
+  addmult(&res->y, vc.x, mi2);
+  return 0;
+}
+
+/* :401-422 GetBoundarySlope */
+static void boundary_slope(cc cell, v2 cell_cm, int n, const cc* nb, const v2* nb_cm, slope* res) {
+  cc phisy = {0, 0, 0, 0}, phisx = {0, 0, 0, 0};
+  double sxsy = 0, sy2 = 0, sx2 = 0;
+  for (int k = 0; k < n; ++k) {
+    phisy = ccadd(phisy, ccscale(ccsub(nb[k], cell), nb_cm[k].y - cell_cm.y));
+    phisx = ccadd(phisx, ccscale(ccsub(nb[k], cell), nb_cm[k].x - cell_cm.x));
+    sxsy += (nb_cm[k].y - cell_cm.y) * (nb_cm[k].x - cell_cm.x);
+    sx2 += (nb_cm[k].x - cell_cm.x) * (nb_cm[k].x - cell_cm.x);
+    sy2 += (nb_cm[k].y - cell_cm.y) * (nb_cm[k].y - cell_cm.y);
+  }
+  const double den = sxsy * sxsy - sx2 * sy2;
+  const cc ax = ccsub(ccscale(phisy, sxsy), ccscale(phisx, sy2));
+  const cc ay = ccsub(ccscale(phisx, sxsy), ccscale(phisy, sx2));
+  res->x.d = ax.d / den; res->x.p = ax.p / den; res->x.vx = ax.vx / den; res->x.vy = ax.vy / den;
+  res->y.d = ay.d / den; res->y.p = ay.p / den; res->y.vx = ay.vx / den; res->y.vy = ay.vy / den;
+}
+
+/* :136-148 PressureRatio, :150-157 is_shock */
+static int is_shock(slope naive, double cell_width, double shockratio, cc cell, int n, const cc* nb,
+                    double pressure_ratio, double cs) {
+  const int cond1 = (naive.x.vx + naive.y.vy) * cell_width < (-shockratio) * cs;
+  double res = 1;
+  const double p = cell.p;
+  for (int k = 0; k < n; ++k) {
+    if (p > nb[k].p)
+      res = smin(res, nb[k].p / p);
+    else
+      res = smin(res, p / nb[k].p);
+  }
+  const int cond2 = res < pressure_ratio;
+  return cond1 || cond2;
+}
+
+/* one ComputationalCell component of :232-267 (ordinary limiter).  velocity
+ * thresholds use |1e-9*v|, density/pressure thresholds 1e-9*q (no abs). */
+static void limit_comp(double dphi, double cv, double cellv, double maxd, double mind, int use_abs,
+                       double* psi) {
+  if (fabs(dphi) > 0.05 * smax(fabs(maxd), fabs(mind)) || cv * cellv < 0) {
+    const double thr = use_abs ? fabs(1e-9 * cellv) : 1e-9 * cellv;
+    const double nthr = use_abs ? -fabs(1e-9 * cellv) : -1e-9 * cellv;
+    if (dphi > thr)
+      *psi = smin(*psi, maxd / dphi);
+    else if (dphi < nthr)
+      *psi = smin(*psi, mind / dphi);
+  }
+}
+
+/* :174-300 slope_limit */
+static void slope_limit(const rg_mesh_view* m, cc cell, v2 cm, int n, const cc* nb, const int* edges,
+                        slope* s) {
+  cc cmax = cell, cmin = cell;
+  for (int k = 0; k < n; ++k) {
+    const int e = edges[k];
+    if (orig(m, fc0(m, e)) == orig(m, fc1(m, e))) continue;
+    cmax.d = smax(cmax.d, nb[k].d);
+    cmax.p = smax(cmax.p, nb[k].p);
+    cmax.vx = smax(cmax.vx, nb[k].vx);
+    cmax.vy = smax(cmax.vy, nb[k].vy);
+    cmin.d = smin(cmin.d, nb[k].d);
+    cmin.p = smin(cmin.p, nb[k].p);
+    cmin.vx = smin(cmin.vx, nb[k].vx);
+    cmin.vy = smin(cmin.vy, nb[k].vy);
+  }
+  const cc maxdiff = ccsub(cmax, cell), mindiff = ccsub(cmin, cell);
+  double psi[4] = {1, 1, 1, 1};
+  for (int k = 0; k < n; ++k) {
+    cc cv = cell;
+    interp2(&cv, *s, centroid(m, edges[k]), cm);
+    const cc dphi = ccsub(cv, cell);
+    limit_comp(dphi.d, cv.d, cell.d, maxdiff.d, mindiff.d, 0, &psi[0]);
+    limit_comp(dphi.p, cv.p, cell.p, maxdiff.p, mindiff.p, 0, &psi[1]);
+    limit_comp(dphi.vx, cv.vx, cell.vx, maxdiff.vx, mindiff.vx, 1, &psi[2]);
+    limit_comp(dphi.vy, cv.vy, cell.vy, maxdiff.vy, mindiff.vy, 1, &psi[3]);
+  }
+  s->x.d *= psi[0]; s->y.d *= psi[0];
+  s->x.p *= psi[1]; s->y.p *= psi[1];
+  s->x.vx *= psi[2]; s->y.vx *= psi[2];
+  s->x.vy *= psi[3]; s->y.vy *= psi[3];
+}
+
+/* one component of :343-366 (shocked limiter); the threshold is 1e-9*q
+ * without abs for every component, as in the reference (:346,352,358,364). */
+static void shocked_comp(double dphi, double cv, double cellv, double maxd, double mind, double nbv,
+                         double theta, double* psi) {
+  if (fabs(dphi) > 0.1 * smax(fabs(maxd), fabs(mind)) || cv * cellv < 0) {
+    if (fabs(dphi) > 1e-9 * cellv) *psi = smin(*psi, smax(theta * (nbv - cellv) / dphi, 0.0));
+  }
+}
+
+/* :302-399 shocked_slope_limit */
+static void shocked_slope_limit(const rg_mesh_view* m, cc cell, v2 cm, int n, const cc* nb,
+                                const int* edges, double theta, slope* s) {
+  cc cmax = cell, cmin = cell;
+  for (int k = 0; k < n; ++k) {
+    cmax.d = smax(cmax.d, nb[k].d);
+    cmax.p = smax(cmax.p, nb[k].p);
+    cmax.vx = smax(cmax.vx, nb[k].vx);
+    cmax.vy = smax(cmax.vy, nb[k].vy);
+    cmin.d = smin(cmin.d, nb[k].d);
+    cmin.p = smin(cmin.p, nb[k].p);
+    cmin.vx = smin(cmin.vx, nb[k].vx);
+    cmin.vy = smin(cmin.vy, nb[k].vy);
+  }
+  const cc maxdiff = ccsub(cmax, cell), mindiff = ccsub(cmin, cell);
+  double psi[4] = {1, 1, 1, 1};
+  for (int k = 0; k < n; ++k) {
+    cc cv = cell;
+    interp2(&cv, *s, centroid(m, edges[k]), cm);
+    const cc dphi = ccsub(cv, cell);
+    shocked_comp(dphi.d, cv.d, cell.d, maxdiff.d, mindiff.d, nb[k].d, theta, &psi[0]);
+    shocked_comp(dphi.p, cv.p, cell.p, maxdiff.p, mindiff.p, nb[k].p, theta, &psi[1]);
+    shocked_comp(dphi.vx, cv.vx, cell.vx, maxdiff.vx, mindiff.vx, nb[k].vx, theta, &psi[2]);
+    shocked_comp(dphi.vy, cv.vy, cell.vy, maxdiff.vy, mindiff.vy, nb[k].vy, theta, &psi[3]);
+  }
+  s->x.d *= psi[0]; s->y.d *= psi[0];
+  s->x.p *= psi[1]; s->y.p *= psi[1];
+  s->x.vx *= psi[2]; s->y.vx *= psi[2];
+  s->x.vy *= psi[3]; s->y.vy *= psi[3];
+}
+
+static void put_cc(double* o, cc c) { o[0] = c.d; o[1] = c.p; o[2] = c.vx; o[3] = c.vy; }
+static cc get_cc(const double* o) { cc c = {o[0], o[1], o[2], o[3]}; return c; }
+
+/* :536-635 LinearGaussImproved::operator() (serial build), with :425-494 calc_slope */
+int ro_lgi(const rg_mesh_view* m, const double* cells, double g, const ro_lgi_params* lp,
+           double* slopes, double* interp, ro_error* err) {
+  const int N = m->n_cells;
+  cc* gs = (cc*)calloc((size_t)(m->n_ghosts > 0 ? m->n_ghosts : 1), sizeof(cc));
+  slope* sl = (slope*)calloc((size_t)N, sizeof(slope));
+  int st = 0;
+  ghost_states(m, cells, lp->ghost_kind, gs);
+  for (int i = 0; i < N && !st; ++i) {
+    const int b = m->cell_face_offset[i], n = m->cell_face_offset[i + 1] - b;
+    const int* edges = m->cell_faces + b;
+    cc nb[64];
+    v2 nb_pt[64], nb_cm[64];
+    if (n > 64) {
+      set_err(err, RG_ERR_TOO_MANY_NEIGHBORS, 2, i, n);
+      st = RG_ERR_TOO_MANY_NEIGHBORS;
+      break;
+    }
+    int bslope = 0;
+    for (int k = 0; k < n; ++k) {
+      const int e = edges[k];
+      const int other = fc0(m, e) == i ? fc1(m, e) : fc0(m, e);
+      nb[k] = any_state(m, cells, gs, other);
+      nb_pt[k] = point(m, other);
+      nb_cm[k] = cmof(m, other);
+      if (orig(m, fc0(m, e)) == orig(m, fc1(m, e))) bslope = 1;
+    }
+    const cc cell = cell_at(cells, i);
+    slope s;
+    if (bslope)
+      boundary_slope(cell, cmof(m, i), n, nb, nb_cm, &s);
+    else {
+      st = naive_slope(m, i, cell, point(m, i), cmof(m, i), m->volume[i], edges, n, nb, nb_pt, nb_cm, &s, err);
+      if (st) break;
+    }
+    if (lp->slf) {
+      if (!is_shock(s, width(m, i), lp->delta_v, cell, n, nb, lp->delta_p, dp2c(g, cell.d, cell.p)))
+        slope_limit(m, cell, cmof(m, i), n, nb, edges, &s);
+      else
+        shocked_slope_limit(m, cell, cmof(m, i), n, nb, edges, lp->theta, &s);
+    }
+    sl[i] = s;
+    if (slopes) {
+      put_cc(slopes + 8 * i, s.x);
+      put_cc(slopes + 8 * i + 4, s.y);
+    }
+    /* :570-590 interpolation of the real side of each edge */
+    for (int k = 0; k < n; ++k) {
+      const int e = edges[k];
+      cc r = cell;
+      interp2(&r, s, centroid(m, e), cmof(m, i));
+      put_cc(interp + 8 * e + (fc0(m, e) == i ? 0 : 4), r);
+    }
+  }
+  if (!st) {
+    /* :596-634 ghost side of boundary edges: ghost state + ghost gradient */
+    for (int e = 0; e < m->n_faces; ++e) {
+      const int a = fc0(m, e), b = fc1(m, e);
+      int side, gp;
+      if (a >= N) { side = 0; gp = a; }
+      else if (b >= N) { side = 1; gp = b; }
+      else continue;
+      cc r = gs[gp - N];
+      slope gg;
+      if (lp->ghost_kind == RG_GHOST_PERIODIC)
+        gg = sl[orig(m, gp)];
+      else
+        memset(&gg, 0, sizeof gg);
+      interp2(&r, gg, centroid(m, e), cmof(m, gp));
+      put_cc(interp + 8 * e + 4 * side, r);
+    }
+  }
+  free(gs);
+  free(sl);
+  return st;
+}
+
+/* modular_flux_calculator.cpp:12-22 calc_parallel_normal and
+ * simple_flux_calculator.cpp:27-31 remove_parallel_component */
+static v2 remove_parallel(v2 v, v2 p) { return vsub(v, vdiv(vscale(p, dot(v, p)), dot(p, p))); }
+
+/* modular_flux_calculator.cpp:39-71 */
+int ro_modular_flux(const rg_mesh_view* m, const double* cells, const double* ev, double g,
+                    const ro_lgi_params* lp, double* fluxes, ro_error* err) {
+  const int N = m->n_cells;
+  double* ip = (double*)malloc(sizeof(double) * 8 * (size_t)(m->n_faces > 0 ? m->n_faces : 1));
+  int st = ro_lgi(m, cells, g, lp, NULL, ip, err);
+  for (int e = 0; e < m->n_faces && !st; ++e) {
+    const int a = fc0(m, e), b = fc1(m, e);
+    const v2 p = parallel(m, e);
+    v2 n;
+    if (a >= 0 && a < N)
+      n = remove_parallel(vsub(vert0(m, e), point(m, a)), p);
+    else
+      n = remove_parallel(vsub(point(m, b), vert0(m, e)), p);
+    const v2 w = {ev[2 * e], ev[2 * e + 1]};
+    const double speed = dot(n, w) / vabs(n);
+    const prim pl = to_prim(g, get_cc(ip + 8 * e)), pr = to_prim(g, get_cc(ip + 8 * e + 4));
+    cons c;
+    st = rotate_solve_rotate_back(pl, pr, speed, n, p, &c, e, err);
+    if (!st) put_flux(fluxes + 4 * e, c);
+  }
+  free(ip);
+  return st;
+}
+
+/* simple_extensive_updater.cpp:11-35 */
+int ro_extensive_update(const rg_mesh_view* m, const double* fluxes, double dt, double* ext,
+                        ro_error* err) {
+  (void)err;
+  const int N = m->n_cells;
+  for (int e = 0; e < m->n_faces; ++e) {
+    const double s = dt * edge_area(m, e);
+    const double dm = fluxes[4 * e] * s, de = fluxes[4 * e + 1] * s;
+    const double dx = fluxes[4 * e + 2] * s, dy = fluxes[4 * e + 3] * s;
+    const int a = fc0(m, e), b = fc1(m, e);
+    if (a >= 0 && a < N) {
+      ext[4 * a] -= dm;
+      ext[4 * a + 1] -= de;
+      ext[4 * a + 2] -= dx;
+      ext[4 * a + 3] -= dy;
+    }
+    if (b >= 0 && b < N) {
+      ext[4 * b] += dm;
+      ext[4 * b + 1] += de;
+      ext[4 * b + 2] += dx;
+      ext[4 * b + 3] += dy;
+    }
+  }
+  return 0;
+}
+
+/* simple_cell_updater.cpp:22-59 regular_update, :85-106 operator() */
+int ro_cell_update(const rg_mesh_view* m, const double* ext, double g, double* cells_out,
+                   ro_error* err) {
+  for (int i = 0; i < m->n_cells; ++i) {
+    const double mass = ext[4 * i], en = ext[4 * i + 1], px = ext[4 * i + 2], py = ext[4 * i + 3];
+    const double volume = m->cd_volume[i];
+    const double d = mass / volume;
+    if (d < 0) {
+      set_err(err, RG_ERR_NEGATIVE_DENSITY, 5, i, d);
+      return RG_ERR_NEGATIVE_DENSITY;
+    }
+    const double vx = px / mass, vy = py / mass;
+    const double energy = en / mass - 0.5 * (vx * vx + vy * vy);
+    if (energy < 0) {
+      set_err(err, RG_ERR_NEGATIVE_ENERGY, 5, i, energy);
+      return RG_ERR_NEGATIVE_ENERGY;
+    }
+    cells_out[4 * i] = d;
+    cells_out[4 * i + 1] = (g - 1) * energy * d;
+    cells_out[4 * i + 2] = vx;
+    cells_out[4 * i + 3] = vy;
+  }
+  return 0;
+}
+
+/* hdsim2d.cpp:41-67 init_extensives (volume = pg.calcVolume = cd_volume) */
+int ro_init_extensives(const rg_mesh_view* m, const double* cells, double g, double* ext) {
+  for (int i = 0; i < m->n_cells; ++i) {
+    const double d = cells[4 * i], p = cells[4 * i + 1], vx = cells[4 * i + 2], vy = cells[4 * i + 3];
+    const double mass = m->cd_volume[i] * d;
+    ext[4 * i] = mass;
+    ext[4 * i + 1] = dp2e(g, d, p) * mass + 0.5 * mass * (vx * vx + vy * vy);
+    ext[4 * i + 2] = vx * mass;
+    ext[4 * i + 3] = vy * mass;
+  }
+  return 0;
+}
+
+/* simple_cfl.cpp:28-47 TimeStepCalculator, :58-71 operator(), lazy_list.hpp:185-191 lazy_min */
+int ro_cfl(const rg_mesh_view* m, const double* cells, const double* ev, double g, double cfl,
+           double* dt, ro_error* err) {
+  (void)err;
+  double best = 0;
+  for (int i = 0; i < m->n_cells; ++i) {
+    double res = 0;
+    const double radius = width(m, i);
+    const double c = dp2c(g, cells[4 * i], cells[4 * i + 1]);
+    const v2 v = {cells[4 * i + 2], cells[4 * i + 3]};
+    for (int k = m->cell_face_offset[i]; k < m->cell_face_offset[i + 1]; ++k) {
+      const int e = m->cell_faces[k];
+      const v2 ve = {ev[2 * e], ev[2 * e + 1]};
+      res = fmax(res, (c + vabs(vsub(v, ve))) / radius);
+    }
+    const double x = 1.0 / res;
+    best = i == 0 ? x : smin(best, x);
+  }
+  *dt = cfl * best;
+  return 0;
+}
+
+int ro_step(const rg_mesh_view* m, double* cells, double* ext, const double* ev, double g,
+            double cfl, int order, const ro_lgi_params* lp, double* dt_out, ro_error* err) {
+  double dt;
+  int st = ro_cfl(m, cells, ev, g, cfl, &dt, err);
+  if (st) return st;
+  double* fl = (double*)malloc(sizeof(double) * 4 * (size_t)(m->n_faces > 0 ? m->n_faces : 1));
+  st = order == 1 ? ro_simple_flux(m, cells, ev, g, fl, err) : ro_modular_flux(m, cells, ev, g, lp, fl, err);
+  if (!st) st = ro_extensive_update(m, fl, dt, ext, err);
+  if (!st) st = ro_cell_update(m, ext, g, cells, err);
+  free(fl);
+  if (dt_out) *dt_out = dt;
+  return st;
+}

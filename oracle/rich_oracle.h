@@ -1,0 +1,62 @@
+/*
+ * rich_oracle.h -- CPU restatement of RICH's per-step hydro hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the parity oracle: tests/, the smoke
+ * check in __graft_entry__.py and bench.py's CPU-baseline leg call it as the
+ * checker.  The product (huji-rich_gb300/) never links or calls it.
+ *
+ * Every function restates one reference function in plain C, operation for
+ * operation and in the reference's evaluation order, on the packed mesh of
+ * include/rich_gb300.h.  It is pinned against fixtures produced by the
+ * reference itself (tests/golden/, generated by tests/golden/make_golden.py
+ * from oracle/ref/ref_dump.cpp): bit-for-bit equality is required.
+ *
+ * Layouts: cells N*4 {density, pressure, vx, vy}; extensives and fluxes
+ * {mass, energy, px, py}; slopes N*8 {d/dx of the 4 cell fields, d/dy ...};
+ * interp E*8 {first side cell, second side cell}.
+ */
+#ifndef RICH_ORACLE_H
+#define RICH_ORACLE_H
+#include <stdint.h>
+#include "rich_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ro_error {
+  int32_t status; /* rg_status code, 0 = ok */
+  int32_t phase;
+  int64_t index;
+  double value;
+} ro_error;
+
+typedef struct ro_lgi_params {
+  int32_t ghost_kind; /* rg_ghost_kind */
+  int32_t slf;
+  double delta_v, theta, delta_p;
+} ro_lgi_params;
+
+int ro_cfl(const rg_mesh_view* m, const double* cells, const double* ev, double gamma, double cfl,
+           double* dt, ro_error* err);
+int ro_simple_flux(const rg_mesh_view* m, const double* cells, const double* ev, double gamma,
+                   double* fluxes, ro_error* err);
+int ro_lgi(const rg_mesh_view* m, const double* cells, double gamma, const ro_lgi_params* lp,
+           double* slopes, double* interp, ro_error* err);
+int ro_modular_flux(const rg_mesh_view* m, const double* cells, const double* ev, double gamma,
+                    const ro_lgi_params* lp, double* fluxes, ro_error* err);
+int ro_extensive_update(const rg_mesh_view* m, const double* fluxes, double dt, double* ext,
+                        ro_error* err);
+int ro_cell_update(const rg_mesh_view* m, const double* ext, double gamma, double* cells_out,
+                   ro_error* err);
+int ro_init_extensives(const rg_mesh_view* m, const double* cells, double gamma, double* ext);
+/* One hdsim::TimeAdvance hot-path pass on a fixed mesh (cfl, flux, extensive
+ * update, cell update), the same edge velocities for CFL and flux.  order 1
+ * ignores lp. */
+int ro_step(const rg_mesh_view* m, double* cells, double* ext, const double* ev, double gamma,
+            double cfl, int order, const ro_lgi_params* lp, double* dt_out, ro_error* err);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

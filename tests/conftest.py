@@ -1,0 +1,38 @@
+"""Shared pytest setup: the `gpu` marker, import paths and fixture loaders."""
+import glob
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PKG = os.path.join(ROOT, "huji-rich_gb300")
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+for p in (ROOT, PKG, os.path.join(ROOT, "oracle")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+GOLDEN_CASES = sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(GOLDEN, "*.npz")))
+
+
+def load_golden(name):
+    """Fixture dict (arrays) + packed mesh for one golden case."""
+    from meshview import PackedMesh
+    z = dict(np.load(os.path.join(GOLDEN, name + ".npz")))
+    z["mesh"] = PackedMesh.from_npz(z)
+    z["gamma"] = float(z["gamma"][0])
+    z["order"] = int(z["order"][0])
+    z["ghost_kind"] = int(z["ghost_kind"][0])
+    z["dt"] = float(z["dt"][0])
+    return z
+
+
+@pytest.fixture(params=GOLDEN_CASES)
+def golden(request):
+    return load_golden(request.param)

@@ -1,0 +1,75 @@
+"""Regenerate the golden fixtures in this directory from the reference itself.
+
+Builds the reference RICH hot path from its own sources (oracle/ref/Makefile,
+outputs only under oracle/_ref/), runs oracle/ref/ref_dump.cpp on each case
+and bundles the .npy arrays it writes into ``<case>.npz``.
+
+Usage (needs the reference source tree; not available at test time):
+
+    python tests/golden/make_golden.py [--ref /path/to/huji-rich] [case ...]
+
+Each fixture holds the packed mesh (``mesh_*``), the state (``cells0``,
+``ext0``), the edge velocities, and the reference's own outputs of one
+hot-path pass (``dt``, ``fluxes``, ``slopes``/``interp`` for second order,
+``ext1``, ``cells1``); cases with ``run > 0`` also hold the state after that
+many ``hdsim::TimeAdvance`` steps (``run_cells``, ``run_ext``, ``run_dts``).
+"""
+import argparse
+import glob
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+
+# name: (ref_dump case, nx, ny, warm steps, run steps)
+CASES = {
+    # 2D Sod, first order, Eulerian: one pass + 20 hdsim steps
+    "sod_o1": ("sod", 50, 10, 0, 20),
+    # the full 200x40 Sod tube of the first benchmark configuration, 200 steps
+    "sod_full_o1": ("sod", 200, 40, 0, 200),
+    # first order with moving (Lagrangian) faces after 3 steps
+    "sod_lagrangian_o1": ("sod_lagrangian", 50, 10, 3, 0),
+    # Sedov, LinearGaussImproved + rigid walls, RoundCells motion, after 3 steps
+    "sedov_o2": ("sedov", 24, 24, 3, 0),
+    # Sedov on a fixed mesh: one pass + 10 hdsim steps
+    "sedov_eulerian_o2": ("sedov_eulerian", 24, 24, 2, 10),
+    # periodic box, LinearGaussImproved + periodic ghosts, Eulerian: one pass + 10 steps
+    "periodic_o2": ("periodic", 16, 16, 2, 10),
+    # periodic box with Lagrangian faces after 2 steps
+    "periodic_lagrangian_o2": ("periodic_lagrangian", 16, 16, 2, 0),
+}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("cases", nargs="*")
+    a = ap.parse_args()
+    subprocess.check_call(["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle", "ref"),
+                           "REF=" + a.ref])
+    exe = os.path.join(ROOT, "oracle", "_ref", "ref_dump")
+    for name in a.cases or sorted(CASES):
+        case, nx, ny, warm, run = CASES[name]
+        with tempfile.TemporaryDirectory() as d:
+            subprocess.check_call([exe, case, d, str(nx), str(ny), str(warm), str(run)])
+            arrays = {os.path.basename(f)[:-4]: np.load(f) for f in glob.glob(os.path.join(d, "*.npy"))}
+        run_keys = [k for k in arrays if k.startswith("runmesh_")]
+        if run_keys and all(np.array_equal(arrays[k], arrays["mesh_" + k[8:]]) for k in run_keys):
+            # hdsim rebuilt an identical tessellation every step (Eulerian):
+            # the run continued on mesh_* itself
+            for k in run_keys:
+                del arrays[k]
+            arrays["run_mesh_unchanged"] = np.array(1)
+        arrays["case_params"] = np.array([nx, ny, warm, run], dtype=np.int64)
+        out = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(out, **arrays)
+        print(f"{name}: {len(arrays)} arrays, {os.path.getsize(out) / 1024:.0f} KiB", file=sys.stderr)
+
+
+if __name__ == "__main__":
+    main()
