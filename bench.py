@@ -1,0 +1,353 @@
+#!/usr/bin/env python3
+"""Benchmark of RICH's per-step hydro hot path on GB300.
+
+Workload (the headline configuration): 2D Sedov-Taylor on [-1,1]^2, a
+512x512 lattice of mesh points jittered by +-1e-3 of a cell (seeded), rigid
+walls, LinearGaussImproved second-order reconstruction, Hllc, IdealGas
+gamma=5/3, CFL 0.3, energy 1 deposited as pressure in r<0.02.  A step is one
+pass of the hot path: SimpleCFL dt, LinearGaussImproved + Hllc face fluxes,
+SimpleExtensiveUpdater gather, SimpleCellUpdater -- hdsim::TimeAdvance's
+plugin work with the mesh held fixed (the Voronoi rebuild is host code and
+out of scope).
+
+value  device-resident inputs; each step timed with CUDA events on the
+       library's stream, L2 flushed (256 MiB write) before every timed step.
+e2e    the same steps through the C ABI with host buffers, as a moving-mesh
+       caller drives it: upload of the packed tessellation and the face
+       velocities, the step, download of cells and extensives.
+--impl reference   the CPU implementation of the path (the C restatement of
+       the reference's algorithm, oracle/rich_oracle.c: the reference sources
+       are not on this machine) on all host cores, one independent
+       simulation per core.
+
+Multi-GPU: replicas only (one independent simulation per rank); value sums
+the cells all ranks updated over the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "huji-rich_gb300")
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+for _p in (PKG, ORACLE_DIR):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "cell-updates/s on 1 GB300: FP32-mixed vs FP64 at stated L1 error; adjoint/fwd cost"
+UNIT = "cell-updates/s"
+NX = NY = 512
+GAMMA = 5.0 / 3.0
+SEED = 2
+FLUSH_BYTES = 256 << 20
+
+
+def workload():
+    import synthetic
+    mesh = synthetic.lattice_mesh(NX, NY, (-1.0, 1.0, -1.0, 1.0), "rigid", seed=SEED)
+    cells = synthetic.sedov_cells(mesh, GAMMA)
+    return mesh, cells
+
+
+def config_block(mesh, precision="fp64"):
+    return {"workload": f"sedov2d_{NX}x{NY}_lgi_hllc_{precision}", "cells": mesh.n_cells,
+            "faces": mesh.n_faces, "ghosts": mesh.n_ghosts, "order": 2,
+            "reconstruction": "LinearGaussImproved(slf, delta_v=0.2, theta=0.5, delta_P=0.7)",
+            "riemann": "Hllc", "eos": "IdealGas(5/3)", "cfl": 0.3,
+            "mesh": f"{NX}x{NY} lattice jittered +-1e-3 cell, seed {SEED}, rigid walls",
+            "face_velocities": "zero in value (fixed mesh); e2e streams mesh + face velocities per step",
+            "l2": "flushed before every timed step (256 MiB write)", "parallelism": "replicas"}
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.count(",") >= 8]
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].strip() == "Active"})
+        power = [float(r[3]) for r in rows if r[3].strip().replace(".", "").isdigit()]
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows),
+                "power_w_max": max(power) if power else None}
+
+
+# ------------------------------------------------------------------ roofline
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel):
+    """dram bytes per launch of `kernel` from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "roofline_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        parts = line.split()
+        if len(parts) >= 2 and parts[0] == kernel and not line.startswith("#"):
+            return float(parts[1])
+    return None
+
+
+def algorithmic_bytes(mesh):
+    """Compulsory bytes per launch of each kernel of a step (FP64, order 2).
+    Geometry-only terms the design precomputes per mesh upload and the
+    intermediates (slopes, fluxes) are not algorithmic."""
+    n, f = mesh.n_cells, mesh.n_faces
+    m = int(mesh.cell_face_offset[-1])
+    return {
+        # cells in 32 + width 8 + CSR offset 4 per cell; face id 4 per CSR entry;
+        # face velocity 16 per face
+        "cfl": 44 * n + 4 * m + 16 * f,
+        # cells in 32, CM 16, mesh point 16, volume 8, CSR offset 4 per cell;
+        # neighbour id 4 per CSR entry
+        "slopes": 76 * n + 4 * m,
+        # face cell pair 8, vertex pair 32, face velocity 16 per face
+        "faces": 56 * f,
+        # extensive in 32 + out 32, cells out 32, cd volume 8, CSR offset 4 per
+        # cell; face id + side 8 per CSR entry
+        "update": 108 * n + 8 * m,
+    }
+
+
+# ------------------------------------------------------------------ CPU
+
+def cpu_steps(mesh, cells, ext, budget_s=10.0, max_steps=60):
+    import oracle
+    ev = np.zeros((mesh.n_faces, 2))
+    lp = oracle.lgi_params(0)
+    c, e = cells, ext
+    c, e, _ = oracle.step(mesh, c, e, ev, GAMMA, 0.3, 2, lp)  # warm
+    t0 = time.perf_counter()
+    k = 0
+    while k < max_steps and (time.perf_counter() - t0 < budget_s or k < 3):
+        c, e, _ = oracle.step(mesh, c, e, ev, GAMMA, 0.3, 2, lp)
+        k += 1
+    return k, time.perf_counter() - t0
+
+
+def _reference_worker(args):
+    steps, warmup = args
+    import oracle
+    mesh, cells = workload()
+    ext = oracle.init_extensives(mesh, cells, GAMMA)
+    ev = np.zeros((mesh.n_faces, 2))
+    lp = oracle.lgi_params(0)
+    c, e = cells, ext
+    for _ in range(warmup):
+        c, e, _ = oracle.step(mesh, c, e, ev, GAMMA, 0.3, 2, lp)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        c, e, _ = oracle.step(mesh, c, e, ev, GAMMA, 0.3, 2, lp)
+    return time.perf_counter() - t0, mesh.n_cells
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    import oracle
+    oracle.build()
+    cores = min(os.cpu_count() or 1, 64)
+    steps = max(1, min(args.steps, 20))
+    warm = max(1, min(args.warmup, 3))
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_reference_worker, [(steps, warm)] * cores)
+    t = max(r[0] for r in res)
+    n = res[0][1]
+    value = cores * n * steps / t
+    mesh, _ = workload()
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
+            "steps": steps, "warmup": warm, "ms_per_step": 1e3 * t / steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_block(mesh),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{cores} independent {NX}x{NY} simulations, one per core, "
+                                       f"{steps} timed steps each (C restatement oracle/rich_oracle.c, "
+                                       "gcc -O2; the reference sources are absent on this machine)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU
+
+def run_gpu(args, world, rank, local_rank):
+    import torch
+    import richgpu
+    import oracle
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    mesh, cells = workload()
+    ext = oracle.init_extensives(mesh, cells, GAMMA)
+    ev0 = np.zeros((mesh.n_faces, 2))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    h = richgpu.Handle(gamma=GAMMA, order=2, ghost_kind=0, device=local_rank)
+    h.upload_mesh(mesh)
+    h.set_cells(cells)
+    h.set_extensives(ext)
+    h.set_edge_velocities(ev0)
+    for _ in range(max(args.warmup, 3)):
+        h.step()
+    stream = torch.cuda.ExternalStream(h.device_buffers().stream)
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    clocks = ClockSampler(local_rank)
+    kms = []
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        _, k = h.step_timed()
+        kms.append(k)
+    torch.cuda.synchronize()
+    barrier()
+    wall = time.perf_counter() - wall0
+    clock = clocks.stop()
+    kms = np.array(kms)
+    step_ms = kms.sum(1)
+    total_ms = max_over_ranks(float(step_ms.sum()))
+    value = world * mesh.n_cells * args.steps / (total_ms * 1e-3)
+    names = ["cfl", "slopes", "faces", "update"]
+    mean_k = kms.mean(0)
+    dom = int(np.argmax(mean_k))
+    alg = algorithmic_bytes(mesh)
+    peak, peak_kind = measured_peaks()
+    achieved = alg[names[dom]] / (mean_k[dom] * 1e-3) / 1e9
+    traffic = ncu_traffic(names[dom])
+    step_alg = 172 * mesh.n_cells + 64 * mesh.n_faces
+
+    # end to end through the C ABI with host buffers (moving-mesh data flow)
+    ke = max(1, min(args.steps, 30))
+    h2d = mesh.nbytes() + 16 * mesh.n_faces
+    d2h = 2 * 32 * mesh.n_cells
+    upload_ms = []
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        h.upload_mesh(mesh)
+        upload_ms.append(h.last_upload_ms())
+        h.set_edge_velocities(ev0)
+        h.step()
+        h.get_cells()
+        h.get_extensives()
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e_value = world * mesh.n_cells * ke / e2e_s
+    launches = 4 * args.steps
+    h.close()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        k, t = cpu_steps(mesh, cells, ext)
+        cpu = {"value": mesh.n_cells * k / t, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"{k} steps of the same {NX}x{NY} workload, one thread, C restatement "
+                         "oracle/rich_oracle.c (gcc -O2); the reference itself is serial"}
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": max(args.warmup, 3), "ms_per_step": total_ms / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": config_block(mesh),
+                "roofline": {"bound": "hbm", "kernel": "k_faces_lgi" if names[dom] == "faces" else names[dom],
+                             "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                             "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)",
+                             "traffic": traffic,
+                             "algorithmic_bytes_per_launch": alg[names[dom]],
+                             "kernel_ms_mean": {n_: float(v) for n_, v in zip(names, mean_k)},
+                             "step_algorithmic_bytes": step_alg,
+                             "step_achieved_gbs": step_alg / (total_ms / args.steps * 1e-3) / 1e9,
+                             "note": "FP64 plain path: bound by GB300's FP64 pipe, not HBM"},
+                "cpu_baseline": cpu,
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                        "d2h_bytes_per_step": int(d2h), "steps": ke,
+                        "upload_ms_mean": float(np.mean(upload_ms))},
+                "gpu_launches": launches, "clocks": clock,
+                "faces_per_s": world * mesh.n_faces * args.steps / (total_ms * 1e-3),
+                "wall_s_timed_region": wall}
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_gpu(args, world, rank, local_rank)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,763 @@
+// rg_capi.cu -- the C ABI (include/rich_gb300.h): handle, mesh upload,
+// state transfer and the plugin operations, on top of the kernels in
+// rg_fp64.cu.
+//
+// Streams: every kernel of a handle runs on its compute stream.  Meshes are
+// double-buffered: rg_upload_mesh copies into the slot the compute stream is
+// not using, on a separate upload stream, computes that slot's geometry there
+// and makes the compute stream wait for it, so an upload overlaps whatever
+// compute work is still in flight on the previous mesh.
+//
+// Every index of a mesh is checked on the host before it is copied: the
+// kernels index with them unchecked.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdint>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "rg_internal.cuh"
+
+using rg::DevStatus;
+
+namespace {
+
+constexpr size_t kAlign = 256;
+inline size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t want) {
+    if (want <= bytes) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e == cudaSuccess) bytes = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+};
+
+struct HostBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t want) {
+    if (want <= bytes) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaHostAlloc(&p, want, cudaHostAllocDefault);
+    if (e == cudaSuccess) bytes = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+  }
+};
+
+// Offsets of every array of one mesh slot inside one allocation.  The input
+// arrays come first and form one contiguous block, mirrored byte for byte by
+// the pinned staging buffer so that one copy moves the whole mesh.
+struct SlotLayout {
+  size_t points, cms, volume, cd_volume, ghost_source, ghost_face, face_cells, face_vertices, cell_off,
+      cell_faces, input_end;
+  size_t area, nrm, nabs, par, dm0, dm1, width, minv, cflags, nbr, hr, ghost_real, ghost_unit, total;
+  void compute(int n, int g, int e, int m) {
+    const size_t np = static_cast<size_t>(n) + g;
+    size_t o = 0;
+    auto take = [&o](size_t bytes) {
+      const size_t at = o;
+      o = align_up(o + bytes);
+      return at;
+    };
+    points = take(16 * np);
+    cms = take(16 * np);
+    volume = take(8 * static_cast<size_t>(n));
+    cd_volume = take(8 * static_cast<size_t>(n));
+    ghost_source = take(4 * static_cast<size_t>(g));
+    ghost_face = take(4 * static_cast<size_t>(g));
+    face_cells = take(8 * static_cast<size_t>(e));
+    face_vertices = take(32 * static_cast<size_t>(e));
+    cell_off = take(4 * (static_cast<size_t>(n) + 1));
+    cell_faces = take(4 * static_cast<size_t>(m));
+    input_end = o;
+    area = take(8 * static_cast<size_t>(e));
+    nrm = take(16 * static_cast<size_t>(e));
+    nabs = take(8 * static_cast<size_t>(e));
+    par = take(16 * static_cast<size_t>(e));
+    dm0 = take(16 * static_cast<size_t>(e));
+    dm1 = take(16 * static_cast<size_t>(e));
+    width = take(8 * static_cast<size_t>(n));
+    minv = take(32 * static_cast<size_t>(n));
+    cflags = take(4 * static_cast<size_t>(n));
+    nbr = take(4 * static_cast<size_t>(m));
+    hr = take(16 * static_cast<size_t>(m));
+    ghost_real = take(4 * static_cast<size_t>(g));
+    ghost_unit = take(16 * static_cast<size_t>(g));
+    total = o;
+  }
+};
+
+struct MeshSlot {
+  int n = 0, g = 0, e = 0, m = 0;
+  bool valid = false;
+  DevBuf buf;
+  SlotLayout lay;
+  rg::MeshDev mesh{};
+  rg::GeomDev geom{};
+  rg_error geom_error{};  // reconstruction failure found by the geometry pass
+  cudaEvent_t last_use = nullptr;
+};
+
+template <class T>
+T* at(void* base, size_t off) {
+  return reinterpret_cast<T*>(static_cast<char*>(base) + off);
+}
+
+}  // namespace
+
+struct rg_handle {
+  rg_config cfg{};
+  cudaStream_t stream = nullptr;
+  cudaStream_t upload_stream = nullptr;
+  cudaEvent_t ev_up0 = nullptr, ev_up1 = nullptr;
+  cudaEvent_t ev_k[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  MeshSlot slots[2];
+  int active = -1;
+  // state
+  DevBuf cells, ext, ev, slopes, fluxes, status_buf;
+  size_t cells_records = 0;
+  bool have_cells = false, have_ext = false, have_ev = false, have_fluxes = false;
+  HostBuf staging, host_status, host_dts;
+  DevStatus* d_status = nullptr;
+  DevStatus* d_geom_status = nullptr;
+  rg_error last{};
+  double last_upload_ms = 0;
+  double last_dt = 0;
+  int step_seq = 0;
+};
+
+namespace {
+
+rg_status cuda_fail(rg_handle* h, cudaError_t e) {
+  if (h) {
+    h->last = rg_error{RG_ERR_CUDA, 0, static_cast<int64_t>(e), 0.0};
+  }
+  cudaGetLastError();
+  return e == cudaErrorMemoryAllocation ? RG_ERR_OUT_OF_MEMORY : RG_ERR_CUDA;
+}
+
+rg_status invalid(rg_handle* h, int64_t index, double value) {
+  if (h) h->last = rg_error{RG_ERR_INVALID_ARGUMENT, 0, index, value};
+  return RG_ERR_INVALID_ARGUMENT;
+}
+
+#define RG_CUDA(h, call)                            \
+  do {                                              \
+    cudaError_t e_ = (call);                        \
+    if (e_ != cudaSuccess) return cuda_fail(h, e_); \
+  } while (0)
+#define RG_TRY(call)                  \
+  do {                                \
+    rg_status s_ = (call);            \
+    if (s_ != RG_OK) return s_;       \
+  } while (0)
+
+// Host-side validation of a packed mesh; returns the index of the first bad
+// entry through *bad (encoded per array) or 0 if the mesh is consistent.
+rg_status validate(rg_handle* h, const rg_mesh_view* v) {
+  if (!v || v->n_cells <= 0 || v->n_ghosts < 0 || v->n_faces < 0) return invalid(h, -1, 0);
+  if (static_cast<int64_t>(v->n_cells) + v->n_ghosts > static_cast<int64_t>(rg::kNbrIdMask))
+    return invalid(h, -2, 0);
+  if (!v->point_xy || !v->cm_xy || !v->volume || !v->cd_volume || !v->face_cells || !v->face_vertices ||
+      !v->cell_face_offset || !v->cell_faces)
+    return invalid(h, -3, 0);
+  if (v->n_ghosts > 0 && (!v->ghost_source || !v->ghost_face)) return invalid(h, -3, 0);
+  const int n = v->n_cells, g = v->n_ghosts, e = v->n_faces;
+  const int np = n + g;
+  for (int f = 0; f < e; ++f) {
+    const int a = v->face_cells[2 * f], b = v->face_cells[2 * f + 1];
+    if (a < 0 || a >= np || b < 0 || b >= np || a == b || (a >= n && b >= n))
+      return invalid(h, f, static_cast<double>(a >= 0 && a < np ? b : a));
+  }
+  for (int k = 0; k < g; ++k) {
+    if (v->ghost_source[k] < 0 || v->ghost_source[k] >= n) return invalid(h, k, v->ghost_source[k]);
+    const int gf = v->ghost_face[k];
+    if (gf < -1 || gf >= e) return invalid(h, k, gf);
+    if (gf >= 0 && v->face_cells[2 * gf] != n + k && v->face_cells[2 * gf + 1] != n + k)
+      return invalid(h, k, gf);
+  }
+  if (v->cell_face_offset[0] != 0) return invalid(h, 0, v->cell_face_offset[0]);
+  for (int i = 0; i < n; ++i) {
+    const int b = v->cell_face_offset[i], en = v->cell_face_offset[i + 1];
+    if (en < b || en - b > (1 << 20)) return invalid(h, i, en);
+    for (int k = b; k < en; ++k) {
+      const int f = v->cell_faces[k];
+      if (f < 0 || f >= e) return invalid(h, i, f);
+      if (k > b && f <= v->cell_faces[k - 1]) return invalid(h, i, f);  // ascending order
+      if (v->face_cells[2 * f] != i && v->face_cells[2 * f + 1] != i) return invalid(h, i, f);
+    }
+  }
+  return RG_OK;
+}
+
+void fill_views(MeshSlot& s) {
+  void* b = s.buf.p;
+  const SlotLayout& L = s.lay;
+  s.mesh.n = s.n;
+  s.mesh.g = s.g;
+  s.mesh.e = s.e;
+  s.mesh.m = s.m;
+  s.mesh.points = at<double2>(b, L.points);
+  s.mesh.cms = at<double2>(b, L.cms);
+  s.mesh.volume = at<double>(b, L.volume);
+  s.mesh.cd_volume = at<double>(b, L.cd_volume);
+  s.mesh.ghost_source = at<int>(b, L.ghost_source);
+  s.mesh.ghost_face = at<int>(b, L.ghost_face);
+  s.mesh.face_cells = at<int2>(b, L.face_cells);
+  s.mesh.face_vertices = at<rg::dbl4>(b, L.face_vertices);
+  s.mesh.cell_off = at<int>(b, L.cell_off);
+  s.mesh.cell_faces = at<int>(b, L.cell_faces);
+  s.geom.area = at<double>(b, L.area);
+  s.geom.nrm = at<double2>(b, L.nrm);
+  s.geom.nabs = at<double>(b, L.nabs);
+  s.geom.par = at<double2>(b, L.par);
+  s.geom.dm0 = at<double2>(b, L.dm0);
+  s.geom.dm1 = at<double2>(b, L.dm1);
+  s.geom.width = at<double>(b, L.width);
+  s.geom.minv = at<rg::dbl4>(b, L.minv);
+  s.geom.cflags = at<int>(b, L.cflags);
+  s.geom.nbr = at<uint32_t>(b, L.nbr);
+  s.geom.hr = at<double2>(b, L.hr);
+  s.geom.ghost_real = at<int>(b, L.ghost_real);
+  s.geom.ghost_unit = at<double2>(b, L.ghost_unit);
+}
+
+rg_status reset_status(rg_handle* h, DevStatus* st, cudaStream_t s) {
+  // error part only: err_key = ~0, err_status = lock = 0
+  RG_CUDA(h, cudaMemsetAsync(&st->err_key, 0xff, sizeof(unsigned long long), s));
+  RG_CUDA(h, cudaMemsetAsync(&st->err_status, 0, 2 * sizeof(int), s));
+  return RG_OK;
+}
+
+// Reads the status block after the stream is idle; returns the error (if any).
+rg_status collect(rg_handle* h, DevStatus* st, cudaStream_t s) {
+  DevStatus* hs = static_cast<DevStatus*>(h->host_status.p);
+  RG_CUDA(h, cudaMemcpyAsync(hs, st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
+  RG_CUDA(h, cudaStreamSynchronize(s));
+  RG_CUDA(h, cudaGetLastError());
+  h->last_dt = hs->dt;
+  if (hs->err_key != ~0ull) {
+    const unsigned long long key = hs->err_key;
+    h->last = rg_error{hs->err_status, static_cast<int32_t>((key >> rg::kKeyPhaseShift) & 0xf),
+                       static_cast<int64_t>(key & rg::kKeyIndexMask), hs->err_value};
+    if (h->last.status == 0) h->last.status = RG_ERR_CUDA;  // key won a lock race; value stale
+    return static_cast<rg_status>(h->last.status);
+  }
+  return RG_OK;
+}
+
+MeshSlot* active_slot(rg_handle* h) { return h->active < 0 ? nullptr : &h->slots[h->active]; }
+
+rg::StepArgs step_args(rg_handle* h) {
+  MeshSlot* s = active_slot(h);
+  rg::StepArgs a{};
+  a.mesh = s->mesh;
+  a.geom = s->geom;
+  a.gamma = h->cfg.gamma;
+  a.cfl = h->cfg.cfl;
+  a.order = h->cfg.order;
+  a.ghost_kind = h->cfg.ghost_kind;
+  a.slf = h->cfg.slope_limiter;
+  a.delta_v = h->cfg.delta_v;
+  a.theta = h->cfg.theta;
+  a.delta_p = h->cfg.delta_p;
+  a.cells = static_cast<double*>(h->cells.p);
+  a.ext = static_cast<double*>(h->ext.p);
+  a.ev = static_cast<const double*>(h->ev.p);
+  a.slopes = static_cast<double*>(h->slopes.p);
+  a.fluxes = static_cast<double*>(h->fluxes.p);
+  a.status = h->d_status;
+  a.dt_host = 0;
+  a.dt_from_device = 0;
+  a.step = 0;
+  return a;
+}
+
+rg_status require(rg_handle* h, bool cells, bool ext, bool ev, bool fluxes) {
+  if (!h) return RG_ERR_INVALID_ARGUMENT;
+  if (h->active < 0 || (cells && !h->have_cells) || (ext && !h->have_ext) || (ev && !h->have_ev) ||
+      (fluxes && !h->have_fluxes)) {
+    h->last = rg_error{RG_ERR_NOT_READY, 0, -1, 0};
+    return RG_ERR_NOT_READY;
+  }
+  return RG_OK;
+}
+
+rg_status mesh_error(rg_handle* h) {
+  MeshSlot* s = active_slot(h);
+  if (h->cfg.order == 2 && s->geom_error.status != 0) {
+    h->last = s->geom_error;
+    return static_cast<rg_status>(s->geom_error.status);
+  }
+  return RG_OK;
+}
+
+// Enqueues one fused step (no host synchronisation).  With ev != nullptr,
+// records ev[0..4] around its kernels.
+rg_status enqueue_step(rg_handle* h, int step, cudaEvent_t* ev = nullptr) {
+  rg::StepArgs a = step_args(h);
+  a.dt_from_device = 1;
+  a.step = step;
+  if (ev) RG_CUDA(h, cudaEventRecord(ev[0], h->stream));
+  RG_CUDA(h, rg::launch_cfl(a, h->stream, h->cfg.order == 2));
+  if (ev) RG_CUDA(h, cudaEventRecord(ev[1], h->stream));
+  if (h->cfg.order == 2) RG_CUDA(h, rg::launch_slopes(a, h->stream));
+  if (ev) RG_CUDA(h, cudaEventRecord(ev[2], h->stream));
+  RG_CUDA(h, rg::launch_faces(a, h->stream, true));
+  if (ev) RG_CUDA(h, cudaEventRecord(ev[3], h->stream));
+  RG_CUDA(h, rg::launch_update(a, h->stream, false, true, true));
+  if (ev) RG_CUDA(h, cudaEventRecord(ev[4], h->stream));
+  h->have_fluxes = false;  // the buffer now holds dt*area-scaled fluxes
+  return RG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void rg_default_config(rg_config* c) {
+  if (!c) return;
+  std::memset(c, 0, sizeof *c);
+  c->gamma = 5.0 / 3.0;
+  c->cfl = 0.3;
+  c->order = 2;
+  c->ghost_kind = RG_GHOST_RIGID_WALL;
+  c->slope_limiter = 1;
+  c->precision = RG_FP64;
+  c->delta_v = 0.2;
+  c->theta = 0.5;
+  c->delta_p = 0.7;
+  c->device = 0;
+}
+
+const char* rg_status_string(rg_status s) {
+  switch (s) {
+    case RG_OK: return "ok";
+    case RG_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case RG_ERR_CUDA: return "CUDA error";
+    case RG_ERR_NOT_READY: return "not ready (mesh or state missing)";
+    case RG_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case RG_ERR_NEGATIVE_DENSITY: return "Negative density";
+    case RG_ERR_NEGATIVE_ENERGY: return "Negative thermal energy";
+    case RG_ERR_HLLC_NAN: return "Hllc::Solved entered with nan";
+    case RG_ERR_HLLC_WAVE_SPEEDS: return "Invalid wave speeds in hllc solver";
+    case RG_ERR_SINGULAR_MATRIX: return "Singular matrix";
+    case RG_ERR_TOO_MANY_NEIGHBORS: return "Cell has too many neighbors";
+  }
+  return "unknown status";
+}
+
+rg_status rg_create(const rg_config* cfg, rg_handle** out) {
+  if (!cfg || !out) return RG_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (cfg->order != 1 && cfg->order != 2) return RG_ERR_INVALID_ARGUMENT;
+  if (cfg->ghost_kind != RG_GHOST_RIGID_WALL && cfg->ghost_kind != RG_GHOST_PERIODIC)
+    return RG_ERR_INVALID_ARGUMENT;
+  if (cfg->precision != RG_FP64 && cfg->precision != RG_FP32_MIXED) return RG_ERR_INVALID_ARGUMENT;
+  if (!(cfg->gamma > 1.0) || !(cfg->cfl > 0.0)) return RG_ERR_INVALID_ARGUMENT;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= cfg->device || cfg->device < 0) {
+    cudaGetLastError();
+    return RG_ERR_CUDA;
+  }
+  rg_handle* h = new (std::nothrow) rg_handle();
+  if (!h) return RG_ERR_OUT_OF_MEMORY;
+  h->cfg = *cfg;
+  auto fail = [&](cudaError_t e) {
+    rg_destroy(h);
+    cudaGetLastError();
+    return e == cudaErrorMemoryAllocation ? RG_ERR_OUT_OF_MEMORY : RG_ERR_CUDA;
+  };
+  cudaError_t e;
+  if ((e = cudaSetDevice(cfg->device)) != cudaSuccess) return fail(e);
+  if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
+  if ((e = cudaStreamCreateWithFlags(&h->upload_stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
+  if ((e = cudaEventCreateWithFlags(&h->ev_up0, cudaEventDefault)) != cudaSuccess) return fail(e);
+  if ((e = cudaEventCreateWithFlags(&h->ev_up1, cudaEventDefault)) != cudaSuccess) return fail(e);
+  for (auto& s : h->slots)
+    if ((e = cudaEventCreateWithFlags(&s.last_use, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
+  for (auto& k : h->ev_k)
+    if ((e = cudaEventCreateWithFlags(&k, cudaEventDefault)) != cudaSuccess) return fail(e);
+  if ((e = h->status_buf.ensure(2 * sizeof(DevStatus))) != cudaSuccess) return fail(e);
+  h->d_status = static_cast<DevStatus*>(h->status_buf.p);
+  h->d_geom_status = h->d_status + 1;
+  DevStatus init{};
+  init.err_key = ~0ull;
+  init.dt_min_bits = rg::kInfBits;
+  DevStatus both[2] = {init, init};
+  if ((e = cudaMemcpy(h->d_status, both, sizeof both, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e);
+  if ((e = h->host_status.ensure(sizeof(DevStatus))) != cudaSuccess) return fail(e);
+  *out = h;
+  return RG_OK;
+}
+
+rg_status rg_destroy(rg_handle* h) {
+  if (!h) return RG_OK;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->upload_stream) cudaStreamSynchronize(h->upload_stream);
+  for (auto& s : h->slots) {
+    s.buf.release();
+    if (s.last_use) cudaEventDestroy(s.last_use);
+  }
+  h->cells.release();
+  h->ext.release();
+  h->ev.release();
+  h->slopes.release();
+  h->fluxes.release();
+  h->status_buf.release();
+  h->staging.release();
+  h->host_status.release();
+  h->host_dts.release();
+  for (auto& k : h->ev_k)
+    if (k) cudaEventDestroy(k);
+  if (h->ev_up0) cudaEventDestroy(h->ev_up0);
+  if (h->ev_up1) cudaEventDestroy(h->ev_up1);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  if (h->upload_stream) cudaStreamDestroy(h->upload_stream);
+  cudaGetLastError();
+  delete h;
+  return RG_OK;
+}
+
+rg_status rg_last_error(const rg_handle* h, rg_error* err) {
+  if (!h || !err) return RG_ERR_INVALID_ARGUMENT;
+  *err = h->last;
+  return RG_OK;
+}
+
+rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t /*flags*/) {
+  if (!h) return RG_ERR_INVALID_ARGUMENT;
+  h->last = rg_error{};
+  const auto t0 = std::chrono::steady_clock::now();
+  if (rg_status st = validate(h, v)) return st;
+  RG_CUDA(h, cudaSetDevice(h->cfg.device));
+  const int n = v->n_cells, g = v->n_ghosts, e = v->n_faces, m = v->cell_face_offset[n];
+  if (h->active >= 0 && active_slot(h)->n != n) {
+    // the cell count changed: the state no longer matches the mesh
+    h->have_cells = h->have_ext = false;
+  }
+  const int next = h->active < 0 ? 0 : 1 - h->active;
+  MeshSlot& s = h->slots[next];
+  // the slot may still be read by kernels enqueued on the previous-but-one mesh
+  RG_CUDA(h, cudaStreamWaitEvent(h->upload_stream, s.last_use, 0));
+  s.lay.compute(n, g, e, m);
+  RG_CUDA(h, cudaStreamSynchronize(h->upload_stream));
+  RG_CUDA(h, s.buf.ensure(s.lay.total));
+  RG_CUDA(h, h->staging.ensure(s.lay.input_end));
+  s.n = n;
+  s.g = g;
+  s.e = e;
+  s.m = m;
+  fill_views(s);
+  // pack into pinned staging with the device layout, then one async copy
+  char* st = static_cast<char*>(h->staging.p);
+  const size_t np = static_cast<size_t>(n) + g;
+  std::memcpy(st + s.lay.points, v->point_xy, 16 * np);
+  std::memcpy(st + s.lay.cms, v->cm_xy, 16 * np);
+  std::memcpy(st + s.lay.volume, v->volume, 8 * static_cast<size_t>(n));
+  std::memcpy(st + s.lay.cd_volume, v->cd_volume, 8 * static_cast<size_t>(n));
+  if (g) {
+    std::memcpy(st + s.lay.ghost_source, v->ghost_source, 4 * static_cast<size_t>(g));
+    std::memcpy(st + s.lay.ghost_face, v->ghost_face, 4 * static_cast<size_t>(g));
+  }
+  std::memcpy(st + s.lay.face_cells, v->face_cells, 8 * static_cast<size_t>(e));
+  std::memcpy(st + s.lay.face_vertices, v->face_vertices, 32 * static_cast<size_t>(e));
+  std::memcpy(st + s.lay.cell_off, v->cell_face_offset, 4 * (static_cast<size_t>(n) + 1));
+  std::memcpy(st + s.lay.cell_faces, v->cell_faces, 4 * static_cast<size_t>(m));
+  RG_CUDA(h, cudaEventRecord(h->ev_up0, h->upload_stream));
+  RG_CUDA(h, cudaMemcpyAsync(s.buf.p, st, s.lay.input_end, cudaMemcpyHostToDevice, h->upload_stream));
+  // geometry pass on the upload stream
+  RG_TRY(reset_status(h, h->d_geom_status, h->upload_stream));
+  rg::GeomArgs ga{};
+  ga.mesh = s.mesh;
+  ga.order = h->cfg.order;
+  void* b = s.buf.p;
+  ga.area = at<double>(b, s.lay.area);
+  ga.nrm = at<double2>(b, s.lay.nrm);
+  ga.nabs = at<double>(b, s.lay.nabs);
+  ga.par = at<double2>(b, s.lay.par);
+  ga.dm0 = at<double2>(b, s.lay.dm0);
+  ga.dm1 = at<double2>(b, s.lay.dm1);
+  ga.width = at<double>(b, s.lay.width);
+  ga.minv = at<rg::dbl4>(b, s.lay.minv);
+  ga.cflags = at<int>(b, s.lay.cflags);
+  ga.nbr = at<uint32_t>(b, s.lay.nbr);
+  ga.hr = at<double2>(b, s.lay.hr);
+  ga.ghost_real = at<int>(b, s.lay.ghost_real);
+  ga.ghost_unit = at<double2>(b, s.lay.ghost_unit);
+  ga.ghost_kind = h->cfg.ghost_kind;
+  ga.status = h->d_geom_status;
+  RG_CUDA(h, rg::launch_geometry(ga, h->upload_stream));
+  RG_CUDA(h, cudaEventRecord(h->ev_up1, h->upload_stream));
+  // state buffers sized for this mesh (cells keep their first n records)
+  const size_t rec = np;
+  if (rec > h->cells_records) {
+    DevBuf nb;
+    RG_CUDA(h, nb.ensure(32 * rec));
+    RG_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (h->cells.p && h->have_cells)
+      RG_CUDA(h, cudaMemcpy(nb.p, h->cells.p, 32 * static_cast<size_t>(n), cudaMemcpyDeviceToDevice));
+    h->cells.release();
+    h->cells = nb;
+    h->cells_records = rec;
+  }
+  const bool ext_keep = h->ext.bytes >= 32 * static_cast<size_t>(n);
+  RG_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (!ext_keep) h->have_ext = false;
+  RG_CUDA(h, h->ext.ensure(32 * static_cast<size_t>(n)));
+  if (h->ev.bytes < 16 * static_cast<size_t>(e)) h->have_ev = false;
+  RG_CUDA(h, h->ev.ensure(16 * static_cast<size_t>(std::max(e, 1))));
+  RG_CUDA(h, h->slopes.ensure(64 * static_cast<size_t>(n)));
+  RG_CUDA(h, h->fluxes.ensure(32 * static_cast<size_t>(std::max(e, 1))));
+  if (h->active >= 0 && active_slot(h)->e != e) h->have_ev = false;
+  h->have_fluxes = false;
+  // geometry errors (reconstruction would throw them) and timing
+  DevStatus* hs = static_cast<DevStatus*>(h->host_status.p);
+  RG_CUDA(h, cudaMemcpyAsync(hs, h->d_geom_status, sizeof(DevStatus), cudaMemcpyDeviceToHost, h->upload_stream));
+  RG_CUDA(h, cudaStreamSynchronize(h->upload_stream));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, h->ev_up0, h->ev_up1);
+  s.geom_error = rg_error{};
+  if (hs->err_key != ~0ull)
+    s.geom_error = rg_error{hs->err_status, 2, static_cast<int64_t>(hs->err_key & rg::kKeyIndexMask), hs->err_value};
+  // later compute work on the stream sees the new slot
+  RG_CUDA(h, cudaStreamWaitEvent(h->stream, h->ev_up1, 0));
+  if (h->active >= 0) RG_CUDA(h, cudaEventRecord(h->slots[h->active].last_use, h->stream));
+  h->active = next;
+  s.valid = true;
+  h->last_upload_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  (void)ms;
+  if (h->cfg.order == 2 && s.geom_error.status) {
+    h->last = s.geom_error;
+    return static_cast<rg_status>(s.geom_error.status);
+  }
+  return RG_OK;
+}
+
+rg_status rg_last_upload_ms(const rg_handle* h, double* ms) {
+  if (!h || !ms) return RG_ERR_INVALID_ARGUMENT;
+  *ms = h->last_upload_ms;
+  return RG_OK;
+}
+
+rg_status rg_set_cells(rg_handle* h, const double* cells) {
+  if (!h || !cells) return RG_ERR_INVALID_ARGUMENT;
+  if (h->active < 0) return require(h, false, false, false, false);
+  RG_CUDA(h, cudaMemcpyAsync(h->cells.p, cells, 32 * static_cast<size_t>(active_slot(h)->n),
+                             cudaMemcpyHostToDevice, h->stream));
+  RG_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->have_cells = true;
+  return RG_OK;
+}
+
+rg_status rg_get_cells(rg_handle* h, double* cells) {
+  if (rg_status st = require(h, true, false, false, false)) return st;
+  if (!cells) return RG_ERR_INVALID_ARGUMENT;
+  RG_CUDA(h, cudaMemcpyAsync(cells, h->cells.p, 32 * static_cast<size_t>(active_slot(h)->n),
+                             cudaMemcpyDeviceToHost, h->stream));
+  RG_CUDA(h, cudaStreamSynchronize(h->stream));
+  return RG_OK;
+}
+
+rg_status rg_set_extensives(rg_handle* h, const double* ext) {
+  if (!h || !ext) return RG_ERR_INVALID_ARGUMENT;
+  if (h->active < 0) return require(h, false, false, false, false);
+  RG_CUDA(h, cudaMemcpyAsync(h->ext.p, ext, 32 * static_cast<size_t>(active_slot(h)->n),
+                             cudaMemcpyHostToDevice, h->stream));
+  RG_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->have_ext = true;
+  return RG_OK;
+}
+
+rg_status rg_get_extensives(rg_handle* h, double* ext) {
+  if (rg_status st = require(h, false, true, false, false)) return st;
+  if (!ext) return RG_ERR_INVALID_ARGUMENT;
+  RG_CUDA(h, cudaMemcpyAsync(ext, h->ext.p, 32 * static_cast<size_t>(active_slot(h)->n),
+                             cudaMemcpyDeviceToHost, h->stream));
+  RG_CUDA(h, cudaStreamSynchronize(h->stream));
+  return RG_OK;
+}
+
+rg_status rg_set_edge_velocities(rg_handle* h, const double* ev) {
+  if (!h || !ev) return RG_ERR_INVALID_ARGUMENT;
+  if (h->active < 0) return require(h, false, false, false, false);
+  RG_CUDA(h, cudaMemcpyAsync(h->ev.p, ev, 16 * static_cast<size_t>(active_slot(h)->e),
+                             cudaMemcpyHostToDevice, h->stream));
+  RG_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->have_ev = true;
+  return RG_OK;
+}
+
+rg_status rg_set_fluxes(rg_handle* h, const double* fl) {
+  if (!h || !fl) return RG_ERR_INVALID_ARGUMENT;
+  if (h->active < 0) return require(h, false, false, false, false);
+  RG_CUDA(h, cudaMemcpyAsync(h->fluxes.p, fl, 32 * static_cast<size_t>(active_slot(h)->e),
+                             cudaMemcpyHostToDevice, h->stream));
+  RG_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->have_fluxes = true;
+  return RG_OK;
+}
+
+rg_status rg_device_buffers(rg_handle* h, rg_device_view* v) {
+  if (!h || !v) return RG_ERR_INVALID_ARGUMENT;
+  if (h->active < 0) return require(h, false, false, false, false);
+  v->cells = static_cast<double*>(h->cells.p);
+  v->extensives = static_cast<double*>(h->ext.p);
+  v->edge_velocities = static_cast<double*>(h->ev.p);
+  v->fluxes = static_cast<double*>(h->fluxes.p);
+  v->stream = h->stream;
+  // a caller writing through these pointers provides the state
+  h->have_cells = h->have_ext = h->have_ev = true;
+  return RG_OK;
+}
+
+rg_status rg_init_extensives(rg_handle* h) {
+  if (rg_status st = require(h, true, false, false, false)) return st;
+  rg::StepArgs a = step_args(h);
+  RG_CUDA(h, rg::launch_init_extensives(a, h->stream));
+  RG_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->have_ext = true;
+  return RG_OK;
+}
+
+rg_status rg_cfl_dt(rg_handle* h, double* dt) {
+  if (rg_status st = require(h, true, false, true, false)) return st;
+  if (!dt) return RG_ERR_INVALID_ARGUMENT;
+  h->last = rg_error{};
+  RG_TRY(reset_status(h, h->d_status, h->stream));
+  rg::StepArgs a = step_args(h);
+  RG_CUDA(h, rg::launch_cfl(a, h->stream, false));
+  rg_status st = collect(h, h->d_status, h->stream);
+  *dt = h->last_dt;
+  return st;
+}
+
+rg_status rg_flux(rg_handle* h, double dt, double* fluxes_out) {
+  if (rg_status st = require(h, true, false, true, false)) return st;
+  h->last = rg_error{};
+  if (rg_status st = mesh_error(h)) return st;
+  RG_TRY(reset_status(h, h->d_status, h->stream));
+  rg::StepArgs a = step_args(h);
+  a.dt_host = dt;
+  if (h->cfg.order == 2) {
+    RG_CUDA(h, rg::launch_ghost_fill(a, h->stream));
+    RG_CUDA(h, rg::launch_slopes(a, h->stream));
+  }
+  RG_CUDA(h, rg::launch_faces(a, h->stream, false));
+  if (rg_status st = collect(h, h->d_status, h->stream)) return st;
+  h->have_fluxes = true;
+  if (fluxes_out) {
+    RG_CUDA(h, cudaMemcpyAsync(fluxes_out, h->fluxes.p, 32 * static_cast<size_t>(active_slot(h)->e),
+                               cudaMemcpyDeviceToHost, h->stream));
+    RG_CUDA(h, cudaStreamSynchronize(h->stream));
+  }
+  return RG_OK;
+}
+
+rg_status rg_extensive_update(rg_handle* h, double dt) {
+  if (rg_status st = require(h, false, true, false, true)) return st;
+  h->last = rg_error{};
+  RG_TRY(reset_status(h, h->d_status, h->stream));
+  rg::StepArgs a = step_args(h);
+  a.dt_host = dt;
+  RG_CUDA(h, rg::launch_update(a, h->stream, true, true, false));
+  return collect(h, h->d_status, h->stream);
+}
+
+rg_status rg_cell_update(rg_handle* h) {
+  if (rg_status st = require(h, false, true, false, false)) return st;
+  h->last = rg_error{};
+  RG_TRY(reset_status(h, h->d_status, h->stream));
+  rg::StepArgs a = step_args(h);
+  RG_CUDA(h, rg::launch_update(a, h->stream, false, false, true));
+  rg_status st = collect(h, h->d_status, h->stream);
+  if (st == RG_OK) h->have_cells = true;
+  return st;
+}
+
+rg_status rg_step_async(rg_handle* h) {
+  if (rg_status st = require(h, true, true, true, false)) return st;
+  if (rg_status st = mesh_error(h)) return st;
+  if (h->step_seq == 0) RG_TRY(reset_status(h, h->d_status, h->stream));
+  rg_status st = enqueue_step(h, h->step_seq);
+  h->step_seq = std::min(h->step_seq + 1, 0x1fff);
+  return st;
+}
+
+rg_status rg_synchronize(rg_handle* h, double* dt_last) {
+  if (!h) return RG_ERR_INVALID_ARGUMENT;
+  h->last = rg_error{};
+  h->step_seq = 0;
+  rg_status st = collect(h, h->d_status, h->stream);
+  if (dt_last) *dt_last = h->last_dt;
+  return st;
+}
+
+rg_status rg_step(rg_handle* h, double* dt_out) {
+  if (rg_status st = require(h, true, true, true, false)) return st;
+  if (rg_status st = mesh_error(h)) return st;
+  h->last = rg_error{};
+  RG_TRY(reset_status(h, h->d_status, h->stream));
+  if (rg_status st = enqueue_step(h, 0)) return st;
+  rg_status st = collect(h, h->d_status, h->stream);
+  if (dt_out) *dt_out = h->last_dt;
+  return st;
+}
+
+rg_status rg_step_timed(rg_handle* h, double* dt_out, float* kernel_ms) {
+  if (rg_status st = require(h, true, true, true, false)) return st;
+  if (rg_status st = mesh_error(h)) return st;
+  if (!kernel_ms) return RG_ERR_INVALID_ARGUMENT;
+  h->last = rg_error{};
+  RG_TRY(reset_status(h, h->d_status, h->stream));
+  if (rg_status st = enqueue_step(h, 0, h->ev_k)) return st;
+  rg_status st = collect(h, h->d_status, h->stream);
+  for (int k = 0; k < 4; ++k) {
+    kernel_ms[k] = 0;
+    RG_CUDA(h, cudaEventElapsedTime(&kernel_ms[k], h->ev_k[k], h->ev_k[k + 1]));
+  }
+  if (dt_out) *dt_out = h->last_dt;
+  return st;
+}
+
+rg_status rg_run(rg_handle* h, int32_t n_steps, double* dt_out) {
+  if (rg_status st = require(h, true, true, true, false)) return st;
+  if (n_steps < 0) return RG_ERR_INVALID_ARGUMENT;
+  if (rg_status st = mesh_error(h)) return st;
+  h->last = rg_error{};
+  RG_TRY(reset_status(h, h->d_status, h->stream));
+  if (dt_out) RG_CUDA(h, h->host_dts.ensure(sizeof(double) * static_cast<size_t>(std::max(n_steps, 1))));
+  double* hd = static_cast<double*>(h->host_dts.p);
+  for (int k = 0; k < n_steps; ++k) {
+    if (rg_status st = enqueue_step(h, std::min(k, 0x1fff))) return st;
+    if (dt_out)
+      RG_CUDA(h, cudaMemcpyAsync(hd + k, &h->d_status->dt, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  }
+  rg_status st = collect(h, h->d_status, h->stream);
+  if (dt_out) std::memcpy(dt_out, hd, sizeof(double) * static_cast<size_t>(n_steps));
+  return st;
+}
+
+}  // extern "C"

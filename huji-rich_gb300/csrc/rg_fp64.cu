@@ -1,0 +1,695 @@
+// rg_fp64.cu -- plain-FP64 kernels of the hydro hot path for sm_103a.
+//
+// Compiled with --fmad=false: every multiply and add rounds separately, in
+// the reference's order, so results are bit-identical to the reference's
+// FP64 path (IEEE division and square root are exact-rounded on the device
+// as on the host).  Each device function cites the reference code it
+// restates (paths relative to the RICH source root).
+//
+// Passes of one step (hdsim::TimeAdvance, hdsim2d.cpp:149-241, fixed mesh):
+//   k_cfl        per cell: SimpleCFL bound, block min, last block writes dt;
+//                extra threads fill the ghost states
+//   k_slopes     per cell: LinearGaussImproved slope + limiter (order 2)
+//   k_faces_*    per face: reconstruction to the face, HLLC in the face frame,
+//                rotation back, optional dt*area scaling
+//   k_update     per cell: ascending-face CSR gather of the face fluxes
+//                (SimpleExtensiveUpdater order, no atomics) + SimpleCellUpdater
+// Geometry-only terms are computed once per mesh upload (k_geom_*).
+#include <math.h>
+
+#include "rg_internal.cuh"
+
+namespace rg {
+namespace {
+
+constexpr int kBlock = 256;
+
+struct Cell { double d, p, vx, vy; };
+struct Prim { double d, p, vx, vy, e, c; };
+struct Cons { double m, mx, my, en; };
+
+__device__ __forceinline__ Cell load_cell(const double* cells, int i) {
+  const double2 a = reinterpret_cast<const double2*>(cells)[2 * i];
+  const double2 b = reinterpret_cast<const double2*>(cells)[2 * i + 1];
+  return Cell{a.x, a.y, b.x, b.y};
+}
+__device__ __forceinline__ void store4(double* out, int i, double a, double b, double c, double d) {
+  reinterpret_cast<double2*>(out)[2 * i] = make_double2(a, b);
+  reinterpret_cast<double2*>(out)[2 * i + 1] = make_double2(c, d);
+}
+__device__ __forceinline__ int orig_of(const MeshDev& m, int p) {
+  return p < m.n ? p : m.ghost_source[p - m.n];
+}
+// computational_cell_2d.cpp:59-68 ComputationalCellAddMult
+__device__ __forceinline__ void addmult(Cell& r, const Cell& o, double s) {
+  r.d += o.d * s;
+  r.p += o.p * s;
+  r.vx += o.vx * s;
+  r.vy += o.vy * s;
+}
+
+// ---------------------------------------------------------------- geometry
+
+// Per face: physical_geometry.cpp:8-11 calcArea, Edge.cpp:83-86 Parallel,
+// spatial_reconstruction.cpp:3-6 CalcCentroid, the flux-frame normal of
+// simple_flux_calculator.cpp:91-93 (order 1) or modular_flux_calculator.cpp:12-22
+// with simple_flux_calculator.cpp:27-31 (order 2).
+__global__ void __launch_bounds__(kBlock) k_geom_faces(GeomArgs a) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= a.mesh.e) return;
+  const int2 fc = a.mesh.face_cells[e];
+  const dbl4 v = a.mesh.face_vertices[e];
+  const double ax = v.x - v.z, ay = v.y - v.w;
+  a.area[e] = sqrt(ax * ax + ay * ay);
+  const double2 p = make_double2(v.z - v.x, v.w - v.y);
+  a.par[e] = p;
+  const double2 mid = make_double2((v.x + v.z) * 0.5, (v.y + v.w) * 0.5);
+  double2 n;
+  if (a.order == 1) {
+    const double2 x0 = a.mesh.points[fc.x], x1 = a.mesh.points[fc.y];
+    n = make_double2(x1.x - x0.x, x1.y - x0.y);
+  } else {
+    double2 w;
+    if (fc.x >= 0 && fc.x < a.mesh.n) {
+      const double2 x0 = a.mesh.points[fc.x];
+      w = make_double2(v.x - x0.x, v.y - x0.y);
+    } else {
+      const double2 x1 = a.mesh.points[fc.y];
+      w = make_double2(x1.x - v.x, x1.y - v.y);
+    }
+    const double sp = w.x * p.x + w.y * p.y;
+    const double pp = p.x * p.x + p.y * p.y;
+    n = make_double2(w.x - (p.x * sp) / pp, w.y - (p.y * sp) / pp);
+  }
+  a.nrm[e] = n;
+  a.nabs[e] = sqrt(n.x * n.x + n.y * n.y);
+  const double2 c0 = a.mesh.cms[fc.x], c1 = a.mesh.cms[fc.y];
+  a.dm0[e] = make_double2(mid.x - c0.x, mid.y - c0.y);
+  a.dm1[e] = make_double2(mid.x - c1.x, mid.y - c1.y);
+}
+
+// Per cell: VoronoiMesh.cpp:410-413 GetWidth; the CSR neighbour words; the
+// state-independent half of calc_naive_slope (LinearGaussImproved.cpp:67-126:
+// matrix, determinant check, inverse, 0.5*r_ij) or of GetBoundarySlope (:401-417).
+__global__ void __launch_bounds__(kBlock) k_geom_cells(GeomArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const MeshDev& m = a.mesh;
+  if (i >= m.n) return;
+  a.width[i] = sqrt(m.volume[i] / kPi);
+  const int b = m.cell_off[i], nn = m.cell_off[i + 1] - b;
+  bool bslope = false;
+  for (int k = 0; k < nn; ++k) {
+    const int e = m.cell_faces[b + k];
+    const int2 fc = m.face_cells[e];
+    const bool first = fc.x == i;
+    const int other = first ? fc.y : fc.x;
+    const bool mirror = orig_of(m, fc.x) == orig_of(m, fc.y);
+    bslope |= mirror;
+    a.nbr[b + k] = static_cast<uint32_t>(other) | (mirror ? kNbrMirror : 0u) | (first ? kNbrFirst : 0u);
+  }
+  const double2 cci = m.cms[i];
+  if (bslope) {
+    double sxsy = 0, sy2 = 0, sx2 = 0;
+    for (int k = 0; k < nn; ++k) {
+      const int other = static_cast<int>(a.nbr[b + k] & kNbrIdMask);
+      const double2 co = m.cms[other];
+      const double dx = co.x - cci.x, dy = co.y - cci.y;
+      a.hr[b + k] = make_double2(dx, dy);
+      sxsy += dy * dx;
+      sx2 += dx * dx;
+      sy2 += dy * dy;
+    }
+    a.minv[i] = make_dbl4(sxsy, sx2, sy2, sxsy * sxsy - sx2 * sy2);
+    a.cflags[i] = kCellBoundarySlope;
+    return;
+  }
+  a.cflags[i] = 0;
+  if (nn > kMaxNaiveNeighbours) {
+    record_error(a.status, 0, RG_ERR_TOO_MANY_NEIGHBORS, 2, i, nn);
+    a.minv[i] = make_dbl4(0, 0, 0, 0);
+    return;
+  }
+  const double2 xi = m.points[i];
+  double m0 = 0, m1 = 0, m2 = 0, m3 = 0;
+  for (int k = 0; k < nn; ++k) {
+    const int e = m.cell_faces[b + k];
+    const int other = static_cast<int>(a.nbr[b + k] & kNbrIdMask);
+    const dbl4 v = m.face_vertices[e];
+    const double2 co = m.cms[other], xo = m.points[other];
+    const double cx = (v.x + v.z) * 0.5 - (co.x + cci.x) * 0.5;
+    const double cy = (v.y + v.w) * 0.5 - (co.y + cci.y) * 0.5;
+    const double lx = v.z - v.x, ly = v.w - v.y;
+    const double len = sqrt(lx * lx + ly * ly);
+    const double dx = xo.x - xi.x, dy = xo.y - xi.y;
+    const double dab = sqrt(dx * dx + dy * dy);
+    const double rx = (dx / dab) * len, ry = (dy / dab) * len;
+    m0 -= cx * rx;
+    m1 -= cy * rx;
+    m2 -= cx * ry;
+    m3 -= cy * ry;
+    a.hr[b + k] = make_double2(rx * 0.5, ry * 0.5);
+  }
+  const double vol = m.volume[i];
+  m0 += vol;
+  m3 += vol;
+  const double det = m0 * m3 - m1 * m2;
+  if (fabs(det) < 1e-10 * vol * vol) record_error(a.status, 0, RG_ERR_SINGULAR_MATRIX, 2, i, det);
+  const double di = 1.0 / det;
+  a.minv[i] = make_dbl4(m3 * di, -m1 * di, -m2 * di, m0 * di);
+}
+
+// Per ghost: which cell it copies and, for rigid walls, the unit normal of
+// RigidWallGenerator.cpp:5-15 (ghost minus real point, divided by its length).
+__global__ void __launch_bounds__(kBlock) k_geom_ghosts(GeomArgs a) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const MeshDev& m = a.mesh;
+  if (g >= m.g) return;
+  const int e = m.ghost_face[g];
+  if (a.ghost_kind == RG_GHOST_PERIODIC || e < 0) {
+    a.ghost_real[g] = m.ghost_source[g];
+    a.ghost_unit[g] = make_double2(0, 0);
+    return;
+  }
+  const int2 fc = m.face_cells[e];
+  const bool ghost_first = fc.x >= m.n;
+  a.ghost_real[g] = ghost_first ? fc.y : fc.x;
+  const double2 x0 = m.points[fc.x], x1 = m.points[fc.y];
+  const double2 nr = ghost_first ? make_double2(x0.x - x1.x, x0.y - x1.y)
+                                 : make_double2(x1.x - x0.x, x1.y - x0.y);
+  const double ab = sqrt(nr.x * nr.x + nr.y * nr.y);
+  a.ghost_unit[g] = make_double2(nr.x / ab, nr.y / ab);
+}
+
+// ---------------------------------------------------------------- per step
+
+// Ghost state (LinearGaussImproved.cpp:543-550 new_cells[ghost]):
+// RigidWallGenerator.cpp:17-37 reflects the real neighbour's velocity,
+// PeriodicGhostGenerator.cpp:3-17 copies the source cell.
+__device__ __forceinline__ void fill_ghost(const StepArgs& a, int g) {
+  Cell c = load_cell(a.cells, a.geom.ghost_real[g]);
+  if (a.ghost_kind != RG_GHOST_PERIODIC) {
+    const double2 u = a.geom.ghost_unit[g];
+    const double s = 2 * (c.vx * u.x + c.vy * u.y);
+    c.vx -= u.x * s;
+    c.vy -= u.y * s;
+  }
+  store4(a.cells, a.mesh.n + g, c.d, c.p, c.vx, c.vy);
+}
+
+// simple_cfl.cpp:28-47 (per cell) and :58-71 + lazy_list.hpp:185-191 (min, times cfl).
+__global__ void __launch_bounds__(kBlock) k_cfl(StepArgs a, int fill_ghosts) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const MeshDev& m = a.mesh;
+  double x = __longlong_as_double(static_cast<long long>(kInfBits));
+  if (t < m.n) {
+    const Cell c = load_cell(a.cells, t);
+    const double radius = a.geom.width[t];
+    const double cs = sqrt(a.gamma * c.p / c.d);
+    double res = 0;
+    const int b = m.cell_off[t], e1 = m.cell_off[t + 1];
+    for (int k = b; k < e1; ++k) {
+      const double2 w = reinterpret_cast<const double2*>(a.ev)[m.cell_faces[k]];
+      const double dx = c.vx - w.x, dy = c.vy - w.y;
+      res = fmax(res, (cs + sqrt(dx * dx + dy * dy)) / radius);
+    }
+    x = 1.0 / res;
+  } else if (fill_ghosts && t < m.n + m.g) {
+    fill_ghost(a, t - m.n);
+  }
+  // min over the block (positive doubles: integer order = numeric order)
+  unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(x));
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long ob = __shfl_xor_sync(0xffffffffu, bits, o);
+    bits = ob < bits ? ob : bits;
+  }
+  __shared__ unsigned long long wmin[kBlock / 32];
+  __shared__ bool last;
+  if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = bits;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long bm = wmin[0];
+    for (int w = 1; w < kBlock / 32; ++w) bm = wmin[w] < bm ? wmin[w] : bm;
+    atomicMin(&a.status->dt_min_bits, bm);
+    __threadfence();
+    last = atomicAdd(&a.status->blocks_done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    // every block's atomicMin is visible here (threadfence before its ticket)
+    __threadfence();
+    const unsigned long long mb = atomicAdd(&a.status->dt_min_bits, 0ull);
+    a.status->dt = a.cfl * __longlong_as_double(static_cast<long long>(mb));
+    a.status->dt_min_bits = kInfBits;  // ready for the next step
+    a.status->blocks_done = 0;
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_ghost_fill(StepArgs a) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < a.mesh.g) fill_ghost(a, g);
+}
+
+__device__ __forceinline__ double step_dt(const StepArgs& a) {
+  return a.dt_from_device ? a.status->dt : a.dt_host;
+}
+
+// one component of the ordinary limiter, LinearGaussImproved.cpp:232-267
+__device__ __forceinline__ void limit_comp(double dphi, double cv, double cellv, double maxd, double mind,
+                                           bool use_abs, double& psi) {
+  if (fabs(dphi) > 0.05 * smax(fabs(maxd), fabs(mind)) || cv * cellv < 0) {
+    const double thr = use_abs ? fabs(1e-9 * cellv) : 1e-9 * cellv;
+    const double nthr = use_abs ? -fabs(1e-9 * cellv) : -1e-9 * cellv;
+    if (dphi > thr)
+      psi = smin(psi, maxd / dphi);
+    else if (dphi < nthr)
+      psi = smin(psi, mind / dphi);
+  }
+}
+
+// one component of the shocked limiter, LinearGaussImproved.cpp:343-366
+// (threshold 1e-9*q without abs for every component, as the reference has it)
+__device__ __forceinline__ void shocked_comp(double dphi, double cv, double cellv, double maxd, double mind,
+                                             double nbv, double theta, double& psi) {
+  if (fabs(dphi) > 0.1 * smax(fabs(maxd), fabs(mind)) || cv * cellv < 0) {
+    if (fabs(dphi) > 1e-9 * cellv) psi = smin(psi, smax(theta * (nbv - cellv) / dphi, 0.0));
+  }
+}
+
+// LinearGaussImproved.cpp:425-494 calc_slope for one cell (serial build).
+__global__ void __launch_bounds__(kBlock) k_slopes(StepArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const MeshDev& m = a.mesh;
+  if (i >= m.n) return;
+  const Cell cell = load_cell(a.cells, i);
+  const int b = m.cell_off[i], nn = m.cell_off[i + 1] - b;
+  const dbl4 mi = a.geom.minv[i];
+  Cell sx, sy;
+  if (a.geom.cflags[i] & kCellBoundarySlope) {
+    // :401-422 GetBoundarySlope
+    Cell phisy{0, 0, 0, 0}, phisx{0, 0, 0, 0};
+    for (int k = 0; k < nn; ++k) {
+      const Cell nb = load_cell(a.cells, static_cast<int>(a.geom.nbr[b + k] & kNbrIdMask));
+      const double2 h = a.geom.hr[b + k];
+      const Cell df{nb.d - cell.d, nb.p - cell.p, nb.vx - cell.vx, nb.vy - cell.vy};
+      phisy.d = phisy.d + df.d * h.y;
+      phisy.p = phisy.p + df.p * h.y;
+      phisy.vx = phisy.vx + df.vx * h.y;
+      phisy.vy = phisy.vy + df.vy * h.y;
+      phisx.d = phisx.d + df.d * h.x;
+      phisx.p = phisx.p + df.p * h.x;
+      phisx.vx = phisx.vx + df.vx * h.x;
+      phisx.vy = phisx.vy + df.vy * h.x;
+    }
+    const double sxsy = mi.x, sx2 = mi.y, sy2 = mi.z, den = mi.w;
+    sx = Cell{(phisy.d * sxsy - phisx.d * sy2) / den, (phisy.p * sxsy - phisx.p * sy2) / den,
+              (phisy.vx * sxsy - phisx.vx * sy2) / den, (phisy.vy * sxsy - phisx.vy * sy2) / den};
+    sy = Cell{(phisx.d * sxsy - phisy.d * sx2) / den, (phisx.p * sxsy - phisy.p * sx2) / den,
+              (phisx.vx * sxsy - phisy.vx * sx2) / den, (phisx.vy * sxsy - phisy.vy * sx2) / den};
+  } else {
+    // :80-133 calc_naive_slope, right-hand side and solve
+    Cell vx{0, 0, 0, 0}, vy{0, 0, 0, 0};
+    for (int k = 0; k < nn; ++k) {
+      const Cell nb = load_cell(a.cells, static_cast<int>(a.geom.nbr[b + k] & kNbrIdMask));
+      const double2 h = a.geom.hr[b + k];
+      if (k == 0) {
+        vx = Cell{cell.d * h.x, cell.p * h.x, cell.vx * h.x, cell.vy * h.x};
+        vy = Cell{cell.d * h.y, cell.p * h.y, cell.vx * h.y, cell.vy * h.y};
+      } else {
+        addmult(vx, cell, h.x);
+        addmult(vy, cell, h.y);
+      }
+      addmult(vy, nb, h.y);
+      addmult(vx, nb, h.x);
+    }
+    sx = Cell{vx.d * mi.x, vx.p * mi.x, vx.vx * mi.x, vx.vy * mi.x};
+    sy = Cell{vy.d * mi.w, vy.p * mi.w, vy.vx * mi.w, vy.vy * mi.w};
+    addmult(sx, vy, mi.y);
+    addmult(sy, vx, mi.z);
+  }
+  if (a.slf) {
+    // :136-157 is_shock / PressureRatio
+    const double cs = sqrt(a.gamma * cell.p / cell.d);
+    bool shock = (sx.vx + sy.vy) * a.geom.width[i] < (-a.delta_v) * cs;
+    if (!shock) {
+      double pr = 1;
+      for (int k = 0; k < nn; ++k) {
+        const double np_ = a.cells[4 * static_cast<int>(a.geom.nbr[b + k] & kNbrIdMask) + 1];
+        if (cell.p > np_)
+          pr = smin(pr, np_ / cell.p);
+        else
+          pr = smin(pr, cell.p / np_);
+      }
+      shock = pr < a.delta_p;
+    }
+    Cell cmax = cell, cmin = cell;
+    for (int k = 0; k < nn; ++k) {
+      const uint32_t w = a.geom.nbr[b + k];
+      if (!shock && (w & kNbrMirror)) continue;  // :194-195 skips self-mirror neighbours
+      const Cell nb = load_cell(a.cells, static_cast<int>(w & kNbrIdMask));
+      cmax.d = smax(cmax.d, nb.d);
+      cmax.p = smax(cmax.p, nb.p);
+      cmax.vx = smax(cmax.vx, nb.vx);
+      cmax.vy = smax(cmax.vy, nb.vy);
+      cmin.d = smin(cmin.d, nb.d);
+      cmin.p = smin(cmin.p, nb.p);
+      cmin.vx = smin(cmin.vx, nb.vx);
+      cmin.vy = smin(cmin.vy, nb.vy);
+    }
+    const Cell maxd{cmax.d - cell.d, cmax.p - cell.p, cmax.vx - cell.vx, cmax.vy - cell.vy};
+    const Cell mind{cmin.d - cell.d, cmin.p - cell.p, cmin.vx - cell.vx, cmin.vy - cell.vy};
+    double psi0 = 1, psi1 = 1, psi2 = 1, psi3 = 1;
+    for (int k = 0; k < nn; ++k) {
+      const uint32_t w = a.geom.nbr[b + k];
+      const int e = m.cell_faces[b + k];
+      const double2 dm = (w & kNbrFirst) ? a.geom.dm0[e] : a.geom.dm1[e];
+      Cell cv = cell;
+      addmult(cv, sx, dm.x);
+      addmult(cv, sy, dm.y);
+      const Cell dphi{cv.d - cell.d, cv.p - cell.p, cv.vx - cell.vx, cv.vy - cell.vy};
+      if (!shock) {
+        // :174-300 slope_limit
+        limit_comp(dphi.d, cv.d, cell.d, maxd.d, mind.d, false, psi0);
+        limit_comp(dphi.p, cv.p, cell.p, maxd.p, mind.p, false, psi1);
+        limit_comp(dphi.vx, cv.vx, cell.vx, maxd.vx, mind.vx, true, psi2);
+        limit_comp(dphi.vy, cv.vy, cell.vy, maxd.vy, mind.vy, true, psi3);
+      } else {
+        // :302-399 shocked_slope_limit
+        const Cell nb = load_cell(a.cells, static_cast<int>(w & kNbrIdMask));
+        shocked_comp(dphi.d, cv.d, cell.d, maxd.d, mind.d, nb.d, a.theta, psi0);
+        shocked_comp(dphi.p, cv.p, cell.p, maxd.p, mind.p, nb.p, a.theta, psi1);
+        shocked_comp(dphi.vx, cv.vx, cell.vx, maxd.vx, mind.vx, nb.vx, a.theta, psi2);
+        shocked_comp(dphi.vy, cv.vy, cell.vy, maxd.vy, mind.vy, nb.vy, a.theta, psi3);
+      }
+    }
+    sx.d *= psi0; sy.d *= psi0;
+    sx.p *= psi1; sy.p *= psi1;
+    sx.vx *= psi2; sy.vx *= psi2;
+    sx.vy *= psi3; sy.vy *= psi3;
+  }
+  double2* o = reinterpret_cast<double2*>(a.slopes) + 4 * i;
+  o[0] = make_double2(sx.d, sx.p);
+  o[1] = make_double2(sx.vx, sx.vy);
+  o[2] = make_double2(sy.d, sy.p);
+  o[3] = make_double2(sy.vx, sy.vy);
+}
+
+// ---------------------------------------------------------------- faces
+
+// simple_flux_calculator.cpp:9-15 convert_to_primitive (ideal_gas.cpp:13-16, 40-44)
+__device__ __forceinline__ Prim to_prim(double g, const Cell& c) {
+  return Prim{c.d, c.p, c.vx, c.vy, c.p / c.d / (g - 1), sqrt(g * c.p / c.d)};
+}
+
+// hydrodynamic_variables.cpp:261-265 TotalEnergyDensity (pow(x,2) is x*x)
+__device__ __forceinline__ double ted(const Prim& p) {
+  const double s = sqrt(p.vx * p.vx + p.vy * p.vy);
+  return p.d * (0.5 * (s * s) + p.e);
+}
+
+// hllc.cpp:97-154 with massflux_ = true; the frame normal is (1,0), so
+// Primitive2Flux's n/abs(n) is (1,0) exactly.  Only the branch's starred
+// state is formed; the others do not reach the result.
+__device__ __forceinline__ bool hllc(Prim l, Prim r, double velocity, Cons& f, const StepArgs& a, int face) {
+  if (isnan(r.vx)) {
+    record_error(a.status, a.step, RG_ERR_HLLC_NAN, 3, face, r.vx);
+    return false;
+  }
+  const double bx = 1 * velocity, by = 0 * velocity;
+  l.vx -= bx;
+  l.vy -= by;
+  r.vx -= bx;
+  r.vy -= by;
+  // :27-43 estimate_wave_speeds
+  const double sl = smin(l.vx - l.c, r.vx - r.c);
+  const double sr = smax(l.vx + l.c, r.vx + r.c);
+  const double ss = (r.p - l.p + l.d * l.vx * (sl - l.vx) - r.d * r.vx * (sr - r.vx)) /
+                    (l.d * (sl - l.vx) - r.d * (sr - r.vx));
+  const bool use_left = sl > 0 || (sl <= 0 && ss >= 0);
+  const bool use_right = !use_left && ((ss < 0 && sr >= 0) || sr < 0);
+  if (!use_left && !use_right) {
+    record_error(a.status, a.step, RG_ERR_HLLC_WAVE_SPEEDS, 3, face, ss);
+    return false;
+  }
+  const Prim& q = use_left ? l : r;
+  const double sk = use_left ? sl : sr;
+  const double e_k = ted(q);
+  // :281-290 Primitive2Flux along (1,0)
+  const double sp = q.vx * 1 + q.vy * 0;
+  const double dsp = q.d * sp;
+  Cons fk{q.d * sp, 1 * q.p + q.vx * dsp, 0 * q.p + q.vy * dsp, (e_k + q.p) * sp};
+  const bool star = use_left ? !(sl > 0) : !(sr < 0);
+  if (star) {
+    // :76-92 starred_state, and fk + sk*(us - u) with u = Primitive2Conserved (:267-272)
+    const double ds = q.d * (sk - q.vx) / (sk - ss);
+    const double usm = ds, usx = ds * ss, usy = ds * q.vy;
+    const double use = e_k * ds / q.d + ds * (ss - q.vx) * (ss + q.p / q.d / (sk - q.vx));
+    fk.m = fk.m + sk * (usm - q.d);
+    fk.mx = fk.mx + (usx - q.vx * q.d) * sk;
+    fk.my = fk.my + (usy - q.vy * q.d) * sk;
+    fk.en = fk.en + sk * (use - e_k);
+  }
+  // :150-152 back to the lab frame along the normal
+  fk.en += (fk.mx * (1 * velocity) + fk.my * (0 * velocity)) + 0.5 * fk.m * velocity * velocity;
+  const double vm = velocity * fk.m;
+  fk.mx += 1 * vm;
+  fk.my += 0 * vm;
+  f = fk;
+  return true;
+}
+
+// simple_flux_calculator.cpp:130-165 rotate / Hllc / rotate_back
+__device__ __forceinline__ bool solve_face(Prim l, Prim r, double velocity, double2 n, double na, double2 p,
+                                           double pa, Cons& out, const StepArgs& a, int face) {
+  const double lx = (l.vx * n.x + l.vy * n.y) / na, ly = (l.vx * p.x + l.vy * p.y) / pa;
+  const double rx = (r.vx * n.x + r.vy * n.y) / na, ry = (r.vx * p.x + r.vy * p.y) / pa;
+  l.vx = lx;
+  l.vy = ly;
+  r.vx = rx;
+  r.vy = ry;
+  Cons c;
+  if (!hllc(l, r, velocity, c, a, face)) return false;
+  out.m = c.m;
+  out.mx = (n.x * c.mx) / na + (p.x * c.my) / pa;
+  out.my = (n.y * c.mx) / na + (p.y * c.my) / pa;
+  out.en = c.en;
+  return true;
+}
+
+__device__ __forceinline__ void write_flux(const StepArgs& a, int e, const Cons& c, bool scaled, double area) {
+  if (scaled) {
+    const double s = step_dt(a) * area;  // simple_extensive_updater.cpp:26-27
+    store4(a.fluxes, e, c.m * s, c.en * s, c.mx * s, c.my * s);
+  } else {
+    store4(a.fluxes, e, c.m, c.en, c.mx, c.my);
+  }
+}
+
+// ModularFluxCalculator (modular_flux_calculator.cpp:39-71) with the face
+// states of LinearGaussImproved (:570-590 real sides, :596-634 ghost sides).
+template <bool kScaled>
+__global__ void __launch_bounds__(kBlock) k_faces_lgi(StepArgs a) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const MeshDev& m = a.mesh;
+  if (e >= m.e) return;
+  const int2 fc = m.face_cells[e];
+  Cell side[2];
+  const int ids[2] = {fc.x, fc.y};
+  const double2 dms[2] = {a.geom.dm0[e], a.geom.dm1[e]};
+#pragma unroll
+  for (int s = 0; s < 2; ++s) {
+    const int pid = ids[s];
+    Cell c = load_cell(a.cells, pid);
+    int sid = pid;
+    bool zero = false;
+    if (pid >= m.n) {
+      if (a.ghost_kind == RG_GHOST_PERIODIC)
+        sid = m.ghost_source[pid - m.n];  // PeriodicGhostGenerator.cpp:19-24
+      else
+        zero = true;  // RigidWallGenerator.cpp:39-54: zero gradient
+    }
+    Cell gx{0, 0, 0, 0}, gy{0, 0, 0, 0};
+    if (!zero) {
+      const double2* sp = reinterpret_cast<const double2*>(a.slopes) + 4 * sid;
+      const double2 s0 = sp[0], s1 = sp[1], s2 = sp[2], s3 = sp[3];
+      gx = Cell{s0.x, s0.y, s1.x, s1.y};
+      gy = Cell{s2.x, s2.y, s3.x, s3.y};
+    }
+    addmult(c, gx, dms[s].x);
+    addmult(c, gy, dms[s].y);
+    side[s] = c;
+  }
+  const double2 w = reinterpret_cast<const double2*>(a.ev)[e];
+  const double2 n = a.geom.nrm[e], p = a.geom.par[e];
+  const double na = a.geom.nabs[e], pa = a.geom.area[e];
+  const double speed = (n.x * w.x + n.y * w.y) / na;
+  Cons c;
+  if (!solve_face(to_prim(a.gamma, side[0]), to_prim(a.gamma, side[1]), speed, n, na, p, pa, c, a, e)) return;
+  write_flux(a, e, c, kScaled, pa);
+}
+
+// simple_flux_calculator.cpp:17-25 reflect (Reflect, geometry.cpp:117-120);
+// keeps the source's energy and sound speed.
+__device__ __forceinline__ Prim reflect(Prim q, double2 axis, double aa) {
+  const double s = 2 * (q.vx * axis.x + q.vy * axis.y);
+  const double pp = aa * aa;
+  const double tx = (axis.x * s) / pp, ty = (axis.y * s) / pp;
+  q.vx = tx - q.vx;
+  q.vy = ty - q.vy;
+  return q;
+}
+
+// SimpleFluxCalculator (simple_flux_calculator.cpp:80-126 riemann_reduce,
+// :216-244).  A ghost that is not its neighbour's own mirror takes its source
+// cell's state.
+template <bool kScaled>
+__global__ void __launch_bounds__(kBlock) k_faces_pcm(StepArgs a) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const MeshDev& m = a.mesh;
+  if (e >= m.e) return;
+  const int2 fc = m.face_cells[e];
+  const double2 p = a.geom.par[e], n = a.geom.nrm[e];
+  const double pa = a.geom.area[e], na = a.geom.nabs[e];
+  const bool va = fc.x < m.n, vb = fc.y < m.n;
+  const int oa = orig_of(m, fc.x), ob = orig_of(m, fc.y);
+  Prim l, r;
+  if (!va) {
+    r = to_prim(a.gamma, load_cell(a.cells, fc.y));
+    l = oa == ob ? reflect(r, p, pa) : to_prim(a.gamma, load_cell(a.cells, oa));
+  } else if (!vb) {
+    l = to_prim(a.gamma, load_cell(a.cells, fc.x));
+    r = oa == ob ? reflect(l, p, pa) : to_prim(a.gamma, load_cell(a.cells, ob));
+  } else {
+    l = to_prim(a.gamma, load_cell(a.cells, fc.x));
+    r = to_prim(a.gamma, load_cell(a.cells, fc.y));
+  }
+  const double2 w = reinterpret_cast<const double2*>(a.ev)[e];
+  const double velocity = (n.x * w.x + n.y * w.y) / na;
+  Cons c;
+  if (!solve_face(l, r, velocity, n, na, p, pa, c, a, e)) return;
+  write_flux(a, e, c, kScaled, pa);
+}
+
+// ---------------------------------------------------------------- cells
+
+// SimpleExtensiveUpdater (simple_extensive_updater.cpp:11-35) as a gather:
+// each cell applies its faces' contributions in ascending face order, which
+// is the order the reference's edge loop applies them to that cell; then
+// SimpleCellUpdater::regular_update (simple_cell_updater.cpp:22-59).
+__global__ void __launch_bounds__(kBlock) k_update(StepArgs a, int from_unscaled, int do_ext, int do_cells) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const MeshDev& m = a.mesh;
+  if (i >= m.n) return;
+  double2* ext2 = reinterpret_cast<double2*>(a.ext);
+  double2 e01 = ext2[2 * i], e23 = ext2[2 * i + 1];
+  double mass = e01.x, en = e01.y, px = e23.x, py = e23.y;
+  if (do_ext) {
+    const double dt = from_unscaled ? step_dt(a) : 0.0;
+    const int b = m.cell_off[i], e1 = m.cell_off[i + 1];
+    for (int k = b; k < e1; ++k) {
+      const int e = m.cell_faces[k];
+      const double2* f = reinterpret_cast<const double2*>(a.fluxes) + 2 * e;
+      const double2 f01 = f[0], f23 = f[1];
+      double dm = f01.x, de = f01.y, dx = f23.x, dy = f23.y;
+      if (from_unscaled) {
+        const double s = dt * a.geom.area[e];
+        dm *= s;
+        de *= s;
+        dx *= s;
+        dy *= s;
+      }
+      if (a.geom.nbr[k] & kNbrFirst) {
+        mass -= dm;
+        en -= de;
+        px -= dx;
+        py -= dy;
+      } else {
+        mass += dm;
+        en += de;
+        px += dx;
+        py += dy;
+      }
+    }
+    ext2[2 * i] = make_double2(mass, en);
+    ext2[2 * i + 1] = make_double2(px, py);
+  }
+  if (do_cells) {
+    const double d = mass / m.cd_volume[i];
+    if (d < 0) {
+      record_error(a.status, a.step, RG_ERR_NEGATIVE_DENSITY, 5, i, d);
+      return;
+    }
+    const double vx = px / mass, vy = py / mass;
+    const double energy = en / mass - 0.5 * (vx * vx + vy * vy);
+    if (energy < 0) {
+      record_error(a.status, a.step, RG_ERR_NEGATIVE_ENERGY, 5, i, energy);
+      return;
+    }
+    store4(a.cells, i, d, (a.gamma - 1) * energy * d, vx, vy);
+  }
+}
+
+// hdsim2d.cpp:41-67 init_extensives
+__global__ void __launch_bounds__(kBlock) k_init_ext(StepArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.mesh.n) return;
+  const Cell c = load_cell(a.cells, i);
+  const double mass = a.mesh.cd_volume[i] * c.d;
+  store4(a.ext, i, mass, c.p / c.d / (a.gamma - 1) * mass + 0.5 * mass * (c.vx * c.vx + c.vy * c.vy),
+         c.vx * mass, c.vy * mass);
+}
+
+inline int blocks(int n) { return (n + kBlock - 1) / kBlock; }
+
+}  // namespace
+
+cudaError_t launch_geometry(const GeomArgs& a, cudaStream_t s) {
+  if (a.mesh.e > 0) k_geom_faces<<<blocks(a.mesh.e), kBlock, 0, s>>>(a);
+  if (a.mesh.n > 0) k_geom_cells<<<blocks(a.mesh.n), kBlock, 0, s>>>(a);
+  if (a.mesh.g > 0) k_geom_ghosts<<<blocks(a.mesh.g), kBlock, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cfl(const StepArgs& a, cudaStream_t s, bool fill_ghosts) {
+  const int total = a.mesh.n + (fill_ghosts ? a.mesh.g : 0);
+  k_cfl<<<blocks(total > 0 ? total : 1), kBlock, 0, s>>>(a, fill_ghosts ? 1 : 0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ghost_fill(const StepArgs& a, cudaStream_t s) {
+  if (a.mesh.g > 0) k_ghost_fill<<<blocks(a.mesh.g), kBlock, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_slopes(const StepArgs& a, cudaStream_t s) {
+  if (a.mesh.n > 0) k_slopes<<<blocks(a.mesh.n), kBlock, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_faces(const StepArgs& a, cudaStream_t s, bool scaled) {
+  if (a.mesh.e == 0) return cudaSuccess;
+  if (a.order == 1) {
+    if (scaled)
+      k_faces_pcm<true><<<blocks(a.mesh.e), kBlock, 0, s>>>(a);
+    else
+      k_faces_pcm<false><<<blocks(a.mesh.e), kBlock, 0, s>>>(a);
+  } else {
+    if (scaled)
+      k_faces_lgi<true><<<blocks(a.mesh.e), kBlock, 0, s>>>(a);
+    else
+      k_faces_lgi<false><<<blocks(a.mesh.e), kBlock, 0, s>>>(a);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_update(const StepArgs& a, cudaStream_t s, bool from_unscaled, bool extensive, bool cells) {
+  if (a.mesh.n > 0)
+    k_update<<<blocks(a.mesh.n), kBlock, 0, s>>>(a, from_unscaled ? 1 : 0, extensive ? 1 : 0, cells ? 1 : 0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_init_extensives(const StepArgs& a, cudaStream_t s) {
+  if (a.mesh.n > 0) k_init_ext<<<blocks(a.mesh.n), kBlock, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace rg

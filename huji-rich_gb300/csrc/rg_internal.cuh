@@ -1,0 +1,182 @@
+// rg_internal.cuh -- device-side data layout shared by the kernels and the
+// C-ABI host code of the GB300 hydro hot path.
+//
+// Layout in HBM (all arrays owned by one rg_handle):
+//   points  double2[np]   mesh points, real cells then ghosts (np = n + g)
+//   cms     double2[np]   cell centres of mass
+//   cells   dbl4-like  double[4*np]: {density, pressure, vx, vy}; entries
+//                         n..np-1 hold ghost states (filled per step)
+//   ext     double[4*n]   {mass, energy, px, py}
+//   faces   int2[e]       (first, second) point ids
+//   face geometry (per upload): area, normal n, |n|, parallel p, mid - cm of
+//                         each side
+//   CSR     cell -> faces, ascending face ids, plus per entry the
+//           neighbour id (with side / mirror flags) and a geometry pair
+// Everything that depends only on the mesh is computed once per upload by
+// the geometry kernels; the per-step kernels only do state-dependent work.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "rich_gb300.h"
+
+namespace rg {
+
+// 32-byte aligned record of four doubles (one cell, face-vertex pair or 2x2 matrix)
+struct __align__(32) dbl4 {
+  double x, y, z, w;
+};
+__host__ __device__ inline dbl4 make_dbl4(double x, double y, double z, double w) { return dbl4{x, y, z, w}; }
+
+constexpr int kMaxNaiveNeighbours = 20;  // LinearGaussImproved.cpp:73
+constexpr double kPi = 3.14159265358979323846;  // M_PI (VoronoiMesh.cpp:412)
+
+// neighbour word of a CSR entry: low 30 bits point id, bit 30 self-mirror
+// face (GetOriginalIndex(first) == GetOriginalIndex(second)), bit 31 the cell
+// is the face's first neighbour (its flux enters with a minus sign).
+constexpr uint32_t kNbrIdMask = 0x3fffffffu;
+constexpr uint32_t kNbrMirror = 0x40000000u;
+constexpr uint32_t kNbrFirst = 0x80000000u;
+
+// per-cell geometry flags
+constexpr int kCellBoundarySlope = 1;  // LinearGaussImproved.cpp:454-464
+
+struct MeshDev {
+  int n, g, e, m;           // cells, ghosts, faces, CSR entries
+  const double2* points;    // np
+  const double2* cms;       // np
+  const double* volume;     // n (Tessellation::GetVolume)
+  const double* cd_volume;  // n (CacheData::volumes)
+  const int* ghost_source;  // g
+  const int* ghost_face;    // g
+  const int2* face_cells;   // e
+  const dbl4* face_vertices;  // e
+  const int* cell_off;      // n+1
+  const int* cell_faces;    // m
+};
+
+struct GeomDev {
+  // per face
+  const double* area;    // |first - second| (= GetLength = calcArea)
+  const double2* nrm;    // flux-frame normal (order 1: x1-x0; order 2: calc_parallel_normal)
+  const double* nabs;    // abs(nrm)
+  const double2* par;    // Parallel(edge) = second - first
+  const double2* dm0;    // CalcCentroid(edge) - cm[first]
+  const double2* dm1;    // CalcCentroid(edge) - cm[second]
+  // per cell
+  const double* width;   // sqrt(volume/pi)
+  const dbl4* minv;   // naive-slope inverse matrix, or (SxSy, Sx2, Sy2, den) for boundary cells
+  const int* cflags;
+  // per CSR entry
+  const uint32_t* nbr;
+  const double2* hr;     // naive: 0.5*r_ij; boundary: cm[other] - cm[cell]
+  // per ghost
+  const int* ghost_real;      // cell whose state the ghost copies / reflects
+  const double2* ghost_unit;  // rigid wall: unit normal (x_ghost - x_real)/|.|
+};
+
+// Device status word.  The error kept is the one with the smallest
+// (phase, index) key, which is the one the reference throws first: its
+// passes run in phase order and each loops in ascending cell / face order.
+struct DevStatus {
+  unsigned long long err_key;  // ~0ull = none
+  double err_value;
+  int err_status;
+  int lock;
+  unsigned long long dt_min_bits;  // CFL min-reduction (positive doubles order as integers)
+  double dt;                       // cfl * min, written by the last CFL block
+  unsigned int blocks_done;        // CFL blocks finished (reset by the last one)
+  int lock_timeouts;
+};
+constexpr unsigned long long kInfBits = 0x7ff0000000000000ull;
+
+// key = step (bits 50..62) | phase (46..49) | index (0..45): within a run of
+// several steps the earliest step's failure wins, as it would on the host.
+constexpr int kKeyPhaseShift = 46;
+constexpr int kKeyStepShift = 50;
+constexpr unsigned long long kKeyIndexMask = (1ull << kKeyPhaseShift) - 1;
+__host__ __device__ inline unsigned long long err_key(int step, int phase, long long index) {
+  return (static_cast<unsigned long long>(step & 0x1fff) << kKeyStepShift) |
+         (static_cast<unsigned long long>(phase & 0xf) << kKeyPhaseShift) |
+         (static_cast<unsigned long long>(index) & kKeyIndexMask);
+}
+
+#ifdef __CUDACC__
+// Records an error; keeps the smallest key.  The lock wait is bounded: if it
+// times out the key is still min-reduced and the value may be stale.
+__device__ inline void record_error(DevStatus* st, int step, int status, int phase, long long index,
+                                    double value) {
+  const unsigned long long key = err_key(step, phase, index);
+  if (key >= atomicAdd(&st->err_key, 0ull)) return;
+  bool done = false;
+  for (int it = 0; it < (1 << 16) && !done; ++it) {
+    if (atomicCAS(&st->lock, 0, 1) == 0) {
+      __threadfence();
+      if (key < st->err_key) {
+        st->err_key = key;
+        st->err_value = value;
+        st->err_status = status;
+      }
+      __threadfence();
+      atomicExch(&st->lock, 0);
+      done = true;
+    }
+  }
+  if (!done) {
+    atomicAdd(&st->lock_timeouts, 1);
+    atomicMin(&st->err_key, key);
+  }
+}
+
+// std::min / std::max semantics
+__device__ __forceinline__ double smin(double a, double b) { return b < a ? b : a; }
+__device__ __forceinline__ double smax(double a, double b) { return a < b ? b : a; }
+#endif
+
+// Kernel launchers (rg_fp64.cu)
+struct StepArgs {
+  MeshDev mesh;
+  GeomDev geom;
+  double gamma, cfl;
+  int order, ghost_kind, slf;
+  double delta_v, theta, delta_p;
+  double* cells;        // 4*np (ghost entries at the end)
+  double* ext;          // 4*n
+  const double* ev;     // 2*e edge velocities
+  double* slopes;       // 8*n
+  double* fluxes;       // 4*e (unscaled or dt*area scaled)
+  DevStatus* status;
+  double dt_host;       // dt given by the caller (split API)
+  int dt_from_device;   // 1: dt = cfl * min from status->dt_min_bits
+  int step;             // step number within an rg_run (error ordering)
+};
+
+struct GeomArgs {
+  MeshDev mesh;
+  int order;
+  double* area;
+  double2* nrm;
+  double* nabs;
+  double2* par;
+  double2* dm0;
+  double2* dm1;
+  double* width;
+  dbl4* minv;
+  int* cflags;
+  uint32_t* nbr;
+  double2* hr;
+  int* ghost_real;
+  double2* ghost_unit;
+  int ghost_kind;
+  DevStatus* status;
+};
+
+cudaError_t launch_geometry(const GeomArgs& a, cudaStream_t s);
+cudaError_t launch_cfl(const StepArgs& a, cudaStream_t s, bool fill_ghosts);
+cudaError_t launch_ghost_fill(const StepArgs& a, cudaStream_t s);
+cudaError_t launch_slopes(const StepArgs& a, cudaStream_t s);
+cudaError_t launch_faces(const StepArgs& a, cudaStream_t s, bool scaled);
+cudaError_t launch_update(const StepArgs& a, cudaStream_t s, bool from_unscaled, bool extensive, bool cells);
+cudaError_t launch_init_extensives(const StepArgs& a, cudaStream_t s);
+
+}  // namespace rg

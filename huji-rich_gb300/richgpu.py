@@ -1,0 +1,212 @@
+"""ctypes binding of librich_gb300.so (the C ABI in include/rich_gb300.h).
+
+This is the reference-facing boundary as a Python caller sees it: every call
+goes through the exported ``rg_*`` functions with host (numpy) buffers, or
+with device buffers through :meth:`Handle.device_buffers`.  There is no CPU
+fallback: loading fails loudly when the library is missing.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from meshview import (REFERENCE_MESSAGES, STATUS_NAMES, PackedMesh, RgConfig, RgError, RgMeshView,
+                      dptr, make_config)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "librich_gb300.so")
+
+# every entry point include/rich_gb300.h declares
+EXPORTS = ("rg_default_config", "rg_create", "rg_destroy", "rg_status_string", "rg_last_error",
+           "rg_upload_mesh", "rg_last_upload_ms", "rg_set_cells", "rg_get_cells",
+           "rg_set_extensives", "rg_get_extensives", "rg_set_edge_velocities",
+           "rg_device_buffers", "rg_init_extensives", "rg_cfl_dt", "rg_flux", "rg_set_fluxes",
+           "rg_extensive_update", "rg_cell_update", "rg_step", "rg_run", "rg_step_async",
+           "rg_synchronize", "rg_step_timed")
+
+
+class RgDeviceView(C.Structure):
+    _fields_ = [("cells", C.c_void_p), ("extensives", C.c_void_p),
+                ("edge_velocities", C.c_void_p), ("fluxes", C.c_void_p), ("stream", C.c_void_p)]
+
+
+class RichError(RuntimeError):
+    """A failure reported by the library; for physical failures the message is
+    the reference's UniversalError text."""
+
+    def __init__(self, status, err=None):
+        self.status = status
+        self.phase = err.phase if err else 0
+        self.index = err.index if err else -1
+        self.value = err.value if err else 0.0
+        msg = REFERENCE_MESSAGES.get(status, STATUS_NAMES.get(status, f"status {status}"))
+        super().__init__(f"{msg} (phase {self.phase}, index {self.index}, value {self.value!r})")
+
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Loads the library (no fallback: raises if it is absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise OSError(f"{path} is missing: build it with huji-rich_gb300/rg_build.py")
+    lib = C.CDLL(path)
+    vp = C.c_void_p
+    dp = C.POINTER(C.c_double)
+    lib.rg_create.argtypes = [C.POINTER(RgConfig), C.POINTER(vp)]
+    lib.rg_destroy.argtypes = [vp]
+    lib.rg_status_string.restype = C.c_char_p
+    lib.rg_last_error.argtypes = [vp, C.POINTER(RgError)]
+    lib.rg_upload_mesh.argtypes = [vp, C.POINTER(RgMeshView), C.c_uint32]
+    lib.rg_last_upload_ms.argtypes = [vp, dp]
+    for f in ("rg_set_cells", "rg_get_cells", "rg_set_extensives", "rg_get_extensives",
+              "rg_set_edge_velocities", "rg_set_fluxes"):
+        getattr(lib, f).argtypes = [vp, dp]
+    lib.rg_device_buffers.argtypes = [vp, C.POINTER(RgDeviceView)]
+    lib.rg_init_extensives.argtypes = [vp]
+    lib.rg_cfl_dt.argtypes = [vp, dp]
+    lib.rg_flux.argtypes = [vp, C.c_double, dp]
+    lib.rg_extensive_update.argtypes = [vp, C.c_double]
+    lib.rg_cell_update.argtypes = [vp]
+    lib.rg_step.argtypes = [vp, dp]
+    lib.rg_run.argtypes = [vp, C.c_int32, dp]
+    lib.rg_step_async.argtypes = [vp]
+    lib.rg_synchronize.argtypes = [vp, dp]
+    lib.rg_step_timed.argtypes = [vp, dp, C.POINTER(C.c_float)]
+    _lib = lib
+    return lib
+
+
+class Handle:
+    """One rg_handle: a simulation's device state on one GPU."""
+
+    def __init__(self, config=None, **kw):
+        self.lib = load()
+        self.config = config or make_config(**kw)
+        h = C.c_void_p()
+        st = self.lib.rg_create(C.byref(self.config), C.byref(h))
+        if st:
+            raise RichError(st)
+        self.h = h
+        self.mesh = None
+
+    def close(self):
+        if self.h:
+            self.lib.rg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, st):
+        if st:
+            err = RgError()
+            self.lib.rg_last_error(self.h, C.byref(err))
+            raise RichError(st, err)
+
+    def last_error(self):
+        err = RgError()
+        self.lib.rg_last_error(self.h, C.byref(err))
+        return err
+
+    # mesh / state -------------------------------------------------------
+    def upload_mesh(self, mesh: PackedMesh, flags=0):
+        self._check(self.lib.rg_upload_mesh(self.h, C.byref(mesh.view()), flags))
+        self.mesh = mesh
+
+    def last_upload_ms(self):
+        v = C.c_double()
+        self.lib.rg_last_upload_ms(self.h, C.byref(v))
+        return v.value
+
+    def set_cells(self, cells):
+        a = np.ascontiguousarray(cells, dtype=np.float64)
+        assert a.size == 4 * self.mesh.n_cells
+        self._check(self.lib.rg_set_cells(self.h, dptr(a)))
+
+    def get_cells(self):
+        out = np.empty((self.mesh.n_cells, 4))
+        self._check(self.lib.rg_get_cells(self.h, dptr(out)))
+        return out
+
+    def set_extensives(self, ext):
+        a = np.ascontiguousarray(ext, dtype=np.float64)
+        assert a.size == 4 * self.mesh.n_cells
+        self._check(self.lib.rg_set_extensives(self.h, dptr(a)))
+
+    def get_extensives(self):
+        out = np.empty((self.mesh.n_cells, 4))
+        self._check(self.lib.rg_get_extensives(self.h, dptr(out)))
+        return out
+
+    def set_edge_velocities(self, ev):
+        a = np.ascontiguousarray(ev, dtype=np.float64)
+        assert a.size == 2 * self.mesh.n_faces
+        self._check(self.lib.rg_set_edge_velocities(self.h, dptr(a)))
+
+    def set_fluxes(self, fl):
+        a = np.ascontiguousarray(fl, dtype=np.float64)
+        assert a.size == 4 * self.mesh.n_faces
+        self._check(self.lib.rg_set_fluxes(self.h, dptr(a)))
+
+    def device_buffers(self):
+        v = RgDeviceView()
+        self._check(self.lib.rg_device_buffers(self.h, C.byref(v)))
+        return v
+
+    def init_extensives(self):
+        self._check(self.lib.rg_init_extensives(self.h))
+
+    # plugin operations ----------------------------------------------------
+    def cfl_dt(self):
+        dt = C.c_double()
+        self._check(self.lib.rg_cfl_dt(self.h, C.byref(dt)))
+        return dt.value
+
+    def flux(self, dt=0.0, download=True):
+        out = np.empty((self.mesh.n_faces, 4)) if download else None
+        self._check(self.lib.rg_flux(self.h, C.c_double(dt), dptr(out) if download else None))
+        return out
+
+    def extensive_update(self, dt):
+        self._check(self.lib.rg_extensive_update(self.h, C.c_double(dt)))
+
+    def cell_update(self):
+        self._check(self.lib.rg_cell_update(self.h))
+
+    def step(self):
+        dt = C.c_double()
+        self._check(self.lib.rg_step(self.h, C.byref(dt)))
+        return dt.value
+
+    def run(self, n_steps):
+        dts = np.empty(max(n_steps, 1))
+        self._check(self.lib.rg_run(self.h, n_steps, dptr(dts)))
+        return dts[:n_steps]
+
+    def step_timed(self):
+        """One fused step; returns (dt, [cfl, slopes, faces, update] kernel ms)."""
+        dt = C.c_double()
+        ms = (C.c_float * 4)()
+        self._check(self.lib.rg_step_timed(self.h, C.byref(dt), ms))
+        return dt.value, list(ms)
+
+    def step_async(self):
+        self._check(self.lib.rg_step_async(self.h))
+
+    def synchronize(self):
+        dt = C.c_double()
+        self._check(self.lib.rg_synchronize(self.h, C.byref(dt)))
+        return dt.value

@@ -199,6 +199,16 @@ rg_status rg_step(rg_handle* h, double* dt_out);
 /* n_steps rg_step calls without a host synchronisation between them; errors
  * are checked once at the end.  dt_out (n_steps, host) may be NULL. */
 rg_status rg_run(rg_handle* h, int32_t n_steps, double* dt_out);
+/* rg_step with CUDA events between its kernels (the work is identical):
+ * kernel_ms[0..3] = CFL (with the ghost fill), LinearGaussImproved slopes
+ * (0 for order 1), face fluxes, gather + cell update. */
+rg_status rg_step_timed(rg_handle* h, double* dt_out, float* kernel_ms);
+/* Enqueues one fused step on the handle's stream and returns at once; its
+ * failures surface at the next rg_synchronize. */
+rg_status rg_step_async(rg_handle* h);
+/* Waits for the handle's stream; returns the first failure of the enqueued
+ * steps and the dt of the last one (dt_last may be NULL). */
+rg_status rg_synchronize(rg_handle* h, double* dt_last);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,200 @@
+"""GPU parity: the CUDA path through the C ABI against the reference fixtures
+and the oracle, bit-for-bit (IEEE ==, FP64 plain path).
+
+Golden cases come from the reference itself (tests/golden/); larger meshes
+come from synthetic.lattice_mesh and are checked against the oracle
+(oracle/rich_oracle.c), which is pinned to the reference by
+test_oracle_golden.py.
+"""
+import numpy as np
+import pytest
+
+import oracle
+import richgpu
+import synthetic
+from conftest import GOLDEN_CASES, load_golden
+from test_oracle_golden import accumulate, exact
+
+pytestmark = pytest.mark.gpu
+
+
+def handle_for(gamma, order, ghost_kind, **kw):
+    return richgpu.Handle(gamma=gamma, order=order, ghost_kind=ghost_kind, device=0, **kw)
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_golden_components(name):
+    """Each plugin operation on the reference's inputs gives the reference's outputs."""
+    g = load_golden(name)
+    with handle_for(g["gamma"], g["order"], g["ghost_kind"]) as h:
+        h.upload_mesh(g["mesh"])
+        h.set_cells(g["cells0"])
+        h.set_edge_velocities(g["ev_cfl"])
+        assert h.cfl_dt() == g["dt"]                                  # SimpleCFL
+        h.set_edge_velocities(g["ev_flux"])
+        exact(h.flux(g["dt"]), g["fluxes"])                            # FluxCalculator
+        h.set_extensives(g["ext0"])
+        h.extensive_update(g["dt"])                                    # SimpleExtensiveUpdater
+        exact(h.get_extensives(), g["ext1"])
+        h.cell_update()                                                # SimpleCellUpdater
+        exact(h.get_cells(), g["cells1"])
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_golden_extensive_update_from_host_fluxes(name):
+    """The extensive updater also accepts fluxes computed elsewhere (rg_set_fluxes)."""
+    g = load_golden(name)
+    with handle_for(g["gamma"], g["order"], g["ghost_kind"]) as h:
+        h.upload_mesh(g["mesh"])
+        h.set_extensives(g["ext0"])
+        h.set_fluxes(g["fluxes"])
+        h.extensive_update(g["dt"])
+        exact(h.get_extensives(), g["ext1"])
+
+
+@pytest.mark.parametrize("name", [c for c in GOLDEN_CASES if "lagrangian" not in c and c != "sedov_o2"])
+def test_golden_hdsim_run(name):
+    """rg_run reproduces N hdsim::TimeAdvance steps (fixed mesh) exactly."""
+    g = load_golden(name)
+    steps = int(g["case_params"][3])
+    with handle_for(g["gamma"], g["order"], g["ghost_kind"]) as h:
+        h.upload_mesh(g["mesh"])
+        h.set_cells(g["cells0"])
+        h.set_extensives(g["ext0"])
+        h.set_edge_velocities(np.zeros((g["mesh"].n_faces, 2)))
+        dts = h.run(steps)
+        exact(accumulate(float(g["time0"][0]), dts), g["run_times"])
+        exact(h.get_extensives(), g["run_ext"])
+        exact(h.get_cells(), g["run_cells"])
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_golden_fused_step(name):
+    """rg_step (dt on the device) equals the split plugin sequence."""
+    g = load_golden(name)
+    with handle_for(g["gamma"], g["order"], g["ghost_kind"]) as h:
+        h.upload_mesh(g["mesh"])
+        h.set_cells(g["cells0"])
+        h.set_extensives(g["ext0"])
+        h.set_edge_velocities(g["ev_cfl"])
+        dt = h.step()
+        cells, ext = h.get_cells(), h.get_extensives()
+    oc, oe, odt = oracle.step(g["mesh"], g["cells0"], g["ext0"], g["ev_cfl"], g["gamma"], 0.3, g["order"],
+                              oracle.lgi_params(g["ghost_kind"]))
+    assert dt == odt
+    exact(ext, oe)
+    exact(cells, oc)
+
+
+def moving_faces(mesh, seed, scale):
+    rng = np.random.default_rng(seed)
+    pv = rng.normal(0, scale, (mesh.n_cells, 2))
+    return synthetic.face_velocities(mesh, pv)
+
+
+CASES = {
+    # name: (mesh args, gamma, order, ghost kind, state)
+    "sod_200x40_o1": ((200, 40, (0.0, 1.0, 0.0, 0.2), "rigid", 1), 1.4, 1, 0, "sod"),
+    "sedov_128_o2": ((128, 128, (-1.0, 1.0, -1.0, 1.0), "rigid", 2), 5 / 3, 2, 0, "sedov"),
+    "periodic_128_o2": ((128, 128, (0.0, 1.0, 0.0, 1.0), "periodic", 3), 5 / 3, 2, 1, "bumps"),
+    "periodic_96x64_o1": ((96, 64, (0.0, 1.0, 0.0, 1.0), "periodic", 4), 5 / 3, 1, 1, "bumps"),
+}
+
+
+def initial(mesh, kind, gamma):
+    return {"sod": synthetic.sod_cells, "sedov": lambda m: synthetic.sedov_cells(m, gamma),
+            "bumps": synthetic.bumps_cells}[kind](mesh)
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_synthetic_multistep_vs_oracle(case):
+    """20 fused steps on a larger seeded mesh equal 20 oracle steps."""
+    (nx, ny, box, bnd, seed), gamma, order, gk, kind = CASES[case]
+    mesh = synthetic.lattice_mesh(nx, ny, box, bnd, seed=seed)
+    cells = initial(mesh, kind, gamma)
+    ext = oracle.init_extensives(mesh, cells, gamma)
+    ev = np.zeros((mesh.n_faces, 2))
+    with handle_for(gamma, order, gk) as h:
+        h.upload_mesh(mesh)
+        h.set_cells(cells)
+        h.init_extensives()
+        exact(h.get_extensives(), ext)                                 # hdsim init_extensives
+        h.set_edge_velocities(ev)
+        dts = h.run(20)
+        gc, ge = h.get_cells(), h.get_extensives()
+    oc, oe, odts = oracle.run(mesh, cells, ext, ev, gamma, 20, 0.3, order, oracle.lgi_params(gk))
+    exact(dts, odts)
+    exact(ge, oe)
+    exact(gc, oc)
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_synthetic_moving_faces_vs_oracle(case):
+    """Non-zero face velocities (moving-mesh boost) on every plugin operation."""
+    (nx, ny, box, bnd, seed), gamma, order, gk, kind = CASES[case]
+    mesh = synthetic.lattice_mesh(nx, ny, box, bnd, seed=seed)
+    cells = initial(mesh, kind, gamma)
+    ext = oracle.init_extensives(mesh, cells, gamma)
+    ev = moving_faces(mesh, seed, 0.05)
+    with handle_for(gamma, order, gk) as h:
+        h.upload_mesh(mesh)
+        h.set_cells(cells)
+        h.set_extensives(ext)
+        h.set_edge_velocities(ev)
+        dt = h.cfl_dt()
+        assert dt == oracle.cfl(mesh, cells, ev, gamma)
+        fl = h.flux(dt)
+        ofl = (oracle.simple_flux(mesh, cells, ev, gamma) if order == 1
+               else oracle.modular_flux(mesh, cells, ev, gamma, oracle.lgi_params(gk)))
+        exact(fl, ofl)
+        h.extensive_update(dt)
+        oe = oracle.extensive_update(mesh, ofl, dt, ext)
+        exact(h.get_extensives(), oe)
+        h.cell_update()
+        exact(h.get_cells(), oracle.cell_update(mesh, oe, gamma))
+
+
+def test_full_size_sedov_512_one_step_vs_oracle():
+    """The headline 512x512 Sedov configuration: one fused step, bit-exact."""
+    mesh = synthetic.lattice_mesh(512, 512, (-1.0, 1.0, -1.0, 1.0), "rigid", seed=2)
+    gamma = 5 / 3
+    cells = synthetic.sedov_cells(mesh, gamma)
+    ext = oracle.init_extensives(mesh, cells, gamma)
+    ev = moving_faces(mesh, 9, 1e-3)
+    with handle_for(gamma, 2, 0) as h:
+        h.upload_mesh(mesh)
+        h.set_cells(cells)
+        h.set_extensives(ext)
+        h.set_edge_velocities(ev)
+        dt = h.step()
+        gc, ge = h.get_cells(), h.get_extensives()
+    oc, oe, odt = oracle.step(mesh, cells, ext, ev, gamma, 0.3, 2, oracle.lgi_params(0))
+    assert dt == odt
+    exact(ge, oe)
+    exact(gc, oc)
+
+
+def test_full_size_conservation_and_determinism():
+    """512x512 Sedov, 100 fused steps: mass, momentum and energy conserved to
+    round-off; a second run is bitwise identical (no atomics on the data path)."""
+    mesh = synthetic.lattice_mesh(512, 512, (-1.0, 1.0, -1.0, 1.0), "rigid", seed=2)
+    gamma = 5 / 3
+    cells = synthetic.sedov_cells(mesh, gamma)
+    ext0 = oracle.init_extensives(mesh, cells, gamma)
+    outs = []
+    for _ in range(2):
+        with handle_for(gamma, 2, 0) as h:
+            h.upload_mesh(mesh)
+            h.set_cells(cells)
+            h.set_extensives(ext0)
+            h.set_edge_velocities(np.zeros((mesh.n_faces, 2)))
+            dts = h.run(100)
+            outs.append((h.get_cells(), h.get_extensives(), dts))
+    c1, e1, d1 = outs[0]
+    c2, e2, d2 = outs[1]
+    assert np.array_equal(c1, c2) and np.array_equal(e1, e2) and np.array_equal(d1, d2)
+    tot0, tot1 = ext0.sum(0), e1.sum(0)
+    assert abs(tot1[0] - tot0[0]) <= 1e-13 * abs(tot0[0])                # mass
+    assert abs(tot1[1] - tot0[1]) <= 1e-12 * abs(tot0[1])                # energy
+    assert abs(tot1[2]) <= 1e-12 and abs(tot1[3]) <= 1e-12               # momentum (starts at 0)
+    assert np.all(np.isfinite(c1))
