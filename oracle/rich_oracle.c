@@ -325,7 +325,7 @@ static int naive_slope(const rg_mesh_view* m, int i, cc cell, v2 center, v2 cell
     return RG_ERR_TOO_MANY_NEIGHBORS;
   }
   double mm[4] = {0, 0, 0, 0};
-  slope vc;
+  slope vc = {{0, 0, 0, 0}, {0, 0, 0, 0}};
   for (int k = 0; k < n; ++k) {
     const int e = edges[k];
     const v2 c_ij = vsub(centroid(m, e), vscale(vadd(nb_cm[k], cell_cm), 0.5));
