@@ -1,0 +1,270 @@
+// rich_gpu_adapters.hpp -- RICH plugin classes backed by the GB300 library.
+//
+// Header-only C++ that a RICH build includes (include path = the RICH source
+// root plus this directory and include/), linking librich_gb300.so.  Each
+// class derives from the reference's own abstract interface, so hdsim
+// (source/newtonian/two_dimensional/hdsim2d.hpp:43) drives them unchanged:
+//
+//   GpuCFL                : TimeStepFunction  (time_step_function.hpp:16-39)
+//   GpuFluxCalculator     : FluxCalculator    (flux_calculator_2d.hpp:19-48)
+//   GpuExtensiveUpdater   : ExtensiveUpdater  (extensive_updater.hpp:19-47)
+//   GpuCellUpdater        : CellUpdater       (cell_updater_2d.hpp:20-45)
+//
+// All four share one GpuContext (one rg_handle).  Per call they upload what
+// hdsim passes (the tessellation only when it changed, which an unchanged
+// Eulerian rebuild does not), run the matching C-ABI operation and copy the
+// result back into hdsim's vectors.  A physical failure is rethrown as the
+// reference's UniversalError with its message and diagnostic entries.
+//
+// Supported: IdealGas, Hllc (massflux = true), SlabSymmetry, first order
+// (SimpleFluxCalculator) or LinearGaussImproved with RigidWallGenerator or
+// PeriodicGhostGenerator, no tracers or stickers.
+#ifndef RICH_GB300_ADAPTERS_HPP
+#define RICH_GB300_ADAPTERS_HPP
+
+#include <cstring>
+#include <stdexcept>
+#include <vector>
+
+#include "rich_gb300.h"
+#include "rich_pack.hpp"
+#include "source/misc/universal_error.hpp"
+#include "source/newtonian/common/ideal_gas.hpp"
+#include "source/newtonian/two_dimensional/cell_updater_2d.hpp"
+#include "source/newtonian/two_dimensional/extensive_updater.hpp"
+#include "source/newtonian/two_dimensional/flux_calculator_2d.hpp"
+#include "source/newtonian/two_dimensional/physical_geometry.hpp"
+#include "source/newtonian/two_dimensional/time_step_function.hpp"
+
+namespace rich_gb300 {
+
+class GpuContext {
+ public:
+  explicit GpuContext(const rg_config& cfg) : cfg_(cfg) {
+    const rg_status st = rg_create(&cfg_, &h_);
+    if (st != RG_OK) throw UniversalError(std::string("rich_gb300: rg_create failed: ") + rg_status_string(st));
+  }
+  ~GpuContext() { rg_destroy(h_); }
+  GpuContext(const GpuContext&) = delete;
+  GpuContext& operator=(const GpuContext&) = delete;
+
+  rg_handle* handle() const { return h_; }
+  const rg_config& config() const { return cfg_; }
+  int n_cells() const { return packed_.n_cells; }
+  int n_faces() const { return packed_.n_faces; }
+
+  // Packs the tessellation and uploads it unless it equals the last upload.
+  void sync_mesh(const Tessellation& tess, const CacheData* cd) const {
+    PackedMesh m;
+    if (cd) {
+      pack_tessellation(tess, *cd, m);
+    } else {
+      SlabSymmetry pg;
+      CacheData local(tess, pg);
+      pack_tessellation(tess, local, m);
+    }
+    if (have_mesh_ && same(m, packed_)) return;
+    packed_ = std::move(m);
+    const rg_mesh_view v = packed_.view();
+    check(rg_upload_mesh(h_, &v, 0));
+    have_mesh_ = true;
+    ++mesh_generation_;
+  }
+
+  void upload_cells(const std::vector<ComputationalCell>& cells) const {
+    std::vector<double> buf(4 * cells.size());
+    for (size_t i = 0; i < cells.size(); ++i) {
+      if (!cells[i].tracers.empty() || !cells[i].stickers.empty())
+        throw UniversalError("rich_gb300: tracers and stickers are not supported");
+      buf[4 * i] = cells[i].density;
+      buf[4 * i + 1] = cells[i].pressure;
+      buf[4 * i + 2] = cells[i].velocity.x;
+      buf[4 * i + 3] = cells[i].velocity.y;
+    }
+    check(rg_set_cells(h_, buf.data()));
+  }
+  void upload_extensives(const std::vector<Extensive>& ext) const {
+    std::vector<double> buf(4 * ext.size());
+    for (size_t i = 0; i < ext.size(); ++i) {
+      buf[4 * i] = ext[i].mass;
+      buf[4 * i + 1] = ext[i].energy;
+      buf[4 * i + 2] = ext[i].momentum.x;
+      buf[4 * i + 3] = ext[i].momentum.y;
+    }
+    check(rg_set_extensives(h_, buf.data()));
+  }
+  void download_extensives(std::vector<Extensive>& ext) const {
+    std::vector<double> buf(4 * ext.size());
+    check(rg_get_extensives(h_, buf.data()));
+    for (size_t i = 0; i < ext.size(); ++i) {
+      ext[i].mass = buf[4 * i];
+      ext[i].energy = buf[4 * i + 1];
+      ext[i].momentum.x = buf[4 * i + 2];
+      ext[i].momentum.y = buf[4 * i + 3];
+    }
+  }
+  void upload_edge_velocities(const std::vector<Vector2D>& ev) const {
+    std::vector<double> buf(2 * ev.size());
+    for (size_t i = 0; i < ev.size(); ++i) {
+      buf[2 * i] = ev[i].x;
+      buf[2 * i + 1] = ev[i].y;
+    }
+    check(rg_set_edge_velocities(h_, buf.data()));
+  }
+
+  // Fluxes the GPU flux calculator left on the device, identified by the
+  // buffer hdsim received (hdsim2d.cpp:176-195 passes that same vector on).
+  void mark_device_fluxes(const std::vector<Extensive>& f) const {
+    flux_data_ = f.data();
+    flux_size_ = f.size();
+    flux_generation_ = mesh_generation_;
+  }
+  bool device_fluxes_match(const std::vector<Extensive>& f) const {
+    return flux_data_ == f.data() && flux_size_ == f.size() && flux_generation_ == mesh_generation_;
+  }
+
+  void check_gamma(const EquationOfState& eos) const {
+    const IdealGas* ig = dynamic_cast<const IdealGas*>(&eos);
+    if (!ig || ig->getAdiabaticIndex() != cfg_.gamma)
+      throw UniversalError("rich_gb300: the equation of state must be IdealGas with the handle's gamma");
+  }
+
+  // Converts a failure into the reference's UniversalError.
+  void check(rg_status st) const {
+    if (st == RG_OK) return;
+    rg_error e;
+    rg_last_error(h_, &e);
+    UniversalError eo(rg_status_string(st));
+    if (st == RG_ERR_NEGATIVE_DENSITY || st == RG_ERR_NEGATIVE_ENERGY ||
+        st == RG_ERR_SINGULAR_MATRIX || st == RG_ERR_TOO_MANY_NEIGHBORS)
+      eo.AddEntry("Cell index", static_cast<double>(e.index));
+    else
+      eo.AddEntry("Edge index", static_cast<double>(e.index));
+    eo.AddEntry("Value", e.value);
+    throw eo;
+  }
+
+ private:
+  static bool same(const PackedMesh& a, const PackedMesh& b) {
+    return a.n_cells == b.n_cells && a.n_ghosts == b.n_ghosts && a.n_faces == b.n_faces &&
+           a.point_xy == b.point_xy && a.cm_xy == b.cm_xy && a.volume == b.volume && a.cd_volume == b.cd_volume &&
+           a.ghost_source == b.ghost_source && a.ghost_face == b.ghost_face && a.face_cells == b.face_cells &&
+           a.face_vertices == b.face_vertices && a.cell_face_offset == b.cell_face_offset &&
+           a.cell_faces == b.cell_faces;
+  }
+
+  rg_config cfg_;
+  rg_handle* h_ = nullptr;
+  mutable PackedMesh packed_;
+  mutable bool have_mesh_ = false;
+  mutable unsigned long mesh_generation_ = 0;
+  mutable const Extensive* flux_data_ = nullptr;
+  mutable size_t flux_size_ = 0;
+  mutable unsigned long flux_generation_ = 0;
+};
+
+// SimpleCFL (simple_cfl.cpp:58-71)
+class GpuCFL : public TimeStepFunction {
+ public:
+  explicit GpuCFL(const GpuContext& ctx) : ctx_(ctx) {}
+  double operator()(const Tessellation& tess, const vector<ComputationalCell>& cells, const EquationOfState& eos,
+                    const vector<Vector2D>& edge_velocities, const double /*time*/,
+                    TracerStickerNames const& /*tsn*/) const override {
+    ctx_.check_gamma(eos);
+    ctx_.sync_mesh(tess, nullptr);
+    ctx_.upload_cells(cells);
+    ctx_.upload_edge_velocities(edge_velocities);
+    double dt = 0;
+    ctx_.check(rg_cfl_dt(ctx_.handle(), &dt));
+    return dt;
+  }
+
+ private:
+  const GpuContext& ctx_;
+};
+
+// SimpleFluxCalculator / ModularFluxCalculator(LinearGaussImproved, Hllc)
+class GpuFluxCalculator : public FluxCalculator {
+ public:
+  explicit GpuFluxCalculator(const GpuContext& ctx) : ctx_(ctx) {}
+  vector<Extensive> operator()(const Tessellation& tess, const vector<Vector2D>& edge_velocities,
+                               const vector<ComputationalCell>& cells, const vector<Extensive>& /*extensives*/,
+                               const CacheData& cd, const EquationOfState& eos, const double /*time*/,
+                               const double dt, TracerStickerNames const& /*tsn*/) const override {
+    ctx_.check_gamma(eos);
+    ctx_.sync_mesh(tess, &cd);
+    ctx_.upload_cells(cells);
+    ctx_.upload_edge_velocities(edge_velocities);
+    std::vector<double> buf(4 * static_cast<size_t>(ctx_.n_faces()));
+    ctx_.check(rg_flux(ctx_.handle(), dt, buf.data()));
+    vector<Extensive> res(static_cast<size_t>(ctx_.n_faces()));
+    for (size_t i = 0; i < res.size(); ++i) {
+      res[i].mass = buf[4 * i];
+      res[i].energy = buf[4 * i + 1];
+      res[i].momentum.x = buf[4 * i + 2];
+      res[i].momentum.y = buf[4 * i + 3];
+    }
+    ctx_.mark_device_fluxes(res);
+    return res;
+  }
+
+ private:
+  const GpuContext& ctx_;
+};
+
+// SimpleExtensiveUpdater (simple_extensive_updater.cpp:11-35)
+class GpuExtensiveUpdater : public ExtensiveUpdater {
+ public:
+  explicit GpuExtensiveUpdater(const GpuContext& ctx) : ctx_(ctx) {}
+  void operator()(const vector<Extensive>& fluxes, const PhysicalGeometry& /*pg*/, const Tessellation& tess,
+                  const double dt, const CacheData& cd, const vector<ComputationalCell>& /*cells*/,
+                  vector<Extensive>& extensives, double /*time*/, TracerStickerNames const& /*tsn*/) const override {
+    ctx_.sync_mesh(tess, &cd);
+    if (!ctx_.device_fluxes_match(fluxes)) {
+      std::vector<double> buf(4 * fluxes.size());
+      for (size_t i = 0; i < fluxes.size(); ++i) {
+        buf[4 * i] = fluxes[i].mass;
+        buf[4 * i + 1] = fluxes[i].energy;
+        buf[4 * i + 2] = fluxes[i].momentum.x;
+        buf[4 * i + 3] = fluxes[i].momentum.y;
+      }
+      ctx_.check(rg_set_fluxes(ctx_.handle(), buf.data()));
+    }
+    ctx_.upload_extensives(extensives);
+    ctx_.check(rg_extensive_update(ctx_.handle(), dt));
+    ctx_.download_extensives(extensives);
+  }
+
+ private:
+  const GpuContext& ctx_;
+};
+
+// SimpleCellUpdater without a condition/action sequence (simple_cell_updater.cpp:85-106)
+class GpuCellUpdater : public CellUpdater {
+ public:
+  explicit GpuCellUpdater(const GpuContext& ctx) : ctx_(ctx) {}
+  vector<ComputationalCell> operator()(const Tessellation& tess, const PhysicalGeometry& /*pg*/,
+                                       const EquationOfState& eos, vector<Extensive>& extensives,
+                                       const vector<ComputationalCell>& /*old*/, const CacheData& cd,
+                                       TracerStickerNames const& /*tsn*/) const override {
+    ctx_.check_gamma(eos);
+    ctx_.sync_mesh(tess, &cd);
+    ctx_.upload_extensives(extensives);
+    ctx_.check(rg_cell_update(ctx_.handle()));
+    std::vector<double> buf(4 * extensives.size());
+    ctx_.check(rg_get_cells(ctx_.handle(), buf.data()));
+    vector<ComputationalCell> res(extensives.size());
+    for (size_t i = 0; i < res.size(); ++i) {
+      res[i].density = buf[4 * i];
+      res[i].pressure = buf[4 * i + 1];
+      res[i].velocity = Vector2D(buf[4 * i + 2], buf[4 * i + 3]);
+    }
+    return res;
+  }
+
+ private:
+  const GpuContext& ctx_;
+};
+
+}  // namespace rich_gb300
+#endif  // RICH_GB300_ADAPTERS_HPP
