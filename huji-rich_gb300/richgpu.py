@@ -22,7 +22,7 @@ EXPORTS = ("rg_default_config", "rg_create", "rg_destroy", "rg_status_string", "
            "rg_set_extensives", "rg_get_extensives", "rg_set_edge_velocities",
            "rg_device_buffers", "rg_init_extensives", "rg_cfl_dt", "rg_flux", "rg_set_fluxes",
            "rg_extensive_update", "rg_cell_update", "rg_step", "rg_run", "rg_step_async",
-           "rg_synchronize", "rg_step_timed")
+           "rg_synchronize", "rg_step_timed", "rg_cfl_dt_noalloc")
 
 
 class RgDeviceView(C.Structure):
@@ -76,6 +76,7 @@ def load(path=LIB_PATH):
     lib.rg_step_async.argtypes = [vp]
     lib.rg_synchronize.argtypes = [vp, dp]
     lib.rg_step_timed.argtypes = [vp, dp, C.POINTER(C.c_float)]
+    lib.rg_cfl_dt_noalloc.argtypes = [C.c_int32, vp, vp, vp, vp, vp, C.c_double, C.c_double, vp, vp]
     _lib = lib
     return lib
 

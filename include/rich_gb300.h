@@ -210,6 +210,26 @@ rg_status rg_step_async(rg_handle* h);
  * steps and the dt of the last one (dt_last may be NULL). */
 rg_status rg_synchronize(rg_handle* h, double* dt_last);
 
+/* Allocation-free time step ----------------------------------------------- */
+/* No counterpart in the reference.  The SimpleCFL dt of rg_cfl_dt for callers
+ * that may not allocate device memory (hosts whose own allocator or arena
+ * owns all GPU memory and must not see cudaMalloc / cudaFree in the step
+ * loop, which would synchronise the device and bypass their accounting).
+ * Every pointer is a caller-owned DEVICE pointer: cells n_cells*4, volume
+ * n_cells (Tessellation::GetVolume), cell_face_offset n_cells+1, cell_faces,
+ * edge_velocities n_faces*2; *dt_out (one double, device) receives the dt,
+ * asynchronously on `stream` (a cudaStream_t, NULL = default stream).
+ * Allocates nothing: its reduction scratch is a fixed 32 KiB device array
+ * inside the library, so n_cells is limited to 1,048,576 (larger values
+ * return RG_ERR_INVALID_ARGUMENT).  All calls share that array: calls that
+ * overlap on the GPU race, so serialise them.  The first call on a device
+ * looks up the array's address with that device current; make it before any
+ * stream capture. */
+rg_status rg_cfl_dt_noalloc(int32_t n_cells, const double* cells, const double* volume,
+                            const int32_t* cell_face_offset, const int32_t* cell_faces,
+                            const double* edge_velocities, double gamma, double cfl,
+                            double* dt_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
