@@ -10,8 +10,13 @@ SimpleExtensiveUpdater gather, SimpleCellUpdater -- hdsim::TimeAdvance's
 plugin work with the mesh held fixed (the Voronoi rebuild is host code and
 out of scope).
 
-value  device-resident inputs; each step timed with CUDA events on the
-       library's stream, L2 flushed (256 MiB write) before every timed step.
+value  the FP32-mixed form (reconstruction, HLLC and CFL in FP32; geometry,
+       volumes, extensive accumulation and the internal energy in FP64), with
+       its density L1 error against the plain FP64 path stated; the plain FP64
+       path (bit-identical to the reference) is measured in the same run and
+       reported under "fp64".  Device-resident inputs; each step timed with
+       CUDA events on the library's stream, L2 flushed (256 MiB write) before
+       every timed step.
 e2e    the same steps through the C ABI with host buffers, as a moving-mesh
        caller drives it: upload of the packed tessellation and the face
        velocities, the step, download of cells and extensives.
@@ -133,12 +138,16 @@ def ncu_traffic(kernel):
     return None
 
 
-def algorithmic_bytes(mesh):
-    """Compulsory bytes per launch of each kernel of a step (FP64, order 2).
+def algorithmic_bytes(mesh, precision=0):
+    """Compulsory bytes per launch of each kernel of a step (order 2).
     Geometry-only terms the design precomputes per mesh upload and the
-    intermediates (slopes, fluxes) are not algorithmic."""
+    intermediates (slopes, fluxes) are not algorithmic.  The FP32-mixed path
+    keeps primitives in FP32 (16 instead of 32 bytes per cell)."""
     n, f = mesh.n_cells, mesh.n_faces
     m = int(mesh.cell_face_offset[-1])
+    if precision == 1:
+        return {"cfl": 28 * n + 4 * m + 16 * f, "slopes": 60 * n + 4 * m, "faces": 56 * f,
+                "update": 92 * n + 8 * m}
     return {
         # cells in 32 + width 8 + CSR offset 4 per cell; face id 4 per CSR entry;
         # face velocity 16 per face
@@ -216,37 +225,25 @@ def run_reference(args, world, rank):
 
 # ------------------------------------------------------------------ GPU
 
-def run_gpu(args, world, rank, local_rank):
+KERNELS = ["cfl", "slopes", "faces", "update"]
+KERNEL_NAMES = {0: {"cfl": "k_cfl", "slopes": "k_slopes", "faces": "k_faces_lgi", "update": "k_update"},
+                1: {"cfl": "k_cfl32", "slopes": "k_slopes32", "faces": "k_faces32_lgi", "update": "k_update_mixed"}}
+
+
+def measure(precision, mesh, cells, ext, args, local_rank, barrier, max_over_ranks):
+    """Warm-up + timed steps of one precision; returns the timing record and
+    the final cells (for the accuracy comparison)."""
     import torch
     import richgpu
-    import oracle
 
-    torch.cuda.set_device(local_rank)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-    mesh, cells = workload()
-    ext = oracle.init_extensives(mesh, cells, GAMMA)
     ev0 = np.zeros((mesh.n_faces, 2))
-
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-
-    def max_over_ranks(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
-
-    h = richgpu.Handle(gamma=GAMMA, order=2, ghost_kind=0, device=local_rank)
+    h = richgpu.Handle(gamma=GAMMA, order=2, ghost_kind=0, precision=precision, device=local_rank)
     h.upload_mesh(mesh)
     h.set_cells(cells)
     h.set_extensives(ext)
     h.set_edge_velocities(ev0)
-    for _ in range(max(args.warmup, 3)):
+    warm = max(args.warmup, 3)
+    for _ in range(warm):
         h.step()
     stream = torch.cuda.ExternalStream(h.device_buffers().stream)
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
@@ -266,67 +263,125 @@ def run_gpu(args, world, rank, local_rank):
     barrier()
     wall = time.perf_counter() - wall0
     clock = clocks.stop()
+    final_cells = h.get_cells()
     kms = np.array(kms)
-    step_ms = kms.sum(1)
-    total_ms = max_over_ranks(float(step_ms.sum()))
-    value = world * mesh.n_cells * args.steps / (total_ms * 1e-3)
-    names = ["cfl", "slopes", "faces", "update"]
-    mean_k = kms.mean(0)
-    dom = int(np.argmax(mean_k))
-    alg = algorithmic_bytes(mesh)
-    peak, peak_kind = measured_peaks()
-    achieved = alg[names[dom]] / (mean_k[dom] * 1e-3) / 1e9
-    traffic = ncu_traffic(names[dom])
-    step_alg = 172 * mesh.n_cells + 64 * mesh.n_faces
+    total_ms = max_over_ranks(float(kms.sum()))
 
-    # end to end through the C ABI with host buffers (moving-mesh data flow)
+    # end to end through the C ABI with host buffers (moving-mesh data flow):
+    # the step's inputs (packed mesh, face velocities) in pinned host memory,
+    # its results (cells, extensives) read back into pinned host memory
+    pmesh, pev, pcells, pext = pinned_io(mesh, ev0, torch)
     ke = max(1, min(args.steps, 30))
-    h2d = mesh.nbytes() + 16 * mesh.n_faces
-    d2h = 2 * 32 * mesh.n_cells
     upload_ms = []
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(ke):
-        h.upload_mesh(mesh)
+        h.upload_mesh(pmesh)
         upload_ms.append(h.last_upload_ms())
-        h.set_edge_velocities(ev0)
+        h.set_edge_velocities(pev)
         h.step()
-        h.get_cells()
-        h.get_extensives()
+        h.get_cells(out=pcells)
+        h.get_extensives(out=pext)
     torch.cuda.synchronize()
     e2e_s = max_over_ranks(time.perf_counter() - t0)
-    e2e_value = world * mesh.n_cells * ke / e2e_s
-    launches = 4 * args.steps
     h.close()
+    del flush
+    return {"kernel_ms": kms.mean(0), "total_ms": total_ms, "wall": wall, "clock": clock,
+            "e2e_s": e2e_s, "e2e_steps": ke, "upload_ms": float(np.mean(upload_ms)),
+            "warmup": warm}, final_cells
+
+
+def pinned_io(mesh, ev, torch):
+    """Copies of the per-step inputs and outputs in pinned (page-locked) host memory."""
+    from meshview import MESH_FIELDS, PackedMesh
+
+    def pin(a):
+        t = torch.empty(a.shape, dtype=getattr(torch, str(a.dtype)), pin_memory=True)
+        out = t.numpy()
+        out[...] = a
+        return out
+    pm = PackedMesh(**{k: pin(getattr(mesh, k)) for k in MESH_FIELDS})
+    return (pm, pin(ev), pin(np.zeros((mesh.n_cells, 4))), pin(np.zeros((mesh.n_cells, 4))))
+
+
+def roofline(rec, mesh, precision):
+    alg = algorithmic_bytes(mesh, precision)
+    dom = int(np.argmax(rec["kernel_ms"]))
+    name = KERNELS[dom]
+    peak, peak_kind = measured_peaks()
+    achieved = alg[name] / (rec["kernel_ms"][dom] * 1e-3) / 1e9
+    kname = KERNEL_NAMES[precision][name]
+    step_alg = (172 if precision == 0 else 140) * mesh.n_cells + 64 * mesh.n_faces
+    step_ms = float(rec["kernel_ms"].sum())
+    return {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)",
+            "traffic": ncu_traffic(kname), "algorithmic_bytes_per_launch": alg[name],
+            "kernel_ms_mean": {KERNEL_NAMES[precision][k]: float(v) for k, v in zip(KERNELS, rec["kernel_ms"])},
+            "step_algorithmic_bytes": step_alg, "step_achieved_gbs": step_alg / (step_ms * 1e-3) / 1e9}
+
+
+def run_gpu(args, world, rank, local_rank):
+    import torch
+    import oracle
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    mesh, cells = workload()
+    ext = oracle.init_extensives(mesh, cells, GAMMA)
+    r64, c64 = measure(0, mesh, cells, ext, args, local_rank, barrier, max_over_ranks)
+    r32, c32 = measure(1, mesh, cells, ext, args, local_rank, barrier, max_over_ranks)
+    l1 = float(np.abs(c32[:, 0] - c64[:, 0]).sum() / np.abs(c64[:, 0]).sum())
+    n, k = mesh.n_cells, args.steps
+    value32 = world * n * k / (r32["total_ms"] * 1e-3)
+    value64 = world * n * k / (r64["total_ms"] * 1e-3)
+    h2d = mesh.nbytes() + 16 * mesh.n_faces
+    d2h = 2 * 32 * n
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        k, t = cpu_steps(mesh, cells, ext)
-        cpu = {"value": mesh.n_cells * k / t, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"{k} steps of the same {NX}x{NY} workload, one thread, C restatement "
+        kc, tc = cpu_steps(mesh, cells, ext)
+        cpu = {"value": n * kc / tc, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"{kc} steps of the same {NX}x{NY} workload (FP64), one thread, C restatement "
                          "oracle/rich_oracle.c (gcc -O2); the reference itself is serial"}
     if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-                "warmup": max(args.warmup, 3), "ms_per_step": total_ms / args.steps,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic", "config": config_block(mesh),
-                "roofline": {"bound": "hbm", "kernel": "k_faces_lgi" if names[dom] == "faces" else names[dom],
-                             "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                             "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)",
-                             "traffic": traffic,
-                             "algorithmic_bytes_per_launch": alg[names[dom]],
-                             "kernel_ms_mean": {n_: float(v) for n_, v in zip(names, mean_k)},
-                             "step_algorithmic_bytes": step_alg,
-                             "step_achieved_gbs": step_alg / (total_ms / args.steps * 1e-3) / 1e9,
-                             "note": "FP64 plain path: bound by GB300's FP64 pipe, not HBM"},
+        line = {"metric": METRIC, "value": value32, "unit": UNIT, "n_gpus": world, "steps": k,
+                "warmup": r32["warmup"], "ms_per_step": r32["total_ms"] / k, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+                "data": "synthetic", "config": config_block(mesh, "fp32mixed"),
+                "precision": "FP32-mixed: reconstruction, HLLC, CFL in FP32; geometry, volumes, "
+                             "extensive accumulation, E/m - v^2/2 in FP64",
+                "l1_density_vs_fp64": l1, "l1_after_steps": r32["warmup"] + k,
+                "roofline": roofline(r32, mesh, 1),
                 "cpu_baseline": cpu,
-                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                        "d2h_bytes_per_step": int(d2h), "steps": ke,
-                        "upload_ms_mean": float(np.mean(upload_ms))},
-                "gpu_launches": launches, "clocks": clock,
-                "faces_per_s": world * mesh.n_faces * args.steps / (total_ms * 1e-3),
-                "wall_s_timed_region": wall}
+                "e2e": {"value": world * n * r32["e2e_steps"] / r32["e2e_s"], "unit": UNIT,
+                        "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                        "steps": r32["e2e_steps"], "upload_ms_mean": r32["upload_ms"]},
+                "gpu_launches": 4 * k, "clocks": r32["clock"],
+                "faces_per_s": world * mesh.n_faces * k / (r32["total_ms"] * 1e-3),
+                "fp64": {"value": value64, "ms_per_step": r64["total_ms"] / k, "dtype": "f64",
+                         "bit_exact_vs_reference": True, "roofline": roofline(r64, mesh, 0),
+                         "note": "plain FP64 path: bound by GB300's FP64 pipe (2 DFMA/clk/SM), not HBM",
+                         "e2e": {"value": world * n * r64["e2e_steps"] / r64["e2e_s"], "unit": UNIT,
+                                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+                         "clocks": r64["clock"]},
+                "speedup_fp32mixed_vs_fp64": value32 / value64,
+                "wall_s_timed_region": r32["wall"] + r64["wall"]}
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

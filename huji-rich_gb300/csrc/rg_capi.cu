@@ -17,9 +17,11 @@
 #include <cstdint>
 #include <cstring>
 #include <new>
+#include <thread>
 #include <vector>
 
 #include "rg_internal.cuh"
+#include "rg_mixed.cuh"
 
 using rg::DevStatus;
 
@@ -72,8 +74,9 @@ struct HostBuf {
 struct SlotLayout {
   size_t points, cms, volume, cd_volume, ghost_source, ghost_face, face_cells, face_vertices, cell_off,
       cell_faces, input_end;
-  size_t area, nrm, nabs, par, dm0, dm1, width, minv, cflags, nbr, hr, ghost_real, ghost_unit, total;
-  void compute(int n, int g, int e, int m) {
+  size_t area, nrm, nabs, par, dm0, dm1, width, minv, cflags, nbr, hr, ghost_real, ghost_unit;
+  size_t nrm32, nabs32, par32, area32, dm0_32, dm1_32, width32, minv32, hr32, gunit32, total;
+  void compute(int n, int g, int e, int m, bool mixed) {
     const size_t np = static_cast<size_t>(n) + g;
     size_t o = 0;
     auto take = [&o](size_t bytes) {
@@ -105,6 +108,17 @@ struct SlotLayout {
     hr = take(16 * static_cast<size_t>(m));
     ghost_real = take(4 * static_cast<size_t>(g));
     ghost_unit = take(16 * static_cast<size_t>(g));
+    const size_t k = mixed ? 1 : 0;  // FP32 copies only for the mixed path
+    nrm32 = take(k * 8 * static_cast<size_t>(e));
+    nabs32 = take(k * 4 * static_cast<size_t>(e));
+    par32 = take(k * 8 * static_cast<size_t>(e));
+    area32 = take(k * 4 * static_cast<size_t>(e));
+    dm0_32 = take(k * 8 * static_cast<size_t>(e));
+    dm1_32 = take(k * 8 * static_cast<size_t>(e));
+    width32 = take(k * 4 * static_cast<size_t>(n));
+    minv32 = take(k * 16 * static_cast<size_t>(n));
+    hr32 = take(k * 8 * static_cast<size_t>(m));
+    gunit32 = take(k * 8 * static_cast<size_t>(g));
     total = o;
   }
 };
@@ -116,6 +130,7 @@ struct MeshSlot {
   SlotLayout lay;
   rg::MeshDev mesh{};
   rg::GeomDev geom{};
+  rg::MixedGeom g32{};
   rg_error geom_error{};  // reconstruction failure found by the geometry pass
   cudaEvent_t last_use = nullptr;
 };
@@ -137,6 +152,9 @@ struct rg_handle {
   int active = -1;
   // state
   DevBuf cells, ext, ev, slopes, fluxes, status_buf;
+  // FP32-mixed path: FP32 primitives (n + g records), slopes, face fluxes, edge velocities
+  DevBuf cells32, slopes32, flux32, ev32;
+  bool mixed = false;
   size_t cells_records = 0;
   bool have_cells = false, have_ext = false, have_ev = false, have_fluxes = false;
   HostBuf staging, host_status, host_dts;
@@ -174,9 +192,10 @@ rg_status invalid(rg_handle* h, int64_t index, double value) {
     if (s_ != RG_OK) return s_;       \
   } while (0)
 
-// Host-side validation of a packed mesh; returns the index of the first bad
-// entry through *bad (encoded per array) or 0 if the mesh is consistent.
-rg_status validate(rg_handle* h, const rg_mesh_view* v) {
+// Host-side checks of a packed mesh view that need no O(size) pass: counts,
+// pointers and the CSR length.  Every index is checked on the device
+// (k_validate) before any other kernel uses the mesh.
+rg_status check_view(rg_handle* h, const rg_mesh_view* v) {
   if (!v || v->n_cells <= 0 || v->n_ghosts < 0 || v->n_faces < 0) return invalid(h, -1, 0);
   if (static_cast<int64_t>(v->n_cells) + v->n_ghosts > static_cast<int64_t>(rg::kNbrIdMask))
     return invalid(h, -2, 0);
@@ -184,32 +203,38 @@ rg_status validate(rg_handle* h, const rg_mesh_view* v) {
       !v->cell_face_offset || !v->cell_faces)
     return invalid(h, -3, 0);
   if (v->n_ghosts > 0 && (!v->ghost_source || !v->ghost_face)) return invalid(h, -3, 0);
-  const int n = v->n_cells, g = v->n_ghosts, e = v->n_faces;
-  const int np = n + g;
-  for (int f = 0; f < e; ++f) {
-    const int a = v->face_cells[2 * f], b = v->face_cells[2 * f + 1];
-    if (a < 0 || a >= np || b < 0 || b >= np || a == b || (a >= n && b >= n))
-      return invalid(h, f, static_cast<double>(a >= 0 && a < np ? b : a));
-  }
-  for (int k = 0; k < g; ++k) {
-    if (v->ghost_source[k] < 0 || v->ghost_source[k] >= n) return invalid(h, k, v->ghost_source[k]);
-    const int gf = v->ghost_face[k];
-    if (gf < -1 || gf >= e) return invalid(h, k, gf);
-    if (gf >= 0 && v->face_cells[2 * gf] != n + k && v->face_cells[2 * gf + 1] != n + k)
-      return invalid(h, k, gf);
-  }
-  if (v->cell_face_offset[0] != 0) return invalid(h, 0, v->cell_face_offset[0]);
-  for (int i = 0; i < n; ++i) {
-    const int b = v->cell_face_offset[i], en = v->cell_face_offset[i + 1];
-    if (en < b || en - b > (1 << 20)) return invalid(h, i, en);
-    for (int k = b; k < en; ++k) {
-      const int f = v->cell_faces[k];
-      if (f < 0 || f >= e) return invalid(h, i, f);
-      if (k > b && f <= v->cell_faces[k - 1]) return invalid(h, i, f);  // ascending order
-      if (v->face_cells[2 * f] != i && v->face_cells[2 * f + 1] != i) return invalid(h, i, f);
-    }
-  }
+  const int m = v->cell_face_offset[v->n_cells];
+  if (v->cell_face_offset[0] != 0 || m < 0 || m > 2 * v->n_faces) return invalid(h, -4, m);
   return RG_OK;
+}
+
+bool is_pinned(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+// memcpy split over a few threads for the large arrays of a mesh.
+void par_memcpy(void* dst, const void* src, size_t bytes) {
+  const size_t kChunk = size_t(4) << 20;
+  const unsigned hw = std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
+  const size_t parts = std::min<size_t>(hw, (bytes + kChunk - 1) / kChunk);
+  if (parts <= 1) {
+    std::memcpy(dst, src, bytes);
+    return;
+  }
+  std::vector<std::thread> pool;
+  const size_t per = (bytes + parts - 1) / parts;
+  for (size_t k = 0; k < parts; ++k) {
+    const size_t off = k * per;
+    if (off >= bytes) break;
+    const size_t len = std::min(per, bytes - off);
+    pool.emplace_back([=] { std::memcpy(static_cast<char*>(dst) + off, static_cast<const char*>(src) + off, len); });
+  }
+  for (auto& t : pool) t.join();
 }
 
 void fill_views(MeshSlot& s) {
@@ -242,6 +267,16 @@ void fill_views(MeshSlot& s) {
   s.geom.hr = at<double2>(b, L.hr);
   s.geom.ghost_real = at<int>(b, L.ghost_real);
   s.geom.ghost_unit = at<double2>(b, L.ghost_unit);
+  s.g32.nrm = at<float2>(b, L.nrm32);
+  s.g32.nabs = at<float>(b, L.nabs32);
+  s.g32.par = at<float2>(b, L.par32);
+  s.g32.area = at<float>(b, L.area32);
+  s.g32.dm0 = at<float2>(b, L.dm0_32);
+  s.g32.dm1 = at<float2>(b, L.dm1_32);
+  s.g32.width = at<float>(b, L.width32);
+  s.g32.minv = at<float4>(b, L.minv32);
+  s.g32.hr = at<float2>(b, L.hr32);
+  s.g32.ghost_unit = at<float2>(b, L.gunit32);
 }
 
 rg_status reset_status(rg_handle* h, DevStatus* st, cudaStream_t s) {
@@ -295,6 +330,32 @@ rg::StepArgs step_args(rg_handle* h) {
   return a;
 }
 
+rg::MixedArgs mixed_args(rg_handle* h) {
+  MeshSlot* s = active_slot(h);
+  rg::MixedArgs a{};
+  a.mesh = s->mesh;
+  a.geom = s->geom;
+  a.g32 = s->g32;
+  a.gamma = static_cast<float>(h->cfg.gamma);
+  a.cfl = h->cfg.cfl;
+  a.order = h->cfg.order;
+  a.ghost_kind = h->cfg.ghost_kind;
+  a.slf = h->cfg.slope_limiter;
+  a.delta_v = static_cast<float>(h->cfg.delta_v);
+  a.theta = static_cast<float>(h->cfg.theta);
+  a.delta_p = static_cast<float>(h->cfg.delta_p);
+  a.cells32 = static_cast<float4*>(h->cells32.p);
+  a.slopes32 = static_cast<float4*>(h->slopes32.p);
+  a.flux32 = static_cast<float4*>(h->flux32.p);
+  a.ev32 = static_cast<const float2*>(h->ev32.p);
+  a.ext = static_cast<double*>(h->ext.p);
+  a.status = h->d_status;
+  a.dt32 = 0;
+  a.dt32_from_device = 0;
+  a.step = 0;
+  return a;
+}
+
 rg_status require(rg_handle* h, bool cells, bool ext, bool ev, bool fluxes) {
   if (!h) return RG_ERR_INVALID_ARGUMENT;
   if (h->active < 0 || (cells && !h->have_cells) || (ext && !h->have_ext) || (ev && !h->have_ev) ||
@@ -317,6 +378,22 @@ rg_status mesh_error(rg_handle* h) {
 // Enqueues one fused step (no host synchronisation).  With ev != nullptr,
 // records ev[0..4] around its kernels.
 rg_status enqueue_step(rg_handle* h, int step, cudaEvent_t* ev = nullptr) {
+  if (h->mixed) {
+    rg::MixedArgs a = mixed_args(h);
+    a.dt32_from_device = 1;
+    a.step = step;
+    if (ev) RG_CUDA(h, cudaEventRecord(ev[0], h->stream));
+    RG_CUDA(h, rg::launch_cfl32(a, h->stream, h->cfg.order == 2));
+    if (ev) RG_CUDA(h, cudaEventRecord(ev[1], h->stream));
+    if (h->cfg.order == 2) RG_CUDA(h, rg::launch_slopes32(a, h->stream));
+    if (ev) RG_CUDA(h, cudaEventRecord(ev[2], h->stream));
+    RG_CUDA(h, rg::launch_faces32(a, h->stream, true));
+    if (ev) RG_CUDA(h, cudaEventRecord(ev[3], h->stream));
+    RG_CUDA(h, rg::launch_update_mixed(a, h->stream, false, true, true));
+    if (ev) RG_CUDA(h, cudaEventRecord(ev[4], h->stream));
+    h->have_fluxes = false;
+    return RG_OK;
+  }
   rg::StepArgs a = step_args(h);
   a.dt_from_device = 1;
   a.step = step;
@@ -385,6 +462,7 @@ rg_status rg_create(const rg_config* cfg, rg_handle** out) {
   rg_handle* h = new (std::nothrow) rg_handle();
   if (!h) return RG_ERR_OUT_OF_MEMORY;
   h->cfg = *cfg;
+  h->mixed = cfg->precision == RG_FP32_MIXED;
   auto fail = [&](cudaError_t e) {
     rg_destroy(h);
     cudaGetLastError();
@@ -426,6 +504,10 @@ rg_status rg_destroy(rg_handle* h) {
   h->ev.release();
   h->slopes.release();
   h->fluxes.release();
+  h->cells32.release();
+  h->slopes32.release();
+  h->flux32.release();
+  h->ev32.release();
   h->status_buf.release();
   h->staging.release();
   h->host_status.release();
@@ -451,18 +533,15 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t /*flags*/
   if (!h) return RG_ERR_INVALID_ARGUMENT;
   h->last = rg_error{};
   const auto t0 = std::chrono::steady_clock::now();
-  if (rg_status st = validate(h, v)) return st;
+  if (rg_status st = check_view(h, v)) return st;
   RG_CUDA(h, cudaSetDevice(h->cfg.device));
   const int n = v->n_cells, g = v->n_ghosts, e = v->n_faces, m = v->cell_face_offset[n];
-  if (h->active >= 0 && active_slot(h)->n != n) {
-    // the cell count changed: the state no longer matches the mesh
-    h->have_cells = h->have_ext = false;
-  }
+  const bool n_changed = h->active >= 0 && active_slot(h)->n != n;
   const int next = h->active < 0 ? 0 : 1 - h->active;
   MeshSlot& s = h->slots[next];
   // the slot may still be read by kernels enqueued on the previous-but-one mesh
   RG_CUDA(h, cudaStreamWaitEvent(h->upload_stream, s.last_use, 0));
-  s.lay.compute(n, g, e, m);
+  s.lay.compute(n, g, e, m, h->mixed);
   RG_CUDA(h, cudaStreamSynchronize(h->upload_stream));
   RG_CUDA(h, s.buf.ensure(s.lay.total));
   RG_CUDA(h, h->staging.ensure(s.lay.input_end));
@@ -471,23 +550,49 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t /*flags*/
   s.e = e;
   s.m = m;
   fill_views(s);
-  // pack into pinned staging with the device layout, then one async copy
+  // inputs: straight from the caller's arrays when they are pinned, through
+  // the pinned staging buffer otherwise
   char* st = static_cast<char*>(h->staging.p);
   const size_t np = static_cast<size_t>(n) + g;
-  std::memcpy(st + s.lay.points, v->point_xy, 16 * np);
-  std::memcpy(st + s.lay.cms, v->cm_xy, 16 * np);
-  std::memcpy(st + s.lay.volume, v->volume, 8 * static_cast<size_t>(n));
-  std::memcpy(st + s.lay.cd_volume, v->cd_volume, 8 * static_cast<size_t>(n));
-  if (g) {
-    std::memcpy(st + s.lay.ghost_source, v->ghost_source, 4 * static_cast<size_t>(g));
-    std::memcpy(st + s.lay.ghost_face, v->ghost_face, 4 * static_cast<size_t>(g));
-  }
-  std::memcpy(st + s.lay.face_cells, v->face_cells, 8 * static_cast<size_t>(e));
-  std::memcpy(st + s.lay.face_vertices, v->face_vertices, 32 * static_cast<size_t>(e));
-  std::memcpy(st + s.lay.cell_off, v->cell_face_offset, 4 * (static_cast<size_t>(n) + 1));
-  std::memcpy(st + s.lay.cell_faces, v->cell_faces, 4 * static_cast<size_t>(m));
+  struct Part {
+    size_t off;
+    const void* src;
+    size_t bytes;
+  } parts[10] = {{s.lay.points, v->point_xy, 16 * np},
+                 {s.lay.cms, v->cm_xy, 16 * np},
+                 {s.lay.volume, v->volume, 8 * static_cast<size_t>(n)},
+                 {s.lay.cd_volume, v->cd_volume, 8 * static_cast<size_t>(n)},
+                 {s.lay.ghost_source, v->ghost_source, 4 * static_cast<size_t>(g)},
+                 {s.lay.ghost_face, v->ghost_face, 4 * static_cast<size_t>(g)},
+                 {s.lay.face_cells, v->face_cells, 8 * static_cast<size_t>(e)},
+                 {s.lay.face_vertices, v->face_vertices, 32 * static_cast<size_t>(e)},
+                 {s.lay.cell_off, v->cell_face_offset, 4 * (static_cast<size_t>(n) + 1)},
+                 {s.lay.cell_faces, v->cell_faces, 4 * static_cast<size_t>(m)}};
   RG_CUDA(h, cudaEventRecord(h->ev_up0, h->upload_stream));
-  RG_CUDA(h, cudaMemcpyAsync(s.buf.p, st, s.lay.input_end, cudaMemcpyHostToDevice, h->upload_stream));
+  for (const Part& p : parts) {
+    if (p.bytes == 0) continue;
+    if (is_pinned(p.src)) {
+      RG_CUDA(h, cudaMemcpyAsync(static_cast<char*>(s.buf.p) + p.off, p.src, p.bytes, cudaMemcpyHostToDevice,
+                                 h->upload_stream));
+    } else {
+      par_memcpy(st + p.off, p.src, p.bytes);
+      RG_CUDA(h, cudaMemcpyAsync(static_cast<char*>(s.buf.p) + p.off, st + p.off, p.bytes, cudaMemcpyHostToDevice,
+                                 h->upload_stream));
+    }
+  }
+  // every index checked before any kernel uses it
+  RG_TRY(reset_status(h, h->d_geom_status, h->upload_stream));
+  RG_CUDA(h, rg::launch_validate(s.mesh, h->d_geom_status, h->upload_stream));
+  {
+    DevStatus* hs = static_cast<DevStatus*>(h->host_status.p);
+    RG_CUDA(h, cudaMemcpyAsync(hs, h->d_geom_status, sizeof(DevStatus), cudaMemcpyDeviceToHost, h->upload_stream));
+    RG_CUDA(h, cudaStreamSynchronize(h->upload_stream));
+    if (hs->err_key != ~0ull) {
+      // the slot holds an invalid mesh: it is not activated
+      s.n = s.g = s.e = s.m = 0;
+      return invalid(h, static_cast<int64_t>(hs->err_key & rg::kKeyIndexMask), hs->err_value);
+    }
+  }
   // geometry pass on the upload stream
   RG_TRY(reset_status(h, h->d_geom_status, h->upload_stream));
   rg::GeomArgs ga{};
@@ -510,7 +615,30 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t /*flags*/
   ga.ghost_kind = h->cfg.ghost_kind;
   ga.status = h->d_geom_status;
   RG_CUDA(h, rg::launch_geometry(ga, h->upload_stream));
+  if (h->mixed) {
+    rg::MixedGeomArgs m32{};
+    m32.n = n;
+    m32.g = g;
+    m32.e = e;
+    m32.m = m;
+    m32.g64 = s.geom;
+    m32.nrm = at<float2>(b, s.lay.nrm32);
+    m32.nabs = at<float>(b, s.lay.nabs32);
+    m32.par = at<float2>(b, s.lay.par32);
+    m32.area = at<float>(b, s.lay.area32);
+    m32.dm0 = at<float2>(b, s.lay.dm0_32);
+    m32.dm1 = at<float2>(b, s.lay.dm1_32);
+    m32.width = at<float>(b, s.lay.width32);
+    m32.minv = at<float4>(b, s.lay.minv32);
+    m32.hr = at<float2>(b, s.lay.hr32);
+    m32.ghost_unit = at<float2>(b, s.lay.gunit32);
+    RG_CUDA(h, rg::launch_geom32(m32, h->upload_stream));
+  }
   RG_CUDA(h, cudaEventRecord(h->ev_up1, h->upload_stream));
+  if (n_changed) {
+    // the cell count changed: the state no longer matches the mesh
+    h->have_cells = h->have_ext = false;
+  }
   // state buffers sized for this mesh (cells keep their first n records)
   const size_t rec = np;
   if (rec > h->cells_records) {
@@ -521,6 +649,14 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t /*flags*/
       RG_CUDA(h, cudaMemcpy(nb.p, h->cells.p, 32 * static_cast<size_t>(n), cudaMemcpyDeviceToDevice));
     h->cells.release();
     h->cells = nb;
+    if (h->mixed) {
+      DevBuf nb32;
+      RG_CUDA(h, nb32.ensure(16 * rec));
+      if (h->cells32.p && h->have_cells)
+        RG_CUDA(h, cudaMemcpy(nb32.p, h->cells32.p, 16 * static_cast<size_t>(n), cudaMemcpyDeviceToDevice));
+      h->cells32.release();
+      h->cells32 = nb32;
+    }
     h->cells_records = rec;
   }
   const bool ext_keep = h->ext.bytes >= 32 * static_cast<size_t>(n);
@@ -531,6 +667,11 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t /*flags*/
   RG_CUDA(h, h->ev.ensure(16 * static_cast<size_t>(std::max(e, 1))));
   RG_CUDA(h, h->slopes.ensure(64 * static_cast<size_t>(n)));
   RG_CUDA(h, h->fluxes.ensure(32 * static_cast<size_t>(std::max(e, 1))));
+  if (h->mixed) {
+    RG_CUDA(h, h->slopes32.ensure(32 * static_cast<size_t>(n)));
+    RG_CUDA(h, h->flux32.ensure(16 * static_cast<size_t>(std::max(e, 1))));
+    RG_CUDA(h, h->ev32.ensure(8 * static_cast<size_t>(std::max(e, 1))));
+  }
   if (h->active >= 0 && active_slot(h)->e != e) h->have_ev = false;
   h->have_fluxes = false;
   // geometry errors (reconstruction would throw them) and timing
@@ -567,6 +708,9 @@ rg_status rg_set_cells(rg_handle* h, const double* cells) {
   if (h->active < 0) return require(h, false, false, false, false);
   RG_CUDA(h, cudaMemcpyAsync(h->cells.p, cells, 32 * static_cast<size_t>(active_slot(h)->n),
                              cudaMemcpyHostToDevice, h->stream));
+  if (h->mixed)
+    RG_CUDA(h, rg::launch_cells_to32(static_cast<const double*>(h->cells.p), static_cast<float4*>(h->cells32.p),
+                                     active_slot(h)->n, h->stream));
   RG_CUDA(h, cudaStreamSynchronize(h->stream));
   h->have_cells = true;
   return RG_OK;
@@ -575,6 +719,9 @@ rg_status rg_set_cells(rg_handle* h, const double* cells) {
 rg_status rg_get_cells(rg_handle* h, double* cells) {
   if (rg_status st = require(h, true, false, false, false)) return st;
   if (!cells) return RG_ERR_INVALID_ARGUMENT;
+  if (h->mixed)
+    RG_CUDA(h, rg::launch_cells_to64(static_cast<const float4*>(h->cells32.p), static_cast<double*>(h->cells.p),
+                                     active_slot(h)->n, h->stream));
   RG_CUDA(h, cudaMemcpyAsync(cells, h->cells.p, 32 * static_cast<size_t>(active_slot(h)->n),
                              cudaMemcpyDeviceToHost, h->stream));
   RG_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -605,6 +752,9 @@ rg_status rg_set_edge_velocities(rg_handle* h, const double* ev) {
   if (h->active < 0) return require(h, false, false, false, false);
   RG_CUDA(h, cudaMemcpyAsync(h->ev.p, ev, 16 * static_cast<size_t>(active_slot(h)->e),
                              cudaMemcpyHostToDevice, h->stream));
+  if (h->mixed)
+    RG_CUDA(h, rg::launch_vec2_to32(static_cast<const double*>(h->ev.p), static_cast<float2*>(h->ev32.p),
+                                    active_slot(h)->e, h->stream));
   RG_CUDA(h, cudaStreamSynchronize(h->stream));
   h->have_ev = true;
   return RG_OK;
@@ -615,6 +765,9 @@ rg_status rg_set_fluxes(rg_handle* h, const double* fl) {
   if (h->active < 0) return require(h, false, false, false, false);
   RG_CUDA(h, cudaMemcpyAsync(h->fluxes.p, fl, 32 * static_cast<size_t>(active_slot(h)->e),
                              cudaMemcpyHostToDevice, h->stream));
+  if (h->mixed)
+    RG_CUDA(h, rg::launch_flux_to32(static_cast<const double*>(h->fluxes.p), static_cast<float4*>(h->flux32.p),
+                                    active_slot(h)->e, h->stream));
   RG_CUDA(h, cudaStreamSynchronize(h->stream));
   h->have_fluxes = true;
   return RG_OK;
@@ -636,6 +789,9 @@ rg_status rg_device_buffers(rg_handle* h, rg_device_view* v) {
 rg_status rg_init_extensives(rg_handle* h) {
   if (rg_status st = require(h, true, false, false, false)) return st;
   rg::StepArgs a = step_args(h);
+  if (h->mixed)
+    RG_CUDA(h, rg::launch_cells_to64(static_cast<const float4*>(h->cells32.p), static_cast<double*>(h->cells.p),
+                                     active_slot(h)->n, h->stream));
   RG_CUDA(h, rg::launch_init_extensives(a, h->stream));
   RG_CUDA(h, cudaStreamSynchronize(h->stream));
   h->have_ext = true;
@@ -647,8 +803,12 @@ rg_status rg_cfl_dt(rg_handle* h, double* dt) {
   if (!dt) return RG_ERR_INVALID_ARGUMENT;
   h->last = rg_error{};
   RG_TRY(reset_status(h, h->d_status, h->stream));
-  rg::StepArgs a = step_args(h);
-  RG_CUDA(h, rg::launch_cfl(a, h->stream, false));
+  if (h->mixed) {
+    RG_CUDA(h, rg::launch_cfl32(mixed_args(h), h->stream, false));
+  } else {
+    rg::StepArgs a = step_args(h);
+    RG_CUDA(h, rg::launch_cfl(a, h->stream, false));
+  }
   rg_status st = collect(h, h->d_status, h->stream);
   *dt = h->last_dt;
   return st;
@@ -659,16 +819,29 @@ rg_status rg_flux(rg_handle* h, double dt, double* fluxes_out) {
   h->last = rg_error{};
   if (rg_status st = mesh_error(h)) return st;
   RG_TRY(reset_status(h, h->d_status, h->stream));
-  rg::StepArgs a = step_args(h);
-  a.dt_host = dt;
-  if (h->cfg.order == 2) {
-    RG_CUDA(h, rg::launch_ghost_fill(a, h->stream));
-    RG_CUDA(h, rg::launch_slopes(a, h->stream));
+  if (h->mixed) {
+    rg::MixedArgs a = mixed_args(h);
+    a.dt32 = static_cast<float>(dt);
+    if (h->cfg.order == 2) {
+      RG_CUDA(h, rg::launch_ghost_fill32(a, h->stream));
+      RG_CUDA(h, rg::launch_slopes32(a, h->stream));
+    }
+    RG_CUDA(h, rg::launch_faces32(a, h->stream, false));
+  } else {
+    rg::StepArgs a = step_args(h);
+    a.dt_host = dt;
+    if (h->cfg.order == 2) {
+      RG_CUDA(h, rg::launch_ghost_fill(a, h->stream));
+      RG_CUDA(h, rg::launch_slopes(a, h->stream));
+    }
+    RG_CUDA(h, rg::launch_faces(a, h->stream, false));
   }
-  RG_CUDA(h, rg::launch_faces(a, h->stream, false));
   if (rg_status st = collect(h, h->d_status, h->stream)) return st;
   h->have_fluxes = true;
   if (fluxes_out) {
+    if (h->mixed)
+      RG_CUDA(h, rg::launch_flux_to64(static_cast<const float4*>(h->flux32.p), static_cast<double*>(h->fluxes.p),
+                                      active_slot(h)->e, h->stream));
     RG_CUDA(h, cudaMemcpyAsync(fluxes_out, h->fluxes.p, 32 * static_cast<size_t>(active_slot(h)->e),
                                cudaMemcpyDeviceToHost, h->stream));
     RG_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -680,9 +853,15 @@ rg_status rg_extensive_update(rg_handle* h, double dt) {
   if (rg_status st = require(h, false, true, false, true)) return st;
   h->last = rg_error{};
   RG_TRY(reset_status(h, h->d_status, h->stream));
-  rg::StepArgs a = step_args(h);
-  a.dt_host = dt;
-  RG_CUDA(h, rg::launch_update(a, h->stream, true, true, false));
+  if (h->mixed) {
+    rg::MixedArgs a = mixed_args(h);
+    a.dt32 = static_cast<float>(dt);
+    RG_CUDA(h, rg::launch_update_mixed(a, h->stream, true, true, false));
+  } else {
+    rg::StepArgs a = step_args(h);
+    a.dt_host = dt;
+    RG_CUDA(h, rg::launch_update(a, h->stream, true, true, false));
+  }
   return collect(h, h->d_status, h->stream);
 }
 
@@ -690,8 +869,12 @@ rg_status rg_cell_update(rg_handle* h) {
   if (rg_status st = require(h, false, true, false, false)) return st;
   h->last = rg_error{};
   RG_TRY(reset_status(h, h->d_status, h->stream));
-  rg::StepArgs a = step_args(h);
-  RG_CUDA(h, rg::launch_update(a, h->stream, false, false, true));
+  if (h->mixed) {
+    RG_CUDA(h, rg::launch_update_mixed(mixed_args(h), h->stream, false, false, true));
+  } else {
+    rg::StepArgs a = step_args(h);
+    RG_CUDA(h, rg::launch_update(a, h->stream, false, false, true));
+  }
   rg_status st = collect(h, h->d_status, h->stream);
   if (st == RG_OK) h->have_cells = true;
   return st;

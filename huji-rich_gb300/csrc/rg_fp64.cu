@@ -180,6 +180,46 @@ __global__ void __launch_bounds__(kBlock) k_geom_ghosts(GeomArgs a) {
   a.ghost_unit[g] = make_double2(nr.x / ab, nr.y / ab);
 }
 
+// Index validation of an uploaded mesh, before any kernel indexes with it.
+// Every read is bounds-checked against the array sizes; the first bad entry
+// (smallest key: faces, then ghosts, then cells) is recorded.  Phase 0 keys:
+// index = array position, value = the offending entry.
+__global__ void __launch_bounds__(kBlock) k_validate(MeshDev m, DevStatus* st) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int np = m.n + m.g;
+  if (t < m.e) {
+    const int2 fc = m.face_cells[t];
+    if (fc.x < 0 || fc.x >= np || fc.y < 0 || fc.y >= np || fc.x == fc.y || (fc.x >= m.n && fc.y >= m.n))
+      record_error(st, 0, RG_ERR_INVALID_ARGUMENT, 0, t, fc.x);
+  }
+  if (t < m.g) {
+    const int src = m.ghost_source[t], gf = m.ghost_face[t];
+    bool bad = src < 0 || src >= m.n || gf < -1 || gf >= m.e;
+    if (!bad && gf >= 0) {
+      const int2 fc = m.face_cells[gf];
+      bad = fc.x != m.n + t && fc.y != m.n + t;
+    }
+    if (bad) record_error(st, 0, RG_ERR_INVALID_ARGUMENT, 0, (1ll << 40) + t, gf);
+  }
+  if (t < m.n) {
+    const int b = m.cell_off[t], e1 = m.cell_off[t + 1];
+    bool bad = (t == 0 && b != 0) || b < 0 || e1 < b || e1 > m.m || e1 - b > (1 << 20);
+    const int lo = b < 0 ? 0 : b, hi = e1 > m.m ? m.m : e1;
+    int prev = -1;
+    for (int k = lo; k < hi && !bad; ++k) {
+      const int f = m.cell_faces[k];
+      if (f < 0 || f >= m.e || f <= prev) {
+        bad = true;
+      } else {
+        const int2 fc = m.face_cells[f];
+        bad = fc.x != t && fc.y != t;
+      }
+      prev = f;
+    }
+    if (bad) record_error(st, 0, RG_ERR_INVALID_ARGUMENT, 0, (2ll << 40) + t, b);
+  }
+}
+
 // ---------------------------------------------------------------- per step
 
 // Ghost state (LinearGaussImproved.cpp:543-550 new_cells[ghost]):
@@ -641,6 +681,13 @@ __global__ void __launch_bounds__(kBlock) k_init_ext(StepArgs a) {
 inline int blocks(int n) { return (n + kBlock - 1) / kBlock; }
 
 }  // namespace
+
+cudaError_t launch_validate(const MeshDev& m, DevStatus* st, cudaStream_t s) {
+  int work = m.e > m.n ? m.e : m.n;
+  work = work > m.g ? work : m.g;
+  k_validate<<<blocks(work > 0 ? work : 1), kBlock, 0, s>>>(m, st);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_geometry(const GeomArgs& a, cudaStream_t s) {
   if (a.mesh.e > 0) k_geom_faces<<<blocks(a.mesh.e), kBlock, 0, s>>>(a);

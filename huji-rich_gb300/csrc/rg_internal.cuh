@@ -171,6 +171,7 @@ struct GeomArgs {
   DevStatus* status;
 };
 
+cudaError_t launch_validate(const MeshDev& m, DevStatus* st, cudaStream_t s);
 cudaError_t launch_geometry(const GeomArgs& a, cudaStream_t s);
 cudaError_t launch_cfl(const StepArgs& a, cudaStream_t s, bool fill_ghosts);
 cudaError_t launch_ghost_fill(const StepArgs& a, cudaStream_t s);

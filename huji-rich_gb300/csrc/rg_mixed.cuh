@@ -1,0 +1,69 @@
+// rg_mixed.cuh -- arguments and launchers of the FP32-mixed kernels
+// (rg_mixed.cu).  FP32 copies of the geometry live next to the FP64
+// geometry of each mesh slot; the neighbour words, cell flags and ghost
+// sources are shared with the FP64 path.
+#pragma once
+#include "rg_internal.cuh"
+
+namespace rg {
+
+struct MixedGeom {
+  const float2* nrm;
+  const float* nabs;
+  const float2* par;
+  const float* area;
+  const float2* dm0;
+  const float2* dm1;
+  const float* width;
+  const float4* minv;
+  const float2* hr;
+  const float2* ghost_unit;
+};
+
+struct MixedGeomArgs {
+  int n, g, e, m;
+  GeomDev g64;  // source (FP64 geometry of the same slot)
+  float2* nrm;
+  float* nabs;
+  float2* par;
+  float* area;
+  float2* dm0;
+  float2* dm1;
+  float* width;
+  float4* minv;
+  float2* hr;
+  float2* ghost_unit;
+};
+
+struct MixedArgs {
+  MeshDev mesh;
+  GeomDev geom;   // FP64 geometry: neighbour words, cell flags, ghost sources
+  MixedGeom g32;
+  float gamma;
+  double cfl;
+  int order, ghost_kind, slf;
+  float delta_v, theta, delta_p;
+  float4* cells32;   // n + g records (ghost states at the end)
+  float4* slopes32;  // 2 per cell
+  float4* flux32;    // per face, unscaled or dt*area scaled
+  const float2* ev32;
+  double* ext;       // FP64 extensives
+  DevStatus* status;
+  float dt32;            // dt given by the caller (split API)
+  int dt32_from_device;  // 1: dt from status->dt (fused step)
+  int step;
+};
+
+cudaError_t launch_geom32(const MixedGeomArgs& a, cudaStream_t s);
+cudaError_t launch_cells_to32(const double* c64, float4* c32, int n, cudaStream_t s);
+cudaError_t launch_cells_to64(const float4* c32, double* c64, int n, cudaStream_t s);
+cudaError_t launch_vec2_to32(const double* v64, float2* v32, int n, cudaStream_t s);
+cudaError_t launch_flux_to64(const float4* f32, double* f64, int n, cudaStream_t s);
+cudaError_t launch_flux_to32(const double* f64, float4* f32, int n, cudaStream_t s);
+cudaError_t launch_cfl32(const MixedArgs& a, cudaStream_t s, bool fill_ghosts);
+cudaError_t launch_ghost_fill32(const MixedArgs& a, cudaStream_t s);
+cudaError_t launch_slopes32(const MixedArgs& a, cudaStream_t s);
+cudaError_t launch_faces32(const MixedArgs& a, cudaStream_t s, bool scaled);
+cudaError_t launch_update_mixed(const MixedArgs& a, cudaStream_t s, bool from_unscaled, bool extensive, bool cells);
+
+}  // namespace rg

@@ -23,6 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 UNITS = {
     "rg_fp64.cu": ["--fmad=false"],
     "rg_capi.cu": [],
+    "rg_mixed.cu": [],
     "rg_noalloc.cu": ["--fmad=false"],
 }
 

@@ -137,8 +137,9 @@ class Handle:
         assert a.size == 4 * self.mesh.n_cells
         self._check(self.lib.rg_set_cells(self.h, dptr(a)))
 
-    def get_cells(self):
-        out = np.empty((self.mesh.n_cells, 4))
+    def get_cells(self, out=None):
+        out = np.empty((self.mesh.n_cells, 4)) if out is None else out
+        assert out.dtype == np.float64 and out.size == 4 * self.mesh.n_cells and out.flags.c_contiguous
         self._check(self.lib.rg_get_cells(self.h, dptr(out)))
         return out
 
@@ -147,8 +148,9 @@ class Handle:
         assert a.size == 4 * self.mesh.n_cells
         self._check(self.lib.rg_set_extensives(self.h, dptr(a)))
 
-    def get_extensives(self):
-        out = np.empty((self.mesh.n_cells, 4))
+    def get_extensives(self, out=None):
+        out = np.empty((self.mesh.n_cells, 4)) if out is None else out
+        assert out.dtype == np.float64 and out.size == 4 * self.mesh.n_cells and out.flags.c_contiguous
         self._check(self.lib.rg_get_extensives(self.h, dptr(out)))
         return out
 

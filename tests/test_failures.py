@@ -173,3 +173,53 @@ def test_gpu_run_reports_first_failing_step():
         with pytest.raises(richgpu.RichError) as ei:
             h.run(5)
         assert ei.value.status == status and ei.value.index == 37
+
+
+def corrupted_meshes():
+    mesh, _, _ = base(8)
+    out = {}
+    fc = mesh.face_cells.copy()
+    fc[5, 1] = mesh.n_cells + mesh.n_ghosts + 3          # neighbour id out of range
+    out["face_out_of_range"] = (fc, None, None)
+    cf = mesh.cell_faces.copy()
+    cf[7] = mesh.n_faces + 10                            # face id out of range
+    out["csr_face_out_of_range"] = (None, cf, None)
+    cf = mesh.cell_faces.copy()
+    cf[3], cf[4] = cf[4], cf[3]                          # not ascending
+    out["csr_not_ascending"] = (None, cf, None)
+    off = mesh.cell_face_offset.copy()
+    off[10] = off[11] + 1                                # offsets not monotone
+    out["offsets_not_monotone"] = (None, None, off)
+    return mesh, out
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(corrupted_meshes()[1]))
+def test_gpu_rejects_invalid_mesh_without_fault(name):
+    """Every index is checked on the device (bounds-checked reads) before any
+    kernel uses it: a corrupted mesh is refused with RG_ERR_INVALID_ARGUMENT
+    and the handle keeps working on its previous mesh."""
+    import richgpu
+    mesh, bad = corrupted_meshes()
+    fc, cf, off = bad[name]
+    fields = {k: getattr(mesh, k) for k in ("point_xy", "cm_xy", "volume", "cd_volume", "ghost_source",
+                                            "ghost_face", "face_cells", "face_vertices",
+                                            "cell_face_offset", "cell_faces")}
+    if fc is not None:
+        fields["face_cells"] = fc
+    if cf is not None:
+        fields["cell_faces"] = cf
+    if off is not None:
+        fields["cell_face_offset"] = off
+    broken = PackedMesh(**fields)
+    good, cells, ext = base(8)
+    with richgpu.Handle(gamma=GAMMA, order=2, ghost_kind=1, device=0) as h:
+        h.upload_mesh(good)
+        h.set_cells(cells)
+        h.set_extensives(ext)
+        h.set_edge_velocities(np.zeros((good.n_faces, 2)))
+        with pytest.raises(richgpu.RichError) as ei:
+            h.upload_mesh(broken)
+        assert ei.value.status == 1
+        h.mesh = good
+        assert h.step() > 0
