@@ -75,7 +75,7 @@ struct SlotLayout {
   size_t points, cms, volume, cd_volume, ghost_source, ghost_face, face_cells, face_vertices, cell_off,
       cell_faces, input_end;
   size_t area, nrm, nabs, par, dm0, dm1, width, minv, cflags, nbr, hr, ghost_real, ghost_unit;
-  size_t nrm32, nabs32, par32, area32, dm0_32, dm1_32, width32, minv32, hr32, gunit32, total;
+  size_t nrm32, nabs32, par32, area32, dm0_32, dm1_32, width32, minv32, hr32, gunit32, icdv32, total;
   void compute(int n, int g, int e, int m, bool mixed) {
     const size_t np = static_cast<size_t>(n) + g;
     size_t o = 0;
@@ -119,6 +119,7 @@ struct SlotLayout {
     minv32 = take(k * 16 * static_cast<size_t>(n));
     hr32 = take(k * 8 * static_cast<size_t>(m));
     gunit32 = take(k * 8 * static_cast<size_t>(g));
+    icdv32 = take(k * 4 * static_cast<size_t>(n));
     total = o;
   }
 };
@@ -277,6 +278,7 @@ void fill_views(MeshSlot& s) {
   s.g32.minv = at<float4>(b, L.minv32);
   s.g32.hr = at<float2>(b, L.hr32);
   s.g32.ghost_unit = at<float2>(b, L.gunit32);
+  s.g32.inv_cd_volume = at<float>(b, L.icdv32);
 }
 
 rg_status reset_status(rg_handle* h, DevStatus* st, cudaStream_t s) {
@@ -337,6 +339,7 @@ rg::MixedArgs mixed_args(rg_handle* h) {
   a.geom = s->geom;
   a.g32 = s->g32;
   a.gamma = static_cast<float>(h->cfg.gamma);
+  a.inv_gm1 = static_cast<float>(1.0 / (h->cfg.gamma - 1.0));
   a.cfl = h->cfg.cfl;
   a.order = h->cfg.order;
   a.ghost_kind = h->cfg.ghost_kind;
@@ -632,6 +635,8 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t /*flags*/
     m32.minv = at<float4>(b, s.lay.minv32);
     m32.hr = at<float2>(b, s.lay.hr32);
     m32.ghost_unit = at<float2>(b, s.lay.gunit32);
+    m32.inv_cd_volume = at<float>(b, s.lay.icdv32);
+    m32.cd_volume = s.mesh.cd_volume;
     RG_CUDA(h, rg::launch_geom32(m32, h->upload_stream));
   }
   RG_CUDA(h, cudaEventRecord(h->ev_up1, h->upload_stream));

@@ -245,13 +245,22 @@ __global__ void __launch_bounds__(kBlock) k_cfl(StepArgs a, int fill_ghosts) {
     const Cell c = load_cell(a.cells, t);
     const double radius = a.geom.width[t];
     const double cs = sqrt(a.gamma * c.p / c.d);
-    double res = 0;
+    // fmax over faces of (cs + sqrt(q_e)) / radius equals (cs + sqrt(max q_e)) /
+    // radius exactly: sqrt, + and / are correctly rounded, hence monotone, so
+    // the maximum commutes with them.  NaN terms are skipped as fmax skips them.
+    double q = 0;
+    bool any = false;
     const int b = m.cell_off[t], e1 = m.cell_off[t + 1];
     for (int k = b; k < e1; ++k) {
       const double2 w = reinterpret_cast<const double2*>(a.ev)[m.cell_faces[k]];
       const double dx = c.vx - w.x, dy = c.vy - w.y;
-      res = fmax(res, (cs + sqrt(dx * dx + dy * dy)) / radius);
+      const double qq = dx * dx + dy * dy;
+      if (!isnan(qq)) {
+        q = fmax(q, qq);
+        any = true;
+      }
     }
+    const double res = any ? fmax(0.0, (cs + sqrt(q)) / radius) : 0.0;
     x = 1.0 / res;
   } else if (fill_ghosts && t < m.n + m.g) {
     fill_ghost(a, t - m.n);
@@ -293,25 +302,78 @@ __device__ __forceinline__ double step_dt(const StepArgs& a) {
   return a.dt_from_device ? a.status->dt : a.dt_host;
 }
 
-// one component of the ordinary limiter, LinearGaussImproved.cpp:232-267
-__device__ __forceinline__ void limit_comp(double dphi, double cv, double cellv, double maxd, double mind,
-                                           bool use_abs, double& psi) {
-  if (fabs(dphi) > 0.05 * smax(fabs(maxd), fabs(mind)) || cv * cellv < 0) {
-    const double thr = use_abs ? fabs(1e-9 * cellv) : 1e-9 * cellv;
-    const double nthr = use_abs ? -fabs(1e-9 * cellv) : -1e-9 * cellv;
-    if (dphi > thr)
-      psi = smin(psi, maxd / dphi);
-    else if (dphi < nthr)
-      psi = smin(psi, mind / dphi);
+// FP32 screening of FP64 quotients.  GB300 issues 64 FP32 operations per FP64
+// one, so a decision that only needs to know on which side of a threshold a
+// correctly rounded FP64 quotient lies is taken from an FP32 estimate when
+// the estimate is clear of the threshold by more than its error, and from the
+// exact FP64 division otherwise.  For |a|,|b| in [2^-120, 2^120] the
+// estimate float(a)/float(b) is within 4 * 2^-24 < 2.5e-7 (relative) of
+// a/b; the margins below are 1e-6, with float(t) itself within 6e-8 of t.
+__device__ __forceinline__ bool fp32_safe(double a) {
+  const double m = fabs(a);
+  return m >= 1e-36 && m <= 1e36;
+}
+
+// psi_f = float(psi) is a usable screen when psi is 0 or a normal float.
+__device__ __forceinline__ bool psi_screenable(double psi, float psi_f) {
+  return psi_f >= 1e-30f || psi == 0.0;
+}
+
+// smin(psi, num/den) for num/den >= 0 (or NaN, which smin ignores), psi >= 0:
+// skips the division when the quotient is provably >= psi.
+__device__ __forceinline__ void min_quotient(double num, double den, double& psi, float& psi_f) {
+  if (fp32_safe(num) && fp32_safe(den) && psi_screenable(psi, psi_f)) {
+    const float qf = static_cast<float>(num) / static_cast<float>(den);
+    if (qf >= psi_f * 1.000001f) return;
+  }
+  const double q = num / den;
+  if (q < psi) {
+    psi = q;
+    psi_f = static_cast<float>(q);
+  }
+}
+
+// one component of the ordinary limiter, LinearGaussImproved.cpp:232-267.
+// thr = 0.05*max(|maxd|,|mind|) (per cell); maxd >= 0 >= mind, so both
+// candidate quotients are >= 0.
+__device__ __forceinline__ void limit_comp(double dphi, double cv, double cellv, double thr, double maxd,
+                                           double mind, bool use_abs, double& psi, float& psi_f) {
+  if (fabs(dphi) > thr || cv * cellv < 0) {
+    const double t1 = use_abs ? fabs(1e-9 * cellv) : 1e-9 * cellv;
+    const double t2 = use_abs ? -fabs(1e-9 * cellv) : -1e-9 * cellv;
+    if (dphi > t1)
+      min_quotient(maxd, dphi, psi, psi_f);
+    else if (dphi < t2)
+      min_quotient(mind, dphi, psi, psi_f);
   }
 }
 
 // one component of the shocked limiter, LinearGaussImproved.cpp:343-366
-// (threshold 1e-9*q without abs for every component, as the reference has it)
-__device__ __forceinline__ void shocked_comp(double dphi, double cv, double cellv, double maxd, double mind,
-                                             double nbv, double theta, double& psi) {
-  if (fabs(dphi) > 0.1 * smax(fabs(maxd), fabs(mind)) || cv * cellv < 0) {
-    if (fabs(dphi) > 1e-9 * cellv) psi = smin(psi, smax(theta * (nbv - cellv) / dphi, 0.0));
+// (threshold 1e-9*q without abs for every component, as the reference has
+// it): psi = smin(psi, smax(theta*(nb-cell)/dphi, 0)).
+__device__ __forceinline__ void shocked_comp(double dphi, double cv, double cellv, double thr, double nbv,
+                                             double theta, double& psi, float& psi_f) {
+  if (fabs(dphi) > thr || cv * cellv < 0) {
+    if (fabs(dphi) > 1e-9 * cellv) {
+      const double num = theta * (nbv - cellv);
+      if (num != 0 && !isnan(num) && !isnan(dphi) && (num < 0) != (dphi < 0)) {
+        // negative quotient: smax(., 0) gives 0
+        if (0.0 < psi) {
+          psi = 0.0;
+          psi_f = 0.0f;
+        }
+        return;
+      }
+      if (num != 0 && fp32_safe(num) && fp32_safe(dphi) && psi_screenable(psi, psi_f)) {
+        const float qf = static_cast<float>(num) / static_cast<float>(dphi);
+        if (qf >= psi_f * 1.000001f) return;
+      }
+      const double x = smax(num / dphi, 0.0);
+      if (x < psi) {
+        psi = x;
+        psi_f = static_cast<float>(x);
+      }
+    }
   }
 }
 
@@ -367,19 +429,44 @@ __global__ void __launch_bounds__(kBlock) k_slopes(StepArgs a) {
     addmult(sy, vx, mi.z);
   }
   if (a.slf) {
-    // :136-157 is_shock / PressureRatio
-    const double cs = sqrt(a.gamma * cell.p / cell.d);
-    bool shock = (sx.vx + sy.vy) * a.geom.width[i] < (-a.delta_v) * cs;
-    if (!shock) {
-      double pr = 1;
-      for (int k = 0; k < nn; ++k) {
-        const double np_ = a.cells[4 * static_cast<int>(a.geom.nbr[b + k] & kNbrIdMask) + 1];
-        if (cell.p > np_)
-          pr = smin(pr, np_ / cell.p);
-        else
-          pr = smin(pr, cell.p / np_);
+    // :136-157 is_shock / PressureRatio.  cond1 is
+    // (div v)*width < -delta_v*cs: false whenever the left side is >= 0,
+    // otherwise screened in FP32 against |left| vs delta_v*cs.
+    const double lhs = (sx.vx + sy.vy) * a.geom.width[i];
+    bool shock = false;
+    if (lhs < 0) {
+      const double gp = a.gamma * cell.p;
+      bool decided = false;
+      if (fp32_safe(lhs) && fp32_safe(gp) && fp32_safe(cell.d)) {
+        const float rhs_f = static_cast<float>(a.delta_v) * sqrtf(static_cast<float>(gp) / static_cast<float>(cell.d));
+        const float l_f = -static_cast<float>(lhs);
+        if (l_f > rhs_f * 1.000002f) {
+          shock = true;
+          decided = true;
+        } else if (l_f < rhs_f * 0.999998f) {
+          decided = true;
+        }
       }
-      shock = pr < a.delta_p;
+      if (!decided) shock = lhs < (-a.delta_v) * sqrt(gp / cell.d);
+    }
+    if (!shock && nn == 0) shock = 1.0 < a.delta_p;  // PressureRatio of no neighbours is 1
+    if (!shock) {
+      // PressureRatio < delta_p  <=>  some neighbour's ratio < delta_p
+      const float dp_f = static_cast<float>(a.delta_p);
+      for (int k = 0; k < nn && !shock; ++k) {
+        const double np_ = a.cells[4 * static_cast<int>(a.geom.nbr[b + k] & kNbrIdMask) + 1];
+        const double num = cell.p > np_ ? np_ : cell.p;
+        const double den = cell.p > np_ ? cell.p : np_;
+        if (fp32_safe(num) && fp32_safe(den)) {
+          const float rf = static_cast<float>(num) / static_cast<float>(den);
+          if (rf < dp_f * 0.999999f) {
+            shock = true;
+            break;
+          }
+          if (rf > dp_f * 1.000001f) continue;
+        }
+        shock = num / den < a.delta_p;
+      }
     }
     Cell cmax = cell, cmin = cell;
     for (int k = 0; k < nn; ++k) {
@@ -397,7 +484,11 @@ __global__ void __launch_bounds__(kBlock) k_slopes(StepArgs a) {
     }
     const Cell maxd{cmax.d - cell.d, cmax.p - cell.p, cmax.vx - cell.vx, cmax.vy - cell.vy};
     const Cell mind{cmin.d - cell.d, cmin.p - cell.p, cmin.vx - cell.vx, cmin.vy - cell.vy};
+    const double f = shock ? 0.1 : 0.05;
+    const Cell thr{f * smax(fabs(maxd.d), fabs(mind.d)), f * smax(fabs(maxd.p), fabs(mind.p)),
+                   f * smax(fabs(maxd.vx), fabs(mind.vx)), f * smax(fabs(maxd.vy), fabs(mind.vy))};
     double psi0 = 1, psi1 = 1, psi2 = 1, psi3 = 1;
+    float pf0 = 1, pf1 = 1, pf2 = 1, pf3 = 1;
     for (int k = 0; k < nn; ++k) {
       const uint32_t w = a.geom.nbr[b + k];
       const int e = m.cell_faces[b + k];
@@ -408,17 +499,17 @@ __global__ void __launch_bounds__(kBlock) k_slopes(StepArgs a) {
       const Cell dphi{cv.d - cell.d, cv.p - cell.p, cv.vx - cell.vx, cv.vy - cell.vy};
       if (!shock) {
         // :174-300 slope_limit
-        limit_comp(dphi.d, cv.d, cell.d, maxd.d, mind.d, false, psi0);
-        limit_comp(dphi.p, cv.p, cell.p, maxd.p, mind.p, false, psi1);
-        limit_comp(dphi.vx, cv.vx, cell.vx, maxd.vx, mind.vx, true, psi2);
-        limit_comp(dphi.vy, cv.vy, cell.vy, maxd.vy, mind.vy, true, psi3);
+        limit_comp(dphi.d, cv.d, cell.d, thr.d, maxd.d, mind.d, false, psi0, pf0);
+        limit_comp(dphi.p, cv.p, cell.p, thr.p, maxd.p, mind.p, false, psi1, pf1);
+        limit_comp(dphi.vx, cv.vx, cell.vx, thr.vx, maxd.vx, mind.vx, true, psi2, pf2);
+        limit_comp(dphi.vy, cv.vy, cell.vy, thr.vy, maxd.vy, mind.vy, true, psi3, pf3);
       } else {
         // :302-399 shocked_slope_limit
         const Cell nb = load_cell(a.cells, static_cast<int>(w & kNbrIdMask));
-        shocked_comp(dphi.d, cv.d, cell.d, maxd.d, mind.d, nb.d, a.theta, psi0);
-        shocked_comp(dphi.p, cv.p, cell.p, maxd.p, mind.p, nb.p, a.theta, psi1);
-        shocked_comp(dphi.vx, cv.vx, cell.vx, maxd.vx, mind.vx, nb.vx, a.theta, psi2);
-        shocked_comp(dphi.vy, cv.vy, cell.vy, maxd.vy, mind.vy, nb.vy, a.theta, psi3);
+        shocked_comp(dphi.d, cv.d, cell.d, thr.d, nb.d, a.theta, psi0, pf0);
+        shocked_comp(dphi.p, cv.p, cell.p, thr.p, nb.p, a.theta, psi1, pf1);
+        shocked_comp(dphi.vx, cv.vx, cell.vx, thr.vx, nb.vx, a.theta, psi2, pf2);
+        shocked_comp(dphi.vy, cv.vy, cell.vy, thr.vy, nb.vy, a.theta, psi3, pf3);
       }
     }
     sx.d *= psi0; sy.d *= psi0;
@@ -454,11 +545,14 @@ __device__ __forceinline__ bool hllc(Prim l, Prim r, double velocity, Cons& f, c
     record_error(a.status, a.step, RG_ERR_HLLC_NAN, 3, face, r.vx);
     return false;
   }
-  const double bx = 1 * velocity, by = 0 * velocity;
-  l.vx -= bx;
-  l.vy -= by;
-  r.vx -= bx;
-  r.vy -= by;
+  // local.Velocity -= velocity*(1,0): the y part subtracts a zero, which can
+  // only change the sign of a zero result, and is left out; so is the whole
+  // boost for a face at rest (velocity +-0)
+  const bool moving = velocity != 0.0;
+  if (moving) {
+    l.vx -= velocity;
+    r.vx -= velocity;
+  }
   // :27-43 estimate_wave_speeds
   const double sl = smin(l.vx - l.c, r.vx - r.c);
   const double sr = smax(l.vx + l.c, r.vx + r.c);
@@ -474,9 +568,10 @@ __device__ __forceinline__ bool hllc(Prim l, Prim r, double velocity, Cons& f, c
   const double sk = use_left ? sl : sr;
   const double e_k = ted(q);
   // :281-290 Primitive2Flux along (1,0)
-  const double sp = q.vx * 1 + q.vy * 0;
-  const double dsp = q.d * sp;
-  Cons fk{q.d * sp, 1 * q.p + q.vx * dsp, 0 * q.p + q.vy * dsp, (e_k + q.p) * sp};
+  // Primitive2Flux along n = (1,0): v.n = vx (the vy*0 term only changes the
+  // sign of a zero), momentum (p + vx*d*vx, vy*d*vx)
+  const double dsp = q.d * q.vx;
+  Cons fk{dsp, q.p + q.vx * dsp, q.vy * dsp, (e_k + q.p) * q.vx};
   const bool star = use_left ? !(sl > 0) : !(sr < 0);
   if (star) {
     // :76-92 starred_state, and fk + sk*(us - u) with u = Primitive2Conserved (:267-272)
@@ -489,10 +584,10 @@ __device__ __forceinline__ bool hllc(Prim l, Prim r, double velocity, Cons& f, c
     fk.en = fk.en + sk * (use - e_k);
   }
   // :150-152 back to the lab frame along the normal
-  fk.en += (fk.mx * (1 * velocity) + fk.my * (0 * velocity)) + 0.5 * fk.m * velocity * velocity;
-  const double vm = velocity * fk.m;
-  fk.mx += 1 * vm;
-  fk.my += 0 * vm;
+  if (moving) {
+    fk.en += fk.mx * velocity + 0.5 * fk.m * velocity * velocity;
+    fk.mx += velocity * fk.m;
+  }
   f = fk;
   return true;
 }
@@ -561,7 +656,8 @@ __global__ void __launch_bounds__(kBlock) k_faces_lgi(StepArgs a) {
   const double2 w = reinterpret_cast<const double2*>(a.ev)[e];
   const double2 n = a.geom.nrm[e], p = a.geom.par[e];
   const double na = a.geom.nabs[e], pa = a.geom.area[e];
-  const double speed = (n.x * w.x + n.y * w.y) / na;
+  // a face at rest has speed +-0 (the sign only reaches signs of zeros)
+  const double speed = (w.x == 0.0 && w.y == 0.0) ? 0.0 : (n.x * w.x + n.y * w.y) / na;
   Cons c;
   if (!solve_face(to_prim(a.gamma, side[0]), to_prim(a.gamma, side[1]), speed, n, na, p, pa, c, a, e)) return;
   write_flux(a, e, c, kScaled, pa);
@@ -603,7 +699,7 @@ __global__ void __launch_bounds__(kBlock) k_faces_pcm(StepArgs a) {
     r = to_prim(a.gamma, load_cell(a.cells, fc.y));
   }
   const double2 w = reinterpret_cast<const double2*>(a.ev)[e];
-  const double velocity = (n.x * w.x + n.y * w.y) / na;
+  const double velocity = (w.x == 0.0 && w.y == 0.0) ? 0.0 : (n.x * w.x + n.y * w.y) / na;
   Cons c;
   if (!solve_face(l, r, velocity, n, na, p, pa, c, a, e)) return;
   write_flux(a, e, c, kScaled, pa);

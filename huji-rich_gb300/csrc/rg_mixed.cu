@@ -54,6 +54,7 @@ __global__ void __launch_bounds__(kBlock) k_geom32(MixedGeomArgs a) {
   }
   for (int i = t; i < a.n; i += stride) {
     a.width[i] = static_cast<float>(g.width[i]);
+    a.inv_cd_volume[i] = static_cast<float>(1.0 / a.cd_volume[i]);
     const dbl4 m = g.minv[i];
     a.minv[i] = make_float4(static_cast<float>(m.x), static_cast<float>(m.y), static_cast<float>(m.z),
                             static_cast<float>(m.w));
@@ -181,16 +182,16 @@ __device__ __forceinline__ void limit32(float dphi, float cv, float cellv, float
     const float t = use_abs ? fabsf(1e-9f * cellv) : 1e-9f * cellv;
     const float nt = use_abs ? -fabsf(1e-9f * cellv) : -1e-9f * cellv;
     if (dphi > t)
-      psi = fminf(psi, maxd / dphi);
+      psi = fminf(psi, __fdividef(maxd, dphi));
     else if (dphi < nt)
-      psi = fminf(psi, mind / dphi);
+      psi = fminf(psi, __fdividef(mind, dphi));
   }
 }
 
 __device__ __forceinline__ void shocked32(float dphi, float cv, float cellv, float thr, float nbv, float theta,
                                           float& psi) {
   if (fabsf(dphi) > thr || cv * cellv < 0.0f) {
-    if (fabsf(dphi) > 1e-9f * cellv) psi = fminf(psi, fmaxf(theta * (nbv - cellv) / dphi, 0.0f));
+    if (fabsf(dphi) > 1e-9f * cellv) psi = fminf(psi, fmaxf(__fdividef(theta * (nbv - cellv), dphi), 0.0f));
   }
 }
 
@@ -235,10 +236,10 @@ __global__ void __launch_bounds__(kBlock) k_slopes32(MixedArgs a) {
     const float cs = sqrtf(a.gamma * cell.p / cell.d);
     bool shock = (sx.vx + sy.vy) * a.g32.width[i] < (-a.delta_v) * cs;
     if (!shock) {
+      // min(p, p_k) / max(p, p_k) < delta_p without the division
       for (int k = 0; k < nn && !shock; ++k) {
         const float np_ = a.cells32[static_cast<int>(a.geom.nbr[b + k] & kNbrIdMask)].y;
-        const float r = cell.p > np_ ? np_ / cell.p : cell.p / np_;
-        shock = r < a.delta_p;
+        shock = fminf(cell.p, np_) < a.delta_p * fmaxf(cell.p, np_);
       }
     }
     C4 cmax = cell, cmin = cell;
@@ -291,9 +292,9 @@ __global__ void __launch_bounds__(kBlock) k_slopes32(MixedArgs a) {
   a.slopes32[2 * i + 1] = make_float4(sy.d, sy.p, sy.vx, sy.vy);
 }
 
-__device__ __forceinline__ P6 prim32(float g, const C4& c) {
-  const float pd = c.p / c.d;
-  return P6{c.d, c.p, c.vx, c.vy, pd / (g - 1.0f), sqrtf(g * pd)};
+__device__ __forceinline__ P6 prim32(float g, float inv_gm1, const C4& c) {
+  const float pd = __fdividef(c.p, c.d);
+  return P6{c.d, c.p, c.vx, c.vy, pd * inv_gm1, sqrtf(g * pd)};
 }
 
 // Hllc (hllc.cpp:97-154, massflux) in FP32 in the face frame.
@@ -306,8 +307,8 @@ __device__ __forceinline__ bool hllc32(P6 l, P6 r, float vel, F4& f, const Mixed
   r.vx -= vel;
   const float sl = fminf(l.vx - l.c, r.vx - r.c);
   const float sr = fmaxf(l.vx + l.c, r.vx + r.c);
-  const float ss = (r.p - l.p + l.d * l.vx * (sl - l.vx) - r.d * r.vx * (sr - r.vx)) /
-                   (l.d * (sl - l.vx) - r.d * (sr - r.vx));
+  const float ss = __fdividef(r.p - l.p + l.d * l.vx * (sl - l.vx) - r.d * r.vx * (sr - r.vx),
+                              l.d * (sl - l.vx) - r.d * (sr - r.vx));
   const bool use_left = sl > 0.0f || (sl <= 0.0f && ss >= 0.0f);
   const bool use_right = !use_left && ((ss < 0.0f && sr >= 0.0f) || sr < 0.0f);
   if (!use_left && !use_right) {
@@ -321,8 +322,9 @@ __device__ __forceinline__ bool hllc32(P6 l, P6 r, float vel, F4& f, const Mixed
   F4 fk{dsp, q.p + q.vx * dsp, q.vy * dsp, (ek + q.p) * q.vx};
   if (use_left ? !(sl > 0.0f) : !(sr < 0.0f)) {
     const float skv = sk - q.vx;
-    const float ds = q.d * skv / (sk - ss);
-    const float use = ds * (ek / q.d + (ss - q.vx) * (ss + q.p / (q.d * skv)));
+    const float ds = __fdividef(q.d * skv, sk - ss);
+    const float id = __fdividef(1.0f, q.d);
+    const float use = ds * (ek * id + (ss - q.vx) * (ss + __fdividef(q.p * id, skv)));
     fk.m += sk * (ds - q.d);
     fk.mx += (ds * ss - dsp) * sk;
     fk.my += (ds * q.vy - q.vy * q.d) * sk;
@@ -336,7 +338,7 @@ __device__ __forceinline__ bool hllc32(P6 l, P6 r, float vel, F4& f, const Mixed
 
 __device__ __forceinline__ bool solve32(P6 l, P6 r, float vel, float2 n, float na, float2 p, float pa, F4& out,
                                         const MixedArgs& a, int face) {
-  const float in = 1.0f / na, ip = 1.0f / pa;
+  const float in = __fdividef(1.0f, na), ip = __fdividef(1.0f, pa);
   const float lx = (l.vx * n.x + l.vy * n.y) * in, ly = (l.vx * p.x + l.vy * p.y) * ip;
   const float rx = (r.vx * n.x + r.vy * n.y) * in, ry = (r.vx * p.x + r.vy * p.y) * ip;
   l.vx = lx;
@@ -391,7 +393,8 @@ __global__ void __launch_bounds__(kBlock) k_faces32_lgi(MixedArgs a) {
   const float na = a.g32.nabs[e], pa = a.g32.area[e];
   const float vel = (n.x * w.x + n.y * w.y) / na;
   F4 c;
-  if (!solve32(prim32(a.gamma, side[0]), prim32(a.gamma, side[1]), vel, n, na, p, pa, c, a, e)) return;
+  if (!solve32(prim32(a.gamma, a.inv_gm1, side[0]), prim32(a.gamma, a.inv_gm1, side[1]), vel, n, na, p, pa, c, a, e))
+    return;
   write32(a, e, c, kScaled, pa);
 }
 
@@ -414,14 +417,14 @@ __global__ void __launch_bounds__(kBlock) k_faces32_pcm(MixedArgs a) {
   };
   P6 l, r;
   if (!va) {
-    r = prim32(a.gamma, ld4(a.cells32, fc.y));
-    l = oa == ob ? reflect(r) : prim32(a.gamma, ld4(a.cells32, oa));
+    r = prim32(a.gamma, a.inv_gm1, ld4(a.cells32, fc.y));
+    l = oa == ob ? reflect(r) : prim32(a.gamma, a.inv_gm1, ld4(a.cells32, oa));
   } else if (!vb) {
-    l = prim32(a.gamma, ld4(a.cells32, fc.x));
-    r = oa == ob ? reflect(l) : prim32(a.gamma, ld4(a.cells32, ob));
+    l = prim32(a.gamma, a.inv_gm1, ld4(a.cells32, fc.x));
+    r = oa == ob ? reflect(l) : prim32(a.gamma, a.inv_gm1, ld4(a.cells32, ob));
   } else {
-    l = prim32(a.gamma, ld4(a.cells32, fc.x));
-    r = prim32(a.gamma, ld4(a.cells32, fc.y));
+    l = prim32(a.gamma, a.inv_gm1, ld4(a.cells32, fc.x));
+    r = prim32(a.gamma, a.inv_gm1, ld4(a.cells32, fc.y));
   }
   const float2 w = a.ev32[e];
   const float vel = (n.x * w.x + n.y * w.y) / na;
@@ -438,8 +441,22 @@ __global__ void __launch_bounds__(kBlock) k_faces32_pcm(MixedArgs a) {
   write32(a, e, c, kScaled, pa);
 }
 
-// Gather in FP64 (ascending faces, SimpleExtensiveUpdater order) and the
-// cell update (simple_cell_updater.cpp:22-59) with e = E/m - v^2/2 in FP64.
+// Error-free FP32 addition (Knuth's TwoSum): s + x == s' + err exactly.
+__device__ __forceinline__ void two_sum(float& s, float& c, float x) {
+  const float t = s + x;
+  const float bb = t - s;
+  const float err = (s - (t - bb)) + (x - bb);
+  s = t;
+  c += err;
+}
+
+// Gather and cell update (simple_extensive_updater.cpp:11-35,
+// simple_cell_updater.cpp:22-59).  The FP32 face contributions of a cell are
+// summed in float-float (TwoSum; ~48-bit, on the FP32 pipe, in ascending face
+// order) and added to the FP64 extensives once per component, so a face's
+// contribution enters its two cells with opposite signs and the extensives
+// keep FP64 precision across steps.  e = E/m - v^2/2 is formed in FP64 with a
+// Newton-refined reciprocal of m.
 __global__ void __launch_bounds__(kBlock) k_update_mixed(MixedArgs a, int from_unscaled, int do_ext, int do_cells) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const MeshDev& m = a.mesh;
@@ -448,44 +465,46 @@ __global__ void __launch_bounds__(kBlock) k_update_mixed(MixedArgs a, int from_u
   const double2 e01 = ext2[2 * i], e23 = ext2[2 * i + 1];
   double mass = e01.x, en = e01.y, px = e23.x, py = e23.y;
   if (do_ext) {
+    float s0 = 0, s1 = 0, s2 = 0, s3 = 0, c0 = 0, c1 = 0, c2 = 0, c3 = 0;
     const int b = m.cell_off[i], e1 = m.cell_off[i + 1];
     for (int k = b; k < e1; ++k) {
       const int e = m.cell_faces[k];
       float4 f = a.flux32[e];
       if (from_unscaled) {
-        const float s = a.dt32 * a.g32.area[e];
-        f = make_float4(f.x * s, f.y * s, f.z * s, f.w * s);
+        const float sc = a.dt32 * a.g32.area[e];
+        f = make_float4(f.x * sc, f.y * sc, f.z * sc, f.w * sc);
       }
-      if (a.geom.nbr[k] & kNbrFirst) {
-        mass -= static_cast<double>(f.x);
-        en -= static_cast<double>(f.y);
-        px -= static_cast<double>(f.z);
-        py -= static_cast<double>(f.w);
-      } else {
-        mass += static_cast<double>(f.x);
-        en += static_cast<double>(f.y);
-        px += static_cast<double>(f.z);
-        py += static_cast<double>(f.w);
-      }
+      if (a.geom.nbr[k] & kNbrFirst) f = make_float4(-f.x, -f.y, -f.z, -f.w);
+      two_sum(s0, c0, f.x);
+      two_sum(s1, c1, f.y);
+      two_sum(s2, c2, f.z);
+      two_sum(s3, c3, f.w);
     }
+    mass += static_cast<double>(s0) + static_cast<double>(c0);
+    en += static_cast<double>(s1) + static_cast<double>(c1);
+    px += static_cast<double>(s2) + static_cast<double>(c2);
+    py += static_cast<double>(s3) + static_cast<double>(c3);
     ext2[2 * i] = make_double2(mass, en);
     ext2[2 * i + 1] = make_double2(px, py);
   }
   if (do_cells) {
-    const float d = static_cast<float>(mass) / static_cast<float>(m.cd_volume[i]);
+    const float mf = static_cast<float>(mass);
+    const float d = mf * a.g32.inv_cd_volume[i];
     if (d < 0.0f) {
       record_error(a.status, a.step, RG_ERR_NEGATIVE_DENSITY, 5, i, d);
       return;
     }
-    const double im = 1.0 / mass;
-    const double vx = px * im, vy = py * im;
-    const double energy = en * im - 0.5 * (vx * vx + vy * vy);
+    double r = static_cast<double>(1.0f / mf);
+    r = r * (2.0 - mass * r);
+    r = r * (2.0 - mass * r);
+    const double kin = 0.5 * (px * px + py * py) * r;
+    const double energy = (en - kin) * r;
     if (energy < 0) {
       record_error(a.status, a.step, RG_ERR_NEGATIVE_ENERGY, 5, i, energy);
       return;
     }
-    a.cells32[i] = make_float4(d, (a.gamma - 1.0f) * static_cast<float>(energy) * d, static_cast<float>(vx),
-                               static_cast<float>(vy));
+    a.cells32[i] = make_float4(d, (a.gamma - 1.0f) * static_cast<float>(energy) * d,
+                               static_cast<float>(px * r), static_cast<float>(py * r));
   }
 }
 

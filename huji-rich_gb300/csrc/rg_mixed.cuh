@@ -18,11 +18,13 @@ struct MixedGeom {
   const float4* minv;
   const float2* hr;
   const float2* ghost_unit;
+  const float* inv_cd_volume;
 };
 
 struct MixedGeomArgs {
   int n, g, e, m;
   GeomDev g64;  // source (FP64 geometry of the same slot)
+  const double* cd_volume;
   float2* nrm;
   float* nabs;
   float2* par;
@@ -33,6 +35,7 @@ struct MixedGeomArgs {
   float4* minv;
   float2* hr;
   float2* ghost_unit;
+  float* inv_cd_volume;
 };
 
 struct MixedArgs {
@@ -40,6 +43,7 @@ struct MixedArgs {
   GeomDev geom;   // FP64 geometry: neighbour words, cell flags, ghost sources
   MixedGeom g32;
   float gamma;
+  float inv_gm1;  // 1/(gamma-1)
   double cfl;
   int order, ghost_kind, slf;
   float delta_v, theta, delta_p;
