@@ -156,6 +156,9 @@ struct rg_handle {
   // FP32-mixed path: FP32 primitives (n + g records), slopes, face fluxes, edge velocities
   DevBuf cells32, slopes32, flux32, ev32;
   bool mixed = false;
+  // Heun mid stage: extensives and cells after the first flux pass
+  DevBuf mid_ext, mid_cells, mid_cells32;
+  bool heun = false;
   size_t cells_records = 0;
   bool have_cells = false, have_ext = false, have_ev = false, have_fluxes = false;
   HostBuf staging, host_status, host_dts;
@@ -378,9 +381,83 @@ rg_status mesh_error(rg_handle* h) {
   return RG_OK;
 }
 
+// hdsim::TimeAdvance2Heun on a fixed mesh (hdsim2d.cpp:323-449): dt once;
+// pass 1 on the cells writes the mid extensives and mid cells; pass 2 on the
+// mid cells continues the mid extensives, averages them with the old ones
+// (average_extensive, hdsim2d.cpp:311-320) and updates the cells.
+rg_status enqueue_heun(rg_handle* h, int step, cudaEvent_t* ev) {
+  const bool o2 = h->cfg.order == 2;
+  if (h->mixed) {
+    rg::MixedArgs a = mixed_args(h);
+    a.dt32_from_device = 1;
+    a.step = step;
+    float4* mid_c = static_cast<float4*>(h->mid_cells32.p);
+    double* mid_e = static_cast<double*>(h->mid_ext.p);
+    if (ev) RG_CUDA(h, cudaEventRecord(ev[0], h->stream));
+    RG_CUDA(h, rg::launch_cfl32(a, h->stream, o2));
+    if (ev) RG_CUDA(h, cudaEventRecord(ev[1], h->stream));
+    if (o2) RG_CUDA(h, rg::launch_slopes32(a, h->stream));
+    RG_CUDA(h, rg::launch_faces32(a, h->stream, true));
+    rg::MixedArgs a1 = a;
+    a1.ext_out = mid_e;
+    a1.cells32_out = mid_c;
+    RG_CUDA(h, rg::launch_update_mixed(a1, h->stream, false, true, true));
+    if (ev) RG_CUDA(h, cudaEventRecord(ev[2], h->stream));
+    rg::MixedArgs a2 = a;
+    a2.cells32 = mid_c;
+    if (o2) {
+      RG_CUDA(h, rg::launch_ghost_fill32(a2, h->stream));
+      RG_CUDA(h, rg::launch_slopes32(a2, h->stream));
+    }
+    RG_CUDA(h, rg::launch_faces32(a2, h->stream, true));
+    if (ev) RG_CUDA(h, cudaEventRecord(ev[3], h->stream));
+    rg::MixedArgs a3 = a2;
+    a3.ext = mid_e;
+    a3.ext_out = static_cast<double*>(h->ext.p);
+    a3.ext_avg = static_cast<const double*>(h->ext.p);
+    a3.cells32_out = static_cast<float4*>(h->cells32.p);
+    RG_CUDA(h, rg::launch_update_mixed(a3, h->stream, false, true, true));
+    if (ev) RG_CUDA(h, cudaEventRecord(ev[4], h->stream));
+  } else {
+    rg::StepArgs a = step_args(h);
+    a.dt_from_device = 1;
+    a.step = step;
+    double* mid_c = static_cast<double*>(h->mid_cells.p);
+    double* mid_e = static_cast<double*>(h->mid_ext.p);
+    if (ev) RG_CUDA(h, cudaEventRecord(ev[0], h->stream));
+    RG_CUDA(h, rg::launch_cfl(a, h->stream, o2));
+    if (ev) RG_CUDA(h, cudaEventRecord(ev[1], h->stream));
+    if (o2) RG_CUDA(h, rg::launch_slopes(a, h->stream));
+    RG_CUDA(h, rg::launch_faces(a, h->stream, true));
+    rg::StepArgs a1 = a;
+    a1.ext_out = mid_e;
+    a1.cells_out = mid_c;
+    RG_CUDA(h, rg::launch_update(a1, h->stream, false, true, true));
+    if (ev) RG_CUDA(h, cudaEventRecord(ev[2], h->stream));
+    rg::StepArgs a2 = a;
+    a2.cells = mid_c;
+    if (o2) {
+      RG_CUDA(h, rg::launch_ghost_fill(a2, h->stream));
+      RG_CUDA(h, rg::launch_slopes(a2, h->stream));
+    }
+    RG_CUDA(h, rg::launch_faces(a2, h->stream, true));
+    if (ev) RG_CUDA(h, cudaEventRecord(ev[3], h->stream));
+    rg::StepArgs a3 = a2;
+    a3.ext = mid_e;
+    a3.ext_out = static_cast<double*>(h->ext.p);
+    a3.ext_avg = static_cast<const double*>(h->ext.p);
+    a3.cells_out = static_cast<double*>(h->cells.p);
+    RG_CUDA(h, rg::launch_update(a3, h->stream, false, true, true));
+    if (ev) RG_CUDA(h, cudaEventRecord(ev[4], h->stream));
+  }
+  h->have_fluxes = false;
+  return RG_OK;
+}
+
 // Enqueues one fused step (no host synchronisation).  With ev != nullptr,
 // records ev[0..4] around its kernels.
 rg_status enqueue_step(rg_handle* h, int step, cudaEvent_t* ev = nullptr) {
+  if (h->heun) return enqueue_heun(h, step, ev);
   if (h->mixed) {
     rg::MixedArgs a = mixed_args(h);
     a.dt32_from_device = 1;
@@ -456,6 +533,8 @@ rg_status rg_create(const rg_config* cfg, rg_handle** out) {
   if (cfg->ghost_kind != RG_GHOST_RIGID_WALL && cfg->ghost_kind != RG_GHOST_PERIODIC)
     return RG_ERR_INVALID_ARGUMENT;
   if (cfg->precision != RG_FP64 && cfg->precision != RG_FP32_MIXED) return RG_ERR_INVALID_ARGUMENT;
+  if (cfg->time_integrator != RG_TIME_ADVANCE && cfg->time_integrator != RG_TIME_ADVANCE_HEUN)
+    return RG_ERR_INVALID_ARGUMENT;
   if (!(cfg->gamma > 1.0) || !(cfg->cfl > 0.0)) return RG_ERR_INVALID_ARGUMENT;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= cfg->device || cfg->device < 0) {
@@ -466,6 +545,7 @@ rg_status rg_create(const rg_config* cfg, rg_handle** out) {
   if (!h) return RG_ERR_OUT_OF_MEMORY;
   h->cfg = *cfg;
   h->mixed = cfg->precision == RG_FP32_MIXED;
+  h->heun = cfg->time_integrator == RG_TIME_ADVANCE_HEUN;
   auto fail = [&](cudaError_t e) {
     rg_destroy(h);
     cudaGetLastError();
@@ -507,6 +587,9 @@ rg_status rg_destroy(rg_handle* h) {
   h->ev.release();
   h->slopes.release();
   h->fluxes.release();
+  h->mid_ext.release();
+  h->mid_cells.release();
+  h->mid_cells32.release();
   h->cells32.release();
   h->slopes32.release();
   h->flux32.release();
@@ -672,6 +755,13 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t /*flags*/
   RG_CUDA(h, h->ev.ensure(16 * static_cast<size_t>(std::max(e, 1))));
   RG_CUDA(h, h->slopes.ensure(64 * static_cast<size_t>(n)));
   RG_CUDA(h, h->fluxes.ensure(32 * static_cast<size_t>(std::max(e, 1))));
+  if (h->heun) {
+    RG_CUDA(h, h->mid_ext.ensure(32 * static_cast<size_t>(n)));
+    if (h->mixed)
+      RG_CUDA(h, h->mid_cells32.ensure(16 * np));
+    else
+      RG_CUDA(h, h->mid_cells.ensure(32 * np));
+  }
   if (h->mixed) {
     RG_CUDA(h, h->slopes32.ensure(32 * static_cast<size_t>(n)));
     RG_CUDA(h, h->flux32.ensure(16 * static_cast<size_t>(std::max(e, 1))));

@@ -745,8 +745,18 @@ __global__ void __launch_bounds__(kBlock) k_update(StepArgs a, int from_unscaled
         py += dy;
       }
     }
-    ext2[2 * i] = make_double2(mass, en);
-    ext2[2 * i + 1] = make_double2(px, py);
+    if (a.ext_avg) {
+      // hdsim2d.cpp:311-320 average_extensive: 0.5*(mid + old)
+      const double2* o = reinterpret_cast<const double2*>(a.ext_avg);
+      const double2 o01 = o[2 * i], o23 = o[2 * i + 1];
+      mass = 0.5 * (mass + o01.x);
+      en = 0.5 * (en + o01.y);
+      px = 0.5 * (px + o23.x);
+      py = 0.5 * (py + o23.y);
+    }
+    double2* out2 = reinterpret_cast<double2*>(a.ext_out ? a.ext_out : a.ext);
+    out2[2 * i] = make_double2(mass, en);
+    out2[2 * i + 1] = make_double2(px, py);
   }
   if (do_cells) {
     const double d = mass / m.cd_volume[i];
@@ -760,7 +770,7 @@ __global__ void __launch_bounds__(kBlock) k_update(StepArgs a, int from_unscaled
       record_error(a.status, a.step, RG_ERR_NEGATIVE_ENERGY, 5, i, energy);
       return;
     }
-    store4(a.cells, i, d, (a.gamma - 1) * energy * d, vx, vy);
+    store4(a.cells_out ? a.cells_out : a.cells, i, d, (a.gamma - 1) * energy * d, vx, vy);
   }
 }
 

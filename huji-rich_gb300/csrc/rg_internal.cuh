@@ -140,8 +140,11 @@ struct StepArgs {
   double gamma, cfl;
   int order, ghost_kind, slf;
   double delta_v, theta, delta_p;
-  double* cells;        // 4*np (ghost entries at the end)
-  double* ext;          // 4*n
+  double* cells;        // 4*np (ghost entries at the end), read by every pass
+  double* ext;          // 4*n, read by the update
+  double* ext_out;      // where the update writes extensives (nullptr: ext)
+  double* cells_out;    // where the update writes cells (nullptr: cells)
+  const double* ext_avg;  // Heun: extensives = 0.5*(gathered + ext_avg) before the cell update
   const double* ev;     // 2*e edge velocities
   double* slopes;       // 8*n
   double* fluxes;       // 4*e (unscaled or dt*area scaled)

@@ -484,8 +484,17 @@ __global__ void __launch_bounds__(kBlock) k_update_mixed(MixedArgs a, int from_u
     en += static_cast<double>(s1) + static_cast<double>(c1);
     px += static_cast<double>(s2) + static_cast<double>(c2);
     py += static_cast<double>(s3) + static_cast<double>(c3);
-    ext2[2 * i] = make_double2(mass, en);
-    ext2[2 * i + 1] = make_double2(px, py);
+    if (a.ext_avg) {
+      const double2* o = reinterpret_cast<const double2*>(a.ext_avg);
+      const double2 o01 = o[2 * i], o23 = o[2 * i + 1];
+      mass = 0.5 * (mass + o01.x);
+      en = 0.5 * (en + o01.y);
+      px = 0.5 * (px + o23.x);
+      py = 0.5 * (py + o23.y);
+    }
+    double2* out2 = reinterpret_cast<double2*>(a.ext_out ? a.ext_out : a.ext);
+    out2[2 * i] = make_double2(mass, en);
+    out2[2 * i + 1] = make_double2(px, py);
   }
   if (do_cells) {
     const float mf = static_cast<float>(mass);
@@ -503,8 +512,9 @@ __global__ void __launch_bounds__(kBlock) k_update_mixed(MixedArgs a, int from_u
       record_error(a.status, a.step, RG_ERR_NEGATIVE_ENERGY, 5, i, energy);
       return;
     }
-    a.cells32[i] = make_float4(d, (a.gamma - 1.0f) * static_cast<float>(energy) * d,
-                               static_cast<float>(px * r), static_cast<float>(py * r));
+    (a.cells32_out ? a.cells32_out : a.cells32)[i] =
+        make_float4(d, (a.gamma - 1.0f) * static_cast<float>(energy) * d, static_cast<float>(px * r),
+                    static_cast<float>(py * r));
   }
 }
 

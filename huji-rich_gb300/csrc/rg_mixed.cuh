@@ -47,7 +47,10 @@ struct MixedArgs {
   double cfl;
   int order, ghost_kind, slf;
   float delta_v, theta, delta_p;
-  float4* cells32;   // n + g records (ghost states at the end)
+  float4* cells32;   // n + g records (ghost states at the end), read by every pass
+  float4* cells32_out;    // where the update writes cells (nullptr: cells32)
+  double* ext_out;        // where the update writes extensives (nullptr: ext)
+  const double* ext_avg;  // Heun: extensives = 0.5*(gathered + ext_avg)
   float4* slopes32;  // 2 per cell
   float4* flux32;    // per face, unscaled or dt*area scaled
   const float2* ev32;

@@ -28,7 +28,7 @@ class RgConfig(C.Structure):
     _fields_ = [("gamma", C.c_double), ("cfl", C.c_double), ("order", C.c_int32),
                 ("ghost_kind", C.c_int32), ("slope_limiter", C.c_int32), ("precision", C.c_int32),
                 ("delta_v", C.c_double), ("theta", C.c_double), ("delta_p", C.c_double),
-                ("device", C.c_int32), ("reserved", C.c_int32)]
+                ("device", C.c_int32), ("time_integrator", C.c_int32)]
 
 
 class RgError(C.Structure):
@@ -54,10 +54,14 @@ REFERENCE_MESSAGES = {10: "Negative density", 11: "Negative thermal energy",
                       15: "Cell has too many neighbors"}
 
 
+TIME_ADVANCE = 0
+TIME_ADVANCE_HEUN = 1
+
+
 def make_config(gamma=5.0 / 3.0, cfl=0.3, order=2, ghost_kind=GHOST_RIGID_WALL, slope_limiter=1,
-                precision=FP64, delta_v=0.2, theta=0.5, delta_p=0.7, device=0):
+                precision=FP64, delta_v=0.2, theta=0.5, delta_p=0.7, device=0, time_integrator=TIME_ADVANCE):
     return RgConfig(gamma, cfl, order, ghost_kind, slope_limiter, precision, delta_v, theta,
-                    delta_p, device, 0)
+                    delta_p, device, time_integrator)
 
 
 class PackedMesh:

@@ -75,6 +75,13 @@ typedef enum rg_ghost_kind {
   RG_GHOST_PERIODIC = 1    /* PeriodicGhostGenerator.cpp:3-24 */
 } rg_ghost_kind;
 
+/* Which hdsim time advance rg_step / rg_run perform (fixed mesh). */
+typedef enum rg_time_integrator {
+  RG_TIME_ADVANCE = 0,      /* hdsim::TimeAdvance (hdsim2d.cpp:149-241): one flux pass */
+  RG_TIME_ADVANCE_HEUN = 1  /* hdsim::TimeAdvance2Heun (hdsim2d.cpp:323-449): two flux passes,
+                               averaged extensives */
+} rg_time_integrator;
+
 typedef enum rg_precision {
   RG_FP64 = 0,      /* plain FP64: every operation in the reference's order */
   RG_FP32_MIXED = 1 /* reconstruction + HLLC in FP32; geometry, volumes,
@@ -92,7 +99,7 @@ typedef struct rg_config {
   double theta;          /* LinearGaussImproved diffusecoeff_, default 0.5 */
   double delta_p;        /* LinearGaussImproved pressure_ratio_, default 0.7 */
   int32_t device;        /* CUDA device ordinal */
-  int32_t reserved;
+  int32_t time_integrator; /* rg_time_integrator: the step rg_step / rg_run take */
 } rg_config;
 
 /* Fills *cfg with the reference's constructor defaults: Hllc(), SimpleCFL(0.3),
@@ -193,15 +200,20 @@ rg_status rg_extensive_update(rg_handle* h, double dt);
 rg_status rg_cell_update(rg_handle* h);
 
 /* hdsim::TimeAdvance's hot path fused on the device (hdsim2d.cpp:149-241 with
- * a fixed mesh): dt = SimpleCFL, fluxes, extensive update, cell update.  dt
- * never leaves the device between the passes; *dt_out receives it. */
+ * a fixed mesh): dt = SimpleCFL, fluxes, extensive update, cell update; or,
+ * with time_integrator = RG_TIME_ADVANCE_HEUN, hdsim::TimeAdvance2Heun
+ * (hdsim2d.cpp:323-449): fluxes on the cells, mid extensives and cells,
+ * fluxes on the mid cells, extensives averaged.  dt never leaves the device
+ * between the passes; *dt_out receives it. */
 rg_status rg_step(rg_handle* h, double* dt_out);
 /* n_steps rg_step calls without a host synchronisation between them; errors
  * are checked once at the end.  dt_out (n_steps, host) may be NULL. */
 rg_status rg_run(rg_handle* h, int32_t n_steps, double* dt_out);
 /* rg_step with CUDA events between its kernels (the work is identical):
  * kernel_ms[0..3] = CFL (with the ghost fill), LinearGaussImproved slopes
- * (0 for order 1), face fluxes, gather + cell update. */
+ * (0 for order 1), face fluxes, gather + cell update.  For the Heun step:
+ * CFL, first pass (slopes + faces + update), second pass (ghost fill +
+ * slopes + faces), final update. */
 rg_status rg_step_timed(rg_handle* h, double* dt_out, float* kernel_ms);
 /* Enqueues one fused step on the handle's stream and returns at once; its
  * failures surface at the next rg_synchronize. */

@@ -134,23 +134,24 @@ def init_extensives(mesh, cells, gamma):
     return out
 
 
-def step(mesh, cells, ext, ev, gamma, cfl_number=0.3, order=2, lp=None):
-    """One fixed-mesh hot-path pass; returns (cells, ext, dt)."""
+def step(mesh, cells, ext, ev, gamma, cfl_number=0.3, order=2, lp=None, heun=False):
+    """One fixed-mesh hot-path pass (hdsim::TimeAdvance, or TimeAdvance2Heun
+    with heun=True); returns (cells, ext, dt)."""
     cells = _f64(cells).copy()
     ext = _f64(ext).copy()
     ev = _f64(ev)
     lp = lp or lgi_params()
     dt = C.c_double()
     err = RoError()
-    _check(lib().ro_step(C.byref(mesh.view()), _d(cells), _d(ext), _d(ev), C.c_double(gamma),
-                         C.c_double(cfl_number), C.c_int(order), C.byref(lp), C.byref(dt),
-                         C.byref(err)), err)
+    fn = lib().ro_step_heun if heun else lib().ro_step
+    _check(fn(C.byref(mesh.view()), _d(cells), _d(ext), _d(ev), C.c_double(gamma),
+              C.c_double(cfl_number), C.c_int(order), C.byref(lp), C.byref(dt), C.byref(err)), err)
     return cells, ext, dt.value
 
 
-def run(mesh, cells, ext, ev, gamma, steps, cfl_number=0.3, order=2, lp=None):
+def run(mesh, cells, ext, ev, gamma, steps, cfl_number=0.3, order=2, lp=None, heun=False):
     dts = []
     for _ in range(steps):
-        cells, ext, dt = step(mesh, cells, ext, ev, gamma, cfl_number, order, lp)
+        cells, ext, dt = step(mesh, cells, ext, ev, gamma, cfl_number, order, lp, heun)
         dts.append(dt)
     return cells, ext, np.array(dts)

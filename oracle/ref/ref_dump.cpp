@@ -5,7 +5,10 @@
 // Test infrastructure only: it links the reference sources built by
 // oracle/ref/Makefile and is never part of the product.
 //
-//   ref_dump <case> <outdir> <nx> <ny> <warm_steps> <run_steps>
+//   ref_dump <case> <outdir> <nx> <ny> <warm_steps> <run_steps> [heun]
+//
+// With "heun" the warm-up and run steps use hdsim::TimeAdvance2Heun
+// (hdsim2d.cpp:323-449) instead of hdsim::TimeAdvance.
 //
 // For every case it writes, for the state reached after <warm_steps>
 // hdsim::TimeAdvance steps (hdsim2d.cpp:149-241):
@@ -51,6 +54,14 @@
 namespace {
 
 std::string g_out;
+bool g_heun = false;
+
+void advance(hdsim& sim) {
+  if (g_heun)
+    sim.TimeAdvance2Heun();
+  else
+    sim.TimeAdvance();
+}
 
 void write_npy(const std::string& name, const char* descr, size_t elem, const void* data,
                size_t rows, size_t cols) {
@@ -204,7 +215,7 @@ void run_and_dump(hdsim& sim, int steps) {
   // every dt without the rounding of a difference.
   std::vector<double> times;
   for (int s = 0; s < steps; ++s) {
-    sim.TimeAdvance();
+    advance(sim);
     times.push_back(sim.getTime());
   }
   dump_f64("run_cells", cells_flat(sim.getAllCells()), 4);
@@ -225,6 +236,7 @@ int main(int argc, char** argv) {
   g_out = argv[2];
   const int nx = std::atoi(argv[3]), ny = std::atoi(argv[4]);
   const int warm = std::atoi(argv[5]), run = std::atoi(argv[6]);
+  g_heun = argc > 7 && std::string(argv[7]) == "heun";
   try {
     SlabSymmetry pg;
     Hllc rs;
@@ -250,7 +262,7 @@ int main(int argc, char** argv) {
         ic[i].pressure = left ? 1 : 0.1;
       }
       hdsim sim(tess, outer, pg, ic, eos, pm, evc, force, tsf, fc, eu, cu);
-      for (int s = 0; s < warm; ++s) sim.TimeAdvance();
+      for (int s = 0; s < warm; ++s) advance(sim);
       dump_scalar("gamma", 1.4);
       dump_scalar("order", 1);
       dump_scalar("ghost_kind", 0);
@@ -282,7 +294,7 @@ int main(int argc, char** argv) {
         ic[i].pressure = abs(tess.GetMeshPoint(static_cast<int>(i))) < rdep ? (5. / 3. - 1) / vin : 1e-6;
       }
       hdsim sim(tess, outer, pg, ic, eos, pm, evc, force, tsf, fc, eu, cu);
-      for (int s = 0; s < warm; ++s) sim.TimeAdvance();
+      for (int s = 0; s < warm; ++s) advance(sim);
       dump_scalar("gamma", 5. / 3.);
       dump_scalar("order", 2);
       dump_scalar("ghost_kind", 0);
@@ -323,7 +335,7 @@ int main(int argc, char** argv) {
         ic[i].velocity = Vector2D(0.1 * std::sin(pi2 * (r.x + 2 * r.y)), 0.1 * std::cos(pi2 * (2 * r.x - r.y)));
       }
       hdsim sim(tess, outer, pg, ic, eos, pm, evc, force, tsf, fc, eu, cu);
-      for (int s = 0; s < warm; ++s) sim.TimeAdvance();
+      for (int s = 0; s < warm; ++s) advance(sim);
       dump_scalar("gamma", 5. / 3.);
       dump_scalar("order", 2);
       dump_scalar("ghost_kind", 1);

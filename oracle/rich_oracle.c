@@ -691,3 +691,35 @@ int ro_step(const rg_mesh_view* m, double* cells, double* ext, const double* ev,
   if (dt_out) *dt_out = dt;
   return st;
 }
+
+/* hdsim2d.cpp:323-449 TimeAdvance2Heun with ZeroForce (which adds dt*0) and a
+ * mesh that does not move: dt, F1 on the cells, mid = ext + dt*area*F1,
+ * mid cells, F2 on the mid cells, mid += dt*area*F2, ext = 0.5*(mid + ext)
+ * (average_extensive, hdsim2d.cpp:311-320), cells from ext. */
+int ro_step_heun(const rg_mesh_view* m, double* cells, double* ext, const double* ev, double g,
+                 double cfl, int order, const ro_lgi_params* lp, double* dt_out, ro_error* err) {
+  double dt;
+  int st = ro_cfl(m, cells, ev, g, cfl, &dt, err);
+  if (st) return st;
+  const size_t n4 = 4 * (size_t)m->n_cells;
+  double* fl = (double*)malloc(sizeof(double) * 4 * (size_t)(m->n_faces > 0 ? m->n_faces : 1));
+  double* mid = (double*)malloc(sizeof(double) * n4);
+  double* mid_cells = (double*)malloc(sizeof(double) * n4);
+  memcpy(mid, ext, sizeof(double) * n4);
+  st = order == 1 ? ro_simple_flux(m, cells, ev, g, fl, err) : ro_modular_flux(m, cells, ev, g, lp, fl, err);
+  if (!st) st = ro_extensive_update(m, fl, dt, mid, err);
+  if (!st) st = ro_cell_update(m, mid, g, mid_cells, err);
+  if (!st)
+    st = order == 1 ? ro_simple_flux(m, mid_cells, ev, g, fl, err)
+                    : ro_modular_flux(m, mid_cells, ev, g, lp, fl, err);
+  if (!st) st = ro_extensive_update(m, fl, dt, mid, err);
+  if (!st) {
+    for (size_t k = 0; k < n4; ++k) ext[k] = 0.5 * (mid[k] + ext[k]);
+    st = ro_cell_update(m, ext, g, cells, err);
+  }
+  free(fl);
+  free(mid);
+  free(mid_cells);
+  if (dt_out) *dt_out = dt;
+  return st;
+}

@@ -56,6 +56,11 @@ int ro_init_extensives(const rg_mesh_view* m, const double* cells, double gamma,
 int ro_step(const rg_mesh_view* m, double* cells, double* ext, const double* ev, double gamma,
             double cfl, int order, const ro_lgi_params* lp, double* dt_out, ro_error* err);
 
+/* hdsim::TimeAdvance2Heun (hdsim2d.cpp:323-449) on a fixed mesh with fixed
+ * edge velocities (its two SimpleCFL calls then agree). */
+int ro_step_heun(const rg_mesh_view* m, double* cells, double* ext, const double* ev, double gamma,
+                 double cfl, int order, const ro_lgi_params* lp, double* dt_out, ro_error* err);
+
 #ifdef __cplusplus
 }
 #endif

@@ -30,6 +30,7 @@ def load_golden(name):
     z["order"] = int(z["order"][0])
     z["ghost_kind"] = int(z["ghost_kind"][0])
     z["dt"] = float(z["dt"][0])
+    z["heun"] = bool(int(z["time_integrator"])) if "time_integrator" in z else False
     return z
 
 

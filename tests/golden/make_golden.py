@@ -26,7 +26,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 
-# name: (ref_dump case, nx, ny, warm steps, run steps)
+# name: (ref_dump case, nx, ny, warm steps, run steps[, "heun"])
 CASES = {
     # 2D Sod, first order, Eulerian: one pass + 20 hdsim steps
     "sod_o1": ("sod", 50, 10, 0, 20),
@@ -42,6 +42,10 @@ CASES = {
     "periodic_o2": ("periodic", 16, 16, 2, 10),
     # periodic box with Lagrangian faces after 2 steps
     "periodic_lagrangian_o2": ("periodic_lagrangian", 16, 16, 2, 0),
+    # hdsim::TimeAdvance2Heun on fixed meshes
+    "sod_heun_o1": ("sod", 50, 10, 0, 20, "heun"),
+    "sedov_eulerian_heun_o2": ("sedov_eulerian", 24, 24, 2, 10, "heun"),
+    "periodic_heun_o2": ("periodic", 16, 16, 2, 10, "heun"),
 }
 
 
@@ -54,9 +58,11 @@ def main():
                            "REF=" + a.ref])
     exe = os.path.join(ROOT, "oracle", "_ref", "ref_dump")
     for name in a.cases or sorted(CASES):
-        case, nx, ny, warm, run = CASES[name]
+        case, nx, ny, warm, run = CASES[name][:5]
+        scheme = CASES[name][5] if len(CASES[name]) > 5 else "first"
         with tempfile.TemporaryDirectory() as d:
-            subprocess.check_call([exe, case, d, str(nx), str(ny), str(warm), str(run)])
+            subprocess.check_call([exe, case, d, str(nx), str(ny), str(warm), str(run)] +
+                                  (["heun"] if scheme == "heun" else []))
             arrays = {os.path.basename(f)[:-4]: np.load(f) for f in glob.glob(os.path.join(d, "*.npy"))}
         run_keys = [k for k in arrays if k.startswith("runmesh_")]
         if run_keys and all(np.array_equal(arrays[k], arrays["mesh_" + k[8:]]) for k in run_keys):
@@ -66,6 +72,7 @@ def main():
                 del arrays[k]
             arrays["run_mesh_unchanged"] = np.array(1)
         arrays["case_params"] = np.array([nx, ny, warm, run], dtype=np.int64)
+        arrays["time_integrator"] = np.array(1 if scheme == "heun" else 0)
         out = os.path.join(HERE, name + ".npz")
         np.savez_compressed(out, **arrays)
         print(f"{name}: {len(arrays)} arrays, {os.path.getsize(out) / 1024:.0f} KiB", file=sys.stderr)

@@ -30,8 +30,9 @@ def initial(mesh, kind, gamma):
             "bumps": synthetic.bumps_cells}[kind](mesh)
 
 
-def run(mesh, cells, ext, gamma, order, gk, precision, steps):
-    with richgpu.Handle(gamma=gamma, order=order, ghost_kind=gk, precision=precision, device=0) as h:
+def run(mesh, cells, ext, gamma, order, gk, precision, steps, heun=0):
+    with richgpu.Handle(gamma=gamma, order=order, ghost_kind=gk, precision=precision, device=0,
+                        time_integrator=heun) as h:
         h.upload_mesh(mesh)
         h.set_cells(cells)
         h.set_extensives(ext)
@@ -55,6 +56,18 @@ def test_mixed_density_l1_vs_fp64(case):
     t0, t1 = ext.sum(0), e32.sum(0)
     assert abs(t1[0] - t0[0]) <= 1e-13 * abs(t0[0])
     assert abs(t1[1] - t0[1]) <= 1e-12 * abs(t0[1])
+
+
+def test_mixed_heun_density_l1_vs_fp64():
+    mesh = synthetic.lattice_mesh(256, 256, (-1.0, 1.0, -1.0, 1.0), "rigid", seed=2)
+    gamma = 5 / 3
+    cells = synthetic.sedov_cells(mesh, gamma)
+    ext = oracle.init_extensives(mesh, cells, gamma)
+    c64, _, _ = run(mesh, cells, ext, gamma, 2, 0, 0, 100, heun=1)
+    c32, e32, _ = run(mesh, cells, ext, gamma, 2, 0, 1, 100, heun=1)
+    l1 = np.abs(c32[:, 0] - c64[:, 0]).sum() / np.abs(c64[:, 0]).sum()
+    assert l1 <= 1e-5, l1
+    assert abs(e32[:, 0].sum() - ext[:, 0].sum()) <= 1e-13 * ext[:, 0].sum()
 
 
 def test_mixed_fused_step_equals_split_plugins():

@@ -54,10 +54,11 @@ def test_golden_extensive_update_from_host_fluxes(name):
 
 @pytest.mark.parametrize("name", [c for c in GOLDEN_CASES if "lagrangian" not in c and c != "sedov_o2"])
 def test_golden_hdsim_run(name):
-    """rg_run reproduces N hdsim::TimeAdvance steps (fixed mesh) exactly."""
+    """rg_run reproduces N hdsim::TimeAdvance (or TimeAdvance2Heun) steps on a
+    fixed mesh exactly."""
     g = load_golden(name)
     steps = int(g["case_params"][3])
-    with handle_for(g["gamma"], g["order"], g["ghost_kind"]) as h:
+    with handle_for(g["gamma"], g["order"], g["ghost_kind"], time_integrator=int(g["heun"])) as h:
         h.upload_mesh(g["mesh"])
         h.set_cells(g["cells0"])
         h.set_extensives(g["ext0"])
@@ -123,6 +124,27 @@ def test_synthetic_multistep_vs_oracle(case):
         dts = h.run(20)
         gc, ge = h.get_cells(), h.get_extensives()
     oc, oe, odts = oracle.run(mesh, cells, ext, ev, gamma, 20, 0.3, order, oracle.lgi_params(gk))
+    exact(dts, odts)
+    exact(ge, oe)
+    exact(gc, oc)
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_synthetic_heun_vs_oracle(case):
+    """10 fused TimeAdvance2Heun steps equal 10 oracle Heun steps."""
+    (nx, ny, box, bnd, seed), gamma, order, gk, kind = CASES[case]
+    mesh = synthetic.lattice_mesh(nx, ny, box, bnd, seed=seed)
+    cells = initial(mesh, kind, gamma)
+    ext = oracle.init_extensives(mesh, cells, gamma)
+    ev = np.zeros((mesh.n_faces, 2))
+    with handle_for(gamma, order, gk, time_integrator=1) as h:
+        h.upload_mesh(mesh)
+        h.set_cells(cells)
+        h.set_extensives(ext)
+        h.set_edge_velocities(ev)
+        dts = h.run(10)
+        gc, ge = h.get_cells(), h.get_extensives()
+    oc, oe, odts = oracle.run(mesh, cells, ext, ev, gamma, 10, 0.3, order, oracle.lgi_params(gk), heun=True)
     exact(dts, odts)
     exact(ge, oe)
     exact(gc, oc)

@@ -70,7 +70,8 @@ def test_cell_update(golden):
 
 
 def test_hdsim_run(golden):
-    """N hdsim::TimeAdvance steps on a mesh that hdsim rebuilt unchanged."""
+    """N hdsim::TimeAdvance (or TimeAdvance2Heun) steps on a mesh that hdsim
+    rebuilt unchanged."""
     g = golden
     if "run_cells" not in g:
         pytest.skip("no multi-step run in this case")
@@ -78,7 +79,7 @@ def test_hdsim_run(golden):
     steps = int(g["case_params"][3])
     ev = np.zeros((g["mesh"].n_faces, 2))
     cells, ext, dts = oracle.run(g["mesh"], g["cells0"], g["ext0"], ev, g["gamma"], steps,
-                                 0.3, g["order"], lp_of(g))
+                                 0.3, g["order"], lp_of(g), heun=g["heun"])
     exact(accumulate(float(g["time0"][0]), dts), g["run_times"])
     exact(ext, g["run_ext"])
     exact(cells, g["run_cells"])
