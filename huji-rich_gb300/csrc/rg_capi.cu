@@ -159,6 +159,12 @@ struct rg_handle {
   // Heun mid stage: extensives and cells after the first flux pass
   DevBuf mid_ext, mid_cells, mid_cells32;
   bool heun = false;
+  // batch of independent problems (n_problems == 0: one problem)
+  int n_problems = 0;
+  DevBuf cell_problem, problem_offsets, gamma_p, gamma32_p, inv_gm1_32_p, dtmin_p, time_p, dt_p;
+  // CUDA graph of one fused step
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
   size_t cells_records = 0;
   bool have_cells = false, have_ext = false, have_ev = false, have_fluxes = false;
   HostBuf staging, host_status, host_dts;
@@ -332,6 +338,14 @@ rg::StepArgs step_args(rg_handle* h) {
   a.dt_host = 0;
   a.dt_from_device = 0;
   a.step = 0;
+  if (h->n_problems > 0) {
+    a.cell_problem = static_cast<const int*>(h->cell_problem.p);
+    a.gamma_p = static_cast<const double*>(h->gamma_p.p);
+    a.dtmin_p = static_cast<unsigned long long*>(h->dtmin_p.p);
+    a.time_p = static_cast<double*>(h->time_p.p);
+    a.dt_p = static_cast<double*>(h->dt_p.p);
+    a.n_problems = h->n_problems;
+  }
   return a;
 }
 
@@ -359,7 +373,23 @@ rg::MixedArgs mixed_args(rg_handle* h) {
   a.dt32 = 0;
   a.dt32_from_device = 0;
   a.step = 0;
+  if (h->n_problems > 0) {
+    a.cell_problem = static_cast<const int*>(h->cell_problem.p);
+    a.gamma_p = static_cast<const float*>(h->gamma32_p.p);
+    a.inv_gm1_p = static_cast<const float*>(h->inv_gm1_32_p.p);
+    a.dtmin_p = static_cast<unsigned long long*>(h->dtmin_p.p);
+    a.time_p = static_cast<double*>(h->time_p.p);
+    a.dt_p = static_cast<double*>(h->dt_p.p);
+    a.n_problems = h->n_problems;
+  }
   return a;
+}
+
+void drop_graph(rg_handle* h) {
+  if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+  if (h->graph) cudaGraphDestroy(h->graph);
+  h->graph_exec = nullptr;
+  h->graph = nullptr;
 }
 
 rg_status require(rg_handle* h, bool cells, bool ext, bool ev, bool fluxes) {
@@ -590,6 +620,11 @@ rg_status rg_destroy(rg_handle* h) {
   h->mid_ext.release();
   h->mid_cells.release();
   h->mid_cells32.release();
+  for (DevBuf* b : {&h->cell_problem, &h->problem_offsets, &h->gamma_p, &h->gamma32_p, &h->inv_gm1_32_p,
+                    &h->dtmin_p, &h->time_p, &h->dt_p})
+    b->release();
+  if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+  if (h->graph) cudaGraphDestroy(h->graph);
   h->cells32.release();
   h->slopes32.release();
   h->flux32.release();
@@ -778,6 +813,9 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t /*flags*/
   s.geom_error = rg_error{};
   if (hs->err_key != ~0ull)
     s.geom_error = rg_error{hs->err_status, 2, static_cast<int64_t>(hs->err_key & rg::kKeyIndexMask), hs->err_value};
+  // a new mesh drops the batch table and the captured step
+  h->n_problems = 0;
+  drop_graph(h);
   // later compute work on the stream sees the new slot
   RG_CUDA(h, cudaStreamWaitEvent(h->stream, h->ev_up1, 0));
   if (h->active >= 0) RG_CUDA(h, cudaEventRecord(h->slots[h->active].last_use, h->stream));
@@ -895,7 +933,7 @@ rg_status rg_init_extensives(rg_handle* h) {
 
 rg_status rg_cfl_dt(rg_handle* h, double* dt) {
   if (rg_status st = require(h, true, false, true, false)) return st;
-  if (!dt) return RG_ERR_INVALID_ARGUMENT;
+  if (!dt || h->n_problems > 0) return invalid(h, -1, 0);
   h->last = rg_error{};
   RG_TRY(reset_status(h, h->d_status, h->stream));
   if (h->mixed) {
@@ -1031,11 +1069,100 @@ rg_status rg_run(rg_handle* h, int32_t n_steps, double* dt_out) {
   for (int k = 0; k < n_steps; ++k) {
     if (rg_status st = enqueue_step(h, std::min(k, 0x1fff))) return st;
     if (dt_out)
-      RG_CUDA(h, cudaMemcpyAsync(hd + k, &h->d_status->dt, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+      RG_CUDA(h, cudaMemcpyAsync(hd + k, h->n_problems > 0 ? static_cast<double*>(h->dt_p.p) : &h->d_status->dt,
+                                 sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   }
   rg_status st = collect(h, h->d_status, h->stream);
   if (dt_out) std::memcpy(dt_out, hd, sizeof(double) * static_cast<size_t>(n_steps));
   return st;
+}
+
+rg_status rg_set_problems(rg_handle* h, int32_t P, const int32_t* offsets, const double* gamma) {
+  if (!h) return RG_ERR_INVALID_ARGUMENT;
+  if (h->active < 0) return require(h, false, false, false, false);
+  h->last = rg_error{};
+  drop_graph(h);
+  MeshSlot* s = active_slot(h);
+  if (P == 0) {
+    h->n_problems = 0;
+    return RG_OK;
+  }
+  if (P < 0 || !offsets || !gamma || h->heun) return invalid(h, -1, P);
+  if (offsets[0] != 0 || offsets[P] != s->n) return invalid(h, -2, offsets[P]);
+  for (int p = 0; p < P; ++p) {
+    if (offsets[p + 1] <= offsets[p]) return invalid(h, p, offsets[p + 1]);
+    if (!(gamma[p] > 1.0)) return invalid(h, p, gamma[p]);
+  }
+  RG_CUDA(h, cudaStreamSynchronize(h->stream));
+  RG_CUDA(h, h->cell_problem.ensure(4 * (static_cast<size_t>(s->n) + s->g)));
+  RG_CUDA(h, h->problem_offsets.ensure(4 * (static_cast<size_t>(P) + 1)));
+  RG_CUDA(h, h->gamma_p.ensure(8 * static_cast<size_t>(P)));
+  RG_CUDA(h, h->gamma32_p.ensure(4 * static_cast<size_t>(P)));
+  RG_CUDA(h, h->inv_gm1_32_p.ensure(4 * static_cast<size_t>(P)));
+  RG_CUDA(h, h->dtmin_p.ensure(8 * static_cast<size_t>(P)));
+  RG_CUDA(h, h->time_p.ensure(8 * static_cast<size_t>(P)));
+  RG_CUDA(h, h->dt_p.ensure(8 * static_cast<size_t>(P)));
+  std::vector<float> g32(static_cast<size_t>(P)), igm(static_cast<size_t>(P));
+  std::vector<unsigned long long> inf(static_cast<size_t>(P), rg::kInfBits);
+  for (int p = 0; p < P; ++p) {
+    g32[static_cast<size_t>(p)] = static_cast<float>(gamma[p]);
+    igm[static_cast<size_t>(p)] = static_cast<float>(1.0 / (gamma[p] - 1.0));
+  }
+  RG_CUDA(h, cudaMemcpy(h->problem_offsets.p, offsets, 4 * (static_cast<size_t>(P) + 1), cudaMemcpyHostToDevice));
+  RG_CUDA(h, cudaMemcpy(h->gamma_p.p, gamma, 8 * static_cast<size_t>(P), cudaMemcpyHostToDevice));
+  RG_CUDA(h, cudaMemcpy(h->gamma32_p.p, g32.data(), 4 * static_cast<size_t>(P), cudaMemcpyHostToDevice));
+  RG_CUDA(h, cudaMemcpy(h->inv_gm1_32_p.p, igm.data(), 4 * static_cast<size_t>(P), cudaMemcpyHostToDevice));
+  RG_CUDA(h, cudaMemcpy(h->dtmin_p.p, inf.data(), 8 * static_cast<size_t>(P), cudaMemcpyHostToDevice));
+  RG_CUDA(h, cudaMemset(h->time_p.p, 0, 8 * static_cast<size_t>(P)));
+  RG_CUDA(h, cudaMemset(h->dt_p.p, 0, 8 * static_cast<size_t>(P)));
+  RG_TRY(reset_status(h, h->d_geom_status, h->stream));
+  RG_CUDA(h, rg::launch_problems(s->mesh, static_cast<const int*>(h->problem_offsets.p), P,
+                                 static_cast<int*>(h->cell_problem.p), h->d_geom_status, h->stream));
+  DevStatus* hs = static_cast<DevStatus*>(h->host_status.p);
+  RG_CUDA(h, cudaMemcpyAsync(hs, h->d_geom_status, sizeof(DevStatus), cudaMemcpyDeviceToHost, h->stream));
+  RG_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (hs->err_key != ~0ull) {
+    h->n_problems = 0;
+    return invalid(h, static_cast<int64_t>(hs->err_key & rg::kKeyIndexMask), hs->err_value);
+  }
+  h->n_problems = P;
+  return RG_OK;
+}
+
+rg_status rg_get_problem_times(rg_handle* h, double* time_out, double* dt_out) {
+  if (!h) return RG_ERR_INVALID_ARGUMENT;
+  if (h->n_problems <= 0) return invalid(h, -1, 0);
+  RG_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (time_out)
+    RG_CUDA(h, cudaMemcpy(time_out, h->time_p.p, 8 * static_cast<size_t>(h->n_problems), cudaMemcpyDeviceToHost));
+  if (dt_out)
+    RG_CUDA(h, cudaMemcpy(dt_out, h->dt_p.p, 8 * static_cast<size_t>(h->n_problems), cudaMemcpyDeviceToHost));
+  return RG_OK;
+}
+
+rg_status rg_run_graph(rg_handle* h, int32_t n_steps) {
+  if (rg_status st = require(h, true, true, true, false)) return st;
+  if (n_steps < 0) return RG_ERR_INVALID_ARGUMENT;
+  if (rg_status st = mesh_error(h)) return st;
+  h->last = rg_error{};
+  if (!h->graph_exec) {
+    RG_CUDA(h, cudaStreamSynchronize(h->stream));
+    RG_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    const rg_status st = enqueue_step(h, 0);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(h->stream, &g);
+    if (st != RG_OK) {
+      if (g) cudaGraphDestroy(g);
+      return st;
+    }
+    if (ce != cudaSuccess) return cuda_fail(h, ce);
+    h->graph = g;
+    RG_CUDA(h, cudaGraphInstantiate(&h->graph_exec, h->graph, 0));
+  }
+  RG_TRY(reset_status(h, h->d_status, h->stream));
+  for (int k = 0; k < n_steps; ++k) RG_CUDA(h, cudaGraphLaunch(h->graph_exec, h->stream));
+  h->have_fluxes = false;
+  return collect(h, h->d_status, h->stream);
 }
 
 }  // extern "C"

@@ -222,6 +222,17 @@ __global__ void __launch_bounds__(kBlock) k_validate(MeshDev m, DevStatus* st) {
 
 // ---------------------------------------------------------------- per step
 
+// Per-problem parameters of a batch (kBatch) or the handle's single values.
+template <bool kBatch>
+__device__ __forceinline__ double gamma_at(const StepArgs& a, int point) {
+  return kBatch ? a.gamma_p[a.cell_problem[point]] : a.gamma;
+}
+template <bool kBatch>
+__device__ __forceinline__ double scaled_dt(const StepArgs& a, int point) {
+  if (kBatch) return a.cfl * __longlong_as_double(static_cast<long long>(a.dtmin_p[a.cell_problem[point]]));
+  return a.dt_from_device ? a.status->dt : a.dt_host;
+}
+
 // Ghost state (LinearGaussImproved.cpp:543-550 new_cells[ghost]):
 // RigidWallGenerator.cpp:17-37 reflects the real neighbour's velocity,
 // PeriodicGhostGenerator.cpp:3-17 copies the source cell.
@@ -237,6 +248,7 @@ __device__ __forceinline__ void fill_ghost(const StepArgs& a, int g) {
 }
 
 // simple_cfl.cpp:28-47 (per cell) and :58-71 + lazy_list.hpp:185-191 (min, times cfl).
+template <bool kBatch>
 __global__ void __launch_bounds__(kBlock) k_cfl(StepArgs a, int fill_ghosts) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const MeshDev& m = a.mesh;
@@ -244,7 +256,7 @@ __global__ void __launch_bounds__(kBlock) k_cfl(StepArgs a, int fill_ghosts) {
   if (t < m.n) {
     const Cell c = load_cell(a.cells, t);
     const double radius = a.geom.width[t];
-    const double cs = sqrt(a.gamma * c.p / c.d);
+    const double cs = sqrt(gamma_at<kBatch>(a, t) * c.p / c.d);
     // fmax over faces of (cs + sqrt(q_e)) / radius equals (cs + sqrt(max q_e)) /
     // radius exactly: sqrt, + and / are correctly rounded, hence monotone, so
     // the maximum commutes with them.  NaN terms are skipped as fmax skips them.
@@ -265,8 +277,13 @@ __global__ void __launch_bounds__(kBlock) k_cfl(StepArgs a, int fill_ghosts) {
   } else if (fill_ghosts && t < m.n + m.g) {
     fill_ghost(a, t - m.n);
   }
-  // min over the block (positive doubles: integer order = numeric order)
   unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(x));
+  if (kBatch) {
+    // per-problem minimum; the update kernel turns it into the problem's dt
+    problem_min(a.dtmin_p, t < m.n ? a.cell_problem[t] : -1, bits);
+    return;
+  }
+  // min over the block (positive doubles: integer order = numeric order)
   for (int o = 16; o > 0; o >>= 1) {
     const unsigned long long ob = __shfl_xor_sync(0xffffffffu, bits, o);
     bits = ob < bits ? ob : bits;
@@ -378,6 +395,7 @@ __device__ __forceinline__ void shocked_comp(double dphi, double cv, double cell
 }
 
 // LinearGaussImproved.cpp:425-494 calc_slope for one cell (serial build).
+template <bool kBatch>
 __global__ void __launch_bounds__(kBlock) k_slopes(StepArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const MeshDev& m = a.mesh;
@@ -435,7 +453,7 @@ __global__ void __launch_bounds__(kBlock) k_slopes(StepArgs a) {
     const double lhs = (sx.vx + sy.vy) * a.geom.width[i];
     bool shock = false;
     if (lhs < 0) {
-      const double gp = a.gamma * cell.p;
+      const double gp = gamma_at<kBatch>(a, i) * cell.p;
       bool decided = false;
       if (fp32_safe(lhs) && fp32_safe(gp) && fp32_safe(cell.d)) {
         const float rhs_f = static_cast<float>(a.delta_v) * sqrtf(static_cast<float>(gp) / static_cast<float>(cell.d));
@@ -610,9 +628,11 @@ __device__ __forceinline__ bool solve_face(Prim l, Prim r, double velocity, doub
   return true;
 }
 
-__device__ __forceinline__ void write_flux(const StepArgs& a, int e, const Cons& c, bool scaled, double area) {
+template <bool kBatch>
+__device__ __forceinline__ void write_flux(const StepArgs& a, int e, int real_side, const Cons& c, bool scaled,
+                                           double area) {
   if (scaled) {
-    const double s = step_dt(a) * area;  // simple_extensive_updater.cpp:26-27
+    const double s = scaled_dt<kBatch>(a, real_side) * area;  // simple_extensive_updater.cpp:26-27
     store4(a.fluxes, e, c.m * s, c.en * s, c.mx * s, c.my * s);
   } else {
     store4(a.fluxes, e, c.m, c.en, c.mx, c.my);
@@ -621,7 +641,7 @@ __device__ __forceinline__ void write_flux(const StepArgs& a, int e, const Cons&
 
 // ModularFluxCalculator (modular_flux_calculator.cpp:39-71) with the face
 // states of LinearGaussImproved (:570-590 real sides, :596-634 ghost sides).
-template <bool kScaled>
+template <bool kScaled, bool kBatch>
 __global__ void __launch_bounds__(kBlock) k_faces_lgi(StepArgs a) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   const MeshDev& m = a.mesh;
@@ -658,9 +678,11 @@ __global__ void __launch_bounds__(kBlock) k_faces_lgi(StepArgs a) {
   const double na = a.geom.nabs[e], pa = a.geom.area[e];
   // a face at rest has speed +-0 (the sign only reaches signs of zeros)
   const double speed = (w.x == 0.0 && w.y == 0.0) ? 0.0 : (n.x * w.x + n.y * w.y) / na;
+  const int real_side = fc.x < m.n ? fc.x : fc.y;
+  const double g = gamma_at<kBatch>(a, real_side);
   Cons c;
-  if (!solve_face(to_prim(a.gamma, side[0]), to_prim(a.gamma, side[1]), speed, n, na, p, pa, c, a, e)) return;
-  write_flux(a, e, c, kScaled, pa);
+  if (!solve_face(to_prim(g, side[0]), to_prim(g, side[1]), speed, n, na, p, pa, c, a, e)) return;
+  write_flux<kBatch>(a, e, real_side, c, kScaled, pa);
 }
 
 // simple_flux_calculator.cpp:17-25 reflect (Reflect, geometry.cpp:117-120);
@@ -677,7 +699,7 @@ __device__ __forceinline__ Prim reflect(Prim q, double2 axis, double aa) {
 // SimpleFluxCalculator (simple_flux_calculator.cpp:80-126 riemann_reduce,
 // :216-244).  A ghost that is not its neighbour's own mirror takes its source
 // cell's state.
-template <bool kScaled>
+template <bool kScaled, bool kBatch>
 __global__ void __launch_bounds__(kBlock) k_faces_pcm(StepArgs a) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   const MeshDev& m = a.mesh;
@@ -687,22 +709,24 @@ __global__ void __launch_bounds__(kBlock) k_faces_pcm(StepArgs a) {
   const double pa = a.geom.area[e], na = a.geom.nabs[e];
   const bool va = fc.x < m.n, vb = fc.y < m.n;
   const int oa = orig_of(m, fc.x), ob = orig_of(m, fc.y);
+  const int real_side = va ? fc.x : fc.y;
+  const double g = gamma_at<kBatch>(a, real_side);
   Prim l, r;
   if (!va) {
-    r = to_prim(a.gamma, load_cell(a.cells, fc.y));
-    l = oa == ob ? reflect(r, p, pa) : to_prim(a.gamma, load_cell(a.cells, oa));
+    r = to_prim(g, load_cell(a.cells, fc.y));
+    l = oa == ob ? reflect(r, p, pa) : to_prim(g, load_cell(a.cells, oa));
   } else if (!vb) {
-    l = to_prim(a.gamma, load_cell(a.cells, fc.x));
-    r = oa == ob ? reflect(l, p, pa) : to_prim(a.gamma, load_cell(a.cells, ob));
+    l = to_prim(g, load_cell(a.cells, fc.x));
+    r = oa == ob ? reflect(l, p, pa) : to_prim(g, load_cell(a.cells, ob));
   } else {
-    l = to_prim(a.gamma, load_cell(a.cells, fc.x));
-    r = to_prim(a.gamma, load_cell(a.cells, fc.y));
+    l = to_prim(g, load_cell(a.cells, fc.x));
+    r = to_prim(g, load_cell(a.cells, fc.y));
   }
   const double2 w = reinterpret_cast<const double2*>(a.ev)[e];
   const double velocity = (w.x == 0.0 && w.y == 0.0) ? 0.0 : (n.x * w.x + n.y * w.y) / na;
   Cons c;
   if (!solve_face(l, r, velocity, n, na, p, pa, c, a, e)) return;
-  write_flux(a, e, c, kScaled, pa);
+  write_flux<kBatch>(a, e, real_side, c, kScaled, pa);
 }
 
 // ---------------------------------------------------------------- cells
@@ -711,9 +735,18 @@ __global__ void __launch_bounds__(kBlock) k_faces_pcm(StepArgs a) {
 // each cell applies its faces' contributions in ascending face order, which
 // is the order the reference's edge loop applies them to that cell; then
 // SimpleCellUpdater::regular_update (simple_cell_updater.cpp:22-59).
+template <bool kBatch>
 __global__ void __launch_bounds__(kBlock) k_update(StepArgs a, int from_unscaled, int do_ext, int do_cells) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const MeshDev& m = a.mesh;
+  if (kBatch && do_ext && !from_unscaled && i < a.n_problems) {
+    // every face of this step has read its problem's minimum: record the dt,
+    // advance the problem's time and reset the minimum for the next step
+    const double dt = a.cfl * __longlong_as_double(static_cast<long long>(a.dtmin_p[i]));
+    a.dt_p[i] = dt;
+    a.time_p[i] += dt;
+    a.dtmin_p[i] = kInfBits;
+  }
   if (i >= m.n) return;
   double2* ext2 = reinterpret_cast<double2*>(a.ext);
   double2 e01 = ext2[2 * i], e23 = ext2[2 * i + 1];
@@ -770,23 +803,65 @@ __global__ void __launch_bounds__(kBlock) k_update(StepArgs a, int from_unscaled
       record_error(a.status, a.step, RG_ERR_NEGATIVE_ENERGY, 5, i, energy);
       return;
     }
-    store4(a.cells_out ? a.cells_out : a.cells, i, d, (a.gamma - 1) * energy * d, vx, vy);
+    store4(a.cells_out ? a.cells_out : a.cells, i, d, (gamma_at<kBatch>(a, i) - 1) * energy * d, vx, vy);
   }
 }
 
 // hdsim2d.cpp:41-67 init_extensives
+template <bool kBatch>
 __global__ void __launch_bounds__(kBlock) k_init_ext(StepArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.mesh.n) return;
   const Cell c = load_cell(a.cells, i);
   const double mass = a.mesh.cd_volume[i] * c.d;
-  store4(a.ext, i, mass, c.p / c.d / (a.gamma - 1) * mass + 0.5 * mass * (c.vx * c.vx + c.vy * c.vy),
+  store4(a.ext, i, mass, c.p / c.d / (gamma_at<kBatch>(a, i) - 1) * mass + 0.5 * mass * (c.vx * c.vx + c.vy * c.vy),
          c.vx * mass, c.vy * mass);
 }
 
 inline int blocks(int n) { return (n + kBlock - 1) / kBlock; }
 
 }  // namespace
+
+// Problem of every point of a batch (real cells by the offset table, ghosts by
+// their source cell) and the check that no face joins two problems.
+__global__ void __launch_bounds__(kBlock) k_problems(MeshDev m, const int* offsets, int P, int* cell_problem,
+                                                     DevStatus* st) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < m.n) {
+    int lo = 0, hi = P;  // largest p with offsets[p] <= t
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (offsets[mid] <= t) lo = mid; else hi = mid;
+    }
+    cell_problem[t] = lo;
+  }
+  __syncthreads();
+  if (t < m.g) {
+    const int src = m.ghost_source[t];
+    int lo = 0, hi = P;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (offsets[mid] <= src) lo = mid; else hi = mid;
+    }
+    cell_problem[m.n + t] = lo;
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_check_problems(MeshDev m, const int* cell_problem, DevStatus* st) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < m.e) {
+    const int2 fc = m.face_cells[t];
+    if (cell_problem[fc.x] != cell_problem[fc.y]) record_error(st, 0, RG_ERR_INVALID_ARGUMENT, 0, t, fc.y);
+  }
+}
+
+cudaError_t launch_problems(const MeshDev& m, const int* offsets, int P, int* cell_problem, DevStatus* st,
+                            cudaStream_t s) {
+  const int work = m.n > m.g ? m.n : m.g;
+  k_problems<<<blocks(work > 0 ? work : 1), kBlock, 0, s>>>(m, offsets, P, cell_problem, st);
+  if (m.e > 0) k_check_problems<<<blocks(m.e), kBlock, 0, s>>>(m, cell_problem, st);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_validate(const MeshDev& m, DevStatus* st, cudaStream_t s) {
   int work = m.e > m.n ? m.e : m.n;
@@ -804,7 +879,10 @@ cudaError_t launch_geometry(const GeomArgs& a, cudaStream_t s) {
 
 cudaError_t launch_cfl(const StepArgs& a, cudaStream_t s, bool fill_ghosts) {
   const int total = a.mesh.n + (fill_ghosts ? a.mesh.g : 0);
-  k_cfl<<<blocks(total > 0 ? total : 1), kBlock, 0, s>>>(a, fill_ghosts ? 1 : 0);
+  if (a.cell_problem)
+    k_cfl<true><<<blocks(total > 0 ? total : 1), kBlock, 0, s>>>(a, fill_ghosts ? 1 : 0);
+  else
+    k_cfl<false><<<blocks(total > 0 ? total : 1), kBlock, 0, s>>>(a, fill_ghosts ? 1 : 0);
   return cudaGetLastError();
 }
 
@@ -814,34 +892,51 @@ cudaError_t launch_ghost_fill(const StepArgs& a, cudaStream_t s) {
 }
 
 cudaError_t launch_slopes(const StepArgs& a, cudaStream_t s) {
-  if (a.mesh.n > 0) k_slopes<<<blocks(a.mesh.n), kBlock, 0, s>>>(a);
+  if (a.mesh.n > 0) {
+    if (a.cell_problem)
+      k_slopes<true><<<blocks(a.mesh.n), kBlock, 0, s>>>(a);
+    else
+      k_slopes<false><<<blocks(a.mesh.n), kBlock, 0, s>>>(a);
+  }
   return cudaGetLastError();
 }
 
 cudaError_t launch_faces(const StepArgs& a, cudaStream_t s, bool scaled) {
   if (a.mesh.e == 0) return cudaSuccess;
+  const int nb = blocks(a.mesh.e);
+  const bool b = a.cell_problem != nullptr;
   if (a.order == 1) {
     if (scaled)
-      k_faces_pcm<true><<<blocks(a.mesh.e), kBlock, 0, s>>>(a);
+      b ? k_faces_pcm<true, true><<<nb, kBlock, 0, s>>>(a) : k_faces_pcm<true, false><<<nb, kBlock, 0, s>>>(a);
     else
-      k_faces_pcm<false><<<blocks(a.mesh.e), kBlock, 0, s>>>(a);
+      b ? k_faces_pcm<false, true><<<nb, kBlock, 0, s>>>(a) : k_faces_pcm<false, false><<<nb, kBlock, 0, s>>>(a);
   } else {
     if (scaled)
-      k_faces_lgi<true><<<blocks(a.mesh.e), kBlock, 0, s>>>(a);
+      b ? k_faces_lgi<true, true><<<nb, kBlock, 0, s>>>(a) : k_faces_lgi<true, false><<<nb, kBlock, 0, s>>>(a);
     else
-      k_faces_lgi<false><<<blocks(a.mesh.e), kBlock, 0, s>>>(a);
+      b ? k_faces_lgi<false, true><<<nb, kBlock, 0, s>>>(a) : k_faces_lgi<false, false><<<nb, kBlock, 0, s>>>(a);
   }
   return cudaGetLastError();
 }
 
 cudaError_t launch_update(const StepArgs& a, cudaStream_t s, bool from_unscaled, bool extensive, bool cells) {
-  if (a.mesh.n > 0)
-    k_update<<<blocks(a.mesh.n), kBlock, 0, s>>>(a, from_unscaled ? 1 : 0, extensive ? 1 : 0, cells ? 1 : 0);
+  const int work = a.cell_problem && a.n_problems > a.mesh.n ? a.n_problems : a.mesh.n;
+  if (work > 0) {
+    if (a.cell_problem)
+      k_update<true><<<blocks(work), kBlock, 0, s>>>(a, from_unscaled ? 1 : 0, extensive ? 1 : 0, cells ? 1 : 0);
+    else
+      k_update<false><<<blocks(work), kBlock, 0, s>>>(a, from_unscaled ? 1 : 0, extensive ? 1 : 0, cells ? 1 : 0);
+  }
   return cudaGetLastError();
 }
 
 cudaError_t launch_init_extensives(const StepArgs& a, cudaStream_t s) {
-  if (a.mesh.n > 0) k_init_ext<<<blocks(a.mesh.n), kBlock, 0, s>>>(a);
+  if (a.mesh.n > 0) {
+    if (a.cell_problem)
+      k_init_ext<true><<<blocks(a.mesh.n), kBlock, 0, s>>>(a);
+    else
+      k_init_ext<false><<<blocks(a.mesh.n), kBlock, 0, s>>>(a);
+  }
   return cudaGetLastError();
 }
 

@@ -152,7 +152,32 @@ struct StepArgs {
   double dt_host;       // dt given by the caller (split API)
   int dt_from_device;   // 1: dt = cfl * min from status->dt_min_bits
   int step;             // step number within an rg_run (error ordering)
+  // batch of independent problems (cell_problem == nullptr: one problem)
+  const int* cell_problem;        // n + g: problem of every point
+  const double* gamma_p;          // per problem
+  unsigned long long* dtmin_p;    // per problem CFL minimum (bit pattern), reset by the update
+  double* time_p;                 // per problem simulated time
+  double* dt_p;                   // per problem last dt
+  int n_problems;
 };
+
+#ifdef __CUDACC__
+// Warp-aggregated atomicMin on per-problem minima: one atomic per warp when
+// the warp's cells belong to one problem (the common case: problems are
+// contiguous), one per lane otherwise.  Inactive lanes pass problem -1.
+__device__ __forceinline__ void problem_min(unsigned long long* mins, int problem, unsigned long long bits) {
+  const int p0 = __shfl_sync(0xffffffffu, problem, 0);
+  if (__all_sync(0xffffffffu, problem == p0 || problem < 0)) {
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long ob = __shfl_xor_sync(0xffffffffu, bits, o);
+      bits = ob < bits ? ob : bits;
+    }
+    if ((threadIdx.x & 31) == 0 && p0 >= 0) atomicMin(&mins[p0], bits);
+  } else if (problem >= 0) {
+    atomicMin(&mins[problem], bits);
+  }
+}
+#endif
 
 struct GeomArgs {
   MeshDev mesh;
@@ -175,6 +200,8 @@ struct GeomArgs {
 };
 
 cudaError_t launch_validate(const MeshDev& m, DevStatus* st, cudaStream_t s);
+cudaError_t launch_problems(const MeshDev& m, const int* offsets, int P, int* cell_problem, DevStatus* st,
+                            cudaStream_t s);
 cudaError_t launch_geometry(const GeomArgs& a, cudaStream_t s);
 cudaError_t launch_cfl(const StepArgs& a, cudaStream_t s, bool fill_ghosts);
 cudaError_t launch_ghost_fill(const StepArgs& a, cudaStream_t s);

@@ -114,6 +114,15 @@ __global__ void __launch_bounds__(kBlock) k_flux_to32(const double* f64, float4*
 
 // ------------------------------------------------------------ per step
 
+template <bool kBatch>
+__device__ __forceinline__ float gamma32(const MixedArgs& a, int point) {
+  return kBatch ? a.gamma_p[a.cell_problem[point]] : a.gamma;
+}
+template <bool kBatch>
+__device__ __forceinline__ float inv_gm1_32(const MixedArgs& a, int point) {
+  return kBatch ? a.inv_gm1_p[a.cell_problem[point]] : a.inv_gm1;
+}
+
 // Ghost state: RigidWallGenerator.cpp:5-15 reflection / PeriodicGhostGenerator copy.
 __device__ __forceinline__ void fill_ghost32(const MixedArgs& a, int q) {
   float4 c = a.cells32[a.geom.ghost_real[q]];
@@ -128,13 +137,14 @@ __device__ __forceinline__ void fill_ghost32(const MixedArgs& a, int q) {
 
 // SimpleCFL (simple_cfl.cpp:28-47, 58-71) in FP32.  max_e (c+|v-w_e|)/R is
 // (c + sqrt(max_e |v-w_e|^2))/R: the bound is monotone in |v-w|.
+template <bool kBatch>
 __global__ void __launch_bounds__(kBlock) k_cfl32(MixedArgs a, int fill_ghosts) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const MeshDev& m = a.mesh;
   float x = __int_as_float(0x7f800000);
   if (t < m.n) {
     const float4 c = a.cells32[t];
-    const float cs = sqrtf(a.gamma * c.y / c.x);
+    const float cs = sqrtf(gamma32<kBatch>(a, t) * c.y / c.x);
     float q = 0.0f;
     const int b = m.cell_off[t], e1 = m.cell_off[t + 1];
     for (int k = b; k < e1; ++k) {
@@ -146,6 +156,11 @@ __global__ void __launch_bounds__(kBlock) k_cfl32(MixedArgs a, int fill_ghosts) 
     x = 1.0f / res;
   } else if (fill_ghosts && t < m.n + m.g) {
     fill_ghost32(a, t - m.n);
+  }
+  if (kBatch) {
+    problem_min(a.dtmin_p, t < m.n ? a.cell_problem[t] : -1,
+                static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(x))));
+    return;
   }
   unsigned int bits = __float_as_uint(x);
   for (int o = 16; o > 0; o >>= 1) bits = min(bits, __shfl_xor_sync(0xffffffffu, bits, o));
@@ -196,6 +211,7 @@ __device__ __forceinline__ void shocked32(float dphi, float cv, float cellv, flo
 }
 
 // LinearGaussImproved::calc_slope (LinearGaussImproved.cpp:425-494) in FP32.
+template <bool kBatch>
 __global__ void __launch_bounds__(kBlock) k_slopes32(MixedArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const MeshDev& m = a.mesh;
@@ -233,7 +249,7 @@ __global__ void __launch_bounds__(kBlock) k_slopes32(MixedArgs a) {
             vy.vy * mi.w + vx.vy * mi.z};
   }
   if (a.slf) {
-    const float cs = sqrtf(a.gamma * cell.p / cell.d);
+    const float cs = sqrtf(gamma32<kBatch>(a, i) * cell.p / cell.d);
     bool shock = (sx.vx + sy.vy) * a.g32.width[i] < (-a.delta_v) * cs;
     if (!shock) {
       // min(p, p_k) / max(p, p_k) < delta_p without the division
@@ -354,13 +370,21 @@ __device__ __forceinline__ bool solve32(P6 l, P6 r, float vel, float2 n, float n
   return true;
 }
 
-__device__ __forceinline__ void write32(const MixedArgs& a, int e, const F4& c, bool scaled, float area) {
+template <bool kBatch>
+__device__ __forceinline__ void write32(const MixedArgs& a, int e, int real_side, const F4& c, bool scaled,
+                                        float area) {
   float s = 1.0f;
-  if (scaled) s = a.dt32_from_device ? static_cast<float>(a.status->dt) * area : a.dt32 * area;
+  if (scaled) {
+    if (kBatch)
+      s = static_cast<float>(a.cfl * __longlong_as_double(static_cast<long long>(
+                                          a.dtmin_p[a.cell_problem[real_side]]))) * area;
+    else
+      s = a.dt32_from_device ? static_cast<float>(a.status->dt) * area : a.dt32 * area;
+  }
   a.flux32[e] = make_float4(c.m * s, c.en * s, c.mx * s, c.my * s);
 }
 
-template <bool kScaled>
+template <bool kScaled, bool kBatch>
 __global__ void __launch_bounds__(kBlock) k_faces32_lgi(MixedArgs a) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   const MeshDev& m = a.mesh;
@@ -392,13 +416,14 @@ __global__ void __launch_bounds__(kBlock) k_faces32_lgi(MixedArgs a) {
   const float2 n = a.g32.nrm[e], p = a.g32.par[e];
   const float na = a.g32.nabs[e], pa = a.g32.area[e];
   const float vel = (n.x * w.x + n.y * w.y) / na;
+  const int real_side = fc.x < m.n ? fc.x : fc.y;
+  const float g = gamma32<kBatch>(a, real_side), igm = inv_gm1_32<kBatch>(a, real_side);
   F4 c;
-  if (!solve32(prim32(a.gamma, a.inv_gm1, side[0]), prim32(a.gamma, a.inv_gm1, side[1]), vel, n, na, p, pa, c, a, e))
-    return;
-  write32(a, e, c, kScaled, pa);
+  if (!solve32(prim32(g, igm, side[0]), prim32(g, igm, side[1]), vel, n, na, p, pa, c, a, e)) return;
+  write32<kBatch>(a, e, real_side, c, kScaled, pa);
 }
 
-template <bool kScaled>
+template <bool kScaled, bool kBatch>
 __global__ void __launch_bounds__(kBlock) k_faces32_pcm(MixedArgs a) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   const MeshDev& m = a.mesh;
@@ -415,16 +440,18 @@ __global__ void __launch_bounds__(kBlock) k_faces32_pcm(MixedArgs a) {
     q.vy = p.y * s - q.vy;
     return q;
   };
+  const int real_side = va ? fc.x : fc.y;
+  const float g = gamma32<kBatch>(a, real_side), igm = inv_gm1_32<kBatch>(a, real_side);
   P6 l, r;
   if (!va) {
-    r = prim32(a.gamma, a.inv_gm1, ld4(a.cells32, fc.y));
-    l = oa == ob ? reflect(r) : prim32(a.gamma, a.inv_gm1, ld4(a.cells32, oa));
+    r = prim32(g, igm, ld4(a.cells32, fc.y));
+    l = oa == ob ? reflect(r) : prim32(g, igm, ld4(a.cells32, oa));
   } else if (!vb) {
-    l = prim32(a.gamma, a.inv_gm1, ld4(a.cells32, fc.x));
-    r = oa == ob ? reflect(l) : prim32(a.gamma, a.inv_gm1, ld4(a.cells32, ob));
+    l = prim32(g, igm, ld4(a.cells32, fc.x));
+    r = oa == ob ? reflect(l) : prim32(g, igm, ld4(a.cells32, ob));
   } else {
-    l = prim32(a.gamma, a.inv_gm1, ld4(a.cells32, fc.x));
-    r = prim32(a.gamma, a.inv_gm1, ld4(a.cells32, fc.y));
+    l = prim32(g, igm, ld4(a.cells32, fc.x));
+    r = prim32(g, igm, ld4(a.cells32, fc.y));
   }
   const float2 w = a.ev32[e];
   const float vel = (n.x * w.x + n.y * w.y) / na;
@@ -438,7 +465,7 @@ __global__ void __launch_bounds__(kBlock) k_faces32_pcm(MixedArgs a) {
     c.m = 0.0f;
     c.en = 0.0f;
   }
-  write32(a, e, c, kScaled, pa);
+  write32<kBatch>(a, e, real_side, c, kScaled, pa);
 }
 
 // Error-free FP32 addition (Knuth's TwoSum): s + x == s' + err exactly.
@@ -457,9 +484,16 @@ __device__ __forceinline__ void two_sum(float& s, float& c, float x) {
 // contribution enters its two cells with opposite signs and the extensives
 // keep FP64 precision across steps.  e = E/m - v^2/2 is formed in FP64 with a
 // Newton-refined reciprocal of m.
+template <bool kBatch>
 __global__ void __launch_bounds__(kBlock) k_update_mixed(MixedArgs a, int from_unscaled, int do_ext, int do_cells) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const MeshDev& m = a.mesh;
+  if (kBatch && do_ext && !from_unscaled && i < a.n_problems) {
+    const double dt = a.cfl * __longlong_as_double(static_cast<long long>(a.dtmin_p[i]));
+    a.dt_p[i] = dt;
+    a.time_p[i] += dt;
+    a.dtmin_p[i] = kInfBits;
+  }
   if (i >= m.n) return;
   double2* ext2 = reinterpret_cast<double2*>(a.ext);
   const double2 e01 = ext2[2 * i], e23 = ext2[2 * i + 1];
@@ -513,7 +547,7 @@ __global__ void __launch_bounds__(kBlock) k_update_mixed(MixedArgs a, int from_u
       return;
     }
     (a.cells32_out ? a.cells32_out : a.cells32)[i] =
-        make_float4(d, (a.gamma - 1.0f) * static_cast<float>(energy) * d, static_cast<float>(px * r),
+        make_float4(d, (gamma32<kBatch>(a, i) - 1.0f) * static_cast<float>(energy) * d, static_cast<float>(px * r),
                     static_cast<float>(py * r));
   }
 }
@@ -552,7 +586,10 @@ cudaError_t launch_flux_to32(const double* f64, float4* f32, int n, cudaStream_t
 
 cudaError_t launch_cfl32(const MixedArgs& a, cudaStream_t s, bool fill_ghosts) {
   const int total = a.mesh.n + (fill_ghosts ? a.mesh.g : 0);
-  k_cfl32<<<blocks(total > 0 ? total : 1), kBlock, 0, s>>>(a, fill_ghosts ? 1 : 0);
+  if (a.cell_problem)
+    k_cfl32<true><<<blocks(total > 0 ? total : 1), kBlock, 0, s>>>(a, fill_ghosts ? 1 : 0);
+  else
+    k_cfl32<false><<<blocks(total > 0 ? total : 1), kBlock, 0, s>>>(a, fill_ghosts ? 1 : 0);
   return cudaGetLastError();
 }
 cudaError_t launch_ghost_fill32(const MixedArgs& a, cudaStream_t s) {
@@ -560,27 +597,39 @@ cudaError_t launch_ghost_fill32(const MixedArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 cudaError_t launch_slopes32(const MixedArgs& a, cudaStream_t s) {
-  if (a.mesh.n > 0) k_slopes32<<<blocks(a.mesh.n), kBlock, 0, s>>>(a);
+  if (a.mesh.n > 0) {
+    if (a.cell_problem)
+      k_slopes32<true><<<blocks(a.mesh.n), kBlock, 0, s>>>(a);
+    else
+      k_slopes32<false><<<blocks(a.mesh.n), kBlock, 0, s>>>(a);
+  }
   return cudaGetLastError();
 }
 cudaError_t launch_faces32(const MixedArgs& a, cudaStream_t s, bool scaled) {
   if (a.mesh.e == 0) return cudaSuccess;
+  const int nb = blocks(a.mesh.e);
+  const bool b = a.cell_problem != nullptr;
   if (a.order == 1) {
     if (scaled)
-      k_faces32_pcm<true><<<blocks(a.mesh.e), kBlock, 0, s>>>(a);
+      b ? k_faces32_pcm<true, true><<<nb, kBlock, 0, s>>>(a) : k_faces32_pcm<true, false><<<nb, kBlock, 0, s>>>(a);
     else
-      k_faces32_pcm<false><<<blocks(a.mesh.e), kBlock, 0, s>>>(a);
+      b ? k_faces32_pcm<false, true><<<nb, kBlock, 0, s>>>(a) : k_faces32_pcm<false, false><<<nb, kBlock, 0, s>>>(a);
   } else {
     if (scaled)
-      k_faces32_lgi<true><<<blocks(a.mesh.e), kBlock, 0, s>>>(a);
+      b ? k_faces32_lgi<true, true><<<nb, kBlock, 0, s>>>(a) : k_faces32_lgi<true, false><<<nb, kBlock, 0, s>>>(a);
     else
-      k_faces32_lgi<false><<<blocks(a.mesh.e), kBlock, 0, s>>>(a);
+      b ? k_faces32_lgi<false, true><<<nb, kBlock, 0, s>>>(a) : k_faces32_lgi<false, false><<<nb, kBlock, 0, s>>>(a);
   }
   return cudaGetLastError();
 }
 cudaError_t launch_update_mixed(const MixedArgs& a, cudaStream_t s, bool from_unscaled, bool extensive, bool cells) {
-  if (a.mesh.n > 0)
-    k_update_mixed<<<blocks(a.mesh.n), kBlock, 0, s>>>(a, from_unscaled ? 1 : 0, extensive ? 1 : 0, cells ? 1 : 0);
+  const int work = a.cell_problem && a.n_problems > a.mesh.n ? a.n_problems : a.mesh.n;
+  if (work > 0) {
+    if (a.cell_problem)
+      k_update_mixed<true><<<blocks(work), kBlock, 0, s>>>(a, from_unscaled ? 1 : 0, extensive ? 1 : 0, cells ? 1 : 0);
+    else
+      k_update_mixed<false><<<blocks(work), kBlock, 0, s>>>(a, from_unscaled ? 1 : 0, extensive ? 1 : 0, cells ? 1 : 0);
+  }
   return cudaGetLastError();
 }
 

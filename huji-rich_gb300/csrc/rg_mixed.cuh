@@ -59,6 +59,14 @@ struct MixedArgs {
   float dt32;            // dt given by the caller (split API)
   int dt32_from_device;  // 1: dt from status->dt (fused step)
   int step;
+  // batch of independent problems (cell_problem == nullptr: one problem)
+  const int* cell_problem;
+  const float* gamma_p;     // per problem
+  const float* inv_gm1_p;   // per problem 1/(gamma-1)
+  unsigned long long* dtmin_p;
+  double* time_p;
+  double* dt_p;
+  int n_problems;
 };
 
 cudaError_t launch_geom32(const MixedGeomArgs& a, cudaStream_t s);

@@ -22,7 +22,8 @@ EXPORTS = ("rg_default_config", "rg_create", "rg_destroy", "rg_status_string", "
            "rg_set_extensives", "rg_get_extensives", "rg_set_edge_velocities",
            "rg_device_buffers", "rg_init_extensives", "rg_cfl_dt", "rg_flux", "rg_set_fluxes",
            "rg_extensive_update", "rg_cell_update", "rg_step", "rg_run", "rg_step_async",
-           "rg_synchronize", "rg_step_timed", "rg_cfl_dt_noalloc")
+           "rg_synchronize", "rg_step_timed", "rg_cfl_dt_noalloc", "rg_set_problems",
+           "rg_get_problem_times", "rg_run_graph")
 
 
 class RgDeviceView(C.Structure):
@@ -77,6 +78,9 @@ def load(path=LIB_PATH):
     lib.rg_synchronize.argtypes = [vp, dp]
     lib.rg_step_timed.argtypes = [vp, dp, C.POINTER(C.c_float)]
     lib.rg_cfl_dt_noalloc.argtypes = [C.c_int32, vp, vp, vp, vp, vp, C.c_double, C.c_double, vp, vp]
+    lib.rg_set_problems.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), dp]
+    lib.rg_get_problem_times.argtypes = [vp, dp, dp]
+    lib.rg_run_graph.argtypes = [vp, C.c_int32]
     _lib = lib
     return lib
 
@@ -205,6 +209,26 @@ class Handle:
         ms = (C.c_float * 4)()
         self._check(self.lib.rg_step_timed(self.h, C.byref(dt), ms))
         return dt.value, list(ms)
+
+    # batches ---------------------------------------------------------------
+    def set_problems(self, offsets, gammas):
+        """Declare the uploaded mesh a batch (problem p owns cells
+        offsets[p]:offsets[p+1]) with per-problem gamma."""
+        off = np.ascontiguousarray(offsets, dtype=np.int32)
+        g = np.ascontiguousarray(gammas, dtype=np.float64)
+        assert off.size == g.size + 1
+        self.n_problems = int(g.size)
+        self._check(self.lib.rg_set_problems(self.h, g.size, off.ctypes.data_as(C.POINTER(C.c_int32)),
+                                             dptr(g)))
+
+    def problem_times(self):
+        t = np.empty(self.n_problems)
+        d = np.empty(self.n_problems)
+        self._check(self.lib.rg_get_problem_times(self.h, dptr(t), dptr(d)))
+        return t, d
+
+    def run_graph(self, n_steps):
+        self._check(self.lib.rg_run_graph(self.h, n_steps))
 
     def step_async(self):
         self._check(self.lib.rg_step_async(self.h))

@@ -149,24 +149,19 @@ def lattice_mesh(nx, ny, box=(0.0, 1.0, 0.0, 1.0), boundary="rigid", seed=0, jit
     order = np.lexsort((ea + eb, key2, key1))
     ea, eb, V, ida, idb = ea[order], eb[order], V[order], ida[order], idb[order]
     ne = len(ea)
-    ghost_ext = np.concatenate([np.stack([np.where(ida < 0, ea, -1), np.where(idb < 0, eb, -1)], 1).ravel()])
-    first_seen = {}
-    ghost_pts = []
-    ghost_face = []
-    gflat = ghost_ext
-    for k in np.nonzero(gflat >= 0)[0]:
-        pt = int(gflat[k])
-        if pt not in first_seen:
-            first_seen[pt] = len(ghost_pts)
-            ghost_pts.append(pt)
-            ghost_face.append(k // 2)
+    gflat = np.stack([np.where(ida < 0, ea, -1), np.where(idb < 0, eb, -1)], 1).ravel()
+    pos = np.nonzero(gflat >= 0)[0]
+    uniq, first = np.unique(gflat[pos], return_index=True)
+    order_first = np.argsort(first, kind="stable")       # ghosts in order of first face
+    ghost_pts = uniq[order_first]
+    ghost_face = (pos[first[order_first]] // 2).astype(np.int32)
     g = len(ghost_pts)
     gmap = np.full(NX * NY, -1, dtype=np.int64)
-    gmap[np.array(ghost_pts, dtype=np.int64)] = n + np.arange(g)
+    gmap[ghost_pts.astype(np.int64)] = n + np.arange(g)
     fa = np.where(ida >= 0, ida, gmap[ea])
     fb = np.where(idb >= 0, idb, gmap[eb])
     face_cells = np.stack([fa, fb], 1).astype(np.int32)
-    ghost_pts = np.array(ghost_pts, dtype=np.int64)
+    ghost_pts = ghost_pts.astype(np.int64)
     point_xy = np.zeros((n + g, 2))
     point_xy[:n, 0] = px.ravel()
     point_xy[:n, 1] = py.ravel()
@@ -181,9 +176,9 @@ def lattice_mesh(nx, ny, box=(0.0, 1.0, 0.0, 1.0), boundary="rigid", seed=0, jit
     sc, sf = side_cell[real_side], side_face[real_side]
     o = np.lexsort((sf, sc))
     sc, sf = sc[o], sf[o]
-    offset = np.zeros(n + 1, dtype=np.int32)
-    np.add.at(offset, sc + 1, 1)
-    offset = np.cumsum(offset).astype(np.int32)
+    offset = np.zeros(n + 1, dtype=np.int64)
+    offset[1:] = np.cumsum(np.bincount(sc, minlength=n))
+    offset = offset.astype(np.int32)
     cell_faces = sf.astype(np.int32)
 
     # volumes and centres of mass with the reference formulas
@@ -192,19 +187,15 @@ def lattice_mesh(nx, ny, box=(0.0, 1.0, 0.0, 1.0), boundary="rigid", seed=0, jit
     xc = point_xy[sc]
     p1, p2 = v0 - xc, v1 - xc
     tri_area = 0.5 * np.abs(p1[:, 0] * p2[:, 1] + p1[:, 1] * (-p2[:, 0]))
-    volume = np.zeros(n)
-    np.add.at(volume, sc, tri_area)
+    volume = np.bincount(sc, weights=tri_area, minlength=n)
     anchor = V[cell_faces[offset[:-1]], 0:2][sc]
     q1, q2 = v0 - anchor, v1 - anchor
     first = np.zeros(len(sc), dtype=bool)
     first[offset[:-1]] = True
     a2 = np.where(first, 0.0, 0.5 * np.abs(q1[:, 0] * q2[:, 1] + q1[:, 1] * (-q2[:, 0])))
-    cd_volume = np.zeros(n)
-    np.add.at(cd_volume, sc, a2)
-    pcx = np.zeros(n)
-    pcy = np.zeros(n)
-    np.add.at(pcx, sc, (a2 / 3.0) * (anchor[:, 0] + v0[:, 0] + v1[:, 0]))
-    np.add.at(pcy, sc, (a2 / 3.0) * (anchor[:, 1] + v0[:, 1] + v1[:, 1]))
+    cd_volume = np.bincount(sc, weights=a2, minlength=n)
+    pcx = np.bincount(sc, weights=(a2 / 3.0) * (anchor[:, 0] + v0[:, 0] + v1[:, 0]), minlength=n)
+    pcy = np.bincount(sc, weights=(a2 / 3.0) * (anchor[:, 1] + v0[:, 1] + v1[:, 1]), minlength=n)
     cm = np.zeros((n + g, 2))
     cm[:n, 0] = pcx / cd_volume
     cm[:n, 1] = pcy / cd_volume
@@ -296,3 +287,81 @@ def face_velocities(mesh, point_velocities, stationary_box=True):
     if stationary_box:
         w[oa == ob] = 0.0
     return np.ascontiguousarray(w)
+
+
+# ------------------------------------------------------------------ batches
+
+def concat_meshes(meshes):
+    """Disjoint union of packed meshes: real cells of every problem first (in
+    problem order), then every problem's ghosts; faces in problem order.
+    Returns the mesh and the problem cell-offset table."""
+    from meshview import PackedMesh
+    ns = np.array([m.n_cells for m in meshes])
+    gs = np.array([m.n_ghosts for m in meshes])
+    es = np.array([m.n_faces for m in meshes])
+    cell_base = np.concatenate([[0], np.cumsum(ns)])
+    N = int(cell_base[-1])
+    ghost_base = N + np.concatenate([[0], np.cumsum(gs)])
+    face_base = np.concatenate([[0], np.cumsum(es)])
+    fc, fv, pts_r, pts_g, cm_r, cm_g, gsrc, gface, offs, cf = ([] for _ in range(10))
+    vol, cdv = [], []
+    for k, m in enumerate(meshes):
+        f = m.face_cells.astype(np.int64)
+        f = np.where(f < m.n_cells, f + cell_base[k], f - m.n_cells + ghost_base[k])
+        fc.append(f)
+        fv.append(m.face_vertices)
+        pts_r.append(m.point_xy[:m.n_cells])
+        pts_g.append(m.point_xy[m.n_cells:])
+        cm_r.append(m.cm_xy[:m.n_cells])
+        cm_g.append(m.cm_xy[m.n_cells:])
+        vol.append(m.volume)
+        cdv.append(m.cd_volume)
+        gsrc.append(m.ghost_source.astype(np.int64) + cell_base[k])
+        gface.append(np.where(m.ghost_face >= 0, m.ghost_face.astype(np.int64) + face_base[k], -1))
+        offs.append(m.cell_face_offset[1:].astype(np.int64) + (0 if k == 0 else offs_total))
+        offs_total = int(offs[-1][-1])
+        cf.append(m.cell_faces.astype(np.int64) + face_base[k])
+    mesh = PackedMesh(point_xy=np.concatenate(pts_r + pts_g), cm_xy=np.concatenate(cm_r + cm_g),
+                      volume=np.concatenate(vol), cd_volume=np.concatenate(cdv),
+                      ghost_source=np.concatenate(gsrc), ghost_face=np.concatenate(gface),
+                      face_cells=np.concatenate(fc), face_vertices=np.concatenate(fv),
+                      cell_face_offset=np.concatenate([[0]] + offs), cell_faces=np.concatenate(cf))
+    return mesh, cell_base.astype(np.int32)
+
+
+def riemann_batch(n_problems=512, seed=11, min_cells=1024, max_cells=65536, jitter=1e-3):
+    """Independent 2D Riemann problems on [0,1]^2 with rigid walls: cell
+    counts log-uniform in [min_cells, max_cells] (square lattices), left and
+    right states split by a random line through the centre, density and
+    pressure log-uniform in [0.1, 10], velocities uniform in [-1, 1]^2,
+    gamma 1.4 or 5/3.  Returns (mesh, problem offsets, gammas, cells)."""
+    meshes, states, gammas = [], [], []
+    for p in range(n_problems):
+        m, c, g = riemann_problem(p, seed, min_cells, max_cells, jitter)
+        meshes.append(m)
+        states.append(c)
+        gammas.append(g)
+    mesh, offsets = concat_meshes(meshes)
+    return mesh, offsets, np.array(gammas), np.concatenate(states), meshes
+
+
+def riemann_problem(p, seed=11, min_cells=1024, max_cells=65536, jitter=1e-3):
+    """Problem p of riemann_batch on its own: (mesh, cells, gamma)."""
+    rng = np.random.default_rng([seed, p])
+    count = np.exp(rng.uniform(np.log(min_cells), np.log(max_cells)))
+    side = max(4, int(round(np.sqrt(count))))
+    m = lattice_mesh(side, side, (0.0, 1.0, 0.0, 1.0), "rigid", seed=seed * 100003 + p, jitter=jitter)
+    ang = rng.uniform(0, 2 * np.pi)
+    nrm = np.array([np.cos(ang), np.sin(ang)])
+    x = m.point_xy[:m.n_cells] - 0.5
+    left = x @ nrm < 0
+    rho = np.exp(rng.uniform(np.log(0.1), np.log(10.0), 2))
+    prs = np.exp(rng.uniform(np.log(0.1), np.log(10.0), 2))
+    vel = rng.uniform(-1.0, 1.0, (2, 2))
+    c = np.zeros((m.n_cells, 4))
+    c[:, 0] = np.where(left, rho[0], rho[1])
+    c[:, 1] = np.where(left, prs[0], prs[1])
+    c[:, 2] = np.where(left, vel[0, 0], vel[1, 0])
+    c[:, 3] = np.where(left, vel[0, 1], vel[1, 1])
+    gamma = 1.4 if rng.uniform() < 0.5 else 5.0 / 3.0
+    return m, c, gamma

@@ -222,6 +222,29 @@ rg_status rg_step_async(rg_handle* h);
  * steps and the dt of the last one (dt_last may be NULL). */
 rg_status rg_synchronize(rg_handle* h, double* dt_last);
 
+/* Batches of independent problems ----------------------------------------- */
+/* No counterpart in the reference (its hdsim runs one problem; this is the
+ * batched form of the path).  Declares the uploaded mesh a batch: problem p
+ * owns the real cells [problem_cell_offset[p], problem_cell_offset[p+1]) and
+ * the ghosts and faces that touch them (a face joining two problems is
+ * rejected).  Each problem has its own IdealGas index gamma[p] and, in
+ * rg_step / rg_run / rg_run_graph, its own SimpleCFL dt and simulated time;
+ * every problem advances one step per step.  n_problems = 0 returns to one
+ * problem.  Call after rg_upload_mesh (an upload drops the table).  Only the
+ * fused steps and the state transfers are available in batch mode (rg_cfl_dt
+ * returns RG_ERR_INVALID_ARGUMENT); TimeAdvance2Heun is not. */
+rg_status rg_set_problems(rg_handle* h, int32_t n_problems, const int32_t* problem_cell_offset,
+                          const double* gamma);
+/* Per-problem simulated time (sum of its dts since rg_set_problems) and last
+ * dt (n_problems doubles each; either may be NULL). */
+rg_status rg_get_problem_times(rg_handle* h, double* time_out, double* dt_last_out);
+
+/* n_steps fused steps replayed from a CUDA graph of one step (captured on
+ * first use and after every upload or configuration change), one host
+ * synchronisation at the end.  Same results as rg_run; a failure is reported
+ * with step 0 in its key. */
+rg_status rg_run_graph(rg_handle* h, int32_t n_steps);
+
 /* Allocation-free time step ----------------------------------------------- */
 /* No counterpart in the reference.  The SimpleCFL dt of rg_cfl_dt for callers
  * that may not allocate device memory (hosts whose own allocator or arena

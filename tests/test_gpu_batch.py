@@ -1,0 +1,112 @@
+"""Batched form: independent problems of uneven size in one handle, each with
+its own gamma and SimpleCFL dt, advanced by one launch per phase.  Every
+problem of a batch must evolve exactly as it does alone (FP64: bit-for-bit,
+and the same for the FP32-mixed path, whose kernels are per cell and per
+face too), and a CUDA-graph replay must equal rg_run."""
+import numpy as np
+import pytest
+
+import oracle
+import richgpu
+import synthetic
+from test_oracle_golden import accumulate, exact
+
+pytestmark = pytest.mark.gpu
+
+
+def small_batch(seed=5, n=12):
+    return synthetic.riemann_batch(n, seed=seed, min_cells=64, max_cells=2500)
+
+
+def init_ext(mesh, cells, offsets, gammas):
+    ext = np.empty_like(cells)
+    for p in range(len(gammas)):
+        a, b = offsets[p], offsets[p + 1]
+        sub = oracle.init_extensives(mesh, cells, gammas[p])
+        ext[a:b] = sub[a:b]
+    return ext
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batch_equals_problems_alone(precision):
+    mesh, off, gam, cells, meshes = small_batch()
+    ext = init_ext(mesh, cells, off, gam)
+    steps = 15
+    with richgpu.Handle(gamma=1.4, order=2, ghost_kind=0, precision=precision, device=0) as h:
+        h.upload_mesh(mesh)
+        h.set_problems(off, gam)
+        h.set_cells(cells)
+        h.set_extensives(ext)
+        h.set_edge_velocities(np.zeros((mesh.n_faces, 2)))
+        h.run(steps)
+        bc, be = h.get_cells(), h.get_extensives()
+        times, last = h.problem_times()
+    for p, m in enumerate(meshes):
+        a, b = off[p], off[p + 1]
+        with richgpu.Handle(gamma=gam[p], order=2, ghost_kind=0, precision=precision, device=0) as h:
+            h.upload_mesh(m)
+            h.set_cells(cells[a:b])
+            h.set_extensives(ext[a:b])
+            h.set_edge_velocities(np.zeros((m.n_faces, 2)))
+            dts = h.run(steps)
+            exact(bc[a:b], h.get_cells())
+            exact(be[a:b], h.get_extensives())
+        assert times[p] == accumulate(0.0, dts)[-1]
+        assert last[p] == dts[-1]
+
+
+def test_batch_fp64_matches_oracle_per_problem():
+    mesh, off, gam, cells, meshes = small_batch(seed=9, n=6)
+    ext = init_ext(mesh, cells, off, gam)
+    with richgpu.Handle(gamma=1.4, order=2, ghost_kind=0, device=0) as h:
+        h.upload_mesh(mesh)
+        h.set_problems(off, gam)
+        h.set_cells(cells)
+        h.set_extensives(ext)
+        h.set_edge_velocities(np.zeros((mesh.n_faces, 2)))
+        h.run(5)
+        bc = h.get_cells()
+    for p, m in enumerate(meshes):
+        a, b = off[p], off[p + 1]
+        oc, _, _ = oracle.run(m, cells[a:b], ext[a:b], np.zeros((m.n_faces, 2)), gam[p], 5, 0.3, 2,
+                              oracle.lgi_params(0))
+        exact(bc[a:b], oc)
+
+
+@pytest.mark.parametrize("batch", [False, True])
+def test_graph_replay_equals_run(batch):
+    if batch:
+        mesh, off, gam, cells, _ = small_batch(seed=2, n=8)
+        ext = init_ext(mesh, cells, off, gam)
+    else:
+        mesh = synthetic.lattice_mesh(96, 96, (-1.0, 1.0, -1.0, 1.0), "rigid", seed=2)
+        cells = synthetic.sedov_cells(mesh)
+        ext = oracle.init_extensives(mesh, cells, 5 / 3)
+    out = []
+    for graph in (False, True):
+        with richgpu.Handle(gamma=5 / 3, order=2, ghost_kind=0, device=0) as h:
+            h.upload_mesh(mesh)
+            if batch:
+                h.set_problems(off, gam)
+            h.set_cells(cells)
+            h.set_extensives(ext)
+            h.set_edge_velocities(np.zeros((mesh.n_faces, 2)))
+            if graph:
+                h.run_graph(12)
+            else:
+                h.run(12)
+            out.append((h.get_cells(), h.get_extensives()))
+    exact(out[0][0], out[1][0])
+    exact(out[0][1], out[1][1])
+
+
+def test_batch_rejects_face_between_problems():
+    mesh = synthetic.lattice_mesh(16, 16, (0.0, 1.0, 0.0, 1.0), "rigid", seed=1)
+    with richgpu.Handle(gamma=1.4, order=2, ghost_kind=0, device=0) as h:
+        h.upload_mesh(mesh)
+        with pytest.raises(richgpu.RichError) as ei:
+            h.set_problems([0, 100, mesh.n_cells], [1.4, 1.4])   # cuts through the lattice
+        assert ei.value.status == 1
+        h.set_problems([0, mesh.n_cells], [1.4])
+        with pytest.raises(richgpu.RichError):
+            h.cfl_dt()                                       # not available in batch mode
