@@ -359,6 +359,7 @@ def run_gpu(args, world, rank, local_rank):
         cpu = {"value": n * kc / tc, "unit": UNIT, "cores": 1, "kind": "port",
                "sample": f"{kc} steps of the same {NX}x{NY} workload (FP64), one thread, C restatement "
                          "oracle/rich_oracle.c (gcc -O2); the reference itself is serial"}
+    adjoint = adjoint_block() if rank == 0 and not args.no_adjoint else None
     if rank == 0:
         line = {"metric": METRIC, "value": value32, "unit": UNIT, "n_gpus": world, "steps": k,
                 "warmup": r32["warmup"], "ms_per_step": r32["total_ms"] / k, "higher_is_better": True,
@@ -381,10 +382,61 @@ def run_gpu(args, world, rank, local_rank):
                                  "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
                          "clocks": r64["clock"]},
                 "speedup_fp32mixed_vs_fp64": value32 / value64,
+                "adjoint": adjoint,
                 "wall_s_timed_region": r32["wall"] + r64["wall"]}
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+# ------------------------------------------------------------------ adjoint
+
+def adjoint_block(reps=3):
+    """Differentiation form on its own workload: 256x256 periodic lattice,
+    rho = 1 + 8 Gaussian bumps, p = 1, velocity from 16 Fourier modes,
+    gamma 5/3, LinearGaussImproved + Hllc, 200 steps at the initial CFL-0.3
+    dt, loss = L2 of the final density against a second seeded field,
+    checkpoints every 20 steps.  Forward = rg_step_fwd, backward =
+    rg_step_bwd (seed upload, recomputation, reverse sweep, gradient
+    download), each a synchronous C-ABI call timed on the host; the cost
+    ratio is backward over forward.  The dot-product residual compares the
+    adjoint with one tangent-linear run."""
+    import richgpu
+    import synthetic
+    mesh = synthetic.lattice_mesh(256, 256, (0.0, 1.0, 0.0, 1.0), "periodic", seed=3)
+    cells = synthetic.bumps_cells(mesh)
+    target = synthetic.bumps_cells(mesh, seed=11)[:, 0]
+    steps, every = 200, 20
+    with richgpu.Handle(gamma=GAMMA, order=2, ghost_kind=1, device=0) as h:
+        h.upload_mesh(mesh)
+        h.set_edge_velocities(np.zeros((mesh.n_faces, 2)))
+        h.set_cells(cells)
+        dt = h.cfl_dt()
+        fwd_ms, bwd_ms = [], []
+        for _ in range(reps + 1):
+            h.set_cells(cells)
+            t0 = time.perf_counter()
+            h.step_fwd(steps, dt, every)
+            t1 = time.perf_counter()
+            wn = h.get_cells()
+            seed = np.zeros_like(wn)
+            seed[:, 0] = 2.0 * (wn[:, 0] - target)
+            t2 = time.perf_counter()
+            g = h.step_bwd(seed)
+            t3 = time.perf_counter()
+            fwd_ms.append((t1 - t0) * 1e3)
+            bwd_ms.append((t3 - t2) * 1e3)
+        fwd_ms, bwd_ms = fwd_ms[1:], bwd_ms[1:]
+        dw = np.random.default_rng(1).normal(size=cells.shape)
+        h.set_cells(cells)
+        tl = h.step_tlm(steps, dt, dw)
+        lhs, rhs = float(np.sum(seed * tl)), float(np.sum(g * dw))
+    f, b = statistics.median(fwd_ms), statistics.median(bwd_ms)
+    return {"workload": "periodic_bumps_256x256_lgi_hllc_fp64_200steps_fixed_dt", "cells": mesh.n_cells,
+            "steps": steps, "checkpoint_every": every, "fwd_ms": f, "bwd_ms": b, "adjoint_over_fwd": b / f,
+            "fwd_cell_updates_per_s": mesh.n_cells * steps / (f * 1e-3),
+            "dot_product_rel": abs(lhs - rhs) / abs(lhs),
+            "timing": "host wall clock around synchronous C-ABI calls, median of %d" % reps}
 
 
 # ------------------------------------------------------------------ batch
@@ -496,6 +548,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint cost measurement")
     ap.add_argument("--workload", default="sedov", choices=["sedov", "riemann_batch"])
     ap.add_argument("--problems", type=int, default=512)
     args = ap.parse_args()

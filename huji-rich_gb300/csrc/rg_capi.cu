@@ -20,163 +20,13 @@
 #include <thread>
 #include <vector>
 
-#include "rg_internal.cuh"
-#include "rg_mixed.cuh"
+#include "rg_handle.cuh"
 
 using rg::DevStatus;
 
-namespace {
+using namespace rgh;
 
-constexpr size_t kAlign = 256;
-inline size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
-
-struct DevBuf {
-  void* p = nullptr;
-  size_t bytes = 0;
-  cudaError_t ensure(size_t want) {
-    if (want <= bytes) return cudaSuccess;
-    if (p) cudaFree(p);
-    p = nullptr;
-    bytes = 0;
-    cudaError_t e = cudaMalloc(&p, want);
-    if (e == cudaSuccess) bytes = want;
-    return e;
-  }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    bytes = 0;
-  }
-};
-
-struct HostBuf {
-  void* p = nullptr;
-  size_t bytes = 0;
-  cudaError_t ensure(size_t want) {
-    if (want <= bytes) return cudaSuccess;
-    if (p) cudaFreeHost(p);
-    p = nullptr;
-    bytes = 0;
-    cudaError_t e = cudaHostAlloc(&p, want, cudaHostAllocDefault);
-    if (e == cudaSuccess) bytes = want;
-    return e;
-  }
-  void release() {
-    if (p) cudaFreeHost(p);
-    p = nullptr;
-    bytes = 0;
-  }
-};
-
-// Offsets of every array of one mesh slot inside one allocation.  The input
-// arrays come first and form one contiguous block, mirrored byte for byte by
-// the pinned staging buffer so that one copy moves the whole mesh.
-struct SlotLayout {
-  size_t points, cms, volume, cd_volume, ghost_source, ghost_face, face_cells, face_vertices, cell_off,
-      cell_faces, input_end;
-  size_t area, nrm, nabs, par, dm0, dm1, width, minv, cflags, nbr, hr, ghost_real, ghost_unit;
-  size_t nrm32, nabs32, par32, area32, dm0_32, dm1_32, width32, minv32, hr32, gunit32, icdv32, total;
-  void compute(int n, int g, int e, int m, bool mixed) {
-    const size_t np = static_cast<size_t>(n) + g;
-    size_t o = 0;
-    auto take = [&o](size_t bytes) {
-      const size_t at = o;
-      o = align_up(o + bytes);
-      return at;
-    };
-    points = take(16 * np);
-    cms = take(16 * np);
-    volume = take(8 * static_cast<size_t>(n));
-    cd_volume = take(8 * static_cast<size_t>(n));
-    ghost_source = take(4 * static_cast<size_t>(g));
-    ghost_face = take(4 * static_cast<size_t>(g));
-    face_cells = take(8 * static_cast<size_t>(e));
-    face_vertices = take(32 * static_cast<size_t>(e));
-    cell_off = take(4 * (static_cast<size_t>(n) + 1));
-    cell_faces = take(4 * static_cast<size_t>(m));
-    input_end = o;
-    area = take(8 * static_cast<size_t>(e));
-    nrm = take(16 * static_cast<size_t>(e));
-    nabs = take(8 * static_cast<size_t>(e));
-    par = take(16 * static_cast<size_t>(e));
-    dm0 = take(16 * static_cast<size_t>(e));
-    dm1 = take(16 * static_cast<size_t>(e));
-    width = take(8 * static_cast<size_t>(n));
-    minv = take(32 * static_cast<size_t>(n));
-    cflags = take(4 * static_cast<size_t>(n));
-    nbr = take(4 * static_cast<size_t>(m));
-    hr = take(16 * static_cast<size_t>(m));
-    ghost_real = take(4 * static_cast<size_t>(g));
-    ghost_unit = take(16 * static_cast<size_t>(g));
-    const size_t k = mixed ? 1 : 0;  // FP32 copies only for the mixed path
-    nrm32 = take(k * 8 * static_cast<size_t>(e));
-    nabs32 = take(k * 4 * static_cast<size_t>(e));
-    par32 = take(k * 8 * static_cast<size_t>(e));
-    area32 = take(k * 4 * static_cast<size_t>(e));
-    dm0_32 = take(k * 8 * static_cast<size_t>(e));
-    dm1_32 = take(k * 8 * static_cast<size_t>(e));
-    width32 = take(k * 4 * static_cast<size_t>(n));
-    minv32 = take(k * 16 * static_cast<size_t>(n));
-    hr32 = take(k * 8 * static_cast<size_t>(m));
-    gunit32 = take(k * 8 * static_cast<size_t>(g));
-    icdv32 = take(k * 4 * static_cast<size_t>(n));
-    total = o;
-  }
-};
-
-struct MeshSlot {
-  int n = 0, g = 0, e = 0, m = 0;
-  bool valid = false;
-  DevBuf buf;
-  SlotLayout lay;
-  rg::MeshDev mesh{};
-  rg::GeomDev geom{};
-  rg::MixedGeom g32{};
-  rg_error geom_error{};  // reconstruction failure found by the geometry pass
-  cudaEvent_t last_use = nullptr;
-};
-
-template <class T>
-T* at(void* base, size_t off) {
-  return reinterpret_cast<T*>(static_cast<char*>(base) + off);
-}
-
-}  // namespace
-
-struct rg_handle {
-  rg_config cfg{};
-  cudaStream_t stream = nullptr;
-  cudaStream_t upload_stream = nullptr;
-  cudaEvent_t ev_up0 = nullptr, ev_up1 = nullptr;
-  cudaEvent_t ev_k[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-  MeshSlot slots[2];
-  int active = -1;
-  // state
-  DevBuf cells, ext, ev, slopes, fluxes, status_buf;
-  // FP32-mixed path: FP32 primitives (n + g records), slopes, face fluxes, edge velocities
-  DevBuf cells32, slopes32, flux32, ev32;
-  bool mixed = false;
-  // Heun mid stage: extensives and cells after the first flux pass
-  DevBuf mid_ext, mid_cells, mid_cells32;
-  bool heun = false;
-  // batch of independent problems (n_problems == 0: one problem)
-  int n_problems = 0;
-  DevBuf cell_problem, problem_offsets, gamma_p, gamma32_p, inv_gm1_32_p, dtmin_p, time_p, dt_p;
-  // CUDA graph of one fused step
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t graph_exec = nullptr;
-  size_t cells_records = 0;
-  bool have_cells = false, have_ext = false, have_ev = false, have_fluxes = false;
-  HostBuf staging, host_status, host_dts;
-  DevStatus* d_status = nullptr;
-  DevStatus* d_geom_status = nullptr;
-  rg_error last{};
-  double last_upload_ms = 0;
-  double last_dt = 0;
-  int step_seq = 0;
-};
-
-namespace {
+namespace rgh {
 
 rg_status cuda_fail(rg_handle* h, cudaError_t e) {
   if (h) {
@@ -191,16 +41,9 @@ rg_status invalid(rg_handle* h, int64_t index, double value) {
   return RG_ERR_INVALID_ARGUMENT;
 }
 
-#define RG_CUDA(h, call)                            \
-  do {                                              \
-    cudaError_t e_ = (call);                        \
-    if (e_ != cudaSuccess) return cuda_fail(h, e_); \
-  } while (0)
-#define RG_TRY(call)                  \
-  do {                                \
-    rg_status s_ = (call);            \
-    if (s_ != RG_OK) return s_;       \
-  } while (0)
+}  // namespace rgh
+
+namespace {
 
 // Host-side checks of a packed mesh view that need no O(size) pass: counts,
 // pointers and the CSR length.  Every index is checked on the device
@@ -290,6 +133,10 @@ void fill_views(MeshSlot& s) {
   s.g32.inv_cd_volume = at<float>(b, L.icdv32);
 }
 
+}  // namespace
+
+namespace rgh {
+
 rg_status reset_status(rg_handle* h, DevStatus* st, cudaStream_t s) {
   // error part only: err_key = ~0, err_status = lock = 0
   RG_CUDA(h, cudaMemsetAsync(&st->err_key, 0xff, sizeof(unsigned long long), s));
@@ -349,6 +196,10 @@ rg::StepArgs step_args(rg_handle* h) {
   return a;
 }
 
+}  // namespace rgh
+
+namespace {
+
 rg::MixedArgs mixed_args(rg_handle* h) {
   MeshSlot* s = active_slot(h);
   rg::MixedArgs a{};
@@ -392,6 +243,10 @@ void drop_graph(rg_handle* h) {
   h->graph = nullptr;
 }
 
+}  // namespace
+
+namespace rgh {
+
 rg_status require(rg_handle* h, bool cells, bool ext, bool ev, bool fluxes) {
   if (!h) return RG_ERR_INVALID_ARGUMENT;
   if (h->active < 0 || (cells && !h->have_cells) || (ext && !h->have_ext) || (ev && !h->have_ev) ||
@@ -410,6 +265,10 @@ rg_status mesh_error(rg_handle* h) {
   }
   return RG_OK;
 }
+
+}  // namespace rgh
+
+namespace {
 
 // hdsim::TimeAdvance2Heun on a fixed mesh (hdsim2d.cpp:323-449): dt once;
 // pass 1 on the cells writes the mid extensives and mid cells; pass 2 on the
@@ -612,6 +471,7 @@ rg_status rg_destroy(rg_handle* h) {
     s.buf.release();
     if (s.last_use) cudaEventDestroy(s.last_use);
   }
+  adjoint_release(h);
   h->cells.release();
   h->ext.release();
   h->ev.release();
@@ -813,9 +673,11 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t /*flags*/
   s.geom_error = rg_error{};
   if (hs->err_key != ~0ull)
     s.geom_error = rg_error{hs->err_status, 2, static_cast<int64_t>(hs->err_key & rg::kKeyIndexMask), hs->err_value};
-  // a new mesh drops the batch table and the captured step
+  // a new mesh drops the batch table, the captured step and the
+  // differentiation buffers
   h->n_problems = 0;
   drop_graph(h);
+  adjoint_release(h);
   // later compute work on the stream sees the new slot
   RG_CUDA(h, cudaStreamWaitEvent(h->stream, h->ev_up1, 0));
   if (h->active >= 0) RG_CUDA(h, cudaEventRecord(h->slots[h->active].last_use, h->stream));

@@ -25,6 +25,9 @@ UNITS = {
     "rg_capi.cu": [],
     "rg_mixed.cu": [],
     "rg_noalloc.cu": ["--fmad=false"],
+    "rg_adjoint.cu": ["--fmad=false"],
+    "rg_adjoint_rev.cu": [],
+    "rg_adjoint_api.cu": [],
 }
 
 

@@ -23,7 +23,7 @@ EXPORTS = ("rg_default_config", "rg_create", "rg_destroy", "rg_status_string", "
            "rg_device_buffers", "rg_init_extensives", "rg_cfl_dt", "rg_flux", "rg_set_fluxes",
            "rg_extensive_update", "rg_cell_update", "rg_step", "rg_run", "rg_step_async",
            "rg_synchronize", "rg_step_timed", "rg_cfl_dt_noalloc", "rg_set_problems",
-           "rg_get_problem_times", "rg_run_graph")
+           "rg_get_problem_times", "rg_run_graph", "rg_step_fwd", "rg_step_bwd", "rg_step_tlm")
 
 
 class RgDeviceView(C.Structure):
@@ -81,6 +81,9 @@ def load(path=LIB_PATH):
     lib.rg_set_problems.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), dp]
     lib.rg_get_problem_times.argtypes = [vp, dp, dp]
     lib.rg_run_graph.argtypes = [vp, C.c_int32]
+    lib.rg_step_fwd.argtypes = [vp, C.c_int32, C.c_double, C.c_int32]
+    lib.rg_step_bwd.argtypes = [vp, dp, dp]
+    lib.rg_step_tlm.argtypes = [vp, C.c_int32, C.c_double, dp, dp]
     _lib = lib
     return lib
 
@@ -237,3 +240,24 @@ class Handle:
         dt = C.c_double()
         self._check(self.lib.rg_synchronize(self.h, C.byref(dt)))
         return dt.value
+
+    # differentiation (fixed dt, periodic LinearGaussImproved + Hllc, FP64)
+    def step_fwd(self, n_steps, dt, checkpoint_every=20):
+        """n_steps fixed-dt steps from the handle's cells, recorded for step_bwd."""
+        self._check(self.lib.rg_step_fwd(self.h, n_steps, dt, checkpoint_every))
+
+    def step_bwd(self, cells_bar):
+        """dL/d(initial cells) from dL/d(final cells) of the last step_fwd."""
+        a = np.ascontiguousarray(cells_bar, dtype=np.float64)
+        assert a.size == 4 * self.mesh.n_cells
+        out = np.empty((self.mesh.n_cells, 4))
+        self._check(self.lib.rg_step_bwd(self.h, dptr(a), dptr(out)))
+        return out
+
+    def step_tlm(self, n_steps, dt, dcells0):
+        """Tangent of the final cells along dcells0 (the handle ends at W_n)."""
+        a = np.ascontiguousarray(dcells0, dtype=np.float64)
+        assert a.size == 4 * self.mesh.n_cells
+        out = np.empty((self.mesh.n_cells, 4))
+        self._check(self.lib.rg_step_tlm(self.h, n_steps, dt, dptr(a), dptr(out)))
+        return out

@@ -245,6 +245,31 @@ rg_status rg_get_problem_times(rg_handle* h, double* time_out, double* dt_last_o
  * with step 0 in its key. */
 rg_status rg_run_graph(rg_handle* h, int32_t n_steps);
 
+/* Differentiation --------------------------------------------------------- */
+/* No counterpart in the reference (it has no differentiation).  The map
+ * differentiated is n_steps hdsim::TimeAdvance steps (hdsim2d.cpp:149-241)
+ * with a FIXED dt on the uploaded mesh: U_0 = init_extensives(W_0),
+ * U_{k+1} = U_k + dt-scaled flux gather of W_k, W_{k+1} = SimpleCellUpdater
+ * (U_{k+1}), W the cells.  Requires order 2 (LinearGaussImproved + Hllc),
+ * periodic ghosts, FP64 and one problem; anything else returns
+ * RG_ERR_INVALID_ARGUMENT.  Branches (limiter candidates, neighbour max/min,
+ * HLLC wave speeds and region) are those of the forward values.
+ *
+ * rg_step_fwd: from the handle's cells W_0 runs n_steps, keeping W and U
+ * every checkpoint_every steps on the device; afterwards the handle holds
+ * W_n and U_n as rg_run leaves them (same values bit for bit as the plain
+ * FP64 step with that dt).
+ * rg_step_bwd: given cells_bar = dL/dW_n (host, n_cells*4) returns
+ * cells0_bar = dL/dW_0 (host, n_cells*4) for the last rg_step_fwd,
+ * recomputing each checkpoint interval forward once.  The handle's state is
+ * left as rg_step_fwd left it.
+ * rg_step_tlm: tangent-linear run: from W_0 (the handle's cells) and a
+ * tangent dcells0 (host, n_cells*4) runs n_steps and returns the tangent of
+ * W_n in dcells (host, n_cells*4); the handle then holds W_n and U_n. */
+rg_status rg_step_fwd(rg_handle* h, int32_t n_steps, double dt, int32_t checkpoint_every);
+rg_status rg_step_bwd(rg_handle* h, const double* cells_bar, double* cells0_bar);
+rg_status rg_step_tlm(rg_handle* h, int32_t n_steps, double dt, const double* dcells0, double* dcells);
+
 /* Allocation-free time step ----------------------------------------------- */
 /* No counterpart in the reference.  The SimpleCFL dt of rg_cfl_dt for callers
  * that may not allocate device memory (hosts whose own allocator or arena

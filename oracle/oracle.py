@@ -155,3 +155,18 @@ def run(mesh, cells, ext, ev, gamma, steps, cfl_number=0.3, order=2, lp=None, he
         cells, ext, dt = step(mesh, cells, ext, ev, gamma, cfl_number, order, lp, heun)
         dts.append(dt)
     return cells, ext, np.array(dts)
+
+
+def run_fixed_dt(mesh, cells, gamma, steps, dt, lp=None):
+    """hdsim::TimeAdvance with a fixed dt on a mesh at rest, composed from
+    the plugin operations (init_extensives, ModularFluxCalculator with
+    LinearGaussImproved, SimpleExtensiveUpdater, SimpleCellUpdater); returns
+    (cells, ext).  The map the adjoint differentiates."""
+    lp = lp or lgi_params(1)
+    ev = np.zeros((mesh.n_faces, 2))
+    ext = init_extensives(mesh, cells, gamma)
+    for _ in range(steps):
+        fl = modular_flux(mesh, cells, ev, gamma, lp)
+        ext = extensive_update(mesh, fl, dt, ext)
+        cells = cell_update(mesh, ext, gamma)
+    return cells, ext
