@@ -242,6 +242,9 @@ def measure(precision, mesh, cells, ext, args, local_rank, barrier, max_over_ran
     h.set_cells(cells)
     h.set_extensives(ext)
     h.set_edge_velocities(ev0)
+    # launch shapes of the per-step kernels chosen by the library's autotuner
+    # on this mesh and state (before the warm-up; the state is unchanged)
+    shapes = h.launch_shapes() if args.no_tune else h.autotune(reps=5)
     warm = max(args.warmup, 3)
     for _ in range(warm):
         h.step()
@@ -289,7 +292,7 @@ def measure(precision, mesh, cells, ext, args, local_rank, barrier, max_over_ran
     del flush
     return {"kernel_ms": kms.mean(0), "total_ms": total_ms, "wall": wall, "clock": clock,
             "e2e_s": e2e_s, "e2e_steps": ke, "upload_ms": float(np.mean(upload_ms)),
-            "warmup": warm}, final_cells
+            "warmup": warm, "shapes": shapes}, final_cells
 
 
 def pinned_io(mesh, ev, torch):
@@ -374,10 +377,12 @@ def run_gpu(args, world, rank, local_rank):
                         "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                         "steps": r32["e2e_steps"], "upload_ms_mean": r32["upload_ms"]},
                 "gpu_launches": 4 * k, "clocks": r32["clock"],
+                "launch_shapes": {kk: [v["block"], v["max_blocks"]] for kk, v in r32["shapes"].items()},
                 "faces_per_s": world * mesh.n_faces * k / (r32["total_ms"] * 1e-3),
                 "fp64": {"value": value64, "ms_per_step": r64["total_ms"] / k, "dtype": "f64",
                          "bit_exact_vs_reference": True, "roofline": roofline(r64, mesh, 0),
                          "note": "plain FP64 path: bound by GB300's FP64 pipe (2 DFMA/clk/SM), not HBM",
+                         "launch_shapes": {kk: [v["block"], v["max_blocks"]] for kk, v in r64["shapes"].items()},
                          "e2e": {"value": world * n * r64["e2e_steps"] / r64["e2e_s"], "unit": UNIT,
                                  "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
                          "clocks": r64["clock"]},
@@ -486,6 +491,7 @@ def run_batch(args, world, rank, local_rank):
         h.set_cells(cells)
         h.set_extensives(ext)
         h.set_edge_velocities(np.zeros((mesh.n_faces, 2)))
+        shapes = h.launch_shapes() if args.no_tune else h.autotune(reps=3)
         for _ in range(max(args.warmup, 3)):
             h.step()
         kms = []
@@ -507,6 +513,7 @@ def run_batch(args, world, rank, local_rank):
         times, _ = h.problem_times()
         res[precision] = {"ms_per_step": float(kms.sum(1).mean()), "kernel_ms": kms.mean(0).tolist(),
                           "graph_ms_per_step": graph_ms, "final_cells": h.get_cells(),
+                          "launch_shapes": {kk: [v["block"], v["max_blocks"]] for kk, v in shapes.items()},
                           "time_min": float(times.min()), "time_max": float(times.max())}
         h.close()
     c32, c64 = res[1].pop("final_cells"), res[0].pop("final_cells")
@@ -549,6 +556,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint cost measurement")
+    ap.add_argument("--no-tune", action="store_true", help="default launch shapes instead of the autotuner's")
     ap.add_argument("--workload", default="sedov", choices=["sedov", "riemann_batch"])
     ap.add_argument("--problems", type=int, default=512)
     args = ap.parse_args()

@@ -185,6 +185,7 @@ rg::StepArgs step_args(rg_handle* h) {
   a.dt_host = 0;
   a.dt_from_device = 0;
   a.step = 0;
+  a.shapes = h->shapes64;
   if (h->n_problems > 0) {
     a.cell_problem = static_cast<const int*>(h->cell_problem.p);
     a.gamma_p = static_cast<const double*>(h->gamma_p.p);
@@ -198,7 +199,7 @@ rg::StepArgs step_args(rg_handle* h) {
 
 }  // namespace rgh
 
-namespace {
+namespace rgh {
 
 rg::MixedArgs mixed_args(rg_handle* h) {
   MeshSlot* s = active_slot(h);
@@ -224,6 +225,7 @@ rg::MixedArgs mixed_args(rg_handle* h) {
   a.dt32 = 0;
   a.dt32_from_device = 0;
   a.step = 0;
+  a.shapes = h->shapes32;
   if (h->n_problems > 0) {
     a.cell_problem = static_cast<const int*>(h->cell_problem.p);
     a.gamma_p = static_cast<const float*>(h->gamma32_p.p);
@@ -243,7 +245,7 @@ void drop_graph(rg_handle* h) {
   h->graph = nullptr;
 }
 
-}  // namespace
+}  // namespace rgh
 
 namespace rgh {
 

@@ -249,52 +249,61 @@ __device__ __forceinline__ void fill_ghost(const StepArgs& a, int g) {
 
 // simple_cfl.cpp:28-47 (per cell) and :58-71 + lazy_list.hpp:185-191 (min, times cfl).
 template <bool kBatch>
-__global__ void __launch_bounds__(kBlock) k_cfl(StepArgs a, int fill_ghosts) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(kMaxBlock) k_cfl(StepArgs a, int fill_ghosts) {
   const MeshDev& m = a.mesh;
-  double x = __longlong_as_double(static_cast<long long>(kInfBits));
-  if (t < m.n) {
-    const Cell c = load_cell(a.cells, t);
-    const double radius = a.geom.width[t];
-    const double cs = sqrt(gamma_at<kBatch>(a, t) * c.p / c.d);
-    // fmax over faces of (cs + sqrt(q_e)) / radius equals (cs + sqrt(max q_e)) /
-    // radius exactly: sqrt, + and / are correctly rounded, hence monotone, so
-    // the maximum commutes with them.  NaN terms are skipped as fmax skips them.
-    double q = 0;
-    bool any = false;
-    const int b = m.cell_off[t], e1 = m.cell_off[t + 1];
-    for (int k = b; k < e1; ++k) {
-      const double2 w = reinterpret_cast<const double2*>(a.ev)[m.cell_faces[k]];
-      const double dx = c.vx - w.x, dy = c.vy - w.y;
-      const double qq = dx * dx + dy * dy;
-      if (!isnan(qq)) {
-        q = fmax(q, qq);
-        any = true;
+  const int total = fill_ghosts ? m.n + m.g : m.n;
+  // this thread's minimum of 1/bound as a bit pattern (positive doubles and
+  // +inf order as integers)
+  unsigned long long bits = kInfBits;
+  // the trip count is uniform across a warp (base is per block), as the
+  // warp-aggregated per-problem minimum of the batch form needs
+  for (int base = blockIdx.x * blockDim.x; base < total; base += gridDim.x * blockDim.x) {
+    const int t = base + threadIdx.x;
+    double x = __longlong_as_double(static_cast<long long>(kInfBits));
+    if (t < m.n) {
+      const Cell c = load_cell(a.cells, t);
+      const double radius = a.geom.width[t];
+      const double cs = sqrt(gamma_at<kBatch>(a, t) * c.p / c.d);
+      // fmax over faces of (cs + sqrt(q_e)) / radius equals (cs + sqrt(max q_e)) /
+      // radius exactly: sqrt, + and / are correctly rounded, hence monotone, so
+      // the maximum commutes with them.  NaN terms are skipped as fmax skips them.
+      double q = 0;
+      bool any = false;
+      const int b = m.cell_off[t], e1 = m.cell_off[t + 1];
+      for (int k = b; k < e1; ++k) {
+        const double2 w = reinterpret_cast<const double2*>(a.ev)[m.cell_faces[k]];
+        const double dx = c.vx - w.x, dy = c.vy - w.y;
+        const double qq = dx * dx + dy * dy;
+        if (!isnan(qq)) {
+          q = fmax(q, qq);
+          any = true;
+        }
       }
+      const double res = any ? fmax(0.0, (cs + sqrt(q)) / radius) : 0.0;
+      x = 1.0 / res;
+    } else if (t < total) {
+      fill_ghost(a, t - m.n);
     }
-    const double res = any ? fmax(0.0, (cs + sqrt(q)) / radius) : 0.0;
-    x = 1.0 / res;
-  } else if (fill_ghosts && t < m.n + m.g) {
-    fill_ghost(a, t - m.n);
+    const unsigned long long xb = static_cast<unsigned long long>(__double_as_longlong(x));
+    if (kBatch)
+      // per-problem minimum; the update kernel turns it into the problem's dt
+      problem_min(a.dtmin_p, t < m.n ? a.cell_problem[t] : -1, xb);
+    else
+      bits = xb < bits ? xb : bits;
   }
-  unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(x));
-  if (kBatch) {
-    // per-problem minimum; the update kernel turns it into the problem's dt
-    problem_min(a.dtmin_p, t < m.n ? a.cell_problem[t] : -1, bits);
-    return;
-  }
-  // min over the block (positive doubles: integer order = numeric order)
+  if (kBatch) return;
+  // min over the block
   for (int o = 16; o > 0; o >>= 1) {
     const unsigned long long ob = __shfl_xor_sync(0xffffffffu, bits, o);
     bits = ob < bits ? ob : bits;
   }
-  __shared__ unsigned long long wmin[kBlock / 32];
+  __shared__ unsigned long long wmin[kMaxBlock / 32];
   __shared__ bool last;
   if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = bits;
   __syncthreads();
   if (threadIdx.x == 0) {
     unsigned long long bm = wmin[0];
-    for (int w = 1; w < kBlock / 32; ++w) bm = wmin[w] < bm ? wmin[w] : bm;
+    for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w) bm = wmin[w] < bm ? wmin[w] : bm;
     atomicMin(&a.status->dt_min_bits, bm);
     __threadfence();
     last = atomicAdd(&a.status->blocks_done, 1u) == gridDim.x - 1;
@@ -396,10 +405,8 @@ __device__ __forceinline__ void shocked_comp(double dphi, double cv, double cell
 
 // LinearGaussImproved.cpp:425-494 calc_slope for one cell (serial build).
 template <bool kBatch>
-__global__ void __launch_bounds__(kBlock) k_slopes(StepArgs a) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void k_slopes_item(const StepArgs& a, int i) {
   const MeshDev& m = a.mesh;
-  if (i >= m.n) return;
   const Cell cell = load_cell(a.cells, i);
   const int b = m.cell_off[i], nn = m.cell_off[i + 1] - b;
   const dbl4 mi = a.geom.minv[i];
@@ -542,6 +549,12 @@ __global__ void __launch_bounds__(kBlock) k_slopes(StepArgs a) {
   o[3] = make_double2(sy.vx, sy.vy);
 }
 
+template <bool kBatch>
+__global__ void __launch_bounds__(kMaxBlock) k_slopes(StepArgs a) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.mesh.n; i += gridDim.x * blockDim.x)
+    k_slopes_item<kBatch>(a, i);
+}
+
 // ---------------------------------------------------------------- faces
 
 // simple_flux_calculator.cpp:9-15 convert_to_primitive (ideal_gas.cpp:13-16, 40-44)
@@ -642,10 +655,8 @@ __device__ __forceinline__ void write_flux(const StepArgs& a, int e, int real_si
 // ModularFluxCalculator (modular_flux_calculator.cpp:39-71) with the face
 // states of LinearGaussImproved (:570-590 real sides, :596-634 ghost sides).
 template <bool kScaled, bool kBatch>
-__global__ void __launch_bounds__(kBlock) k_faces_lgi(StepArgs a) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void k_faces_lgi_item(const StepArgs& a, int e) {
   const MeshDev& m = a.mesh;
-  if (e >= m.e) return;
   const int2 fc = m.face_cells[e];
   Cell side[2];
   const int ids[2] = {fc.x, fc.y};
@@ -685,6 +696,12 @@ __global__ void __launch_bounds__(kBlock) k_faces_lgi(StepArgs a) {
   write_flux<kBatch>(a, e, real_side, c, kScaled, pa);
 }
 
+template <bool kScaled, bool kBatch>
+__global__ void __launch_bounds__(kMaxBlock) k_faces_lgi(StepArgs a) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < a.mesh.e; e += gridDim.x * blockDim.x)
+    k_faces_lgi_item<kScaled, kBatch>(a, e);
+}
+
 // simple_flux_calculator.cpp:17-25 reflect (Reflect, geometry.cpp:117-120);
 // keeps the source's energy and sound speed.
 __device__ __forceinline__ Prim reflect(Prim q, double2 axis, double aa) {
@@ -700,10 +717,8 @@ __device__ __forceinline__ Prim reflect(Prim q, double2 axis, double aa) {
 // :216-244).  A ghost that is not its neighbour's own mirror takes its source
 // cell's state.
 template <bool kScaled, bool kBatch>
-__global__ void __launch_bounds__(kBlock) k_faces_pcm(StepArgs a) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void k_faces_pcm_item(const StepArgs& a, int e) {
   const MeshDev& m = a.mesh;
-  if (e >= m.e) return;
   const int2 fc = m.face_cells[e];
   const double2 p = a.geom.par[e], n = a.geom.nrm[e];
   const double pa = a.geom.area[e], na = a.geom.nabs[e];
@@ -729,6 +744,12 @@ __global__ void __launch_bounds__(kBlock) k_faces_pcm(StepArgs a) {
   write_flux<kBatch>(a, e, real_side, c, kScaled, pa);
 }
 
+template <bool kScaled, bool kBatch>
+__global__ void __launch_bounds__(kMaxBlock) k_faces_pcm(StepArgs a) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < a.mesh.e; e += gridDim.x * blockDim.x)
+    k_faces_pcm_item<kScaled, kBatch>(a, e);
+}
+
 // ---------------------------------------------------------------- cells
 
 // SimpleExtensiveUpdater (simple_extensive_updater.cpp:11-35) as a gather:
@@ -736,18 +757,8 @@ __global__ void __launch_bounds__(kBlock) k_faces_pcm(StepArgs a) {
 // is the order the reference's edge loop applies them to that cell; then
 // SimpleCellUpdater::regular_update (simple_cell_updater.cpp:22-59).
 template <bool kBatch>
-__global__ void __launch_bounds__(kBlock) k_update(StepArgs a, int from_unscaled, int do_ext, int do_cells) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void k_update_item(const StepArgs& a, int i, int from_unscaled, int do_ext, int do_cells) {
   const MeshDev& m = a.mesh;
-  if (kBatch && do_ext && !from_unscaled && i < a.n_problems) {
-    // every face of this step has read its problem's minimum: record the dt,
-    // advance the problem's time and reset the minimum for the next step
-    const double dt = a.cfl * __longlong_as_double(static_cast<long long>(a.dtmin_p[i]));
-    a.dt_p[i] = dt;
-    a.time_p[i] += dt;
-    a.dtmin_p[i] = kInfBits;
-  }
-  if (i >= m.n) return;
   double2* ext2 = reinterpret_cast<double2*>(a.ext);
   double2 e01 = ext2[2 * i], e23 = ext2[2 * i + 1];
   double mass = e01.x, en = e01.y, px = e23.x, py = e23.y;
@@ -805,6 +816,22 @@ __global__ void __launch_bounds__(kBlock) k_update(StepArgs a, int from_unscaled
     }
     store4(a.cells_out ? a.cells_out : a.cells, i, d, (gamma_at<kBatch>(a, i) - 1) * energy * d, vx, vy);
   }
+}
+
+template <bool kBatch>
+__global__ void __launch_bounds__(kMaxBlock) k_update(StepArgs a, int from_unscaled, int do_ext, int do_cells) {
+  const int t0 = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+  if (kBatch && do_ext && !from_unscaled) {
+    for (int p = t0; p < a.n_problems; p += stride) {
+      // every face of this step has read its problem's minimum: record the dt,
+      // advance the problem's time and reset the minimum for the next step
+      const double dt = a.cfl * __longlong_as_double(static_cast<long long>(a.dtmin_p[p]));
+      a.dt_p[p] = dt;
+      a.time_p[p] += dt;
+      a.dtmin_p[p] = kInfBits;
+    }
+  }
+  for (int i = t0; i < a.mesh.n; i += stride) k_update_item<kBatch>(a, i, from_unscaled, do_ext, do_cells);
 }
 
 // hdsim2d.cpp:41-67 init_extensives
@@ -880,9 +907,9 @@ cudaError_t launch_geometry(const GeomArgs& a, cudaStream_t s) {
 cudaError_t launch_cfl(const StepArgs& a, cudaStream_t s, bool fill_ghosts) {
   const int total = a.mesh.n + (fill_ghosts ? a.mesh.g : 0);
   if (a.cell_problem)
-    k_cfl<true><<<blocks(total > 0 ? total : 1), kBlock, 0, s>>>(a, fill_ghosts ? 1 : 0);
+    k_cfl<true><<<grid_of(a.shapes.cfl, total), a.shapes.cfl.block, 0, s>>>(a, fill_ghosts ? 1 : 0);
   else
-    k_cfl<false><<<blocks(total > 0 ? total : 1), kBlock, 0, s>>>(a, fill_ghosts ? 1 : 0);
+    k_cfl<false><<<grid_of(a.shapes.cfl, total), a.shapes.cfl.block, 0, s>>>(a, fill_ghosts ? 1 : 0);
   return cudaGetLastError();
 }
 
@@ -894,27 +921,27 @@ cudaError_t launch_ghost_fill(const StepArgs& a, cudaStream_t s) {
 cudaError_t launch_slopes(const StepArgs& a, cudaStream_t s) {
   if (a.mesh.n > 0) {
     if (a.cell_problem)
-      k_slopes<true><<<blocks(a.mesh.n), kBlock, 0, s>>>(a);
+      k_slopes<true><<<grid_of(a.shapes.slopes, a.mesh.n), a.shapes.slopes.block, 0, s>>>(a);
     else
-      k_slopes<false><<<blocks(a.mesh.n), kBlock, 0, s>>>(a);
+      k_slopes<false><<<grid_of(a.shapes.slopes, a.mesh.n), a.shapes.slopes.block, 0, s>>>(a);
   }
   return cudaGetLastError();
 }
 
 cudaError_t launch_faces(const StepArgs& a, cudaStream_t s, bool scaled) {
   if (a.mesh.e == 0) return cudaSuccess;
-  const int nb = blocks(a.mesh.e);
+  const int nb = grid_of(a.shapes.faces, a.mesh.e), bs = a.shapes.faces.block;
   const bool b = a.cell_problem != nullptr;
   if (a.order == 1) {
     if (scaled)
-      b ? k_faces_pcm<true, true><<<nb, kBlock, 0, s>>>(a) : k_faces_pcm<true, false><<<nb, kBlock, 0, s>>>(a);
+      b ? k_faces_pcm<true, true><<<nb, bs, 0, s>>>(a) : k_faces_pcm<true, false><<<nb, bs, 0, s>>>(a);
     else
-      b ? k_faces_pcm<false, true><<<nb, kBlock, 0, s>>>(a) : k_faces_pcm<false, false><<<nb, kBlock, 0, s>>>(a);
+      b ? k_faces_pcm<false, true><<<nb, bs, 0, s>>>(a) : k_faces_pcm<false, false><<<nb, bs, 0, s>>>(a);
   } else {
     if (scaled)
-      b ? k_faces_lgi<true, true><<<nb, kBlock, 0, s>>>(a) : k_faces_lgi<true, false><<<nb, kBlock, 0, s>>>(a);
+      b ? k_faces_lgi<true, true><<<nb, bs, 0, s>>>(a) : k_faces_lgi<true, false><<<nb, bs, 0, s>>>(a);
     else
-      b ? k_faces_lgi<false, true><<<nb, kBlock, 0, s>>>(a) : k_faces_lgi<false, false><<<nb, kBlock, 0, s>>>(a);
+      b ? k_faces_lgi<false, true><<<nb, bs, 0, s>>>(a) : k_faces_lgi<false, false><<<nb, bs, 0, s>>>(a);
   }
   return cudaGetLastError();
 }
@@ -923,9 +950,9 @@ cudaError_t launch_update(const StepArgs& a, cudaStream_t s, bool from_unscaled,
   const int work = a.cell_problem && a.n_problems > a.mesh.n ? a.n_problems : a.mesh.n;
   if (work > 0) {
     if (a.cell_problem)
-      k_update<true><<<blocks(work), kBlock, 0, s>>>(a, from_unscaled ? 1 : 0, extensive ? 1 : 0, cells ? 1 : 0);
+      k_update<true><<<grid_of(a.shapes.update, work), a.shapes.update.block, 0, s>>>(a, from_unscaled ? 1 : 0, extensive ? 1 : 0, cells ? 1 : 0);
     else
-      k_update<false><<<blocks(work), kBlock, 0, s>>>(a, from_unscaled ? 1 : 0, extensive ? 1 : 0, cells ? 1 : 0);
+      k_update<false><<<grid_of(a.shapes.update, work), a.shapes.update.block, 0, s>>>(a, from_unscaled ? 1 : 0, extensive ? 1 : 0, cells ? 1 : 0);
   }
   return cudaGetLastError();
 }

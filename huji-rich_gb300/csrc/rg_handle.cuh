@@ -163,6 +163,8 @@ struct rg_handle {
   double last_upload_ms = 0;
   double last_dt = 0;
   int step_seq = 0;
+  // launch shapes of the per-step kernels (rg_autotune / rg_set_launch_shapes)
+  rg::StepShapes shapes64, shapes32;
   // differentiation: checkpoints, recomputation buffers, reverse adjacency
   rg_adjoint_state* adj = nullptr;
 };
@@ -176,6 +178,8 @@ rg_status reset_status(rg_handle* h, rg::DevStatus* st, cudaStream_t s);
 rg_status collect(rg_handle* h, rg::DevStatus* st, cudaStream_t s);
 MeshSlot* active_slot(rg_handle* h);
 rg::StepArgs step_args(rg_handle* h);
+rg::MixedArgs mixed_args(rg_handle* h);
+void drop_graph(rg_handle* h);
 rg_status require(rg_handle* h, bool cells, bool ext, bool ev, bool fluxes);
 rg_status mesh_error(rg_handle* h);
 // frees the differentiation buffers (rg_destroy; a new mesh drops them too)

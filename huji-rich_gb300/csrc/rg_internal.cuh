@@ -133,6 +133,27 @@ __device__ __forceinline__ double smin(double a, double b) { return b < a ? b : 
 __device__ __forceinline__ double smax(double a, double b) { return a < b ? b : a; }
 #endif
 
+// Launch shape of a per-item kernel (cells, faces): `block` threads per block
+// (a multiple of 32, at most kMaxBlock); max_blocks == 0 launches one thread
+// per item, max_blocks > 0 at most that many blocks striding over the items
+// (a persistent grid, typically a multiple of the SM count).  Results do not
+// depend on the shape: every item is computed by one thread from the same
+// inputs, and the only cross-item reductions are minima.
+constexpr int kMaxBlock = 512;
+struct LaunchShape {
+  int block;
+  int max_blocks;
+};
+constexpr LaunchShape kDefaultShape{256, 0};
+inline int grid_of(const LaunchShape& s, int items) {
+  const int need = items > 0 ? (items + s.block - 1) / s.block : 1;
+  return s.max_blocks > 0 && need > s.max_blocks ? s.max_blocks : need;
+}
+// per-step kernels of one path (FP64 or FP32-mixed)
+struct StepShapes {
+  LaunchShape cfl = kDefaultShape, slopes = kDefaultShape, faces = kDefaultShape, update = kDefaultShape;
+};
+
 // Kernel launchers (rg_fp64.cu)
 struct StepArgs {
   MeshDev mesh;
@@ -159,6 +180,7 @@ struct StepArgs {
   double* time_p;                 // per problem simulated time
   double* dt_p;                   // per problem last dt
   int n_problems;
+  StepShapes shapes;  // launch shapes (host side; the kernels ignore it)
 };
 
 #ifdef __CUDACC__

@@ -138,39 +138,44 @@ __device__ __forceinline__ void fill_ghost32(const MixedArgs& a, int q) {
 // SimpleCFL (simple_cfl.cpp:28-47, 58-71) in FP32.  max_e (c+|v-w_e|)/R is
 // (c + sqrt(max_e |v-w_e|^2))/R: the bound is monotone in |v-w|.
 template <bool kBatch>
-__global__ void __launch_bounds__(kBlock) k_cfl32(MixedArgs a, int fill_ghosts) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(kMaxBlock) k_cfl32(MixedArgs a, int fill_ghosts) {
   const MeshDev& m = a.mesh;
-  float x = __int_as_float(0x7f800000);
-  if (t < m.n) {
-    const float4 c = a.cells32[t];
-    const float cs = sqrtf(gamma32<kBatch>(a, t) * c.y / c.x);
-    float q = 0.0f;
-    const int b = m.cell_off[t], e1 = m.cell_off[t + 1];
-    for (int k = b; k < e1; ++k) {
-      const float2 w = a.ev32[m.cell_faces[k]];
-      const float dx = c.z - w.x, dy = c.w - w.y;
-      q = fmaxf(q, fmaf(dx, dx, dy * dy));
+  const int total = fill_ghosts ? m.n + m.g : m.n;
+  unsigned int bits = 0x7f800000u;  // this thread's minimum (+inf; non-negative floats order as integers)
+  // warp-uniform trip count (see k_cfl)
+  for (int base = blockIdx.x * blockDim.x; base < total; base += gridDim.x * blockDim.x) {
+    const int t = base + threadIdx.x;
+    float x = __int_as_float(0x7f800000);
+    if (t < m.n) {
+      const float4 c = a.cells32[t];
+      const float cs = sqrtf(gamma32<kBatch>(a, t) * c.y / c.x);
+      float q = 0.0f;
+      const int b = m.cell_off[t], e1 = m.cell_off[t + 1];
+      for (int k = b; k < e1; ++k) {
+        const float2 w = a.ev32[m.cell_faces[k]];
+        const float dx = c.z - w.x, dy = c.w - w.y;
+        q = fmaxf(q, fmaf(dx, dx, dy * dy));
+      }
+      const float res = (cs + sqrtf(q)) / a.g32.width[t];
+      x = 1.0f / res;
+    } else if (t < total) {
+      fill_ghost32(a, t - m.n);
     }
-    const float res = (cs + sqrtf(q)) / a.g32.width[t];
-    x = 1.0f / res;
-  } else if (fill_ghosts && t < m.n + m.g) {
-    fill_ghost32(a, t - m.n);
+    if (kBatch)
+      problem_min(a.dtmin_p, t < m.n ? a.cell_problem[t] : -1,
+                  static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(x))));
+    else
+      bits = min(bits, __float_as_uint(x));
   }
-  if (kBatch) {
-    problem_min(a.dtmin_p, t < m.n ? a.cell_problem[t] : -1,
-                static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(x))));
-    return;
-  }
-  unsigned int bits = __float_as_uint(x);
+  if (kBatch) return;
   for (int o = 16; o > 0; o >>= 1) bits = min(bits, __shfl_xor_sync(0xffffffffu, bits, o));
-  __shared__ unsigned int wmin[kBlock / 32];
+  __shared__ unsigned int wmin[kMaxBlock / 32];
   __shared__ bool last;
   if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = bits;
   __syncthreads();
   if (threadIdx.x == 0) {
     unsigned int bm = wmin[0];
-    for (int w = 1; w < kBlock / 32; ++w) bm = min(bm, wmin[w]);
+    for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w) bm = min(bm, wmin[w]);
     atomicMin(reinterpret_cast<unsigned long long*>(&a.status->dt_min_bits),
               static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(__uint_as_float(bm)))));
     __threadfence();
@@ -212,10 +217,8 @@ __device__ __forceinline__ void shocked32(float dphi, float cv, float cellv, flo
 
 // LinearGaussImproved::calc_slope (LinearGaussImproved.cpp:425-494) in FP32.
 template <bool kBatch>
-__global__ void __launch_bounds__(kBlock) k_slopes32(MixedArgs a) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void k_slopes32_item(const MixedArgs& a, int i) {
   const MeshDev& m = a.mesh;
-  if (i >= m.n) return;
   const C4 cell = ld4(a.cells32, i);
   const int b = m.cell_off[i], nn = m.cell_off[i + 1] - b;
   const float4 mi = a.g32.minv[i];
@@ -308,6 +311,12 @@ __global__ void __launch_bounds__(kBlock) k_slopes32(MixedArgs a) {
   a.slopes32[2 * i + 1] = make_float4(sy.d, sy.p, sy.vx, sy.vy);
 }
 
+template <bool kBatch>
+__global__ void __launch_bounds__(kMaxBlock) k_slopes32(MixedArgs a) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.mesh.n; i += gridDim.x * blockDim.x)
+    k_slopes32_item<kBatch>(a, i);
+}
+
 __device__ __forceinline__ P6 prim32(float g, float inv_gm1, const C4& c) {
   const float pd = __fdividef(c.p, c.d);
   return P6{c.d, c.p, c.vx, c.vy, pd * inv_gm1, sqrtf(g * pd)};
@@ -385,10 +394,8 @@ __device__ __forceinline__ void write32(const MixedArgs& a, int e, int real_side
 }
 
 template <bool kScaled, bool kBatch>
-__global__ void __launch_bounds__(kBlock) k_faces32_lgi(MixedArgs a) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void k_faces32_lgi_item(const MixedArgs& a, int e) {
   const MeshDev& m = a.mesh;
-  if (e >= m.e) return;
   const int2 fc = m.face_cells[e];
   const int ids[2] = {fc.x, fc.y};
   const float2 dms[2] = {a.g32.dm0[e], a.g32.dm1[e]};
@@ -424,10 +431,14 @@ __global__ void __launch_bounds__(kBlock) k_faces32_lgi(MixedArgs a) {
 }
 
 template <bool kScaled, bool kBatch>
-__global__ void __launch_bounds__(kBlock) k_faces32_pcm(MixedArgs a) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(kMaxBlock) k_faces32_lgi(MixedArgs a) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < a.mesh.e; e += gridDim.x * blockDim.x)
+    k_faces32_lgi_item<kScaled, kBatch>(a, e);
+}
+
+template <bool kScaled, bool kBatch>
+__device__ __forceinline__ void k_faces32_pcm_item(const MixedArgs& a, int e) {
   const MeshDev& m = a.mesh;
-  if (e >= m.e) return;
   const int2 fc = m.face_cells[e];
   const float2 p = a.g32.par[e], n = a.g32.nrm[e];
   const float pa = a.g32.area[e], na = a.g32.nabs[e];
@@ -468,6 +479,12 @@ __global__ void __launch_bounds__(kBlock) k_faces32_pcm(MixedArgs a) {
   write32<kBatch>(a, e, real_side, c, kScaled, pa);
 }
 
+template <bool kScaled, bool kBatch>
+__global__ void __launch_bounds__(kMaxBlock) k_faces32_pcm(MixedArgs a) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < a.mesh.e; e += gridDim.x * blockDim.x)
+    k_faces32_pcm_item<kScaled, kBatch>(a, e);
+}
+
 // Error-free FP32 addition (Knuth's TwoSum): s + x == s' + err exactly.
 __device__ __forceinline__ void two_sum(float& s, float& c, float x) {
   const float t = s + x;
@@ -485,16 +502,8 @@ __device__ __forceinline__ void two_sum(float& s, float& c, float x) {
 // keep FP64 precision across steps.  e = E/m - v^2/2 is formed in FP64 with a
 // Newton-refined reciprocal of m.
 template <bool kBatch>
-__global__ void __launch_bounds__(kBlock) k_update_mixed(MixedArgs a, int from_unscaled, int do_ext, int do_cells) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void k_update_mixed_item(const MixedArgs& a, int i, int from_unscaled, int do_ext, int do_cells) {
   const MeshDev& m = a.mesh;
-  if (kBatch && do_ext && !from_unscaled && i < a.n_problems) {
-    const double dt = a.cfl * __longlong_as_double(static_cast<long long>(a.dtmin_p[i]));
-    a.dt_p[i] = dt;
-    a.time_p[i] += dt;
-    a.dtmin_p[i] = kInfBits;
-  }
-  if (i >= m.n) return;
   double2* ext2 = reinterpret_cast<double2*>(a.ext);
   const double2 e01 = ext2[2 * i], e23 = ext2[2 * i + 1];
   double mass = e01.x, en = e01.y, px = e23.x, py = e23.y;
@@ -552,6 +561,20 @@ __global__ void __launch_bounds__(kBlock) k_update_mixed(MixedArgs a, int from_u
   }
 }
 
+template <bool kBatch>
+__global__ void __launch_bounds__(kMaxBlock) k_update_mixed(MixedArgs a, int from_unscaled, int do_ext, int do_cells) {
+  const int t0 = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+  if (kBatch && do_ext && !from_unscaled) {
+    for (int p = t0; p < a.n_problems; p += stride) {
+      const double dt = a.cfl * __longlong_as_double(static_cast<long long>(a.dtmin_p[p]));
+      a.dt_p[p] = dt;
+      a.time_p[p] += dt;
+      a.dtmin_p[p] = kInfBits;
+    }
+  }
+  for (int i = t0; i < a.mesh.n; i += stride) k_update_mixed_item<kBatch>(a, i, from_unscaled, do_ext, do_cells);
+}
+
 inline int blocks(int n) { return (n + kBlock - 1) / kBlock; }
 
 }  // namespace
@@ -587,9 +610,9 @@ cudaError_t launch_flux_to32(const double* f64, float4* f32, int n, cudaStream_t
 cudaError_t launch_cfl32(const MixedArgs& a, cudaStream_t s, bool fill_ghosts) {
   const int total = a.mesh.n + (fill_ghosts ? a.mesh.g : 0);
   if (a.cell_problem)
-    k_cfl32<true><<<blocks(total > 0 ? total : 1), kBlock, 0, s>>>(a, fill_ghosts ? 1 : 0);
+    k_cfl32<true><<<grid_of(a.shapes.cfl, total), a.shapes.cfl.block, 0, s>>>(a, fill_ghosts ? 1 : 0);
   else
-    k_cfl32<false><<<blocks(total > 0 ? total : 1), kBlock, 0, s>>>(a, fill_ghosts ? 1 : 0);
+    k_cfl32<false><<<grid_of(a.shapes.cfl, total), a.shapes.cfl.block, 0, s>>>(a, fill_ghosts ? 1 : 0);
   return cudaGetLastError();
 }
 cudaError_t launch_ghost_fill32(const MixedArgs& a, cudaStream_t s) {
@@ -599,26 +622,26 @@ cudaError_t launch_ghost_fill32(const MixedArgs& a, cudaStream_t s) {
 cudaError_t launch_slopes32(const MixedArgs& a, cudaStream_t s) {
   if (a.mesh.n > 0) {
     if (a.cell_problem)
-      k_slopes32<true><<<blocks(a.mesh.n), kBlock, 0, s>>>(a);
+      k_slopes32<true><<<grid_of(a.shapes.slopes, a.mesh.n), a.shapes.slopes.block, 0, s>>>(a);
     else
-      k_slopes32<false><<<blocks(a.mesh.n), kBlock, 0, s>>>(a);
+      k_slopes32<false><<<grid_of(a.shapes.slopes, a.mesh.n), a.shapes.slopes.block, 0, s>>>(a);
   }
   return cudaGetLastError();
 }
 cudaError_t launch_faces32(const MixedArgs& a, cudaStream_t s, bool scaled) {
   if (a.mesh.e == 0) return cudaSuccess;
-  const int nb = blocks(a.mesh.e);
+  const int nb = grid_of(a.shapes.faces, a.mesh.e), bs = a.shapes.faces.block;
   const bool b = a.cell_problem != nullptr;
   if (a.order == 1) {
     if (scaled)
-      b ? k_faces32_pcm<true, true><<<nb, kBlock, 0, s>>>(a) : k_faces32_pcm<true, false><<<nb, kBlock, 0, s>>>(a);
+      b ? k_faces32_pcm<true, true><<<nb, bs, 0, s>>>(a) : k_faces32_pcm<true, false><<<nb, bs, 0, s>>>(a);
     else
-      b ? k_faces32_pcm<false, true><<<nb, kBlock, 0, s>>>(a) : k_faces32_pcm<false, false><<<nb, kBlock, 0, s>>>(a);
+      b ? k_faces32_pcm<false, true><<<nb, bs, 0, s>>>(a) : k_faces32_pcm<false, false><<<nb, bs, 0, s>>>(a);
   } else {
     if (scaled)
-      b ? k_faces32_lgi<true, true><<<nb, kBlock, 0, s>>>(a) : k_faces32_lgi<true, false><<<nb, kBlock, 0, s>>>(a);
+      b ? k_faces32_lgi<true, true><<<nb, bs, 0, s>>>(a) : k_faces32_lgi<true, false><<<nb, bs, 0, s>>>(a);
     else
-      b ? k_faces32_lgi<false, true><<<nb, kBlock, 0, s>>>(a) : k_faces32_lgi<false, false><<<nb, kBlock, 0, s>>>(a);
+      b ? k_faces32_lgi<false, true><<<nb, bs, 0, s>>>(a) : k_faces32_lgi<false, false><<<nb, bs, 0, s>>>(a);
   }
   return cudaGetLastError();
 }
@@ -626,9 +649,9 @@ cudaError_t launch_update_mixed(const MixedArgs& a, cudaStream_t s, bool from_un
   const int work = a.cell_problem && a.n_problems > a.mesh.n ? a.n_problems : a.mesh.n;
   if (work > 0) {
     if (a.cell_problem)
-      k_update_mixed<true><<<blocks(work), kBlock, 0, s>>>(a, from_unscaled ? 1 : 0, extensive ? 1 : 0, cells ? 1 : 0);
+      k_update_mixed<true><<<grid_of(a.shapes.update, work), a.shapes.update.block, 0, s>>>(a, from_unscaled ? 1 : 0, extensive ? 1 : 0, cells ? 1 : 0);
     else
-      k_update_mixed<false><<<blocks(work), kBlock, 0, s>>>(a, from_unscaled ? 1 : 0, extensive ? 1 : 0, cells ? 1 : 0);
+      k_update_mixed<false><<<grid_of(a.shapes.update, work), a.shapes.update.block, 0, s>>>(a, from_unscaled ? 1 : 0, extensive ? 1 : 0, cells ? 1 : 0);
   }
   return cudaGetLastError();
 }

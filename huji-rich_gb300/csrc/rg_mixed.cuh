@@ -67,6 +67,7 @@ struct MixedArgs {
   double* time_p;
   double* dt_p;
   int n_problems;
+  StepShapes shapes;  // launch shapes (host side; the kernels ignore it)
 };
 
 cudaError_t launch_geom32(const MixedGeomArgs& a, cudaStream_t s);

@@ -28,6 +28,7 @@ UNITS = {
     "rg_adjoint.cu": ["--fmad=false"],
     "rg_adjoint_rev.cu": [],
     "rg_adjoint_api.cu": [],
+    "rg_tune.cu": [],
 }
 
 

@@ -23,7 +23,14 @@ EXPORTS = ("rg_default_config", "rg_create", "rg_destroy", "rg_status_string", "
            "rg_device_buffers", "rg_init_extensives", "rg_cfl_dt", "rg_flux", "rg_set_fluxes",
            "rg_extensive_update", "rg_cell_update", "rg_step", "rg_run", "rg_step_async",
            "rg_synchronize", "rg_step_timed", "rg_cfl_dt_noalloc", "rg_set_problems",
-           "rg_get_problem_times", "rg_run_graph", "rg_step_fwd", "rg_step_bwd", "rg_step_tlm")
+           "rg_get_problem_times", "rg_run_graph", "rg_step_fwd", "rg_step_bwd", "rg_step_tlm",
+           "rg_autotune", "rg_set_launch_shapes", "rg_get_launch_shapes")
+
+KERNELS = ("cfl", "slopes", "faces", "update")
+
+
+class RgLaunchShapes(C.Structure):
+    _fields_ = [("block", C.c_int32 * 4), ("max_blocks", C.c_int32 * 4), ("ms", C.c_float * 4)]
 
 
 class RgDeviceView(C.Structure):
@@ -84,6 +91,9 @@ def load(path=LIB_PATH):
     lib.rg_step_fwd.argtypes = [vp, C.c_int32, C.c_double, C.c_int32]
     lib.rg_step_bwd.argtypes = [vp, dp, dp]
     lib.rg_step_tlm.argtypes = [vp, C.c_int32, C.c_double, dp, dp]
+    lib.rg_autotune.argtypes = [vp, C.c_int32, C.POINTER(RgLaunchShapes)]
+    lib.rg_set_launch_shapes.argtypes = [vp, C.POINTER(RgLaunchShapes)]
+    lib.rg_get_launch_shapes.argtypes = [vp, C.POINTER(RgLaunchShapes)]
     _lib = lib
     return lib
 
@@ -261,3 +271,29 @@ class Handle:
         out = np.empty((self.mesh.n_cells, 4))
         self._check(self.lib.rg_step_tlm(self.h, n_steps, dt, dptr(a), dptr(out)))
         return out
+
+    # launch shapes of the per-step kernels
+    @staticmethod
+    def _shapes_dict(r):
+        return {k: {"block": r.block[i], "max_blocks": r.max_blocks[i], "ms": r.ms[i]}
+                for i, k in enumerate(KERNELS)}
+
+    def autotune(self, reps=5):
+        """Times every candidate launch shape per kernel and keeps the fastest."""
+        r = RgLaunchShapes()
+        self._check(self.lib.rg_autotune(self.h, reps, C.byref(r)))
+        return self._shapes_dict(r)
+
+    def launch_shapes(self):
+        r = RgLaunchShapes()
+        self._check(self.lib.rg_get_launch_shapes(self.h, C.byref(r)))
+        return self._shapes_dict(r)
+
+    def set_launch_shapes(self, shapes):
+        """shapes: {kernel: (block, max_blocks)} for some of KERNELS."""
+        r = RgLaunchShapes()
+        self._check(self.lib.rg_get_launch_shapes(self.h, C.byref(r)))
+        for k, (b, mb) in shapes.items():
+            i = KERNELS.index(k)
+            r.block[i], r.max_blocks[i] = b, mb
+        self._check(self.lib.rg_set_launch_shapes(self.h, C.byref(r)))

@@ -245,6 +245,26 @@ rg_status rg_get_problem_times(rg_handle* h, double* time_out, double* dt_last_o
  * with step 0 in its key. */
 rg_status rg_run_graph(rg_handle* h, int32_t n_steps);
 
+/* Launch shapes and the autotuner ------------------------------------------ */
+/* No counterpart in the reference.  The per-step kernels (rg_kernel order:
+ * CFL, slopes, face fluxes, gather+update) of the handle's current path
+ * (rg_config.precision; batch or single problem) each run with a launch
+ * shape: threads per block (a multiple of 32, 32..512) and max_blocks (0: one
+ * thread per cell or face; > 0: a persistent grid of at most that many blocks
+ * striding over the items).  Results are identical for every shape. */
+typedef enum { RG_KERNEL_CFL = 0, RG_KERNEL_SLOPES = 1, RG_KERNEL_FACES = 2, RG_KERNEL_UPDATE = 3 } rg_kernel;
+typedef struct {
+  int32_t block[4];
+  int32_t max_blocks[4];
+  float ms[4]; /* rg_autotune: mean time per launch of the chosen shape (ms) */
+} rg_launch_shapes;
+/* Times every candidate shape of each per-step kernel on the uploaded mesh
+ * and the current state (reps launches each; the state is left unchanged)
+ * and keeps the fastest.  Needs the cells, extensives and edge velocities. */
+rg_status rg_autotune(rg_handle* h, int32_t reps, rg_launch_shapes* chosen);
+rg_status rg_set_launch_shapes(rg_handle* h, const rg_launch_shapes* shapes);
+rg_status rg_get_launch_shapes(const rg_handle* h, rg_launch_shapes* shapes);
+
 /* Differentiation --------------------------------------------------------- */
 /* No counterpart in the reference (it has no differentiation).  The map
  * differentiated is n_steps hdsim::TimeAdvance steps (hdsim2d.cpp:149-241)
