@@ -248,7 +248,7 @@ def measure(precision, mesh, cells, ext, args, local_rank, barrier, max_over_ran
     warm = max(args.warmup, 3)
     for _ in range(warm):
         h.step()
-    stream = torch.cuda.ExternalStream(h.device_buffers().stream)
+    stream = torch.cuda.ExternalStream(h.stream())
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     clocks = ClockSampler(local_rank)
     kms = []
@@ -500,7 +500,7 @@ def run_batch(args, world, rank, local_rank):
             _, k = h.step_timed()
             kms.append(k)
         kms = np.array(kms)
-        stream = torch.cuda.ExternalStream(h.device_buffers().stream)
+        stream = torch.cuda.ExternalStream(h.stream())
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         h.run_graph(1)
         with torch.cuda.stream(stream):

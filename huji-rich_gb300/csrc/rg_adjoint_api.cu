@@ -200,6 +200,7 @@ rg_status rg_step_fwd(rg_handle* h, int32_t n_steps, double dt, int32_t every) {
   if (every < 1) return invalid(h, -12, every);
   rg_adjoint_state* A = h->adj;
   A->have_forward = false;
+  h->dt_next_ready = false;
   MeshSlot* s = active_slot(h);
   const size_t n = static_cast<size_t>(s->n), np = n + static_cast<size_t>(s->g);
   const int n_ckpt = (n_steps + every - 1) / every;
@@ -308,6 +309,7 @@ rg_status rg_step_tlm(rg_handle* h, int32_t n_steps, double dt, const double* dc
   if (rg_status st = check_run(h, n_steps, dt)) return st;
   rg_adjoint_state* A = h->adj;
   A->have_forward = false;
+  h->dt_next_ready = false;
   MeshSlot* s = active_slot(h);
   const size_t n = static_cast<size_t>(s->n), ne = static_cast<size_t>(std::max(s->e, 1));
   RG_CUDA(h, A->dcells.ensure(32 * n));

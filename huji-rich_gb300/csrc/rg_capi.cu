@@ -128,7 +128,8 @@ void fill_views(MeshSlot& s) {
   s.g32.dm1 = at<float2>(b, L.dm1_32);
   s.g32.width = at<float>(b, L.width32);
   s.g32.minv = at<float4>(b, L.minv32);
-  s.g32.hr = at<float2>(b, L.hr32);
+  s.g32.ent = at<float4>(b, L.ent32);
+  s.g32.fsign = at<int>(b, L.fsign32);
   s.g32.ghost_unit = at<float2>(b, L.gunit32);
   s.g32.inv_cd_volume = at<float>(b, L.icdv32);
 }
@@ -186,6 +187,7 @@ rg::StepArgs step_args(rg_handle* h) {
   a.dt_from_device = 0;
   a.step = 0;
   a.shapes = h->shapes64;
+  a.ev_zero = h->ev_zero && !h->external_state;
   if (h->n_problems > 0) {
     a.cell_problem = static_cast<const int*>(h->cell_problem.p);
     a.gamma_p = static_cast<const double*>(h->gamma_p.p);
@@ -226,6 +228,7 @@ rg::MixedArgs mixed_args(rg_handle* h) {
   a.dt32_from_device = 0;
   a.step = 0;
   a.shapes = h->shapes32;
+  a.ev_zero = h->ev_zero && !h->external_state;
   if (h->n_problems > 0) {
     a.cell_problem = static_cast<const int*>(h->cell_problem.p);
     a.gamma_p = static_cast<const float*>(h->gamma32_p.p);
@@ -271,6 +274,11 @@ rg_status mesh_error(rg_handle* h) {
 }  // namespace rgh
 
 namespace {
+
+// Fused steps (the update computes the next step's dt): one problem, order 2
+// (the slopes kernel moves the dt into place before the face kernel reads
+// it), no caller access to the device buffers.
+bool fusable(const rg_handle* h) { return h->cfg.order == 2 && h->n_problems == 0 && !h->external_state; }
 
 // hdsim::TimeAdvance2Heun on a fixed mesh (hdsim2d.cpp:323-449): dt once;
 // pass 1 on the cells writes the mid extensives and mid cells; pass 2 on the
@@ -353,30 +361,40 @@ rg_status enqueue_step(rg_handle* h, int step, cudaEvent_t* ev = nullptr) {
     rg::MixedArgs a = mixed_args(h);
     a.dt32_from_device = 1;
     a.step = step;
+    const bool fuse = fusable(h), have_dt = fuse && h->dt_next_ready;
     if (ev) RG_CUDA(h, cudaEventRecord(ev[0], h->stream));
-    RG_CUDA(h, rg::launch_cfl32(a, h->stream, h->cfg.order == 2));
+    if (!have_dt) RG_CUDA(h, rg::launch_cfl32(a, h->stream, false));
     if (ev) RG_CUDA(h, cudaEventRecord(ev[1], h->stream));
+    a.take_next_dt = have_dt;
     if (h->cfg.order == 2) RG_CUDA(h, rg::launch_slopes32(a, h->stream));
+    a.take_next_dt = 0;
     if (ev) RG_CUDA(h, cudaEventRecord(ev[2], h->stream));
     RG_CUDA(h, rg::launch_faces32(a, h->stream, true));
     if (ev) RG_CUDA(h, cudaEventRecord(ev[3], h->stream));
+    a.cfl_next = fuse;
     RG_CUDA(h, rg::launch_update_mixed(a, h->stream, false, true, true));
     if (ev) RG_CUDA(h, cudaEventRecord(ev[4], h->stream));
+    h->dt_next_ready = fuse;
     h->have_fluxes = false;
     return RG_OK;
   }
   rg::StepArgs a = step_args(h);
   a.dt_from_device = 1;
   a.step = step;
+  const bool fuse = fusable(h), have_dt = fuse && h->dt_next_ready;
   if (ev) RG_CUDA(h, cudaEventRecord(ev[0], h->stream));
-  RG_CUDA(h, rg::launch_cfl(a, h->stream, h->cfg.order == 2));
+  if (!have_dt) RG_CUDA(h, rg::launch_cfl(a, h->stream, false));
   if (ev) RG_CUDA(h, cudaEventRecord(ev[1], h->stream));
+  a.take_next_dt = have_dt;
   if (h->cfg.order == 2) RG_CUDA(h, rg::launch_slopes(a, h->stream));
+  a.take_next_dt = 0;
   if (ev) RG_CUDA(h, cudaEventRecord(ev[2], h->stream));
   RG_CUDA(h, rg::launch_faces(a, h->stream, true));
   if (ev) RG_CUDA(h, cudaEventRecord(ev[3], h->stream));
+  a.cfl_next = fuse;
   RG_CUDA(h, rg::launch_update(a, h->stream, false, true, true));
   if (ev) RG_CUDA(h, cudaEventRecord(ev[4], h->stream));
+  h->dt_next_ready = fuse;
   h->have_fluxes = false;  // the buffer now holds dt*area-scaled fluxes
   return RG_OK;
 }
@@ -474,6 +492,7 @@ rg_status rg_destroy(rg_handle* h) {
     if (s.last_use) cudaEventDestroy(s.last_use);
   }
   adjoint_release(h);
+  h->flag_buf.release();
   h->cells.release();
   h->ext.release();
   h->ev.release();
@@ -515,6 +534,7 @@ rg_status rg_last_error(const rg_handle* h, rg_error* err) {
 rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t /*flags*/) {
   if (!h) return RG_ERR_INVALID_ARGUMENT;
   h->last = rg_error{};
+  h->dt_next_ready = false;
   const auto t0 = std::chrono::steady_clock::now();
   if (rg_status st = check_view(h, v)) return st;
   RG_CUDA(h, cudaSetDevice(h->cfg.device));
@@ -613,7 +633,9 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t /*flags*/
     m32.dm1 = at<float2>(b, s.lay.dm1_32);
     m32.width = at<float>(b, s.lay.width32);
     m32.minv = at<float4>(b, s.lay.minv32);
-    m32.hr = at<float2>(b, s.lay.hr32);
+    m32.ent = at<float4>(b, s.lay.ent32);
+    m32.fsign = at<int>(b, s.lay.fsign32);
+    m32.cell_faces = s.mesh.cell_faces;
     m32.ghost_unit = at<float2>(b, s.lay.gunit32);
     m32.inv_cd_volume = at<float>(b, s.lay.icdv32);
     m32.cd_volume = s.mesh.cd_volume;
@@ -702,6 +724,7 @@ rg_status rg_last_upload_ms(const rg_handle* h, double* ms) {
 
 rg_status rg_set_cells(rg_handle* h, const double* cells) {
   if (!h || !cells) return RG_ERR_INVALID_ARGUMENT;
+  h->dt_next_ready = false;
   if (h->active < 0) return require(h, false, false, false, false);
   RG_CUDA(h, cudaMemcpyAsync(h->cells.p, cells, 32 * static_cast<size_t>(active_slot(h)->n),
                              cudaMemcpyHostToDevice, h->stream));
@@ -746,13 +769,22 @@ rg_status rg_get_extensives(rg_handle* h, double* ext) {
 
 rg_status rg_set_edge_velocities(rg_handle* h, const double* ev) {
   if (!h || !ev) return RG_ERR_INVALID_ARGUMENT;
+  h->dt_next_ready = false;
   if (h->active < 0) return require(h, false, false, false, false);
   RG_CUDA(h, cudaMemcpyAsync(h->ev.p, ev, 16 * static_cast<size_t>(active_slot(h)->e),
                              cudaMemcpyHostToDevice, h->stream));
   if (h->mixed)
     RG_CUDA(h, rg::launch_vec2_to32(static_cast<const double*>(h->ev.p), static_cast<float2*>(h->ev32.p),
                                     active_slot(h)->e, h->stream));
+  // all faces at rest (Eulerian mesh): the kernels then read no face velocities
+  RG_CUDA(h, h->flag_buf.ensure(sizeof(int)));
+  RG_CUDA(h, cudaMemsetAsync(h->flag_buf.p, 0, sizeof(int), h->stream));
+  RG_CUDA(h, rg::launch_any_nonzero(static_cast<const double*>(h->ev.p), 2LL * active_slot(h)->e,
+                                    static_cast<int*>(h->flag_buf.p), h->stream));
+  int* hflag = reinterpret_cast<int*>(h->host_status.p);
+  RG_CUDA(h, cudaMemcpyAsync(hflag, h->flag_buf.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   RG_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->ev_zero = *hflag == 0;
   h->have_ev = true;
   return RG_OK;
 }
@@ -778,8 +810,16 @@ rg_status rg_device_buffers(rg_handle* h, rg_device_view* v) {
   v->edge_velocities = static_cast<double*>(h->ev.p);
   v->fluxes = static_cast<double*>(h->fluxes.p);
   v->stream = h->stream;
-  // a caller writing through these pointers provides the state
+  // a caller writing through these pointers provides the state, at any time
   h->have_cells = h->have_ext = h->have_ev = true;
+  h->external_state = true;
+  h->dt_next_ready = false;
+  return RG_OK;
+}
+
+rg_status rg_stream(const rg_handle* h, void** stream) {
+  if (!h || !stream) return RG_ERR_INVALID_ARGUMENT;
+  *stream = h->stream;
   return RG_OK;
 }
 
@@ -865,6 +905,7 @@ rg_status rg_extensive_update(rg_handle* h, double dt) {
 rg_status rg_cell_update(rg_handle* h) {
   if (rg_status st = require(h, false, true, false, false)) return st;
   h->last = rg_error{};
+  h->dt_next_ready = false;
   RG_TRY(reset_status(h, h->d_status, h->stream));
   if (h->mixed) {
     RG_CUDA(h, rg::launch_update_mixed(mixed_args(h), h->stream, false, false, true));
@@ -946,6 +987,7 @@ rg_status rg_set_problems(rg_handle* h, int32_t P, const int32_t* offsets, const
   if (h->active < 0) return require(h, false, false, false, false);
   h->last = rg_error{};
   drop_graph(h);
+  h->dt_next_ready = false;
   MeshSlot* s = active_slot(h);
   if (P == 0) {
     h->n_problems = 0;
@@ -1009,6 +1051,17 @@ rg_status rg_run_graph(rg_handle* h, int32_t n_steps) {
   if (n_steps < 0) return RG_ERR_INVALID_ARGUMENT;
   if (rg_status st = mesh_error(h)) return st;
   h->last = rg_error{};
+  if (n_steps == 0) return RG_OK;
+  RG_TRY(reset_status(h, h->d_status, h->stream));
+  if (fusable(h) && !h->dt_next_ready) {
+    // one step with its own CFL pass; the captured step is the fused form,
+    // which takes the dt the previous step's update computed
+    RG_TRY(enqueue_step(h, 0));
+    if (--n_steps == 0) {
+      h->have_fluxes = false;
+      return collect(h, h->d_status, h->stream);
+    }
+  }
   if (!h->graph_exec) {
     RG_CUDA(h, cudaStreamSynchronize(h->stream));
     RG_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
@@ -1023,7 +1076,6 @@ rg_status rg_run_graph(rg_handle* h, int32_t n_steps) {
     h->graph = g;
     RG_CUDA(h, cudaGraphInstantiate(&h->graph_exec, h->graph, 0));
   }
-  RG_TRY(reset_status(h, h->d_status, h->stream));
   for (int k = 0; k < n_steps; ++k) RG_CUDA(h, cudaGraphLaunch(h->graph_exec, h->stream));
   h->have_fluxes = false;
   return collect(h, h->d_status, h->stream);

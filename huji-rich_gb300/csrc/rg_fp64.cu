@@ -236,7 +236,7 @@ __device__ __forceinline__ double scaled_dt(const StepArgs& a, int point) {
 // Ghost state (LinearGaussImproved.cpp:543-550 new_cells[ghost]):
 // RigidWallGenerator.cpp:17-37 reflects the real neighbour's velocity,
 // PeriodicGhostGenerator.cpp:3-17 copies the source cell.
-__device__ __forceinline__ void fill_ghost(const StepArgs& a, int g) {
+__device__ __forceinline__ Cell ghost_state(const StepArgs& a, int g) {
   Cell c = load_cell(a.cells, a.geom.ghost_real[g]);
   if (a.ghost_kind != RG_GHOST_PERIODIC) {
     const double2 u = a.geom.ghost_unit[g];
@@ -244,7 +244,16 @@ __device__ __forceinline__ void fill_ghost(const StepArgs& a, int g) {
     c.vx -= u.x * s;
     c.vy -= u.y * s;
   }
+  return c;
+}
+__device__ __forceinline__ void fill_ghost(const StepArgs& a, int g) {
+  const Cell c = ghost_state(a, g);
   store4(a.cells, a.mesh.n + g, c.d, c.p, c.vx, c.vy);
+}
+// State of point p: a real cell's record, or a ghost's state formed from the
+// current state of its cell (the per-step kernels read no ghost records)
+__device__ __forceinline__ Cell point_state(const StepArgs& a, int p) {
+  return p < a.mesh.n ? load_cell(a.cells, p) : ghost_state(a, p - a.mesh.n);
 }
 
 // simple_cfl.cpp:28-47 (per cell) and :58-71 + lazy_list.hpp:185-191 (min, times cfl).
@@ -270,13 +279,22 @@ __global__ void __launch_bounds__(kMaxBlock) k_cfl(StepArgs a, int fill_ghosts) 
       double q = 0;
       bool any = false;
       const int b = m.cell_off[t], e1 = m.cell_off[t + 1];
-      for (int k = b; k < e1; ++k) {
-        const double2 w = reinterpret_cast<const double2*>(a.ev)[m.cell_faces[k]];
-        const double dx = c.vx - w.x, dy = c.vy - w.y;
-        const double qq = dx * dx + dy * dy;
-        if (!isnan(qq)) {
+      if (a.ev_zero) {
+        // every face at rest: each term is vx^2 + vy^2 (v - 0 == v)
+        const double qq = c.vx * c.vx + c.vy * c.vy;
+        if (e1 > b && !isnan(qq)) {
           q = fmax(q, qq);
           any = true;
+        }
+      } else {
+        for (int k = b; k < e1; ++k) {
+          const double2 w = reinterpret_cast<const double2*>(a.ev)[m.cell_faces[k]];
+          const double dx = c.vx - w.x, dy = c.vy - w.y;
+          const double qq = dx * dx + dy * dy;
+          if (!isnan(qq)) {
+            q = fmax(q, qq);
+            any = true;
+          }
         }
       }
       const double res = any ? fmax(0.0, (cs + sqrt(q)) / radius) : 0.0;
@@ -292,31 +310,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_cfl(StepArgs a, int fill_ghosts) 
       bits = xb < bits ? xb : bits;
   }
   if (kBatch) return;
-  // min over the block
-  for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long ob = __shfl_xor_sync(0xffffffffu, bits, o);
-    bits = ob < bits ? ob : bits;
-  }
-  __shared__ unsigned long long wmin[kMaxBlock / 32];
-  __shared__ bool last;
-  if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = bits;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned long long bm = wmin[0];
-    for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w) bm = wmin[w] < bm ? wmin[w] : bm;
-    atomicMin(&a.status->dt_min_bits, bm);
-    __threadfence();
-    last = atomicAdd(&a.status->blocks_done, 1u) == gridDim.x - 1;
-  }
-  __syncthreads();
-  if (last && threadIdx.x == 0) {
-    // every block's atomicMin is visible here (threadfence before its ticket)
-    __threadfence();
-    const unsigned long long mb = atomicAdd(&a.status->dt_min_bits, 0ull);
-    a.status->dt = a.cfl * __longlong_as_double(static_cast<long long>(mb));
-    a.status->dt_min_bits = kInfBits;  // ready for the next step
-    a.status->blocks_done = 0;
-  }
+  grid_min_times(a.status, bits, a.cfl, &a.status->dt);
 }
 
 __global__ void __launch_bounds__(kBlock) k_ghost_fill(StepArgs a) {
@@ -415,7 +409,7 @@ __device__ __forceinline__ void k_slopes_item(const StepArgs& a, int i) {
     // :401-422 GetBoundarySlope
     Cell phisy{0, 0, 0, 0}, phisx{0, 0, 0, 0};
     for (int k = 0; k < nn; ++k) {
-      const Cell nb = load_cell(a.cells, static_cast<int>(a.geom.nbr[b + k] & kNbrIdMask));
+      const Cell nb = point_state(a, static_cast<int>(a.geom.nbr[b + k] & kNbrIdMask));
       const double2 h = a.geom.hr[b + k];
       const Cell df{nb.d - cell.d, nb.p - cell.p, nb.vx - cell.vx, nb.vy - cell.vy};
       phisy.d = phisy.d + df.d * h.y;
@@ -436,7 +430,7 @@ __device__ __forceinline__ void k_slopes_item(const StepArgs& a, int i) {
     // :80-133 calc_naive_slope, right-hand side and solve
     Cell vx{0, 0, 0, 0}, vy{0, 0, 0, 0};
     for (int k = 0; k < nn; ++k) {
-      const Cell nb = load_cell(a.cells, static_cast<int>(a.geom.nbr[b + k] & kNbrIdMask));
+      const Cell nb = point_state(a, static_cast<int>(a.geom.nbr[b + k] & kNbrIdMask));
       const double2 h = a.geom.hr[b + k];
       if (k == 0) {
         vx = Cell{cell.d * h.x, cell.p * h.x, cell.vx * h.x, cell.vy * h.x};
@@ -479,7 +473,7 @@ __device__ __forceinline__ void k_slopes_item(const StepArgs& a, int i) {
       // PressureRatio < delta_p  <=>  some neighbour's ratio < delta_p
       const float dp_f = static_cast<float>(a.delta_p);
       for (int k = 0; k < nn && !shock; ++k) {
-        const double np_ = a.cells[4 * static_cast<int>(a.geom.nbr[b + k] & kNbrIdMask) + 1];
+        const double np_ = point_state(a, static_cast<int>(a.geom.nbr[b + k] & kNbrIdMask)).p;
         const double num = cell.p > np_ ? np_ : cell.p;
         const double den = cell.p > np_ ? cell.p : np_;
         if (fp32_safe(num) && fp32_safe(den)) {
@@ -497,7 +491,7 @@ __device__ __forceinline__ void k_slopes_item(const StepArgs& a, int i) {
     for (int k = 0; k < nn; ++k) {
       const uint32_t w = a.geom.nbr[b + k];
       if (!shock && (w & kNbrMirror)) continue;  // :194-195 skips self-mirror neighbours
-      const Cell nb = load_cell(a.cells, static_cast<int>(w & kNbrIdMask));
+      const Cell nb = point_state(a, static_cast<int>(w & kNbrIdMask));
       cmax.d = smax(cmax.d, nb.d);
       cmax.p = smax(cmax.p, nb.p);
       cmax.vx = smax(cmax.vx, nb.vx);
@@ -530,7 +524,7 @@ __device__ __forceinline__ void k_slopes_item(const StepArgs& a, int i) {
         limit_comp(dphi.vy, cv.vy, cell.vy, thr.vy, maxd.vy, mind.vy, true, psi3, pf3);
       } else {
         // :302-399 shocked_slope_limit
-        const Cell nb = load_cell(a.cells, static_cast<int>(w & kNbrIdMask));
+        const Cell nb = point_state(a, static_cast<int>(w & kNbrIdMask));
         shocked_comp(dphi.d, cv.d, cell.d, thr.d, nb.d, a.theta, psi0, pf0);
         shocked_comp(dphi.p, cv.p, cell.p, thr.p, nb.p, a.theta, psi1, pf1);
         shocked_comp(dphi.vx, cv.vx, cell.vx, thr.vx, nb.vx, a.theta, psi2, pf2);
@@ -551,6 +545,9 @@ __device__ __forceinline__ void k_slopes_item(const StepArgs& a, int i) {
 
 template <bool kBatch>
 __global__ void __launch_bounds__(kMaxBlock) k_slopes(StepArgs a) {
+  // the dt of this step, computed by the previous step's update (the face
+  // kernel, launched after this one, reads status->dt)
+  if (a.take_next_dt && blockIdx.x == 0 && threadIdx.x == 0) a.status->dt = a.status->dt_next;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.mesh.n; i += gridDim.x * blockDim.x)
     k_slopes_item<kBatch>(a, i);
 }
@@ -664,7 +661,7 @@ __device__ __forceinline__ void k_faces_lgi_item(const StepArgs& a, int e) {
 #pragma unroll
   for (int s = 0; s < 2; ++s) {
     const int pid = ids[s];
-    Cell c = load_cell(a.cells, pid);
+    Cell c = point_state(a, pid);
     int sid = pid;
     bool zero = false;
     if (pid >= m.n) {
@@ -684,7 +681,7 @@ __device__ __forceinline__ void k_faces_lgi_item(const StepArgs& a, int e) {
     addmult(c, gy, dms[s].y);
     side[s] = c;
   }
-  const double2 w = reinterpret_cast<const double2*>(a.ev)[e];
+  const double2 w = a.ev_zero ? make_double2(0.0, 0.0) : reinterpret_cast<const double2*>(a.ev)[e];
   const double2 n = a.geom.nrm[e], p = a.geom.par[e];
   const double na = a.geom.nabs[e], pa = a.geom.area[e];
   // a face at rest has speed +-0 (the sign only reaches signs of zeros)
@@ -737,7 +734,7 @@ __device__ __forceinline__ void k_faces_pcm_item(const StepArgs& a, int e) {
     l = to_prim(g, load_cell(a.cells, fc.x));
     r = to_prim(g, load_cell(a.cells, fc.y));
   }
-  const double2 w = reinterpret_cast<const double2*>(a.ev)[e];
+  const double2 w = a.ev_zero ? make_double2(0.0, 0.0) : reinterpret_cast<const double2*>(a.ev)[e];
   const double velocity = (w.x == 0.0 && w.y == 0.0) ? 0.0 : (n.x * w.x + n.y * w.y) / na;
   Cons c;
   if (!solve_face(l, r, velocity, n, na, p, pa, c, a, e)) return;
@@ -757,7 +754,8 @@ __global__ void __launch_bounds__(kMaxBlock) k_faces_pcm(StepArgs a) {
 // is the order the reference's edge loop applies them to that cell; then
 // SimpleCellUpdater::regular_update (simple_cell_updater.cpp:22-59).
 template <bool kBatch>
-__device__ __forceinline__ void k_update_item(const StepArgs& a, int i, int from_unscaled, int do_ext, int do_cells) {
+__device__ __forceinline__ unsigned long long k_update_item(const StepArgs& a, int i, int from_unscaled, int do_ext,
+                                                         int do_cells) {
   const MeshDev& m = a.mesh;
   double2* ext2 = reinterpret_cast<double2*>(a.ext);
   double2 e01 = ext2[2 * i], e23 = ext2[2 * i + 1];
@@ -806,16 +804,44 @@ __device__ __forceinline__ void k_update_item(const StepArgs& a, int i, int from
     const double d = mass / m.cd_volume[i];
     if (d < 0) {
       record_error(a.status, a.step, RG_ERR_NEGATIVE_DENSITY, 5, i, d);
-      return;
+      return kInfBits;
     }
     const double vx = px / mass, vy = py / mass;
     const double energy = en / mass - 0.5 * (vx * vx + vy * vy);
     if (energy < 0) {
       record_error(a.status, a.step, RG_ERR_NEGATIVE_ENERGY, 5, i, energy);
-      return;
+      return kInfBits;
     }
-    store4(a.cells_out ? a.cells_out : a.cells, i, d, (gamma_at<kBatch>(a, i) - 1) * energy * d, vx, vy);
+    const double pres = (gamma_at<kBatch>(a, i) - 1) * energy * d;
+    store4(a.cells_out ? a.cells_out : a.cells, i, d, pres, vx, vy);
+    if (a.cfl_next) {
+      // the next step's SimpleCFL bound of this cell, as k_cfl computes it
+      // from the record just stored
+      const double cs = sqrt(gamma_at<kBatch>(a, i) * pres / d);
+      double q = 0;
+      bool any = false;
+      if (a.ev_zero) {
+        const double qq = vx * vx + vy * vy;
+        if (m.cell_off[i + 1] > m.cell_off[i] && !isnan(qq)) {
+          q = fmax(q, qq);
+          any = true;
+        }
+      } else {
+        for (int k = m.cell_off[i]; k < m.cell_off[i + 1]; ++k) {
+          const double2 w = reinterpret_cast<const double2*>(a.ev)[m.cell_faces[k]];
+          const double dx = vx - w.x, dy = vy - w.y;
+          const double qq = dx * dx + dy * dy;
+          if (!isnan(qq)) {
+            q = fmax(q, qq);
+            any = true;
+          }
+        }
+      }
+      const double res = any ? fmax(0.0, (cs + sqrt(q)) / a.geom.width[i]) : 0.0;
+      return static_cast<unsigned long long>(__double_as_longlong(1.0 / res));
+    }
   }
+  return kInfBits;
 }
 
 template <bool kBatch>
@@ -831,7 +857,12 @@ __global__ void __launch_bounds__(kMaxBlock) k_update(StepArgs a, int from_unsca
       a.dtmin_p[p] = kInfBits;
     }
   }
-  for (int i = t0; i < a.mesh.n; i += stride) k_update_item<kBatch>(a, i, from_unscaled, do_ext, do_cells);
+  unsigned long long bits = kInfBits;
+  for (int i = t0; i < a.mesh.n; i += stride) {
+    const unsigned long long b = k_update_item<kBatch>(a, i, from_unscaled, do_ext, do_cells);
+    bits = b < bits ? b : bits;
+  }
+  if (!kBatch && a.cfl_next) grid_min_times(a.status, bits, a.cfl, &a.status->dt_next);
 }
 
 // hdsim2d.cpp:41-67 init_extensives
@@ -843,6 +874,15 @@ __global__ void __launch_bounds__(kBlock) k_init_ext(StepArgs a) {
   const double mass = a.mesh.cd_volume[i] * c.d;
   store4(a.ext, i, mass, c.p / c.d / (gamma_at<kBatch>(a, i) - 1) * mass + 0.5 * mass * (c.vx * c.vx + c.vy * c.vy),
          c.vx * mass, c.vy * mass);
+}
+
+// *flag = 1 if any of v[0..n) is not +-0 (NaN counts as nonzero)
+__global__ void __launch_bounds__(kBlock) k_any_nonzero(const double* v, long long n, int* flag) {
+  bool any = false;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x)
+    any = any || !(v[i] == 0.0);
+  if (__any_sync(0xffffffffu, any) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
 }
 
 inline int blocks(int n) { return (n + kBlock - 1) / kBlock; }
@@ -887,6 +927,14 @@ cudaError_t launch_problems(const MeshDev& m, const int* offsets, int P, int* ce
   const int work = m.n > m.g ? m.n : m.g;
   k_problems<<<blocks(work > 0 ? work : 1), kBlock, 0, s>>>(m, offsets, P, cell_problem, st);
   if (m.e > 0) k_check_problems<<<blocks(m.e), kBlock, 0, s>>>(m, cell_problem, st);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_any_nonzero(const double* v, long long n, int* flag, cudaStream_t s) {
+  if (n > 0) {
+    const long long nb = (n + kBlock - 1) / kBlock;
+    k_any_nonzero<<<static_cast<int>(nb < 4096 ? nb : 4096), kBlock, 0, s>>>(v, n, flag);
+  }
   return cudaGetLastError();
 }
 

@@ -61,7 +61,7 @@ struct SlotLayout {
   size_t points, cms, volume, cd_volume, ghost_source, ghost_face, face_cells, face_vertices, cell_off,
       cell_faces, input_end;
   size_t area, nrm, nabs, par, dm0, dm1, width, minv, cflags, nbr, hr, ghost_real, ghost_unit;
-  size_t nrm32, nabs32, par32, area32, dm0_32, dm1_32, width32, minv32, hr32, gunit32, icdv32, total;
+  size_t nrm32, nabs32, par32, area32, dm0_32, dm1_32, width32, minv32, ent32, fsign32, gunit32, icdv32, total;
   void compute(int n, int g, int e, int m, bool mixed) {
     const size_t np = static_cast<size_t>(n) + g;
     size_t o = 0;
@@ -103,7 +103,8 @@ struct SlotLayout {
     dm1_32 = take(k * 8 * static_cast<size_t>(e));
     width32 = take(k * 4 * static_cast<size_t>(n));
     minv32 = take(k * 16 * static_cast<size_t>(n));
-    hr32 = take(k * 8 * static_cast<size_t>(m));
+    ent32 = take(k * 16 * static_cast<size_t>(m));
+    fsign32 = take(k * 4 * static_cast<size_t>(m));
     gunit32 = take(k * 8 * static_cast<size_t>(g));
     icdv32 = take(k * 4 * static_cast<size_t>(n));
     total = o;
@@ -165,6 +166,17 @@ struct rg_handle {
   int step_seq = 0;
   // launch shapes of the per-step kernels (rg_autotune / rg_set_launch_shapes)
   rg::StepShapes shapes64, shapes32;
+  // Fused steps: the update kernel of a fused step also computes the next
+  // step's SimpleCFL dt (status->dt_next) from the cells it writes and the
+  // current face velocities, so the next fused step needs no CFL pass.  Any
+  // change of the cells, face velocities or mesh clears dt_next_ready; a
+  // caller with the device pointers (rg_device_buffers) may write them at
+  // any time, so fusing stops for that handle.
+  bool dt_next_ready = false;
+  bool external_state = false;
+  // every face velocity last set is +-0 (checked on the device when set)
+  bool ev_zero = false;
+  rgh::DevBuf flag_buf;
   // differentiation: checkpoints, recomputation buffers, reverse adjacency
   rg_adjoint_state* adj = nullptr;
 };

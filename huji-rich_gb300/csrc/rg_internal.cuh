@@ -87,6 +87,7 @@ struct DevStatus {
   double dt;                       // cfl * min, written by the last CFL block
   unsigned int blocks_done;        // CFL blocks finished (reset by the last one)
   int lock_timeouts;
+  double dt_next;                  // next step's dt, computed by the update of this one
 };
 constexpr unsigned long long kInfBits = 0x7ff0000000000000ull;
 
@@ -131,6 +132,39 @@ __device__ inline void record_error(DevStatus* st, int step, int status, int pha
 // std::min / std::max semantics
 __device__ __forceinline__ double smin(double a, double b) { return b < a ? b : a; }
 __device__ __forceinline__ double smax(double a, double b) { return a < b ? b : a; }
+
+constexpr int kMaxBlockWarps = 16;  // kMaxBlock / 32
+
+// Grid-wide minimum of non-negative doubles given as bit patterns (one value
+// per thread; every thread of the grid calls this once), then *out =
+// cfl * minimum, written by the last block to finish: SimpleCFL's
+// `cfl * min` (simple_cfl.cpp:58-71).  Leaves the reduction words reset.
+__device__ inline void grid_min_times(DevStatus* st, unsigned long long bits, double cfl, double* out) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long ob = __shfl_xor_sync(0xffffffffu, bits, o);
+    bits = ob < bits ? ob : bits;
+  }
+  __shared__ unsigned long long wmin[kMaxBlockWarps];
+  __shared__ bool last;
+  if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = bits;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long bm = wmin[0];
+    for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w) bm = wmin[w] < bm ? wmin[w] : bm;
+    atomicMin(&st->dt_min_bits, bm);
+    __threadfence();
+    last = atomicAdd(&st->blocks_done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    // every block's atomicMin is visible here (threadfence before its ticket)
+    __threadfence();
+    const unsigned long long mb = atomicAdd(&st->dt_min_bits, 0ull);
+    *out = cfl * __longlong_as_double(static_cast<long long>(mb));
+    st->dt_min_bits = kInfBits;  // ready for the next reduction
+    st->blocks_done = 0;
+  }
+}
 #endif
 
 // Launch shape of a per-item kernel (cells, faces): `block` threads per block
@@ -173,6 +207,9 @@ struct StepArgs {
   double dt_host;       // dt given by the caller (split API)
   int dt_from_device;   // 1: dt = cfl * min from status->dt_min_bits
   int step;             // step number within an rg_run (error ordering)
+  int cfl_next;         // the update also computes the next step's SimpleCFL dt (status->dt_next)
+  int ev_zero;          // every face velocity is +-0: kernels read none
+  int take_next_dt;     // the slopes kernel first moves status->dt_next to status->dt
   // batch of independent problems (cell_problem == nullptr: one problem)
   const int* cell_problem;        // n + g: problem of every point
   const double* gamma_p;          // per problem
@@ -221,6 +258,7 @@ struct GeomArgs {
   DevStatus* status;
 };
 
+cudaError_t launch_any_nonzero(const double* v, long long n, int* flag, cudaStream_t s);
 cudaError_t launch_validate(const MeshDev& m, DevStatus* st, cudaStream_t s);
 cudaError_t launch_problems(const MeshDev& m, const int* offsets, int P, int* cell_problem, DevStatus* st,
                             cudaStream_t s);

@@ -61,7 +61,12 @@ __global__ void __launch_bounds__(kBlock) k_geom32(MixedGeomArgs a) {
   }
   for (int k = t; k < a.m; k += stride) {
     const double2 h = g.hr[k];
-    a.hr[k] = make_float2(static_cast<float>(h.x), static_cast<float>(h.y));
+    const int e = a.cell_faces[k];
+    const bool first = g.nbr[k] & kNbrFirst;
+    const double2 d = first ? g.dm0[e] : g.dm1[e];
+    a.ent[k] = make_float4(static_cast<float>(h.x), static_cast<float>(h.y), static_cast<float>(d.x),
+                           static_cast<float>(d.y));
+    a.fsign[k] = e | (first ? static_cast<int>(0x80000000u) : 0);
   }
   for (int q = t; q < a.g; q += stride) {
     const double2 u = g.ghost_unit[q];
@@ -124,7 +129,7 @@ __device__ __forceinline__ float inv_gm1_32(const MixedArgs& a, int point) {
 }
 
 // Ghost state: RigidWallGenerator.cpp:5-15 reflection / PeriodicGhostGenerator copy.
-__device__ __forceinline__ void fill_ghost32(const MixedArgs& a, int q) {
+__device__ __forceinline__ float4 ghost_state32(const MixedArgs& a, int q) {
   float4 c = a.cells32[a.geom.ghost_real[q]];
   if (a.ghost_kind != RG_GHOST_PERIODIC) {
     const float2 u = a.g32.ghost_unit[q];
@@ -132,7 +137,14 @@ __device__ __forceinline__ void fill_ghost32(const MixedArgs& a, int q) {
     c.z -= u.x * s;
     c.w -= u.y * s;
   }
-  a.cells32[a.mesh.n + q] = c;
+  return c;
+}
+__device__ __forceinline__ void fill_ghost32(const MixedArgs& a, int q) { a.cells32[a.mesh.n + q] = ghost_state32(a, q); }
+// State of point p: a real cell's record, or a ghost's state formed from the
+// current state of its cell (the per-step kernels read no ghost records)
+__device__ __forceinline__ C4 point32(const MixedArgs& a, int p) {
+  const float4 v = p < a.mesh.n ? a.cells32[p] : ghost_state32(a, p - a.mesh.n);
+  return C4{v.x, v.y, v.z, v.w};
 }
 
 // SimpleCFL (simple_cfl.cpp:28-47, 58-71) in FP32.  max_e (c+|v-w_e|)/R is
@@ -151,10 +163,14 @@ __global__ void __launch_bounds__(kMaxBlock) k_cfl32(MixedArgs a, int fill_ghost
       const float cs = sqrtf(gamma32<kBatch>(a, t) * c.y / c.x);
       float q = 0.0f;
       const int b = m.cell_off[t], e1 = m.cell_off[t + 1];
-      for (int k = b; k < e1; ++k) {
-        const float2 w = a.ev32[m.cell_faces[k]];
-        const float dx = c.z - w.x, dy = c.w - w.y;
-        q = fmaxf(q, fmaf(dx, dx, dy * dy));
+      if (a.ev_zero) {
+        if (e1 > b) q = fmaxf(q, fmaf(c.z, c.z, c.w * c.w));
+      } else {
+        for (int k = b; k < e1; ++k) {
+          const float2 w = a.ev32[m.cell_faces[k]];
+          const float dx = c.z - w.x, dy = c.w - w.y;
+          q = fmaxf(q, fmaf(dx, dx, dy * dy));
+        }
       }
       const float res = (cs + sqrtf(q)) / a.g32.width[t];
       x = 1.0f / res;
@@ -168,27 +184,8 @@ __global__ void __launch_bounds__(kMaxBlock) k_cfl32(MixedArgs a, int fill_ghost
       bits = min(bits, __float_as_uint(x));
   }
   if (kBatch) return;
-  for (int o = 16; o > 0; o >>= 1) bits = min(bits, __shfl_xor_sync(0xffffffffu, bits, o));
-  __shared__ unsigned int wmin[kMaxBlock / 32];
-  __shared__ bool last;
-  if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = bits;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned int bm = wmin[0];
-    for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w) bm = min(bm, wmin[w]);
-    atomicMin(reinterpret_cast<unsigned long long*>(&a.status->dt_min_bits),
-              static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(__uint_as_float(bm)))));
-    __threadfence();
-    last = atomicAdd(&a.status->blocks_done, 1u) == gridDim.x - 1;
-  }
-  __syncthreads();
-  if (last && threadIdx.x == 0) {
-    __threadfence();
-    const unsigned long long mb = atomicAdd(&a.status->dt_min_bits, 0ull);
-    a.status->dt = a.cfl * __longlong_as_double(static_cast<long long>(mb));
-    a.status->dt_min_bits = kInfBits;
-    a.status->blocks_done = 0;
-  }
+  grid_min_times(a.status, static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(__uint_as_float(bits)))),
+                 a.cfl, &a.status->dt);
 }
 
 __global__ void __launch_bounds__(kBlock) k_ghost_fill32(MixedArgs a) {
@@ -222,30 +219,42 @@ __device__ __forceinline__ void k_slopes32_item(const MixedArgs& a, int i) {
   const C4 cell = ld4(a.cells32, i);
   const int b = m.cell_off[i], nn = m.cell_off[i + 1] - b;
   const float4 mi = a.g32.minv[i];
+  const bool boundary = a.geom.cflags[i] & kCellBoundarySlope;
+  // one pass over the neighbours: the gradient's sums, the neighbour
+  // max / min over all neighbours and over those that are not self-mirror
+  // ghosts (the unshocked limiter skips those, LinearGaussImproved.cpp:194-195)
+  // and the pressure-ratio shock test
+  C4 vx{0, 0, 0, 0}, vy{0, 0, 0, 0};
+  C4 amax = cell, amin = cell, nmax = cell, nmin = cell;
+  bool ratio_shock = false;
+  for (int k = 0; k < nn; ++k) {
+    const uint32_t w = a.geom.nbr[b + k];
+    const C4 nb = point32(a, static_cast<int>(w & kNbrIdMask));
+    const float4 en = a.g32.ent[b + k];
+    // boundary cells: least squares on differences (:401-422); others: the
+    // Green-Gauss sum of 0.5 r_ij (cell + neighbour) (:80-133)
+    const C4 s = boundary ? C4{nb.d - cell.d, nb.p - cell.p, nb.vx - cell.vx, nb.vy - cell.vy}
+                          : C4{cell.d + nb.d, cell.p + nb.p, cell.vx + nb.vx, cell.vy + nb.vy};
+    addm(vx, s, en.x);
+    addm(vy, s, en.y);
+    amax = C4{fmaxf(amax.d, nb.d), fmaxf(amax.p, nb.p), fmaxf(amax.vx, nb.vx), fmaxf(amax.vy, nb.vy)};
+    amin = C4{fminf(amin.d, nb.d), fminf(amin.p, nb.p), fminf(amin.vx, nb.vx), fminf(amin.vy, nb.vy)};
+    if (!(w & kNbrMirror)) {
+      nmax = C4{fmaxf(nmax.d, nb.d), fmaxf(nmax.p, nb.p), fmaxf(nmax.vx, nb.vx), fmaxf(nmax.vy, nb.vy)};
+      nmin = C4{fminf(nmin.d, nb.d), fminf(nmin.p, nb.p), fminf(nmin.vx, nb.vx), fminf(nmin.vy, nb.vy)};
+    }
+    // min(p, p_k) / max(p, p_k) < delta_p without the division
+    ratio_shock = ratio_shock || fminf(cell.p, nb.p) < a.delta_p * fmaxf(cell.p, nb.p);
+  }
   C4 sx, sy;
-  if (a.geom.cflags[i] & kCellBoundarySlope) {
-    C4 py{0, 0, 0, 0}, px{0, 0, 0, 0};
-    for (int k = 0; k < nn; ++k) {
-      const C4 nb = ld4(a.cells32, static_cast<int>(a.geom.nbr[b + k] & kNbrIdMask));
-      const float2 h = a.g32.hr[b + k];
-      const C4 df{nb.d - cell.d, nb.p - cell.p, nb.vx - cell.vx, nb.vy - cell.vy};
-      addm(py, df, h.y);
-      addm(px, df, h.x);
-    }
+  if (boundary) {
+    // vx, vy hold sum(df*dx), sum(df*dy); mi = (SxSy, Sx2, Sy2, den)
     const float inv = 1.0f / mi.w;
-    sx = C4{(py.d * mi.x - px.d * mi.z) * inv, (py.p * mi.x - px.p * mi.z) * inv,
-            (py.vx * mi.x - px.vx * mi.z) * inv, (py.vy * mi.x - px.vy * mi.z) * inv};
-    sy = C4{(px.d * mi.x - py.d * mi.y) * inv, (px.p * mi.x - py.p * mi.y) * inv,
-            (px.vx * mi.x - py.vx * mi.y) * inv, (px.vy * mi.x - py.vy * mi.y) * inv};
+    sx = C4{(vy.d * mi.x - vx.d * mi.z) * inv, (vy.p * mi.x - vx.p * mi.z) * inv,
+            (vy.vx * mi.x - vx.vx * mi.z) * inv, (vy.vy * mi.x - vx.vy * mi.z) * inv};
+    sy = C4{(vx.d * mi.x - vy.d * mi.y) * inv, (vx.p * mi.x - vy.p * mi.y) * inv,
+            (vx.vx * mi.x - vy.vx * mi.y) * inv, (vx.vy * mi.x - vy.vy * mi.y) * inv};
   } else {
-    C4 vx{0, 0, 0, 0}, vy{0, 0, 0, 0};
-    for (int k = 0; k < nn; ++k) {
-      const C4 nb = ld4(a.cells32, static_cast<int>(a.geom.nbr[b + k] & kNbrIdMask));
-      const float2 h = a.g32.hr[b + k];
-      const C4 s{cell.d + nb.d, cell.p + nb.p, cell.vx + nb.vx, cell.vy + nb.vy};
-      addm(vx, s, h.x);
-      addm(vy, s, h.y);
-    }
     sx = C4{vx.d * mi.x + vy.d * mi.y, vx.p * mi.x + vy.p * mi.y, vx.vx * mi.x + vy.vx * mi.y,
             vx.vy * mi.x + vy.vy * mi.y};
     sy = C4{vy.d * mi.w + vx.d * mi.z, vy.p * mi.w + vx.p * mi.z, vy.vx * mi.w + vx.vx * mi.z,
@@ -253,28 +262,8 @@ __device__ __forceinline__ void k_slopes32_item(const MixedArgs& a, int i) {
   }
   if (a.slf) {
     const float cs = sqrtf(gamma32<kBatch>(a, i) * cell.p / cell.d);
-    bool shock = (sx.vx + sy.vy) * a.g32.width[i] < (-a.delta_v) * cs;
-    if (!shock) {
-      // min(p, p_k) / max(p, p_k) < delta_p without the division
-      for (int k = 0; k < nn && !shock; ++k) {
-        const float np_ = a.cells32[static_cast<int>(a.geom.nbr[b + k] & kNbrIdMask)].y;
-        shock = fminf(cell.p, np_) < a.delta_p * fmaxf(cell.p, np_);
-      }
-    }
-    C4 cmax = cell, cmin = cell;
-    for (int k = 0; k < nn; ++k) {
-      const uint32_t w = a.geom.nbr[b + k];
-      if (!shock && (w & kNbrMirror)) continue;
-      const C4 nb = ld4(a.cells32, static_cast<int>(w & kNbrIdMask));
-      cmax.d = fmaxf(cmax.d, nb.d);
-      cmax.p = fmaxf(cmax.p, nb.p);
-      cmax.vx = fmaxf(cmax.vx, nb.vx);
-      cmax.vy = fmaxf(cmax.vy, nb.vy);
-      cmin.d = fminf(cmin.d, nb.d);
-      cmin.p = fminf(cmin.p, nb.p);
-      cmin.vx = fminf(cmin.vx, nb.vx);
-      cmin.vy = fminf(cmin.vy, nb.vy);
-    }
+    const bool shock = (sx.vx + sy.vy) * a.g32.width[i] < (-a.delta_v) * cs || ratio_shock;
+    const C4 cmax = shock ? amax : nmax, cmin = shock ? amin : nmin;
     const C4 maxd{cmax.d - cell.d, cmax.p - cell.p, cmax.vx - cell.vx, cmax.vy - cell.vy};
     const C4 mind{cmin.d - cell.d, cmin.p - cell.p, cmin.vx - cell.vx, cmin.vy - cell.vy};
     const float f = shock ? 0.1f : 0.05f;
@@ -282,12 +271,10 @@ __device__ __forceinline__ void k_slopes32_item(const MixedArgs& a, int i) {
                  f * fmaxf(fabsf(maxd.vx), fabsf(mind.vx)), f * fmaxf(fabsf(maxd.vy), fabsf(mind.vy))};
     float psi0 = 1, psi1 = 1, psi2 = 1, psi3 = 1;
     for (int k = 0; k < nn; ++k) {
-      const uint32_t w = a.geom.nbr[b + k];
-      const int e = m.cell_faces[b + k];
-      const float2 dm = (w & kNbrFirst) ? a.g32.dm0[e] : a.g32.dm1[e];
+      const float4 en = a.g32.ent[b + k];
       C4 cv = cell;
-      addm(cv, sx, dm.x);
-      addm(cv, sy, dm.y);
+      addm(cv, sx, en.z);
+      addm(cv, sy, en.w);
       const C4 dphi{cv.d - cell.d, cv.p - cell.p, cv.vx - cell.vx, cv.vy - cell.vy};
       if (!shock) {
         limit32(dphi.d, cv.d, cell.d, thr.d, maxd.d, mind.d, false, psi0);
@@ -295,7 +282,7 @@ __device__ __forceinline__ void k_slopes32_item(const MixedArgs& a, int i) {
         limit32(dphi.vx, cv.vx, cell.vx, thr.vx, maxd.vx, mind.vx, true, psi2);
         limit32(dphi.vy, cv.vy, cell.vy, thr.vy, maxd.vy, mind.vy, true, psi3);
       } else {
-        const C4 nb = ld4(a.cells32, static_cast<int>(w & kNbrIdMask));
+        const C4 nb = point32(a, static_cast<int>(a.geom.nbr[b + k] & kNbrIdMask));
         shocked32(dphi.d, cv.d, cell.d, thr.d, nb.d, a.theta, psi0);
         shocked32(dphi.p, cv.p, cell.p, thr.p, nb.p, a.theta, psi1);
         shocked32(dphi.vx, cv.vx, cell.vx, thr.vx, nb.vx, a.theta, psi2);
@@ -313,6 +300,8 @@ __device__ __forceinline__ void k_slopes32_item(const MixedArgs& a, int i) {
 
 template <bool kBatch>
 __global__ void __launch_bounds__(kMaxBlock) k_slopes32(MixedArgs a) {
+  // the dt of this step, computed by the previous step's update
+  if (a.take_next_dt && blockIdx.x == 0 && threadIdx.x == 0) a.status->dt = a.status->dt_next;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.mesh.n; i += gridDim.x * blockDim.x)
     k_slopes32_item<kBatch>(a, i);
 }
@@ -403,7 +392,7 @@ __device__ __forceinline__ void k_faces32_lgi_item(const MixedArgs& a, int e) {
 #pragma unroll
   for (int s = 0; s < 2; ++s) {
     const int pid = ids[s];
-    C4 c = ld4(a.cells32, pid);
+    C4 c = point32(a, pid);
     int sid = pid;
     bool zero = false;
     if (pid >= m.n) {
@@ -419,7 +408,7 @@ __device__ __forceinline__ void k_faces32_lgi_item(const MixedArgs& a, int e) {
     }
     side[s] = c;
   }
-  const float2 w = a.ev32[e];
+  const float2 w = a.ev_zero ? make_float2(0.0f, 0.0f) : a.ev32[e];
   const float2 n = a.g32.nrm[e], p = a.g32.par[e];
   const float na = a.g32.nabs[e], pa = a.g32.area[e];
   const float vel = (n.x * w.x + n.y * w.y) / na;
@@ -464,7 +453,7 @@ __device__ __forceinline__ void k_faces32_pcm_item(const MixedArgs& a, int e) {
     l = prim32(g, igm, ld4(a.cells32, fc.x));
     r = prim32(g, igm, ld4(a.cells32, fc.y));
   }
-  const float2 w = a.ev32[e];
+  const float2 w = a.ev_zero ? make_float2(0.0f, 0.0f) : a.ev32[e];
   const float vel = (n.x * w.x + n.y * w.y) / na;
   F4 c;
   if (!solve32(l, r, vel, n, na, p, pa, c, a, e)) return;
@@ -502,7 +491,8 @@ __device__ __forceinline__ void two_sum(float& s, float& c, float x) {
 // keep FP64 precision across steps.  e = E/m - v^2/2 is formed in FP64 with a
 // Newton-refined reciprocal of m.
 template <bool kBatch>
-__device__ __forceinline__ void k_update_mixed_item(const MixedArgs& a, int i, int from_unscaled, int do_ext, int do_cells) {
+__device__ __forceinline__ unsigned long long k_update_mixed_item(const MixedArgs& a, int i, int from_unscaled,
+                                                               int do_ext, int do_cells) {
   const MeshDev& m = a.mesh;
   double2* ext2 = reinterpret_cast<double2*>(a.ext);
   const double2 e01 = ext2[2 * i], e23 = ext2[2 * i + 1];
@@ -511,13 +501,14 @@ __device__ __forceinline__ void k_update_mixed_item(const MixedArgs& a, int i, i
     float s0 = 0, s1 = 0, s2 = 0, s3 = 0, c0 = 0, c1 = 0, c2 = 0, c3 = 0;
     const int b = m.cell_off[i], e1 = m.cell_off[i + 1];
     for (int k = b; k < e1; ++k) {
-      const int e = m.cell_faces[k];
+      const int fs = a.g32.fsign[k];
+      const int e = fs & 0x7fffffff;
       float4 f = a.flux32[e];
       if (from_unscaled) {
         const float sc = a.dt32 * a.g32.area[e];
         f = make_float4(f.x * sc, f.y * sc, f.z * sc, f.w * sc);
       }
-      if (a.geom.nbr[k] & kNbrFirst) f = make_float4(-f.x, -f.y, -f.z, -f.w);
+      if (fs < 0) f = make_float4(-f.x, -f.y, -f.z, -f.w);
       two_sum(s0, c0, f.x);
       two_sum(s1, c1, f.y);
       two_sum(s2, c2, f.z);
@@ -544,21 +535,40 @@ __device__ __forceinline__ void k_update_mixed_item(const MixedArgs& a, int i, i
     const float d = mf * a.g32.inv_cd_volume[i];
     if (d < 0.0f) {
       record_error(a.status, a.step, RG_ERR_NEGATIVE_DENSITY, 5, i, d);
-      return;
+      return kInfBits;
     }
+    // 1/m: the FP32 reciprocal (relative error < 2^-23) and one Newton step
+    // (relative error < 2^-45, far below the FP32 rounding of the results)
     double r = static_cast<double>(1.0f / mf);
-    r = r * (2.0 - mass * r);
     r = r * (2.0 - mass * r);
     const double kin = 0.5 * (px * px + py * py) * r;
     const double energy = (en - kin) * r;
     if (energy < 0) {
       record_error(a.status, a.step, RG_ERR_NEGATIVE_ENERGY, 5, i, energy);
-      return;
+      return kInfBits;
     }
-    (a.cells32_out ? a.cells32_out : a.cells32)[i] =
-        make_float4(d, (gamma32<kBatch>(a, i) - 1.0f) * static_cast<float>(energy) * d, static_cast<float>(px * r),
-                    static_cast<float>(py * r));
+    const float4 c = make_float4(d, (gamma32<kBatch>(a, i) - 1.0f) * static_cast<float>(energy) * d,
+                                 static_cast<float>(px * r), static_cast<float>(py * r));
+    (a.cells32_out ? a.cells32_out : a.cells32)[i] = c;
+    if (a.cfl_next) {
+      // the next step's SimpleCFL bound of this cell, as k_cfl32 computes it
+      // from the record just stored
+      const float cs = sqrtf(gamma32<kBatch>(a, i) * c.y / c.x);
+      float q = 0.0f;
+      if (a.ev_zero) {
+        if (m.cell_off[i + 1] > m.cell_off[i]) q = fmaxf(q, fmaf(c.z, c.z, c.w * c.w));
+      } else {
+        for (int k = m.cell_off[i]; k < m.cell_off[i + 1]; ++k) {
+          const float2 w = a.ev32[a.g32.fsign[k] & 0x7fffffff];
+          const float dx = c.z - w.x, dy = c.w - w.y;
+          q = fmaxf(q, fmaf(dx, dx, dy * dy));
+        }
+      }
+      const float res = (cs + sqrtf(q)) / a.g32.width[i];
+      return static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(1.0f / res)));
+    }
   }
+  return kInfBits;
 }
 
 template <bool kBatch>
@@ -572,7 +582,12 @@ __global__ void __launch_bounds__(kMaxBlock) k_update_mixed(MixedArgs a, int fro
       a.dtmin_p[p] = kInfBits;
     }
   }
-  for (int i = t0; i < a.mesh.n; i += stride) k_update_mixed_item<kBatch>(a, i, from_unscaled, do_ext, do_cells);
+  unsigned long long bits = kInfBits;
+  for (int i = t0; i < a.mesh.n; i += stride) {
+    const unsigned long long b = k_update_mixed_item<kBatch>(a, i, from_unscaled, do_ext, do_cells);
+    bits = b < bits ? b : bits;
+  }
+  if (!kBatch && a.cfl_next) grid_min_times(a.status, bits, a.cfl, &a.status->dt_next);
 }
 
 inline int blocks(int n) { return (n + kBlock - 1) / kBlock; }

@@ -16,7 +16,13 @@ struct MixedGeom {
   const float2* dm1;
   const float* width;
   const float4* minv;
-  const float2* hr;
+  // per CSR entry (cell i, face k): {hr.x, hr.y, dm.x, dm.y} with hr the LGI
+  // stencil vector (0.5 r_ij, or the CM offset of a boundary-slope cell) and
+  // dm = face centroid - CM of cell i; one 16-byte record read in order
+  const float4* ent;
+  // per CSR entry: face index, bit 31 set when the cell is the face's first
+  // neighbour (the flux enters with a minus sign)
+  const int* fsign;
   const float2* ghost_unit;
   const float* inv_cd_volume;
 };
@@ -33,7 +39,9 @@ struct MixedGeomArgs {
   float2* dm1;
   float* width;
   float4* minv;
-  float2* hr;
+  float4* ent;
+  int* fsign;
+  const int* cell_faces;
   float2* ghost_unit;
   float* inv_cd_volume;
 };
@@ -59,6 +67,9 @@ struct MixedArgs {
   float dt32;            // dt given by the caller (split API)
   int dt32_from_device;  // 1: dt from status->dt (fused step)
   int step;
+  int cfl_next;          // the update also computes the next step's dt (status->dt_next)
+  int ev_zero;          // every face velocity is +-0: kernels read none
+  int take_next_dt;      // the slopes kernel first moves status->dt_next to status->dt
   // batch of independent problems (cell_problem == nullptr: one problem)
   const int* cell_problem;
   const float* gamma_p;     // per problem

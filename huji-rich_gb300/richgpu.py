@@ -24,7 +24,7 @@ EXPORTS = ("rg_default_config", "rg_create", "rg_destroy", "rg_status_string", "
            "rg_extensive_update", "rg_cell_update", "rg_step", "rg_run", "rg_step_async",
            "rg_synchronize", "rg_step_timed", "rg_cfl_dt_noalloc", "rg_set_problems",
            "rg_get_problem_times", "rg_run_graph", "rg_step_fwd", "rg_step_bwd", "rg_step_tlm",
-           "rg_autotune", "rg_set_launch_shapes", "rg_get_launch_shapes")
+           "rg_autotune", "rg_set_launch_shapes", "rg_get_launch_shapes", "rg_stream")
 
 KERNELS = ("cfl", "slopes", "faces", "update")
 
@@ -92,6 +92,7 @@ def load(path=LIB_PATH):
     lib.rg_step_bwd.argtypes = [vp, dp, dp]
     lib.rg_step_tlm.argtypes = [vp, C.c_int32, C.c_double, dp, dp]
     lib.rg_autotune.argtypes = [vp, C.c_int32, C.POINTER(RgLaunchShapes)]
+    lib.rg_stream.argtypes = [vp, C.POINTER(vp)]
     lib.rg_set_launch_shapes.argtypes = [vp, C.POINTER(RgLaunchShapes)]
     lib.rg_get_launch_shapes.argtypes = [vp, C.POINTER(RgLaunchShapes)]
     _lib = lib
@@ -185,6 +186,12 @@ class Handle:
         v = RgDeviceView()
         self._check(self.lib.rg_device_buffers(self.h, C.byref(v)))
         return v
+
+    def stream(self):
+        """The handle's CUDA stream (an integer handle), without handing out state."""
+        v = C.c_void_p()
+        self._check(self.lib.rg_stream(self.h, C.byref(v)))
+        return v.value
 
     def init_extensives(self):
         self._check(self.lib.rg_init_extensives(self.h))

@@ -245,6 +245,11 @@ rg_status rg_get_problem_times(rg_handle* h, double* time_out, double* dt_last_o
  * with step 0 in its key. */
 rg_status rg_run_graph(rg_handle* h, int32_t n_steps);
 
+/* The CUDA stream (cudaStream_t) all kernels of the handle run on, for
+ * callers that order their own work with the handle's (no reference
+ * counterpart).  Unlike rg_device_buffers it hands out no state pointers. */
+rg_status rg_stream(const rg_handle* h, void** stream);
+
 /* Launch shapes and the autotuner ------------------------------------------ */
 /* No counterpart in the reference.  The per-step kernels (rg_kernel order:
  * CFL, slopes, face fluxes, gather+update) of the handle's current path

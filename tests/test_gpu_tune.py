@@ -128,3 +128,44 @@ def test_invalid_shapes_are_rejected():
             with pytest.raises(richgpu.RichError) as ei:
                 h.set_launch_shapes(bad)
             assert ei.value.status == 1
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_fused_steps_equal_steps_with_a_cfl_pass(precision):
+    """A fused step takes its dt from the previous step's update; a handle
+    whose device buffers were handed out (fusion off) runs the CFL pass every
+    step.  Both give the same states and dts bit for bit."""
+    mesh, cells, ext = sedov(128)
+    outs = []
+    for external in (False, True):
+        with richgpu.Handle(gamma=5 / 3, order=2, ghost_kind=0, precision=precision, device=0) as h:
+            h.upload_mesh(mesh)
+            if external:
+                h.device_buffers()
+            h.set_cells(cells)
+            h.set_extensives(ext)
+            h.set_edge_velocities(np.zeros((mesh.n_faces, 2)))
+            dts = list(h.run(7))
+            dts += [h.step() for _ in range(3)]
+            h.run_graph(4)
+            outs.append((h.get_cells(), h.get_extensives(), np.array(dts)))
+    for a, b in zip(outs[0], outs[1]):
+        exact(a, b)
+
+
+def test_new_face_velocities_reach_the_next_dt():
+    """Setting face velocities between fused steps: the next step's dt is the
+    SimpleCFL dt of the new velocities (FP64, equal to the oracle's)."""
+    mesh, cells, ext = sedov(96)
+    rng = np.random.default_rng(8)
+    with richgpu.Handle(gamma=5 / 3, order=2, ghost_kind=0, device=0) as h:
+        h.upload_mesh(mesh)
+        h.set_cells(cells)
+        h.set_extensives(ext)
+        h.set_edge_velocities(np.zeros((mesh.n_faces, 2)))
+        h.run(3)
+        ev = synthetic.face_velocities(mesh, rng.normal(0, 0.5, (mesh.n_cells, 2)))
+        h.set_edge_velocities(ev)
+        c3 = h.get_cells()
+        dt = h.step()
+    assert dt == oracle.cfl(mesh, c3, ev, 5 / 3)
