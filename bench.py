@@ -377,12 +377,12 @@ def run_gpu(args, world, rank, local_rank):
                         "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                         "steps": r32["e2e_steps"], "upload_ms_mean": r32["upload_ms"]},
                 "gpu_launches": 4 * k, "clocks": r32["clock"],
-                "launch_shapes": {kk: [v["block"], v["max_blocks"]] for kk, v in r32["shapes"].items()},
+                "launch_shapes": {kk: [v["block"], v["max_blocks"], v["variant"]] for kk, v in r32["shapes"].items()},
                 "faces_per_s": world * mesh.n_faces * k / (r32["total_ms"] * 1e-3),
                 "fp64": {"value": value64, "ms_per_step": r64["total_ms"] / k, "dtype": "f64",
                          "bit_exact_vs_reference": True, "roofline": roofline(r64, mesh, 0),
                          "note": "plain FP64 path: bound by GB300's FP64 pipe (2 DFMA/clk/SM), not HBM",
-                         "launch_shapes": {kk: [v["block"], v["max_blocks"]] for kk, v in r64["shapes"].items()},
+                         "launch_shapes": {kk: [v["block"], v["max_blocks"], v["variant"]] for kk, v in r64["shapes"].items()},
                          "e2e": {"value": world * n * r64["e2e_steps"] / r64["e2e_s"], "unit": UNIT,
                                  "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
                          "clocks": r64["clock"]},
@@ -513,7 +513,7 @@ def run_batch(args, world, rank, local_rank):
         times, _ = h.problem_times()
         res[precision] = {"ms_per_step": float(kms.sum(1).mean()), "kernel_ms": kms.mean(0).tolist(),
                           "graph_ms_per_step": graph_ms, "final_cells": h.get_cells(),
-                          "launch_shapes": {kk: [v["block"], v["max_blocks"]] for kk, v in shapes.items()},
+                          "launch_shapes": {kk: [v["block"], v["max_blocks"], v["variant"]] for kk, v in shapes.items()},
                           "time_min": float(times.min()), "time_max": float(times.max())}
         h.close()
     c32, c64 = res[1].pop("final_cells"), res[0].pop("final_cells")

@@ -88,6 +88,7 @@ struct DevStatus {
   unsigned int blocks_done;        // CFL blocks finished (reset by the last one)
   int lock_timeouts;
   double dt_next;                  // next step's dt, computed by the update of this one
+  float dt32, dt_next32;           // the same rounded to FP32 (FP32-mixed face kernels)
 };
 constexpr unsigned long long kInfBits = 0x7ff0000000000000ull;
 
@@ -139,7 +140,8 @@ constexpr int kMaxBlockWarps = 16;  // kMaxBlock / 32
 // per thread; every thread of the grid calls this once), then *out =
 // cfl * minimum, written by the last block to finish: SimpleCFL's
 // `cfl * min` (simple_cfl.cpp:58-71).  Leaves the reduction words reset.
-__device__ inline void grid_min_times(DevStatus* st, unsigned long long bits, double cfl, double* out) {
+__device__ inline void grid_min_times(DevStatus* st, unsigned long long bits, double cfl, double* out,
+                                      float* out32 = nullptr) {
   for (int o = 16; o > 0; o >>= 1) {
     const unsigned long long ob = __shfl_xor_sync(0xffffffffu, bits, o);
     bits = ob < bits ? ob : bits;
@@ -161,6 +163,7 @@ __device__ inline void grid_min_times(DevStatus* st, unsigned long long bits, do
     __threadfence();
     const unsigned long long mb = atomicAdd(&st->dt_min_bits, 0ull);
     *out = cfl * __longlong_as_double(static_cast<long long>(mb));
+    if (out32) *out32 = static_cast<float>(*out);
     st->dt_min_bits = kInfBits;  // ready for the next reduction
     st->blocks_done = 0;
   }
@@ -174,11 +177,18 @@ __device__ inline void grid_min_times(DevStatus* st, unsigned long long bits, do
 // depend on the shape: every item is computed by one thread from the same
 // inputs, and the only cross-item reductions are minima.
 constexpr int kMaxBlock = 512;
+// variant: 0 the kernel's plain build (blocks of up to kMaxBlock threads);
+// the FP32-mixed slopes kernel also has 1, its neighbour loops unrolled by
+// two, and 2 and 3, register-capped builds for blocks of up to 256 threads
+// with 5 or 6 blocks resident per SM (more warps in flight against fewer
+// registers per thread).
 struct LaunchShape {
   int block;
   int max_blocks;
+  int variant;
 };
-constexpr LaunchShape kDefaultShape{256, 0};
+constexpr LaunchShape kDefaultShape{256, 0, 0};
+constexpr int kCappedBlock = 256;
 inline int grid_of(const LaunchShape& s, int items) {
   const int need = items > 0 ? (items + s.block - 1) / s.block : 1;
   return s.max_blocks > 0 && need > s.max_blocks ? s.max_blocks : need;

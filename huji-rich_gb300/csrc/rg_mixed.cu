@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_cfl32(MixedArgs a, int fill_ghost
   }
   if (kBatch) return;
   grid_min_times(a.status, static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(__uint_as_float(bits)))),
-                 a.cfl, &a.status->dt);
+                 a.cfl, &a.status->dt, &a.status->dt32);
 }
 
 __global__ void __launch_bounds__(kBlock) k_ghost_fill32(MixedArgs a) {
@@ -213,7 +213,7 @@ __device__ __forceinline__ void shocked32(float dphi, float cv, float cellv, flo
 }
 
 // LinearGaussImproved::calc_slope (LinearGaussImproved.cpp:425-494) in FP32.
-template <bool kBatch>
+template <bool kBatch, int kUnroll>
 __device__ __forceinline__ void k_slopes32_item(const MixedArgs& a, int i) {
   const MeshDev& m = a.mesh;
   const C4 cell = ld4(a.cells32, i);
@@ -227,6 +227,7 @@ __device__ __forceinline__ void k_slopes32_item(const MixedArgs& a, int i) {
   C4 vx{0, 0, 0, 0}, vy{0, 0, 0, 0};
   C4 amax = cell, amin = cell, nmax = cell, nmin = cell;
   bool ratio_shock = false;
+#pragma unroll(kUnroll)
   for (int k = 0; k < nn; ++k) {
     const uint32_t w = a.geom.nbr[b + k];
     const C4 nb = point32(a, static_cast<int>(w & kNbrIdMask));
@@ -270,6 +271,7 @@ __device__ __forceinline__ void k_slopes32_item(const MixedArgs& a, int i) {
     const C4 thr{f * fmaxf(fabsf(maxd.d), fabsf(mind.d)), f * fmaxf(fabsf(maxd.p), fabsf(mind.p)),
                  f * fmaxf(fabsf(maxd.vx), fabsf(mind.vx)), f * fmaxf(fabsf(maxd.vy), fabsf(mind.vy))};
     float psi0 = 1, psi1 = 1, psi2 = 1, psi3 = 1;
+#pragma unroll(kUnroll)
     for (int k = 0; k < nn; ++k) {
       const float4 en = a.g32.ent[b + k];
       C4 cv = cell;
@@ -298,12 +300,16 @@ __device__ __forceinline__ void k_slopes32_item(const MixedArgs& a, int i) {
   a.slopes32[2 * i + 1] = make_float4(sy.d, sy.p, sy.vx, sy.vy);
 }
 
-template <bool kBatch>
-__global__ void __launch_bounds__(kMaxBlock) k_slopes32(MixedArgs a) {
+template <bool kBatch, int kMinBlocks, int kUnroll>
+__global__ void __launch_bounds__(kMinBlocks ? kCappedBlock : kMaxBlock, kMinBlocks ? kMinBlocks : 1)
+    k_slopes32(MixedArgs a) {
   // the dt of this step, computed by the previous step's update
-  if (a.take_next_dt && blockIdx.x == 0 && threadIdx.x == 0) a.status->dt = a.status->dt_next;
+  if (a.take_next_dt && blockIdx.x == 0 && threadIdx.x == 0) {
+    a.status->dt = a.status->dt_next;
+    a.status->dt32 = a.status->dt_next32;
+  }
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.mesh.n; i += gridDim.x * blockDim.x)
-    k_slopes32_item<kBatch>(a, i);
+    k_slopes32_item<kBatch, kUnroll>(a, i);
 }
 
 __device__ __forceinline__ P6 prim32(float g, float inv_gm1, const C4& c) {
@@ -377,7 +383,7 @@ __device__ __forceinline__ void write32(const MixedArgs& a, int e, int real_side
       s = static_cast<float>(a.cfl * __longlong_as_double(static_cast<long long>(
                                           a.dtmin_p[a.cell_problem[real_side]]))) * area;
     else
-      s = a.dt32_from_device ? static_cast<float>(a.status->dt) * area : a.dt32 * area;
+      s = (a.dt32_from_device ? a.status->dt32 : a.dt32) * area;
   }
   a.flux32[e] = make_float4(c.m * s, c.en * s, c.mx * s, c.my * s);
 }
@@ -474,6 +480,20 @@ __global__ void __launch_bounds__(kMaxBlock) k_faces32_pcm(MixedArgs a) {
     k_faces32_pcm_item<kScaled, kBatch>(a, e);
 }
 
+// float -> double on the integer pipe.  GB300 issues FP64-pipe instructions,
+// conversions included, at 2 per clock per SM against 64 for integer ones,
+// and the update kernel is bound by that pipe.  Exact for zeros, normal
+// floats, infinities and NaNs; a subnormal float (below 1.2e-38 in
+// magnitude) becomes a zero of its sign.
+__device__ __forceinline__ double widen(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned ex = (u >> 23) & 0xffu;
+  const unsigned dex = ex == 0u ? 0u : (ex == 0xffu ? 0x7ffu : ex + 896u);  // rebias 127 -> 1023
+  const unsigned mant = ex == 0u ? 0u : (u & 0x7fffffu);
+  const unsigned hi = (u & 0x80000000u) | (dex << 20) | (mant >> 3);
+  return __hiloint2double(static_cast<int>(hi), static_cast<int>(mant << 29));
+}
+
 // Error-free FP32 addition (Knuth's TwoSum): s + x == s' + err exactly.
 __device__ __forceinline__ void two_sum(float& s, float& c, float x) {
   const float t = s + x;
@@ -514,10 +534,10 @@ __device__ __forceinline__ unsigned long long k_update_mixed_item(const MixedArg
       two_sum(s2, c2, f.z);
       two_sum(s3, c3, f.w);
     }
-    mass += static_cast<double>(s0) + static_cast<double>(c0);
-    en += static_cast<double>(s1) + static_cast<double>(c1);
-    px += static_cast<double>(s2) + static_cast<double>(c2);
-    py += static_cast<double>(s3) + static_cast<double>(c3);
+    mass += widen(s0) + widen(c0);
+    en += widen(s1) + widen(c1);
+    px += widen(s2) + widen(c2);
+    py += widen(s3) + widen(c3);
     if (a.ext_avg) {
       const double2* o = reinterpret_cast<const double2*>(a.ext_avg);
       const double2 o01 = o[2 * i], o23 = o[2 * i + 1];
@@ -539,16 +559,17 @@ __device__ __forceinline__ unsigned long long k_update_mixed_item(const MixedArg
     }
     // 1/m: the FP32 reciprocal (relative error < 2^-23) and one Newton step
     // (relative error < 2^-45, far below the FP32 rounding of the results)
-    double r = static_cast<double>(1.0f / mf);
+    double r = widen(1.0f / mf);
     r = r * (2.0 - mass * r);
-    const double kin = 0.5 * (px * px + py * py) * r;
-    const double energy = (en - kin) * r;
+    // e = E/m - v^2/2 in FP64 (the cancellation at high Mach numbers)
+    const double vx = px * r, vy = py * r;
+    const double energy = en * r - 0.5 * (vx * vx + vy * vy);
     if (energy < 0) {
       record_error(a.status, a.step, RG_ERR_NEGATIVE_ENERGY, 5, i, energy);
       return kInfBits;
     }
     const float4 c = make_float4(d, (gamma32<kBatch>(a, i) - 1.0f) * static_cast<float>(energy) * d,
-                                 static_cast<float>(px * r), static_cast<float>(py * r));
+                                 static_cast<float>(vx), static_cast<float>(vy));
     (a.cells32_out ? a.cells32_out : a.cells32)[i] = c;
     if (a.cfl_next) {
       // the next step's SimpleCFL bound of this cell, as k_cfl32 computes it
@@ -587,7 +608,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_update_mixed(MixedArgs a, int fro
     const unsigned long long b = k_update_mixed_item<kBatch>(a, i, from_unscaled, do_ext, do_cells);
     bits = b < bits ? b : bits;
   }
-  if (!kBatch && a.cfl_next) grid_min_times(a.status, bits, a.cfl, &a.status->dt_next);
+  if (!kBatch && a.cfl_next) grid_min_times(a.status, bits, a.cfl, &a.status->dt_next, &a.status->dt_next32);
 }
 
 inline int blocks(int n) { return (n + kBlock - 1) / kBlock; }
@@ -636,10 +657,17 @@ cudaError_t launch_ghost_fill32(const MixedArgs& a, cudaStream_t s) {
 }
 cudaError_t launch_slopes32(const MixedArgs& a, cudaStream_t s) {
   if (a.mesh.n > 0) {
-    if (a.cell_problem)
-      k_slopes32<true><<<grid_of(a.shapes.slopes, a.mesh.n), a.shapes.slopes.block, 0, s>>>(a);
-    else
-      k_slopes32<false><<<grid_of(a.shapes.slopes, a.mesh.n), a.shapes.slopes.block, 0, s>>>(a);
+    const LaunchShape& sh = a.shapes.slopes;
+    const int nb = grid_of(sh, a.mesh.n), bs = sh.block;
+    const bool b = a.cell_problem != nullptr;
+    // builds: 0 plain, 1 neighbour loops unrolled by 2, 2 and 3 register-capped
+    // for 5 and 6 resident blocks of up to 256 threads
+    switch (sh.variant) {
+      case 1: b ? k_slopes32<true, 0, 2><<<nb, bs, 0, s>>>(a) : k_slopes32<false, 0, 2><<<nb, bs, 0, s>>>(a); break;
+      case 2: b ? k_slopes32<true, 5, 1><<<nb, bs, 0, s>>>(a) : k_slopes32<false, 5, 1><<<nb, bs, 0, s>>>(a); break;
+      case 3: b ? k_slopes32<true, 6, 1><<<nb, bs, 0, s>>>(a) : k_slopes32<false, 6, 1><<<nb, bs, 0, s>>>(a); break;
+      default: b ? k_slopes32<true, 0, 1><<<nb, bs, 0, s>>>(a) : k_slopes32<false, 0, 1><<<nb, bs, 0, s>>>(a);
+    }
   }
   return cudaGetLastError();
 }

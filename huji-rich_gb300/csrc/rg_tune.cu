@@ -2,7 +2,10 @@
 // (rg_autotune, rg_set_launch_shapes, rg_get_launch_shapes).
 //
 // Candidates per kernel: 64, 128, 256 or 512 threads per block, times one
-// thread per item or a persistent grid of 2, 4 or 8 blocks per SM.  Each
+// thread per item or a persistent grid of 2, 4 or 8 blocks per SM, times the
+// kernel's builds (the FP32-mixed slopes kernel also has a build with its
+// neighbour loops unrolled by two and two register-capped builds, for blocks
+// of up to 256 threads).  Each
 // candidate runs `reps` launches on the handle's stream, on the uploaded mesh
 // and the current state, each timed alone with CUDA events after a write of
 // a buffer larger than L2 (a kernel of a step finds most of its inputs in
@@ -39,6 +42,7 @@ void to_c(const rg::StepShapes& s, rg_launch_shapes* out) {
   for (int k = 0; k < 4; ++k) {
     out->block[k] = slot(c, k)->block;
     out->max_blocks[k] = slot(c, k)->max_blocks;
+    out->variant[k] = slot(c, k)->variant;
   }
 }
 
@@ -76,10 +80,14 @@ rg_status launch_one(rg_handle* h, int k, const rg::LaunchShape& sh, void* ext_s
   return RG_OK;
 }
 
+int n_variants(const rg_handle* h, int k) { return h->mixed && k == RG_KERNEL_SLOPES ? 4 : 1; }
+bool capped(int k, int v) { return k == RG_KERNEL_SLOPES && v >= 2; }
+
 rg_status check_shapes(rg_handle* h, const rg_launch_shapes* s) {
   for (int k = 0; k < 4; ++k) {
-    const int b = s->block[k];
+    const int b = s->block[k], v = s->variant[k];
     if (b < 32 || b > rg::kMaxBlock || b % 32 != 0 || s->max_blocks[k] < 0) return invalid(h, k, b);
+    if (v < 0 || v >= n_variants(h, k) || (capped(k, v) && b > rg::kCappedBlock)) return invalid(h, k, v);
   }
   return RG_OK;
 }
@@ -93,7 +101,7 @@ rg_status rg_set_launch_shapes(rg_handle* h, const rg_launch_shapes* s) {
   h->last = rg_error{};
   if (rg_status st = check_shapes(h, s)) return st;
   rg::StepShapes& dst = path_shapes(h);
-  for (int k = 0; k < 4; ++k) *slot(dst, k) = rg::LaunchShape{s->block[k], s->max_blocks[k]};
+  for (int k = 0; k < 4; ++k) *slot(dst, k) = rg::LaunchShape{s->block[k], s->max_blocks[k], s->variant[k]};
   drop_graph(h);
   return RG_OK;
 }
@@ -136,9 +144,11 @@ rg_status rg_autotune(rg_handle* h, int32_t reps, rg_launch_shapes* chosen) {
   for (int k = 0; k < 4; ++k) {
     float best = 0;
     rg::LaunchShape best_shape = *slot(cur, k);
+    for (int v = 0; v < n_variants(h, k); ++v)
     for (int b : kBlocks) {
+      if (capped(k, v) && b > rg::kCappedBlock) continue;
       for (int per_sm : kPerSm) {
-        const rg::LaunchShape sh{b, per_sm * sms};
+        const rg::LaunchShape sh{b, per_sm * sms, v};
         RG_TRY(launch_one(h, k, sh, ext_scr.p, cells_scr.p));  // warm
         float ms = 0;
         for (int r = 0; r < reps; ++r) {

@@ -30,7 +30,8 @@ KERNELS = ("cfl", "slopes", "faces", "update")
 
 
 class RgLaunchShapes(C.Structure):
-    _fields_ = [("block", C.c_int32 * 4), ("max_blocks", C.c_int32 * 4), ("ms", C.c_float * 4)]
+    _fields_ = [("block", C.c_int32 * 4), ("max_blocks", C.c_int32 * 4), ("variant", C.c_int32 * 4),
+                ("ms", C.c_float * 4)]
 
 
 class RgDeviceView(C.Structure):
@@ -282,7 +283,7 @@ class Handle:
     # launch shapes of the per-step kernels
     @staticmethod
     def _shapes_dict(r):
-        return {k: {"block": r.block[i], "max_blocks": r.max_blocks[i], "ms": r.ms[i]}
+        return {k: {"block": r.block[i], "max_blocks": r.max_blocks[i], "variant": r.variant[i], "ms": r.ms[i]}
                 for i, k in enumerate(KERNELS)}
 
     def autotune(self, reps=5):
@@ -297,10 +298,11 @@ class Handle:
         return self._shapes_dict(r)
 
     def set_launch_shapes(self, shapes):
-        """shapes: {kernel: (block, max_blocks)} for some of KERNELS."""
+        """shapes: {kernel: (block, max_blocks[, variant])} for some of KERNELS."""
         r = RgLaunchShapes()
         self._check(self.lib.rg_get_launch_shapes(self.h, C.byref(r)))
-        for k, (b, mb) in shapes.items():
+        for k, shape in shapes.items():
             i = KERNELS.index(k)
-            r.block[i], r.max_blocks[i] = b, mb
+            r.block[i], r.max_blocks[i] = shape[0], shape[1]
+            r.variant[i] = shape[2] if len(shape) > 2 else 0
         self._check(self.lib.rg_set_launch_shapes(self.h, C.byref(r)))

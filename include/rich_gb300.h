@@ -261,7 +261,10 @@ typedef enum { RG_KERNEL_CFL = 0, RG_KERNEL_SLOPES = 1, RG_KERNEL_FACES = 2, RG_
 typedef struct {
   int32_t block[4];
   int32_t max_blocks[4];
-  float ms[4]; /* rg_autotune: mean time per launch of the chosen shape (ms) */
+  int32_t variant[4]; /* build: 0; the FP32-mixed slopes kernel also has 1 (loops unrolled
+                         by two) and 2, 3 (register-capped: blocks of at most 256 threads,
+                         5 or 6 resident per SM) */
+  float ms[4];        /* rg_autotune: mean time per launch of the chosen shape (ms) */
 } rg_launch_shapes;
 /* Times every candidate shape of each per-step kernel on the uploaded mesh
  * and the current state (reps launches each; the state is left unchanged)

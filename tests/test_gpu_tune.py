@@ -20,6 +20,12 @@ SHAPES = [
     {"cfl": (512, 152), "slopes": (64, 304), "faces": (256, 152), "update": (128, 608)},
     {"cfl": (32, 7), "slopes": (96, 5), "faces": (480, 3), "update": (64, 1)},
 ]
+# the FP32-mixed slopes kernel's other builds (unrolled, register-capped)
+MIXED_SHAPES = [{"slopes": (128, 0, 1)}, {"slopes": (256, 608, 2)}, {"slopes": (64, 0, 3)}]
+
+
+def shapes_for(precision):
+    return SHAPES + (MIXED_SHAPES if precision == 1 else [])
 
 
 def sedov(n=160):
@@ -46,7 +52,7 @@ def run(mesh, cells, ext, precision, shapes, steps=12, heun=0, order=2):
 def test_results_do_not_depend_on_the_launch_shape(precision, order, heun):
     mesh, cells, ext = sedov()
     ref = run(mesh, cells, ext, precision, None, heun=heun, order=order)
-    for shapes in SHAPES:
+    for shapes in shapes_for(precision):
         got = run(mesh, cells, ext, precision, shapes, heun=heun, order=order)
         for a, b in zip(got, ref):
             exact(a, b)
@@ -59,7 +65,7 @@ def test_batch_results_do_not_depend_on_the_launch_shape(precision):
     for p in range(len(gam)):
         ext[off[p]:off[p + 1]] = oracle.init_extensives(mesh, cells, gam[p])[off[p]:off[p + 1]]
     outs = []
-    for shapes in [None] + SHAPES:
+    for shapes in [None] + shapes_for(precision):
         with richgpu.Handle(gamma=1.4, order=2, ghost_kind=0, precision=precision, device=0) as h:
             h.upload_mesh(mesh)
             h.set_problems(off, gam)
@@ -124,7 +130,8 @@ def test_invalid_shapes_are_rejected():
     mesh, cells, ext = sedov(32)
     with richgpu.Handle(gamma=5 / 3, order=2, ghost_kind=0, device=0) as h:
         h.upload_mesh(mesh)
-        for bad in ({"cfl": (48, 0)}, {"faces": (1024, 0)}, {"update": (0, 0)}, {"slopes": (64, -1)}):
+        for bad in ({"cfl": (48, 0)}, {"faces": (1024, 0)}, {"update": (0, 0)}, {"slopes": (64, -1)},
+                    {"slopes": (128, 0, 1)}, {"faces": (128, 0, 1)}):
             with pytest.raises(richgpu.RichError) as ei:
                 h.set_launch_shapes(bad)
             assert ei.value.status == 1
