@@ -99,3 +99,45 @@ class PackedMesh:
 def dptr(a):
     assert a.dtype == np.float64 and a.flags.c_contiguous
     return a.ctypes.data_as(_dp)
+
+
+# ---------------------------------------------------------------- 3D
+
+MESH3_FIELDS = ("face_cells", "face_normal", "face_area", "volume", "width", "cell_face_offset", "cell_faces")
+_DTYPES3 = {"face_cells": np.int32, "face_normal": np.float64, "face_area": np.float64,
+            "volume": np.float64, "width": np.float64, "cell_face_offset": np.int32,
+            "cell_faces": np.int32}
+
+
+class RgMesh3DView(C.Structure):
+    _fields_ = [("n_cells", C.c_int32), ("n_faces", C.c_int32), ("face_cells", _ip), ("face_normal", _dp),
+                ("face_area", _dp), ("volume", _dp), ("width", _dp), ("cell_face_offset", _ip),
+                ("cell_faces", _ip)]
+
+
+class PackedMesh3D:
+    """Packed 3D tessellation: numpy arrays laid out as rg_mesh3d_view describes."""
+
+    def __init__(self, **arrays):
+        for k in MESH3_FIELDS:
+            setattr(self, k, np.ascontiguousarray(arrays[k], dtype=_DTYPES3[k]))
+        self.n_cells = int(self.volume.shape[0])
+        self.n_faces = int(self.face_cells.shape[0])
+        self._view = None
+
+    @classmethod
+    def from_npz(cls, z, prefix="mesh3_"):
+        names = {"face_normal": "normal", "face_area": "area"}
+        return cls(**{k: z[prefix + names.get(k, k)] for k in MESH3_FIELDS})
+
+    def view(self):
+        if self._view is None:
+            def p(a, t):
+                return a.ctypes.data_as(t)
+            self._view = RgMesh3DView(self.n_cells, self.n_faces, p(self.face_cells, _ip), p(self.face_normal, _dp),
+                                      p(self.face_area, _dp), p(self.volume, _dp), p(self.width, _dp),
+                                      p(self.cell_face_offset, _ip), p(self.cell_faces, _ip))
+        return self._view
+
+    def nbytes(self):
+        return sum(getattr(self, k).nbytes for k in MESH3_FIELDS)

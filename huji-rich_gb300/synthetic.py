@@ -365,3 +365,110 @@ def riemann_problem(p, seed=11, min_cells=1024, max_cells=65536, jitter=1e-3):
     c[:, 3] = np.where(left, vel[0, 1], vel[1, 1])
     gamma = 1.4 if rng.uniform() < 0.5 else 5.0 / 3.0
     return m, c, gamma
+
+
+# ---------------------------------------------------------------- 3D
+
+def cube_grid(nx, ny, nz, lo=(0.0, 0.0, 0.0), hi=(1.0, 0.8, 0.6)):
+    """Packed CubeGrid (CubeGrid.cpp:23-160): faces normal to z, then y, then
+    x, in the reference's index order; boundary faces have -1 outside; cell
+    faces in ascending face order; Normal (CubeGrid.cpp:280-287) = (0,0,dz),
+    (0,dy,0), (dx,0,0); Face::GetArea (Face.cpp:24-30) of the four vertices
+    (two triangles, each 0.5*|(v1-v0) x (v2-v0)|), the vertices formed as
+    CubeGrid forms them.  Cell index = i*ny*nz + j*nz + k for the cell at
+    (x index i, y index j, z index k)."""
+    from meshview import PackedMesh3D
+    lo = np.asarray(lo, dtype=np.float64)
+    hi = np.asarray(hi, dtype=np.float64)
+    dx, dy, dz = (hi[0] - lo[0]) / nx, (hi[1] - lo[1]) / ny, (hi[2] - lo[2]) / nz
+
+    def cell(i, j, k):
+        return i * ny * nz + j * nz + k
+
+    def area(vs):
+        # vs: (..., 4, 3) vertices; 0.5*abs(Cross(v[i+1]-v0, v[i+2]-v0)) summed over i = 0, 1
+        res = np.zeros(vs.shape[:-2])
+        for t in range(2):
+            a = vs[..., t + 1, :] - vs[..., 0, :]
+            b = vs[..., t + 2, :] - vs[..., 0, :]
+            cx = a[..., 1] * b[..., 2] - a[..., 2] * b[..., 1]
+            cy = a[..., 2] * b[..., 0] - a[..., 0] * b[..., 2]
+            cz = a[..., 0] * b[..., 1] - a[..., 1] * b[..., 0]
+            res = res + 0.5 * np.sqrt(cx * cx + cy * cy + cz * cz)
+        return res
+
+    faces, areas, normals = [], [], []
+    # z faces: index i*nx + j + k*ny*nx for k in 0..nz, i (y) in 0..ny-1, j (x) in 0..nx-1
+    side = [lo, lo + [dx, 0, 0], lo + [dx, dy, 0], lo + [0, dy, 0]]
+    k, i, j = np.meshgrid(np.arange(nz + 1), np.arange(ny), np.arange(nx), indexing="ij")
+    k, i, j = k.ravel(), i.ravel(), j.ravel()
+    # side + Vector3D(dx*j, 0, dz*k) + Vector3D(0, dy*i, 0)
+    vz = np.asarray(side, dtype=np.float64)[None] + np.stack([dx * j, 0 * j, dz * k], -1)[:, None, :].astype(np.float64)
+    vz = vz + np.stack([0 * i, dy * i, 0 * i], -1)[:, None, :].astype(np.float64)
+    fz = np.stack([np.where(k == 0, -1, cell(j, i, k - 1)), np.where(k == nz, -1, cell(j, i, k))], -1)
+    faces.append(fz)
+    areas.append(area(vz))
+    normals.append(np.tile([0.0, 0.0, dz], (len(fz), 1)))
+    # y faces: index i*nx*nz + k + j*nz + nx*(nz+1)*ny for k in 0..nz-1, i (y) in 0..ny, j (x) in 0..nx-1
+    side = [lo, lo + [dx, 0, 0], lo + [dx, 0, dz], lo + [0, 0, dz]]
+    k, i, j = np.meshgrid(np.arange(nz), np.arange(ny + 1), np.arange(nx), indexing="ij")
+    idx = (i * nx * nz + k + j * nz).ravel()
+    k, i, j = k.ravel(), i.ravel(), j.ravel()
+    # side + Vector3D(dx*j, dy*i, 0) + Vector3D(0, 0, dz*k)
+    vy = np.asarray(side, dtype=np.float64)[None] + np.stack([dx * j, dy * i, 0 * j], -1)[:, None, :].astype(np.float64)
+    vy = vy + np.stack([0 * k, 0 * k, dz * k], -1)[:, None, :].astype(np.float64)
+    fy = np.stack([np.where(i == 0, -1, cell(j, i - 1, k)), np.where(i == ny, -1, cell(j, i, k))], -1)
+    order = np.argsort(idx, kind="stable")
+    faces.append(fy[order])
+    areas.append(area(vy)[order])
+    normals.append(np.tile([0.0, dy, 0.0], (len(fy), 1)))
+    # x faces: index i*nz + j*ny*nz + k + offsets for k in 0..nz-1, i (y) in 0..ny-1, j (x) in 0..nx
+    side = [lo, lo + [0, dy, 0], lo + [0, dy, dz], lo + [0, 0, dz]]
+    k, i, j = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx + 1), indexing="ij")
+    idx = (i * nz + j * ny * nz + k).ravel()
+    k, i, j = k.ravel(), i.ravel(), j.ravel()
+    # side + Vector3D(0, dy*i, 0) + Vector3D(dx*j, 0, dz*k)
+    vx = np.asarray(side, dtype=np.float64)[None] + np.stack([0 * i, dy * i, 0 * i], -1)[:, None, :].astype(np.float64)
+    vx = vx + np.stack([dx * j, 0 * j, dz * k], -1)[:, None, :].astype(np.float64)
+    fx = np.stack([np.where(j == 0, -1, cell(j - 1, i, k)), np.where(j == nx, -1, cell(j, i, k))], -1)
+    order = np.argsort(idx, kind="stable")
+    faces.append(fx[order])
+    areas.append(area(vx)[order])
+    normals.append(np.tile([dx, 0.0, 0.0], (len(fx), 1)))
+    face_cells = np.concatenate(faces).astype(np.int32)
+    n = nx * ny * nz
+    # cell -> faces in ascending face order
+    owner = np.concatenate([face_cells[:, 0], face_cells[:, 1]])
+    fid = np.concatenate([np.arange(len(face_cells))] * 2)
+    keep = owner >= 0
+    owner, fid = owner[keep], fid[keep]
+    order = np.lexsort((fid, owner))
+    counts = np.bincount(owner, minlength=n)
+    off = np.concatenate([[0], np.cumsum(counts)]).astype(np.int32)
+    return PackedMesh3D(face_cells=face_cells, face_normal=np.concatenate(normals), face_area=np.concatenate(areas),
+                        volume=np.full(n, dx * dy * dz), width=np.full(n, min(min(dx, dy), dz)),
+                        cell_face_offset=off, cell_faces=fid[order].astype(np.int32))
+
+
+def cube_centres(nx, ny, nz, lo=(0.0, 0.0, 0.0), hi=(1.0, 0.8, 0.6)):
+    """CubeGrid mesh points (CubeGrid.cpp:138-151), in cell order."""
+    lo = np.asarray(lo, dtype=np.float64)
+    hi = np.asarray(hi, dtype=np.float64)
+    dx, dy, dz = (hi[0] - lo[0]) / nx, (hi[1] - lo[1]) / ny, (hi[2] - lo[2]) / nz
+    i, j, k = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    p = np.stack([i * dx + 0.5 * dx, j * dy + 0.5 * dy, k * dz + 0.5 * dz], -1).reshape(-1, 3)
+    return lo + p
+
+
+def cube_blast_cells(nx, ny, nz, lo=(0.0, 0.0, 0.0), hi=(1.0, 0.8, 0.6), seed=3, gamma=5 / 3):
+    """A 3D workload state: ambient gas (rho 1, p 1e-2) with a hot sphere
+    (p 10) at the box centre and a seeded small random velocity field."""
+    x = cube_centres(nx, ny, nz, lo, hi)
+    c = np.asarray(lo) + 0.5 * (np.asarray(hi) - np.asarray(lo))
+    r = np.sqrt(((x - c) ** 2).sum(1))
+    rng = np.random.default_rng(seed)
+    cells = np.zeros((len(x), 5))
+    cells[:, 0] = 1.0
+    cells[:, 1] = np.where(r < 0.1, 10.0, 1e-2)
+    cells[:, 2:] = rng.uniform(-0.05, 0.05, (len(x), 3))
+    return cells

@@ -142,6 +142,32 @@ typedef struct rg_mesh_view {
   const int32_t* cell_faces;
 } rg_mesh_view;
 
+/*
+ * A 3D tessellation packed for the first-order 3D path (HDSim3D with
+ * FirstOrderHydroFlux, hdsim_3d.cpp:63-76 update_extensive,
+ * DefaultCellUpdater, CourantFriedrichsLewy).  Faces with a neighbour outside
+ * the domain (CubeGrid's boundary faces, Tessellation3D::BoundaryFace) carry
+ * -1 for it and are rigid walls.
+ *
+ *   face_cells       n_faces*2  Face::neighbors (first, second), -1 outside
+ *   face_normal      n_faces*3  Tessellation3D::Normal (normalised by the library)
+ *   face_area        n_faces    Face::GetArea
+ *   volume, width    n_cells    Tessellation3D::GetVolume, GetWidth
+ *   cell_face_offset n_cells+1, cell_faces: Tessellation3D::GetCellFaces,
+ *                    ascending face ids
+ */
+typedef struct rg_mesh3d_view {
+  int32_t n_cells;
+  int32_t n_faces;
+  const int32_t* face_cells;
+  const double* face_normal;
+  const double* face_area;
+  const double* volume;
+  const double* width;
+  const int32_t* cell_face_offset;
+  const int32_t* cell_faces;
+} rg_mesh3d_view;
+
 /* Device addresses of the handle's state, for callers that keep data on the
  * GPU (all valid until the next rg_upload_mesh or rg_destroy). */
 typedef struct rg_device_view {

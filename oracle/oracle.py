@@ -170,3 +170,76 @@ def run_fixed_dt(mesh, cells, gamma, steps, dt, lp=None):
         ext = extensive_update(mesh, fl, dt, ext)
         cells = cell_update(mesh, ext, gamma)
     return cells, ext
+
+
+# ---------------------------------------------------------------- 3D first-order path
+
+def _setup3():
+    L = lib()
+    if getattr(L, "_ro3", False):
+        return L
+    from meshview import RgMesh3DView
+    m3 = C.POINTER(RgMesh3DView)
+    dp = C.POINTER(C.c_double)
+    L.ro3_init_extensives.argtypes = [m3, dp, C.c_double, dp]
+    L.ro3_init_extensives.restype = None
+    L.ro3_cfl.argtypes = [m3, dp, C.c_double, C.c_double]
+    L.ro3_cfl.restype = C.c_double
+    L.ro3_flux.argtypes = [m3, dp, dp, C.c_double, dp, C.POINTER(RoError)]
+    L.ro3_extensive_update.argtypes = [m3, dp, C.c_double, dp]
+    L.ro3_extensive_update.restype = None
+    L.ro3_cell_update.argtypes = [m3, dp, C.c_double, dp, C.POINTER(RoError)]
+    L.ro3_step.argtypes = [m3, dp, dp, C.c_double, C.c_double, dp, C.POINTER(RoError)]
+    L._ro3 = True
+    return L
+
+
+def init_extensives3(mesh, cells, gamma):
+    out = np.zeros((mesh.n_cells, 5))
+    cells = _f64(cells)
+    _setup3().ro3_init_extensives(C.byref(mesh.view()), _d(cells), gamma, _d(out))
+    return out
+
+
+def cfl3(mesh, cells, gamma, cfl_number=0.3):
+    cells = _f64(cells)
+    return _setup3().ro3_cfl(C.byref(mesh.view()), _d(cells), gamma, cfl_number)
+
+
+def flux3(mesh, cells, gamma, face_velocity=None):
+    out = np.zeros((mesh.n_faces, 5))
+    err = RoError()
+    cells = _f64(cells)
+    fv = None if face_velocity is None else _d(_f64(face_velocity))
+    _check(_setup3().ro3_flux(C.byref(mesh.view()), _d(cells), fv, gamma, _d(out), C.byref(err)), err)
+    return out
+
+
+def extensive_update3(mesh, fluxes, dt, ext):
+    ext = _f64(ext).copy()
+    fluxes = _f64(fluxes)
+    _setup3().ro3_extensive_update(C.byref(mesh.view()), _d(fluxes), dt, _d(ext))
+    return ext
+
+
+def cell_update3(mesh, ext, gamma):
+    out = np.zeros((mesh.n_cells, 5))
+    err = RoError()
+    ext = _f64(ext)
+    _check(_setup3().ro3_cell_update(C.byref(mesh.view()), _d(ext), gamma, _d(out), C.byref(err)), err)
+    return out
+
+
+def run3(mesh, cells, ext, gamma, steps, cfl_number=0.3):
+    """HDSim3D::timeAdvance steps on a fixed mesh; returns (cells, ext, dts)."""
+    cells = _f64(cells).copy()
+    ext = _f64(ext).copy()
+    L = _setup3()
+    dts = []
+    for _ in range(steps):
+        dt = C.c_double()
+        err = RoError()
+        _check(L.ro3_step(C.byref(mesh.view()), _d(cells), _d(ext), gamma, cfl_number, C.byref(dt), C.byref(err)),
+               err)
+        dts.append(dt.value)
+    return cells, ext, np.array(dts)

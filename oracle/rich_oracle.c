@@ -723,3 +723,198 @@ int ro_step_heun(const rg_mesh_view* m, double* cells, double* ext, const double
   if (dt_out) *dt_out = dt;
   return st;
 }
+
+/* ========================================================================
+ * 3D first-order path (HDSim3D on a CubeGrid-like packed mesh)
+ * ======================================================================== */
+
+typedef struct { double x, y, z; } v3;
+typedef struct { double d, p; v3 v; } cc3;
+typedef struct { double m; v3 mom; double en; } cons3;
+
+/* Vector3D.cpp: abs, ScalarProd, operator*(double, Vector3D) (v.x*d), /, -, + */
+static double v3abs(v3 v) { return sqrt(v.x * v.x + v.y * v.y + v.z * v.z); }
+static double v3dot(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static v3 v3scale(double d, v3 v) { v3 r = {v.x * d, v.y * d, v.z * d}; return r; }
+static v3 v3div(v3 v, double d) { v3 r = {v.x / d, v.y / d, v.z / d}; return r; }
+static v3 v3sub(v3 a, v3 b) { v3 r = {a.x - b.x, a.y - b.y, a.z - b.z}; return r; }
+static v3 v3add(v3 a, v3 b) { v3 r = {a.x + b.x, a.y + b.y, a.z + b.z}; return r; }
+
+static cc3 cell3(const double* c, int i) {
+  cc3 r = {c[5 * i], c[5 * i + 1], {c[5 * i + 2], c[5 * i + 3], c[5 * i + 4]}};
+  return r;
+}
+static v3 normal3(const rg_mesh3d_view* m, int f) {
+  v3 n = {m->face_normal[3 * f], m->face_normal[3 * f + 1], m->face_normal[3 * f + 2]};
+  return v3div(n, v3abs(n)); /* FirstOrderHydroFlux.cpp:11-14 normalize */
+}
+
+/* FirstOrderHydroFlux.cpp:32-40 calc_primitive: (d, p, (v.n, |v - (v.n)n|), e, c) */
+static prim prim3(double g, cc3 c, v3 n) {
+  const double sp = v3dot(c.v, n);
+  prim r;
+  r.d = c.d;
+  r.p = c.p;
+  r.vx = sp;
+  r.vy = v3abs(v3sub(c.v, v3scale(sp, n)));
+  r.e = dp2e(g, c.d, c.p);
+  r.c = dp2c(g, c.d, c.p);
+  return r;
+}
+
+/* FirstOrderHydroFlux.cpp:16-30 GetParallel */
+static v3 parallel3(v3 vel, v3 n) {
+  v3 par = v3sub(vel, v3scale(v3dot(vel, n), n));
+  const double p = v3abs(par);
+  const double v = v3abs(vel);
+  if (1e-9 > fabs(v - 0)) return par;
+  if (p < 1e-8 * v)
+    par = v3div(par, v);
+  else
+    par = v3div(par, p);
+  return par;
+}
+
+/* Vector3D.cpp:203-206 Reflect: v - 2*ScalarProd(v,n)*n/pow(abs(n),2) (pow(x,2) folds to x*x) */
+static v3 reflect3(v3 v, v3 n) {
+  const double s = 2 * v3dot(v, n);
+  const double a = v3abs(n);
+  return v3sub(v, v3div(v3scale(s, n), a * a));
+}
+
+static cons3 rebuild(cons sol, v3 n, v3 par) {
+  cons3 r;
+  r.m = sol.m;
+  r.mom = v3add(v3scale(sol.mx, n), v3scale(sol.my, par));
+  r.en = sol.en;
+  return r;
+}
+
+/* FirstOrderHydroFlux.cpp:98-114 operator(), :42-66 CalcRigidWall, :68-88 CalcSingleFluxInBulk */
+int ro3_flux(const rg_mesh3d_view* m, const double* cells, const double* fvel, double gamma, double* fluxes,
+             ro_error* err) {
+  for (int f = 0; f < m->n_faces; ++f) {
+    const int a = m->face_cells[2 * f], b = m->face_cells[2 * f + 1];
+    const v3 n = normal3(m, f);
+    cons sol;
+    cons3 res;
+    if (a < 0 || b < 0) {
+      const int real_first = a >= 0;
+      const cc3 real = cell3(cells, real_first ? a : b);
+      const prim preal = prim3(gamma, real, n);
+      const v3 par = parallel3(real.v, n);
+      cc3 other = real;
+      other.v = reflect3(real.v, n);
+      const prim pghost = prim3(gamma, other, n);
+      const double fv = 0;
+      const int st = real_first ? hllc(preal, pghost, fv, &sol, f, err) : hllc(pghost, preal, fv, &sol, f, err);
+      if (st) return st;
+      res = rebuild(sol, n, par);
+    } else {
+      v3 w = {0, 0, 0};
+      if (fvel) {
+        w.x = fvel[3 * f];
+        w.y = fvel[3 * f + 1];
+        w.z = fvel[3 * f + 2];
+      }
+      const double fv = v3dot(w, n);
+      const cc3 ca = cell3(cells, a), cb = cell3(cells, b);
+      const int st = hllc(prim3(gamma, ca, n), prim3(gamma, cb, n), fv, &sol, f, err);
+      if (st) return st;
+      const cc3 donor = sol.m > 0 ? ca : cb;
+      res = rebuild(sol, n, parallel3(donor.v, n));
+    }
+    double* o = fluxes + 5 * f;
+    o[0] = res.m;
+    o[1] = res.mom.x;
+    o[2] = res.mom.y;
+    o[3] = res.mom.z;
+    o[4] = res.en;
+  }
+  return 0;
+}
+
+/* hdsim_3d.cpp:63-76 update_extensive: delta = dt*area*flux per face, in face order */
+void ro3_extensive_update(const rg_mesh3d_view* m, const double* fluxes, double dt, double* ext) {
+  for (int f = 0; f < m->n_faces; ++f) {
+    const double s = dt * m->face_area[f];
+    const double* fl = fluxes + 5 * f;
+    double d[5];
+    for (int q = 0; q < 5; ++q) d[q] = s * fl[q];
+    const int a = m->face_cells[2 * f], b = m->face_cells[2 * f + 1];
+    if (a >= 0)
+      for (int q = 0; q < 5; ++q) ext[5 * a + q] -= d[q];
+    if (b >= 0)
+      for (int q = 0; q < 5; ++q) ext[5 * b + q] += d[q];
+  }
+}
+
+/* hdsim_3d.cpp:78-104 AllCellsUpdater (extensive/volume) with DefaultCellUpdater
+ * (default_cell_updater.cpp:5-14) and IdealGas::de2p (ideal_gas.cpp:18-23) */
+int ro3_cell_update(const rg_mesh3d_view* m, const double* ext, double gamma, double* cells, ro_error* err) {
+  for (int i = 0; i < m->n_cells; ++i) {
+    const double V = m->volume[i];
+    const double* e = ext + 5 * i;
+    const double mass = e[0] / V;
+    const v3 mom = {e[1] / V, e[2] / V, e[3] / V};
+    const double en = e[4] / V;
+    const double density = mass;
+    const v3 vel = v3div(mom, density);
+    const double thermal = en - 0.5 * density * v3dot(vel, vel);
+    const double eint = thermal / density;
+    if (eint < 0) {
+      set_err(err, RG_ERR_NEGATIVE_ENERGY, 5, i, eint);
+      return RG_ERR_NEGATIVE_ENERGY;
+    }
+    double* c = cells + 5 * i;
+    c[0] = density;
+    c[1] = (gamma - 1) * eint * density;
+    c[2] = vel.x;
+    c[3] = vel.y;
+    c[4] = vel.z;
+  }
+  return 0;
+}
+
+/* extensive_generator.cpp:3-28: volume * (d, d*v, d*(0.5*v.v + e)) */
+void ro3_init_extensives(const rg_mesh3d_view* m, const double* cells, double gamma, double* ext) {
+  for (int i = 0; i < m->n_cells; ++i) {
+    const cc3 c = cell3(cells, i);
+    const double V = m->volume[i];
+    const v3 mom = v3scale(c.d, c.v);
+    const double en = c.d * (0.5 * v3dot(c.v, c.v) + dp2e(gamma, c.d, c.p));
+    double* e = ext + 5 * i;
+    e[0] = V * c.d;
+    e[1] = mom.x * V;
+    e[2] = mom.y * V;
+    e[3] = mom.z * V;
+    e[4] = V * en;
+  }
+}
+
+/* CourantFriedrichsLewy.cpp:23-46: cfl * min width/(|v| + c) */
+double ro3_cfl(const rg_mesh3d_view* m, const double* cells, double gamma, double cfl) {
+  double best = 0;
+  for (int i = 0; i < m->n_cells; ++i) {
+    const cc3 c = cell3(cells, i);
+    const double b = m->width[i] / (v3abs(c.v) + dp2c(gamma, c.d, c.p));
+    best = i == 0 ? b : smin(best, b);
+  }
+  return cfl * best;
+}
+
+int ro3_step(const rg_mesh3d_view* m, double* cells, double* ext, double gamma, double cfl, double* dt_out,
+             ro_error* err) {
+  const double dt = ro3_cfl(m, cells, gamma, cfl);
+  double* fl = (double*)malloc(sizeof(double) * 5 * (size_t)(m->n_faces > 0 ? m->n_faces : 1));
+  if (!fl) return RG_ERR_OUT_OF_MEMORY;
+  int st = ro3_flux(m, cells, NULL, gamma, fl, err);
+  if (!st) {
+    ro3_extensive_update(m, fl, dt, ext);
+    st = ro3_cell_update(m, ext, gamma, cells, err);
+  }
+  free(fl);
+  *dt_out = dt;
+  return st;
+}
+

@@ -61,6 +61,19 @@ int ro_step(const rg_mesh_view* m, double* cells, double* ext, const double* ev,
 int ro_step_heun(const rg_mesh_view* m, double* cells, double* ext, const double* ev, double gamma,
                  double cfl, int order, const ro_lgi_params* lp, double* dt_out, ro_error* err);
 
+/* 3D first-order path on the packed 3D mesh.  Cells N*5 {density, pressure,
+ * vx, vy, vz}; extensives and fluxes N*5 {mass, px, py, pz, energy}
+ * (Conserved3D order).  face_velocity: n_faces*3 or NULL (faces at rest). */
+void ro3_init_extensives(const rg_mesh3d_view* m, const double* cells, double gamma, double* ext);
+double ro3_cfl(const rg_mesh3d_view* m, const double* cells, double gamma, double cfl);
+int ro3_flux(const rg_mesh3d_view* m, const double* cells, const double* face_velocity, double gamma,
+             double* fluxes, ro_error* err);
+void ro3_extensive_update(const rg_mesh3d_view* m, const double* fluxes, double dt, double* ext);
+int ro3_cell_update(const rg_mesh3d_view* m, const double* ext, double gamma, double* cells, ro_error* err);
+/* HDSim3D::timeAdvance (hdsim_3d.cpp:133-145) on a fixed mesh */
+int ro3_step(const rg_mesh3d_view* m, double* cells, double* ext, double gamma, double cfl, double* dt_out,
+             ro_error* err);
+
 #ifdef __cplusplus
 }
 #endif

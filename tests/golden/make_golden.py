@@ -48,6 +48,17 @@ CASES = {
     "periodic_heun_o2": ("periodic", 16, 16, 2, 10, "heun"),
 }
 
+# 3D first-order path (oracle/ref/ref_dump3d.cpp), written to 3d/<name>.npz:
+# name: (ref_dump3d case, nx, ny, nz, run steps)
+CASES3D = {
+    # seeded density, pressure and velocity per cell: every HLLC branch, tangential flow
+    "cube_random": ("random", 6, 5, 4, 8),
+    # a Sod tube along x at rest
+    "cube_sod": ("sod", 24, 4, 3, 30),
+    # uniform gas with a sheared velocity field
+    "cube_shear": ("shear", 8, 8, 6, 15),
+}
+
 
 def main():
     ap = argparse.ArgumentParser()
@@ -57,10 +68,22 @@ def main():
     subprocess.check_call(["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle", "ref"),
                            "REF=" + a.ref])
     exe = os.path.join(ROOT, "oracle", "_ref", "ref_dump")
-    for name in a.cases or sorted(CASES):
+    scratch = os.path.join(ROOT, "oracle", "_ref")
+    exe3 = os.path.join(ROOT, "oracle", "_ref", "ref_dump3d")
+    os.makedirs(os.path.join(HERE, "3d"), exist_ok=True)
+    for name in [c for c in (a.cases or sorted(CASES3D)) if c in CASES3D]:
+        case, nx, ny, nz, run = CASES3D[name]
+        with tempfile.TemporaryDirectory(dir=scratch) as d:
+            subprocess.check_call([exe3, case, d, str(nx), str(ny), str(nz), str(run)])
+            arrays = {os.path.basename(f)[:-4]: np.load(f) for f in glob.glob(os.path.join(d, "*.npy"))}
+        arrays["case_params"] = np.array([nx, ny, nz, run], dtype=np.int64)
+        out = os.path.join(HERE, "3d", name + ".npz")
+        np.savez_compressed(out, **arrays)
+        print(f"{name}: {len(arrays)} arrays, {os.path.getsize(out) / 1024:.0f} KiB", file=sys.stderr)
+    for name in [c for c in (a.cases or sorted(CASES)) if c in CASES]:
         case, nx, ny, warm, run = CASES[name][:5]
         scheme = CASES[name][5] if len(CASES[name]) > 5 else "first"
-        with tempfile.TemporaryDirectory() as d:
+        with tempfile.TemporaryDirectory(dir=scratch) as d:
             subprocess.check_call([exe, case, d, str(nx), str(ny), str(warm), str(run)] +
                                   (["heun"] if scheme == "heun" else []))
             arrays = {os.path.basename(f)[:-4]: np.load(f) for f in glob.glob(os.path.join(d, "*.npy"))}
