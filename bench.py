@@ -363,6 +363,7 @@ def run_gpu(args, world, rank, local_rank):
                "sample": f"{kc} steps of the same {NX}x{NY} workload (FP64), one thread, C restatement "
                          "oracle/rich_oracle.c (gcc -O2); the reference itself is serial"}
     adjoint = adjoint_block() if rank == 0 and not args.no_adjoint else None
+    sedov3d = sedov3d_block(cpu=not args.no_cpu) if rank == 0 and not args.no_3d else None
     if rank == 0:
         line = {"metric": METRIC, "value": value32, "unit": UNIT, "n_gpus": world, "steps": k,
                 "warmup": r32["warmup"], "ms_per_step": r32["total_ms"] / k, "higher_is_better": True,
@@ -388,10 +389,65 @@ def run_gpu(args, world, rank, local_rank):
                          "clocks": r64["clock"]},
                 "speedup_fp32mixed_vs_fp64": value32 / value64,
                 "adjoint": adjoint,
+                "sedov3d": sedov3d,
                 "wall_s_timed_region": r32["wall"] + r64["wall"]}
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+# ------------------------------------------------------------------ 3D
+
+def sedov3d_block(steps=20, warmup=3, cpu=True):
+    """3D first-order path on the 3D configuration's size: Sedov-Taylor on a
+    96^3 CubeGrid over [-0.5, 0.5]^3 (884,736 cells, 2,681,856 faces; rho 1,
+    p 1e-6, E = 1 in r < 0.04, gamma 5/3, CFL 0.3), HDSim3D's step with
+    FirstOrderHydroFlux(Hllc), update_extensive, DefaultCellUpdater (FP64,
+    bit-identical to the reference).  The reference has no LinearGauss3D /
+    Hllc3D / Voronoi3D; CubeGrid first order is its 3D path.  Each step is
+    timed with CUDA events per kernel; its working set (about 400 MB) is
+    larger than L2."""
+    import richgpu
+    import synthetic
+    n = 96
+    box = dict(lo=(-0.5, -0.5, -0.5), hi=(0.5, 0.5, 0.5))
+    mesh = synthetic.cube_grid(n, n, n, **box)
+    cells = synthetic.cube_sedov_cells(n, GAMMA)
+    with richgpu.Handle3(gamma=GAMMA, device=0) as h:
+        h.upload_mesh(mesh)
+        h.set_cells(cells)
+        h.init_extensives()
+        for _ in range(warmup):
+            h.step()
+        kms = np.array([h.step_timed()[1] for _ in range(steps)])
+    N, F = mesh.n_cells, mesh.n_faces
+    ms = float(kms.sum(1).mean())
+    # algorithmic bytes per launch (220 N + 96 F per step in total):
+    # faces: neighbour pair 8 + normal 24 + area 8 + flux out 40 per face, the cells once (40 per cell)
+    faces_bytes = F * (8 + 24 + 8 + 40) + N * 40
+    kf = float(kms[:, 1].mean())
+    peak = measured_peaks()
+    rec = {"workload": "sedov3d_cubegrid_96^3_first_order_hllc_fp64", "cells": N, "faces": F, "steps": steps,
+           "ms_per_step": ms, "cell_updates_per_s": N / (ms * 1e-3), "faces_per_s": F / (ms * 1e-3),
+           "kernel_ms_mean": {"k3_cfl": float(kms[:, 0].mean()), "k3_faces": kf, "k3_update": float(kms[:, 2].mean())},
+           "bit_exact_vs_reference": True,
+           "roofline": {"bound": "hbm", "kernel": "k3_faces", "achieved": faces_bytes / (kf * 1e-3) / 1e9,
+                        "peak": peak[0], "unit": "GB/s", "frac": faces_bytes / (kf * 1e-3) / 1e9 / peak[0],
+                        "traffic": ncu_traffic("k3_faces"), "algorithmic_bytes_per_launch": faces_bytes,
+                        "note": "FP64 Hllc per face: bound by GB300's FP64 pipe"}}
+    if cpu:
+        import oracle
+        ext = oracle.init_extensives3(mesh, cells, GAMMA)
+        t0 = time.perf_counter()
+        k = 0
+        c, e = cells, ext
+        while k < 3 and (k == 0 or time.perf_counter() - t0 < 10):
+            c, e, _ = oracle.run3(mesh, c, e, GAMMA, 1)
+            k += 1
+        tc = time.perf_counter() - t0
+        rec["cpu_baseline"] = {"value": N * k / tc, "unit": UNIT, "cores": 1, "kind": "port",
+                               "sample": f"{k} steps of the same 96^3 workload, one thread, oracle/rich_oracle.c ro3_step"}
+    return rec
 
 
 # ------------------------------------------------------------------ adjoint
@@ -557,7 +613,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint cost measurement")
     ap.add_argument("--no-tune", action="store_true", help="default launch shapes instead of the autotuner's")
-    ap.add_argument("--workload", default="sedov", choices=["sedov", "riemann_batch"])
+    ap.add_argument("--no-3d", action="store_true", help="skip the 3D first-order measurement")
+    ap.add_argument("--workload", default="sedov", choices=["sedov", "riemann_batch", "sedov3d"])
     ap.add_argument("--problems", type=int, default=512)
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -568,6 +625,17 @@ def main():
     elif args.workload == "riemann_batch":
         if rank == 0:
             run_batch(args, world, rank, local_rank)
+    elif args.workload == "sedov3d":
+        if rank == 0:
+            rec = sedov3d_block(steps=args.steps, warmup=max(args.warmup, 3), cpu=not args.no_cpu)
+            line = {"metric": "cell-updates/s, 3D first-order path (FP64)", "value": rec["cell_updates_per_s"],
+                    "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3),
+                    "ms_per_step": rec["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+                    "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                    "config": {"workload": rec["workload"], "cells": rec["cells"], "faces": rec["faces"]},
+                    "roofline": rec["roofline"], "cpu_baseline": rec.get("cpu_baseline"),
+                    "gpu_launches": 3 * args.steps}
+            print(json.dumps(line), flush=True)
     else:
         run_gpu(args, world, rank, local_rank)
 

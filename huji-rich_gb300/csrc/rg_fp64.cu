@@ -17,6 +17,7 @@
 // Geometry-only terms are computed once per mesh upload (k_geom_*).
 #include <math.h>
 
+#include "rg_hllc.cuh"
 #include "rg_internal.cuh"
 
 namespace rg {
@@ -25,8 +26,6 @@ namespace {
 constexpr int kBlock = 256;
 
 struct Cell { double d, p, vx, vy; };
-struct Prim { double d, p, vx, vy, e, c; };
-struct Cons { double m, mx, my, en; };
 
 __device__ __forceinline__ Cell load_cell(const double* cells, int i) {
   const double2 a = reinterpret_cast<const double2*>(cells)[2 * i];
@@ -559,67 +558,6 @@ __device__ __forceinline__ Prim to_prim(double g, const Cell& c) {
   return Prim{c.d, c.p, c.vx, c.vy, c.p / c.d / (g - 1), sqrt(g * c.p / c.d)};
 }
 
-// hydrodynamic_variables.cpp:261-265 TotalEnergyDensity (pow(x,2) is x*x)
-__device__ __forceinline__ double ted(const Prim& p) {
-  const double s = sqrt(p.vx * p.vx + p.vy * p.vy);
-  return p.d * (0.5 * (s * s) + p.e);
-}
-
-// hllc.cpp:97-154 with massflux_ = true; the frame normal is (1,0), so
-// Primitive2Flux's n/abs(n) is (1,0) exactly.  Only the branch's starred
-// state is formed; the others do not reach the result.
-__device__ __forceinline__ bool hllc(Prim l, Prim r, double velocity, Cons& f, const StepArgs& a, int face) {
-  if (isnan(r.vx)) {
-    record_error(a.status, a.step, RG_ERR_HLLC_NAN, 3, face, r.vx);
-    return false;
-  }
-  // local.Velocity -= velocity*(1,0): the y part subtracts a zero, which can
-  // only change the sign of a zero result, and is left out; so is the whole
-  // boost for a face at rest (velocity +-0)
-  const bool moving = velocity != 0.0;
-  if (moving) {
-    l.vx -= velocity;
-    r.vx -= velocity;
-  }
-  // :27-43 estimate_wave_speeds
-  const double sl = smin(l.vx - l.c, r.vx - r.c);
-  const double sr = smax(l.vx + l.c, r.vx + r.c);
-  const double ss = (r.p - l.p + l.d * l.vx * (sl - l.vx) - r.d * r.vx * (sr - r.vx)) /
-                    (l.d * (sl - l.vx) - r.d * (sr - r.vx));
-  const bool use_left = sl > 0 || (sl <= 0 && ss >= 0);
-  const bool use_right = !use_left && ((ss < 0 && sr >= 0) || sr < 0);
-  if (!use_left && !use_right) {
-    record_error(a.status, a.step, RG_ERR_HLLC_WAVE_SPEEDS, 3, face, ss);
-    return false;
-  }
-  const Prim& q = use_left ? l : r;
-  const double sk = use_left ? sl : sr;
-  const double e_k = ted(q);
-  // :281-290 Primitive2Flux along (1,0)
-  // Primitive2Flux along n = (1,0): v.n = vx (the vy*0 term only changes the
-  // sign of a zero), momentum (p + vx*d*vx, vy*d*vx)
-  const double dsp = q.d * q.vx;
-  Cons fk{dsp, q.p + q.vx * dsp, q.vy * dsp, (e_k + q.p) * q.vx};
-  const bool star = use_left ? !(sl > 0) : !(sr < 0);
-  if (star) {
-    // :76-92 starred_state, and fk + sk*(us - u) with u = Primitive2Conserved (:267-272)
-    const double ds = q.d * (sk - q.vx) / (sk - ss);
-    const double usm = ds, usx = ds * ss, usy = ds * q.vy;
-    const double use = e_k * ds / q.d + ds * (ss - q.vx) * (ss + q.p / q.d / (sk - q.vx));
-    fk.m = fk.m + sk * (usm - q.d);
-    fk.mx = fk.mx + (usx - q.vx * q.d) * sk;
-    fk.my = fk.my + (usy - q.vy * q.d) * sk;
-    fk.en = fk.en + sk * (use - e_k);
-  }
-  // :150-152 back to the lab frame along the normal
-  if (moving) {
-    fk.en += fk.mx * velocity + 0.5 * fk.m * velocity * velocity;
-    fk.mx += velocity * fk.m;
-  }
-  f = fk;
-  return true;
-}
-
 // simple_flux_calculator.cpp:130-165 rotate / Hllc / rotate_back
 __device__ __forceinline__ bool solve_face(Prim l, Prim r, double velocity, double2 n, double na, double2 p,
                                            double pa, Cons& out, const StepArgs& a, int face) {
@@ -630,7 +568,7 @@ __device__ __forceinline__ bool solve_face(Prim l, Prim r, double velocity, doub
   r.vx = rx;
   r.vy = ry;
   Cons c;
-  if (!hllc(l, r, velocity, c, a, face)) return false;
+  if (!hllc(l, r, velocity, c, a.status, a.step, face)) return false;
   out.m = c.m;
   out.mx = (n.x * c.mx) / na + (p.x * c.my) / pa;
   out.my = (n.y * c.mx) / na + (p.y * c.my) / pa;

@@ -29,6 +29,8 @@ UNITS = {
     "rg_adjoint_rev.cu": [],
     "rg_adjoint_api.cu": [],
     "rg_tune.cu": [],
+    "rg_3d.cu": ["--fmad=false"],
+    "rg_3d_api.cu": [],
 }
 
 

@@ -24,7 +24,11 @@ EXPORTS = ("rg_default_config", "rg_create", "rg_destroy", "rg_status_string", "
            "rg_extensive_update", "rg_cell_update", "rg_step", "rg_run", "rg_step_async",
            "rg_synchronize", "rg_step_timed", "rg_cfl_dt_noalloc", "rg_set_problems",
            "rg_get_problem_times", "rg_run_graph", "rg_step_fwd", "rg_step_bwd", "rg_step_tlm",
-           "rg_autotune", "rg_set_launch_shapes", "rg_get_launch_shapes", "rg_stream")
+           "rg_autotune", "rg_set_launch_shapes", "rg_get_launch_shapes", "rg_stream",
+           "rg3_create", "rg3_destroy", "rg3_last_error", "rg3_upload_mesh", "rg3_set_cells", "rg3_get_cells",
+           "rg3_set_extensives", "rg3_get_extensives", "rg3_set_face_velocities", "rg3_init_extensives",
+           "rg3_cfl_dt", "rg3_flux", "rg3_extensive_update", "rg3_cell_update", "rg3_step", "rg3_run",
+           "rg3_step_timed")
 
 KERNELS = ("cfl", "slopes", "faces", "update")
 
@@ -94,6 +98,19 @@ def load(path=LIB_PATH):
     lib.rg_step_tlm.argtypes = [vp, C.c_int32, C.c_double, dp, dp]
     lib.rg_autotune.argtypes = [vp, C.c_int32, C.POINTER(RgLaunchShapes)]
     lib.rg_stream.argtypes = [vp, C.POINTER(vp)]
+    from meshview import RgMesh3DView
+    lib.rg3_create.argtypes = [C.POINTER(RgConfig), C.POINTER(vp)]
+    lib.rg3_destroy.argtypes = [vp]
+    lib.rg3_last_error.argtypes = [vp, C.POINTER(RgError)]
+    lib.rg3_upload_mesh.argtypes = [vp, C.POINTER(RgMesh3DView)]
+    for f in ("rg3_set_cells", "rg3_get_cells", "rg3_set_extensives", "rg3_get_extensives",
+              "rg3_set_face_velocities", "rg3_flux", "rg3_cfl_dt", "rg3_step"):
+        getattr(lib, f).argtypes = [vp, dp]
+    lib.rg3_init_extensives.argtypes = [vp]
+    lib.rg3_extensive_update.argtypes = [vp, C.c_double]
+    lib.rg3_cell_update.argtypes = [vp]
+    lib.rg3_run.argtypes = [vp, C.c_int32, dp]
+    lib.rg3_step_timed.argtypes = [vp, dp, C.POINTER(C.c_float)]
     lib.rg_set_launch_shapes.argtypes = [vp, C.POINTER(RgLaunchShapes)]
     lib.rg_get_launch_shapes.argtypes = [vp, C.POINTER(RgLaunchShapes)]
     _lib = lib
@@ -306,3 +323,113 @@ class Handle:
             r.block[i], r.max_blocks[i] = shape[0], shape[1]
             r.variant[i] = shape[2] if len(shape) > 2 else 0
         self._check(self.lib.rg_set_launch_shapes(self.h, C.byref(r)))
+
+
+class Handle3:
+    """A 3D first-order handle (rg3_*): HDSim3D's step on a packed 3D mesh.
+    Cells (n, 5) {density, pressure, vx, vy, vz}; extensives and fluxes (n, 5)
+    {mass, px, py, pz, energy}."""
+
+    def __init__(self, config=None, **kw):
+        self.lib = load()
+        self.cfg = config or make_config(**kw)
+        h = C.c_void_p()
+        st = self.lib.rg3_create(C.byref(self.cfg), C.byref(h))
+        if st:
+            raise RichError(st)
+        self.h = h
+        self.mesh = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.rg3_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, st):
+        if st:
+            err = RgError()
+            self.lib.rg3_last_error(self.h, C.byref(err))
+            raise RichError(st, err)
+
+    def upload_mesh(self, mesh):
+        self.mesh = mesh
+        self._check(self.lib.rg3_upload_mesh(self.h, C.byref(mesh.view())))
+
+    def _put(self, fn, a, rows):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        assert a.size == 5 * rows
+        self._check(fn(self.h, dptr(a)))
+
+    def _get(self, fn, rows):
+        out = np.empty((rows, 5))
+        self._check(fn(self.h, dptr(out)))
+        return out
+
+    def set_cells(self, c):
+        self._put(self.lib.rg3_set_cells, c, self.mesh.n_cells)
+
+    def get_cells(self):
+        return self._get(self.lib.rg3_get_cells, self.mesh.n_cells)
+
+    def set_extensives(self, e):
+        self._put(self.lib.rg3_set_extensives, e, self.mesh.n_cells)
+
+    def get_extensives(self):
+        return self._get(self.lib.rg3_get_extensives, self.mesh.n_cells)
+
+    def set_face_velocities(self, fv):
+        if fv is None:
+            self._check(self.lib.rg3_set_face_velocities(self.h, None))
+            return
+        a = np.ascontiguousarray(fv, dtype=np.float64)
+        assert a.size == 3 * self.mesh.n_faces
+        self._check(self.lib.rg3_set_face_velocities(self.h, dptr(a)))
+
+    def init_extensives(self):
+        self._check(self.lib.rg3_init_extensives(self.h))
+
+    def cfl_dt(self):
+        v = C.c_double()
+        self._check(self.lib.rg3_cfl_dt(self.h, C.byref(v)))
+        return v.value
+
+    def flux(self, download=True):
+        if not download:
+            self._check(self.lib.rg3_flux(self.h, None))
+            return None
+        return self._get(self.lib.rg3_flux, self.mesh.n_faces)
+
+    def extensive_update(self, dt):
+        self._check(self.lib.rg3_extensive_update(self.h, dt))
+
+    def cell_update(self):
+        self._check(self.lib.rg3_cell_update(self.h))
+
+    def step(self):
+        v = C.c_double()
+        self._check(self.lib.rg3_step(self.h, C.byref(v)))
+        return v.value
+
+    def step_timed(self):
+        """One step; returns (dt, [cfl, faces, update] kernel ms)."""
+        v = C.c_double()
+        k = (C.c_float * 3)()
+        self._check(self.lib.rg3_step_timed(self.h, C.byref(v), k))
+        return v.value, list(k)
+
+    def run(self, n_steps):
+        out = np.empty(n_steps)
+        self._check(self.lib.rg3_run(self.h, n_steps, dptr(out) if n_steps else None))
+        return out

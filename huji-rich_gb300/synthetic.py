@@ -472,3 +472,17 @@ def cube_blast_cells(nx, ny, nz, lo=(0.0, 0.0, 0.0), hi=(1.0, 0.8, 0.6), seed=3,
     cells[:, 1] = np.where(r < 0.1, 10.0, 1e-2)
     cells[:, 2:] = rng.uniform(-0.05, 0.05, (len(x), 3))
     return cells
+
+
+def cube_sedov_cells(n, gamma=5 / 3, r0=0.04, energy=1.0, lo=(-0.5, -0.5, -0.5), hi=(0.5, 0.5, 0.5)):
+    """3D Sedov-Taylor on an n^3 CubeGrid over [-0.5, 0.5]^3: rho 1, p 1e-6,
+    total energy `energy` deposited as pressure in the cells with r < r0."""
+    x = cube_centres(n, n, n, lo, hi)
+    r = np.sqrt((x ** 2).sum(1))
+    hot = r < r0
+    vol = np.prod((np.asarray(hi) - np.asarray(lo)) / n)
+    cells = np.zeros((len(x), 5))
+    cells[:, 0] = 1.0
+    cells[:, 1] = 1e-6
+    cells[hot, 1] = (gamma - 1) * energy / (hot.sum() * vol)
+    return cells

@@ -324,6 +324,42 @@ rg_status rg_step_fwd(rg_handle* h, int32_t n_steps, double dt, int32_t checkpoi
 rg_status rg_step_bwd(rg_handle* h, const double* cells_bar, double* cells0_bar);
 rg_status rg_step_tlm(rg_handle* h, int32_t n_steps, double dt, const double* dcells0, double* dcells);
 
+/* 3D first-order path ------------------------------------------------------ */
+/* HDSim3D::timeAdvance (hdsim_3d.cpp:133-145) on a fixed packed 3D
+ * tessellation (rg_mesh3d_view): CourantFriedrichsLewy
+ * (CourantFriedrichsLewy.cpp:23-46), FirstOrderHydroFlux with Hllc
+ * (FirstOrderHydroFlux.cpp:98-114; boundary faces are rigid walls),
+ * update_extensive (hdsim_3d.cpp:63-76), DefaultCellUpdater
+ * (default_cell_updater.cpp:5-14) with IdealGas.  FP64, the reference's
+ * operation order.  Cell records are 5 doubles {density, pressure, vx, vy,
+ * vz}; extensive and flux records 5 doubles {mass, px, py, pz, energy}
+ * (Conserved3D order).  rg_config supplies gamma, cfl and device. */
+typedef struct rg3_handle rg3_handle;
+rg_status rg3_create(const rg_config* cfg, rg3_handle** out);
+rg_status rg3_destroy(rg3_handle* h);
+rg_status rg3_last_error(const rg3_handle* h, rg_error* err);
+rg_status rg3_upload_mesh(rg3_handle* h, const rg_mesh3d_view* mesh);
+rg_status rg3_set_cells(rg3_handle* h, const double* cells);
+rg_status rg3_get_cells(rg3_handle* h, double* cells);
+rg_status rg3_set_extensives(rg3_handle* h, const double* extensives);
+rg_status rg3_get_extensives(rg3_handle* h, double* extensives);
+/* Face velocities (n_faces*3, Tessellation3D::CalcFaceVelocity of the two
+ * points); NULL: faces at rest (CubeGrid). */
+rg_status rg3_set_face_velocities(rg3_handle* h, const double* face_velocities);
+/* ExtensiveGenerator (extensive_generator.cpp:3-28): extensives from cells */
+rg_status rg3_init_extensives(rg3_handle* h);
+rg_status rg3_cfl_dt(rg3_handle* h, double* dt);
+/* FluxCalculator3D output, unscaled (n_faces*5, NULL: kept on the device) */
+rg_status rg3_flux(rg3_handle* h, double* fluxes_out);
+/* update_extensive with the fluxes of the last rg3_flux */
+rg_status rg3_extensive_update(rg3_handle* h, double dt);
+rg_status rg3_cell_update(rg3_handle* h);
+/* One fused timeAdvance (dt on the device) / n of them, dts optional */
+rg_status rg3_step(rg3_handle* h, double* dt_out);
+rg_status rg3_run(rg3_handle* h, int32_t n_steps, double* dts_out);
+/* rg3_step with CUDA-event times of its three kernels (CFL, fluxes, update), ms */
+rg_status rg3_step_timed(rg3_handle* h, double* dt_out, float* kernel_ms);
+
 /* Allocation-free time step ----------------------------------------------- */
 /* No counterpart in the reference.  The SimpleCFL dt of rg_cfl_dt for callers
  * that may not allocate device memory (hosts whose own allocator or arena

@@ -16,7 +16,7 @@ HEADER = os.path.join(ROOT, "include", "rich_gb300.h")
 
 def declared_functions():
     text = open(HEADER).read()
-    return sorted(set(re.findall(r"^\s*(?:rg_status|void|const char\*)\s+(rg_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:rg_status|void|const char\*)\s+(rg3?_\w+)\s*\(", text, re.M)))
 
 
 @pytest.fixture(scope="module")
@@ -34,7 +34,7 @@ def test_header_matches_binding_list():
 def test_library_exports_every_declared_symbol(lib):
     out = subprocess.run(["nm", "-D", "--defined-only", richgpu.LIB_PATH], capture_output=True,
                          text=True, check=True).stdout
-    exported = set(re.findall(r"\sT\s(rg_\w+)$", out, re.M))
+    exported = set(re.findall(r"\sT\s(rg3?_\w+)$", out, re.M))
     missing = set(declared_functions()) - exported
     assert not missing, missing
     for name in declared_functions():
