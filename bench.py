@@ -413,13 +413,18 @@ def sedov3d_block(steps=20, warmup=3, cpu=True):
     box = dict(lo=(-0.5, -0.5, -0.5), hi=(0.5, 0.5, 0.5))
     mesh = synthetic.cube_grid(n, n, n, **box)
     cells = synthetic.cube_sedov_cells(n, GAMMA)
-    with richgpu.Handle3(gamma=GAMMA, device=0) as h:
-        h.upload_mesh(mesh)
-        h.set_cells(cells)
-        h.init_extensives()
-        for _ in range(warmup):
-            h.step()
-        kms = np.array([h.step_timed()[1] for _ in range(steps)])
+    def timed(precision):
+        with richgpu.Handle3(gamma=GAMMA, device=0, precision=precision) as h:
+            h.upload_mesh(mesh)
+            h.set_cells(cells)
+            h.init_extensives()
+            for _ in range(warmup):
+                h.step()
+            k = np.array([h.step_timed()[1] for _ in range(steps)])
+            return k, h.get_cells()
+
+    kms, c64 = timed(0)
+    kms32, c32 = timed(1)
     N, F = mesh.n_cells, mesh.n_faces
     ms = float(kms.sum(1).mean())
     # algorithmic bytes per launch (220 N + 96 F per step in total):
@@ -435,6 +440,18 @@ def sedov3d_block(steps=20, warmup=3, cpu=True):
                         "peak": peak[0], "unit": "GB/s", "frac": faces_bytes / (kf * 1e-3) / 1e9 / peak[0],
                         "traffic": ncu_traffic("k3_faces"), "algorithmic_bytes_per_launch": faces_bytes,
                         "note": "FP64 Hllc per face: bound by GB300's FP64 pipe"}}
+    ms32 = float(kms32.sum(1).mean())
+    kf32 = float(kms32[:, 1].mean())
+    faces_bytes32 = F * (8 + 16 + 4 + 20) + N * 20  # FP32 normal, area, flux out; FP32 cells
+    rec["fp32_mixed"] = {
+        "ms_per_step": ms32, "cell_updates_per_s": N / (ms32 * 1e-3),
+        "kernel_ms_mean": {"k3m_cfl": float(kms32[:, 0].mean()), "k3m_faces": kf32,
+                           "k3m_update": float(kms32[:, 2].mean())},
+        "l1_density_vs_fp64": float(np.abs(c32[:, 0] - c64[:, 0]).sum() / np.abs(c64[:, 0]).sum()),
+        "l1_after_steps": warmup + steps,
+        "roofline": {"bound": "hbm", "kernel": "k3m_faces", "achieved": faces_bytes32 / (kf32 * 1e-3) / 1e9,
+                     "peak": peak[0], "unit": "GB/s", "frac": faces_bytes32 / (kf32 * 1e-3) / 1e9 / peak[0],
+                     "traffic": ncu_traffic("k3m_faces"), "algorithmic_bytes_per_launch": faces_bytes32}}
     if cpu:
         import oracle
         ext = oracle.init_extensives3(mesh, cells, GAMMA)
@@ -634,7 +651,8 @@ def main():
                     "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                     "config": {"workload": rec["workload"], "cells": rec["cells"], "faces": rec["faces"]},
                     "roofline": rec["roofline"], "cpu_baseline": rec.get("cpu_baseline"),
-                    "gpu_launches": 3 * args.steps}
+                    "gpu_launches": 6 * args.steps, "fp32_mixed": rec["fp32_mixed"],
+                    "kernel_ms_mean": rec["kernel_ms_mean"]}
             print(json.dumps(line), flush=True)
     else:
         run_gpu(args, world, rank, local_rank)

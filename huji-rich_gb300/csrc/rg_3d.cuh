@@ -41,6 +41,40 @@ struct Step3Args {
   int step;
 };
 
+// FP32-mixed 3D path (rg_3d_mixed.cu): FP32 primitives, unit normals,
+// areas and widths, Hllc and CFL in FP32; FP64 extensives, volumes, the
+// float-float accumulation of each cell's FP32 face fluxes and the
+// internal-energy conversion.
+struct Mixed3Args {
+  Mesh3Dev mesh;              // FP64 mesh (face pairs, CSR, volumes)
+  const int* fsign;
+  const float4* nhat32;       // unit normal (x, y, z, 0)
+  const float* area32;
+  const float* width32;
+  float gamma;
+  double cfl;
+  float4* cells32;            // {density, pressure, vx, vy}
+  float* vz32;                // vz
+  double* ext;                // 6 per cell, FP64
+  float4* flux32;             // {mass, px, py, pz} per face
+  float* fen32;               // energy flux per face
+  const float* fvel;          // 3 per face, or nullptr
+  DevStatus* status;
+  float dt32;                 // dt given by the caller (split API)
+  int dt_from_device;
+  int step;
+};
+
+cudaError_t launch3m_geometry(const Mesh3Dev& m, const dbl4* nhat, float4* nhat32, float* area32, float* width32,
+                              cudaStream_t s);
+cudaError_t launch3m_cells_to32(const double* c64, float4* c32, float* vz32, int n, cudaStream_t s);
+cudaError_t launch3m_cells_to64(const float4* c32, const float* vz32, double* c64, int n, cudaStream_t s);
+cudaError_t launch3m_flux_to64(const float4* f32, const float* fen32, double* f64, int e, cudaStream_t s);
+cudaError_t launch3m_d2f(const double* a, float* b, int n, cudaStream_t s);
+cudaError_t launch3m_cfl(const Mixed3Args& a, cudaStream_t s);
+cudaError_t launch3m_faces(const Mixed3Args& a, bool scaled, cudaStream_t s);
+cudaError_t launch3m_update(const Mixed3Args& a, bool from_unscaled, bool do_ext, bool do_cells, cudaStream_t s);
+
 cudaError_t launch3_validate(const Mesh3Dev& m, DevStatus* st, cudaStream_t s);
 cudaError_t launch3_geometry(const Mesh3Dev& m, dbl4* nhat, int* fsign, cudaStream_t s);
 cudaError_t launch3_init_extensives(const Step3Args& a, cudaStream_t s);

@@ -45,6 +45,9 @@ struct rg3_handle {
   Buf face_cells, normal, area, volume, width, cell_off, cell_faces, nhat, fsign;
   Buf cells, ext, fluxes, fvel, status_buf;
   bool fvel_set = false;
+  // FP32-mixed path (rg_config.precision == RG_FP32_MIXED)
+  bool mixed = false;
+  Buf nhat32, area32, width32, cells32, vz32, flux32, fen32, fvel32;
   DevStatus* d_status = nullptr;
   DevStatus* h_status = nullptr;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -115,6 +118,34 @@ rg::Step3Args args(rg3_handle* h) {
   return a;
 }
 
+rg::Mixed3Args margs(rg3_handle* h) {
+  const rg::Step3Args b = args(h);
+  rg::Mixed3Args a{};
+  a.mesh = b.mesh;
+  a.fsign = b.fsign;
+  a.nhat32 = static_cast<const float4*>(h->nhat32.p);
+  a.area32 = static_cast<const float*>(h->area32.p);
+  a.width32 = static_cast<const float*>(h->width32.p);
+  a.gamma = static_cast<float>(h->cfg.gamma);
+  a.cfl = h->cfg.cfl;
+  a.cells32 = static_cast<float4*>(h->cells32.p);
+  a.vz32 = static_cast<float*>(h->vz32.p);
+  a.ext = static_cast<double*>(h->ext.p);
+  a.flux32 = static_cast<float4*>(h->flux32.p);
+  a.fen32 = static_cast<float*>(h->fen32.p);
+  a.fvel = h->fvel_set ? static_cast<const float*>(h->fvel32.p) : nullptr;
+  a.status = h->d_status;
+  return a;
+}
+
+// the FP64 cell records from the FP32 ones (mixed path, before they are read)
+rg_status sync_cells64(rg3_handle* h) {
+  if (h->mixed)
+    RG3_CUDA(h, rg::launch3m_cells_to64(static_cast<const float4*>(h->cells32.p), static_cast<const float*>(h->vz32.p),
+                                        static_cast<double*>(h->cells.p), h->n, h->stream));
+  return RG_OK;
+}
+
 // 5-double host records <-> 6-double device records
 rg_status put5(rg3_handle* h, Buf& dst, const double* src, int rows) {
   RG3_CUDA(h, cudaMemcpy2DAsync(dst.p, 48, src, 40, 40, static_cast<size_t>(rows), cudaMemcpyHostToDevice,
@@ -130,15 +161,26 @@ rg_status get5(rg3_handle* h, double* dst, const Buf& src, int rows) {
 }
 
 rg_status enqueue_step(rg3_handle* h, int step, bool timed = false) {
-  rg::Step3Args a = args(h);
-  a.dt_from_device = 1;
-  a.step = step;
   if (timed) RG3_CUDA(h, cudaEventRecord(h->ev[0], h->stream));
-  RG3_CUDA(h, rg::launch3_cfl(a, h->stream));
-  if (timed) RG3_CUDA(h, cudaEventRecord(h->ev[1], h->stream));
-  RG3_CUDA(h, rg::launch3_faces(a, true, h->stream));
-  if (timed) RG3_CUDA(h, cudaEventRecord(h->ev[2], h->stream));
-  RG3_CUDA(h, rg::launch3_update(a, false, true, true, h->stream));
+  if (h->mixed) {
+    rg::Mixed3Args a = margs(h);
+    a.dt_from_device = 1;
+    a.step = step;
+    RG3_CUDA(h, rg::launch3m_cfl(a, h->stream));
+    if (timed) RG3_CUDA(h, cudaEventRecord(h->ev[1], h->stream));
+    RG3_CUDA(h, rg::launch3m_faces(a, true, h->stream));
+    if (timed) RG3_CUDA(h, cudaEventRecord(h->ev[2], h->stream));
+    RG3_CUDA(h, rg::launch3m_update(a, false, true, true, h->stream));
+  } else {
+    rg::Step3Args a = args(h);
+    a.dt_from_device = 1;
+    a.step = step;
+    RG3_CUDA(h, rg::launch3_cfl(a, h->stream));
+    if (timed) RG3_CUDA(h, cudaEventRecord(h->ev[1], h->stream));
+    RG3_CUDA(h, rg::launch3_faces(a, true, h->stream));
+    if (timed) RG3_CUDA(h, cudaEventRecord(h->ev[2], h->stream));
+    RG3_CUDA(h, rg::launch3_update(a, false, true, true, h->stream));
+  }
   if (timed) RG3_CUDA(h, cudaEventRecord(h->ev[3], h->stream));
   h->have_fluxes = false;
   return RG_OK;
@@ -157,9 +199,11 @@ rg_status rg3_create(const rg_config* cfg, rg3_handle** out) {
     cudaGetLastError();
     return RG_ERR_CUDA;
   }
+  if (cfg->precision != RG_FP64 && cfg->precision != RG_FP32_MIXED) return RG_ERR_INVALID_ARGUMENT;
   rg3_handle* h = new (std::nothrow) rg3_handle();
   if (!h) return RG_ERR_OUT_OF_MEMORY;
   h->cfg = *cfg;
+  h->mixed = cfg->precision == RG_FP32_MIXED;
   cudaError_t e;
   if ((e = cudaSetDevice(cfg->device)) != cudaSuccess || (e = cudaStreamCreateWithFlags(&h->stream,
                                                                                          cudaStreamNonBlocking)) !=
@@ -188,7 +232,8 @@ rg_status rg3_destroy(rg3_handle* h) {
   if (!h) return RG_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
   for (Buf* b : {&h->face_cells, &h->normal, &h->area, &h->volume, &h->width, &h->cell_off, &h->cell_faces,
-                 &h->nhat, &h->fsign, &h->cells, &h->ext, &h->fluxes, &h->fvel, &h->status_buf})
+                 &h->nhat, &h->fsign, &h->cells, &h->ext, &h->fluxes, &h->fvel, &h->status_buf, &h->nhat32,
+                 &h->area32, &h->width32, &h->cells32, &h->vz32, &h->flux32, &h->fen32, &h->fvel32})
     b->release();
   if (h->h_status) cudaFreeHost(h->h_status);
   for (cudaEvent_t& v : h->ev)
@@ -259,6 +304,19 @@ rg_status rg3_upload_mesh(rg3_handle* h, const rg_mesh3d_view* v) {
   }
   RG3_CUDA(h, rg::launch3_geometry(a.mesh, static_cast<rg::dbl4*>(h->nhat.p), static_cast<int*>(h->fsign.p),
                                    h->stream));
+  if (h->mixed) {
+    RG3_CUDA(h, h->nhat32.ensure(16 * E));
+    RG3_CUDA(h, h->area32.ensure(4 * E));
+    RG3_CUDA(h, h->width32.ensure(4 * N));
+    RG3_CUDA(h, h->cells32.ensure(16 * N));
+    RG3_CUDA(h, h->vz32.ensure(4 * N));
+    RG3_CUDA(h, h->flux32.ensure(16 * E));
+    RG3_CUDA(h, h->fen32.ensure(4 * E));
+    RG3_CUDA(h, h->fvel32.ensure(12 * E));
+    RG3_CUDA(h, rg::launch3m_geometry(a.mesh, static_cast<const rg::dbl4*>(h->nhat.p),
+                                      static_cast<float4*>(h->nhat32.p), static_cast<float*>(h->area32.p),
+                                      static_cast<float*>(h->width32.p), h->stream));
+  }
   RG3_CUDA(h, cudaStreamSynchronize(h->stream));
   h->have_mesh = true;
   return RG_OK;
@@ -268,6 +326,11 @@ rg_status rg3_set_cells(rg3_handle* h, const double* cells) {
   if (!h || !cells) return RG_ERR_INVALID_ARGUMENT;
   if (!h->have_mesh) return not_ready(h);
   if (rg_status st = put5(h, h->cells, cells, h->n)) return st;
+  if (h->mixed) {
+    RG3_CUDA(h, rg::launch3m_cells_to32(static_cast<const double*>(h->cells.p), static_cast<float4*>(h->cells32.p),
+                                        static_cast<float*>(h->vz32.p), h->n, h->stream));
+    RG3_CUDA(h, cudaStreamSynchronize(h->stream));
+  }
   h->have_cells = true;
   return RG_OK;
 }
@@ -275,6 +338,7 @@ rg_status rg3_set_cells(rg3_handle* h, const double* cells) {
 rg_status rg3_get_cells(rg3_handle* h, double* cells) {
   if (!h || !cells) return RG_ERR_INVALID_ARGUMENT;
   if (!h->have_cells) return not_ready(h);
+  if (rg_status st = sync_cells64(h)) return st;
   return get5(h, cells, h->cells, h->n);
 }
 
@@ -298,6 +362,9 @@ rg_status rg3_set_face_velocities(rg3_handle* h, const double* fv) {
   h->fvel_set = fv != nullptr;
   if (fv) {
     RG3_CUDA(h, cudaMemcpyAsync(h->fvel.p, fv, 24 * static_cast<size_t>(h->e), cudaMemcpyHostToDevice, h->stream));
+    if (h->mixed)
+      RG3_CUDA(h, rg::launch3m_d2f(static_cast<const double*>(h->fvel.p), static_cast<float*>(h->fvel32.p), 3 * h->e,
+                                   h->stream));
     RG3_CUDA(h, cudaStreamSynchronize(h->stream));
   }
   return RG_OK;
@@ -306,6 +373,7 @@ rg_status rg3_set_face_velocities(rg3_handle* h, const double* fv) {
 rg_status rg3_init_extensives(rg3_handle* h) {
   if (!h) return RG_ERR_INVALID_ARGUMENT;
   if (!h->have_cells) return not_ready(h);
+  if (rg_status st = sync_cells64(h)) return st;
   RG3_CUDA(h, rg::launch3_init_extensives(args(h), h->stream));
   RG3_CUDA(h, cudaStreamSynchronize(h->stream));
   h->have_ext = true;
@@ -317,7 +385,10 @@ rg_status rg3_cfl_dt(rg3_handle* h, double* dt) {
   if (!h->have_cells) return not_ready(h);
   h->last = rg_error{};
   if (rg_status st = reset(h)) return st;
-  RG3_CUDA(h, rg::launch3_cfl(args(h), h->stream));
+  if (h->mixed)
+    RG3_CUDA(h, rg::launch3m_cfl(margs(h), h->stream));
+  else
+    RG3_CUDA(h, rg::launch3_cfl(args(h), h->stream));
   return collect(h, dt);
 }
 
@@ -326,10 +397,17 @@ rg_status rg3_flux(rg3_handle* h, double* fluxes_out) {
   if (!h->have_cells) return not_ready(h);
   h->last = rg_error{};
   if (rg_status st = reset(h)) return st;
-  RG3_CUDA(h, rg::launch3_faces(args(h), false, h->stream));
+  if (h->mixed)
+    RG3_CUDA(h, rg::launch3m_faces(margs(h), false, h->stream));
+  else
+    RG3_CUDA(h, rg::launch3_faces(args(h), false, h->stream));
   if (rg_status st = collect(h)) return st;
   h->have_fluxes = true;
-  return fluxes_out ? get5(h, fluxes_out, h->fluxes, h->e) : RG_OK;
+  if (!fluxes_out) return RG_OK;
+  if (h->mixed)
+    RG3_CUDA(h, rg::launch3m_flux_to64(static_cast<const float4*>(h->flux32.p), static_cast<const float*>(h->fen32.p),
+                                       static_cast<double*>(h->fluxes.p), h->e, h->stream));
+  return get5(h, fluxes_out, h->fluxes, h->e);
 }
 
 rg_status rg3_extensive_update(rg3_handle* h, double dt) {
@@ -337,9 +415,15 @@ rg_status rg3_extensive_update(rg3_handle* h, double dt) {
   if (!h->have_ext || !h->have_fluxes) return not_ready(h);
   h->last = rg_error{};
   if (rg_status st = reset(h)) return st;
-  rg::Step3Args a = args(h);
-  a.dt_host = dt;
-  RG3_CUDA(h, rg::launch3_update(a, true, true, false, h->stream));
+  if (h->mixed) {
+    rg::Mixed3Args a = margs(h);
+    a.dt32 = static_cast<float>(dt);
+    RG3_CUDA(h, rg::launch3m_update(a, true, true, false, h->stream));
+  } else {
+    rg::Step3Args a = args(h);
+    a.dt_host = dt;
+    RG3_CUDA(h, rg::launch3_update(a, true, true, false, h->stream));
+  }
   return collect(h);
 }
 
@@ -348,7 +432,10 @@ rg_status rg3_cell_update(rg3_handle* h) {
   if (!h->have_ext) return not_ready(h);
   h->last = rg_error{};
   if (rg_status st = reset(h)) return st;
-  RG3_CUDA(h, rg::launch3_update(args(h), false, false, true, h->stream));
+  if (h->mixed)
+    RG3_CUDA(h, rg::launch3m_update(margs(h), false, false, true, h->stream));
+  else
+    RG3_CUDA(h, rg::launch3_update(args(h), false, false, true, h->stream));
   const rg_status st = collect(h);
   if (st == RG_OK) h->have_cells = true;
   return st;

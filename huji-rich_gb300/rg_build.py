@@ -31,6 +31,7 @@ UNITS = {
     "rg_tune.cu": [],
     "rg_3d.cu": ["--fmad=false"],
     "rg_3d_api.cu": [],
+    "rg_3d_mixed.cu": [],
 }
 
 

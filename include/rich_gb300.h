@@ -333,7 +333,9 @@ rg_status rg_step_tlm(rg_handle* h, int32_t n_steps, double dt, const double* dc
  * (default_cell_updater.cpp:5-14) with IdealGas.  FP64, the reference's
  * operation order.  Cell records are 5 doubles {density, pressure, vx, vy,
  * vz}; extensive and flux records 5 doubles {mass, px, py, pz, energy}
- * (Conserved3D order).  rg_config supplies gamma, cfl and device. */
+ * (Conserved3D order).  rg_config supplies gamma, cfl, device and precision:
+ * RG_FP32_MIXED runs the per-face work and the CFL bound in FP32 and keeps
+ * the extensives, volumes, the accumulation and E/m - v^2/2 in FP64. */
 typedef struct rg3_handle rg3_handle;
 rg_status rg3_create(const rg_config* cfg, rg3_handle** out);
 rg_status rg3_destroy(rg3_handle* h);

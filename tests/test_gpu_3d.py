@@ -123,3 +123,61 @@ def test_invalid_mesh_is_rejected():
         with pytest.raises(richgpu.RichError) as ei:
             h.upload_mesh(m)
         assert ei.value.status == 1
+
+
+# ---------------------------------------------------------------- FP32-mixed
+
+def run3(mesh, cells, precision, steps, gamma=5 / 3):
+    with richgpu.Handle3(gamma=gamma, device=0, precision=precision) as h:
+        h.upload_mesh(mesh)
+        h.set_cells(cells)
+        h.init_extensives()
+        e0 = h.get_extensives()
+        dts = h.run(steps)
+        return h.get_cells(), h.get_extensives(), e0, dts
+
+
+@pytest.mark.parametrize("case", ["blast32", "sedov48"])
+def test_mixed_density_l1_vs_fp64_and_conservation(case):
+    if case == "blast32":
+        mesh, cells, steps = synthetic.cube_grid(32, 32, 32), synthetic.cube_blast_cells(32, 32, 32), 60
+    else:
+        box = dict(lo=(-0.5, -0.5, -0.5), hi=(0.5, 0.5, 0.5))
+        mesh, cells, steps = synthetic.cube_grid(48, 48, 48, **box), synthetic.cube_sedov_cells(48), 60
+    c64, _, _, _ = run3(mesh, cells, 0, steps)
+    c32, e32, e0, _ = run3(mesh, cells, 1, steps)
+    l1 = np.abs(c32[:, 0] - c64[:, 0]).sum() / np.abs(c64[:, 0]).sum()
+    assert l1 <= 1e-5, l1
+    assert np.all(np.isfinite(c32))
+    # the FP32 flux of a face enters its two cells with opposite signs; walls carry no mass or energy
+    assert abs(e32[:, 0].sum() - e0[:, 0].sum()) <= 1e-13 * e0[:, 0].sum()
+    assert abs(e32[:, 4].sum() - e0[:, 4].sum()) <= 1e-12 * e0[:, 4].sum()
+
+
+def test_mixed_split_operations_equal_the_fused_step():
+    mesh = synthetic.cube_grid(20, 16, 12)
+    cells = synthetic.cube_blast_cells(20, 16, 12)
+    with richgpu.Handle3(gamma=5 / 3, device=0, precision=1) as h:
+        h.upload_mesh(mesh)
+        h.set_cells(cells)
+        h.init_extensives()
+        e0 = h.get_extensives()
+        dt = h.step()
+        fc, fe = h.get_cells(), h.get_extensives()
+        h.set_cells(cells)
+        h.set_extensives(e0)
+        assert h.cfl_dt() == dt
+        h.flux(download=False)
+        h.extensive_update(dt)
+        h.cell_update()
+        exact(h.get_extensives(), fe)
+        exact(h.get_cells(), fc)
+
+
+def test_mixed_full_size_sedov_96():
+    box = dict(lo=(-0.5, -0.5, -0.5), hi=(0.5, 0.5, 0.5))
+    mesh, cells = synthetic.cube_grid(96, 96, 96, **box), synthetic.cube_sedov_cells(96)
+    c64, _, _, _ = run3(mesh, cells, 0, 20)
+    c32, _, _, _ = run3(mesh, cells, 1, 20)
+    l1 = np.abs(c32[:, 0] - c64[:, 0]).sum() / np.abs(c64[:, 0]).sum()
+    assert l1 <= 1e-5, l1
