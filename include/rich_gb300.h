@@ -299,6 +299,56 @@ rg_status rg_autotune(rg_handle* h, int32_t reps, rg_launch_shapes* chosen);
 rg_status rg_set_launch_shapes(rg_handle* h, const rg_launch_shapes* shapes);
 rg_status rg_get_launch_shapes(const rg_handle* h, rg_launch_shapes* shapes);
 
+/* Tracers and stickers ---------------------------------------------------- */
+/* ComputationalCell::tracers / ::stickers (computational_cell_2d.hpp:19-36)
+ * and Extensive::tracers (extensive.hpp) on the FP64 path, with the
+ * reference's plugins that read them:
+ *   hdsim's TracerStickerNames (hdsim2d.hpp:86-101, names sorted by hdsim's
+ *     constructor, hdsim2d.cpp:121-136): tracer j and sticker bit k are the
+ *     j-th / k-th names in sorted order;
+ *   LinearGaussImproved(..., calc_tracers, skip_key)
+ *     (LinearGaussImproved.hpp:45-58): tracers outside calc_tracers get zero
+ *     slopes, limited ones use the velocity form of both limiters; cells
+ *     carrying the skip_key sticker are left out of the limiters' neighbour
+ *     max/min and of the shocked limiter's edges (this changes hydro slopes
+ *     too);
+ *   ModularFluxCalculator / SimpleFluxCalculator tracer fluxes
+ *     (modular_flux_calculator.cpp:24-35, simple_flux_calculator.cpp:193-213):
+ *     mass flux times the upwind side's tracer;
+ *   SimpleExtensiveUpdater (dt*area scaling of every extensive tracer);
+ *   SimpleCellUpdater (simple_cell_updater.cpp:22-106): tracer = extensive
+ *     tracer / mass; the tracer named "Entropy" is recomputed as
+ *     IdealGas::dp2s(d, p) = p*pow(d, -gamma) and its extensive set to s*mass;
+ *     a sequence entry (HasSticker(name), SkipUpdate()) keeps the old cell of
+ *     every cell with that sticker (its extensives still take the fluxes).
+ * Tracer arrays are cell-major: n_cells*n_tracers (cells[i].tracers[j] at
+ * i*n_tracers + j); tracer fluxes n_faces*n_tracers; tracer slopes
+ * n_cells*2*n_tracers (x derivatives then y derivatives of each cell).
+ * Stickers are one uint32 bit mask per cell.  Ghost points take the tracers
+ * and stickers of the cell they copy.  The FP32-mixed path, batches, Heun
+ * and differentiation return RG_ERR_INVALID_ARGUMENT while tracers or
+ * stickers are configured.  Entropy uses the device pow(): that one tracer
+ * agrees with the host libm to a few ulp; everything else is bit for bit. */
+#define RG_MAX_TRACERS 8
+typedef struct rg_tracer_config {
+  int32_t n_tracers;        /* 0..RG_MAX_TRACERS */
+  uint32_t limited_mask;    /* bit j: tracer j is in LinearGaussImproved's calc_tracers */
+  int32_t entropy_tracer;   /* index of the "Entropy" tracer, -1: none */
+  int32_t skip_sticker;     /* sticker bit of LinearGaussImproved's skip_key, -1: none */
+  int32_t frozen_sticker;   /* sticker bit of SimpleCellUpdater's HasSticker + SkipUpdate, -1: none */
+} rg_tracer_config;
+/* cfg == NULL or {0, 0, -1, -1, -1}: no tracers, no stickers (the default).
+ * Tracer values start unset (rg_set_tracers), stickers all clear. */
+rg_status rg_set_tracer_config(rg_handle* h, const rg_tracer_config* cfg);
+rg_status rg_set_tracers(rg_handle* h, const double* tracers);
+rg_status rg_get_tracers(rg_handle* h, double* tracers);
+rg_status rg_set_extensive_tracers(rg_handle* h, const double* tracers);
+rg_status rg_get_extensive_tracers(rg_handle* h, double* tracers);
+rg_status rg_set_stickers(rg_handle* h, const uint32_t* stickers);
+/* after rg_flux: the unscaled tracer fluxes and the tracer slopes (order 2) */
+rg_status rg_get_tracer_fluxes(rg_handle* h, double* tracer_fluxes);
+rg_status rg_get_tracer_slopes(rg_handle* h, double* tracer_slopes);
+
 /* Differentiation --------------------------------------------------------- */
 /* No counterpart in the reference (it has no differentiation).  The map
  * differentiated is n_steps hdsim::TimeAdvance steps (hdsim2d.cpp:149-241)

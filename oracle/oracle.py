@@ -172,6 +172,116 @@ def run_fixed_dt(mesh, cells, gamma, steps, dt, lp=None):
     return cells, ext
 
 
+# ---------------------------------------------------------------- tracers and stickers
+
+class RoTracers(C.Structure):
+    _fields_ = [("n", C.c_int32), ("limited", C.c_uint32), ("entropy", C.c_int32),
+                ("skip_mask", C.c_uint32), ("frozen_mask", C.c_uint32),
+                ("stickers", C.POINTER(C.c_uint32))]
+
+
+class TracerSetup:
+    """Tracer count, calc_tracers mask, "Entropy" index, skip_key and
+    SkipUpdate sticker bits (-1: none) and the per-cell sticker masks."""
+
+    def __init__(self, n, limited=0, entropy=-1, skip_sticker=-1, frozen_sticker=-1, stickers=None):
+        self.n, self.limited, self.entropy = n, limited, entropy
+        self.skip_sticker, self.frozen_sticker = skip_sticker, frozen_sticker
+        self.stickers = None if stickers is None else np.ascontiguousarray(stickers, dtype=np.uint32)
+
+    def c(self):
+        st = None if self.stickers is None else self.stickers.ctypes.data_as(C.POINTER(C.c_uint32))
+        return RoTracers(self.n, self.limited, self.entropy,
+                         (1 << self.skip_sticker) if self.skip_sticker >= 0 else 0,
+                         (1 << self.frozen_sticker) if self.frozen_sticker >= 0 else 0, st)
+
+
+def _setup_tr():
+    L = lib()
+    if getattr(L, "_rotr", False):
+        return L
+    dp = C.POINTER(C.c_double)
+    L.ro_extensive_update_tr.restype = None
+    L.ro_extensive_update_tr.argtypes = [C.c_void_p, dp, C.c_int, C.c_double, dp]
+    L.ro_init_extensives_tr.restype = None
+    L.ro_init_extensives_tr.argtypes = [C.c_void_p, dp, dp, C.c_int, dp]
+    L._rotr = True
+    return L
+
+
+def lgi_tr(mesh, cells, tr, gamma, lp, ts):
+    n, N, E = ts.n, mesh.n_cells, mesh.n_faces
+    slopes, interp = np.zeros((N, 8)), np.zeros((E, 8))
+    tsl, tip = np.zeros((N, 2 * n)), np.zeros((E, 2 * n))
+    cells, tr = _f64(cells), _f64(tr)
+    err, tc = RoError(), ts.c()
+    _check(_setup_tr().ro_lgi_tr(C.byref(mesh.view()), _d(cells), _d(tr), C.c_double(gamma), C.byref(lp),
+                                 C.byref(tc), _d(slopes), _d(interp), _d(tsl), _d(tip), C.byref(err)), err)
+    return slopes, interp, tsl, tip
+
+
+def flux_tr(mesh, cells, tr, ev, gamma, order, lp, ts):
+    """(fluxes, tracer fluxes) of SimpleFluxCalculator (order 1) or
+    ModularFluxCalculator with LinearGaussImproved (order 2)."""
+    E = mesh.n_faces
+    fl, tfl = np.zeros((E, 4)), np.zeros((E, max(ts.n, 1)))
+    cells, tr, ev = _f64(cells), _f64(tr), _f64(ev)
+    err, tc = RoError(), ts.c()
+    L = _setup_tr()
+    if order == 1:
+        st = L.ro_simple_flux_tr(C.byref(mesh.view()), _d(cells), _d(tr), _d(ev), C.c_double(gamma), C.byref(tc),
+                                 _d(fl), _d(tfl), C.byref(err))
+    else:
+        st = L.ro_modular_flux_tr(C.byref(mesh.view()), _d(cells), _d(tr), _d(ev), C.c_double(gamma), C.byref(lp),
+                                  C.byref(tc), _d(fl), _d(tfl), C.byref(err))
+    _check(st, err)
+    return fl, tfl[:, :ts.n]
+
+
+def extensive_update_tr(mesh, tfluxes, dt, tr_ext):
+    tr_ext = _f64(tr_ext).copy()
+    nt = tr_ext.shape[1]
+    _setup_tr().ro_extensive_update_tr(C.byref(mesh.view()), _d(_f64(tfluxes)), nt, dt, _d(tr_ext))
+    return tr_ext
+
+
+def cell_update_tr(mesh, ext, tr_ext, old_cells, old_tr, gamma, ts):
+    """SimpleCellUpdater with tracers; returns (cells, tracers, extensive tracers)."""
+    N = mesh.n_cells
+    cells, tr = np.zeros((N, 4)), np.zeros((N, ts.n))
+    tr_ext = _f64(tr_ext).copy()
+    err, tc = RoError(), ts.c()
+    _check(_setup_tr().ro_cell_update_tr(C.byref(mesh.view()), _d(_f64(ext)), _d(tr_ext), _d(_f64(old_cells)),
+                                         _d(_f64(old_tr)), C.c_double(gamma), C.byref(tc), _d(cells), _d(tr),
+                                         C.byref(err)), err)
+    return cells, tr, tr_ext
+
+
+def init_extensives_tr(mesh, cells, tr):
+    tr = _f64(tr)
+    out = np.zeros_like(tr)
+    _setup_tr().ro_init_extensives_tr(C.byref(mesh.view()), _d(_f64(cells)), _d(tr), tr.shape[1], _d(out))
+    return out
+
+
+def run_tr(mesh, cells, ext, tr, tr_ext, ev, gamma, steps, ts, cfl_number=0.3, order=2, lp=None):
+    """hdsim::TimeAdvance steps with tracers on a fixed mesh; returns
+    (cells, ext, tracers, extensive tracers, dts)."""
+    cells, ext = _f64(cells).copy(), _f64(ext).copy()
+    tr, tr_ext = _f64(tr).copy(), _f64(tr_ext).copy()
+    ev = _f64(ev)
+    lp = lp or lgi_params()
+    L = _setup_tr()
+    dts = []
+    for _ in range(steps):
+        dt, err, tc = C.c_double(), RoError(), ts.c()
+        _check(L.ro_step_tr(C.byref(mesh.view()), _d(cells), _d(ext), _d(tr), _d(tr_ext), _d(ev), C.c_double(gamma),
+                            C.c_double(cfl_number), C.c_int(order), C.byref(lp), C.byref(tc), C.byref(dt),
+                            C.byref(err)), err)
+        dts.append(dt.value)
+    return cells, ext, tr, tr_ext, np.array(dts)
+
+
 # ---------------------------------------------------------------- 3D first-order path
 
 def _setup3():

@@ -10,6 +10,13 @@
 // With "heun" the warm-up and run steps use hdsim::TimeAdvance2Heun
 // (hdsim2d.cpp:323-449) instead of hdsim::TimeAdvance.
 //
+// Cases named <case>_tracers add tracers and stickers: tracer names
+// {"A", "Entropy", "Z"} ("A" in LinearGaussImproved's calc_tracers,
+// "Entropy" recomputed by SimpleCellUpdater, "Z" piecewise constant), sticker
+// names {"frozen", "skip"} ("skip" is LinearGaussImproved's skip_key, cells
+// with "frozen" keep their state through HasSticker + SkipUpdate), and dump
+// the tracer / sticker arrays beside the others (tr_*).
+//
 // For every case it writes, for the state reached after <warm_steps>
 // hdsim::TimeAdvance steps (hdsim2d.cpp:149-241):
 //   mesh_*          the packed tessellation (huji-rich_gb300/host/rich_pack.hpp)
@@ -25,6 +32,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <memory>
 #include <random>
 #include <string>
@@ -114,6 +122,20 @@ std::vector<double> ext_flat(const std::vector<Extensive>& e) {
   }
   return r;
 }
+std::vector<double> tracers_flat(const std::vector<ComputationalCell>& c) {
+  std::vector<double> r;
+  for (const auto& x : c)
+    for (double t : x.tracers) r.push_back(t);
+  return r;
+}
+std::vector<double> ext_tracers_flat(const std::vector<Extensive>& e) {
+  std::vector<double> r;
+  for (const auto& x : e)
+    for (double t : x.tracers) r.push_back(t);
+  return r;
+}
+size_t g_ntr = 0;
+
 std::vector<double> vec_flat(const std::vector<Vector2D>& v) {
   std::vector<double> r;
   for (const auto& x : v) {
@@ -167,6 +189,17 @@ void dump_components(hdsim& sim, const PhysicalGeometry& pg, const EquationOfSta
   dump_mesh("mesh_", tess, pg);
   dump_f64("cells0", cells_flat(cells), 4);
   dump_f64("ext0", ext_flat(ext), 4);
+  if (g_ntr) {
+    dump_f64("tr_cells0", tracers_flat(cells), g_ntr);
+    dump_f64("tr_ext0", ext_tracers_flat(ext), g_ntr);
+    std::vector<int32_t> st;
+    for (const auto& c : cells) {
+      int32_t bits = 0;
+      for (size_t k = 0; k < c.stickers.size(); ++k) bits |= c.stickers[k] ? (1 << k) : 0;
+      st.push_back(bits);
+    }
+    dump_i32("tr_stickers", st, 0);
+  }
   dump_scalar("time0", t);
   vector<Vector2D> pv = pm(tess, cells, t, tsn);
   vector<Vector2D> ev = evc(tess, pv);
@@ -200,14 +233,35 @@ void dump_components(hdsim& sim, const PhysicalGeometry& pg, const EquationOfSta
       }
     dump_f64("slopes", sl, 8);
     dump_f64("interp", ip, 8);
+    if (g_ntr) {
+      std::vector<double> tsl, tip;
+      for (const Slope& s : lgi->GetSlopes()) {
+        for (double t : s.xderivative.tracers) tsl.push_back(t);
+        for (double t : s.yderivative.tracers) tsl.push_back(t);
+      }
+      for (const auto& pr : interp) {
+        for (double t : pr.first.tracers) tip.push_back(t);
+        for (double t : pr.second.tracers) tip.push_back(t);
+      }
+      dump_f64("tr_slopes", tsl, 2 * g_ntr);
+      dump_f64("tr_interp", tip, 2 * g_ntr);
+    }
   }
   const vector<Extensive> fl = fc(tess, ev, cells, ext, cd, eos, t, dt, tsn);
   dump_f64("fluxes", ext_flat(fl), 4);
   vector<Extensive> ext1 = ext;
   eu(fl, pg, tess, dt, cd, cells, ext1, t, tsn);
   dump_f64("ext1", ext_flat(ext1), 4);
+  if (g_ntr) {
+    dump_f64("tr_fluxes", ext_tracers_flat(fl), g_ntr);
+    dump_f64("tr_ext1", ext_tracers_flat(ext1), g_ntr);
+  }
   const vector<ComputationalCell> cells1 = cu(tess, pg, eos, ext1, cells, cd, tsn);
   dump_f64("cells1", cells_flat(cells1), 4);
+  if (g_ntr) {
+    dump_f64("tr_cells1", tracers_flat(cells1), g_ntr);
+    dump_f64("tr_ext1b", ext_tracers_flat(ext1), g_ntr);  // after the cell updater (entropy tracer)
+  }
 }
 
 void run_and_dump(hdsim& sim, int steps) {
@@ -220,6 +274,10 @@ void run_and_dump(hdsim& sim, int steps) {
   }
   dump_f64("run_cells", cells_flat(sim.getAllCells()), 4);
   dump_f64("run_ext", ext_flat(sim.getAllExtensives()), 4);
+  if (g_ntr) {
+    dump_f64("tr_run_cells", tracers_flat(sim.getAllCells()), g_ntr);
+    dump_f64("tr_run_ext", ext_tracers_flat(sim.getAllExtensives()), g_ntr);
+  }
   dump_scalar("run_time", sim.getTime());
   dump_f64("run_times", times, 0);
   dump_mesh("runmesh_", sim.getTessellation(), SlabSymmetry());
@@ -232,7 +290,33 @@ int main(int argc, char** argv) {
     std::fprintf(stderr, "usage: ref_dump <case> <outdir> <nx> <ny> <warm> <run>\n");
     return 2;
   }
-  const std::string which = argv[1];
+  std::string which = argv[1];
+  const std::string sfx = "_tracers";
+  const bool tracers = which.size() > sfx.size() && which.compare(which.size() - sfx.size(), sfx.size(), sfx) == 0;
+  if (tracers) {
+    which = which.substr(0, which.size() - sfx.size());
+    g_ntr = 3;
+  }
+  // tracer / sticker setup of the _tracers cases (names sorted, as the
+  // reference's binary_find lookups need)
+  const TracerStickerNames tsn = tracers ? TracerStickerNames({"A", "Entropy", "Z"}, {"frozen", "skip"})
+                                         : TracerStickerNames();
+  const vector<string> calc_tracers = tracers ? vector<string>{"A"} : vector<string>();
+  const string skip_key = tracers ? "skip" : "";
+  // frozen_r: stickers only on cells at least this far from the origin (a
+  // frozen or limiter-skipped cell next to a blast drives the state there to
+  // negative pressure, which the reference asserts on)
+  auto add_tracers = [&](vector<ComputationalCell>& ic, const Tessellation& tess, double gamma,
+                         double frozen_r = 0.0) {
+    if (!tracers) return;
+    for (size_t i = 0; i < ic.size(); ++i) {
+      const Vector2D r = tess.GetMeshPoint(static_cast<int>(i));
+      ic[i].tracers = {r.x + (r.y > 0.1 ? 0.5 : 0.0), ic[i].pressure * std::pow(ic[i].density, -gamma),
+                       abs(r) < 0.3 ? 1.0 : 0.0};
+      const size_t h = std::hash<size_t>()(i * 2654435761u);
+      ic[i].stickers = {h % 17 == 3 && abs(r) >= frozen_r, h % 11 == 5 && abs(r) >= frozen_r};
+    }
+  };
   g_out = argv[2];
   const int nx = std::atoi(argv[3]), ny = std::atoi(argv[4]);
   const int warm = std::atoi(argv[5]), run = std::atoi(argv[6]);
@@ -243,7 +327,9 @@ int main(int argc, char** argv) {
     ZeroForce force;
     SimpleCFL tsf(0.3);
     SimpleExtensiveUpdater eu;
-    SimpleCellUpdater cu;
+    vector<pair<const SimpleCellUpdater::Condition*, const SimpleCellUpdater::Action*> > seq;
+    if (tracers) seq.push_back({new HasSticker("frozen"), new SkipUpdate()});
+    SimpleCellUpdater cu(seq);
     if (which == "sod" || which == "sod_lagrangian") {
       // 2D Sod tube: [0,1]x[0,0.2], reflective walls, piecewise-constant Hllc, gamma 1.4.
       SquareBox outer(Vector2D(0, 0), Vector2D(1, 0.2));
@@ -261,7 +347,8 @@ int main(int argc, char** argv) {
         ic[i].density = left ? 1 : 0.125;
         ic[i].pressure = left ? 1 : 0.1;
       }
-      hdsim sim(tess, outer, pg, ic, eos, pm, evc, force, tsf, fc, eu, cu);
+      add_tracers(ic, tess, 1.4);
+      hdsim sim(tess, outer, pg, ic, eos, pm, evc, force, tsf, fc, eu, cu, tsn);
       for (int s = 0; s < warm; ++s) advance(sim);
       dump_scalar("gamma", 1.4);
       dump_scalar("order", 1);
@@ -281,7 +368,7 @@ int main(int argc, char** argv) {
                                                : static_cast<const PointMotion&>(eul);
       StationaryBox evc;
       RigidWallGenerator gpg;
-      LinearGaussImproved sr(eos, gpg);
+      LinearGaussImproved sr(eos, gpg, true, 0.2, 0.5, 0.7, calc_tracers, skip_key);
       ModularFluxCalculator fc(sr, rs);
       const double dx = 2.0 / nx;
       const double rdep = std::max(0.02, 1.5 * dx);
@@ -293,7 +380,8 @@ int main(int argc, char** argv) {
         ic[i].density = 1;
         ic[i].pressure = abs(tess.GetMeshPoint(static_cast<int>(i))) < rdep ? (5. / 3. - 1) / vin : 1e-6;
       }
-      hdsim sim(tess, outer, pg, ic, eos, pm, evc, force, tsf, fc, eu, cu);
+      add_tracers(ic, tess, 5. / 3., 0.6);
+      hdsim sim(tess, outer, pg, ic, eos, pm, evc, force, tsf, fc, eu, cu, tsn);
       for (int s = 0; s < warm; ++s) advance(sim);
       dump_scalar("gamma", 5. / 3.);
       dump_scalar("order", 2);
@@ -311,7 +399,7 @@ int main(int argc, char** argv) {
                                                   : static_cast<const PointMotion&>(lag);
       PeriodicEdgeVelocities evc;
       PeriodicGhostGenerator gpg;
-      LinearGaussImproved sr(eos, gpg);
+      LinearGaussImproved sr(eos, gpg, true, 0.2, 0.5, 0.7, calc_tracers, skip_key);
       ModularFluxCalculator fc(sr, rs);
       std::mt19937_64 gen(7);
       std::uniform_real_distribution<double> u01(0, 1);
@@ -334,7 +422,8 @@ int main(int argc, char** argv) {
         ic[i].pressure = 1;
         ic[i].velocity = Vector2D(0.1 * std::sin(pi2 * (r.x + 2 * r.y)), 0.1 * std::cos(pi2 * (2 * r.x - r.y)));
       }
-      hdsim sim(tess, outer, pg, ic, eos, pm, evc, force, tsf, fc, eu, cu);
+      add_tracers(ic, tess, 5. / 3.);
+      hdsim sim(tess, outer, pg, ic, eos, pm, evc, force, tsf, fc, eu, cu, tsn);
       for (int s = 0; s < warm; ++s) advance(sim);
       dump_scalar("gamma", 5. / 3.);
       dump_scalar("order", 2);

@@ -278,6 +278,19 @@ static cc ccadd(cc a, cc b) { cc r = {a.d + b.d, a.p + b.p, a.vx + b.vx, a.vy + 
 
 typedef struct { cc x, y; } slope;
 
+/* Tracers of one cell and of its neighbours during LinearGaussImproved
+ * (ComputationalCell::tracers, computational_cell_2d.hpp): every
+ * ComputationalCell operation above applies to each tracer exactly as to a
+ * hydro field, so the tracer parts run beside the hydro ones with the same
+ * scalars. */
+#define RO_MAX_NB 64
+typedef struct {
+  int nt;
+  double ct[RG_MAX_TRACERS];              /* the cell's tracers */
+  double nb[RO_MAX_NB][RG_MAX_TRACERS];   /* neighbours' tracers (ghosts: copied cell's) */
+  double sx[RG_MAX_TRACERS], sy[RG_MAX_TRACERS];  /* tracer slopes */
+} trcell;
+
 /* Ghost states: RigidWallGenerator.cpp:17-37 / PeriodicGhostGenerator.cpp:3-17.
  * new_cells[ghost] for every ghost (LinearGaussImproved.cpp:543-550). */
 static void ghost_states(const rg_mesh_view* m, const double* cells, int ghost_kind, cc* gs) {
@@ -319,13 +332,15 @@ static void interp2(cc* r, slope s, v2 target, v2 cm) {
 /* :67-134 calc_naive_slope */
 static int naive_slope(const rg_mesh_view* m, int i, cc cell, v2 center, v2 cell_cm, double vol,
                        const int* edges, int n, const cc* nb, const v2* nb_pt, const v2* nb_cm,
-                       slope* res, ro_error* err) {
+                       slope* res, trcell* t, ro_error* err) {
   if (n > 20) {
     set_err(err, RG_ERR_TOO_MANY_NEIGHBORS, 2, i, n);
     return RG_ERR_TOO_MANY_NEIGHBORS;
   }
   double mm[4] = {0, 0, 0, 0};
   slope vc = {{0, 0, 0, 0}, {0, 0, 0, 0}};
+  double tvx[RG_MAX_TRACERS], tvy[RG_MAX_TRACERS];
+  const int nt = t ? t->nt : 0;
   for (int k = 0; k < n; ++k) {
     const int e = edges[k];
     const v2 c_ij = vsub(centroid(m, e), vscale(vadd(nb_cm[k], cell_cm), 0.5));
@@ -345,6 +360,17 @@ static int naive_slope(const rg_mesh_view* m, int i, cc cell, v2 center, v2 cell
     }
     addmult(&vc.y, nb[k], r_ij.y * 0.5);
     addmult(&vc.x, nb[k], r_ij.x * 0.5);
+    for (int j = 0; j < nt; ++j) {
+      if (k == 0) {
+        tvx[j] = t->ct[j] * (r_ij.x * 0.5);
+        tvy[j] = t->ct[j] * (r_ij.y * 0.5);
+      } else {
+        tvx[j] += t->ct[j] * (r_ij.x * 0.5);
+        tvy[j] += t->ct[j] * (r_ij.y * 0.5);
+      }
+      tvy[j] += t->nb[k][j] * (r_ij.y * 0.5);
+      tvx[j] += t->nb[k][j] * (r_ij.x * 0.5);
+    }
   }
   mm[0] += vol;
   mm[3] += vol;
@@ -359,16 +385,28 @@ static int naive_slope(const rg_mesh_view* m, int i, cc cell, v2 center, v2 cell
   res->y = ccscale(vc.y, mi3);
   addmult(&res->x, vc.y, mi1);
   addmult(&res->y, vc.x, mi2);
+  for (int j = 0; j < nt; ++j) {
+    t->sx[j] = tvx[j] * mi0;
+    t->sy[j] = tvy[j] * mi3;
+    t->sx[j] += tvy[j] * mi1;
+    t->sy[j] += tvx[j] * mi2;
+  }
   return 0;
 }
 
 /* :401-422 GetBoundarySlope */
-static void boundary_slope(cc cell, v2 cell_cm, int n, const cc* nb, const v2* nb_cm, slope* res) {
+static void boundary_slope(cc cell, v2 cell_cm, int n, const cc* nb, const v2* nb_cm, slope* res, trcell* t) {
   cc phisy = {0, 0, 0, 0}, phisx = {0, 0, 0, 0};
+  double tpy[RG_MAX_TRACERS] = {0}, tpx[RG_MAX_TRACERS] = {0};
+  const int nt = t ? t->nt : 0;
   double sxsy = 0, sy2 = 0, sx2 = 0;
   for (int k = 0; k < n; ++k) {
     phisy = ccadd(phisy, ccscale(ccsub(nb[k], cell), nb_cm[k].y - cell_cm.y));
     phisx = ccadd(phisx, ccscale(ccsub(nb[k], cell), nb_cm[k].x - cell_cm.x));
+    for (int j = 0; j < nt; ++j) {
+      tpy[j] = tpy[j] + (t->nb[k][j] - t->ct[j]) * (nb_cm[k].y - cell_cm.y);
+      tpx[j] = tpx[j] + (t->nb[k][j] - t->ct[j]) * (nb_cm[k].x - cell_cm.x);
+    }
     sxsy += (nb_cm[k].y - cell_cm.y) * (nb_cm[k].x - cell_cm.x);
     sx2 += (nb_cm[k].x - cell_cm.x) * (nb_cm[k].x - cell_cm.x);
     sy2 += (nb_cm[k].y - cell_cm.y) * (nb_cm[k].y - cell_cm.y);
@@ -378,6 +416,10 @@ static void boundary_slope(cc cell, v2 cell_cm, int n, const cc* nb, const v2* n
   const cc ay = ccsub(ccscale(phisx, sxsy), ccscale(phisy, sx2));
   res->x.d = ax.d / den; res->x.p = ax.p / den; res->x.vx = ax.vx / den; res->x.vy = ax.vy / den;
   res->y.d = ay.d / den; res->y.p = ay.p / den; res->y.vx = ay.vx / den; res->y.vy = ay.vy / den;
+  for (int j = 0; j < nt; ++j) {
+    t->sx[j] = (tpy[j] * sxsy - tpx[j] * sy2) / den;
+    t->sy[j] = (tpx[j] * sxsy - tpy[j] * sx2) / den;
+  }
 }
 
 /* :136-148 PressureRatio, :150-157 is_shock */
@@ -412,11 +454,22 @@ static void limit_comp(double dphi, double cv, double cellv, double maxd, double
 
 /* :174-300 slope_limit */
 static void slope_limit(const rg_mesh_view* m, cc cell, v2 cm, int n, const cc* nb, const int* edges,
-                        slope* s) {
+                        const int* skip, slope* s, trcell* t) {
+  const int nt = t ? t->nt : 0;
   cc cmax = cell, cmin = cell;
+  double tmax[RG_MAX_TRACERS], tmin[RG_MAX_TRACERS], tpsi[RG_MAX_TRACERS];
+  for (int j = 0; j < nt; ++j) {
+    tmax[j] = tmin[j] = t->ct[j];
+    tpsi[j] = 1;
+  }
   for (int k = 0; k < n; ++k) {
     const int e = edges[k];
+    if (skip[k]) continue; /* :192-193 neighbours with the skip_key sticker */
     if (orig(m, fc0(m, e)) == orig(m, fc1(m, e))) continue;
+    for (int j = 0; j < nt; ++j) {
+      tmax[j] = smax(tmax[j], t->nb[k][j]);
+      tmin[j] = smin(tmin[j], t->nb[k][j]);
+    }
     cmax.d = smax(cmax.d, nb[k].d);
     cmax.p = smax(cmax.p, nb[k].p);
     cmax.vx = smax(cmax.vx, nb[k].vx);
@@ -430,17 +483,29 @@ static void slope_limit(const rg_mesh_view* m, cc cell, v2 cm, int n, const cc* 
   double psi[4] = {1, 1, 1, 1};
   for (int k = 0; k < n; ++k) {
     cc cv = cell;
-    interp2(&cv, *s, centroid(m, edges[k]), cm);
+    const v2 target = centroid(m, edges[k]);
+    interp2(&cv, *s, target, cm);
     const cc dphi = ccsub(cv, cell);
     limit_comp(dphi.d, cv.d, cell.d, maxdiff.d, mindiff.d, 0, &psi[0]);
     limit_comp(dphi.p, cv.p, cell.p, maxdiff.p, mindiff.p, 0, &psi[1]);
     limit_comp(dphi.vx, cv.vx, cell.vx, maxdiff.vx, mindiff.vx, 1, &psi[2]);
     limit_comp(dphi.vy, cv.vy, cell.vy, maxdiff.vy, mindiff.vy, 1, &psi[3]);
+    /* :268-283 tracers: the velocity form, |1e-9*tracer| dead band */
+    for (int j = 0; j < nt; ++j) {
+      double cvt = t->ct[j];
+      cvt += t->sx[j] * (target.x - cm.x);
+      cvt += t->sy[j] * (target.y - cm.y);
+      limit_comp(cvt - t->ct[j], cvt, t->ct[j], tmax[j] - t->ct[j], tmin[j] - t->ct[j], 1, &tpsi[j]);
+    }
   }
   s->x.d *= psi[0]; s->y.d *= psi[0];
   s->x.p *= psi[1]; s->y.p *= psi[1];
   s->x.vx *= psi[2]; s->y.vx *= psi[2];
   s->x.vy *= psi[3]; s->y.vy *= psi[3];
+  for (int j = 0; j < nt; ++j) {
+    t->sx[j] *= tpsi[j];
+    t->sy[j] *= tpsi[j];
+  }
 }
 
 /* one component of :343-366 (shocked limiter); the threshold is 1e-9*q
@@ -454,9 +519,20 @@ static void shocked_comp(double dphi, double cv, double cellv, double maxd, doub
 
 /* :302-399 shocked_slope_limit */
 static void shocked_slope_limit(const rg_mesh_view* m, cc cell, v2 cm, int n, const cc* nb,
-                                const int* edges, double theta, slope* s) {
+                                const int* edges, const int* skip, double theta, slope* s, trcell* t) {
+  const int nt = t ? t->nt : 0;
   cc cmax = cell, cmin = cell;
+  double tmax[RG_MAX_TRACERS], tmin[RG_MAX_TRACERS], tpsi[RG_MAX_TRACERS];
+  for (int j = 0; j < nt; ++j) {
+    tmax[j] = tmin[j] = t->ct[j];
+    tpsi[j] = 1;
+  }
   for (int k = 0; k < n; ++k) {
+    if (skip[k]) continue; /* :314-315 */
+    for (int j = 0; j < nt; ++j) {
+      tmax[j] = smax(tmax[j], t->nb[k][j]);
+      tmin[j] = smin(tmin[j], t->nb[k][j]);
+    }
     cmax.d = smax(cmax.d, nb[k].d);
     cmax.p = smax(cmax.p, nb[k].p);
     cmax.vx = smax(cmax.vx, nb[k].vx);
@@ -469,40 +545,85 @@ static void shocked_slope_limit(const rg_mesh_view* m, cc cell, v2 cm, int n, co
   const cc maxdiff = ccsub(cmax, cell), mindiff = ccsub(cmin, cell);
   double psi[4] = {1, 1, 1, 1};
   for (int k = 0; k < n; ++k) {
+    if (skip[k]) continue; /* :339-340 */
     cc cv = cell;
-    interp2(&cv, *s, centroid(m, edges[k]), cm);
+    const v2 target = centroid(m, edges[k]);
+    interp2(&cv, *s, target, cm);
     const cc dphi = ccsub(cv, cell);
     shocked_comp(dphi.d, cv.d, cell.d, maxdiff.d, mindiff.d, nb[k].d, theta, &psi[0]);
     shocked_comp(dphi.p, cv.p, cell.p, maxdiff.p, mindiff.p, nb[k].p, theta, &psi[1]);
     shocked_comp(dphi.vx, cv.vx, cell.vx, maxdiff.vx, mindiff.vx, nb[k].vx, theta, &psi[2]);
     shocked_comp(dphi.vy, cv.vy, cell.vy, maxdiff.vy, mindiff.vy, nb[k].vy, theta, &psi[3]);
+    /* :367-385 tracers: threshold |1e-9*tracer| */
+    for (int j = 0; j < nt; ++j) {
+      const double ctj = t->ct[j];
+      double cvt = ctj;
+      cvt += t->sx[j] * (target.x - cm.x);
+      cvt += t->sy[j] * (target.y - cm.y);
+      const double dphi_t = cvt - ctj, maxd = tmax[j] - ctj, mind = tmin[j] - ctj;
+      if (fabs(dphi_t) > 0.1 * smax(fabs(maxd), fabs(mind)) || cvt * ctj < 0) {
+        if (fabs(dphi_t) > fabs(1e-9 * ctj))
+          tpsi[j] = smin(tpsi[j], smax(theta * (t->nb[k][j] - ctj) / dphi_t, 0.0));
+      }
+    }
   }
   s->x.d *= psi[0]; s->y.d *= psi[0];
   s->x.p *= psi[1]; s->y.p *= psi[1];
   s->x.vx *= psi[2]; s->y.vx *= psi[2];
   s->x.vy *= psi[3]; s->y.vy *= psi[3];
+  for (int j = 0; j < nt; ++j) {
+    t->sx[j] *= tpsi[j];
+    t->sy[j] *= tpsi[j];
+  }
 }
 
 static void put_cc(double* o, cc c) { o[0] = c.d; o[1] = c.p; o[2] = c.vx; o[3] = c.vy; }
 static cc get_cc(const double* o) { cc c = {o[0], o[1], o[2], o[3]}; return c; }
 
-/* :536-635 LinearGaussImproved::operator() (serial build), with :425-494 calc_slope */
-int ro_lgi(const rg_mesh_view* m, const double* cells, double g, const ro_lgi_params* lp,
-           double* slopes, double* interp, ro_error* err) {
+/* The cell whose tracers and stickers point p carries: p itself, or the cell
+ * a ghost copies (PeriodicGhostGenerator.cpp:3-17: the source;
+ * RigidWallGenerator.cpp:17-37: the real side of the ghost's face); -1 for
+ * a ghost on no face. */
+static int copied_cell(const rg_mesh_view* m, int p, int ghost_kind) {
   const int N = m->n_cells;
+  if (p < N) return p;
+  const int g = p - N;
+  if (ghost_kind == RG_GHOST_PERIODIC) return m->ghost_source[g];
+  const int e = m->ghost_face[g];
+  if (e < 0) return -1;
+  return fc0(m, e) >= N ? fc1(m, e) : fc0(m, e);
+}
+
+static uint32_t stickers_of(const ro_tracers* t, int c) {
+  return t && t->stickers && c >= 0 ? t->stickers[c] : 0u;
+}
+
+/* :536-635 LinearGaussImproved::operator() (serial build), with :425-494 calc_slope */
+int ro_lgi_tr(const rg_mesh_view* m, const double* cells, const double* tr, double g, const ro_lgi_params* lp,
+              const ro_tracers* t, double* slopes, double* interp, double* tslopes, double* tinterp,
+              ro_error* err) {
+  const int N = m->n_cells;
+  const int nt = t ? t->n : 0;
   cc* gs = (cc*)calloc((size_t)(m->n_ghosts > 0 ? m->n_ghosts : 1), sizeof(cc));
   slope* sl = (slope*)calloc((size_t)N, sizeof(slope));
+  double* tsl = (double*)calloc((size_t)N * 2 * (nt > 0 ? nt : 1), sizeof(double));
+  trcell* tc = nt > 0 ? (trcell*)calloc(1, sizeof(trcell)) : NULL;
   int st = 0;
   ghost_states(m, cells, lp->ghost_kind, gs);
   for (int i = 0; i < N && !st; ++i) {
     const int b = m->cell_face_offset[i], n = m->cell_face_offset[i + 1] - b;
     const int* edges = m->cell_faces + b;
-    cc nb[64];
-    v2 nb_pt[64], nb_cm[64];
-    if (n > 64) {
+    cc nb[RO_MAX_NB];
+    v2 nb_pt[RO_MAX_NB], nb_cm[RO_MAX_NB];
+    int skip[RO_MAX_NB];
+    if (n > RO_MAX_NB) {
       set_err(err, RG_ERR_TOO_MANY_NEIGHBORS, 2, i, n);
       st = RG_ERR_TOO_MANY_NEIGHBORS;
       break;
+    }
+    if (tc) {
+      tc->nt = nt;
+      for (int j = 0; j < nt; ++j) tc->ct[j] = tr[(size_t)i * nt + j];
     }
     int bslope = 0;
     for (int k = 0; k < n; ++k) {
@@ -512,32 +633,50 @@ int ro_lgi(const rg_mesh_view* m, const double* cells, double g, const ro_lgi_pa
       nb_pt[k] = point(m, other);
       nb_cm[k] = cmof(m, other);
       if (orig(m, fc0(m, e)) == orig(m, fc1(m, e))) bslope = 1;
+      const int src = copied_cell(m, other, lp->ghost_kind);
+      skip[k] = t && t->skip_mask && (stickers_of(t, src) & t->skip_mask) != 0;
+      for (int j = 0; j < nt; ++j) tc->nb[k][j] = src >= 0 ? tr[(size_t)src * nt + j] : 0.0;
     }
     const cc cell = cell_at(cells, i);
     slope s;
     if (bslope)
-      boundary_slope(cell, cmof(m, i), n, nb, nb_cm, &s);
+      boundary_slope(cell, cmof(m, i), n, nb, nb_cm, &s, tc);
     else {
-      st = naive_slope(m, i, cell, point(m, i), cmof(m, i), m->volume[i], edges, n, nb, nb_pt, nb_cm, &s, err);
+      st = naive_slope(m, i, cell, point(m, i), cmof(m, i), m->volume[i], edges, n, nb, nb_pt, nb_cm, &s, tc, err);
       if (st) break;
     }
+    /* :470-479 tracers outside calc_tracers get zero slopes */
+    for (int j = 0; j < nt; ++j)
+      if (!((t->limited >> j) & 1u)) tc->sx[j] = tc->sy[j] = 0;
     if (lp->slf) {
       if (!is_shock(s, width(m, i), lp->delta_v, cell, n, nb, lp->delta_p, dp2c(g, cell.d, cell.p)))
-        slope_limit(m, cell, cmof(m, i), n, nb, edges, &s);
+        slope_limit(m, cell, cmof(m, i), n, nb, edges, skip, &s, tc);
       else
-        shocked_slope_limit(m, cell, cmof(m, i), n, nb, edges, lp->theta, &s);
+        shocked_slope_limit(m, cell, cmof(m, i), n, nb, edges, skip, lp->theta, &s, tc);
     }
     sl[i] = s;
     if (slopes) {
       put_cc(slopes + 8 * i, s.x);
       put_cc(slopes + 8 * i + 4, s.y);
     }
+    for (int j = 0; j < nt; ++j) {
+      tsl[(size_t)i * 2 * nt + j] = tc->sx[j];
+      tsl[(size_t)i * 2 * nt + nt + j] = tc->sy[j];
+    }
     /* :570-590 interpolation of the real side of each edge */
     for (int k = 0; k < n; ++k) {
       const int e = edges[k];
       cc r = cell;
-      interp2(&r, s, centroid(m, e), cmof(m, i));
-      put_cc(interp + 8 * e + (fc0(m, e) == i ? 0 : 4), r);
+      const v2 target = centroid(m, e), cm = cmof(m, i);
+      interp2(&r, s, target, cm);
+      const int side = fc0(m, e) == i ? 0 : 1;
+      put_cc(interp + 8 * e + 4 * side, r);
+      for (int j = 0; j < nt; ++j) {
+        double rt = tc->ct[j];
+        rt += tc->sx[j] * (target.x - cm.x);
+        rt += tc->sy[j] * (target.y - cm.y);
+        if (tinterp) tinterp[(size_t)e * 2 * nt + (size_t)side * nt + j] = rt;
+      }
     }
   }
   if (!st) {
@@ -550,29 +689,56 @@ int ro_lgi(const rg_mesh_view* m, const double* cells, double g, const ro_lgi_pa
       else continue;
       cc r = gs[gp - N];
       slope gg;
-      if (lp->ghost_kind == RG_GHOST_PERIODIC)
+      const int periodic = lp->ghost_kind == RG_GHOST_PERIODIC;
+      if (periodic)
         gg = sl[orig(m, gp)];
       else
         memset(&gg, 0, sizeof gg);
-      interp2(&r, gg, centroid(m, e), cmof(m, gp));
+      const v2 target = centroid(m, e), cm = cmof(m, gp);
+      interp2(&r, gg, target, cm);
       put_cc(interp + 8 * e + 4 * side, r);
+      /* tracers: the copied cell's values; periodic ghosts take the source's
+       * gradient, rigid walls a zero one (RigidWallGenerator.cpp:39-54) */
+      const int src = copied_cell(m, gp, lp->ghost_kind);
+      for (int j = 0; j < nt; ++j) {
+        double rt = src >= 0 ? tr[(size_t)src * nt + j] : 0.0;
+        const double gx = periodic ? tsl[(size_t)orig(m, gp) * 2 * nt + j] : 0.0;
+        const double gy = periodic ? tsl[(size_t)orig(m, gp) * 2 * nt + nt + j] : 0.0;
+        rt += gx * (target.x - cm.x);
+        rt += gy * (target.y - cm.y);
+        if (tinterp) tinterp[(size_t)e * 2 * nt + (size_t)side * nt + j] = rt;
+      }
     }
   }
+  if (tslopes && nt > 0) memcpy(tslopes, tsl, sizeof(double) * (size_t)N * 2 * nt);
   free(gs);
   free(sl);
+  free(tsl);
+  free(tc);
   return st;
+}
+
+int ro_lgi(const rg_mesh_view* m, const double* cells, double g, const ro_lgi_params* lp,
+           double* slopes, double* interp, ro_error* err) {
+  return ro_lgi_tr(m, cells, NULL, g, lp, NULL, slopes, interp, NULL, NULL, err);
 }
 
 /* modular_flux_calculator.cpp:12-22 calc_parallel_normal and
  * simple_flux_calculator.cpp:27-31 remove_parallel_component */
 static v2 remove_parallel(v2 v, v2 p) { return vsub(v, vdiv(vscale(p, dot(v, p)), dot(p, p))); }
 
-/* modular_flux_calculator.cpp:39-71 */
-int ro_modular_flux(const rg_mesh_view* m, const double* cells, const double* ev, double g,
-                    const ro_lgi_params* lp, double* fluxes, ro_error* err) {
+/* modular_flux_calculator.cpp:39-71, tracer fluxes :24-35
+ * (convert_conserved_to_extensive: Mass * the first side's interpolated
+ * tracer when Mass > 0, else the second side's) */
+int ro_modular_flux_tr(const rg_mesh_view* m, const double* cells, const double* tr, const double* ev, double g,
+                       const ro_lgi_params* lp, const ro_tracers* t, double* fluxes, double* tfluxes,
+                       ro_error* err) {
   const int N = m->n_cells;
-  double* ip = (double*)malloc(sizeof(double) * 8 * (size_t)(m->n_faces > 0 ? m->n_faces : 1));
-  int st = ro_lgi(m, cells, g, lp, NULL, ip, err);
+  const int nt = t ? t->n : 0;
+  const size_t E = (size_t)(m->n_faces > 0 ? m->n_faces : 1);
+  double* ip = (double*)malloc(sizeof(double) * 8 * E);
+  double* tip = nt > 0 ? (double*)malloc(sizeof(double) * 2 * nt * E) : NULL;
+  int st = ro_lgi_tr(m, cells, tr, g, lp, t, NULL, ip, NULL, tip, err);
   for (int e = 0; e < m->n_faces && !st; ++e) {
     const int a = fc0(m, e), b = fc1(m, e);
     const v2 p = parallel(m, e);
@@ -586,10 +752,44 @@ int ro_modular_flux(const rg_mesh_view* m, const double* cells, const double* ev
     const prim pl = to_prim(g, get_cc(ip + 8 * e)), pr = to_prim(g, get_cc(ip + 8 * e + 4));
     cons c;
     st = rotate_solve_rotate_back(pl, pr, speed, n, p, &c, e, err);
-    if (!st) put_flux(fluxes + 4 * e, c);
+    if (st) break;
+    put_flux(fluxes + 4 * e, c);
+    for (int j = 0; j < nt; ++j)
+      tfluxes[(size_t)e * nt + j] = c.m * (c.m > 0 ? tip[(size_t)e * 2 * nt + j] : tip[(size_t)e * 2 * nt + nt + j]);
   }
   free(ip);
+  free(tip);
   return st;
+}
+
+int ro_modular_flux(const rg_mesh_view* m, const double* cells, const double* ev, double g,
+                    const ro_lgi_params* lp, double* fluxes, ro_error* err) {
+  return ro_modular_flux_tr(m, cells, NULL, ev, g, lp, NULL, fluxes, NULL, err);
+}
+
+/* simple_flux_calculator.cpp:193-213 calc_tracer_flux: Mass times the
+ * upwind point's tracer, 0 when the upwind point is a self-mirror ghost (or
+ * Mass is 0).  A non-mirror ghost (periodic) reads the tracer of its source
+ * cell, as the hydro state does. */
+int ro_simple_flux_tr(const rg_mesh_view* m, const double* cells, const double* tr, const double* ev, double g,
+                      const ro_tracers* t, double* fluxes, double* tfluxes, ro_error* err) {
+  const int st = ro_simple_flux(m, cells, ev, g, fluxes, err);
+  const int nt = t ? t->n : 0;
+  if (st || nt == 0) return st;
+  const int N = m->n_cells;
+  for (int e = 0; e < m->n_faces; ++e) {
+    const int a = fc0(m, e), b = fc1(m, e);
+    const double mass = fluxes[4 * e];
+    const int mirror = orig(m, a) == orig(m, b);
+    int up = -1;
+    if (mass > 0 && a >= 0 && (a < N || !mirror))
+      up = a;
+    else if (mass < 0 && b >= 0 && (b < N || !mirror))
+      up = b;
+    for (int j = 0; j < nt; ++j)
+      tfluxes[(size_t)e * nt + j] = up >= 0 ? mass * tr[(size_t)orig(m, up) * nt + j] : 0.0;
+  }
+  return 0;
 }
 
 /* simple_extensive_updater.cpp:11-35 */
@@ -656,6 +856,71 @@ int ro_init_extensives(const rg_mesh_view* m, const double* cells, double g, dou
   return 0;
 }
 
+/* simple_extensive_updater.cpp:11-35 for the extensive tracers: delta =
+ * flux * (dt*area), subtracted from the first cell, added to the second */
+void ro_extensive_update_tr(const rg_mesh_view* m, const double* tfluxes, int nt, double dt, double* tr_ext) {
+  const int N = m->n_cells;
+  for (int e = 0; e < m->n_faces; ++e) {
+    const double s = dt * edge_area(m, e);
+    const int a = fc0(m, e), b = fc1(m, e);
+    for (int j = 0; j < nt; ++j) {
+      const double d = tfluxes[(size_t)e * nt + j] * s;
+      if (a >= 0 && a < N) tr_ext[(size_t)a * nt + j] -= d;
+      if (b >= 0 && b < N) tr_ext[(size_t)b * nt + j] += d;
+    }
+  }
+}
+
+/* simple_cell_updater.cpp:61-83 update_single with the sequence
+ * {(HasSticker(frozen), SkipUpdate())} (:107-140: the old cell, tracers and
+ * stickers included), else :22-59 regular_update: tracers = extensive
+ * tracers / mass, the "Entropy" tracer = IdealGas::dp2s (ideal_gas.cpp:52-55,
+ * p*pow(d,-gamma)) with its extensive set to s*mass. */
+int ro_cell_update_tr(const rg_mesh_view* m, const double* ext, double* tr_ext, const double* old_cells,
+                      const double* old_tr, double g, const ro_tracers* t, double* cells_out, double* tr_out,
+                      ro_error* err) {
+  const int nt = t ? t->n : 0;
+  for (int i = 0; i < m->n_cells; ++i) {
+    if (t && t->frozen_mask && t->stickers && (t->stickers[i] & t->frozen_mask)) {
+      memcpy(cells_out + 4 * i, old_cells + 4 * i, 4 * sizeof(double));
+      for (int j = 0; j < nt; ++j) tr_out[(size_t)i * nt + j] = old_tr[(size_t)i * nt + j];
+      continue;
+    }
+    const double mass = ext[4 * i], en = ext[4 * i + 1], px = ext[4 * i + 2], py = ext[4 * i + 3];
+    const double d = mass / m->cd_volume[i];
+    if (d < 0) {
+      set_err(err, RG_ERR_NEGATIVE_DENSITY, 5, i, d);
+      return RG_ERR_NEGATIVE_DENSITY;
+    }
+    const double vx = px / mass, vy = py / mass;
+    const double energy = en / mass - 0.5 * (vx * vx + vy * vy);
+    for (int j = 0; j < nt; ++j) tr_out[(size_t)i * nt + j] = tr_ext[(size_t)i * nt + j] / mass;
+    if (energy < 0) {
+      set_err(err, RG_ERR_NEGATIVE_ENERGY, 5, i, energy);
+      return RG_ERR_NEGATIVE_ENERGY;
+    }
+    const double pres = (g - 1) * energy * d;
+    cells_out[4 * i] = d;
+    cells_out[4 * i + 1] = pres;
+    cells_out[4 * i + 2] = vx;
+    cells_out[4 * i + 3] = vy;
+    if (t && t->entropy >= 0 && t->entropy < nt) {
+      const double sv = pres * pow(d, -g);
+      tr_out[(size_t)i * nt + t->entropy] = sv;
+      tr_ext[(size_t)i * nt + t->entropy] = sv * mass;
+    }
+  }
+  return 0;
+}
+
+/* hdsim2d.cpp:56-63 init_extensives: tracer * mass */
+void ro_init_extensives_tr(const rg_mesh_view* m, const double* cells, const double* tr, int nt, double* tr_ext) {
+  for (int i = 0; i < m->n_cells; ++i) {
+    const double mass = m->cd_volume[i] * cells[4 * i];
+    for (int j = 0; j < nt; ++j) tr_ext[(size_t)i * nt + j] = tr[(size_t)i * nt + j] * mass;
+  }
+}
+
 /* simple_cfl.cpp:28-47 TimeStepCalculator, :58-71 operator(), lazy_list.hpp:185-191 lazy_min */
 int ro_cfl(const rg_mesh_view* m, const double* cells, const double* ev, double g, double cfl,
            double* dt, ro_error* err) {
@@ -688,6 +953,33 @@ int ro_step(const rg_mesh_view* m, double* cells, double* ext, const double* ev,
   if (!st) st = ro_extensive_update(m, fl, dt, ext, err);
   if (!st) st = ro_cell_update(m, ext, g, cells, err);
   free(fl);
+  if (dt_out) *dt_out = dt;
+  return st;
+}
+
+int ro_step_tr(const rg_mesh_view* m, double* cells, double* ext, double* tr, double* tr_ext, const double* ev,
+               double g, double cfl, int order, const ro_lgi_params* lp, const ro_tracers* t, double* dt_out,
+               ro_error* err) {
+  double dt;
+  int st = ro_cfl(m, cells, ev, g, cfl, &dt, err);
+  if (st) return st;
+  const int nt = t ? t->n : 0;
+  const size_t E = (size_t)(m->n_faces > 0 ? m->n_faces : 1), N = (size_t)m->n_cells;
+  double* fl = (double*)malloc(sizeof(double) * 4 * E);
+  double* tfl = (double*)malloc(sizeof(double) * E * (nt > 0 ? nt : 1));
+  double* old_cells = (double*)malloc(sizeof(double) * 4 * N);
+  double* old_tr = (double*)malloc(sizeof(double) * N * (nt > 0 ? nt : 1));
+  memcpy(old_cells, cells, sizeof(double) * 4 * N);
+  if (nt > 0) memcpy(old_tr, tr, sizeof(double) * N * nt);
+  st = order == 1 ? ro_simple_flux_tr(m, cells, tr, ev, g, t, fl, tfl, err)
+                  : ro_modular_flux_tr(m, cells, tr, ev, g, lp, t, fl, tfl, err);
+  if (!st) st = ro_extensive_update(m, fl, dt, ext, err);
+  if (!st) ro_extensive_update_tr(m, tfl, nt, dt, tr_ext);
+  if (!st) st = ro_cell_update_tr(m, ext, tr_ext, old_cells, old_tr, g, t, cells, tr, err);
+  free(fl);
+  free(tfl);
+  free(old_cells);
+  free(old_tr);
   if (dt_out) *dt_out = dt;
   return st;
 }

@@ -61,6 +61,39 @@ int ro_step(const rg_mesh_view* m, double* cells, double* ext, const double* ev,
 int ro_step_heun(const rg_mesh_view* m, double* cells, double* ext, const double* ev, double gamma,
                  double cfl, int order, const ro_lgi_params* lp, double* dt_out, ro_error* err);
 
+/* Tracers and stickers (rg_tracer_config's meaning).  tr / tr_ext arrays
+ * are n_cells*n cell-major; tslopes n_cells*2n (x then y); tinterp
+ * n_faces*2n (first side, second side); tfluxes n_faces*n. */
+typedef struct ro_tracers {
+  int32_t n;
+  uint32_t limited;        /* bit j: tracer j in calc_tracers */
+  int32_t entropy;         /* -1: none */
+  uint32_t skip_mask;      /* sticker bits of skip_key, 0: none */
+  uint32_t frozen_mask;    /* sticker bits of HasSticker + SkipUpdate, 0: none */
+  const uint32_t* stickers;  /* n_cells, NULL: none */
+} ro_tracers;
+
+int ro_lgi_tr(const rg_mesh_view* m, const double* cells, const double* tr, double gamma,
+              const ro_lgi_params* lp, const ro_tracers* t, double* slopes, double* interp,
+              double* tslopes, double* tinterp, ro_error* err);
+int ro_modular_flux_tr(const rg_mesh_view* m, const double* cells, const double* tr, const double* ev,
+                       double gamma, const ro_lgi_params* lp, const ro_tracers* t, double* fluxes,
+                       double* tfluxes, ro_error* err);
+int ro_simple_flux_tr(const rg_mesh_view* m, const double* cells, const double* tr, const double* ev,
+                      double gamma, const ro_tracers* t, double* fluxes, double* tfluxes, ro_error* err);
+void ro_extensive_update_tr(const rg_mesh_view* m, const double* tfluxes, int nt, double dt, double* tr_ext);
+/* old cells / tracers: the state before the update (SkipUpdate keeps it);
+ * tr_ext is updated in place for the entropy tracer */
+int ro_cell_update_tr(const rg_mesh_view* m, const double* ext, double* tr_ext, const double* old_cells,
+                      const double* old_tr, double gamma, const ro_tracers* t, double* cells_out,
+                      double* tr_out, ro_error* err);
+void ro_init_extensives_tr(const rg_mesh_view* m, const double* cells, const double* tr, int nt,
+                           double* tr_ext);
+/* hdsim::TimeAdvance on a fixed mesh with tracers and stickers */
+int ro_step_tr(const rg_mesh_view* m, double* cells, double* ext, double* tr, double* tr_ext,
+               const double* ev, double gamma, double cfl, int order, const ro_lgi_params* lp,
+               const ro_tracers* t, double* dt_out, ro_error* err);
+
 /* 3D first-order path on the packed 3D mesh.  Cells N*5 {density, pressure,
  * vx, vy, vz}; extensives and fluxes N*5 {mass, px, py, pz, energy}
  * (Conserved3D order).  face_velocity: n_faces*3 or NULL (faces at rest). */

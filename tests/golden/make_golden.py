@@ -48,6 +48,18 @@ CASES = {
     "periodic_heun_o2": ("periodic", 16, 16, 2, 10, "heun"),
 }
 
+# Tracers and stickers (ref_dump's <case>_tracers forms), written to
+# tracers/<name>.npz: tracers {"A" (in calc_tracers), "Entropy", "Z"},
+# stickers {"frozen" (HasSticker + SkipUpdate), "skip" (LinearGaussImproved's
+# skip_key)}; name: (ref_dump case, nx, ny, warm steps, run steps)
+CASES_TRACERS = {
+    "sod_tracers_o1": ("sod_tracers", 50, 10, 0, 20),
+    "sedov_eulerian_tracers_o2": ("sedov_eulerian_tracers", 24, 24, 2, 10),
+    "periodic_tracers_o2": ("periodic_tracers", 16, 16, 2, 10),
+    # RoundCells motion after 3 steps: one pass with moving faces
+    "sedov_tracers_o2": ("sedov_tracers", 24, 24, 3, 0),
+}
+
 # 3D first-order path (oracle/ref/ref_dump3d.cpp), written to 3d/<name>.npz:
 # name: (ref_dump3d case, nx, ny, nz, run steps)
 CASES3D = {
@@ -80,9 +92,13 @@ def main():
         out = os.path.join(HERE, "3d", name + ".npz")
         np.savez_compressed(out, **arrays)
         print(f"{name}: {len(arrays)} arrays, {os.path.getsize(out) / 1024:.0f} KiB", file=sys.stderr)
-    for name in [c for c in (a.cases or sorted(CASES)) if c in CASES]:
-        case, nx, ny, warm, run = CASES[name][:5]
-        scheme = CASES[name][5] if len(CASES[name]) > 5 else "first"
+    os.makedirs(os.path.join(HERE, "tracers"), exist_ok=True)
+    todo = [(c, CASES[c], HERE) for c in (a.cases or sorted(CASES)) if c in CASES]
+    todo += [(c, CASES_TRACERS[c], os.path.join(HERE, "tracers"))
+             for c in (a.cases or sorted(CASES_TRACERS)) if c in CASES_TRACERS]
+    for name, spec, outdir in todo:
+        case, nx, ny, warm, run = spec[:5]
+        scheme = spec[5] if len(spec) > 5 else "first"
         with tempfile.TemporaryDirectory(dir=scratch) as d:
             subprocess.check_call([exe, case, d, str(nx), str(ny), str(warm), str(run)] +
                                   (["heun"] if scheme == "heun" else []))
@@ -96,7 +112,7 @@ def main():
             arrays["run_mesh_unchanged"] = np.array(1)
         arrays["case_params"] = np.array([nx, ny, warm, run], dtype=np.int64)
         arrays["time_integrator"] = np.array(1 if scheme == "heun" else 0)
-        out = os.path.join(HERE, name + ".npz")
+        out = os.path.join(outdir, name + ".npz")
         np.savez_compressed(out, **arrays)
         print(f"{name}: {len(arrays)} arrays, {os.path.getsize(out) / 1024:.0f} KiB", file=sys.stderr)
 
