@@ -196,6 +196,15 @@ rg::StepArgs step_args(rg_handle* h) {
     a.dt_p = static_cast<double*>(h->dt_p.p);
     a.n_problems = h->n_problems;
   }
+  if (tracers_on(h)) {
+    a.stickers = static_cast<const uint32_t*>(h->stickers.p);
+    a.skip_mask = h->tcfg.skip_sticker >= 0 ? 1u << h->tcfg.skip_sticker : 0u;
+    a.frozen_mask = h->tcfg.frozen_sticker >= 0 ? 1u << h->tcfg.frozen_sticker : 0u;
+    if (h->tcfg.n_tracers > 0) {
+      a.mflux = static_cast<double*>(h->mflux.p);
+      if (h->cfg.order == 2) a.shock = static_cast<unsigned char*>(h->shock.p);
+    }
+  }
   return a;
 }
 
@@ -382,17 +391,22 @@ rg_status enqueue_step(rg_handle* h, int step, cudaEvent_t* ev = nullptr) {
   a.dt_from_device = 1;
   a.step = step;
   const bool fuse = fusable(h), have_dt = fuse && h->dt_next_ready;
+  const bool tr = h->tcfg.n_tracers > 0;
+  const rg::TracerArgs ta = tracer_args(h);
   if (ev) RG_CUDA(h, cudaEventRecord(ev[0], h->stream));
   if (!have_dt) RG_CUDA(h, rg::launch_cfl(a, h->stream, false));
   if (ev) RG_CUDA(h, cudaEventRecord(ev[1], h->stream));
   a.take_next_dt = have_dt;
   if (h->cfg.order == 2) RG_CUDA(h, rg::launch_slopes(a, h->stream));
   a.take_next_dt = 0;
+  if (tr && h->cfg.order == 2) RG_CUDA(h, rg::launch_tr_slopes(a, ta, h->stream));
   if (ev) RG_CUDA(h, cudaEventRecord(ev[2], h->stream));
   RG_CUDA(h, rg::launch_faces(a, h->stream, true));
+  if (tr) RG_CUDA(h, rg::launch_tr_faces(a, ta, h->stream, true));
   if (ev) RG_CUDA(h, cudaEventRecord(ev[3], h->stream));
   a.cfl_next = fuse;
   RG_CUDA(h, rg::launch_update(a, h->stream, false, true, true));
+  if (tr) RG_CUDA(h, rg::launch_tr_update(a, ta, h->stream, false, true, true));
   if (ev) RG_CUDA(h, cudaEventRecord(ev[4], h->stream));
   h->dt_next_ready = fuse;
   h->have_fluxes = false;  // the buffer now holds dt*area-scaled fluxes
@@ -492,6 +506,7 @@ rg_status rg_destroy(rg_handle* h) {
     if (s.last_use) cudaEventDestroy(s.last_use);
   }
   adjoint_release(h);
+  tracer_release(h);
   h->flag_buf.release();
   h->cells.release();
   h->ext.release();
@@ -707,6 +722,7 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t /*flags*/
   if (h->active >= 0) RG_CUDA(h, cudaEventRecord(h->slots[h->active].last_use, h->stream));
   h->active = next;
   s.valid = true;
+  if (tracers_on(h)) RG_TRY(tracer_buffers(h));
   h->last_upload_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   (void)ms;
   if (h->cfg.order == 2 && s.geom_error.status) {
@@ -830,6 +846,10 @@ rg_status rg_init_extensives(rg_handle* h) {
     RG_CUDA(h, rg::launch_cells_to64(static_cast<const float4*>(h->cells32.p), static_cast<double*>(h->cells.p),
                                      active_slot(h)->n, h->stream));
   RG_CUDA(h, rg::launch_init_extensives(a, h->stream));
+  if (h->tcfg.n_tracers > 0 && h->have_tr) {
+    RG_CUDA(h, rg::launch_tr_init(a, tracer_args(h), h->stream));
+    h->have_tr_ext = true;
+  }
   RG_CUDA(h, cudaStreamSynchronize(h->stream));
   h->have_ext = true;
   return RG_OK;
@@ -853,6 +873,7 @@ rg_status rg_cfl_dt(rg_handle* h, double* dt) {
 
 rg_status rg_flux(rg_handle* h, double dt, double* fluxes_out) {
   if (rg_status st = require(h, true, false, true, false)) return st;
+  if (rg_status st = require_tracers(h, false)) return st;
   h->last = rg_error{};
   if (rg_status st = mesh_error(h)) return st;
   RG_TRY(reset_status(h, h->d_status, h->stream));
@@ -867,11 +888,15 @@ rg_status rg_flux(rg_handle* h, double dt, double* fluxes_out) {
   } else {
     rg::StepArgs a = step_args(h);
     a.dt_host = dt;
+    const bool tr = h->tcfg.n_tracers > 0;
+    const rg::TracerArgs ta = tracer_args(h);
     if (h->cfg.order == 2) {
       RG_CUDA(h, rg::launch_ghost_fill(a, h->stream));
       RG_CUDA(h, rg::launch_slopes(a, h->stream));
+      if (tr) RG_CUDA(h, rg::launch_tr_slopes(a, ta, h->stream));
     }
     RG_CUDA(h, rg::launch_faces(a, h->stream, false));
+    if (tr) RG_CUDA(h, rg::launch_tr_faces(a, ta, h->stream, false));
   }
   if (rg_status st = collect(h, h->d_status, h->stream)) return st;
   h->have_fluxes = true;
@@ -888,6 +913,7 @@ rg_status rg_flux(rg_handle* h, double dt, double* fluxes_out) {
 
 rg_status rg_extensive_update(rg_handle* h, double dt) {
   if (rg_status st = require(h, false, true, false, true)) return st;
+  if (rg_status st = require_tracers(h, true)) return st;
   h->last = rg_error{};
   RG_TRY(reset_status(h, h->d_status, h->stream));
   if (h->mixed) {
@@ -898,12 +924,14 @@ rg_status rg_extensive_update(rg_handle* h, double dt) {
     rg::StepArgs a = step_args(h);
     a.dt_host = dt;
     RG_CUDA(h, rg::launch_update(a, h->stream, true, true, false));
+    if (h->tcfg.n_tracers > 0) RG_CUDA(h, rg::launch_tr_update(a, tracer_args(h), h->stream, true, true, false));
   }
   return collect(h, h->d_status, h->stream);
 }
 
 rg_status rg_cell_update(rg_handle* h) {
   if (rg_status st = require(h, false, true, false, false)) return st;
+  if (rg_status st = require_tracers(h, true)) return st;
   h->last = rg_error{};
   h->dt_next_ready = false;
   RG_TRY(reset_status(h, h->d_status, h->stream));
@@ -912,6 +940,7 @@ rg_status rg_cell_update(rg_handle* h) {
   } else {
     rg::StepArgs a = step_args(h);
     RG_CUDA(h, rg::launch_update(a, h->stream, false, false, true));
+    if (h->tcfg.n_tracers > 0) RG_CUDA(h, rg::launch_tr_update(a, tracer_args(h), h->stream, false, false, true));
   }
   rg_status st = collect(h, h->d_status, h->stream);
   if (st == RG_OK) h->have_cells = true;
@@ -920,6 +949,7 @@ rg_status rg_cell_update(rg_handle* h) {
 
 rg_status rg_step_async(rg_handle* h) {
   if (rg_status st = require(h, true, true, true, false)) return st;
+  if (rg_status st = require_tracers(h, true)) return st;
   if (rg_status st = mesh_error(h)) return st;
   if (h->step_seq == 0) RG_TRY(reset_status(h, h->d_status, h->stream));
   rg_status st = enqueue_step(h, h->step_seq);
@@ -938,6 +968,7 @@ rg_status rg_synchronize(rg_handle* h, double* dt_last) {
 
 rg_status rg_step(rg_handle* h, double* dt_out) {
   if (rg_status st = require(h, true, true, true, false)) return st;
+  if (rg_status st = require_tracers(h, true)) return st;
   if (rg_status st = mesh_error(h)) return st;
   h->last = rg_error{};
   RG_TRY(reset_status(h, h->d_status, h->stream));
@@ -949,6 +980,7 @@ rg_status rg_step(rg_handle* h, double* dt_out) {
 
 rg_status rg_step_timed(rg_handle* h, double* dt_out, float* kernel_ms) {
   if (rg_status st = require(h, true, true, true, false)) return st;
+  if (rg_status st = require_tracers(h, true)) return st;
   if (rg_status st = mesh_error(h)) return st;
   if (!kernel_ms) return RG_ERR_INVALID_ARGUMENT;
   h->last = rg_error{};
@@ -965,6 +997,7 @@ rg_status rg_step_timed(rg_handle* h, double* dt_out, float* kernel_ms) {
 
 rg_status rg_run(rg_handle* h, int32_t n_steps, double* dt_out) {
   if (rg_status st = require(h, true, true, true, false)) return st;
+  if (rg_status st = require_tracers(h, true)) return st;
   if (n_steps < 0) return RG_ERR_INVALID_ARGUMENT;
   if (rg_status st = mesh_error(h)) return st;
   h->last = rg_error{};
@@ -993,7 +1026,7 @@ rg_status rg_set_problems(rg_handle* h, int32_t P, const int32_t* offsets, const
     h->n_problems = 0;
     return RG_OK;
   }
-  if (P < 0 || !offsets || !gamma || h->heun) return invalid(h, -1, P);
+  if (P < 0 || !offsets || !gamma || h->heun || tracers_on(h)) return invalid(h, -1, P);
   if (offsets[0] != 0 || offsets[P] != s->n) return invalid(h, -2, offsets[P]);
   for (int p = 0; p < P; ++p) {
     if (offsets[p + 1] <= offsets[p]) return invalid(h, p, offsets[p + 1]);
@@ -1048,6 +1081,7 @@ rg_status rg_get_problem_times(rg_handle* h, double* time_out, double* dt_out) {
 
 rg_status rg_run_graph(rg_handle* h, int32_t n_steps) {
   if (rg_status st = require(h, true, true, true, false)) return st;
+  if (rg_status st = require_tracers(h, true)) return st;
   if (n_steps < 0) return RG_ERR_INVALID_ARGUMENT;
   if (rg_status st = mesh_error(h)) return st;
   h->last = rg_error{};

@@ -17,35 +17,13 @@
 // Geometry-only terms are computed once per mesh upload (k_geom_*).
 #include <math.h>
 
+#include "rg_fp64.cuh"
 #include "rg_hllc.cuh"
-#include "rg_internal.cuh"
 
 namespace rg {
 namespace {
 
 constexpr int kBlock = 256;
-
-struct Cell { double d, p, vx, vy; };
-
-__device__ __forceinline__ Cell load_cell(const double* cells, int i) {
-  const double2 a = reinterpret_cast<const double2*>(cells)[2 * i];
-  const double2 b = reinterpret_cast<const double2*>(cells)[2 * i + 1];
-  return Cell{a.x, a.y, b.x, b.y};
-}
-__device__ __forceinline__ void store4(double* out, int i, double a, double b, double c, double d) {
-  reinterpret_cast<double2*>(out)[2 * i] = make_double2(a, b);
-  reinterpret_cast<double2*>(out)[2 * i + 1] = make_double2(c, d);
-}
-__device__ __forceinline__ int orig_of(const MeshDev& m, int p) {
-  return p < m.n ? p : m.ghost_source[p - m.n];
-}
-// computational_cell_2d.cpp:59-68 ComputationalCellAddMult
-__device__ __forceinline__ void addmult(Cell& r, const Cell& o, double s) {
-  r.d += o.d * s;
-  r.p += o.p * s;
-  r.vx += o.vx * s;
-  r.vy += o.vy * s;
-}
 
 // ---------------------------------------------------------------- geometry
 
@@ -221,40 +199,6 @@ __global__ void __launch_bounds__(kBlock) k_validate(MeshDev m, DevStatus* st) {
 
 // ---------------------------------------------------------------- per step
 
-// Per-problem parameters of a batch (kBatch) or the handle's single values.
-template <bool kBatch>
-__device__ __forceinline__ double gamma_at(const StepArgs& a, int point) {
-  return kBatch ? a.gamma_p[a.cell_problem[point]] : a.gamma;
-}
-template <bool kBatch>
-__device__ __forceinline__ double scaled_dt(const StepArgs& a, int point) {
-  if (kBatch) return a.cfl * __longlong_as_double(static_cast<long long>(a.dtmin_p[a.cell_problem[point]]));
-  return a.dt_from_device ? a.status->dt : a.dt_host;
-}
-
-// Ghost state (LinearGaussImproved.cpp:543-550 new_cells[ghost]):
-// RigidWallGenerator.cpp:17-37 reflects the real neighbour's velocity,
-// PeriodicGhostGenerator.cpp:3-17 copies the source cell.
-__device__ __forceinline__ Cell ghost_state(const StepArgs& a, int g) {
-  Cell c = load_cell(a.cells, a.geom.ghost_real[g]);
-  if (a.ghost_kind != RG_GHOST_PERIODIC) {
-    const double2 u = a.geom.ghost_unit[g];
-    const double s = 2 * (c.vx * u.x + c.vy * u.y);
-    c.vx -= u.x * s;
-    c.vy -= u.y * s;
-  }
-  return c;
-}
-__device__ __forceinline__ void fill_ghost(const StepArgs& a, int g) {
-  const Cell c = ghost_state(a, g);
-  store4(a.cells, a.mesh.n + g, c.d, c.p, c.vx, c.vy);
-}
-// State of point p: a real cell's record, or a ghost's state formed from the
-// current state of its cell (the per-step kernels read no ghost records)
-__device__ __forceinline__ Cell point_state(const StepArgs& a, int p) {
-  return p < a.mesh.n ? load_cell(a.cells, p) : ghost_state(a, p - a.mesh.n);
-}
-
 // simple_cfl.cpp:28-47 (per cell) and :58-71 + lazy_list.hpp:185-191 (min, times cfl).
 template <bool kBatch>
 __global__ void __launch_bounds__(kMaxBlock) k_cfl(StepArgs a, int fill_ghosts) {
@@ -315,85 +259,6 @@ __global__ void __launch_bounds__(kMaxBlock) k_cfl(StepArgs a, int fill_ghosts) 
 __global__ void __launch_bounds__(kBlock) k_ghost_fill(StepArgs a) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g < a.mesh.g) fill_ghost(a, g);
-}
-
-__device__ __forceinline__ double step_dt(const StepArgs& a) {
-  return a.dt_from_device ? a.status->dt : a.dt_host;
-}
-
-// FP32 screening of FP64 quotients.  GB300 issues 64 FP32 operations per FP64
-// one, so a decision that only needs to know on which side of a threshold a
-// correctly rounded FP64 quotient lies is taken from an FP32 estimate when
-// the estimate is clear of the threshold by more than its error, and from the
-// exact FP64 division otherwise.  For |a|,|b| in [2^-120, 2^120] the
-// estimate float(a)/float(b) is within 4 * 2^-24 < 2.5e-7 (relative) of
-// a/b; the margins below are 1e-6, with float(t) itself within 6e-8 of t.
-__device__ __forceinline__ bool fp32_safe(double a) {
-  const double m = fabs(a);
-  return m >= 1e-36 && m <= 1e36;
-}
-
-// psi_f = float(psi) is a usable screen when psi is 0 or a normal float.
-__device__ __forceinline__ bool psi_screenable(double psi, float psi_f) {
-  return psi_f >= 1e-30f || psi == 0.0;
-}
-
-// smin(psi, num/den) for num/den >= 0 (or NaN, which smin ignores), psi >= 0:
-// skips the division when the quotient is provably >= psi.
-__device__ __forceinline__ void min_quotient(double num, double den, double& psi, float& psi_f) {
-  if (fp32_safe(num) && fp32_safe(den) && psi_screenable(psi, psi_f)) {
-    const float qf = static_cast<float>(num) / static_cast<float>(den);
-    if (qf >= psi_f * 1.000001f) return;
-  }
-  const double q = num / den;
-  if (q < psi) {
-    psi = q;
-    psi_f = static_cast<float>(q);
-  }
-}
-
-// one component of the ordinary limiter, LinearGaussImproved.cpp:232-267.
-// thr = 0.05*max(|maxd|,|mind|) (per cell); maxd >= 0 >= mind, so both
-// candidate quotients are >= 0.
-__device__ __forceinline__ void limit_comp(double dphi, double cv, double cellv, double thr, double maxd,
-                                           double mind, bool use_abs, double& psi, float& psi_f) {
-  if (fabs(dphi) > thr || cv * cellv < 0) {
-    const double t1 = use_abs ? fabs(1e-9 * cellv) : 1e-9 * cellv;
-    const double t2 = use_abs ? -fabs(1e-9 * cellv) : -1e-9 * cellv;
-    if (dphi > t1)
-      min_quotient(maxd, dphi, psi, psi_f);
-    else if (dphi < t2)
-      min_quotient(mind, dphi, psi, psi_f);
-  }
-}
-
-// one component of the shocked limiter, LinearGaussImproved.cpp:343-366
-// (threshold 1e-9*q without abs for every component, as the reference has
-// it): psi = smin(psi, smax(theta*(nb-cell)/dphi, 0)).
-__device__ __forceinline__ void shocked_comp(double dphi, double cv, double cellv, double thr, double nbv,
-                                             double theta, double& psi, float& psi_f) {
-  if (fabs(dphi) > thr || cv * cellv < 0) {
-    if (fabs(dphi) > 1e-9 * cellv) {
-      const double num = theta * (nbv - cellv);
-      if (num != 0 && !isnan(num) && !isnan(dphi) && (num < 0) != (dphi < 0)) {
-        // negative quotient: smax(., 0) gives 0
-        if (0.0 < psi) {
-          psi = 0.0;
-          psi_f = 0.0f;
-        }
-        return;
-      }
-      if (num != 0 && fp32_safe(num) && fp32_safe(dphi) && psi_screenable(psi, psi_f)) {
-        const float qf = static_cast<float>(num) / static_cast<float>(dphi);
-        if (qf >= psi_f * 1.000001f) return;
-      }
-      const double x = smax(num / dphi, 0.0);
-      if (x < psi) {
-        psi = x;
-        psi_f = static_cast<float>(x);
-      }
-    }
-  }
 }
 
 // LinearGaussImproved.cpp:425-494 calc_slope for one cell (serial build).
@@ -486,10 +351,12 @@ __device__ __forceinline__ void k_slopes_item(const StepArgs& a, int i) {
         shock = num / den < a.delta_p;
       }
     }
+    if (a.shock) a.shock[i] = shock ? 1 : 0;
     Cell cmax = cell, cmin = cell;
     for (int k = 0; k < nn; ++k) {
       const uint32_t w = a.geom.nbr[b + k];
       if (!shock && (w & kNbrMirror)) continue;  // :194-195 skips self-mirror neighbours
+      if (skipped(a, static_cast<int>(w & kNbrIdMask))) continue;  // :192-193, :314-315 skip_key
       const Cell nb = point_state(a, static_cast<int>(w & kNbrIdMask));
       cmax.d = smax(cmax.d, nb.d);
       cmax.p = smax(cmax.p, nb.p);
@@ -509,6 +376,7 @@ __device__ __forceinline__ void k_slopes_item(const StepArgs& a, int i) {
     float pf0 = 1, pf1 = 1, pf2 = 1, pf3 = 1;
     for (int k = 0; k < nn; ++k) {
       const uint32_t w = a.geom.nbr[b + k];
+      if (shock && skipped(a, static_cast<int>(w & kNbrIdMask))) continue;  // :339-340
       const int e = m.cell_faces[b + k];
       const double2 dm = (w & kNbrFirst) ? a.geom.dm0[e] : a.geom.dm1[e];
       Cell cv = cell;
@@ -628,6 +496,7 @@ __device__ __forceinline__ void k_faces_lgi_item(const StepArgs& a, int e) {
   const double g = gamma_at<kBatch>(a, real_side);
   Cons c;
   if (!solve_face(to_prim(g, side[0]), to_prim(g, side[1]), speed, n, na, p, pa, c, a, e)) return;
+  if (a.mflux) a.mflux[e] = c.m;
   write_flux<kBatch>(a, e, real_side, c, kScaled, pa);
 }
 
@@ -676,6 +545,7 @@ __device__ __forceinline__ void k_faces_pcm_item(const StepArgs& a, int e) {
   const double velocity = (w.x == 0.0 && w.y == 0.0) ? 0.0 : (n.x * w.x + n.y * w.y) / na;
   Cons c;
   if (!solve_face(l, r, velocity, n, na, p, pa, c, a, e)) return;
+  if (a.mflux) a.mflux[e] = c.m;
   write_flux<kBatch>(a, e, real_side, c, kScaled, pa);
 }
 
@@ -686,6 +556,36 @@ __global__ void __launch_bounds__(kMaxBlock) k_faces_pcm(StepArgs a) {
 }
 
 // ---------------------------------------------------------------- cells
+
+// The next step's SimpleCFL bound of cell i with state (d, pres, vx, vy), as
+// k_cfl computes it, as the bit pattern of 1/bound.
+template <bool kBatch>
+__device__ __forceinline__ unsigned long long cfl_bound_bits(const StepArgs& a, int i, double d, double pres,
+                                                             double vx, double vy) {
+  const MeshDev& m = a.mesh;
+  const double cs = sqrt(gamma_at<kBatch>(a, i) * pres / d);
+  double q = 0;
+  bool any = false;
+  if (a.ev_zero) {
+    const double qq = vx * vx + vy * vy;
+    if (m.cell_off[i + 1] > m.cell_off[i] && !isnan(qq)) {
+      q = fmax(q, qq);
+      any = true;
+    }
+  } else {
+    for (int k = m.cell_off[i]; k < m.cell_off[i + 1]; ++k) {
+      const double2 w = reinterpret_cast<const double2*>(a.ev)[m.cell_faces[k]];
+      const double dx = vx - w.x, dy = vy - w.y;
+      const double qq = dx * dx + dy * dy;
+      if (!isnan(qq)) {
+        q = fmax(q, qq);
+        any = true;
+      }
+    }
+  }
+  const double res = any ? fmax(0.0, (cs + sqrt(q)) / a.geom.width[i]) : 0.0;
+  return static_cast<unsigned long long>(__double_as_longlong(1.0 / res));
+}
 
 // SimpleExtensiveUpdater (simple_extensive_updater.cpp:11-35) as a gather:
 // each cell applies its faces' contributions in ascending face order, which
@@ -739,6 +639,13 @@ __device__ __forceinline__ unsigned long long k_update_item(const StepArgs& a, i
     out2[2 * i + 1] = make_double2(px, py);
   }
   if (do_cells) {
+    if (a.frozen_mask && (a.stickers[i] & a.frozen_mask)) {
+      // simple_cell_updater.cpp:61-83 with (HasSticker, SkipUpdate): the old
+      // cell stays (its extensives above still took the fluxes)
+      if (!a.cfl_next) return kInfBits;
+      const Cell c = load_cell(a.cells, i);
+      return cfl_bound_bits<kBatch>(a, i, c.d, c.p, c.vx, c.vy);
+    }
     const double d = mass / m.cd_volume[i];
     if (d < 0) {
       record_error(a.status, a.step, RG_ERR_NEGATIVE_DENSITY, 5, i, d);
@@ -752,32 +659,8 @@ __device__ __forceinline__ unsigned long long k_update_item(const StepArgs& a, i
     }
     const double pres = (gamma_at<kBatch>(a, i) - 1) * energy * d;
     store4(a.cells_out ? a.cells_out : a.cells, i, d, pres, vx, vy);
-    if (a.cfl_next) {
-      // the next step's SimpleCFL bound of this cell, as k_cfl computes it
-      // from the record just stored
-      const double cs = sqrt(gamma_at<kBatch>(a, i) * pres / d);
-      double q = 0;
-      bool any = false;
-      if (a.ev_zero) {
-        const double qq = vx * vx + vy * vy;
-        if (m.cell_off[i + 1] > m.cell_off[i] && !isnan(qq)) {
-          q = fmax(q, qq);
-          any = true;
-        }
-      } else {
-        for (int k = m.cell_off[i]; k < m.cell_off[i + 1]; ++k) {
-          const double2 w = reinterpret_cast<const double2*>(a.ev)[m.cell_faces[k]];
-          const double dx = vx - w.x, dy = vy - w.y;
-          const double qq = dx * dx + dy * dy;
-          if (!isnan(qq)) {
-            q = fmax(q, qq);
-            any = true;
-          }
-        }
-      }
-      const double res = any ? fmax(0.0, (cs + sqrt(q)) / a.geom.width[i]) : 0.0;
-      return static_cast<unsigned long long>(__double_as_longlong(1.0 / res));
-    }
+    // the next step's SimpleCFL bound of this cell, from the record just stored
+    if (a.cfl_next) return cfl_bound_bits<kBatch>(a, i, d, pres, vx, vy);
   }
   return kInfBits;
 }

@@ -1,0 +1,161 @@
+// rg_fp64.cuh -- device helpers shared by the plain-FP64 kernels
+// (rg_fp64.cu) and the tracer kernels (rg_tracers.cu): cell records, ghost
+// and point states, the FP32 screening of FP64 limiter quotients and one
+// component of each LinearGaussImproved limiter.  Both units are compiled
+// with --fmad=false.
+#pragma once
+#include <math.h>
+
+#include "rg_internal.cuh"
+
+namespace rg {
+namespace {
+
+struct Cell { double d, p, vx, vy; };
+
+__device__ __forceinline__ Cell load_cell(const double* cells, int i) {
+  const double2 a = reinterpret_cast<const double2*>(cells)[2 * i];
+  const double2 b = reinterpret_cast<const double2*>(cells)[2 * i + 1];
+  return Cell{a.x, a.y, b.x, b.y};
+}
+__device__ __forceinline__ void store4(double* out, int i, double a, double b, double c, double d) {
+  reinterpret_cast<double2*>(out)[2 * i] = make_double2(a, b);
+  reinterpret_cast<double2*>(out)[2 * i + 1] = make_double2(c, d);
+}
+__device__ __forceinline__ int orig_of(const MeshDev& m, int p) {
+  return p < m.n ? p : m.ghost_source[p - m.n];
+}
+// computational_cell_2d.cpp:59-68 ComputationalCellAddMult
+__device__ __forceinline__ void addmult(Cell& r, const Cell& o, double s) {
+  r.d += o.d * s;
+  r.p += o.p * s;
+  r.vx += o.vx * s;
+  r.vy += o.vy * s;
+}
+
+// Per-problem parameters of a batch (kBatch) or the handle's single values.
+template <bool kBatch>
+__device__ __forceinline__ double gamma_at(const StepArgs& a, int point) {
+  return kBatch ? a.gamma_p[a.cell_problem[point]] : a.gamma;
+}
+template <bool kBatch>
+__device__ __forceinline__ double scaled_dt(const StepArgs& a, int point) {
+  if (kBatch) return a.cfl * __longlong_as_double(static_cast<long long>(a.dtmin_p[a.cell_problem[point]]));
+  return a.dt_from_device ? a.status->dt : a.dt_host;
+}
+
+// Ghost state (LinearGaussImproved.cpp:543-550 new_cells[ghost]):
+// RigidWallGenerator.cpp:17-37 reflects the real neighbour's velocity,
+// PeriodicGhostGenerator.cpp:3-17 copies the source cell.
+__device__ __forceinline__ Cell ghost_state(const StepArgs& a, int g) {
+  Cell c = load_cell(a.cells, a.geom.ghost_real[g]);
+  if (a.ghost_kind != RG_GHOST_PERIODIC) {
+    const double2 u = a.geom.ghost_unit[g];
+    const double s = 2 * (c.vx * u.x + c.vy * u.y);
+    c.vx -= u.x * s;
+    c.vy -= u.y * s;
+  }
+  return c;
+}
+__device__ __forceinline__ void fill_ghost(const StepArgs& a, int g) {
+  const Cell c = ghost_state(a, g);
+  store4(a.cells, a.mesh.n + g, c.d, c.p, c.vx, c.vy);
+}
+// State of point p: a real cell's record, or a ghost's state formed from the
+// current state of its cell (the per-step kernels read no ghost records)
+__device__ __forceinline__ Cell point_state(const StepArgs& a, int p) {
+  return p < a.mesh.n ? load_cell(a.cells, p) : ghost_state(a, p - a.mesh.n);
+}
+
+// The cell whose tracers and stickers point p carries: p itself, or the
+// cell a ghost copies (RigidWallGenerator.cpp:17-37 and
+// PeriodicGhostGenerator.cpp:3-17 copy the whole ComputationalCell).
+__device__ __forceinline__ int copied_cell(const StepArgs& a, int p) {
+  return p < a.mesh.n ? p : a.geom.ghost_real[p - a.mesh.n];
+}
+// point p carries LinearGaussImproved's skip_key sticker (:192-193, :314-315, :339-340)
+__device__ __forceinline__ bool skipped(const StepArgs& a, int p) {
+  return a.skip_mask != 0 && (a.stickers[copied_cell(a, p)] & a.skip_mask) != 0;
+}
+
+__device__ __forceinline__ double step_dt(const StepArgs& a) {
+  return a.dt_from_device ? a.status->dt : a.dt_host;
+}
+
+// FP32 screening of FP64 quotients.  GB300 issues 64 FP32 operations per FP64
+// one, so a decision that only needs to know on which side of a threshold a
+// correctly rounded FP64 quotient lies is taken from an FP32 estimate when
+// the estimate is clear of the threshold by more than its error, and from the
+// exact FP64 division otherwise.  For |a|,|b| in [2^-120, 2^120] the
+// estimate float(a)/float(b) is within 4 * 2^-24 < 2.5e-7 (relative) of
+// a/b; the margins below are 1e-6, with float(t) itself within 6e-8 of t.
+__device__ __forceinline__ bool fp32_safe(double a) {
+  const double m = fabs(a);
+  return m >= 1e-36 && m <= 1e36;
+}
+
+// psi_f = float(psi) is a usable screen when psi is 0 or a normal float.
+__device__ __forceinline__ bool psi_screenable(double psi, float psi_f) {
+  return psi_f >= 1e-30f || psi == 0.0;
+}
+
+// smin(psi, num/den) for num/den >= 0 (or NaN, which smin ignores), psi >= 0:
+// skips the division when the quotient is provably >= psi.
+__device__ __forceinline__ void min_quotient(double num, double den, double& psi, float& psi_f) {
+  if (fp32_safe(num) && fp32_safe(den) && psi_screenable(psi, psi_f)) {
+    const float qf = static_cast<float>(num) / static_cast<float>(den);
+    if (qf >= psi_f * 1.000001f) return;
+  }
+  const double q = num / den;
+  if (q < psi) {
+    psi = q;
+    psi_f = static_cast<float>(q);
+  }
+}
+
+// one component of the ordinary limiter, LinearGaussImproved.cpp:232-267.
+// thr = 0.05*max(|maxd|,|mind|) (per cell); maxd >= 0 >= mind, so both
+// candidate quotients are >= 0.
+__device__ __forceinline__ void limit_comp(double dphi, double cv, double cellv, double thr, double maxd,
+                                           double mind, bool use_abs, double& psi, float& psi_f) {
+  if (fabs(dphi) > thr || cv * cellv < 0) {
+    const double t1 = use_abs ? fabs(1e-9 * cellv) : 1e-9 * cellv;
+    const double t2 = use_abs ? -fabs(1e-9 * cellv) : -1e-9 * cellv;
+    if (dphi > t1)
+      min_quotient(maxd, dphi, psi, psi_f);
+    else if (dphi < t2)
+      min_quotient(mind, dphi, psi, psi_f);
+  }
+}
+
+// one component of the shocked limiter, LinearGaussImproved.cpp:343-366
+// (threshold 1e-9*q without abs for every hydro component, as the reference
+// has it; |1e-9*q| for tracers, :377): psi = smin(psi, smax(theta*(nb-cell)/dphi, 0)).
+__device__ __forceinline__ void shocked_comp(double dphi, double cv, double cellv, double thr, double nbv,
+                                             double theta, double& psi, float& psi_f, bool abs_thr = false) {
+  if (fabs(dphi) > thr || cv * cellv < 0) {
+    if (fabs(dphi) > (abs_thr ? fabs(1e-9 * cellv) : 1e-9 * cellv)) {
+      const double num = theta * (nbv - cellv);
+      if (num != 0 && !isnan(num) && !isnan(dphi) && (num < 0) != (dphi < 0)) {
+        // negative quotient: smax(., 0) gives 0
+        if (0.0 < psi) {
+          psi = 0.0;
+          psi_f = 0.0f;
+        }
+        return;
+      }
+      if (num != 0 && fp32_safe(num) && fp32_safe(dphi) && psi_screenable(psi, psi_f)) {
+        const float qf = static_cast<float>(num) / static_cast<float>(dphi);
+        if (qf >= psi_f * 1.000001f) return;
+      }
+      const double x = smax(num / dphi, 0.0);
+      if (x < psi) {
+        psi = x;
+        psi_f = static_cast<float>(x);
+      }
+    }
+  }
+}
+
+}  // namespace
+}  // namespace rg

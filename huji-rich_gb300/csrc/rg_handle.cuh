@@ -179,6 +179,13 @@ struct rg_handle {
   rgh::DevBuf flag_buf;
   // differentiation: checkpoints, recomputation buffers, reverse adjacency
   rg_adjoint_state* adj = nullptr;
+  // tracers and stickers (rg_set_tracer_config): cell tracers, extensive
+  // tracers, tracer slopes and fluxes, each face's unscaled mass flux, each
+  // cell's shock decision and sticker mask; sized for tr_n cells, tr_e faces
+  rg_tracer_config tcfg{0, 0u, -1, -1, -1};
+  rgh::DevBuf tr, tr_ext, tr_slopes, tr_flux, mflux, shock, stickers;
+  bool have_tr = false, have_tr_ext = false;
+  int tr_n = -1, tr_e = -1;
 };
 
 
@@ -196,6 +203,15 @@ rg_status require(rg_handle* h, bool cells, bool ext, bool ev, bool fluxes);
 rg_status mesh_error(rg_handle* h);
 // frees the differentiation buffers (rg_destroy; a new mesh drops them too)
 void adjoint_release(rg_handle* h);
+// tracers or stickers configured (rg_tracer_api.cu)
+bool tracers_on(const rg_handle* h);
+// sizes the tracer buffers for the active mesh; a new cell count clears the
+// tracer state and the stickers
+rg_status tracer_buffers(rg_handle* h);
+rg::TracerArgs tracer_args(rg_handle* h);
+// NOT_READY unless the tracer state a step needs is set
+rg_status require_tracers(rg_handle* h, bool ext);
+void tracer_release(rg_handle* h);
 
 }  // namespace rgh
 

@@ -227,7 +227,27 @@ struct StepArgs {
   double* time_p;                 // per problem simulated time
   double* dt_p;                   // per problem last dt
   int n_problems;
+  // stickers (ComputationalCell::stickers as one bit mask per cell)
+  const uint32_t* stickers;       // n
+  uint32_t skip_mask;             // LinearGaussImproved's skip_key bit (0: none)
+  uint32_t frozen_mask;           // HasSticker + SkipUpdate bit (0: none)
+  // tracer passes: the faces kernel keeps each face's unscaled mass flux and
+  // the slopes kernel each cell's shock decision
+  double* mflux;                  // e, or nullptr
+  unsigned char* shock;           // n, or nullptr
   StepShapes shapes;  // launch shapes (host side; the kernels ignore it)
+};
+
+// Tracers (ComputationalCell::tracers, Extensive::tracers), cell-major.
+constexpr int kMaxTracers = RG_MAX_TRACERS;
+struct TracerArgs {
+  int nt;
+  uint32_t limited;       // bit j: tracer j in LinearGaussImproved's calc_tracers
+  int entropy;            // the "Entropy" tracer, -1: none
+  double* tr;             // n*nt
+  double* tr_ext;         // n*nt
+  double* tr_slopes;      // n*2*nt (x derivatives, then y)
+  double* tr_flux;        // e*nt (unscaled or dt*area scaled, as the hydro fluxes)
 };
 
 #ifdef __CUDACC__
@@ -279,5 +299,11 @@ cudaError_t launch_slopes(const StepArgs& a, cudaStream_t s);
 cudaError_t launch_faces(const StepArgs& a, cudaStream_t s, bool scaled);
 cudaError_t launch_update(const StepArgs& a, cudaStream_t s, bool from_unscaled, bool extensive, bool cells);
 cudaError_t launch_init_extensives(const StepArgs& a, cudaStream_t s);
+// Tracer passes (rg_tracers.cu), each after its hydro pass
+cudaError_t launch_tr_slopes(const StepArgs& a, const TracerArgs& t, cudaStream_t s);
+cudaError_t launch_tr_faces(const StepArgs& a, const TracerArgs& t, cudaStream_t s, bool scaled);
+cudaError_t launch_tr_update(const StepArgs& a, const TracerArgs& t, cudaStream_t s, bool from_unscaled,
+                             bool extensive, bool cells);
+cudaError_t launch_tr_init(const StepArgs& a, const TracerArgs& t, cudaStream_t s);
 
 }  // namespace rg

@@ -32,6 +32,8 @@ UNITS = {
     "rg_3d.cu": ["--fmad=false"],
     "rg_3d_api.cu": [],
     "rg_3d_mixed.cu": [],
+    "rg_tracers.cu": ["--fmad=false"],
+    "rg_tracer_api.cu": [],
 }
 
 

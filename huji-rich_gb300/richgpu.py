@@ -28,7 +28,9 @@ EXPORTS = ("rg_default_config", "rg_create", "rg_destroy", "rg_status_string", "
            "rg3_create", "rg3_destroy", "rg3_last_error", "rg3_upload_mesh", "rg3_set_cells", "rg3_get_cells",
            "rg3_set_extensives", "rg3_get_extensives", "rg3_set_face_velocities", "rg3_init_extensives",
            "rg3_cfl_dt", "rg3_flux", "rg3_extensive_update", "rg3_cell_update", "rg3_step", "rg3_run",
-           "rg3_step_timed")
+           "rg3_step_timed", "rg_set_tracer_config", "rg_set_tracers", "rg_get_tracers",
+           "rg_set_extensive_tracers", "rg_get_extensive_tracers", "rg_set_stickers",
+           "rg_get_tracer_fluxes", "rg_get_tracer_slopes")
 
 KERNELS = ("cfl", "slopes", "faces", "update")
 
@@ -36,6 +38,11 @@ KERNELS = ("cfl", "slopes", "faces", "update")
 class RgLaunchShapes(C.Structure):
     _fields_ = [("block", C.c_int32 * 4), ("max_blocks", C.c_int32 * 4), ("variant", C.c_int32 * 4),
                 ("ms", C.c_float * 4)]
+
+
+class RgTracerConfig(C.Structure):
+    _fields_ = [("n_tracers", C.c_int32), ("limited_mask", C.c_uint32), ("entropy_tracer", C.c_int32),
+                ("skip_sticker", C.c_int32), ("frozen_sticker", C.c_int32)]
 
 
 class RgDeviceView(C.Structure):
@@ -111,6 +118,11 @@ def load(path=LIB_PATH):
     lib.rg3_cell_update.argtypes = [vp]
     lib.rg3_run.argtypes = [vp, C.c_int32, dp]
     lib.rg3_step_timed.argtypes = [vp, dp, C.POINTER(C.c_float)]
+    lib.rg_set_tracer_config.argtypes = [vp, C.POINTER(RgTracerConfig)]
+    for f in ("rg_set_tracers", "rg_get_tracers", "rg_set_extensive_tracers", "rg_get_extensive_tracers",
+              "rg_get_tracer_fluxes", "rg_get_tracer_slopes"):
+        getattr(lib, f).argtypes = [vp, dp]
+    lib.rg_set_stickers.argtypes = [vp, C.POINTER(C.c_uint32)]
     lib.rg_set_launch_shapes.argtypes = [vp, C.POINTER(RgLaunchShapes)]
     lib.rg_get_launch_shapes.argtypes = [vp, C.POINTER(RgLaunchShapes)]
     _lib = lib
@@ -247,6 +259,54 @@ class Handle:
         ms = (C.c_float * 4)()
         self._check(self.lib.rg_step_timed(self.h, C.byref(dt), ms))
         return dt.value, list(ms)
+
+    # tracers and stickers --------------------------------------------------
+    def set_tracer_config(self, n_tracers=0, limited=(), entropy=-1, skip_sticker=-1, frozen_sticker=-1):
+        """Tracer count, the tracers in LinearGaussImproved's calc_tracers
+        (indices), the "Entropy" tracer, the skip_key sticker bit and the
+        HasSticker + SkipUpdate sticker bit (-1: none)."""
+        mask = 0
+        for j in limited:
+            mask |= 1 << j
+        c = RgTracerConfig(n_tracers, mask, entropy, skip_sticker, frozen_sticker)
+        self._check(self.lib.rg_set_tracer_config(self.h, C.byref(c)))
+        self.n_tracers = n_tracers
+
+    def _tr_io(self, fn, arr, cols):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        assert a.size == cols * self.mesh.n_cells
+        self._check(fn(self.h, dptr(a)))
+
+    def set_tracers(self, tr):
+        self._tr_io(self.lib.rg_set_tracers, tr, self.n_tracers)
+
+    def get_tracers(self):
+        out = np.empty((self.mesh.n_cells, self.n_tracers))
+        self._check(self.lib.rg_get_tracers(self.h, dptr(out)))
+        return out
+
+    def set_extensive_tracers(self, tr):
+        self._tr_io(self.lib.rg_set_extensive_tracers, tr, self.n_tracers)
+
+    def get_extensive_tracers(self):
+        out = np.empty((self.mesh.n_cells, self.n_tracers))
+        self._check(self.lib.rg_get_extensive_tracers(self.h, dptr(out)))
+        return out
+
+    def set_stickers(self, stickers):
+        a = np.ascontiguousarray(stickers, dtype=np.uint32)
+        assert a.size == self.mesh.n_cells
+        self._check(self.lib.rg_set_stickers(self.h, a.ctypes.data_as(C.POINTER(C.c_uint32))))
+
+    def tracer_fluxes(self):
+        out = np.empty((self.mesh.n_faces, self.n_tracers))
+        self._check(self.lib.rg_get_tracer_fluxes(self.h, dptr(out)))
+        return out
+
+    def tracer_slopes(self):
+        out = np.empty((self.mesh.n_cells, 2 * self.n_tracers))
+        self._check(self.lib.rg_get_tracer_slopes(self.h, dptr(out)))
+        return out
 
     # batches ---------------------------------------------------------------
     def set_problems(self, offsets, gammas):
