@@ -172,6 +172,63 @@ def run_fixed_dt(mesh, cells, gamma, steps, dt, lp=None):
     return cells, ext
 
 
+# ---------------------------------------------------------------- geometry and point motion
+
+class RoMotion(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("edges", C.c_int32), ("chi", C.c_double), ("eta", C.c_double),
+                ("cold", C.c_int32), ("correct_overshoot", C.c_int32), ("box", C.c_double * 4)]
+
+
+def motion(kind=0, edges=0, chi=0.15, eta=0.02, cold=0, correct_overshoot=0, box=(0, 0, 0, 0)):
+    """kind 0 Eulerian, 1 Lagrangian, 2 RoundCells(Lagrangian); edges 0
+    StationaryBox, 1 PeriodicEdgeVelocities; box {left, right, down, up}."""
+    return RoMotion(int(kind), int(edges), chi, eta, int(cold), int(correct_overshoot), (C.c_double * 4)(*box))
+
+
+def _setup_geo():
+    L = lib()
+    if getattr(L, "_rogeo", False):
+        return L
+    dp = C.POINTER(C.c_double)
+    mp = C.POINTER(RoMotion)
+    L.ro_cell_geometry.restype = None
+    L.ro_cell_geometry.argtypes = [C.c_void_p, C.c_int, dp, dp, dp, dp]
+    for f in ("ro_point_velocities", "ro_edge_velocities", "ro_apply_fix"):
+        getattr(L, f).restype = None
+    L.ro_point_velocities.argtypes = [C.c_void_p, dp, C.c_double, mp, dp]
+    L.ro_apply_fix.argtypes = [C.c_void_p, dp, C.c_double, mp, C.c_double, dp]
+    L.ro_edge_velocities.argtypes = [C.c_void_p, mp, dp, dp]
+    L._rogeo = True
+    return L
+
+
+def cell_geometry(mesh, ghost_kind, box):
+    """(volume, cm_xy of all points, cd_volume) from points and face vertices."""
+    n, g = mesh.n_cells, mesh.n_ghosts
+    vol, cm, cdv = np.zeros(n), np.zeros((n + g, 2)), np.zeros(n)
+    b = _f64(box)
+    _setup_geo().ro_cell_geometry(C.byref(mesh.view()), ghost_kind, _d(b), _d(vol), _d(cm), _d(cdv))
+    return vol, cm, cdv
+
+
+def point_velocities(mesh, cells, gamma, mo):
+    pv = np.zeros((mesh.n_cells, 2))
+    _setup_geo().ro_point_velocities(C.byref(mesh.view()), _d(_f64(cells)), gamma, C.byref(mo), _d(pv))
+    return pv
+
+
+def apply_fix(mesh, cells, gamma, mo, dt, pv):
+    pv = _f64(pv).copy()
+    _setup_geo().ro_apply_fix(C.byref(mesh.view()), _d(_f64(cells)), gamma, C.byref(mo), dt, _d(pv))
+    return pv
+
+
+def edge_velocities(mesh, mo, pv):
+    ev = np.zeros((mesh.n_faces, 2))
+    _setup_geo().ro_edge_velocities(C.byref(mesh.view()), C.byref(mo), _d(_f64(pv)), _d(ev))
+    return ev
+
+
 # ---------------------------------------------------------------- tracers and stickers
 
 class RoTracers(C.Structure):

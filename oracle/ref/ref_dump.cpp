@@ -63,6 +63,11 @@ namespace {
 
 std::string g_out;
 bool g_heun = false;
+double g_box[4] = {0, 0, 0, 0};  // the OuterBoundary's (left, right, down, up)
+// the case's point motion and edge velocities: kind (0 Eulerian, 1
+// Lagrangian, 2 RoundCells(Lagrangian)), edges (0 StationaryBox, 1
+// PeriodicEdgeVelocities), chi, eta, cold, CorrectPointsOverShoot active
+double g_motion[6] = {0, 0, 0, 0, 0, 0};
 
 void advance(hdsim& sim) {
   if (g_heun)
@@ -201,13 +206,17 @@ void dump_components(hdsim& sim, const PhysicalGeometry& pg, const EquationOfSta
     dump_i32("tr_stickers", st, 0);
   }
   dump_scalar("time0", t);
+  dump_f64("outer_box", std::vector<double>(g_box, g_box + 4), 0);
+  dump_f64("motion", std::vector<double>(g_motion, g_motion + 6), 0);
   vector<Vector2D> pv = pm(tess, cells, t, tsn);
   vector<Vector2D> ev = evc(tess, pv);
   const double dt = tsf(tess, cells, eos, ev, t, tsn);
+  dump_f64("pv_cfl", vec_flat(pv), 2);
   dump_f64("ev_cfl", vec_flat(ev), 2);
   dump_scalar("dt", dt);
   pv = pm.ApplyFix(tess, cells, t, dt, pv, tsn);
   ev = evc(tess, pv);
+  dump_f64("pv_flux", vec_flat(pv), 2);
   dump_f64("ev_flux", vec_flat(ev), 2);
   CacheData cd(tess, pg);
   if (lgi) {
@@ -333,6 +342,7 @@ int main(int argc, char** argv) {
     if (which == "sod" || which == "sod_lagrangian") {
       // 2D Sod tube: [0,1]x[0,0.2], reflective walls, piecewise-constant Hllc, gamma 1.4.
       SquareBox outer(Vector2D(0, 0), Vector2D(1, 0.2));
+      g_box[0] = 0, g_box[1] = 1, g_box[2] = 0, g_box[3] = 0.2;
       VoronoiMesh tess(jittered_lattice(nx, ny, 0, 1, 0, 0.2, 1, 1e-3), outer);
       IdealGas eos(1.4);
       Eulerian eul;
@@ -340,6 +350,7 @@ int main(int argc, char** argv) {
       const PointMotion& pm = which == "sod" ? static_cast<const PointMotion&>(eul)
                                              : static_cast<const PointMotion&>(lag);
       StationaryBox evc;
+      g_motion[0] = which == "sod" ? 0 : 1;
       SimpleFluxCalculator fc(rs);
       vector<ComputationalCell> ic(static_cast<size_t>(tess.GetPointNo()));
       for (size_t i = 0; i < ic.size(); ++i) {
@@ -359,6 +370,7 @@ int main(int argc, char** argv) {
       // Sedov-Taylor on [-1,1]^2, RoundCells(Lagrangian) (or Eulerian),
       // LinearGaussImproved + rigid walls.
       SquareBox outer(Vector2D(-1, -1), Vector2D(1, 1));
+      g_box[0] = -1, g_box[1] = 1, g_box[2] = -1, g_box[3] = 1;
       VoronoiMesh tess(jittered_lattice(nx, ny, -1, 1, -1, 1, 2, 1e-3), outer);
       IdealGas eos(5. / 3.);
       Lagrangian lag;
@@ -367,6 +379,8 @@ int main(int argc, char** argv) {
       const PointMotion& pm = which == "sedov" ? static_cast<const PointMotion&>(round)
                                                : static_cast<const PointMotion&>(eul);
       StationaryBox evc;
+      // RoundCells(lag, eos): chi 0.15, eta 0.02, hot, periodic default outer (no overshoot fix)
+      if (which == "sedov") g_motion[0] = 2, g_motion[2] = 0.15, g_motion[3] = 0.02;
       RigidWallGenerator gpg;
       LinearGaussImproved sr(eos, gpg, true, 0.2, 0.5, 0.7, calc_tracers, skip_key);
       ModularFluxCalculator fc(sr, rs);
@@ -391,6 +405,7 @@ int main(int argc, char** argv) {
     } else if (which == "periodic" || which == "periodic_lagrangian") {
       // Periodic [0,1]^2, LinearGaussImproved + PeriodicGhostGenerator, smooth bumps + velocity modes.
       PeriodicBox outer(0, 1, 1, 0);
+      g_box[0] = 0, g_box[1] = 1, g_box[2] = 0, g_box[3] = 1;
       VoronoiMesh tess(jittered_lattice(nx, ny, 0, 1, 0, 1, 3, 1e-3), outer);
       IdealGas eos(5. / 3.);
       Eulerian eul;
@@ -398,6 +413,8 @@ int main(int argc, char** argv) {
       const PointMotion& pm = which == "periodic" ? static_cast<const PointMotion&>(eul)
                                                   : static_cast<const PointMotion&>(lag);
       PeriodicEdgeVelocities evc;
+      g_motion[0] = which == "periodic" ? 0 : 1;
+      g_motion[1] = 1;
       PeriodicGhostGenerator gpg;
       LinearGaussImproved sr(eos, gpg, true, 0.2, 0.5, 0.7, calc_tracers, skip_key);
       ModularFluxCalculator fc(sr, rs);
@@ -429,6 +446,36 @@ int main(int argc, char** argv) {
       dump_scalar("order", 2);
       dump_scalar("ghost_kind", 1);
       dump_components(sim, pg, eos, pm, evc, tsf, fc, eu, cu, &sr);
+      if (run > 0) run_and_dump(sim, run);
+    } else if (which == "wallflow_cold") {
+      // Fast flow into the walls of [0,1]^2 on a RoundCells(Lagrangian, cold)
+      // mesh with the box as its outer boundary: RoundCells::ApplyFix's
+      // calc_dw(dt) and CorrectPointsOverShoot (round_cells.cpp:15-63,
+      // 96-134) act; LinearGaussImproved + rigid walls.
+      SquareBox outer(Vector2D(0, 0), Vector2D(1, 1));
+      g_box[0] = 0, g_box[1] = 1, g_box[2] = 0, g_box[3] = 1;
+      VoronoiMesh tess(jittered_lattice(nx, ny, 0, 1, 0, 1, 4, 1e-3), outer);
+      IdealGas eos(5. / 3.);
+      Lagrangian lag;
+      RoundCells round(lag, eos, outer, 0.15, 0.02, true);
+      StationaryBox evc;
+      g_motion[0] = 2, g_motion[2] = 0.15, g_motion[3] = 0.02, g_motion[4] = 1, g_motion[5] = 1;
+      RigidWallGenerator gpg;
+      LinearGaussImproved sr(eos, gpg);
+      ModularFluxCalculator fc(sr, rs);
+      vector<ComputationalCell> ic(static_cast<size_t>(tess.GetPointNo()));
+      for (size_t i = 0; i < ic.size(); ++i) {
+        const Vector2D r = tess.GetMeshPoint(static_cast<int>(i));
+        ic[i].density = 1 + 0.2 * std::sin(6 * r.x) * std::cos(5 * r.y);
+        ic[i].pressure = 0.01;
+        ic[i].velocity = Vector2D(1.0 + 0.2 * std::sin(7 * r.y), 0.6 - 0.3 * std::cos(4 * r.x));
+      }
+      hdsim sim(tess, outer, pg, ic, eos, round, evc, force, tsf, fc, eu, cu);
+      for (int s = 0; s < warm; ++s) advance(sim);
+      dump_scalar("gamma", 5. / 3.);
+      dump_scalar("order", 2);
+      dump_scalar("ghost_kind", 0);
+      dump_components(sim, pg, eos, round, evc, tsf, fc, eu, cu, &sr);
       if (run > 0) run_and_dump(sim, run);
     } else {
       std::fprintf(stderr, "unknown case %s\n", which.c_str());

@@ -1017,6 +1017,197 @@ int ro_step_heun(const rg_mesh_view* m, double* cells, double* ext, const double
 }
 
 /* ========================================================================
+ * Geometry and point motion (tessellation, CacheData, PointMotion,
+ * EdgeVelocityCalculator)
+ * ======================================================================== */
+
+/* geometry.cpp:138-141 zcross, :100-104 ScalarProd: 0.5*|p1 . zcross(p2)| */
+static double half_cross(v2 p1, v2 p2) {
+  const v2 z = {p2.y, -p2.x};
+  return 0.5 * fabs(dot(p1, z));
+}
+
+void ro_cell_geometry(const rg_mesh_view* m, int ghost_kind, const double* box, double* volume, double* cm_xy,
+                      double* cd_volume) {
+  const int N = m->n_cells;
+  for (int i = 0; i < N; ++i) {
+    const int b = m->cell_face_offset[i], e1 = m->cell_face_offset[i + 1];
+    /* VoronoiMesh.cpp:420-434 GetVolume: fan from the mesh point */
+    const v2 c = point(m, i);
+    double area = 0;
+    for (int k = b; k < e1; ++k) {
+      const int e = m->cell_faces[k];
+      area += half_cross(vsub(vert0(m, e), c), vsub(vert1(m, e), c));
+    }
+    volume[i] = area;
+    /* VoronoiMesh.cpp:436-451 CalcCellCM: fan from the first edge's first
+     * vertex; physical_geometry.cpp:13-21 SlabSymmetry::calcVolume sums the
+     * same triangles (triangle_area.cpp calc_triangle_area) in the same order */
+    const v2 anchor = vert0(m, m->cell_faces[b]);
+    v2 pc = {0, 0};
+    double a2 = 0, vol = 0;
+    for (int k = b + 1; k < e1; ++k) {
+      const int e = m->cell_faces[k];
+      const v2 f = vert0(m, e), s = vert1(m, e);
+      const double t = half_cross(vsub(f, anchor), vsub(s, anchor));
+      a2 += t;
+      pc = vadd(pc, vscale(vadd(vadd(anchor, f), s), t / 3.));
+      vol += half_cross(vsub(f, anchor), vsub(s, anchor));
+    }
+    cm_xy[2 * i] = pc.x / a2;
+    cm_xy[2 * i + 1] = pc.y / a2;
+    cd_volume[i] = vol;
+  }
+  /* VoronoiMesh.cpp:355-398 ghost CMs: periodic copies are shifted by the
+   * ghost's offset from its source point; rigid-wall copies are reflected
+   * (GetReflection, :316-330) about the box side they lie beyond */
+  for (int g = 0; g < m->n_ghosts; ++g) {
+    const int p = N + g, src = m->ghost_source[g];
+    const v2 cs = {cm_xy[2 * src], cm_xy[2 * src + 1]};
+    v2 r;
+    if (ghost_kind == RG_GHOST_PERIODIC) {
+      r = vadd(cs, vsub(point(m, p), point(m, src)));
+    } else {
+      const v2 q = point(m, p);
+      r = cs;
+      if (q.x > box[1]) {
+        const v2 d = {2 * (box[1] - cs.x), 0};
+        r = vadd(cs, d);
+      } else if (q.y > box[3]) {
+        const v2 d = {0, 2 * (box[3] - cs.y)};
+        r = vadd(cs, d);
+      } else if (q.x < box[0]) {
+        const v2 d = {2 * (box[0] - cs.x), 0};
+        r = vadd(cs, d);
+      } else if (q.y < box[2]) {
+        const v2 d = {0, 2 * (box[2] - cs.y)};
+        r = vadd(cs, d);
+      }
+    }
+    cm_xy[2 * p] = r.x;
+    cm_xy[2 * p + 1] = r.y;
+  }
+}
+
+/* round_cells.cpp:69-81 calc_dw (hot form) */
+static v2 round_dw(const rg_mesh_view* m, const double* cells, double g, const ro_motion* mo, int i) {
+  const v2 r = point(m, i), s = cmof(m, i);
+  const double d = vabs(vsub(s, r));
+  const double R = width(m, i);
+  const v2 zero = {0, 0};
+  if (d < 0.9 * mo->eta * R) return zero;
+  const v2 v = {cells[4 * i + 2], cells[4 * i + 3]};
+  const double c = smax(dp2c(g, cells[4 * i], cells[4 * i + 1]), vabs(v));
+  return vdiv(vscale(vsub(s, r), mo->chi * c), R);
+}
+
+/* round_cells.cpp:83-103 calc_dw (cold form, with dt); the neighbour test
+ * compares the neighbour's id with the neighbour count, as the reference does */
+static v2 round_dw_cold(const rg_mesh_view* m, const double* cells, double g, const ro_motion* mo, int i,
+                        double dt) {
+  const v2 r = point(m, i), s = cmof(m, i);
+  const double d = vabs(vsub(s, r));
+  const double R = width(m, i);
+  const v2 zero = {0, 0};
+  if (d < 0.9 * mo->eta * R) return zero;
+  const int b = m->cell_face_offset[i], nn = m->cell_face_offset[i + 1] - b;
+  const v2 v = {cells[4 * i + 2], cells[4 * i + 3]};
+  double cs = smax(vabs(v), dp2c(g, cells[4 * i], cells[4 * i + 1]));
+  for (int k = 0; k < nn; ++k) {
+    const int e = m->cell_faces[b + k];
+    const int nb = fc0(m, e) != i ? fc0(m, e) : fc1(m, e);
+    if (orig(m, nb) == i || nb > nn) continue;
+    const v2 vn = {cells[4 * nb + 2], cells[4 * nb + 3]};
+    cs = smax(cs, dp2c(g, cells[4 * nb], cells[4 * nb + 1]));
+    cs = smax(cs, vabs(vn));
+  }
+  const double c_dt = d / dt;
+  return vdiv(vscale(vsub(s, r), mo->chi * smin(c_dt, cs)), R);
+}
+
+void ro_point_velocities(const rg_mesh_view* m, const double* cells, double g, const ro_motion* mo, double* pv) {
+  for (int i = 0; i < m->n_cells; ++i) {
+    v2 w = {0, 0};
+    if (mo->kind >= 1) { /* lagrangian.cpp:3-13 */
+      w.x = cells[4 * i + 2];
+      w.y = cells[4 * i + 3];
+    }
+    if (mo->kind == 2 && !mo->cold) w = vadd(w, round_dw(m, cells, g, mo, i)); /* round_cells.cpp:105-119 */
+    pv[2 * i] = w.x;
+    pv[2 * i + 1] = w.y;
+  }
+}
+
+/* round_cells.cpp:15-63 CorrectPointsOverShoot for one point */
+static v2 overshoot(const rg_mesh_view* m, const ro_motion* mo, int i, double dt, v2 v) {
+  const v2 p = point(m, i);
+  const double R = width(m, i);
+  const double inv_dt = 1.0 / dt;
+  const double L = mo->box[0], Rt = mo->box[1], D = mo->box[2], U = mo->box[3];
+  if ((v.x * dt * 2 + p.x) > Rt) {
+    double f = 0.25 * (Rt - p.x) * inv_dt / vabs(v);
+    if (R * 0.1 > (Rt - p.x)) f *= -0.1;
+    v = vscale(v, f);
+  }
+  if ((v.x * dt * 2 + p.x) < L) {
+    double f = 0.25 * (p.x - L) * inv_dt / vabs(v);
+    if (R * 0.1 > (p.x - L)) f *= -0.1;
+    v = vscale(v, f);
+  }
+  if ((v.y * dt * 2 + p.y) > U) {
+    double f = 0.25 * (U - p.y) * inv_dt / vabs(v);
+    if (R * 0.1 > (U - p.y)) f *= -0.1;
+    v = vscale(v, f);
+  }
+  if ((v.y * dt * 2 + p.y) < D) {
+    double f = 0.25 * (p.y - D) * inv_dt / vabs(v);
+    if (R * 0.1 > (p.y - D)) f *= -0.1;
+    v = vscale(v, f);
+  }
+  return v;
+}
+
+/* round_cells.cpp:121-134 RoundCells::ApplyFix (point_motion.cpp:5-9: the
+ * wrapped motion leaves the velocities) */
+void ro_apply_fix(const rg_mesh_view* m, const double* cells, double g, const ro_motion* mo, double dt, double* pv) {
+  if (mo->kind != 2) return;
+  for (int i = 0; i < m->n_cells; ++i) {
+    v2 w = {pv[2 * i], pv[2 * i + 1]};
+    if (mo->cold) w = vadd(w, round_dw_cold(m, cells, g, mo, i, dt));
+    if (mo->correct_overshoot) w = overshoot(m, mo, i, dt, w);
+    pv[2 * i] = w.x;
+    pv[2 * i + 1] = w.y;
+  }
+}
+
+/* VoronoiMesh.cpp:146-151 CalcFaceVelocity (pow(x,2) is x*x) */
+static v2 face_velocity(v2 wl, v2 wr, v2 rl, v2 rr, v2 f) {
+  const v2 mid = vdiv(vadd(rr, rl), 2);
+  const v2 dr = vsub(rr, rl);
+  const double a = vabs(dr);
+  const v2 wp = vdiv(vscale(dr, dot(vsub(wl, wr), vsub(f, mid))), a * a);
+  return vadd(vscale(vadd(wl, wr), 0.5), wp);
+}
+
+/* stationary_box.cpp:20-40 (0 on a face between a point and its own copy)
+ * and periodic_edge_velocities.cpp:5-21; a ghost takes its source point's
+ * velocity (StationaryBox indexes the point velocities with the ghost id,
+ * which only a face of a point and its own copy could reach) */
+void ro_edge_velocities(const rg_mesh_view* m, const ro_motion* mo, const double* pv, double* ev) {
+  for (int e = 0; e < m->n_faces; ++e) {
+    const int a = fc0(m, e), b = fc1(m, e);
+    const int oa = orig(m, a), ob = orig(m, b);
+    v2 w = {0, 0};
+    if (mo->edges == 1 || oa != ob) {
+      const v2 wl = {pv[2 * oa], pv[2 * oa + 1]}, wr = {pv[2 * ob], pv[2 * ob + 1]};
+      w = face_velocity(wl, wr, point(m, a), point(m, b), centroid(m, e));
+    }
+    ev[2 * e] = w.x;
+    ev[2 * e + 1] = w.y;
+  }
+}
+
+/* ========================================================================
  * 3D first-order path (HDSim3D on a CubeGrid-like packed mesh)
  * ======================================================================== */
 

@@ -94,6 +94,32 @@ int ro_step_tr(const rg_mesh_view* m, double* cells, double* ext, double* tr, do
                const double* ev, double gamma, double cfl, int order, const ro_lgi_params* lp,
                const ro_tracers* t, double* dt_out, ro_error* err);
 
+/* Geometry of a packed mesh from its points and face vertices, as the
+ * reference's tessellation and CacheData compute it: volume (GetVolume), the
+ * cell CMs of real cells (CalcCellCM) and ghosts (periodic shift or
+ * reflection about the box side, box = {left, right, down, up}), cd_volume
+ * (SlabSymmetry::calcVolume).  cm_xy holds (n_cells + n_ghosts)*2. */
+void ro_cell_geometry(const rg_mesh_view* m, int ghost_kind, const double* box, double* volume, double* cm_xy,
+                      double* cd_volume);
+
+/* Point motion and edge velocities (hdsim::TimeAdvance's first half). */
+typedef struct ro_motion {
+  int32_t kind;             /* 0 Eulerian, 1 Lagrangian, 2 RoundCells(Lagrangian) */
+  int32_t edges;            /* 0 StationaryBox, 1 PeriodicEdgeVelocities */
+  double chi, eta;          /* RoundCells parameters */
+  int32_t cold;             /* RoundCells cold switch */
+  int32_t correct_overshoot; /* RoundCells outer boundary is not periodic */
+  double box[4];            /* RoundCells outer boundary {left, right, down, up} */
+} ro_motion;
+/* PointMotion::operator() for the n_cells points: pv n_cells*2 */
+void ro_point_velocities(const rg_mesh_view* m, const double* cells, double gamma, const ro_motion* mo,
+                         double* pv);
+/* PointMotion::ApplyFix, in place */
+void ro_apply_fix(const rg_mesh_view* m, const double* cells, double gamma, const ro_motion* mo, double dt,
+                  double* pv);
+/* EdgeVelocityCalculator::operator(): ev n_faces*2 */
+void ro_edge_velocities(const rg_mesh_view* m, const ro_motion* mo, const double* pv, double* ev);
+
 /* 3D first-order path on the packed 3D mesh.  Cells N*5 {density, pressure,
  * vx, vy, vz}; extensives and fluxes N*5 {mass, px, py, pz, energy}
  * (Conserved3D order).  face_velocity: n_faces*3 or NULL (faces at rest). */

@@ -46,6 +46,9 @@ CASES = {
     "sod_heun_o1": ("sod", 50, 10, 0, 20, "heun"),
     "sedov_eulerian_heun_o2": ("sedov_eulerian", 24, 24, 2, 10, "heun"),
     "periodic_heun_o2": ("periodic", 16, 16, 2, 10, "heun"),
+    # RoundCells(Lagrangian, cold) with the box as its outer boundary, flow
+    # into the walls: ApplyFix's calc_dw(dt) and CorrectPointsOverShoot act
+    "wallflow_cold_o2": ("wallflow_cold", 24, 24, 2, 0),
 }
 
 # Tracers and stickers (ref_dump's <case>_tracers forms), written to

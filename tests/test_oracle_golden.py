@@ -91,3 +91,34 @@ def test_init_extensives(golden):
     if int(g["case_params"][2]) != 0:
         pytest.skip("state is not the initial one")
     exact(oracle.init_extensives(g["mesh"], g["cells0"], g["gamma"]), g["ext0"])
+
+
+def motion_of(g):
+    """The case's PointMotion / EdgeVelocityCalculator as recorded by the dump."""
+    k, edges, chi, eta, cold, fix = g["motion"]
+    return oracle.motion(k, edges, chi, eta, cold, fix, tuple(g["outer_box"]))
+
+
+def test_cell_geometry(golden):
+    """Tessellation::GetVolume, CalcCellCM (with the ghosts' reflected or
+    shifted CMs) and SlabSymmetry::calcVolume from points and face vertices."""
+    g = golden
+    m = g["mesh"]
+    vol, cm, cdv = oracle.cell_geometry(m, g["ghost_kind"], g["outer_box"])
+    exact(vol, m.volume)
+    exact(cdv, m.cd_volume)
+    exact(cm, m.cm_xy)
+
+
+def test_point_motion_and_edge_velocities(golden):
+    """PointMotion (Eulerian, Lagrangian, RoundCells hot and cold with
+    CorrectPointsOverShoot), ApplyFix and the edge velocities both times
+    hdsim::TimeAdvance computes them."""
+    g = golden
+    mo = motion_of(g)
+    pv = oracle.point_velocities(g["mesh"], g["cells0"], g["gamma"], mo)
+    exact(pv, g["pv_cfl"])
+    exact(oracle.edge_velocities(g["mesh"], mo, pv), g["ev_cfl"])
+    pv = oracle.apply_fix(g["mesh"], g["cells0"], g["gamma"], mo, g["dt"], pv)
+    exact(pv, g["pv_flux"])
+    exact(oracle.edge_velocities(g["mesh"], mo, pv), g["ev_flux"])
