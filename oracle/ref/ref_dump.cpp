@@ -454,7 +454,21 @@ int main(int argc, char** argv) {
       // 96-134) act; LinearGaussImproved + rigid walls.
       SquareBox outer(Vector2D(0, 0), Vector2D(1, 1));
       g_box[0] = 0, g_box[1] = 1, g_box[2] = 0, g_box[3] = 1;
-      VoronoiMesh tess(jittered_lattice(nx, ny, 0, 1, 0, 1, 4, 1e-3), outer);
+      // some points of the last column and the last row close to the right
+      // and upper walls, where the flow would carry them out of the box
+      std::vector<Vector2D> pts = jittered_lattice(nx, ny, 0, 1, 0, 1, 4, 1e-3);
+      const double hx = 1.0 / nx, hy = 1.0 / ny;
+      for (int j = 0; j < ny; ++j) {
+        Vector2D& q = pts[static_cast<size_t>((nx - 1) * ny + j)];
+        if (j % 6 == 1) q.x = 1 - 0.02 * hx;
+        if (j % 6 == 4) q.x = 1 - 0.12 * hx;
+      }
+      for (int i = 0; i < nx - 1; ++i) {
+        Vector2D& q = pts[static_cast<size_t>(i * ny + ny - 1)];
+        if (i % 5 == 2) q.y = 1 - 0.03 * hy;
+        if (i % 5 == 0) q.y = 1 - 0.15 * hy;
+      }
+      VoronoiMesh tess(pts, outer);
       IdealGas eos(5. / 3.);
       Lagrangian lag;
       RoundCells round(lag, eos, outer, 0.15, 0.02, true);
