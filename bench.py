@@ -67,7 +67,12 @@ def config_block(mesh, precision="fp64"):
             "reconstruction": "LinearGaussImproved(slf, delta_v=0.2, theta=0.5, delta_P=0.7)",
             "riemann": "Hllc", "eos": "IdealGas(5/3)", "cfl": 0.3,
             "mesh": f"{NX}x{NY} lattice jittered +-1e-3 cell, seed {SEED}, rigid walls",
-            "face_velocities": "zero in value (fixed mesh); e2e streams mesh + face velocities per step",
+            "point_motion": "RoundCells(Lagrangian, chi 0.15, eta 0.02) + StationaryBox face velocities, "
+                            "computed on the device (the timed kernels read them)",
+            "geometry": "volumes and CMs computed on the device from points and face vertices",
+            "e2e_step": "upload points + topology + face vertices (pinned), RoundCells motion, face velocities, "
+                        "dt, ApplyFix, fluxes and extensive update on the device (rg_advance_begin), "
+                        "cell update (rg_cell_update), read back cells, extensives and point velocities",
             "l2": "flushed before every timed step (256 MiB write)", "parallelism": "replicas"}
 
 
@@ -236,12 +241,16 @@ def measure(precision, mesh, cells, ext, args, local_rank, barrier, max_over_ran
     import torch
     import richgpu
 
-    ev0 = np.zeros((mesh.n_faces, 2))
     h = richgpu.Handle(gamma=GAMMA, order=2, ghost_kind=0, precision=precision, device=local_rank)
-    h.upload_mesh(mesh)
+    h.set_outer_box(-1.0, 1.0, -1.0, 1.0)
+    h.upload_mesh(mesh, flags=richgpu.MESH_DEVICE_GEOMETRY)
+    # RoundCells(Lagrangian) with StationaryBox face velocities, as the Sedov
+    # configuration moves its mesh; the face velocities are computed on the
+    # device and every timed kernel reads them
+    h.set_point_motion(kind=2, edges=0, chi=0.15, eta=0.02)
     h.set_cells(cells)
     h.set_extensives(ext)
-    h.set_edge_velocities(ev0)
+    h.point_velocities()
     # launch shapes of the per-step kernels chosen by the library's autotuner
     # on this mesh and state (before the warm-up; the state is unchanged)
     shapes = h.launch_shapes() if args.no_tune else h.autotune(reps=5)
@@ -271,19 +280,21 @@ def measure(precision, mesh, cells, ext, args, local_rank, barrier, max_over_ran
     total_ms = max_over_ranks(float(kms.sum()))
 
     # end to end through the C ABI with host buffers (moving-mesh data flow):
-    # the step's inputs (packed mesh, face velocities) in pinned host memory,
-    # its results (cells, extensives) read back into pinned host memory
-    pmesh, pev, pcells, pext = pinned_io(mesh, ev0, torch)
+    # each step uploads the tessellation the host would have rebuilt (points,
+    # topology, face vertices, from pinned memory), runs hdsim::TimeAdvance's
+    # first half on the device (rg_advance_begin) and the cell update, and
+    # reads the cells, extensives and point velocities back into pinned memory
+    pmesh, ppv, pcells, pext = pinned_io(mesh, np.zeros((mesh.n_cells, 2)), torch)
     ke = max(1, min(args.steps, 30))
     upload_ms = []
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(ke):
-        h.upload_mesh(pmesh)
+        h.upload_mesh(pmesh, flags=richgpu.MESH_DEVICE_GEOMETRY)
         upload_ms.append(h.last_upload_ms())
-        h.set_edge_velocities(pev)
-        h.step()
+        h.advance_begin(out=ppv)
+        h.cell_update()
         h.get_cells(out=pcells)
         h.get_extensives(out=pext)
     torch.cuda.synchronize()
@@ -353,8 +364,8 @@ def run_gpu(args, world, rank, local_rank):
     n, k = mesh.n_cells, args.steps
     value32 = world * n * k / (r32["total_ms"] * 1e-3)
     value64 = world * n * k / (r64["total_ms"] * 1e-3)
-    h2d = mesh.nbytes() + 16 * mesh.n_faces
-    d2h = 2 * 32 * n
+    h2d = mesh.topology_nbytes()
+    d2h = 2 * 32 * n + 16 * n + 8
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -364,6 +375,7 @@ def run_gpu(args, world, rank, local_rank):
                          "oracle/rich_oracle.c (gcc -O2); the reference itself is serial"}
     adjoint = adjoint_block() if rank == 0 and not args.no_adjoint else None
     sedov3d = sedov3d_block(cpu=not args.no_cpu) if rank == 0 and not args.no_3d else None
+    tracers = tracers_block(r64["total_ms"] / k) if rank == 0 and not args.no_tracers else None
     if rank == 0:
         line = {"metric": METRIC, "value": value32, "unit": UNIT, "n_gpus": world, "steps": k,
                 "warmup": r32["warmup"], "ms_per_step": r32["total_ms"] / k, "higher_is_better": True,
@@ -390,10 +402,65 @@ def run_gpu(args, world, rank, local_rank):
                 "speedup_fp32mixed_vs_fp64": value32 / value64,
                 "adjoint": adjoint,
                 "sedov3d": sedov3d,
+                "tracers": tracers,
                 "wall_s_timed_region": r32["wall"] + r64["wall"]}
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+# ------------------------------------------------------------------ tracers
+
+def tracers_block(fp64_ms_per_step, steps=20, warmup=3):
+    """The FP64 step of the same 512^2 Sedov workload with three tracers
+    ("A" limited by LinearGaussImproved, "Entropy" recomputed by the cell
+    updater, "Z" piecewise constant) and two stickers (HasSticker +
+    SkipUpdate on 1% of the cells, LinearGaussImproved's skip_key on 2%, all
+    outside r = 0.5): ms per step and the cost over the tracer-free step.
+    Bit-identical to the reference (the entropy tracer to a few ulp)."""
+    import torch
+    import richgpu
+    import oracle
+    mesh, cells = workload()
+    ext = oracle.init_extensives(mesh, cells, GAMMA)
+    rng = np.random.default_rng(17)
+    n = mesh.n_cells
+    xy = mesh.point_xy[:n]
+    r = np.hypot(xy[:, 0], xy[:, 1])
+    tr = np.stack([xy[:, 0], cells[:, 1] * cells[:, 0] ** -GAMMA, (r < 0.3).astype(float)], axis=1)
+    far = r > 0.5
+    stickers = ((rng.random(n) < 0.01) & far).astype(np.uint32) | \
+        (((rng.random(n) < 0.02) & far).astype(np.uint32) << 1)
+    with richgpu.Handle(gamma=GAMMA, order=2, ghost_kind=0, device=0) as h:
+        h.upload_mesh(mesh)
+        h.set_tracer_config(3, limited=[0], entropy=1, skip_sticker=1, frozen_sticker=0)
+        h.set_stickers(stickers)
+        h.set_cells(cells)
+        h.set_tracers(tr)
+        h.set_extensives(ext)
+        h.init_extensives()
+        h.set_edge_velocities(np.zeros((mesh.n_faces, 2)))
+        for _ in range(warmup):
+            h.step()
+        stream = torch.cuda.ExternalStream(h.stream())
+        flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+        kms = []
+        torch.cuda.synchronize()
+        for _ in range(steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            _, k = h.step_timed()
+            kms.append(k)
+        torch.cuda.synchronize()
+        del flush
+    kms = np.array(kms).mean(0)
+    ms = float(kms.sum())
+    return {"workload": "sedov2d_512x512_lgi_hllc_fp64_3tracers_2stickers", "n_tracers": 3,
+            "ms_per_step": ms, "value": n / (ms * 1e-3), "unit": UNIT, "steps": steps, "warmup": warmup,
+            "phase_ms": {"cfl": float(kms[0]), "slopes+tracer_slopes": float(kms[1]),
+                         "faces+tracer_faces": float(kms[2]), "update+tracer_update": float(kms[3])},
+            "cost_vs_tracer_free_fp64": ms / fp64_ms_per_step,
+            "gpu_launches_per_step": 7, "l2": "flushed before every timed step (256 MiB write)"}
 
 
 # ------------------------------------------------------------------ 3D
@@ -630,6 +697,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint cost measurement")
     ap.add_argument("--no-tune", action="store_true", help="default launch shapes instead of the autotuner's")
+    ap.add_argument("--no-tracers", action="store_true", help="skip the tracer-path measurement")
     ap.add_argument("--no-3d", action="store_true", help="skip the 3D first-order measurement")
     ap.add_argument("--workload", default="sedov", choices=["sedov", "riemann_batch", "sedov3d"])
     ap.add_argument("--problems", type=int, default=512)

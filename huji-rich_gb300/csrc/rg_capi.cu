@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "rg_handle.cuh"
+#include "rg_motion.cuh"
 
 using rg::DevStatus;
 
@@ -48,13 +49,16 @@ namespace {
 // Host-side checks of a packed mesh view that need no O(size) pass: counts,
 // pointers and the CSR length.  Every index is checked on the device
 // (k_validate) before any other kernel uses the mesh.
-rg_status check_view(rg_handle* h, const rg_mesh_view* v) {
+rg_status check_view(rg_handle* h, const rg_mesh_view* v, bool device_geometry) {
   if (!v || v->n_cells <= 0 || v->n_ghosts < 0 || v->n_faces < 0) return invalid(h, -1, 0);
   if (static_cast<int64_t>(v->n_cells) + v->n_ghosts > static_cast<int64_t>(rg::kNbrIdMask))
     return invalid(h, -2, 0);
-  if (!v->point_xy || !v->cm_xy || !v->volume || !v->cd_volume || !v->face_cells || !v->face_vertices ||
-      !v->cell_face_offset || !v->cell_faces)
+  if (!v->point_xy || !v->face_cells || !v->face_vertices || !v->cell_face_offset || !v->cell_faces)
     return invalid(h, -3, 0);
+  if (!device_geometry && (!v->cm_xy || !v->volume || !v->cd_volume)) return invalid(h, -3, 0);
+  // rigid-wall ghost CMs are reflected about the box's sides
+  if (device_geometry && v->n_ghosts > 0 && h->cfg.ghost_kind != RG_GHOST_PERIODIC && !h->have_box)
+    return invalid(h, -5, 0);
   if (v->n_ghosts > 0 && (!v->ghost_source || !v->ghost_face)) return invalid(h, -3, 0);
   const int m = v->cell_face_offset[v->n_cells];
   if (v->cell_face_offset[0] != 0 || m < 0 || m > 2 * v->n_faces) return invalid(h, -4, m);
@@ -113,6 +117,7 @@ void fill_views(MeshSlot& s) {
   s.geom.par = at<double2>(b, L.par);
   s.geom.dm0 = at<double2>(b, L.dm0);
   s.geom.dm1 = at<double2>(b, L.dm1);
+  s.geom.dab = at<double>(b, L.dab);
   s.geom.width = at<double>(b, L.width);
   s.geom.minv = at<rg::dbl4>(b, L.minv);
   s.geom.cflags = at<int>(b, L.cflags);
@@ -507,6 +512,7 @@ rg_status rg_destroy(rg_handle* h) {
   }
   adjoint_release(h);
   tracer_release(h);
+  h->pv.release();
   h->flag_buf.release();
   h->cells.release();
   h->ext.release();
@@ -546,12 +552,13 @@ rg_status rg_last_error(const rg_handle* h, rg_error* err) {
   return RG_OK;
 }
 
-rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t /*flags*/) {
+rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t flags) {
   if (!h) return RG_ERR_INVALID_ARGUMENT;
   h->last = rg_error{};
   h->dt_next_ready = false;
   const auto t0 = std::chrono::steady_clock::now();
-  if (rg_status st = check_view(h, v)) return st;
+  const bool device_geometry = (flags & RG_MESH_DEVICE_GEOMETRY) != 0;
+  if (rg_status st = check_view(h, v, device_geometry)) return st;
   RG_CUDA(h, cudaSetDevice(h->cfg.device));
   const int n = v->n_cells, g = v->n_ghosts, e = v->n_faces, m = v->cell_face_offset[n];
   const bool n_changed = h->active >= 0 && active_slot(h)->n != n;
@@ -588,7 +595,7 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t /*flags*/
                  {s.lay.cell_faces, v->cell_faces, 4 * static_cast<size_t>(m)}};
   RG_CUDA(h, cudaEventRecord(h->ev_up0, h->upload_stream));
   for (const Part& p : parts) {
-    if (p.bytes == 0) continue;
+    if (p.bytes == 0 || p.src == nullptr) continue;  // device geometry: computed below
     if (is_pinned(p.src)) {
       RG_CUDA(h, cudaMemcpyAsync(static_cast<char*>(s.buf.p) + p.off, p.src, p.bytes, cudaMemcpyHostToDevice,
                                  h->upload_stream));
@@ -613,6 +620,10 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t /*flags*/
   }
   // geometry pass on the upload stream
   RG_TRY(reset_status(h, h->d_geom_status, h->upload_stream));
+  if (device_geometry)
+    RG_CUDA(h, rg::launch_device_geometry(s.mesh, at<double2>(s.buf.p, s.lay.cms), at<double>(s.buf.p, s.lay.volume),
+                                          at<double>(s.buf.p, s.lay.cd_volume), h->cfg.ghost_kind, h->box,
+                                          h->upload_stream));
   rg::GeomArgs ga{};
   ga.mesh = s.mesh;
   ga.order = h->cfg.order;
@@ -623,6 +634,9 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t /*flags*/
   ga.par = at<double2>(b, s.lay.par);
   ga.dm0 = at<double2>(b, s.lay.dm0);
   ga.dm1 = at<double2>(b, s.lay.dm1);
+  ga.dab = at<double>(b, s.lay.dab);
+  ga.rij = at<double2>(b, s.lay.rij);
+  ga.cij = at<double2>(b, s.lay.cij);
   ga.width = at<double>(b, s.lay.width);
   ga.minv = at<rg::dbl4>(b, s.lay.minv);
   ga.cflags = at<int>(b, s.lay.cflags);

@@ -63,6 +63,19 @@ __global__ void __launch_bounds__(kBlock) k_geom_faces(GeomArgs a) {
   const double2 c0 = a.mesh.cms[fc.x], c1 = a.mesh.cms[fc.y];
   a.dm0[e] = make_double2(mid.x - c0.x, mid.y - c0.y);
   a.dm1[e] = make_double2(mid.x - c1.x, mid.y - c1.y);
+  // |x1 - x0| (VoronoiMesh::CalcFaceVelocity's |rR - rL|) and the per-face
+  // halves of calc_naive_slope (LinearGaussImproved.cpp:85-88): r_ij =
+  // normalize(x_other - x_cell)*length and c_ij = centroid - 0.5*(cm_other +
+  // cm_cell).  The second cell's r_ij is exactly -r_ij (x_a - x_b = -(x_b -
+  // x_a), and rounding is sign-symmetric) and its c_ij the same (the sum
+  // commutes), so each face computes them once.
+  const double2 x0 = a.mesh.points[fc.x], x1 = a.mesh.points[fc.y];
+  const double ddx = x1.x - x0.x, ddy = x1.y - x0.y;
+  const double dab = sqrt(ddx * ddx + ddy * ddy);
+  a.dab[e] = dab;
+  const double len = a.area[e];  // Edge::GetLength = |second - first| = |first - second|
+  a.rij[e] = make_double2((ddx / dab) * len, (ddy / dab) * len);
+  a.cij[e] = make_double2(mid.x - (c1.x + c0.x) * 0.5, mid.y - (c1.y + c0.y) * 0.5);
 }
 
 // Per cell: VoronoiMesh.cpp:410-413 GetWidth; the CSR neighbour words; the
@@ -106,24 +119,16 @@ __global__ void __launch_bounds__(kBlock) k_geom_cells(GeomArgs a) {
     a.minv[i] = make_dbl4(0, 0, 0, 0);
     return;
   }
-  const double2 xi = m.points[i];
   double m0 = 0, m1 = 0, m2 = 0, m3 = 0;
   for (int k = 0; k < nn; ++k) {
     const int e = m.cell_faces[b + k];
-    const int other = static_cast<int>(a.nbr[b + k] & kNbrIdMask);
-    const dbl4 v = m.face_vertices[e];
-    const double2 co = m.cms[other], xo = m.points[other];
-    const double cx = (v.x + v.z) * 0.5 - (co.x + cci.x) * 0.5;
-    const double cy = (v.y + v.w) * 0.5 - (co.y + cci.y) * 0.5;
-    const double lx = v.z - v.x, ly = v.w - v.y;
-    const double len = sqrt(lx * lx + ly * ly);
-    const double dx = xo.x - xi.x, dy = xo.y - xi.y;
-    const double dab = sqrt(dx * dx + dy * dy);
-    const double rx = (dx / dab) * len, ry = (dy / dab) * len;
-    m0 -= cx * rx;
-    m1 -= cy * rx;
-    m2 -= cx * ry;
-    m3 -= cy * ry;
+    const bool first = (a.nbr[b + k] & kNbrFirst) != 0;
+    const double2 r = a.rij[e], c = a.cij[e];
+    const double rx = first ? r.x : -r.x, ry = first ? r.y : -r.y;
+    m0 -= c.x * rx;
+    m1 -= c.y * rx;
+    m2 -= c.x * ry;
+    m3 -= c.y * ry;
     a.hr[b + k] = make_double2(rx * 0.5, ry * 0.5);
   }
   const double vol = m.volume[i];

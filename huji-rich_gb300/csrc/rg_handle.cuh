@@ -60,7 +60,7 @@ struct HostBuf {
 struct SlotLayout {
   size_t points, cms, volume, cd_volume, ghost_source, ghost_face, face_cells, face_vertices, cell_off,
       cell_faces, input_end;
-  size_t area, nrm, nabs, par, dm0, dm1, width, minv, cflags, nbr, hr, ghost_real, ghost_unit;
+  size_t area, nrm, nabs, par, dm0, dm1, dab, rij, cij, width, minv, cflags, nbr, hr, ghost_real, ghost_unit;
   size_t nrm32, nabs32, par32, area32, dm0_32, dm1_32, width32, minv32, ent32, fsign32, gunit32, icdv32, total;
   void compute(int n, int g, int e, int m, bool mixed) {
     const size_t np = static_cast<size_t>(n) + g;
@@ -87,6 +87,9 @@ struct SlotLayout {
     par = take(16 * static_cast<size_t>(e));
     dm0 = take(16 * static_cast<size_t>(e));
     dm1 = take(16 * static_cast<size_t>(e));
+    dab = take(8 * static_cast<size_t>(e));
+    rij = take(16 * static_cast<size_t>(e));
+    cij = take(16 * static_cast<size_t>(e));
     width = take(8 * static_cast<size_t>(n));
     minv = take(32 * static_cast<size_t>(n));
     cflags = take(4 * static_cast<size_t>(n));
@@ -186,6 +189,12 @@ struct rg_handle {
   rgh::DevBuf tr, tr_ext, tr_slopes, tr_flux, mflux, shock, stickers;
   bool have_tr = false, have_tr_ext = false;
   int tr_n = -1, tr_e = -1;
+  // device-side point motion (rg_set_point_motion), the outer boundary's box
+  // (rg_set_outer_box) and the point velocities of the last motion call
+  rg_point_motion motion{RG_MOTION_EULERIAN, RG_EDGES_STATIONARY_BOX, 0.15, 0.02, 0, 0};
+  double box[4] = {0, 0, 0, 0};
+  bool have_box = false;
+  rgh::DevBuf pv;
 };
 
 

@@ -63,6 +63,7 @@ struct GeomDev {
   const double2* par;    // Parallel(edge) = second - first
   const double2* dm0;    // CalcCentroid(edge) - cm[first]
   const double2* dm1;    // CalcCentroid(edge) - cm[second]
+  const double* dab;     // |x_second - x_first|
   // per cell
   const double* width;   // sqrt(volume/pi)
   const dbl4* minv;   // naive-slope inverse matrix, or (SxSy, Sx2, Sy2, den) for boundary cells
@@ -277,6 +278,9 @@ struct GeomArgs {
   double2* par;
   double2* dm0;
   double2* dm1;
+  double* dab;
+  double2* rij;  // calc_naive_slope's r_ij as the first cell sees it (the second sees -r_ij)
+  double2* cij;  // calc_naive_slope's c_ij (the same for both cells)
   double* width;
   dbl4* minv;
   int* cflags;

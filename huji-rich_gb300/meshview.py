@@ -95,6 +95,16 @@ class PackedMesh:
     def nbytes(self):
         return sum(getattr(self, k).nbytes for k in MESH_FIELDS)
 
+    def topology_view(self):
+        """The view without cm_xy, volume and cd_volume (NULL): for uploads with
+        RG_MESH_DEVICE_GEOMETRY, which computes them on the device."""
+        v = self.view()
+        return RgMeshView(v.n_cells, v.n_ghosts, v.n_faces, 0, v.point_xy, None, None, None, v.ghost_source,
+                          v.ghost_face, v.face_cells, v.face_vertices, v.cell_face_offset, v.cell_faces)
+
+    def topology_nbytes(self):
+        return sum(getattr(self, k).nbytes for k in MESH_FIELDS if k not in ("cm_xy", "volume", "cd_volume"))
+
 
 def dptr(a):
     assert a.dtype == np.float64 and a.flags.c_contiguous

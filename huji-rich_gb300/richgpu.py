@@ -30,7 +30,11 @@ EXPORTS = ("rg_default_config", "rg_create", "rg_destroy", "rg_status_string", "
            "rg3_cfl_dt", "rg3_flux", "rg3_extensive_update", "rg3_cell_update", "rg3_step", "rg3_run",
            "rg3_step_timed", "rg_set_tracer_config", "rg_set_tracers", "rg_get_tracers",
            "rg_set_extensive_tracers", "rg_get_extensive_tracers", "rg_set_stickers",
-           "rg_get_tracer_fluxes", "rg_get_tracer_slopes")
+           "rg_get_tracer_fluxes", "rg_get_tracer_slopes", "rg_set_outer_box", "rg_set_point_motion",
+           "rg_point_velocities", "rg_apply_fix", "rg_get_edge_velocities", "rg_get_geometry",
+           "rg_advance_begin")
+
+MESH_DEVICE_GEOMETRY = 2  # RG_MESH_DEVICE_GEOMETRY
 
 KERNELS = ("cfl", "slopes", "faces", "update")
 
@@ -43,6 +47,11 @@ class RgLaunchShapes(C.Structure):
 class RgTracerConfig(C.Structure):
     _fields_ = [("n_tracers", C.c_int32), ("limited_mask", C.c_uint32), ("entropy_tracer", C.c_int32),
                 ("skip_sticker", C.c_int32), ("frozen_sticker", C.c_int32)]
+
+
+class RgPointMotion(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("edges", C.c_int32), ("chi", C.c_double), ("eta", C.c_double),
+                ("cold", C.c_int32), ("correct_overshoot", C.c_int32)]
 
 
 class RgDeviceView(C.Structure):
@@ -123,6 +132,13 @@ def load(path=LIB_PATH):
               "rg_get_tracer_fluxes", "rg_get_tracer_slopes"):
         getattr(lib, f).argtypes = [vp, dp]
     lib.rg_set_stickers.argtypes = [vp, C.POINTER(C.c_uint32)]
+    lib.rg_set_outer_box.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double]
+    lib.rg_set_point_motion.argtypes = [vp, C.POINTER(RgPointMotion)]
+    lib.rg_point_velocities.argtypes = [vp, dp]
+    lib.rg_apply_fix.argtypes = [vp, C.c_double, dp]
+    lib.rg_get_edge_velocities.argtypes = [vp, dp]
+    lib.rg_get_geometry.argtypes = [vp, dp, dp, dp]
+    lib.rg_advance_begin.argtypes = [vp, dp, dp]
     lib.rg_set_launch_shapes.argtypes = [vp, C.POINTER(RgLaunchShapes)]
     lib.rg_get_launch_shapes.argtypes = [vp, C.POINTER(RgLaunchShapes)]
     _lib = lib
@@ -172,7 +188,10 @@ class Handle:
 
     # mesh / state -------------------------------------------------------
     def upload_mesh(self, mesh: PackedMesh, flags=0):
-        self._check(self.lib.rg_upload_mesh(self.h, C.byref(mesh.view()), flags))
+        """flags & MESH_DEVICE_GEOMETRY: only points, topology and face
+        vertices are sent; volumes and CMs are computed on the device."""
+        view = mesh.topology_view() if flags & MESH_DEVICE_GEOMETRY else mesh.view()
+        self._check(self.lib.rg_upload_mesh(self.h, C.byref(view), flags))
         self.mesh = mesh
 
     def last_upload_ms(self):
@@ -259,6 +278,48 @@ class Handle:
         ms = (C.c_float * 4)()
         self._check(self.lib.rg_step_timed(self.h, C.byref(dt), ms))
         return dt.value, list(ms)
+
+    # point motion on the device ------------------------------------------------
+    def set_outer_box(self, left, right, down, up):
+        self._check(self.lib.rg_set_outer_box(self.h, left, right, down, up))
+
+    def set_point_motion(self, kind=0, edges=0, chi=0.15, eta=0.02, cold=False, correct_overshoot=False):
+        """kind 0 Eulerian, 1 Lagrangian, 2 RoundCells(Lagrangian); edges 0
+        StationaryBox, 1 PeriodicEdgeVelocities."""
+        pm = RgPointMotion(int(kind), int(edges), chi, eta, int(cold), int(correct_overshoot))
+        self._check(self.lib.rg_set_point_motion(self.h, C.byref(pm)))
+
+    def point_velocities(self):
+        out = np.empty((self.mesh.n_cells, 2))
+        self._check(self.lib.rg_point_velocities(self.h, dptr(out)))
+        return out
+
+    def apply_fix(self, dt):
+        out = np.empty((self.mesh.n_cells, 2))
+        self._check(self.lib.rg_apply_fix(self.h, C.c_double(dt), dptr(out)))
+        return out
+
+    def edge_velocities(self):
+        out = np.empty((self.mesh.n_faces, 2))
+        self._check(self.lib.rg_get_edge_velocities(self.h, dptr(out)))
+        return out
+
+    def geometry(self):
+        """(volume, cm_xy of all points, cd_volume) of the mesh in use."""
+        n, g = self.mesh.n_cells, self.mesh.n_ghosts
+        vol, cm, cdv = np.empty(n), np.empty((n + g, 2)), np.empty(n)
+        self._check(self.lib.rg_get_geometry(self.h, dptr(vol), dptr(cm), dptr(cdv)))
+        return vol, cm, cdv
+
+    def advance_begin(self, download_pv=True, out=None):
+        """hdsim::TimeAdvance up to MoveMeshPoints; returns (dt, point
+        velocities), the latter into `out` when given."""
+        dt = C.c_double()
+        pv = out if out is not None else (np.empty((self.mesh.n_cells, 2)) if download_pv else None)
+        if pv is not None:
+            assert pv.dtype == np.float64 and pv.size == 2 * self.mesh.n_cells and pv.flags.c_contiguous
+        self._check(self.lib.rg_advance_begin(self.h, C.byref(dt), dptr(pv) if pv is not None else None))
+        return dt.value, pv
 
     # tracers and stickers --------------------------------------------------
     def set_tracer_config(self, n_tracers=0, limited=(), entropy=-1, skip_sticker=-1, frozen_sticker=-1):

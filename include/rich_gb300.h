@@ -180,6 +180,13 @@ typedef struct rg_device_view {
 
 /* Upload flags */
 #define RG_MESH_STATIC 1u /* mesh will not change: later uploads may be skipped by the caller */
+/* cm_xy, volume and cd_volume are computed on the device from the points and
+ * face vertices (and may be NULL): Tessellation::GetVolume
+ * (VoronoiMesh.cpp:420-434), CalcCellCM (:436-451) with the ghosts' shifted
+ * (periodic) or reflected (rigid walls, the box of rg_set_outer_box) CMs
+ * (:316-330, 355-398), SlabSymmetry::calcVolume (physical_geometry.cpp:13-21).
+ * Bit-identical to the reference's values. */
+#define RG_MESH_DEVICE_GEOMETRY 2u
 
 typedef struct rg_handle rg_handle;
 
@@ -298,6 +305,48 @@ typedef struct {
 rg_status rg_autotune(rg_handle* h, int32_t reps, rg_launch_shapes* chosen);
 rg_status rg_set_launch_shapes(rg_handle* h, const rg_launch_shapes* shapes);
 rg_status rg_get_launch_shapes(const rg_handle* h, rg_launch_shapes* shapes);
+
+/* Point motion on the device ---------------------------------------------- */
+/* hdsim::TimeAdvance's first half (hdsim2d.cpp:149-195) on the device: the
+ * PointMotion's point velocities, the EdgeVelocityCalculator's face
+ * velocities, SimpleCFL on them, PointMotion::ApplyFix with that dt, the face
+ * velocities again, the fluxes and the extensive update.  The host then moves
+ * the points (MoveMeshPoints), rebuilds the tessellation, uploads it (with
+ * RG_MESH_DEVICE_GEOMETRY only points, topology and face vertices cross the
+ * bus) and calls rg_cell_update, which uses the new mesh's volumes as
+ * hdsim's cell update does. */
+typedef enum rg_motion_kind {
+  RG_MOTION_EULERIAN = 0,    /* eulerian.cpp: points at rest */
+  RG_MOTION_LAGRANGIAN = 1,  /* lagrangian.cpp:3-13: the cell velocity */
+  RG_MOTION_ROUND_CELLS = 2  /* RoundCells(Lagrangian) (round_cells.cpp) */
+} rg_motion_kind;
+typedef enum rg_edge_velocity_kind {
+  RG_EDGES_STATIONARY_BOX = 0, /* stationary_box.cpp:20-40: 0 on a point's face with its own copy */
+  RG_EDGES_PERIODIC = 1        /* periodic_edge_velocities.cpp:5-21 */
+} rg_edge_velocity_kind;
+typedef struct rg_point_motion {
+  int32_t kind;              /* rg_motion_kind */
+  int32_t edges;             /* rg_edge_velocity_kind */
+  double chi, eta;           /* RoundCells chi, eta (defaults 0.15, 0.02) */
+  int32_t cold;              /* RoundCells cold switch */
+  int32_t correct_overshoot; /* RoundCells' outer boundary is not periodic: CorrectPointsOverShoot
+                                with the box of rg_set_outer_box */
+} rg_point_motion;
+/* the OuterBoundary's box (GetGridBoundary Left, Right, Down, Up) */
+rg_status rg_set_outer_box(rg_handle* h, double left, double right, double down, double up);
+rg_status rg_set_point_motion(rg_handle* h, const rg_point_motion* pm);
+/* PointMotion::operator() and the face velocities from it (the handle's edge
+ * velocities); point_velocities_out (n_cells*2) may be NULL */
+rg_status rg_point_velocities(rg_handle* h, double* point_velocities_out);
+/* PointMotion::ApplyFix with dt on the current point velocities, then the face
+ * velocities again */
+rg_status rg_apply_fix(rg_handle* h, double dt, double* point_velocities_out);
+rg_status rg_get_edge_velocities(rg_handle* h, double* edge_velocities_out);
+/* the mesh geometry in use (computed on the device or uploaded) */
+rg_status rg_get_geometry(rg_handle* h, double* volume, double* cm_xy, double* cd_volume);
+/* point velocities, face velocities, dt, ApplyFix, face velocities, fluxes,
+ * extensive update (one host synchronisation, at the end) */
+rg_status rg_advance_begin(rg_handle* h, double* dt_out, double* point_velocities_out);
 
 /* Tracers and stickers ---------------------------------------------------- */
 /* ComputationalCell::tracers / ::stickers (computational_cell_2d.hpp:19-36)

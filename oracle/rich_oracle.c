@@ -1102,7 +1102,9 @@ static v2 round_dw(const rg_mesh_view* m, const double* cells, double g, const r
 }
 
 /* round_cells.cpp:83-103 calc_dw (cold form, with dt); the neighbour test
- * compares the neighbour's id with the neighbour count, as the reference does */
+ * compares the neighbour's id with the neighbour count, as the reference does;
+ * ids past the real cells, which the reference would read out of range, are
+ * left out */
 static v2 round_dw_cold(const rg_mesh_view* m, const double* cells, double g, const ro_motion* mo, int i,
                         double dt) {
   const v2 r = point(m, i), s = cmof(m, i);
@@ -1116,7 +1118,7 @@ static v2 round_dw_cold(const rg_mesh_view* m, const double* cells, double g, co
   for (int k = 0; k < nn; ++k) {
     const int e = m->cell_faces[b + k];
     const int nb = fc0(m, e) != i ? fc0(m, e) : fc1(m, e);
-    if (orig(m, nb) == i || nb > nn) continue;
+    if (orig(m, nb) == i || nb > nn || nb >= m->n_cells) continue;
     const v2 vn = {cells[4 * nb + 2], cells[4 * nb + 3]};
     cs = smax(cs, dp2c(g, cells[4 * nb], cells[4 * nb + 1]));
     cs = smax(cs, vabs(vn));

@@ -19,6 +19,9 @@ def pytest_configure(config):
 
 
 GOLDEN_CASES = sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(GOLDEN, "*.npz")))
+# cases that also hold an N-step hdsim run on a mesh hdsim rebuilt unchanged
+RUN_CASES = [c for c in GOLDEN_CASES
+             if "run_mesh_unchanged" in np.load(os.path.join(GOLDEN, c + ".npz")).files]
 
 
 def load_golden(name):

@@ -12,7 +12,7 @@ import pytest
 import oracle
 import richgpu
 import synthetic
-from conftest import GOLDEN_CASES, load_golden
+from conftest import GOLDEN_CASES, RUN_CASES, load_golden
 from test_oracle_golden import accumulate, exact
 
 pytestmark = pytest.mark.gpu
@@ -52,7 +52,7 @@ def test_golden_extensive_update_from_host_fluxes(name):
         exact(h.get_extensives(), g["ext1"])
 
 
-@pytest.mark.parametrize("name", [c for c in GOLDEN_CASES if "lagrangian" not in c and c != "sedov_o2"])
+@pytest.mark.parametrize("name", RUN_CASES)
 def test_golden_hdsim_run(name):
     """rg_run reproduces N hdsim::TimeAdvance (or TimeAdvance2Heun) steps on a
     fixed mesh exactly."""
