@@ -134,25 +134,32 @@ def init_extensives(mesh, cells, gamma):
     return out
 
 
-def step(mesh, cells, ext, ev, gamma, cfl_number=0.3, order=2, lp=None, heun=False):
+def step(mesh, cells, ext, ev, gamma, cfl_number=0.3, order=2, lp=None, heun=False, areas=None):
     """One fixed-mesh hot-path pass (hdsim::TimeAdvance, or TimeAdvance2Heun
-    with heun=True); returns (cells, ext, dt)."""
+    with heun=True); returns (cells, ext, dt).  areas: CacheData face areas
+    of a non-slab PhysicalGeometry (the mesh's cd_volume holds its volumes)."""
     cells = _f64(cells).copy()
     ext = _f64(ext).copy()
     ev = _f64(ev)
     lp = lp or lgi_params()
     dt = C.c_double()
     err = RoError()
+    if areas is not None:
+        assert not heun
+        _check(lib().ro_step_areas(C.byref(mesh.view()), _d(cells), _d(ext), _d(ev), C.c_double(gamma),
+                                   C.c_double(cfl_number), C.c_int(order), C.byref(lp), _d(_f64(areas)),
+                                   C.byref(dt), C.byref(err)), err)
+        return cells, ext, dt.value
     fn = lib().ro_step_heun if heun else lib().ro_step
     _check(fn(C.byref(mesh.view()), _d(cells), _d(ext), _d(ev), C.c_double(gamma),
               C.c_double(cfl_number), C.c_int(order), C.byref(lp), C.byref(dt), C.byref(err)), err)
     return cells, ext, dt.value
 
 
-def run(mesh, cells, ext, ev, gamma, steps, cfl_number=0.3, order=2, lp=None, heun=False):
+def run(mesh, cells, ext, ev, gamma, steps, cfl_number=0.3, order=2, lp=None, heun=False, areas=None):
     dts = []
     for _ in range(steps):
-        cells, ext, dt = step(mesh, cells, ext, ev, gamma, cfl_number, order, lp, heun)
+        cells, ext, dt = step(mesh, cells, ext, ev, gamma, cfl_number, order, lp, heun, areas)
         dts.append(dt)
     return cells, ext, np.array(dts)
 
@@ -198,6 +205,10 @@ def _setup_geo():
     L.ro_point_velocities.argtypes = [C.c_void_p, dp, C.c_double, mp, dp]
     L.ro_apply_fix.argtypes = [C.c_void_p, dp, C.c_double, mp, C.c_double, dp]
     L.ro_edge_velocities.argtypes = [C.c_void_p, mp, dp, dp]
+    L.ro_cyl_geometry.restype = None
+    L.ro_cyl_geometry.argtypes = [C.c_void_p, dp, dp, dp, dp]
+    L.ro_extensive_update_areas.restype = None
+    L.ro_extensive_update_areas.argtypes = [C.c_void_p, dp, dp, C.c_double, dp]
     L._rogeo = True
     return L
 
@@ -209,6 +220,20 @@ def cell_geometry(mesh, ghost_kind, box):
     b = _f64(box)
     _setup_geo().ro_cell_geometry(C.byref(mesh.view()), ghost_kind, _d(b), _d(vol), _d(cm), _d(cdv))
     return vol, cm, cdv
+
+
+def cyl_geometry(mesh, origin, direction):
+    """CylindricalSymmetry's CacheData face areas and cell volumes."""
+    areas, vols = np.zeros(mesh.n_faces), np.zeros(mesh.n_cells)
+    L = _setup_geo()
+    L.ro_cyl_geometry(C.byref(mesh.view()), _d(_f64(origin)), _d(_f64(direction)), _d(areas), _d(vols))
+    return areas, vols
+
+
+def extensive_update_areas(mesh, fluxes, areas, dt, ext):
+    ext = _f64(ext).copy()
+    _setup_geo().ro_extensive_update_areas(C.byref(mesh.view()), _d(_f64(fluxes)), _d(_f64(areas)), dt, _d(ext))
+    return ext
 
 
 def point_velocities(mesh, cells, gamma, mo):

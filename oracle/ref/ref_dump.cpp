@@ -68,6 +68,8 @@ double g_box[4] = {0, 0, 0, 0};  // the OuterBoundary's (left, right, down, up)
 // Lagrangian, 2 RoundCells(Lagrangian)), edges (0 StationaryBox, 1
 // PeriodicEdgeVelocities), chi, eta, cold, CorrectPointsOverShoot active
 double g_motion[6] = {0, 0, 0, 0, 0, 0};
+// the PhysicalGeometry: kind (0 SlabSymmetry, 1 CylindricalSymmetry), axis origin, axis direction
+double g_geometry[5] = {0, 0, 0, 0, 0};
 
 void advance(hdsim& sim) {
   if (g_heun)
@@ -154,6 +156,9 @@ void dump_mesh(const std::string& prefix, const Tessellation& tess, const Physic
   CacheData cd(tess, pg);
   rich_gb300::PackedMesh m;
   rich_gb300::pack_tessellation(tess, cd, m);
+  std::vector<double> areas;
+  for (size_t e = 0; e < tess.getAllEdges().size(); ++e) areas.push_back(cd.areas[e]);
+  dump_f64(prefix + "cd_area", areas, 0);
   dump_f64(prefix + "point_xy", m.point_xy, 2);
   dump_f64(prefix + "cm_xy", m.cm_xy, 2);
   dump_f64(prefix + "volume", m.volume, 0);
@@ -208,6 +213,7 @@ void dump_components(hdsim& sim, const PhysicalGeometry& pg, const EquationOfSta
   dump_scalar("time0", t);
   dump_f64("outer_box", std::vector<double>(g_box, g_box + 4), 0);
   dump_f64("motion", std::vector<double>(g_motion, g_motion + 6), 0);
+  dump_f64("geometry", std::vector<double>(g_geometry, g_geometry + 5), 0);
   vector<Vector2D> pv = pm(tess, cells, t, tsn);
   vector<Vector2D> ev = evc(tess, pv);
   const double dt = tsf(tess, cells, eos, ev, t, tsn);
@@ -273,7 +279,7 @@ void dump_components(hdsim& sim, const PhysicalGeometry& pg, const EquationOfSta
   }
 }
 
-void run_and_dump(hdsim& sim, int steps) {
+void run_and_dump(hdsim& sim, int steps, const PhysicalGeometry& pg = SlabSymmetry()) {
   // hdsim keeps time_ += dt (hdsim2d.cpp:238); the sequence of times pins
   // every dt without the rounding of a difference.
   std::vector<double> times;
@@ -289,7 +295,7 @@ void run_and_dump(hdsim& sim, int steps) {
   }
   dump_scalar("run_time", sim.getTime());
   dump_f64("run_times", times, 0);
-  dump_mesh("runmesh_", sim.getTessellation(), SlabSymmetry());
+  dump_mesh("runmesh_", sim.getTessellation(), pg);
 }
 
 }  // namespace
@@ -447,6 +453,37 @@ int main(int argc, char** argv) {
       dump_scalar("ghost_kind", 1);
       dump_components(sim, pg, eos, pm, evc, tsf, fc, eu, cu, &sr);
       if (run > 0) run_and_dump(sim, run);
+    } else if (which == "cyl_blast") {
+      // Cylindrical symmetry about the y axis (r = x) on [0,1]^2: a blast at
+      // the origin corner, Eulerian, LinearGaussImproved + rigid walls; the
+      // PhysicalGeometry gives CacheData's face areas and cell volumes
+      // (physical_geometry.cpp:62-110) and the complementary source term is
+      // not applied (ZeroForce).
+      SquareBox outer(Vector2D(0, 0), Vector2D(1, 1));
+      g_box[0] = 0, g_box[1] = 1, g_box[2] = 0, g_box[3] = 1;
+      CylindricalSymmetry cpg(Vector2D(0, 0), Vector2D(0, 1));
+      g_geometry[0] = 1, g_geometry[1] = 0, g_geometry[2] = 0, g_geometry[3] = 0, g_geometry[4] = 1;
+      VoronoiMesh tess(jittered_lattice(nx, ny, 0, 1, 0, 1, 5, 1e-3), outer);
+      IdealGas eos(5. / 3.);
+      Eulerian eul;
+      StationaryBox evc;
+      RigidWallGenerator gpg;
+      LinearGaussImproved sr(eos, gpg);
+      ModularFluxCalculator fc(sr, rs);
+      vector<ComputationalCell> ic(static_cast<size_t>(tess.GetPointNo()));
+      for (size_t i = 0; i < ic.size(); ++i) {
+        const Vector2D r = tess.GetMeshPoint(static_cast<int>(i));
+        ic[i].density = 1 + 0.3 * r.y;
+        ic[i].pressure = abs(r) < 0.15 ? 10.0 : 0.1;
+        ic[i].velocity = Vector2D(0.05 * r.y, -0.05 * r.x);
+      }
+      hdsim sim(tess, outer, cpg, ic, eos, eul, evc, force, tsf, fc, eu, cu);
+      for (int s = 0; s < warm; ++s) advance(sim);
+      dump_scalar("gamma", 5. / 3.);
+      dump_scalar("order", 2);
+      dump_scalar("ghost_kind", 0);
+      dump_components(sim, cpg, eos, eul, evc, tsf, fc, eu, cu, &sr);
+      if (run > 0) run_and_dump(sim, run, cpg);
     } else if (which == "wallflow_cold") {
       // Fast flow into the walls of [0,1]^2 on a RoundCells(Lagrangian, cold)
       // mesh with the box as its outer boundary: RoundCells::ApplyFix's

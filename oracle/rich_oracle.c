@@ -1089,6 +1089,84 @@ void ro_cell_geometry(const rg_mesh_view* m, int ghost_kind, const double* box, 
   }
 }
 
+/* physical_geometry.cpp:44-60 Axis and change_coordinate: (along, |across|) */
+typedef struct { v2 origin, dir; } axis2;
+static v2 change_coordinate(v2 v, axis2 a) {
+  const v2 d = vsub(v, a.origin);
+  const v2 z = {a.dir.y, -a.dir.x};
+  v2 r = {dot(d, a.dir), fabs(dot(d, z))};
+  return r;
+}
+/* :75-82 calc_cone_segment_volume (pow(x,2.) is x*x) */
+static double cone_segment(v2 p1, v2 p2, axis2 a) {
+  const v2 q1 = change_coordinate(p1, a), q2 = change_coordinate(p2, a);
+  return (RO_PI / 3.) * (q2.x - q1.x) * (q1.y * q1.y + q2.y * q2.y + q1.y * q2.y);
+}
+
+void ro_cyl_geometry(const rg_mesh_view* m, const double* origin, const double* direction, double* areas,
+                     double* volumes) {
+  const v2 dd = {direction[0], direction[1]};
+  axis2 a;
+  a.origin.x = origin[0];
+  a.origin.y = origin[1];
+  a.dir = vdiv(dd, vabs(dd)); /* physical_geometry.cpp:40-42 */
+  for (int e = 0; e < m->n_faces; ++e) {
+    /* :66-71 calcArea */
+    const v2 p1 = change_coordinate(vert0(m, e), a), p2 = change_coordinate(vert1(m, e), a);
+    const double dy = p2.y - p1.y, dx = p2.x - p1.x;
+    areas[e] = RO_PI * (p1.y + p2.y) * sqrt(dy * dy + dx * dx);
+  }
+  for (int i = 0; i < m->n_cells; ++i) {
+    /* :94-104 calcVolume over the cell's edges, :84-92 calc_triangular_ring_volume */
+    const int b = m->cell_face_offset[i], e1 = m->cell_face_offset[i + 1];
+    const v2 anchor = vert0(m, m->cell_faces[b]);
+    double res = 0;
+    for (int k = b + 1; k < e1; ++k) {
+      const int e = m->cell_faces[k];
+      const v2 f = vert0(m, e), s2 = vert1(m, e);
+      res += fabs(cone_segment(anchor, f, a) + cone_segment(f, s2, a) + cone_segment(s2, anchor, a));
+    }
+    volumes[i] = res;
+  }
+}
+
+void ro_extensive_update_areas(const rg_mesh_view* m, const double* fluxes, const double* areas, double dt,
+                               double* ext) {
+  const int N = m->n_cells;
+  for (int e = 0; e < m->n_faces; ++e) {
+    const double s = dt * areas[e];
+    const double dm = fluxes[4 * e] * s, de = fluxes[4 * e + 1] * s;
+    const double dx = fluxes[4 * e + 2] * s, dy = fluxes[4 * e + 3] * s;
+    const int a = fc0(m, e), b = fc1(m, e);
+    if (a >= 0 && a < N) {
+      ext[4 * a] -= dm;
+      ext[4 * a + 1] -= de;
+      ext[4 * a + 2] -= dx;
+      ext[4 * a + 3] -= dy;
+    }
+    if (b >= 0 && b < N) {
+      ext[4 * b] += dm;
+      ext[4 * b + 1] += de;
+      ext[4 * b + 2] += dx;
+      ext[4 * b + 3] += dy;
+    }
+  }
+}
+
+int ro_step_areas(const rg_mesh_view* m, double* cells, double* ext, const double* ev, double g, double cfl,
+                  int order, const ro_lgi_params* lp, const double* areas, double* dt_out, ro_error* err) {
+  double dt;
+  int st = ro_cfl(m, cells, ev, g, cfl, &dt, err);
+  if (st) return st;
+  double* fl = (double*)malloc(sizeof(double) * 4 * (size_t)(m->n_faces > 0 ? m->n_faces : 1));
+  st = order == 1 ? ro_simple_flux(m, cells, ev, g, fl, err) : ro_modular_flux(m, cells, ev, g, lp, fl, err);
+  if (!st) ro_extensive_update_areas(m, fl, areas, dt, ext);
+  if (!st) st = ro_cell_update(m, ext, g, cells, err);
+  free(fl);
+  if (dt_out) *dt_out = dt;
+  return st;
+}
+
 /* round_cells.cpp:69-81 calc_dw (hot form) */
 static v2 round_dw(const rg_mesh_view* m, const double* cells, double g, const ro_motion* mo, int i) {
   const v2 r = point(m, i), s = cmof(m, i);

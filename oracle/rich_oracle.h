@@ -102,6 +102,18 @@ int ro_step_tr(const rg_mesh_view* m, double* cells, double* ext, double* tr, do
 void ro_cell_geometry(const rg_mesh_view* m, int ghost_kind, const double* box, double* volume, double* cm_xy,
                       double* cd_volume);
 
+/* CylindricalSymmetry (physical_geometry.cpp:62-110) about the axis through
+ * origin along direction (normalised as Axis does): CacheData's face areas
+ * (n_faces) and cell volumes (n_cells). */
+void ro_cyl_geometry(const rg_mesh_view* m, const double* origin, const double* direction, double* areas,
+                     double* volumes);
+/* SimpleExtensiveUpdater with given face areas (CacheData::areas) */
+void ro_extensive_update_areas(const rg_mesh_view* m, const double* fluxes, const double* areas, double dt,
+                               double* ext);
+/* ro_step with given face areas (the mesh's cd_volume holds the matching volumes) */
+int ro_step_areas(const rg_mesh_view* m, double* cells, double* ext, const double* ev, double gamma, double cfl,
+                  int order, const ro_lgi_params* lp, const double* areas, double* dt_out, ro_error* err);
+
 /* Point motion and edge velocities (hdsim::TimeAdvance's first half). */
 typedef struct ro_motion {
   int32_t kind;             /* 0 Eulerian, 1 Lagrangian, 2 RoundCells(Lagrangian) */

@@ -49,6 +49,8 @@ CASES = {
     # RoundCells(Lagrangian, cold) with the box as its outer boundary, flow
     # into the walls: ApplyFix's calc_dw(dt) and CorrectPointsOverShoot act
     "wallflow_cold_o2": ("wallflow_cold", 24, 24, 2, 0),
+    # CylindricalSymmetry (axis x = 0) face areas and cell volumes: one pass + 10 steps
+    "cyl_blast_o2": ("cyl_blast", 24, 24, 2, 10),
 }
 
 # Tracers and stickers (ref_dump's <case>_tracers forms), written to

@@ -59,9 +59,25 @@ def test_lgi_slopes_and_interp(golden):
     exact(interp, g["interp"])
 
 
+def cylindrical(g):
+    return int(g["geometry"][0]) == 1
+
+
+def areas_of(g):
+    """CacheData face areas: None for SlabSymmetry (the edge lengths the
+    oracle computes), CylindricalSymmetry's otherwise."""
+    if not cylindrical(g):
+        return None
+    return oracle.cyl_geometry(g["mesh"], g["geometry"][1:3], g["geometry"][3:5])[0]
+
+
 def test_extensive_update(golden):
     g = golden
-    exact(oracle.extensive_update(g["mesh"], g["fluxes"], g["dt"], g["ext0"]), g["ext1"])
+    if cylindrical(g):
+        ext1 = oracle.extensive_update_areas(g["mesh"], g["fluxes"], areas_of(g), g["dt"], g["ext0"])
+    else:
+        ext1 = oracle.extensive_update(g["mesh"], g["fluxes"], g["dt"], g["ext0"])
+    exact(ext1, g["ext1"])
 
 
 def test_cell_update(golden):
@@ -79,7 +95,7 @@ def test_hdsim_run(golden):
     steps = int(g["case_params"][3])
     ev = np.zeros((g["mesh"].n_faces, 2))
     cells, ext, dts = oracle.run(g["mesh"], g["cells0"], g["ext0"], ev, g["gamma"], steps,
-                                 0.3, g["order"], lp_of(g), heun=g["heun"])
+                                 0.3, g["order"], lp_of(g), heun=g["heun"], areas=areas_of(g))
     exact(accumulate(float(g["time0"][0]), dts), g["run_times"])
     exact(ext, g["run_ext"])
     exact(cells, g["run_cells"])
@@ -101,13 +117,21 @@ def motion_of(g):
 
 def test_cell_geometry(golden):
     """Tessellation::GetVolume, CalcCellCM (with the ghosts' reflected or
-    shifted CMs) and SlabSymmetry::calcVolume from points and face vertices."""
+    shifted CMs) and the PhysicalGeometry's CacheData volumes and areas
+    (SlabSymmetry, CylindricalSymmetry) from points and face vertices."""
     g = golden
     m = g["mesh"]
     vol, cm, cdv = oracle.cell_geometry(m, g["ghost_kind"], g["outer_box"])
     exact(vol, m.volume)
-    exact(cdv, m.cd_volume)
     exact(cm, m.cm_xy)
+    if cylindrical(g):
+        areas, cdv = oracle.cyl_geometry(m, g["geometry"][1:3], g["geometry"][3:5])
+        exact(areas, g["mesh_cd_area"])
+    else:
+        # SlabSymmetry::calcArea = |first - second| (physical_geometry.cpp:8-11)
+        d = m.face_vertices[:, 0:2] - m.face_vertices[:, 2:4]
+        exact(np.sqrt(d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]), g["mesh_cd_area"])
+    exact(cdv, m.cd_volume)
 
 
 def test_point_motion_and_edge_velocities(golden):
