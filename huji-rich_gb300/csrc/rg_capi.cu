@@ -118,6 +118,7 @@ void fill_views(MeshSlot& s) {
   s.geom.dm0 = at<double2>(b, L.dm0);
   s.geom.dm1 = at<double2>(b, L.dm1);
   s.geom.dab = at<double>(b, L.dab);
+  s.geom.xarea = L.own_xarea ? at<double>(b, L.xarea) : s.geom.area;
   s.geom.width = at<double>(b, L.width);
   s.geom.minv = at<rg::dbl4>(b, L.minv);
   s.geom.cflags = at<int>(b, L.cflags);
@@ -129,6 +130,7 @@ void fill_views(MeshSlot& s) {
   s.g32.nabs = at<float>(b, L.nabs32);
   s.g32.par = at<float2>(b, L.par32);
   s.g32.area = at<float>(b, L.area32);
+  s.g32.xarea = L.own_xarea ? at<float>(b, L.xarea32) : s.g32.area;
   s.g32.dm0 = at<float2>(b, L.dm0_32);
   s.g32.dm1 = at<float2>(b, L.dm1_32);
   s.g32.width = at<float>(b, L.width32);
@@ -566,7 +568,7 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t flags) {
   MeshSlot& s = h->slots[next];
   // the slot may still be read by kernels enqueued on the previous-but-one mesh
   RG_CUDA(h, cudaStreamWaitEvent(h->upload_stream, s.last_use, 0));
-  s.lay.compute(n, g, e, m, h->mixed);
+  s.lay.compute(n, g, e, m, h->mixed, h->pgeo.kind == RG_GEOMETRY_CYLINDRICAL);
   RG_CUDA(h, cudaStreamSynchronize(h->upload_stream));
   RG_CUDA(h, s.buf.ensure(s.lay.total));
   RG_CUDA(h, h->staging.ensure(s.lay.input_end));
@@ -624,6 +626,10 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t flags) {
     RG_CUDA(h, rg::launch_device_geometry(s.mesh, at<double2>(s.buf.p, s.lay.cms), at<double>(s.buf.p, s.lay.volume),
                                           at<double>(s.buf.p, s.lay.cd_volume), h->cfg.ghost_kind, h->box,
                                           h->upload_stream));
+  if (h->pgeo.kind == RG_GEOMETRY_CYLINDRICAL)
+    RG_CUDA(h, rg::launch_cyl_geometry(s.mesh, at<double>(s.buf.p, s.lay.xarea),
+                                       device_geometry ? at<double>(s.buf.p, s.lay.cd_volume) : nullptr,
+                                       h->pgeo.origin, h->pgeo.direction, h->upload_stream));
   rg::GeomArgs ga{};
   ga.mesh = s.mesh;
   ga.order = h->cfg.order;
@@ -658,6 +664,7 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t flags) {
     m32.nabs = at<float>(b, s.lay.nabs32);
     m32.par = at<float2>(b, s.lay.par32);
     m32.area = at<float>(b, s.lay.area32);
+    m32.xarea = s.lay.own_xarea ? at<float>(b, s.lay.xarea32) : m32.area;
     m32.dm0 = at<float2>(b, s.lay.dm0_32);
     m32.dm1 = at<float2>(b, s.lay.dm1_32);
     m32.width = at<float>(b, s.lay.width32);

@@ -502,7 +502,7 @@ __device__ __forceinline__ void k_faces_lgi_item(const StepArgs& a, int e) {
   Cons c;
   if (!solve_face(to_prim(g, side[0]), to_prim(g, side[1]), speed, n, na, p, pa, c, a, e)) return;
   if (a.mflux) a.mflux[e] = c.m;
-  write_flux<kBatch>(a, e, real_side, c, kScaled, pa);
+  write_flux<kBatch>(a, e, real_side, c, kScaled, a.geom.xarea[e]);
 }
 
 template <bool kScaled, bool kBatch>
@@ -551,7 +551,7 @@ __device__ __forceinline__ void k_faces_pcm_item(const StepArgs& a, int e) {
   Cons c;
   if (!solve_face(l, r, velocity, n, na, p, pa, c, a, e)) return;
   if (a.mflux) a.mflux[e] = c.m;
-  write_flux<kBatch>(a, e, real_side, c, kScaled, pa);
+  write_flux<kBatch>(a, e, real_side, c, kScaled, a.geom.xarea[e]);
 }
 
 template <bool kScaled, bool kBatch>
@@ -612,7 +612,7 @@ __device__ __forceinline__ unsigned long long k_update_item(const StepArgs& a, i
       const double2 f01 = f[0], f23 = f[1];
       double dm = f01.x, de = f01.y, dx = f23.x, dy = f23.y;
       if (from_unscaled) {
-        const double s = dt * a.geom.area[e];
+        const double s = dt * a.geom.xarea[e];
         dm *= s;
         de *= s;
         dx *= s;

@@ -60,9 +60,13 @@ struct HostBuf {
 struct SlotLayout {
   size_t points, cms, volume, cd_volume, ghost_source, ghost_face, face_cells, face_vertices, cell_off,
       cell_faces, input_end;
-  size_t area, nrm, nabs, par, dm0, dm1, dab, rij, cij, width, minv, cflags, nbr, hr, ghost_real, ghost_unit;
-  size_t nrm32, nabs32, par32, area32, dm0_32, dm1_32, width32, minv32, ent32, fsign32, gunit32, icdv32, total;
-  void compute(int n, int g, int e, int m, bool mixed) {
+  size_t area, nrm, nabs, par, dm0, dm1, dab, rij, cij, xarea, width, minv, cflags, nbr, hr, ghost_real,
+      ghost_unit;
+  size_t nrm32, nabs32, par32, area32, xarea32, dm0_32, dm1_32, width32, minv32, ent32, fsign32, gunit32, icdv32,
+      total;
+  bool own_xarea = false;  // a non-slab PhysicalGeometry: CacheData areas differ from the edge lengths
+  void compute(int n, int g, int e, int m, bool mixed, bool cyl = false) {
+    own_xarea = cyl;
     const size_t np = static_cast<size_t>(n) + g;
     size_t o = 0;
     auto take = [&o](size_t bytes) {
@@ -90,6 +94,7 @@ struct SlotLayout {
     dab = take(8 * static_cast<size_t>(e));
     rij = take(16 * static_cast<size_t>(e));
     cij = take(16 * static_cast<size_t>(e));
+    xarea = take(cyl ? 8 * static_cast<size_t>(e) : 0);
     width = take(8 * static_cast<size_t>(n));
     minv = take(32 * static_cast<size_t>(n));
     cflags = take(4 * static_cast<size_t>(n));
@@ -102,6 +107,7 @@ struct SlotLayout {
     nabs32 = take(k * 4 * static_cast<size_t>(e));
     par32 = take(k * 8 * static_cast<size_t>(e));
     area32 = take(k * 4 * static_cast<size_t>(e));
+    xarea32 = take(cyl ? k * 4 * static_cast<size_t>(e) : 0);
     dm0_32 = take(k * 8 * static_cast<size_t>(e));
     dm1_32 = take(k * 8 * static_cast<size_t>(e));
     width32 = take(k * 4 * static_cast<size_t>(n));
@@ -192,6 +198,8 @@ struct rg_handle {
   // device-side point motion (rg_set_point_motion), the outer boundary's box
   // (rg_set_outer_box) and the point velocities of the last motion call
   rg_point_motion motion{RG_MOTION_EULERIAN, RG_EDGES_STATIONARY_BOX, 0.15, 0.02, 0, 0};
+  // PhysicalGeometry (rg_set_physical_geometry), applied at each upload
+  rg_physical_geometry pgeo{RG_GEOMETRY_SLAB, {0, 0}, {0, 1}};
   double box[4] = {0, 0, 0, 0};
   bool have_box = false;
   rgh::DevBuf pv;

@@ -64,6 +64,7 @@ struct GeomDev {
   const double2* dm0;    // CalcCentroid(edge) - cm[first]
   const double2* dm1;    // CalcCentroid(edge) - cm[second]
   const double* dab;     // |x_second - x_first|
+  const double* xarea;   // CacheData::areas of the PhysicalGeometry (SlabSymmetry: area)
   // per cell
   const double* width;   // sqrt(volume/pi)
   const dbl4* minv;   // naive-slope inverse matrix, or (SxSy, Sx2, Sy2, den) for boundary cells

@@ -49,6 +49,7 @@ __global__ void __launch_bounds__(kBlock) k_geom32(MixedGeomArgs a) {
     a.nabs[e] = static_cast<float>(g.nabs[e]);
     a.par[e] = make_float2(static_cast<float>(p.x), static_cast<float>(p.y));
     a.area[e] = static_cast<float>(g.area[e]);
+    if (a.xarea != a.area) a.xarea[e] = static_cast<float>(g.xarea[e]);
     a.dm0[e] = make_float2(static_cast<float>(d0.x), static_cast<float>(d0.y));
     a.dm1[e] = make_float2(static_cast<float>(d1.x), static_cast<float>(d1.y));
   }
@@ -422,7 +423,7 @@ __device__ __forceinline__ void k_faces32_lgi_item(const MixedArgs& a, int e) {
   const float g = gamma32<kBatch>(a, real_side), igm = inv_gm1_32<kBatch>(a, real_side);
   F4 c;
   if (!solve32(prim32(g, igm, side[0]), prim32(g, igm, side[1]), vel, n, na, p, pa, c, a, e)) return;
-  write32<kBatch>(a, e, real_side, c, kScaled, pa);
+  write32<kBatch>(a, e, real_side, c, kScaled, a.g32.xarea[e]);
 }
 
 template <bool kScaled, bool kBatch>
@@ -471,7 +472,7 @@ __device__ __forceinline__ void k_faces32_pcm_item(const MixedArgs& a, int e) {
     c.m = 0.0f;
     c.en = 0.0f;
   }
-  write32<kBatch>(a, e, real_side, c, kScaled, pa);
+  write32<kBatch>(a, e, real_side, c, kScaled, a.g32.xarea[e]);
 }
 
 template <bool kScaled, bool kBatch>
@@ -525,7 +526,7 @@ __device__ __forceinline__ unsigned long long k_update_mixed_item(const MixedArg
       const int e = fs & 0x7fffffff;
       float4 f = a.flux32[e];
       if (from_unscaled) {
-        const float sc = a.dt32 * a.g32.area[e];
+        const float sc = a.dt32 * a.g32.xarea[e];
         f = make_float4(f.x * sc, f.y * sc, f.z * sc, f.w * sc);
       }
       if (fs < 0) f = make_float4(-f.x, -f.y, -f.z, -f.w);

@@ -12,6 +12,7 @@ struct MixedGeom {
   const float* nabs;
   const float2* par;
   const float* area;
+  const float* xarea;  // CacheData::areas (SlabSymmetry: area)
   const float2* dm0;
   const float2* dm1;
   const float* width;
@@ -35,6 +36,7 @@ struct MixedGeomArgs {
   float* nabs;
   float2* par;
   float* area;
+  float* xarea;  // == area for SlabSymmetry
   float2* dm0;
   float2* dm1;
   float* width;

@@ -84,6 +84,52 @@ __global__ void __launch_bounds__(kMoBlock) k_ghost_cms(MeshDev m, double2* cms,
 
 __device__ __forceinline__ double vabs2(double x, double y) { return sqrt(x * x + y * y); }
 
+// CylindricalSymmetry (physical_geometry.cpp:44-110): Axis normalises its
+// direction (:40-42); change_coordinate gives (along, |across|).
+struct CylAxis {
+  double ox, oy, dx, dy;
+};
+__device__ __forceinline__ CylAxis cyl_axis(dbl4 od) {
+  const double ab = vabs2(od.z, od.w);
+  return CylAxis{od.x, od.y, od.z / ab, od.w / ab};
+}
+__device__ __forceinline__ double2 change_coordinate(double vx, double vy, const CylAxis& a) {
+  const double px = vx - a.ox, py = vy - a.oy;
+  return make_double2(px * a.dx + py * a.dy, fabs(px * a.dy + py * (-a.dx)));
+}
+// :75-82 calc_cone_segment_volume (pow(x,2.) is x*x)
+__device__ __forceinline__ double cone_segment(double2 p1, double2 p2, const CylAxis& a) {
+  const double2 q1 = change_coordinate(p1.x, p1.y, a), q2 = change_coordinate(p2.x, p2.y, a);
+  return (kPi / 3.) * (q2.x - q1.x) * (q1.y * q1.y + q2.y * q2.y + q1.y * q2.y);
+}
+
+__global__ void __launch_bounds__(kMoBlock) k_cyl_geometry(MeshDev m, double* xarea, double* cd_volume, dbl4 od) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const CylAxis a = cyl_axis(od);
+  if (t < m.e) {
+    // :66-71 calcArea
+    const dbl4 v = m.face_vertices[t];
+    const double2 p1 = change_coordinate(v.x, v.y, a), p2 = change_coordinate(v.z, v.w, a);
+    const double dy = p2.y - p1.y, dx = p2.x - p1.x;
+    xarea[t] = kPi * (p1.y + p2.y) * sqrt(dy * dy + dx * dx);
+  }
+  if (cd_volume && t < m.n) {
+    // :94-104 calcVolume over the cell's edges, :84-92 calc_triangular_ring_volume
+    const int b = m.cell_off[t], e1 = m.cell_off[t + 1];
+    if (e1 > b) {
+      const dbl4 v0 = m.face_vertices[m.cell_faces[b]];
+      const double2 an = make_double2(v0.x, v0.y);
+      double res = 0;
+      for (int k = b + 1; k < e1; ++k) {
+        const dbl4 v = m.face_vertices[m.cell_faces[k]];
+        const double2 f = make_double2(v.x, v.y), s = make_double2(v.z, v.w);
+        res += fabs(cone_segment(an, f, a) + cone_segment(f, s, a) + cone_segment(s, an, a));
+      }
+      cd_volume[t] = res;
+    }
+  }
+}
+
 __device__ __forceinline__ double sound(double g, const double* c) { return sqrt(g * c[1] / c[0]); }
 
 __global__ void __launch_bounds__(kMoBlock) k_point_velocities(StepArgs a, MotionArgs mo) {
@@ -196,6 +242,15 @@ cudaError_t launch_device_geometry(const MeshDev& m, double2* cms, double* volum
                                    int ghost_kind, const double* box, cudaStream_t s) {
   if (m.n > 0) k_dev_geometry<<<mo_blocks(m.n), kMoBlock, 0, s>>>(m, cms, volume, cd_volume);
   if (m.g > 0) k_ghost_cms<<<mo_blocks(m.g), kMoBlock, 0, s>>>(m, cms, ghost_kind, make_dbl4(box[0], box[1], box[2], box[3]));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cyl_geometry(const MeshDev& m, double* xarea, double* cd_volume, const double* origin,
+                                const double* direction, cudaStream_t s) {
+  const int work = m.e > m.n ? m.e : m.n;
+  if (work > 0)
+    k_cyl_geometry<<<mo_blocks(work), kMoBlock, 0, s>>>(m, xarea, cd_volume,
+                                                        make_dbl4(origin[0], origin[1], direction[0], direction[1]));
   return cudaGetLastError();
 }
 

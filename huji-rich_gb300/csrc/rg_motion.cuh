@@ -20,6 +20,9 @@ struct MotionArgs {
 // vertices (box = left, right, down, up; used for rigid-wall ghost CMs)
 cudaError_t launch_device_geometry(const MeshDev& m, double2* cms, double* volume, double* cd_volume,
                                    int ghost_kind, const double* box, cudaStream_t s);
+// CylindricalSymmetry's CacheData face areas and (cd_volume != nullptr) cell volumes
+cudaError_t launch_cyl_geometry(const MeshDev& m, double* xarea, double* cd_volume, const double* origin,
+                                const double* direction, cudaStream_t s);
 cudaError_t launch_point_velocities(const StepArgs& a, const MotionArgs& mo, cudaStream_t s);
 cudaError_t launch_apply_fix(const StepArgs& a, const MotionArgs& mo, cudaStream_t s);
 cudaError_t launch_edge_velocities(const StepArgs& a, const MotionArgs& mo, cudaStream_t s);

@@ -130,11 +130,21 @@ rg_status rg_get_edge_velocities(rg_handle* h, double* ev) {
   return RG_OK;
 }
 
-rg_status rg_get_geometry(rg_handle* h, double* volume, double* cm_xy, double* cd_volume) {
+rg_status rg_set_physical_geometry(rg_handle* h, const rg_physical_geometry* pg) {
+  if (!h || !pg) return RG_ERR_INVALID_ARGUMENT;
+  if (pg->kind != RG_GEOMETRY_SLAB && pg->kind != RG_GEOMETRY_CYLINDRICAL) return invalid(h, 0, pg->kind);
+  if (pg->kind == RG_GEOMETRY_CYLINDRICAL && !(pg->direction[0] != 0 || pg->direction[1] != 0))
+    return invalid(h, 1, 0);
+  h->pgeo = *pg;
+  return RG_OK;
+}
+
+rg_status rg_get_geometry(rg_handle* h, double* volume, double* cm_xy, double* cd_volume, double* cd_area) {
   if (rg_status st = require(h, false, false, false, false)) return st;
   MeshSlot* s = active_slot(h);
   RG_CUDA(h, cudaStreamSynchronize(h->stream));
   const size_t n = static_cast<size_t>(s->n), np = n + static_cast<size_t>(s->g);
+  if (cd_area) RG_CUDA(h, cudaMemcpy(cd_area, s->geom.xarea, 8 * static_cast<size_t>(s->e), cudaMemcpyDeviceToHost));
   if (volume) RG_CUDA(h, cudaMemcpy(volume, s->mesh.volume, 8 * n, cudaMemcpyDeviceToHost));
   if (cm_xy) RG_CUDA(h, cudaMemcpy(cm_xy, s->mesh.cms, 16 * np, cudaMemcpyDeviceToHost));
   if (cd_volume) RG_CUDA(h, cudaMemcpy(cd_volume, s->mesh.cd_volume, 8 * n, cudaMemcpyDeviceToHost));

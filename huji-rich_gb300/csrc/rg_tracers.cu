@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(kTrBlock) k_tr_slopes(StepArgs a, TracerArgs t
 }
 
 __device__ __forceinline__ double tr_scale(const StepArgs& a, int e) {
-  return scaled_dt<false>(a, 0) * a.geom.area[e];  // simple_extensive_updater.cpp:26-27
+  return scaled_dt<false>(a, 0) * a.geom.xarea[e];  // simple_extensive_updater.cpp:26-27
 }
 
 // ModularFluxCalculator tracer fluxes: Mass * (Mass > 0 ? first : second)
@@ -247,7 +247,7 @@ __global__ void __launch_bounds__(kTrBlock) k_tr_update(StepArgs a, TracerArgs t
     for (int k = m.cell_off[i]; k < m.cell_off[i + 1]; ++k) {
       const int e = m.cell_faces[k];
       const bool minus = (a.geom.nbr[k] & kNbrFirst) != 0;
-      const double s = from_unscaled ? dt * a.geom.area[e] : 1.0;
+      const double s = from_unscaled ? dt * a.geom.xarea[e] : 1.0;
       const double* f = t.tr_flux + static_cast<size_t>(e) * nt;
 #pragma unroll
       for (int j = 0; j < kMaxTracers; ++j) {

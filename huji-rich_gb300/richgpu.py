@@ -32,7 +32,7 @@ EXPORTS = ("rg_default_config", "rg_create", "rg_destroy", "rg_status_string", "
            "rg_set_extensive_tracers", "rg_get_extensive_tracers", "rg_set_stickers",
            "rg_get_tracer_fluxes", "rg_get_tracer_slopes", "rg_set_outer_box", "rg_set_point_motion",
            "rg_point_velocities", "rg_apply_fix", "rg_get_edge_velocities", "rg_get_geometry",
-           "rg_advance_begin")
+           "rg_advance_begin", "rg_set_physical_geometry")
 
 MESH_DEVICE_GEOMETRY = 2  # RG_MESH_DEVICE_GEOMETRY
 
@@ -52,6 +52,10 @@ class RgTracerConfig(C.Structure):
 class RgPointMotion(C.Structure):
     _fields_ = [("kind", C.c_int32), ("edges", C.c_int32), ("chi", C.c_double), ("eta", C.c_double),
                 ("cold", C.c_int32), ("correct_overshoot", C.c_int32)]
+
+
+class RgPhysicalGeometry(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("origin", C.c_double * 2), ("direction", C.c_double * 2)]
 
 
 class RgDeviceView(C.Structure):
@@ -137,7 +141,8 @@ def load(path=LIB_PATH):
     lib.rg_point_velocities.argtypes = [vp, dp]
     lib.rg_apply_fix.argtypes = [vp, C.c_double, dp]
     lib.rg_get_edge_velocities.argtypes = [vp, dp]
-    lib.rg_get_geometry.argtypes = [vp, dp, dp, dp]
+    lib.rg_get_geometry.argtypes = [vp, dp, dp, dp, dp]
+    lib.rg_set_physical_geometry.argtypes = [vp, C.POINTER(RgPhysicalGeometry)]
     lib.rg_advance_begin.argtypes = [vp, dp, dp]
     lib.rg_set_launch_shapes.argtypes = [vp, C.POINTER(RgLaunchShapes)]
     lib.rg_get_launch_shapes.argtypes = [vp, C.POINTER(RgLaunchShapes)]
@@ -304,12 +309,19 @@ class Handle:
         self._check(self.lib.rg_get_edge_velocities(self.h, dptr(out)))
         return out
 
-    def geometry(self):
-        """(volume, cm_xy of all points, cd_volume) of the mesh in use."""
+    def geometry(self, areas=False):
+        """(volume, cm_xy of all points, cd_volume[, CacheData face areas]) of
+        the mesh in use."""
         n, g = self.mesh.n_cells, self.mesh.n_ghosts
-        vol, cm, cdv = np.empty(n), np.empty((n + g, 2)), np.empty(n)
-        self._check(self.lib.rg_get_geometry(self.h, dptr(vol), dptr(cm), dptr(cdv)))
-        return vol, cm, cdv
+        vol, cm, cdv, ar = np.empty(n), np.empty((n + g, 2)), np.empty(n), np.empty(self.mesh.n_faces)
+        self._check(self.lib.rg_get_geometry(self.h, dptr(vol), dptr(cm), dptr(cdv), dptr(ar)))
+        return (vol, cm, cdv, ar) if areas else (vol, cm, cdv)
+
+    def set_physical_geometry(self, kind=0, origin=(0.0, 0.0), direction=(0.0, 1.0)):
+        """0 SlabSymmetry, 1 CylindricalSymmetry about the axis through
+        origin along direction; applies from the next upload."""
+        pg = RgPhysicalGeometry(int(kind), (C.c_double * 2)(*origin), (C.c_double * 2)(*direction))
+        self._check(self.lib.rg_set_physical_geometry(self.h, C.byref(pg)))
 
     def advance_begin(self, download_pv=True, out=None):
         """hdsim::TimeAdvance up to MoveMeshPoints; returns (dt, point

@@ -342,8 +342,27 @@ rg_status rg_point_velocities(rg_handle* h, double* point_velocities_out);
  * velocities again */
 rg_status rg_apply_fix(rg_handle* h, double dt, double* point_velocities_out);
 rg_status rg_get_edge_velocities(rg_handle* h, double* edge_velocities_out);
-/* the mesh geometry in use (computed on the device or uploaded) */
-rg_status rg_get_geometry(rg_handle* h, double* volume, double* cm_xy, double* cd_volume);
+/* the mesh geometry in use (computed on the device or uploaded); cd_area:
+ * CacheData's face areas (n_faces) of the PhysicalGeometry.  Any pointer may
+ * be NULL. */
+rg_status rg_get_geometry(rg_handle* h, double* volume, double* cm_xy, double* cd_volume, double* cd_area);
+
+/* PhysicalGeometry (physical_geometry.hpp): SlabSymmetry (the default) or
+ * CylindricalSymmetry about the axis through origin along direction
+ * (physical_geometry.cpp:62-110).  It sets CacheData's face areas, by which
+ * SimpleExtensiveUpdater scales the fluxes, and, with RG_MESH_DEVICE_GEOMETRY,
+ * the cell volumes (cd_volume) the cell updater divides by; uploaded
+ * cd_volume arrays are the caller's CacheData volumes.  Takes effect at the
+ * next rg_upload_mesh.  The source term the reference pairs with it
+ * (CylindricalComplementary) is an external force, outside these passes.
+ * Differentiation returns RG_ERR_INVALID_ARGUMENT with CylindricalSymmetry. */
+typedef enum rg_geometry_kind { RG_GEOMETRY_SLAB = 0, RG_GEOMETRY_CYLINDRICAL = 1 } rg_geometry_kind;
+typedef struct rg_physical_geometry {
+  int32_t kind;         /* rg_geometry_kind */
+  double origin[2];     /* axis origin (CylindricalSymmetry) */
+  double direction[2];  /* axis direction, any length (Axis normalises it) */
+} rg_physical_geometry;
+rg_status rg_set_physical_geometry(rg_handle* h, const rg_physical_geometry* pg);
 /* point velocities, face velocities, dt, ApplyFix, face velocities, fluxes,
  * extensive update (one host synchronisation, at the end) */
 rg_status rg_advance_begin(rg_handle* h, double* dt_out, double* point_velocities_out);

@@ -37,6 +37,17 @@ def load_golden(name):
     return z
 
 
+def set_geometry(h, g):
+    """The fixture's PhysicalGeometry on a handle (before its upload)."""
+    if "geometry" in g and int(g["geometry"][0]) == 1:
+        h.set_physical_geometry(1, tuple(g["geometry"][1:3]), tuple(g["geometry"][3:5]))
+
+
+def upload_golden(h, g, flags=0):
+    set_geometry(h, g)
+    h.upload_mesh(g["mesh"], flags=flags)
+
+
 @pytest.fixture(params=GOLDEN_CASES)
 def golden(request):
     return load_golden(request.param)

@@ -14,7 +14,7 @@ import pytest
 import oracle
 import richgpu
 import synthetic
-from conftest import GOLDEN_CASES, load_golden
+from conftest import GOLDEN_CASES, load_golden, upload_golden
 from test_oracle_golden import exact
 
 pytestmark = pytest.mark.gpu
@@ -31,19 +31,60 @@ def motion_kw(g):
 def device_handle(g, **kw):
     h = richgpu.Handle(gamma=g["gamma"], order=g["order"], ghost_kind=g["ghost_kind"], device=0, **kw)
     h.set_outer_box(*g["outer_box"])
-    h.upload_mesh(g["mesh"], flags=DG)
+    upload_golden(h, g, flags=DG)
     return h
 
 
 @pytest.mark.parametrize("name", GOLDEN_CASES)
 def test_device_geometry(name):
+    """Volumes, CMs (real and ghost) and the PhysicalGeometry's CacheData
+    volumes and face areas (SlabSymmetry, CylindricalSymmetry)."""
     g = load_golden(name)
     m = g["mesh"]
     with device_handle(g) as h:
-        vol, cm, cdv = h.geometry()
+        vol, cm, cdv, areas = h.geometry(areas=True)
     exact(vol, m.volume)
     exact(cm, m.cm_xy)
     exact(cdv, m.cd_volume)
+    exact(areas, g["mesh_cd_area"])
+
+
+def test_cylindrical_areas_with_uploaded_geometry():
+    """CylindricalSymmetry with the caller's CacheData volumes uploaded: the
+    device still forms the face areas, and a pass matches the reference."""
+    g = load_golden("cyl_blast_o2")
+    with richgpu.Handle(gamma=g["gamma"], order=2, ghost_kind=0, device=0) as h:
+        upload_golden(h, g)
+        exact(h.geometry(areas=True)[3], g["mesh_cd_area"])
+        h.set_cells(g["cells0"])
+        h.set_extensives(g["ext0"])
+        h.set_edge_velocities(g["ev_flux"])
+        exact(h.flux(g["dt"]), g["fluxes"])
+        h.extensive_update(g["dt"])
+        exact(h.get_extensives(), g["ext1"])
+        h.set_physical_geometry(0)
+        h.upload_mesh(g["mesh"])                 # back to SlabSymmetry: edge lengths
+        d = g["mesh"].face_vertices[:, 0:2] - g["mesh"].face_vertices[:, 2:4]
+        exact(h.geometry(areas=True)[3], np.sqrt(d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]))
+
+
+def test_cylindrical_mixed_precision_run():
+    """The FP32-mixed path scales its fluxes by the cylindrical areas too:
+    10 steps stay close to the FP64 path's."""
+    g = load_golden("cyl_blast_o2")
+    out = []
+    for precision in (0, 1):
+        with richgpu.Handle(gamma=g["gamma"], order=2, ghost_kind=0, device=0, precision=precision) as h:
+            h.set_outer_box(*g["outer_box"])
+            upload_golden(h, g, flags=DG)
+            h.set_cells(g["cells0"])
+            h.set_extensives(g["ext0"])
+            h.set_edge_velocities(np.zeros((g["mesh"].n_faces, 2)))
+            h.run(10)
+            out.append(h.get_cells())
+    exact(out[0], g["run_cells"])
+    l1 = np.abs(out[1][:, 0] - out[0][:, 0]).sum() / np.abs(out[0][:, 0]).sum()
+    assert l1 < 1e-5, l1
 
 
 @pytest.mark.parametrize("name", GOLDEN_CASES)

@@ -12,8 +12,8 @@ import pytest
 import oracle
 import richgpu
 import synthetic
-from conftest import GOLDEN_CASES, RUN_CASES, load_golden
-from test_oracle_golden import accumulate, exact
+from conftest import GOLDEN_CASES, RUN_CASES, load_golden, upload_golden
+from test_oracle_golden import accumulate, areas_of, exact
 
 pytestmark = pytest.mark.gpu
 
@@ -27,7 +27,7 @@ def test_golden_components(name):
     """Each plugin operation on the reference's inputs gives the reference's outputs."""
     g = load_golden(name)
     with handle_for(g["gamma"], g["order"], g["ghost_kind"]) as h:
-        h.upload_mesh(g["mesh"])
+        upload_golden(h, g)
         h.set_cells(g["cells0"])
         h.set_edge_velocities(g["ev_cfl"])
         assert h.cfl_dt() == g["dt"]                                  # SimpleCFL
@@ -45,7 +45,7 @@ def test_golden_extensive_update_from_host_fluxes(name):
     """The extensive updater also accepts fluxes computed elsewhere (rg_set_fluxes)."""
     g = load_golden(name)
     with handle_for(g["gamma"], g["order"], g["ghost_kind"]) as h:
-        h.upload_mesh(g["mesh"])
+        upload_golden(h, g)
         h.set_extensives(g["ext0"])
         h.set_fluxes(g["fluxes"])
         h.extensive_update(g["dt"])
@@ -59,7 +59,7 @@ def test_golden_hdsim_run(name):
     g = load_golden(name)
     steps = int(g["case_params"][3])
     with handle_for(g["gamma"], g["order"], g["ghost_kind"], time_integrator=int(g["heun"])) as h:
-        h.upload_mesh(g["mesh"])
+        upload_golden(h, g)
         h.set_cells(g["cells0"])
         h.set_extensives(g["ext0"])
         h.set_edge_velocities(np.zeros((g["mesh"].n_faces, 2)))
@@ -74,14 +74,14 @@ def test_golden_fused_step(name):
     """rg_step (dt on the device) equals the split plugin sequence."""
     g = load_golden(name)
     with handle_for(g["gamma"], g["order"], g["ghost_kind"]) as h:
-        h.upload_mesh(g["mesh"])
+        upload_golden(h, g)
         h.set_cells(g["cells0"])
         h.set_extensives(g["ext0"])
         h.set_edge_velocities(g["ev_cfl"])
         dt = h.step()
         cells, ext = h.get_cells(), h.get_extensives()
     oc, oe, odt = oracle.step(g["mesh"], g["cells0"], g["ext0"], g["ev_cfl"], g["gamma"], 0.3, g["order"],
-                              oracle.lgi_params(g["ghost_kind"]))
+                              oracle.lgi_params(g["ghost_kind"]), areas=areas_of(g))
     assert dt == odt
     exact(ext, oe)
     exact(cells, oc)
