@@ -629,7 +629,7 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t flags) {
   if (h->pgeo.kind == RG_GEOMETRY_CYLINDRICAL)
     RG_CUDA(h, rg::launch_cyl_geometry(s.mesh, at<double>(s.buf.p, s.lay.xarea),
                                        device_geometry ? at<double>(s.buf.p, s.lay.cd_volume) : nullptr,
-                                       h->pgeo.origin, h->pgeo.direction, h->upload_stream));
+                                       h->pgeo.origin, h->pgeo.direction, h->pgeo.unit != 0, h->upload_stream));
   rg::GeomArgs ga{};
   ga.mesh = s.mesh;
   ga.order = h->cfg.order;

@@ -199,7 +199,7 @@ struct rg_handle {
   // (rg_set_outer_box) and the point velocities of the last motion call
   rg_point_motion motion{RG_MOTION_EULERIAN, RG_EDGES_STATIONARY_BOX, 0.15, 0.02, 0, 0};
   // PhysicalGeometry (rg_set_physical_geometry), applied at each upload
-  rg_physical_geometry pgeo{RG_GEOMETRY_SLAB, {0, 0}, {0, 1}};
+  rg_physical_geometry pgeo{RG_GEOMETRY_SLAB, {0, 0}, {0, 1}, 0};
   double box[4] = {0, 0, 0, 0};
   bool have_box = false;
   rgh::DevBuf pv;

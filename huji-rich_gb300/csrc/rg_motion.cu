@@ -89,7 +89,8 @@ __device__ __forceinline__ double vabs2(double x, double y) { return sqrt(x * x 
 struct CylAxis {
   double ox, oy, dx, dy;
 };
-__device__ __forceinline__ CylAxis cyl_axis(dbl4 od) {
+__device__ __forceinline__ CylAxis cyl_axis(dbl4 od, bool unit) {
+  if (unit) return CylAxis{od.x, od.y, od.z, od.w};
   const double ab = vabs2(od.z, od.w);
   return CylAxis{od.x, od.y, od.z / ab, od.w / ab};
 }
@@ -103,9 +104,10 @@ __device__ __forceinline__ double cone_segment(double2 p1, double2 p2, const Cyl
   return (kPi / 3.) * (q2.x - q1.x) * (q1.y * q1.y + q2.y * q2.y + q1.y * q2.y);
 }
 
-__global__ void __launch_bounds__(kMoBlock) k_cyl_geometry(MeshDev m, double* xarea, double* cd_volume, dbl4 od) {
+__global__ void __launch_bounds__(kMoBlock) k_cyl_geometry(MeshDev m, double* xarea, double* cd_volume, dbl4 od,
+                                                            int unit) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const CylAxis a = cyl_axis(od);
+  const CylAxis a = cyl_axis(od, unit != 0);
   if (t < m.e) {
     // :66-71 calcArea
     const dbl4 v = m.face_vertices[t];
@@ -246,11 +248,11 @@ cudaError_t launch_device_geometry(const MeshDev& m, double2* cms, double* volum
 }
 
 cudaError_t launch_cyl_geometry(const MeshDev& m, double* xarea, double* cd_volume, const double* origin,
-                                const double* direction, cudaStream_t s) {
+                                const double* direction, bool unit, cudaStream_t s) {
   const int work = m.e > m.n ? m.e : m.n;
   if (work > 0)
-    k_cyl_geometry<<<mo_blocks(work), kMoBlock, 0, s>>>(m, xarea, cd_volume,
-                                                        make_dbl4(origin[0], origin[1], direction[0], direction[1]));
+    k_cyl_geometry<<<mo_blocks(work), kMoBlock, 0, s>>>(
+        m, xarea, cd_volume, make_dbl4(origin[0], origin[1], direction[0], direction[1]), unit ? 1 : 0);
   return cudaGetLastError();
 }
 

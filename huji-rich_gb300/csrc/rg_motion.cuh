@@ -22,7 +22,7 @@ cudaError_t launch_device_geometry(const MeshDev& m, double2* cms, double* volum
                                    int ghost_kind, const double* box, cudaStream_t s);
 // CylindricalSymmetry's CacheData face areas and (cd_volume != nullptr) cell volumes
 cudaError_t launch_cyl_geometry(const MeshDev& m, double* xarea, double* cd_volume, const double* origin,
-                                const double* direction, cudaStream_t s);
+                                const double* direction, bool unit, cudaStream_t s);
 cudaError_t launch_point_velocities(const StepArgs& a, const MotionArgs& mo, cudaStream_t s);
 cudaError_t launch_apply_fix(const StepArgs& a, const MotionArgs& mo, cudaStream_t s);
 cudaError_t launch_edge_velocities(const StepArgs& a, const MotionArgs& mo, cudaStream_t s);

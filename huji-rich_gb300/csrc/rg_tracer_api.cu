@@ -162,6 +162,16 @@ rg_status rg_set_stickers(rg_handle* h, const uint32_t* stickers) {
   return RG_OK;
 }
 
+rg_status rg_set_tracer_fluxes(rg_handle* h, const double* in) {
+  if (rg_status st = ready(h, in)) return st;
+  const size_t bytes = 8 * static_cast<size_t>(active_slot(h)->e) * h->tcfg.n_tracers;
+  if (bytes) {
+    RG_CUDA(h, cudaMemcpyAsync(h->tr_flux.p, in, bytes, cudaMemcpyHostToDevice, h->stream));
+    RG_CUDA(h, cudaStreamSynchronize(h->stream));
+  }
+  return RG_OK;
+}
+
 rg_status rg_get_tracer_fluxes(rg_handle* h, double* out) {
   if (rg_status st = ready(h, out)) return st;
   if (!h->have_fluxes) return require(h, false, false, false, true);

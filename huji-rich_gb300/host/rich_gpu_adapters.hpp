@@ -16,14 +16,20 @@
 // result back into hdsim's vectors.  A physical failure is rethrown as the
 // reference's UniversalError with its message and diagnostic entries.
 //
-// Supported: IdealGas, Hllc (massflux = true), SlabSymmetry, first order
-// (SimpleFluxCalculator) or LinearGaussImproved with RigidWallGenerator or
-// PeriodicGhostGenerator, no tracers or stickers.
+// Supported: IdealGas, Hllc (massflux = true), SlabSymmetry or
+// CylindricalSymmetry, first order (SimpleFluxCalculator) or
+// LinearGaussImproved with RigidWallGenerator or PeriodicGhostGenerator, and
+// tracers and stickers: the GpuTracerSpec names what the replaced plugins
+// were built with (LinearGaussImproved's calc_tracers and skip_key, the
+// sticker of a SimpleCellUpdater sequence {(HasSticker, SkipUpdate)}); the
+// "Entropy" tracer is recomputed as SimpleCellUpdater does.
 #ifndef RICH_GB300_ADAPTERS_HPP
 #define RICH_GB300_ADAPTERS_HPP
 
+#include <cstdint>
 #include <cstring>
 #include <stdexcept>
+#include <string>
 #include <vector>
 
 #include "rich_gb300.h"
@@ -38,9 +44,16 @@
 
 namespace rich_gb300 {
 
+// What the replaced reference plugins were constructed with.
+struct GpuTracerSpec {
+  std::vector<std::string> calc_tracers;  // LinearGaussImproved(..., calc_tracers, skip_key)
+  std::string skip_key;                   // "" = none
+  std::string frozen_sticker;             // SimpleCellUpdater's HasSticker(name) + SkipUpdate, "" = none
+};
+
 class GpuContext {
  public:
-  explicit GpuContext(const rg_config& cfg) : cfg_(cfg) {
+  explicit GpuContext(const rg_config& cfg, GpuTracerSpec spec = GpuTracerSpec()) : cfg_(cfg), spec_(spec) {
     const rg_status st = rg_create(&cfg_, &h_);
     if (st != RG_OK) throw UniversalError(std::string("rich_gb300: rg_create failed: ") + rg_status_string(st));
   }
@@ -52,6 +65,23 @@ class GpuContext {
   const rg_config& config() const { return cfg_; }
   int n_cells() const { return packed_.n_cells; }
   int n_faces() const { return packed_.n_faces; }
+
+  // The PhysicalGeometry whose CacheData areas scale the fluxes; hdsim passes
+  // it to the extensive and cell updaters, the flux calculator sees only the
+  // CacheData, so a cylindrical simulation names it up front.
+  void set_physical_geometry(const PhysicalGeometry& pg) const {
+    rg_physical_geometry g{RG_GEOMETRY_SLAB, {0, 0}, {0, 1}, 1};
+    if (const CylindricalSymmetry* c = dynamic_cast<const CylindricalSymmetry*>(&pg)) {
+      const Axis& a = c->getAxis();
+      g = rg_physical_geometry{RG_GEOMETRY_CYLINDRICAL, {a.origin.x, a.origin.y}, {a.direction.x, a.direction.y}, 1};
+    }
+    if (g.kind != pgeo_.kind || g.origin[0] != pgeo_.origin[0] || g.origin[1] != pgeo_.origin[1] ||
+        g.direction[0] != pgeo_.direction[0] || g.direction[1] != pgeo_.direction[1]) {
+      pgeo_ = g;
+      check(rg_set_physical_geometry(h_, &pgeo_));
+      have_mesh_ = false;  // the areas are formed at upload
+    }
+  }
 
   // Packs the tessellation and uploads it unless it equals the last upload.
   void sync_mesh(const Tessellation& tess, const CacheData* cd) const {
@@ -71,17 +101,56 @@ class GpuContext {
     ++mesh_generation_;
   }
 
+  // Tracer configuration from hdsim's sorted names (hdsim2d.cpp:121-136) and
+  // the spec; set once, from the first cells with tracers or stickers.
+  void sync_tracers(const std::vector<ComputationalCell>& cells, const TracerStickerNames& tsn) const {
+    const size_t nt = cells.empty() ? 0 : cells[0].tracers.size();
+    const size_t ns = cells.empty() ? 0 : cells[0].stickers.size();
+    if (nt == 0 && ns == 0) return;
+    if (nt > RG_MAX_TRACERS || ns > 32)
+      throw UniversalError("rich_gb300: more tracers or stickers than the library holds");
+    rg_tracer_config c{static_cast<int32_t>(nt), 0u, -1, -1, -1};
+    for (size_t j = 0; j < nt && j < tsn.tracer_names.size(); ++j) {
+      for (const std::string& name : spec_.calc_tracers)
+        if (name == tsn.tracer_names[j]) c.limited_mask |= 1u << j;
+      if (tsn.tracer_names[j] == "Entropy") c.entropy_tracer = static_cast<int32_t>(j);
+    }
+    for (size_t k = 0; k < ns && k < tsn.sticker_names.size(); ++k) {
+      if (!spec_.skip_key.empty() && tsn.sticker_names[k] == spec_.skip_key) c.skip_sticker = static_cast<int32_t>(k);
+      if (!spec_.frozen_sticker.empty() && tsn.sticker_names[k] == spec_.frozen_sticker)
+        c.frozen_sticker = static_cast<int32_t>(k);
+    }
+    if (!have_tcfg_ || std::memcmp(&c, &tcfg_, sizeof c) != 0) {
+      check(rg_set_tracer_config(h_, &c));
+      tcfg_ = c;
+      have_tcfg_ = true;
+    }
+  }
+  int n_tracers() const { return have_tcfg_ ? tcfg_.n_tracers : 0; }
+  bool tracers_configured() const { return have_tcfg_; }
+
   void upload_cells(const std::vector<ComputationalCell>& cells) const {
     std::vector<double> buf(4 * cells.size());
     for (size_t i = 0; i < cells.size(); ++i) {
-      if (!cells[i].tracers.empty() || !cells[i].stickers.empty())
-        throw UniversalError("rich_gb300: tracers and stickers are not supported");
       buf[4 * i] = cells[i].density;
       buf[4 * i + 1] = cells[i].pressure;
       buf[4 * i + 2] = cells[i].velocity.x;
       buf[4 * i + 3] = cells[i].velocity.y;
     }
     check(rg_set_cells(h_, buf.data()));
+    if (!have_tcfg_) return;
+    const size_t nt = static_cast<size_t>(tcfg_.n_tracers);
+    if (nt > 0) {
+      std::vector<double> tr(nt * cells.size());
+      for (size_t i = 0; i < cells.size(); ++i)
+        for (size_t j = 0; j < nt; ++j) tr[i * nt + j] = cells[i].tracers[j];
+      check(rg_set_tracers(h_, tr.data()));
+    }
+    std::vector<uint32_t> st(cells.size(), 0u);
+    for (size_t i = 0; i < cells.size(); ++i)
+      for (size_t k = 0; k < cells[i].stickers.size() && k < 32; ++k)
+        if (cells[i].stickers[k]) st[i] |= 1u << k;
+    check(rg_set_stickers(h_, st.data()));
   }
   void upload_extensives(const std::vector<Extensive>& ext) const {
     std::vector<double> buf(4 * ext.size());
@@ -92,6 +161,13 @@ class GpuContext {
       buf[4 * i + 3] = ext[i].momentum.y;
     }
     check(rg_set_extensives(h_, buf.data()));
+    const size_t nt = static_cast<size_t>(n_tracers());
+    if (nt > 0) {
+      std::vector<double> tr(nt * ext.size());
+      for (size_t i = 0; i < ext.size(); ++i)
+        for (size_t j = 0; j < nt; ++j) tr[i * nt + j] = ext[i].tracers[j];
+      check(rg_set_extensive_tracers(h_, tr.data()));
+    }
   }
   void download_extensives(std::vector<Extensive>& ext) const {
     std::vector<double> buf(4 * ext.size());
@@ -101,6 +177,15 @@ class GpuContext {
       ext[i].energy = buf[4 * i + 1];
       ext[i].momentum.x = buf[4 * i + 2];
       ext[i].momentum.y = buf[4 * i + 3];
+    }
+    const size_t nt = static_cast<size_t>(n_tracers());
+    if (nt > 0) {
+      std::vector<double> tr(nt * ext.size());
+      check(rg_get_extensive_tracers(h_, tr.data()));
+      for (size_t i = 0; i < ext.size(); ++i) {
+        ext[i].tracers.resize(nt);
+        for (size_t j = 0; j < nt; ++j) ext[i].tracers[j] = tr[i * nt + j];
+      }
     }
   }
   void upload_edge_velocities(const std::vector<Vector2D>& ev) const {
@@ -154,7 +239,11 @@ class GpuContext {
   }
 
   rg_config cfg_;
+  GpuTracerSpec spec_;
   rg_handle* h_ = nullptr;
+  mutable rg_tracer_config tcfg_{0, 0u, -1, -1, -1};
+  mutable bool have_tcfg_ = false;
+  mutable rg_physical_geometry pgeo_{RG_GEOMETRY_SLAB, {0, 0}, {0, 1}, 1};
   mutable PackedMesh packed_;
   mutable bool have_mesh_ = false;
   mutable unsigned long mesh_generation_ = 0;
@@ -169,9 +258,10 @@ class GpuCFL : public TimeStepFunction {
   explicit GpuCFL(const GpuContext& ctx) : ctx_(ctx) {}
   double operator()(const Tessellation& tess, const vector<ComputationalCell>& cells, const EquationOfState& eos,
                     const vector<Vector2D>& edge_velocities, const double /*time*/,
-                    TracerStickerNames const& /*tsn*/) const override {
+                    TracerStickerNames const& tsn) const override {
     ctx_.check_gamma(eos);
     ctx_.sync_mesh(tess, nullptr);
+    ctx_.sync_tracers(cells, tsn);
     ctx_.upload_cells(cells);
     ctx_.upload_edge_velocities(edge_velocities);
     double dt = 0;
@@ -190,9 +280,10 @@ class GpuFluxCalculator : public FluxCalculator {
   vector<Extensive> operator()(const Tessellation& tess, const vector<Vector2D>& edge_velocities,
                                const vector<ComputationalCell>& cells, const vector<Extensive>& /*extensives*/,
                                const CacheData& cd, const EquationOfState& eos, const double /*time*/,
-                               const double dt, TracerStickerNames const& /*tsn*/) const override {
+                               const double dt, TracerStickerNames const& tsn) const override {
     ctx_.check_gamma(eos);
     ctx_.sync_mesh(tess, &cd);
+    ctx_.sync_tracers(cells, tsn);
     ctx_.upload_cells(cells);
     ctx_.upload_edge_velocities(edge_velocities);
     std::vector<double> buf(4 * static_cast<size_t>(ctx_.n_faces()));
@@ -203,6 +294,12 @@ class GpuFluxCalculator : public FluxCalculator {
       res[i].energy = buf[4 * i + 1];
       res[i].momentum.x = buf[4 * i + 2];
       res[i].momentum.y = buf[4 * i + 3];
+    }
+    const size_t nt = static_cast<size_t>(ctx_.n_tracers());
+    if (nt > 0) {
+      std::vector<double> tf(nt * res.size());
+      ctx_.check(rg_get_tracer_fluxes(ctx_.handle(), tf.data()));
+      for (size_t i = 0; i < res.size(); ++i) res[i].tracers.assign(tf.begin() + i * nt, tf.begin() + (i + 1) * nt);
     }
     ctx_.mark_device_fluxes(res);
     return res;
@@ -216,10 +313,12 @@ class GpuFluxCalculator : public FluxCalculator {
 class GpuExtensiveUpdater : public ExtensiveUpdater {
  public:
   explicit GpuExtensiveUpdater(const GpuContext& ctx) : ctx_(ctx) {}
-  void operator()(const vector<Extensive>& fluxes, const PhysicalGeometry& /*pg*/, const Tessellation& tess,
-                  const double dt, const CacheData& cd, const vector<ComputationalCell>& /*cells*/,
-                  vector<Extensive>& extensives, double /*time*/, TracerStickerNames const& /*tsn*/) const override {
+  void operator()(const vector<Extensive>& fluxes, const PhysicalGeometry& pg, const Tessellation& tess,
+                  const double dt, const CacheData& cd, const vector<ComputationalCell>& cells,
+                  vector<Extensive>& extensives, double /*time*/, TracerStickerNames const& tsn) const override {
+    ctx_.set_physical_geometry(pg);
     ctx_.sync_mesh(tess, &cd);
+    ctx_.sync_tracers(cells, tsn);
     if (!ctx_.device_fluxes_match(fluxes)) {
       std::vector<double> buf(4 * fluxes.size());
       for (size_t i = 0; i < fluxes.size(); ++i) {
@@ -229,6 +328,13 @@ class GpuExtensiveUpdater : public ExtensiveUpdater {
         buf[4 * i + 3] = fluxes[i].momentum.y;
       }
       ctx_.check(rg_set_fluxes(ctx_.handle(), buf.data()));
+      const size_t nt = static_cast<size_t>(ctx_.n_tracers());
+      if (nt > 0) {
+        std::vector<double> tf(nt * fluxes.size());
+        for (size_t i = 0; i < fluxes.size(); ++i)
+          for (size_t j = 0; j < nt; ++j) tf[i * nt + j] = fluxes[i].tracers[j];
+        ctx_.check(rg_set_tracer_fluxes(ctx_.handle(), tf.data()));
+      }
     }
     ctx_.upload_extensives(extensives);
     ctx_.check(rg_extensive_update(ctx_.handle(), dt));
@@ -243,12 +349,15 @@ class GpuExtensiveUpdater : public ExtensiveUpdater {
 class GpuCellUpdater : public CellUpdater {
  public:
   explicit GpuCellUpdater(const GpuContext& ctx) : ctx_(ctx) {}
-  vector<ComputationalCell> operator()(const Tessellation& tess, const PhysicalGeometry& /*pg*/,
+  vector<ComputationalCell> operator()(const Tessellation& tess, const PhysicalGeometry& pg,
                                        const EquationOfState& eos, vector<Extensive>& extensives,
-                                       const vector<ComputationalCell>& /*old*/, const CacheData& cd,
-                                       TracerStickerNames const& /*tsn*/) const override {
+                                       const vector<ComputationalCell>& old, const CacheData& cd,
+                                       TracerStickerNames const& tsn) const override {
     ctx_.check_gamma(eos);
+    ctx_.set_physical_geometry(pg);
     ctx_.sync_mesh(tess, &cd);
+    ctx_.sync_tracers(old, tsn);
+    if (ctx_.tracers_configured()) ctx_.upload_cells(old);  // tracers / SkipUpdate read the old cells
     ctx_.upload_extensives(extensives);
     ctx_.check(rg_cell_update(ctx_.handle()));
     std::vector<double> buf(4 * extensives.size());
@@ -258,6 +367,14 @@ class GpuCellUpdater : public CellUpdater {
       res[i].density = buf[4 * i];
       res[i].pressure = buf[4 * i + 1];
       res[i].velocity = Vector2D(buf[4 * i + 2], buf[4 * i + 3]);
+      if (i < old.size()) res[i].stickers = old[i].stickers;  // simple_cell_updater.cpp:36
+    }
+    const size_t nt = static_cast<size_t>(ctx_.n_tracers());
+    if (nt > 0) {
+      std::vector<double> tr(nt * res.size());
+      ctx_.check(rg_get_tracers(ctx_.handle(), tr.data()));
+      for (size_t i = 0; i < res.size(); ++i) res[i].tracers.assign(tr.begin() + i * nt, tr.begin() + (i + 1) * nt);
+      ctx_.download_extensives(extensives);  // the entropy tracer's extensive (simple_cell_updater.cpp:47)
     }
     return res;
   }

@@ -32,7 +32,7 @@ EXPORTS = ("rg_default_config", "rg_create", "rg_destroy", "rg_status_string", "
            "rg_set_extensive_tracers", "rg_get_extensive_tracers", "rg_set_stickers",
            "rg_get_tracer_fluxes", "rg_get_tracer_slopes", "rg_set_outer_box", "rg_set_point_motion",
            "rg_point_velocities", "rg_apply_fix", "rg_get_edge_velocities", "rg_get_geometry",
-           "rg_advance_begin", "rg_set_physical_geometry")
+           "rg_advance_begin", "rg_set_physical_geometry", "rg_set_tracer_fluxes")
 
 MESH_DEVICE_GEOMETRY = 2  # RG_MESH_DEVICE_GEOMETRY
 
@@ -55,7 +55,8 @@ class RgPointMotion(C.Structure):
 
 
 class RgPhysicalGeometry(C.Structure):
-    _fields_ = [("kind", C.c_int32), ("origin", C.c_double * 2), ("direction", C.c_double * 2)]
+    _fields_ = [("kind", C.c_int32), ("origin", C.c_double * 2), ("direction", C.c_double * 2),
+                ("unit", C.c_int32)]
 
 
 class RgDeviceView(C.Structure):
@@ -133,7 +134,7 @@ def load(path=LIB_PATH):
     lib.rg3_step_timed.argtypes = [vp, dp, C.POINTER(C.c_float)]
     lib.rg_set_tracer_config.argtypes = [vp, C.POINTER(RgTracerConfig)]
     for f in ("rg_set_tracers", "rg_get_tracers", "rg_set_extensive_tracers", "rg_get_extensive_tracers",
-              "rg_get_tracer_fluxes", "rg_get_tracer_slopes"):
+              "rg_get_tracer_fluxes", "rg_get_tracer_slopes", "rg_set_tracer_fluxes"):
         getattr(lib, f).argtypes = [vp, dp]
     lib.rg_set_stickers.argtypes = [vp, C.POINTER(C.c_uint32)]
     lib.rg_set_outer_box.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double]
@@ -320,7 +321,7 @@ class Handle:
     def set_physical_geometry(self, kind=0, origin=(0.0, 0.0), direction=(0.0, 1.0)):
         """0 SlabSymmetry, 1 CylindricalSymmetry about the axis through
         origin along direction; applies from the next upload."""
-        pg = RgPhysicalGeometry(int(kind), (C.c_double * 2)(*origin), (C.c_double * 2)(*direction))
+        pg = RgPhysicalGeometry(int(kind), (C.c_double * 2)(*origin), (C.c_double * 2)(*direction), 0)
         self._check(self.lib.rg_set_physical_geometry(self.h, C.byref(pg)))
 
     def advance_begin(self, download_pv=True, out=None):

@@ -360,7 +360,9 @@ typedef enum rg_geometry_kind { RG_GEOMETRY_SLAB = 0, RG_GEOMETRY_CYLINDRICAL = 
 typedef struct rg_physical_geometry {
   int32_t kind;         /* rg_geometry_kind */
   double origin[2];     /* axis origin (CylindricalSymmetry) */
-  double direction[2];  /* axis direction, any length (Axis normalises it) */
+  double direction[2];  /* axis direction: any length (normalised as Axis's constructor does,
+                           physical_geometry.cpp:40-42), or Axis::direction itself with unit = 1 */
+  int32_t unit;         /* 1: direction is already the Axis's normalised direction */
 } rg_physical_geometry;
 rg_status rg_set_physical_geometry(rg_handle* h, const rg_physical_geometry* pg);
 /* point velocities, face velocities, dt, ApplyFix, face velocities, fluxes,
@@ -413,6 +415,8 @@ rg_status rg_get_tracers(rg_handle* h, double* tracers);
 rg_status rg_set_extensive_tracers(rg_handle* h, const double* tracers);
 rg_status rg_get_extensive_tracers(rg_handle* h, double* tracers);
 rg_status rg_set_stickers(rg_handle* h, const uint32_t* stickers);
+/* tracer fluxes computed elsewhere (the tracer part of rg_set_fluxes), n_faces*n_tracers */
+rg_status rg_set_tracer_fluxes(rg_handle* h, const double* tracer_fluxes);
 /* after rg_flux: the unscaled tracer fluxes and the tracer slopes (order 2) */
 rg_status rg_get_tracer_fluxes(rg_handle* h, double* tracer_fluxes);
 rg_status rg_get_tracer_slopes(rg_handle* h, double* tracer_slopes);
