@@ -16,8 +16,10 @@
 //                 extensive / mass and the "Entropy" tracer
 //                 (simple_cell_updater.cpp:22-59), or the old tracers of a
 //                 SkipUpdate cell
-// Tracers are cell-major (cell i's tracer j at i*nt + j); the loops over j
-// run to kMaxTracers with a guard so the per-cell arrays stay in registers.
+// Tracers are cell-major (cell i's tracer j at i*nt + j).  The per-cell
+// kernels are instantiated for each tracer count NT (1..kMaxTracers) so their
+// loops over tracers have exact compile-time bounds: the per-cell arrays stay
+// in registers and no FP64 work is spent on absent tracers.
 #include <math.h>
 
 #include "rg_fp64.cuh"
@@ -32,11 +34,13 @@ __device__ __forceinline__ const double* tracers_of(const StepArgs& a, const Tra
 }
 
 // LinearGaussImproved.cpp:425-494 calc_slope, tracer part, for cell i.
+template <int NT>
 __global__ void __launch_bounds__(kTrBlock) k_tr_slopes(StepArgs a, TracerArgs t) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const MeshDev& m = a.mesh;
   if (i >= m.n) return;
-  const int nt = t.nt;
+  constexpr int nt = NT;
+  constexpr int kMaxTracers = NT;
   const int b = m.cell_off[i], nn = m.cell_off[i + 1] - b;
   const dbl4 mi = a.geom.minv[i];
   double ct[kMaxTracers], sx[kMaxTracers], sy[kMaxTracers];
@@ -232,12 +236,14 @@ __global__ void __launch_bounds__(kTrBlock) k_tr_faces_pcm(StepArgs a, TracerArg
 // SimpleExtensiveUpdater for the extensive tracers (gather in ascending face
 // order) and SimpleCellUpdater's tracer part; runs after the hydro update,
 // whose new mass, density and pressure it reads.
+template <int NT>
 __global__ void __launch_bounds__(kTrBlock) k_tr_update(StepArgs a, TracerArgs t, int from_unscaled, int do_ext,
                                                          int do_cells) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const MeshDev& m = a.mesh;
   if (i >= m.n) return;
-  const int nt = t.nt;
+  constexpr int nt = NT;
+  constexpr int kMaxTracers = NT;
   double te[kMaxTracers];
   double* ext_t = t.tr_ext + static_cast<size_t>(i) * nt;
 #pragma unroll
@@ -297,8 +303,24 @@ inline int tr_blocks(int n) { return (n + kTrBlock - 1) / kTrBlock; }
 
 }  // namespace
 
+// kernel K instantiated for NT = t.nt
+#define RG_TR_DISPATCH(K, grid, s, ...)                                  \
+  switch (t.nt) {                                                         \
+    case 1: K<1><<<grid, kTrBlock, 0, s>>>(__VA_ARGS__); break;           \
+    case 2: K<2><<<grid, kTrBlock, 0, s>>>(__VA_ARGS__); break;           \
+    case 3: K<3><<<grid, kTrBlock, 0, s>>>(__VA_ARGS__); break;           \
+    case 4: K<4><<<grid, kTrBlock, 0, s>>>(__VA_ARGS__); break;           \
+    case 5: K<5><<<grid, kTrBlock, 0, s>>>(__VA_ARGS__); break;           \
+    case 6: K<6><<<grid, kTrBlock, 0, s>>>(__VA_ARGS__); break;           \
+    case 7: K<7><<<grid, kTrBlock, 0, s>>>(__VA_ARGS__); break;           \
+    case 8: K<8><<<grid, kTrBlock, 0, s>>>(__VA_ARGS__); break;           \
+    default: break;                                                       \
+  }
+
 cudaError_t launch_tr_slopes(const StepArgs& a, const TracerArgs& t, cudaStream_t s) {
-  if (a.mesh.n > 0 && t.nt > 0) k_tr_slopes<<<tr_blocks(a.mesh.n), kTrBlock, 0, s>>>(a, t);
+  if (a.mesh.n > 0 && t.nt > 0 && t.nt <= kMaxTracers) {
+    RG_TR_DISPATCH(k_tr_slopes, tr_blocks(a.mesh.n), s, a, t)
+  }
   return cudaGetLastError();
 }
 
@@ -314,9 +336,10 @@ cudaError_t launch_tr_faces(const StepArgs& a, const TracerArgs& t, cudaStream_t
 
 cudaError_t launch_tr_update(const StepArgs& a, const TracerArgs& t, cudaStream_t s, bool from_unscaled,
                              bool extensive, bool cells) {
-  if (a.mesh.n > 0 && t.nt > 0)
-    k_tr_update<<<tr_blocks(a.mesh.n), kTrBlock, 0, s>>>(a, t, from_unscaled ? 1 : 0, extensive ? 1 : 0,
-                                                         cells ? 1 : 0);
+  if (a.mesh.n > 0 && t.nt > 0 && t.nt <= kMaxTracers) {
+    const int fu = from_unscaled ? 1 : 0, ex = extensive ? 1 : 0, ce = cells ? 1 : 0;
+    RG_TR_DISPATCH(k_tr_update, tr_blocks(a.mesh.n), s, a, t, fu, ex, ce)
+  }
   return cudaGetLastError();
 }
 
