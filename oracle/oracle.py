@@ -179,6 +179,52 @@ def run_fixed_dt(mesh, cells, gamma, steps, dt, lp=None):
     return cells, ext
 
 
+# ---------------------------------------------------------------- condition/action flux schemes
+
+class RoFluxRule(C.Structure):
+    _fields_ = [("seq", C.c_int32), ("cond", C.c_int32), ("sticker", C.c_int32), ("action", C.c_int32),
+                ("in_", C.c_int32)]
+
+
+def _rules(rows):
+    rows = np.asarray(rows, dtype=np.int32).reshape(-1, 5)
+    arr = (RoFluxRule * len(rows))(*[RoFluxRule(*map(int, r)) for r in rows])
+    return arr, len(rows)
+
+
+def _stickers(st):
+    if st is None:
+        return None, None
+    st = np.ascontiguousarray(st, dtype=np.uint32)
+    return st, st.ctypes.data_as(C.POINTER(C.c_uint32))
+
+
+def cas_flux(mesh, cells, ev, gamma, order, lp, rules, stickers=None):
+    """Fluxes of ConditionActionSequence (order 1) / ConditionActionSequence2
+    (order 2, LinearGaussImproved face states) with the given rule rows."""
+    out = np.zeros((mesh.n_faces, 4))
+    arr, nr = _rules(rules)
+    st, stp = _stickers(stickers)
+    err = RoError()
+    _check(lib().ro_cas_flux(C.byref(mesh.view()), _d(_f64(cells)), _d(_f64(ev)), C.c_double(gamma), C.c_int(order),
+                             C.byref(lp), arr, C.c_int(nr), stp, _d(out), C.byref(err)), err)
+    return out
+
+
+def run_cas(mesh, cells, ext, ev, gamma, steps, order, lp, rules, stickers=None, frozen_mask=0, cfl_number=0.3):
+    cells, ext = _f64(cells).copy(), _f64(ext).copy()
+    arr, nr = _rules(rules)
+    st, stp = _stickers(stickers)
+    dts = []
+    for _ in range(steps):
+        dt, err = C.c_double(), RoError()
+        _check(lib().ro_step_cas(C.byref(mesh.view()), _d(cells), _d(ext), _d(_f64(ev)), C.c_double(gamma),
+                                 C.c_double(cfl_number), C.c_int(order), C.byref(lp), arr, C.c_int(nr), stp,
+                                 C.c_uint32(frozen_mask), C.byref(dt), C.byref(err)), err)
+        dts.append(dt.value)
+    return cells, ext, np.array(dts)
+
+
 # ---------------------------------------------------------------- geometry and point motion
 
 class RoMotion(C.Structure):

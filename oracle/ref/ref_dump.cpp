@@ -44,6 +44,8 @@
 #include "source/newtonian/two_dimensional/geometric_outer_boundaries/SquareBox.hpp"
 #include "source/newtonian/two_dimensional/ghost_point_generators/PeriodicGhostGenerator.hpp"
 #include "source/newtonian/two_dimensional/ghost_point_generators/RigidWallGenerator.hpp"
+#include "source/newtonian/two_dimensional/condition_action_sequence.hpp"
+#include "source/newtonian/two_dimensional/condition_action_sequence_2.hpp"
 #include "source/newtonian/two_dimensional/hdsim2d.hpp"
 #include "source/newtonian/two_dimensional/interpolations/LinearGaussImproved.hpp"
 #include "source/newtonian/two_dimensional/modular_flux_calculator.hpp"
@@ -70,6 +72,12 @@ double g_box[4] = {0, 0, 0, 0};  // the OuterBoundary's (left, right, down, up)
 double g_motion[6] = {0, 0, 0, 0, 0, 0};
 // the PhysicalGeometry: kind (0 SlabSymmetry, 1 CylindricalSymmetry), axis origin, axis direction
 double g_geometry[5] = {0, 0, 0, 0, 0};
+// condition/action flux rules, one row each: sequence (0 ConditionActionSequence's
+// first-order list, 1 ConditionActionSequence2's list), condition (0
+// IsBoundaryEdge, 1 IsBulkEdge, 2 RegularSpecialEdge), sticker bit, action (0
+// RegularFlux, 1 RigidWallFlux, 2 FreeFlowFlux, 3 RegularFlux2, 4
+// RigidWallFlux2, 5 Ratchet), Ratchet's `in`
+std::vector<int32_t> g_rules;
 
 void advance(hdsim& sim) {
   if (g_heun)
@@ -214,6 +222,7 @@ void dump_components(hdsim& sim, const PhysicalGeometry& pg, const EquationOfSta
   dump_f64("outer_box", std::vector<double>(g_box, g_box + 4), 0);
   dump_f64("motion", std::vector<double>(g_motion, g_motion + 6), 0);
   dump_f64("geometry", std::vector<double>(g_geometry, g_geometry + 5), 0);
+  if (!g_rules.empty()) dump_i32("flux_rules", g_rules, 5);
   vector<Vector2D> pv = pm(tess, cells, t, tsn);
   vector<Vector2D> ev = evc(tess, pv);
   const double dt = tsf(tess, cells, eos, ev, t, tsn);
@@ -452,6 +461,88 @@ int main(int argc, char** argv) {
       dump_scalar("order", 2);
       dump_scalar("ghost_kind", 1);
       dump_components(sim, pg, eos, pm, evc, tsf, fc, eu, cu, &sr);
+      if (run > 0) run_and_dump(sim, run);
+    } else if (which == "cas_free" || which == "cas2_wall" || which == "cas2_ratchet") {
+      // Condition/action flux schemes on [0,1]^2 with reflecting-wall ghosts:
+      //  cas_free: ConditionActionSequence (first order) {(IsBoundaryEdge,
+      //    FreeFlowFlux), (RegularSpecialEdge("obstacle"), RigidWallFlux),
+      //    (IsBulkEdge, RegularFlux)}, a diagonal Sod problem around an
+      //    obstacle disc;
+      //  cas2_wall: ConditionActionSequence2 {} then {(IsBoundaryEdge,
+      //    RigidWallFlux2), (RegularSpecialEdge("obstacle"), RigidWallFlux2),
+      //    (IsBulkEdge, RegularFlux2)} with LinearGaussImproved, flow past an
+      //    obstacle disc (RegularSpecialEdge reads both neighbours' cells, so
+      //    boundary edges are matched first);
+      //  cas2_ratchet: ConditionActionSequence2 {} then {(IsBoundaryEdge,
+      //    Ratchet(out)), (IsBulkEdge, RegularFlux2)}, a blast venting through
+      //    the walls.
+      SquareBox outer(Vector2D(0, 0), Vector2D(1, 1));
+      g_box[0] = 0, g_box[1] = 1, g_box[2] = 0, g_box[3] = 1;
+      VoronoiMesh tess(jittered_lattice(nx, ny, 0, 1, 0, 1, 6, 1e-3), outer);
+      IdealGas eos(5. / 3.);
+      Eulerian eul;
+      StationaryBox evc;
+      RigidWallGenerator gpg;
+      LinearGaussImproved sr(eos, gpg);
+      typedef ConditionActionSequence CAS;
+      vector<pair<const CAS::Condition*, const CAS::Action*> > seq1;
+      vector<pair<const CAS::Condition*, const ConditionActionSequence2::Action2*> > seq2;
+      const bool first = which == "cas_free";
+      if (first) {
+        seq1.push_back({new IsBoundaryEdge(), new FreeFlowFlux(rs)});
+        seq1.push_back({new RegularSpecialEdge("obstacle"), new RigidWallFlux(rs)});
+        seq1.push_back({new IsBulkEdge(), new RegularFlux(rs)});
+        g_rules = {0, 0, -1, 2, 0, 0, 2, 0, 1, 0, 0, 1, -1, 0, 0};
+      } else if (which == "cas2_wall") {
+        seq2.push_back({new IsBoundaryEdge(), new RigidWallFlux2(rs)});
+        seq2.push_back({new RegularSpecialEdge("obstacle"), new RigidWallFlux2(rs)});
+        seq2.push_back({new IsBulkEdge(), new RegularFlux2(rs)});
+        g_rules = {1, 0, -1, 4, 0, 1, 2, 0, 4, 0, 1, 1, -1, 3, 0};
+      } else {
+        seq2.push_back({new IsBoundaryEdge(), new Ratchet(rs, false)});
+        seq2.push_back({new IsBulkEdge(), new RegularFlux2(rs)});
+        g_rules = {1, 0, -1, 5, 0, 1, 1, -1, 3, 0};
+      }
+      CAS fc1(seq1);
+      ConditionActionSequence2 fc2(seq1, seq2, sr);
+      const FluxCalculator& fc = first ? static_cast<const FluxCalculator&>(fc1)
+                                       : static_cast<const FluxCalculator&>(fc2);
+      const bool obstacle = which != "cas2_ratchet";
+      const TracerStickerNames names = obstacle ? TracerStickerNames({}, {"obstacle"}) : TracerStickerNames();
+      vector<ComputationalCell> ic(static_cast<size_t>(tess.GetPointNo()));
+      for (size_t i = 0; i < ic.size(); ++i) {
+        const Vector2D r = tess.GetMeshPoint(static_cast<int>(i));
+        if (first) {
+          const bool left = r.x + r.y < 1;
+          ic[i].density = left ? 1 : 0.125;
+          ic[i].pressure = left ? 1 : 0.1;
+          ic[i].stickers = {abs(r - Vector2D(0.6, 0.6)) < 0.12};
+        } else if (which == "cas2_wall") {
+          ic[i].density = 1;
+          ic[i].pressure = 1;
+          ic[i].velocity = Vector2D(0.6, 0.1);
+          ic[i].stickers = {abs(r - Vector2D(0.45, 0.5)) < 0.15};
+        } else {
+          ic[i].density = 1;
+          ic[i].pressure = abs(r - Vector2D(0.5, 0.5)) < 0.2 ? 5.0 : 0.5;
+          ic[i].velocity = Vector2D(0.3 * (r.x - 0.5), 0.3 * (r.y - 0.5));
+        }
+      }
+      // obstacle cells keep their state (HasSticker + SkipUpdate)
+      vector<pair<const SimpleCellUpdater::Condition*, const SimpleCellUpdater::Action*> > keep;
+      if (obstacle) keep.push_back({new HasSticker("obstacle"), new SkipUpdate()});
+      SimpleCellUpdater ocu(keep);
+      hdsim sim(tess, outer, pg, ic, eos, eul, evc, force, tsf, fc, eu, ocu, names);
+      for (int s = 0; s < warm; ++s) advance(sim);
+      dump_scalar("gamma", 5. / 3.);
+      dump_scalar("order", first ? 1 : 2);
+      dump_scalar("ghost_kind", 0);
+      if (obstacle) {
+        std::vector<int32_t> st;
+        for (const auto& c : sim.getAllCells()) st.push_back(c.stickers[0] ? 1 : 0);
+        dump_i32("tr_stickers", st, 0);
+      }
+      dump_components(sim, pg, eos, eul, evc, tsf, fc, eu, ocu, first ? nullptr : &sr);
       if (run > 0) run_and_dump(sim, run);
     } else if (which == "cyl_blast") {
       // Cylindrical symmetry about the y axis (r = x) on [0,1]^2: a blast at

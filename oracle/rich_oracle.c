@@ -1089,6 +1089,132 @@ void ro_cell_geometry(const rg_mesh_view* m, int ghost_kind, const double* box, 
   }
 }
 
+/* ---------------- condition/action flux schemes ---------------- */
+
+/* geometry.cpp normalize: v/abs(v) */
+static v2 vnormalize(v2 v) { return vdiv(v, vabs(v)); }
+
+static int has_sticker(const uint32_t* st, const rg_mesh_view* m, int p, int bit) {
+  return st && bit >= 0 && ((st[orig(m, p)] >> bit) & 1u);
+}
+
+/* condition_action_sequence.cpp:228-289: (applies, aux) */
+static int cas_condition(const rg_mesh_view* m, const ro_flux_rule* r, int e, const uint32_t* st, int* aux) {
+  const int N = m->n_cells, a = fc0(m, e), b = fc1(m, e);
+  *aux = 0;
+  if (r->cond == 0) { /* IsBoundaryEdge, serial build */
+    if (a < 0 || a >= N) return 1;
+    if (b < 0 || b >= N) { *aux = 1; return 1; }
+    return 0;
+  }
+  if (r->cond == 1) /* IsBulkEdge */
+    return a >= 0 && b >= 0 && ((a < N && b < N) || orig(m, a) != orig(m, b));
+  /* RegularSpecialEdge: exactly one side carries the sticker; aux = the second does */
+  const int sa = has_sticker(st, m, a, r->sticker), sb = has_sticker(st, m, b, r->sticker);
+  if (sa) return !sb;
+  if (sb) { *aux = 1; return 1; }
+  return 0;
+}
+
+/* condition_action_sequence.cpp:127-138 rigid_wall_states */
+static void wall_states(prim s, v2 p, int aux, prim* l, prim* r) {
+  if (aux) { *l = s; *r = reflect(s, p); }
+  else { *r = s; *l = reflect(s, p); }
+}
+
+/* the wall frame of RigidWallFlux / FreeFlowFlux (:140-158, :186-204) */
+static v2 wall_normal(const rg_mesh_view* m, int e, int aux, v2 p) {
+  const v2 w = aux ? vsub(vert0(m, e), point(m, fc0(m, e))) : vsub(point(m, fc1(m, e)), vert0(m, e));
+  return vnormalize(remove_parallel(w, p));
+}
+
+int ro_cas_flux(const rg_mesh_view* m, const double* cells, const double* ev, double g, int order,
+                const ro_lgi_params* lp, const ro_flux_rule* rules, int n_rules, const uint32_t* st,
+                double* fluxes, ro_error* err) {
+  double* ip = NULL;
+  int rc = 0;
+  if (order == 2) {
+    ip = (double*)malloc(sizeof(double) * 8 * (size_t)(m->n_faces > 0 ? m->n_faces : 1));
+    rc = ro_lgi(m, cells, g, lp, NULL, ip, err);
+  }
+  for (int e = 0; e < m->n_faces && !rc; ++e) {
+    const int a = fc0(m, e), b = fc1(m, e);
+    int chosen = -1, aux = 0;
+    for (int pass = 0; pass < 2 && chosen < 0; ++pass)
+      for (int k = 0; k < n_rules && chosen < 0; ++k)
+        if (rules[k].seq == pass && cas_condition(m, &rules[k], e, st, &aux)) chosen = k;
+    if (chosen < 0) { /* condition_action_sequence_2.cpp:73 "Error in ConditionActionSequence" */
+      set_err(err, RG_ERR_INVALID_ARGUMENT, 3, e, 0);
+      rc = RG_ERR_INVALID_ARGUMENT;
+      break;
+    }
+    const ro_flux_rule* r = &rules[chosen];
+    const v2 p = vnormalize(vsub(vert1(m, e), vert0(m, e)));
+    const v2 w = {ev[2 * e], ev[2 * e + 1]};
+    const cc c0 = cell_at(cells, orig(m, a)), c1 = cell_at(cells, orig(m, b));
+    const cc s0 = ip ? get_cc(ip + 8 * e) : c0, s1 = ip ? get_cc(ip + 8 * e + 4) : c1;
+    int action = r->action;
+    if (action == 5) {
+      /* condition_action_sequence_2.cpp:232-249 Ratchet */
+      const v2 nn = aux ? vsub(point(m, b), point(m, a)) : vsub(point(m, a), point(m, b));
+      const cc sc = aux ? c0 : c1;
+      const v2 vel = {sc.vx, sc.vy};
+      action = dot(nn, vel) * (2 * (double)(r->in != 0) - 1) < 0 ? 2 : 4;
+    }
+    cons c;
+    prim l, rr;
+    v2 n;
+    double v = 0;
+    if (action == 0 || action == 3) {
+      /* RegularFlux (condition_action_sequence.cpp:84-110), RegularFlux2
+       * (condition_action_sequence_2.cpp:129-157) */
+      n = vnormalize(vsub(point(m, b), point(m, a)));
+      v = dot(n, w);
+      l = to_prim(g, action == 0 ? c0 : s0);
+      rr = to_prim(g, action == 0 ? c1 : s1);
+    } else if (action == 1 || action == 4) {
+      /* RigidWallFlux (:140-184), RigidWallFlux2 (:183-228) */
+      n = wall_normal(m, e, aux, p);
+      const cc sc = action == 1 ? (aux ? c0 : c1) : (aux ? s0 : s1);
+      wall_states(to_prim(g, sc), p, aux, &l, &rr);
+    } else {
+      /* FreeFlowFlux (:186-220) */
+      n = wall_normal(m, e, aux, p);
+      l = rr = to_prim(g, aux ? c0 : c1);
+    }
+    rc = rotate_solve_rotate_back(l, rr, v, n, p, &c, e, err);
+    if (!rc) put_flux(fluxes + 4 * e, c);
+  }
+  free(ip);
+  return rc;
+}
+
+int ro_step_cas(const rg_mesh_view* m, double* cells, double* ext, const double* ev, double g, double cfl,
+                int order, const ro_lgi_params* lp, const ro_flux_rule* rules, int n_rules, const uint32_t* st,
+                uint32_t frozen_mask, double* dt_out, ro_error* err) {
+  double dt;
+  int rc = ro_cfl(m, cells, ev, g, cfl, &dt, err);
+  if (rc) return rc;
+  const size_t N = (size_t)m->n_cells;
+  double* fl = (double*)malloc(sizeof(double) * 4 * (size_t)(m->n_faces > 0 ? m->n_faces : 1));
+  double* old = (double*)malloc(sizeof(double) * 4 * N);
+  memcpy(old, cells, sizeof(double) * 4 * N);
+  rc = ro_cas_flux(m, cells, ev, g, order, lp, rules, n_rules, st, fl, err);
+  if (!rc) rc = ro_extensive_update(m, fl, dt, ext, err);
+  if (!rc) {
+    ro_tracers t;
+    memset(&t, 0, sizeof t);
+    t.entropy = -1;
+    t.frozen_mask = frozen_mask;
+    t.stickers = st;
+    rc = ro_cell_update_tr(m, ext, NULL, old, NULL, g, &t, cells, NULL, err);
+  }
+  free(fl);
+  free(old);
+  if (dt_out) *dt_out = dt;
+  return rc;
+}
+
 /* physical_geometry.cpp:44-60 Axis and change_coordinate: (along, |across|) */
 typedef struct { v2 origin, dir; } axis2;
 static v2 change_coordinate(v2 v, axis2 a) {

@@ -102,6 +102,25 @@ int ro_step_tr(const rg_mesh_view* m, double* cells, double* ext, double* tr, do
 void ro_cell_geometry(const rg_mesh_view* m, int ghost_kind, const double* box, double* volume, double* cm_xy,
                       double* cd_volume);
 
+/* Condition/action flux schemes: ConditionActionSequence
+ * (condition_action_sequence.cpp) and ConditionActionSequence2
+ * (condition_action_sequence_2.cpp).  A rule: seq 0 (the first-order list,
+ * evaluated first) or 1 (ConditionActionSequence2's list); cond 0
+ * IsBoundaryEdge, 1 IsBulkEdge, 2 RegularSpecialEdge(sticker bit); action 0
+ * RegularFlux, 1 RigidWallFlux, 2 FreeFlowFlux (cell states), 3 RegularFlux2,
+ * 4 RigidWallFlux2, 5 Ratchet(in) (LinearGaussImproved face states, lp). */
+typedef struct ro_flux_rule {
+  int32_t seq, cond, sticker, action, in;
+} ro_flux_rule;
+int ro_cas_flux(const rg_mesh_view* m, const double* cells, const double* ev, double gamma, int order,
+                const ro_lgi_params* lp, const ro_flux_rule* rules, int n_rules, const uint32_t* stickers,
+                double* fluxes, ro_error* err);
+/* hdsim::TimeAdvance with a condition/action flux calculator on a fixed
+ * mesh; cells with a bit of frozen_mask keep their state (SkipUpdate) */
+int ro_step_cas(const rg_mesh_view* m, double* cells, double* ext, const double* ev, double gamma, double cfl,
+                int order, const ro_lgi_params* lp, const ro_flux_rule* rules, int n_rules, const uint32_t* stickers,
+                uint32_t frozen_mask, double* dt_out, ro_error* err);
+
 /* CylindricalSymmetry (physical_geometry.cpp:62-110) about the axis through
  * origin along direction (normalised as Axis does): CacheData's face areas
  * (n_faces) and cell volumes (n_cells). */

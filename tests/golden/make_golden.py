@@ -51,6 +51,11 @@ CASES = {
     "wallflow_cold_o2": ("wallflow_cold", 24, 24, 2, 0),
     # CylindricalSymmetry (axis x = 0) face areas and cell volumes: one pass + 10 steps
     "cyl_blast_o2": ("cyl_blast", 24, 24, 2, 10),
+    # condition/action flux schemes: free-flow walls (first order), rigid
+    # walls and a rigid obstacle of "obstacle"-sticker cells, outflow ratchets
+    "cas_free_o1": ("cas_free", 24, 24, 2, 10),
+    "cas2_wall_o2": ("cas2_wall", 24, 24, 2, 10),
+    "cas2_ratchet_o2": ("cas2_ratchet", 24, 24, 2, 10),
 }
 
 # Tracers and stickers (ref_dump's <case>_tracers forms), written to

@@ -41,9 +41,21 @@ def test_cfl(golden):
     assert dt == g["dt"]
 
 
+def flux_rules(g):
+    """The case's condition/action flux rules, or None (Simple/ModularFluxCalculator)."""
+    return g.get("flux_rules")
+
+
+def stickers_of(g):
+    return g["tr_stickers"].astype(np.uint32) if "tr_stickers" in g else None
+
+
 def test_fluxes(golden):
     g = golden
-    if g["order"] == 1:
+    if flux_rules(g) is not None:
+        f = oracle.cas_flux(g["mesh"], g["cells0"], g["ev_flux"], g["gamma"], g["order"], lp_of(g), flux_rules(g),
+                            stickers_of(g))
+    elif g["order"] == 1:
         f = oracle.simple_flux(g["mesh"], g["cells0"], g["ev_flux"], g["gamma"])
     else:
         f = oracle.modular_flux(g["mesh"], g["cells0"], g["ev_flux"], g["gamma"], lp_of(g))
@@ -82,6 +94,13 @@ def test_extensive_update(golden):
 
 def test_cell_update(golden):
     g = golden
+    if flux_rules(g) is not None and stickers_of(g) is not None:
+        # obstacle cells keep their state (HasSticker + SkipUpdate)
+        ts = oracle.TracerSetup(0, frozen_sticker=0, stickers=stickers_of(g))
+        cells, _, _ = oracle.cell_update_tr(g["mesh"], g["ext1"], np.zeros((g["mesh"].n_cells, 0)), g["cells0"],
+                                            np.zeros((g["mesh"].n_cells, 0)), g["gamma"], ts)
+        exact(cells, g["cells1"])
+        return
     exact(oracle.cell_update(g["mesh"], g["ext1"], g["gamma"]), g["cells1"])
 
 
@@ -94,8 +113,13 @@ def test_hdsim_run(golden):
     assert "run_mesh_unchanged" in g
     steps = int(g["case_params"][3])
     ev = np.zeros((g["mesh"].n_faces, 2))
-    cells, ext, dts = oracle.run(g["mesh"], g["cells0"], g["ext0"], ev, g["gamma"], steps,
-                                 0.3, g["order"], lp_of(g), heun=g["heun"], areas=areas_of(g))
+    if flux_rules(g) is not None:
+        st = stickers_of(g)
+        cells, ext, dts = oracle.run_cas(g["mesh"], g["cells0"], g["ext0"], ev, g["gamma"], steps, g["order"],
+                                         lp_of(g), flux_rules(g), st, 1 if st is not None else 0)
+    else:
+        cells, ext, dts = oracle.run(g["mesh"], g["cells0"], g["ext0"], ev, g["gamma"], steps,
+                                     0.3, g["order"], lp_of(g), heun=g["heun"], areas=areas_of(g))
     exact(accumulate(float(g["time0"][0]), dts), g["run_times"])
     exact(ext, g["run_ext"])
     exact(cells, g["run_cells"])
