@@ -70,7 +70,7 @@ T* ptr(DevBuf& b, size_t elem_offset = 0) {
 
 rg_status check_config(rg_handle* h) {
   if (h->cfg.order != 2 || h->cfg.ghost_kind != RG_GHOST_PERIODIC || h->mixed || h->heun || h->n_problems > 0 ||
-      tracers_on(h) || active_slot(h)->lay.own_xarea)
+      tracers_on(h) || active_slot(h)->lay.own_xarea || h->n_rules > 0)
     return invalid(h, -10, h->cfg.order);
   return RG_OK;
 }

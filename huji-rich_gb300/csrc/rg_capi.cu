@@ -203,6 +203,15 @@ rg::StepArgs step_args(rg_handle* h) {
     a.dt_p = static_cast<double*>(h->dt_p.p);
     a.n_problems = h->n_problems;
   }
+  a.n_rules = h->n_rules;
+  for (int k = 0; k < h->n_rules; ++k) {
+    const rg_flux_rule& r = h->rules[k];
+    a.rules[k][0] = r.sequence;
+    a.rules[k][1] = r.condition;
+    a.rules[k][2] = r.sticker;
+    a.rules[k][3] = r.action;
+    a.rules[k][4] = r.ratchet_in;
+  }
   if (tracers_on(h)) {
     a.stickers = static_cast<const uint32_t*>(h->stickers.p);
     a.skip_mask = h->tcfg.skip_sticker >= 0 ? 1u << h->tcfg.skip_sticker : 0u;
@@ -1047,7 +1056,7 @@ rg_status rg_set_problems(rg_handle* h, int32_t P, const int32_t* offsets, const
     h->n_problems = 0;
     return RG_OK;
   }
-  if (P < 0 || !offsets || !gamma || h->heun || tracers_on(h)) return invalid(h, -1, P);
+  if (P < 0 || !offsets || !gamma || h->heun || tracers_on(h) || h->n_rules > 0) return invalid(h, -1, P);
   if (offsets[0] != 0 || offsets[P] != s->n) return invalid(h, -2, offsets[P]);
   for (int p = 0; p < P; ++p) {
     if (offsets[p + 1] <= offsets[p]) return invalid(h, p, offsets[p + 1]);

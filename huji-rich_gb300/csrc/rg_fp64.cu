@@ -560,6 +560,145 @@ __global__ void __launch_bounds__(kMaxBlock) k_faces_pcm(StepArgs a) {
     k_faces_pcm_item<kScaled, kBatch>(a, e);
 }
 
+// ---------------------------------------------------------------- condition/action fluxes
+
+// geometry.cpp normalize: v/abs(v)
+__device__ __forceinline__ double2 normalize2(double x, double y) {
+  const double ab = sqrt(x * x + y * y);
+  return make_double2(x / ab, y / ab);
+}
+// simple_flux_calculator.cpp:27-31 remove_parallel_component, then normalize
+__device__ __forceinline__ double2 wall_normal(double wx, double wy, double2 p) {
+  const double s = wx * p.x + wy * p.y, pp = p.x * p.x + p.y * p.y;
+  return normalize2(wx - (p.x * s) / pp, wy - (p.y * s) / pp);
+}
+__device__ __forceinline__ bool has_sticker(const StepArgs& a, int p, int bit) {
+  return a.stickers != nullptr && ((a.stickers[orig_of(a.mesh, p)] >> bit) & 1u) != 0;
+}
+
+// One face of ConditionActionSequence (condition_action_sequence.cpp:17-61)
+// or ConditionActionSequence2 (condition_action_sequence_2.cpp:40-127): the
+// first rule of sequence 0, else of sequence 1, whose condition holds picks
+// the action; cell states are the cells' own records (a periodic ghost reads
+// its source cell), face states LinearGaussImproved's (order 2).
+template <bool kScaled>
+__device__ __forceinline__ void k_faces_cas_item(const StepArgs& a, int e) {
+  const MeshDev& m = a.mesh;
+  const int2 fc = m.face_cells[e];
+  int chosen = -1;
+  bool aux = false;
+  for (int pass = 0; pass < 2 && chosen < 0; ++pass) {
+    for (int k = 0; k < a.n_rules && chosen < 0; ++k) {
+      if (a.rules[k][0] != pass) continue;
+      const int cond = a.rules[k][1];
+      bool applies = false, ax = false;
+      if (cond == RG_COND_BOUNDARY_EDGE) {  // :228-253, serial build
+        if (fc.x >= m.n) applies = true;
+        else if (fc.y >= m.n) applies = ax = true;
+      } else if (cond == RG_COND_BULK_EDGE) {  // :255-271
+        applies = (fc.x < m.n && fc.y < m.n) || orig_of(m, fc.x) != orig_of(m, fc.y);
+      } else {  // :273-289 RegularSpecialEdge: exactly one side carries the sticker
+        const bool sa = has_sticker(a, fc.x, a.rules[k][2]), sb = has_sticker(a, fc.y, a.rules[k][2]);
+        applies = sa ? !sb : sb;
+        ax = !sa && sb;
+      }
+      if (applies) {
+        chosen = k;
+        aux = ax;
+      }
+    }
+  }
+  if (chosen < 0) {  // "Error in ConditionActionSequence"
+    record_error(a.status, a.step, RG_ERR_INVALID_ARGUMENT, 3, e, 0.0);
+    return;
+  }
+  const dbl4 v = m.face_vertices[e];
+  const double2 p = normalize2(v.z - v.x, v.w - v.y);
+  const double pa = sqrt(p.x * p.x + p.y * p.y);
+  const double g = a.gamma;
+  const Cell c0 = load_cell(a.cells, orig_of(m, fc.x)), c1 = load_cell(a.cells, orig_of(m, fc.y));
+  int action = a.rules[chosen][3];
+  if (action == RG_ACT_RATCHET) {
+    // condition_action_sequence_2.cpp:232-249
+    const double2 x0 = m.points[fc.x], x1 = m.points[fc.y];
+    const double nx = aux ? x1.x - x0.x : x0.x - x1.x, ny = aux ? x1.y - x0.y : x0.y - x1.y;
+    const Cell& sc = aux ? c0 : c1;
+    const double sign = 2.0 * (a.rules[chosen][4] != 0 ? 1.0 : 0.0) - 1.0;
+    action = (nx * sc.vx + ny * sc.vy) * sign < 0 ? RG_ACT_FREE_FLOW : RG_ACT_RIGID_WALL2;
+  }
+  // LinearGaussImproved face states (order 2), as k_faces_lgi_item forms them
+  Cell s0 = c0, s1 = c1;
+  if (action == RG_ACT_REGULAR2 || action == RG_ACT_RIGID_WALL2) {
+    const int ids[2] = {fc.x, fc.y};
+    const double2 dms[2] = {a.geom.dm0[e], a.geom.dm1[e]};
+    Cell side[2];
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const int pid = ids[s];
+      Cell c = point_state(a, pid);
+      int sid = pid;
+      bool zero = false;
+      if (pid >= m.n) {
+        if (a.ghost_kind == RG_GHOST_PERIODIC)
+          sid = m.ghost_source[pid - m.n];
+        else
+          zero = true;
+      }
+      Cell gx{0, 0, 0, 0}, gy{0, 0, 0, 0};
+      if (!zero) {
+        const double2* sp = reinterpret_cast<const double2*>(a.slopes) + 4 * sid;
+        const double2 q0 = sp[0], q1 = sp[1], q2 = sp[2], q3 = sp[3];
+        gx = Cell{q0.x, q0.y, q1.x, q1.y};
+        gy = Cell{q2.x, q2.y, q3.x, q3.y};
+      }
+      addmult(c, gx, dms[s].x);
+      addmult(c, gy, dms[s].y);
+      side[s] = c;
+    }
+    s0 = side[0];
+    s1 = side[1];
+  }
+  Prim l, r;
+  double2 n;
+  double vel = 0;
+  if (action == RG_ACT_REGULAR || action == RG_ACT_REGULAR2) {
+    // condition_action_sequence.cpp:84-110, condition_action_sequence_2.cpp:129-157
+    const double2 x0 = m.points[fc.x], x1 = m.points[fc.y];
+    n = normalize2(x1.x - x0.x, x1.y - x0.y);
+    const double2 w = a.ev_zero ? make_double2(0.0, 0.0) : reinterpret_cast<const double2*>(a.ev)[e];
+    vel = n.x * w.x + n.y * w.y;
+    l = to_prim(g, action == RG_ACT_REGULAR ? c0 : s0);
+    r = to_prim(g, action == RG_ACT_REGULAR ? c1 : s1);
+  } else {
+    // RigidWallFlux / RigidWallFlux2 / FreeFlowFlux: the wall frame
+    const double2 x0 = m.points[fc.x], x1 = m.points[fc.y];
+    n = aux ? wall_normal(v.x - x0.x, v.y - x0.y, p) : wall_normal(x1.x - v.x, x1.y - v.y, p);
+    if (action == RG_ACT_FREE_FLOW) {
+      l = r = to_prim(g, aux ? c0 : c1);
+    } else {
+      const Prim q = to_prim(g, action == RG_ACT_RIGID_WALL ? (aux ? c0 : c1) : (aux ? s0 : s1));
+      if (aux) {
+        l = q;
+        r = reflect(q, p, pa);
+      } else {
+        r = q;
+        l = reflect(q, p, pa);
+      }
+    }
+  }
+  const double na = sqrt(n.x * n.x + n.y * n.y);
+  Cons c;
+  if (!solve_face(l, r, vel, n, na, p, pa, c, a, e)) return;
+  const int real_side = fc.x < m.n ? fc.x : fc.y;
+  write_flux<false>(a, e, real_side, c, kScaled, a.geom.xarea[e]);
+}
+
+template <bool kScaled>
+__global__ void __launch_bounds__(kMaxBlock) k_faces_cas(StepArgs a) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < a.mesh.e; e += gridDim.x * blockDim.x)
+    k_faces_cas_item<kScaled>(a, e);
+}
+
 // ---------------------------------------------------------------- cells
 
 // The next step's SimpleCFL bound of cell i with state (d, pres, vx, vy), as
@@ -806,6 +945,10 @@ cudaError_t launch_faces(const StepArgs& a, cudaStream_t s, bool scaled) {
   if (a.mesh.e == 0) return cudaSuccess;
   const int nb = grid_of(a.shapes.faces, a.mesh.e), bs = a.shapes.faces.block;
   const bool b = a.cell_problem != nullptr;
+  if (a.n_rules > 0) {
+    scaled ? k_faces_cas<true><<<nb, bs, 0, s>>>(a) : k_faces_cas<false><<<nb, bs, 0, s>>>(a);
+    return cudaGetLastError();
+  }
   if (a.order == 1) {
     if (scaled)
       b ? k_faces_pcm<true, true><<<nb, bs, 0, s>>>(a) : k_faces_pcm<true, false><<<nb, bs, 0, s>>>(a);

@@ -191,7 +191,10 @@ struct rg_handle {
   // tracers and stickers (rg_set_tracer_config): cell tracers, extensive
   // tracers, tracer slopes and fluxes, each face's unscaled mass flux, each
   // cell's shock decision and sticker mask; sized for tr_n cells, tr_e faces
-  rg_tracer_config tcfg{0, 0u, -1, -1, -1};
+  rg_tracer_config tcfg{0, 0, 0u, -1, -1, -1};
+  // condition/action flux rules (rg_set_flux_rules)
+  int n_rules = 0;
+  rg_flux_rule rules[RG_MAX_FLUX_RULES];
   rgh::DevBuf tr, tr_ext, tr_slopes, tr_flux, mflux, shock, stickers;
   bool have_tr = false, have_tr_ext = false;
   int tr_n = -1, tr_e = -1;

@@ -237,6 +237,9 @@ struct StepArgs {
   // the slopes kernel each cell's shock decision
   double* mflux;                  // e, or nullptr
   unsigned char* shock;           // n, or nullptr
+  // condition/action flux rules (0: Simple/ModularFluxCalculator)
+  int n_rules;
+  int rules[RG_MAX_FLUX_RULES][5];  // sequence, condition, sticker, action, ratchet_in
   StepShapes shapes;  // launch shapes (host side; the kernels ignore it)
 };
 

@@ -18,7 +18,8 @@ using namespace rgh;
 namespace rgh {
 
 bool tracers_on(const rg_handle* h) {
-  return h->tcfg.n_tracers > 0 || h->tcfg.skip_sticker >= 0 || h->tcfg.frozen_sticker >= 0;
+  return h->tcfg.n_tracers > 0 || h->tcfg.n_stickers > 0 || h->tcfg.skip_sticker >= 0 ||
+         h->tcfg.frozen_sticker >= 0;
 }
 
 void tracer_release(rg_handle* h) {
@@ -103,14 +104,16 @@ extern "C" {
 rg_status rg_set_tracer_config(rg_handle* h, const rg_tracer_config* cfg) {
   if (!h) return RG_ERR_INVALID_ARGUMENT;
   h->last = rg_error{};
-  const rg_tracer_config off{0, 0u, -1, -1, -1};
+  const rg_tracer_config off{0, 0, 0u, -1, -1, -1};
   const rg_tracer_config c = cfg ? *cfg : off;
   if (c.n_tracers < 0 || c.n_tracers > RG_MAX_TRACERS) return invalid(h, 0, c.n_tracers);
+  if (c.n_stickers < 0 || c.n_stickers > 32) return invalid(h, 6, c.n_stickers);
+  if (c.n_tracers > 0 && h->n_rules > 0) return invalid(h, 7, 0);  // condition/action fluxes carry no tracers
   if (c.n_tracers < 32 && (c.limited_mask >> c.n_tracers) != 0) return invalid(h, 1, c.limited_mask);
   if (c.entropy_tracer < -1 || c.entropy_tracer >= c.n_tracers) return invalid(h, 2, c.entropy_tracer);
   if (c.skip_sticker < -1 || c.skip_sticker > 31) return invalid(h, 3, c.skip_sticker);
   if (c.frozen_sticker < -1 || c.frozen_sticker > 31) return invalid(h, 4, c.frozen_sticker);
-  const bool on = c.n_tracers > 0 || c.skip_sticker >= 0 || c.frozen_sticker >= 0;
+  const bool on = c.n_tracers > 0 || c.n_stickers > 0 || c.skip_sticker >= 0 || c.frozen_sticker >= 0;
   // the FP32-mixed path, Heun and batches have no tracer passes
   if (on && (h->mixed || h->heun || h->n_problems > 0)) return invalid(h, 5, 0);
   RG_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -124,6 +127,27 @@ rg_status rg_set_tracer_config(rg_handle* h, const rg_tracer_config* cfg) {
   }
   if (nt_changed) h->have_tr = h->have_tr_ext = false;
   return tracer_buffers(h);
+}
+
+rg_status rg_set_flux_rules(rg_handle* h, int32_t n_rules, const rg_flux_rule* rules) {
+  if (!h || n_rules < 0 || (n_rules > 0 && !rules)) return RG_ERR_INVALID_ARGUMENT;
+  if (n_rules > RG_MAX_FLUX_RULES) return invalid(h, -1, n_rules);
+  if (n_rules > 0 && (h->mixed || h->n_problems > 0 || h->tcfg.n_tracers > 0)) return invalid(h, -2, 0);
+  for (int k = 0; k < n_rules; ++k) {
+    const rg_flux_rule& r = rules[k];
+    const bool ok = (r.sequence == 0 || r.sequence == 1) && r.condition >= 0 && r.condition <= 2 &&
+                    (r.condition != RG_COND_SPECIAL_EDGE || (r.sticker >= 0 && r.sticker < 32)) &&
+                    (r.sequence == 0 ? (r.action >= 0 && r.action <= 2) : (r.action >= 3 && r.action <= 5)) &&
+                    (r.sequence == 0 || h->cfg.order == 2);
+    if (!ok) return invalid(h, k, r.action);
+    if (r.condition == RG_COND_SPECIAL_EDGE && !tracers_on(h)) return invalid(h, k, -1);  // no stickers kept
+  }
+  RG_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->n_rules = n_rules;
+  for (int k = 0; k < n_rules; ++k) h->rules[k] = rules[k];
+  drop_graph(h);
+  h->dt_next_ready = false;
+  return RG_OK;
 }
 
 rg_status rg_set_tracers(rg_handle* h, const double* tracers) {

@@ -109,7 +109,7 @@ class GpuContext {
     if (nt == 0 && ns == 0) return;
     if (nt > RG_MAX_TRACERS || ns > 32)
       throw UniversalError("rich_gb300: more tracers or stickers than the library holds");
-    rg_tracer_config c{static_cast<int32_t>(nt), 0u, -1, -1, -1};
+    rg_tracer_config c{static_cast<int32_t>(nt), static_cast<int32_t>(ns), 0u, -1, -1, -1};
     for (size_t j = 0; j < nt && j < tsn.tracer_names.size(); ++j) {
       for (const std::string& name : spec_.calc_tracers)
         if (name == tsn.tracer_names[j]) c.limited_mask |= 1u << j;
@@ -127,6 +127,12 @@ class GpuContext {
     }
   }
   int n_tracers() const { return have_tcfg_ ? tcfg_.n_tracers : 0; }
+  // ConditionActionSequence / ConditionActionSequence2 in place of the
+  // Simple/ModularFluxCalculator (rg_flux_rule rows; see rich_gb300.h).
+  // RegularSpecialEdge reads the cells' stickers, which sync_tracers keeps.
+  void set_flux_rules(const std::vector<rg_flux_rule>& rules) const {
+    check(rg_set_flux_rules(h_, static_cast<int32_t>(rules.size()), rules.empty() ? nullptr : rules.data()));
+  }
   bool tracers_configured() const { return have_tcfg_; }
 
   void upload_cells(const std::vector<ComputationalCell>& cells) const {
@@ -241,7 +247,7 @@ class GpuContext {
   rg_config cfg_;
   GpuTracerSpec spec_;
   rg_handle* h_ = nullptr;
-  mutable rg_tracer_config tcfg_{0, 0u, -1, -1, -1};
+  mutable rg_tracer_config tcfg_{0, 0, 0u, -1, -1, -1};
   mutable bool have_tcfg_ = false;
   mutable rg_physical_geometry pgeo_{RG_GEOMETRY_SLAB, {0, 0}, {0, 1}, 1};
   mutable PackedMesh packed_;

@@ -32,7 +32,7 @@ EXPORTS = ("rg_default_config", "rg_create", "rg_destroy", "rg_status_string", "
            "rg_set_extensive_tracers", "rg_get_extensive_tracers", "rg_set_stickers",
            "rg_get_tracer_fluxes", "rg_get_tracer_slopes", "rg_set_outer_box", "rg_set_point_motion",
            "rg_point_velocities", "rg_apply_fix", "rg_get_edge_velocities", "rg_get_geometry",
-           "rg_advance_begin", "rg_set_physical_geometry", "rg_set_tracer_fluxes")
+           "rg_advance_begin", "rg_set_physical_geometry", "rg_set_tracer_fluxes", "rg_set_flux_rules")
 
 MESH_DEVICE_GEOMETRY = 2  # RG_MESH_DEVICE_GEOMETRY
 
@@ -45,8 +45,13 @@ class RgLaunchShapes(C.Structure):
 
 
 class RgTracerConfig(C.Structure):
-    _fields_ = [("n_tracers", C.c_int32), ("limited_mask", C.c_uint32), ("entropy_tracer", C.c_int32),
-                ("skip_sticker", C.c_int32), ("frozen_sticker", C.c_int32)]
+    _fields_ = [("n_tracers", C.c_int32), ("n_stickers", C.c_int32), ("limited_mask", C.c_uint32),
+                ("entropy_tracer", C.c_int32), ("skip_sticker", C.c_int32), ("frozen_sticker", C.c_int32)]
+
+
+class RgFluxRule(C.Structure):
+    _fields_ = [("sequence", C.c_int32), ("condition", C.c_int32), ("sticker", C.c_int32), ("action", C.c_int32),
+                ("ratchet_in", C.c_int32)]
 
 
 class RgPointMotion(C.Structure):
@@ -137,6 +142,7 @@ def load(path=LIB_PATH):
               "rg_get_tracer_fluxes", "rg_get_tracer_slopes", "rg_set_tracer_fluxes"):
         getattr(lib, f).argtypes = [vp, dp]
     lib.rg_set_stickers.argtypes = [vp, C.POINTER(C.c_uint32)]
+    lib.rg_set_flux_rules.argtypes = [vp, C.c_int32, C.POINTER(RgFluxRule)]
     lib.rg_set_outer_box.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double]
     lib.rg_set_point_motion.argtypes = [vp, C.POINTER(RgPointMotion)]
     lib.rg_point_velocities.argtypes = [vp, dp]
@@ -335,14 +341,16 @@ class Handle:
         return dt.value, pv
 
     # tracers and stickers --------------------------------------------------
-    def set_tracer_config(self, n_tracers=0, limited=(), entropy=-1, skip_sticker=-1, frozen_sticker=-1):
+    def set_tracer_config(self, n_tracers=0, limited=(), entropy=-1, skip_sticker=-1, frozen_sticker=-1,
+                          n_stickers=0):
         """Tracer count, the tracers in LinearGaussImproved's calc_tracers
         (indices), the "Entropy" tracer, the skip_key sticker bit and the
-        HasSticker + SkipUpdate sticker bit (-1: none)."""
+        HasSticker + SkipUpdate sticker bit (-1: none); n_stickers keeps
+        stickers for the flux rules."""
         mask = 0
         for j in limited:
             mask |= 1 << j
-        c = RgTracerConfig(n_tracers, mask, entropy, skip_sticker, frozen_sticker)
+        c = RgTracerConfig(n_tracers, n_stickers, mask, entropy, skip_sticker, frozen_sticker)
         self._check(self.lib.rg_set_tracer_config(self.h, C.byref(c)))
         self.n_tracers = n_tracers
 
@@ -381,6 +389,13 @@ class Handle:
         out = np.empty((self.mesh.n_cells, 2 * self.n_tracers))
         self._check(self.lib.rg_get_tracer_slopes(self.h, dptr(out)))
         return out
+
+    def set_flux_rules(self, rules):
+        """Condition/action flux rules: rows (sequence, condition, sticker,
+        action, ratchet_in); an empty list restores the default flux calculator."""
+        rows = [tuple(int(x) for x in r) for r in np.asarray(rules, dtype=np.int64).reshape(-1, 5)]
+        arr = (RgFluxRule * max(len(rows), 1))(*[RgFluxRule(*r) for r in rows])
+        self._check(self.lib.rg_set_flux_rules(self.h, len(rows), arr))
 
     # batches ---------------------------------------------------------------
     def set_problems(self, offsets, gammas):

@@ -369,6 +369,39 @@ rg_status rg_set_physical_geometry(rg_handle* h, const rg_physical_geometry* pg)
  * extensive update (one host synchronisation, at the end) */
 rg_status rg_advance_begin(rg_handle* h, double* dt_out, double* point_velocities_out);
 
+/* Condition/action flux schemes --------------------------------------------- */
+/* ConditionActionSequence (condition_action_sequence.cpp, order 1) and
+ * ConditionActionSequence2 (condition_action_sequence_2.cpp, order 2 with
+ * LinearGaussImproved's face states) as the flux calculator: per face the
+ * first rule of sequence 0 whose condition holds, else the first of
+ * sequence 1, picks the flux action; no rule holding is reported as
+ * RG_ERR_INVALID_ARGUMENT (phase 3, the face) like the reference's "Error in
+ * ConditionActionSequence".  RegularSpecialEdge reads the sticker bit of
+ * rg_set_stickers.  FP64 path, no tracers; n_rules = 0 restores the
+ * Simple/ModularFluxCalculator of the configured order. */
+#define RG_MAX_FLUX_RULES 8
+typedef enum rg_flux_condition {
+  RG_COND_BOUNDARY_EDGE = 0,  /* IsBoundaryEdge (:228-253) */
+  RG_COND_BULK_EDGE = 1,      /* IsBulkEdge (:255-271) */
+  RG_COND_SPECIAL_EDGE = 2    /* RegularSpecialEdge(sticker) (:273-289) */
+} rg_flux_condition;
+typedef enum rg_flux_action {
+  RG_ACT_REGULAR = 0,      /* RegularFlux (:84-110): cell states */
+  RG_ACT_RIGID_WALL = 1,   /* RigidWallFlux (:140-184) */
+  RG_ACT_FREE_FLOW = 2,    /* FreeFlowFlux (:186-220) */
+  RG_ACT_REGULAR2 = 3,     /* RegularFlux2 (condition_action_sequence_2.cpp:129-157): face states */
+  RG_ACT_RIGID_WALL2 = 4,  /* RigidWallFlux2 (:183-228) */
+  RG_ACT_RATCHET = 5       /* Ratchet(in) (:232-249) */
+} rg_flux_action;
+typedef struct rg_flux_rule {
+  int32_t sequence;   /* 0: ConditionActionSequence's list (actions 0-2), 1: ConditionActionSequence2's (3-5) */
+  int32_t condition;  /* rg_flux_condition */
+  int32_t sticker;    /* RG_COND_SPECIAL_EDGE's sticker bit */
+  int32_t action;     /* rg_flux_action */
+  int32_t ratchet_in; /* Ratchet's `in` */
+} rg_flux_rule;
+rg_status rg_set_flux_rules(rg_handle* h, int32_t n_rules, const rg_flux_rule* rules);
+
 /* Tracers and stickers ---------------------------------------------------- */
 /* ComputationalCell::tracers / ::stickers (computational_cell_2d.hpp:19-36)
  * and Extensive::tracers (extensive.hpp) on the FP64 path, with the
@@ -402,12 +435,14 @@ rg_status rg_advance_begin(rg_handle* h, double* dt_out, double* point_velocitie
 #define RG_MAX_TRACERS 8
 typedef struct rg_tracer_config {
   int32_t n_tracers;        /* 0..RG_MAX_TRACERS */
+  int32_t n_stickers;       /* sticker bits in use (0..32); stickers are also kept when a sticker bit
+                               below is set */
   uint32_t limited_mask;    /* bit j: tracer j is in LinearGaussImproved's calc_tracers */
   int32_t entropy_tracer;   /* index of the "Entropy" tracer, -1: none */
   int32_t skip_sticker;     /* sticker bit of LinearGaussImproved's skip_key, -1: none */
   int32_t frozen_sticker;   /* sticker bit of SimpleCellUpdater's HasSticker + SkipUpdate, -1: none */
 } rg_tracer_config;
-/* cfg == NULL or {0, 0, -1, -1, -1}: no tracers, no stickers (the default).
+/* cfg == NULL or {0, 0, 0, -1, -1, -1}: no tracers, no stickers (the default).
  * Tracer values start unset (rg_set_tracers), stickers all clear. */
 rg_status rg_set_tracer_config(rg_handle* h, const rg_tracer_config* cfg);
 rg_status rg_set_tracers(rg_handle* h, const double* tracers);

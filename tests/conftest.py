@@ -44,8 +44,19 @@ def set_geometry(h, g):
 
 
 def upload_golden(h, g, flags=0):
+    """Upload the fixture's mesh with its PhysicalGeometry and, for the
+    condition/action cases, its flux rules and obstacle stickers (frozen by
+    HasSticker + SkipUpdate)."""
     set_geometry(h, g)
+    rules = g.get("flux_rules")
+    stickers = g.get("tr_stickers") if rules is not None else None
+    if stickers is not None:
+        h.set_tracer_config(0, n_stickers=1, frozen_sticker=0)
     h.upload_mesh(g["mesh"], flags=flags)
+    if stickers is not None:
+        h.set_stickers(stickers.astype(np.uint32))
+    if rules is not None:
+        h.set_flux_rules(rules)
 
 
 @pytest.fixture(params=GOLDEN_CASES)

@@ -13,7 +13,7 @@ import oracle
 import richgpu
 import synthetic
 from conftest import GOLDEN_CASES, RUN_CASES, load_golden, upload_golden
-from test_oracle_golden import accumulate, areas_of, exact
+from test_oracle_golden import accumulate, areas_of, exact, oracle_pass
 
 pytestmark = pytest.mark.gpu
 
@@ -80,9 +80,8 @@ def test_golden_fused_step(name):
         h.set_edge_velocities(g["ev_cfl"])
         dt = h.step()
         cells, ext = h.get_cells(), h.get_extensives()
-    oc, oe, odt = oracle.step(g["mesh"], g["cells0"], g["ext0"], g["ev_cfl"], g["gamma"], 0.3, g["order"],
-                              oracle.lgi_params(g["ghost_kind"]), areas=areas_of(g))
-    assert dt == odt
+    oc, oe, odts = oracle_pass(g, g["cells0"], g["ext0"], g["ev_cfl"], heun=False)
+    assert dt == odts[0]
     exact(ext, oe)
     exact(cells, oc)
 
@@ -220,3 +219,51 @@ def test_full_size_conservation_and_determinism():
     assert abs(tot1[1] - tot0[1]) <= 1e-12 * abs(tot0[1])                # energy
     assert abs(tot1[2]) <= 1e-12 and abs(tot1[3]) <= 1e-12               # momentum (starts at 0)
     assert np.all(np.isfinite(c1))
+
+
+def test_condition_action_large_vs_oracle():
+    """ConditionActionSequence2 on a 192^2 rigid box: rigid walls, an obstacle
+    of sticker cells (frozen), outflow ratchets are exercised on a second
+    case; 12 fused steps against the oracle."""
+    mesh = synthetic.lattice_mesh(192, 192, (0.0, 1.0, 0.0, 1.0), "rigid", seed=21)
+    cells = synthetic.bumps_cells(mesh, seed=21)
+    n = mesh.n_cells
+    xy = mesh.point_xy[:n]
+    st = (np.hypot(xy[:, 0] - 0.4, xy[:, 1] - 0.55) < 0.12).astype(np.uint32)
+    cells[st == 1, 2:] = 0.0
+    ext = oracle.init_extensives(mesh, cells, 5 / 3)
+    ev = np.zeros((mesh.n_faces, 2))
+    lp = oracle.lgi_params(ghost_kind=0)
+    for rules in ([[1, 0, -1, 4, 0], [1, 2, 0, 4, 0], [1, 1, -1, 3, 0]],
+                  [[0, 2, 0, 1, 0], [1, 0, -1, 5, 0], [1, 1, -1, 3, 0]]):
+        oc, oe, odts = oracle.run_cas(mesh, cells, ext, ev, 5 / 3, 12, 2, lp, rules, st, 1)
+        with richgpu.Handle(gamma=5 / 3, order=2, ghost_kind=0, device=0) as h:
+            h.set_tracer_config(0, n_stickers=1, frozen_sticker=0)
+            h.upload_mesh(mesh)
+            h.set_stickers(st)
+            h.set_flux_rules(rules)
+            h.set_cells(cells)
+            h.set_extensives(ext)
+            h.set_edge_velocities(ev)
+            exact(h.run(12), odts)
+            exact(h.get_cells(), oc)
+            exact(h.get_extensives(), oe)
+
+
+def test_condition_action_rules_checked():
+    mesh = synthetic.lattice_mesh(16, 16, (0.0, 1.0, 0.0, 1.0), "rigid", seed=3)
+    with richgpu.Handle(gamma=5 / 3, order=1, ghost_kind=0, device=0) as h:
+        h.upload_mesh(mesh)
+        with pytest.raises(richgpu.RichError):
+            h.set_flux_rules([[1, 1, -1, 3, 0]])           # ConditionActionSequence2 needs order 2
+        with pytest.raises(richgpu.RichError):
+            h.set_flux_rules([[0, 2, 0, 1, 0]])            # RegularSpecialEdge without stickers kept
+        h.set_flux_rules([[0, 1, -1, 0, 0]])               # bulk edges only: boundary faces match nothing
+        h.set_cells(synthetic.sod_cells(mesh))
+        h.init_extensives()
+        h.set_edge_velocities(np.zeros((mesh.n_faces, 2)))
+        with pytest.raises(richgpu.RichError) as ei:
+            h.step()
+        assert ei.value.status == 1 and ei.value.phase == 3
+        h.set_flux_rules([])
+        h.step()

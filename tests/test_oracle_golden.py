@@ -133,6 +133,18 @@ def test_init_extensives(golden):
     exact(oracle.init_extensives(g["mesh"], g["cells0"], g["gamma"]), g["ext0"])
 
 
+def oracle_pass(g, cells, ext, ev, steps=1, heun=None):
+    """hdsim::TimeAdvance (TimeAdvance2Heun with heun) steps of the case's own
+    plugins on the fixture mesh; heun=None takes the fixture's."""
+    heun = g["heun"] if heun is None else heun
+    if flux_rules(g) is not None:
+        st = stickers_of(g)
+        return oracle.run_cas(g["mesh"], cells, ext, ev, g["gamma"], steps, g["order"], lp_of(g), flux_rules(g), st,
+                              1 if st is not None else 0)
+    return oracle.run(g["mesh"], cells, ext, ev, g["gamma"], steps, 0.3, g["order"], lp_of(g), heun=heun,
+                      areas=areas_of(g))
+
+
 def motion_of(g):
     """The case's PointMotion / EdgeVelocityCalculator as recorded by the dump."""
     k, edges, chi, eta, cold, fix = g["motion"]
