@@ -577,10 +577,36 @@ def adjoint_block(reps=3):
         tl = h.step_tlm(steps, dt, dw)
         lhs, rhs = float(np.sum(seed * tl)), float(np.sum(g * dw))
     f, b = statistics.median(fwd_ms), statistics.median(bwd_ms)
+    # the FP32-mixed step's adjoint on the same problem and dt
+    with richgpu.Handle(gamma=GAMMA, order=2, ghost_kind=1, device=0, precision=1) as h:
+        h.upload_mesh(mesh)
+        h.set_edge_velocities(np.zeros((mesh.n_faces, 2)))
+        fwd32, bwd32 = [], []
+        for _ in range(reps + 1):
+            h.set_cells(cells)
+            t0 = time.perf_counter()
+            h.step_fwd(steps, dt, every)
+            t1 = time.perf_counter()
+            wn32 = h.get_cells()
+            seed32 = np.zeros_like(wn32)
+            seed32[:, 0] = 2.0 * (wn32[:, 0] - target)
+            t2 = time.perf_counter()
+            g32 = h.step_bwd(seed32)
+            t3 = time.perf_counter()
+            fwd32.append((t1 - t0) * 1e3)
+            bwd32.append((t3 - t2) * 1e3)
+    f32, b32 = statistics.median(fwd32[1:]), statistics.median(bwd32[1:])
     return {"workload": "periodic_bumps_256x256_lgi_hllc_fp64_200steps_fixed_dt", "cells": mesh.n_cells,
             "steps": steps, "checkpoint_every": every, "fwd_ms": f, "bwd_ms": b, "adjoint_over_fwd": b / f,
             "fwd_cell_updates_per_s": mesh.n_cells * steps / (f * 1e-3),
             "dot_product_rel": abs(lhs - rhs) / abs(lhs),
+            "fp32_mixed": {"fwd_ms": f32, "bwd_ms": b32, "adjoint_over_fwd": b32 / f32,
+                           "bwd_speedup_vs_fp64": b / b32,
+                           "gradient_rel_l2_vs_fp64": float(np.linalg.norm(g32 - g) / np.linalg.norm(g)),
+                           "final_density_l1_vs_fp64": float(np.abs(wn32[:, 0] - wn[:, 0]).sum()
+                                                             / np.abs(wn[:, 0]).sum()),
+                           "note": "FP32-mixed step forward; reverse with FP32 reconstruction, limiter and "
+                                   "Hllc and FP64 gathers and cell update"},
             "timing": "host wall clock around synchronous C-ABI calls, median of %d" % reps}
 
 

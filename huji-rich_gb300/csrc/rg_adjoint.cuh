@@ -73,5 +73,11 @@ cudaError_t adj_launch_seed(const AdjArgs& a, const double* wbar, double* ubar, 
 // for the first step (grad != nullptr), to the gradient with respect to W_0.
 cudaError_t adj_launch_reverse(const AdjArgs& a, const double* ubar_in, double* ubar_out, double* grad,
                                cudaStream_t s);
+// the transposed cell update and gather alone (shared by both precisions)
+cudaError_t adj_launch_update(const AdjArgs& a, const double* ubar_in, double* ubar_out, double* grad,
+                              cudaStream_t s);
+// rg_adjoint_rev32.cu: the same reverse step with the face and cell kernels in FP32
+cudaError_t adj_launch_reverse32(const AdjArgs& a, const double* ubar_in, double* ubar_out, double* grad,
+                                 cudaStream_t s);
 
 }  // namespace rg

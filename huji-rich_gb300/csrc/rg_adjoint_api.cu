@@ -14,6 +14,11 @@
 // The reverse adjacency (which face sides and CSR entries read each cell)
 // is built once per mesh on the host, in ascending order, so every reverse
 // gather is deterministic.
+// FP32-mixed handles differentiate the FP32-mixed step: the forward and the
+// recomputation run the FP32-mixed kernels, the recomputation records the
+// limiter trace of the FP32 slopes (k_slopes32_trace), and the reverse runs
+// the face and cell kernels in FP32 with the FP64 transposed gather and cell
+// update (adj_launch_reverse32).  Checkpoints hold the FP32 primitives.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -41,10 +46,12 @@ struct rg_adjoint_state {
   // reverse sweep and tangent work arrays
   DevBuf ubar0, ubar1, side_bar, self_bar, entry_bar, io;
   DevBuf dcells, dslopes, dflux, dext;
+  // FP32-mixed recomputation: the interval's running FP32 primitives and extensives
+  DevBuf w_cells32, w_ext;
   void release() {
     for (DevBuf* b : {&side_off, &sides, &target_off, &targets, &ckpt_cells, &ckpt_ext, &final_ext, &seg_cells,
                       &seg_ext, &seg_slopes, &seg_trace, &ubar0, &ubar1, &side_bar, &self_bar, &entry_bar, &io,
-                      &dcells, &dslopes, &dflux, &dext})
+                      &dcells, &dslopes, &dflux, &dext, &w_cells32, &w_ext})
       b->release();
     adjacency = have_forward = false;
   }
@@ -68,8 +75,9 @@ T* ptr(DevBuf& b, size_t elem_offset = 0) {
   return static_cast<T*>(b.p) + elem_offset;
 }
 
-rg_status check_config(rg_handle* h) {
-  if (h->cfg.order != 2 || h->cfg.ghost_kind != RG_GHOST_PERIODIC || h->mixed || h->heun || h->n_problems > 0 ||
+rg_status check_config(rg_handle* h, bool allow_mixed = true) {
+  if (h->cfg.order != 2 || h->cfg.ghost_kind != RG_GHOST_PERIODIC || (h->mixed && !allow_mixed) || h->heun ||
+      h->n_problems > 0 ||
       tracers_on(h) || active_slot(h)->lay.own_xarea || h->n_rules > 0)
     return invalid(h, -10, h->cfg.order);
   return RG_OK;
@@ -182,12 +190,28 @@ rg_status enqueue_plain_step(rg_handle* h, const rg::StepArgs& a, bool faces_and
   return RG_OK;
 }
 
-rg_status check_run(rg_handle* h, int32_t n_steps, double dt) {
+rg_status check_run(rg_handle* h, int32_t n_steps, double dt, bool allow_mixed = true) {
   if (rg_status st = require(h, true, false, false, false)) return st;
-  if (rg_status st = check_config(h)) return st;
+  if (rg_status st = check_config(h, allow_mixed)) return st;
   if (n_steps < 1 || !(dt > 0)) return invalid(h, -11, dt);
   if (rg_status st = mesh_error(h)) return st;
   return ensure_adjacency(h);
+}
+
+// One FP32-mixed step with a fixed dt on the FP32 primitives and FP64
+// extensives of `m` (in place).
+rg_status enqueue_mixed_step(rg_handle* h, const rg::MixedArgs& m) {
+  RG_CUDA(h, rg::launch_slopes32(m, h->stream));
+  RG_CUDA(h, rg::launch_faces32(m, h->stream, true));
+  RG_CUDA(h, rg::launch_update_mixed(m, h->stream, false, true, true));
+  return RG_OK;
+}
+
+rg::MixedArgs mixed_fixed_dt(rg_handle* h, double dt) {
+  rg::MixedArgs m = mixed_args(h);
+  m.dt32 = static_cast<float>(dt);
+  m.dt32_from_device = 0;
+  return m;
 }
 
 }  // namespace
@@ -215,8 +239,28 @@ rg_status rg_step_fwd(rg_handle* h, int32_t n_steps, double dt, int32_t every) {
   RG_TRY(reset_status(h, h->d_status, h->stream));
   rg::StepArgs a = step_args(h);
   a.dt_host = dt;
-  RG_CUDA(h, rg::launch_init_extensives(a, h->stream));
-  for (int k = 0; k < n_steps; ++k) {
+  if (h->mixed) {
+    // U_0 from the FP32 primitives the mixed steps start from
+    RG_CUDA(h, rg::launch_cells_to64(static_cast<const float4*>(h->cells32.p), static_cast<double*>(h->cells.p),
+                                     s->n, h->stream));
+    RG_CUDA(h, rg::launch_init_extensives(a, h->stream));
+    const rg::MixedArgs mx = mixed_fixed_dt(h, dt);
+    for (int k = 0; k < n_steps; ++k) {
+      if (k % every == 0) {
+        const size_t c = static_cast<size_t>(k / every);
+        RG_CUDA(h, cudaMemcpyAsync(ptr<double>(A->ckpt_cells, 4 * n * c), h->cells32.p, 16 * n,
+                                   cudaMemcpyDeviceToDevice, h->stream));
+        RG_CUDA(h, cudaMemcpyAsync(ptr<double>(A->ckpt_ext, 4 * n * c), h->ext.p, 32 * n, cudaMemcpyDeviceToDevice,
+                                   h->stream));
+      }
+      rg::MixedArgs mk = mx;
+      mk.step = std::min(k, 0x1fff);
+      RG_TRY(enqueue_mixed_step(h, mk));
+    }
+  } else {
+    RG_CUDA(h, rg::launch_init_extensives(a, h->stream));
+  }
+  for (int k = 0; k < (h->mixed ? 0 : n_steps); ++k) {
     if (k % every == 0) {
       const size_t c = static_cast<size_t>(k / every);
       RG_CUDA(h, cudaMemcpyAsync(ptr<double>(A->ckpt_cells, 4 * n * c), h->cells.p, 32 * n, cudaMemcpyDeviceToDevice,
@@ -259,7 +303,48 @@ rg_status rg_step_bwd(rg_handle* h, const double* cells_bar, double* cells0_bar)
   RG_CUDA(h, rg::adj_launch_seed(base, ptr<double>(A->io), cur, h->stream));
   rg::StepArgs a = step_args(h);
   a.dt_host = A->dt;
-  for (int c = A->n_ckpt - 1; c >= 0; --c) {
+  if (h->mixed) {
+    RG_CUDA(h, A->w_cells32.ensure(16 * np));
+    RG_CUDA(h, A->w_ext.ensure(32 * n));
+  }
+  for (int c = A->n_ckpt - 1; c >= 0 && h->mixed; --c) {
+    // FP32-mixed: recompute the interval with the mixed kernels, recording
+    // each step's state (widened), extensives, FP32 slopes and their trace
+    const int start = c * A->every;
+    const int len = std::min(A->every, A->n_steps - start);
+    RG_CUDA(h, cudaMemcpyAsync(A->w_cells32.p, ptr<double>(A->ckpt_cells, 4 * n * static_cast<size_t>(c)), 16 * n,
+                               cudaMemcpyDeviceToDevice, h->stream));
+    RG_CUDA(h, cudaMemcpyAsync(A->w_ext.p, ptr<double>(A->ckpt_ext, 4 * n * static_cast<size_t>(c)), 32 * n,
+                               cudaMemcpyDeviceToDevice, h->stream));
+    rg::MixedArgs mx = mixed_fixed_dt(h, A->dt);
+    mx.cells32 = static_cast<float4*>(A->w_cells32.p);
+    mx.ext = ptr<double>(A->w_ext);
+    for (int j = 0; j < len; ++j) {
+      const size_t J = static_cast<size_t>(j);
+      RG_CUDA(h, cudaMemcpyAsync(ptr<double>(A->seg_ext, 4 * n * J), A->w_ext.p, 32 * n, cudaMemcpyDeviceToDevice,
+                                 h->stream));
+      RG_CUDA(h, rg::launch_cells_to64(mx.cells32, ptr<double>(A->seg_cells, 4 * np * J), s->n, h->stream));
+      RG_CUDA(h, rg::launch_slopes32_trace(mx, ptr<double>(A->seg_slopes, 8 * n * J),
+                                           ptr<rg::SlopeTrace>(A->seg_trace, n * J), h->stream));
+      if (j + 1 < len) {
+        rg::MixedArgs mj = mx;
+        mj.step = std::min(start + j, 0x1fff);
+        RG_TRY(enqueue_mixed_step(h, mj));
+      }
+    }
+    for (int j = len - 1; j >= 0; --j) {
+      const size_t J = static_cast<size_t>(j);
+      rg::AdjArgs r = base;
+      r.cells = ptr<double>(A->seg_cells, 4 * np * J);
+      r.ext = ptr<double>(A->seg_ext, 4 * n * J);
+      r.slopes = ptr<double>(A->seg_slopes, 8 * n * J);
+      r.trace = ptr<rg::SlopeTrace>(A->seg_trace, n * J);
+      const bool first = start + j == 0;
+      RG_CUDA(h, rg::adj_launch_reverse32(r, cur, nxt, first ? ptr<double>(A->io) : nullptr, h->stream));
+      std::swap(cur, nxt);
+    }
+  }
+  for (int c = h->mixed ? -1 : A->n_ckpt - 1; c >= 0; --c) {
     const int start = c * A->every;
     const int len = std::min(A->every, A->n_steps - start);
     RG_CUDA(h, cudaMemcpyAsync(A->seg_cells.p, ptr<double>(A->ckpt_cells, 4 * n * static_cast<size_t>(c)), 32 * n,
@@ -307,7 +392,7 @@ rg_status rg_step_bwd(rg_handle* h, const double* cells_bar, double* cells0_bar)
 rg_status rg_step_tlm(rg_handle* h, int32_t n_steps, double dt, const double* dcells0, double* dcells) {
   if (!h || !dcells0 || !dcells) return RG_ERR_INVALID_ARGUMENT;
   h->last = rg_error{};
-  if (rg_status st = check_run(h, n_steps, dt)) return st;
+  if (rg_status st = check_run(h, n_steps, dt, false)) return st;  // the tangent-linear model is FP64
   rg_adjoint_state* A = h->adj;
   A->have_forward = false;
   h->dt_next_ready = false;

@@ -1,5 +1,6 @@
 // rg_adjoint_rev.cu -- hand-written reverse sweep of one differentiated step
-// (FP64).  With Ubar_{k+1} = dL/dU_{k+1} given, one reverse step is
+// (FP64; rg_adjoint_rev32.cu builds the face and cell kernels again in FP32
+// for the FP32-mixed adjoint).  With Ubar_{k+1} = dL/dU_{k+1} given, one reverse step is
 //     Wbar_k = G'(W_k)^T Ubar_{k+1}
 //     Ubar_k = Ubar_{k+1} + C'(U_k)^T Wbar_k      (k > 0)
 //     dL/dW_0 = Wbar_0 + I'(W_0)^T Ubar_1          (k = 0)
@@ -27,6 +28,11 @@
 
 #include "rg_adjoint.cuh"
 
+#ifndef RG_ADJ_REAL
+#define RG_ADJ_REAL double
+#define RG_ADJ_FP64 1
+#endif
+
 namespace rg {
 namespace {
 
@@ -46,6 +52,26 @@ __device__ __forceinline__ void store_raw(double* c, int i, const double v[4]) {
 }
 __device__ __forceinline__ int source_of(const MeshDev& m, int p) { return p < m.n ? p : m.ghost_source[p - m.n]; }
 
+// Working precision of the face and cell reverse kernels: double here;
+// rg_adjoint_rev32.cu compiles them again with float (the FP32-mixed
+// adjoint), loading and storing the same FP64 arrays.
+using real = RG_ADJ_REAL;
+struct rv2 {
+  real x, y;
+};
+__device__ __forceinline__ rv2 r2(double2 v) { return rv2{static_cast<real>(v.x), static_cast<real>(v.y)}; }
+__device__ __forceinline__ void load_r(const double* c, int i, real o[4]) {
+  double t[4];
+  load_raw(c, i, t);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) o[q] = static_cast<real>(t[q]);
+}
+__device__ __forceinline__ void store_r(double* c, int i, const real v[4]) {
+  const double t[4] = {v[0], v[1], v[2], v[3]};
+  store_raw(c, i, t);
+}
+
+#if RG_ADJ_FP64
 // Periodic meshes only: every ghost has a source, no CSR entry is a
 // self-mirror and no cell uses the boundary slope.
 __global__ void __launch_bounds__(kBlock) k_adj_check(AdjArgs a) {
@@ -81,63 +107,65 @@ __global__ void __launch_bounds__(kBlock) k_adj_seed(AdjArgs a, const double* wb
   store_raw(ubar, i, ub);
 }
 
+#endif  // RG_ADJ_FP64
+
 // Reverse of primitive conversion, rotation into the face frame, Hllc
 // (hllc.cpp:97-154, massflux, face at rest) and the rotation back: from fb
 // (adjoint of {mass, energy, px, py}) to the adjoints of the two states.
-__device__ void hllc_reverse(double g, double2 n, double na, double2 p, double pa, const double L[4],
-                             const double R[4], const double fb[4], double lb[4], double rb[4]) {
+__device__ void hllc_reverse(real g, rv2 n, real na, rv2 p, real pa, const real L[4], const real R[4],
+                             const real fb[4], real lb[4], real rb[4]) {
   // forward values
-  const double dL = L[0], pL = L[1], dR = R[0], pR = R[1];
-  const double eL = pL / dL / (g - 1), cL = sqrt(g * pL / dL);
-  const double eR = pR / dR / (g - 1), cR = sqrt(g * pR / dR);
-  const double lu = (L[2] * n.x + L[3] * n.y) / na, lv = (L[2] * p.x + L[3] * p.y) / pa;
-  const double ru = (R[2] * n.x + R[3] * n.y) / na, rv = (R[2] * p.x + R[3] * p.y) / pa;
+  const real dL = L[0], pL = L[1], dR = R[0], pR = R[1];
+  const real eL = pL / dL / (g - real(1)), cL = sqrt(g * pL / dL);
+  const real eR = pR / dR / (g - real(1)), cR = sqrt(g * pR / dR);
+  const real lu = (L[2] * n.x + L[3] * n.y) / na, lv = (L[2] * p.x + L[3] * p.y) / pa;
+  const real ru = (R[2] * n.x + R[3] * n.y) / na, rv = (R[2] * p.x + R[3] * p.y) / pa;
   const bool sl_right = (ru - cR) < (lu - cL);
-  const double sl = sl_right ? ru - cR : lu - cL;
+  const real sl = sl_right ? ru - cR : lu - cL;
   const bool sr_right = (lu + cL) < (ru + cR);
-  const double sr = sr_right ? ru + cR : lu + cL;
-  const double num = pR - pL + dL * lu * (sl - lu) - dR * ru * (sr - ru);
-  const double den = dL * (sl - lu) - dR * (sr - ru);
-  const double ss = num / den;
+  const real sr = sr_right ? ru + cR : lu + cL;
+  const real num = pR - pL + dL * lu * (sl - lu) - dR * ru * (sr - ru);
+  const real den = dL * (sl - lu) - dR * (sr - ru);
+  const real ss = num / den;
   const bool left = sl > 0 || (sl <= 0 && ss >= 0);
   const bool star = left ? !(sl > 0) : !(sr < 0);
-  const double qd = left ? dL : dR, qp = left ? pL : pR, qe = left ? eL : eR;
-  const double qu = left ? lu : ru, qv = left ? lv : rv, sk = left ? sl : sr;
-  const double k2 = qu * qu + qv * qv;
-  const double ek = qd * (0.5 * k2 + qe);
+  const real qd = left ? dL : dR, qp = left ? pL : pR, qe = left ? eL : eR;
+  const real qu = left ? lu : ru, qv = left ? lv : rv, sk = left ? sl : sr;
+  const real k2 = qu * qu + qv * qv;
+  const real ek = qd * (real(0.5) * k2 + qe);
   // adjoint of the face-frame flux {fm, fmx, fmy, fen}
-  const double bfm = fb[0], bfen = fb[1];
-  const double bfmx = (n.x * fb[2] + n.y * fb[3]) / na;
-  const double bfmy = (p.x * fb[2] + p.y * fb[3]) / pa;
-  double bd = 0, bp = 0, bu = 0, bv = 0, be = 0, bek = 0, bsk = 0, bss = 0;
+  const real bfm = fb[0], bfen = fb[1];
+  const real bfmx = (n.x * fb[2] + n.y * fb[3]) / na;
+  const real bfmy = (p.x * fb[2] + p.y * fb[3]) / pa;
+  real bd = 0, bp = 0, bu = 0, bv = 0, be = 0, bek = 0, bsk = 0, bss = 0;
   if (star) {
     // ds = qd K/D, use = ek ds/qd + ds A B with K = sk - qu, D = sk - ss,
     // A = ss - qu, B = ss + Q, Q = qp/(qd K); fluxes gain sk*(u* - u)
-    const double K = sk - qu, D = sk - ss;
-    const double ds = qd * K / D;
-    const double Q = qp / qd / K;
-    const double A = ss - qu, B = ss + Q;
-    const double use = ek * ds / qd + ds * A * B;
+    const real K = sk - qu, D = sk - ss;
+    const real ds = qd * K / D;
+    const real Q = qp / qd / K;
+    const real A = ss - qu, B = ss + Q;
+    const real use = ek * ds / qd + ds * A * B;
     bsk += bfm * (ds - qd) + bfmx * (ds * ss - qu * qd) + bfmy * (ds * qv - qv * qd) + bfen * (use - ek);
-    double bds = (bfm + bfmx * ss + bfmy * qv) * sk;
+    real bds = (bfm + bfmx * ss + bfmy * qv) * sk;
     bd -= (bfm + bfmx * qu + bfmy * qv) * sk;
     bu -= bfmx * qd * sk;
     bv += bfmy * (ds - qd) * sk;
     bss += bfmx * ds * sk;
-    const double buse = bfen * sk;
+    const real buse = bfen * sk;
     bek -= bfen * sk;
     bek += buse * ds / qd;
     bds += buse * (ek / qd + A * B);
     bd -= buse * ek * ds / (qd * qd);
-    const double bA = buse * ds * B, bB = buse * ds * A;
+    const real bA = buse * ds * B, bB = buse * ds * A;
     bss += bA + bB;
     bu -= bA;
     bp += bB / (qd * K);
     bd -= bB * Q / qd;
-    double bK = -bB * Q / K;
+    real bK = -bB * Q / K;
     bd += bds * K / D;
     bK += bds * qd / D;
-    const double bD = -bds * ds / D;
+    const real bD = -bds * ds / D;
     bsk += bK + bD;
     bu -= bK;
     bss -= bD;
@@ -145,32 +173,32 @@ __device__ void hllc_reverse(double g, double2 n, double na, double2 p, double p
   // physical flux along the normal: fm = qd qu, fmx = qp + qu qd qu,
   // fmy = qv qd qu, fen = (ek + qp) qu; ek = qd (|v|^2/2 + qe)
   bd += bfm * qu + bfmx * qu * qu + bfmy * qv * qu;
-  bu += bfm * qd + 2.0 * bfmx * qd * qu + bfmy * qv * qd + bfen * (ek + qp);
+  bu += bfm * qd + real(2.0) * bfmx * qd * qu + bfmy * qv * qd + bfen * (ek + qp);
   bv += bfmy * qd * qu;
   bp += bfmx + bfen * qu;
   bek += bfen * qu;
-  bd += bek * (0.5 * k2 + qe);
+  bd += bek * (real(0.5) * k2 + qe);
   bu += bek * qd * qu;
   bv += bek * qd * qv;
   be += bek * qd;
   // distribute to the chosen side, then the wave-speed paths
-  double bdL = 0, bpL = 0, buL = 0, bvL = 0, beL = 0, bcL = 0;
-  double bdR = 0, bpR = 0, buR = 0, bvR = 0, beR = 0, bcR = 0;
-  double bsl = 0, bsr = 0;
+  real bdL = 0, bpL = 0, buL = 0, bvL = 0, beL = 0, bcL = 0;
+  real bdR = 0, bpR = 0, buR = 0, bvR = 0, beR = 0, bcR = 0;
+  real bsl = 0, bsr = 0;
   if (left) {
     bdL = bd, bpL = bp, buL = bu, bvL = bv, beL = be, bsl = bsk;
   } else {
     bdR = bd, bpR = bp, buR = bu, bvR = bv, beR = be, bsr = bsk;
   }
   // ss = num/den
-  const double bnum = bss / den, bden = -bss * ss / den;
+  const real bnum = bss / den, bden = -bss * ss / den;
   bpR += bnum;
   bpL -= bnum;
   bdL += bnum * lu * (sl - lu) + bden * (sl - lu);
-  buL += bnum * dL * (sl - 2.0 * lu) - bden * dL;
+  buL += bnum * dL * (sl - real(2.0) * lu) - bden * dL;
   bsl += (bnum * lu + bden) * dL;
   bdR -= bnum * ru * (sr - ru) + bden * (sr - ru);
-  buR -= bnum * dR * (sr - 2.0 * ru) - bden * dR;
+  buR -= bnum * dR * (sr - real(2.0) * ru) - bden * dR;
   bsr -= (bnum * ru + bden) * dR;
   // sl = min(lu - cL, ru - cR), sr = max(lu + cL, ru + cR)
   if (sl_right) {
@@ -188,10 +216,10 @@ __device__ void hllc_reverse(double g, double2 n, double na, double2 p, double p
     bcL += bsr;
   }
   // e = p/(d (gamma-1)), c = sqrt(gamma p/d)
-  bpL += beL / (dL * (g - 1)) + bcL * g / (2.0 * cL * dL);
-  bdL -= beL * eL / dL + bcL * cL / (2.0 * dL);
-  bpR += beR / (dR * (g - 1)) + bcR * g / (2.0 * cR * dR);
-  bdR -= beR * eR / dR + bcR * cR / (2.0 * dR);
+  bpL += beL / (dL * (g - real(1))) + bcL * g / (real(2.0) * cL * dL);
+  bdL -= beL * eL / dL + bcL * cL / (real(2.0) * dL);
+  bpR += beR / (dR * (g - real(1))) + bcR * g / (real(2.0) * cR * dR);
+  bdR -= beR * eR / dR + bcR * cR / (real(2.0) * dR);
   // rotation into the face frame: u = v.n/|n|, v_t = v.par/|par|
   lb[0] = bdL;
   lb[1] = bpL;
@@ -203,12 +231,12 @@ __device__ void hllc_reverse(double g, double2 n, double na, double2 p, double p
   rb[3] = buR * n.y / na + bvR * p.y / pa;
 }
 
-__device__ __forceinline__ void face_state(const AdjArgs& a, int pid, double2 dm, double c[4]) {
+__device__ __forceinline__ void face_state(const AdjArgs& a, int pid, rv2 dm, real c[4]) {
   const int sid = source_of(a.mesh, pid);
-  double gx[4], gy[4];
-  load_raw(a.cells, sid, c);
-  load_raw(a.slopes, 2 * sid, gx);
-  load_raw(a.slopes, 2 * sid + 1, gy);
+  real gx[4], gy[4];
+  load_r(a.cells, sid, c);
+  load_r(a.slopes, 2 * sid, gx);
+  load_r(a.slopes, 2 * sid + 1, gy);
 #pragma unroll
   for (int q = 0; q < 4; ++q) c[q] = c[q] + gx[q] * dm.x + gy[q] * dm.y;
 }
@@ -218,28 +246,31 @@ __global__ void __launch_bounds__(kBlock) k_adj_faces(AdjArgs a, const double* u
   const MeshDev& m = a.mesh;
   if (e >= m.e) return;
   const int2 fc = m.face_cells[e];
+  // the transposed gather of the extensive update stays in FP64
   const double s = a.dt * a.geom.area[e];
-  double fb[4] = {0, 0, 0, 0};
+  double fbd[4] = {0, 0, 0, 0};
   if (fc.y < m.n) {
     double u[4];
     load_raw(ubar, fc.y, u);
 #pragma unroll
-    for (int q = 0; q < 4; ++q) fb[q] += u[q];
+    for (int q = 0; q < 4; ++q) fbd[q] += u[q];
   }
   if (fc.x < m.n) {
     double u[4];
     load_raw(ubar, fc.x, u);
 #pragma unroll
-    for (int q = 0; q < 4; ++q) fb[q] -= u[q];
+    for (int q = 0; q < 4; ++q) fbd[q] -= u[q];
   }
+  real fb[4];
 #pragma unroll
-  for (int q = 0; q < 4; ++q) fb[q] *= s;
-  double L[4], R[4], lb[4], rb[4];
-  face_state(a, fc.x, a.geom.dm0[e], L);
-  face_state(a, fc.y, a.geom.dm1[e], R);
-  hllc_reverse(a.gamma, a.geom.nrm[e], a.geom.nabs[e], a.geom.par[e], a.geom.area[e], L, R, fb, lb, rb);
-  store_raw(a.side_bar, 2 * e, lb);
-  store_raw(a.side_bar, 2 * e + 1, rb);
+  for (int q = 0; q < 4; ++q) fb[q] = static_cast<real>(fbd[q] * s);
+  real L[4], R[4], lb[4], rb[4];
+  face_state(a, fc.x, r2(a.geom.dm0[e]), L);
+  face_state(a, fc.y, r2(a.geom.dm1[e]), R);
+  hllc_reverse(static_cast<real>(a.gamma), r2(a.geom.nrm[e]), static_cast<real>(a.geom.nabs[e]), r2(a.geom.par[e]),
+               static_cast<real>(a.geom.area[e]), L, R, fb, lb, rb);
+  store_r(a.side_bar, 2 * e, lb);
+  store_r(a.side_bar, 2 * e + 1, rb);
 }
 
 __global__ void __launch_bounds__(kBlock) k_adj_cell(AdjArgs a) {
@@ -247,13 +278,13 @@ __global__ void __launch_bounds__(kBlock) k_adj_cell(AdjArgs a) {
   const MeshDev& m = a.mesh;
   if (i >= m.n) return;
   // face-state adjoints -> state adjoint w and slope adjoints bx, by
-  double w[4] = {0, 0, 0, 0}, bx[4] = {0, 0, 0, 0}, by[4] = {0, 0, 0, 0};
+  real w[4] = {0, 0, 0, 0}, bx[4] = {0, 0, 0, 0}, by[4] = {0, 0, 0, 0};
   for (int k = a.side_off[i]; k < a.side_off[i + 1]; ++k) {
     const int s = a.sides[k];
     const int e = s >> 1;
-    const double2 dm = (s & 1) ? a.geom.dm1[e] : a.geom.dm0[e];
-    double sb[4];
-    load_raw(a.side_bar, s, sb);
+    const rv2 dm = r2((s & 1) ? a.geom.dm1[e] : a.geom.dm0[e]);
+    real sb[4];
+    load_r(a.side_bar, s, sb);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       w[q] += sb[q];
@@ -264,7 +295,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_cell(AdjArgs a) {
   // limiter: s = naive*psi
   const SlopeTrace& tr = a.trace[i];
   const int b = m.cell_off[i], nn = m.cell_off[i + 1] - b;
-  double bnx[4], bny[4], extra[4];
+  real bnx[4], bny[4], extra[4];
   int ex_at[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
@@ -276,50 +307,53 @@ __global__ void __launch_bounds__(kBlock) k_adj_cell(AdjArgs a) {
     ex_at[q] = -1;
     if (k == kTraceNone) continue;
     const int kind = (code >> 8) & 3;
-    const double psi = tr.psi[q];
+    const real psi = static_cast<real>(tr.psi[q]);
     bnx[q] = bx[q] * psi;
     bny[q] = by[q] * psi;
     if (kind == 3) continue;  // clamped to zero: no dependence
     // psi = N/D with D = naive_x dm.x + naive_y dm.y (the centroid difference)
     // and N = coef*(W[neighbour] - W[cell])
-    const double nx = tr.naive[q], ny = tr.naive[4 + q];
-    const double bpsi = bx[q] * nx + by[q] * ny;
-    const double D = tr.dphi[q];
-    const double bN = bpsi / D, bD = -bpsi * psi / D;
+    const real nx = static_cast<real>(tr.naive[q]), ny = static_cast<real>(tr.naive[4 + q]);
+    const real bpsi = bx[q] * nx + by[q] * ny;
+    const real D = static_cast<real>(tr.dphi[q]);
+    const real bN = bpsi / D, bD = -bpsi * psi / D;
     const int e = m.cell_faces[b + k];
-    const double2 dm = (a.geom.nbr[b + k] & kNbrFirst) ? a.geom.dm0[e] : a.geom.dm1[e];
+    const rv2 dm = r2((a.geom.nbr[b + k] & kNbrFirst) ? a.geom.dm0[e] : a.geom.dm1[e]);
     bnx[q] += bD * dm.x;
     bny[q] += bD * dm.y;
     const int ex = (code >> 16) - 1;
     if (ex >= 0) {
-      extra[q] = (kind == 2 ? a.theta : 1.0) * bN;
+      extra[q] = (kind == 2 ? static_cast<real>(a.theta) : real(1)) * bN;
       ex_at[q] = ex;
       w[q] -= extra[q];
     }
   }
   // naive slope: nx = vx*mi.x + vy*mi.y, ny = vx*mi.z + vy*mi.w,
   // v = sum_k h_k (W[cell] + W[neighbour k])
-  const dbl4 mi = a.geom.minv[i];
-  double bvx[4], bvy[4];
+  const dbl4 mid = a.geom.minv[i];
+  const real mix = static_cast<real>(mid.x), miy = static_cast<real>(mid.y), miz = static_cast<real>(mid.z),
+             miw = static_cast<real>(mid.w);
+  real bvx[4], bvy[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
-    bvx[q] = bnx[q] * mi.x + bny[q] * mi.z;
-    bvy[q] = bnx[q] * mi.y + bny[q] * mi.w;
+    bvx[q] = bnx[q] * mix + bny[q] * miz;
+    bvy[q] = bnx[q] * miy + bny[q] * miw;
   }
   for (int k = 0; k < nn; ++k) {
-    const double2 h = a.geom.hr[b + k];
-    double c[4];
+    const rv2 h = r2(a.geom.hr[b + k]);
+    real c[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       c[q] = bvx[q] * h.x + bvy[q] * h.y;
       w[q] += c[q];
       if (ex_at[q] == k) c[q] += extra[q];
     }
-    store_raw(a.entry_bar, b + k, c);
+    store_r(a.entry_bar, b + k, c);
   }
-  store_raw(a.self_bar, i, w);
+  store_r(a.self_bar, i, w);
 }
 
+#if RG_ADJ_FP64
 __global__ void __launch_bounds__(kBlock) k_adj_update(AdjArgs a, const double* ubar_in, double* ubar_out,
                                                        double* grad) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -356,10 +390,13 @@ __global__ void __launch_bounds__(kBlock) k_adj_update(AdjArgs a, const double* 
   store_raw(ubar_out, i, ub);
 }
 
+#endif  // RG_ADJ_FP64
+
 inline int blocks(int n) { return (n + kBlock - 1) / kBlock; }
 
 }  // namespace
 
+#if RG_ADJ_FP64
 cudaError_t adj_launch_check(const AdjArgs& a, cudaStream_t s) {
   const int n = a.mesh.m > a.mesh.n ? a.mesh.m : a.mesh.n;
   k_adj_check<<<blocks(n), kBlock, 0, s>>>(a);
@@ -371,12 +408,25 @@ cudaError_t adj_launch_seed(const AdjArgs& a, const double* wbar, double* ubar, 
   return cudaGetLastError();
 }
 
+cudaError_t adj_launch_update(const AdjArgs& a, const double* ubar_in, double* ubar_out, double* grad,
+                              cudaStream_t s) {
+  k_adj_update<<<blocks(a.mesh.n), kBlock, 0, s>>>(a, ubar_in, ubar_out, grad);
+  return cudaGetLastError();
+}
+
 cudaError_t adj_launch_reverse(const AdjArgs& a, const double* ubar_in, double* ubar_out, double* grad,
                                cudaStream_t s) {
   k_adj_faces<<<blocks(a.mesh.e), kBlock, 0, s>>>(a, ubar_in);
   k_adj_cell<<<blocks(a.mesh.n), kBlock, 0, s>>>(a);
-  k_adj_update<<<blocks(a.mesh.n), kBlock, 0, s>>>(a, ubar_in, ubar_out, grad);
-  return cudaGetLastError();
+  return adj_launch_update(a, ubar_in, ubar_out, grad, s);
 }
+#else
+cudaError_t adj_launch_reverse32(const AdjArgs& a, const double* ubar_in, double* ubar_out, double* grad,
+                                 cudaStream_t s) {
+  k_adj_faces<<<blocks(a.mesh.e), kBlock, 0, s>>>(a, ubar_in);
+  k_adj_cell<<<blocks(a.mesh.n), kBlock, 0, s>>>(a);
+  return adj_launch_update(a, ubar_in, ubar_out, grad, s);
+}
+#endif
 
 }  // namespace rg

@@ -15,6 +15,7 @@
 // gather and the energy conversion), not by the flux arithmetic.
 #include <math.h>
 
+#include "rg_adjoint.cuh"
 #include "rg_mixed.cuh"
 
 namespace rg {
@@ -211,6 +212,113 @@ __device__ __forceinline__ void shocked32(float dphi, float cv, float cellv, flo
   if (fabsf(dphi) > thr || cv * cellv < 0.0f) {
     if (fabsf(dphi) > 1e-9f * cellv) psi = fminf(psi, fmaxf(__fdividef(theta * (nbv - cellv), dphi), 0.0f));
   }
+}
+
+// The FP32 slopes of a periodic mesh (no self-mirror neighbour, no boundary
+// slope) with the limiter trace the adjoint's reverse slope kernel reads
+// (SlopeTrace: the unlimited slope, each component's factor, the centroid
+// difference and neighbour of its active candidate).  The arithmetic is
+// k_slopes32_item's; the arg max / min follow the first strict improvement
+// as std::max / std::min do, and each psi is the smallest candidate taken in
+// edge order, which is what fminf over the candidates gives.
+__global__ void __launch_bounds__(kBlock) k_slopes32_trace(MixedArgs a, double* slopes64, SlopeTrace* trace) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const MeshDev& m = a.mesh;
+  if (i >= m.n) return;
+  const C4 cell = ld4(a.cells32, i);
+  const int b = m.cell_off[i], nn = m.cell_off[i + 1] - b;
+  const float4 mi = a.g32.minv[i];
+  C4 vx{0, 0, 0, 0}, vy{0, 0, 0, 0};
+  float cmax[4] = {cell.d, cell.p, cell.vx, cell.vy}, cmin[4] = {cell.d, cell.p, cell.vx, cell.vy};
+  int amax[4] = {-1, -1, -1, -1}, amin[4] = {-1, -1, -1, -1};
+  bool ratio_shock = false;
+  for (int k = 0; k < nn; ++k) {
+    const C4 nb = point32(a, static_cast<int>(a.geom.nbr[b + k] & kNbrIdMask));
+    const float4 en = a.g32.ent[b + k];
+    const C4 s2{cell.d + nb.d, cell.p + nb.p, cell.vx + nb.vx, cell.vy + nb.vy};
+    addm(vx, s2, en.x);
+    addm(vy, s2, en.y);
+    const float nv[4] = {nb.d, nb.p, nb.vx, nb.vy};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      if (cmax[q] < nv[q]) {
+        cmax[q] = nv[q];
+        amax[q] = k;
+      }
+      if (nv[q] < cmin[q]) {
+        cmin[q] = nv[q];
+        amin[q] = k;
+      }
+    }
+    ratio_shock = ratio_shock || fminf(cell.p, nb.p) < a.delta_p * fmaxf(cell.p, nb.p);
+  }
+  float sx[4] = {vx.d * mi.x + vy.d * mi.y, vx.p * mi.x + vy.p * mi.y, vx.vx * mi.x + vy.vx * mi.y,
+                 vx.vy * mi.x + vy.vy * mi.y};
+  float sy[4] = {vy.d * mi.w + vx.d * mi.z, vy.p * mi.w + vx.p * mi.z, vy.vx * mi.w + vx.vx * mi.z,
+                 vy.vy * mi.w + vx.vy * mi.z};
+  SlopeTrace& tr = trace[i];
+  const float cq[4] = {cell.d, cell.p, cell.vx, cell.vy};
+  float psi[4] = {1, 1, 1, 1};
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    tr.naive[q] = sx[q];
+    tr.naive[4 + q] = sy[q];
+    tr.dphi[q] = 0;
+    tr.code[q] = kTraceNone;
+  }
+  if (a.slf) {
+    const float cs = sqrtf(a.gamma * cell.p / cell.d);
+    const bool shock = (sx[2] + sy[3]) * a.g32.width[i] < (-a.delta_v) * cs || ratio_shock;
+    const float f = shock ? 0.1f : 0.05f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float maxd = cmax[q] - cq[q], mind = cmin[q] - cq[q];
+      const float thr = f * fmaxf(fabsf(maxd), fabsf(mind));
+      for (int k = 0; k < nn; ++k) {
+        const float4 en = a.g32.ent[b + k];
+        float cv = fmaf(sx[q], en.z, cq[q]);
+        cv = fmaf(sy[q], en.w, cv);
+        const float dphi = cv - cq[q];
+        if (!(fabsf(dphi) > thr || cv * cq[q] < 0.0f)) continue;
+        if (!shock) {
+          const bool use_abs = q >= 2;
+          const float t = use_abs ? fabsf(1e-9f * cq[q]) : 1e-9f * cq[q];
+          const float nt = use_abs ? -fabsf(1e-9f * cq[q]) : -1e-9f * cq[q];
+          const bool up = dphi > t;
+          if (up || dphi < nt) {
+            const float cand = __fdividef(up ? maxd : mind, dphi);
+            if (cand < psi[q]) {
+              psi[q] = cand;
+              tr.code[q] = k | ((up ? 0 : 1) << 8) | (((up ? amax[q] : amin[q]) + 1) << 16);
+              tr.dphi[q] = dphi;
+            }
+          }
+        } else if (fabsf(dphi) > 1e-9f * cq[q]) {
+          const C4 nb = point32(a, static_cast<int>(a.geom.nbr[b + k] & kNbrIdMask));
+          const float nv[4] = {nb.d, nb.p, nb.vx, nb.vy};
+          const float cand = __fdividef(a.theta * (nv[q] - cq[q]), dphi);
+          const bool clamp = cand < 0.0f;
+          const float x = clamp ? 0.0f : cand;
+          if (x < psi[q]) {
+            psi[q] = x;
+            tr.code[q] = k | ((clamp ? 3 : 2) << 8) | ((k + 1) << 16);
+            tr.dphi[q] = dphi;
+          }
+        }
+      }
+    }
+  }
+  double2* o = reinterpret_cast<double2*>(slopes64) + 4 * i;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    tr.psi[q] = psi[q];
+    sx[q] *= psi[q];
+    sy[q] *= psi[q];
+  }
+  o[0] = make_double2(sx[0], sx[1]);
+  o[1] = make_double2(sx[2], sx[3]);
+  o[2] = make_double2(sy[0], sy[1]);
+  o[3] = make_double2(sy[2], sy[3]);
 }
 
 // LinearGaussImproved::calc_slope (LinearGaussImproved.cpp:425-494) in FP32.
@@ -656,6 +764,11 @@ cudaError_t launch_ghost_fill32(const MixedArgs& a, cudaStream_t s) {
   if (a.mesh.g > 0) k_ghost_fill32<<<blocks(a.mesh.g), kBlock, 0, s>>>(a);
   return cudaGetLastError();
 }
+cudaError_t launch_slopes32_trace(const MixedArgs& a, double* slopes64, SlopeTrace* trace, cudaStream_t s) {
+  if (a.mesh.n > 0) k_slopes32_trace<<<(a.mesh.n + kBlock - 1) / kBlock, kBlock, 0, s>>>(a, slopes64, trace);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_slopes32(const MixedArgs& a, cudaStream_t s) {
   if (a.mesh.n > 0) {
     const LaunchShape& sh = a.shapes.slopes;

@@ -90,6 +90,10 @@ cudaError_t launch_vec2_to32(const double* v64, float2* v32, int n, cudaStream_t
 cudaError_t launch_flux_to64(const float4* f32, double* f64, int n, cudaStream_t s);
 cudaError_t launch_flux_to32(const double* f64, float4* f32, int n, cudaStream_t s);
 cudaError_t launch_cfl32(const MixedArgs& a, cudaStream_t s, bool fill_ghosts);
+// the FP32 slopes with the adjoint's limiter trace, slopes widened to FP64
+// (periodic meshes; rg_adjoint.cuh's SlopeTrace)
+struct SlopeTrace;
+cudaError_t launch_slopes32_trace(const MixedArgs& a, double* slopes64, SlopeTrace* trace, cudaStream_t s);
 cudaError_t launch_ghost_fill32(const MixedArgs& a, cudaStream_t s);
 cudaError_t launch_slopes32(const MixedArgs& a, cudaStream_t s);
 cudaError_t launch_faces32(const MixedArgs& a, cudaStream_t s, bool scaled);

@@ -36,7 +36,10 @@ UNITS = {
     "rg_tracer_api.cu": [],
     "rg_motion.cu": ["--fmad=false"],
     "rg_motion_api.cu": [],
+    "rg_adjoint_rev32.cu": [],
 }
+# units that include another unit's source
+EXTRA_DEPS = {"rg_adjoint_rev32.cu": ["rg_adjoint_rev.cu"]}
 
 
 def nvcc():
@@ -69,7 +72,8 @@ def build(force=False, verbose=False):
         s = os.path.join(CSRC, src)
         o = os.path.join(OUT_DIR, src + ".o")
         objs.append(o)
-        if force or not _newer(o, deps + [s]):
+        extra = [os.path.join(CSRC, d) for d in EXTRA_DEPS.get(src, [])]
+        if force or not _newer(o, deps + [s] + extra):
             jobs.append([cc] + common + flags + ["-c", s, "-o", o])
     with cf.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         res = list(ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), jobs))
