@@ -38,6 +38,34 @@ __device__ __forceinline__ void addm(C4& r, const C4& o, float s) {
   r.vy = fmaf(o.vy, s, r.vy);
 }
 
+// a*b + c*d and a*b - c*d as one product and one fused multiply-add, written
+// out so that every build of the slopes kernel (and its trace) rounds alike
+// whatever the compiler would contract
+__device__ __forceinline__ float dot2(float a, float b, float c, float d) {
+  return __fmaf_rn(c, d, __fmul_rn(a, b));
+}
+__device__ __forceinline__ float dif2(float a, float b, float c, float d) {
+  return __fmaf_rn(-c, d, __fmul_rn(a, b));
+}
+// the unlimited slope from the neighbour sums vx, vy: boundary cells' least
+// squares (mi = SxSy, Sx2, Sy2, den) or the Green-Gauss inverse (mi = the
+// 2x2 matrix, row major)
+__device__ __forceinline__ void naive_slope(bool boundary, const C4& vx, const C4& vy, const float4& mi, C4& sx,
+                                            C4& sy) {
+  if (boundary) {
+    const float inv = 1.0f / mi.w;
+    sx = C4{__fmul_rn(dif2(vy.d, mi.x, vx.d, mi.z), inv), __fmul_rn(dif2(vy.p, mi.x, vx.p, mi.z), inv),
+            __fmul_rn(dif2(vy.vx, mi.x, vx.vx, mi.z), inv), __fmul_rn(dif2(vy.vy, mi.x, vx.vy, mi.z), inv)};
+    sy = C4{__fmul_rn(dif2(vx.d, mi.x, vy.d, mi.y), inv), __fmul_rn(dif2(vx.p, mi.x, vy.p, mi.y), inv),
+            __fmul_rn(dif2(vx.vx, mi.x, vy.vx, mi.y), inv), __fmul_rn(dif2(vx.vy, mi.x, vy.vy, mi.y), inv)};
+  } else {
+    sx = C4{dot2(vx.d, mi.x, vy.d, mi.y), dot2(vx.p, mi.x, vy.p, mi.y), dot2(vx.vx, mi.x, vy.vx, mi.y),
+            dot2(vx.vy, mi.x, vy.vy, mi.y)};
+    sy = C4{dot2(vy.d, mi.w, vx.d, mi.z), dot2(vy.p, mi.w, vx.p, mi.z), dot2(vy.vx, mi.w, vx.vx, mi.z),
+            dot2(vy.vy, mi.w, vx.vy, mi.z)};
+  }
+}
+
 // ------------------------------------------------------------ geometry copies
 
 __global__ void __launch_bounds__(kBlock) k_geom32(MixedGeomArgs a) {
@@ -252,10 +280,10 @@ __global__ void __launch_bounds__(kBlock) k_slopes32_trace(MixedArgs a, double* 
     }
     ratio_shock = ratio_shock || fminf(cell.p, nb.p) < a.delta_p * fmaxf(cell.p, nb.p);
   }
-  float sx[4] = {vx.d * mi.x + vy.d * mi.y, vx.p * mi.x + vy.p * mi.y, vx.vx * mi.x + vy.vx * mi.y,
-                 vx.vy * mi.x + vy.vy * mi.y};
-  float sy[4] = {vy.d * mi.w + vx.d * mi.z, vy.p * mi.w + vx.p * mi.z, vy.vx * mi.w + vx.vx * mi.z,
-                 vy.vy * mi.w + vx.vy * mi.z};
+  C4 nx, ny;
+  naive_slope(false, vx, vy, mi, nx, ny);
+  float sx[4] = {nx.d, nx.p, nx.vx, nx.vy};
+  float sy[4] = {ny.d, ny.p, ny.vx, ny.vy};
   SlopeTrace& tr = trace[i];
   const float cq[4] = {cell.d, cell.p, cell.vx, cell.vy};
   float psi[4] = {1, 1, 1, 1};
@@ -356,20 +384,9 @@ __device__ __forceinline__ void k_slopes32_item(const MixedArgs& a, int i) {
     // min(p, p_k) / max(p, p_k) < delta_p without the division
     ratio_shock = ratio_shock || fminf(cell.p, nb.p) < a.delta_p * fmaxf(cell.p, nb.p);
   }
+  // boundary cells: vx, vy hold sum(df*dx), sum(df*dy)
   C4 sx, sy;
-  if (boundary) {
-    // vx, vy hold sum(df*dx), sum(df*dy); mi = (SxSy, Sx2, Sy2, den)
-    const float inv = 1.0f / mi.w;
-    sx = C4{(vy.d * mi.x - vx.d * mi.z) * inv, (vy.p * mi.x - vx.p * mi.z) * inv,
-            (vy.vx * mi.x - vx.vx * mi.z) * inv, (vy.vy * mi.x - vx.vy * mi.z) * inv};
-    sy = C4{(vx.d * mi.x - vy.d * mi.y) * inv, (vx.p * mi.x - vy.p * mi.y) * inv,
-            (vx.vx * mi.x - vy.vx * mi.y) * inv, (vx.vy * mi.x - vy.vy * mi.y) * inv};
-  } else {
-    sx = C4{vx.d * mi.x + vy.d * mi.y, vx.p * mi.x + vy.p * mi.y, vx.vx * mi.x + vy.vx * mi.y,
-            vx.vy * mi.x + vy.vy * mi.y};
-    sy = C4{vy.d * mi.w + vx.d * mi.z, vy.p * mi.w + vx.p * mi.z, vy.vx * mi.w + vx.vx * mi.z,
-            vy.vy * mi.w + vx.vy * mi.z};
-  }
+  naive_slope(boundary, vx, vy, mi, sx, sy);
   if (a.slf) {
     const float cs = sqrtf(gamma32<kBatch>(a, i) * cell.p / cell.d);
     const bool shock = (sx.vx + sy.vy) * a.g32.width[i] < (-a.delta_v) * cs || ratio_shock;
@@ -407,6 +424,108 @@ __device__ __forceinline__ void k_slopes32_item(const MixedArgs& a, int i) {
   }
   a.slopes32[2 * i] = make_float4(sx.d, sx.p, sx.vx, sx.vy);
   a.slopes32[2 * i + 1] = make_float4(sy.d, sy.p, sy.vx, sy.vy);
+}
+
+// The same slope with the neighbour states and stencil records of cells
+// with at most kPrefetch neighbours loaded up front, all independent, so
+// their latencies overlap; the arithmetic runs over them in the order of
+// k_slopes32_item and gives the same bits.  Cells with more neighbours take
+// k_slopes32_item.
+constexpr int kPrefetch = 8;
+template <bool kBatch>
+__device__ __forceinline__ void k_slopes32_pf_item(const MixedArgs& a, int i) {
+  const MeshDev& m = a.mesh;
+  const int b = m.cell_off[i], nn = m.cell_off[i + 1] - b;
+  if (nn > kPrefetch) {
+    k_slopes32_item<kBatch, 1>(a, i);
+    return;
+  }
+  const C4 cell = ld4(a.cells32, i);
+  const float4 mi = a.g32.minv[i];
+  const bool boundary = a.geom.cflags[i] & kCellBoundarySlope;
+  C4 nbk[kPrefetch];
+  float4 enk[kPrefetch];
+  uint32_t wk[kPrefetch];
+#pragma unroll
+  for (int k = 0; k < kPrefetch; ++k) {
+    if (k < nn) {
+      wk[k] = a.geom.nbr[b + k];
+      enk[k] = a.g32.ent[b + k];
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < kPrefetch; ++k)
+    if (k < nn) nbk[k] = point32(a, static_cast<int>(wk[k] & kNbrIdMask));
+  C4 vx{0, 0, 0, 0}, vy{0, 0, 0, 0};
+  C4 amax = cell, amin = cell, nmax = cell, nmin = cell;
+  bool ratio_shock = false;
+#pragma unroll
+  for (int k = 0; k < kPrefetch; ++k) {
+    if (k >= nn) break;
+    const C4& nb = nbk[k];
+    const float4 en = enk[k];
+    const C4 s = boundary ? C4{nb.d - cell.d, nb.p - cell.p, nb.vx - cell.vx, nb.vy - cell.vy}
+                          : C4{cell.d + nb.d, cell.p + nb.p, cell.vx + nb.vx, cell.vy + nb.vy};
+    addm(vx, s, en.x);
+    addm(vy, s, en.y);
+    amax = C4{fmaxf(amax.d, nb.d), fmaxf(amax.p, nb.p), fmaxf(amax.vx, nb.vx), fmaxf(amax.vy, nb.vy)};
+    amin = C4{fminf(amin.d, nb.d), fminf(amin.p, nb.p), fminf(amin.vx, nb.vx), fminf(amin.vy, nb.vy)};
+    if (!(wk[k] & kNbrMirror)) {
+      nmax = C4{fmaxf(nmax.d, nb.d), fmaxf(nmax.p, nb.p), fmaxf(nmax.vx, nb.vx), fmaxf(nmax.vy, nb.vy)};
+      nmin = C4{fminf(nmin.d, nb.d), fminf(nmin.p, nb.p), fminf(nmin.vx, nb.vx), fminf(nmin.vy, nb.vy)};
+    }
+    ratio_shock = ratio_shock || fminf(cell.p, nb.p) < a.delta_p * fmaxf(cell.p, nb.p);
+  }
+  C4 sx, sy;
+  naive_slope(boundary, vx, vy, mi, sx, sy);
+  if (a.slf) {
+    const float cs = sqrtf(gamma32<kBatch>(a, i) * cell.p / cell.d);
+    const bool shock = (sx.vx + sy.vy) * a.g32.width[i] < (-a.delta_v) * cs || ratio_shock;
+    const C4 cmax = shock ? amax : nmax, cmin = shock ? amin : nmin;
+    const C4 maxd{cmax.d - cell.d, cmax.p - cell.p, cmax.vx - cell.vx, cmax.vy - cell.vy};
+    const C4 mind{cmin.d - cell.d, cmin.p - cell.p, cmin.vx - cell.vx, cmin.vy - cell.vy};
+    const float f = shock ? 0.1f : 0.05f;
+    const C4 thr{f * fmaxf(fabsf(maxd.d), fabsf(mind.d)), f * fmaxf(fabsf(maxd.p), fabsf(mind.p)),
+                 f * fmaxf(fabsf(maxd.vx), fabsf(mind.vx)), f * fmaxf(fabsf(maxd.vy), fabsf(mind.vy))};
+    float psi0 = 1, psi1 = 1, psi2 = 1, psi3 = 1;
+#pragma unroll
+    for (int k = 0; k < kPrefetch; ++k) {
+      if (k >= nn) break;
+      const float4 en = enk[k];
+      C4 cv = cell;
+      addm(cv, sx, en.z);
+      addm(cv, sy, en.w);
+      const C4 dphi{cv.d - cell.d, cv.p - cell.p, cv.vx - cell.vx, cv.vy - cell.vy};
+      if (!shock) {
+        limit32(dphi.d, cv.d, cell.d, thr.d, maxd.d, mind.d, false, psi0);
+        limit32(dphi.p, cv.p, cell.p, thr.p, maxd.p, mind.p, false, psi1);
+        limit32(dphi.vx, cv.vx, cell.vx, thr.vx, maxd.vx, mind.vx, true, psi2);
+        limit32(dphi.vy, cv.vy, cell.vy, thr.vy, maxd.vy, mind.vy, true, psi3);
+      } else {
+        const C4& nb = nbk[k];
+        shocked32(dphi.d, cv.d, cell.d, thr.d, nb.d, a.theta, psi0);
+        shocked32(dphi.p, cv.p, cell.p, thr.p, nb.p, a.theta, psi1);
+        shocked32(dphi.vx, cv.vx, cell.vx, thr.vx, nb.vx, a.theta, psi2);
+        shocked32(dphi.vy, cv.vy, cell.vy, thr.vy, nb.vy, a.theta, psi3);
+      }
+    }
+    sx.d *= psi0; sy.d *= psi0;
+    sx.p *= psi1; sy.p *= psi1;
+    sx.vx *= psi2; sy.vx *= psi2;
+    sx.vy *= psi3; sy.vy *= psi3;
+  }
+  a.slopes32[2 * i] = make_float4(sx.d, sx.p, sx.vx, sx.vy);
+  a.slopes32[2 * i + 1] = make_float4(sy.d, sy.p, sy.vx, sy.vy);
+}
+
+template <bool kBatch>
+__global__ void __launch_bounds__(kMaxBlock) k_slopes32_pf(MixedArgs a) {
+  if (a.take_next_dt && blockIdx.x == 0 && threadIdx.x == 0) {
+    a.status->dt = a.status->dt_next;
+    a.status->dt32 = a.status->dt_next32;
+  }
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.mesh.n; i += gridDim.x * blockDim.x)
+    k_slopes32_pf_item<kBatch>(a, i);
 }
 
 template <bool kBatch, int kMinBlocks, int kUnroll>
@@ -775,8 +894,9 @@ cudaError_t launch_slopes32(const MixedArgs& a, cudaStream_t s) {
     const int nb = grid_of(sh, a.mesh.n), bs = sh.block;
     const bool b = a.cell_problem != nullptr;
     // builds: 0 plain, 1 neighbour loops unrolled by 2, 2 and 3 register-capped
-    // for 5 and 6 resident blocks of up to 256 threads
+    // for 5 and 6 resident blocks of up to 256 threads, 4 neighbours prefetched
     switch (sh.variant) {
+      case 4: b ? k_slopes32_pf<true><<<nb, bs, 0, s>>>(a) : k_slopes32_pf<false><<<nb, bs, 0, s>>>(a); break;
       case 1: b ? k_slopes32<true, 0, 2><<<nb, bs, 0, s>>>(a) : k_slopes32<false, 0, 2><<<nb, bs, 0, s>>>(a); break;
       case 2: b ? k_slopes32<true, 5, 1><<<nb, bs, 0, s>>>(a) : k_slopes32<false, 5, 1><<<nb, bs, 0, s>>>(a); break;
       case 3: b ? k_slopes32<true, 6, 1><<<nb, bs, 0, s>>>(a) : k_slopes32<false, 6, 1><<<nb, bs, 0, s>>>(a); break;

@@ -80,8 +80,8 @@ rg_status launch_one(rg_handle* h, int k, const rg::LaunchShape& sh, void* ext_s
   return RG_OK;
 }
 
-int n_variants(const rg_handle* h, int k) { return h->mixed && k == RG_KERNEL_SLOPES ? 4 : 1; }
-bool capped(int k, int v) { return k == RG_KERNEL_SLOPES && v >= 2; }
+int n_variants(const rg_handle* h, int k) { return h->mixed && k == RG_KERNEL_SLOPES ? 5 : 1; }
+bool capped(int k, int v) { return k == RG_KERNEL_SLOPES && (v == 2 || v == 3); }
 
 rg_status check_shapes(rg_handle* h, const rg_launch_shapes* s) {
   for (int k = 0; k < 4; ++k) {

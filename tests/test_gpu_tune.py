@@ -21,7 +21,8 @@ SHAPES = [
     {"cfl": (32, 7), "slopes": (96, 5), "faces": (480, 3), "update": (64, 1)},
 ]
 # the FP32-mixed slopes kernel's other builds (unrolled, register-capped)
-MIXED_SHAPES = [{"slopes": (128, 0, 1)}, {"slopes": (256, 608, 2)}, {"slopes": (64, 0, 3)}]
+MIXED_SHAPES = [{"slopes": (128, 0, 1)}, {"slopes": (256, 608, 2)}, {"slopes": (64, 0, 3)},
+                {"slopes": (128, 0, 4)}, {"slopes": (256, 1216, 4)}]
 
 
 def shapes_for(precision):
