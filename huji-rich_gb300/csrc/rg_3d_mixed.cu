@@ -7,6 +7,7 @@
 #include <math.h>
 
 #include "rg_3d.cuh"
+#include "rg_convert.cuh"
 #include "rg_hllc.cuh"
 
 namespace rg {
@@ -69,19 +70,18 @@ __global__ void __launch_bounds__(kBlock) k3m_geometry(Mesh3Dev m, const dbl4* n
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t < m.e) {
     const dbl4 v = nhat[t];
-    n32[t] = make_float4(static_cast<float>(v.x), static_cast<float>(v.y), static_cast<float>(v.z), 0.0f);
-    a32[t] = static_cast<float>(m.area[t]);
+    n32[t] = make_float4(narrow(v.x), narrow(v.y), narrow(v.z), 0.0f);
+    a32[t] = narrow(m.area[t]);
   }
-  if (t < m.n) w32[t] = static_cast<float>(m.width[t]);
+  if (t < m.n) w32[t] = narrow(m.width[t]);
 }
 
 __global__ void __launch_bounds__(kBlock) k3m_to32(const double* c64, float4* c32, float* vz, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double* c = c64 + 6 * i;
-  c32[i] = make_float4(static_cast<float>(c[0]), static_cast<float>(c[1]), static_cast<float>(c[2]),
-                       static_cast<float>(c[3]));
-  vz[i] = static_cast<float>(c[4]);
+  c32[i] = make_float4(narrow(c[0]), narrow(c[1]), narrow(c[2]), narrow(c[3]));
+  vz[i] = narrow(c[4]);
 }
 
 __global__ void __launch_bounds__(kBlock) k3m_to64(const float4* c32, const float* vz, double* c64, int n) {
@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(kBlock) k3m_cfl(Mixed3Args a) {
   if (i < a.mesh.n) {
     const C3 c = load32(a, i);
     const float b = a.width32[i] / (fabs3(c.v) + sqrtf(a.gamma * c.p / c.d));
-    bits = static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(b)));
+    bits = static_cast<unsigned long long>(__double_as_longlong(widen_exact(b)));
   }
   grid_min_times(a.status, bits, a.cfl, &a.status->dt, &a.status->dt32);
 }
@@ -188,7 +188,7 @@ __global__ void __launch_bounds__(kBlock) k3m_update(Mixed3Args a, int from_unsc
   }
   if (do_cells) {
     const double V = m.volume[i];
-    const float mf = static_cast<float>(u[0]);
+    const float mf = narrow(u[0]);
     // 1/m from the FP32 reciprocal and one Newton step
     double r = widen(1.0f / mf);
     r = r * (2.0 - u[0] * r);
@@ -198,16 +198,16 @@ __global__ void __launch_bounds__(kBlock) k3m_update(Mixed3Args a, int from_unsc
       record_error(a.status, a.step, RG_ERR_NEGATIVE_ENERGY, 5, i, eint);
       return;
     }
-    const float d = static_cast<float>(u[0] / V);
-    a.cells32[i] = make_float4(d, (a.gamma - 1.0f) * static_cast<float>(eint) * d, static_cast<float>(vx),
-                               static_cast<float>(vy));
-    a.vz32[i] = static_cast<float>(vz);
+    // m / V in FP32 from the rounded mass and volume (the result is stored in FP32)
+    const float d = mf / narrow(V);
+    a.cells32[i] = make_float4(d, (a.gamma - 1.0f) * narrow(eint) * d, narrow(vx), narrow(vy));
+    a.vz32[i] = narrow(vz);
   }
 }
 
 __global__ void __launch_bounds__(kBlock) k3m_d2f(const double* a, float* b, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) b[i] = static_cast<float>(a[i]);
+  if (i < n) b[i] = narrow(a[i]);
 }
 
 inline int blocks(int n) { return n > 0 ? (n + kBlock - 1) / kBlock : 1; }

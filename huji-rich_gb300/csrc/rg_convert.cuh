@@ -1,0 +1,115 @@
+// rg_convert.cuh -- float <-> double conversions on the integer pipe, and a
+// division by 3 without the FP64 division sequence.
+//
+// GB300 issues FP64-pipe instructions, the float <-> double conversions
+// included, at 2 per clock per SM against 64 per clock for integer ones.
+// The kernels that convert many values (the FP32 copies of the per-mesh
+// geometry, the FP32-mixed update) form the results from the IEEE-754 bit
+// patterns instead.  Host-compilable, so the same code is checked against
+// the C cast on the CPU.
+#pragma once
+
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#ifndef __CUDACC__
+#define RG_CONV_FN static inline
+#else
+#define RG_CONV_FN __host__ __device__ __forceinline__
+#endif
+
+namespace rg {
+
+RG_CONV_FN uint64_t conv_dbits(double x) {
+#ifdef __CUDA_ARCH__
+  return static_cast<uint64_t>(__double_as_longlong(x));
+#else
+  uint64_t u;
+  memcpy(&u, &x, 8);
+  return u;
+#endif
+}
+RG_CONV_FN uint32_t conv_fbits(float x) {
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(x);
+#else
+  uint32_t u;
+  memcpy(&u, &x, 4);
+  return u;
+#endif
+}
+RG_CONV_FN float conv_float(uint32_t u) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(u);
+#else
+  float f;
+  memcpy(&f, &u, 4);
+  return f;
+#endif
+}
+RG_CONV_FN double conv_double(uint32_t hi, uint32_t lo) {
+#ifdef __CUDA_ARCH__
+  return __hiloint2double(static_cast<int>(hi), static_cast<int>(lo));
+#else
+  const uint64_t u = (static_cast<uint64_t>(hi) << 32) | lo;
+  double d;
+  memcpy(&d, &u, 8);
+  return d;
+#endif
+}
+
+// double -> float rounded to nearest, ties to even: static_cast<float>(x)
+// for every x.  Results in the normal float range and zeros are formed on
+// the integer pipe (the 29 dropped significand bits decide the rounding; a
+// carry out of the significand raises the exponent, and out of the largest
+// exponent gives the infinity the rounding calls for); subnormal results,
+// infinities and NaNs take the hardware conversion.
+RG_CONV_FN float narrow(double x) {
+  const uint64_t u = conv_dbits(x);
+  const uint32_t hi = static_cast<uint32_t>(u >> 32), lo = static_cast<uint32_t>(u);
+  const uint32_t ex = (hi >> 20) & 0x7ffu;
+  // double exponents 897..1150 are the normal float exponents 1..254
+  if (ex - 897u < 254u) {
+    uint32_t f = (hi & 0x80000000u) | ((ex - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const uint32_t rest = lo & 0x1fffffffu, half = 0x10000000u;
+    f += (rest > half || (rest == half && (f & 1u))) ? 1u : 0u;
+    return conv_float(f);
+  }
+  if (((hi & 0x7fffffffu) | lo) == 0u) return conv_float(hi & 0x80000000u);
+  return static_cast<float>(x);
+}
+
+// float -> double, exact (static_cast<double>(f) for every f): zeros,
+// normal floats, infinities and NaNs on the integer pipe, subnormal floats
+// through the hardware conversion.
+RG_CONV_FN double widen_exact(float f) {
+  const uint32_t u = conv_fbits(f);
+  const uint32_t ex = (u >> 23) & 0xffu, mant = u & 0x7fffffu;
+  if (ex == 0u && mant != 0u) return static_cast<double>(f);
+  const uint32_t dex = ex == 0u ? 0u : (ex == 0xffu ? 0x7ffu : ex + 896u);  // rebias 127 -> 1023
+  return conv_double((u & 0x80000000u) | (dex << 20) | (mant >> 3), mant << 29);
+}
+
+// t / 3 rounded to nearest (t >= 0) without a division.  RN(1/3) is 1/3
+// less 2^-54 of itself, so q = RN(t * RN(1/3)) is within one ulp of t/3,
+// the fused remainder t - 3q is exact, and the fused correction
+// RN(q + r * RN(1/3)) is RN(t/3) (Markstein's correction step for a
+// divisor whose reciprocal is correctly rounded).  Below 2^-900, where the
+// remainder could lose bits, above 2^1000, and for infinities and NaN: the
+// division.
+RG_CONV_FN double third_of(double t) {
+  constexpr double kThird = 1.0 / 3.0;
+  if (!(t >= 0x1p-900 && t <= 0x1p1000)) return t / 3.;
+#ifdef __CUDA_ARCH__
+  const double q = __dmul_rn(t, kThird);
+  return __fma_rn(__fma_rn(-q, 3.0, t), kThird, q);
+#else
+  const double q = t * kThird;
+  return fma(fma(-q, 3.0, t), kThird, q);
+#endif
+}
+
+}  // namespace rg
+
+#undef RG_CONV_FN

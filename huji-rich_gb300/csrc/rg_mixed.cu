@@ -4,7 +4,7 @@
 // CFL bound run in FP32 (FMA allowed) on FP32 copies of the primitives and of
 // the geometry; the geometry itself is computed in FP64 by the geometry pass
 // (rg_fp64.cu) and rounded once per mesh upload.  FP64 stays where the
-// the benchmark spec keeps it: cell volumes, the extensive accumulation (each face's
+// precision is needed: cell volumes, the extensive accumulation (each face's
 // dt*area-scaled flux is widened to FP64 and summed per cell in ascending
 // face order, so every face adds exactly what its neighbour subtracts) and
 // the internal energy e = E/m - v^2/2, whose cancellation at high Mach
@@ -16,6 +16,7 @@
 #include <math.h>
 
 #include "rg_adjoint.cuh"
+#include "rg_convert.cuh"
 #include "rg_mixed.cuh"
 
 namespace rg {
@@ -67,6 +68,7 @@ __device__ __forceinline__ void naive_slope(bool boundary, const C4& vx, const C
 }
 
 // ------------------------------------------------------------ geometry copies
+// (the roundings on the integer pipe: rg_convert.cuh)
 
 __global__ void __launch_bounds__(kBlock) k_geom32(MixedGeomArgs a) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -74,33 +76,33 @@ __global__ void __launch_bounds__(kBlock) k_geom32(MixedGeomArgs a) {
   const GeomDev& g = a.g64;
   for (int e = t; e < a.e; e += stride) {
     const double2 n = g.nrm[e], p = g.par[e], d0 = g.dm0[e], d1 = g.dm1[e];
-    a.nrm[e] = make_float2(static_cast<float>(n.x), static_cast<float>(n.y));
-    a.nabs[e] = static_cast<float>(g.nabs[e]);
-    a.par[e] = make_float2(static_cast<float>(p.x), static_cast<float>(p.y));
-    a.area[e] = static_cast<float>(g.area[e]);
-    if (a.xarea != a.area) a.xarea[e] = static_cast<float>(g.xarea[e]);
-    a.dm0[e] = make_float2(static_cast<float>(d0.x), static_cast<float>(d0.y));
-    a.dm1[e] = make_float2(static_cast<float>(d1.x), static_cast<float>(d1.y));
+    a.nrm[e] = make_float2(narrow(n.x), narrow(n.y));
+    a.nabs[e] = narrow(g.nabs[e]);
+    a.par[e] = make_float2(narrow(p.x), narrow(p.y));
+    a.area[e] = narrow(g.area[e]);
+    if (a.xarea != a.area) a.xarea[e] = narrow(g.xarea[e]);
+    a.dm0[e] = make_float2(narrow(d0.x), narrow(d0.y));
+    a.dm1[e] = make_float2(narrow(d1.x), narrow(d1.y));
   }
   for (int i = t; i < a.n; i += stride) {
-    a.width[i] = static_cast<float>(g.width[i]);
-    a.inv_cd_volume[i] = static_cast<float>(1.0 / a.cd_volume[i]);
+    a.width[i] = narrow(g.width[i]);
+    // the FP32 reciprocal of the rounded volume (an FP64 division would cost
+    // more than the rest of the kernel)
+    a.inv_cd_volume[i] = __frcp_rn(narrow(a.cd_volume[i]));
     const dbl4 m = g.minv[i];
-    a.minv[i] = make_float4(static_cast<float>(m.x), static_cast<float>(m.y), static_cast<float>(m.z),
-                            static_cast<float>(m.w));
+    a.minv[i] = make_float4(narrow(m.x), narrow(m.y), narrow(m.z), narrow(m.w));
   }
   for (int k = t; k < a.m; k += stride) {
     const double2 h = g.hr[k];
     const int e = a.cell_faces[k];
     const bool first = g.nbr[k] & kNbrFirst;
     const double2 d = first ? g.dm0[e] : g.dm1[e];
-    a.ent[k] = make_float4(static_cast<float>(h.x), static_cast<float>(h.y), static_cast<float>(d.x),
-                           static_cast<float>(d.y));
+    a.ent[k] = make_float4(narrow(h.x), narrow(h.y), narrow(d.x), narrow(d.y));
     a.fsign[k] = e | (first ? static_cast<int>(0x80000000u) : 0);
   }
   for (int q = t; q < a.g; q += stride) {
     const double2 u = g.ghost_unit[q];
-    a.ghost_unit[q] = make_float2(static_cast<float>(u.x), static_cast<float>(u.y));
+    a.ghost_unit[q] = make_float2(narrow(u.x), narrow(u.y));
   }
 }
 
@@ -111,31 +113,30 @@ __global__ void __launch_bounds__(kBlock) k_cells_to32(const double* c64, float4
   if (i >= n) return;
   const double2 a = reinterpret_cast<const double2*>(c64)[2 * i];
   const double2 b = reinterpret_cast<const double2*>(c64)[2 * i + 1];
-  c32[i] = make_float4(static_cast<float>(a.x), static_cast<float>(a.y), static_cast<float>(b.x),
-                       static_cast<float>(b.y));
+  c32[i] = make_float4(narrow(a.x), narrow(a.y), narrow(b.x), narrow(b.y));
 }
 
 __global__ void __launch_bounds__(kBlock) k_cells_to64(const float4* c32, double* c64, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float4 v = c32[i];
-  reinterpret_cast<double2*>(c64)[2 * i] = make_double2(v.x, v.y);
-  reinterpret_cast<double2*>(c64)[2 * i + 1] = make_double2(v.z, v.w);
+  reinterpret_cast<double2*>(c64)[2 * i] = make_double2(widen_exact(v.x), widen_exact(v.y));
+  reinterpret_cast<double2*>(c64)[2 * i + 1] = make_double2(widen_exact(v.z), widen_exact(v.w));
 }
 
 __global__ void __launch_bounds__(kBlock) k_vec2_to32(const double* v64, float2* v32, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double2 v = reinterpret_cast<const double2*>(v64)[i];
-  v32[i] = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
+  v32[i] = make_float2(narrow(v.x), narrow(v.y));
 }
 
 __global__ void __launch_bounds__(kBlock) k_flux_to64(const float4* f32, double* f64, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float4 v = f32[i];
-  reinterpret_cast<double2*>(f64)[2 * i] = make_double2(v.x, v.y);
-  reinterpret_cast<double2*>(f64)[2 * i + 1] = make_double2(v.z, v.w);
+  reinterpret_cast<double2*>(f64)[2 * i] = make_double2(widen_exact(v.x), widen_exact(v.y));
+  reinterpret_cast<double2*>(f64)[2 * i + 1] = make_double2(widen_exact(v.z), widen_exact(v.w));
 }
 
 __global__ void __launch_bounds__(kBlock) k_flux_to32(const double* f64, float4* f32, int n) {
@@ -143,8 +144,7 @@ __global__ void __launch_bounds__(kBlock) k_flux_to32(const double* f64, float4*
   if (i >= n) return;
   const double2 a = reinterpret_cast<const double2*>(f64)[2 * i];
   const double2 b = reinterpret_cast<const double2*>(f64)[2 * i + 1];
-  f32[i] = make_float4(static_cast<float>(a.x), static_cast<float>(a.y), static_cast<float>(b.x),
-                       static_cast<float>(b.y));
+  f32[i] = make_float4(narrow(a.x), narrow(a.y), narrow(b.x), narrow(b.y));
 }
 
 // ------------------------------------------------------------ per step
@@ -209,12 +209,12 @@ __global__ void __launch_bounds__(kMaxBlock) k_cfl32(MixedArgs a, int fill_ghost
     }
     if (kBatch)
       problem_min(a.dtmin_p, t < m.n ? a.cell_problem[t] : -1,
-                  static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(x))));
+                  static_cast<unsigned long long>(__double_as_longlong(widen_exact(x))));
     else
       bits = min(bits, __float_as_uint(x));
   }
   if (kBatch) return;
-  grid_min_times(a.status, static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(__uint_as_float(bits)))),
+  grid_min_times(a.status, static_cast<unsigned long long>(__double_as_longlong(widen_exact(__uint_as_float(bits)))),
                  a.cfl, &a.status->dt, &a.status->dt32);
 }
 
@@ -608,7 +608,7 @@ __device__ __forceinline__ void write32(const MixedArgs& a, int e, int real_side
   float s = 1.0f;
   if (scaled) {
     if (kBatch)
-      s = static_cast<float>(a.cfl * __longlong_as_double(static_cast<long long>(
+      s = narrow(a.cfl * __longlong_as_double(static_cast<long long>(
                                           a.dtmin_p[a.cell_problem[real_side]]))) * area;
     else
       s = (a.dt32_from_device ? a.status->dt32 : a.dt32) * area;
@@ -779,7 +779,7 @@ __device__ __forceinline__ unsigned long long k_update_mixed_item(const MixedArg
     out2[2 * i + 1] = make_double2(px, py);
   }
   if (do_cells) {
-    const float mf = static_cast<float>(mass);
+    const float mf = narrow(mass);
     const float d = mf * a.g32.inv_cd_volume[i];
     if (d < 0.0f) {
       record_error(a.status, a.step, RG_ERR_NEGATIVE_DENSITY, 5, i, d);
@@ -796,8 +796,7 @@ __device__ __forceinline__ unsigned long long k_update_mixed_item(const MixedArg
       record_error(a.status, a.step, RG_ERR_NEGATIVE_ENERGY, 5, i, energy);
       return kInfBits;
     }
-    const float4 c = make_float4(d, (gamma32<kBatch>(a, i) - 1.0f) * static_cast<float>(energy) * d,
-                                 static_cast<float>(vx), static_cast<float>(vy));
+    const float4 c = make_float4(d, (gamma32<kBatch>(a, i) - 1.0f) * narrow(energy) * d, narrow(vx), narrow(vy));
     (a.cells32_out ? a.cells32_out : a.cells32)[i] = c;
     if (a.cfl_next) {
       // the next step's SimpleCFL bound of this cell, as k_cfl32 computes it
@@ -814,7 +813,7 @@ __device__ __forceinline__ unsigned long long k_update_mixed_item(const MixedArg
         }
       }
       const float res = (cs + sqrtf(q)) / a.g32.width[i];
-      return static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(1.0f / res)));
+      return static_cast<unsigned long long>(__double_as_longlong(widen_exact(1.0f / res)));
     }
   }
   return kInfBits;

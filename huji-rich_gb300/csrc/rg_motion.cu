@@ -18,6 +18,7 @@
 //                       through VoronoiMesh::CalcFaceVelocity (:146-151)
 #include <math.h>
 
+#include "rg_convert.cuh"
 #include "rg_motion.cuh"
 
 namespace rg {
@@ -51,7 +52,7 @@ __global__ void __launch_bounds__(kMoBlock) k_dev_geometry(MeshDev m, double2* c
     }
     const double t = half_cross(make_double2(v.x - an.x, v.y - an.y), make_double2(v.z - an.x, v.w - an.y));
     a2 += t;
-    const double s = t / 3.;
+    const double s = third_of(t);
     pc.x += ((an.x + v.x) + v.z) * s;
     pc.y += ((an.y + v.y) + v.w) * s;
   }

@@ -1,0 +1,90 @@
+// Checks rg::narrow and rg::widen_exact (huji-rich_gb300/csrc/rg_convert.cuh,
+// the integer-pipe float <-> double conversions of the FP32-mixed kernels)
+// against the C casts, bit for bit: random bit patterns, values across the
+// float range, rounding ties and carries, the special values, and a stride
+// through every float; and rg::third_of against the division t / 3 over
+// random magnitudes and the special values.  Exit status 0 when every value
+// agrees.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <random>
+
+#include "rg_convert.cuh"
+
+static long n_bad = 0;
+
+static void check_narrow(double x) {
+  const float a = rg::narrow(x), b = static_cast<float>(x);
+  uint32_t ua, ub;
+  memcpy(&ua, &a, 4);
+  memcpy(&ub, &b, 4);
+  if (ua != ub && !(std::isnan(a) && std::isnan(b))) {
+    if (n_bad < 5) printf("narrow(%a) = %a, cast %a\n", x, a, b);
+    ++n_bad;
+  }
+}
+
+int main() {
+  std::mt19937_64 g(20260101);
+  for (long i = 0; i < 4000000; ++i) {
+    const uint64_t u = g();
+    double x;
+    memcpy(&x, &u, 8);
+    check_narrow(x);
+  }
+  std::uniform_real_distribution<double> ud(-1, 1);
+  for (long i = 0; i < 2000000; ++i) check_narrow(ud(g) * std::ldexp(1.0, static_cast<int>(g() % 300) - 150));
+  // halfway cases and their neighbours, carries into the exponent
+  for (long i = 0; i < 2000000; ++i) {
+    const uint32_t fu = static_cast<uint32_t>(g());
+    float f;
+    memcpy(&f, &fu, 4);
+    if (!std::isfinite(f)) continue;
+    double x = f;
+    uint64_t u;
+    memcpy(&u, &x, 8);
+    u += (uint64_t{1} << 28) + (g() % 3) - 1;
+    memcpy(&x, &u, 8);
+    check_narrow(x);
+    check_narrow(-x);
+    check_narrow(std::nextafter(static_cast<double>(f), 1e300));
+  }
+  const double special[] = {0.0, -0.0, INFINITY, -INFINITY, NAN, 3.4028235677973366e38, 3.4028235e38, 3.5e38,
+                            1.1754943508222875e-38, 1.1754942e-38, 1e-45, 1.4e-45, 7e-46, 2.1e-45, 1e300, -1e-300};
+  for (double x : special) check_narrow(x);
+  for (uint64_t u = 0; u < (uint64_t{1} << 32); u += 613) {
+    const uint32_t fu = static_cast<uint32_t>(u);
+    float f;
+    memcpy(&f, &fu, 4);
+    const double a = rg::widen_exact(f), b = static_cast<double>(f);
+    uint64_t ua, ub;
+    memcpy(&ua, &a, 8);
+    memcpy(&ub, &b, 8);
+    if (ua != ub && !(std::isnan(a) && std::isnan(b))) {
+      if (n_bad < 5) printf("widen_exact(%a) = %a\n", static_cast<double>(f), a);
+      ++n_bad;
+    }
+  }
+  for (long i = 0; i < 4000000; ++i) {
+    const uint64_t bits = (static_cast<uint64_t>(3 + g() % 2040) << 52) | (g() & 0xfffffffffffffull);
+    double t;
+    memcpy(&t, &bits, 8);
+    if (i % 5 == 0) t = std::nextafter(3.0 * std::floor(t / 3.0), 1e308);
+    const double a = rg::third_of(t), b = t / 3.0;
+    if (memcmp(&a, &b, 8) != 0) {
+      if (n_bad < 5) printf("third_of(%a) = %a, division %a\n", t, a, b);
+      ++n_bad;
+    }
+  }
+  const double special3[] = {0.0, INFINITY, NAN, 0x1p-1074, 0x1p-900, 0x1p1000, 1.7976931348623157e308, 3.0, 1.0};
+  for (double t : special3) {
+    const double a = rg::third_of(t), b = t / 3.0;
+    if (memcmp(&a, &b, 8) != 0 && !(std::isnan(a) && std::isnan(b))) {
+      printf("third_of(%a) = %a, division %a\n", t, a, b);
+      ++n_bad;
+    }
+  }
+  printf("%ld mismatches\n", n_bad);
+  return n_bad == 0 ? 0 : 1;
+}
