@@ -1,12 +1,16 @@
-// rg_convert.cuh -- float <-> double conversions on the integer pipe, and a
-// division by 3 without the FP64 division sequence.
+// rg_convert.cuh -- float <-> double conversions and double comparisons on
+// the integer pipe, and a division by 3 without the FP64 division sequence.
 //
-// GB300 issues FP64-pipe instructions, the float <-> double conversions
-// included, at 2 per clock per SM against 64 per clock for integer ones.
-// The kernels that convert many values (the FP32 copies of the per-mesh
-// geometry, the FP32-mixed update) form the results from the IEEE-754 bit
-// patterns instead.  Host-compilable, so the same code is checked against
-// the C cast on the CPU.
+// GB300 issues FP64-pipe instructions, the float <-> double conversions and
+// the double comparisons included, at about one per clock per SM against 64
+// per clock for integer ones, and its FP64 kernels leave most issue slots
+// idle.  The kernels that convert or compare many values (the FP32 copies of
+// the per-mesh geometry, the FP32-mixed update, the FP64 limiter's tests and
+// its FP32 screening) form the results from the IEEE-754 bit patterns
+// instead, with the same results as the hardware instruction for every
+// input.  (Full double orderings on the integer pipe cost the limiter more
+// in registers than they save; its min / max stay FP64 comparisons.)  Host-compilable, so the same
+// code is checked against the C casts and operators on the CPU.
 #pragma once
 
 #include <math.h>
@@ -89,6 +93,43 @@ RG_CONV_FN double widen_exact(float f) {
   if (ex == 0u && mant != 0u) return static_cast<double>(f);
   const uint32_t dex = ex == 0u ? 0u : (ex == 0xffu ? 0x7ffu : ex + 896u);  // rebias 127 -> 1023
   return conv_double((u & 0x80000000u) | (dex << 20) | (mant >> 3), mant << 29);
+}
+
+// ---------------------------------------------------------------- comparisons
+// IEEE-754 semantics: false when either operand is NaN, -0 == +0.
+
+constexpr uint64_t kMagMask = 0x7fffffffffffffffull;
+constexpr uint64_t kInfBits64 = 0x7ff0000000000000ull;
+
+// |a| > t for t >= 0 or NaN
+RG_CONV_FN bool abs_gt(double a, double t) {
+  const uint64_t ma = conv_dbits(a) & kMagMask, ut = conv_dbits(t);
+  return ma <= kInfBits64 && ut <= kInfBits64 && ma > ut;
+}
+// |a| in [lo, hi] for 0 < lo <= hi finite (the FP32 screening range test)
+RG_CONV_FN bool abs_within(double a, double lo, double hi) {
+  const uint64_t ma = conv_dbits(a) & kMagMask;
+  return ma >= conv_dbits(lo) && ma <= conv_dbits(hi);
+}
+// a * b < 0 as the FP64 multiply rounds it.  Nonzero normal operands whose
+// exponents sum to at least -1020 give a product of at least 2^-1020 in
+// magnitude: negative exactly when the signs differ.  Zeros give a zero or
+// NaN product; infinities, NaNs, subnormals and tiny products take the
+// multiply.
+RG_CONV_FN bool prod_neg(double a, double b) {
+  const uint64_t ua = conv_dbits(a), ub = conv_dbits(b);
+  const uint32_t ea = static_cast<uint32_t>(ua >> 52) & 0x7ffu, eb = static_cast<uint32_t>(ub >> 52) & 0x7ffu;
+  if (((ua | ub) & kMagMask) != 0u && ((ua & kMagMask) == 0u || (ub & kMagMask) == 0u)) {
+    // one zero and one nonzero: a zero product, or NaN for an infinity
+    return false;
+  }
+  if (ea - 1u < 2046u && eb - 1u < 2046u && ea + eb >= 1026u) return ((ua ^ ub) >> 63) != 0u;
+#ifdef __CUDA_ARCH__
+  return __dmul_rn(a, b) < 0;
+#else
+  const volatile double p = a * b;
+  return p < 0;
+#endif
 }
 
 // t / 3 rounded to nearest (t >= 0) without a division.  RN(1/3) is 1/3

@@ -326,8 +326,8 @@ __device__ __forceinline__ void k_slopes_item(const StepArgs& a, int i) {
       const double gp = gamma_at<kBatch>(a, i) * cell.p;
       bool decided = false;
       if (fp32_safe(lhs) && fp32_safe(gp) && fp32_safe(cell.d)) {
-        const float rhs_f = static_cast<float>(a.delta_v) * sqrtf(static_cast<float>(gp) / static_cast<float>(cell.d));
-        const float l_f = -static_cast<float>(lhs);
+        const float rhs_f = narrow(a.delta_v) * sqrtf(narrow(gp) / narrow(cell.d));
+        const float l_f = -narrow(lhs);
         if (l_f > rhs_f * 1.000002f) {
           shock = true;
           decided = true;
@@ -340,13 +340,13 @@ __device__ __forceinline__ void k_slopes_item(const StepArgs& a, int i) {
     if (!shock && nn == 0) shock = 1.0 < a.delta_p;  // PressureRatio of no neighbours is 1
     if (!shock) {
       // PressureRatio < delta_p  <=>  some neighbour's ratio < delta_p
-      const float dp_f = static_cast<float>(a.delta_p);
+      const float dp_f = narrow(a.delta_p);
       for (int k = 0; k < nn && !shock; ++k) {
         const double np_ = point_state(a, static_cast<int>(a.geom.nbr[b + k] & kNbrIdMask)).p;
         const double num = cell.p > np_ ? np_ : cell.p;
         const double den = cell.p > np_ ? cell.p : np_;
         if (fp32_safe(num) && fp32_safe(den)) {
-          const float rf = static_cast<float>(num) / static_cast<float>(den);
+          const float rf = narrow(num) / narrow(den);
           if (rf < dp_f * 0.999999f) {
             shock = true;
             break;

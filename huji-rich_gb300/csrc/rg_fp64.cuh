@@ -89,27 +89,26 @@ __device__ __forceinline__ double step_dt(const StepArgs& a) {
 // exact FP64 division otherwise.  For |a|,|b| in [2^-120, 2^120] the
 // estimate float(a)/float(b) is within 4 * 2^-24 < 2.5e-7 (relative) of
 // a/b; the margins below are 1e-6, with float(t) itself within 6e-8 of t.
-__device__ __forceinline__ bool fp32_safe(double a) {
-  const double m = fabs(a);
-  return m >= 1e-36 && m <= 1e36;
-}
+// The range tests, the roundings to float and the limiter's |dphi| > thr and
+// sign-of-product tests run on the integer pipe (rg_convert.cuh).
+__device__ __forceinline__ bool fp32_safe(double a) { return abs_within(a, 1e-36, 1e36); }
 
 // psi_f = float(psi) is a usable screen when psi is 0 or a normal float.
 __device__ __forceinline__ bool psi_screenable(double psi, float psi_f) {
-  return psi_f >= 1e-30f || psi == 0.0;
+  return psi_f >= 1e-30f || (conv_dbits(psi) & kMagMask) == 0u;
 }
 
 // smin(psi, num/den) for num/den >= 0 (or NaN, which smin ignores), psi >= 0:
 // skips the division when the quotient is provably >= psi.
 __device__ __forceinline__ void min_quotient(double num, double den, double& psi, float& psi_f) {
   if (fp32_safe(num) && fp32_safe(den) && psi_screenable(psi, psi_f)) {
-    const float qf = static_cast<float>(num) / static_cast<float>(den);
+    const float qf = narrow(num) / narrow(den);
     if (qf >= psi_f * 1.000001f) return;
   }
   const double q = num / den;
   if (q < psi) {
     psi = q;
-    psi_f = static_cast<float>(q);
+    psi_f = narrow(q);
   }
 }
 
@@ -118,7 +117,7 @@ __device__ __forceinline__ void min_quotient(double num, double den, double& psi
 // candidate quotients are >= 0.
 __device__ __forceinline__ void limit_comp(double dphi, double cv, double cellv, double thr, double maxd,
                                            double mind, bool use_abs, double& psi, float& psi_f) {
-  if (fabs(dphi) > thr || cv * cellv < 0) {
+  if (abs_gt(dphi, thr) || prod_neg(cv, cellv)) {
     const double t1 = use_abs ? fabs(1e-9 * cellv) : 1e-9 * cellv;
     const double t2 = use_abs ? -fabs(1e-9 * cellv) : -1e-9 * cellv;
     if (dphi > t1)
@@ -133,7 +132,7 @@ __device__ __forceinline__ void limit_comp(double dphi, double cv, double cellv,
 // has it; |1e-9*q| for tracers, :377): psi = smin(psi, smax(theta*(nb-cell)/dphi, 0)).
 __device__ __forceinline__ void shocked_comp(double dphi, double cv, double cellv, double thr, double nbv,
                                              double theta, double& psi, float& psi_f, bool abs_thr = false) {
-  if (fabs(dphi) > thr || cv * cellv < 0) {
+  if (abs_gt(dphi, thr) || prod_neg(cv, cellv)) {
     if (fabs(dphi) > (abs_thr ? fabs(1e-9 * cellv) : 1e-9 * cellv)) {
       const double num = theta * (nbv - cellv);
       if (num != 0 && !isnan(num) && !isnan(dphi) && (num < 0) != (dphi < 0)) {
@@ -145,13 +144,13 @@ __device__ __forceinline__ void shocked_comp(double dphi, double cv, double cell
         return;
       }
       if (num != 0 && fp32_safe(num) && fp32_safe(dphi) && psi_screenable(psi, psi_f)) {
-        const float qf = static_cast<float>(num) / static_cast<float>(dphi);
+        const float qf = narrow(num) / narrow(dphi);
         if (qf >= psi_f * 1.000001f) return;
       }
       const double x = smax(num / dphi, 0.0);
       if (x < psi) {
         psi = x;
-        psi_f = static_cast<float>(x);
+        psi_f = narrow(x);
       }
     }
   }

@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "rg_convert.cuh"
 #include "rich_gb300.h"
 
 namespace rg {

@@ -2,9 +2,9 @@
 // the integer-pipe float <-> double conversions of the FP32-mixed kernels)
 // against the C casts, bit for bit: random bit patterns, values across the
 // float range, rounding ties and carries, the special values, and a stride
-// through every float; and rg::third_of against the division t / 3 over
-// random magnitudes and the special values.  Exit status 0 when every value
-// agrees.
+// through every float; rg::third_of against the division t / 3 over
+// random magnitudes and the special values; and the integer-pipe double
+// tests (abs_gt, abs_within, prod_neg) against the C operators.  Exit status 0 when every value agrees.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -82,6 +82,39 @@ int main() {
     const double a = rg::third_of(t), b = t / 3.0;
     if (memcmp(&a, &b, 8) != 0 && !(std::isnan(a) && std::isnan(b))) {
       printf("third_of(%a) = %a, division %a\n", t, a, b);
+      ++n_bad;
+    }
+  }
+  // comparisons: values drawn from a pool that mixes special values, zeros
+  // of both signs, subnormals, tiny and huge magnitudes and random bits
+  const double pool_special[] = {0.0, -0.0, INFINITY, -INFINITY, NAN, -NAN, 0x1p-1074, -0x1p-1074, 0x1p-1022,
+                                 -0x1p-1022, 1e-36, 1e36, 1.0, -1.0, 0x1p-511, 0x1p-510, 0x1p-509, -0x1p-512,
+                                 1.7976931348623157e308, -1.7976931348623157e308, 0x1.8p-1022, 3.0};
+  const int n_special = sizeof(pool_special) / sizeof(pool_special[0]);
+  auto draw = [&]() -> double {
+    const uint64_t r = g();
+    switch (r % 5) {
+      case 0: return pool_special[(r >> 8) % n_special];
+      case 1: {
+        uint64_t u = g();
+        double x;
+        memcpy(&x, &u, 8);
+        return x;
+      }
+      case 2: return ud(g) * std::ldexp(1.0, static_cast<int>(g() % 2100) - 1075);
+      case 3: return ud(g) * std::ldexp(1.0, static_cast<int>(g() % 40) - 20);
+      default: return std::ldexp(static_cast<double>(static_cast<int>(g() % 7) - 3), static_cast<int>(g() % 8));
+    }
+  };
+  for (long i = 0; i < 6000000; ++i) {
+    const double a = draw(), b = draw();
+    const double t = std::fabs(draw());
+    bool ok = rg::abs_gt(a, t) == (std::fabs(a) > t) &&
+              rg::abs_within(a, 1e-36, 1e36) == (std::fabs(a) >= 1e-36 && std::fabs(a) <= 1e36);
+    volatile double p = a * b;
+    ok = ok && rg::prod_neg(a, b) == (p < 0);
+    if (!ok) {
+      if (n_bad < 5) printf("comparison mismatch at a=%a b=%a t=%a\n", a, b, t);
       ++n_bad;
     }
   }

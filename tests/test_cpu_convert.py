@@ -1,7 +1,7 @@
-"""The integer-pipe float <-> double conversions of the FP32-mixed kernels
-and the division-free t / 3 of the device geometry
-(huji-rich_gb300/csrc/rg_convert.cuh) agree bit for bit with the C casts and
-the division.  The header is host-compilable: the same source is built with
+"""The integer-pipe float <-> double conversions of the FP32-mixed kernels,
+the integer-pipe double comparisons of the FP64 kernels and the
+division-free t / 3 of the device geometry (huji-rich_gb300/csrc/rg_convert.cuh)
+agree bit for bit with the C casts, operators and division.  The header is host-compilable: the same source is built with
 g++ here."""
 import os
 import shutil
