@@ -182,9 +182,10 @@ __device__ inline void grid_min_times(DevStatus* st, unsigned long long bits, do
 constexpr int kMaxBlock = 512;
 // variant: 0 the kernel's plain build (blocks of up to kMaxBlock threads);
 // the FP32-mixed slopes kernel also has 1, its neighbour loops unrolled by
-// two, and 2 and 3, register-capped builds for blocks of up to 256 threads
+// two, 2 and 3, register-capped builds for blocks of up to 256 threads
 // with 5 or 6 blocks resident per SM (more warps in flight against fewer
-// registers per thread).
+// registers per thread), and 4, which loads the neighbour words, stencil
+// records and states of cells with up to 8 neighbours before any arithmetic.
 struct LaunchShape {
   int block;
   int max_blocks;
