@@ -267,3 +267,34 @@ def test_condition_action_rules_checked():
         assert ei.value.status == 1 and ei.value.phase == 3
         h.set_flux_rules([])
         h.step()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_upload_overlapped_with_running_steps(precision):
+    """hdsim's loop on an Eulerian mesh rebuilds the same tessellation every
+    step: rg_step_async enqueues a step on one mesh slot and rg_upload_mesh
+    fills the other slot (side stream) while that step runs.  The cells and
+    extensives equal a run without the interleaved uploads, bit for bit, and
+    every upload sees the step before it finished."""
+    mesh = synthetic.lattice_mesh(192, 192, (-1.0, 1.0, -1.0, 1.0), "rigid", seed=4)
+    gamma = 5 / 3
+    cells = synthetic.sedov_cells(mesh, gamma)
+    ext0 = oracle.init_extensives(mesh, cells, gamma)
+    outs = []
+    for interleave in (False, True):
+        with handle_for(gamma, 2, 0, precision=precision) as h:
+            h.upload_mesh(mesh)
+            h.set_cells(cells)
+            h.set_extensives(ext0)
+            h.set_edge_velocities(np.zeros((mesh.n_faces, 2)))
+            dts = []
+            for _ in range(8):
+                if interleave:
+                    h.step_async()
+                    h.upload_mesh(mesh)
+                    dts.append(h.synchronize())
+                else:
+                    dts.append(h.step())
+            outs.append((h.get_cells(), h.get_extensives(), np.array(dts)))
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)
