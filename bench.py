@@ -635,15 +635,35 @@ def run_batch(args, world, rank, local_rank):
     """512 independent 2D Riemann problems (cell counts log-uniform in
     [1024, 65536], rigid walls, LinearGaussImproved + Hllc, gamma 1.4 or 5/3)
     advanced together: one launch per phase for all problems, per-problem
-    dt; also replayed from a CUDA graph of one step."""
+    dt; also replayed from a CUDA graph of one step.  With N ranks each rank
+    advances a contiguous range of the problems holding about 1/N of the
+    cells (sharding.problem_shard): no collective on the data path, the
+    timing is the maximum over ranks and `value` counts every rank's cells."""
     import torch
     import oracle
     import richgpu
     import synthetic
+    from sharding import problem_shard
 
     torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def reduce(x, op):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=op)
+        return float(t.item())
+
+    counts = [synthetic.riemann_problem_cells(p, BATCH_SEED) for p in range(args.problems)]
+    lo, hi = problem_shard(counts, world, rank)
+    if hi <= lo:
+        raise SystemExit(f"rank {rank}: no problems in its shard ({args.problems} problems, {world} ranks)")
     t0 = time.perf_counter()
-    mesh, off, gam, cells, meshes = synthetic.riemann_batch(args.problems, seed=BATCH_SEED)
+    mesh, off, gam, cells, meshes = synthetic.riemann_batch_range(range(lo, hi), seed=BATCH_SEED)
     gen_s = time.perf_counter() - t0
     ext = np.empty_like(cells)
     for p in range(len(gam)):
@@ -661,10 +681,15 @@ def run_batch(args, world, rank, local_rank):
         for _ in range(max(args.warmup, 3)):
             h.step()
         kms = []
+        if dist is not None:
+            dist.barrier()
         torch.cuda.synchronize()
         for _ in range(args.steps):
             _, k = h.step_timed()
             kms.append(k)
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
         kms = np.array(kms)
         stream = torch.cuda.ExternalStream(h.stream())
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -684,9 +709,20 @@ def run_batch(args, world, rank, local_rank):
         h.close()
     c32, c64 = res[1].pop("final_cells"), res[0].pop("final_cells")
     l1 = float(np.abs(c32[:, 0] - c64[:, 0]).sum() / np.abs(c64[:, 0]).sum())
-    n = mesh.n_cells
+    # every rank's cells over the slowest rank's step time
+    if dist is not None:
+        from torch.distributed import ReduceOp
+        l1 = reduce(l1, ReduceOp.MAX)
+        for r in res.values():
+            for key in ("ms_per_step", "graph_ms_per_step"):
+                r[key] = reduce(r[key], ReduceOp.MAX)
+    n = int(reduce(float(mesh.n_cells), dist.ReduceOp.SUM if dist is not None else None))
+    n_faces = int(reduce(float(mesh.n_faces), dist.ReduceOp.SUM if dist is not None else None))
+    if rank != 0:
+        dist.destroy_process_group()
+        return
     cpu = None
-    if not args.no_cpu:
+    if not args.no_cpu and world == 1:
         import multiprocessing as mp
         cores = min(os.cpu_count() or 1, 64)
         sample = list(range(0, args.problems, max(1, args.problems // (2 * cores))))[:2 * cores]
@@ -702,16 +738,19 @@ def run_batch(args, world, rank, local_rank):
             "ms_per_step": res[1]["ms_per_step"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
             "config": {"workload": f"riemann_batch_{args.problems}", "problems": args.problems, "cells": n,
-                       "faces": mesh.n_faces, "order": 2, "reconstruction": "LinearGaussImproved",
+                       "faces": n_faces, "order": 2, "reconstruction": "LinearGaussImproved",
                        "riemann": "Hllc", "gamma": "1.4 or 5/3 per problem", "dt": "per problem (SimpleCFL 0.3)",
                        "launch": "one launch per phase for all problems; graph of one step replayed",
-                       "generation_s": gen_s},
+                       "parallelism": f"problems sharded over {world} rank(s), contiguous ranges of ~equal cells",
+                       "rank0_problems": [lo, hi], "generation_s": gen_s},
             "l1_density_vs_fp64": l1,
             "fp32mixed": {k: v for k, v in res[1].items()},
             "fp64": {"value": n / (res[0]["ms_per_step"] * 1e-3), **res[0]},
             "graph_value_fp32mixed": n / (res[1]["graph_ms_per_step"] * 1e-3),
             "cpu_baseline": cpu, "gpu_launches": 4 * args.steps}
     print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
 
 
 def main():
@@ -734,8 +773,7 @@ def main():
     if args.impl == "reference":
         run_reference(args, world, rank)
     elif args.workload == "riemann_batch":
-        if rank == 0:
-            run_batch(args, world, rank, local_rank)
+        run_batch(args, world, rank, local_rank)
     elif args.workload == "sedov3d":
         if rank == 0:
             rec = sedov3d_block(steps=args.steps, warmup=max(args.warmup, 3), cpu=not args.no_cpu)

@@ -335,8 +335,14 @@ def riemann_batch(n_problems=512, seed=11, min_cells=1024, max_cells=65536, jitt
     right states split by a random line through the centre, density and
     pressure log-uniform in [0.1, 10], velocities uniform in [-1, 1]^2,
     gamma 1.4 or 5/3.  Returns (mesh, problem offsets, gammas, cells)."""
+    return riemann_batch_range(range(n_problems), seed, min_cells, max_cells, jitter)
+
+
+def riemann_batch_range(problems, seed=11, min_cells=1024, max_cells=65536, jitter=1e-3):
+    """The batch of the given problems of riemann_batch, in their order (one
+    rank's shard)."""
     meshes, states, gammas = [], [], []
-    for p in range(n_problems):
+    for p in problems:
         m, c, g = riemann_problem(p, seed, min_cells, max_cells, jitter)
         meshes.append(m)
         states.append(c)
@@ -345,11 +351,20 @@ def riemann_batch(n_problems=512, seed=11, min_cells=1024, max_cells=65536, jitt
     return mesh, offsets, np.array(gammas), np.concatenate(states), meshes
 
 
+def _riemann_side(rng, min_cells, max_cells):
+    count = np.exp(rng.uniform(np.log(min_cells), np.log(max_cells)))
+    return max(4, int(round(np.sqrt(count))))
+
+
+def riemann_problem_cells(p, seed=11, min_cells=1024, max_cells=65536):
+    """Cell count of problem p of riemann_batch, without building its mesh."""
+    return _riemann_side(np.random.default_rng([seed, p]), min_cells, max_cells) ** 2
+
+
 def riemann_problem(p, seed=11, min_cells=1024, max_cells=65536, jitter=1e-3):
     """Problem p of riemann_batch on its own: (mesh, cells, gamma)."""
     rng = np.random.default_rng([seed, p])
-    count = np.exp(rng.uniform(np.log(min_cells), np.log(max_cells)))
-    side = max(4, int(round(np.sqrt(count))))
+    side = _riemann_side(rng, min_cells, max_cells)
     m = lattice_mesh(side, side, (0.0, 1.0, 0.0, 1.0), "rigid", seed=seed * 100003 + p, jitter=jitter)
     ang = rng.uniform(0, 2 * np.pi)
     nrm = np.array([np.cos(ang), np.sin(ang)])
