@@ -735,7 +735,7 @@ def run_batch(args, world, rank, local_rank):
                          "(C restatement oracle/rich_oracle.c)"}
     line = {"metric": METRIC, "value": n / (res[1]["ms_per_step"] * 1e-3), "unit": UNIT,
             "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3),
-            "ms_per_step": res[1]["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": res[1]["ms_per_step"], "higher_is_better": True, "scaling": "strong",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
             "config": {"workload": f"riemann_batch_{args.problems}", "problems": args.problems, "cells": n,
                        "faces": n_faces, "order": 2, "reconstruction": "LinearGaussImproved",
