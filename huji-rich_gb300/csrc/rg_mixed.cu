@@ -377,12 +377,18 @@ __device__ __forceinline__ void k_slopes32_item(const MixedArgs& a, int i) {
     addm(vy, s, en.y);
     amax = C4{fmaxf(amax.d, nb.d), fmaxf(amax.p, nb.p), fmaxf(amax.vx, nb.vx), fmaxf(amax.vy, nb.vy)};
     amin = C4{fminf(amin.d, nb.d), fminf(amin.p, nb.p), fminf(amin.vx, nb.vx), fminf(amin.vy, nb.vy)};
-    if (!(w & kNbrMirror)) {
+    if (boundary && !(w & kNbrMirror)) {
       nmax = C4{fmaxf(nmax.d, nb.d), fmaxf(nmax.p, nb.p), fmaxf(nmax.vx, nb.vx), fmaxf(nmax.vy, nb.vy)};
       nmin = C4{fminf(nmin.d, nb.d), fminf(nmin.p, nb.p), fminf(nmin.vx, nb.vx), fminf(nmin.vy, nb.vy)};
     }
     // min(p, p_k) / max(p, p_k) < delta_p without the division
     ratio_shock = ratio_shock || fminf(cell.p, nb.p) < a.delta_p * fmaxf(cell.p, nb.p);
+  }
+  if (!boundary) {
+    // a cell with a self-mirror neighbour takes the boundary slope: every
+    // other cell's neighbours count in both extrema
+    nmax = amax;
+    nmin = amin;
   }
   // boundary cells: vx, vy hold sum(df*dx), sum(df*dy)
   C4 sx, sy;
@@ -470,11 +476,17 @@ __device__ __forceinline__ void k_slopes32_pf_item(const MixedArgs& a, int i) {
     addm(vy, s, en.y);
     amax = C4{fmaxf(amax.d, nb.d), fmaxf(amax.p, nb.p), fmaxf(amax.vx, nb.vx), fmaxf(amax.vy, nb.vy)};
     amin = C4{fminf(amin.d, nb.d), fminf(amin.p, nb.p), fminf(amin.vx, nb.vx), fminf(amin.vy, nb.vy)};
-    if (!(wk[k] & kNbrMirror)) {
+    if (boundary && !(wk[k] & kNbrMirror)) {
       nmax = C4{fmaxf(nmax.d, nb.d), fmaxf(nmax.p, nb.p), fmaxf(nmax.vx, nb.vx), fmaxf(nmax.vy, nb.vy)};
       nmin = C4{fminf(nmin.d, nb.d), fminf(nmin.p, nb.p), fminf(nmin.vx, nb.vx), fminf(nmin.vy, nb.vy)};
     }
     ratio_shock = ratio_shock || fminf(cell.p, nb.p) < a.delta_p * fmaxf(cell.p, nb.p);
+  }
+  if (!boundary) {
+    // a cell with a self-mirror neighbour takes the boundary slope: every
+    // other cell's neighbours count in both extrema
+    nmax = amax;
+    nmin = amin;
   }
   C4 sx, sy;
   naive_slope(boundary, vx, vy, mi, sx, sy);
