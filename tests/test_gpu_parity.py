@@ -6,6 +6,8 @@ come from synthetic.lattice_mesh and are checked against the oracle
 (oracle/rich_oracle.c), which is pinned to the reference by
 test_oracle_golden.py.
 """
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -298,3 +300,52 @@ def test_upload_overlapped_with_running_steps(precision):
             outs.append((h.get_cells(), h.get_extensives(), np.array(dts)))
     for a, b in zip(*outs):
         assert np.array_equal(a, b)
+
+
+TINY = [(1, "rigid"), (2, "rigid"), (3, "rigid"), (2, "periodic"), (3, "periodic"), (5, "periodic")]
+
+
+@pytest.mark.parametrize("nx,boundary", TINY)
+@pytest.mark.parametrize("order", [1, 2])
+def test_tiny_meshes_vs_oracle(nx, boundary, order):
+    """The smallest tessellations: one cell walled in by four ghosts, 2x2
+    and 3x3 lattices whose periodic images make a cell its own neighbour's
+    neighbour several times over.  Five steps, bit for bit; the FP32-mixed
+    path runs them too."""
+    mesh = synthetic.lattice_mesh(nx, nx, (0.0, 1.0, 0.0, 1.0), boundary, seed=3)
+    cells = synthetic.bumps_cells(mesh) if boundary == "periodic" else synthetic.sod_cells(mesh)
+    gamma, ghost_kind = 1.4, 1 if boundary == "periodic" else 0
+    ext = oracle.init_extensives(mesh, cells, gamma)
+    ev = np.zeros((mesh.n_faces, 2))
+    c_ref, e_ref, dt_ref = oracle.run(mesh, cells, ext, ev, gamma, 5, order=order,
+                                      lp=oracle.lgi_params(ghost_kind=ghost_kind))
+    for precision in (0, 1):
+        with handle_for(gamma, order, ghost_kind, precision=precision) as h:
+            h.upload_mesh(mesh)
+            h.set_cells(cells)
+            h.set_extensives(ext)
+            h.set_edge_velocities(ev)
+            dts = h.run(5)
+            c, e = h.get_cells(), h.get_extensives()
+        if precision == 0:
+            exact(c, c_ref)
+            exact(e, e_ref)
+            assert np.array_equal(dts, dt_ref)
+        else:
+            assert np.all(np.isfinite(c))
+            assert np.allclose(c[:, 0], c_ref[:, 0], rtol=1e-4)
+
+
+def test_empty_mesh_rejected():
+    """A view with no cells is refused on the host, before any device work."""
+    mesh = synthetic.lattice_mesh(4, 4, (0.0, 1.0, 0.0, 1.0), "periodic", seed=1)
+    with handle_for(1.4, 2, 1) as h:
+        v = mesh.view()
+        n0 = v.n_cells
+        v.n_cells = 0
+        try:
+            with pytest.raises(richgpu.RichError) as ei:
+                h._check(h.lib.rg_upload_mesh(h.h, ctypes.byref(v), 0))
+        finally:
+            v.n_cells = n0
+        assert ei.value.status == 1
