@@ -183,11 +183,14 @@ def run_fixed_dt(mesh, cells, gamma, steps, dt, lp=None):
 
 class RoFluxRule(C.Structure):
     _fields_ = [("seq", C.c_int32), ("cond", C.c_int32), ("sticker", C.c_int32), ("action", C.c_int32),
-                ("in_", C.c_int32)]
+                ("in_", C.c_int32), ("massflux", C.c_int32)]
 
 
 def _rules(rows):
-    rows = np.asarray(rows, dtype=np.int32).reshape(-1, 5)
+    """Rule rows (sequence, condition, sticker, action, ratchet in[, LagrangianFlux massflux bits])."""
+    rows = np.atleast_2d(np.asarray(rows, dtype=np.int32))
+    if rows.shape[1] == 5:
+        rows = np.concatenate([rows, np.zeros((len(rows), 1), np.int32)], axis=1)
     arr = (RoFluxRule * len(rows))(*[RoFluxRule(*map(int, r)) for r in rows])
     return arr, len(rows)
 
@@ -199,19 +202,31 @@ def _stickers(st):
     return st, st.ctypes.data_as(C.POINTER(C.c_uint32))
 
 
-def cas_flux(mesh, cells, ev, gamma, order, lp, rules, stickers=None):
+def cas_flux(mesh, cells, ev, gamma, order, lp, rules, stickers=None, lagrangian=False):
     """Fluxes of ConditionActionSequence (order 1) / ConditionActionSequence2
-    (order 2, LinearGaussImproved face states) with the given rule rows."""
+    (order 2, LinearGaussImproved face states) with the given rule rows; with
+    lagrangian=True also LagrangianFlux's per-face ws_ and edge_vel_."""
     out = np.zeros((mesh.n_faces, 4))
+    ws, lev = np.zeros(mesh.n_faces), np.zeros(mesh.n_faces)
     arr, nr = _rules(rules)
     st, stp = _stickers(stickers)
     err = RoError()
     _check(lib().ro_cas_flux(C.byref(mesh.view()), _d(_f64(cells)), _d(_f64(ev)), C.c_double(gamma), C.c_int(order),
-                             C.byref(lp), arr, C.c_int(nr), stp, _d(out), C.byref(err)), err)
+                             C.byref(lp), arr, C.c_int(nr), stp, _d(out), _d(ws), _d(lev), C.byref(err)), err)
+    return (out, ws, lev) if lagrangian else out
+
+
+def lagrangian_update(mesh, ws, lag_ev, dt, ext, areas=None):
+    """LagrangianExtensiveUpdater's correction of extensives already updated by
+    SimpleExtensiveUpdater (LagrangianExtensiveUpdater.cpp:8-80)."""
+    out = _f64(ext).copy()
+    lib().ro_lagrangian_update(C.byref(mesh.view()), _d(_f64(ws)), _d(_f64(lag_ev)), C.c_double(dt),
+                               None if areas is None else _d(_f64(areas)), _d(out))
     return out
 
 
-def run_cas(mesh, cells, ext, ev, gamma, steps, order, lp, rules, stickers=None, frozen_mask=0, cfl_number=0.3):
+def run_cas(mesh, cells, ext, ev, gamma, steps, order, lp, rules, stickers=None, frozen_mask=0, cfl_number=0.3,
+            lagrangian_update=False):
     cells, ext = _f64(cells).copy(), _f64(ext).copy()
     arr, nr = _rules(rules)
     st, stp = _stickers(stickers)
@@ -220,7 +235,8 @@ def run_cas(mesh, cells, ext, ev, gamma, steps, order, lp, rules, stickers=None,
         dt, err = C.c_double(), RoError()
         _check(lib().ro_step_cas(C.byref(mesh.view()), _d(cells), _d(ext), _d(_f64(ev)), C.c_double(gamma),
                                  C.c_double(cfl_number), C.c_int(order), C.byref(lp), arr, C.c_int(nr), stp,
-                                 C.c_uint32(frozen_mask), C.byref(dt), C.byref(err)), err)
+                                 C.c_uint32(frozen_mask), C.c_int(1 if lagrangian_update else 0), C.byref(dt),
+                                 C.byref(err)), err)
         dts.append(dt.value)
     return cells, ext, np.array(dts)
 

@@ -38,6 +38,7 @@
 #include <string>
 
 #include "rich_pack.hpp"
+#include "source/newtonian/common/LagrangianHLLC.hpp"
 #include "source/newtonian/common/hllc.hpp"
 #include "source/newtonian/common/ideal_gas.hpp"
 #include "source/newtonian/two_dimensional/geometric_outer_boundaries/PeriodicBox.hpp"
@@ -47,6 +48,7 @@
 #include "source/newtonian/two_dimensional/condition_action_sequence.hpp"
 #include "source/newtonian/two_dimensional/condition_action_sequence_2.hpp"
 #include "source/newtonian/two_dimensional/hdsim2d.hpp"
+#include "source/newtonian/two_dimensional/LagrangianExtensiveUpdater.hpp"
 #include "source/newtonian/two_dimensional/interpolations/LinearGaussImproved.hpp"
 #include "source/newtonian/two_dimensional/modular_flux_calculator.hpp"
 #include "source/newtonian/two_dimensional/periodic_edge_velocities.hpp"
@@ -76,8 +78,12 @@ double g_geometry[5] = {0, 0, 0, 0, 0};
 // first-order list, 1 ConditionActionSequence2's list), condition (0
 // IsBoundaryEdge, 1 IsBulkEdge, 2 RegularSpecialEdge), sticker bit, action (0
 // RegularFlux, 1 RigidWallFlux, 2 FreeFlowFlux, 3 RegularFlux2, 4
-// RigidWallFlux2, 5 Ratchet), Ratchet's `in`
+// RigidWallFlux2, 5 Ratchet, 6 LagrangianFlux), Ratchet's `in`, LagrangianFlux's
+// massflux bits (bit 0 its first LagrangianHLLC's, bit 1 its second's)
 std::vector<int32_t> g_rules;
+// the case's LagrangianFlux: its per-face ws_ / edge_vel_ are dumped after
+// the flux pass (LagrangianExtensiveUpdater reads and resets them)
+const LagrangianFlux* g_lflux = nullptr;
 
 void advance(hdsim& sim) {
   if (g_heun)
@@ -222,7 +228,7 @@ void dump_components(hdsim& sim, const PhysicalGeometry& pg, const EquationOfSta
   dump_f64("outer_box", std::vector<double>(g_box, g_box + 4), 0);
   dump_f64("motion", std::vector<double>(g_motion, g_motion + 6), 0);
   dump_f64("geometry", std::vector<double>(g_geometry, g_geometry + 5), 0);
-  if (!g_rules.empty()) dump_i32("flux_rules", g_rules, 5);
+  if (!g_rules.empty()) dump_i32("flux_rules", g_rules, 6);
   vector<Vector2D> pv = pm(tess, cells, t, tsn);
   vector<Vector2D> ev = evc(tess, pv);
   const double dt = tsf(tess, cells, eos, ev, t, tsn);
@@ -273,6 +279,10 @@ void dump_components(hdsim& sim, const PhysicalGeometry& pg, const EquationOfSta
   }
   const vector<Extensive> fl = fc(tess, ev, cells, ext, cd, eos, t, dt, tsn);
   dump_f64("fluxes", ext_flat(fl), 4);
+  if (g_lflux) {
+    dump_f64("lag_ws", g_lflux->ws_, 0);
+    dump_f64("lag_ev", g_lflux->edge_vel_, 0);
+  }
   vector<Extensive> ext1 = ext;
   eu(fl, pg, tess, dt, cd, cells, ext1, t, tsn);
   dump_f64("ext1", ext_flat(ext1), 4);
@@ -492,16 +502,16 @@ int main(int argc, char** argv) {
         seq1.push_back({new IsBoundaryEdge(), new FreeFlowFlux(rs)});
         seq1.push_back({new RegularSpecialEdge("obstacle"), new RigidWallFlux(rs)});
         seq1.push_back({new IsBulkEdge(), new RegularFlux(rs)});
-        g_rules = {0, 0, -1, 2, 0, 0, 2, 0, 1, 0, 0, 1, -1, 0, 0};
+        g_rules = {0, 0, -1, 2, 0, 0, 0, 2, 0, 1, 0, 0, 0, 1, -1, 0, 0, 0};
       } else if (which == "cas2_wall") {
         seq2.push_back({new IsBoundaryEdge(), new RigidWallFlux2(rs)});
         seq2.push_back({new RegularSpecialEdge("obstacle"), new RigidWallFlux2(rs)});
         seq2.push_back({new IsBulkEdge(), new RegularFlux2(rs)});
-        g_rules = {1, 0, -1, 4, 0, 1, 2, 0, 4, 0, 1, 1, -1, 3, 0};
+        g_rules = {1, 0, -1, 4, 0, 0, 1, 2, 0, 4, 0, 0, 1, 1, -1, 3, 0, 0};
       } else {
         seq2.push_back({new IsBoundaryEdge(), new Ratchet(rs, false)});
         seq2.push_back({new IsBulkEdge(), new RegularFlux2(rs)});
-        g_rules = {1, 0, -1, 5, 0, 1, 1, -1, 3, 0};
+        g_rules = {1, 0, -1, 5, 0, 0, 1, 1, -1, 3, 0, 0};
       }
       CAS fc1(seq1);
       ConditionActionSequence2 fc2(seq1, seq2, sr);
@@ -544,6 +554,64 @@ int main(int argc, char** argv) {
       }
       dump_components(sim, pg, eos, eul, evc, tsf, fc, eu, ocu, first ? nullptr : &sr);
       if (run > 0) run_and_dump(sim, run);
+    } else if (which == "cas2_lag" || which == "cas2_lag_move") {
+      // LagrangianFlux (condition_action_sequence_2.cpp:252-294) with
+      // LinearGaussImproved face states and two LagrangianHLLC solvers
+      // chosen by WallsMassFlux, and LagrangianExtensiveUpdater around
+      // SimpleExtensiveUpdater, on [0,1]^2 with reflecting walls:
+      //  cas2_lag: Eulerian; {(IsBoundaryEdge, RigidWallFlux2),
+      //    (IsBulkEdge, LagrangianFlux(LagrangianHLLC(false), LagrangianHLLC(true)))};
+      //  cas2_lag_move: Lagrangian point motion; {(IsBulkEdge, LagrangianFlux),
+      //    (IsBoundaryEdge, LagrangianFlux)} with LagrangianHLLC(true),
+      //    LagrangianHLLC(false) (the wall faces take the second: WallsMassFlux
+      //    is false where a ghost mirrors its cell).
+      SquareBox outer(Vector2D(0, 0), Vector2D(1, 1));
+      g_box[0] = 0, g_box[1] = 1, g_box[2] = 0, g_box[3] = 1;
+      VoronoiMesh tess(jittered_lattice(nx, ny, 0, 1, 0, 1, 8, 1e-3), outer);
+      IdealGas eos(5. / 3.);
+      const bool move = which == "cas2_lag_move";
+      Eulerian eul;
+      Lagrangian lag;
+      const PointMotion& pm = move ? static_cast<const PointMotion&>(lag) : static_cast<const PointMotion&>(eul);
+      g_motion[0] = move ? 1 : 0;
+      StationaryBox evc;
+      RigidWallGenerator gpg;
+      LinearGaussImproved sr(eos, gpg);
+      LagrangianHLLC lrs1(move), lrs2(!move);  // massflux: false, true (cas2_lag); true, false (cas2_lag_move)
+      WallsMassFlux walls;
+      LagrangianFlux lflux(lrs1, lrs2, walls);
+      g_lflux = &lflux;
+      typedef ConditionActionSequence CAS;
+      vector<pair<const CAS::Condition*, const CAS::Action*> > seq1;
+      vector<pair<const CAS::Condition*, const ConditionActionSequence2::Action2*> > seq2;
+      if (!move) {
+        seq2.push_back({new IsBoundaryEdge(), new RigidWallFlux2(rs)});
+        seq2.push_back({new IsBulkEdge(), &lflux});
+        g_rules = {1, 0, -1, 4, 0, 0, 1, 1, -1, 6, 0, 2};
+      } else {
+        seq2.push_back({new IsBulkEdge(), &lflux});
+        seq2.push_back({new IsBoundaryEdge(), &lflux});
+        g_rules = {1, 1, -1, 6, 0, 1, 1, 0, -1, 6, 0, 1};
+      }
+      ConditionActionSequence2 fc(seq1, seq2, sr);
+      SimpleExtensiveUpdater beu;
+      LagrangianExtensiveUpdater leu(lflux, beu);
+      vector<ComputationalCell> ic(static_cast<size_t>(tess.GetPointNo()));
+      for (size_t i = 0; i < ic.size(); ++i) {
+        const Vector2D r = tess.GetMeshPoint(static_cast<int>(i));
+        ic[i].density = 1 + 0.3 * std::sin(6.283185307179586 * (r.x + 0.5 * r.y));
+        ic[i].pressure = abs(r - Vector2D(0.4, 0.55)) < 0.15 ? 4.0 : 0.6;
+        ic[i].velocity = Vector2D(0.25 * std::cos(6.283185307179586 * r.y), -0.15 * std::sin(6.283185307179586 * r.x));
+      }
+      hdsim sim(tess, outer, pg, ic, eos, pm, evc, force, tsf, fc, leu, cu);
+      for (int s = 0; s < warm; ++s) advance(sim);
+      dump_scalar("gamma", 5. / 3.);
+      dump_scalar("order", 2);
+      dump_scalar("ghost_kind", 0);
+      dump_scalar("lagrangian_updater", 1);
+      dump_components(sim, pg, eos, pm, evc, tsf, fc, leu, cu, &sr);
+      if (run > 0) run_and_dump(sim, run);
+      g_lflux = nullptr;
     } else if (which == "cyl_blast") {
       // Cylindrical symmetry about the y axis (r = x) on [0,1]^2: a blast at
       // the origin corner, Eulerian, LinearGaussImproved + rigid walls; the

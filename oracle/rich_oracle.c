@@ -193,6 +193,80 @@ static int hllc(prim left, prim right, double velocity, cons* out, int64_t face,
   return 0;
 }
 
+/* LagrangianHLLC.cpp:85-175 LagrangianHLLC::operator(): Hllc's flux, with
+ * massflux = 0 taken in the frame of the contact (estimate_wave_speeds of the
+ * boosted states), and the transferred internal energy `energy` (the
+ * contact speed when massflux = 0) */
+static int lhllc(prim left, prim right, double velocity, int massflux, cons* out, double* energy, int64_t face,
+                 ro_error* err) {
+  if (isnan(right.vx)) {
+    set_err(err, RG_ERR_HLLC_NAN, 3, face, right.vx);
+    return RG_ERR_HLLC_NAN;
+  }
+  const double bx = 1 * velocity, by = 0 * velocity;
+  left.vx -= bx;
+  left.vy -= by;
+  right.vx -= bx;
+  right.vy -= by;
+  double en = 0;
+  if (!massflux) {
+    const double sl2 = smin(left.vx - left.c, right.vx - right.c);
+    const double sr2 = smax(left.vx + left.c, right.vx + right.c);
+    const double ss2 = (right.p - left.p + left.d * left.vx * (sl2 - left.vx) - right.d * right.vx * (sr2 - right.vx)) /
+                       (left.d * (sl2 - left.vx) - right.d * (sr2 - right.vx));
+    const double cx = ss2 * 1, cy = ss2 * 0;
+    left.vx -= cx;
+    left.vy -= cy;
+    right.vx -= cx;
+    right.vy -= cy;
+    velocity += ss2;
+    en = ss2;
+  }
+  const double dl = left.d, pl = left.p, vl = left.vx, cl = left.c;
+  const double dr = right.d, pr = right.p, vr = right.vx, cr = right.c;
+  const double sl = smin(vl - cl, vr - cr);
+  const double sr = smax(vl + cl, vr + cr);
+  const double ss = (pr - pl + dl * vl * (sl - vl) - dr * vr * (sr - vr)) / (dl * (sl - vl) - dr * (sr - vr));
+  const cons ul = p2c(left), ur = p2c(right);
+  const cons fl = p2f_x(left), fr = p2f_x(right);
+  const cons usl = starred(left, sl, ss), usr = starred(right, sr, ss);
+  const v2 xdir = {1, 0};
+  const v2 vlv = {left.vx, left.vy}, vrv = {right.vx, right.vy};
+  cons f;
+  if (sl > 0) {
+    f = fl;
+    if (massflux) en = dot(vlv, xdir) * left.e * left.d;
+  } else if (sl <= 0 && ss >= 0) {
+    f.m = fl.m + sl * (usl.m - ul.m);
+    f.mx = fl.mx + (usl.mx - ul.mx) * sl;
+    f.my = fl.my + (usl.my - ul.my) * sl;
+    f.en = fl.en + sl * (usl.en - ul.en);
+    if (massflux)
+      en = dot(vlv, xdir) * left.e * left.d + sl * left.e * ((sl - left.vx) / (sl - ss) - 1) * left.d;
+  } else if (ss < 0 && sr >= 0) {
+    f.m = fr.m + sr * (usr.m - ur.m);
+    f.mx = fr.mx + (usr.mx - ur.mx) * sr;
+    f.my = fr.my + (usr.my - ur.my) * sr;
+    f.en = fr.en + sr * (usr.en - ur.en);
+    if (massflux) en = (dot(vrv, xdir) * right.e + sr * right.e * ((sr - right.vx) / (sr - ss) - 1)) * right.d;
+  } else if (sr < 0) {
+    f = fr;
+    if (massflux) en = dot(vrv, xdir) * right.e * right.d;
+  } else {
+    set_err(err, RG_ERR_HLLC_WAVE_SPEEDS, 3, face, ss);
+    return RG_ERR_HLLC_WAVE_SPEEDS;
+  }
+  const v2 vn = {1 * velocity, 0 * velocity};
+  const v2 mom = {f.mx, f.my};
+  f.en += dot(mom, vn) + 0.5 * f.m * velocity * velocity;
+  const double vm = velocity * f.m;
+  f.mx += 1 * vm;
+  f.my += 0 * vm;
+  *out = f;
+  *energy = en;
+  return 0;
+}
+
 /* simple_flux_calculator.cpp:130-140 rotate: (Projection(v,n), Projection(v,p)) */
 static prim rotate(prim s, v2 n, v2 p) {
   const v2 v = {s.vx, s.vy};
@@ -217,6 +291,21 @@ static int rotate_solve_rotate_back(prim left, prim right, double velocity, v2 n
 }
 
 static void put_flux(double* f, cons c) { f[0] = c.m; f[1] = c.en; f[2] = c.mx; f[3] = c.my; }
+
+/* rotate_solve_rotate_back with LagrangianHLLC (LagrangianFlux, condition_action_sequence_2.cpp:284-290) */
+static int rotate_solve_rotate_back_lag(prim left, prim right, double velocity, int massflux, v2 n, v2 p, cons* out,
+                                        double* energy, int64_t face, ro_error* err) {
+  cons c;
+  const int st = lhllc(rotate(left, n, p), rotate(right, n, p), velocity, massflux, &c, energy, face, err);
+  if (st) return st;
+  const v2 a = vdiv(vscale(n, c.mx), vabs(n));
+  const v2 b = vdiv(vscale(p, c.my), vabs(p));
+  out->m = c.m;
+  out->mx = a.x + b.x;
+  out->my = a.y + b.y;
+  out->en = c.en;
+  return 0;
+}
 
 /* State of a point (real cell or ghost) as SimpleFluxCalculator sees it:
  * a ghost that is not a self-mirror takes its source cell's state (the
@@ -1130,7 +1219,7 @@ static v2 wall_normal(const rg_mesh_view* m, int e, int aux, v2 p) {
 
 int ro_cas_flux(const rg_mesh_view* m, const double* cells, const double* ev, double g, int order,
                 const ro_lgi_params* lp, const ro_flux_rule* rules, int n_rules, const uint32_t* st,
-                double* fluxes, ro_error* err) {
+                double* fluxes, double* lag_ws, double* lag_ev, ro_error* err) {
   double* ip = NULL;
   int rc = 0;
   if (order == 2) {
@@ -1165,6 +1254,26 @@ int ro_cas_flux(const rg_mesh_view* m, const double* cells, const double* ev, do
     prim l, rr;
     v2 n;
     double v = 0;
+    if (lag_ws) lag_ws[e] = 0;
+    if (lag_ev) lag_ev[e] = 0;
+    if (action == 6) {
+      /* LagrangianFlux: CAS2's calc_parallel_normal (:17-27), the face speed,
+       * WallsMassFlux (:300-312) choosing the solver, ws_ / edge_vel_ */
+      const v2 pp = parallel(m, e);
+      const int N = m->n_cells;
+      const v2 nn = (a >= 0 && a < N) ? remove_parallel(vsub(vert0(m, e), point(m, a)), pp)
+                                      : remove_parallel(vsub(point(m, b), vert0(m, e)), pp);
+      const double speed = dot(nn, w) / vabs(nn);
+      const int lag = orig(m, a) != orig(m, b);
+      const int mf = lag ? (r->massflux & 1) : ((r->massflux >> 1) & 1);
+      double energy = 0;
+      rc = rotate_solve_rotate_back_lag(to_prim(g, s0), to_prim(g, s1), speed, mf, nn, pp, &c, &energy, e, err);
+      if (rc) break;
+      put_flux(fluxes + 4 * e, c);
+      if (lag_ws) lag_ws[e] = lag ? energy : 0;
+      if (lag_ev) lag_ev[e] = speed;
+      continue;
+    }
     if (action == 0 || action == 3) {
       /* RegularFlux (condition_action_sequence.cpp:84-110), RegularFlux2
        * (condition_action_sequence_2.cpp:129-157) */
@@ -1189,18 +1298,43 @@ int ro_cas_flux(const rg_mesh_view* m, const double* cells, const double* ev, do
   return rc;
 }
 
+void ro_lagrangian_update(const rg_mesh_view* m, const double* ws, const double* ev, double dt,
+                          const double* areas, double* ext) {
+  for (int i = 0; i < m->n_cells; ++i) {
+    double dv = 0, dvw = 0;
+    for (int k = m->cell_face_offset[i]; k < m->cell_face_offset[i + 1]; ++k) {
+      const int e = m->cell_faces[k];
+      const double area = areas ? areas[e] : edge_length(m, e);
+      if (fc0(m, e) == i) {
+        dv += area * dt * ev[e];
+        dvw += area * dt * ws[e];
+      } else {
+        dv -= area * dt * ev[e];
+        dvw -= area * dt * ws[e];
+      }
+    }
+    const double V = m->cd_volume[i];
+    const double a = (V + dv) / (V + dv + dvw);
+    for (int c = 0; c < 4; ++c) ext[4 * i + c] *= a;
+  }
+}
+
 int ro_step_cas(const rg_mesh_view* m, double* cells, double* ext, const double* ev, double g, double cfl,
                 int order, const ro_lgi_params* lp, const ro_flux_rule* rules, int n_rules, const uint32_t* st,
-                uint32_t frozen_mask, double* dt_out, ro_error* err) {
+                uint32_t frozen_mask, int lagrangian_update, double* dt_out, ro_error* err) {
   double dt;
   int rc = ro_cfl(m, cells, ev, g, cfl, &dt, err);
   if (rc) return rc;
   const size_t N = (size_t)m->n_cells;
-  double* fl = (double*)malloc(sizeof(double) * 4 * (size_t)(m->n_faces > 0 ? m->n_faces : 1));
+  const size_t E = (size_t)(m->n_faces > 0 ? m->n_faces : 1);
+  double* fl = (double*)malloc(sizeof(double) * 4 * E);
+  double* ws = (double*)calloc(E, sizeof(double));
+  double* lev = (double*)calloc(E, sizeof(double));
   double* old = (double*)malloc(sizeof(double) * 4 * N);
   memcpy(old, cells, sizeof(double) * 4 * N);
-  rc = ro_cas_flux(m, cells, ev, g, order, lp, rules, n_rules, st, fl, err);
+  rc = ro_cas_flux(m, cells, ev, g, order, lp, rules, n_rules, st, fl, ws, lev, err);
   if (!rc) rc = ro_extensive_update(m, fl, dt, ext, err);
+  if (!rc && lagrangian_update) ro_lagrangian_update(m, ws, lev, dt, NULL, ext);
   if (!rc) {
     ro_tracers t;
     memset(&t, 0, sizeof t);
@@ -1210,6 +1344,8 @@ int ro_step_cas(const rg_mesh_view* m, double* cells, double* ext, const double*
     rc = ro_cell_update_tr(m, ext, NULL, old, NULL, g, &t, cells, NULL, err);
   }
   free(fl);
+  free(ws);
+  free(lev);
   free(old);
   if (dt_out) *dt_out = dt;
   return rc;

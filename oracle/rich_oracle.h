@@ -108,18 +108,31 @@ void ro_cell_geometry(const rg_mesh_view* m, int ghost_kind, const double* box, 
  * evaluated first) or 1 (ConditionActionSequence2's list); cond 0
  * IsBoundaryEdge, 1 IsBulkEdge, 2 RegularSpecialEdge(sticker bit); action 0
  * RegularFlux, 1 RigidWallFlux, 2 FreeFlowFlux (cell states), 3 RegularFlux2,
- * 4 RigidWallFlux2, 5 Ratchet(in) (LinearGaussImproved face states, lp). */
+ * 4 RigidWallFlux2, 5 Ratchet(in), 6 LagrangianFlux (LinearGaussImproved face
+ * states, lp).  LagrangianFlux (condition_action_sequence_2.cpp:252-294) has
+ * two LagrangianHLLC solvers, the first where WallsMassFlux holds (the face
+ * is not a self-mirror), the second elsewhere; massflux bit 0 / bit 1 are
+ * their LagrangianHLLC(massflux) flags.  lag_ws / lag_ev (NULL allowed)
+ * receive the action's ws_ / edge_vel_ per face, zero for other actions. */
 typedef struct ro_flux_rule {
-  int32_t seq, cond, sticker, action, in;
+  int32_t seq, cond, sticker, action, in, massflux;
 } ro_flux_rule;
 int ro_cas_flux(const rg_mesh_view* m, const double* cells, const double* ev, double gamma, int order,
                 const ro_lgi_params* lp, const ro_flux_rule* rules, int n_rules, const uint32_t* stickers,
-                double* fluxes, ro_error* err);
+                double* fluxes, double* lag_ws, double* lag_ev, ro_error* err);
+/* LagrangianExtensiveUpdater (LagrangianExtensiveUpdater.cpp:8-80) after the
+ * base update: per cell dV = sum area*dt*edge_vel and dv_ws = sum area*dt*ws
+ * over its faces (+ as the first neighbour, - as the second, in face order),
+ * then every extensive times (V + dV) / (V + dV + dv_ws), V the CacheData
+ * volume; areas NULL = the edge lengths (SlabSymmetry) */
+void ro_lagrangian_update(const rg_mesh_view* m, const double* lag_ws, const double* lag_ev, double dt,
+                          const double* areas, double* ext);
 /* hdsim::TimeAdvance with a condition/action flux calculator on a fixed
- * mesh; cells with a bit of frozen_mask keep their state (SkipUpdate) */
+ * mesh; cells with a bit of frozen_mask keep their state (SkipUpdate);
+ * lagrangian_update: LagrangianExtensiveUpdater around SimpleExtensiveUpdater */
 int ro_step_cas(const rg_mesh_view* m, double* cells, double* ext, const double* ev, double gamma, double cfl,
                 int order, const ro_lgi_params* lp, const ro_flux_rule* rules, int n_rules, const uint32_t* stickers,
-                uint32_t frozen_mask, double* dt_out, ro_error* err);
+                uint32_t frozen_mask, int lagrangian_update, double* dt_out, ro_error* err);
 
 /* CylindricalSymmetry (physical_geometry.cpp:62-110) about the axis through
  * origin along direction (normalised as Axis does): CacheData's face areas

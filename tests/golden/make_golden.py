@@ -56,6 +56,10 @@ CASES = {
     "cas_free_o1": ("cas_free", 24, 24, 2, 10),
     "cas2_wall_o2": ("cas2_wall", 24, 24, 2, 10),
     "cas2_ratchet_o2": ("cas2_ratchet", 24, 24, 2, 10),
+    # LagrangianFlux (LagrangianHLLC pair, WallsMassFlux) + LagrangianExtensiveUpdater:
+    # Eulerian with 10 hdsim steps, and one pass on Lagrangian-moving faces
+    "cas2_lag_o2": ("cas2_lag", 24, 24, 2, 10),
+    "cas2_lag_move_o2": ("cas2_lag_move", 24, 24, 2, 0),
 }
 
 # Tracers and stickers (ref_dump's <case>_tracers forms), written to

@@ -50,6 +50,12 @@ def stickers_of(g):
     return g["tr_stickers"].astype(np.uint32) if "tr_stickers" in g else None
 
 
+def lagrangian(g):
+    """LagrangianExtensiveUpdater around SimpleExtensiveUpdater (its
+    LagrangianFlux's ws_ / edge_vel_ are in lag_ws / lag_ev)."""
+    return "lagrangian_updater" in g
+
+
 def test_fluxes(golden):
     g = golden
     if flux_rules(g) is not None:
@@ -89,7 +95,22 @@ def test_extensive_update(golden):
         ext1 = oracle.extensive_update_areas(g["mesh"], g["fluxes"], areas_of(g), g["dt"], g["ext0"])
     else:
         ext1 = oracle.extensive_update(g["mesh"], g["fluxes"], g["dt"], g["ext0"])
+    if lagrangian(g):
+        ext1 = oracle.lagrangian_update(g["mesh"], g["lag_ws"], g["lag_ev"], g["dt"], ext1)
     exact(ext1, g["ext1"])
+
+
+def test_lagrangian_flux_ws_and_face_speeds(golden):
+    """LagrangianFlux's per-face outputs: LagrangianHLLC's transferred energy
+    (the contact speed for massflux = false) where WallsMassFlux holds, 0
+    elsewhere, and every face's speed along its normal."""
+    g = golden
+    if not lagrangian(g):
+        pytest.skip("no LagrangianFlux in this case")
+    _, ws, lev = oracle.cas_flux(g["mesh"], g["cells0"], g["ev_flux"], g["gamma"], g["order"], lp_of(g),
+                                 flux_rules(g), stickers_of(g), lagrangian=True)
+    exact(ws, g["lag_ws"])
+    exact(lev, g["lag_ev"])
 
 
 def test_cell_update(golden):
@@ -116,7 +137,8 @@ def test_hdsim_run(golden):
     if flux_rules(g) is not None:
         st = stickers_of(g)
         cells, ext, dts = oracle.run_cas(g["mesh"], g["cells0"], g["ext0"], ev, g["gamma"], steps, g["order"],
-                                         lp_of(g), flux_rules(g), st, 1 if st is not None else 0)
+                                         lp_of(g), flux_rules(g), st, 1 if st is not None else 0,
+                                         lagrangian_update=lagrangian(g))
     else:
         cells, ext, dts = oracle.run(g["mesh"], g["cells0"], g["ext0"], ev, g["gamma"], steps,
                                      0.3, g["order"], lp_of(g), heun=g["heun"], areas=areas_of(g))
@@ -140,7 +162,7 @@ def oracle_pass(g, cells, ext, ev, steps=1, heun=None):
     if flux_rules(g) is not None:
         st = stickers_of(g)
         return oracle.run_cas(g["mesh"], cells, ext, ev, g["gamma"], steps, g["order"], lp_of(g), flux_rules(g), st,
-                              1 if st is not None else 0)
+                              1 if st is not None else 0, lagrangian_update=lagrangian(g))
     return oracle.run(g["mesh"], cells, ext, ev, g["gamma"], steps, 0.3, g["order"], lp_of(g), heun=heun,
                       areas=areas_of(g))
 
