@@ -211,6 +211,12 @@ rg::StepArgs step_args(rg_handle* h) {
     a.rules[k][2] = r.sticker;
     a.rules[k][3] = r.action;
     a.rules[k][4] = r.ratchet_in;
+    a.rules[k][5] = r.massflux;
+  }
+  if (h->lag_rule && h->lag_ws.p) {
+    a.lag_ws = static_cast<double*>(h->lag_ws.p);
+    a.lag_ev = static_cast<double*>(h->lag_ev.p);
+    a.lag_update = h->lag_update ? 1 : 0;
   }
   if (tracers_on(h)) {
     a.stickers = static_cast<const uint32_t*>(h->stickers.p);
@@ -523,6 +529,8 @@ rg_status rg_destroy(rg_handle* h) {
   }
   adjoint_release(h);
   tracer_release(h);
+  h->lag_ws.release();
+  h->lag_ev.release();
   h->pv.release();
   h->flag_buf.release();
   h->cells.release();
@@ -753,6 +761,7 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t flags) {
   h->active = next;
   s.valid = true;
   if (tracers_on(h)) RG_TRY(tracer_buffers(h));
+  RG_TRY(lagrangian_buffers(h));
   h->last_upload_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   (void)ms;
   if (h->cfg.order == 2 && s.geom_error.status) {

@@ -449,6 +449,25 @@ __device__ __forceinline__ bool solve_face(Prim l, Prim r, double velocity, doub
   return true;
 }
 
+// rotate / LagrangianHLLC / rotate_back (LagrangianFlux, condition_action_sequence_2.cpp:284-290)
+__device__ __forceinline__ bool solve_face_lagrangian(Prim l, Prim r, double velocity, bool massflux, double2 n,
+                                                      double na, double2 p, double pa, Cons& out, double& energy,
+                                                      const StepArgs& a, int face) {
+  const double lx = (l.vx * n.x + l.vy * n.y) / na, ly = (l.vx * p.x + l.vy * p.y) / pa;
+  const double rx = (r.vx * n.x + r.vy * n.y) / na, ry = (r.vx * p.x + r.vy * p.y) / pa;
+  l.vx = lx;
+  l.vy = ly;
+  r.vx = rx;
+  r.vy = ry;
+  Cons c;
+  if (!lagrangian_hllc(l, r, velocity, massflux, c, energy, a.status, a.step, face)) return false;
+  out.m = c.m;
+  out.mx = (n.x * c.mx) / na + (p.x * c.my) / pa;
+  out.my = (n.y * c.mx) / na + (p.y * c.my) / pa;
+  out.en = c.en;
+  return true;
+}
+
 template <bool kBatch>
 __device__ __forceinline__ void write_flux(const StepArgs& a, int e, int real_side, const Cons& c, bool scaled,
                                            double area) {
@@ -612,6 +631,11 @@ __device__ __forceinline__ void k_faces_cas_item(const StepArgs& a, int e) {
     record_error(a.status, a.step, RG_ERR_INVALID_ARGUMENT, 3, e, 0.0);
     return;
   }
+  if (a.lag_ws) {
+    // LagrangianFlux::Reset: faces of other actions carry no ws / speed
+    a.lag_ws[e] = 0.0;
+    a.lag_ev[e] = 0.0;
+  }
   const dbl4 v = m.face_vertices[e];
   const double2 p = normalize2(v.z - v.x, v.w - v.y);
   const double pa = sqrt(p.x * p.x + p.y * p.y);
@@ -628,7 +652,7 @@ __device__ __forceinline__ void k_faces_cas_item(const StepArgs& a, int e) {
   }
   // LinearGaussImproved face states (order 2), as k_faces_lgi_item forms them
   Cell s0 = c0, s1 = c1;
-  if (action == RG_ACT_REGULAR2 || action == RG_ACT_RIGID_WALL2) {
+  if (action == RG_ACT_REGULAR2 || action == RG_ACT_RIGID_WALL2 || action == RG_ACT_LAGRANGIAN) {
     const int ids[2] = {fc.x, fc.y};
     const double2 dms[2] = {a.geom.dm0[e], a.geom.dm1[e]};
     Cell side[2];
@@ -657,6 +681,25 @@ __device__ __forceinline__ void k_faces_cas_item(const StepArgs& a, int e) {
     }
     s0 = side[0];
     s1 = side[1];
+  }
+  if (action == RG_ACT_LAGRANGIAN) {
+    // condition_action_sequence_2.cpp:270-294: ModularFluxCalculator's frame
+    // and face speed, WallsMassFlux (:300-312) picking rs or rs2
+    const double2 w = a.ev_zero ? make_double2(0.0, 0.0) : reinterpret_cast<const double2*>(a.ev)[e];
+    const double2 nn = a.geom.nrm[e], pp = a.geom.par[e];
+    const double na = a.geom.nabs[e], ppa = a.geom.area[e];
+    const double speed = (w.x == 0.0 && w.y == 0.0) ? 0.0 : (nn.x * w.x + nn.y * w.y) / na;
+    const bool lag = orig_of(m, fc.x) != orig_of(m, fc.y);
+    const bool mf = (((lag ? a.rules[chosen][5] : a.rules[chosen][5] >> 1)) & 1) != 0;
+    Cons c;
+    double energy = 0.0;
+    if (!solve_face_lagrangian(to_prim(g, s0), to_prim(g, s1), speed, mf, nn, na, pp, ppa, c, energy, a, e)) return;
+    if (a.lag_ws) {
+      a.lag_ws[e] = lag ? energy : 0.0;
+      a.lag_ev[e] = speed;
+    }
+    write_flux<false>(a, e, fc.x < m.n ? fc.x : fc.y, c, kScaled, a.geom.xarea[e]);
+    return;
   }
   Prim l, r;
   double2 n;
@@ -768,6 +811,30 @@ __device__ __forceinline__ unsigned long long k_update_item(const StepArgs& a, i
         px += dx;
         py += dy;
       }
+    }
+    if (a.lag_update) {
+      // LagrangianExtensiveUpdater.cpp:32-56: dV, dV_ws over the cell's faces
+      // in face order, then every extensive times (V + dV) / (V + dV + dV_ws)
+      const double dtl = step_dt(a);
+      double dv = 0.0, dvw = 0.0;
+      for (int k = b; k < e1; ++k) {
+        const int e = m.cell_faces[k];
+        const double ar = a.geom.xarea[e];
+        const double t1 = ar * dtl * a.lag_ev[e], t2 = ar * dtl * a.lag_ws[e];
+        if (a.geom.nbr[k] & kNbrFirst) {
+          dv += t1;
+          dvw += t2;
+        } else {
+          dv -= t1;
+          dvw -= t2;
+        }
+      }
+      const double vol = m.cd_volume[i];
+      const double f = (vol + dv) / (vol + dv + dvw);
+      mass *= f;
+      en *= f;
+      px *= f;
+      py *= f;
     }
     if (a.ext_avg) {
       // hdsim2d.cpp:311-320 average_extensive: 0.5*(mid + old)

@@ -195,6 +195,10 @@ struct rg_handle {
   // condition/action flux rules (rg_set_flux_rules)
   int n_rules = 0;
   rg_flux_rule rules[RG_MAX_FLUX_RULES];
+  // LagrangianFlux's ws_ / edge_vel_ per face (sized when a rule uses it) and
+  // LagrangianExtensiveUpdater (rg_set_lagrangian_updater)
+  rgh::DevBuf lag_ws, lag_ev;
+  bool lag_rule = false, lag_update = false;
   rgh::DevBuf tr, tr_ext, tr_slopes, tr_flux, mflux, shock, stickers;
   bool have_tr = false, have_tr_ext = false;
   int tr_n = -1, tr_e = -1;
@@ -228,6 +232,8 @@ bool tracers_on(const rg_handle* h);
 // sizes the tracer buffers for the active mesh; a new cell count clears the
 // tracer state and the stickers
 rg_status tracer_buffers(rg_handle* h);
+// sizes LagrangianFlux's per-face buffers for the active mesh (a rule uses it)
+rg_status lagrangian_buffers(rg_handle* h);
 rg::TracerArgs tracer_args(rg_handle* h);
 // NOT_READY unless the tracer state a step needs is set
 rg_status require_tracers(rg_handle* h, bool ext);

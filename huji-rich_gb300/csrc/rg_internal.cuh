@@ -241,7 +241,12 @@ struct StepArgs {
   unsigned char* shock;           // n, or nullptr
   // condition/action flux rules (0: Simple/ModularFluxCalculator)
   int n_rules;
-  int rules[RG_MAX_FLUX_RULES][5];  // sequence, condition, sticker, action, ratchet_in
+  int rules[RG_MAX_FLUX_RULES][6];  // sequence, condition, sticker, action, ratchet_in, massflux bits
+  // LagrangianFlux's per-face outputs (nullptr: no LagrangianFlux rule) and
+  // whether the extensive update applies LagrangianExtensiveUpdater's scaling
+  double* lag_ws;                 // e
+  double* lag_ev;                 // e
+  int lag_update;
   StepShapes shapes;  // launch shapes (host side; the kernels ignore it)
 };
 

@@ -133,6 +133,9 @@ class GpuContext {
   void set_flux_rules(const std::vector<rg_flux_rule>& rules) const {
     check(rg_set_flux_rules(h_, static_cast<int32_t>(rules.size()), rules.empty() ? nullptr : rules.data()));
   }
+  // LagrangianExtensiveUpdater(lflux, SimpleExtensiveUpdater) in place of
+  // SimpleExtensiveUpdater, for rules with RG_ACT_LAGRANGIAN (LagrangianFlux)
+  void set_lagrangian_updater(bool on) const { check(rg_set_lagrangian_updater(h_, on ? 1 : 0)); }
   bool tracers_configured() const { return have_tcfg_; }
 
   void upload_cells(const std::vector<ComputationalCell>& cells) const {

@@ -32,7 +32,8 @@ EXPORTS = ("rg_default_config", "rg_create", "rg_destroy", "rg_status_string", "
            "rg_set_extensive_tracers", "rg_get_extensive_tracers", "rg_set_stickers",
            "rg_get_tracer_fluxes", "rg_get_tracer_slopes", "rg_set_outer_box", "rg_set_point_motion",
            "rg_point_velocities", "rg_apply_fix", "rg_get_edge_velocities", "rg_get_geometry",
-           "rg_advance_begin", "rg_set_physical_geometry", "rg_set_tracer_fluxes", "rg_set_flux_rules")
+           "rg_advance_begin", "rg_set_physical_geometry", "rg_set_tracer_fluxes", "rg_set_flux_rules",
+           "rg_set_lagrangian_updater", "rg_get_lagrangian_faces", "rg_set_lagrangian_faces")
 
 MESH_DEVICE_GEOMETRY = 2  # RG_MESH_DEVICE_GEOMETRY
 
@@ -51,7 +52,7 @@ class RgTracerConfig(C.Structure):
 
 class RgFluxRule(C.Structure):
     _fields_ = [("sequence", C.c_int32), ("condition", C.c_int32), ("sticker", C.c_int32), ("action", C.c_int32),
-                ("ratchet_in", C.c_int32)]
+                ("ratchet_in", C.c_int32), ("massflux", C.c_int32)]
 
 
 class RgPointMotion(C.Structure):
@@ -143,6 +144,9 @@ def load(path=LIB_PATH):
         getattr(lib, f).argtypes = [vp, dp]
     lib.rg_set_stickers.argtypes = [vp, C.POINTER(C.c_uint32)]
     lib.rg_set_flux_rules.argtypes = [vp, C.c_int32, C.POINTER(RgFluxRule)]
+    lib.rg_set_lagrangian_updater.argtypes = [vp, C.c_int32]
+    lib.rg_get_lagrangian_faces.argtypes = [vp, dp, dp]
+    lib.rg_set_lagrangian_faces.argtypes = [vp, dp, dp]
     lib.rg_set_outer_box.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double]
     lib.rg_set_point_motion.argtypes = [vp, C.POINTER(RgPointMotion)]
     lib.rg_point_velocities.argtypes = [vp, dp]
@@ -392,10 +396,32 @@ class Handle:
 
     def set_flux_rules(self, rules):
         """Condition/action flux rules: rows (sequence, condition, sticker,
-        action, ratchet_in); an empty list restores the default flux calculator."""
-        rows = [tuple(int(x) for x in r) for r in np.asarray(rules, dtype=np.int64).reshape(-1, 5)]
+        action, ratchet_in[, LagrangianFlux massflux bits]); an empty list
+        restores the default flux calculator."""
+        a = np.asarray(rules, dtype=np.int64)
+        a = a.reshape(-1, a.shape[-1] if a.size else 6)
+        if a.shape[1] == 5:
+            a = np.concatenate([a, np.zeros((len(a), 1), np.int64)], axis=1)
+        rows = [tuple(int(x) for x in r) for r in a]
         arr = (RgFluxRule * max(len(rows), 1))(*[RgFluxRule(*r) for r in rows])
         self._check(self.lib.rg_set_flux_rules(self.h, len(rows), arr))
+
+    def set_lagrangian_updater(self, on=True):
+        """LagrangianExtensiveUpdater around SimpleExtensiveUpdater."""
+        self._check(self.lib.rg_set_lagrangian_updater(self.h, 1 if on else 0))
+
+    def lagrangian_faces(self):
+        """(ws_, edge_vel_) of the last flux pass's LagrangianFlux."""
+        ws, ev = np.empty(self.mesh.n_faces), np.empty(self.mesh.n_faces)
+        self._check(self.lib.rg_get_lagrangian_faces(self.h, dptr(ws), dptr(ev)))
+        return ws, ev
+
+    def set_lagrangian_faces(self, ws, edge_vel):
+        """LagrangianFlux's ws_ / edge_vel_ from the host (with set_fluxes)."""
+        a = np.ascontiguousarray(ws, dtype=np.float64)
+        b = np.ascontiguousarray(edge_vel, dtype=np.float64)
+        assert a.size == b.size == self.mesh.n_faces
+        self._check(self.lib.rg_set_lagrangian_faces(self.h, dptr(a), dptr(b)))
 
     # batches ---------------------------------------------------------------
     def set_problems(self, offsets, gammas):

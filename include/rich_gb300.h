@@ -391,7 +391,10 @@ typedef enum rg_flux_action {
   RG_ACT_FREE_FLOW = 2,    /* FreeFlowFlux (:186-220) */
   RG_ACT_REGULAR2 = 3,     /* RegularFlux2 (condition_action_sequence_2.cpp:129-157): face states */
   RG_ACT_RIGID_WALL2 = 4,  /* RigidWallFlux2 (:183-228) */
-  RG_ACT_RATCHET = 5       /* Ratchet(in) (:232-249) */
+  RG_ACT_RATCHET = 5,      /* Ratchet(in) (:232-249) */
+  RG_ACT_LAGRANGIAN = 6    /* LagrangianFlux(rs, rs2, WallsMassFlux) (:252-312): face states, a
+                              LagrangianHLLC (LagrangianHLLC.cpp:85-175) where the face is not a
+                              self-mirror (rs), another elsewhere (rs2) */
 } rg_flux_action;
 typedef struct rg_flux_rule {
   int32_t sequence;   /* 0: ConditionActionSequence's list (actions 0-2), 1: ConditionActionSequence2's (3-5) */
@@ -399,8 +402,21 @@ typedef struct rg_flux_rule {
   int32_t sticker;    /* RG_COND_SPECIAL_EDGE's sticker bit */
   int32_t action;     /* rg_flux_action */
   int32_t ratchet_in; /* Ratchet's `in` */
+  int32_t massflux;   /* LagrangianFlux: bit 0 rs's LagrangianHLLC(massflux), bit 1 rs2's */
 } rg_flux_rule;
 rg_status rg_set_flux_rules(rg_handle* h, int32_t n_rules, const rg_flux_rule* rules);
+/* LagrangianExtensiveUpdater(lflux, SimpleExtensiveUpdater)
+ * (LagrangianExtensiveUpdater.cpp:8-80) as the extensive updater (on != 0):
+ * after the flux gather every cell's extensives are multiplied by
+ * (V + dV) / (V + dV + dV_ws), dV and dV_ws the sums over its faces of
+ * area*dt times the last LagrangianFlux pass's face speed and ws (+ as the
+ * first neighbour, - as the second, in face order), V its CacheData volume.
+ * Faces of other actions carry 0 (LagrangianFlux::Reset). */
+rg_status rg_set_lagrangian_updater(rg_handle* h, int32_t on);
+/* the last flux pass's LagrangianFlux ws_ and edge_vel_ (n_faces each), and
+ * the same from the host (for fluxes given by rg_set_fluxes) */
+rg_status rg_get_lagrangian_faces(rg_handle* h, double* ws, double* edge_vel);
+rg_status rg_set_lagrangian_faces(rg_handle* h, const double* ws, const double* edge_vel);
 
 /* Tracers and stickers ---------------------------------------------------- */
 /* ComputationalCell::tracers / ::stickers (computational_cell_2d.hpp:19-36)

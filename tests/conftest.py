@@ -45,8 +45,8 @@ def set_geometry(h, g):
 
 def upload_golden(h, g, flags=0):
     """Upload the fixture's mesh with its PhysicalGeometry and, for the
-    condition/action cases, its flux rules and obstacle stickers (frozen by
-    HasSticker + SkipUpdate)."""
+    condition/action cases, its flux rules, obstacle stickers (frozen by
+    HasSticker + SkipUpdate) and LagrangianExtensiveUpdater."""
     set_geometry(h, g)
     rules = g.get("flux_rules")
     stickers = g.get("tr_stickers") if rules is not None else None
@@ -57,6 +57,8 @@ def upload_golden(h, g, flags=0):
         h.set_stickers(stickers.astype(np.uint32))
     if rules is not None:
         h.set_flux_rules(rules)
+    if "lagrangian_updater" in g:
+        h.set_lagrangian_updater(True)
 
 
 @pytest.fixture(params=GOLDEN_CASES)

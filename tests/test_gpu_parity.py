@@ -50,6 +50,9 @@ def test_golden_extensive_update_from_host_fluxes(name):
         upload_golden(h, g)
         h.set_extensives(g["ext0"])
         h.set_fluxes(g["fluxes"])
+        if "lag_ws" in g:
+            # LagrangianExtensiveUpdater reads its LagrangianFlux's face data
+            h.set_lagrangian_faces(g["lag_ws"], g["lag_ev"])
         h.extensive_update(g["dt"])
         exact(h.get_extensives(), g["ext1"])
 
@@ -252,6 +255,60 @@ def test_condition_action_large_vs_oracle():
             exact(h.get_extensives(), oe)
 
 
+@pytest.mark.parametrize("massflux", [1, 2, 3])
+def test_lagrangian_flux_large_vs_oracle(massflux):
+    """LagrangianFlux on every face (bulk faces take rs, the wall faces rs2
+    by WallsMassFlux) with LagrangianExtensiveUpdater on a 160^2 rigid box,
+    for each LagrangianHLLC massflux pairing, 10 fused steps against the
+    oracle; then one pass on moving faces with the per-face ws and speeds."""
+    mesh = synthetic.lattice_mesh(160, 160, (0.0, 1.0, 0.0, 1.0), "rigid", seed=23)
+    cells = synthetic.bumps_cells(mesh, seed=23)
+    ext = oracle.init_extensives(mesh, cells, 5 / 3)
+    ev = np.zeros((mesh.n_faces, 2))
+    lp = oracle.lgi_params(ghost_kind=0)
+    rules = [[1, 1, -1, 6, 0, massflux], [1, 0, -1, 6, 0, massflux]]
+    oc, oe, odts = oracle.run_cas(mesh, cells, ext, ev, 5 / 3, 10, 2, lp, rules, lagrangian_update=True)
+    pv = cells[:, 2:4].copy()
+    mev = synthetic.face_velocities(mesh, pv)
+    of, ows, oev = oracle.cas_flux(mesh, cells, mev, 5 / 3, 2, lp, rules, lagrangian=True)
+    with richgpu.Handle(gamma=5 / 3, order=2, ghost_kind=0, device=0) as h:
+        h.upload_mesh(mesh)
+        h.set_flux_rules(rules)
+        h.set_lagrangian_updater(True)
+        h.set_cells(cells)
+        h.set_extensives(ext)
+        h.set_edge_velocities(ev)
+        exact(h.run(10), odts)
+        exact(h.get_cells(), oc)
+        exact(h.get_extensives(), oe)
+        h.set_cells(cells)
+        h.set_edge_velocities(mev)
+        exact(h.flux(odts[0]), of)
+        ws, lev = h.lagrangian_faces()
+    exact(ws, ows)
+    exact(lev, oev)
+    assert np.count_nonzero(ows) > 0 and np.count_nonzero(oev) > 0
+
+
+@pytest.mark.parametrize("name", ["cas2_lag_o2", "cas2_lag_move_o2"])
+def test_lagrangian_faces_vs_reference(name):
+    """LagrangianFlux's per-face ws_ and edge_vel_ after a flux pass, against
+    the reference's own (the fluxes, extensives and cells of these cases are
+    in the golden-case tests above)."""
+    g = load_golden(name)
+    with handle_for(g["gamma"], g["order"], g["ghost_kind"]) as h:
+        upload_golden(h, g)
+        h.set_cells(g["cells0"])
+        h.set_extensives(g["ext0"])
+        h.set_edge_velocities(g["ev_flux"])
+        exact(h.flux(g["dt"]), g["fluxes"])
+        ws, lev = h.lagrangian_faces()
+        exact(ws, g["lag_ws"])
+        exact(lev, g["lag_ev"])
+        h.extensive_update(g["dt"])
+        exact(h.get_extensives(), g["ext1"])
+
+
 def test_condition_action_rules_checked():
     mesh = synthetic.lattice_mesh(16, 16, (0.0, 1.0, 0.0, 1.0), "rigid", seed=3)
     with richgpu.Handle(gamma=5 / 3, order=1, ghost_kind=0, device=0) as h:
@@ -260,6 +317,8 @@ def test_condition_action_rules_checked():
             h.set_flux_rules([[1, 1, -1, 3, 0]])           # ConditionActionSequence2 needs order 2
         with pytest.raises(richgpu.RichError):
             h.set_flux_rules([[0, 2, 0, 1, 0]])            # RegularSpecialEdge without stickers kept
+        with pytest.raises(richgpu.RichError):
+            h.set_flux_rules([[0, 1, -1, 6, 0, 1]])        # LagrangianFlux is a ConditionActionSequence2 action
         h.set_flux_rules([[0, 1, -1, 0, 0]])               # bulk edges only: boundary faces match nothing
         h.set_cells(synthetic.sod_cells(mesh))
         h.init_extensives()
