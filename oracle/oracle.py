@@ -408,9 +408,9 @@ def init_extensives_tr(mesh, cells, tr):
     return out
 
 
-def run_tr(mesh, cells, ext, tr, tr_ext, ev, gamma, steps, ts, cfl_number=0.3, order=2, lp=None):
-    """hdsim::TimeAdvance steps with tracers on a fixed mesh; returns
-    (cells, ext, tracers, extensive tracers, dts)."""
+def run_tr(mesh, cells, ext, tr, tr_ext, ev, gamma, steps, ts, cfl_number=0.3, order=2, lp=None, heun=False):
+    """hdsim::TimeAdvance (TimeAdvance2Heun with heun) steps with tracers on a
+    fixed mesh; returns (cells, ext, tracers, extensive tracers, dts)."""
     cells, ext = _f64(cells).copy(), _f64(ext).copy()
     tr, tr_ext = _f64(tr).copy(), _f64(tr_ext).copy()
     ev = _f64(ev)
@@ -419,9 +419,9 @@ def run_tr(mesh, cells, ext, tr, tr_ext, ev, gamma, steps, ts, cfl_number=0.3, o
     dts = []
     for _ in range(steps):
         dt, err, tc = C.c_double(), RoError(), ts.c()
-        _check(L.ro_step_tr(C.byref(mesh.view()), _d(cells), _d(ext), _d(tr), _d(tr_ext), _d(ev), C.c_double(gamma),
-                            C.c_double(cfl_number), C.c_int(order), C.byref(lp), C.byref(tc), C.byref(dt),
-                            C.byref(err)), err)
+        fn = L.ro_step_heun_tr if heun else L.ro_step_tr
+        _check(fn(C.byref(mesh.view()), _d(cells), _d(ext), _d(tr), _d(tr_ext), _d(ev), C.c_double(gamma),
+                  C.c_double(cfl_number), C.c_int(order), C.byref(lp), C.byref(tc), C.byref(dt), C.byref(err)), err)
         dts.append(dt.value)
     return cells, ext, tr, tr_ext, np.array(dts)
 

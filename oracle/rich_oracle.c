@@ -1073,6 +1073,57 @@ int ro_step_tr(const rg_mesh_view* m, double* cells, double* ext, double* tr, do
   return st;
 }
 
+int ro_step_heun_tr(const rg_mesh_view* m, double* cells, double* ext, double* tr, double* tr_ext,
+                    const double* ev, double g, double cfl, int order, const ro_lgi_params* lp, const ro_tracers* t,
+                    double* dt_out, ro_error* err) {
+  double dt;
+  int st = ro_cfl(m, cells, ev, g, cfl, &dt, err);
+  if (st) return st;
+  const int nt = t ? t->n : 0;
+  const size_t E = (size_t)(m->n_faces > 0 ? m->n_faces : 1), N = (size_t)m->n_cells;
+  const size_t ntr = N * (size_t)(nt > 0 ? nt : 1);
+  double* fl = (double*)malloc(sizeof(double) * 4 * E);
+  double* tfl = (double*)malloc(sizeof(double) * E * (nt > 0 ? nt : 1));
+  double* mid = (double*)malloc(sizeof(double) * 4 * N);
+  double* mid_cells = (double*)malloc(sizeof(double) * 4 * N);
+  double* mid_tr = (double*)malloc(sizeof(double) * ntr);
+  double* mid_tr_ext = (double*)malloc(sizeof(double) * ntr);
+  memcpy(mid, ext, sizeof(double) * 4 * N);
+  if (nt > 0) memcpy(mid_tr_ext, tr_ext, sizeof(double) * N * nt);
+  /* first half: fluxes of the step's cells, mid = ext + dt*area*F1, mid cells */
+  st = order == 1 ? ro_simple_flux_tr(m, cells, tr, ev, g, t, fl, tfl, err)
+                  : ro_modular_flux_tr(m, cells, tr, ev, g, lp, t, fl, tfl, err);
+  if (!st) st = ro_extensive_update(m, fl, dt, mid, err);
+  if (!st) ro_extensive_update_tr(m, tfl, nt, dt, mid_tr_ext);
+  if (!st) st = ro_cell_update_tr(m, mid, mid_tr_ext, cells, tr, g, t, mid_cells, mid_tr, err);
+  /* second half: fluxes of the mid cells, mid += dt*area*F2 */
+  if (!st)
+    st = order == 1 ? ro_simple_flux_tr(m, mid_cells, mid_tr, ev, g, t, fl, tfl, err)
+                    : ro_modular_flux_tr(m, mid_cells, mid_tr, ev, g, lp, t, fl, tfl, err);
+  if (!st) st = ro_extensive_update(m, fl, dt, mid, err);
+  if (!st) ro_extensive_update_tr(m, tfl, nt, dt, mid_tr_ext);
+  if (!st) {
+    /* average_extensive (hdsim2d.cpp:311-320), then the cells from it */
+    for (size_t k = 0; k < 4 * N; ++k) ext[k] = 0.5 * (mid[k] + ext[k]);
+    for (size_t k = 0; k < N * (size_t)nt; ++k) tr_ext[k] = 0.5 * (mid_tr_ext[k] + tr_ext[k]);
+    double* old_cells = (double*)malloc(sizeof(double) * 4 * N);
+    double* old_tr = (double*)malloc(sizeof(double) * ntr);
+    memcpy(old_cells, cells, sizeof(double) * 4 * N);
+    if (nt > 0) memcpy(old_tr, tr, sizeof(double) * N * nt);
+    st = ro_cell_update_tr(m, ext, tr_ext, old_cells, old_tr, g, t, cells, tr, err);
+    free(old_cells);
+    free(old_tr);
+  }
+  free(fl);
+  free(tfl);
+  free(mid);
+  free(mid_cells);
+  free(mid_tr);
+  free(mid_tr_ext);
+  if (dt_out) *dt_out = dt;
+  return st;
+}
+
 /* hdsim2d.cpp:323-449 TimeAdvance2Heun with ZeroForce (which adds dt*0) and a
  * mesh that does not move: dt, F1 on the cells, mid = ext + dt*area*F1,
  * mid cells, F2 on the mid cells, mid += dt*area*F2, ext = 0.5*(mid + ext)

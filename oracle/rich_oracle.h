@@ -93,6 +93,13 @@ void ro_init_extensives_tr(const rg_mesh_view* m, const double* cells, const dou
 int ro_step_tr(const rg_mesh_view* m, double* cells, double* ext, double* tr, double* tr_ext,
                const double* ev, double gamma, double cfl, int order, const ro_lgi_params* lp,
                const ro_tracers* t, double* dt_out, ro_error* err);
+/* hdsim::TimeAdvance2Heun (hdsim2d.cpp:323-449) on a fixed mesh with tracers
+ * and stickers: the cell updater's SkipUpdate keeps the step's old cells at
+ * the midpoint and at the end, and its entropy tracer rewrites the tracer
+ * extensive of the extensives it is given (mid, then the average) */
+int ro_step_heun_tr(const rg_mesh_view* m, double* cells, double* ext, double* tr, double* tr_ext,
+                    const double* ev, double gamma, double cfl, int order, const ro_lgi_params* lp,
+                    const ro_tracers* t, double* dt_out, ro_error* err);
 
 /* Geometry of a packed mesh from its points and face vertices, as the
  * reference's tessellation and CacheData compute it: volume (GetVolume), the

@@ -72,6 +72,9 @@ CASES_TRACERS = {
     "periodic_tracers_o2": ("periodic_tracers", 16, 16, 2, 10),
     # RoundCells motion after 3 steps: one pass with moving faces
     "sedov_tracers_o2": ("sedov_tracers", 24, 24, 3, 0),
+    # TimeAdvance2Heun with tracers, stickers (frozen cells) and the entropy tracer
+    "sedov_eulerian_heun_tracers_o2": ("sedov_eulerian_tracers", 24, 24, 2, 10, "heun"),
+    "periodic_heun_tracers_o2": ("periodic_tracers", 16, 16, 2, 10, "heun"),
 }
 
 # 3D first-order path (oracle/ref/ref_dump3d.cpp), written to 3d/<name>.npz:

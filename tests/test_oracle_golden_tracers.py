@@ -92,7 +92,7 @@ def test_hdsim_run(tg):
     steps = int(g["case_params"][3])
     ev = np.zeros((g["mesh"].n_faces, 2))
     cells, ext, tr, tr_ext, dts = oracle.run_tr(g["mesh"], g["cells0"], g["ext0"], g["tr_cells0"], g["tr_ext0"], ev,
-                                                g["gamma"], steps, g["ts"], 0.3, g["order"], lp_of(g))
+                                                g["gamma"], steps, g["ts"], 0.3, g["order"], lp_of(g), heun=g["heun"])
     exact(accumulate(float(g["time0"][0]), dts), g["run_times"])
     exact(ext, g["run_ext"])
     exact(cells, g["run_cells"])
