@@ -354,23 +354,40 @@ rg_status enqueue_heun(rg_handle* h, int step, cudaEvent_t* ev) {
     a.step = step;
     double* mid_c = static_cast<double*>(h->mid_cells.p);
     double* mid_e = static_cast<double*>(h->mid_ext.p);
+    // tracers: the same two halves, mid tracers and extensive tracers beside
+    // the mid cells and extensives (the tracer kernels of a half run after
+    // its hydro kernels, whose mass fluxes and shock decisions they read)
+    const bool tr = h->tcfg.n_tracers > 0;
+    const rg::TracerArgs ta = tracer_args(h);
+    rg::TracerArgs ta1 = ta, ta2 = ta, ta3 = ta;
+    ta1.tr_out = ta2.tr = static_cast<double*>(h->mid_tr.p);
+    ta1.tr_ext_out = ta3.tr_ext = static_cast<double*>(h->mid_tr_ext.p);
+    ta3.tr_ext_out = ta.tr_ext;
+    ta3.tr_ext_avg = ta.tr_ext;
     if (ev) RG_CUDA(h, cudaEventRecord(ev[0], h->stream));
     RG_CUDA(h, rg::launch_cfl(a, h->stream, o2));
     if (ev) RG_CUDA(h, cudaEventRecord(ev[1], h->stream));
-    if (o2) RG_CUDA(h, rg::launch_slopes(a, h->stream));
+    if (o2) {
+      RG_CUDA(h, rg::launch_slopes(a, h->stream));
+      if (tr) RG_CUDA(h, rg::launch_tr_slopes(a, ta, h->stream));
+    }
     RG_CUDA(h, rg::launch_faces(a, h->stream, true));
+    if (tr) RG_CUDA(h, rg::launch_tr_faces(a, ta, h->stream, true));
     rg::StepArgs a1 = a;
     a1.ext_out = mid_e;
     a1.cells_out = mid_c;
     RG_CUDA(h, rg::launch_update(a1, h->stream, false, true, true));
+    if (tr) RG_CUDA(h, rg::launch_tr_update(a1, ta1, h->stream, false, true, true));
     if (ev) RG_CUDA(h, cudaEventRecord(ev[2], h->stream));
     rg::StepArgs a2 = a;
     a2.cells = mid_c;
     if (o2) {
       RG_CUDA(h, rg::launch_ghost_fill(a2, h->stream));
       RG_CUDA(h, rg::launch_slopes(a2, h->stream));
+      if (tr) RG_CUDA(h, rg::launch_tr_slopes(a2, ta2, h->stream));
     }
     RG_CUDA(h, rg::launch_faces(a2, h->stream, true));
+    if (tr) RG_CUDA(h, rg::launch_tr_faces(a2, ta2, h->stream, true));
     if (ev) RG_CUDA(h, cudaEventRecord(ev[3], h->stream));
     rg::StepArgs a3 = a2;
     a3.ext = mid_e;
@@ -378,6 +395,7 @@ rg_status enqueue_heun(rg_handle* h, int step, cudaEvent_t* ev) {
     a3.ext_avg = static_cast<const double*>(h->ext.p);
     a3.cells_out = static_cast<double*>(h->cells.p);
     RG_CUDA(h, rg::launch_update(a3, h->stream, false, true, true));
+    if (tr) RG_CUDA(h, rg::launch_tr_update(a3, ta3, h->stream, false, true, true));
     if (ev) RG_CUDA(h, cudaEventRecord(ev[4], h->stream));
   }
   h->have_fluxes = false;

@@ -853,8 +853,9 @@ __device__ __forceinline__ unsigned long long k_update_item(const StepArgs& a, i
     if (a.frozen_mask && (a.stickers[i] & a.frozen_mask)) {
       // simple_cell_updater.cpp:61-83 with (HasSticker, SkipUpdate): the old
       // cell stays (its extensives above still took the fluxes)
-      if (!a.cfl_next) return kInfBits;
       const Cell c = load_cell(a.cells, i);
+      if (a.cells_out) store4(a.cells_out, i, c.d, c.p, c.vx, c.vy);
+      if (!a.cfl_next) return kInfBits;
       return cfl_bound_bits<kBatch>(a, i, c.d, c.p, c.vx, c.vy);
     }
     const double d = mass / m.cd_volume[i];

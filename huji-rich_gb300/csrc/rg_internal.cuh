@@ -260,6 +260,12 @@ struct TracerArgs {
   double* tr_ext;         // n*nt
   double* tr_slopes;      // n*2*nt (x derivatives, then y)
   double* tr_flux;        // e*nt (unscaled or dt*area scaled, as the hydro fluxes)
+  // TimeAdvance2Heun: the update writes the cell and extensive tracers to
+  // tr_out / tr_ext_out (nullptr: in place) and averages the extensive
+  // tracers with tr_ext_avg (average_extensive) when set
+  double* tr_out;         // n*nt
+  double* tr_ext_out;     // n*nt
+  const double* tr_ext_avg;  // n*nt
 };
 
 #ifdef __CUDACC__

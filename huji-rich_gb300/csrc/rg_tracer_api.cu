@@ -23,7 +23,8 @@ bool tracers_on(const rg_handle* h) {
 }
 
 void tracer_release(rg_handle* h) {
-  for (DevBuf* b : {&h->tr, &h->tr_ext, &h->tr_slopes, &h->tr_flux, &h->mflux, &h->shock, &h->stickers})
+  for (DevBuf* b : {&h->tr, &h->tr_ext, &h->tr_slopes, &h->tr_flux, &h->mflux, &h->shock, &h->stickers,
+                    &h->mid_tr, &h->mid_tr_ext})
     b->release();
   h->have_tr = h->have_tr_ext = false;
   h->tr_n = h->tr_e = -1;
@@ -48,6 +49,10 @@ rg_status tracer_buffers(rg_handle* h) {
   RG_CUDA(h, h->tr_flux.ensure(8 * e * nt));
   RG_CUDA(h, h->mflux.ensure(8 * e));
   RG_CUDA(h, h->shock.ensure(n));
+  if (h->heun) {
+    RG_CUDA(h, h->mid_tr.ensure(8 * n * nt));
+    RG_CUDA(h, h->mid_tr_ext.ensure(8 * n * nt));
+  }
   h->tr_n = s->n;
   h->tr_e = s->e;
   drop_graph(h);
@@ -130,8 +135,8 @@ rg_status rg_set_tracer_config(rg_handle* h, const rg_tracer_config* cfg) {
   if (c.skip_sticker < -1 || c.skip_sticker > 31) return invalid(h, 3, c.skip_sticker);
   if (c.frozen_sticker < -1 || c.frozen_sticker > 31) return invalid(h, 4, c.frozen_sticker);
   const bool on = c.n_tracers > 0 || c.n_stickers > 0 || c.skip_sticker >= 0 || c.frozen_sticker >= 0;
-  // the FP32-mixed path, Heun and batches have no tracer passes
-  if (on && (h->mixed || h->heun || h->n_problems > 0)) return invalid(h, 5, 0);
+  // the FP32-mixed path and batches have no tracer passes
+  if (on && (h->mixed || h->n_problems > 0)) return invalid(h, 5, 0);
   RG_CUDA(h, cudaStreamSynchronize(h->stream));
   const bool nt_changed = c.n_tracers != h->tcfg.n_tracers;
   h->tcfg = c;

@@ -267,9 +267,23 @@ __global__ void __launch_bounds__(kTrBlock) k_tr_update(StepArgs a, TracerArgs t
       }
     }
   }
-  if (do_cells && !(a.frozen_mask && (a.stickers[i] & a.frozen_mask))) {
+  if (t.tr_ext_avg) {
+    // hdsim2d.cpp:311-320 average_extensive: 0.5*(mid + old)
+    const double* o = t.tr_ext_avg + static_cast<size_t>(i) * nt;
+#pragma unroll
+    for (int j = 0; j < kMaxTracers; ++j)
+      if (j < nt) te[j] = 0.5 * (te[j] + o[j]);
+  }
+  const bool frozen = a.frozen_mask && (a.stickers[i] & a.frozen_mask);
+  if (do_cells && frozen && t.tr_out) {
+    // SkipUpdate keeps the step's old cell, its tracers included
+#pragma unroll
+    for (int j = 0; j < kMaxTracers; ++j)
+      if (j < nt) t.tr_out[static_cast<size_t>(i) * nt + j] = t.tr[static_cast<size_t>(i) * nt + j];
+  }
+  if (do_cells && !frozen) {
     const double mass = (a.ext_out ? a.ext_out : a.ext)[4 * i];
-    double* tr = t.tr + static_cast<size_t>(i) * nt;
+    double* tr = (t.tr_out ? t.tr_out : t.tr) + static_cast<size_t>(i) * nt;
 #pragma unroll
     for (int j = 0; j < kMaxTracers; ++j)
       if (j < nt) tr[j] = te[j] / mass;
@@ -283,10 +297,11 @@ __global__ void __launch_bounds__(kTrBlock) k_tr_update(StepArgs a, TracerArgs t
         if (j == t.entropy) te[j] = sv * mass;
     }
   }
-  if (do_ext || (do_cells && t.entropy >= 0)) {
+  if (do_ext || (do_cells && t.entropy >= 0) || t.tr_ext_out) {
+    double* out = t.tr_ext_out ? t.tr_ext_out + static_cast<size_t>(i) * nt : ext_t;
 #pragma unroll
     for (int j = 0; j < kMaxTracers; ++j)
-      if (j < nt) ext_t[j] = te[j];
+      if (j < nt) out[j] = te[j];
   }
 }
 

@@ -35,6 +35,7 @@ def tracers_match(got, want):
 
 
 def tracer_handle(g, **kw):
+    kw.setdefault("time_integrator", 1 if g["heun"] else 0)
     h = richgpu.Handle(gamma=g["gamma"], order=g["order"], ghost_kind=g["ghost_kind"], device=0, **kw)
     h.upload_mesh(g["mesh"])
     h.set_tracer_config(3, limited=[0], entropy=ENTROPY, skip_sticker=1, frozen_sticker=0)
@@ -105,11 +106,12 @@ def big_case(n, boundary, seed=9):
     return mesh, cells, tr, stickers
 
 
-@pytest.mark.parametrize("boundary,order", [("periodic", 2), ("rigid", 2), ("rigid", 1)])
-def test_large_run_vs_oracle(boundary, order):
+@pytest.mark.parametrize("boundary,order,heun", [("periodic", 2, False), ("rigid", 2, False), ("rigid", 1, False),
+                                               ("rigid", 2, True), ("periodic", 2, True)])
+def test_large_run_vs_oracle(boundary, order, heun):
     """A 160^2 lattice, five tracers (three limited), the entropy tracer,
-    5% frozen cells and 8% limiter-skipped cells: 12 fused steps against the
-    oracle."""
+    5% frozen cells and 8% limiter-skipped cells: 12 fused steps (hdsim's
+    TimeAdvance or TimeAdvance2Heun) against the oracle."""
     mesh, cells, tr, stickers = big_case(160, boundary)
     gamma, steps = 5 / 3, 12
     ghost = 1 if boundary == "periodic" else 0
@@ -118,8 +120,9 @@ def test_large_run_vs_oracle(boundary, order):
     tr_ext = oracle.init_extensives_tr(mesh, cells, tr)
     ev = np.zeros((mesh.n_faces, 2))
     lp = oracle.lgi_params(ghost_kind=ghost)
-    oc, oe, otr, ote, odts = oracle.run_tr(mesh, cells, ext, tr, tr_ext, ev, gamma, steps, ts, 0.3, order, lp)
-    with richgpu.Handle(gamma=gamma, order=order, ghost_kind=ghost, device=0) as h:
+    oc, oe, otr, ote, odts = oracle.run_tr(mesh, cells, ext, tr, tr_ext, ev, gamma, steps, ts, 0.3, order, lp,
+                                           heun=heun)
+    with richgpu.Handle(gamma=gamma, order=order, ghost_kind=ghost, device=0, time_integrator=1 if heun else 0) as h:
         h.upload_mesh(mesh)
         h.set_tracer_config(5, limited=[0, 2, 4], entropy=1, skip_sticker=3, frozen_sticker=0)
         h.set_stickers(stickers)
@@ -186,8 +189,7 @@ def test_unsupported_combinations_and_readiness():
             h.set_tracer_config(2)
         assert ei.value.status == 1
     with richgpu.Handle(gamma=5 / 3, order=2, ghost_kind=0, device=0, time_integrator=1) as h:
-        with pytest.raises(richgpu.RichError):
-            h.set_tracer_config(0, frozen_sticker=0)
+        h.set_tracer_config(0, frozen_sticker=0)          # TimeAdvance2Heun carries tracers and stickers
     with richgpu.Handle(gamma=5 / 3, order=2, ghost_kind=0, device=0) as h:
         h.upload_mesh(mesh)
         with pytest.raises(richgpu.RichError):
