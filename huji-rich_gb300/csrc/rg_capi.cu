@@ -518,8 +518,7 @@ rg_status rg_create(const rg_config* cfg, rg_handle** out) {
   if ((e = cudaSetDevice(cfg->device)) != cudaSuccess) return fail(e);
   if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
   if ((e = cudaStreamCreateWithFlags(&h->upload_stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
-  if ((e = cudaEventCreateWithFlags(&h->ev_up0, cudaEventDefault)) != cudaSuccess) return fail(e);
-  if ((e = cudaEventCreateWithFlags(&h->ev_up1, cudaEventDefault)) != cudaSuccess) return fail(e);
+  if ((e = cudaEventCreateWithFlags(&h->ev_uploaded, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
   for (auto& s : h->slots)
     if ((e = cudaEventCreateWithFlags(&s.last_use, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
   for (auto& k : h->ev_k)
@@ -574,8 +573,7 @@ rg_status rg_destroy(rg_handle* h) {
   h->host_dts.release();
   for (auto& k : h->ev_k)
     if (k) cudaEventDestroy(k);
-  if (h->ev_up0) cudaEventDestroy(h->ev_up0);
-  if (h->ev_up1) cudaEventDestroy(h->ev_up1);
+  if (h->ev_uploaded) cudaEventDestroy(h->ev_uploaded);
   if (h->stream) cudaStreamDestroy(h->stream);
   if (h->upload_stream) cudaStreamDestroy(h->upload_stream);
   cudaGetLastError();
@@ -630,7 +628,6 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t flags) {
                  {s.lay.face_vertices, v->face_vertices, 32 * static_cast<size_t>(e)},
                  {s.lay.cell_off, v->cell_face_offset, 4 * (static_cast<size_t>(n) + 1)},
                  {s.lay.cell_faces, v->cell_faces, 4 * static_cast<size_t>(m)}};
-  RG_CUDA(h, cudaEventRecord(h->ev_up0, h->upload_stream));
   for (const Part& p : parts) {
     if (p.bytes == 0 || p.src == nullptr) continue;  // device geometry: computed below
     if (is_pinned(p.src)) {
@@ -712,7 +709,7 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t flags) {
     m32.cd_volume = s.mesh.cd_volume;
     RG_CUDA(h, rg::launch_geom32(m32, h->upload_stream));
   }
-  RG_CUDA(h, cudaEventRecord(h->ev_up1, h->upload_stream));
+  RG_CUDA(h, cudaEventRecord(h->ev_uploaded, h->upload_stream));
   if (n_changed) {
     // the cell count changed: the state no longer matches the mesh
     h->have_cells = h->have_ext = false;
@@ -763,8 +760,6 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t flags) {
   DevStatus* hs = static_cast<DevStatus*>(h->host_status.p);
   RG_CUDA(h, cudaMemcpyAsync(hs, h->d_geom_status, sizeof(DevStatus), cudaMemcpyDeviceToHost, h->upload_stream));
   RG_CUDA(h, cudaStreamSynchronize(h->upload_stream));
-  float ms = 0;
-  cudaEventElapsedTime(&ms, h->ev_up0, h->ev_up1);
   s.geom_error = rg_error{};
   if (hs->err_key != ~0ull)
     s.geom_error = rg_error{hs->err_status, 2, static_cast<int64_t>(hs->err_key & rg::kKeyIndexMask), hs->err_value};
@@ -774,14 +769,13 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t flags) {
   drop_graph(h);
   adjoint_release(h);
   // later compute work on the stream sees the new slot
-  RG_CUDA(h, cudaStreamWaitEvent(h->stream, h->ev_up1, 0));
+  RG_CUDA(h, cudaStreamWaitEvent(h->stream, h->ev_uploaded, 0));
   if (h->active >= 0) RG_CUDA(h, cudaEventRecord(h->slots[h->active].last_use, h->stream));
   h->active = next;
   s.valid = true;
   if (tracers_on(h)) RG_TRY(tracer_buffers(h));
   RG_TRY(lagrangian_buffers(h));
   h->last_upload_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-  (void)ms;
   if (h->cfg.order == 2 && s.geom_error.status) {
     h->last = s.geom_error;
     return static_cast<rg_status>(s.geom_error.status);

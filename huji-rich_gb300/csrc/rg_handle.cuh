@@ -146,7 +146,7 @@ struct rg_handle {
   rg_config cfg{};
   cudaStream_t stream = nullptr;
   cudaStream_t upload_stream = nullptr;
-  cudaEvent_t ev_up0 = nullptr, ev_up1 = nullptr;
+  cudaEvent_t ev_uploaded = nullptr;  // the upload stream's work for the newest mesh slot
   cudaEvent_t ev_k[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   rgh::MeshSlot slots[2];
   int active = -1;
