@@ -196,7 +196,7 @@ __device__ void lgi_slope(const AdjArgs& a, int i, V4<T>& sx, V4<T>& sy) {
         cv = cv + sy.v[q] * dm.y;
         const T dphi = cv - cell.v[q];
         const double dv = val(dphi);
-        if (!(fabs(dv) > thr || val(cv) * cq < 0)) continue;
+        if (!(abs_gt(dv, thr) || prod_neg(val(cv), cq))) continue;  // integer-pipe tests (rg_convert.cuh)
         if (!shock) {
           const bool use_abs = q >= 2;
           const double t1 = use_abs ? fabs(1e-9 * cq) : 1e-9 * cq;
