@@ -34,6 +34,7 @@ UNITS = {
     "rg_3d_mixed.cu": [],
     "rg_tracers.cu": ["--fmad=false"],
     "rg_tracer_api.cu": [],
+    "rg_rules_api.cu": [],
     "rg_motion.cu": ["--fmad=false"],
     "rg_motion_api.cu": [],
     "rg_adjoint_rev32.cu": [],
