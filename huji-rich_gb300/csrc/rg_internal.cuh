@@ -185,7 +185,8 @@ constexpr int kMaxBlock = 512;
 // two, 2 and 3, register-capped builds for blocks of up to 256 threads
 // with 5 or 6 blocks resident per SM (more warps in flight against fewer
 // registers per thread), and 4, which loads the neighbour words, stencil
-// records and states of cells with up to 8 neighbours before any arithmetic.
+// records and states of cells with up to 8 neighbours before any arithmetic;
+// the FP32-mixed update kernel has register-capped builds 2 and 3 too.
 struct LaunchShape {
   int block;
   int max_blocks;

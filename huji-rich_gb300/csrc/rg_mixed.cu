@@ -831,8 +831,11 @@ __device__ __forceinline__ unsigned long long k_update_mixed_item(const MixedArg
   return kInfBits;
 }
 
-template <bool kBatch>
-__global__ void __launch_bounds__(kMaxBlock) k_update_mixed(MixedArgs a, int from_unscaled, int do_ext, int do_cells) {
+// kMinBlocks > 0: register-capped builds for blocks of up to kCappedBlock
+// threads with kMinBlocks resident per SM (launch-shape variants 2 and 3)
+template <bool kBatch, int kMinBlocks = 0>
+__global__ void __launch_bounds__(kMinBlocks ? kCappedBlock : kMaxBlock, kMinBlocks ? kMinBlocks : 1)
+    k_update_mixed(MixedArgs a, int from_unscaled, int do_ext, int do_cells) {
   const int t0 = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
   if (kBatch && do_ext && !from_unscaled) {
     for (int p = t0; p < a.n_problems; p += stride) {
@@ -936,10 +939,22 @@ cudaError_t launch_faces32(const MixedArgs& a, cudaStream_t s, bool scaled) {
 cudaError_t launch_update_mixed(const MixedArgs& a, cudaStream_t s, bool from_unscaled, bool extensive, bool cells) {
   const int work = a.cell_problem && a.n_problems > a.mesh.n ? a.n_problems : a.mesh.n;
   if (work > 0) {
-    if (a.cell_problem)
-      k_update_mixed<true><<<grid_of(a.shapes.update, work), a.shapes.update.block, 0, s>>>(a, from_unscaled ? 1 : 0, extensive ? 1 : 0, cells ? 1 : 0);
-    else
-      k_update_mixed<false><<<grid_of(a.shapes.update, work), a.shapes.update.block, 0, s>>>(a, from_unscaled ? 1 : 0, extensive ? 1 : 0, cells ? 1 : 0);
+    const LaunchShape& sh = a.shapes.update;
+    const int nb = grid_of(sh, work), bs = sh.block;
+    const int fu = from_unscaled ? 1 : 0, ex = extensive ? 1 : 0, ce = cells ? 1 : 0;
+    const bool b = a.cell_problem != nullptr;
+    // builds: 0 plain, 2 and 3 register-capped for 5 and 6 resident blocks
+    // of up to 256 threads
+    switch (sh.variant) {
+      case 2:
+        b ? k_update_mixed<true, 5><<<nb, bs, 0, s>>>(a, fu, ex, ce) : k_update_mixed<false, 5><<<nb, bs, 0, s>>>(a, fu, ex, ce);
+        break;
+      case 3:
+        b ? k_update_mixed<true, 6><<<nb, bs, 0, s>>>(a, fu, ex, ce) : k_update_mixed<false, 6><<<nb, bs, 0, s>>>(a, fu, ex, ce);
+        break;
+      default:
+        b ? k_update_mixed<true><<<nb, bs, 0, s>>>(a, fu, ex, ce) : k_update_mixed<false><<<nb, bs, 0, s>>>(a, fu, ex, ce);
+    }
   }
   return cudaGetLastError();
 }

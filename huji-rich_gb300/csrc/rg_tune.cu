@@ -80,8 +80,12 @@ rg_status launch_one(rg_handle* h, int k, const rg::LaunchShape& sh, void* ext_s
   return RG_OK;
 }
 
-int n_variants(const rg_handle* h, int k) { return h->mixed && k == RG_KERNEL_SLOPES ? 5 : 1; }
-bool capped(int k, int v) { return k == RG_KERNEL_SLOPES && (v == 2 || v == 3); }
+// mixed slopes: builds 0-4; mixed update: 0, (1 = 0), 2, 3 (register-capped)
+int n_variants(const rg_handle* h, int k) {
+  if (!h->mixed) return 1;
+  return k == RG_KERNEL_SLOPES ? 5 : (k == RG_KERNEL_UPDATE ? 4 : 1);
+}
+bool capped(int k, int v) { return (k == RG_KERNEL_SLOPES || k == RG_KERNEL_UPDATE) && (v == 2 || v == 3); }
 
 rg_status check_shapes(rg_handle* h, const rg_launch_shapes* s) {
   for (int k = 0; k < 4; ++k) {
@@ -147,6 +151,7 @@ rg_status rg_autotune(rg_handle* h, int32_t reps, rg_launch_shapes* chosen) {
     for (int v = 0; v < n_variants(h, k); ++v)
     for (int b : kBlocks) {
       if (capped(k, v) && b > rg::kCappedBlock) continue;
+      if (k == RG_KERNEL_UPDATE && v == 1) continue;  // the update has no unrolled build
       for (int per_sm : kPerSm) {
         const rg::LaunchShape sh{b, per_sm * sms, v};
         RG_TRY(launch_one(h, k, sh, ext_scr.p, cells_scr.p));  // warm

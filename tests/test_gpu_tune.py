@@ -22,7 +22,8 @@ SHAPES = [
 ]
 # the FP32-mixed slopes kernel's other builds (unrolled, register-capped)
 MIXED_SHAPES = [{"slopes": (128, 0, 1)}, {"slopes": (256, 608, 2)}, {"slopes": (64, 0, 3)},
-                {"slopes": (128, 0, 4)}, {"slopes": (256, 1216, 4)}]
+                {"slopes": (128, 0, 4)}, {"slopes": (256, 1216, 4)},
+                {"update": (256, 0, 2)}, {"update": (128, 912, 3)}]
 
 
 def shapes_for(precision):
