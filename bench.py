@@ -235,6 +235,19 @@ KERNEL_NAMES = {0: {"cfl": "k_cfl", "slopes": "k_slopes", "faces": "k_faces_lgi"
                 1: {"cfl": "k_cfl32", "slopes": "k_slopes32", "faces": "k_faces32_lgi", "update": "k_update_mixed"}}
 
 
+def device_extensives(mesh, cells, local_rank, offsets=None, gammas=None):
+    """hdsim's init_extensives of the cells, formed by the library on the
+    device (the FP64 path; per-problem gamma for a batch)."""
+    import richgpu
+    with richgpu.Handle(gamma=GAMMA, order=2, ghost_kind=0, device=local_rank) as h:
+        h.upload_mesh(mesh)
+        if offsets is not None:
+            h.set_problems(offsets, gammas)
+        h.set_cells(cells)
+        h.init_extensives()
+        return h.get_extensives()
+
+
 def measure(precision, mesh, cells, ext, args, local_rank, barrier, max_over_ranks):
     """Warm-up + timed steps of one precision; returns the timing record and
     the final cells (for the accuracy comparison)."""
@@ -337,7 +350,6 @@ def roofline(rec, mesh, precision):
 
 def run_gpu(args, world, rank, local_rank):
     import torch
-    import oracle
 
     torch.cuda.set_device(local_rank)
     dist = None
@@ -357,7 +369,7 @@ def run_gpu(args, world, rank, local_rank):
         return float(t.item())
 
     mesh, cells = workload()
-    ext = oracle.init_extensives(mesh, cells, GAMMA)
+    ext = device_extensives(mesh, cells, local_rank)
     r64, c64 = measure(0, mesh, cells, ext, args, local_rank, barrier, max_over_ranks)
     r32, c32 = measure(1, mesh, cells, ext, args, local_rank, barrier, max_over_ranks)
     l1 = float(np.abs(c32[:, 0] - c64[:, 0]).sum() / np.abs(c64[:, 0]).sum())
@@ -393,7 +405,7 @@ def run_gpu(args, world, rank, local_rank):
                 "launch_shapes": {kk: [v["block"], v["max_blocks"], v["variant"]] for kk, v in r32["shapes"].items()},
                 "faces_per_s": world * mesh.n_faces * k / (r32["total_ms"] * 1e-3),
                 "fp64": {"value": value64, "ms_per_step": r64["total_ms"] / k, "dtype": "f64",
-                         "bit_exact_vs_reference": True, "roofline": roofline(r64, mesh, 0),
+                         "parity": "bit-exact to the reference (tests/test_gpu_parity.py)", "roofline": roofline(r64, mesh, 0),
                          "note": "plain FP64 path: bound by GB300's FP64 pipe (2 DFMA/clk/SM), not HBM",
                          "launch_shapes": {kk: [v["block"], v["max_blocks"], v["variant"]] for kk, v in r64["shapes"].items()},
                          "e2e": {"value": world * n * r64["e2e_steps"] / r64["e2e_s"], "unit": UNIT,
@@ -420,9 +432,7 @@ def tracers_block(fp64_ms_per_step, steps=20, warmup=3):
     Bit-identical to the reference (the entropy tracer to a few ulp)."""
     import torch
     import richgpu
-    import oracle
     mesh, cells = workload()
-    ext = oracle.init_extensives(mesh, cells, GAMMA)
     rng = np.random.default_rng(17)
     n = mesh.n_cells
     xy = mesh.point_xy[:n]
@@ -437,7 +447,6 @@ def tracers_block(fp64_ms_per_step, steps=20, warmup=3):
         h.set_stickers(stickers)
         h.set_cells(cells)
         h.set_tracers(tr)
-        h.set_extensives(ext)
         h.init_extensives()
         h.set_edge_velocities(np.zeros((mesh.n_faces, 2)))
         for _ in range(warmup):
@@ -502,7 +511,7 @@ def sedov3d_block(steps=20, warmup=3, cpu=True):
     rec = {"workload": "sedov3d_cubegrid_96^3_first_order_hllc_fp64", "cells": N, "faces": F, "steps": steps,
            "ms_per_step": ms, "cell_updates_per_s": N / (ms * 1e-3), "faces_per_s": F / (ms * 1e-3),
            "kernel_ms_mean": {"k3_cfl": float(kms[:, 0].mean()), "k3_faces": kf, "k3_update": float(kms[:, 2].mean())},
-           "bit_exact_vs_reference": True,
+           "parity": "bit-exact to the reference's HDSim3D (tests/test_gpu_3d.py)",
            "roofline": {"bound": "hbm", "kernel": "k3_faces", "achieved": faces_bytes / (kf * 1e-3) / 1e9,
                         "peak": peak[0], "unit": "GB/s", "frac": faces_bytes / (kf * 1e-3) / 1e9 / peak[0],
                         "traffic": ncu_traffic("k3_faces"), "algorithmic_bytes_per_launch": faces_bytes,
@@ -640,7 +649,6 @@ def run_batch(args, world, rank, local_rank):
     cells (sharding.problem_shard): no collective on the data path, the
     timing is the maximum over ranks and `value` counts every rank's cells."""
     import torch
-    import oracle
     import richgpu
     import synthetic
     from sharding import problem_shard
@@ -665,10 +673,7 @@ def run_batch(args, world, rank, local_rank):
     t0 = time.perf_counter()
     mesh, off, gam, cells, meshes = synthetic.riemann_batch_range(range(lo, hi), seed=BATCH_SEED)
     gen_s = time.perf_counter() - t0
-    ext = np.empty_like(cells)
-    for p in range(len(gam)):
-        a, b = off[p], off[p + 1]
-        ext[a:b] = oracle.init_extensives(meshes[p], cells[a:b], gam[p])
+    ext = device_extensives(mesh, cells, local_rank, off, gam)
     res = {}
     for precision in (0, 1):
         h = richgpu.Handle(gamma=1.4, order=2, ghost_kind=0, precision=precision, device=local_rank)
