@@ -110,3 +110,15 @@ def test_batch_rejects_face_between_problems():
         h.set_problems([0, mesh.n_cells], [1.4])
         with pytest.raises(richgpu.RichError):
             h.cfl_dt()                                       # not available in batch mode
+
+
+def test_batch_init_extensives_per_problem_gamma():
+    """hdsim's init_extensives on a batch, formed on the device with each
+    problem's gamma, equals the oracle's per problem bit for bit."""
+    mesh, off, gam, cells, meshes = small_batch(seed=9, n=9)
+    with richgpu.Handle(gamma=1.4, order=2, ghost_kind=0, device=0) as h:
+        h.upload_mesh(mesh)
+        h.set_problems(off, gam)
+        h.set_cells(cells)
+        h.init_extensives()
+        exact(h.get_extensives(), init_ext(mesh, cells, off, gam))
