@@ -331,6 +331,7 @@ rg_status enqueue_heun(rg_handle* h, int step, cudaEvent_t* ev) {
     rg::MixedArgs a1 = a;
     a1.ext_out = mid_e;
     a1.cells32_out = mid_c;
+    a1.batch_keep_dt = 1;  // a batch keeps each problem's dt for the second half
     RG_CUDA(h, rg::launch_update_mixed(a1, h->stream, false, true, true));
     if (ev) RG_CUDA(h, cudaEventRecord(ev[2], h->stream));
     rg::MixedArgs a2 = a;
@@ -376,6 +377,7 @@ rg_status enqueue_heun(rg_handle* h, int step, cudaEvent_t* ev) {
     rg::StepArgs a1 = a;
     a1.ext_out = mid_e;
     a1.cells_out = mid_c;
+    a1.batch_keep_dt = 1;  // a batch keeps each problem's dt for the second half
     RG_CUDA(h, rg::launch_update(a1, h->stream, false, true, true));
     if (tr) RG_CUDA(h, rg::launch_tr_update(a1, ta1, h->stream, false, true, true));
     if (ev) RG_CUDA(h, cudaEventRecord(ev[2], h->stream));
@@ -1077,7 +1079,7 @@ rg_status rg_set_problems(rg_handle* h, int32_t P, const int32_t* offsets, const
     h->n_problems = 0;
     return RG_OK;
   }
-  if (P < 0 || !offsets || !gamma || h->heun || tracers_on(h) || h->n_rules > 0) return invalid(h, -1, P);
+  if (P < 0 || !offsets || !gamma || tracers_on(h) || h->n_rules > 0) return invalid(h, -1, P);
   if (offsets[0] != 0 || offsets[P] != s->n) return invalid(h, -2, offsets[P]);
   for (int p = 0; p < P; ++p) {
     if (offsets[p + 1] <= offsets[p]) return invalid(h, p, offsets[p + 1]);

@@ -880,7 +880,7 @@ __device__ __forceinline__ unsigned long long k_update_item(const StepArgs& a, i
 template <bool kBatch>
 __global__ void __launch_bounds__(kMaxBlock) k_update(StepArgs a, int from_unscaled, int do_ext, int do_cells) {
   const int t0 = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
-  if (kBatch && do_ext && !from_unscaled) {
+  if (kBatch && do_ext && !from_unscaled && !a.batch_keep_dt) {
     for (int p = t0; p < a.n_problems; p += stride) {
       // every face of this step has read its problem's minimum: record the dt,
       // advance the problem's time and reset the minimum for the next step

@@ -225,6 +225,8 @@ struct StepArgs {
   int cfl_next;         // the update also computes the next step's SimpleCFL dt (status->dt_next)
   int ev_zero;          // every face velocity is +-0: kernels read none
   int take_next_dt;     // the slopes kernel first moves status->dt_next to status->dt
+  int batch_keep_dt;    // batch: the update leaves the per-problem dt, time and minimum
+                        // as they are (TimeAdvance2Heun's first half)
   // batch of independent problems (cell_problem == nullptr: one problem)
   const int* cell_problem;        // n + g: problem of every point
   const double* gamma_p;          // per problem

@@ -837,7 +837,7 @@ template <bool kBatch, int kMinBlocks = 0>
 __global__ void __launch_bounds__(kMinBlocks ? kCappedBlock : kMaxBlock, kMinBlocks ? kMinBlocks : 1)
     k_update_mixed(MixedArgs a, int from_unscaled, int do_ext, int do_cells) {
   const int t0 = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
-  if (kBatch && do_ext && !from_unscaled) {
+  if (kBatch && do_ext && !from_unscaled && !a.batch_keep_dt) {
     for (int p = t0; p < a.n_problems; p += stride) {
       const double dt = a.cfl * __longlong_as_double(static_cast<long long>(a.dtmin_p[p]));
       a.dt_p[p] = dt;

@@ -28,11 +28,15 @@ def init_ext(mesh, cells, offsets, gammas):
 
 
 @pytest.mark.parametrize("precision", [0, 1])
-def test_batch_equals_problems_alone(precision):
+@pytest.mark.parametrize("heun", [0, 1])
+def test_batch_equals_problems_alone(precision, heun):
+    """hdsim::TimeAdvance, and TimeAdvance2Heun (each problem's dt held for
+    both halves), of a batch equal every problem's solo run."""
     mesh, off, gam, cells, meshes = small_batch()
     ext = init_ext(mesh, cells, off, gam)
     steps = 15
-    with richgpu.Handle(gamma=1.4, order=2, ghost_kind=0, precision=precision, device=0) as h:
+    with richgpu.Handle(gamma=1.4, order=2, ghost_kind=0, precision=precision, device=0,
+                        time_integrator=heun) as h:
         h.upload_mesh(mesh)
         h.set_problems(off, gam)
         h.set_cells(cells)
@@ -43,7 +47,8 @@ def test_batch_equals_problems_alone(precision):
         times, last = h.problem_times()
     for p, m in enumerate(meshes):
         a, b = off[p], off[p + 1]
-        with richgpu.Handle(gamma=gam[p], order=2, ghost_kind=0, precision=precision, device=0) as h:
+        with richgpu.Handle(gamma=gam[p], order=2, ghost_kind=0, precision=precision, device=0,
+                            time_integrator=heun) as h:
             h.upload_mesh(m)
             h.set_cells(cells[a:b])
             h.set_extensives(ext[a:b])
@@ -122,3 +127,23 @@ def test_batch_init_extensives_per_problem_gamma():
         h.set_cells(cells)
         h.init_extensives()
         exact(h.get_extensives(), init_ext(mesh, cells, off, gam))
+
+
+def test_batch_heun_fp64_matches_oracle_per_problem():
+    """TimeAdvance2Heun on a batch against the oracle's Heun step per problem."""
+    mesh, off, gam, cells, meshes = small_batch(seed=13, n=5)
+    ext = init_ext(mesh, cells, off, gam)
+    with richgpu.Handle(gamma=1.4, order=2, ghost_kind=0, device=0, time_integrator=1) as h:
+        h.upload_mesh(mesh)
+        h.set_problems(off, gam)
+        h.set_cells(cells)
+        h.set_extensives(ext)
+        h.set_edge_velocities(np.zeros((mesh.n_faces, 2)))
+        h.run(5)
+        bc, be = h.get_cells(), h.get_extensives()
+    for p, m in enumerate(meshes):
+        a, b = off[p], off[p + 1]
+        oc, oe, _ = oracle.run(m, cells[a:b], ext[a:b], np.zeros((m.n_faces, 2)), gam[p], 5, 0.3, 2,
+                               oracle.lgi_params(0), heun=True)
+        exact(bc[a:b], oc)
+        exact(be[a:b], oe)
