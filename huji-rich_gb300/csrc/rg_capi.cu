@@ -1079,7 +1079,7 @@ rg_status rg_set_problems(rg_handle* h, int32_t P, const int32_t* offsets, const
     h->n_problems = 0;
     return RG_OK;
   }
-  if (P < 0 || !offsets || !gamma || tracers_on(h) || h->n_rules > 0) return invalid(h, -1, P);
+  if (P < 0 || !offsets || !gamma || h->n_rules > 0) return invalid(h, -1, P);
   if (offsets[0] != 0 || offsets[P] != s->n) return invalid(h, -2, offsets[P]);
   for (int p = 0; p < P; ++p) {
     if (offsets[p + 1] <= offsets[p]) return invalid(h, p, offsets[p + 1]);

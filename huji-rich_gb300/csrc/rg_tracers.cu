@@ -174,8 +174,14 @@ __global__ void __launch_bounds__(kTrBlock) k_tr_slopes(StepArgs a, TracerArgs t
   }
 }
 
+// dt*area of face e (simple_extensive_updater.cpp:26-27); in a batch the dt
+// of the problem of the face's real side, as the hydro face kernel scales it
 __device__ __forceinline__ double tr_scale(const StepArgs& a, int e) {
-  return scaled_dt<false>(a, 0) * a.geom.xarea[e];  // simple_extensive_updater.cpp:26-27
+  if (a.cell_problem) {
+    const int2 fc = a.mesh.face_cells[e];
+    return scaled_dt<true>(a, fc.x < a.mesh.n ? fc.x : fc.y) * a.geom.xarea[e];
+  }
+  return scaled_dt<false>(a, 0) * a.geom.xarea[e];
 }
 
 // ModularFluxCalculator tracer fluxes: Mass * (Mass > 0 ? first : second)
@@ -290,7 +296,7 @@ __global__ void __launch_bounds__(kTrBlock) k_tr_update(StepArgs a, TracerArgs t
     if (t.entropy >= 0) {
       // ideal_gas.cpp:52-55 dp2s of the updated cell
       const Cell c = load_cell(a.cells_out ? a.cells_out : a.cells, i);
-      const double sv = c.p * pow(c.d, -a.gamma);
+      const double sv = c.p * pow(c.d, -(a.cell_problem ? a.gamma_p[a.cell_problem[i]] : a.gamma));
       tr[t.entropy] = sv;
 #pragma unroll
       for (int j = 0; j < kMaxTracers; ++j)

@@ -147,3 +147,44 @@ def test_batch_heun_fp64_matches_oracle_per_problem():
                                oracle.lgi_params(0), heun=True)
         exact(bc[a:b], oc)
         exact(be[a:b], oe)
+
+
+@pytest.mark.parametrize("heun", [0, 1])
+def test_batch_with_tracers_equals_problems_alone(heun):
+    """Tracers and stickers in a batch: three tracers (one limited, the
+    entropy tracer with each problem's gamma), frozen and limiter-skipped
+    cells; every problem's cells, extensives and tracers bit for bit as
+    alone, with TimeAdvance and TimeAdvance2Heun."""
+    mesh, off, gam, cells, meshes = small_batch(seed=21, n=7)
+    rng = np.random.default_rng(21)
+    n = mesh.n_cells
+    tr = np.stack([rng.uniform(-1, 1, n), cells[:, 1], (rng.random(n) < 0.5).astype(float)], axis=1)
+    st = (rng.random(n) < 0.03).astype(np.uint32) | ((rng.random(n) < 0.05).astype(np.uint32) << 1)
+    steps = 8
+
+    def configure(h, o, g, c, t, s):
+        h.set_tracer_config(3, limited=[0], entropy=1, skip_sticker=1, frozen_sticker=0)
+        if o is not None:
+            h.set_problems(o, g)
+        h.set_stickers(s)
+        h.set_cells(c)
+        h.set_tracers(t)
+        h.init_extensives()
+
+    with richgpu.Handle(gamma=1.4, order=2, ghost_kind=0, device=0, time_integrator=heun) as h:
+        h.upload_mesh(mesh)
+        configure(h, off, gam, cells, tr, st)
+        h.set_edge_velocities(np.zeros((mesh.n_faces, 2)))
+        h.run(steps)
+        bc, be, bt, bte = h.get_cells(), h.get_extensives(), h.get_tracers(), h.get_extensive_tracers()
+    for p, m in enumerate(meshes):
+        a, b = off[p], off[p + 1]
+        with richgpu.Handle(gamma=gam[p], order=2, ghost_kind=0, device=0, time_integrator=heun) as h:
+            h.upload_mesh(m)
+            configure(h, None, None, cells[a:b], tr[a:b], st[a:b])
+            h.set_edge_velocities(np.zeros((m.n_faces, 2)))
+            h.run(steps)
+            exact(bc[a:b], h.get_cells())
+            exact(be[a:b], h.get_extensives())
+            exact(bt[a:b], h.get_tracers())
+            exact(bte[a:b], h.get_extensive_tracers())
