@@ -265,7 +265,10 @@ rg_status rg_synchronize(rg_handle* h, double* dt_last);
  * every problem advances one step per step.  n_problems = 0 returns to one
  * problem.  Call after rg_upload_mesh (an upload drops the table).  Only the
  * fused steps and the state transfers are available in batch mode (rg_cfl_dt
- * returns RG_ERR_INVALID_ARGUMENT); TimeAdvance2Heun is not. */
+ * returns RG_ERR_INVALID_ARGUMENT); the steps are TimeAdvance or
+ * TimeAdvance2Heun (cfg.time_integrator), with tracers and stickers on the
+ * FP64 path; condition/action flux rules and differentiation are
+ * single-problem only. */
 rg_status rg_set_problems(rg_handle* h, int32_t n_problems, const int32_t* problem_cell_offset,
                           const double* gamma);
 /* Per-problem simulated time (sum of its dts since rg_set_problems) and last
@@ -445,9 +448,10 @@ rg_status rg_set_lagrangian_faces(rg_handle* h, const double* ws, const double* 
  * i*n_tracers + j); tracer fluxes n_faces*n_tracers; tracer slopes
  * n_cells*2*n_tracers (x derivatives then y derivatives of each cell).
  * Stickers are one uint32 bit mask per cell.  Ghost points take the tracers
- * and stickers of the cell they copy.  The FP32-mixed path, batches, Heun
- * and differentiation return RG_ERR_INVALID_ARGUMENT while tracers or
- * stickers are configured.  Entropy uses the device pow(): that one tracer
+ * and stickers of the cell they copy.  Tracers run with TimeAdvance and
+ * TimeAdvance2Heun, on single problems and batches; the FP32-mixed path and
+ * differentiation return RG_ERR_INVALID_ARGUMENT while tracers or stickers
+ * are configured.  Entropy uses the device pow(): that one tracer
  * agrees with the host libm to a few ulp; everything else is bit for bit. */
 #define RG_MAX_TRACERS 8
 typedef struct rg_tracer_config {
