@@ -19,7 +19,9 @@ value  the FP32-mixed form (reconstruction, HLLC and CFL in FP32; geometry,
        every timed step.
 e2e    the same steps through the C ABI with host buffers, as a moving-mesh
        caller drives it: upload of the packed tessellation and the face
-       velocities, the step, download of cells and extensives.
+       velocities, the step, download of cells and extensives; "link" times
+       one pinned copy each way of the same byte counts, the floor of the
+       step's copies.
 --impl reference   the CPU implementation of the path (the C restatement of
        the reference's algorithm, oracle/rich_oracle.c: the reference sources
        are not on this machine) on all host cores, one independent
@@ -332,6 +334,32 @@ def pinned_io(mesh, ev, torch):
     return (pm, pin(ev), pin(np.zeros((mesh.n_cells, 4))), pin(np.zeros((mesh.n_cells, 4))))
 
 
+def link_floor(h2d, d2h, reps=20):
+    """Host<->device link speed for the e2e step's byte counts: one pinned
+    copy each way of the same size, timed with CUDA events (the e2e copies
+    cannot be faster than this)."""
+    import torch
+    out = {}
+    for name, nbytes in (("h2d", h2d), ("d2h", d2h)):
+        host = torch.empty(int(nbytes), dtype=torch.uint8, pin_memory=True)
+        dev = torch.empty(int(nbytes), dtype=torch.uint8, device="cuda")
+        src, dst = (host, dev) if name == "h2d" else (dev, host)
+        for _ in range(3):
+            dst.copy_(src, non_blocking=True)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record()
+        for _ in range(reps):
+            dst.copy_(src, non_blocking=True)
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / reps
+        out[name + "_ms"] = ms
+        out[name + "_gbs"] = nbytes / (ms * 1e-3) / 1e9
+    out["copy_floor_ms"] = out["h2d_ms"] + out["d2h_ms"]
+    return out
+
+
 def roofline(rec, mesh, precision):
     alg = algorithmic_bytes(mesh, precision)
     dom = int(np.argmax(rec["kernel_ms"]))
@@ -400,7 +428,8 @@ def run_gpu(args, world, rank, local_rank):
                 "cpu_baseline": cpu,
                 "e2e": {"value": world * n * r32["e2e_steps"] / r32["e2e_s"], "unit": UNIT,
                         "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                        "steps": r32["e2e_steps"], "upload_ms_mean": r32["upload_ms"]},
+                        "steps": r32["e2e_steps"], "ms_per_step": r32["e2e_s"] * 1e3 / r32["e2e_steps"],
+                        "upload_ms_mean": r32["upload_ms"], "link": link_floor(h2d, d2h)},
                 "gpu_launches": 4 * k, "clocks": r32["clock"],
                 "launch_shapes": {kk: [v["block"], v["max_blocks"], v["variant"]] for kk, v in r32["shapes"].items()},
                 "faces_per_s": world * mesh.n_faces * k / (r32["total_ms"] * 1e-3),
