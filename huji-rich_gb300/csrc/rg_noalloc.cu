@@ -18,10 +18,21 @@
 // (the per-block minima are always written before they are read).  Calls
 // that overlap on the GPU (two streams, or two host threads) race on the
 // array: serialise them.  The first call on each device looks up the array's
-// device address (cudaGetSymbolAddress) with that device current; make that
-// first call before any stream capture.
+// device address (cudaGetSymbolAddress) with that device current.  Under the
+// CUDA runtime's lazy module loading (its default) that lookup is also when
+// the driver loads this library's device code and creates the array, which
+// takes driver memory and can block the device once: make the first call
+// during set-up, before the caller's allocator takes over and before any
+// stream capture.
+//
+// The caller's pointers are checked before anything is enqueued: each must
+// be device (or managed) memory of the current device, `cells` and
+// `edge_velocities` 16-byte aligned (the kernel reads them as double2), the
+// others naturally aligned.  Indices are not checked: a cell_faces entry
+// outside the edge_velocities array is read out of bounds.
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <mutex>
 
 #include "rg_internal.cuh"
@@ -116,6 +127,20 @@ __global__ void __launch_bounds__(kBlock)
   }
 }
 
+bool aligned(const void* p, uintptr_t a) { return (reinterpret_cast<uintptr_t>(p) & (a - 1)) == 0; }
+
+// True when p is device or managed memory that `device` can address (a host
+// pointer, pinned or not, would fault the kernel or read the wrong memory).
+bool on_device(const void* p, int device) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (a.type == cudaMemoryTypeDevice) return a.device == device;
+  return a.type == cudaMemoryTypeManaged;
+}
+
 }  // namespace
 
 extern "C" rg_status rg_cfl_dt_noalloc(int32_t n_cells, const double* cells, const double* volume,
@@ -125,11 +150,18 @@ extern "C" rg_status rg_cfl_dt_noalloc(int32_t n_cells, const double* cells, con
   if (n_cells <= 0 || n_cells > kMaxCells) return RG_ERR_INVALID_ARGUMENT;
   if (!cells || !volume || !cell_face_offset || !cell_faces || !edge_velocities || !dt_out)
     return RG_ERR_INVALID_ARGUMENT;
+  // double2 loads need 16-byte alignment; the scalar arrays their own size
+  if (!aligned(cells, 16) || !aligned(edge_velocities, 16) || !aligned(volume, 8) || !aligned(dt_out, 8) ||
+      !aligned(cell_face_offset, 4) || !aligned(cell_faces, 4))
+    return RG_ERR_INVALID_ARGUMENT;
   int device = 0;
   if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= kMaxDevices) {
     cudaGetLastError();
     return RG_ERR_CUDA;
   }
+  const void* ptrs[] = {cells, volume, cell_face_offset, cell_faces, edge_velocities, dt_out};
+  for (const void* p : ptrs)
+    if (!on_device(p, device)) return RG_ERR_INVALID_ARGUMENT;
   unsigned long long* scratch = nullptr;
   if (scratch_address(device, &scratch) != cudaSuccess) {
     cudaGetLastError();

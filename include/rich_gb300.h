@@ -545,15 +545,27 @@ rg_status rg3_step_timed(rg3_handle* h, double* dt_out, float* kernel_ms);
  * that may not allocate device memory (hosts whose own allocator or arena
  * owns all GPU memory and must not see cudaMalloc / cudaFree in the step
  * loop, which would synchronise the device and bypass their accounting).
- * Every pointer is a caller-owned DEVICE pointer: cells n_cells*4, volume
- * n_cells (Tessellation::GetVolume), cell_face_offset n_cells+1, cell_faces,
- * edge_velocities n_faces*2; *dt_out (one double, device) receives the dt,
- * asynchronously on `stream` (a cudaStream_t, NULL = default stream).
+ * Every pointer is a caller-owned DEVICE pointer of the current device
+ * (device or managed memory; anything else returns RG_ERR_INVALID_ARGUMENT
+ * before any work is enqueued):
+ *   cells            n_cells*4 {density, pressure, vx, vy}, 16-byte aligned
+ *   volume           n_cells cell areas, 8-byte aligned
+ *   cell_face_offset n_cells+1 and cell_faces: each cell's faces, 4-byte aligned
+ *   edge_velocities  n_faces*2 face velocities, 16-byte aligned
+ *   dt_out           one double, 8-byte aligned: receives the dt,
+ * asynchronously on `stream` (a cudaStream_t of the current device, NULL =
+ * default stream).  A misaligned pointer returns RG_ERR_INVALID_ARGUMENT.
+ * Indices are NOT validated (there is no face count): a cell_faces entry
+ * outside edge_velocities is read out of bounds, so pass a mesh that an
+ * rg_handle has accepted or that the caller has checked.
  * Allocates nothing: its reduction scratch is a fixed 32 KiB device array
  * inside the library, so n_cells is limited to 1,048,576 (larger values
  * return RG_ERR_INVALID_ARGUMENT).  All calls share that array: calls that
  * overlap on the GPU race, so serialise them.  The first call on a device
- * looks up the array's address with that device current; make it before any
+ * looks up the array's address with that device current; under lazy module
+ * loading (the CUDA default) that first call also loads the library's
+ * device code and creates the array, which takes driver memory: make it
+ * during set-up, before the caller's allocator takes over and before any
  * stream capture. */
 rg_status rg_cfl_dt_noalloc(int32_t n_cells, const double* cells, const double* volume,
                             const int32_t* cell_face_offset, const int32_t* cell_faces,
