@@ -11,10 +11,19 @@
 //   GpuCellUpdater        : CellUpdater       (cell_updater_2d.hpp:20-45)
 //
 // All four share one GpuContext (one rg_handle).  Per call they upload what
-// hdsim passes (the tessellation only when it changed, which an unchanged
-// Eulerian rebuild does not), run the matching C-ABI operation and copy the
-// result back into hdsim's vectors.  A physical failure is rethrown as the
-// reference's UniversalError with its message and diagnostic entries.
+// hdsim passes, run the matching C-ABI operation and copy the result back
+// into hdsim's vectors.  The tessellation is packed and uploaded only when it
+// changed: the context keeps the mesh points (real and ghost) of the last
+// upload, and a tessellation with the same point count, edge count and
+// bitwise-equal points is the same Voronoi mesh (VoronoiMesh builds it
+// deterministically from its points), so an Eulerian rebuild and the calls
+// that follow a step's MoveMeshPoints reuse the upload.  With
+// set_outer_boundary the device computes the volumes and CMs itself
+// (RG_MESH_DEVICE_GEOMETRY, bit-identical to the reference's), so the host
+// packs only points, topology and face vertices and never evaluates
+// CacheData's lazy volumes.  The fluxes stay on the device between the flux
+// calculator and the extensive updater.  A physical failure is rethrown as
+// the reference's UniversalError with its message and diagnostic entries.
 //
 // Supported: IdealGas, Hllc (massflux = true), SlabSymmetry or
 // CylindricalSymmetry, first order (SimpleFluxCalculator) or
@@ -38,6 +47,7 @@
 #include "source/newtonian/common/ideal_gas.hpp"
 #include "source/newtonian/two_dimensional/cell_updater_2d.hpp"
 #include "source/newtonian/two_dimensional/extensive_updater.hpp"
+#include "source/newtonian/two_dimensional/OuterBoundary.hpp"
 #include "source/newtonian/two_dimensional/flux_calculator_2d.hpp"
 #include "source/newtonian/two_dimensional/physical_geometry.hpp"
 #include "source/newtonian/two_dimensional/time_step_function.hpp"
@@ -83,23 +93,42 @@ class GpuContext {
     }
   }
 
-  // Packs the tessellation and uploads it unless it equals the last upload.
+  // The simulation's outer boundary: the device then forms the cell volumes
+  // and CMs (ghost CMs reflected about, or shifted across, its sides) from
+  // the points and face vertices, and the host packs no geometry.
+  void set_outer_boundary(const OuterBoundary& ob) const {
+    check(rg_set_outer_box(h_, ob.GetGridBoundary(Left), ob.GetGridBoundary(Right), ob.GetGridBoundary(Down),
+                           ob.GetGridBoundary(Up)));
+    if (!device_geometry_) have_mesh_ = false;
+    device_geometry_ = true;
+  }
+
+  // Packs the tessellation and uploads it unless it is the last upload's.
+  // Without device geometry the packed CacheData volumes need the
+  // simulation's CacheData; a call without one (the time-step function)
+  // packs slab volumes, which the next call that has the CacheData replaces.
   void sync_mesh(const Tessellation& tess, const CacheData* cd) const {
-    PackedMesh m;
-    if (cd) {
-      pack_tessellation(tess, *cd, m);
+    const bool replace_provisional = provisional_ && cd && !device_geometry_;
+    if (have_mesh_ && !replace_provisional && mesh_unchanged(tess)) return;
+    if (device_geometry_) {
+      pack_topology(tess, packed_);
+      provisional_ = false;
+    } else if (cd) {
+      pack_tessellation(tess, *cd, packed_);
+      provisional_ = false;
     } else {
       SlabSymmetry pg;
       CacheData local(tess, pg);
-      pack_tessellation(tess, local, m);
+      pack_tessellation(tess, local, packed_);
+      provisional_ = true;
     }
-    if (have_mesh_ && same(m, packed_)) return;
-    packed_ = std::move(m);
+    remember_points(tess);
     const rg_mesh_view v = packed_.view();
-    check(rg_upload_mesh(h_, &v, 0));
+    check(rg_upload_mesh(h_, &v, device_geometry_ ? RG_MESH_DEVICE_GEOMETRY : 0u));
     have_mesh_ = true;
     ++mesh_generation_;
   }
+  unsigned long mesh_generation() const { return mesh_generation_; }
 
   // Tracer configuration from hdsim's sorted names (hdsim2d.cpp:121-136) and
   // the spec; set once, from the first cells with tracers or stickers.
@@ -239,12 +268,29 @@ class GpuContext {
   }
 
  private:
-  static bool same(const PackedMesh& a, const PackedMesh& b) {
-    return a.n_cells == b.n_cells && a.n_ghosts == b.n_ghosts && a.n_faces == b.n_faces &&
-           a.point_xy == b.point_xy && a.cm_xy == b.cm_xy && a.volume == b.volume && a.cd_volume == b.cd_volume &&
-           a.ghost_source == b.ghost_source && a.ghost_face == b.ghost_face && a.face_cells == b.face_cells &&
-           a.face_vertices == b.face_vertices && a.cell_face_offset == b.cell_face_offset &&
-           a.cell_faces == b.cell_faces;
+  // Same point count, edge count and bitwise-equal points (real and ghost)
+  // as at the last upload.
+  bool mesh_unchanged(const Tessellation& tess) const {
+    const int total = tess.GetTotalPointNumber();
+    if (tess.GetPointNo() != packed_.n_cells || static_cast<int>(tess.getAllEdges().size()) != packed_.n_faces ||
+        2 * static_cast<size_t>(total) != key_points_.size())
+      return false;
+    for (int i = 0; i < total; ++i) {
+      const Vector2D p = tess.GetMeshPoint(i);
+      if (std::memcmp(&p.x, &key_points_[2 * static_cast<size_t>(i)], sizeof(double)) != 0 ||
+          std::memcmp(&p.y, &key_points_[2 * static_cast<size_t>(i) + 1], sizeof(double)) != 0)
+        return false;
+    }
+    return true;
+  }
+  void remember_points(const Tessellation& tess) const {
+    const int total = tess.GetTotalPointNumber();
+    key_points_.resize(2 * static_cast<size_t>(total));
+    for (int i = 0; i < total; ++i) {
+      const Vector2D p = tess.GetMeshPoint(i);
+      key_points_[2 * static_cast<size_t>(i)] = p.x;
+      key_points_[2 * static_cast<size_t>(i) + 1] = p.y;
+    }
   }
 
   rg_config cfg_;
@@ -254,7 +300,10 @@ class GpuContext {
   mutable bool have_tcfg_ = false;
   mutable rg_physical_geometry pgeo_{RG_GEOMETRY_SLAB, {0, 0}, {0, 1}, 1};
   mutable PackedMesh packed_;
+  mutable std::vector<double> key_points_;
   mutable bool have_mesh_ = false;
+  mutable bool device_geometry_ = false;
+  mutable bool provisional_ = false;
   mutable unsigned long mesh_generation_ = 0;
   mutable const Extensive* flux_data_ = nullptr;
   mutable size_t flux_size_ = 0;

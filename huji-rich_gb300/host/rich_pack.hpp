@@ -23,7 +23,6 @@
 
 #include <cstdint>
 #include <stdexcept>
-#include <unordered_map>
 #include <vector>
 
 #include "rich_gb300.h"
@@ -45,9 +44,9 @@ struct PackedMesh {
     v.n_faces = n_faces;
     v.reserved = 0;
     v.point_xy = point_xy.data();
-    v.cm_xy = cm_xy.data();
-    v.volume = volume.data();
-    v.cd_volume = cd_volume.data();
+    v.cm_xy = cm_xy.empty() ? nullptr : cm_xy.data();
+    v.volume = volume.empty() ? nullptr : volume.data();
+    v.cd_volume = cd_volume.empty() ? nullptr : cd_volume.data();
     v.ghost_source = ghost_source.data();
     v.ghost_face = ghost_face.data();
     v.face_cells = face_cells.data();
@@ -58,15 +57,20 @@ struct PackedMesh {
   }
 };
 
-inline void pack_tessellation(const Tessellation& tess, const CacheData& cd, PackedMesh& m) {
+// Topology, mesh points and face vertices: what the device needs when it
+// computes the volumes and CMs itself (RG_MESH_DEVICE_GEOMETRY).  cm_xy,
+// volume and cd_volume are left empty.
+inline void pack_topology(const Tessellation& tess, PackedMesh& m) {
   const int n = tess.GetPointNo();
+  const int total = tess.GetTotalPointNumber();
   const std::vector<Edge>& edges = tess.getAllEdges();
   const int ne = static_cast<int>(edges.size());
   m.n_cells = n;
   m.n_faces = ne;
   m.ghost_point.clear();
   m.ghost_face.clear();
-  std::unordered_map<int, int32_t> slot;
+  // ghost points are tessellation indices in [n, total): a dense slot table
+  std::vector<int32_t> slot(total > n ? static_cast<size_t>(total - n) : 0, -1);
   m.face_cells.resize(2 * static_cast<size_t>(ne));
   m.face_vertices.resize(4 * static_cast<size_t>(ne));
   for (int e = 0; e < ne; ++e) {
@@ -74,56 +78,74 @@ inline void pack_tessellation(const Tessellation& tess, const CacheData& cd, Pac
     const int nb[2] = {edge.neighbors.first, edge.neighbors.second};
     for (int s = 0; s < 2; ++s) {
       int32_t id = nb[s];
-      if (nb[s] < 0) throw std::runtime_error("rich_pack: edge with a negative neighbour");
+      if (nb[s] < 0 || nb[s] >= total) throw std::runtime_error("rich_pack: edge neighbour outside the tessellation");
       if (nb[s] >= n) {
-        auto it = slot.find(nb[s]);
-        if (it == slot.end()) {
-          const int32_t g = static_cast<int32_t>(m.ghost_point.size());
-          it = slot.emplace(nb[s], g).first;
+        int32_t& g = slot[static_cast<size_t>(nb[s] - n)];
+        if (g < 0) {
+          g = static_cast<int32_t>(m.ghost_point.size());
           m.ghost_point.push_back(nb[s]);
           m.ghost_face.push_back(e);
         }
-        id = n + it->second;
+        id = n + g;
       }
       m.face_cells[2 * static_cast<size_t>(e) + s] = id;
     }
-    m.face_vertices[4 * static_cast<size_t>(e) + 0] = edge.vertices.first.x;
-    m.face_vertices[4 * static_cast<size_t>(e) + 1] = edge.vertices.first.y;
-    m.face_vertices[4 * static_cast<size_t>(e) + 2] = edge.vertices.second.x;
-    m.face_vertices[4 * static_cast<size_t>(e) + 3] = edge.vertices.second.y;
+    double* fv = &m.face_vertices[4 * static_cast<size_t>(e)];
+    fv[0] = edge.vertices.first.x;
+    fv[1] = edge.vertices.first.y;
+    fv[2] = edge.vertices.second.x;
+    fv[3] = edge.vertices.second.y;
   }
   const int ng = static_cast<int>(m.ghost_point.size());
   m.n_ghosts = ng;
   const size_t np = static_cast<size_t>(n + ng);
   m.point_xy.resize(2 * np);
-  m.cm_xy.resize(2 * np);
   m.ghost_source.resize(static_cast<size_t>(ng));
   for (size_t p = 0; p < np; ++p) {
     const int ref = p < static_cast<size_t>(n) ? static_cast<int>(p) : m.ghost_point[p - n];
-    const Vector2D& x = tess.GetMeshPoint(ref);
-    const Vector2D& c = tess.GetCellCM(ref);
+    const Vector2D x = tess.GetMeshPoint(ref);
     m.point_xy[2 * p] = x.x;
     m.point_xy[2 * p + 1] = x.y;
+    if (p >= static_cast<size_t>(n)) m.ghost_source[p - n] = tess.GetOriginalIndex(ref);
+  }
+  m.cell_face_offset.resize(static_cast<size_t>(n) + 1);
+  m.cell_faces.resize(static_cast<size_t>(2 * ne));
+  m.cell_face_offset[0] = 0;
+  size_t k = 0;
+  for (int i = 0; i < n; ++i) {
+    const std::vector<int>& ce = tess.GetCellEdges(i);
+    if (k + ce.size() > m.cell_faces.size()) throw std::runtime_error("rich_pack: more cell faces than 2 per edge");
+    for (size_t j = 0; j < ce.size(); ++j) {
+      if (j > 0 && ce[j] <= ce[j - 1])
+        throw std::runtime_error("rich_pack: GetCellEdges is not in ascending edge order");
+      m.cell_faces[k++] = ce[j];
+    }
+    m.cell_face_offset[static_cast<size_t>(i) + 1] = static_cast<int32_t>(k);
+  }
+  m.cell_faces.resize(k);
+  m.cm_xy.clear();
+  m.volume.clear();
+  m.cd_volume.clear();
+}
+
+// Everything, with the volumes and CMs the host tessellation and CacheData
+// computed (uploaded without RG_MESH_DEVICE_GEOMETRY).
+inline void pack_tessellation(const Tessellation& tess, const CacheData& cd, PackedMesh& m) {
+  pack_topology(tess, m);
+  const int n = m.n_cells;
+  const size_t np = static_cast<size_t>(n + m.n_ghosts);
+  m.cm_xy.resize(2 * np);
+  for (size_t p = 0; p < np; ++p) {
+    const int ref = p < static_cast<size_t>(n) ? static_cast<int>(p) : m.ghost_point[p - n];
+    const Vector2D& c = tess.GetCellCM(ref);
     m.cm_xy[2 * p] = c.x;
     m.cm_xy[2 * p + 1] = c.y;
-    if (p >= static_cast<size_t>(n)) m.ghost_source[p - n] = tess.GetOriginalIndex(ref);
   }
   m.volume.resize(static_cast<size_t>(n));
   m.cd_volume.resize(static_cast<size_t>(n));
-  m.cell_face_offset.resize(static_cast<size_t>(n) + 1);
-  m.cell_faces.clear();
-  m.cell_faces.reserve(static_cast<size_t>(2 * ne));
-  m.cell_face_offset[0] = 0;
   for (int i = 0; i < n; ++i) {
     m.volume[static_cast<size_t>(i)] = tess.GetVolume(i);
     m.cd_volume[static_cast<size_t>(i)] = cd.volumes[static_cast<size_t>(i)];
-    const std::vector<int>& ce = tess.GetCellEdges(i);
-    for (size_t k = 0; k < ce.size(); ++k) {
-      if (k > 0 && ce[k] <= ce[k - 1])
-        throw std::runtime_error("rich_pack: GetCellEdges is not in ascending edge order");
-      m.cell_faces.push_back(ce[k]);
-    }
-    m.cell_face_offset[static_cast<size_t>(i) + 1] = static_cast<int32_t>(m.cell_faces.size());
   }
 }
 

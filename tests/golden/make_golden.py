@@ -17,6 +17,7 @@ many ``hdsim::TimeAdvance`` steps (``run_cells``, ``run_ext``, ``run_dts``).
 import argparse
 import glob
 import os
+import platform
 import subprocess
 import sys
 import tempfile
@@ -91,14 +92,16 @@ CASES3D = {
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("RICH_REFERENCE"),
+                    help="reference source tree (default: oracle/ref/Makefile's REF)")
     ap.add_argument("cases", nargs="*")
     a = ap.parse_args()
-    subprocess.check_call(["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle", "ref"),
-                           "REF=" + a.ref])
-    exe = os.path.join(ROOT, "oracle", "_ref", "ref_dump")
-    scratch = os.path.join(ROOT, "oracle", "_ref")
-    exe3 = os.path.join(ROOT, "oracle", "_ref", "ref_dump3d")
+    mk = ["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle", "ref")]
+    subprocess.check_call(mk + ["stage"] + (["REF=" + a.ref] if a.ref else []))
+    subprocess.check_call(mk + ["all"])
+    scratch = os.path.join(ROOT, "oracle", "_ref", platform.machine())
+    exe = os.path.join(scratch, "ref_dump")
+    exe3 = os.path.join(scratch, "ref_dump3d")
     os.makedirs(os.path.join(HERE, "3d"), exist_ok=True)
     for name in [c for c in (a.cases or sorted(CASES3D)) if c in CASES3D]:
         case, nx, ny, nz, run = CASES3D[name]

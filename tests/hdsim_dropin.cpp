@@ -1,0 +1,575 @@
+// hdsim_dropin.cpp -- hdsim driven through the GPU plugins, beside hdsim
+// driven through the reference's own plugins.
+//
+// Test driver only: it links the reference's sources (built by
+// oracle/ref/Makefile) and the product library librich_gb300.so through the
+// adapters in huji-rich_gb300/host/rich_gpu_adapters.hpp, exactly as a RICH
+// simulation would use them: the driver builds two (or three) complete
+// simulations -- tessellation, outer boundary, point motion, edge
+// velocities, source term, and the plugin set -- and calls
+// hdsim::TimeAdvance / TimeAdvance2Heun (hdsim2d.cpp:149-241, 323-449) on
+// each.  The stock set is SimpleCFL, SimpleFluxCalculator or
+// ModularFluxCalculator(LinearGaussImproved, Hllc), SimpleExtensiveUpdater
+// and SimpleCellUpdater; the GPU set is GpuCFL, GpuFluxCalculator,
+// GpuExtensiveUpdater and GpuCellUpdater over one GpuContext.  Nothing else
+// differs: the host rebuilds each simulation's Voronoi mesh in
+// MoveMeshPoints and moves its points as the reference does.
+//
+//   hdsim_dropin compare <case> <n> <steps> [hostgeom]
+//       stock and GPU FP64 simulations in lockstep; after every step the
+//       cells, extensives (with tracers), mesh points and time of the two
+//       are compared with == (the "Entropy" tracer within 1e-15 relative);
+//       prints one JSON line (first differing step, counts).  The GPU
+//       plugins form volumes and CMs on the device unless "hostgeom" is
+//       given, which uploads the host tessellation's and CacheData's.
+//   hdsim_dropin accuracy <case> <n> <steps> [stock]
+//       GPU FP64 and GPU FP32-mixed simulations (and the stock one with
+//       "stock") in lockstep; prints the density L1 of FP32-mixed against
+//       FP64 (and of FP64 against stock) at the end, cells matched by mesh
+//       point (the runs' points differ slightly, and so may their order).
+//   hdsim_dropin time <case> <n> <steps> <set>
+//       one simulation (set = stock | gpu | gpu32): wall time per step and
+//       the time spent inside the four plugin calls, the rest being the
+//       host's point motion, edge velocities and Voronoi rebuild.
+//
+// Cases:
+//   sod       Sod tube [0,1]x[0,0.2], 5n x n jittered lattice, rigid walls,
+//             Eulerian, first order (SimpleFluxCalculator), gamma 1.4
+//   sedov     Sedov-Taylor on [-1,1]^2, n x n, RoundCells(Lagrangian),
+//             LinearGaussImproved + RigidWallGenerator, gamma 5/3
+//   periodic  periodic [0,1]^2, n x n, Eulerian, LinearGaussImproved +
+//             PeriodicGhostGenerator, PeriodicEdgeVelocities,
+//             TimeAdvance2Heun
+//   tracers   the sedov case with tracers {"A", "Entropy", "Z"} and stickers
+//             {"frozen", "skip"} (LinearGaussImproved's calc_tracers {"A"}
+//             and skip_key "skip"; HasSticker("frozen") + SkipUpdate)
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <functional>
+#include <memory>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "rich_gpu_adapters.hpp"
+#include "source/newtonian/common/hllc.hpp"
+#include "source/newtonian/common/ideal_gas.hpp"
+#include "source/newtonian/two_dimensional/geometric_outer_boundaries/PeriodicBox.hpp"
+#include "source/newtonian/two_dimensional/geometric_outer_boundaries/SquareBox.hpp"
+#include "source/newtonian/two_dimensional/ghost_point_generators/PeriodicGhostGenerator.hpp"
+#include "source/newtonian/two_dimensional/ghost_point_generators/RigidWallGenerator.hpp"
+#include "source/newtonian/two_dimensional/hdsim2d.hpp"
+#include "source/newtonian/two_dimensional/interpolations/LinearGaussImproved.hpp"
+#include "source/newtonian/two_dimensional/modular_flux_calculator.hpp"
+#include "source/newtonian/two_dimensional/periodic_edge_velocities.hpp"
+#include "source/newtonian/two_dimensional/point_motions/eulerian.hpp"
+#include "source/newtonian/two_dimensional/point_motions/lagrangian.hpp"
+#include "source/newtonian/two_dimensional/point_motions/round_cells.hpp"
+#include "source/newtonian/two_dimensional/simple_cell_updater.hpp"
+#include "source/newtonian/two_dimensional/simple_cfl.hpp"
+#include "source/newtonian/two_dimensional/simple_extensive_updater.hpp"
+#include "source/newtonian/two_dimensional/simple_flux_calculator.hpp"
+#include "source/newtonian/two_dimensional/source_terms/zero_force.hpp"
+#include "source/newtonian/two_dimensional/stationary_box.hpp"
+#include "source/tessellation/VoronoiMesh.hpp"
+
+namespace {
+
+double now() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// Seconds spent inside each plugin call of one simulation.
+struct PluginClock {
+  double tsf = 0, fc = 0, eu = 0, cu = 0;
+  double total() const { return tsf + fc + eu + cu; }
+};
+
+// Forwarding plugins that time the wrapped one (the same wrappers go around
+// both plugin sets).
+class TimedTSF : public TimeStepFunction {
+ public:
+  TimedTSF(const TimeStepFunction& in, double& acc) : in_(in), acc_(acc) {}
+  double operator()(const Tessellation& t, const vector<ComputationalCell>& c, const EquationOfState& e,
+                    const vector<Vector2D>& ev, const double time, TracerStickerNames const& n) const override {
+    const double t0 = now();
+    const double r = in_(t, c, e, ev, time, n);
+    acc_ += now() - t0;
+    return r;
+  }
+
+ private:
+  const TimeStepFunction& in_;
+  double& acc_;
+};
+
+class TimedFC : public FluxCalculator {
+ public:
+  TimedFC(const FluxCalculator& in, double& acc) : in_(in), acc_(acc) {}
+  vector<Extensive> operator()(const Tessellation& t, const vector<Vector2D>& ev, const vector<ComputationalCell>& c,
+                               const vector<Extensive>& x, const CacheData& cd, const EquationOfState& e,
+                               const double time, const double dt, TracerStickerNames const& n) const override {
+    const double t0 = now();
+    vector<Extensive> r = in_(t, ev, c, x, cd, e, time, dt, n);
+    acc_ += now() - t0;
+    return r;
+  }
+
+ private:
+  const FluxCalculator& in_;
+  double& acc_;
+};
+
+class TimedEU : public ExtensiveUpdater {
+ public:
+  TimedEU(const ExtensiveUpdater& in, double& acc) : in_(in), acc_(acc) {}
+  void operator()(const vector<Extensive>& f, const PhysicalGeometry& pg, const Tessellation& t, const double dt,
+                  const CacheData& cd, const vector<ComputationalCell>& c, vector<Extensive>& x, double time,
+                  TracerStickerNames const& n) const override {
+    const double t0 = now();
+    in_(f, pg, t, dt, cd, c, x, time, n);
+    acc_ += now() - t0;
+  }
+
+ private:
+  const ExtensiveUpdater& in_;
+  double& acc_;
+};
+
+class TimedCU : public CellUpdater {
+ public:
+  TimedCU(const CellUpdater& in, double& acc) : in_(in), acc_(acc) {}
+  vector<ComputationalCell> operator()(const Tessellation& t, const PhysicalGeometry& pg, const EquationOfState& e,
+                                       vector<Extensive>& x, const vector<ComputationalCell>& old,
+                                       const CacheData& cd, TracerStickerNames const& n) const override {
+    const double t0 = now();
+    vector<ComputationalCell> r = in_(t, pg, e, x, old, cd, n);
+    acc_ += now() - t0;
+    return r;
+  }
+
+ private:
+  const CellUpdater& in_;
+  double& acc_;
+};
+
+std::vector<Vector2D> jittered_lattice(int nx, int ny, double x0, double x1, double y0, double y1, unsigned seed) {
+  std::mt19937_64 gen(seed);
+  std::uniform_real_distribution<double> u(-1e-3, 1e-3);
+  std::vector<Vector2D> r;
+  const double dx = (x1 - x0) / nx, dy = (y1 - y0) / ny;
+  for (int i = 0; i < nx; ++i)
+    for (int j = 0; j < ny; ++j) {
+      const double ux = u(gen), uy = u(gen);
+      r.push_back(Vector2D(x0 + (i + 0.5 + ux) * dx, y0 + (j + 0.5 + uy) * dy));
+    }
+  return r;
+}
+
+// Tracer compared within a relative tolerance instead of ==: the "Entropy"
+// tracer, which SimpleCellUpdater recomputes as p * pow(d, -gamma)
+// (simple_cell_updater.cpp:44-48) with the host's libm pow and the GPU with
+// the device pow (a few ulp apart); -1 = none.  Nothing else reads it.
+int g_entropy = -1;
+double g_entropy_max_rel = 0;
+const double kEntropyRel = 1e-15;
+
+enum Set { kStock = 0, kGpu64 = 1, kGpu32 = 2 };
+
+// One complete simulation: everything hdsim holds by reference lives here.
+struct Sim {
+  PluginClock clock;
+  bool heun = false;
+  std::unique_ptr<OuterBoundary> outer;
+  std::unique_ptr<VoronoiMesh> tess;
+  SlabSymmetry pg;
+  std::unique_ptr<IdealGas> eos;
+  Hllc rs;
+  Eulerian eul;
+  Lagrangian lag;
+  std::unique_ptr<RoundCells> round;
+  std::unique_ptr<EdgeVelocityCalculator> evc;
+  ZeroForce force;
+  std::unique_ptr<GhostPointGenerator> ghosts;
+  std::unique_ptr<LinearGaussImproved> sr;
+  // stock plugins
+  std::unique_ptr<SimpleCFL> s_tsf;
+  std::unique_ptr<FluxCalculator> s_fc;
+  SimpleExtensiveUpdater s_eu;
+  std::unique_ptr<SimpleCellUpdater> s_cu;
+  // GPU plugins
+  std::unique_ptr<rich_gb300::GpuContext> ctx;
+  std::unique_ptr<rich_gb300::GpuCFL> g_tsf;
+  std::unique_ptr<rich_gb300::GpuFluxCalculator> g_fc;
+  std::unique_ptr<rich_gb300::GpuExtensiveUpdater> g_eu;
+  std::unique_ptr<rich_gb300::GpuCellUpdater> g_cu;
+  // timing wrappers around whichever set is active
+  std::unique_ptr<TimedTSF> t_tsf;
+  std::unique_ptr<TimedFC> t_fc;
+  std::unique_ptr<TimedEU> t_eu;
+  std::unique_ptr<TimedCU> t_cu;
+  std::unique_ptr<hdsim> sim;
+
+  void advance() {
+    if (heun)
+      sim->TimeAdvance2Heun();
+    else
+      sim->TimeAdvance();
+  }
+};
+
+// The GPU plugins form volumes and CMs on the device (the adapters'
+// set_outer_boundary); false: the host packs the tessellation's and
+// CacheData's own.
+bool g_device_geometry = true;
+
+std::unique_ptr<Sim> make_sim(const std::string& which, int n, Set set) {
+  std::unique_ptr<Sim> s(new Sim);
+  const bool tracers = which == "tracers";
+  g_entropy = tracers ? 1 : -1;  // sorted names {"A", "Entropy", "Z"}
+  const std::string base = tracers ? "sedov" : which;
+  const TracerStickerNames tsn = tracers ? TracerStickerNames({"A", "Entropy", "Z"}, {"frozen", "skip"})
+                                         : TracerStickerNames();
+  const vector<string> calc_tracers = tracers ? vector<string>{"A"} : vector<string>();
+  const string skip_key = tracers ? "skip" : "";
+  vector<pair<const SimpleCellUpdater::Condition*, const SimpleCellUpdater::Action*> > seq;
+  if (tracers) seq.push_back({new HasSticker("frozen"), new SkipUpdate()});
+  s->s_cu.reset(new SimpleCellUpdater(seq));
+  s->s_tsf.reset(new SimpleCFL(0.3));
+
+  rg_config cfg;
+  rg_default_config(&cfg);
+  cfg.precision = set == kGpu32 ? RG_FP32_MIXED : RG_FP64;
+  rich_gb300::GpuTracerSpec spec;
+  spec.calc_tracers = calc_tracers;
+  spec.skip_key = skip_key;
+  spec.frozen_sticker = tracers ? "frozen" : "";
+
+  const PointMotion* pm = &s->eul;
+  vector<ComputationalCell> ic;
+  double gamma = 5.0 / 3.0;
+  if (base == "sod") {
+    s->outer.reset(new SquareBox(Vector2D(0, 0), Vector2D(1, 0.2)));
+    s->tess.reset(new VoronoiMesh(jittered_lattice(5 * n, n, 0, 1, 0, 0.2, 1), *s->outer));
+    gamma = 1.4;
+    s->eos.reset(new IdealGas(gamma));
+    s->evc.reset(new StationaryBox());
+    s->s_fc.reset(new SimpleFluxCalculator(s->rs));
+    cfg.order = 1;
+    ic.resize(static_cast<size_t>(s->tess->GetPointNo()));
+    for (size_t i = 0; i < ic.size(); ++i) {
+      const bool left = s->tess->GetMeshPoint(static_cast<int>(i)).x < 0.5;
+      ic[i].density = left ? 1 : 0.125;
+      ic[i].pressure = left ? 1 : 0.1;
+    }
+  } else if (base == "sedov") {
+    s->outer.reset(new SquareBox(Vector2D(-1, -1), Vector2D(1, 1)));
+    s->tess.reset(new VoronoiMesh(jittered_lattice(n, n, -1, 1, -1, 1, 2), *s->outer));
+    s->eos.reset(new IdealGas(gamma));
+    s->round.reset(new RoundCells(s->lag, *s->eos));
+    pm = s->round.get();
+    s->evc.reset(new StationaryBox());
+    s->ghosts.reset(new RigidWallGenerator());
+    s->sr.reset(new LinearGaussImproved(*s->eos, *s->ghosts, true, 0.2, 0.5, 0.7, calc_tracers, skip_key));
+    s->s_fc.reset(new ModularFluxCalculator(*s->sr, s->rs));
+    cfg.order = 2;
+    cfg.ghost_kind = RG_GHOST_RIGID_WALL;
+    const double rdep = std::max(0.02, 1.5 * 2.0 / n);
+    double vin = 0;
+    for (int i = 0; i < s->tess->GetPointNo(); ++i)
+      if (abs(s->tess->GetMeshPoint(i)) < rdep) vin += s->tess->GetVolume(i);
+    ic.resize(static_cast<size_t>(s->tess->GetPointNo()));
+    for (size_t i = 0; i < ic.size(); ++i) {
+      ic[i].density = 1;
+      ic[i].pressure = abs(s->tess->GetMeshPoint(static_cast<int>(i))) < rdep ? (gamma - 1) / vin : 1e-6;
+    }
+    if (tracers)
+      for (size_t i = 0; i < ic.size(); ++i) {
+        const Vector2D r = s->tess->GetMeshPoint(static_cast<int>(i));
+        ic[i].tracers = {r.x + (r.y > 0.1 ? 0.5 : 0.0), ic[i].pressure * std::pow(ic[i].density, -gamma),
+                         abs(r) < 0.3 ? 1.0 : 0.0};
+        const size_t h = std::hash<size_t>()(i * 2654435761u);
+        ic[i].stickers = {h % 17 == 3 && abs(r) >= 0.6, h % 11 == 5 && abs(r) >= 0.6};
+      }
+  } else if (base == "periodic") {
+    s->heun = true;
+    s->outer.reset(new PeriodicBox(0, 1, 1, 0));
+    s->tess.reset(new VoronoiMesh(jittered_lattice(n, n, 0, 1, 0, 1, 3), *s->outer));
+    s->eos.reset(new IdealGas(gamma));
+    s->evc.reset(new PeriodicEdgeVelocities());
+    s->ghosts.reset(new PeriodicGhostGenerator());
+    s->sr.reset(new LinearGaussImproved(*s->eos, *s->ghosts, true, 0.2, 0.5, 0.7));
+    s->s_fc.reset(new ModularFluxCalculator(*s->sr, s->rs));
+    cfg.order = 2;
+    cfg.ghost_kind = RG_GHOST_PERIODIC;
+    std::mt19937_64 gen(7);
+    std::uniform_real_distribution<double> u01(0, 1);
+    double bx[8], by[8], bw[8];
+    for (int k = 0; k < 8; ++k) {
+      bx[k] = u01(gen);
+      by[k] = u01(gen);
+      bw[k] = 0.02 + 0.08 * u01(gen);
+    }
+    ic.resize(static_cast<size_t>(s->tess->GetPointNo()));
+    const double pi2 = 2 * M_PI;
+    for (size_t i = 0; i < ic.size(); ++i) {
+      const Vector2D r = s->tess->GetMeshPoint(static_cast<int>(i));
+      double rho = 1;
+      for (int k = 0; k < 8; ++k) {
+        const double ddx = r.x - bx[k], ddy = r.y - by[k];
+        rho += 0.1 * std::exp(-(ddx * ddx + ddy * ddy) / (bw[k] * bw[k]));
+      }
+      ic[i].density = rho;
+      ic[i].pressure = 1;
+      ic[i].velocity = Vector2D(0.1 * std::sin(pi2 * (r.x + 2 * r.y)), 0.1 * std::cos(pi2 * (2 * r.x - r.y)));
+    }
+  } else {
+    throw std::runtime_error("unknown case " + which);
+  }
+  cfg.gamma = gamma;
+  cfg.time_integrator = s->heun ? RG_TIME_ADVANCE_HEUN : RG_TIME_ADVANCE;
+
+  const TimeStepFunction* tsf = s->s_tsf.get();
+  const FluxCalculator* fc = s->s_fc.get();
+  const ExtensiveUpdater* eu = &s->s_eu;
+  const CellUpdater* cu = s->s_cu.get();
+  if (set != kStock) {
+    s->ctx.reset(new rich_gb300::GpuContext(cfg, spec));
+    if (g_device_geometry) s->ctx->set_outer_boundary(*s->outer);
+    s->g_tsf.reset(new rich_gb300::GpuCFL(*s->ctx));
+    s->g_fc.reset(new rich_gb300::GpuFluxCalculator(*s->ctx));
+    s->g_eu.reset(new rich_gb300::GpuExtensiveUpdater(*s->ctx));
+    s->g_cu.reset(new rich_gb300::GpuCellUpdater(*s->ctx));
+    tsf = s->g_tsf.get();
+    fc = s->g_fc.get();
+    eu = s->g_eu.get();
+    cu = s->g_cu.get();
+  }
+  s->t_tsf.reset(new TimedTSF(*tsf, s->clock.tsf));
+  s->t_fc.reset(new TimedFC(*fc, s->clock.fc));
+  s->t_eu.reset(new TimedEU(*eu, s->clock.eu));
+  s->t_cu.reset(new TimedCU(*cu, s->clock.cu));
+  s->sim.reset(new hdsim(*s->tess, *s->outer, s->pg, ic, *s->eos, *pm, *s->evc, s->force, *s->t_tsf, *s->t_fc,
+                         *s->t_eu, *s->t_cu, tsn));
+  return s;
+}
+
+// IEEE == of two doubles, with NaN equal to NaN (a NaN on both sides is the
+// same failure; on one side only it is a difference)
+bool same(double a, double b) { return a == b || (std::isnan(a) && std::isnan(b)); }
+
+bool same_tracer(size_t j, double a, double b) {
+  if (static_cast<int>(j) != g_entropy) return same(a, b);
+  if (same(a, b)) return true;
+  const double rel = std::fabs(a - b) / std::max(std::fabs(a), std::fabs(b));
+  g_entropy_max_rel = std::max(g_entropy_max_rel, rel);
+  return rel <= kEntropyRel;
+}
+
+// Number of differing values between the two simulations' cells,
+// extensives (tracers included), mesh points and time.
+size_t count_differences(const hdsim& a, const hdsim& b) {
+  const vector<ComputationalCell>& ca = a.getAllCells();
+  const vector<ComputationalCell>& cb = b.getAllCells();
+  const vector<Extensive>& ea = a.getAllExtensives();
+  const vector<Extensive>& eb = b.getAllExtensives();
+  if (ca.size() != cb.size() || ea.size() != eb.size()) return static_cast<size_t>(-1);
+  size_t d = same(a.getTime(), b.getTime()) ? 0 : 1;
+  for (size_t i = 0; i < ca.size(); ++i) {
+    d += !same(ca[i].density, cb[i].density) + !same(ca[i].pressure, cb[i].pressure) +
+         !same(ca[i].velocity.x, cb[i].velocity.x) + !same(ca[i].velocity.y, cb[i].velocity.y);
+    if (ca[i].tracers.size() != cb[i].tracers.size() || ca[i].stickers != cb[i].stickers) ++d;
+    for (size_t j = 0; j < ca[i].tracers.size() && j < cb[i].tracers.size(); ++j)
+      d += !same_tracer(j, ca[i].tracers[j], cb[i].tracers[j]);
+  }
+  for (size_t i = 0; i < ea.size(); ++i) {
+    d += !same(ea[i].mass, eb[i].mass) + !same(ea[i].energy, eb[i].energy) +
+         !same(ea[i].momentum.x, eb[i].momentum.x) + !same(ea[i].momentum.y, eb[i].momentum.y);
+    if (ea[i].tracers.size() != eb[i].tracers.size()) ++d;
+    for (size_t j = 0; j < ea[i].tracers.size() && j < eb[i].tracers.size(); ++j)
+      d += !same_tracer(j, ea[i].tracers[j], eb[i].tracers[j]);
+  }
+  // the meshes the next step starts from
+  const Tessellation& ta = a.getTessellation();
+  const Tessellation& tb = b.getTessellation();
+  if (ta.GetPointNo() != tb.GetPointNo()) return d + 1;
+  for (int i = 0; i < ta.GetPointNo(); ++i)
+    d += !same(ta.GetMeshPoint(i).x, tb.GetMeshPoint(i).x) + !same(ta.GetMeshPoint(i).y, tb.GetMeshPoint(i).y);
+  return d;
+}
+
+// Density L1 of `a` against `b`, relative to b's, each cell of `a` matched
+// with the cell of `b` whose mesh point is nearest (a grid of buckets over
+// b's points; the runs' points differ by far less than a cell).
+double density_l1(const hdsim& a, const hdsim& b, size_t* unmatched) {
+  const Tessellation& ta = a.getTessellation();
+  const Tessellation& tb = b.getTessellation();
+  const vector<ComputationalCell>& ca = a.getAllCells();
+  const vector<ComputationalCell>& cb = b.getAllCells();
+  const int nb = tb.GetPointNo();
+  double x0 = 1e300, x1 = -1e300, y0 = 1e300, y1 = -1e300;
+  for (int i = 0; i < nb; ++i) {
+    const Vector2D p = tb.GetMeshPoint(i);
+    x0 = std::min(x0, p.x), x1 = std::max(x1, p.x), y0 = std::min(y0, p.y), y1 = std::max(y1, p.y);
+  }
+  const int g = std::max(1, static_cast<int>(std::sqrt(static_cast<double>(nb))));
+  const double hx = (x1 - x0) / g + 1e-300, hy = (y1 - y0) / g + 1e-300;
+  std::vector<std::vector<int>> bucket(static_cast<size_t>(g) * g);
+  auto cell_of = [&](const Vector2D& p, int& bx, int& by) {
+    bx = std::min(g - 1, std::max(0, static_cast<int>((p.x - x0) / hx)));
+    by = std::min(g - 1, std::max(0, static_cast<int>((p.y - y0) / hy)));
+  };
+  for (int i = 0; i < nb; ++i) {
+    int bx, by;
+    cell_of(tb.GetMeshPoint(i), bx, by);
+    bucket[static_cast<size_t>(by) * g + bx].push_back(i);
+  }
+  double num = 0, den = 0;
+  *unmatched = 0;
+  for (int i = 0; i < ta.GetPointNo(); ++i) {
+    const Vector2D p = ta.GetMeshPoint(i);
+    int bx, by, best = -1;
+    double bd = 1e300;
+    cell_of(p, bx, by);
+    for (int yy = std::max(0, by - 1); yy <= std::min(g - 1, by + 1); ++yy)
+      for (int xx = std::max(0, bx - 1); xx <= std::min(g - 1, bx + 1); ++xx)
+        for (int j : bucket[static_cast<size_t>(yy) * g + xx]) {
+          const double d = abs(tb.GetMeshPoint(j) - p);
+          if (d < bd) bd = d, best = j;
+        }
+    if (best < 0) {
+      ++*unmatched;
+      continue;
+    }
+    num += std::fabs(ca[static_cast<size_t>(i)].density - cb[static_cast<size_t>(best)].density);
+    den += std::fabs(cb[static_cast<size_t>(best)].density);
+  }
+  return num / den;
+}
+
+void print_clock(const char* name, const Sim& s, int steps, double wall) {
+  std::printf("\"%s\": {\"ms_per_step\": %.6f, \"plugin_ms_per_step\": %.6f, \"cfl_ms\": %.6f, \"flux_ms\": %.6f, "
+              "\"extensive_update_ms\": %.6f, \"cell_update_ms\": %.6f, \"host_rest_ms_per_step\": %.6f}",
+              name, 1e3 * wall / steps, 1e3 * s.clock.total() / steps, 1e3 * s.clock.tsf / steps,
+              1e3 * s.clock.fc / steps, 1e3 * s.clock.eu / steps, 1e3 * s.clock.cu / steps,
+              1e3 * (wall - s.clock.total()) / steps);
+}
+
+int usage() {
+  std::fprintf(stderr,
+               "usage: hdsim_dropin compare <case> <n> <steps>\n"
+               "       hdsim_dropin accuracy <case> <n> <steps> [stock]\n"
+               "       hdsim_dropin time <case> <n> <steps> <stock|gpu|gpu32>\n");
+  return 2;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  if (argc < 5) return usage();
+  for (int k = 5; k < argc; ++k)
+    if (std::string(argv[k]) == "hostgeom") g_device_geometry = false;
+  const std::string mode = argv[1], which = argv[2];
+  const int n = std::atoi(argv[3]), steps = std::atoi(argv[4]);
+  try {
+    if (mode == "compare") {
+      std::unique_ptr<Sim> a = make_sim(which, n, kStock);
+      std::unique_ptr<Sim> b = make_sim(which, n, kGpu64);
+      int first_diff = -1;
+      size_t diffs = count_differences(*a->sim, *b->sim);
+      if (diffs) first_diff = 0;
+      double wa = 0, wb = 0;
+      for (int k = 1; k <= steps && first_diff < 0; ++k) {
+        double t0 = now();
+        a->advance();
+        wa += now() - t0;
+        t0 = now();
+        b->advance();
+        wb += now() - t0;
+        diffs = count_differences(*a->sim, *b->sim);
+        if (diffs) first_diff = k;
+      }
+      std::printf("{\"mode\": \"compare\", \"case\": \"%s\", \"n\": %d, \"cells\": %d, \"steps\": %d, "
+                  "\"time\": %.17g, \"cycle\": %d, \"equal\": %s, \"first_differing_step\": %d, "
+                  "\"differing_values\": %zu, \"device_geometry\": %s, \"entropy_max_rel_diff\": %.3e, ",
+                  which.c_str(), n, a->tess->GetPointNo(), steps, b->sim->getTime(), b->sim->getCycle(),
+                  first_diff < 0 ? "true" : "false", first_diff, diffs, g_device_geometry ? "true" : "false",
+                  g_entropy_max_rel);
+      print_clock("stock", *a, steps, wa);
+      std::printf(", ");
+      print_clock("gpu", *b, steps, wb);
+      std::printf("}\n");
+      return first_diff < 0 ? 0 : 1;
+    }
+    if (mode == "accuracy") {
+      const bool stock = argc > 5 && std::string(argv[5]) == "stock";
+      std::unique_ptr<Sim> g64 = make_sim(which, n, kGpu64);
+      std::unique_ptr<Sim> g32 = make_sim(which, n, kGpu32);
+      std::unique_ptr<Sim> ref = stock ? make_sim(which, n, kStock) : nullptr;
+      double w64 = 0, w32 = 0, wr = 0;
+      int first_diff = -1;
+      for (int k = 1; k <= steps; ++k) {
+        double t0 = now();
+        g64->advance();
+        w64 += now() - t0;
+        t0 = now();
+        g32->advance();
+        w32 += now() - t0;
+        if (ref) {
+          t0 = now();
+          ref->advance();
+          wr += now() - t0;
+          if (first_diff < 0 && count_differences(*ref->sim, *g64->sim)) first_diff = k;
+        }
+      }
+      size_t un32 = 0, un64 = 0;
+      const double l1_32 = density_l1(*g32->sim, *g64->sim, &un32);
+      std::printf("{\"mode\": \"accuracy\", \"case\": \"%s\", \"n\": %d, \"cells\": %d, \"steps\": %d, "
+                  "\"time_fp64\": %.17g, \"time_fp32mixed\": %.17g, \"l1_density_fp32mixed_vs_fp64\": %.6e, "
+                  "\"unmatched\": %zu, ",
+                  which.c_str(), n, g64->tess->GetPointNo(), steps, g64->sim->getTime(), g32->sim->getTime(), l1_32,
+                  un32);
+      if (ref) {
+        const double l1_64 = density_l1(*g64->sim, *ref->sim, &un64);
+        std::printf("\"l1_density_fp64_vs_stock\": %.6e, \"fp64_equal_to_stock\": %s, \"first_differing_step\": %d, "
+                    "\"time_stock\": %.17g, ",
+                    l1_64, first_diff < 0 ? "true" : "false", first_diff, ref->sim->getTime());
+        print_clock("stock", *ref, steps, wr);
+        std::printf(", ");
+      }
+      print_clock("gpu_fp64", *g64, steps, w64);
+      std::printf(", ");
+      print_clock("gpu_fp32mixed", *g32, steps, w32);
+      std::printf("}\n");
+      return 0;
+    }
+    if (mode == "time") {
+      if (argc < 6) return usage();
+      const std::string set = argv[5];
+      const Set s = set == "stock" ? kStock : set == "gpu" ? kGpu64 : set == "gpu32" ? kGpu32 : kStock;
+      std::unique_ptr<Sim> a = make_sim(which, n, s);
+      a->advance();  // warm-up: first upload, module load
+      a->clock = PluginClock();
+      const double t0 = now();
+      for (int k = 0; k < steps; ++k) a->advance();
+      const double wall = now() - t0;
+      std::printf("{\"mode\": \"time\", \"case\": \"%s\", \"n\": %d, \"cells\": %d, \"steps\": %d, \"set\": \"%s\", ",
+                  which.c_str(), n, a->tess->GetPointNo(), steps, set.c_str());
+      print_clock(set.c_str(), *a, steps, wall);
+      std::printf("}\n");
+      return 0;
+    }
+  } catch (UniversalError& e) {
+    std::fprintf(stderr, "UniversalError: %s\n", e.GetErrorMessage().c_str());
+    for (size_t i = 0; i < e.GetFields().size(); ++i)
+      std::fprintf(stderr, "  %s = %.17g\n", e.GetFields()[i].c_str(), e.GetValues()[i]);
+    return 3;
+  } catch (std::exception& e) {
+    std::fprintf(stderr, "error: %s\n", e.what());
+    return 3;
+  }
+  return usage();
+}

@@ -1,6 +1,8 @@
 """The RICH-side adapters (huji-rich_gb300/host/rich_gpu_adapters.hpp) compile
-against the reference's own plugin interfaces.  Needs the reference source
-tree (only where the fixtures are generated); skipped elsewhere."""
+against the reference's own plugin interfaces.  Needs the reference's sources
+as oracle/ref/Makefile stages them (oracle/_ref/src, made by build() where the
+reference tree is present); skipped elsewhere.  The GPU tests
+(tests/test_gpu_hdsim.py) link and run the same adapters inside hdsim."""
 import os
 import shutil
 import subprocess
@@ -8,11 +10,11 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("RICH_SOURCE_TREE", "/root/reference")
+REF = os.path.join(ROOT, "oracle", "_ref", "src")
 
 
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "source")) or not shutil.which("g++"),
-                    reason="reference source tree not present")
+                    reason="staged reference sources not present")
 def test_adapters_compile_against_reference_headers():
     cmd = ["g++", "-std=c++17", "-fsyntax-only", "-w", "-include", "cassert", "-include", "cmath",
            "-I" + os.path.join(ROOT, "oracle", "ref", "shim"), "-I" + REF, "-I" + os.path.join(REF, "source"),
