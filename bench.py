@@ -22,10 +22,19 @@ e2e    the same steps through the C ABI with host buffers, as a moving-mesh
        velocities, the step, download of cells and extensives; "link" times
        one pinned copy each way of the same byte counts, the floor of the
        step's copies.
---impl reference   the CPU implementation of the path (the C restatement of
-       the reference's algorithm, oracle/rich_oracle.c: the reference sources
-       are not on this machine) on all host cores, one independent
-       simulation per core.
+e2e_hdsim  the same Sedov problem advanced by the reference's own hdsim
+       (tests/hdsim_dropin.cpp, linked with the reference built by
+       oracle/ref/Makefile) with the GPU plugins, RoundCells moving the points
+       and the host rebuilding the Voronoi mesh every step, beside hdsim with
+       the reference's own plugins: what a RICH user sees per step.
+batch  the batched form (512 independent Riemann problems, one launch per
+       phase, CUDA graph), FP32-mixed and FP64, with its own roofline.
+--impl reference   the reference's own CPU implementation of the path
+       (oracle/ref/ref_bench.cpp: SimpleCFL, ModularFluxCalculator(
+       LinearGaussImproved, Hllc), SimpleExtensiveUpdater, SimpleCellUpdater
+       on the same mesh points, initial state and RoundCells face velocities)
+       on all host cores, one independent simulation per core; where the
+       reference could not be built, the C restatement oracle/rich_oracle.c.
 
 Multi-GPU: replicas only (one independent simulation per rank); value sums
 the cells all ranks updated over the slowest rank's time.
@@ -33,6 +42,7 @@ the cells all ranks updated over the slowest rank's time.
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -54,6 +64,8 @@ NX = NY = 512
 GAMMA = 5.0 / 3.0
 SEED = 2
 FLUSH_BYTES = 256 << 20
+# the reference built for this machine by oracle/ref/Makefile (through build())
+REF_BIN = os.path.join(ROOT, "oracle", "_ref", platform.machine())
 
 
 def workload():
@@ -63,19 +75,28 @@ def workload():
     return mesh, cells
 
 
-def config_block(mesh, precision="fp64"):
-    return {"workload": f"sedov2d_{NX}x{NY}_lgi_hllc_{precision}", "cells": mesh.n_cells,
+def config_block(mesh):
+    """The workload, the same for both arms (implementation notes are kept
+    out of it: see impl_notes)."""
+    return {"workload": f"sedov2d_{NX}x{NY}_lgi_hllc", "cells": mesh.n_cells,
             "faces": mesh.n_faces, "ghosts": mesh.n_ghosts, "order": 2,
             "reconstruction": "LinearGaussImproved(slf, delta_v=0.2, theta=0.5, delta_P=0.7)",
             "riemann": "Hllc", "eos": "IdealGas(5/3)", "cfl": 0.3,
             "mesh": f"{NX}x{NY} lattice jittered +-1e-3 cell, seed {SEED}, rigid walls",
-            "point_motion": "RoundCells(Lagrangian, chi 0.15, eta 0.02) + StationaryBox face velocities, "
-                            "computed on the device (the timed kernels read them)",
-            "geometry": "volumes and CMs computed on the device from points and face vertices",
-            "e2e_step": "upload points + topology + face vertices (pinned), RoundCells motion, face velocities, "
-                        "dt, ApplyFix, fluxes and extensive update on the device (rg_advance_begin), "
-                        "cell update (rg_cell_update), read back cells, extensives and point velocities",
+            "initial": "rho 1, p 1e-6, energy 1 deposited as pressure in r < 0.02",
+            "point_motion": "RoundCells(Lagrangian, chi 0.15, eta 0.02) + StationaryBox face velocities, formed "
+                            "once before timing; every timed flux pass reads them",
+            "step": "SimpleCFL dt, LinearGaussImproved + Hllc fluxes, SimpleExtensiveUpdater, SimpleCellUpdater "
+                    "on a fixed mesh",
             "l2": "flushed before every timed step (256 MiB write)", "parallelism": "replicas"}
+
+
+IMPL_NOTES = {
+    "geometry": "volumes and CMs computed on the device from points and face vertices",
+    "face_velocities": "RoundCells point velocities and StationaryBox face velocities computed on the device",
+    "e2e_step": "upload points + topology + face vertices (pinned), RoundCells motion, face velocities, dt, "
+                "ApplyFix, fluxes and extensive update on the device (rg_advance_begin), cell update "
+                "(rg_cell_update), read back cells, extensives and point velocities"}
 
 
 # ------------------------------------------------------------------ clocks
@@ -172,9 +193,46 @@ def algorithmic_bytes(mesh, precision=0):
 
 # ------------------------------------------------------------------ CPU
 
+def roundcells_face_velocities(mesh, cells):
+    """RoundCells(Lagrangian, chi 0.15, eta 0.02) point velocities through
+    StationaryBox, as the C restatement computes them (the GPU arm forms the
+    same on the device)."""
+    import oracle
+    mo = oracle.motion(kind=2, edges=0, chi=0.15, eta=0.02, box=(-1.0, 1.0, -1.0, 1.0))
+    pv = oracle.point_velocities(mesh, cells, GAMMA, mo)
+    return oracle.edge_velocities(mesh, mo, pv)
+
+
+def write_workload(mesh, cells, d):
+    """The mesh points and initial cells the reference's own driver reads."""
+    pts = os.path.join(d, "points.f64")
+    cel = os.path.join(d, "cells.f64")
+    np.ascontiguousarray(mesh.point_xy[:mesh.n_cells], dtype="<f8").tofile(pts)
+    np.ascontiguousarray(cells, dtype="<f8").tofile(cel)
+    return pts, cel
+
+
+def ref_bench(mesh, cells, procs, warm, steps):
+    """Runs `procs` copies of the reference's own hot path
+    (oracle/ref/ref_bench.cpp), one simulation per process, at the same
+    time; returns their JSON records, or None where it was not built."""
+    exe = os.path.join(REF_BIN, "ref_bench")
+    if not os.path.exists(exe):
+        return None
+    with tempfile.TemporaryDirectory() as d:
+        pts, cel = write_workload(mesh, cells, d)
+        ps = [subprocess.Popen([exe, pts, cel, str(NX), str(NY), str(warm), str(steps)],
+                               stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+              for _ in range(procs)]
+        out = [p.communicate() for p in ps]
+    if any(p.returncode != 0 for p in ps):
+        raise RuntimeError("ref_bench failed: " + out[0][1][-500:])
+    return [json.loads(o[0].strip().splitlines()[-1]) for o in out]
+
+
 def cpu_steps(mesh, cells, ext, budget_s=10.0, max_steps=60):
     import oracle
-    ev = np.zeros((mesh.n_faces, 2))
+    ev = roundcells_face_velocities(mesh, cells)
     lp = oracle.lgi_params(0)
     c, e = cells, ext
     c, e, _ = oracle.step(mesh, c, e, ev, GAMMA, 0.3, 2, lp)  # warm
@@ -186,12 +244,30 @@ def cpu_steps(mesh, cells, ext, budget_s=10.0, max_steps=60):
     return k, time.perf_counter() - t0
 
 
+def cpu_baseline_block(mesh, cells, ext):
+    """One host core: the reference's own code where it was built, else the C
+    restatement; a sample of about 5-10 s of the same workload."""
+    n = mesh.n_cells
+    res = ref_bench(mesh, cells, 1, 1, 10)
+    if res is not None:
+        r = res[0]
+        return {"value": n * r["steps"] / r["seconds"], "unit": UNIT, "cores": 1, "kind": "reference",
+                "sample": f"{r['steps']} steps (after 1 warm-up) of the same {NX}x{NY} workload (FP64), one "
+                          "process: the reference's SimpleCFL, ModularFluxCalculator(LinearGaussImproved, Hllc), "
+                          "SimpleExtensiveUpdater, SimpleCellUpdater (oracle/ref/ref_bench.cpp, g++ -O2)",
+                "ms_per_step": r["ms_per_step"]}
+    kc, tc = cpu_steps(mesh, cells, ext)
+    return {"value": n * kc / tc, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{kc} steps of the same {NX}x{NY} workload (FP64), one thread, C restatement "
+                      "oracle/rich_oracle.c (gcc -O2); the reference itself is serial"}
+
+
 def _reference_worker(args):
     steps, warmup = args
     import oracle
     mesh, cells = workload()
     ext = oracle.init_extensives(mesh, cells, GAMMA)
-    ev = np.zeros((mesh.n_faces, 2))
+    ev = roundcells_face_velocities(mesh, cells)
     lp = oracle.lgi_params(0)
     c, e = cells, ext
     for _ in range(warmup):
@@ -203,29 +279,41 @@ def _reference_worker(args):
 
 
 def run_reference(args, world, rank):
+    """The reference arm: the reference's own CPU hot path on every host core
+    (one simulation per core), on this arm's workload, steps and warm-up."""
     if rank != 0:
         return
-    import multiprocessing as mp
-    import oracle
-    oracle.build()
     cores = min(os.cpu_count() or 1, 64)
-    steps = max(1, min(args.steps, 20))
-    warm = max(1, min(args.warmup, 3))
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(cores) as pool:
-        res = pool.map(_reference_worker, [(steps, warm)] * cores)
-    t = max(r[0] for r in res)
-    n = res[0][1]
+    steps = max(1, min(args.steps, 30))
+    warm = max(3, min(args.warmup, 10))
+    mesh, cells = workload()
+    res = ref_bench(mesh, cells, cores, warm, steps)
+    if res is not None:
+        t = max(r["seconds"] for r in res)
+        kind = "reference"
+        sample = (f"{cores} independent {NX}x{NY} simulations, one process per core, {warm} warm-up + {steps} "
+                  "timed steps each: the reference's own SimpleCFL, ModularFluxCalculator(LinearGaussImproved, "
+                  "Hllc), SimpleExtensiveUpdater and SimpleCellUpdater (oracle/ref/ref_bench.cpp, compiled from "
+                  "the reference's sources with g++ -O2 on this machine), RoundCells face velocities")
+    else:
+        import multiprocessing as mp
+        import oracle
+        oracle.build()
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(cores) as pool:
+            out = pool.map(_reference_worker, [(steps, warm)] * cores)
+        t = max(r[0] for r in out)
+        kind = "port"
+        sample = (f"{cores} independent {NX}x{NY} simulations, one per core, {warm} warm-up + {steps} timed steps "
+                  "each (C restatement oracle/rich_oracle.c, gcc -O2; the reference could not be built here), "
+                  "RoundCells face velocities")
+    n = mesh.n_cells
     value = cores * n * steps / t
-    mesh, _ = workload()
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
             "steps": steps, "warmup": warm, "ms_per_step": 1e3 * t / steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": config_block(mesh),
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{cores} independent {NX}x{NY} simulations, one per core, "
-                                       f"{steps} timed steps each (C restatement oracle/rich_oracle.c, "
-                                       "gcc -O2; the reference sources are absent on this machine)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -409,18 +497,18 @@ def run_gpu(args, world, rank, local_rank):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        kc, tc = cpu_steps(mesh, cells, ext)
-        cpu = {"value": n * kc / tc, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"{kc} steps of the same {NX}x{NY} workload (FP64), one thread, C restatement "
-                         "oracle/rich_oracle.c (gcc -O2); the reference itself is serial"}
+        cpu = cpu_baseline_block(mesh, cells, ext)
     adjoint = adjoint_block() if rank == 0 and not args.no_adjoint else None
     sedov3d = sedov3d_block(cpu=not args.no_cpu) if rank == 0 and not args.no_3d else None
     tracers = tracers_block(r64["total_ms"] / k) if rank == 0 and not args.no_tracers else None
+    batch = batch_block(cpu=not args.no_cpu) if rank == 0 and world == 1 and not args.no_batch else None
+    hdsim = hdsim_block() if rank == 0 and world == 1 and not args.no_hdsim else None
     if rank == 0:
         line = {"metric": METRIC, "value": value32, "unit": UNIT, "n_gpus": world, "steps": k,
                 "warmup": r32["warmup"], "ms_per_step": r32["total_ms"] / k, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
-                "data": "synthetic", "config": config_block(mesh, "fp32mixed"),
+                "data": "synthetic", "config": config_block(mesh),
+                "impl_notes": IMPL_NOTES,
                 "precision": "FP32-mixed: reconstruction, HLLC, CFL in FP32; geometry, volumes, "
                              "extensive accumulation, E/m - v^2/2 in FP64",
                 "l1_density_vs_fp64": l1, "l1_after_steps": r32["warmup"] + k,
@@ -444,6 +532,8 @@ def run_gpu(args, world, rank, local_rank):
                 "adjoint": adjoint,
                 "sedov3d": sedov3d,
                 "tracers": tracers,
+                "batch": batch,
+                "e2e_hdsim": hdsim,
                 "wall_s_timed_region": r32["wall"] + r64["wall"]}
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -669,6 +759,107 @@ def _batch_cpu_worker(args):
 BATCH_SEED = 11
 
 
+def batch_measure(lo, hi, steps, warmup, tune, local_rank, barrier=lambda: None):
+    """Generates problems [lo, hi) of the batched workload and times `steps`
+    steps of both precisions (CUDA events per kernel, then a CUDA graph of one
+    step replayed `steps` times).  Returns the per-precision records, the
+    batch mesh and the generation time."""
+    import torch
+    import richgpu
+    import synthetic
+    t0 = time.perf_counter()
+    mesh, off, gam, cells, _ = synthetic.riemann_batch_range(range(lo, hi), seed=BATCH_SEED)
+    gen_s = time.perf_counter() - t0
+    ext = device_extensives(mesh, cells, local_rank, off, gam)
+    res = {}
+    for precision in (0, 1):
+        h = richgpu.Handle(gamma=1.4, order=2, ghost_kind=0, precision=precision, device=local_rank)
+        h.upload_mesh(mesh)
+        h.set_problems(off, gam)
+        h.set_cells(cells)
+        h.set_extensives(ext)
+        h.set_edge_velocities(np.zeros((mesh.n_faces, 2)))
+        shapes = h.autotune(reps=3) if tune else h.launch_shapes()
+        for _ in range(max(warmup, 3)):
+            h.step()
+        kms = []
+        barrier()
+        torch.cuda.synchronize()
+        for _ in range(steps):
+            _, k = h.step_timed()
+            kms.append(k)
+        torch.cuda.synchronize()
+        barrier()
+        kms = np.array(kms)
+        stream = torch.cuda.ExternalStream(h.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        h.run_graph(1)
+        with torch.cuda.stream(stream):
+            e0.record()
+        h.run_graph(steps)
+        with torch.cuda.stream(stream):
+            e1.record()
+        torch.cuda.synchronize()
+        graph_ms = e0.elapsed_time(e1) / steps
+        times, _ = h.problem_times()
+        res[precision] = {"ms_per_step": float(kms.sum(1).mean()), "kernel_ms": kms.mean(0).tolist(),
+                          "graph_ms_per_step": graph_ms, "final_cells": h.get_cells(),
+                          "launch_shapes": {kk: [v["block"], v["max_blocks"], v["variant"]] for kk, v in shapes.items()},
+                          "time_min": float(times.min()), "time_max": float(times.max())}
+        h.close()
+    return res, mesh, gen_s
+
+
+def batch_cpu_baseline(problems):
+    import multiprocessing as mp
+    cores = min(os.cpu_count() or 1, 64)
+    sample = list(range(0, problems, max(1, problems // (2 * cores))))[:2 * cores]
+    chunks = [sample[k::cores] for k in range(cores)]
+    with mp.get_context("spawn").Pool(cores) as pool:
+        out = pool.map(_batch_cpu_worker, [(c, 2) for c in chunks if c])
+    t_wall = max(o[1] for o in out)
+    return {"value": sum(o[0] for o in out) / t_wall, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{len(sample)} of the {problems} problems, 2 steps each, one process per core "
+                      "(C restatement oracle/rich_oracle.c; the reference has no batched driver)"}
+
+
+def batch_roofline(res, mesh):
+    """The dominant kernel of the FP32-mixed batch step against HBM: the
+    single-problem byte counts (every problem's cells and faces once) plus the
+    per-point problem index (4 B) the batch kernels read."""
+    alg = algorithmic_bytes(mesh, 1)
+    n = mesh.n_cells
+    kms = np.array(res[1]["kernel_ms"])
+    dom = int(np.argmax(kms))
+    name = KERNELS[dom]
+    nbytes = alg[name] + 4 * n
+    peak, peak_kind = measured_peaks()
+    achieved = nbytes / (kms[dom] * 1e-3) / 1e9
+    return {"bound": "hbm", "kernel": KERNEL_NAMES[1][name] + "<batch>", "achieved": achieved, "peak": peak,
+            "unit": "GB/s", "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)",
+            "algorithmic_bytes_per_launch": nbytes,
+            "kernel_ms_mean": {KERNEL_NAMES[1][k]: float(v) for k, v in zip(KERNELS, kms)}}
+
+
+def batch_block(steps=20, warmup=3, problems=512, tune=True, cpu=True):
+    """The batched form inside the default benchmark run: all `problems`
+    problems on this GPU, both precisions, graph replay, roofline and a CPU
+    sample."""
+    res, mesh, gen_s = batch_measure(0, problems, steps, warmup, tune, 0)
+    c32, c64 = res[1].pop("final_cells"), res[0].pop("final_cells")
+    n = mesh.n_cells
+    return {"workload": f"riemann_batch_{problems}", "problems": problems, "cells": n, "faces": mesh.n_faces,
+            "steps": steps, "warmup": max(warmup, 3), "value": n / (res[1]["ms_per_step"] * 1e-3), "unit": UNIT,
+            "ms_per_step": res[1]["ms_per_step"], "dtype": "f32+f64",
+            "graph_value": n / (res[1]["graph_ms_per_step"] * 1e-3),
+            "l1_density_vs_fp64": float(np.abs(c32[:, 0] - c64[:, 0]).sum() / np.abs(c64[:, 0]).sum()),
+            "fp32mixed": res[1], "fp64": {"value": n / (res[0]["ms_per_step"] * 1e-3), **res[0]},
+            "roofline": batch_roofline(res, mesh),
+            "cpu_baseline": batch_cpu_baseline(problems) if cpu else None,
+            "generation_s": gen_s, "gpu_launches_per_step": 4,
+            "launch": "one launch per phase for all problems, per-problem dt; graph of one step replayed"}
+
+
 def run_batch(args, world, rank, local_rank):
     """512 independent 2D Riemann problems (cell counts log-uniform in
     [1024, 65536], rigid walls, LinearGaussImproved + Hllc, gamma 1.4 or 5/3)
@@ -678,7 +869,6 @@ def run_batch(args, world, rank, local_rank):
     cells (sharding.problem_shard): no collective on the data path, the
     timing is the maximum over ranks and `value` counts every rank's cells."""
     import torch
-    import richgpu
     import synthetic
     from sharding import problem_shard
 
@@ -699,50 +889,11 @@ def run_batch(args, world, rank, local_rank):
     lo, hi = problem_shard(counts, world, rank)
     if hi <= lo:
         raise SystemExit(f"rank {rank}: no problems in its shard ({args.problems} problems, {world} ranks)")
-    t0 = time.perf_counter()
-    mesh, off, gam, cells, meshes = synthetic.riemann_batch_range(range(lo, hi), seed=BATCH_SEED)
-    gen_s = time.perf_counter() - t0
-    ext = device_extensives(mesh, cells, local_rank, off, gam)
-    res = {}
-    for precision in (0, 1):
-        h = richgpu.Handle(gamma=1.4, order=2, ghost_kind=0, precision=precision, device=local_rank)
-        h.upload_mesh(mesh)
-        h.set_problems(off, gam)
-        h.set_cells(cells)
-        h.set_extensives(ext)
-        h.set_edge_velocities(np.zeros((mesh.n_faces, 2)))
-        shapes = h.launch_shapes() if args.no_tune else h.autotune(reps=3)
-        for _ in range(max(args.warmup, 3)):
-            h.step()
-        kms = []
-        if dist is not None:
-            dist.barrier()
-        torch.cuda.synchronize()
-        for _ in range(args.steps):
-            _, k = h.step_timed()
-            kms.append(k)
-        torch.cuda.synchronize()
-        if dist is not None:
-            dist.barrier()
-        kms = np.array(kms)
-        stream = torch.cuda.ExternalStream(h.stream())
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        h.run_graph(1)
-        with torch.cuda.stream(stream):
-            e0.record()
-        h.run_graph(args.steps)
-        with torch.cuda.stream(stream):
-            e1.record()
-        torch.cuda.synchronize()
-        graph_ms = e0.elapsed_time(e1) / args.steps
-        times, _ = h.problem_times()
-        res[precision] = {"ms_per_step": float(kms.sum(1).mean()), "kernel_ms": kms.mean(0).tolist(),
-                          "graph_ms_per_step": graph_ms, "final_cells": h.get_cells(),
-                          "launch_shapes": {kk: [v["block"], v["max_blocks"], v["variant"]] for kk, v in shapes.items()},
-                          "time_min": float(times.min()), "time_max": float(times.max())}
-        h.close()
+    res, mesh, gen_s = batch_measure(lo, hi, args.steps, args.warmup, not args.no_tune, local_rank,
+                                     barrier=(dist.barrier if dist is not None else lambda: None))
     c32, c64 = res[1].pop("final_cells"), res[0].pop("final_cells")
     l1 = float(np.abs(c32[:, 0] - c64[:, 0]).sum() / np.abs(c64[:, 0]).sum())
+    roof = batch_roofline(res, mesh)
     # every rank's cells over the slowest rank's step time
     if dist is not None:
         from torch.distributed import ReduceOp
@@ -755,18 +906,7 @@ def run_batch(args, world, rank, local_rank):
     if rank != 0:
         dist.destroy_process_group()
         return
-    cpu = None
-    if not args.no_cpu and world == 1:
-        import multiprocessing as mp
-        cores = min(os.cpu_count() or 1, 64)
-        sample = list(range(0, args.problems, max(1, args.problems // (2 * cores))))[:2 * cores]
-        chunks = [sample[k::cores] for k in range(cores)]
-        with mp.get_context("spawn").Pool(cores) as pool:
-            out = pool.map(_batch_cpu_worker, [(c, 2) for c in chunks if c])
-        t_wall = max(o[1] for o in out)
-        cpu = {"value": sum(o[0] for o in out) / t_wall, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"{len(sample)} of the {args.problems} problems, 2 steps each, one process per core "
-                         "(C restatement oracle/rich_oracle.c)"}
+    cpu = batch_cpu_baseline(args.problems) if (not args.no_cpu and world == 1) else None
     line = {"metric": METRIC, "value": n / (res[1]["ms_per_step"] * 1e-3), "unit": UNIT,
             "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3),
             "ms_per_step": res[1]["ms_per_step"], "higher_is_better": True, "scaling": "strong",
@@ -777,7 +917,7 @@ def run_batch(args, world, rank, local_rank):
                        "launch": "one launch per phase for all problems; graph of one step replayed",
                        "parallelism": f"problems sharded over {world} rank(s), contiguous ranges of ~equal cells",
                        "rank0_problems": [lo, hi], "generation_s": gen_s},
-            "l1_density_vs_fp64": l1,
+            "l1_density_vs_fp64": l1, "roofline": roof,
             "fp32mixed": {k: v for k, v in res[1].items()},
             "fp64": {"value": n / (res[0]["ms_per_step"] * 1e-3), **res[0]},
             "graph_value_fp32mixed": n / (res[1]["graph_ms_per_step"] * 1e-3),
@@ -785,6 +925,43 @@ def run_batch(args, world, rank, local_rank):
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+# ------------------------------------------------------------------ hdsim
+
+def hdsim_block(n=NX, steps=5, stock_steps=2):
+    """hdsim::TimeAdvance of the Sedov problem (n x n, RoundCells(Lagrangian),
+    LinearGaussImproved + Hllc) with the GPU plugins and with the
+    reference's own plugins, the host moving the points and rebuilding the
+    Voronoi mesh every step (tests/hdsim_dropin.cpp, `time` mode): ms per
+    step, the part spent in the four plugin calls and the host's rest."""
+    exe = os.path.join(REF_BIN, "hdsim_dropin")
+    if not os.path.exists(exe):
+        return {"unavailable": "hdsim_dropin was not built (the reference's sources are not staged)"}
+    rec = {"workload": f"hdsim::TimeAdvance sedov {n}x{n}, RoundCells(Lagrangian), StationaryBox, "
+                       "LinearGaussImproved + Hllc, host VoronoiMesh rebuild every step",
+           "note": "each step: host point motion and face velocities, GPU plugins (CFL, fluxes, extensive and "
+                   "cell update through rich_gpu_adapters.hpp, C ABI), host MoveMeshPoints + VoronoiMesh rebuild"}
+    for name, set_, k in (("fp32_mixed", "gpu32", steps), ("fp64", "gpu", steps), ("stock", "stock", stock_steps)):
+        r = subprocess.run([exe, "time", "sedov", str(n), str(k), set_], capture_output=True, text=True,
+                           timeout=900)
+        lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+        if r.returncode != 0 or not lines:
+            rec[name] = {"failed": r.stderr[-300:]}
+            continue
+        d = json.loads(lines[-1])
+        t = d[set_]
+        rec[name] = {"ms_per_step": t["ms_per_step"], "cell_updates_per_s": d["cells"] / (t["ms_per_step"] * 1e-3),
+                     "plugin_ms_per_step": t["plugin_ms_per_step"], "host_rest_ms_per_step": t["host_rest_ms_per_step"],
+                     "steps": k, "plugins_ms": {kk: t[kk] for kk in ("cfl_ms", "flux_ms", "extensive_update_ms",
+                                                                       "cell_update_ms")}}
+    if all("ms_per_step" in rec.get(k, {}) for k in ("fp32_mixed", "fp64", "stock")):
+        rec["value"] = rec["fp32_mixed"]["cell_updates_per_s"]
+        rec["unit"] = UNIT
+        rec["speedup_vs_stock_fp32_mixed"] = rec["stock"]["ms_per_step"] / rec["fp32_mixed"]["ms_per_step"]
+        rec["speedup_vs_stock_fp64"] = rec["stock"]["ms_per_step"] / rec["fp64"]["ms_per_step"]
+        rec["plugin_speedup_vs_stock_fp64"] = rec["stock"]["plugin_ms_per_step"] / rec["fp64"]["plugin_ms_per_step"]
+    return rec
 
 
 def main():
@@ -798,6 +975,8 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="default launch shapes instead of the autotuner's")
     ap.add_argument("--no-tracers", action="store_true", help="skip the tracer-path measurement")
     ap.add_argument("--no-3d", action="store_true", help="skip the 3D first-order measurement")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-form measurement")
+    ap.add_argument("--no-hdsim", action="store_true", help="skip hdsim driven through the GPU plugins")
     ap.add_argument("--workload", default="sedov", choices=["sedov", "riemann_batch", "sedov3d"])
     ap.add_argument("--problems", type=int, default=512)
     args = ap.parse_args()

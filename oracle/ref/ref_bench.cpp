@@ -5,13 +5,14 @@
 // oracle/ref/Makefile.  One process runs one simulation on one core (the
 // reference is serial); the benchmark starts one process per host core.
 //
-//   ref_bench <points.f64> <nx> <ny> <warmup> <steps>
+//   ref_bench <points.f64> <cells.f64> <nx> <ny> <warmup> <steps>
 //
 // Workload: 2D Sedov-Taylor on [-1,1]^2 (SquareBox, rigid walls), the mesh
 // points read from <points.f64> (nx*ny (x, y) pairs, little-endian float64;
 // the benchmark writes the same jittered lattice its GPU arm uses), a
-// VoronoiMesh of them, IdealGas(5/3), rho 1, p 1e-6, energy 1 deposited as
-// pressure within r < max(0.02, 1.5 dx).  A step is the plugin work of
+// VoronoiMesh of them, IdealGas(5/3), and the initial cells read from
+// <cells.f64> (nx*ny {density, pressure, vx, vy}: the GPU arm's initial
+// state, rho 1, p 1e-6, energy 1 deposited as pressure within r < 0.02).  A step is the plugin work of
 // hdsim::TimeAdvance (hdsim2d.cpp:149-241) on a fixed mesh, in hdsim's
 // order: SimpleCFL(0.3) (:161-165), ModularFluxCalculator(
 // LinearGaussImproved(RigidWallGenerator), Hllc) (:176-184),
@@ -50,20 +51,24 @@ double now() {
 }  // namespace
 
 int main(int argc, char** argv) {
-  if (argc < 6) {
-    std::fprintf(stderr, "usage: ref_bench <points.f64> <nx> <ny> <warmup> <steps>\n");
+  if (argc < 7) {
+    std::fprintf(stderr, "usage: ref_bench <points.f64> <cells.f64> <nx> <ny> <warmup> <steps>\n");
     return 2;
   }
-  const int nx = std::atoi(argv[2]), ny = std::atoi(argv[3]);
-  const int warm = std::atoi(argv[4]), steps = std::atoi(argv[5]);
+  const int nx = std::atoi(argv[3]), ny = std::atoi(argv[4]);
+  const int warm = std::atoi(argv[5]), steps = std::atoi(argv[6]);
   const size_t np = static_cast<size_t>(nx) * static_cast<size_t>(ny);
-  std::vector<double> xy(2 * np);
-  FILE* f = std::fopen(argv[1], "rb");
-  if (!f || std::fread(xy.data(), sizeof(double), xy.size(), f) != xy.size()) {
-    std::fprintf(stderr, "ref_bench: cannot read %zu points from %s\n", np, argv[1]);
-    return 2;
+  std::vector<double> xy(2 * np), c0(4 * np);
+  for (int k = 0; k < 2; ++k) {
+    std::vector<double>& dst = k == 0 ? xy : c0;
+    FILE* f = std::fopen(argv[1 + k], "rb");
+    const bool ok = f && std::fread(dst.data(), sizeof(double), dst.size(), f) == dst.size();
+    if (f) std::fclose(f);
+    if (!ok) {
+      std::fprintf(stderr, "ref_bench: cannot read %zu values from %s\n", dst.size(), argv[1 + k]);
+      return 2;
+    }
   }
-  std::fclose(f);
   try {
     const double t_setup = now();
     std::vector<Vector2D> pts(np);
@@ -86,14 +91,11 @@ int main(int argc, char** argv) {
     const TracerStickerNames tsn;
 
     const int n = tess.GetPointNo();
-    const double rdep = std::max(0.02, 1.5 * 2.0 / nx);
-    double vin = 0;
-    for (int i = 0; i < n; ++i)
-      if (abs(tess.GetMeshPoint(i)) < rdep) vin += tess.GetVolume(i);
     std::vector<ComputationalCell> cells(static_cast<size_t>(n));
-    for (int i = 0; i < n; ++i) {
-      cells[static_cast<size_t>(i)].density = 1;
-      cells[static_cast<size_t>(i)].pressure = abs(tess.GetMeshPoint(i)) < rdep ? (gamma - 1) / vin : 1e-6;
+    for (size_t i = 0; i < static_cast<size_t>(n); ++i) {
+      cells[i].density = c0[4 * i];
+      cells[i].pressure = c0[4 * i + 1];
+      cells[i].velocity = Vector2D(c0[4 * i + 2], c0[4 * i + 3]);
     }
     CacheData cd(tess, pg);
     // hdsim's init_extensives (hdsim2d.cpp:41-67)
