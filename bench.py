@@ -68,11 +68,47 @@ FLUSH_BYTES = 256 << 20
 REF_BIN = os.path.join(ROOT, "oracle", "_ref", platform.machine())
 
 
-def workload():
+def reference_mesh(nx, ny, box, boundary, seed):
+    """The reference's own tessellation of the jittered lattice: VoronoiMesh
+    of synthetic.jittered_points in input order, packed by rich_pack.hpp
+    (oracle/ref/ref_dump.cpp, mesh_rigid / mesh_periodic), or None where the
+    reference was not built."""
+    exe = os.path.join(REF_BIN, "ref_dump")
+    if not os.path.exists(exe):
+        return None
     import synthetic
-    mesh = synthetic.lattice_mesh(NX, NY, (-1.0, 1.0, -1.0, 1.0), "rigid", seed=SEED)
-    cells = synthetic.sedov_cells(mesh, GAMMA)
-    return mesh, cells
+    from meshview import MESH_FIELDS, PackedMesh
+    px, py = synthetic.jittered_points(nx, ny, *box, seed)
+    with tempfile.TemporaryDirectory() as d:
+        np.stack([px.ravel(), py.ravel()], 1).astype("<f8").tofile(os.path.join(d, "points.f64"))
+        np.array(box, dtype="<f8").tofile(os.path.join(d, "box.f64"))
+        r = subprocess.run([exe, "mesh_" + boundary, d, str(nx), str(ny), "0", "0"], capture_output=True, text=True)
+        if r.returncode != 0:
+            return None
+        return PackedMesh(**{k: np.load(os.path.join(d, "mesh_" + k + ".npy")) for k in MESH_FIELDS})
+
+
+_WORKLOAD = {}
+
+
+def workload():
+    """The Sedov workload's mesh and initial cells: the reference's own
+    VoronoiMesh of the jittered lattice where the reference is built here,
+    else the same mesh from synthetic.lattice_mesh (the same cells, faces and
+    ghosts up to a renumbering, geometry equal to rounding:
+    tests/test_cpu_mesh_pin.py)."""
+    if "mesh" not in _WORKLOAD:
+        import synthetic
+        box = (-1.0, 1.0, -1.0, 1.0)
+        mesh = reference_mesh(NX, NY, box, "rigid", SEED)
+        _WORKLOAD["source"] = "reference VoronoiMesh (oracle/ref/ref_dump.cpp mesh_rigid, input order)"
+        if mesh is None:
+            mesh = synthetic.lattice_mesh(NX, NY, box, "rigid", seed=SEED)
+            _WORKLOAD["source"] = "synthetic.lattice_mesh (the reference was not built here)"
+        _WORKLOAD["mesh"] = mesh
+    mesh = _WORKLOAD["mesh"]
+    import synthetic
+    return mesh, synthetic.sedov_cells(mesh, GAMMA)
 
 
 def config_block(mesh):
@@ -82,7 +118,7 @@ def config_block(mesh):
             "faces": mesh.n_faces, "ghosts": mesh.n_ghosts, "order": 2,
             "reconstruction": "LinearGaussImproved(slf, delta_v=0.2, theta=0.5, delta_P=0.7)",
             "riemann": "Hllc", "eos": "IdealGas(5/3)", "cfl": 0.3,
-            "mesh": f"{NX}x{NY} lattice jittered +-1e-3 cell, seed {SEED}, rigid walls",
+            "mesh": f"Voronoi mesh of a {NX}x{NY} lattice jittered +-1e-3 cell (seed {SEED}), rigid walls",
             "initial": "rho 1, p 1e-6, energy 1 deposited as pressure in r < 0.02",
             "point_motion": "RoundCells(Lagrangian, chi 0.15, eta 0.02) + StationaryBox face velocities, formed "
                             "once before timing; every timed flux pass reads them",
@@ -503,12 +539,13 @@ def run_gpu(args, world, rank, local_rank):
     tracers = tracers_block(r64["total_ms"] / k) if rank == 0 and not args.no_tracers else None
     batch = batch_block(cpu=not args.no_cpu) if rank == 0 and world == 1 and not args.no_batch else None
     hdsim = hdsim_block() if rank == 0 and world == 1 and not args.no_hdsim else None
+    accuracy = accuracy_block() if rank == 0 and world == 1 and not args.no_hdsim else None
     if rank == 0:
         line = {"metric": METRIC, "value": value32, "unit": UNIT, "n_gpus": world, "steps": k,
                 "warmup": r32["warmup"], "ms_per_step": r32["total_ms"] / k, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
                 "data": "synthetic", "config": config_block(mesh),
-                "impl_notes": IMPL_NOTES,
+                "impl_notes": dict(IMPL_NOTES, mesh_source=_WORKLOAD.get("source")),
                 "precision": "FP32-mixed: reconstruction, HLLC, CFL in FP32; geometry, volumes, "
                              "extensive accumulation, E/m - v^2/2 in FP64",
                 "l1_density_vs_fp64": l1, "l1_after_steps": r32["warmup"] + k,
@@ -534,6 +571,8 @@ def run_gpu(args, world, rank, local_rank):
                 "tracers": tracers,
                 "batch": batch,
                 "e2e_hdsim": hdsim,
+                "accuracy_hdsim_moving_mesh": accuracy,
+                "accuracy_hdsim_512x500": recorded_accuracy(),
                 "wall_s_timed_region": r32["wall"] + r64["wall"]}
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -929,6 +968,51 @@ def run_batch(args, world, rank, local_rank):
 
 # ------------------------------------------------------------------ hdsim
 
+def accuracy_block(n=128, steps=200):
+    """Accuracy on the moving-mesh Sedov configuration through hdsim: the
+    GPU FP64 and FP32-mixed plugins in lockstep and the reference's own
+    plugins at the same time in another process (tests/hdsim_dropin.cpp,
+    `accuracy` mode), RoundCells moving the points and the host rebuilding
+    the Voronoi mesh every step.  Density L1 (relative) after `steps` steps,
+    and whether the FP64 plugins' state equalled the stock one's after every
+    step."""
+    exe = os.path.join(REF_BIN, "hdsim_dropin")
+    if not os.path.exists(exe):
+        return {"unavailable": "hdsim_dropin was not built (the reference's sources are not staged)"}
+    r = subprocess.run([exe, "accuracy", "sedov", str(n), str(steps), "stock"], capture_output=True, text=True,
+                       timeout=7200)
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    if r.returncode != 0 or not lines:
+        return {"failed": r.stderr[-500:]}
+    d = json.loads(lines[-1])
+    return {"workload": f"hdsim::TimeAdvance sedov {n}x{n}, RoundCells(Lagrangian), host VoronoiMesh rebuild "
+                        f"every step, {steps} steps",
+            "l1_density_fp32mixed_vs_fp64": d["l1_density_fp32mixed_vs_fp64"],
+            "l1_density_fp64_vs_stock": d["l1_density_fp64_vs_stock"],
+            "l1_density_fp32mixed_vs_stock": d["l1_density_fp32mixed_vs_stock"],
+            "fp64_equal_to_stock_every_step": d["fp64_equal_to_stock"],
+            "first_differing_step": d["first_differing_step"], "unmatched_cells": d["unmatched"],
+            "time": {"stock": d["time_stock"], "fp64": d["time_fp64"], "fp32_mixed": d["time_fp32mixed"]},
+            "ms_per_step": {"stock": d["stock"]["ms_per_step"], "fp64": d["gpu_fp64"]["ms_per_step"],
+                            "fp32_mixed": d["gpu_fp32mixed"]["ms_per_step"]}}
+
+
+def recorded_accuracy():
+    """The 512^2 x 500-step record of accuracy_block (bench.py --workload
+    accuracy), kept in profiles/accuracy_sedov512.md: its run takes minutes,
+    longer than a default benchmark run."""
+    p = os.path.join(ROOT, "profiles", "accuracy_sedov512.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("{") and '"l1_density_fp32mixed_vs_fp64"' in line:
+            rec = json.loads(line)
+            rec["source"] = "recorded: profiles/accuracy_sedov512.md (python bench.py --workload accuracy)"
+            return rec
+    return None
+
+
+
 def hdsim_block(n=NX, steps=5, stock_steps=2):
     """hdsim::TimeAdvance of the Sedov problem (n x n, RoundCells(Lagrangian),
     LinearGaussImproved + Hllc) with the GPU plugins and with the
@@ -977,7 +1061,9 @@ def main():
     ap.add_argument("--no-3d", action="store_true", help="skip the 3D first-order measurement")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-form measurement")
     ap.add_argument("--no-hdsim", action="store_true", help="skip hdsim driven through the GPU plugins")
-    ap.add_argument("--workload", default="sedov", choices=["sedov", "riemann_batch", "sedov3d"])
+    ap.add_argument("--workload", default="sedov", choices=["sedov", "riemann_batch", "sedov3d", "accuracy"])
+    ap.add_argument("--accuracy-n", type=int, default=512)
+    ap.add_argument("--accuracy-steps", type=int, default=500)
     ap.add_argument("--problems", type=int, default=512)
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -985,6 +1071,9 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.workload == "accuracy":
+        if rank == 0:
+            print(json.dumps(accuracy_block(args.accuracy_n, args.accuracy_steps)), flush=True)
     elif args.workload == "riemann_batch":
         run_batch(args, world, rank, local_rank)
     elif args.workload == "sedov3d":

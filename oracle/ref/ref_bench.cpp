@@ -10,7 +10,8 @@
 // Workload: 2D Sedov-Taylor on [-1,1]^2 (SquareBox, rigid walls), the mesh
 // points read from <points.f64> (nx*ny (x, y) pairs, little-endian float64;
 // the benchmark writes the same jittered lattice its GPU arm uses), a
-// VoronoiMesh of them, IdealGas(5/3), and the initial cells read from
+// VoronoiMesh of them (Hilbert-ordered, the reference's default), IdealGas(5/3),
+// and the initial cells read from
 // <cells.f64> (nx*ny {density, pressure, vx, vy}: the GPU arm's initial
 // state, rho 1, p 1e-6, energy 1 deposited as pressure within r < 0.02).  A step is the plugin work of
 // hdsim::TimeAdvance (hdsim2d.cpp:149-241) on a fixed mesh, in hdsim's
@@ -23,6 +24,8 @@
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
+#include <map>
+#include <utility>
 #include <string>
 #include <vector>
 
@@ -91,11 +94,20 @@ int main(int argc, char** argv) {
     const TracerStickerNames tsn;
 
     const int n = tess.GetPointNo();
+    // VoronoiMesh keeps its points in Hilbert order (its default): each mesh
+    // point takes the initial cell of the input point with its coordinates
+    std::map<std::pair<double, double>, size_t> input;
+    for (size_t i = 0; i < np; ++i) input[std::make_pair(xy[2 * i], xy[2 * i + 1])] = i;
     std::vector<ComputationalCell> cells(static_cast<size_t>(n));
-    for (size_t i = 0; i < static_cast<size_t>(n); ++i) {
-      cells[i].density = c0[4 * i];
-      cells[i].pressure = c0[4 * i + 1];
-      cells[i].velocity = Vector2D(c0[4 * i + 2], c0[4 * i + 3]);
+    for (int i = 0; i < n; ++i) {
+      const Vector2D r = tess.GetMeshPoint(i);
+      const auto it = input.find(std::make_pair(r.x, r.y));
+      if (it == input.end()) throw UniversalError("ref_bench: a mesh point is not an input point");
+      const size_t j = it->second;
+      ComputationalCell& c = cells[static_cast<size_t>(i)];
+      c.density = c0[4 * j];
+      c.pressure = c0[4 * j + 1];
+      c.velocity = Vector2D(c0[4 * j + 2], c0[4 * j + 3]);
     }
     CacheData cd(tess, pg);
     // hdsim's init_extensives (hdsim2d.cpp:41-67)

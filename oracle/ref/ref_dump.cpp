@@ -17,7 +17,11 @@
 // with "frozen" keep their state through HasSticker + SkipUpdate), and dump
 // the tracer / sticker arrays beside the others (tr_*).
 //
-// For every case it writes, for the state reached after <warm_steps>
+// Cases mesh_rigid / mesh_periodic write only the packed tessellation of the
+// points in <outdir>/points.f64 (box in <outdir>/box.f64): the pin of the
+// test meshes' own tessellator (huji-rich_gb300/synthetic.py).
+//
+// For every other case it writes, for the state reached after <warm_steps>
 // hdsim::TimeAdvance steps (hdsim2d.cpp:149-241):
 //   mesh_*          the packed tessellation (huji-rich_gb300/host/rich_pack.hpp)
 //   cells0, ext0    ComputationalCell / Extensive state
@@ -356,6 +360,32 @@ int main(int argc, char** argv) {
   const int warm = std::atoi(argv[5]), run = std::atoi(argv[6]);
   g_heun = argc > 7 && std::string(argv[7]) == "heun";
   try {
+    if (which == "mesh_rigid" || which == "mesh_periodic") {
+      // The packed tessellation of given points: <outdir>/points.f64 holds
+      // nx*ny (x, y) pairs and <outdir>/box.f64 the box (x0, x1, y0, y1); the
+      // VoronoiMesh keeps the input order (no Hilbert reordering), so its
+      // cells are numbered as the points are.
+      std::vector<double> xy(2 * static_cast<size_t>(nx) * ny), box(4);
+      for (int k = 0; k < 2; ++k) {
+        std::vector<double>& dst = k == 0 ? xy : box;
+        const std::string path = g_out + (k == 0 ? "/points.f64" : "/box.f64");
+        FILE* f = std::fopen(path.c_str(), "rb");
+        const bool ok = f && std::fread(dst.data(), sizeof(double), dst.size(), f) == dst.size();
+        if (f) std::fclose(f);
+        if (!ok) throw std::runtime_error("cannot read " + path);
+      }
+      std::vector<Vector2D> pts(xy.size() / 2);
+      for (size_t i = 0; i < pts.size(); ++i) pts[i] = Vector2D(xy[2 * i], xy[2 * i + 1]);
+      SlabSymmetry pg;
+      std::unique_ptr<OuterBoundary> outer;
+      if (which == "mesh_rigid")
+        outer.reset(new SquareBox(Vector2D(box[0], box[2]), Vector2D(box[1], box[3])));
+      else
+        outer.reset(new PeriodicBox(box[0], box[1], box[3], box[2]));
+      VoronoiMesh tess(pts, *outer, false);
+      dump_mesh("mesh_", tess, pg);
+      return 0;
+    }
     SlabSymmetry pg;
     Hllc rs;
     ZeroForce force;

@@ -90,6 +90,35 @@ CASES3D = {
 }
 
 
+# The tessellator of the test and benchmark meshes (synthetic.lattice_mesh)
+# pinned to the reference's VoronoiMesh of the same points, written to
+# mesh/<name>.npz: name: (nx, ny, box, boundary, seed)
+MESH_PINS = {
+    "lattice64_rigid": (64, 64, (-1.0, 1.0, -1.0, 1.0), "rigid", 2),
+    "lattice64_periodic": (64, 64, (0.0, 1.0, 0.0, 1.0), "periodic", 3),
+    "lattice48x16_rigid": (48, 16, (0.0, 1.0, 0.0, 0.2), "rigid", 1),
+}
+
+
+def mesh_pins(exe, scratch, names):
+    sys.path.insert(0, os.path.join(ROOT, "huji-rich_gb300"))
+    import synthetic
+    os.makedirs(os.path.join(HERE, "mesh"), exist_ok=True)
+    for name in [c for c in (names or sorted(MESH_PINS)) if c in MESH_PINS]:
+        nx, ny, box, boundary, seed = MESH_PINS[name]
+        px, py = synthetic.jittered_points(nx, ny, *box, seed)
+        with tempfile.TemporaryDirectory(dir=scratch) as d:
+            np.stack([px.ravel(), py.ravel()], 1).astype("<f8").tofile(os.path.join(d, "points.f64"))
+            np.array(box, dtype="<f8").tofile(os.path.join(d, "box.f64"))
+            subprocess.check_call([exe, "mesh_" + boundary, d, str(nx), str(ny), "0", "0"])
+            arrays = {os.path.basename(f)[:-4]: np.load(f) for f in glob.glob(os.path.join(d, "*.npy"))}
+        arrays["case_params"] = np.array([nx, ny, seed], dtype=np.int64)
+        arrays["box"] = np.array(box)
+        out = os.path.join(HERE, "mesh", name + ".npz")
+        np.savez_compressed(out, **arrays)
+        print(f"{name}: {len(arrays)} arrays, {os.path.getsize(out) / 1024:.0f} KiB", file=sys.stderr)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("RICH_REFERENCE"),
@@ -102,6 +131,7 @@ def main():
     scratch = os.path.join(ROOT, "oracle", "_ref", platform.machine())
     exe = os.path.join(scratch, "ref_dump")
     exe3 = os.path.join(scratch, "ref_dump3d")
+    mesh_pins(exe, scratch, a.cases)
     os.makedirs(os.path.join(HERE, "3d"), exist_ok=True)
     for name in [c for c in (a.cases or sorted(CASES3D)) if c in CASES3D]:
         case, nx, ny, nz, run = CASES3D[name]

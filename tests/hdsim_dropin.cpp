@@ -23,10 +23,12 @@
 //       plugins form volumes and CMs on the device unless "hostgeom" is
 //       given, which uploads the host tessellation's and CacheData's.
 //   hdsim_dropin accuracy <case> <n> <steps> [stock]
-//       GPU FP64 and GPU FP32-mixed simulations (and the stock one with
-//       "stock") in lockstep; prints the density L1 of FP32-mixed against
-//       FP64 (and of FP64 against stock) at the end, cells matched by mesh
-//       point (the runs' points differ slightly, and so may their order).
+//       GPU FP64 and GPU FP32-mixed simulations in lockstep (and, with
+//       "stock", the stock one in a child process at the same time, whose
+//       state hash after every step is compared with the FP64 one's); prints
+//       the density L1 of FP32-mixed against FP64 (and of both against
+//       stock) at the end, cells matched by mesh point (the runs' points
+//       differ slightly, and so may their order).
 //   hdsim_dropin time <case> <n> <steps> <set>
 //       one simulation (set = stock | gpu | gpu32): wall time per step and
 //       the time spent inside the four plugin calls, the rest being the
@@ -53,6 +55,9 @@
 #include <random>
 #include <string>
 #include <vector>
+
+#include <sys/wait.h>
+#include <unistd.h>
 
 #include "rich_gpu_adapters.hpp"
 #include "source/newtonian/common/hllc.hpp"
@@ -401,53 +406,117 @@ size_t count_differences(const hdsim& a, const hdsim& b) {
   return d;
 }
 
+// Mesh points, densities and time of a simulation.
+struct Snapshot {
+  std::vector<double> xy, rho;
+  double time = 0;
+};
+
+Snapshot snapshot(const hdsim& a) {
+  Snapshot r;
+  const Tessellation& t = a.getTessellation();
+  const vector<ComputationalCell>& c = a.getAllCells();
+  for (int i = 0; i < t.GetPointNo(); ++i) {
+    r.xy.push_back(t.GetMeshPoint(i).x);
+    r.xy.push_back(t.GetMeshPoint(i).y);
+    r.rho.push_back(c[static_cast<size_t>(i)].density);
+  }
+  r.time = a.getTime();
+  return r;
+}
+
+// FNV-1a over the bit patterns of every cell and extensive value (tracers
+// included), mesh point and the time, with -0 taken as +0: equal states
+// (in the sense of count_differences without tolerances) hash equally.
+uint64_t state_hash(const hdsim& a) {
+  uint64_t h = 1469598103934665603ull;
+  auto add = [&h](double x) {
+    x = x + 0.0;  // -0 -> +0
+    uint64_t b;
+    std::memcpy(&b, &x, 8);
+    for (int k = 0; k < 8; ++k) {
+      h ^= (b >> (8 * k)) & 0xffu;
+      h *= 1099511628211ull;
+    }
+  };
+  for (const ComputationalCell& c : a.getAllCells()) {
+    add(c.density), add(c.pressure), add(c.velocity.x), add(c.velocity.y);
+    for (double t : c.tracers) add(t);
+  }
+  for (const Extensive& e : a.getAllExtensives()) {
+    add(e.mass), add(e.energy), add(e.momentum.x), add(e.momentum.y);
+    for (double t : e.tracers) add(t);
+  }
+  const Tessellation& t = a.getTessellation();
+  for (int i = 0; i < t.GetPointNo(); ++i) add(t.GetMeshPoint(i).x), add(t.GetMeshPoint(i).y);
+  add(a.getTime());
+  return h;
+}
+
 // Density L1 of `a` against `b`, relative to b's, each cell of `a` matched
 // with the cell of `b` whose mesh point is nearest (a grid of buckets over
 // b's points; the runs' points differ by far less than a cell).
-double density_l1(const hdsim& a, const hdsim& b, size_t* unmatched) {
-  const Tessellation& ta = a.getTessellation();
-  const Tessellation& tb = b.getTessellation();
-  const vector<ComputationalCell>& ca = a.getAllCells();
-  const vector<ComputationalCell>& cb = b.getAllCells();
-  const int nb = tb.GetPointNo();
+double density_l1(const Snapshot& a, const Snapshot& b, size_t* unmatched) {
+  const size_t na = a.rho.size(), nb = b.rho.size();
   double x0 = 1e300, x1 = -1e300, y0 = 1e300, y1 = -1e300;
-  for (int i = 0; i < nb; ++i) {
-    const Vector2D p = tb.GetMeshPoint(i);
-    x0 = std::min(x0, p.x), x1 = std::max(x1, p.x), y0 = std::min(y0, p.y), y1 = std::max(y1, p.y);
+  for (size_t i = 0; i < nb; ++i) {
+    x0 = std::min(x0, b.xy[2 * i]), x1 = std::max(x1, b.xy[2 * i]);
+    y0 = std::min(y0, b.xy[2 * i + 1]), y1 = std::max(y1, b.xy[2 * i + 1]);
   }
   const int g = std::max(1, static_cast<int>(std::sqrt(static_cast<double>(nb))));
   const double hx = (x1 - x0) / g + 1e-300, hy = (y1 - y0) / g + 1e-300;
-  std::vector<std::vector<int>> bucket(static_cast<size_t>(g) * g);
-  auto cell_of = [&](const Vector2D& p, int& bx, int& by) {
-    bx = std::min(g - 1, std::max(0, static_cast<int>((p.x - x0) / hx)));
-    by = std::min(g - 1, std::max(0, static_cast<int>((p.y - y0) / hy)));
+  std::vector<std::vector<size_t>> bucket(static_cast<size_t>(g) * g);
+  auto cell_of = [&](double px, double py, int& bx, int& by) {
+    bx = std::min(g - 1, std::max(0, static_cast<int>((px - x0) / hx)));
+    by = std::min(g - 1, std::max(0, static_cast<int>((py - y0) / hy)));
   };
-  for (int i = 0; i < nb; ++i) {
+  for (size_t i = 0; i < nb; ++i) {
     int bx, by;
-    cell_of(tb.GetMeshPoint(i), bx, by);
+    cell_of(b.xy[2 * i], b.xy[2 * i + 1], bx, by);
     bucket[static_cast<size_t>(by) * g + bx].push_back(i);
   }
   double num = 0, den = 0;
   *unmatched = 0;
-  for (int i = 0; i < ta.GetPointNo(); ++i) {
-    const Vector2D p = ta.GetMeshPoint(i);
-    int bx, by, best = -1;
+  for (size_t i = 0; i < na; ++i) {
+    const double px = a.xy[2 * i], py = a.xy[2 * i + 1];
+    int bx, by;
+    size_t best = nb;
     double bd = 1e300;
-    cell_of(p, bx, by);
+    cell_of(px, py, bx, by);
     for (int yy = std::max(0, by - 1); yy <= std::min(g - 1, by + 1); ++yy)
       for (int xx = std::max(0, bx - 1); xx <= std::min(g - 1, bx + 1); ++xx)
-        for (int j : bucket[static_cast<size_t>(yy) * g + xx]) {
-          const double d = abs(tb.GetMeshPoint(j) - p);
+        for (size_t j : bucket[static_cast<size_t>(yy) * g + xx]) {
+          const double d = std::hypot(b.xy[2 * j] - px, b.xy[2 * j + 1] - py);
           if (d < bd) bd = d, best = j;
         }
-    if (best < 0) {
+    if (best == nb) {
       ++*unmatched;
       continue;
     }
-    num += std::fabs(ca[static_cast<size_t>(i)].density - cb[static_cast<size_t>(best)].density);
-    den += std::fabs(cb[static_cast<size_t>(best)].density);
+    num += std::fabs(a.rho[i] - b.rho[best]);
+    den += std::fabs(b.rho[best]);
   }
   return num / den;
+}
+
+// Writes / reads a block of bytes through a pipe.
+bool write_all(int fd, const void* p, size_t n) {
+  const char* c = static_cast<const char*>(p);
+  while (n > 0) {
+    const ssize_t k = ::write(fd, c, n);
+    if (k <= 0) return false;
+    c += k, n -= static_cast<size_t>(k);
+  }
+  return true;
+}
+bool read_all(int fd, void* p, size_t n) {
+  char* c = static_cast<char*>(p);
+  while (n > 0) {
+    const ssize_t k = ::read(fd, c, n);
+    if (k <= 0) return false;
+    c += k, n -= static_cast<size_t>(k);
+  }
+  return true;
 }
 
 void print_clock(const char* name, const Sim& s, int steps, double wall) {
@@ -506,11 +575,47 @@ int main(int argc, char** argv) {
     }
     if (mode == "accuracy") {
       const bool stock = argc > 5 && std::string(argv[5]) == "stock";
+      // The stock simulation runs in a child process forked before any CUDA
+      // call (it never touches the GPU), concurrently with the two GPU
+      // ones; it sends back its per-step state hashes, final points and
+      // densities, and its timings.
+      int fds[2] = {-1, -1};
+      pid_t child = -1;
+      if (stock) {
+        if (pipe(fds) != 0) throw std::runtime_error("pipe failed");
+        child = fork();
+        if (child < 0) throw std::runtime_error("fork failed");
+        if (child == 0) {
+          ::close(fds[0]);
+          int rc = 0;
+          try {
+            std::unique_ptr<Sim> ref = make_sim(which, n, kStock);
+            std::vector<uint64_t> hashes;
+            const double t0 = now();
+            for (int k = 1; k <= steps; ++k) {
+              ref->advance();
+              hashes.push_back(state_hash(*ref->sim));
+            }
+            const double wall = now() - t0;
+            const Snapshot sn = snapshot(*ref->sim);
+            const uint64_t np = sn.rho.size();
+            const double clk[6] = {wall, ref->clock.tsf, ref->clock.fc, ref->clock.eu, ref->clock.cu, sn.time};
+            if (!write_all(fds[1], hashes.data(), 8 * hashes.size()) || !write_all(fds[1], &np, 8) ||
+                !write_all(fds[1], sn.xy.data(), 16 * np) || !write_all(fds[1], sn.rho.data(), 8 * np) ||
+                !write_all(fds[1], clk, sizeof clk))
+              rc = 4;
+          } catch (...) {
+            rc = 5;
+          }
+          ::close(fds[1]);
+          _exit(rc);
+        }
+        ::close(fds[1]);
+      }
       std::unique_ptr<Sim> g64 = make_sim(which, n, kGpu64);
       std::unique_ptr<Sim> g32 = make_sim(which, n, kGpu32);
-      std::unique_ptr<Sim> ref = stock ? make_sim(which, n, kStock) : nullptr;
-      double w64 = 0, w32 = 0, wr = 0;
-      int first_diff = -1;
+      std::vector<uint64_t> h64;
+      double w64 = 0, w32 = 0;
       for (int k = 1; k <= steps; ++k) {
         double t0 = now();
         g64->advance();
@@ -518,27 +623,42 @@ int main(int argc, char** argv) {
         t0 = now();
         g32->advance();
         w32 += now() - t0;
-        if (ref) {
-          t0 = now();
-          ref->advance();
-          wr += now() - t0;
-          if (first_diff < 0 && count_differences(*ref->sim, *g64->sim)) first_diff = k;
-        }
+        if (stock) h64.push_back(state_hash(*g64->sim));
       }
+      const Snapshot s64 = snapshot(*g64->sim), s32 = snapshot(*g32->sim);
       size_t un32 = 0, un64 = 0;
-      const double l1_32 = density_l1(*g32->sim, *g64->sim, &un32);
+      const double l1_32 = density_l1(s32, s64, &un32);
       std::printf("{\"mode\": \"accuracy\", \"case\": \"%s\", \"n\": %d, \"cells\": %d, \"steps\": %d, "
                   "\"time_fp64\": %.17g, \"time_fp32mixed\": %.17g, \"l1_density_fp32mixed_vs_fp64\": %.6e, "
                   "\"unmatched\": %zu, ",
-                  which.c_str(), n, g64->tess->GetPointNo(), steps, g64->sim->getTime(), g32->sim->getTime(), l1_32,
-                  un32);
-      if (ref) {
-        const double l1_64 = density_l1(*g64->sim, *ref->sim, &un64);
-        std::printf("\"l1_density_fp64_vs_stock\": %.6e, \"fp64_equal_to_stock\": %s, \"first_differing_step\": %d, "
-                    "\"time_stock\": %.17g, ",
-                    l1_64, first_diff < 0 ? "true" : "false", first_diff, ref->sim->getTime());
-        print_clock("stock", *ref, steps, wr);
-        std::printf(", ");
+                  which.c_str(), n, g64->tess->GetPointNo(), steps, s64.time, s32.time, l1_32, un32);
+      if (stock) {
+        std::vector<uint64_t> hs(static_cast<size_t>(steps));
+        uint64_t np = 0;
+        Snapshot sr;
+        double clk[6] = {0, 0, 0, 0, 0, 0};
+        bool ok = read_all(fds[0], hs.data(), 8 * hs.size()) && read_all(fds[0], &np, 8);
+        if (ok) {
+          sr.xy.resize(2 * np);
+          sr.rho.resize(np);
+          ok = read_all(fds[0], sr.xy.data(), 16 * np) && read_all(fds[0], sr.rho.data(), 8 * np) &&
+               read_all(fds[0], clk, sizeof clk);
+        }
+        ::close(fds[0]);
+        int status = 0;
+        waitpid(child, &status, 0);
+        if (!ok || !WIFEXITED(status) || WEXITSTATUS(status) != 0)
+          throw std::runtime_error("the stock simulation's process failed");
+        sr.time = clk[5];
+        int first_diff = -1;
+        for (int k = 0; k < steps && first_diff < 0; ++k)
+          if (hs[static_cast<size_t>(k)] != h64[static_cast<size_t>(k)]) first_diff = k + 1;
+        const double l1_64 = density_l1(s64, sr, &un64);
+        std::printf("\"l1_density_fp64_vs_stock\": %.6e, \"l1_density_fp32mixed_vs_stock\": %.6e, "
+                    "\"fp64_equal_to_stock\": %s, \"first_differing_step\": %d, \"time_stock\": %.17g, "
+                    "\"stock\": {\"ms_per_step\": %.6f, \"plugin_ms_per_step\": %.6f}, ",
+                    l1_64, density_l1(s32, sr, &un64), first_diff < 0 ? "true" : "false", first_diff, sr.time,
+                    1e3 * clk[0] / steps, 1e3 * (clk[1] + clk[2] + clk[3] + clk[4]) / steps);
       }
       print_clock("gpu_fp64", *g64, steps, w64);
       std::printf(", ");
