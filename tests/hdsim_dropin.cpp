@@ -29,6 +29,11 @@
 //       the density L1 of FP32-mixed against FP64 (and of both against
 //       stock) at the end, cells matched by mesh point (the runs' points
 //       differ slightly, and so may their order).
+//   hdsim_dropin sensitivity <case> <n> <steps> <delta> <every>
+//       the problem's own sensitivity, on the CPU: the stock simulation
+//       against the stock simulation from initial densities perturbed by a
+//       relative delta; density L1 and relative time difference every
+//       `every` steps.
 //   hdsim_dropin time <case> <n> <steps> <set>
 //       one simulation (set = stock | gpu | gpu32): wall time per step and
 //       the time spent inside the four plugin calls, the rest being the
@@ -230,6 +235,9 @@ struct Sim {
 // set_outer_boundary); false: the host packs the tessellation's and
 // CacheData's own.
 bool g_device_geometry = true;
+// Relative perturbation of the initial densities (sensitivity mode): cell i
+// gets density * (1 + delta * u_i), u_i uniform in [-1, 1] from a fixed seed.
+double g_perturb = 0;
 
 std::unique_ptr<Sim> make_sim(const std::string& which, int n, Set set) {
   std::unique_ptr<Sim> s(new Sim);
@@ -333,6 +341,11 @@ std::unique_ptr<Sim> make_sim(const std::string& which, int n, Set set) {
     }
   } else {
     throw std::runtime_error("unknown case " + which);
+  }
+  if (g_perturb != 0) {
+    std::mt19937_64 gen(99);
+    std::uniform_real_distribution<double> u(-1, 1);
+    for (ComputationalCell& c : ic) c.density *= 1 + g_perturb * u(gen);
   }
   cfg.gamma = gamma;
   cfg.time_integrator = s->heun ? RG_TIME_ADVANCE_HEUN : RG_TIME_ADVANCE;
@@ -531,6 +544,7 @@ int usage() {
   std::fprintf(stderr,
                "usage: hdsim_dropin compare <case> <n> <steps>\n"
                "       hdsim_dropin accuracy <case> <n> <steps> [stock]\n"
+               "       hdsim_dropin sensitivity <case> <n> <steps> <delta> <every>\n"
                "       hdsim_dropin time <case> <n> <steps> <stock|gpu|gpu32>\n");
   return 2;
 }
@@ -664,6 +678,33 @@ int main(int argc, char** argv) {
       std::printf(", ");
       print_clock("gpu_fp32mixed", *g32, steps, w32);
       std::printf("}\n");
+      return 0;
+    }
+    if (mode == "sensitivity") {
+      // The problem's own sensitivity: the stock simulation against the stock
+      // simulation from initial densities perturbed by a relative `delta`
+      // (CPU only); density L1 every `every` steps.
+      if (argc < 7) return usage();
+      const double delta = std::atof(argv[5]);
+      const int every = std::atoi(argv[6]);
+      std::unique_ptr<Sim> a = make_sim(which, n, kStock);
+      g_perturb = delta;
+      std::unique_ptr<Sim> b = make_sim(which, n, kStock);
+      g_perturb = 0;
+      std::printf("{\"mode\": \"sensitivity\", \"case\": \"%s\", \"n\": %d, \"delta\": %g, \"l1\": [", which.c_str(), n,
+                  delta);
+      for (int k = 1; k <= steps; ++k) {
+        a->advance();
+        b->advance();
+        if (k % every == 0 || k == steps) {
+          size_t un = 0;
+          std::printf("%s[%d, %.6e, %.6e]", k == every ? "" : ", ", k,
+                      density_l1(snapshot(*b->sim), snapshot(*a->sim), &un),
+                      (b->sim->getTime() - a->sim->getTime()) / a->sim->getTime());
+          std::fflush(stdout);
+        }
+      }
+      std::printf("]}\n");
       return 0;
     }
     if (mode == "time") {
