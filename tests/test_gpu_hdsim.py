@@ -26,12 +26,13 @@ pytestmark = pytest.mark.gpu
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 DRIVER = os.path.join(ROOT, "oracle", "_ref", platform.machine(), "hdsim_dropin")
+DRIVER3D = os.path.join(ROOT, "oracle", "_ref", platform.machine(), "hdsim3d_dropin")
 
 
-def run_driver(*args, timeout=900):
-    assert os.path.exists(DRIVER), (
-        f"{DRIVER} is missing: build() builds it (make -C oracle/ref dropin) from the staged reference sources")
-    r = subprocess.run([DRIVER] + [str(a) for a in args], capture_output=True, text=True, timeout=timeout)
+def run_driver(*args, timeout=900, exe=DRIVER):
+    assert os.path.exists(exe), (
+        f"{exe} is missing: build() builds it (make -C oracle/ref dropin) from the staged reference sources")
+    r = subprocess.run([exe] + [str(a) for a in args], capture_output=True, text=True, timeout=timeout)
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
     assert lines, f"driver printed no result (rc {r.returncode}):\n{r.stdout[-2000:]}\n{r.stderr[-2000:]}"
     return r.returncode, json.loads(lines[-1]), r.stderr
@@ -72,3 +73,22 @@ def test_hdsim_with_gpu_plugins_fp32_mixed_accuracy_on_moving_mesh():
     assert res["unmatched"] == 0
     # density L1 of the FP32-mixed path against FP64, relative
     assert res["l1_density_fp32mixed_vs_fp64"] <= 1e-5, res
+
+
+@pytest.mark.parametrize("case,n,steps", [
+    # Sedov-Taylor on a 24^3 CubeGrid (the 3D configuration's problem, smaller)
+    ("sedov", 24, 30),
+    # seeded states in every cell: every Hllc branch, tangential flow
+    ("random", 10, 12),
+    # a Sod tube along x
+    ("sod", 16, 30),
+])
+def test_hdsim3d_with_gpu_plugins_equals_hdsim3d_with_reference_plugins(case, n, steps):
+    """HDSim3D::timeAdvance with GpuTimeStep3D and GpuFluxCalculator3D
+    (rich_gpu_adapters3d.hpp) against CourantFriedrichsLewy and
+    FirstOrderHydroFlux(Hllc): cells and each step's dt equal after every
+    step (tests/hdsim3d_dropin.cpp)."""
+    rc, res, err = run_driver("compare", case, n, steps, exe=DRIVER3D)
+    assert res["equal"], (f"{case}: first differing step {res['first_differing_step']}, "
+                          f"{res['differing_values']} values differ\n{err[-2000:]}")
+    assert rc == 0
