@@ -445,6 +445,27 @@ def measure(precision, mesh, cells, ext, args, local_rank, barrier, max_over_ran
             "warmup": warm, "shapes": shapes}, final_cells
 
 
+def fixed_mesh_l1(mesh, cells, ext, steps, local_rank):
+    """Density L1 (relative) of the FP32-mixed path against the FP64 path
+    after `steps` steps of the timed workload from the same initial state
+    (the fixed mesh with RoundCells face velocities, dt from SimpleCFL on
+    each path)."""
+    import richgpu
+    out = []
+    for precision in (0, 1):
+        with richgpu.Handle(gamma=GAMMA, order=2, ghost_kind=0, precision=precision, device=local_rank) as h:
+            h.set_outer_box(-1.0, 1.0, -1.0, 1.0)
+            h.upload_mesh(mesh, flags=richgpu.MESH_DEVICE_GEOMETRY)
+            h.set_point_motion(kind=2, edges=0, chi=0.15, eta=0.02)
+            h.set_cells(cells)
+            h.set_extensives(ext)
+            h.point_velocities()
+            h.run(steps)
+            out.append(h.get_cells())
+    c64, c32 = out
+    return float(np.abs(c32[:, 0] - c64[:, 0]).sum() / np.abs(c64[:, 0]).sum())
+
+
 def pinned_io(mesh, ev, torch):
     """Copies of the per-step inputs and outputs in pinned (page-locked) host memory."""
     from meshview import MESH_FIELDS, PackedMesh
@@ -525,6 +546,7 @@ def run_gpu(args, world, rank, local_rank):
     r64, c64 = measure(0, mesh, cells, ext, args, local_rank, barrier, max_over_ranks)
     r32, c32 = measure(1, mesh, cells, ext, args, local_rank, barrier, max_over_ranks)
     l1 = float(np.abs(c32[:, 0] - c64[:, 0]).sum() / np.abs(c64[:, 0]).sum())
+    l1_500 = fixed_mesh_l1(mesh, cells, ext, 500, local_rank) if rank == 0 else None
     n, k = mesh.n_cells, args.steps
     value32 = world * n * k / (r32["total_ms"] * 1e-3)
     value64 = world * n * k / (r64["total_ms"] * 1e-3)
@@ -549,6 +571,7 @@ def run_gpu(args, world, rank, local_rank):
                 "precision": "FP32-mixed: reconstruction, HLLC, CFL in FP32; geometry, volumes, "
                              "extensive accumulation, E/m - v^2/2 in FP64",
                 "l1_density_vs_fp64": l1, "l1_after_steps": r32["warmup"] + k,
+                "l1_density_vs_fp64_500_steps": l1_500,
                 "roofline": roofline(r32, mesh, 1),
                 "cpu_baseline": cpu,
                 "e2e": {"value": world * n * r32["e2e_steps"] / r32["e2e_s"], "unit": UNIT,
