@@ -223,23 +223,25 @@ __global__ void __launch_bounds__(kBlock) k_ghost_fill32(MixedArgs a) {
   if (q < a.mesh.g) fill_ghost32(a, q);
 }
 
+// The limiters' candidate of one neighbour, without branches: the candidate
+// quotient is always formed and taken only where the limiter takes it, so
+// psi is the same bits as with the limiter's if / else-if, and a warp's
+// lanes never diverge here.
 __device__ __forceinline__ void limit32(float dphi, float cv, float cellv, float thr, float maxd, float mind,
                                         bool use_abs, float& psi) {
-  if (fabsf(dphi) > thr || cv * cellv < 0.0f) {
-    const float t = use_abs ? fabsf(1e-9f * cellv) : 1e-9f * cellv;
-    const float nt = use_abs ? -fabsf(1e-9f * cellv) : -1e-9f * cellv;
-    if (dphi > t)
-      psi = fminf(psi, __fdividef(maxd, dphi));
-    else if (dphi < nt)
-      psi = fminf(psi, __fdividef(mind, dphi));
-  }
+  const bool active = fabsf(dphi) > thr || cv * cellv < 0.0f;
+  const float t = use_abs ? fabsf(1e-9f * cellv) : 1e-9f * cellv;
+  const float nt = use_abs ? -fabsf(1e-9f * cellv) : -1e-9f * cellv;
+  const bool up = dphi > t;
+  const float cand = __fdividef(up ? maxd : mind, dphi);
+  psi = active && (up || dphi < nt) ? fminf(psi, cand) : psi;
 }
 
 __device__ __forceinline__ void shocked32(float dphi, float cv, float cellv, float thr, float nbv, float theta,
                                           float& psi) {
-  if (fabsf(dphi) > thr || cv * cellv < 0.0f) {
-    if (fabsf(dphi) > 1e-9f * cellv) psi = fminf(psi, fmaxf(__fdividef(theta * (nbv - cellv), dphi), 0.0f));
-  }
+  const bool active = (fabsf(dphi) > thr || cv * cellv < 0.0f) && fabsf(dphi) > 1e-9f * cellv;
+  const float cand = fmaxf(__fdividef(theta * (nbv - cellv), dphi), 0.0f);
+  psi = active ? fminf(psi, cand) : psi;
 }
 
 // The FP32 slopes of a periodic mesh (no self-mirror neighbour, no boundary
