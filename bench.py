@@ -131,8 +131,10 @@ IMPL_NOTES = {
     "geometry": "volumes and CMs computed on the device from points and face vertices",
     "face_velocities": "RoundCells point velocities and StationaryBox face velocities computed on the device",
     "e2e_step": "upload points + topology + face vertices (pinned), RoundCells motion, face velocities, dt, "
-                "ApplyFix, fluxes and extensive update on the device (rg_advance_begin), cell update "
-                "(rg_cell_update), read back cells, extensives and point velocities"}
+                "ApplyFix, fluxes and extensive update on the device (rg_advance_begin, point velocities "
+                "read back), cell update (rg_cell_update), cells and extensives read back "
+                "(rg_get_state_async: the copy overlaps the next step's mesh upload; the host waits for "
+                "it before the next step's computation)"}
 
 
 # ------------------------------------------------------------------ clocks
@@ -429,13 +431,17 @@ def measure(precision, mesh, cells, ext, args, local_rank, barrier, max_over_ran
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(ke):
+    for k in range(ke):
         h.upload_mesh(pmesh, flags=richgpu.MESH_DEVICE_GEOMETRY)
         upload_ms.append(h.last_upload_ms())
+        if k:
+            # the previous step's cells and extensives, copied while this
+            # step's mesh went up
+            h.wait_state()
         h.advance_begin(out=ppv)
         h.cell_update()
-        h.get_cells(out=pcells)
-        h.get_extensives(out=pext)
+        h.get_state_async(pcells, pext)
+    h.wait_state()
     torch.cuda.synchronize()
     e2e_s = max_over_ranks(time.perf_counter() - t0)
     h.close()

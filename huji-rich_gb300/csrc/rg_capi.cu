@@ -521,6 +521,9 @@ rg_status rg_create(const rg_config* cfg, rg_handle** out) {
   if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
   if ((e = cudaStreamCreateWithFlags(&h->upload_stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreateWithFlags(&h->ev_uploaded, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
+  if ((e = cudaStreamCreateWithFlags(&h->download_stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
+  if ((e = cudaEventCreateWithFlags(&h->ev_state, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
+  if ((e = cudaEventCreateWithFlags(&h->ev_downloaded, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
   for (auto& s : h->slots)
     if ((e = cudaEventCreateWithFlags(&s.last_use, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
   for (auto& k : h->ev_k)
@@ -542,6 +545,7 @@ rg_status rg_destroy(rg_handle* h) {
   if (!h) return RG_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->upload_stream) cudaStreamSynchronize(h->upload_stream);
+  if (h->download_stream) cudaStreamSynchronize(h->download_stream);
   for (auto& s : h->slots) {
     s.buf.release();
     if (s.last_use) cudaEventDestroy(s.last_use);
@@ -576,8 +580,11 @@ rg_status rg_destroy(rg_handle* h) {
   for (auto& k : h->ev_k)
     if (k) cudaEventDestroy(k);
   if (h->ev_uploaded) cudaEventDestroy(h->ev_uploaded);
+  if (h->ev_state) cudaEventDestroy(h->ev_state);
+  if (h->ev_downloaded) cudaEventDestroy(h->ev_downloaded);
   if (h->stream) cudaStreamDestroy(h->stream);
   if (h->upload_stream) cudaStreamDestroy(h->upload_stream);
+  if (h->download_stream) cudaStreamDestroy(h->download_stream);
   cudaGetLastError();
   delete h;
   return RG_OK;
@@ -737,7 +744,19 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t flags) {
     h->cells_records = rec;
   }
   const bool ext_keep = h->ext.bytes >= 32 * static_cast<size_t>(n);
-  RG_CUDA(h, cudaStreamSynchronize(h->stream));
+  // the compute stream may still use the state buffers (a step in flight,
+  // an rg_get_state_async copy it waits for): wait for it only when one of
+  // them is reallocated below
+  {
+    const size_t e1 = static_cast<size_t>(std::max(e, 1)), nn = static_cast<size_t>(n);
+    bool grows = !ext_keep || h->ev.bytes < 16 * e1 || h->slopes.bytes < 64 * nn || h->fluxes.bytes < 32 * e1;
+    if (h->heun)
+      grows = grows || h->mid_ext.bytes < 32 * nn ||
+              (h->mixed ? h->mid_cells32.bytes < 16 * np : h->mid_cells.bytes < 32 * np);
+    if (h->mixed)
+      grows = grows || h->slopes32.bytes < 32 * nn || h->flux32.bytes < 16 * e1 || h->ev32.bytes < 8 * e1;
+    if (grows) RG_CUDA(h, cudaStreamSynchronize(h->stream));
+  }
   if (!ext_keep) h->have_ext = false;
   RG_CUDA(h, h->ext.ensure(32 * static_cast<size_t>(n)));
   if (h->ev.bytes < 16 * static_cast<size_t>(e)) h->have_ev = false;
@@ -814,6 +833,32 @@ rg_status rg_get_cells(rg_handle* h, double* cells) {
   RG_CUDA(h, cudaMemcpyAsync(cells, h->cells.p, 32 * static_cast<size_t>(active_slot(h)->n),
                              cudaMemcpyDeviceToHost, h->stream));
   RG_CUDA(h, cudaStreamSynchronize(h->stream));
+  return RG_OK;
+}
+
+rg_status rg_get_state_async(rg_handle* h, double* cells, double* ext) {
+  if (!h || (!cells && !ext)) return RG_ERR_INVALID_ARGUMENT;
+  if (rg_status st = require(h, cells != nullptr, ext != nullptr, false, false)) return st;
+  const size_t bytes = 32 * static_cast<size_t>(active_slot(h)->n);
+  if (cells && h->mixed)
+    RG_CUDA(h, rg::launch_cells_to64(static_cast<const float4*>(h->cells32.p), static_cast<double*>(h->cells.p),
+                                     active_slot(h)->n, h->stream));
+  RG_CUDA(h, cudaEventRecord(h->ev_state, h->stream));
+  RG_CUDA(h, cudaStreamWaitEvent(h->download_stream, h->ev_state, 0));
+  if (cells)
+    RG_CUDA(h, cudaMemcpyAsync(cells, h->cells.p, bytes, cudaMemcpyDeviceToHost, h->download_stream));
+  if (ext) RG_CUDA(h, cudaMemcpyAsync(ext, h->ext.p, bytes, cudaMemcpyDeviceToHost, h->download_stream));
+  RG_CUDA(h, cudaEventRecord(h->ev_downloaded, h->download_stream));
+  // everything enqueued on the compute stream later waits for the copies
+  RG_CUDA(h, cudaStreamWaitEvent(h->stream, h->ev_downloaded, 0));
+  h->state_pending = true;
+  return RG_OK;
+}
+
+rg_status rg_wait_state(rg_handle* h) {
+  if (!h) return RG_ERR_INVALID_ARGUMENT;
+  if (h->state_pending) RG_CUDA(h, cudaEventSynchronize(h->ev_downloaded));
+  h->state_pending = false;
   return RG_OK;
 }
 

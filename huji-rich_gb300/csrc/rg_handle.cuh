@@ -147,6 +147,11 @@ struct rg_handle {
   cudaStream_t stream = nullptr;
   cudaStream_t upload_stream = nullptr;
   cudaEvent_t ev_uploaded = nullptr;  // the upload stream's work for the newest mesh slot
+  // rg_get_state_async: its copies run on download_stream after ev_state
+  // (recorded on stream); stream waits for ev_downloaded before later work
+  cudaStream_t download_stream = nullptr;
+  cudaEvent_t ev_state = nullptr, ev_downloaded = nullptr;
+  bool state_pending = false;
   cudaEvent_t ev_k[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   rgh::MeshSlot slots[2];
   int active = -1;

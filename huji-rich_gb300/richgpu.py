@@ -19,7 +19,8 @@ LIB_PATH = os.path.join(HERE, "librich_gb300.so")
 # every entry point include/rich_gb300.h declares
 EXPORTS = ("rg_default_config", "rg_create", "rg_destroy", "rg_status_string", "rg_last_error",
            "rg_upload_mesh", "rg_last_upload_ms", "rg_set_cells", "rg_get_cells",
-           "rg_set_extensives", "rg_get_extensives", "rg_set_edge_velocities",
+           "rg_set_extensives", "rg_get_extensives", "rg_get_state_async", "rg_wait_state",
+           "rg_set_edge_velocities",
            "rg_device_buffers", "rg_init_extensives", "rg_cfl_dt", "rg_flux", "rg_set_fluxes",
            "rg_extensive_update", "rg_cell_update", "rg_step", "rg_run", "rg_step_async",
            "rg_synchronize", "rg_step_timed", "rg_cfl_dt_noalloc", "rg_set_problems",
@@ -106,6 +107,8 @@ def load(path=LIB_PATH):
               "rg_set_edge_velocities", "rg_set_fluxes"):
         getattr(lib, f).argtypes = [vp, dp]
     lib.rg_device_buffers.argtypes = [vp, C.POINTER(RgDeviceView)]
+    lib.rg_get_state_async.argtypes = [vp, dp, dp]
+    lib.rg_wait_state.argtypes = [vp]
     lib.rg_init_extensives.argtypes = [vp]
     lib.rg_cfl_dt.argtypes = [vp, dp]
     lib.rg_flux.argtypes = [vp, C.c_double, dp]
@@ -236,6 +239,16 @@ class Handle:
         assert out.dtype == np.float64 and out.size == 4 * self.mesh.n_cells and out.flags.c_contiguous
         self._check(self.lib.rg_get_extensives(self.h, dptr(out)))
         return out
+
+    def get_state_async(self, cells_out, ext_out):
+        """Starts copying the cells and extensives into the given (pinned)
+        arrays without waiting; read them after wait_state()."""
+        for o in (cells_out, ext_out):
+            assert o.dtype == np.float64 and o.size == 4 * self.mesh.n_cells and o.flags.c_contiguous
+        self._check(self.lib.rg_get_state_async(self.h, dptr(cells_out), dptr(ext_out)))
+
+    def wait_state(self):
+        self._check(self.lib.rg_wait_state(self.h))
 
     def set_edge_velocities(self, ev):
         a = np.ascontiguousarray(ev, dtype=np.float64)

@@ -211,6 +211,18 @@ rg_status rg_last_upload_ms(const rg_handle* h, double* ms);
 rg_status rg_set_cells(rg_handle* h, const double* cells);
 rg_status rg_get_cells(rg_handle* h, double* cells);
 rg_status rg_set_extensives(rg_handle* h, const double* extensives);
+/* No counterpart in the reference.  rg_get_cells / rg_get_extensives
+ * without waiting: copies the cells and the extensives (either may be NULL)
+ * into the caller's host arrays on the handle's download stream once the
+ * work enqueued so far has finished, and returns at once.  The copies run
+ * beside a following rg_upload_mesh (its own stream; the host link is full
+ * duplex), and every computation enqueued on the handle afterwards waits for
+ * them on the device.  The arrays must not be read or freed before
+ * rg_wait_state returns; they should be pinned host memory (pageable memory
+ * is copied before the call returns). */
+rg_status rg_get_state_async(rg_handle* h, double* cells, double* extensives);
+/* Waits for the copies of the last rg_get_state_async. */
+rg_status rg_wait_state(rg_handle* h);
 rg_status rg_get_extensives(rg_handle* h, double* extensives);
 rg_status rg_set_edge_velocities(rg_handle* h, const double* edge_velocities);
 rg_status rg_device_buffers(rg_handle* h, rg_device_view* view);

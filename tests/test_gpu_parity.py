@@ -361,6 +361,57 @@ def test_upload_overlapped_with_running_steps(precision):
         assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_state_download_overlapped_with_next_upload(precision):
+    """A moving-mesh caller's loop: upload the tessellation (device
+    geometry), hdsim::TimeAdvance's first half (rg_advance_begin: RoundCells
+    motion, dt, fluxes, extensive update), the cell update, then the cells
+    and extensives back to the host.  With rg_get_state_async the download
+    of step k runs while the mesh of step k+1 is uploaded; every step's
+    cells, extensives and dt equal the synchronous loop's bit for bit."""
+    torch = pytest.importorskip("torch")
+    mesh = synthetic.lattice_mesh(160, 160, (-1.0, 1.0, -1.0, 1.0), "rigid", seed=4)
+    gamma = 5 / 3
+    cells = synthetic.sedov_cells(mesh, gamma)
+    ext0 = oracle.init_extensives(mesh, cells, gamma)
+
+    def pinned(shape):
+        return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+
+    runs = []
+    for overlap in (False, True):
+        with handle_for(gamma, 2, 0, precision=precision) as h:
+            h.set_outer_box(-1.0, 1.0, -1.0, 1.0)
+            h.upload_mesh(mesh, flags=richgpu.MESH_DEVICE_GEOMETRY)
+            h.set_point_motion(kind=2, edges=0, chi=0.15, eta=0.02)
+            h.set_cells(cells)
+            h.set_extensives(ext0)
+            bufs = [(pinned((mesh.n_cells, 4)), pinned((mesh.n_cells, 4))) for _ in range(2)]
+            out = []
+            pending = None
+            for k in range(6):
+                h.upload_mesh(mesh, flags=richgpu.MESH_DEVICE_GEOMETRY)
+                if pending is not None:
+                    h.wait_state()
+                    out.append(tuple(a.copy() for a in pending))
+                dt, _ = h.advance_begin()
+                h.cell_update()
+                c_out, e_out = bufs[k % 2]
+                if overlap:
+                    h.get_state_async(c_out, e_out)
+                    pending = (c_out, e_out, np.array([dt]))
+                else:
+                    out.append((h.get_cells(), h.get_extensives(), np.array([dt])))
+            if pending is not None:
+                h.wait_state()
+                out.append(tuple(a.copy() for a in pending))
+        runs.append(out)
+    assert len(runs[0]) == len(runs[1]) == 6
+    for a, b in zip(*runs):
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)
+
+
 TINY = [(1, "rigid"), (2, "rigid"), (3, "rigid"), (2, "periodic"), (3, "periodic"), (5, "periodic")]
 
 
