@@ -269,6 +269,15 @@ rg::MixedArgs mixed_args(rg_handle* h) {
     a.dt_p = static_cast<double*>(h->dt_p.p);
     a.n_problems = h->n_problems;
   }
+  if (tracers_on(h)) {
+    a.stickers = static_cast<const uint32_t*>(h->stickers.p);
+    a.skip_mask = h->tcfg.skip_sticker >= 0 ? 1u << h->tcfg.skip_sticker : 0u;
+    a.frozen_mask = h->tcfg.frozen_sticker >= 0 ? 1u << h->tcfg.frozen_sticker : 0u;
+    if (h->tcfg.n_tracers > 0) {
+      a.mflux = static_cast<double*>(h->mflux.p);
+      if (h->cfg.order == 2) a.shock = static_cast<unsigned char*>(h->shock.p);
+    }
+  }
   return a;
 }
 
@@ -413,17 +422,32 @@ rg_status enqueue_step(rg_handle* h, int step, cudaEvent_t* ev = nullptr) {
     a.dt32_from_device = 1;
     a.step = step;
     const bool fuse = fusable(h), have_dt = fuse && h->dt_next_ready;
+    // tracers: the FP64 tracer passes after each FP32 hydro pass, reading
+    // its shock decisions and mass fluxes (the dt from the device)
+    const bool tr = h->tcfg.n_tracers > 0;
+    rg::StepArgs a64 = step_args(h);
+    a64.dt_from_device = 1;
+    a64.step = step;
+    const rg::TracerArgs ta = tracer_args(h);
     if (ev) RG_CUDA(h, cudaEventRecord(ev[0], h->stream));
     if (!have_dt) RG_CUDA(h, rg::launch_cfl32(a, h->stream, false));
     if (ev) RG_CUDA(h, cudaEventRecord(ev[1], h->stream));
     a.take_next_dt = have_dt;
     if (h->cfg.order == 2) RG_CUDA(h, rg::launch_slopes32(a, h->stream));
     a.take_next_dt = 0;
+    if (tr && h->cfg.order == 2) RG_CUDA(h, rg::launch_tr_slopes(a64, ta, h->stream));
     if (ev) RG_CUDA(h, cudaEventRecord(ev[2], h->stream));
     RG_CUDA(h, rg::launch_faces32(a, h->stream, true));
+    if (tr) RG_CUDA(h, rg::launch_tr_faces(a64, ta, h->stream, true));
     if (ev) RG_CUDA(h, cudaEventRecord(ev[3], h->stream));
     a.cfl_next = fuse;
     RG_CUDA(h, rg::launch_update_mixed(a, h->stream, false, true, true));
+    if (tr) {
+      // the entropy tracer reads the new cells in FP64
+      RG_CUDA(h, rg::launch_cells_to64(static_cast<const float4*>(h->cells32.p), static_cast<double*>(h->cells.p),
+                                       active_slot(h)->n, h->stream));
+      RG_CUDA(h, rg::launch_tr_update(a64, ta, h->stream, false, true, true));
+    }
     if (ev) RG_CUDA(h, cudaEventRecord(ev[4], h->stream));
     h->dt_next_ready = fuse;
     h->have_fluxes = false;
@@ -978,11 +1002,17 @@ rg_status rg_flux(rg_handle* h, double dt, double* fluxes_out) {
   if (h->mixed) {
     rg::MixedArgs a = mixed_args(h);
     a.dt32 = static_cast<float>(dt);
+    const bool tr = h->tcfg.n_tracers > 0;
+    rg::StepArgs a64 = step_args(h);
+    a64.dt_host = dt;
+    const rg::TracerArgs ta = tracer_args(h);
     if (h->cfg.order == 2) {
       RG_CUDA(h, rg::launch_ghost_fill32(a, h->stream));
       RG_CUDA(h, rg::launch_slopes32(a, h->stream));
+      if (tr) RG_CUDA(h, rg::launch_tr_slopes(a64, ta, h->stream));
     }
     RG_CUDA(h, rg::launch_faces32(a, h->stream, false));
+    if (tr) RG_CUDA(h, rg::launch_tr_faces(a64, ta, h->stream, false));
   } else {
     rg::StepArgs a = step_args(h);
     a.dt_host = dt;
@@ -1018,6 +1048,11 @@ rg_status rg_extensive_update(rg_handle* h, double dt) {
     rg::MixedArgs a = mixed_args(h);
     a.dt32 = static_cast<float>(dt);
     RG_CUDA(h, rg::launch_update_mixed(a, h->stream, true, true, false));
+    if (h->tcfg.n_tracers > 0) {
+      rg::StepArgs a64 = step_args(h);
+      a64.dt_host = dt;
+      RG_CUDA(h, rg::launch_tr_update(a64, tracer_args(h), h->stream, true, true, false));
+    }
   } else {
     rg::StepArgs a = step_args(h);
     a.dt_host = dt;
@@ -1035,6 +1070,12 @@ rg_status rg_cell_update(rg_handle* h) {
   RG_TRY(reset_status(h, h->d_status, h->stream));
   if (h->mixed) {
     RG_CUDA(h, rg::launch_update_mixed(mixed_args(h), h->stream, false, false, true));
+    if (h->tcfg.n_tracers > 0) {
+      // the entropy tracer reads the new cells in FP64
+      RG_CUDA(h, rg::launch_cells_to64(static_cast<const float4*>(h->cells32.p), static_cast<double*>(h->cells.p),
+                                       active_slot(h)->n, h->stream));
+      RG_CUDA(h, rg::launch_tr_update(step_args(h), tracer_args(h), h->stream, false, false, true));
+    }
   } else {
     rg::StepArgs a = step_args(h);
     RG_CUDA(h, rg::launch_update(a, h->stream, false, false, true));

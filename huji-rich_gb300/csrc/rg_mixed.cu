@@ -177,6 +177,11 @@ __device__ __forceinline__ C4 point32(const MixedArgs& a, int p) {
   return C4{v.x, v.y, v.z, v.w};
 }
 
+// point p carries LinearGaussImproved's skip_key sticker (a ghost: its cell's)
+__device__ __forceinline__ bool skipped32(const MixedArgs& a, int p) {
+  return a.skip_mask != 0 && (a.stickers[p < a.mesh.n ? p : a.geom.ghost_real[p - a.mesh.n]] & a.skip_mask) != 0;
+}
+
 // SimpleCFL (simple_cfl.cpp:28-47, 58-71) in FP32.  max_e (c+|v-w_e|)/R is
 // (c + sqrt(max_e |v-w_e|^2))/R: the bound is monotone in |v-w|.
 template <bool kBatch>
@@ -377,11 +382,15 @@ __device__ __forceinline__ void k_slopes32_item(const MixedArgs& a, int i) {
                           : C4{cell.d + nb.d, cell.p + nb.p, cell.vx + nb.vx, cell.vy + nb.vy};
     addm(vx, s, en.x);
     addm(vy, s, en.y);
-    amax = C4{fmaxf(amax.d, nb.d), fmaxf(amax.p, nb.p), fmaxf(amax.vx, nb.vx), fmaxf(amax.vy, nb.vy)};
-    amin = C4{fminf(amin.d, nb.d), fminf(amin.p, nb.p), fminf(amin.vx, nb.vx), fminf(amin.vy, nb.vy)};
-    if (boundary && !(w & kNbrMirror)) {
-      nmax = C4{fmaxf(nmax.d, nb.d), fmaxf(nmax.p, nb.p), fmaxf(nmax.vx, nb.vx), fmaxf(nmax.vy, nb.vy)};
-      nmin = C4{fminf(nmin.d, nb.d), fminf(nmin.p, nb.p), fminf(nmin.vx, nb.vx), fminf(nmin.vy, nb.vy)};
+    // neighbours with LinearGaussImproved's skip_key sticker stay out of
+    // both extrema (:192-193, :314-315)
+    if (!skipped32(a, static_cast<int>(w & kNbrIdMask))) {
+      amax = C4{fmaxf(amax.d, nb.d), fmaxf(amax.p, nb.p), fmaxf(amax.vx, nb.vx), fmaxf(amax.vy, nb.vy)};
+      amin = C4{fminf(amin.d, nb.d), fminf(amin.p, nb.p), fminf(amin.vx, nb.vx), fminf(amin.vy, nb.vy)};
+      if (boundary && !(w & kNbrMirror)) {
+        nmax = C4{fmaxf(nmax.d, nb.d), fmaxf(nmax.p, nb.p), fmaxf(nmax.vx, nb.vx), fmaxf(nmax.vy, nb.vy)};
+        nmin = C4{fminf(nmin.d, nb.d), fminf(nmin.p, nb.p), fminf(nmin.vx, nb.vx), fminf(nmin.vy, nb.vy)};
+      }
     }
     // min(p, p_k) / max(p, p_k) < delta_p without the division
     ratio_shock = ratio_shock || fminf(cell.p, nb.p) < a.delta_p * fmaxf(cell.p, nb.p);
@@ -398,6 +407,7 @@ __device__ __forceinline__ void k_slopes32_item(const MixedArgs& a, int i) {
   if (a.slf) {
     const float cs = sqrtf(gamma32<kBatch>(a, i) * cell.p / cell.d);
     const bool shock = (sx.vx + sy.vy) * a.g32.width[i] < (-a.delta_v) * cs || ratio_shock;
+    if (a.shock) a.shock[i] = shock ? 1 : 0;  // read by the tracer slopes
     const C4 cmax = shock ? amax : nmax, cmin = shock ? amin : nmin;
     const C4 maxd{cmax.d - cell.d, cmax.p - cell.p, cmax.vx - cell.vx, cmax.vy - cell.vy};
     const C4 mind{cmin.d - cell.d, cmin.p - cell.p, cmin.vx - cell.vx, cmin.vy - cell.vy};
@@ -418,7 +428,9 @@ __device__ __forceinline__ void k_slopes32_item(const MixedArgs& a, int i) {
         limit32(dphi.vx, cv.vx, cell.vx, thr.vx, maxd.vx, mind.vx, true, psi2);
         limit32(dphi.vy, cv.vy, cell.vy, thr.vy, maxd.vy, mind.vy, true, psi3);
       } else {
-        const C4 nb = point32(a, static_cast<int>(a.geom.nbr[b + k] & kNbrIdMask));
+        const int p = static_cast<int>(a.geom.nbr[b + k] & kNbrIdMask);
+        if (skipped32(a, p)) continue;  // :339-340
+        const C4 nb = point32(a, p);
         shocked32(dphi.d, cv.d, cell.d, thr.d, nb.d, a.theta, psi0);
         shocked32(dphi.p, cv.p, cell.p, thr.p, nb.p, a.theta, psi1);
         shocked32(dphi.vx, cv.vx, cell.vx, thr.vx, nb.vx, a.theta, psi2);
@@ -476,11 +488,13 @@ __device__ __forceinline__ void k_slopes32_pf_item(const MixedArgs& a, int i) {
                           : C4{cell.d + nb.d, cell.p + nb.p, cell.vx + nb.vx, cell.vy + nb.vy};
     addm(vx, s, en.x);
     addm(vy, s, en.y);
-    amax = C4{fmaxf(amax.d, nb.d), fmaxf(amax.p, nb.p), fmaxf(amax.vx, nb.vx), fmaxf(amax.vy, nb.vy)};
-    amin = C4{fminf(amin.d, nb.d), fminf(amin.p, nb.p), fminf(amin.vx, nb.vx), fminf(amin.vy, nb.vy)};
-    if (boundary && !(wk[k] & kNbrMirror)) {
-      nmax = C4{fmaxf(nmax.d, nb.d), fmaxf(nmax.p, nb.p), fmaxf(nmax.vx, nb.vx), fmaxf(nmax.vy, nb.vy)};
-      nmin = C4{fminf(nmin.d, nb.d), fminf(nmin.p, nb.p), fminf(nmin.vx, nb.vx), fminf(nmin.vy, nb.vy)};
+    if (!skipped32(a, static_cast<int>(wk[k] & kNbrIdMask))) {
+      amax = C4{fmaxf(amax.d, nb.d), fmaxf(amax.p, nb.p), fmaxf(amax.vx, nb.vx), fmaxf(amax.vy, nb.vy)};
+      amin = C4{fminf(amin.d, nb.d), fminf(amin.p, nb.p), fminf(amin.vx, nb.vx), fminf(amin.vy, nb.vy)};
+      if (boundary && !(wk[k] & kNbrMirror)) {
+        nmax = C4{fmaxf(nmax.d, nb.d), fmaxf(nmax.p, nb.p), fmaxf(nmax.vx, nb.vx), fmaxf(nmax.vy, nb.vy)};
+        nmin = C4{fminf(nmin.d, nb.d), fminf(nmin.p, nb.p), fminf(nmin.vx, nb.vx), fminf(nmin.vy, nb.vy)};
+      }
     }
     ratio_shock = ratio_shock || fminf(cell.p, nb.p) < a.delta_p * fmaxf(cell.p, nb.p);
   }
@@ -495,6 +509,7 @@ __device__ __forceinline__ void k_slopes32_pf_item(const MixedArgs& a, int i) {
   if (a.slf) {
     const float cs = sqrtf(gamma32<kBatch>(a, i) * cell.p / cell.d);
     const bool shock = (sx.vx + sy.vy) * a.g32.width[i] < (-a.delta_v) * cs || ratio_shock;
+    if (a.shock) a.shock[i] = shock ? 1 : 0;  // read by the tracer slopes
     const C4 cmax = shock ? amax : nmax, cmin = shock ? amin : nmin;
     const C4 maxd{cmax.d - cell.d, cmax.p - cell.p, cmax.vx - cell.vx, cmax.vy - cell.vy};
     const C4 mind{cmin.d - cell.d, cmin.p - cell.p, cmin.vx - cell.vx, cmin.vy - cell.vy};
@@ -516,6 +531,7 @@ __device__ __forceinline__ void k_slopes32_pf_item(const MixedArgs& a, int i) {
         limit32(dphi.vx, cv.vx, cell.vx, thr.vx, maxd.vx, mind.vx, true, psi2);
         limit32(dphi.vy, cv.vy, cell.vy, thr.vy, maxd.vy, mind.vy, true, psi3);
       } else {
+        if (skipped32(a, static_cast<int>(wk[k] & kNbrIdMask))) continue;
         const C4& nb = nbk[k];
         shocked32(dphi.d, cv.d, cell.d, thr.d, nb.d, a.theta, psi0);
         shocked32(dphi.p, cv.p, cell.p, thr.p, nb.p, a.theta, psi1);
@@ -628,6 +644,8 @@ __device__ __forceinline__ void write32(const MixedArgs& a, int e, int real_side
       s = (a.dt32_from_device ? a.status->dt32 : a.dt32) * area;
   }
   a.flux32[e] = make_float4(c.m * s, c.en * s, c.mx * s, c.my * s);
+  // the unscaled mass flux the tracer faces kernel upwinds with
+  if (a.mflux) a.mflux[e] = static_cast<double>(c.m);
 }
 
 template <bool kScaled, bool kBatch>
@@ -793,6 +811,26 @@ __device__ __forceinline__ unsigned long long k_update_mixed_item(const MixedArg
     out2[2 * i + 1] = make_double2(px, py);
   }
   if (do_cells) {
+    if (a.frozen_mask && (a.stickers[i] & a.frozen_mask)) {
+      // simple_cell_updater.cpp:61-83 with (HasSticker, SkipUpdate): the old
+      // cell stays (its extensives above still took the fluxes)
+      const float4 c = a.cells32[i];
+      if (a.cells32_out) a.cells32_out[i] = c;
+      if (!a.cfl_next) return kInfBits;
+      const float cs = sqrtf(gamma32<kBatch>(a, i) * c.y / c.x);
+      float q = 0.0f;
+      if (a.ev_zero) {
+        if (m.cell_off[i + 1] > m.cell_off[i]) q = fmaxf(q, fmaf(c.z, c.z, c.w * c.w));
+      } else {
+        for (int k = m.cell_off[i]; k < m.cell_off[i + 1]; ++k) {
+          const float2 w = a.ev32[a.g32.fsign[k] & 0x7fffffff];
+          const float dx = c.z - w.x, dy = c.w - w.y;
+          q = fmaxf(q, fmaf(dx, dx, dy * dy));
+        }
+      }
+      const float res = (cs + sqrtf(q)) / a.g32.width[i];
+      return static_cast<unsigned long long>(__double_as_longlong(widen_exact(1.0f / res)));
+    }
     const float mf = narrow(mass);
     const float d = mf * a.g32.inv_cd_volume[i];
     if (d < 0.0f) {

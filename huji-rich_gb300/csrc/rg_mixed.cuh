@@ -82,6 +82,14 @@ struct MixedArgs {
   double* time_p;
   double* dt_p;
   int n_problems;
+  // stickers and the FP64 tracer passes (as StepArgs): the skip_key and
+  // SkipUpdate bits, each cell's shock decision and each face's unscaled
+  // mass flux for the tracer kernels (nullptr / 0: none)
+  const uint32_t* stickers;
+  uint32_t skip_mask;
+  uint32_t frozen_mask;
+  unsigned char* shock;
+  double* mflux;
   StepShapes shapes;  // launch shapes (host side; the kernels ignore it)
 };
 

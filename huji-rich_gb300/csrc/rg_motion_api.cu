@@ -186,12 +186,19 @@ rg_status rg_advance_begin(rg_handle* h, double* dt_out, double* pv_out) {
   if (h->mixed) {
     rg::MixedArgs m = mixed_args(h);
     m.dt32_from_device = 1;
+    const bool tr = h->tcfg.n_tracers > 0;
+    rg::StepArgs a64 = step_args(h);
+    a64.dt_from_device = 1;
+    const rg::TracerArgs ta = tracer_args(h);
     if (o2) {
       RG_CUDA(h, rg::launch_ghost_fill32(m, h->stream));
       RG_CUDA(h, rg::launch_slopes32(m, h->stream));
+      if (tr) RG_CUDA(h, rg::launch_tr_slopes(a64, ta, h->stream));
     }
     RG_CUDA(h, rg::launch_faces32(m, h->stream, true));
+    if (tr) RG_CUDA(h, rg::launch_tr_faces(a64, ta, h->stream, true));
     RG_CUDA(h, rg::launch_update_mixed(m, h->stream, false, true, false));
+    if (tr) RG_CUDA(h, rg::launch_tr_update(a64, ta, h->stream, false, true, false));
   } else {
     rg::StepArgs a = step_args(h);
     a.dt_from_device = 1;

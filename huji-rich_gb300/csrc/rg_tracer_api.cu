@@ -119,8 +119,9 @@ rg_status rg_set_tracer_config(rg_handle* h, const rg_tracer_config* cfg) {
   if (c.skip_sticker < -1 || c.skip_sticker > 31) return invalid(h, 3, c.skip_sticker);
   if (c.frozen_sticker < -1 || c.frozen_sticker > 31) return invalid(h, 4, c.frozen_sticker);
   const bool on = c.n_tracers > 0 || c.n_stickers > 0 || c.skip_sticker >= 0 || c.frozen_sticker >= 0;
-  // the FP32-mixed path has no tracer passes
-  if (on && h->mixed) return invalid(h, 5, 0);
+  // the FP32-mixed path runs its tracer passes with hdsim::TimeAdvance (fused
+  // or through the plugin calls), not in the fused TimeAdvance2Heun step
+  if (on && h->mixed && h->heun) return invalid(h, 5, 0);
   RG_CUDA(h, cudaStreamSynchronize(h->stream));
   const bool nt_changed = c.n_tracers != h->tcfg.n_tracers;
   h->tcfg = c;

@@ -461,10 +461,14 @@ rg_status rg_set_lagrangian_faces(rg_handle* h, const double* ws, const double* 
  * n_cells*2*n_tracers (x derivatives then y derivatives of each cell).
  * Stickers are one uint32 bit mask per cell.  Ghost points take the tracers
  * and stickers of the cell they copy.  Tracers run with TimeAdvance and
- * TimeAdvance2Heun, on single problems and batches; the FP32-mixed path and
- * differentiation return RG_ERR_INVALID_ARGUMENT while tracers or stickers
- * are configured.  Entropy uses the device pow(): that one tracer
- * agrees with the host libm to a few ulp; everything else is bit for bit. */
+ * TimeAdvance2Heun, on single problems and batches.  On the FP32-mixed path
+ * the FP32 hydro passes honour the stickers and the tracer passes run in
+ * FP64 on their shock decisions and mass fluxes, with TimeAdvance (fused,
+ * split or rg_advance_begin); a FP32-mixed handle with the fused
+ * TimeAdvance2Heun, and differentiation, return RG_ERR_INVALID_ARGUMENT
+ * while tracers or stickers are configured.  Entropy uses the device pow():
+ * that one tracer agrees with the host libm to a few ulp; everything else
+ * on the FP64 path is bit for bit. */
 #define RG_MAX_TRACERS 8
 typedef struct rg_tracer_config {
   int32_t n_tracers;        /* 0..RG_MAX_TRACERS */

@@ -420,8 +420,11 @@ size_t count_differences(const hdsim& a, const hdsim& b) {
 }
 
 // Mesh points, densities and time of a simulation.
+// Mesh points, densities, tracers (cell-major, nt per cell) and time of a
+// simulation.
 struct Snapshot {
-  std::vector<double> xy, rho;
+  std::vector<double> xy, rho, tr;
+  size_t nt = 0;
   double time = 0;
 };
 
@@ -429,10 +432,12 @@ Snapshot snapshot(const hdsim& a) {
   Snapshot r;
   const Tessellation& t = a.getTessellation();
   const vector<ComputationalCell>& c = a.getAllCells();
+  r.nt = c.empty() ? 0 : c[0].tracers.size();
   for (int i = 0; i < t.GetPointNo(); ++i) {
     r.xy.push_back(t.GetMeshPoint(i).x);
     r.xy.push_back(t.GetMeshPoint(i).y);
     r.rho.push_back(c[static_cast<size_t>(i)].density);
+    for (size_t j = 0; j < r.nt; ++j) r.tr.push_back(c[static_cast<size_t>(i)].tracers[j]);
   }
   r.time = a.getTime();
   return r;
@@ -469,7 +474,8 @@ uint64_t state_hash(const hdsim& a) {
 // Density L1 of `a` against `b`, relative to b's, each cell of `a` matched
 // with the cell of `b` whose mesh point is nearest (a grid of buckets over
 // b's points; the runs' points differ by far less than a cell).
-double density_l1(const Snapshot& a, const Snapshot& b, size_t* unmatched) {
+// column -1: density; j >= 0: tracer j
+double density_l1(const Snapshot& a, const Snapshot& b, size_t* unmatched, int column = -1) {
   const size_t na = a.rho.size(), nb = b.rho.size();
   double x0 = 1e300, x1 = -1e300, y0 = 1e300, y1 = -1e300;
   for (size_t i = 0; i < nb; ++i) {
@@ -506,8 +512,10 @@ double density_l1(const Snapshot& a, const Snapshot& b, size_t* unmatched) {
       ++*unmatched;
       continue;
     }
-    num += std::fabs(a.rho[i] - b.rho[best]);
-    den += std::fabs(b.rho[best]);
+    const double va = column < 0 ? a.rho[i] : a.tr[i * a.nt + static_cast<size_t>(column)];
+    const double vb = column < 0 ? b.rho[best] : b.tr[best * b.nt + static_cast<size_t>(column)];
+    num += std::fabs(va - vb);
+    den += std::fabs(vb);
   }
   return num / den;
 }
@@ -642,10 +650,12 @@ int main(int argc, char** argv) {
       const Snapshot s64 = snapshot(*g64->sim), s32 = snapshot(*g32->sim);
       size_t un32 = 0, un64 = 0;
       const double l1_32 = density_l1(s32, s64, &un32);
+      double l1_tr = 0;  // the largest tracer column's
+      for (size_t j = 0; j < s64.nt; ++j) l1_tr = std::max(l1_tr, density_l1(s32, s64, &un64, static_cast<int>(j)));
       std::printf("{\"mode\": \"accuracy\", \"case\": \"%s\", \"n\": %d, \"cells\": %d, \"steps\": %d, "
                   "\"time_fp64\": %.17g, \"time_fp32mixed\": %.17g, \"l1_density_fp32mixed_vs_fp64\": %.6e, "
-                  "\"unmatched\": %zu, ",
-                  which.c_str(), n, g64->tess->GetPointNo(), steps, s64.time, s32.time, l1_32, un32);
+                  "\"l1_tracers_fp32mixed_vs_fp64\": %.6e, \"unmatched\": %zu, ",
+                  which.c_str(), n, g64->tess->GetPointNo(), steps, s64.time, s32.time, l1_32, l1_tr, un32);
       if (stock) {
         std::vector<uint64_t> hs(static_cast<size_t>(steps));
         uint64_t np = 0;

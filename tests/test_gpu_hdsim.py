@@ -75,6 +75,18 @@ def test_hdsim_with_gpu_plugins_fp32_mixed_accuracy_on_moving_mesh():
     assert res["l1_density_fp32mixed_vs_fp64"] <= 1e-5, res
 
 
+def test_hdsim_with_gpu_plugins_fp32_mixed_tracers():
+    """The FP32-mixed plugins with tracers and stickers (the tracers case:
+    Sedov 64^2 with RoundCells, {"A", "Entropy", "Z"}, frozen and
+    limiter-skipped cells) against the FP64 plugins through hdsim, 60
+    steps: density and every tracer within 1e-5 relative L1."""
+    rc, res, err = run_driver("accuracy", "tracers", 64, 60)
+    assert rc == 0, err[-2000:]
+    assert res["unmatched"] == 0
+    assert res["l1_density_fp32mixed_vs_fp64"] <= 1e-5, res
+    assert res["l1_tracers_fp32mixed_vs_fp64"] <= 1e-5, res
+
+
 @pytest.mark.parametrize("case,n,steps", [
     # Sedov-Taylor on a 24^3 CubeGrid (the 3D configuration's problem, smaller)
     ("sedov", 24, 30),

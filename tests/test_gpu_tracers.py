@@ -182,11 +182,65 @@ def test_stickers_only_without_tracers():
         exact(h.get_cells()[frozen], cells[frozen])
 
 
+MIXED_L1 = 1e-5  # relative L1 of the FP32-mixed path against FP64, per column
+
+
+def rel_l1(a, b):
+    return float(np.abs(a - b).sum() / max(np.abs(b).sum(), 1e-300))
+
+
+@pytest.mark.parametrize("boundary,order,problems", [("rigid", 2, 1), ("periodic", 2, 1), ("rigid", 1, 1),
+                                                    ("rigid", 2, 2)])
+def test_fp32_mixed_tracers_against_fp64(boundary, order, problems):
+    """Tracers and stickers on the FP32-mixed path: its FP32 hydro passes
+    keep each cell's shock decision and each face's mass flux, honour the
+    skip_key and SkipUpdate stickers, and the FP64 tracer passes run on
+    them.  12 fused steps of the 160^2 case (five tracers, the entropy
+    tracer, 5% frozen and 8% limiter-skipped cells) against the FP64 path:
+    density and every tracer column within 1e-5 relative L1, the frozen
+    cells' states unchanged, the dt sequence within FP32 rounding.  With
+    two problems the mesh is split in a batch (per-problem dt)."""
+    mesh, cells, tr, stickers = big_case(160, boundary)
+    gamma, steps = 5 / 3, 12
+    ghost = 1 if boundary == "periodic" else 0
+    offsets = None
+    if problems > 1:
+        # two independent copies of the case (the second seeded differently)
+        m2, c2, t2, s2 = big_case(96, boundary, seed=5)
+        mesh, offsets = synthetic.concat_meshes([mesh, m2])
+        cells, tr, stickers = np.vstack([cells, c2]), np.vstack([tr, t2]), np.concatenate([stickers, s2])
+    outs = []
+    for precision in (0, 1):
+        with richgpu.Handle(gamma=gamma, order=order, ghost_kind=ghost, device=0, precision=precision) as h:
+            h.upload_mesh(mesh)
+            if problems > 1:
+                h.set_problems(offsets, [gamma, 1.4])
+            h.set_tracer_config(5, limited=[0, 2, 4], entropy=1, skip_sticker=3, frozen_sticker=0)
+            h.set_stickers(stickers)
+            h.set_cells(cells)
+            h.set_tracers(tr)
+            h.init_extensives()
+            h.set_edge_velocities(np.zeros((mesh.n_faces, 2)))
+            dts = h.run(steps)
+            outs.append((dts, h.get_cells(), h.get_tracers(), h.get_extensive_tracers()))
+    (d64, c64, t64, e64), (d32, c32, t32, e32) = outs
+    if problems == 1:
+        np.testing.assert_allclose(d32, d64, rtol=1e-5)
+    assert rel_l1(c32[:, 0], c64[:, 0]) <= MIXED_L1
+    for j in range(5):
+        assert rel_l1(t32[:, j], t64[:, j]) <= MIXED_L1, j
+        assert rel_l1(e32[:, j], e64[:, j]) <= MIXED_L1, j
+    frozen = (stickers & 1) == 1
+    exact(c32[frozen], cells[frozen].astype(np.float32).astype(np.float64))
+
+
 def test_unsupported_combinations_and_readiness():
     mesh, cells, tr, _ = big_case(16, "rigid", seed=1)
     with richgpu.Handle(gamma=5 / 3, order=2, ghost_kind=0, device=0, precision=1) as h:
+        h.set_tracer_config(2)                           # FP32-mixed hdsim::TimeAdvance carries tracers
+    with richgpu.Handle(gamma=5 / 3, order=2, ghost_kind=0, device=0, precision=1, time_integrator=1) as h:
         with pytest.raises(richgpu.RichError) as ei:
-            h.set_tracer_config(2)
+            h.set_tracer_config(2)                       # not the FP32-mixed fused TimeAdvance2Heun
         assert ei.value.status == 1
     with richgpu.Handle(gamma=5 / 3, order=2, ghost_kind=0, device=0, time_integrator=1) as h:
         h.set_tracer_config(0, frozen_sticker=0)          # TimeAdvance2Heun carries tracers and stickers
