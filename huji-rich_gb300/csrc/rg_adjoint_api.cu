@@ -327,9 +327,11 @@ rg_status rg_step_bwd(rg_handle* h, const double* cells_bar, double* cells0_bar)
       RG_CUDA(h, rg::launch_slopes32_trace(mx, ptr<double>(A->seg_slopes, 8 * n * J),
                                            ptr<rg::SlopeTrace>(A->seg_trace, n * J), h->stream));
       if (j + 1 < len) {
+        // the rest of the step: the trace kernel has left the FP32 slopes
         rg::MixedArgs mj = mx;
         mj.step = std::min(start + j, 0x1fff);
-        RG_TRY(enqueue_mixed_step(h, mj));
+        RG_CUDA(h, rg::launch_faces32(mj, h->stream, true));
+        RG_CUDA(h, rg::launch_update_mixed(mj, h->stream, false, true, true));
       }
     }
     for (int j = len - 1; j >= 0; --j) {

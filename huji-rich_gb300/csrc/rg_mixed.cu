@@ -250,7 +250,8 @@ __device__ __forceinline__ void shocked32(float dphi, float cv, float cellv, flo
 }
 
 // The FP32 slopes of a periodic mesh (no self-mirror neighbour, no boundary
-// slope) with the limiter trace the adjoint's reverse slope kernel reads
+// slope), written widened and as the FP32 slopes the face kernel reads, with
+// the limiter trace the adjoint's reverse slope kernel reads
 // (SlopeTrace: the unlimited slope, each component's factor, the centroid
 // difference and neighbour of its active candidate).  The arithmetic is
 // k_slopes32_item's; the arg max / min follow the first strict improvement
@@ -354,6 +355,9 @@ __global__ void __launch_bounds__(kBlock) k_slopes32_trace(MixedArgs a, double* 
   o[1] = make_double2(sx[2], sx[3]);
   o[2] = make_double2(sy[0], sy[1]);
   o[3] = make_double2(sy[2], sy[3]);
+  // the same slopes for the face kernel of the recomputed step
+  a.slopes32[2 * i] = make_float4(sx[0], sx[1], sx[2], sx[3]);
+  a.slopes32[2 * i + 1] = make_float4(sy[0], sy[1], sy[2], sy[3]);
 }
 
 // LinearGaussImproved::calc_slope (LinearGaussImproved.cpp:425-494) in FP32.
