@@ -415,8 +415,11 @@ __device__ __forceinline__ void k_slopes_item(const StepArgs& a, int i) {
   o[3] = make_double2(sy.vx, sy.vy);
 }
 
-template <bool kBatch>
-__global__ void __launch_bounds__(kMaxBlock) k_slopes(StepArgs a) {
+// kMinBlocks > 0: register-capped builds for blocks of up to kCappedBlock
+// threads with kMinBlocks resident per SM (launch-shape variants 2 and 3)
+template <bool kBatch, int kMinBlocks = 0>
+__global__ void __launch_bounds__(kMinBlocks ? kCappedBlock : kMaxBlock, kMinBlocks ? kMinBlocks : 1)
+    k_slopes(StepArgs a) {
   // the dt of this step, computed by the previous step's update (the face
   // kernel, launched after this one, reads status->dt)
   if (a.take_next_dt && blockIdx.x == 0 && threadIdx.x == 0) a.status->dt = a.status->dt_next;
@@ -1001,10 +1004,16 @@ cudaError_t launch_ghost_fill(const StepArgs& a, cudaStream_t s) {
 
 cudaError_t launch_slopes(const StepArgs& a, cudaStream_t s) {
   if (a.mesh.n > 0) {
-    if (a.cell_problem)
-      k_slopes<true><<<grid_of(a.shapes.slopes, a.mesh.n), a.shapes.slopes.block, 0, s>>>(a);
-    else
-      k_slopes<false><<<grid_of(a.shapes.slopes, a.mesh.n), a.shapes.slopes.block, 0, s>>>(a);
+    const LaunchShape& sh = a.shapes.slopes;
+    const int nb = grid_of(sh, a.mesh.n), bs = sh.block;
+    const bool b = a.cell_problem != nullptr;
+    // builds: 0 plain, 2 and 3 register-capped for 3 and 4 resident blocks of
+    // up to 256 threads
+    switch (sh.variant) {
+      case 2: b ? k_slopes<true, 3><<<nb, bs, 0, s>>>(a) : k_slopes<false, 3><<<nb, bs, 0, s>>>(a); break;
+      case 3: b ? k_slopes<true, 4><<<nb, bs, 0, s>>>(a) : k_slopes<false, 4><<<nb, bs, 0, s>>>(a); break;
+      default: b ? k_slopes<true><<<nb, bs, 0, s>>>(a) : k_slopes<false><<<nb, bs, 0, s>>>(a);
+    }
   }
   return cudaGetLastError();
 }

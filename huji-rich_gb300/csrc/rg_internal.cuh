@@ -186,7 +186,9 @@ constexpr int kMaxBlock = 512;
 // with 5 or 6 blocks resident per SM (more warps in flight against fewer
 // registers per thread), and 4, which loads the neighbour words, stencil
 // records and states of cells with up to 8 neighbours before any arithmetic;
-// the FP32-mixed update kernel has register-capped builds 2 and 3 too.
+// the FP32-mixed update kernel has register-capped builds 2 and 3 too, and the
+// FP64 slopes kernel register-capped builds 2 and 3 for 3 and 4 resident
+// blocks.
 struct LaunchShape {
   int block;
   int max_blocks;

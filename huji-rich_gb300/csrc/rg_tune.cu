@@ -80,9 +80,10 @@ rg_status launch_one(rg_handle* h, int k, const rg::LaunchShape& sh, void* ext_s
   return RG_OK;
 }
 
-// mixed slopes: builds 0-4; mixed update: 0, (1 = 0), 2, 3 (register-capped)
+// mixed slopes: builds 0-4; mixed update: 0, (1 = 0), 2, 3 (register-capped);
+// FP64 slopes: 0, (1 = 0), 2, 3 (register-capped)
 int n_variants(const rg_handle* h, int k) {
-  if (!h->mixed) return 1;
+  if (!h->mixed) return k == RG_KERNEL_SLOPES ? 4 : 1;
   return k == RG_KERNEL_SLOPES ? 5 : (k == RG_KERNEL_UPDATE ? 4 : 1);
 }
 bool capped(int k, int v) { return (k == RG_KERNEL_SLOPES || k == RG_KERNEL_UPDATE) && (v == 2 || v == 3); }

@@ -312,7 +312,9 @@ typedef struct {
   int32_t variant[4]; /* build: 0; the FP32-mixed slopes kernel also has 1 (loops unrolled
                          by two), 2, 3 (register-capped: blocks of at most 256 threads,
                          5 or 6 resident per SM) and 4 (up to 8 neighbours loaded up front);
-                         the FP32-mixed update kernel 2 and 3 (register-capped) */
+                         the FP32-mixed update kernel 2 and 3 (register-capped); the
+                         FP64 slopes kernel 2 and 3 (register-capped: blocks of at most
+                         256 threads, 3 or 4 resident per SM) */
   float ms[4];        /* rg_autotune: mean time per launch of the chosen shape (ms) */
 } rg_launch_shapes;
 /* Times every candidate shape of each per-step kernel on the uploaded mesh
