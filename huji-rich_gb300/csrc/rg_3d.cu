@@ -31,7 +31,7 @@ struct V3 {
 __device__ __forceinline__ double vabs(V3 v) { return sqrt(v.x * v.x + v.y * v.y + v.z * v.z); }
 __device__ __forceinline__ double vdot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 __device__ __forceinline__ V3 vscale(double d, V3 v) { return V3{v.x * d, v.y * d, v.z * d}; }
-__device__ __forceinline__ V3 vdiv(V3 v, double d) { return V3{v.x / d, v.y / d, v.z / d}; }
+__device__ __forceinline__ V3 vdiv(V3 v, double d) { return V3{quot(v.x, d), quot(v.y, d), quot(v.z, d)}; }
 __device__ __forceinline__ V3 vsub(V3 a, V3 b) { return V3{a.x - b.x, a.y - b.y, a.z - b.z}; }
 __device__ __forceinline__ V3 vadd(V3 a, V3 b) { return V3{a.x + b.x, a.y + b.y, a.z + b.z}; }
 
@@ -51,8 +51,8 @@ __device__ __forceinline__ void store6(double* out, int i, double a, double b, d
   r[2] = make_double2(e, 0.0);
 }
 
-__device__ __forceinline__ double dp2e(double g, double d, double p) { return p / d / (g - 1); }
-__device__ __forceinline__ double dp2c(double g, double d, double p) { return sqrt(g * p / d); }
+__device__ __forceinline__ double dp2e(double g, double d, double p) { return quot(quot(p, d), g - 1); }
+__device__ __forceinline__ double dp2c(double g, double d, double p) { return sqrt(quot(g * p, d)); }
 
 // FirstOrderHydroFlux.cpp:32-40 calc_primitive: (d, p, (v.n, |v - (v.n)n|), e, c)
 __device__ __forceinline__ Prim prim3(double g, const Cell3& c, V3 n) {
@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(kBlock) k3_cfl(Step3Args a) {
   unsigned long long bits = kInfBits;
   if (i < a.mesh.n) {
     const Cell3 c = load_cell3(a.cells, i);
-    const double b = a.mesh.width[i] / (vabs(c.v) + dp2c(a.gamma, c.d, c.p));
+    const double b = quot(a.mesh.width[i], vabs(c.v) + dp2c(a.gamma, c.d, c.p));
     bits = static_cast<unsigned long long>(__double_as_longlong(b));
   }
   grid_min_times(a.status, bits, a.cfl, &a.status->dt);
@@ -200,10 +200,10 @@ __global__ void __launch_bounds__(kBlock) k3_update(Step3Args a, int from_unscal
   }
   if (do_cells) {
     const double V = m.volume[i];
-    const double density = u[0] / V;
-    const V3 vel = vdiv(V3{u[1] / V, u[2] / V, u[3] / V}, density);
-    const double thermal = u[4] / V - 0.5 * density * vdot(vel, vel);
-    const double eint = thermal / density;
+    const double density = quot(u[0], V);
+    const V3 vel = vdiv(V3{quot(u[1], V), quot(u[2], V), quot(u[3], V)}, density);
+    const double thermal = quot(u[4], V) - 0.5 * density * vdot(vel, vel);
+    const double eint = quot(thermal, density);
     if (eint < 0) {
       record_error(a.status, a.step, RG_ERR_NEGATIVE_ENERGY, 5, i, eint);
       return;

@@ -215,7 +215,7 @@ RG_DIV_FN bool div_rn_fast(double a, double b, const Seed& seed, double* q) {
 #if defined(__CUDACC__)
 // The IEEE division for the operands outside the fast path, kept out of line
 // so that the compiler cannot compute it ahead of the branch.
-__device__ __noinline__ double div_ieee(double a, double b) { return a / b; }
+static __device__ __noinline__ double div_ieee(double a, double b) { return a / b; }
 
 // a / b, bitwise (the fast path above, a / b outside it)
 __device__ __forceinline__ double div_rn(double a, double b) {
@@ -223,6 +223,10 @@ __device__ __forceinline__ double div_rn(double a, double b) {
   if (div_rn_fast(a, b, RcpSeedDevice{}, &q)) return q;
   return div_ieee(a, b);
 }
+
+// a / b of the kernels' real type: div_rn for double, the FP32 division for float
+__device__ __forceinline__ double quot(double a, double b) { return div_rn(a, b); }
+__device__ __forceinline__ float quot(float a, float b) { return a / b; }
 #endif
 
 }  // namespace rg

@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(kBlock) k_geom_faces(GeomArgs a) {
     }
     const double sp = w.x * p.x + w.y * p.y;
     const double pp = p.x * p.x + p.y * p.y;
-    n = make_double2(w.x - (p.x * sp) / pp, w.y - (p.y * sp) / pp);
+    n = make_double2(w.x - quot(p.x * sp, pp), w.y - quot(p.y * sp, pp));
   }
   a.nrm[e] = n;
   a.nabs[e] = sqrt(n.x * n.x + n.y * n.y);
@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(kBlock) k_geom_faces(GeomArgs a) {
   const double dab = sqrt(ddx * ddx + ddy * ddy);
   a.dab[e] = dab;
   const double len = a.area[e];  // Edge::GetLength = |second - first| = |first - second|
-  a.rij[e] = make_double2((ddx / dab) * len, (ddy / dab) * len);
+  a.rij[e] = make_double2(quot(ddx, dab) * len, quot(ddy, dab) * len);
   a.cij[e] = make_double2(mid.x - (c1.x + c0.x) * 0.5, mid.y - (c1.y + c0.y) * 0.5);
 }
 
@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(kBlock) k_geom_cells(GeomArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const MeshDev& m = a.mesh;
   if (i >= m.n) return;
-  a.width[i] = sqrt(m.volume[i] / kPi);
+  a.width[i] = sqrt(quot(m.volume[i], kPi));
   const int b = m.cell_off[i], nn = m.cell_off[i + 1] - b;
   bool bslope = false;
   for (int k = 0; k < nn; ++k) {
@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(kBlock) k_geom_cells(GeomArgs a) {
   m3 += vol;
   const double det = m0 * m3 - m1 * m2;
   if (fabs(det) < 1e-10 * vol * vol) record_error(a.status, 0, RG_ERR_SINGULAR_MATRIX, 2, i, det);
-  const double di = 1.0 / det;
+  const double di = quot(1.0, det);
   a.minv[i] = make_dbl4(m3 * di, -m1 * di, -m2 * di, m0 * di);
 }
 
@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(kBlock) k_geom_ghosts(GeomArgs a) {
   const double2 nr = ghost_first ? make_double2(x0.x - x1.x, x0.y - x1.y)
                                  : make_double2(x1.x - x0.x, x1.y - x0.y);
   const double ab = sqrt(nr.x * nr.x + nr.y * nr.y);
-  a.ghost_unit[g] = make_double2(nr.x / ab, nr.y / ab);
+  a.ghost_unit[g] = make_double2(quot(nr.x, ab), quot(nr.y, ab));
 }
 
 // Index validation of an uploaded mesh, before any kernel indexes with it.
@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_cfl(StepArgs a, int fill_ghosts) 
     if (t < m.n) {
       const Cell c = load_cell(a.cells, t);
       const double radius = a.geom.width[t];
-      const double cs = sqrt(gamma_at<kBatch>(a, t) * c.p / c.d);
+      const double cs = sqrt(quot(gamma_at<kBatch>(a, t) * c.p, c.d));
       // fmax over faces of (cs + sqrt(q_e)) / radius equals (cs + sqrt(max q_e)) /
       // radius exactly: sqrt, + and / are correctly rounded, hence monotone, so
       // the maximum commutes with them.  NaN terms are skipped as fmax skips them.
@@ -245,8 +245,8 @@ __global__ void __launch_bounds__(kMaxBlock) k_cfl(StepArgs a, int fill_ghosts) 
           }
         }
       }
-      const double res = any ? fmax(0.0, (cs + sqrt(q)) / radius) : 0.0;
-      x = 1.0 / res;
+      const double res = any ? fmax(0.0, quot(cs + sqrt(q), radius)) : 0.0;
+      x = quot(1.0, res);
     } else if (t < total) {
       fill_ghost(a, t - m.n);
     }
@@ -291,10 +291,10 @@ __device__ __forceinline__ void k_slopes_item(const StepArgs& a, int i) {
       phisx.vy = phisx.vy + df.vy * h.x;
     }
     const double sxsy = mi.x, sx2 = mi.y, sy2 = mi.z, den = mi.w;
-    sx = Cell{(phisy.d * sxsy - phisx.d * sy2) / den, (phisy.p * sxsy - phisx.p * sy2) / den,
-              (phisy.vx * sxsy - phisx.vx * sy2) / den, (phisy.vy * sxsy - phisx.vy * sy2) / den};
-    sy = Cell{(phisx.d * sxsy - phisy.d * sx2) / den, (phisx.p * sxsy - phisy.p * sx2) / den,
-              (phisx.vx * sxsy - phisy.vx * sx2) / den, (phisx.vy * sxsy - phisy.vy * sx2) / den};
+    sx = Cell{quot(phisy.d * sxsy - phisx.d * sy2, den), quot(phisy.p * sxsy - phisx.p * sy2, den),
+              quot(phisy.vx * sxsy - phisx.vx * sy2, den), quot(phisy.vy * sxsy - phisx.vy * sy2, den)};
+    sy = Cell{quot(phisx.d * sxsy - phisy.d * sx2, den), quot(phisx.p * sxsy - phisy.p * sx2, den),
+              quot(phisx.vx * sxsy - phisy.vx * sx2, den), quot(phisx.vy * sxsy - phisy.vy * sx2, den)};
   } else {
     // :80-133 calc_naive_slope, right-hand side and solve
     Cell vx{0, 0, 0, 0}, vy{0, 0, 0, 0};
@@ -335,7 +335,7 @@ __device__ __forceinline__ void k_slopes_item(const StepArgs& a, int i) {
           decided = true;
         }
       }
-      if (!decided) shock = lhs < (-a.delta_v) * sqrt(gp / cell.d);
+      if (!decided) shock = lhs < (-a.delta_v) * sqrt(quot(gp, cell.d));
     }
     if (!shock && nn == 0) shock = 1.0 < a.delta_p;  // PressureRatio of no neighbours is 1
     if (!shock) {
@@ -353,7 +353,7 @@ __device__ __forceinline__ void k_slopes_item(const StepArgs& a, int i) {
           }
           if (rf > dp_f * 1.000001f) continue;
         }
-        shock = num / den < a.delta_p;
+        shock = quot(num, den) < a.delta_p;
       }
     }
     if (a.shock) a.shock[i] = shock ? 1 : 0;
@@ -431,14 +431,14 @@ __global__ void __launch_bounds__(kMinBlocks ? kCappedBlock : kMaxBlock, kMinBlo
 
 // simple_flux_calculator.cpp:9-15 convert_to_primitive (ideal_gas.cpp:13-16, 40-44)
 __device__ __forceinline__ Prim to_prim(double g, const Cell& c) {
-  return Prim{c.d, c.p, c.vx, c.vy, c.p / c.d / (g - 1), sqrt(g * c.p / c.d)};
+  return Prim{c.d, c.p, c.vx, c.vy, quot(quot(c.p, c.d), g - 1), sqrt(quot(g * c.p, c.d))};
 }
 
 // simple_flux_calculator.cpp:130-165 rotate / Hllc / rotate_back
 __device__ __forceinline__ bool solve_face(Prim l, Prim r, double velocity, double2 n, double na, double2 p,
                                            double pa, Cons& out, const StepArgs& a, int face) {
-  const double lx = (l.vx * n.x + l.vy * n.y) / na, ly = (l.vx * p.x + l.vy * p.y) / pa;
-  const double rx = (r.vx * n.x + r.vy * n.y) / na, ry = (r.vx * p.x + r.vy * p.y) / pa;
+  const double lx = quot(l.vx * n.x + l.vy * n.y, na), ly = quot(l.vx * p.x + l.vy * p.y, pa);
+  const double rx = quot(r.vx * n.x + r.vy * n.y, na), ry = quot(r.vx * p.x + r.vy * p.y, pa);
   l.vx = lx;
   l.vy = ly;
   r.vx = rx;
@@ -446,8 +446,8 @@ __device__ __forceinline__ bool solve_face(Prim l, Prim r, double velocity, doub
   Cons c;
   if (!hllc(l, r, velocity, c, a.status, a.step, face)) return false;
   out.m = c.m;
-  out.mx = (n.x * c.mx) / na + (p.x * c.my) / pa;
-  out.my = (n.y * c.mx) / na + (p.y * c.my) / pa;
+  out.mx = quot(n.x * c.mx, na) + quot(p.x * c.my, pa);
+  out.my = quot(n.y * c.mx, na) + quot(p.y * c.my, pa);
   out.en = c.en;
   return true;
 }
@@ -456,8 +456,8 @@ __device__ __forceinline__ bool solve_face(Prim l, Prim r, double velocity, doub
 __device__ __forceinline__ bool solve_face_lagrangian(Prim l, Prim r, double velocity, bool massflux, double2 n,
                                                       double na, double2 p, double pa, Cons& out, double& energy,
                                                       const StepArgs& a, int face) {
-  const double lx = (l.vx * n.x + l.vy * n.y) / na, ly = (l.vx * p.x + l.vy * p.y) / pa;
-  const double rx = (r.vx * n.x + r.vy * n.y) / na, ry = (r.vx * p.x + r.vy * p.y) / pa;
+  const double lx = quot(l.vx * n.x + l.vy * n.y, na), ly = quot(l.vx * p.x + l.vy * p.y, pa);
+  const double rx = quot(r.vx * n.x + r.vy * n.y, na), ry = quot(r.vx * p.x + r.vy * p.y, pa);
   l.vx = lx;
   l.vy = ly;
   r.vx = rx;
@@ -465,8 +465,8 @@ __device__ __forceinline__ bool solve_face_lagrangian(Prim l, Prim r, double vel
   Cons c;
   if (!lagrangian_hllc(l, r, velocity, massflux, c, energy, a.status, a.step, face)) return false;
   out.m = c.m;
-  out.mx = (n.x * c.mx) / na + (p.x * c.my) / pa;
-  out.my = (n.y * c.mx) / na + (p.y * c.my) / pa;
+  out.mx = quot(n.x * c.mx, na) + quot(p.x * c.my, pa);
+  out.my = quot(n.y * c.mx, na) + quot(p.y * c.my, pa);
   out.en = c.en;
   return true;
 }
@@ -518,7 +518,7 @@ __device__ __forceinline__ void k_faces_lgi_item(const StepArgs& a, int e) {
   const double2 n = a.geom.nrm[e], p = a.geom.par[e];
   const double na = a.geom.nabs[e], pa = a.geom.area[e];
   // a face at rest has speed +-0 (the sign only reaches signs of zeros)
-  const double speed = (w.x == 0.0 && w.y == 0.0) ? 0.0 : (n.x * w.x + n.y * w.y) / na;
+  const double speed = (w.x == 0.0 && w.y == 0.0) ? 0.0 : quot(n.x * w.x + n.y * w.y, na);
   const int real_side = fc.x < m.n ? fc.x : fc.y;
   const double g = gamma_at<kBatch>(a, real_side);
   Cons c;
@@ -538,7 +538,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_faces_lgi(StepArgs a) {
 __device__ __forceinline__ Prim reflect(Prim q, double2 axis, double aa) {
   const double s = 2 * (q.vx * axis.x + q.vy * axis.y);
   const double pp = aa * aa;
-  const double tx = (axis.x * s) / pp, ty = (axis.y * s) / pp;
+  const double tx = quot(axis.x * s, pp), ty = quot(axis.y * s, pp);
   q.vx = tx - q.vx;
   q.vy = ty - q.vy;
   return q;
@@ -569,7 +569,7 @@ __device__ __forceinline__ void k_faces_pcm_item(const StepArgs& a, int e) {
     r = to_prim(g, load_cell(a.cells, fc.y));
   }
   const double2 w = a.ev_zero ? make_double2(0.0, 0.0) : reinterpret_cast<const double2*>(a.ev)[e];
-  const double velocity = (w.x == 0.0 && w.y == 0.0) ? 0.0 : (n.x * w.x + n.y * w.y) / na;
+  const double velocity = (w.x == 0.0 && w.y == 0.0) ? 0.0 : quot(n.x * w.x + n.y * w.y, na);
   Cons c;
   if (!solve_face(l, r, velocity, n, na, p, pa, c, a, e)) return;
   if (a.mflux) a.mflux[e] = c.m;
@@ -587,12 +587,12 @@ __global__ void __launch_bounds__(kMaxBlock) k_faces_pcm(StepArgs a) {
 // geometry.cpp normalize: v/abs(v)
 __device__ __forceinline__ double2 normalize2(double x, double y) {
   const double ab = sqrt(x * x + y * y);
-  return make_double2(x / ab, y / ab);
+  return make_double2(quot(x, ab), quot(y, ab));
 }
 // simple_flux_calculator.cpp:27-31 remove_parallel_component, then normalize
 __device__ __forceinline__ double2 wall_normal(double wx, double wy, double2 p) {
   const double s = wx * p.x + wy * p.y, pp = p.x * p.x + p.y * p.y;
-  return normalize2(wx - (p.x * s) / pp, wy - (p.y * s) / pp);
+  return normalize2(wx - quot(p.x * s, pp), wy - quot(p.y * s, pp));
 }
 __device__ __forceinline__ bool has_sticker(const StepArgs& a, int p, int bit) {
   return a.stickers != nullptr && ((a.stickers[orig_of(a.mesh, p)] >> bit) & 1u) != 0;
@@ -691,7 +691,7 @@ __device__ __forceinline__ void k_faces_cas_item(const StepArgs& a, int e) {
     const double2 w = a.ev_zero ? make_double2(0.0, 0.0) : reinterpret_cast<const double2*>(a.ev)[e];
     const double2 nn = a.geom.nrm[e], pp = a.geom.par[e];
     const double na = a.geom.nabs[e], ppa = a.geom.area[e];
-    const double speed = (w.x == 0.0 && w.y == 0.0) ? 0.0 : (nn.x * w.x + nn.y * w.y) / na;
+    const double speed = (w.x == 0.0 && w.y == 0.0) ? 0.0 : quot(nn.x * w.x + nn.y * w.y, na);
     const bool lag = orig_of(m, fc.x) != orig_of(m, fc.y);
     const bool mf = (((lag ? a.rules[chosen][5] : a.rules[chosen][5] >> 1)) & 1) != 0;
     Cons c;
@@ -753,7 +753,7 @@ template <bool kBatch>
 __device__ __forceinline__ unsigned long long cfl_bound_bits(const StepArgs& a, int i, double d, double pres,
                                                              double vx, double vy) {
   const MeshDev& m = a.mesh;
-  const double cs = sqrt(gamma_at<kBatch>(a, i) * pres / d);
+  const double cs = sqrt(quot(gamma_at<kBatch>(a, i) * pres, d));
   double q = 0;
   bool any = false;
   if (a.ev_zero) {
@@ -773,8 +773,8 @@ __device__ __forceinline__ unsigned long long cfl_bound_bits(const StepArgs& a, 
       }
     }
   }
-  const double res = any ? fmax(0.0, (cs + sqrt(q)) / a.geom.width[i]) : 0.0;
-  return static_cast<unsigned long long>(__double_as_longlong(1.0 / res));
+  const double res = any ? fmax(0.0, quot(cs + sqrt(q), a.geom.width[i])) : 0.0;
+  return static_cast<unsigned long long>(__double_as_longlong(quot(1.0, res)));
 }
 
 // SimpleExtensiveUpdater (simple_extensive_updater.cpp:11-35) as a gather:
@@ -833,7 +833,7 @@ __device__ __forceinline__ unsigned long long k_update_item(const StepArgs& a, i
         }
       }
       const double vol = m.cd_volume[i];
-      const double f = (vol + dv) / (vol + dv + dvw);
+      const double f = quot(vol + dv, vol + dv + dvw);
       mass *= f;
       en *= f;
       px *= f;
@@ -861,13 +861,13 @@ __device__ __forceinline__ unsigned long long k_update_item(const StepArgs& a, i
       if (!a.cfl_next) return kInfBits;
       return cfl_bound_bits<kBatch>(a, i, c.d, c.p, c.vx, c.vy);
     }
-    const double d = mass / m.cd_volume[i];
+    const double d = quot(mass, m.cd_volume[i]);
     if (d < 0) {
       record_error(a.status, a.step, RG_ERR_NEGATIVE_DENSITY, 5, i, d);
       return kInfBits;
     }
-    const double vx = px / mass, vy = py / mass;
-    const double energy = en / mass - 0.5 * (vx * vx + vy * vy);
+    const double vx = quot(px, mass), vy = quot(py, mass);
+    const double energy = quot(en, mass) - 0.5 * (vx * vx + vy * vy);
     if (energy < 0) {
       record_error(a.status, a.step, RG_ERR_NEGATIVE_ENERGY, 5, i, energy);
       return kInfBits;
@@ -908,7 +908,7 @@ __global__ void __launch_bounds__(kBlock) k_init_ext(StepArgs a) {
   if (i >= a.mesh.n) return;
   const Cell c = load_cell(a.cells, i);
   const double mass = a.mesh.cd_volume[i] * c.d;
-  store4(a.ext, i, mass, c.p / c.d / (gamma_at<kBatch>(a, i) - 1) * mass + 0.5 * mass * (c.vx * c.vx + c.vy * c.vy),
+  store4(a.ext, i, mass, quot(quot(c.p, c.d), gamma_at<kBatch>(a, i) - 1) * mass + 0.5 * mass * (c.vx * c.vx + c.vy * c.vy),
          c.vx * mass, c.vy * mass);
 }
 

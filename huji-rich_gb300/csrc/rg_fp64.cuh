@@ -6,6 +6,7 @@
 #pragma once
 #include <math.h>
 
+#include "rg_div.cuh"
 #include "rg_internal.cuh"
 
 namespace rg {
@@ -105,7 +106,7 @@ __device__ __forceinline__ void min_quotient(double num, double den, double& psi
     const float qf = narrow(num) / narrow(den);
     if (qf >= psi_f * 1.000001f) return;
   }
-  const double q = num / den;
+  const double q = quot(num, den);
   if (q < psi) {
     psi = q;
     psi_f = narrow(q);
@@ -147,7 +148,7 @@ __device__ __forceinline__ void shocked_comp(double dphi, double cv, double cell
         const float qf = narrow(num) / narrow(dphi);
         if (qf >= psi_f * 1.000001f) return;
       }
-      const double x = smax(num / dphi, 0.0);
+      const double x = smax(quot(num, dphi), 0.0);
       if (x < psi) {
         psi = x;
         psi_f = narrow(x);

@@ -2,8 +2,10 @@
 // templated on the real type: double for the plain path, shared by the 2D
 // kernels (rg_fp64.cu) and the 3D first-order kernels (rg_3d.cu), both
 // compiled with --fmad=false so every operation rounds as the reference's;
-// float for the FP32-mixed 3D kernels (rg_3d_mixed.cu).
+// float for the FP32-mixed 3D kernels (rg_3d_mixed.cu).  FP64 quotients are
+// formed by rg::div_rn (rg_div.cuh: the same bits as the IEEE division).
 #pragma once
+#include "rg_div.cuh"
 #include "rg_internal.cuh"
 
 namespace rg {
@@ -48,8 +50,8 @@ __device__ __forceinline__ bool hllc(PrimT<R> l, PrimT<R> r, R velocity, ConsT<R
   const R a1 = l.vx - l.c, b1 = r.vx - r.c, a2 = l.vx + l.c, b2 = r.vx + r.c;
   const R sl = b1 < a1 ? b1 : a1;  // std::min
   const R sr = a2 < b2 ? b2 : a2;  // std::max
-  const R ss = (r.p - l.p + l.d * l.vx * (sl - l.vx) - r.d * r.vx * (sr - r.vx)) /
-                    (l.d * (sl - l.vx) - r.d * (sr - r.vx));
+  const R ss = quot(r.p - l.p + l.d * l.vx * (sl - l.vx) - r.d * r.vx * (sr - r.vx),
+                    l.d * (sl - l.vx) - r.d * (sr - r.vx));
   const bool use_left = sl > R(0) || (sl <= R(0) && ss >= R(0));
   const bool use_right = !use_left && ((ss < R(0) && sr >= R(0)) || sr < R(0));
   if (!use_left && !use_right) {
@@ -67,9 +69,9 @@ __device__ __forceinline__ bool hllc(PrimT<R> l, PrimT<R> r, R velocity, ConsT<R
   const bool star = use_left ? !(sl > R(0)) : !(sr < R(0));
   if (star) {
     // :76-92 starred_state, and fk + sk*(us - u) with u = Primitive2Conserved (:267-272)
-    const R ds = q.d * (sk - q.vx) / (sk - ss);
+    const R ds = quot(q.d * (sk - q.vx), sk - ss);
     const R usm = ds, usx = ds * ss, usy = ds * q.vy;
-    const R use = e_k * ds / q.d + ds * (ss - q.vx) * (ss + q.p / q.d / (sk - q.vx));
+    const R use = quot(e_k * ds, q.d) + ds * (ss - q.vx) * (ss + quot(quot(q.p, q.d), sk - q.vx));
     fk.m = fk.m + sk * (usm - q.d);
     fk.mx = fk.mx + (usx - q.vx * q.d) * sk;
     fk.my = fk.my + (usy - q.vy * q.d) * sk;
@@ -104,8 +106,8 @@ __device__ __forceinline__ bool lagrangian_hllc(Prim l, Prim r, double velocity,
   if (!massflux) {
     const double a1 = l.vx - l.c, b1 = r.vx - r.c, a2 = l.vx + l.c, b2 = r.vx + r.c;
     const double sl2 = b1 < a1 ? b1 : a1, sr2 = a2 < b2 ? b2 : a2;
-    const double ss2 = (r.p - l.p + l.d * l.vx * (sl2 - l.vx) - r.d * r.vx * (sr2 - r.vx)) /
-                       (l.d * (sl2 - l.vx) - r.d * (sr2 - r.vx));
+    const double ss2 = quot(r.p - l.p + l.d * l.vx * (sl2 - l.vx) - r.d * r.vx * (sr2 - r.vx),
+                            l.d * (sl2 - l.vx) - r.d * (sr2 - r.vx));
     l.vx -= ss2;
     r.vx -= ss2;
     velocity += ss2;
@@ -114,8 +116,8 @@ __device__ __forceinline__ bool lagrangian_hllc(Prim l, Prim r, double velocity,
   const double a1 = l.vx - l.c, b1 = r.vx - r.c, a2 = l.vx + l.c, b2 = r.vx + r.c;
   const double sl = b1 < a1 ? b1 : a1;
   const double sr = a2 < b2 ? b2 : a2;
-  const double ss = (r.p - l.p + l.d * l.vx * (sl - l.vx) - r.d * r.vx * (sr - r.vx)) /
-                    (l.d * (sl - l.vx) - r.d * (sr - r.vx));
+  const double ss = quot(r.p - l.p + l.d * l.vx * (sl - l.vx) - r.d * r.vx * (sr - r.vx),
+                         l.d * (sl - l.vx) - r.d * (sr - r.vx));
   const bool use_left = sl > 0.0 || (sl <= 0.0 && ss >= 0.0);
   const bool use_right = !use_left && ((ss < 0.0 && sr >= 0.0) || sr < 0.0);
   if (!use_left && !use_right) {
@@ -131,15 +133,15 @@ __device__ __forceinline__ bool lagrangian_hllc(Prim l, Prim r, double velocity,
   // ScalarProd(local.Velocity, (1,0))
   const double sp = q.vx * 1.0 + q.vy * 0.0;
   if (star) {
-    const double ds = q.d * (sk - q.vx) / (sk - ss);
+    const double ds = quot(q.d * (sk - q.vx), sk - ss);
     const double usm = ds, usx = ds * ss, usy = ds * q.vy;
-    const double use = e_k * ds / q.d + ds * (ss - q.vx) * (ss + q.p / q.d / (sk - q.vx));
+    const double use = quot(e_k * ds, q.d) + ds * (ss - q.vx) * (ss + quot(quot(q.p, q.d), sk - q.vx));
     fk.m = fk.m + sk * (usm - q.d);
     fk.mx = fk.mx + (usx - q.vx * q.d) * sk;
     fk.my = fk.my + (usy - q.vy * q.d) * sk;
     fk.en = fk.en + sk * (use - e_k);
     if (massflux) {
-      const double frac = (sk - q.vx) / (sk - ss) - 1.0;
+      const double frac = quot(sk - q.vx, sk - ss) - 1.0;
       en = use_left ? sp * q.e * q.d + sk * q.e * frac * q.d : (sp * q.e + sk * q.e * frac) * q.d;
     }
   } else if (massflux) {

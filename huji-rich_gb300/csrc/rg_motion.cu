@@ -19,6 +19,7 @@
 #include <math.h>
 
 #include "rg_convert.cuh"
+#include "rg_div.cuh"
 #include "rg_motion.cuh"
 
 namespace rg {
@@ -57,7 +58,7 @@ __global__ void __launch_bounds__(kMoBlock) k_dev_geometry(MeshDev m, double2* c
     pc.y += ((an.y + v.y) + v.w) * s;
   }
   volume[i] = area;
-  cms[i] = make_double2(pc.x / a2, pc.y / a2);
+  cms[i] = make_double2(quot(pc.x, a2), quot(pc.y, a2));
   cd_volume[i] = a2;
 }
 
@@ -93,7 +94,7 @@ struct CylAxis {
 __device__ __forceinline__ CylAxis cyl_axis(dbl4 od, bool unit) {
   if (unit) return CylAxis{od.x, od.y, od.z, od.w};
   const double ab = vabs2(od.z, od.w);
-  return CylAxis{od.x, od.y, od.z / ab, od.w / ab};
+  return CylAxis{od.x, od.y, quot(od.z, ab), quot(od.w, ab)};
 }
 __device__ __forceinline__ double2 change_coordinate(double vx, double vy, const CylAxis& a) {
   const double px = vx - a.ox, py = vy - a.oy;
@@ -133,7 +134,7 @@ __global__ void __launch_bounds__(kMoBlock) k_cyl_geometry(MeshDev m, double* xa
   }
 }
 
-__device__ __forceinline__ double sound(double g, const double* c) { return sqrt(g * c[1] / c[0]); }
+__device__ __forceinline__ double sound(double g, const double* c) { return sqrt(quot(g * c[1], c[0])); }
 
 __global__ void __launch_bounds__(kMoBlock) k_point_velocities(StepArgs a, MotionArgs mo) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -149,8 +150,8 @@ __global__ void __launch_bounds__(kMoBlock) k_point_velocities(StepArgs a, Motio
     if (!(d < 0.9 * mo.eta * R)) {
       const double cs = smax(sound(a.gamma, c), vabs2(c[2], c[3]));
       const double f = mo.chi * cs;
-      w.x += ((s.x - r.x) * f) / R;
-      w.y += ((s.y - r.y) * f) / R;
+      w.x += quot((s.x - r.x) * f, R);
+      w.y += quot((s.y - r.y) * f, R);
     }
   }
   mo.pv[i] = w;
@@ -182,31 +183,31 @@ __global__ void __launch_bounds__(kMoBlock) k_apply_fix(StepArgs a, MotionArgs m
         cs = smax(cs, sound(a.gamma, cn));
         cs = smax(cs, vabs2(cn[2], cn[3]));
       }
-      const double f = mo.chi * smin(d / dt, cs);
-      v.x += ((s.x - r.x) * f) / R;
-      v.y += ((s.y - r.y) * f) / R;
+      const double f = mo.chi * smin(quot(d, dt), cs);
+      v.x += quot((s.x - r.x) * f, R);
+      v.y += quot((s.y - r.y) * f, R);
     }
   }
   if (mo.fix) {
-    const double inv_dt = 1.0 / dt;
+    const double inv_dt = quot(1.0, dt);
     const dbl4 bx = mo.box;  // left, right, down, up
     if ((v.x * dt * 2 + r.x) > bx.y) {
-      double f = 0.25 * (bx.y - r.x) * inv_dt / vabs2(v.x, v.y);
+      double f = quot(0.25 * (bx.y - r.x) * inv_dt, vabs2(v.x, v.y));
       if (R * 0.1 > (bx.y - r.x)) f *= -0.1;
       v = make_double2(v.x * f, v.y * f);
     }
     if ((v.x * dt * 2 + r.x) < bx.x) {
-      double f = 0.25 * (r.x - bx.x) * inv_dt / vabs2(v.x, v.y);
+      double f = quot(0.25 * (r.x - bx.x) * inv_dt, vabs2(v.x, v.y));
       if (R * 0.1 > (r.x - bx.x)) f *= -0.1;
       v = make_double2(v.x * f, v.y * f);
     }
     if ((v.y * dt * 2 + r.y) > bx.w) {
-      double f = 0.25 * (bx.w - r.y) * inv_dt / vabs2(v.x, v.y);
+      double f = quot(0.25 * (bx.w - r.y) * inv_dt, vabs2(v.x, v.y));
       if (R * 0.1 > (bx.w - r.y)) f *= -0.1;
       v = make_double2(v.x * f, v.y * f);
     }
     if ((v.y * dt * 2 + r.y) < bx.z) {
-      double f = 0.25 * (r.y - bx.z) * inv_dt / vabs2(v.x, v.y);
+      double f = quot(0.25 * (r.y - bx.z) * inv_dt, vabs2(v.x, v.y));
       if (R * 0.1 > (r.y - bx.z)) f *= -0.1;
       v = make_double2(v.x * f, v.y * f);
     }
@@ -232,7 +233,7 @@ __global__ void __launch_bounds__(kMoBlock) k_edge_velocities(StepArgs a, Motion
     const double ab = a.geom.dab[e];  // sqrt(dx*dx + dy*dy), per mesh upload
     const double sp = (wl.x - wr.x) * (fx - mx) + (wl.y - wr.y) * (fy - my);
     const double den = ab * ab;
-    w = make_double2((wl.x + wr.x) * 0.5 + (dx * sp) / den, (wl.y + wr.y) * 0.5 + (dy * sp) / den);
+    w = make_double2((wl.x + wr.x) * 0.5 + quot(dx * sp, den), (wl.y + wr.y) * 0.5 + quot(dy * sp, den));
   }
   mo.ev[e] = w;
 }

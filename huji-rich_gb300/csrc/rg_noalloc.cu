@@ -35,6 +35,7 @@
 #include <cstdint>
 #include <mutex>
 
+#include "rg_div.cuh"
 #include "rg_internal.cuh"
 
 namespace {
@@ -78,15 +79,15 @@ __global__ void __launch_bounds__(kBlock)
   if (i < n) {
     const double2 dp = reinterpret_cast<const double2*>(cells)[2 * i];
     const double2 uv = reinterpret_cast<const double2*>(cells)[2 * i + 1];
-    const double radius = sqrt(volume[i] / rg::kPi);
-    const double cs = sqrt(gamma * dp.y / dp.x);
+    const double radius = sqrt(rg::quot(volume[i], rg::kPi));
+    const double cs = sqrt(rg::quot(gamma * dp.y, dp.x));
     double res = 0;
     for (int k = off[i]; k < off[i + 1]; ++k) {
       const double2 w = reinterpret_cast<const double2*>(ev)[faces[k]];
       const double dx = uv.x - w.x, dy = uv.y - w.y;
-      res = fmax(res, (cs + sqrt(dx * dx + dy * dy)) / radius);
+      res = fmax(res, rg::quot(cs + sqrt(dx * dx + dy * dy), radius));
     }
-    x = 1.0 / res;
+    x = rg::quot(1.0, res);
   }
   unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(x));
   for (int o = 16; o > 0; o >>= 1) {

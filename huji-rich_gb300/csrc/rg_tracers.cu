@@ -69,8 +69,8 @@ __global__ void __launch_bounds__(kTrBlock) k_tr_slopes(StepArgs a, TracerArgs t
     const double sxsy = mi.x, sx2 = mi.y, sy2 = mi.z, den = mi.w;
 #pragma unroll
     for (int j = 0; j < kMaxTracers; ++j) {
-      sx[j] = (py[j] * sxsy - px[j] * sy2) / den;
-      sy[j] = (px[j] * sxsy - py[j] * sx2) / den;
+      sx[j] = quot(py[j] * sxsy - px[j] * sy2, den);
+      sy[j] = quot(px[j] * sxsy - py[j] * sx2, den);
     }
   } else {
     // :80-133 calc_naive_slope with the mesh's 0.5*r_ij and inverse matrix
@@ -292,7 +292,7 @@ __global__ void __launch_bounds__(kTrBlock) k_tr_update(StepArgs a, TracerArgs t
     double* tr = (t.tr_out ? t.tr_out : t.tr) + static_cast<size_t>(i) * nt;
 #pragma unroll
     for (int j = 0; j < kMaxTracers; ++j)
-      if (j < nt) tr[j] = te[j] / mass;
+      if (j < nt) tr[j] = quot(te[j], mass);
     if (t.entropy >= 0) {
       // ideal_gas.cpp:52-55 dp2s of the updated cell
       const Cell c = load_cell(a.cells_out ? a.cells_out : a.cells, i);

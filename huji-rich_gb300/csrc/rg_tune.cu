@@ -3,9 +3,10 @@
 //
 // Candidates per kernel: 64, 128, 256 or 512 threads per block, times one
 // thread per item or a persistent grid of 2, 4 or 8 blocks per SM, times the
-// kernel's builds (the FP32-mixed slopes kernel also has a build with its
-// neighbour loops unrolled by two and two register-capped builds, for blocks
-// of up to 256 threads).  Each
+// kernel's builds (the slopes kernels and the FP32-mixed update kernel also
+// have register-capped builds for blocks of up to 256 threads; the FP32-mixed
+// slopes kernel a build with its neighbour loops unrolled by two and one
+// that loads the neighbour data up front).  Each
 // candidate runs `reps` launches on the handle's stream, on the uploaded mesh
 // and the current state, each timed alone with CUDA events after a write of
 // a buffer larger than L2 (a kernel of a step finds most of its inputs in
@@ -80,19 +81,22 @@ rg_status launch_one(rg_handle* h, int k, const rg::LaunchShape& sh, void* ext_s
   return RG_OK;
 }
 
-// mixed slopes: builds 0-4; mixed update: 0, (1 = 0), 2, 3 (register-capped);
-// FP64 slopes: 0, (1 = 0), 2, 3 (register-capped)
-int n_variants(const rg_handle* h, int k) {
-  if (!h->mixed) return k == RG_KERNEL_SLOPES ? 4 : 1;
-  return k == RG_KERNEL_SLOPES ? 5 : (k == RG_KERNEL_UPDATE ? 4 : 1);
+// Builds of kernel k on the handle's path: mixed slopes 0-4; mixed update 0,
+// 2, 3 (register-capped); FP64 slopes 0, 2, 3 (register-capped); otherwise 0.
+bool has_build(const rg_handle* h, int k, int v) {
+  if (v == 0) return true;
+  if (k == RG_KERNEL_SLOPES) return h->mixed ? v >= 1 && v <= 4 : v == 2 || v == 3;
+  if (k == RG_KERNEL_UPDATE) return h->mixed && (v == 2 || v == 3);
+  return false;
 }
+constexpr int kMaxVariant = 4;
 bool capped(int k, int v) { return (k == RG_KERNEL_SLOPES || k == RG_KERNEL_UPDATE) && (v == 2 || v == 3); }
 
 rg_status check_shapes(rg_handle* h, const rg_launch_shapes* s) {
   for (int k = 0; k < 4; ++k) {
     const int b = s->block[k], v = s->variant[k];
     if (b < 32 || b > rg::kMaxBlock || b % 32 != 0 || s->max_blocks[k] < 0) return invalid(h, k, b);
-    if (v < 0 || v >= n_variants(h, k) || (capped(k, v) && b > rg::kCappedBlock)) return invalid(h, k, v);
+    if (v < 0 || !has_build(h, k, v) || (capped(k, v) && b > rg::kCappedBlock)) return invalid(h, k, v);
   }
   return RG_OK;
 }
@@ -149,10 +153,9 @@ rg_status rg_autotune(rg_handle* h, int32_t reps, rg_launch_shapes* chosen) {
   for (int k = 0; k < 4; ++k) {
     float best = 0;
     rg::LaunchShape best_shape = *slot(cur, k);
-    for (int v = 0; v < n_variants(h, k); ++v)
+    for (int v = 0; v <= kMaxVariant; ++v)
     for (int b : kBlocks) {
-      if (capped(k, v) && b > rg::kCappedBlock) continue;
-      if (k == RG_KERNEL_UPDATE && v == 1) continue;  // the update has no unrolled build
+      if (!has_build(h, k, v) || (capped(k, v) && b > rg::kCappedBlock)) continue;
       for (int per_sm : kPerSm) {
         const rg::LaunchShape sh{b, per_sm * sms, v};
         RG_TRY(launch_one(h, k, sh, ext_scr.p, cells_scr.p));  // warm

@@ -26,8 +26,12 @@ MIXED_SHAPES = [{"slopes": (128, 0, 1)}, {"slopes": (256, 608, 2)}, {"slopes": (
                 {"update": (256, 0, 2)}, {"update": (128, 912, 3)}]
 
 
+# the FP64 slopes kernel's register-capped builds
+FP64_SHAPES = [{"slopes": (256, 0, 2)}, {"slopes": (128, 608, 3)}]
+
+
 def shapes_for(precision):
-    return SHAPES + (MIXED_SHAPES if precision == 1 else [])
+    return SHAPES + (MIXED_SHAPES if precision == 1 else FP64_SHAPES)
 
 
 def sedov(n=160):
@@ -133,7 +137,8 @@ def test_invalid_shapes_are_rejected():
     with richgpu.Handle(gamma=5 / 3, order=2, ghost_kind=0, device=0) as h:
         h.upload_mesh(mesh)
         for bad in ({"cfl": (48, 0)}, {"faces": (1024, 0)}, {"update": (0, 0)}, {"slopes": (64, -1)},
-                    {"slopes": (128, 0, 1)}, {"faces": (128, 0, 1)}):
+                    {"slopes": (128, 0, 1)}, {"slopes": (512, 0, 2)}, {"slopes": (128, 0, 4)},
+                    {"faces": (128, 0, 1)}, {"update": (128, 0, 2)}):
             with pytest.raises(richgpu.RichError) as ei:
                 h.set_launch_shapes(bad)
             assert ei.value.status == 1
