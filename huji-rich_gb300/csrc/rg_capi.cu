@@ -126,6 +126,7 @@ void fill_views(MeshSlot& s) {
   s.geom.hr = at<double2>(b, L.hr);
   s.geom.ghost_real = at<int>(b, L.ghost_real);
   s.geom.ghost_unit = at<double2>(b, L.ghost_unit);
+  s.geom.cell_order = at<int>(b, L.cell_order);
   s.g32.nrm = at<float2>(b, L.nrm32);
   s.g32.nabs = at<float>(b, L.nabs32);
   s.g32.par = at<float2>(b, L.par32);
@@ -715,6 +716,7 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t flags) {
   ga.hr = at<double2>(b, s.lay.hr);
   ga.ghost_real = at<int>(b, s.lay.ghost_real);
   ga.ghost_unit = at<double2>(b, s.lay.ghost_unit);
+  ga.cell_order = at<int>(b, s.lay.cell_order);
   ga.ghost_kind = h->cfg.ghost_kind;
   ga.status = h->d_geom_status;
   RG_CUDA(h, rg::launch_geometry(ga, h->upload_stream));

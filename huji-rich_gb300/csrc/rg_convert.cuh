@@ -8,9 +8,9 @@
 // the per-mesh geometry, the FP32-mixed update, the FP64 limiter's tests and
 // its FP32 screening) form the results from the IEEE-754 bit patterns
 // instead, with the same results as the hardware instruction for every
-// input.  (Full double orderings on the integer pipe cost the limiter more
-// in registers than they save; its min / max stay FP64 comparisons.)  Host-compilable, so the same
-// code is checked against the C casts and operators on the CPU.
+// input, the orderings of the FP64 limiter's extrema and thresholds
+// included.  Host-compilable, so the same code is checked against the C
+// casts and operators on the CPU.
 #pragma once
 
 #include <math.h>
@@ -131,6 +131,23 @@ RG_CONV_FN bool prod_neg(double a, double b) {
   return p < 0;
 #endif
 }
+
+// The IEEE order of non-NaN doubles as signed integers: -0 and +0 map to 0,
+// a larger value to a larger key.
+RG_CONV_FN int64_t order_key(uint64_t u) {
+  const int64_t m = static_cast<int64_t>(u & kMagMask);
+  return (u >> 63) ? -m : m;
+}
+RG_CONV_FN bool nan_bits(uint64_t u) { return (u & kMagMask) > kInfBits64; }
+// a < b (false when either is NaN; -0 == +0)
+RG_CONV_FN bool lt(double a, double b) {
+  const uint64_t ua = conv_dbits(a), ub = conv_dbits(b);
+  return !nan_bits(ua) && !nan_bits(ub) && order_key(ua) < order_key(ub);
+}
+// std::max(a, b) = a < b ? b : a and std::min(a, b) = b < a ? b : a, bit for
+// bit (the first operand on equality, -0 against +0 and NaN included)
+RG_CONV_FN double max_first(double a, double b) { return lt(a, b) ? b : a; }
+RG_CONV_FN double min_first(double a, double b) { return lt(b, a) ? b : a; }
 
 // t / 3 rounded to nearest (t >= 0) without a division.  RN(1/3) is 1/3
 // less 2^-54 of itself, so q = RN(t * RN(1/3)) is within one ulp of t/3,

@@ -162,6 +162,31 @@ __global__ void __launch_bounds__(kBlock) k_geom_ghosts(GeomArgs a) {
   a.ghost_unit[g] = make_double2(quot(nr.x, ab), quot(nr.y, ab));
 }
 
+// Per tile of kOrderTile cells: the order in which the FP64 slopes and update
+// kernels take them, by (boundary-slope flag, neighbour count) and then by
+// index.  Their per-cell loops run over a cell's neighbours, so a warp whose
+// cells have equal counts runs no lane idle; every cell is still computed by
+// one thread from the same inputs, so the results do not depend on the order.
+__global__ void __launch_bounds__(kOrderTile) k_cell_order(GeomArgs a) {
+  __shared__ int key[kOrderTile];
+  const int t = threadIdx.x, base = blockIdx.x * kOrderTile, i = base + t;
+  const int n = a.mesh.n, count = n - base < kOrderTile ? n - base : kOrderTile;
+  int k = 0;
+  if (i < n) {
+    const int nn = a.mesh.cell_off[i + 1] - a.mesh.cell_off[i];
+    k = (nn < 0 ? 0 : (nn > 63 ? 63 : nn)) | ((a.cflags[i] & kCellBoundarySlope) ? 64 : 0);
+  }
+  key[t] = k;
+  __syncthreads();
+  if (i >= n) return;
+  int rank = 0;
+  for (int j = 0; j < count; ++j) {
+    const int kj = key[j];
+    rank += (kj < k || (kj == k && j < t)) ? 1 : 0;
+  }
+  a.cell_order[base + rank] = i;
+}
+
 // Index validation of an uploaded mesh, before any kernel indexes with it.
 // Every read is bounds-checked against the array sizes; the first bad entry
 // (smallest key: faces, then ghosts, then cells) is recorded.  Phase 0 keys:
@@ -322,7 +347,7 @@ __device__ __forceinline__ void k_slopes_item(const StepArgs& a, int i) {
     // otherwise screened in FP32 against |left| vs delta_v*cs.
     const double lhs = (sx.vx + sy.vy) * a.geom.width[i];
     bool shock = false;
-    if (lhs < 0) {
+    if (lt(lhs, 0.0)) {
       const double gp = gamma_at<kBatch>(a, i) * cell.p;
       bool decided = false;
       if (fp32_safe(lhs) && fp32_safe(gp) && fp32_safe(cell.d)) {
@@ -343,8 +368,9 @@ __device__ __forceinline__ void k_slopes_item(const StepArgs& a, int i) {
       const float dp_f = narrow(a.delta_p);
       for (int k = 0; k < nn && !shock; ++k) {
         const double np_ = point_state(a, static_cast<int>(a.geom.nbr[b + k] & kNbrIdMask)).p;
-        const double num = cell.p > np_ ? np_ : cell.p;
-        const double den = cell.p > np_ ? cell.p : np_;
+        const bool lower = lt(np_, cell.p);
+        const double num = lower ? np_ : cell.p;
+        const double den = lower ? cell.p : np_;
         if (fp32_safe(num) && fp32_safe(den)) {
           const float rf = narrow(num) / narrow(den);
           if (rf < dp_f * 0.999999f) {
@@ -353,7 +379,7 @@ __device__ __forceinline__ void k_slopes_item(const StepArgs& a, int i) {
           }
           if (rf > dp_f * 1.000001f) continue;
         }
-        shock = quot(num, den) < a.delta_p;
+        shock = lt(quot(num, den), a.delta_p);
       }
     }
     if (a.shock) a.shock[i] = shock ? 1 : 0;
@@ -363,20 +389,20 @@ __device__ __forceinline__ void k_slopes_item(const StepArgs& a, int i) {
       if (!shock && (w & kNbrMirror)) continue;  // :194-195 skips self-mirror neighbours
       if (skipped(a, static_cast<int>(w & kNbrIdMask))) continue;  // :192-193, :314-315 skip_key
       const Cell nb = point_state(a, static_cast<int>(w & kNbrIdMask));
-      cmax.d = smax(cmax.d, nb.d);
-      cmax.p = smax(cmax.p, nb.p);
-      cmax.vx = smax(cmax.vx, nb.vx);
-      cmax.vy = smax(cmax.vy, nb.vy);
-      cmin.d = smin(cmin.d, nb.d);
-      cmin.p = smin(cmin.p, nb.p);
-      cmin.vx = smin(cmin.vx, nb.vx);
-      cmin.vy = smin(cmin.vy, nb.vy);
+      cmax.d = max_first(cmax.d, nb.d);
+      cmax.p = max_first(cmax.p, nb.p);
+      cmax.vx = max_first(cmax.vx, nb.vx);
+      cmax.vy = max_first(cmax.vy, nb.vy);
+      cmin.d = min_first(cmin.d, nb.d);
+      cmin.p = min_first(cmin.p, nb.p);
+      cmin.vx = min_first(cmin.vx, nb.vx);
+      cmin.vy = min_first(cmin.vy, nb.vy);
     }
     const Cell maxd{cmax.d - cell.d, cmax.p - cell.p, cmax.vx - cell.vx, cmax.vy - cell.vy};
     const Cell mind{cmin.d - cell.d, cmin.p - cell.p, cmin.vx - cell.vx, cmin.vy - cell.vy};
     const double f = shock ? 0.1 : 0.05;
-    const Cell thr{f * smax(fabs(maxd.d), fabs(mind.d)), f * smax(fabs(maxd.p), fabs(mind.p)),
-                   f * smax(fabs(maxd.vx), fabs(mind.vx)), f * smax(fabs(maxd.vy), fabs(mind.vy))};
+    const Cell thr{f * max_first(fabs(maxd.d), fabs(mind.d)), f * max_first(fabs(maxd.p), fabs(mind.p)),
+                   f * max_first(fabs(maxd.vx), fabs(mind.vx)), f * max_first(fabs(maxd.vy), fabs(mind.vy))};
     double psi0 = 1, psi1 = 1, psi2 = 1, psi3 = 1;
     float pf0 = 1, pf1 = 1, pf2 = 1, pf3 = 1;
     for (int k = 0; k < nn; ++k) {
@@ -423,8 +449,9 @@ __global__ void __launch_bounds__(kMinBlocks ? kCappedBlock : kMaxBlock, kMinBlo
   // the dt of this step, computed by the previous step's update (the face
   // kernel, launched after this one, reads status->dt)
   if (a.take_next_dt && blockIdx.x == 0 && threadIdx.x == 0) a.status->dt = a.status->dt_next;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.mesh.n; i += gridDim.x * blockDim.x)
-    k_slopes_item<kBatch>(a, i);
+  const int* order = a.geom.cell_order;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < a.mesh.n; t += gridDim.x * blockDim.x)
+    k_slopes_item<kBatch>(a, order ? order[t] : t);
 }
 
 // ---------------------------------------------------------------- faces
@@ -894,8 +921,9 @@ __global__ void __launch_bounds__(kMaxBlock) k_update(StepArgs a, int from_unsca
     }
   }
   unsigned long long bits = kInfBits;
-  for (int i = t0; i < a.mesh.n; i += stride) {
-    const unsigned long long b = k_update_item<kBatch>(a, i, from_unscaled, do_ext, do_cells);
+  const int* order = a.geom.cell_order;
+  for (int t = t0; t < a.mesh.n; t += stride) {
+    const unsigned long long b = k_update_item<kBatch>(a, order ? order[t] : t, from_unscaled, do_ext, do_cells);
     bits = b < bits ? b : bits;
   }
   if (!kBatch && a.cfl_next) grid_min_times(a.status, bits, a.cfl, &a.status->dt_next);
@@ -984,6 +1012,7 @@ cudaError_t launch_validate(const MeshDev& m, DevStatus* st, cudaStream_t s) {
 cudaError_t launch_geometry(const GeomArgs& a, cudaStream_t s) {
   if (a.mesh.e > 0) k_geom_faces<<<blocks(a.mesh.e), kBlock, 0, s>>>(a);
   if (a.mesh.n > 0) k_geom_cells<<<blocks(a.mesh.n), kBlock, 0, s>>>(a);
+  if (a.mesh.n > 0 && a.cell_order) k_cell_order<<<(a.mesh.n + kOrderTile - 1) / kOrderTile, kOrderTile, 0, s>>>(a);
   if (a.mesh.g > 0) k_geom_ghosts<<<blocks(a.mesh.g), kBlock, 0, s>>>(a);
   return cudaGetLastError();
 }

@@ -107,7 +107,7 @@ __device__ __forceinline__ void min_quotient(double num, double den, double& psi
     if (qf >= psi_f * 1.000001f) return;
   }
   const double q = quot(num, den);
-  if (q < psi) {
+  if (lt(q, psi)) {
     psi = q;
     psi_f = narrow(q);
   }
@@ -115,15 +115,16 @@ __device__ __forceinline__ void min_quotient(double num, double den, double& psi
 
 // one component of the ordinary limiter, LinearGaussImproved.cpp:232-267.
 // thr = 0.05*max(|maxd|,|mind|) (per cell); maxd >= 0 >= mind, so both
-// candidate quotients are >= 0.
+// candidate quotients are >= 0.  The comparisons run on the integer pipe
+// (rg_convert.cuh); the lower threshold -1e-9*q (or -|1e-9*q|) is exactly
+// the negated upper one, the rounding being sign-symmetric.
 __device__ __forceinline__ void limit_comp(double dphi, double cv, double cellv, double thr, double maxd,
                                            double mind, bool use_abs, double& psi, float& psi_f) {
   if (abs_gt(dphi, thr) || prod_neg(cv, cellv)) {
     const double t1 = use_abs ? fabs(1e-9 * cellv) : 1e-9 * cellv;
-    const double t2 = use_abs ? -fabs(1e-9 * cellv) : -1e-9 * cellv;
-    if (dphi > t1)
+    if (lt(t1, dphi))
       min_quotient(maxd, dphi, psi, psi_f);
-    else if (dphi < t2)
+    else if (lt(dphi, -t1))
       min_quotient(mind, dphi, psi, psi_f);
   }
 }
@@ -134,11 +135,14 @@ __device__ __forceinline__ void limit_comp(double dphi, double cv, double cellv,
 __device__ __forceinline__ void shocked_comp(double dphi, double cv, double cellv, double thr, double nbv,
                                              double theta, double& psi, float& psi_f, bool abs_thr = false) {
   if (abs_gt(dphi, thr) || prod_neg(cv, cellv)) {
-    if (fabs(dphi) > (abs_thr ? fabs(1e-9 * cellv) : 1e-9 * cellv)) {
+    if (lt(abs_thr ? fabs(1e-9 * cellv) : 1e-9 * cellv, fabs(dphi))) {
       const double num = theta * (nbv - cellv);
-      if (num != 0 && !isnan(num) && !isnan(dphi) && (num < 0) != (dphi < 0)) {
+      const uint64_t un = conv_dbits(num), ud = conv_dbits(dphi);
+      // num != 0, neither NaN, (num < 0) != (dphi < 0)
+      const bool num_neg = (un >> 63) != 0u, dphi_neg = (ud >> 63) != 0u && (ud & kMagMask) != 0u;
+      if ((un & kMagMask) != 0u && !nan_bits(un) && !nan_bits(ud) && num_neg != dphi_neg) {
         // negative quotient: smax(., 0) gives 0
-        if (0.0 < psi) {
+        if (lt(0.0, psi)) {
           psi = 0.0;
           psi_f = 0.0f;
         }
@@ -148,8 +152,8 @@ __device__ __forceinline__ void shocked_comp(double dphi, double cv, double cell
         const float qf = narrow(num) / narrow(dphi);
         if (qf >= psi_f * 1.000001f) return;
       }
-      const double x = smax(quot(num, dphi), 0.0);
-      if (x < psi) {
+      const double x = max_first(quot(num, dphi), 0.0);
+      if (lt(x, psi)) {
         psi = x;
         psi_f = narrow(x);
       }

@@ -61,7 +61,7 @@ struct SlotLayout {
   size_t points, cms, volume, cd_volume, ghost_source, ghost_face, face_cells, face_vertices, cell_off,
       cell_faces, input_end;
   size_t area, nrm, nabs, par, dm0, dm1, dab, rij, cij, xarea, width, minv, cflags, nbr, hr, ghost_real,
-      ghost_unit;
+      ghost_unit, cell_order;
   size_t nrm32, nabs32, par32, area32, xarea32, dm0_32, dm1_32, width32, minv32, ent32, fsign32, gunit32, icdv32,
       total;
   bool own_xarea = false;  // a non-slab PhysicalGeometry: CacheData areas differ from the edge lengths
@@ -102,6 +102,7 @@ struct SlotLayout {
     hr = take(16 * static_cast<size_t>(m));
     ghost_real = take(4 * static_cast<size_t>(g));
     ghost_unit = take(16 * static_cast<size_t>(g));
+    cell_order = take(4 * static_cast<size_t>(n));
     const size_t k = mixed ? 1 : 0;  // FP32 copies only for the mixed path
     nrm32 = take(k * 8 * static_cast<size_t>(e));
     nabs32 = take(k * 4 * static_cast<size_t>(e));

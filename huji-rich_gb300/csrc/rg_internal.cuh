@@ -76,7 +76,12 @@ struct GeomDev {
   // per ghost
   const int* ghost_real;      // cell whose state the ghost copies / reflects
   const double2* ghost_unit;  // rigid wall: unit normal (x_ghost - x_real)/|.|
+  // the cell each thread of the FP64 slopes and update kernels takes: within
+  // every tile of kOrderTile cells, the cells ordered by (boundary-slope
+  // flag, neighbour count), ties by index (null: thread i takes cell i)
+  const int* cell_order;
 };
+constexpr int kOrderTile = 256;
 
 // Device status word.  The error kept is the one with the smallest
 // (phase, index) key, which is the one the reference throws first: its
@@ -310,6 +315,7 @@ struct GeomArgs {
   double2* hr;
   int* ghost_real;
   double2* ghost_unit;
+  int* cell_order;
   int ghost_kind;
   DevStatus* status;
 };

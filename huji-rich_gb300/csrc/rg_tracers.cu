@@ -121,8 +121,8 @@ __global__ void __launch_bounds__(kTrBlock) k_tr_slopes(StepArgs a, TracerArgs t
 #pragma unroll
       for (int j = 0; j < kMaxTracers; ++j) {
         if (j < nt) {
-          cmax[j] = smax(cmax[j], nb[j]);
-          cmin[j] = smin(cmin[j], nb[j]);
+          cmax[j] = max_first(cmax[j], nb[j]);
+          cmin[j] = min_first(cmin[j], nb[j]);
         }
       }
     }
@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(kTrBlock) k_tr_slopes(StepArgs a, TracerArgs t
     for (int j = 0; j < kMaxTracers; ++j) {
       maxd[j] = cmax[j] - ct[j];
       mind[j] = cmin[j] - ct[j];
-      thr[j] = f * smax(fabs(maxd[j]), fabs(mind[j]));
+      thr[j] = f * max_first(fabs(maxd[j]), fabs(mind[j]));
       psi[j] = 1.0;
       pf[j] = 1.0f;
     }

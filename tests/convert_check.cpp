@@ -4,7 +4,8 @@
 // float range, rounding ties and carries, the special values, and a stride
 // through every float; rg::third_of against the division t / 3 over
 // random magnitudes and the special values; and the integer-pipe double
-// tests (abs_gt, abs_within, prod_neg) against the C operators.  Exit status 0 when every value agrees.
+// tests (abs_gt, abs_within, prod_neg, lt, max_first, min_first) against the
+// C operators.  Exit status 0 when every value agrees.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -113,6 +114,15 @@ int main() {
               rg::abs_within(a, 1e-36, 1e36) == (std::fabs(a) >= 1e-36 && std::fabs(a) <= 1e36);
     volatile double p = a * b;
     ok = ok && rg::prod_neg(a, b) == (p < 0);
+    ok = ok && rg::lt(a, b) == (a < b) && rg::lt(b, a) == (b < a) && rg::lt(a, a) == (a < a);
+    const double mx = rg::max_first(a, b), mn = rg::min_first(a, b);
+    const double rmx = a < b ? b : a, rmn = b < a ? b : a;
+    uint64_t u1, u2, u3, u4;
+    memcpy(&u1, &mx, 8);
+    memcpy(&u2, &rmx, 8);
+    memcpy(&u3, &mn, 8);
+    memcpy(&u4, &rmn, 8);
+    ok = ok && u1 == u2 && u3 == u4;
     if (!ok) {
       if (n_bad < 5) printf("comparison mismatch at a=%a b=%a t=%a\n", a, b, t);
       ++n_bad;
