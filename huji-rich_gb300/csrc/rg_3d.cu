@@ -28,7 +28,7 @@ struct V3 {
   double x, y, z;
 };
 // Vector3D.cpp: abs, ScalarProd, d*v (v.x*d), v/d, -, +
-__device__ __forceinline__ double vabs(V3 v) { return sqrt(v.x * v.x + v.y * v.y + v.z * v.z); }
+__device__ __forceinline__ double vabs(V3 v) { return root(v.x * v.x + v.y * v.y + v.z * v.z); }
 __device__ __forceinline__ double vdot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 __device__ __forceinline__ V3 vscale(double d, V3 v) { return V3{v.x * d, v.y * d, v.z * d}; }
 __device__ __forceinline__ V3 vdiv(V3 v, double d) { return V3{quot(v.x, d), quot(v.y, d), quot(v.z, d)}; }
@@ -52,7 +52,7 @@ __device__ __forceinline__ void store6(double* out, int i, double a, double b, d
 }
 
 __device__ __forceinline__ double dp2e(double g, double d, double p) { return quot(quot(p, d), g - 1); }
-__device__ __forceinline__ double dp2c(double g, double d, double p) { return sqrt(quot(g * p, d)); }
+__device__ __forceinline__ double dp2c(double g, double d, double p) { return root(quot(g * p, d)); }
 
 // FirstOrderHydroFlux.cpp:32-40 calc_primitive: (d, p, (v.n, |v - (v.n)n|), e, c)
 __device__ __forceinline__ Prim prim3(double g, const Cell3& c, V3 n) {

@@ -1,4 +1,5 @@
-// rg_div.cuh -- correctly rounded FP64 division on the integer and FP32 pipes.
+// rg_div.cuh -- correctly rounded FP64 division and square root on the
+// integer and FP32 pipes.
 //
 // GB300 issues about 2 FP64 operations per clock per SM against 64-128
 // 32-bit integer or FP32 ones, and an IEEE FP64 division costs about ten
@@ -212,6 +213,83 @@ RG_DIV_FN bool div_rn_fast(double a, double b, const Seed& seed, double* q) {
   return true;
 }
 
+// The FP32 reciprocal square root approximation of the device (the seed of sqrt_rn_fast).
+struct RsqrtSeedDevice {
+#if defined(__CUDACC__)
+  __device__ __forceinline__ float operator()(float f) const {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(f));
+    return r;
+  }
+#endif
+};
+
+// sqrt(x) correctly rounded on the fast path (x a positive normal double or
+// a zero); returns false (and leaves *r) otherwise.  Seed: a callable float
+// -> float approximating 1/sqrt(f) on [1, 4).  With Mx the 53-bit
+// significand, x = m * 2^E, m = Mx * 2^(odd - 52) in [1, 4), E even, the
+// result significand is S = nearest integer to sqrt(N), N = Mx * 2^(52 + odd):
+//  1. y ~ 1/sqrt(f), f = m truncated to 24 bits; e = 1 - f*y^2 (the step is
+//     taken only when |e| <= 2^-21, else sqrt(x)); s0 = f*y, within
+//     1.5 * 2^-22 of sqrt(m); the remainder m - s0^2 in float-float (s0^2
+//     split exactly by an FMA, m as f plus its low part) and one Newton step
+//     c = (m - s0^2) / (2 s0) with 1/s0 ~ y + y*e; S1 = (s0 + c) * 2^52 in
+//     fixed point, within 2^-42 (relative) of sqrt(N), so |N - S1^2| < 2^66.
+//  2. The remainder N - S1^2 exactly in 128 bits; k = (its top bits as a
+//     float) / (2 S1), rounded: error below 2^-4, so S2 = S1 + k is within
+//     1/2 + 2^-4 of sqrt(N).
+//  3. R = N - S2^2, exact modulo 2^64 (|R| < 2^55): sqrt(N) > S2 + 1/2 iff
+//     R > S2, and sqrt(N) < S2 - 1/2 iff R <= -S2 (N and S2 are integers,
+//     so (S2 +- 1/2)^2 is never N: no ties).  S = S2 + 1, S2 - 1 or S2; S =
+//     2^53 carries into the exponent field.
+template <class Seed>
+RG_DIV_FN bool sqrt_rn_fast(double x, const Seed& seed, double* r) {
+  using namespace div_detail;
+  const uint64_t ux = d2u(x);
+  if ((ux & ~kSign) == 0u) {
+    *r = x;  // sqrt(+-0) = +-0
+    return true;
+  }
+  const uint32_t ex = static_cast<uint32_t>(ux >> 52);  // with the sign: negative x is out of range
+  if (ex - 1u >= 2046u) return false;                   // negative, subnormal, infinite or NaN
+  const uint32_t odd = (ex & 1u) ^ 1u;                  // ex - 1023 odd
+  const uint64_t mx = (ux & kFrac) | kHidden;
+  // step 1 (f in [1, 4); the low part is the 29 bits below f's significand)
+  const float f = u2f(((127u + odd) << 23) | static_cast<uint32_t>((ux & kFrac) >> 29));
+  const float f_lo = mul32(static_cast<float>(static_cast<uint32_t>(ux & 0x1fffffffu)),
+                           odd ? 4.440892098500626e-16f : 2.220446049250313e-16f);
+  const float y = seed(f);
+  const float e = fma32(-f, mul32(y, y), 1.0f);
+  if (!(e <= 4.76837158203125e-07f && e >= -4.76837158203125e-07f)) return false;  // |e| <= 2^-21
+  const float s0 = mul32(f, y);
+  const float p = mul32(s0, s0);
+  const float pe = fma32(s0, s0, -p);
+  const float rm = ((f - p) - pe) + f_lo;  // m - s0^2 (f - p is exact)
+  const float inv = fma32(y, e, y);        // 1 / s0
+  const float c = mul32(mul32(rm, inv), 0.5f);
+  // s0 in [0.5, 2]: s0 * 2^24 is an integer below 2^25 + 1; |c| < 2^-19, so
+  // |c * 2^50| < 2^31
+  const uint64_t S1 = (static_cast<uint64_t>(f2u_int(mul32(s0, 16777216.0f))) << 28) +
+                      static_cast<uint64_t>(static_cast<int64_t>(f2i_rn(mul32(c, 1125899906842624.0f))) * 4);
+  // step 2: N - S1^2 in 128 bits, then its top bits
+  const uint64_t n_lo = mx << (52 + odd), n_hi = mx >> (12 - odd);
+  const uint64_t q_lo = S1 * S1, q_hi = umulhi(S1, S1);
+  const uint64_t r_lo = n_lo - q_lo;
+  const uint64_t r_hi = n_hi - q_hi - (n_lo < q_lo ? 1u : 0u);
+  const int64_t r48 = static_cast<int64_t>((r_hi << 16) | (r_lo >> 48));  // floor(remainder / 2^48), |.| < 2^18
+  // k = remainder / (2 S1) = remainder * inv * 2^-53
+  const int32_t k = f2i_rn(mul32(mul32(static_cast<float>(static_cast<int32_t>(r48)), inv), 0.03125f));
+  const uint64_t S2 = S1 + static_cast<uint64_t>(static_cast<int64_t>(k));
+  // step 3: exact remainder and rounding
+  const int64_t R = static_cast<int64_t>(n_lo - S2 * S2);
+  const int64_t s2 = static_cast<int64_t>(S2);
+  const uint64_t S = S2 + (R > s2 ? 1u : 0u) - (R <= -s2 ? 1u : 0u);
+  // exponent field E/2 + 1023 (E = ex - 1023 - odd, even); S's hidden bit adds the one
+  const int field = (static_cast<int>(ex) - static_cast<int>(odd) - 1023) / 2 + 1022;
+  *r = u2d((static_cast<uint64_t>(field) << 52) + S);
+  return true;
+}
+
 #if defined(__CUDACC__)
 // The IEEE division for the operands outside the fast path, kept out of line
 // so that the compiler cannot compute it ahead of the branch.
@@ -224,9 +302,21 @@ __device__ __forceinline__ double div_rn(double a, double b) {
   return div_ieee(a, b);
 }
 
+static __device__ __noinline__ double sqrt_ieee(double x) { return sqrt(x); }
+
+// sqrt(x), bitwise (the fast path above, sqrt(x) outside it)
+__device__ __forceinline__ double sqrt_rn(double x) {
+  double r;
+  if (sqrt_rn_fast(x, RsqrtSeedDevice{}, &r)) return r;
+  return sqrt_ieee(x);
+}
+
 // a / b of the kernels' real type: div_rn for double, the FP32 division for float
 __device__ __forceinline__ double quot(double a, double b) { return div_rn(a, b); }
 __device__ __forceinline__ float quot(float a, float b) { return a / b; }
+// sqrt of the kernels' real type: sqrt_rn for double, the FP32 square root for float
+__device__ __forceinline__ double root(double x) { return sqrt_rn(x); }
+__device__ __forceinline__ float root(float x) { return sqrtf(x); }
 #endif
 
 }  // namespace rg

@@ -37,7 +37,7 @@ __global__ void __launch_bounds__(kBlock) k_geom_faces(GeomArgs a) {
   const int2 fc = a.mesh.face_cells[e];
   const dbl4 v = a.mesh.face_vertices[e];
   const double ax = v.x - v.z, ay = v.y - v.w;
-  a.area[e] = sqrt(ax * ax + ay * ay);
+  a.area[e] = root(ax * ax + ay * ay);
   const double2 p = make_double2(v.z - v.x, v.w - v.y);
   a.par[e] = p;
   const double2 mid = make_double2((v.x + v.z) * 0.5, (v.y + v.w) * 0.5);
@@ -59,7 +59,7 @@ __global__ void __launch_bounds__(kBlock) k_geom_faces(GeomArgs a) {
     n = make_double2(w.x - quot(p.x * sp, pp), w.y - quot(p.y * sp, pp));
   }
   a.nrm[e] = n;
-  a.nabs[e] = sqrt(n.x * n.x + n.y * n.y);
+  a.nabs[e] = root(n.x * n.x + n.y * n.y);
   const double2 c0 = a.mesh.cms[fc.x], c1 = a.mesh.cms[fc.y];
   a.dm0[e] = make_double2(mid.x - c0.x, mid.y - c0.y);
   a.dm1[e] = make_double2(mid.x - c1.x, mid.y - c1.y);
@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(kBlock) k_geom_faces(GeomArgs a) {
   // commutes), so each face computes them once.
   const double2 x0 = a.mesh.points[fc.x], x1 = a.mesh.points[fc.y];
   const double ddx = x1.x - x0.x, ddy = x1.y - x0.y;
-  const double dab = sqrt(ddx * ddx + ddy * ddy);
+  const double dab = root(ddx * ddx + ddy * ddy);
   a.dab[e] = dab;
   const double len = a.area[e];  // Edge::GetLength = |second - first| = |first - second|
   a.rij[e] = make_double2(quot(ddx, dab) * len, quot(ddy, dab) * len);
@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(kBlock) k_geom_cells(GeomArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const MeshDev& m = a.mesh;
   if (i >= m.n) return;
-  a.width[i] = sqrt(quot(m.volume[i], kPi));
+  a.width[i] = root(quot(m.volume[i], kPi));
   const int b = m.cell_off[i], nn = m.cell_off[i + 1] - b;
   bool bslope = false;
   for (int k = 0; k < nn; ++k) {
@@ -158,7 +158,7 @@ __global__ void __launch_bounds__(kBlock) k_geom_ghosts(GeomArgs a) {
   const double2 x0 = m.points[fc.x], x1 = m.points[fc.y];
   const double2 nr = ghost_first ? make_double2(x0.x - x1.x, x0.y - x1.y)
                                  : make_double2(x1.x - x0.x, x1.y - x0.y);
-  const double ab = sqrt(nr.x * nr.x + nr.y * nr.y);
+  const double ab = root(nr.x * nr.x + nr.y * nr.y);
   a.ghost_unit[g] = make_double2(quot(nr.x, ab), quot(nr.y, ab));
 }
 
@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_cfl(StepArgs a, int fill_ghosts) 
     if (t < m.n) {
       const Cell c = load_cell(a.cells, t);
       const double radius = a.geom.width[t];
-      const double cs = sqrt(quot(gamma_at<kBatch>(a, t) * c.p, c.d));
+      const double cs = root(quot(gamma_at<kBatch>(a, t) * c.p, c.d));
       // fmax over faces of (cs + sqrt(q_e)) / radius equals (cs + sqrt(max q_e)) /
       // radius exactly: sqrt, + and / are correctly rounded, hence monotone, so
       // the maximum commutes with them.  NaN terms are skipped as fmax skips them.
@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_cfl(StepArgs a, int fill_ghosts) 
           }
         }
       }
-      const double res = any ? fmax(0.0, quot(cs + sqrt(q), radius)) : 0.0;
+      const double res = any ? fmax(0.0, quot(cs + root(q), radius)) : 0.0;
       x = quot(1.0, res);
     } else if (t < total) {
       fill_ghost(a, t - m.n);
@@ -360,7 +360,7 @@ __device__ __forceinline__ void k_slopes_item(const StepArgs& a, int i) {
           decided = true;
         }
       }
-      if (!decided) shock = lhs < (-a.delta_v) * sqrt(quot(gp, cell.d));
+      if (!decided) shock = lhs < (-a.delta_v) * root(quot(gp, cell.d));
     }
     if (!shock && nn == 0) shock = 1.0 < a.delta_p;  // PressureRatio of no neighbours is 1
     if (!shock) {
@@ -458,7 +458,7 @@ __global__ void __launch_bounds__(kMinBlocks ? kCappedBlock : kMaxBlock, kMinBlo
 
 // simple_flux_calculator.cpp:9-15 convert_to_primitive (ideal_gas.cpp:13-16, 40-44)
 __device__ __forceinline__ Prim to_prim(double g, const Cell& c) {
-  return Prim{c.d, c.p, c.vx, c.vy, quot(quot(c.p, c.d), g - 1), sqrt(quot(g * c.p, c.d))};
+  return Prim{c.d, c.p, c.vx, c.vy, quot(quot(c.p, c.d), g - 1), root(quot(g * c.p, c.d))};
 }
 
 // simple_flux_calculator.cpp:130-165 rotate / Hllc / rotate_back
@@ -613,7 +613,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_faces_pcm(StepArgs a) {
 
 // geometry.cpp normalize: v/abs(v)
 __device__ __forceinline__ double2 normalize2(double x, double y) {
-  const double ab = sqrt(x * x + y * y);
+  const double ab = root(x * x + y * y);
   return make_double2(quot(x, ab), quot(y, ab));
 }
 // simple_flux_calculator.cpp:27-31 remove_parallel_component, then normalize
@@ -668,7 +668,7 @@ __device__ __forceinline__ void k_faces_cas_item(const StepArgs& a, int e) {
   }
   const dbl4 v = m.face_vertices[e];
   const double2 p = normalize2(v.z - v.x, v.w - v.y);
-  const double pa = sqrt(p.x * p.x + p.y * p.y);
+  const double pa = root(p.x * p.x + p.y * p.y);
   const double g = a.gamma;
   const Cell c0 = load_cell(a.cells, orig_of(m, fc.x)), c1 = load_cell(a.cells, orig_of(m, fc.y));
   int action = a.rules[chosen][3];
@@ -759,7 +759,7 @@ __device__ __forceinline__ void k_faces_cas_item(const StepArgs& a, int e) {
       }
     }
   }
-  const double na = sqrt(n.x * n.x + n.y * n.y);
+  const double na = root(n.x * n.x + n.y * n.y);
   Cons c;
   if (!solve_face(l, r, vel, n, na, p, pa, c, a, e)) return;
   const int real_side = fc.x < m.n ? fc.x : fc.y;
@@ -780,7 +780,7 @@ template <bool kBatch>
 __device__ __forceinline__ unsigned long long cfl_bound_bits(const StepArgs& a, int i, double d, double pres,
                                                              double vx, double vy) {
   const MeshDev& m = a.mesh;
-  const double cs = sqrt(quot(gamma_at<kBatch>(a, i) * pres, d));
+  const double cs = root(quot(gamma_at<kBatch>(a, i) * pres, d));
   double q = 0;
   bool any = false;
   if (a.ev_zero) {
@@ -800,7 +800,7 @@ __device__ __forceinline__ unsigned long long cfl_bound_bits(const StepArgs& a, 
       }
     }
   }
-  const double res = any ? fmax(0.0, quot(cs + sqrt(q), a.geom.width[i])) : 0.0;
+  const double res = any ? fmax(0.0, quot(cs + root(q), a.geom.width[i])) : 0.0;
   return static_cast<unsigned long long>(__double_as_longlong(quot(1.0, res)));
 }
 

@@ -24,7 +24,7 @@ using Cons = ConsT<double>;
 // hydrodynamic_variables.cpp:261-265 TotalEnergyDensity (pow(x,2) is x*x)
 template <class R>
 __device__ __forceinline__ R ted(const PrimT<R>& p) {
-  const R s = sqrt(p.vx * p.vx + p.vy * p.vy);
+  const R s = root(p.vx * p.vx + p.vy * p.vy);
   return p.d * (R(0.5) * (s * s) + p.e);
 }
 

@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(kMoBlock) k_ghost_cms(MeshDev m, double2* cms,
   cms[p] = r;
 }
 
-__device__ __forceinline__ double vabs2(double x, double y) { return sqrt(x * x + y * y); }
+__device__ __forceinline__ double vabs2(double x, double y) { return root(x * x + y * y); }
 
 // CylindricalSymmetry (physical_geometry.cpp:44-110): Axis normalises its
 // direction (:40-42); change_coordinate gives (along, |across|).
@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(kMoBlock) k_cyl_geometry(MeshDev m, double* xa
     const dbl4 v = m.face_vertices[t];
     const double2 p1 = change_coordinate(v.x, v.y, a), p2 = change_coordinate(v.z, v.w, a);
     const double dy = p2.y - p1.y, dx = p2.x - p1.x;
-    xarea[t] = kPi * (p1.y + p2.y) * sqrt(dy * dy + dx * dx);
+    xarea[t] = kPi * (p1.y + p2.y) * root(dy * dy + dx * dx);
   }
   if (cd_volume && t < m.n) {
     // :94-104 calcVolume over the cell's edges, :84-92 calc_triangular_ring_volume
@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(kMoBlock) k_cyl_geometry(MeshDev m, double* xa
   }
 }
 
-__device__ __forceinline__ double sound(double g, const double* c) { return sqrt(quot(g * c[1], c[0])); }
+__device__ __forceinline__ double sound(double g, const double* c) { return root(quot(g * c[1], c[0])); }
 
 __global__ void __launch_bounds__(kMoBlock) k_point_velocities(StepArgs a, MotionArgs mo) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;

@@ -79,13 +79,13 @@ __global__ void __launch_bounds__(kBlock)
   if (i < n) {
     const double2 dp = reinterpret_cast<const double2*>(cells)[2 * i];
     const double2 uv = reinterpret_cast<const double2*>(cells)[2 * i + 1];
-    const double radius = sqrt(rg::quot(volume[i], rg::kPi));
-    const double cs = sqrt(rg::quot(gamma * dp.y, dp.x));
+    const double radius = rg::root(rg::quot(volume[i], rg::kPi));
+    const double cs = rg::root(rg::quot(gamma * dp.y, dp.x));
     double res = 0;
     for (int k = off[i]; k < off[i + 1]; ++k) {
       const double2 w = reinterpret_cast<const double2*>(ev)[faces[k]];
       const double dx = uv.x - w.x, dy = uv.y - w.y;
-      res = fmax(res, rg::quot(cs + sqrt(dx * dx + dy * dy), radius));
+      res = fmax(res, rg::quot(cs + rg::root(dx * dx + dy * dy), radius));
     }
     x = rg::quot(1.0, res);
   }

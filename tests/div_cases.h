@@ -1,5 +1,6 @@
-// div_cases.h -- operand families for the FP64 division checks
-// (tests/div_check.cpp on the host, tests/div_check_gpu.cu on the device).
+// div_cases.h -- operand families for the FP64 division and square root
+// checks (tests/div_check.cpp and tests/sqrt_check.cpp on the host,
+// tests/div_check_gpu.cu on the device).
 //
 // Families: random bit patterns (every class of double), random normal
 // operands over the whole exponent range, operands of moderate size,
@@ -9,6 +10,7 @@
 // differences at the edges of the division's fast path.
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <random>
@@ -105,6 +107,63 @@ void generate(std::mt19937_64& rng, long long n, F&& check) {
       check(from(sgn() | static_cast<uint64_t>(ea) << 52 | frac()),
             from(sgn() | static_cast<uint64_t>(eb) << 52 | frac()));
     }
+  }
+}
+
+
+// calls check(x) for about 11 n values of x: random bit patterns, random
+// positive normals over the whole exponent range and near 1, exact squares
+// of 26-bit integers and their neighbours, values next to (S + 1/2)^2 for a
+// 53-bit S (the rounding midpoints of the square root), powers of two and
+// their neighbours, zeros
+template <class F>
+void generate_sqrt(std::mt19937_64& rng, long long n, F&& check) {
+  std::uniform_int_distribution<uint64_t> u64;
+  const uint64_t kFrac = (uint64_t(1) << 52) - 1;
+  for (long long i = 0; i < n; ++i) check(from(u64(rng)));
+  for (long long i = 0; i < n; ++i) check(from((1 + u64(rng) % 2046) << 52 | (u64(rng) & kFrac)));
+  for (long long i = 0; i < n; ++i) check(from((1021 + u64(rng) % 4) << 52 | (u64(rng) & kFrac)));
+  // exact squares of 26-bit integers (scaled), and their neighbours
+  for (long long i = 0; i < n; ++i) {
+    const uint64_t S = (uint64_t(1) << 25) | (u64(rng) & ((uint64_t(1) << 25) - 1));
+    const double sq = static_cast<double>(S * S);  // < 2^52: exact
+    const double x = ldexp(sq, static_cast<int>(u64(rng) % 200) - 100);
+    check(x);
+    check(from(bits(x) + 1));
+    check(from(bits(x) - 1));
+  }
+  // next to (S + 1/2)^2 for a 53-bit S: x = RN((S + 1/2)^2 * 2^e) and neighbours
+  for (long long i = 0; i < n; ++i) {
+    const uint64_t S = (uint64_t(1) << 52) | (u64(rng) & kFrac);
+    const unsigned __int128 T = static_cast<unsigned __int128>(2 * S + 1) * (2 * S + 1);  // 4 (S + 1/2)^2, < 2^108
+    int top = 127;
+    while (!((T >> top) & 1)) --top;
+    const int sh = top - 52;
+    unsigned __int128 m = T >> sh;
+    const unsigned __int128 rem = T & ((static_cast<unsigned __int128>(1) << sh) - 1);
+    const unsigned __int128 half = static_cast<unsigned __int128>(1) << (sh - 1);
+    if (rem > half || (rem == half && (m & 1))) m += 1;
+    int top2 = sh;
+    if (m >> 53) {
+      m >>= 1;
+      ++top2;
+    }
+    // value m * 2^(top2 - 2) * 2^(2j) for an even scale
+    const int j = static_cast<int>(u64(rng) % 200) - 100;
+    const double x = ldexp(static_cast<double>(static_cast<uint64_t>(m)), top2 - 2 - 104 + 2 * j);
+    check(x);
+    check(from(bits(x) + 1));
+    check(from(bits(x) - 1));
+  }
+  // powers of two and their neighbours, zeros
+  for (long long i = 0; i < n / 4 + 1; ++i) {
+    const uint64_t e = 1 + u64(rng) % 2046;
+    const uint64_t u = e << 52;
+    check(from(u));
+    check(from(u + 1 + u64(rng) % 3));
+    check(from(u - 1 - u64(rng) % 3));
+    check(0.0);
+    check(-0.0);
   }
 }
 

@@ -11,6 +11,9 @@
 //    at most 2^-22 and falls back above it).
 // 3. Throughput: 64 divisions per thread over 152 * 8 blocks of 256 threads,
 //    rg::div_rn against a / b, timed with CUDA events.
+// 4. The same for the square root: rg::sqrt_rn against sqrt on the families
+//    of divcases::generate_sqrt, the FP32 reciprocal square root
+//    approximation on every float in [1, 4), and the throughput.
 // Prints one JSON line.
 #include <cuda_runtime.h>
 
@@ -49,6 +52,40 @@ __global__ void k_rcp_error(unsigned long long* worst) {
   const float r = rg::RcpSeedDevice{}(f);
   const double e = fabs(1.0 - static_cast<double>(f) * static_cast<double>(r));
   atomicMax(worst, static_cast<unsigned long long>(__double_as_longlong(e)));
+}
+
+__global__ void k_sqrt(const double* x, double* r_new, double* r_ref, unsigned char* fast, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double r;
+    const bool f = rg::sqrt_rn_fast(x[i], rg::RsqrtSeedDevice{}, &r);
+    r_new[i] = f ? r : sqrt(x[i]);
+    fast[i] = f ? 1 : 0;
+    r_ref[i] = sqrt(x[i]);
+  }
+}
+
+// max over f in [1, 4) of |1 - f * rsqrt(f)^2|
+__global__ void k_rsqrt_error(unsigned long long* worst) {
+  const unsigned m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= (1u << 24)) return;
+  const float f = __uint_as_float((0x3f800000u + (m >> 23 << 23)) | (m & 0x7fffffu));
+  const float y = rg::RsqrtSeedDevice{}(f);
+  const double e = fabs(1.0 - static_cast<double>(f) * static_cast<double>(y) * static_cast<double>(y));
+  atomicMax(worst, static_cast<unsigned long long>(__double_as_longlong(e)));
+}
+
+template <bool kNew>
+__global__ void k_sqrt_throughput(const double* a, unsigned long long* sink) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned long long ua = static_cast<unsigned long long>(__double_as_longlong(fabs(a[t])));
+  unsigned long long acc = 0;
+#pragma unroll 4
+  for (int k = 0; k < 64; ++k) {
+    const double x = __longlong_as_double(static_cast<long long>(ua + 977ull * k));
+    const double r = kNew ? rg::sqrt_rn(x) : sqrt(x);
+    acc ^= static_cast<unsigned long long>(__double_as_longlong(r));
+  }
+  sink[t] = acc;
 }
 
 template <bool kNew>
@@ -140,8 +177,55 @@ int main(int argc, char** argv) {
   CK(cudaEventElapsedTime(&ms_new, e0, e1));
   CK(cudaEventElapsedTime(&ms_ref, e1, e2));
   const double divs = 64.0 * lanes;
+  // square roots
+  std::vector<double> hx;
+  divcases::generate_sqrt(rng, per, [&](double x) { hx.push_back(x); });
+  const long long ns = static_cast<long long>(hx.size());
+  double *x, *rn, *rr;
+  unsigned char* sfast;
+  CK(cudaMalloc(&x, ns * sizeof(double)));
+  CK(cudaMalloc(&rn, ns * sizeof(double)));
+  CK(cudaMalloc(&rr, ns * sizeof(double)));
+  CK(cudaMalloc(&sfast, ns));
+  CK(cudaMemcpy(x, hx.data(), ns * sizeof(double), cudaMemcpyHostToDevice));
+  k_sqrt<<<152 * 16, 256>>>(x, rn, rr, sfast, ns);
+  CK(cudaGetLastError());
+  std::vector<double> hsn(ns), hsr(ns);
+  std::vector<unsigned char> hsf(ns);
+  CK(cudaMemcpy(hsn.data(), rn, ns * sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(hsr.data(), rr, ns * sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(hsf.data(), sfast, ns, cudaMemcpyDeviceToHost));
+  long long sbad = 0, sfastn = 0;
+  double sbad_x = 0;
+  for (long long i = 0; i < ns; ++i) {
+    sfastn += hsf[i];
+    const bool nan_n = hsn[i] != hsn[i], nan_r = hsr[i] != hsr[i];
+    if (!(divcases::bits(hsn[i]) == divcases::bits(hsr[i]) || (nan_n && nan_r))) {
+      if (!sbad) sbad_x = hx[i];
+      ++sbad;
+    }
+  }
+  CK(cudaMemset(worst, 0, sizeof *worst));
+  k_rsqrt_error<<<(1 << 24) / 256, 256>>>(worst);
+  CK(cudaMemcpy(&hw, worst, sizeof hw, cudaMemcpyDeviceToHost));
+  double rsqrt_err;
+  std::memcpy(&rsqrt_err, &hw, sizeof rsqrt_err);
+  k_sqrt_throughput<true><<<blocks, threads>>>(a + off, sink);
+  k_sqrt_throughput<false><<<blocks, threads>>>(a + off, sink);
+  CK(cudaEventRecord(e0));
+  k_sqrt_throughput<true><<<blocks, threads>>>(a + off, sink);
+  CK(cudaEventRecord(e1));
+  k_sqrt_throughput<false><<<blocks, threads>>>(a + off, sink);
+  CK(cudaEventRecord(e2));
+  CK(cudaEventSynchronize(e2));
+  float sms_new = 0, sms_ref = 0;
+  CK(cudaEventElapsedTime(&sms_new, e0, e1));
+  CK(cudaEventElapsedTime(&sms_ref, e1, e2));
   std::printf("{\"cases\": %lld, \"mismatches\": %lld, \"fast\": %lld, \"first_a\": %.17g, \"first_b\": %.17g, "
-              "\"rcp_max_rel_error\": %.6g, \"div_rn_gdiv_per_s\": %.4g, \"ieee_div_gdiv_per_s\": %.4g}\n",
-              n, bad, nfast, bad_a, bad_b, rcp_err, divs / (ms_new * 1e6), divs / (ms_ref * 1e6));
-  return bad == 0 ? 0 : 1;
+              "\"rcp_max_rel_error\": %.6g, \"div_rn_gdiv_per_s\": %.4g, \"ieee_div_gdiv_per_s\": %.4g, "
+              "\"sqrt_cases\": %lld, \"sqrt_mismatches\": %lld, \"sqrt_fast\": %lld, \"sqrt_first_x\": %.17g, "
+              "\"rsqrt_max_rel_error\": %.6g, \"sqrt_rn_gsqrt_per_s\": %.4g, \"ieee_sqrt_gsqrt_per_s\": %.4g}\n",
+              n, bad, nfast, bad_a, bad_b, rcp_err, divs / (ms_new * 1e6), divs / (ms_ref * 1e6), ns, sbad, sfastn,
+              sbad_x, rsqrt_err, divs / (sms_new * 1e6), divs / (sms_ref * 1e6));
+  return bad == 0 && sbad == 0 ? 0 : 1;
 }
