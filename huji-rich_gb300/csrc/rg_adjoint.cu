@@ -16,6 +16,7 @@
 #include <math.h>
 
 #include "rg_adjoint.cuh"
+#include "rg_div.cuh"
 
 namespace rg {
 namespace {
@@ -27,22 +28,26 @@ constexpr int kBlock = 256;
 struct Dual {
   double v, d;
 };
+using ::rg::quot;  // the double overload, beside the Dual ones below
 __device__ __forceinline__ Dual operator+(Dual a, Dual b) { return Dual{a.v + b.v, a.d + b.d}; }
 __device__ __forceinline__ Dual operator-(Dual a, Dual b) { return Dual{a.v - b.v, a.d - b.d}; }
 __device__ __forceinline__ Dual operator*(Dual a, Dual b) { return Dual{a.v * b.v, a.d * b.v + a.v * b.d}; }
 __device__ __forceinline__ Dual operator/(Dual a, Dual b) {
-  const double q = a.v / b.v;
-  return Dual{q, (a.d - q * b.d) / b.v};
+  const double q = quot(a.v, b.v);
+  return Dual{q, quot(a.d - q * b.d, b.v)};
 }
 __device__ __forceinline__ Dual operator*(Dual a, double b) { return Dual{a.v * b, a.d * b}; }
 __device__ __forceinline__ Dual operator*(double a, Dual b) { return Dual{a * b.v, a * b.d}; }
-__device__ __forceinline__ Dual operator/(Dual a, double b) { return Dual{a.v / b, a.d / b}; }
+__device__ __forceinline__ Dual operator/(Dual a, double b) { return Dual{quot(a.v, b), quot(a.d, b)}; }
+// quotients of the templated code: rg::quot for double, the operators for Dual
+__device__ __forceinline__ Dual quot(Dual a, Dual b) { return a / b; }
+__device__ __forceinline__ Dual quot(Dual a, double b) { return a / b; }
 __device__ __forceinline__ Dual operator-(Dual a, double b) { return Dual{a.v - b, a.d}; }
 __device__ __forceinline__ Dual dsqrt(Dual a) {
-  const double s = sqrt(a.v);
-  return Dual{s, a.d / (2.0 * s)};
+  const double s = root(a.v);
+  return Dual{s, quot(a.d, 2.0 * s)};
 }
-__device__ __forceinline__ double dsqrt(double a) { return sqrt(a); }
+__device__ __forceinline__ double dsqrt(double a) { return root(a); }
 __device__ __forceinline__ double val(double x) { return x; }
 __device__ __forceinline__ double val(Dual x) { return x.v; }
 __device__ __forceinline__ double tan_of(Dual x) { return x.d; }
@@ -151,13 +156,13 @@ __device__ void lgi_slope(const AdjArgs& a, int i, V4<T>& sx, V4<T>& sy) {
     for (int q = 0; q < 4; ++q) cq_[q] = val(cell.v[q]);
     // is_shock: (div v)*width < -delta_v*cs, or some neighbour pressure ratio < delta_p
     const double lhs = (val(sx.v[2]) + val(sy.v[3])) * a.geom.width[i];
-    bool shock = lhs < (-a.delta_v) * sqrt(a.gamma * cq_[1] / cq_[0]);
+    bool shock = lhs < (-a.delta_v) * root(quot(a.gamma * cq_[1], cq_[0]));
     if (!shock && nn == 0) shock = 1.0 < a.delta_p;
     for (int k = 0; k < nn && !shock; ++k) {
       const double np_ = a.cells[4 * entry_source(a, b + k) + 1];
       const double num = cq_[1] > np_ ? np_ : cq_[1];
       const double den = cq_[1] > np_ ? cq_[1] : np_;
-      shock = num / den < a.delta_p;
+      shock = quot(num, den) < a.delta_p;
     }
     // neighbour max / min (the first strict improvement is kept, as std::max/min)
     double cmax[4], cmin[4];
@@ -203,7 +208,7 @@ __device__ void lgi_slope(const AdjArgs& a, int i, V4<T>& sx, V4<T>& sy) {
           const double t2 = use_abs ? -fabs(1e-9 * cq) : -1e-9 * cq;
           if (dv > t1 || dv < t2) {
             const bool up = dv > t1;
-            const T cand = (up ? nmax : nmin) / dphi;
+            const T cand = quot(up ? nmax : nmin, dphi);
             if (val(cand) < val(psi[q])) {
               psi[q] = cand;
               const int ex = up ? amax[q] : amin[q];
@@ -213,7 +218,7 @@ __device__ void lgi_slope(const AdjArgs& a, int i, V4<T>& sx, V4<T>& sy) {
           }
         } else if (fabs(dv) > 1e-9 * cq) {
           const T nb = load4<T>(a.cells, a.dcells, entry_source(a, b + k)).v[q];
-          const T cand = (a.theta * (nb - cell.v[q])) / dphi;
+          const T cand = quot(a.theta * (nb - cell.v[q]), dphi);
           const bool clamp = val(cand) < 0.0;  // std::max(cand, 0)
           const T x = clamp ? constant<T>(0.0) : cand;
           if (val(x) < val(psi[q])) {
@@ -272,7 +277,7 @@ __global__ void __launch_bounds__(kBlock) k_tl_slopes(AdjArgs a) {
 // with |v| = sqrt(vx^2 + vy^2) squared again; the tangent uses |v|^2 directly
 // (the square root has no derivative at rest).
 __device__ __forceinline__ double ted(double d, double vx, double vy, double e) {
-  const double s = sqrt(vx * vx + vy * vy);
+  const double s = root(vx * vx + vy * vy);
   return d * (0.5 * (s * s) + e);
 }
 __device__ __forceinline__ Dual ted(Dual d, Dual vx, Dual vy, Dual e) {
@@ -290,10 +295,10 @@ __device__ bool face_flux(const AdjArgs& a, int e, const V4<T>& L, const V4<T>& 
   const double g = a.gamma;
   const double2 n = a.geom.nrm[e], p = a.geom.par[e];
   const double na = a.geom.nabs[e], pa = a.geom.area[e];
-  const T le = L.v[1] / L.v[0] / (g - 1), lc = dsqrt(g * L.v[1] / L.v[0]);
-  const T re = R.v[1] / R.v[0] / (g - 1), rc = dsqrt(g * R.v[1] / R.v[0]);
-  const T lu = (L.v[2] * n.x + L.v[3] * n.y) / na, lv = (L.v[2] * p.x + L.v[3] * p.y) / pa;
-  const T ru = (R.v[2] * n.x + R.v[3] * n.y) / na, rv = (R.v[2] * p.x + R.v[3] * p.y) / pa;
+  const T le = quot(quot(L.v[1], L.v[0]), g - 1), lc = dsqrt(quot(g * L.v[1], L.v[0]));
+  const T re = quot(quot(R.v[1], R.v[0]), g - 1), rc = dsqrt(quot(g * R.v[1], R.v[0]));
+  const T lu = quot(L.v[2] * n.x + L.v[3] * n.y, na), lv = quot(L.v[2] * p.x + L.v[3] * p.y, pa);
+  const T ru = quot(R.v[2] * n.x + R.v[3] * n.y, na), rv = quot(R.v[2] * p.x + R.v[3] * p.y, pa);
   const T a1 = lu - lc, b1 = ru - rc, a2 = lu + lc, b2 = ru + rc;
   const T sl = val(b1) < val(a1) ? b1 : a1;
   const T sr = val(a2) < val(b2) ? b2 : a2;
@@ -309,8 +314,8 @@ __device__ bool face_flux(const AdjArgs& a, int e, const V4<T>& L, const V4<T>& 
   const T dsp = qd * qu;
   T fm = dsp, fmx = qp + qu * dsp, fmy = qv * dsp, fen = (ek + qp) * qu;
   if (use_left ? !(val(sl) > 0) : !(val(sr) < 0)) {
-    const T ds = qd * (sk - qu) / (sk - ss);
-    const T use = ek * ds / qd + ds * (ss - qu) * (ss + qp / qd / (sk - qu));
+    const T ds = quot(qd * (sk - qu), sk - ss);
+    const T use = quot(ek * ds, qd) + ds * (ss - qu) * (ss + quot(quot(qp, qd), sk - qu));
     fm = fm + sk * (ds - qd);
     fmx = fmx + (ds * ss - qu * qd) * sk;
     fmy = fmy + (ds * qv - qv * qd) * sk;
@@ -318,8 +323,8 @@ __device__ bool face_flux(const AdjArgs& a, int e, const V4<T>& L, const V4<T>& 
   }
   out[0] = fm;
   out[1] = fen;
-  out[2] = (n.x * fmx) / na + (p.x * fmy) / pa;
-  out[3] = (n.y * fmx) / na + (p.y * fmy) / pa;
+  out[2] = quot(n.x * fmx, na) + quot(p.x * fmy, pa);
+  out[3] = quot(n.y * fmx, na) + quot(p.y * fmy, pa);
   return true;
 }
 
@@ -384,21 +389,21 @@ __global__ void __launch_bounds__(kBlock) k_tl_update(AdjArgs a) {
   store_raw(a.dext, i, du[0], du[1], du[2], du[3]);
   const double V = m.cd_volume[i];
   const double mass = u[0], en = u[1];
-  const double d = mass / V;
+  const double d = quot(mass, V);
   if (d < 0) {
     record_error(a.status, 0, RG_ERR_NEGATIVE_DENSITY, 5, i, d);
     return;
   }
-  const double vx = u[2] / mass, vy = u[3] / mass;
-  const double energy = en / mass - 0.5 * (vx * vx + vy * vy);
+  const double vx = quot(u[2], mass), vy = quot(u[3], mass);
+  const double energy = quot(en, mass) - 0.5 * (vx * vx + vy * vy);
   if (energy < 0) {
     record_error(a.status, 0, RG_ERR_NEGATIVE_ENERGY, 5, i, energy);
     return;
   }
   store_raw(a.cells_out, i, d, (a.gamma - 1) * energy * d, vx, vy);
-  const double dd = du[0] / V;
-  const double dvx = (du[2] - vx * du[0]) / mass, dvy = (du[3] - vy * du[0]) / mass;
-  const double de = (du[1] - (en / mass) * du[0]) / mass - (vx * dvx + vy * dvy);
+  const double dd = quot(du[0], V);
+  const double dvx = quot(du[2] - vx * du[0], mass), dvy = quot(du[3] - vy * du[0], mass);
+  const double de = quot(du[1] - quot(en, mass) * du[0], mass) - (vx * dvx + vy * dvy);
   store_raw(a.dcells_out, i, dd, (a.gamma - 1) * (de * d + energy * dd), dvx, dvy);
 }
 
@@ -412,10 +417,10 @@ __global__ void __launch_bounds__(kBlock) k_tl_init(AdjArgs a) {
   const double V = a.mesh.cd_volume[i];
   const double mass = V * c[0];
   const double k2 = c[2] * c[2] + c[3] * c[3];
-  store_raw(a.ext_rw, i, mass, c[1] / c[0] / (a.gamma - 1) * mass + 0.5 * mass * k2, c[2] * mass, c[3] * mass);
+  store_raw(a.ext_rw, i, mass, quot(quot(c[1], c[0]), a.gamma - 1) * mass + 0.5 * mass * k2, c[2] * mass, c[3] * mass);
   const double dm = V * t[0];
   // E = V p / (gamma - 1) + V d |v|^2 / 2
-  const double dE = V * t[1] / (a.gamma - 1) + 0.5 * V * t[0] * k2 + V * c[0] * (c[2] * t[2] + c[3] * t[3]);
+  const double dE = quot(V * t[1], a.gamma - 1) + 0.5 * V * t[0] * k2 + V * c[0] * (c[2] * t[2] + c[3] * t[3]);
   store_raw(a.dext, i, dm, dE, t[2] * mass + c[2] * dm, t[3] * mass + c[3] * dm);
 }
 

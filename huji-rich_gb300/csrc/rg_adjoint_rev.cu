@@ -27,6 +27,7 @@
 #include <math.h>
 
 #include "rg_adjoint.cuh"
+#include "rg_div.cuh"
 
 #ifndef RG_ADJ_REAL
 #define RG_ADJ_REAL double
@@ -86,15 +87,15 @@ __global__ void __launch_bounds__(kBlock) k_adj_check(AdjArgs a) {
 __device__ __forceinline__ void cell_update_transpose(double gamma, double V, const double u[4], const double w[4],
                                                       double ub[4]) {
   const double mass = u[0], en = u[1];
-  const double d = mass / V, vx = u[2] / mass, vy = u[3] / mass;
-  const double e = en / mass - 0.5 * (vx * vx + vy * vy);
+  const double d = quot(mass, V), vx = quot(u[2], mass), vy = quot(u[3], mass);
+  const double e = quot(en, mass) - 0.5 * (vx * vx + vy * vy);
   const double be = w[1] * (gamma - 1) * d;
   const double bd = w[0] + w[1] * (gamma - 1) * e;
   const double bvx = w[2] - be * vx, bvy = w[3] - be * vy;
-  ub[0] += bd / V - (be * en / mass + bvx * vx + bvy * vy) / mass;
-  ub[1] += be / mass;
-  ub[2] += bvx / mass;
-  ub[3] += bvy / mass;
+  ub[0] += quot(bd, V) - quot(quot(be * en, mass) + bvx * vx + bvy * vy, mass);
+  ub[1] += quot(be, mass);
+  ub[2] += quot(bvx, mass);
+  ub[3] += quot(bvy, mass);
 }
 
 __global__ void __launch_bounds__(kBlock) k_adj_seed(AdjArgs a, const double* wbar, double* ubar) {
@@ -116,17 +117,17 @@ __device__ void hllc_reverse(real g, rv2 n, real na, rv2 p, real pa, const real 
                              const real fb[4], real lb[4], real rb[4]) {
   // forward values
   const real dL = L[0], pL = L[1], dR = R[0], pR = R[1];
-  const real eL = pL / dL / (g - real(1)), cL = sqrt(g * pL / dL);
-  const real eR = pR / dR / (g - real(1)), cR = sqrt(g * pR / dR);
-  const real lu = (L[2] * n.x + L[3] * n.y) / na, lv = (L[2] * p.x + L[3] * p.y) / pa;
-  const real ru = (R[2] * n.x + R[3] * n.y) / na, rv = (R[2] * p.x + R[3] * p.y) / pa;
+  const real eL = quot(quot(pL, dL), g - real(1)), cL = root(quot(g * pL, dL));
+  const real eR = quot(quot(pR, dR), g - real(1)), cR = root(quot(g * pR, dR));
+  const real lu = quot(L[2] * n.x + L[3] * n.y, na), lv = quot(L[2] * p.x + L[3] * p.y, pa);
+  const real ru = quot(R[2] * n.x + R[3] * n.y, na), rv = quot(R[2] * p.x + R[3] * p.y, pa);
   const bool sl_right = (ru - cR) < (lu - cL);
   const real sl = sl_right ? ru - cR : lu - cL;
   const bool sr_right = (lu + cL) < (ru + cR);
   const real sr = sr_right ? ru + cR : lu + cL;
   const real num = pR - pL + dL * lu * (sl - lu) - dR * ru * (sr - ru);
   const real den = dL * (sl - lu) - dR * (sr - ru);
-  const real ss = num / den;
+  const real ss = quot(num, den);
   const bool left = sl > 0 || (sl <= 0 && ss >= 0);
   const bool star = left ? !(sl > 0) : !(sr < 0);
   const real qd = left ? dL : dR, qp = left ? pL : pR, qe = left ? eL : eR;
@@ -135,17 +136,17 @@ __device__ void hllc_reverse(real g, rv2 n, real na, rv2 p, real pa, const real 
   const real ek = qd * (real(0.5) * k2 + qe);
   // adjoint of the face-frame flux {fm, fmx, fmy, fen}
   const real bfm = fb[0], bfen = fb[1];
-  const real bfmx = (n.x * fb[2] + n.y * fb[3]) / na;
-  const real bfmy = (p.x * fb[2] + p.y * fb[3]) / pa;
+  const real bfmx = quot(n.x * fb[2] + n.y * fb[3], na);
+  const real bfmy = quot(p.x * fb[2] + p.y * fb[3], pa);
   real bd = 0, bp = 0, bu = 0, bv = 0, be = 0, bek = 0, bsk = 0, bss = 0;
   if (star) {
     // ds = qd K/D, use = ek ds/qd + ds A B with K = sk - qu, D = sk - ss,
     // A = ss - qu, B = ss + Q, Q = qp/(qd K); fluxes gain sk*(u* - u)
     const real K = sk - qu, D = sk - ss;
-    const real ds = qd * K / D;
-    const real Q = qp / qd / K;
+    const real ds = quot(qd * K, D);
+    const real Q = quot(quot(qp, qd), K);
     const real A = ss - qu, B = ss + Q;
-    const real use = ek * ds / qd + ds * A * B;
+    const real use = quot(ek * ds, qd) + ds * A * B;
     bsk += bfm * (ds - qd) + bfmx * (ds * ss - qu * qd) + bfmy * (ds * qv - qv * qd) + bfen * (use - ek);
     real bds = (bfm + bfmx * ss + bfmy * qv) * sk;
     bd -= (bfm + bfmx * qu + bfmy * qv) * sk;
@@ -154,18 +155,18 @@ __device__ void hllc_reverse(real g, rv2 n, real na, rv2 p, real pa, const real 
     bss += bfmx * ds * sk;
     const real buse = bfen * sk;
     bek -= bfen * sk;
-    bek += buse * ds / qd;
-    bds += buse * (ek / qd + A * B);
-    bd -= buse * ek * ds / (qd * qd);
+    bek += quot(buse * ds, qd);
+    bds += buse * (quot(ek, qd) + A * B);
+    bd -= quot(buse * ek * ds, qd * qd);
     const real bA = buse * ds * B, bB = buse * ds * A;
     bss += bA + bB;
     bu -= bA;
-    bp += bB / (qd * K);
-    bd -= bB * Q / qd;
-    real bK = -bB * Q / K;
-    bd += bds * K / D;
-    bK += bds * qd / D;
-    const real bD = -bds * ds / D;
+    bp += quot(bB, qd * K);
+    bd -= quot(bB * Q, qd);
+    real bK = quot(-bB * Q, K);
+    bd += quot(bds * K, D);
+    bK += quot(bds * qd, D);
+    const real bD = quot(-bds * ds, D);
     bsk += bK + bD;
     bu -= bK;
     bss -= bD;
@@ -191,7 +192,7 @@ __device__ void hllc_reverse(real g, rv2 n, real na, rv2 p, real pa, const real 
     bdR = bd, bpR = bp, buR = bu, bvR = bv, beR = be, bsr = bsk;
   }
   // ss = num/den
-  const real bnum = bss / den, bden = -bss * ss / den;
+  const real bnum = quot(bss, den), bden = quot(-bss * ss, den);
   bpR += bnum;
   bpL -= bnum;
   bdL += bnum * lu * (sl - lu) + bden * (sl - lu);
@@ -216,19 +217,19 @@ __device__ void hllc_reverse(real g, rv2 n, real na, rv2 p, real pa, const real 
     bcL += bsr;
   }
   // e = p/(d (gamma-1)), c = sqrt(gamma p/d)
-  bpL += beL / (dL * (g - real(1))) + bcL * g / (real(2.0) * cL * dL);
-  bdL -= beL * eL / dL + bcL * cL / (real(2.0) * dL);
-  bpR += beR / (dR * (g - real(1))) + bcR * g / (real(2.0) * cR * dR);
-  bdR -= beR * eR / dR + bcR * cR / (real(2.0) * dR);
+  bpL += quot(beL, dL * (g - real(1))) + quot(bcL * g, real(2.0) * cL * dL);
+  bdL -= quot(beL * eL, dL) + quot(bcL * cL, real(2.0) * dL);
+  bpR += quot(beR, dR * (g - real(1))) + quot(bcR * g, real(2.0) * cR * dR);
+  bdR -= quot(beR * eR, dR) + quot(bcR * cR, real(2.0) * dR);
   // rotation into the face frame: u = v.n/|n|, v_t = v.par/|par|
   lb[0] = bdL;
   lb[1] = bpL;
-  lb[2] = buL * n.x / na + bvL * p.x / pa;
-  lb[3] = buL * n.y / na + bvL * p.y / pa;
+  lb[2] = quot(buL * n.x, na) + quot(bvL * p.x, pa);
+  lb[3] = quot(buL * n.y, na) + quot(bvL * p.y, pa);
   rb[0] = bdR;
   rb[1] = bpR;
-  rb[2] = buR * n.x / na + bvR * p.x / pa;
-  rb[3] = buR * n.y / na + bvR * p.y / pa;
+  rb[2] = quot(buR * n.x, na) + quot(bvR * p.x, pa);
+  rb[3] = quot(buR * n.y, na) + quot(bvR * p.y, pa);
 }
 
 __device__ __forceinline__ void face_state(const AdjArgs& a, int pid, rv2 dm, real c[4]) {
@@ -316,7 +317,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_cell(AdjArgs a) {
     const real nx = static_cast<real>(tr.naive[q]), ny = static_cast<real>(tr.naive[4 + q]);
     const real bpsi = bx[q] * nx + by[q] * ny;
     const real D = static_cast<real>(tr.dphi[q]);
-    const real bN = bpsi / D, bD = -bpsi * psi / D;
+    const real bN = quot(bpsi, D), bD = quot(-bpsi * psi, D);
     const int e = m.cell_faces[b + k];
     const rv2 dm = r2((a.geom.nbr[b + k] & kNbrFirst) ? a.geom.dm0[e] : a.geom.dm1[e]);
     bnx[q] += bD * dm.x;
@@ -378,7 +379,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_update(AdjArgs a, const double* 
     const double mass = V * c[0];
     double g[4];
     g[0] = w[0] + V * (ub[0] + 0.5 * k2 * ub[1] + c[2] * ub[2] + c[3] * ub[3]);
-    g[1] = w[1] + V / (a.gamma - 1) * ub[1];
+    g[1] = w[1] + quot(V, a.gamma - 1) * ub[1];
     g[2] = w[2] + mass * (c[2] * ub[1] + ub[2]);
     g[3] = w[3] + mass * (c[3] * ub[1] + ub[3]);
     store_raw(grad, i, g);
