@@ -52,6 +52,15 @@ RG_CONV_FN float conv_float(uint32_t u) {
   return f;
 #endif
 }
+RG_CONV_FN double conv_double_bits(uint64_t u) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double(static_cast<long long>(u));
+#else
+  double d;
+  memcpy(&d, &u, 8);
+  return d;
+#endif
+}
 RG_CONV_FN double conv_double(uint32_t hi, uint32_t lo) {
 #ifdef __CUDA_ARCH__
   return __hiloint2double(static_cast<int>(hi), static_cast<int>(lo));
@@ -139,15 +148,20 @@ RG_CONV_FN int64_t order_key(uint64_t u) {
   return (u >> 63) ? -m : m;
 }
 RG_CONV_FN bool nan_bits(uint64_t u) { return (u & kMagMask) > kInfBits64; }
-// a < b (false when either is NaN; -0 == +0)
-RG_CONV_FN bool lt(double a, double b) {
-  const uint64_t ua = conv_dbits(a), ub = conv_dbits(b);
+// a < b on the bit patterns of two doubles (false when either is NaN; -0 == +0)
+RG_CONV_FN bool lt_u(uint64_t ua, uint64_t ub) {
   return !nan_bits(ua) && !nan_bits(ub) && order_key(ua) < order_key(ub);
 }
+RG_CONV_FN bool lt(double a, double b) { return lt_u(conv_dbits(a), conv_dbits(b)); }
 // std::max(a, b) = a < b ? b : a and std::min(a, b) = b < a ? b : a, bit for
-// bit (the first operand on equality, -0 against +0 and NaN included)
+// bit (the first operand on equality, -0 against +0 and NaN included).  The
+// _u forms select between bit patterns, so that no FP64 instruction moves
+// the chosen value.
+RG_CONV_FN uint64_t max_first_u(uint64_t a, uint64_t b) { return lt_u(a, b) ? b : a; }
+RG_CONV_FN uint64_t min_first_u(uint64_t a, uint64_t b) { return lt_u(b, a) ? b : a; }
 RG_CONV_FN double max_first(double a, double b) { return lt(a, b) ? b : a; }
 RG_CONV_FN double min_first(double a, double b) { return lt(b, a) ? b : a; }
+RG_CONV_FN uint64_t abs_u(double a) { return conv_dbits(a) & kMagMask; }
 
 // t / 3 rounded to nearest (t >= 0) without a division.  RN(1/3) is 1/3
 // less 2^-54 of itself, so q = RN(t * RN(1/3)) is within one ulp of t/3,

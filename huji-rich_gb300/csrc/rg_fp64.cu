@@ -383,33 +383,37 @@ __device__ __forceinline__ void k_slopes_item(const StepArgs& a, int i) {
       }
     }
     if (a.shock) a.shock[i] = shock ? 1 : 0;
-    Cell cmax = cell, cmin = cell;
+    // neighbour extrema as bit patterns (std::max / std::min on the integer pipe)
+    uint64_t mx[4] = {conv_dbits(cell.d), conv_dbits(cell.p), conv_dbits(cell.vx), conv_dbits(cell.vy)};
+    uint64_t mn[4] = {mx[0], mx[1], mx[2], mx[3]};
     for (int k = 0; k < nn; ++k) {
       const uint32_t w = a.geom.nbr[b + k];
       if (!shock && (w & kNbrMirror)) continue;  // :194-195 skips self-mirror neighbours
       if (skipped(a, static_cast<int>(w & kNbrIdMask))) continue;  // :192-193, :314-315 skip_key
       const Cell nb = point_state(a, static_cast<int>(w & kNbrIdMask));
-      cmax.d = max_first(cmax.d, nb.d);
-      cmax.p = max_first(cmax.p, nb.p);
-      cmax.vx = max_first(cmax.vx, nb.vx);
-      cmax.vy = max_first(cmax.vy, nb.vy);
-      cmin.d = min_first(cmin.d, nb.d);
-      cmin.p = min_first(cmin.p, nb.p);
-      cmin.vx = min_first(cmin.vx, nb.vx);
-      cmin.vy = min_first(cmin.vy, nb.vy);
+      const uint64_t nbb[4] = {conv_dbits(nb.d), conv_dbits(nb.p), conv_dbits(nb.vx), conv_dbits(nb.vy)};
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        mx[q] = max_first_u(mx[q], nbb[q]);
+        mn[q] = min_first_u(mn[q], nbb[q]);
+      }
     }
-    const Cell maxd{cmax.d - cell.d, cmax.p - cell.p, cmax.vx - cell.vx, cmax.vy - cell.vy};
-    const Cell mind{cmin.d - cell.d, cmin.p - cell.p, cmin.vx - cell.vx, cmin.vy - cell.vy};
+    const Cell maxd{conv_double_bits(mx[0]) - cell.d, conv_double_bits(mx[1]) - cell.p,
+                    conv_double_bits(mx[2]) - cell.vx, conv_double_bits(mx[3]) - cell.vy};
+    const Cell mind{conv_double_bits(mn[0]) - cell.d, conv_double_bits(mn[1]) - cell.p,
+                    conv_double_bits(mn[2]) - cell.vx, conv_double_bits(mn[3]) - cell.vy};
     const double f = shock ? 0.1 : 0.05;
-    const Cell thr{f * max_first(fabs(maxd.d), fabs(mind.d)), f * max_first(fabs(maxd.p), fabs(mind.p)),
-                   f * max_first(fabs(maxd.vx), fabs(mind.vx)), f * max_first(fabs(maxd.vy), fabs(mind.vy))};
-    double psi0 = 1, psi1 = 1, psi2 = 1, psi3 = 1;
+    const Cell thr{f * conv_double_bits(max_first_u(abs_u(maxd.d), abs_u(mind.d))),
+                   f * conv_double_bits(max_first_u(abs_u(maxd.p), abs_u(mind.p))),
+                   f * conv_double_bits(max_first_u(abs_u(maxd.vx), abs_u(mind.vx))),
+                   f * conv_double_bits(max_first_u(abs_u(maxd.vy), abs_u(mind.vy)))};
+    uint64_t psi0 = kOneBits, psi1 = kOneBits, psi2 = kOneBits, psi3 = kOneBits;
     float pf0 = 1, pf1 = 1, pf2 = 1, pf3 = 1;
     for (int k = 0; k < nn; ++k) {
       const uint32_t w = a.geom.nbr[b + k];
       if (shock && skipped(a, static_cast<int>(w & kNbrIdMask))) continue;  // :339-340
       const int e = m.cell_faces[b + k];
-      const double2 dm = (w & kNbrFirst) ? a.geom.dm0[e] : a.geom.dm1[e];
+      const double2 dm = centroid_offset(a.geom, w, e);
       Cell cv = cell;
       addmult(cv, sx, dm.x);
       addmult(cv, sy, dm.y);
@@ -429,10 +433,12 @@ __device__ __forceinline__ void k_slopes_item(const StepArgs& a, int i) {
         shocked_comp(dphi.vy, cv.vy, cell.vy, thr.vy, nb.vy, a.theta, psi3, pf3);
       }
     }
-    sx.d *= psi0; sy.d *= psi0;
-    sx.p *= psi1; sy.p *= psi1;
-    sx.vx *= psi2; sy.vx *= psi2;
-    sx.vy *= psi3; sy.vy *= psi3;
+    const double p0 = conv_double_bits(psi0), p1 = conv_double_bits(psi1), p2 = conv_double_bits(psi2),
+                 p3 = conv_double_bits(psi3);
+    sx.d *= p0; sy.d *= p0;
+    sx.p *= p1; sy.p *= p1;
+    sx.vx *= p2; sy.vx *= p2;
+    sx.vy *= p3; sy.vy *= p3;
   }
   double2* o = reinterpret_cast<double2*>(a.slopes) + 4 * i;
   o[0] = make_double2(sx.d, sx.p);

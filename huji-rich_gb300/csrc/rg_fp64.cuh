@@ -67,6 +67,10 @@ __device__ __forceinline__ void fill_ghost(const StepArgs& a, int g) {
 __device__ __forceinline__ Cell point_state(const StepArgs& a, int p) {
   return p < a.mesh.n ? load_cell(a.cells, p) : ghost_state(a, p - a.mesh.n);
 }
+// dm0[e] or dm1[e] (centroid minus the first / second cell's CM), chosen by pointer
+__device__ __forceinline__ double2 centroid_offset(const GeomDev& g, uint32_t w, int e) {
+  return ((w & kNbrFirst) ? g.dm0 : g.dm1)[e];
+}
 
 // The cell whose tracers and stickers point p carries: p itself, or the
 // cell a ghost copies (RigidWallGenerator.cpp:17-37 and
@@ -94,21 +98,26 @@ __device__ __forceinline__ double step_dt(const StepArgs& a) {
 // sign-of-product tests run on the integer pipe (rg_convert.cuh).
 __device__ __forceinline__ bool fp32_safe(double a) { return abs_within(a, 1e-36, 1e36); }
 
+// The limiter's running minimum psi is carried as its bit pattern (selections
+// on the integer pipe) with psi_f = float(psi) beside it.
+constexpr uint64_t kOneBits = 0x3ff0000000000000ull;  // 1.0
+
 // psi_f = float(psi) is a usable screen when psi is 0 or a normal float.
-__device__ __forceinline__ bool psi_screenable(double psi, float psi_f) {
-  return psi_f >= 1e-30f || (conv_dbits(psi) & kMagMask) == 0u;
+__device__ __forceinline__ bool psi_screenable(uint64_t psi, float psi_f) {
+  return psi_f >= 1e-30f || (psi & kMagMask) == 0u;
 }
 
 // smin(psi, num/den) for num/den >= 0 (or NaN, which smin ignores), psi >= 0:
 // skips the division when the quotient is provably >= psi.
-__device__ __forceinline__ void min_quotient(double num, double den, double& psi, float& psi_f) {
+__device__ __forceinline__ void min_quotient(double num, double den, uint64_t& psi, float& psi_f) {
   if (fp32_safe(num) && fp32_safe(den) && psi_screenable(psi, psi_f)) {
     const float qf = narrow(num) / narrow(den);
     if (qf >= psi_f * 1.000001f) return;
   }
   const double q = quot(num, den);
-  if (lt(q, psi)) {
-    psi = q;
+  const uint64_t uq = conv_dbits(q);
+  if (lt_u(uq, psi)) {
+    psi = uq;
     psi_f = narrow(q);
   }
 }
@@ -119,12 +128,13 @@ __device__ __forceinline__ void min_quotient(double num, double den, double& psi
 // (rg_convert.cuh); the lower threshold -1e-9*q (or -|1e-9*q|) is exactly
 // the negated upper one, the rounding being sign-symmetric.
 __device__ __forceinline__ void limit_comp(double dphi, double cv, double cellv, double thr, double maxd,
-                                           double mind, bool use_abs, double& psi, float& psi_f) {
+                                           double mind, bool use_abs, uint64_t& psi, float& psi_f) {
   if (abs_gt(dphi, thr) || prod_neg(cv, cellv)) {
-    const double t1 = use_abs ? fabs(1e-9 * cellv) : 1e-9 * cellv;
-    if (lt(t1, dphi))
+    const uint64_t t1 = use_abs ? abs_u(1e-9 * cellv) : conv_dbits(1e-9 * cellv);
+    const uint64_t ud = conv_dbits(dphi);
+    if (lt_u(t1, ud))
       min_quotient(maxd, dphi, psi, psi_f);
-    else if (lt(dphi, -t1))
+    else if (lt_u(ud, t1 ^ 0x8000000000000000ull))
       min_quotient(mind, dphi, psi, psi_f);
   }
 }
@@ -133,17 +143,17 @@ __device__ __forceinline__ void limit_comp(double dphi, double cv, double cellv,
 // (threshold 1e-9*q without abs for every hydro component, as the reference
 // has it; |1e-9*q| for tracers, :377): psi = smin(psi, smax(theta*(nb-cell)/dphi, 0)).
 __device__ __forceinline__ void shocked_comp(double dphi, double cv, double cellv, double thr, double nbv,
-                                             double theta, double& psi, float& psi_f, bool abs_thr = false) {
+                                             double theta, uint64_t& psi, float& psi_f, bool abs_thr = false) {
   if (abs_gt(dphi, thr) || prod_neg(cv, cellv)) {
-    if (lt(abs_thr ? fabs(1e-9 * cellv) : 1e-9 * cellv, fabs(dphi))) {
+    if (lt_u(abs_thr ? abs_u(1e-9 * cellv) : conv_dbits(1e-9 * cellv), abs_u(dphi))) {
       const double num = theta * (nbv - cellv);
       const uint64_t un = conv_dbits(num), ud = conv_dbits(dphi);
       // num != 0, neither NaN, (num < 0) != (dphi < 0)
       const bool num_neg = (un >> 63) != 0u, dphi_neg = (ud >> 63) != 0u && (ud & kMagMask) != 0u;
       if ((un & kMagMask) != 0u && !nan_bits(un) && !nan_bits(ud) && num_neg != dphi_neg) {
         // negative quotient: smax(., 0) gives 0
-        if (lt(0.0, psi)) {
-          psi = 0.0;
+        if (lt_u(0u, psi)) {
+          psi = 0u;
           psi_f = 0.0f;
         }
         return;
@@ -152,10 +162,11 @@ __device__ __forceinline__ void shocked_comp(double dphi, double cv, double cell
         const float qf = narrow(num) / narrow(dphi);
         if (qf >= psi_f * 1.000001f) return;
       }
-      const double x = max_first(quot(num, dphi), 0.0);
-      if (lt(x, psi)) {
-        psi = x;
-        psi_f = narrow(x);
+      const double q = quot(num, dphi);
+      const uint64_t ux = max_first_u(conv_dbits(q), 0u);
+      if (lt_u(ux, psi)) {
+        psi = ux;
+        psi_f = narrow(conv_double_bits(ux));
       }
     }
   }

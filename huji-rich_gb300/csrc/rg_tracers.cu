@@ -110,9 +110,9 @@ __global__ void __launch_bounds__(kTrBlock) k_tr_slopes(StepArgs a, TracerArgs t
     if (!((t.limited >> j) & 1u)) sx[j] = sy[j] = 0.0;
   if (a.slf) {
     const bool shock = a.shock[i] != 0;
-    double cmax[kMaxTracers], cmin[kMaxTracers];
+    uint64_t cmax[kMaxTracers], cmin[kMaxTracers];  // bit patterns
 #pragma unroll
-    for (int j = 0; j < kMaxTracers; ++j) cmax[j] = cmin[j] = ct[j];
+    for (int j = 0; j < kMaxTracers; ++j) cmax[j] = cmin[j] = conv_dbits(ct[j]);
     for (int k = 0; k < nn; ++k) {
       const uint32_t w = a.geom.nbr[b + k];
       if (!shock && (w & kNbrMirror)) continue;  // :194-195
@@ -121,20 +121,21 @@ __global__ void __launch_bounds__(kTrBlock) k_tr_slopes(StepArgs a, TracerArgs t
 #pragma unroll
       for (int j = 0; j < kMaxTracers; ++j) {
         if (j < nt) {
-          cmax[j] = max_first(cmax[j], nb[j]);
-          cmin[j] = min_first(cmin[j], nb[j]);
+          cmax[j] = max_first_u(cmax[j], conv_dbits(nb[j]));
+          cmin[j] = min_first_u(cmin[j], conv_dbits(nb[j]));
         }
       }
     }
     const double f = shock ? 0.1 : 0.05;
-    double maxd[kMaxTracers], mind[kMaxTracers], thr[kMaxTracers], psi[kMaxTracers];
+    double maxd[kMaxTracers], mind[kMaxTracers], thr[kMaxTracers];
+    uint64_t psi[kMaxTracers];
     float pf[kMaxTracers];
 #pragma unroll
     for (int j = 0; j < kMaxTracers; ++j) {
-      maxd[j] = cmax[j] - ct[j];
-      mind[j] = cmin[j] - ct[j];
-      thr[j] = f * max_first(fabs(maxd[j]), fabs(mind[j]));
-      psi[j] = 1.0;
+      maxd[j] = conv_double_bits(cmax[j]) - ct[j];
+      mind[j] = conv_double_bits(cmin[j]) - ct[j];
+      thr[j] = f * conv_double_bits(max_first_u(abs_u(maxd[j]), abs_u(mind[j])));
+      psi[j] = kOneBits;
       pf[j] = 1.0f;
     }
     for (int k = 0; k < nn; ++k) {
@@ -142,7 +143,7 @@ __global__ void __launch_bounds__(kTrBlock) k_tr_slopes(StepArgs a, TracerArgs t
       const int other = static_cast<int>(w & kNbrIdMask);
       if (shock && skipped(a, other)) continue;  // :339-340
       const int e = m.cell_faces[b + k];
-      const double2 dm = (w & kNbrFirst) ? a.geom.dm0[e] : a.geom.dm1[e];
+      const double2 dm = centroid_offset(a.geom, w, e);
       const double* nb = tracers_of(a, t, other);
 #pragma unroll
       for (int j = 0; j < kMaxTracers; ++j) {
@@ -160,8 +161,8 @@ __global__ void __launch_bounds__(kTrBlock) k_tr_slopes(StepArgs a, TracerArgs t
     }
 #pragma unroll
     for (int j = 0; j < kMaxTracers; ++j) {
-      sx[j] *= psi[j];
-      sy[j] *= psi[j];
+      sx[j] *= conv_double_bits(psi[j]);
+      sy[j] *= conv_double_bits(psi[j]);
     }
   }
   double* o = t.tr_slopes + static_cast<size_t>(i) * 2 * nt;
