@@ -322,17 +322,22 @@ __device__ __forceinline__ void k_slopes_item(const StepArgs& a, int i) {
               quot(phisx.vx * sxsy - phisy.vx * sx2, den), quot(phisx.vy * sxsy - phisy.vy * sx2, den)};
   } else {
     // :80-133 calc_naive_slope, right-hand side and solve
+    // the first neighbour starts the sums (cell*h, then + nb*h); the loop
+    // takes the rest, so no iteration joins two computed values
     Cell vx{0, 0, 0, 0}, vy{0, 0, 0, 0};
-    for (int k = 0; k < nn; ++k) {
+    if (nn > 0) {
+      const Cell nb = point_state(a, static_cast<int>(a.geom.nbr[b] & kNbrIdMask));
+      const double2 h = a.geom.hr[b];
+      vx = Cell{cell.d * h.x, cell.p * h.x, cell.vx * h.x, cell.vy * h.x};
+      vy = Cell{cell.d * h.y, cell.p * h.y, cell.vx * h.y, cell.vy * h.y};
+      addmult(vy, nb, h.y);
+      addmult(vx, nb, h.x);
+    }
+    for (int k = 1; k < nn; ++k) {
       const Cell nb = point_state(a, static_cast<int>(a.geom.nbr[b + k] & kNbrIdMask));
       const double2 h = a.geom.hr[b + k];
-      if (k == 0) {
-        vx = Cell{cell.d * h.x, cell.p * h.x, cell.vx * h.x, cell.vy * h.x};
-        vy = Cell{cell.d * h.y, cell.p * h.y, cell.vx * h.y, cell.vy * h.y};
-      } else {
-        addmult(vx, cell, h.x);
-        addmult(vy, cell, h.y);
-      }
+      addmult(vx, cell, h.x);
+      addmult(vy, cell, h.y);
       addmult(vy, nb, h.y);
       addmult(vx, nb, h.x);
     }
