@@ -686,10 +686,13 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t flags) {
       return invalid(h, static_cast<int64_t>(hs->err_key & rg::kKeyIndexMask), hs->err_value);
     }
   }
-  // geometry pass on the upload stream
+  // geometry pass on the upload stream (the per-cell kernels take cells in
+  // the per-tile neighbour-count order, computed first)
   RG_TRY(reset_status(h, h->d_geom_status, h->upload_stream));
+  RG_CUDA(h, rg::launch_cell_order(s.mesh, at<int>(s.buf.p, s.lay.cell_order), at<int>(s.buf.p, s.lay.cflags),
+                                   h->upload_stream));
   if (device_geometry)
-    RG_CUDA(h, rg::launch_device_geometry(s.mesh, at<double2>(s.buf.p, s.lay.cms), at<double>(s.buf.p, s.lay.volume),
+    RG_CUDA(h, rg::launch_device_geometry(s.mesh, at<int>(s.buf.p, s.lay.cell_order), at<double2>(s.buf.p, s.lay.cms), at<double>(s.buf.p, s.lay.volume),
                                           at<double>(s.buf.p, s.lay.cd_volume), h->cfg.ghost_kind, h->box,
                                           h->upload_stream));
   if (h->pgeo.kind == RG_GEOMETRY_CYLINDRICAL)

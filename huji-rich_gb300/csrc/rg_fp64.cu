@@ -37,7 +37,8 @@ __global__ void __launch_bounds__(kBlock) k_geom_faces(GeomArgs a) {
   const int2 fc = a.mesh.face_cells[e];
   const dbl4 v = a.mesh.face_vertices[e];
   const double ax = v.x - v.z, ay = v.y - v.w;
-  a.area[e] = root(ax * ax + ay * ay);
+  const double area = root(ax * ax + ay * ay);
+  a.area[e] = area;
   const double2 p = make_double2(v.z - v.x, v.w - v.y);
   a.par[e] = p;
   const double2 mid = make_double2((v.x + v.z) * 0.5, (v.y + v.w) * 0.5);
@@ -73,8 +74,8 @@ __global__ void __launch_bounds__(kBlock) k_geom_faces(GeomArgs a) {
   const double ddx = x1.x - x0.x, ddy = x1.y - x0.y;
   const double dab = root(ddx * ddx + ddy * ddy);
   a.dab[e] = dab;
-  const double len = a.area[e];  // Edge::GetLength = |second - first| = |first - second|
-  a.rij[e] = make_double2(quot(ddx, dab) * len, quot(ddy, dab) * len);
+  // Edge::GetLength = |second - first| = |first - second| = area
+  a.rij[e] = make_double2(quot(ddx, dab) * area, quot(ddy, dab) * area);
   a.cij[e] = make_double2(mid.x - (c1.x + c0.x) * 0.5, mid.y - (c1.y + c0.y) * 0.5);
 }
 
@@ -82,26 +83,24 @@ __global__ void __launch_bounds__(kBlock) k_geom_faces(GeomArgs a) {
 // state-independent half of calc_naive_slope (LinearGaussImproved.cpp:67-126:
 // matrix, determinant check, inverse, 0.5*r_ij) or of GetBoundarySlope (:401-417).
 __global__ void __launch_bounds__(kBlock) k_geom_cells(GeomArgs a) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const MeshDev& m = a.mesh;
-  if (i >= m.n) return;
+  if (t >= m.n) return;
+  const int i = a.cell_order ? a.cell_order[t] : t;
   a.width[i] = root(quot(m.volume[i], kPi));
   const int b = m.cell_off[i], nn = m.cell_off[i + 1] - b;
-  bool bslope = false;
-  for (int k = 0; k < nn; ++k) {
-    const int e = m.cell_faces[b + k];
-    const int2 fc = m.face_cells[e];
-    const bool first = fc.x == i;
-    const int other = first ? fc.y : fc.x;
-    const bool mirror = orig_of(m, fc.x) == orig_of(m, fc.y);
-    bslope |= mirror;
-    a.nbr[b + k] = static_cast<uint32_t>(other) | (mirror ? kNbrMirror : 0u) | (first ? kNbrFirst : 0u);
-  }
-  const double2 cci = m.cms[i];
-  if (bslope) {
+  // k_cell_order has set the boundary-slope flag (a face between a point and
+  // its own mirror image); one pass over the faces writes the neighbour words
+  // and the flag's half of the slope
+  if (a.cflags[i] & kCellBoundarySlope) {
+    const double2 cci = m.cms[i];
     double sxsy = 0, sy2 = 0, sx2 = 0;
     for (int k = 0; k < nn; ++k) {
-      const int other = static_cast<int>(a.nbr[b + k] & kNbrIdMask);
+      const int2 fc = m.face_cells[m.cell_faces[b + k]];
+      const bool first = fc.x == i;
+      const int other = first ? fc.y : fc.x;
+      const bool mirror = orig_of(m, fc.x) == orig_of(m, fc.y);
+      a.nbr[b + k] = static_cast<uint32_t>(other) | (mirror ? kNbrMirror : 0u) | (first ? kNbrFirst : 0u);
       const double2 co = m.cms[other];
       const double dx = co.x - cci.x, dy = co.y - cci.y;
       a.hr[b + k] = make_double2(dx, dy);
@@ -110,21 +109,29 @@ __global__ void __launch_bounds__(kBlock) k_geom_cells(GeomArgs a) {
       sy2 += dy * dy;
     }
     a.minv[i] = make_dbl4(sxsy, sx2, sy2, sxsy * sxsy - sx2 * sy2);
-    a.cflags[i] = kCellBoundarySlope;
     return;
   }
-  a.cflags[i] = 0;
   if (nn > kMaxNaiveNeighbours) {
     record_error(a.status, 0, RG_ERR_TOO_MANY_NEIGHBORS, 2, i, nn);
     a.minv[i] = make_dbl4(0, 0, 0, 0);
+    for (int k = 0; k < nn; ++k) {
+      const int2 fc = m.face_cells[m.cell_faces[b + k]];
+      const bool first = fc.x == i;
+      a.nbr[b + k] = static_cast<uint32_t>(first ? fc.y : fc.x) | (first ? kNbrFirst : 0u);
+    }
     return;
   }
+  // no neighbour of this cell is a mirror image of it
   double m0 = 0, m1 = 0, m2 = 0, m3 = 0;
   for (int k = 0; k < nn; ++k) {
     const int e = m.cell_faces[b + k];
-    const bool first = (a.nbr[b + k] & kNbrFirst) != 0;
+    const int2 fc = m.face_cells[e];
+    const bool first = fc.x == i;
+    a.nbr[b + k] = static_cast<uint32_t>(first ? fc.y : fc.x) | (first ? kNbrFirst : 0u);
     const double2 r = a.rij[e], c = a.cij[e];
-    const double rx = first ? r.x : -r.x, ry = first ? r.y : -r.y;
+    // -r_ij for the second cell: a sign flip of the bit pattern
+    const uint64_t flip = first ? 0u : 0x8000000000000000ull;
+    const double rx = conv_double_bits(conv_dbits(r.x) ^ flip), ry = conv_double_bits(conv_dbits(r.y) ^ flip);
     m0 -= c.x * rx;
     m1 -= c.y * rx;
     m2 -= c.x * ry;
@@ -162,19 +169,29 @@ __global__ void __launch_bounds__(kBlock) k_geom_ghosts(GeomArgs a) {
   a.ghost_unit[g] = make_double2(quot(nr.x, ab), quot(nr.y, ab));
 }
 
-// Per tile of kOrderTile cells: the order in which the FP64 slopes and update
-// kernels take them, by (boundary-slope flag, neighbour count) and then by
-// index.  Their per-cell loops run over a cell's neighbours, so a warp whose
-// cells have equal counts runs no lane idle; every cell is still computed by
-// one thread from the same inputs, so the results do not depend on the order.
-__global__ void __launch_bounds__(kOrderTile) k_cell_order(GeomArgs a) {
+// Per tile of kOrderTile cells: the order in which the per-cell FP64 kernels
+// (device geometry, the per-cell geometry pass, slopes, update) take them, by
+// (boundary-slope flag, neighbour count) and then by index.  Their per-cell
+// loops run over a cell's neighbours, so a warp whose cells have equal counts
+// runs no lane idle; every cell is still computed by one thread from the same
+// inputs, so the results do not depend on the order.  The flag is
+// LinearGaussImproved's (a face between a point and its own mirror image),
+// taken from the topology and stored as the cell's flag for the per-cell
+// geometry pass; runs after the index validation.
+__global__ void __launch_bounds__(kOrderTile) k_cell_order(MeshDev m, int* order, int* cflags) {
   __shared__ int key[kOrderTile];
   const int t = threadIdx.x, base = blockIdx.x * kOrderTile, i = base + t;
-  const int n = a.mesh.n, count = n - base < kOrderTile ? n - base : kOrderTile;
+  const int n = m.n, count = n - base < kOrderTile ? n - base : kOrderTile;
   int k = 0;
   if (i < n) {
-    const int nn = a.mesh.cell_off[i + 1] - a.mesh.cell_off[i];
-    k = (nn < 0 ? 0 : (nn > 63 ? 63 : nn)) | ((a.cflags[i] & kCellBoundarySlope) ? 64 : 0);
+    const int b = m.cell_off[i], nn = m.cell_off[i + 1] - b;
+    bool mirror = false;
+    for (int j = 0; j < nn; ++j) {
+      const int2 fc = m.face_cells[m.cell_faces[b + j]];
+      mirror |= orig_of(m, fc.x) == orig_of(m, fc.y);
+    }
+    k = (nn < 0 ? 0 : (nn > 63 ? 63 : nn)) | (mirror ? 64 : 0);
+    cflags[i] = mirror ? kCellBoundarySlope : 0;
   }
   key[t] = k;
   __syncthreads();
@@ -184,7 +201,7 @@ __global__ void __launch_bounds__(kOrderTile) k_cell_order(GeomArgs a) {
     const int kj = key[j];
     rank += (kj < k || (kj == k && j < t)) ? 1 : 0;
   }
-  a.cell_order[base + rank] = i;
+  order[base + rank] = i;
 }
 
 // Index validation of an uploaded mesh, before any kernel indexes with it.
@@ -1020,10 +1037,14 @@ cudaError_t launch_validate(const MeshDev& m, DevStatus* st, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+cudaError_t launch_cell_order(const MeshDev& m, int* order, int* cflags, cudaStream_t s) {
+  if (m.n > 0) k_cell_order<<<(m.n + kOrderTile - 1) / kOrderTile, kOrderTile, 0, s>>>(m, order, cflags);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_geometry(const GeomArgs& a, cudaStream_t s) {
   if (a.mesh.e > 0) k_geom_faces<<<blocks(a.mesh.e), kBlock, 0, s>>>(a);
   if (a.mesh.n > 0) k_geom_cells<<<blocks(a.mesh.n), kBlock, 0, s>>>(a);
-  if (a.mesh.n > 0 && a.cell_order) k_cell_order<<<(a.mesh.n + kOrderTile - 1) / kOrderTile, kOrderTile, 0, s>>>(a);
   if (a.mesh.g > 0) k_geom_ghosts<<<blocks(a.mesh.g), kBlock, 0, s>>>(a);
   return cudaGetLastError();
 }

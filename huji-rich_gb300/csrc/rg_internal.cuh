@@ -324,6 +324,7 @@ cudaError_t launch_any_nonzero(const double* v, long long n, int* flag, cudaStre
 cudaError_t launch_validate(const MeshDev& m, DevStatus* st, cudaStream_t s);
 cudaError_t launch_problems(const MeshDev& m, const int* offsets, int P, int* cell_problem, DevStatus* st,
                             cudaStream_t s);
+cudaError_t launch_cell_order(const MeshDev& m, int* order, int* cflags, cudaStream_t s);
 cudaError_t launch_geometry(const GeomArgs& a, cudaStream_t s);
 cudaError_t launch_cfl(const StepArgs& a, cudaStream_t s, bool fill_ghosts);
 cudaError_t launch_ghost_fill(const StepArgs& a, cudaStream_t s);

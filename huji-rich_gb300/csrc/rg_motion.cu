@@ -32,25 +32,29 @@ __device__ __forceinline__ double half_cross(double2 p1, double2 p2) {
   return 0.5 * fabs(p1.x * p2.y + p1.y * (-p2.x));
 }
 
-__global__ void __launch_bounds__(kMoBlock) k_dev_geometry(MeshDev m, double2* cms, double* volume,
-                                                            double* cd_volume) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= m.n) return;
+// Cells taken in `order` (per tile by neighbour count; null: thread i, cell i).
+__global__ void __launch_bounds__(kMoBlock) k_dev_geometry(MeshDev m, const int* order, double2* cms,
+                                                            double* volume, double* cd_volume) {
+  const int th = blockIdx.x * blockDim.x + threadIdx.x;
+  if (th >= m.n) return;
+  const int i = order ? order[th] : th;
   const int b = m.cell_off[i], e1 = m.cell_off[i + 1];
   const double2 c = m.points[i];
   // one pass over the faces: the volume's fan from the mesh point and the
   // CM's fan from the first face's first vertex, each summed in face order
+  // (the first face starts the volume's sum and fixes the CM's anchor)
   double area = 0;
   double2 pc = make_double2(0, 0);
   double a2 = 0;
   double2 an = make_double2(0, 0);
-  for (int k = b; k < e1; ++k) {
+  if (b < e1) {
+    const dbl4 v = m.face_vertices[m.cell_faces[b]];
+    area += half_cross(make_double2(v.x - c.x, v.y - c.y), make_double2(v.z - c.x, v.w - c.y));
+    an = make_double2(v.x, v.y);
+  }
+  for (int k = b + 1; k < e1; ++k) {
     const dbl4 v = m.face_vertices[m.cell_faces[k]];
     area += half_cross(make_double2(v.x - c.x, v.y - c.y), make_double2(v.z - c.x, v.w - c.y));
-    if (k == b) {
-      an = make_double2(v.x, v.y);
-      continue;
-    }
     const double t = half_cross(make_double2(v.x - an.x, v.y - an.y), make_double2(v.z - an.x, v.w - an.y));
     a2 += t;
     const double s = third_of(t);
@@ -242,9 +246,9 @@ inline int mo_blocks(int n) { return (n + kMoBlock - 1) / kMoBlock; }
 
 }  // namespace
 
-cudaError_t launch_device_geometry(const MeshDev& m, double2* cms, double* volume, double* cd_volume,
-                                   int ghost_kind, const double* box, cudaStream_t s) {
-  if (m.n > 0) k_dev_geometry<<<mo_blocks(m.n), kMoBlock, 0, s>>>(m, cms, volume, cd_volume);
+cudaError_t launch_device_geometry(const MeshDev& m, const int* order, double2* cms, double* volume,
+                                   double* cd_volume, int ghost_kind, const double* box, cudaStream_t s) {
+  if (m.n > 0) k_dev_geometry<<<mo_blocks(m.n), kMoBlock, 0, s>>>(m, order, cms, volume, cd_volume);
   if (m.g > 0) k_ghost_cms<<<mo_blocks(m.g), kMoBlock, 0, s>>>(m, cms, ghost_kind, make_dbl4(box[0], box[1], box[2], box[3]));
   return cudaGetLastError();
 }

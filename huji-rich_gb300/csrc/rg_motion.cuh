@@ -18,7 +18,7 @@ struct MotionArgs {
 
 // volume, real and ghost CMs and cd_volume of a mesh from its points and face
 // vertices (box = left, right, down, up; used for rigid-wall ghost CMs)
-cudaError_t launch_device_geometry(const MeshDev& m, double2* cms, double* volume, double* cd_volume,
+cudaError_t launch_device_geometry(const MeshDev& m, const int* order, double2* cms, double* volume, double* cd_volume,
                                    int ghost_kind, const double* box, cudaStream_t s);
 // CylindricalSymmetry's CacheData face areas and (cd_volume != nullptr) cell volumes
 cudaError_t launch_cyl_geometry(const MeshDev& m, double* xarea, double* cd_volume, const double* origin,
