@@ -553,15 +553,16 @@ rg_status rg_create(const rg_config* cfg, rg_handle** out) {
     if ((e = cudaEventCreateWithFlags(&s.last_use, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
   for (auto& k : h->ev_k)
     if ((e = cudaEventCreateWithFlags(&k, cudaEventDefault)) != cudaSuccess) return fail(e);
-  if ((e = h->status_buf.ensure(2 * sizeof(DevStatus))) != cudaSuccess) return fail(e);
+  if ((e = h->status_buf.ensure(3 * sizeof(DevStatus))) != cudaSuccess) return fail(e);
   h->d_status = static_cast<DevStatus*>(h->status_buf.p);
   h->d_geom_status = h->d_status + 1;
+  h->d_valid_status = h->d_status + 2;
   DevStatus init{};
   init.err_key = ~0ull;
   init.dt_min_bits = rg::kInfBits;
-  DevStatus both[2] = {init, init};
-  if ((e = cudaMemcpy(h->d_status, both, sizeof both, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e);
-  if ((e = h->host_status.ensure(sizeof(DevStatus))) != cudaSuccess) return fail(e);
+  DevStatus all[3] = {init, init, init};
+  if ((e = cudaMemcpy(h->d_status, all, sizeof all, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e);
+  if ((e = h->host_status.ensure(2 * sizeof(DevStatus))) != cudaSuccess) return fail(e);
   *out = h;
   return RG_OK;
 }
@@ -673,34 +674,28 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t flags) {
                                  h->upload_stream));
     }
   }
-  // every index checked before any kernel uses it
-  RG_TRY(reset_status(h, h->d_geom_status, h->upload_stream));
-  RG_CUDA(h, rg::launch_validate(s.mesh, h->d_geom_status, h->upload_stream));
-  {
-    DevStatus* hs = static_cast<DevStatus*>(h->host_status.p);
-    RG_CUDA(h, cudaMemcpyAsync(hs, h->d_geom_status, sizeof(DevStatus), cudaMemcpyDeviceToHost, h->upload_stream));
-    RG_CUDA(h, cudaStreamSynchronize(h->upload_stream));
-    if (hs->err_key != ~0ull) {
-      // the slot holds an invalid mesh: it is not activated
-      s.n = s.g = s.e = s.m = 0;
-      return invalid(h, static_cast<int64_t>(hs->err_key & rg::kKeyIndexMask), hs->err_value);
-    }
-  }
+  // every index is checked before any kernel uses it: the validation runs
+  // first on the upload stream and the geometry kernels behind it return at
+  // once when it has failed, so the host reads both results after one wait
+  RG_TRY(reset_status(h, h->d_valid_status, h->upload_stream));
+  RG_CUDA(h, rg::launch_validate(s.mesh, h->d_valid_status, h->upload_stream));
+  rg::MeshDev gm = s.mesh;
+  gm.invalid = &h->d_valid_status->err_key;
   // geometry pass on the upload stream (the per-cell kernels take cells in
   // the per-tile neighbour-count order, computed first)
   RG_TRY(reset_status(h, h->d_geom_status, h->upload_stream));
-  RG_CUDA(h, rg::launch_cell_order(s.mesh, at<int>(s.buf.p, s.lay.cell_order), at<int>(s.buf.p, s.lay.cflags),
+  RG_CUDA(h, rg::launch_cell_order(gm, at<int>(s.buf.p, s.lay.cell_order), at<int>(s.buf.p, s.lay.cflags),
                                    h->upload_stream));
   if (device_geometry)
-    RG_CUDA(h, rg::launch_device_geometry(s.mesh, at<int>(s.buf.p, s.lay.cell_order), at<double2>(s.buf.p, s.lay.cms), at<double>(s.buf.p, s.lay.volume),
+    RG_CUDA(h, rg::launch_device_geometry(gm, at<int>(s.buf.p, s.lay.cell_order), at<double2>(s.buf.p, s.lay.cms), at<double>(s.buf.p, s.lay.volume),
                                           at<double>(s.buf.p, s.lay.cd_volume), h->cfg.ghost_kind, h->box,
                                           h->upload_stream));
   if (h->pgeo.kind == RG_GEOMETRY_CYLINDRICAL)
-    RG_CUDA(h, rg::launch_cyl_geometry(s.mesh, at<double>(s.buf.p, s.lay.xarea),
+    RG_CUDA(h, rg::launch_cyl_geometry(gm, at<double>(s.buf.p, s.lay.xarea),
                                        device_geometry ? at<double>(s.buf.p, s.lay.cd_volume) : nullptr,
                                        h->pgeo.origin, h->pgeo.direction, h->pgeo.unit != 0, h->upload_stream));
   rg::GeomArgs ga{};
-  ga.mesh = s.mesh;
+  ga.mesh = gm;
   ga.order = h->cfg.order;
   void* b = s.buf.p;
   ga.area = at<double>(b, s.lay.area);
@@ -745,9 +740,20 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t flags) {
     m32.ghost_unit = at<float2>(b, s.lay.gunit32);
     m32.inv_cd_volume = at<float>(b, s.lay.icdv32);
     m32.cd_volume = s.mesh.cd_volume;
+    m32.invalid = gm.invalid;
     RG_CUDA(h, rg::launch_geom32(m32, h->upload_stream));
   }
   RG_CUDA(h, cudaEventRecord(h->ev_uploaded, h->upload_stream));
+  // the geometry errors (hs[0]; reconstruction would throw them) and the
+  // validation (hs[1])
+  DevStatus* hs = static_cast<DevStatus*>(h->host_status.p);
+  RG_CUDA(h, cudaMemcpyAsync(hs, h->d_geom_status, 2 * sizeof(DevStatus), cudaMemcpyDeviceToHost, h->upload_stream));
+  RG_CUDA(h, cudaStreamSynchronize(h->upload_stream));
+  if (hs[1].err_key != ~0ull) {
+    // the slot holds an invalid mesh: it is not activated
+    s.n = s.g = s.e = s.m = 0;
+    return invalid(h, static_cast<int64_t>(hs[1].err_key & rg::kKeyIndexMask), hs[1].err_value);
+  }
   if (n_changed) {
     // the cell count changed: the state no longer matches the mesh
     h->have_cells = h->have_ext = false;
@@ -806,10 +812,6 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t flags) {
   }
   if (h->active >= 0 && active_slot(h)->e != e) h->have_ev = false;
   h->have_fluxes = false;
-  // geometry errors (reconstruction would throw them) and timing
-  DevStatus* hs = static_cast<DevStatus*>(h->host_status.p);
-  RG_CUDA(h, cudaMemcpyAsync(hs, h->d_geom_status, sizeof(DevStatus), cudaMemcpyDeviceToHost, h->upload_stream));
-  RG_CUDA(h, cudaStreamSynchronize(h->upload_stream));
   s.geom_error = rg_error{};
   if (hs->err_key != ~0ull)
     s.geom_error = rg_error{hs->err_status, 2, static_cast<int64_t>(hs->err_key & rg::kKeyIndexMask), hs->err_value};

@@ -1,5 +1,5 @@
 // rg_convert.cuh -- float <-> double conversions and double comparisons on
-// the integer pipe, and a division by 3 without the FP64 division sequence.
+// the integer pipe.
 //
 // GB300 issues FP64-pipe instructions, the float <-> double conversions and
 // the double comparisons included, at about one per clock per SM against 64
@@ -162,25 +162,6 @@ RG_CONV_FN uint64_t min_first_u(uint64_t a, uint64_t b) { return lt_u(b, a) ? b 
 RG_CONV_FN double max_first(double a, double b) { return lt(a, b) ? b : a; }
 RG_CONV_FN double min_first(double a, double b) { return lt(b, a) ? b : a; }
 RG_CONV_FN uint64_t abs_u(double a) { return conv_dbits(a) & kMagMask; }
-
-// t / 3 rounded to nearest (t >= 0) without a division.  RN(1/3) is 1/3
-// less 2^-54 of itself, so q = RN(t * RN(1/3)) is within one ulp of t/3,
-// the fused remainder t - 3q is exact, and the fused correction
-// RN(q + r * RN(1/3)) is RN(t/3) (Markstein's correction step for a
-// divisor whose reciprocal is correctly rounded).  Below 2^-900, where the
-// remainder could lose bits, above 2^1000, and for infinities and NaN: the
-// division.
-RG_CONV_FN double third_of(double t) {
-  constexpr double kThird = 1.0 / 3.0;
-  if (!(t >= 0x1p-900 && t <= 0x1p1000)) return t / 3.;
-#ifdef __CUDA_ARCH__
-  const double q = __dmul_rn(t, kThird);
-  return __fma_rn(__fma_rn(-q, 3.0, t), kThird, q);
-#else
-  const double q = t * kThird;
-  return fma(fma(-q, 3.0, t), kThird, q);
-#endif
-}
 
 }  // namespace rg
 

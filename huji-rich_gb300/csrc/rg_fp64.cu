@@ -33,7 +33,7 @@ constexpr int kBlock = 256;
 // with simple_flux_calculator.cpp:27-31 (order 2).
 __global__ void __launch_bounds__(kBlock) k_geom_faces(GeomArgs a) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= a.mesh.e) return;
+  if (e >= a.mesh.e || mesh_rejected(a.mesh)) return;
   const int2 fc = a.mesh.face_cells[e];
   const dbl4 v = a.mesh.face_vertices[e];
   const double ax = v.x - v.z, ay = v.y - v.w;
@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(kBlock) k_geom_faces(GeomArgs a) {
 __global__ void __launch_bounds__(kBlock) k_geom_cells(GeomArgs a) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const MeshDev& m = a.mesh;
-  if (t >= m.n) return;
+  if (t >= m.n || mesh_rejected(m)) return;
   const int i = a.cell_order ? a.cell_order[t] : t;
   a.width[i] = root(quot(m.volume[i], kPi));
   const int b = m.cell_off[i], nn = m.cell_off[i + 1] - b;
@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(kBlock) k_geom_cells(GeomArgs a) {
 __global__ void __launch_bounds__(kBlock) k_geom_ghosts(GeomArgs a) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   const MeshDev& m = a.mesh;
-  if (g >= m.g) return;
+  if (g >= m.g || mesh_rejected(m)) return;
   const int e = m.ghost_face[g];
   if (a.ghost_kind == RG_GHOST_PERIODIC || e < 0) {
     a.ghost_real[g] = m.ghost_source[g];
@@ -179,11 +179,17 @@ __global__ void __launch_bounds__(kBlock) k_geom_ghosts(GeomArgs a) {
 // taken from the topology and stored as the cell's flag for the per-cell
 // geometry pass; runs after the index validation.
 __global__ void __launch_bounds__(kOrderTile) k_cell_order(MeshDev m, int* order, int* cflags) {
-  __shared__ int key[kOrderTile];
-  const int t = threadIdx.x, base = blockIdx.x * kOrderTile, i = base + t;
-  const int n = m.n, count = n - base < kOrderTile ? n - base : kOrderTile;
+  constexpr int kKeys = 128, kWarps = kOrderTile / 32;
+  // count[w][k]: cells of warp w with key k, then their offset within key k
+  __shared__ int count[kWarps][kKeys];
+  __shared__ int start[kKeys];
+  if (mesh_rejected(m)) return;
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const int base = blockIdx.x * kOrderTile, i = base + t, n = m.n;
+  for (int j = t; j < kWarps * kKeys; j += kOrderTile) count[j / kKeys][j % kKeys] = 0;
+  const bool live = i < n;
   int k = 0;
-  if (i < n) {
+  if (live) {
     const int b = m.cell_off[i], nn = m.cell_off[i + 1] - b;
     bool mirror = false;
     for (int j = 0; j < nn; ++j) {
@@ -193,15 +199,37 @@ __global__ void __launch_bounds__(kOrderTile) k_cell_order(MeshDev m, int* order
     k = (nn < 0 ? 0 : (nn > 63 ? 63 : nn)) | (mirror ? 64 : 0);
     cflags[i] = mirror ? kCellBoundarySlope : 0;
   }
-  key[t] = k;
   __syncthreads();
-  if (i >= n) return;
-  int rank = 0;
-  for (int j = 0; j < count; ++j) {
-    const int kj = key[j];
-    rank += (kj < k || (kj == k && j < t)) ? 1 : 0;
+  // rank within the warp among equal keys (lanes in ascending order)
+  const unsigned act = __ballot_sync(0xffffffffu, live);
+  int before = 0;
+  if (live) {
+    const unsigned peers = __match_any_sync(act, k);
+    before = __popc(peers & ((1u << lane) - 1u));
+    if (lane == __ffs(peers) - 1) count[w][k] = __popc(peers);
   }
-  order[base + rank] = i;
+  __syncthreads();
+  // per key: offsets of the warps (ascending), then the key's total
+  if (t < kKeys) {
+    int sum = 0;
+    for (int ww = 0; ww < kWarps; ++ww) {
+      const int c = count[ww][t];
+      count[ww][t] = sum;
+      sum += c;
+    }
+    start[t] = sum;
+  }
+  __syncthreads();
+  if (t == 0) {
+    int sum = 0;
+    for (int kk = 0; kk < kKeys; ++kk) {
+      const int c = start[kk];
+      start[kk] = sum;
+      sum += c;
+    }
+  }
+  __syncthreads();
+  if (live) order[base + start[k] + count[w][k] + before] = i;
 }
 
 // Index validation of an uploaded mesh, before any kernel indexes with it.

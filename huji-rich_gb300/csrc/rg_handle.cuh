@@ -175,6 +175,7 @@ struct rg_handle {
   rgh::HostBuf staging, host_status, host_dts;
   rg::DevStatus* d_status = nullptr;
   rg::DevStatus* d_geom_status = nullptr;
+  rg::DevStatus* d_valid_status = nullptr;  // index validation of an upload (follows d_geom_status)
   rg_error last{};
   double last_upload_ms = 0;
   double last_dt = 0;

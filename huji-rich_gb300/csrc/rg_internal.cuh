@@ -54,7 +54,12 @@ struct MeshDev {
   const dbl4* face_vertices;  // e
   const int* cell_off;      // n+1
   const int* cell_faces;    // m
+  // the upload's geometry pass runs behind the index validation without
+  // waiting for its result on the host: its kernels return at once when this
+  // error key of the validation is set (nullptr: no check)
+  const unsigned long long* invalid;
 };
+__device__ __forceinline__ bool mesh_rejected(const MeshDev& m) { return m.invalid && *m.invalid != ~0ull; }
 
 struct GeomDev {
   // per face

@@ -71,6 +71,7 @@ __device__ __forceinline__ void naive_slope(bool boundary, const C4& vx, const C
 // (the roundings on the integer pipe: rg_convert.cuh)
 
 __global__ void __launch_bounds__(kBlock) k_geom32(MixedGeomArgs a) {
+  if (a.invalid && *a.invalid != ~0ull) return;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int stride = gridDim.x * blockDim.x;
   const GeomDev& g = a.g64;

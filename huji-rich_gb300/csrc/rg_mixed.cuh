@@ -46,6 +46,7 @@ struct MixedGeomArgs {
   const int* cell_faces;
   float2* ghost_unit;
   float* inv_cd_volume;
+  const unsigned long long* invalid;  // MeshDev::invalid of the upload
 };
 
 struct MixedArgs {

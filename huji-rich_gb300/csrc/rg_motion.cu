@@ -36,7 +36,7 @@ __device__ __forceinline__ double half_cross(double2 p1, double2 p2) {
 __global__ void __launch_bounds__(kMoBlock) k_dev_geometry(MeshDev m, const int* order, double2* cms,
                                                             double* volume, double* cd_volume) {
   const int th = blockIdx.x * blockDim.x + threadIdx.x;
-  if (th >= m.n) return;
+  if (th >= m.n || mesh_rejected(m)) return;
   const int i = order ? order[th] : th;
   const int b = m.cell_off[i], e1 = m.cell_off[i + 1];
   const double2 c = m.points[i];
@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(kMoBlock) k_dev_geometry(MeshDev m, const int*
     area += half_cross(make_double2(v.x - c.x, v.y - c.y), make_double2(v.z - c.x, v.w - c.y));
     const double t = half_cross(make_double2(v.x - an.x, v.y - an.y), make_double2(v.z - an.x, v.w - an.y));
     a2 += t;
-    const double s = third_of(t);
+    const double s = quot(t, 3.0);
     pc.x += ((an.x + v.x) + v.z) * s;
     pc.y += ((an.y + v.y) + v.w) * s;
   }
@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(kMoBlock) k_dev_geometry(MeshDev m, const int*
 
 __global__ void __launch_bounds__(kMoBlock) k_ghost_cms(MeshDev m, double2* cms, int ghost_kind, dbl4 box) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= m.g) return;
+  if (g >= m.g || mesh_rejected(m)) return;
   const int p = m.n + g, src = m.ghost_source[g];
   const double2 cs = cms[src];
   const double2 q = m.points[p];
@@ -112,6 +112,7 @@ __device__ __forceinline__ double cone_segment(double2 p1, double2 p2, const Cyl
 
 __global__ void __launch_bounds__(kMoBlock) k_cyl_geometry(MeshDev m, double* xarea, double* cd_volume, dbl4 od,
                                                             int unit) {
+  if (mesh_rejected(m)) return;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const CylAxis a = cyl_axis(od, unit != 0);
   if (t < m.e) {

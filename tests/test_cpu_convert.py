@@ -1,7 +1,7 @@
 """The integer-pipe float <-> double conversions of the FP32-mixed kernels,
-the integer-pipe double comparisons of the FP64 kernels and the
-division-free t / 3 of the device geometry (huji-rich_gb300/csrc/rg_convert.cuh)
-agree bit for bit with the C casts, operators and division.  The header is host-compilable: the same source is built with
+the integer-pipe double comparisons and selections of the FP64 kernels
+(huji-rich_gb300/csrc/rg_convert.cuh) agree bit for bit with the C casts and
+operators.  The header is host-compilable: the same source is built with
 g++ here."""
 import os
 import shutil
@@ -13,7 +13,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 @pytest.mark.skipif(not shutil.which("g++"), reason="needs g++")
-def test_conversions_and_third_match_the_casts_and_division(tmp_path):
+def test_conversions_and_comparisons_match_the_casts_and_operators(tmp_path):
     exe = str(tmp_path / "convert_check")
     cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I" + os.path.join(ROOT, "huji-rich_gb300", "csrc"),
            os.path.join(ROOT, "tests", "convert_check.cpp"), "-o", exe]
