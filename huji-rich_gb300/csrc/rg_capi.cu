@@ -225,6 +225,7 @@ rg::StepArgs step_args(rg_handle* h) {
     a.frozen_mask = h->tcfg.frozen_sticker >= 0 ? 1u << h->tcfg.frozen_sticker : 0u;
     if (h->tcfg.n_tracers > 0) {
       a.mflux = static_cast<double*>(h->mflux.p);
+      if (h->n_rules > 0) a.tr_side = static_cast<unsigned char*>(h->tr_side.p);
       if (h->cfg.order == 2) a.shock = static_cast<unsigned char*>(h->shock.p);
     }
   }

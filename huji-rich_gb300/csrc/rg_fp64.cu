@@ -713,6 +713,7 @@ __device__ __forceinline__ void k_faces_cas_item(const StepArgs& a, int e) {
       }
     }
   }
+  if (a.tr_side) a.tr_side[e] = 0;  // no tracer flux unless an action sets one
   if (chosen < 0) {  // "Error in ConditionActionSequence"
     record_error(a.status, a.step, RG_ERR_INVALID_ARGUMENT, 3, e, 0.0);
     return;
@@ -784,6 +785,11 @@ __device__ __forceinline__ void k_faces_cas_item(const StepArgs& a, int e) {
       a.lag_ws[e] = lag ? energy : 0.0;
       a.lag_ev[e] = speed;
     }
+    // convert_conserved_to_extensive (:29-40): Mass * the face value upwind
+    if (a.tr_side) {
+      a.mflux[e] = c.m;
+      a.tr_side[e] = kTrSideFace | (c.m > 0 ? kTrSideFirst : kTrSideSecond);
+    }
     write_flux<false>(a, e, fc.x < m.n ? fc.x : fc.y, c, kScaled, a.geom.xarea[e]);
     return;
   }
@@ -818,6 +824,18 @@ __device__ __forceinline__ void k_faces_cas_item(const StepArgs& a, int e) {
   const double na = root(n.x * n.x + n.y * n.y);
   Cons c;
   if (!solve_face(l, r, vel, n, na, p, pa, c, a, e)) return;
+  if (a.tr_side) {
+    // the tracer flux is Mass times the tracers of: the upwind cell
+    // (RegularFlux, condition_action_sequence.cpp:110-114) or face value
+    // (RegularFlux2, condition_action_sequence_2.cpp:156), the cell on the
+    // aux side (RigidWallFlux, FreeFlowFlux: :178, :221) or its face value
+    // (RigidWallFlux2, condition_action_sequence_2.cpp:221)
+    a.mflux[e] = c.m;
+    const bool regular = action == RG_ACT_REGULAR || action == RG_ACT_REGULAR2;
+    const bool face = action == RG_ACT_REGULAR2 || action == RG_ACT_RIGID_WALL2;
+    const bool first = regular ? c.m > 0 : aux;
+    a.tr_side[e] = (face ? kTrSideFace : 0) | (first ? kTrSideFirst : kTrSideSecond);
+  }
   const int real_side = fc.x < m.n ? fc.x : fc.y;
   write_flux<false>(a, e, real_side, c, kScaled, a.geom.xarea[e]);
 }
@@ -899,24 +917,7 @@ __device__ __forceinline__ unsigned long long k_update_item(const StepArgs& a, i
       }
     }
     if (a.lag_update) {
-      // LagrangianExtensiveUpdater.cpp:32-56: dV, dV_ws over the cell's faces
-      // in face order, then every extensive times (V + dV) / (V + dV + dV_ws)
-      const double dtl = step_dt(a);
-      double dv = 0.0, dvw = 0.0;
-      for (int k = b; k < e1; ++k) {
-        const int e = m.cell_faces[k];
-        const double ar = a.geom.xarea[e];
-        const double t1 = ar * dtl * a.lag_ev[e], t2 = ar * dtl * a.lag_ws[e];
-        if (a.geom.nbr[k] & kNbrFirst) {
-          dv += t1;
-          dvw += t2;
-        } else {
-          dv -= t1;
-          dvw -= t2;
-        }
-      }
-      const double vol = m.cd_volume[i];
-      const double f = quot(vol + dv, vol + dv + dvw);
+      const double f = lag_factor(a, i);
       mass *= f;
       en *= f;
       px *= f;

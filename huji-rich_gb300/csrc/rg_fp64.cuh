@@ -87,6 +87,29 @@ __device__ __forceinline__ double step_dt(const StepArgs& a) {
   return a.dt_from_device ? a.status->dt : a.dt_host;
 }
 
+// LagrangianExtensiveUpdater.cpp:32-56 for cell i: dV, dV_ws over the cell's
+// faces in face order, and the factor (V + dV) / (V + dV + dV_ws) that every
+// extensive of the cell (its tracers included) is multiplied by
+__device__ __forceinline__ double lag_factor(const StepArgs& a, int i) {
+  const MeshDev& m = a.mesh;
+  const double dtl = step_dt(a);
+  double dv = 0.0, dvw = 0.0;
+  for (int k = m.cell_off[i]; k < m.cell_off[i + 1]; ++k) {
+    const int e = m.cell_faces[k];
+    const double ar = a.geom.xarea[e];
+    const double t1 = ar * dtl * a.lag_ev[e], t2 = ar * dtl * a.lag_ws[e];
+    if (a.geom.nbr[k] & kNbrFirst) {
+      dv += t1;
+      dvw += t2;
+    } else {
+      dv -= t1;
+      dvw -= t2;
+    }
+  }
+  const double vol = m.cd_volume[i];
+  return quot(vol + dv, vol + dv + dvw);
+}
+
 // FP32 screening of FP64 quotients.  GB300 issues 64 FP32 operations per FP64
 // one, so a decision that only needs to know on which side of a threshold a
 // correctly rounded FP64 quotient lies is taken from an FP32 estimate when

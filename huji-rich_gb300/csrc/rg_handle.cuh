@@ -206,7 +206,7 @@ struct rg_handle {
   // LagrangianExtensiveUpdater (rg_set_lagrangian_updater)
   rgh::DevBuf lag_ws, lag_ev;
   bool lag_rule = false, lag_update = false;
-  rgh::DevBuf tr, tr_ext, tr_slopes, tr_flux, mflux, shock, stickers;
+  rgh::DevBuf tr, tr_ext, tr_slopes, tr_flux, mflux, tr_side, shock, stickers;
   rgh::DevBuf mid_tr, mid_tr_ext;  // TimeAdvance2Heun's mid tracers (n*nt each)
   bool have_tr = false, have_tr_ext = false;
   int tr_n = -1, tr_e = -1;

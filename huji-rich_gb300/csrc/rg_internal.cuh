@@ -216,6 +216,10 @@ struct StepShapes {
 };
 
 // Kernel launchers (rg_fp64.cu)
+// tracer source of a condition/action face: the first or the second
+// neighbour, its own cell's tracers or LinearGaussImproved's face value
+constexpr unsigned char kTrSideFirst = 1, kTrSideSecond = 2, kTrSideFace = 4;
+
 struct StepArgs {
   MeshDev mesh;
   GeomDev geom;
@@ -253,6 +257,9 @@ struct StepArgs {
   // tracer passes: the faces kernel keeps each face's unscaled mass flux and
   // the slopes kernel each cell's shock decision
   double* mflux;                  // e, or nullptr
+  // e, or nullptr: for the condition/action fluxes, where face e's tracer
+  // flux takes its tracers (kTrSide* bits), written beside mflux
+  unsigned char* tr_side;
   unsigned char* shock;           // n, or nullptr
   // condition/action flux rules (0: Simple/ModularFluxCalculator)
   int n_rules;

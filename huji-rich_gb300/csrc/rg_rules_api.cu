@@ -37,7 +37,7 @@ extern "C" {
 rg_status rg_set_flux_rules(rg_handle* h, int32_t n_rules, const rg_flux_rule* rules) {
   if (!h || n_rules < 0 || (n_rules > 0 && !rules)) return RG_ERR_INVALID_ARGUMENT;
   if (n_rules > RG_MAX_FLUX_RULES) return invalid(h, -1, n_rules);
-  if (n_rules > 0 && (h->mixed || h->n_problems > 0 || h->tcfg.n_tracers > 0)) return invalid(h, -2, 0);
+  if (n_rules > 0 && (h->mixed || h->n_problems > 0)) return invalid(h, -2, 0);
   for (int k = 0; k < n_rules; ++k) {
     const rg_flux_rule& r = rules[k];
     const bool ok = (r.sequence == 0 || r.sequence == 1) && r.condition >= 0 && r.condition <= 2 &&

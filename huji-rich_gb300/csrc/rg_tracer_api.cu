@@ -23,7 +23,7 @@ bool tracers_on(const rg_handle* h) {
 }
 
 void tracer_release(rg_handle* h) {
-  for (DevBuf* b : {&h->tr, &h->tr_ext, &h->tr_slopes, &h->tr_flux, &h->mflux, &h->shock, &h->stickers,
+  for (DevBuf* b : {&h->tr, &h->tr_ext, &h->tr_slopes, &h->tr_flux, &h->mflux, &h->tr_side, &h->shock, &h->stickers,
                     &h->mid_tr, &h->mid_tr_ext})
     b->release();
   h->have_tr = h->have_tr_ext = false;
@@ -48,6 +48,7 @@ rg_status tracer_buffers(rg_handle* h) {
   RG_CUDA(h, h->tr_slopes.ensure(16 * n * nt));
   RG_CUDA(h, h->tr_flux.ensure(8 * e * nt));
   RG_CUDA(h, h->mflux.ensure(8 * e));
+  RG_CUDA(h, h->tr_side.ensure(e));
   RG_CUDA(h, h->shock.ensure(n));
   if (h->heun) {
     RG_CUDA(h, h->mid_tr.ensure(8 * n * nt));
@@ -113,7 +114,6 @@ rg_status rg_set_tracer_config(rg_handle* h, const rg_tracer_config* cfg) {
   const rg_tracer_config c = cfg ? *cfg : off;
   if (c.n_tracers < 0 || c.n_tracers > RG_MAX_TRACERS) return invalid(h, 0, c.n_tracers);
   if (c.n_stickers < 0 || c.n_stickers > 32) return invalid(h, 6, c.n_stickers);
-  if (c.n_tracers > 0 && h->n_rules > 0) return invalid(h, 7, 0);  // condition/action fluxes carry no tracers
   if (c.n_tracers < 32 && (c.limited_mask >> c.n_tracers) != 0) return invalid(h, 1, c.limited_mask);
   if (c.entropy_tracer < -1 || c.entropy_tracer >= c.n_tracers) return invalid(h, 2, c.entropy_tracer);
   if (c.skip_sticker < -1 || c.skip_sticker > 31) return invalid(h, 3, c.skip_sticker);

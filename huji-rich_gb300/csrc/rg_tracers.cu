@@ -215,6 +215,49 @@ __global__ void __launch_bounds__(kTrBlock) k_tr_faces_lgi(StepArgs a, TracerArg
   }
 }
 
+// The condition/action fluxes' tracer part: Mass times the tracers of the
+// side the face's action chose (a.tr_side): that neighbour's own cell (a
+// ghost's cell, as the hydro state), or its LinearGaussImproved face value as
+// k_tr_faces_lgi forms it.  Faces with no action carry none.
+template <bool kScaled>
+__global__ void __launch_bounds__(kTrBlock) k_tr_faces_cas(StepArgs a, TracerArgs t) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const MeshDev& m = a.mesh;
+  if (e >= m.e) return;
+  const int nt = t.nt;
+  const unsigned char side = a.tr_side[e];
+  double* o = t.tr_flux + static_cast<size_t>(e) * nt;
+  if (!(side & (kTrSideFirst | kTrSideSecond))) {
+    for (int j = 0; j < nt; ++j) o[j] = 0.0;
+    return;
+  }
+  const int2 fc = m.face_cells[e];
+  const double mass = a.mflux[e];
+  const bool first = (side & kTrSideFirst) != 0;
+  const int pid = first ? fc.x : fc.y;
+  const double s = kScaled ? tr_scale(a, e) : 1.0;
+  if (side & kTrSideFace) {
+    const double2 dm = (first ? a.geom.dm0 : a.geom.dm1)[e];
+    const int src = copied_cell(a, pid);
+    const bool zero_grad = pid >= m.n && a.ghost_kind != RG_GHOST_PERIODIC;
+    const double* q = t.tr + static_cast<size_t>(src) * nt;
+    const double* g = t.tr_slopes + static_cast<size_t>(src) * 2 * nt;
+    for (int j = 0; j < nt; ++j) {
+      double v = q[j];
+      v += (zero_grad ? 0.0 : g[j]) * dm.x;
+      v += (zero_grad ? 0.0 : g[nt + j]) * dm.y;
+      const double f = mass * v;
+      o[j] = kScaled ? f * s : f;
+    }
+  } else {
+    const double* q = t.tr + static_cast<size_t>(orig_of(m, pid)) * nt;
+    for (int j = 0; j < nt; ++j) {
+      const double f = mass * q[j];
+      o[j] = kScaled ? f * s : f;
+    }
+  }
+}
+
 // SimpleFluxCalculator calc_tracer_flux (simple_flux_calculator.cpp:193-213):
 // Mass * the upwind point's tracer, 0 when that point is a self-mirror ghost
 // or Mass is 0; a periodic ghost reads its source cell, as the hydro state does.
@@ -272,6 +315,13 @@ __global__ void __launch_bounds__(kTrBlock) k_tr_update(StepArgs a, TracerArgs t
             te[j] += d;
         }
       }
+    }
+    if (a.lag_update) {
+      // LagrangianExtensiveUpdater scales every extensive of the cell
+      const double f = lag_factor(a, i);
+#pragma unroll
+      for (int j = 0; j < kMaxTracers; ++j)
+        if (j < nt) te[j] *= f;
     }
   }
   if (t.tr_ext_avg) {
@@ -349,7 +399,9 @@ cudaError_t launch_tr_slopes(const StepArgs& a, const TracerArgs& t, cudaStream_
 cudaError_t launch_tr_faces(const StepArgs& a, const TracerArgs& t, cudaStream_t s, bool scaled) {
   if (a.mesh.e == 0 || t.nt == 0) return cudaSuccess;
   const int nb = tr_blocks(a.mesh.e);
-  if (a.order == 1)
+  if (a.n_rules > 0)
+    scaled ? k_tr_faces_cas<true><<<nb, kTrBlock, 0, s>>>(a, t) : k_tr_faces_cas<false><<<nb, kTrBlock, 0, s>>>(a, t);
+  else if (a.order == 1)
     scaled ? k_tr_faces_pcm<true><<<nb, kTrBlock, 0, s>>>(a, t) : k_tr_faces_pcm<false><<<nb, kTrBlock, 0, s>>>(a, t);
   else
     scaled ? k_tr_faces_lgi<true><<<nb, kTrBlock, 0, s>>>(a, t) : k_tr_faces_lgi<false><<<nb, kTrBlock, 0, s>>>(a, t);

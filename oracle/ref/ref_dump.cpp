@@ -10,7 +10,9 @@
 // With "heun" the warm-up and run steps use hdsim::TimeAdvance2Heun
 // (hdsim2d.cpp:323-449) instead of hdsim::TimeAdvance.
 //
-// Cases named <case>_tracers add tracers and stickers: tracer names
+// Cases named <case>_tracers add tracers and stickers (the condition/action
+// cases cas*_tracers: tracers {"A", "Z"} with "A" in calc_tracers, and the
+// case's own stickers): tracer names
 // {"A", "Entropy", "Z"} ("A" in LinearGaussImproved's calc_tracers,
 // "Entropy" recomputed by SimpleCellUpdater, "Z" piecewise constant), sticker
 // names {"frozen", "skip"} ("skip" is LinearGaussImproved's skip_key, cells
@@ -335,6 +337,19 @@ int main(int argc, char** argv) {
     which = which.substr(0, which.size() - sfx.size());
     g_ntr = 3;
   }
+  // the condition/action cases' tracer forms carry two plain tracers {"A",
+  // "Z"} ("A" in LinearGaussImproved's calc_tracers) and the case's own
+  // stickers
+  const bool cas_case = which.compare(0, 3, "cas") == 0;
+  if (tracers && cas_case) g_ntr = 2;
+  const vector<string> cas_calc = tracers ? vector<string>{"A"} : vector<string>();
+  auto cas_tracers = [&](vector<ComputationalCell>& ic, const Tessellation& tess) {
+    if (!tracers) return;
+    for (size_t i = 0; i < ic.size(); ++i) {
+      const Vector2D r = tess.GetMeshPoint(static_cast<int>(i));
+      ic[i].tracers = {r.x + (r.y > 0.4 ? 0.5 : 0.0), abs(r - Vector2D(0.3, 0.3)) < 0.2 ? 1.0 : 0.0};
+    }
+  };
   // tracer / sticker setup of the _tracers cases (names sorted, as the
   // reference's binary_find lookups need)
   const TracerStickerNames tsn = tracers ? TracerStickerNames({"A", "Entropy", "Z"}, {"frozen", "skip"})
@@ -392,7 +407,7 @@ int main(int argc, char** argv) {
     SimpleCFL tsf(0.3);
     SimpleExtensiveUpdater eu;
     vector<pair<const SimpleCellUpdater::Condition*, const SimpleCellUpdater::Action*> > seq;
-    if (tracers) seq.push_back({new HasSticker("frozen"), new SkipUpdate()});
+    if (tracers && !cas_case) seq.push_back({new HasSticker("frozen"), new SkipUpdate()});
     SimpleCellUpdater cu(seq);
     if (which == "sod" || which == "sod_lagrangian") {
       // 2D Sod tube: [0,1]x[0,0.2], reflective walls, piecewise-constant Hllc, gamma 1.4.
@@ -523,7 +538,7 @@ int main(int argc, char** argv) {
       Eulerian eul;
       StationaryBox evc;
       RigidWallGenerator gpg;
-      LinearGaussImproved sr(eos, gpg);
+      LinearGaussImproved sr(eos, gpg, true, 0.2, 0.5, 0.7, cas_calc);
       typedef ConditionActionSequence CAS;
       vector<pair<const CAS::Condition*, const CAS::Action*> > seq1;
       vector<pair<const CAS::Condition*, const ConditionActionSequence2::Action2*> > seq2;
@@ -548,7 +563,8 @@ int main(int argc, char** argv) {
       const FluxCalculator& fc = first ? static_cast<const FluxCalculator&>(fc1)
                                        : static_cast<const FluxCalculator&>(fc2);
       const bool obstacle = which != "cas2_ratchet";
-      const TracerStickerNames names = obstacle ? TracerStickerNames({}, {"obstacle"}) : TracerStickerNames();
+      const vector<string> tnames = tracers ? vector<string>{"A", "Z"} : vector<string>();
+      const TracerStickerNames names = obstacle ? TracerStickerNames(tnames, {"obstacle"}) : TracerStickerNames(tnames, {});
       vector<ComputationalCell> ic(static_cast<size_t>(tess.GetPointNo()));
       for (size_t i = 0; i < ic.size(); ++i) {
         const Vector2D r = tess.GetMeshPoint(static_cast<int>(i));
@@ -568,6 +584,7 @@ int main(int argc, char** argv) {
           ic[i].velocity = Vector2D(0.3 * (r.x - 0.5), 0.3 * (r.y - 0.5));
         }
       }
+      cas_tracers(ic, tess);
       // obstacle cells keep their state (HasSticker + SkipUpdate)
       vector<pair<const SimpleCellUpdater::Condition*, const SimpleCellUpdater::Action*> > keep;
       if (obstacle) keep.push_back({new HasSticker("obstacle"), new SkipUpdate()});
@@ -577,7 +594,7 @@ int main(int argc, char** argv) {
       dump_scalar("gamma", 5. / 3.);
       dump_scalar("order", first ? 1 : 2);
       dump_scalar("ghost_kind", 0);
-      if (obstacle) {
+      if (obstacle && !g_ntr) {
         std::vector<int32_t> st;
         for (const auto& c : sim.getAllCells()) st.push_back(c.stickers[0] ? 1 : 0);
         dump_i32("tr_stickers", st, 0);
@@ -606,7 +623,7 @@ int main(int argc, char** argv) {
       g_motion[0] = move ? 1 : 0;
       StationaryBox evc;
       RigidWallGenerator gpg;
-      LinearGaussImproved sr(eos, gpg);
+      LinearGaussImproved sr(eos, gpg, true, 0.2, 0.5, 0.7, cas_calc);
       LagrangianHLLC lrs1(move), lrs2(!move);  // massflux: false, true (cas2_lag); true, false (cas2_lag_move)
       WallsMassFlux walls;
       LagrangianFlux lflux(lrs1, lrs2, walls);
@@ -633,7 +650,9 @@ int main(int argc, char** argv) {
         ic[i].pressure = abs(r - Vector2D(0.4, 0.55)) < 0.15 ? 4.0 : 0.6;
         ic[i].velocity = Vector2D(0.25 * std::cos(6.283185307179586 * r.y), -0.15 * std::sin(6.283185307179586 * r.x));
       }
-      hdsim sim(tess, outer, pg, ic, eos, pm, evc, force, tsf, fc, leu, cu);
+      cas_tracers(ic, tess);
+      const TracerStickerNames lnames(tracers ? vector<string>{"A", "Z"} : vector<string>(), {});
+      hdsim sim(tess, outer, pg, ic, eos, pm, evc, force, tsf, fc, leu, cu, lnames);
       for (int s = 0; s < warm; ++s) advance(sim);
       dump_scalar("gamma", 5. / 3.);
       dump_scalar("order", 2);

@@ -78,6 +78,16 @@ CASES_TRACERS = {
     "periodic_heun_tracers_o2": ("periodic_tracers", 16, 16, 2, 10, "heun"),
 }
 
+# The condition/action cases with tracers (ref_dump's cas*_tracers forms),
+# written to cas_tracers/<name>.npz: tracers {"A" (in calc_tracers), "Z"},
+# the cases' own stickers; name: (ref_dump case, nx, ny, warm steps, run steps)
+CASES_CAS_TRACERS = {
+    "cas_free_tracers_o1": ("cas_free_tracers", 24, 24, 2, 10),
+    "cas2_wall_tracers_o2": ("cas2_wall_tracers", 24, 24, 2, 10),
+    "cas2_ratchet_tracers_o2": ("cas2_ratchet_tracers", 24, 24, 2, 10),
+    "cas2_lag_tracers_o2": ("cas2_lag_tracers", 24, 24, 2, 10),
+}
+
 # 3D first-order path (oracle/ref/ref_dump3d.cpp), written to 3d/<name>.npz:
 # name: (ref_dump3d case, nx, ny, nz, run steps)
 CASES3D = {
@@ -146,6 +156,9 @@ def main():
     todo = [(c, CASES[c], HERE) for c in (a.cases or sorted(CASES)) if c in CASES]
     todo += [(c, CASES_TRACERS[c], os.path.join(HERE, "tracers"))
              for c in (a.cases or sorted(CASES_TRACERS)) if c in CASES_TRACERS]
+    os.makedirs(os.path.join(HERE, "cas_tracers"), exist_ok=True)
+    todo += [(c, CASES_CAS_TRACERS[c], os.path.join(HERE, "cas_tracers"))
+             for c in (a.cases or sorted(CASES_CAS_TRACERS)) if c in CASES_CAS_TRACERS]
     for name, spec, outdir in todo:
         case, nx, ny, warm, run = spec[:5]
         scheme = spec[5] if len(spec) > 5 else "first"
