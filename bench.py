@@ -574,8 +574,9 @@ def run_gpu(args, world, rank, local_rank):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
                 "data": "synthetic", "config": config_block(mesh),
                 "impl_notes": dict(IMPL_NOTES, mesh_source=_WORKLOAD.get("source")),
-                "precision": "FP32-mixed: reconstruction, HLLC, CFL in FP32; geometry, volumes, "
-                             "extensive accumulation, E/m - v^2/2 in FP64",
+                "precision": "FP32-mixed: reconstruction, HLLC, CFL in FP32 (FP32 geometry from FP64 "
+                             "coordinate differences); volumes, CMs, motion, extensive accumulation, "
+                             "E/m - v^2/2 in FP64",
                 "l1_density_vs_fp64": l1, "l1_after_steps": r32["warmup"] + k,
                 "l1_density_vs_fp64_500_steps": l1_500,
                 "roofline": roofline(r32, mesh, 1),

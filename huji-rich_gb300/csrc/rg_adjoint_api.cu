@@ -80,7 +80,9 @@ rg_status check_config(rg_handle* h, bool allow_mixed = true) {
       h->n_problems > 0 ||
       tracers_on(h) || active_slot(h)->lay.own_xarea || h->n_rules > 0)
     return invalid(h, -10, h->cfg.order);
-  return RG_OK;
+  // the reverse kernels read the FP64 geometry (rounded to FP32 for an
+  // FP32-mixed handle, as its forward kernels then use it)
+  return ensure_geom64(h);
 }
 
 rg::AdjArgs adj_args(rg_handle* h) {

@@ -483,6 +483,88 @@ rg_status enqueue_step(rg_handle* h, int step, cudaEvent_t* ev = nullptr) {
 
 }  // namespace
 
+namespace rgh {
+
+// The per-face and per-cell geometry of slot s on stream st: the FP64 pass
+// (and, for the FP32-mixed path, its rounded FP32 copies) when full64, else
+// the FP32-mixed path's direct FP32 geometry with the few FP64 arrays its
+// motion and neighbour walks read.
+rg_status geometry_pass(rg_handle* h, MeshSlot& s, const rg::MeshDev& gm, bool full64, cudaStream_t st) {
+  rg::GeomArgs ga{};
+  ga.mesh = gm;
+  ga.order = h->cfg.order;
+  void* b = s.buf.p;
+  ga.area = at<double>(b, s.lay.area);
+  ga.nrm = at<double2>(b, s.lay.nrm);
+  ga.nabs = at<double>(b, s.lay.nabs);
+  ga.par = at<double2>(b, s.lay.par);
+  ga.dm0 = at<double2>(b, s.lay.dm0);
+  ga.dm1 = at<double2>(b, s.lay.dm1);
+  ga.dab = at<double>(b, s.lay.dab);
+  ga.rij = at<double2>(b, s.lay.rij);
+  ga.cij = at<double2>(b, s.lay.cij);
+  ga.width = at<double>(b, s.lay.width);
+  ga.minv = at<rg::dbl4>(b, s.lay.minv);
+  ga.cflags = at<int>(b, s.lay.cflags);
+  ga.nbr = at<uint32_t>(b, s.lay.nbr);
+  ga.hr = at<double2>(b, s.lay.hr);
+  ga.ghost_real = at<int>(b, s.lay.ghost_real);
+  ga.ghost_unit = at<double2>(b, s.lay.ghost_unit);
+  ga.cell_order = at<int>(b, s.lay.cell_order);
+  ga.ghost_kind = h->cfg.ghost_kind;
+  ga.status = h->d_geom_status;
+  if (full64) RG_CUDA(h, rg::launch_geometry(ga, st));
+  s.geom64 = full64;
+  if (h->mixed) {
+    rg::MixedGeomArgs m32{};
+    m32.n = s.n;
+    m32.g = s.g;
+    m32.e = s.e;
+    m32.m = s.m;
+    m32.g64 = s.geom;
+    m32.nrm = at<float2>(b, s.lay.nrm32);
+    m32.nabs = at<float>(b, s.lay.nabs32);
+    m32.par = at<float2>(b, s.lay.par32);
+    m32.area = at<float>(b, s.lay.area32);
+    m32.xarea = s.lay.own_xarea ? at<float>(b, s.lay.xarea32) : m32.area;
+    m32.dm0 = at<float2>(b, s.lay.dm0_32);
+    m32.dm1 = at<float2>(b, s.lay.dm1_32);
+    m32.width = at<float>(b, s.lay.width32);
+    m32.minv = at<float4>(b, s.lay.minv32);
+    m32.ent = at<float4>(b, s.lay.ent32);
+    m32.fsign = at<int>(b, s.lay.fsign32);
+    m32.cell_faces = s.mesh.cell_faces;
+    m32.ghost_unit = at<float2>(b, s.lay.gunit32);
+    m32.inv_cd_volume = at<float>(b, s.lay.icdv32);
+    m32.cd_volume = s.mesh.cd_volume;
+    m32.invalid = gm.invalid;
+    m32.rij = at<float2>(b, s.lay.rij);
+    m32.cij = at<float2>(b, s.lay.cij);
+    if (full64) {
+      RG_CUDA(h, rg::launch_geom32(m32, st));
+    } else {
+      RG_CUDA(h, rg::launch_geom_ghosts(ga, st));
+      RG_CUDA(h, rg::launch_geom32_direct(ga, m32, st));
+    }
+  }
+  return RG_OK;
+}
+
+// The FP64 geometry of the active slot, for the FP64 passes that run on an
+// FP32-mixed handle (tracers, differentiation, rg_get_geometry): formed on
+// the compute stream once per mesh, with the FP32 copies rounded from it.
+rg_status ensure_geom64(rg_handle* h) {
+  if (h->active < 0) return RG_OK;
+  MeshSlot& s = h->slots[h->active];
+  if (s.geom64) return RG_OK;
+  RG_CUDA(h, cudaStreamWaitEvent(h->stream, h->ev_uploaded, 0));
+  rg::MeshDev gm = s.mesh;
+  gm.invalid = nullptr;
+  return geometry_pass(h, s, gm, true, h->stream);
+}
+
+}  // namespace rgh
+
 extern "C" {
 
 void rg_default_config(rg_config* c) {
@@ -695,55 +777,10 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t flags) {
     RG_CUDA(h, rg::launch_cyl_geometry(gm, at<double>(s.buf.p, s.lay.xarea),
                                        device_geometry ? at<double>(s.buf.p, s.lay.cd_volume) : nullptr,
                                        h->pgeo.origin, h->pgeo.direction, h->pgeo.unit != 0, h->upload_stream));
-  rg::GeomArgs ga{};
-  ga.mesh = gm;
-  ga.order = h->cfg.order;
-  void* b = s.buf.p;
-  ga.area = at<double>(b, s.lay.area);
-  ga.nrm = at<double2>(b, s.lay.nrm);
-  ga.nabs = at<double>(b, s.lay.nabs);
-  ga.par = at<double2>(b, s.lay.par);
-  ga.dm0 = at<double2>(b, s.lay.dm0);
-  ga.dm1 = at<double2>(b, s.lay.dm1);
-  ga.dab = at<double>(b, s.lay.dab);
-  ga.rij = at<double2>(b, s.lay.rij);
-  ga.cij = at<double2>(b, s.lay.cij);
-  ga.width = at<double>(b, s.lay.width);
-  ga.minv = at<rg::dbl4>(b, s.lay.minv);
-  ga.cflags = at<int>(b, s.lay.cflags);
-  ga.nbr = at<uint32_t>(b, s.lay.nbr);
-  ga.hr = at<double2>(b, s.lay.hr);
-  ga.ghost_real = at<int>(b, s.lay.ghost_real);
-  ga.ghost_unit = at<double2>(b, s.lay.ghost_unit);
-  ga.cell_order = at<int>(b, s.lay.cell_order);
-  ga.ghost_kind = h->cfg.ghost_kind;
-  ga.status = h->d_geom_status;
-  RG_CUDA(h, rg::launch_geometry(ga, h->upload_stream));
-  if (h->mixed) {
-    rg::MixedGeomArgs m32{};
-    m32.n = n;
-    m32.g = g;
-    m32.e = e;
-    m32.m = m;
-    m32.g64 = s.geom;
-    m32.nrm = at<float2>(b, s.lay.nrm32);
-    m32.nabs = at<float>(b, s.lay.nabs32);
-    m32.par = at<float2>(b, s.lay.par32);
-    m32.area = at<float>(b, s.lay.area32);
-    m32.xarea = s.lay.own_xarea ? at<float>(b, s.lay.xarea32) : m32.area;
-    m32.dm0 = at<float2>(b, s.lay.dm0_32);
-    m32.dm1 = at<float2>(b, s.lay.dm1_32);
-    m32.width = at<float>(b, s.lay.width32);
-    m32.minv = at<float4>(b, s.lay.minv32);
-    m32.ent = at<float4>(b, s.lay.ent32);
-    m32.fsign = at<int>(b, s.lay.fsign32);
-    m32.cell_faces = s.mesh.cell_faces;
-    m32.ghost_unit = at<float2>(b, s.lay.gunit32);
-    m32.inv_cd_volume = at<float>(b, s.lay.icdv32);
-    m32.cd_volume = s.mesh.cd_volume;
-    m32.invalid = gm.invalid;
-    RG_CUDA(h, rg::launch_geom32(m32, h->upload_stream));
-  }
+  // the FP32-mixed path without tracers takes its FP32 geometry straight
+  // from the inputs; the FP64 geometry is formed when something needs it
+  // (ensure_geom64)
+  RG_TRY(geometry_pass(h, s, gm, !h->mixed || tracers_on(h), h->upload_stream));
   RG_CUDA(h, cudaEventRecord(h->ev_uploaded, h->upload_stream));
   // the geometry errors (hs[0]; reconstruction would throw them) and the
   // validation (hs[1])

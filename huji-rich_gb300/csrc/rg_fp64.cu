@@ -1078,6 +1078,11 @@ cudaError_t launch_geometry(const GeomArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+cudaError_t launch_geom_ghosts(const GeomArgs& a, cudaStream_t s) {
+  if (a.mesh.g > 0) k_geom_ghosts<<<blocks(a.mesh.g), kBlock, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_cfl(const StepArgs& a, cudaStream_t s, bool fill_ghosts) {
   const int total = a.mesh.n + (fill_ghosts ? a.mesh.g : 0);
   if (a.cell_problem)

@@ -23,9 +23,6 @@ __device__ __forceinline__ void store4(double* out, int i, double a, double b, d
   reinterpret_cast<double2*>(out)[2 * i] = make_double2(a, b);
   reinterpret_cast<double2*>(out)[2 * i + 1] = make_double2(c, d);
 }
-__device__ __forceinline__ int orig_of(const MeshDev& m, int p) {
-  return p < m.n ? p : m.ghost_source[p - m.n];
-}
 // computational_cell_2d.cpp:59-68 ComputationalCellAddMult
 __device__ __forceinline__ void addmult(Cell& r, const Cell& o, double s) {
   r.d += o.d * s;

@@ -130,6 +130,9 @@ struct MeshSlot {
   rg::GeomDev geom{};
   rg::MixedGeom g32{};
   rg_error geom_error{};  // reconstruction failure found by the geometry pass
+  // the FP64 per-face / per-cell geometry is formed (an FP32-mixed handle
+  // without tracers uploads only its FP32 geometry: ensure_geom64)
+  bool geom64 = true;
   cudaEvent_t last_use = nullptr;
 };
 
@@ -233,6 +236,8 @@ rg::MixedArgs mixed_args(rg_handle* h);
 void drop_graph(rg_handle* h);
 rg_status require(rg_handle* h, bool cells, bool ext, bool ev, bool fluxes);
 rg_status mesh_error(rg_handle* h);
+// forms the active slot's FP64 geometry where an FP32-mixed upload left it out
+rg_status ensure_geom64(rg_handle* h);
 // frees the differentiation buffers (rg_destroy; a new mesh drops them too)
 void adjoint_release(rg_handle* h);
 // tracers or stickers configured (rg_tracer_api.cu)

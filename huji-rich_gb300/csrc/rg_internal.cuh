@@ -119,6 +119,11 @@ __host__ __device__ inline unsigned long long err_key(int step, int phase, long 
 #ifdef __CUDACC__
 // Records an error; keeps the smallest key.  The lock wait is bounded: if it
 // times out the key is still min-reduced and the value may be stale.
+// the real cell a point stands for (a ghost: the cell it copies)
+__device__ __forceinline__ int orig_of(const MeshDev& m, int p) {
+  return p < m.n ? p : m.ghost_source[p - m.n];
+}
+
 __device__ inline void record_error(DevStatus* st, int step, int status, int phase, long long index,
                                     double value) {
   const unsigned long long key = err_key(step, phase, index);
@@ -338,6 +343,7 @@ cudaError_t launch_problems(const MeshDev& m, const int* offsets, int P, int* ce
                             cudaStream_t s);
 cudaError_t launch_cell_order(const MeshDev& m, int* order, int* cflags, cudaStream_t s);
 cudaError_t launch_geometry(const GeomArgs& a, cudaStream_t s);
+cudaError_t launch_geom_ghosts(const GeomArgs& a, cudaStream_t s);  // the ghost part of launch_geometry
 cudaError_t launch_cfl(const StepArgs& a, cudaStream_t s, bool fill_ghosts);
 cudaError_t launch_ghost_fill(const StepArgs& a, cudaStream_t s);
 cudaError_t launch_slopes(const StepArgs& a, cudaStream_t s);

@@ -2,8 +2,10 @@
 //
 // Reconstruction (LinearGaussImproved / piecewise constant), HLLC and the
 // CFL bound run in FP32 (FMA allowed) on FP32 copies of the primitives and of
-// the geometry; the geometry itself is computed in FP64 by the geometry pass
-// (rg_fp64.cu) and rounded once per mesh upload.  FP64 stays where the
+// the geometry.  The FP32 geometry is formed once per mesh upload from FP64
+// coordinate differences (k_geom_faces32, k_geom_cells32), or rounded from
+// the FP64 geometry pass (rg_fp64.cu) where FP64 passes run on the same mesh
+// (tracers, differentiation).  FP64 stays where the
 // precision is needed: cell volumes, the extensive accumulation (each face's
 // dt*area-scaled flux is widened to FP64 and summed per cell in ascending
 // face order, so every face adds exactly what its neighbour subtracts) and
@@ -17,6 +19,7 @@
 
 #include "rg_adjoint.cuh"
 #include "rg_convert.cuh"
+#include "rg_div.cuh"
 #include "rg_mixed.cuh"
 
 namespace rg {
@@ -105,6 +108,127 @@ __global__ void __launch_bounds__(kBlock) k_geom32(MixedGeomArgs a) {
     const double2 u = g.ghost_unit[q];
     a.ghost_unit[q] = make_float2(narrow(u.x), narrow(u.y));
   }
+}
+
+// FP32 geometry without the FP64 pass.  Each FP32 value below is formed
+// from FP64 coordinate differences (points, face vertices, CMs: the
+// cancelling operations), each rounded once, and then in FP32; it lies
+// within a few FP32 ulps of the rounded FP64 value k_geom32 would copy, at a
+// fraction of the FP64-pipe work (GB300: 2 FP64 operations per clock per SM).
+__global__ void __launch_bounds__(kBlock) k_geom_faces32(GeomArgs ga, MixedGeomArgs a) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const MeshDev& m = ga.mesh;
+  if (e >= m.e || mesh_rejected(m)) return;
+  const int2 fc = m.face_cells[e];
+  const dbl4 v = m.face_vertices[e];
+  // Parallel(edge) = second - first; calcArea = its length
+  const float px = narrow(v.z - v.x), py = narrow(v.w - v.y);
+  const float area = sqrtf(px * px + py * py);
+  a.par[e] = make_float2(px, py);
+  a.area[e] = area;
+  if (a.xarea != a.area) a.xarea[e] = narrow(a.g64.xarea[e]);
+  const double2 x0 = m.points[fc.x], x1 = m.points[fc.y];
+  const double ddx = x1.x - x0.x, ddy = x1.y - x0.y;
+  // |x1 - x0| in FP64 for the face velocities, as k_geom_faces forms it
+  // (products and sum rounded separately: this file allows contraction)
+  const double dab = root(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)));
+  ga.dab[e] = dab;
+  const float dx = narrow(ddx), dy = narrow(ddy);
+  if (ga.order == 1) {
+    a.nrm[e] = make_float2(dx, dy);
+    a.nabs[e] = sqrtf(dx * dx + dy * dy);
+  } else {
+    // calc_parallel_normal: the part of w = (vertex - point) normal to the
+    // face, p_perp (p_perp . w) / |p|^2 with p_perp = (-p.y, p.x).  The flux
+    // reads only its direction (n / |n|), so it is kept as +-p_perp with
+    // |n| = |p|: the two periodic images of a face then carry bit-equal
+    // normals and fluxes, and what one cell loses the other gains.
+    const bool real0 = fc.x >= 0 && fc.x < m.n;
+    const float wx = real0 ? narrow(v.x - x0.x) : narrow(x1.x - v.x);
+    const float wy = real0 ? narrow(v.y - x0.y) : narrow(x1.y - v.y);
+    const bool up = px * wy - py * wx >= 0.0f;
+    a.nrm[e] = up ? make_float2(-py, px) : make_float2(py, -px);
+    a.nabs[e] = area;
+  }
+  const double mx = (v.x + v.z) * 0.5, my = (v.y + v.w) * 0.5;
+  const double2 c0 = m.cms[fc.x], c1 = m.cms[fc.y];
+  const float2 d0 = make_float2(narrow(mx - c0.x), narrow(my - c0.y));
+  const float2 d1 = make_float2(narrow(mx - c1.x), narrow(my - c1.y));
+  a.dm0[e] = d0;
+  a.dm1[e] = d1;
+  // calc_naive_slope's r_ij (as the first cell sees it) and c_ij
+  const float s = area / narrow(dab);
+  a.rij[e] = make_float2(dx * s, dy * s);
+  a.cij[e] = make_float2(0.5f * (d0.x + d1.x), 0.5f * (d0.y + d1.y));
+}
+
+__global__ void __launch_bounds__(kBlock) k_geom_cells32(GeomArgs ga, MixedGeomArgs a) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const MeshDev& m = ga.mesh;
+  if (mesh_rejected(m)) return;
+  if (t < m.g) {
+    const double2 u = a.g64.ghost_unit[t];
+    a.ghost_unit[t] = make_float2(narrow(u.x), narrow(u.y));
+  }
+  if (t >= m.n) return;
+  const int i = ga.cell_order ? ga.cell_order[t] : t;
+  const double width = root(quot(m.volume[i], kPi));
+  ga.width[i] = width;
+  a.width[i] = narrow(width);
+  a.inv_cd_volume[i] = __frcp_rn(narrow(m.cd_volume[i]));
+  const int b = m.cell_off[i], nn = m.cell_off[i + 1] - b;
+  if (ga.cflags[i] & kCellBoundarySlope) {
+    // GetBoundarySlope's sums over the CM offsets
+    const double2 cci = m.cms[i];
+    float sxsy = 0, sy2 = 0, sx2 = 0;
+    for (int k = 0; k < nn; ++k) {
+      const int e = m.cell_faces[b + k];
+      const int2 fc = m.face_cells[e];
+      const bool first = fc.x == i;
+      const int other = first ? fc.y : fc.x;
+      const bool mirror = orig_of(m, fc.x) == orig_of(m, fc.y);
+      ga.nbr[b + k] = static_cast<uint32_t>(other) | (mirror ? kNbrMirror : 0u) | (first ? kNbrFirst : 0u);
+      const double2 co = m.cms[other];
+      const float dx = narrow(co.x - cci.x), dy = narrow(co.y - cci.y);
+      const float2 d = first ? a.dm0[e] : a.dm1[e];
+      a.ent[b + k] = make_float4(dx, dy, d.x, d.y);
+      a.fsign[b + k] = e | (first ? static_cast<int>(0x80000000u) : 0);
+      sxsy += dy * dx;
+      sx2 += dx * dx;
+      sy2 += dy * dy;
+    }
+    a.minv[i] = make_float4(sxsy, sx2, sy2, sxsy * sxsy - sx2 * sy2);
+    return;
+  }
+  const bool too_many = nn > kMaxNaiveNeighbours;
+  if (too_many) record_error(ga.status, 0, RG_ERR_TOO_MANY_NEIGHBORS, 2, i, nn);
+  float m0 = 0, m1 = 0, m2 = 0, m3 = 0;
+  for (int k = 0; k < nn; ++k) {
+    const int e = m.cell_faces[b + k];
+    const int2 fc = m.face_cells[e];
+    const bool first = fc.x == i;
+    ga.nbr[b + k] = static_cast<uint32_t>(first ? fc.y : fc.x) | (first ? kNbrFirst : 0u);
+    const float2 r = a.rij[e], c = a.cij[e];
+    const float rx = first ? r.x : -r.x, ry = first ? r.y : -r.y;
+    m0 -= c.x * rx;
+    m1 -= c.y * rx;
+    m2 -= c.x * ry;
+    m3 -= c.y * ry;
+    const float2 d = first ? a.dm0[e] : a.dm1[e];
+    a.ent[b + k] = make_float4(rx * 0.5f, ry * 0.5f, d.x, d.y);
+    a.fsign[b + k] = e | (first ? static_cast<int>(0x80000000u) : 0);
+  }
+  if (too_many) {
+    a.minv[i] = make_float4(0, 0, 0, 0);
+    return;
+  }
+  const float vol = narrow(m.volume[i]);
+  m0 += vol;
+  m3 += vol;
+  const float det = m0 * m3 - m1 * m2;
+  if (fabsf(det) < 1e-10f * vol * vol) record_error(ga.status, 0, RG_ERR_SINGULAR_MATRIX, 2, i, det);
+  const float di = 1.0f / det;
+  a.minv[i] = make_float4(m3 * di, -m1 * di, -m2 * di, m0 * di);
 }
 
 // ------------------------------------------------------------ conversions
@@ -906,6 +1030,13 @@ cudaError_t launch_geom32(const MixedGeomArgs& a, cudaStream_t s) {
   const int work = a.e > a.m ? (a.e > a.n ? a.e : a.n) : (a.m > a.n ? a.m : a.n);
   const int nb = blocks(work > 0 ? work : 1);
   k_geom32<<<nb < 4096 ? nb : 4096, kBlock, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_geom32_direct(const GeomArgs& ga, const MixedGeomArgs& a, cudaStream_t s) {
+  if (a.e > 0) k_geom_faces32<<<blocks(a.e), kBlock, 0, s>>>(ga, a);
+  const int work = a.n > a.g ? a.n : a.g;
+  if (work > 0) k_geom_cells32<<<blocks(work), kBlock, 0, s>>>(ga, a);
   return cudaGetLastError();
 }
 

@@ -47,6 +47,10 @@ struct MixedGeomArgs {
   float2* ghost_unit;
   float* inv_cd_volume;
   const unsigned long long* invalid;  // MeshDev::invalid of the upload
+  // launch_geom32_direct's per-face halves of the naive slope (FP32), kept
+  // between its face and cell passes in the FP64 r_ij / c_ij storage
+  float2* rij;
+  float2* cij;
 };
 
 struct MixedArgs {
@@ -95,6 +99,12 @@ struct MixedArgs {
 };
 
 cudaError_t launch_geom32(const MixedGeomArgs& a, cudaStream_t s);
+// The FP32 geometry straight from the FP64 inputs, without the FP64 geometry
+// pass: coordinate differences in FP64 rounded once to FP32, everything
+// after them in FP32.  Also writes the FP64 values the FP64 motion kernels
+// read (|x1 - x0| per face, sqrt(V/pi) per cell, bit-equal to the FP64 pass)
+// and the neighbour words; the ghost pass (launch_geom_ghosts) runs first.
+cudaError_t launch_geom32_direct(const GeomArgs& ga, const MixedGeomArgs& a, cudaStream_t s);
 cudaError_t launch_cells_to32(const double* c64, float4* c32, int n, cudaStream_t s);
 cudaError_t launch_cells_to64(const float4* c32, double* c64, int n, cudaStream_t s);
 cudaError_t launch_vec2_to32(const double* v64, float2* v32, int n, cudaStream_t s);

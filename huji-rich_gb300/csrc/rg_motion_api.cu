@@ -141,6 +141,7 @@ rg_status rg_set_physical_geometry(rg_handle* h, const rg_physical_geometry* pg)
 
 rg_status rg_get_geometry(rg_handle* h, double* volume, double* cm_xy, double* cd_volume, double* cd_area) {
   if (rg_status st = require(h, false, false, false, false)) return st;
+  if (cd_area) RG_TRY(ensure_geom64(h));
   MeshSlot* s = active_slot(h);
   RG_CUDA(h, cudaStreamSynchronize(h->stream));
   const size_t n = static_cast<size_t>(s->n), np = n + static_cast<size_t>(s->g);

@@ -132,7 +132,9 @@ rg_status rg_set_tracer_config(rg_handle* h, const rg_tracer_config* cfg) {
     return RG_OK;
   }
   if (nt_changed) h->have_tr = h->have_tr_ext = false;
-  return tracer_buffers(h);
+  RG_TRY(tracer_buffers(h));
+  // the tracer passes read the FP64 geometry
+  return ensure_geom64(h);
 }
 
 rg_status rg_set_tracers(rg_handle* h, const double* tracers) {

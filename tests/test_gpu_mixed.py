@@ -1,5 +1,6 @@
-"""FP32-mixed form: reconstruction, HLLC and CFL in FP32; geometry, volumes,
-extensive accumulation and the internal-energy conversion in FP64.
+"""FP32-mixed form: reconstruction, HLLC and CFL in FP32 (on FP32 geometry
+formed from FP64 coordinate differences); volumes, centroids, the point
+motion, extensive accumulation and the internal-energy conversion in FP64.
 
 Accuracy is stated against the FP64 path, which the other GPU tests pin
 bit-for-bit to the oracle and the reference fixtures: the relative density
@@ -13,6 +14,7 @@ import pytest
 import oracle
 import richgpu
 import synthetic
+from test_oracle_golden import exact
 
 pytestmark = pytest.mark.gpu
 
@@ -109,3 +111,42 @@ def test_mixed_reports_negative_density():
         with pytest.raises(richgpu.RichError) as ei:
             h.step()
         assert ei.value.status == 10 and ei.value.index == 12
+
+
+def test_direct_fp32_geometry_against_rounded_fp64_geometry():
+    """Without tracers an FP32-mixed upload forms the FP32 geometry straight
+    from the FP64 inputs; asking for the FP64 face areas (rg_get_geometry)
+    forms the FP64 geometry and rounds the FP32 copies from it.  The FP64
+    motion reads the same FP64 widths and |x1 - x0| either way (point and face
+    velocities bit-equal on the same state), and the states after a few
+    RoundCells steps agree to FP32 round-off."""
+    mesh = synthetic.lattice_mesh(128, 128, (-1.0, 1.0, -1.0, 1.0), "rigid", seed=2)
+    cells = synthetic.sedov_cells(mesh, 5 / 3)
+    ext = oracle.init_extensives(mesh, cells, 5 / 3)
+    out = []
+    for rounded in (False, True):
+        with richgpu.Handle(gamma=5 / 3, order=2, ghost_kind=0, precision=1, device=0) as h:
+            h.set_outer_box(-1.0, 1.0, -1.0, 1.0)
+            h.upload_mesh(mesh, flags=richgpu.MESH_DEVICE_GEOMETRY)
+            h.set_point_motion(kind=2, edges=0, chi=0.15, eta=0.02)
+            if rounded:
+                h.geometry(areas=True)
+            h.set_cells(cells)
+            h.set_extensives(ext)
+            steps = []
+            for _ in range(4):
+                dt, pv = h.advance_begin()
+                steps.append((dt, pv, h.edge_velocities()))
+                h.cell_update()
+            out.append((steps, h.get_cells(), h.get_extensives()))
+    (s0, c0, e0), (s1, c1, e1) = out
+    exact(s0[0][1], s1[0][1])
+    exact(s0[0][2], s1[0][2])
+    for k in range(4):
+        assert abs(s0[k][0] - s1[k][0]) <= 1e-6 * s1[k][0]
+    l1 = np.abs(c0[:, 0] - c1[:, 0]).sum() / np.abs(c1[:, 0]).sum()
+    assert l1 <= 1e-7, l1
+    assert np.all(np.isfinite(c0))
+    # conservation holds on either geometry
+    t0 = ext.sum(0)
+    assert abs(e0.sum(0)[0] - t0[0]) <= 1e-13 * abs(t0[0])
