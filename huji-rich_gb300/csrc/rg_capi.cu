@@ -538,8 +538,7 @@ rg_status geometry_pass(rg_handle* h, MeshSlot& s, const rg::MeshDev& gm, bool f
     m32.inv_cd_volume = at<float>(b, s.lay.icdv32);
     m32.cd_volume = s.mesh.cd_volume;
     m32.invalid = gm.invalid;
-    m32.rij = at<float2>(b, s.lay.rij);
-    m32.cij = at<float2>(b, s.lay.cij);
+    m32.frec = at<float4>(b, s.lay.frec32);
     if (full64) {
       RG_CUDA(h, rg::launch_geom32(m32, st));
     } else {

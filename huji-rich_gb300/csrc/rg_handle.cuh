@@ -63,7 +63,7 @@ struct SlotLayout {
   size_t area, nrm, nabs, par, dm0, dm1, dab, rij, cij, xarea, width, minv, cflags, nbr, hr, ghost_real,
       ghost_unit, cell_order;
   size_t nrm32, nabs32, par32, area32, xarea32, dm0_32, dm1_32, width32, minv32, ent32, fsign32, gunit32, icdv32,
-      total;
+      frec32, total;
   bool own_xarea = false;  // a non-slab PhysicalGeometry: CacheData areas differ from the edge lengths
   void compute(int n, int g, int e, int m, bool mixed, bool cyl = false) {
     own_xarea = cyl;
@@ -117,6 +117,7 @@ struct SlotLayout {
     fsign32 = take(k * 4 * static_cast<size_t>(m));
     gunit32 = take(k * 8 * static_cast<size_t>(g));
     icdv32 = take(k * 4 * static_cast<size_t>(n));
+    frec32 = take(k * 32 * static_cast<size_t>(e));
     total = o;
   }
 };

@@ -110,56 +110,55 @@ __global__ void __launch_bounds__(kBlock) k_geom32(MixedGeomArgs a) {
   }
 }
 
-// FP32 geometry without the FP64 pass.  Each FP32 value below is formed
-// from FP64 coordinate differences (points, face vertices, CMs: the
-// cancelling operations), each rounded once, and then in FP32; it lies
-// within a few FP32 ulps of the rounded FP64 value k_geom32 would copy, at a
-// fraction of the FP64-pipe work (GB300: 2 FP64 operations per clock per SM).
+// The FP32-mixed geometry without the FP64 geometry pass.  The face
+// geometry is formed in FP64 and rounded once, as the FP64 pass forms it:
+// vertex differences (Parallel), areas, centroid offsets (CalcCentroid - CM)
+// and |x1 - x0|.  The normal is kept as +-(-p.y, p.x) with |n| = |p|, p the
+// FP64 vertex difference: calc_parallel_normal's direction, exact in FP64 and
+// bit-equal for the two periodic images of a face (so what one cell loses
+// the other gains).  The reconstruction stencil (r_ij, c_ij, the naive
+// slope's matrix and inverse, the boundary slope's sums) is formed in FP32,
+// as the FP32 reconstruction uses it.  The FP64 pass costs GB300's FP64 pipe
+// (2 operations per clock per SM) for quantities that were only rounded.
 __global__ void __launch_bounds__(kBlock) k_geom_faces32(GeomArgs ga, MixedGeomArgs a) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   const MeshDev& m = ga.mesh;
   if (e >= m.e || mesh_rejected(m)) return;
   const int2 fc = m.face_cells[e];
   const dbl4 v = m.face_vertices[e];
-  // Parallel(edge) = second - first; calcArea = its length
-  const float px = narrow(v.z - v.x), py = narrow(v.w - v.y);
-  const float area = sqrtf(px * px + py * py);
+  // products and sums rounded separately below (this file allows contraction;
+  // the FP64 pass does not)
+  const double ax = v.x - v.z, ay = v.y - v.w;
+  const float area = narrow(root(__dadd_rn(__dmul_rn(ax, ax), __dmul_rn(ay, ay))));
+  // second - first = -(first - second) exactly
+  const float px = -narrow(ax), py = -narrow(ay);
   a.par[e] = make_float2(px, py);
   a.area[e] = area;
   if (a.xarea != a.area) a.xarea[e] = narrow(a.g64.xarea[e]);
   const double2 x0 = m.points[fc.x], x1 = m.points[fc.y];
   const double ddx = x1.x - x0.x, ddy = x1.y - x0.y;
-  // |x1 - x0| in FP64 for the face velocities, as k_geom_faces forms it
-  // (products and sum rounded separately: this file allows contraction)
   const double dab = root(__dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)));
-  ga.dab[e] = dab;
-  const float dx = narrow(ddx), dy = narrow(ddy);
+  ga.dab[e] = dab;  // the face velocities read it in FP64
+  const float dx = narrow(ddx), dy = narrow(ddy), dab32 = narrow(dab);
   if (ga.order == 1) {
-    a.nrm[e] = make_float2(dx, dy);
-    a.nabs[e] = sqrtf(dx * dx + dy * dy);
+    a.nrm[e] = make_float2(dx, dy);  // x1 - x0
+    a.nabs[e] = dab32;
   } else {
-    // calc_parallel_normal: the part of w = (vertex - point) normal to the
-    // face, p_perp (p_perp . w) / |p|^2 with p_perp = (-p.y, p.x).  The flux
-    // reads only its direction (n / |n|), so it is kept as +-p_perp with
-    // |n| = |p|: the two periodic images of a face then carry bit-equal
-    // normals and fluxes, and what one cell loses the other gains.
-    const bool real0 = fc.x >= 0 && fc.x < m.n;
-    const float wx = real0 ? narrow(v.x - x0.x) : narrow(x1.x - v.x);
-    const float wy = real0 ? narrow(v.y - x0.y) : narrow(x1.y - v.y);
-    const bool up = px * wy - py * wx >= 0.0f;
+    // pointing from the first neighbour to the second, as w - (w.p) p / p.p
+    // of calc_parallel_normal does (w from a point to the face's line)
+    const bool up = px * dy - py * dx >= 0.0f;
     a.nrm[e] = up ? make_float2(-py, px) : make_float2(py, -px);
     a.nabs[e] = area;
   }
-  const double mx = (v.x + v.z) * 0.5, my = (v.y + v.w) * 0.5;
+  const double mx = __dmul_rn(__dadd_rn(v.x, v.z), 0.5), my = __dmul_rn(__dadd_rn(v.y, v.w), 0.5);
   const double2 c0 = m.cms[fc.x], c1 = m.cms[fc.y];
-  const float2 d0 = make_float2(narrow(mx - c0.x), narrow(my - c0.y));
-  const float2 d1 = make_float2(narrow(mx - c1.x), narrow(my - c1.y));
-  a.dm0[e] = d0;
-  a.dm1[e] = d1;
-  // calc_naive_slope's r_ij (as the first cell sees it) and c_ij
-  const float s = area / narrow(dab);
-  a.rij[e] = make_float2(dx * s, dy * s);
-  a.cij[e] = make_float2(0.5f * (d0.x + d1.x), 0.5f * (d0.y + d1.y));
+  const float4 dm = make_float4(narrow(mx - c0.x), narrow(my - c0.y), narrow(mx - c1.x), narrow(my - c1.y));
+  a.dm0[e] = make_float2(dm.x, dm.y);
+  a.dm1[e] = make_float2(dm.z, dm.w);
+  // calc_naive_slope's r_ij as the first neighbour sees it (FP32)
+  const float s = area / dab32;
+  a.frec[2 * e] = make_float4(dx * s, dy * s, __int_as_float(fc.x), __int_as_float(fc.y));
+  a.frec[2 * e + 1] = dm;
 }
 
 __global__ void __launch_bounds__(kBlock) k_geom_cells32(GeomArgs ga, MixedGeomArgs a) {
@@ -182,16 +181,16 @@ __global__ void __launch_bounds__(kBlock) k_geom_cells32(GeomArgs ga, MixedGeomA
     const double2 cci = m.cms[i];
     float sxsy = 0, sy2 = 0, sx2 = 0;
     for (int k = 0; k < nn; ++k) {
-      const int e = m.cell_faces[b + k];
-      const int2 fc = m.face_cells[e];
-      const bool first = fc.x == i;
-      const int other = first ? fc.y : fc.x;
-      const bool mirror = orig_of(m, fc.x) == orig_of(m, fc.y);
+      const int e = __ldg(m.cell_faces + b + k);
+      const float4 r0 = __ldg(a.frec + 2 * e), r1 = __ldg(a.frec + 2 * e + 1);
+      const int f0 = __float_as_int(r0.z), f1 = __float_as_int(r0.w);
+      const bool first = f0 == i;
+      const int other = first ? f1 : f0;
+      const bool mirror = orig_of(m, f0) == orig_of(m, f1);
       ga.nbr[b + k] = static_cast<uint32_t>(other) | (mirror ? kNbrMirror : 0u) | (first ? kNbrFirst : 0u);
       const double2 co = m.cms[other];
       const float dx = narrow(co.x - cci.x), dy = narrow(co.y - cci.y);
-      const float2 d = first ? a.dm0[e] : a.dm1[e];
-      a.ent[b + k] = make_float4(dx, dy, d.x, d.y);
+      a.ent[b + k] = make_float4(dx, dy, first ? r1.x : r1.z, first ? r1.y : r1.w);
       a.fsign[b + k] = e | (first ? static_cast<int>(0x80000000u) : 0);
       sxsy += dy * dx;
       sx2 += dx * dx;
@@ -203,19 +202,21 @@ __global__ void __launch_bounds__(kBlock) k_geom_cells32(GeomArgs ga, MixedGeomA
   const bool too_many = nn > kMaxNaiveNeighbours;
   if (too_many) record_error(ga.status, 0, RG_ERR_TOO_MANY_NEIGHBORS, 2, i, nn);
   float m0 = 0, m1 = 0, m2 = 0, m3 = 0;
+#pragma unroll 2
   for (int k = 0; k < nn; ++k) {
-    const int e = m.cell_faces[b + k];
-    const int2 fc = m.face_cells[e];
-    const bool first = fc.x == i;
-    ga.nbr[b + k] = static_cast<uint32_t>(first ? fc.y : fc.x) | (first ? kNbrFirst : 0u);
-    const float2 r = a.rij[e], c = a.cij[e];
-    const float rx = first ? r.x : -r.x, ry = first ? r.y : -r.y;
-    m0 -= c.x * rx;
-    m1 -= c.y * rx;
-    m2 -= c.x * ry;
-    m3 -= c.y * ry;
-    const float2 d = first ? a.dm0[e] : a.dm1[e];
-    a.ent[b + k] = make_float4(rx * 0.5f, ry * 0.5f, d.x, d.y);
+    const int e = __ldg(m.cell_faces + b + k);
+    const float4 r0 = __ldg(a.frec + 2 * e), r1 = __ldg(a.frec + 2 * e + 1);
+    const int f0 = __float_as_int(r0.z), f1 = __float_as_int(r0.w);
+    const bool first = f0 == i;
+    ga.nbr[b + k] = static_cast<uint32_t>(first ? f1 : f0) | (first ? kNbrFirst : 0u);
+    // -r_ij for the second neighbour; c_ij = centroid - (cm_a + cm_b) / 2
+    const float rx = first ? r0.x : -r0.x, ry = first ? r0.y : -r0.y;
+    const float cx = 0.5f * (r1.x + r1.z), cy = 0.5f * (r1.y + r1.w);
+    m0 -= cx * rx;
+    m1 -= cy * rx;
+    m2 -= cx * ry;
+    m3 -= cy * ry;
+    a.ent[b + k] = make_float4(rx * 0.5f, ry * 0.5f, first ? r1.x : r1.z, first ? r1.y : r1.w);
     a.fsign[b + k] = e | (first ? static_cast<int>(0x80000000u) : 0);
   }
   if (too_many) {

@@ -47,10 +47,10 @@ struct MixedGeomArgs {
   float2* ghost_unit;
   float* inv_cd_volume;
   const unsigned long long* invalid;  // MeshDev::invalid of the upload
-  // launch_geom32_direct's per-face halves of the naive slope (FP32), kept
-  // between its face and cell passes in the FP64 r_ij / c_ij storage
-  float2* rij;
-  float2* cij;
+  // launch_geom32_direct's per-face record, two float4 per face, from its
+  // face pass to its cell pass: {r_ij.x, r_ij.y, first, second} (the two
+  // neighbours' indices as bit patterns) and {dm0.x, dm0.y, dm1.x, dm1.y}
+  float4* frec;
 };
 
 struct MixedArgs {
@@ -99,11 +99,14 @@ struct MixedArgs {
 };
 
 cudaError_t launch_geom32(const MixedGeomArgs& a, cudaStream_t s);
-// The FP32 geometry straight from the FP64 inputs, without the FP64 geometry
-// pass: coordinate differences in FP64 rounded once to FP32, everything
-// after them in FP32.  Also writes the FP64 values the FP64 motion kernels
-// read (|x1 - x0| per face, sqrt(V/pi) per cell, bit-equal to the FP64 pass)
-// and the neighbour words; the ghost pass (launch_geom_ghosts) runs first.
+// The FP32-mixed path's geometry without the FP64 geometry pass: the face
+// geometry (vertex differences, areas, centroid offsets, |x1 - x0|) in FP64
+// rounded once, the normal as the exact perpendicular of the FP64 vertex
+// difference, and the reconstruction stencil (the naive slope's matrix, its
+// inverse, 0.5 r_ij) in FP32.  Also writes the FP64 values the FP64 motion
+// kernels read (|x1 - x0| per face, sqrt(V/pi) per cell, bit-equal to the
+// FP64 pass) and the neighbour words; the ghost pass (launch_geom_ghosts)
+// runs first.
 cudaError_t launch_geom32_direct(const GeomArgs& ga, const MixedGeomArgs& a, cudaStream_t s);
 cudaError_t launch_cells_to32(const double* c64, float4* c32, int n, cudaStream_t s);
 cudaError_t launch_cells_to64(const float4* c32, double* c64, int n, cudaStream_t s);
