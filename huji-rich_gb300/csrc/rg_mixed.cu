@@ -778,32 +778,30 @@ __device__ __forceinline__ void write32(const MixedArgs& a, int e, int real_side
   if (a.mflux) a.mflux[e] = static_cast<double>(c.m);
 }
 
-template <bool kScaled, bool kBatch>
-__device__ __forceinline__ void k_faces32_lgi_item(const MixedArgs& a, int e) {
+// LinearGaussImproved's face value of point pid at offset dm from its CM
+__device__ __forceinline__ C4 side32(const MixedArgs& a, int pid, float2 dm) {
   const MeshDev& m = a.mesh;
-  const int2 fc = m.face_cells[e];
-  const int ids[2] = {fc.x, fc.y};
-  const float2 dms[2] = {a.g32.dm0[e], a.g32.dm1[e]};
-  C4 side[2];
-#pragma unroll
-  for (int s = 0; s < 2; ++s) {
-    const int pid = ids[s];
-    C4 c = point32(a, pid);
-    int sid = pid;
-    bool zero = false;
-    if (pid >= m.n) {
-      if (a.ghost_kind == RG_GHOST_PERIODIC)
-        sid = m.ghost_source[pid - m.n];
-      else
-        zero = true;
-    }
-    if (!zero) {
-      const C4 gx = ld4(a.slopes32, 2 * sid), gy = ld4(a.slopes32, 2 * sid + 1);
-      addm(c, gx, dms[s].x);
-      addm(c, gy, dms[s].y);
-    }
-    side[s] = c;
+  C4 c = point32(a, pid);
+  int sid = pid;
+  bool zero = false;
+  if (pid >= m.n) {
+    if (a.ghost_kind == RG_GHOST_PERIODIC)
+      sid = m.ghost_source[pid - m.n];
+    else
+      zero = true;
   }
+  if (!zero) {
+    const C4 gx = ld4(a.slopes32, 2 * sid), gy = ld4(a.slopes32, 2 * sid + 1);
+    addm(c, gx, dm.x);
+    addm(c, gy, dm.y);
+  }
+  return c;
+}
+
+// Hllc on face e's two face values, scaled and written
+template <bool kScaled, bool kBatch>
+__device__ __forceinline__ void face32_solve(const MixedArgs& a, int e, int2 fc, const C4& s0, const C4& s1) {
+  const MeshDev& m = a.mesh;
   const float2 w = a.ev_zero ? make_float2(0.0f, 0.0f) : a.ev32[e];
   const float2 n = a.g32.nrm[e], p = a.g32.par[e];
   const float na = a.g32.nabs[e], pa = a.g32.area[e];
@@ -811,14 +809,44 @@ __device__ __forceinline__ void k_faces32_lgi_item(const MixedArgs& a, int e) {
   const int real_side = fc.x < m.n ? fc.x : fc.y;
   const float g = gamma32<kBatch>(a, real_side), igm = inv_gm1_32<kBatch>(a, real_side);
   F4 c;
-  if (!solve32(prim32(g, igm, side[0]), prim32(g, igm, side[1]), vel, n, na, p, pa, c, a, e)) return;
+  if (!solve32(prim32(g, igm, s0), prim32(g, igm, s1), vel, n, na, p, pa, c, a, e)) return;
   write32<kBatch>(a, e, real_side, c, kScaled, a.g32.xarea[e]);
+}
+
+template <bool kScaled, bool kBatch>
+__device__ __forceinline__ void k_faces32_lgi_item(const MixedArgs& a, int e) {
+  const int2 fc = a.mesh.face_cells[e];
+  const C4 s0 = side32(a, fc.x, a.g32.dm0[e]);
+  const C4 s1 = side32(a, fc.y, a.g32.dm1[e]);
+  face32_solve<kScaled, kBatch>(a, e, fc, s0, s1);
 }
 
 template <bool kScaled, bool kBatch>
 __global__ void __launch_bounds__(kMaxBlock) k_faces32_lgi(MixedArgs a) {
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < a.mesh.e; e += gridDim.x * blockDim.x)
     k_faces32_lgi_item<kScaled, kBatch>(a, e);
+}
+
+// Two threads per face (launch-shape build 1): lane s of a pair forms face
+// value s (half the gathers in each thread's dependent chain, twice the
+// threads in flight); the pair swaps the two values with shuffles and the
+// even lane solves and writes.  Each value comes from the same code as in
+// k_faces32_lgi_item, so the fluxes are bit-identical to the one-thread build.
+template <bool kScaled, bool kBatch>
+__global__ void __launch_bounds__(kMaxBlock) k_faces32_lgi_pair(MixedArgs a) {
+  const int s = threadIdx.x & 1;
+  const unsigned pair = 3u << (threadIdx.x & 30);
+  const int stride = (gridDim.x * blockDim.x) >> 1;
+  for (int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 1; e < a.mesh.e; e += stride) {
+    const int2 fc = a.mesh.face_cells[e];
+    const C4 mine = side32(a, s ? fc.y : fc.x, s ? a.g32.dm1[e] : a.g32.dm0[e]);
+    C4 other;
+    other.d = __shfl_xor_sync(pair, mine.d, 1);
+    other.p = __shfl_xor_sync(pair, mine.p, 1);
+    other.vx = __shfl_xor_sync(pair, mine.vx, 1);
+    other.vy = __shfl_xor_sync(pair, mine.vy, 1);
+    if (s == 0) face32_solve<kScaled, kBatch>(a, e, fc, mine, other);
+  }
 }
 
 template <bool kScaled, bool kBatch>
@@ -1105,6 +1133,13 @@ cudaError_t launch_faces32(const MixedArgs& a, cudaStream_t s, bool scaled) {
       b ? k_faces32_pcm<true, true><<<nb, bs, 0, s>>>(a) : k_faces32_pcm<true, false><<<nb, bs, 0, s>>>(a);
     else
       b ? k_faces32_pcm<false, true><<<nb, bs, 0, s>>>(a) : k_faces32_pcm<false, false><<<nb, bs, 0, s>>>(a);
+  } else if (a.shapes.faces.variant == 1) {
+    // two threads per face: the one-thread-per-item grid covers 2 e threads
+    const int np = grid_of(a.shapes.faces, 2 * a.mesh.e);
+    if (scaled)
+      b ? k_faces32_lgi_pair<true, true><<<np, bs, 0, s>>>(a) : k_faces32_lgi_pair<true, false><<<np, bs, 0, s>>>(a);
+    else
+      b ? k_faces32_lgi_pair<false, true><<<np, bs, 0, s>>>(a) : k_faces32_lgi_pair<false, false><<<np, bs, 0, s>>>(a);
   } else {
     if (scaled)
       b ? k_faces32_lgi<true, true><<<nb, bs, 0, s>>>(a) : k_faces32_lgi<true, false><<<nb, bs, 0, s>>>(a);

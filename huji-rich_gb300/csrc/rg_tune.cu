@@ -6,7 +6,8 @@
 // kernel's builds (the slopes kernels and the FP32-mixed update kernel also
 // have register-capped builds for blocks of up to 256 threads; the FP32-mixed
 // slopes kernel a build with its neighbour loops unrolled by two and one
-// that loads the neighbour data up front).  Each
+// that loads the neighbour data up front; the FP32-mixed face kernel one
+// or two threads per face).  Each
 // candidate runs `reps` launches on the handle's stream, on the uploaded mesh
 // and the current state, each timed alone with CUDA events after a write of
 // a buffer larger than L2 (a kernel of a step finds most of its inputs in
@@ -82,11 +83,13 @@ rg_status launch_one(rg_handle* h, int k, const rg::LaunchShape& sh, void* ext_s
 }
 
 // Builds of kernel k on the handle's path: mixed slopes 0-4; mixed update 0,
-// 2, 3 (register-capped); FP64 slopes 0, 2, 3 (register-capped); otherwise 0.
+// 2, 3 (register-capped); mixed faces 0, 1 (two threads per face); FP64
+// slopes 0, 2, 3 (register-capped); otherwise 0.
 bool has_build(const rg_handle* h, int k, int v) {
   if (v == 0) return true;
   if (k == RG_KERNEL_SLOPES) return h->mixed ? v >= 1 && v <= 4 : v == 2 || v == 3;
   if (k == RG_KERNEL_UPDATE) return h->mixed && (v == 2 || v == 3);
+  if (k == RG_KERNEL_FACES) return h->mixed && v == 1;
   return false;
 }
 constexpr int kMaxVariant = 4;

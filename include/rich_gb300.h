@@ -313,6 +313,7 @@ typedef struct {
                          by two), 2, 3 (register-capped: blocks of at most 256 threads,
                          5 or 6 resident per SM) and 4 (up to 8 neighbours loaded up front);
                          the FP32-mixed update kernel 2 and 3 (register-capped); the
+                         FP32-mixed face kernel 1 (two threads per face, second order); the
                          FP64 slopes kernel 2 and 3 (register-capped: blocks of at most
                          256 threads, 3 or 4 resident per SM) */
   float ms[4];        /* rg_autotune: mean time per launch of the chosen shape (ms) */

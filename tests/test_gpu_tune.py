@@ -20,10 +20,12 @@ SHAPES = [
     {"cfl": (512, 152), "slopes": (64, 304), "faces": (256, 152), "update": (128, 608)},
     {"cfl": (32, 7), "slopes": (96, 5), "faces": (480, 3), "update": (64, 1)},
 ]
-# the FP32-mixed slopes kernel's other builds (unrolled, register-capped)
+# the FP32-mixed slopes kernel's other builds (unrolled, register-capped) and the
+# face kernel's two-threads-per-face build
 MIXED_SHAPES = [{"slopes": (128, 0, 1)}, {"slopes": (256, 608, 2)}, {"slopes": (64, 0, 3)},
                 {"slopes": (128, 0, 4)}, {"slopes": (256, 1216, 4)},
-                {"update": (256, 0, 2)}, {"update": (128, 912, 3)}]
+                {"update": (256, 0, 2)}, {"update": (128, 912, 3)},
+                {"faces": (128, 0, 1)}, {"faces": (256, 608, 1)}, {"faces": (96, 5, 1)}]
 
 
 # the FP64 slopes kernel's register-capped builds
