@@ -875,6 +875,17 @@ def batch_measure(lo, hi, steps, warmup, tune, local_rank, barrier=lambda: None)
                           "graph_ms_per_step": graph_ms, "final_cells": h.get_cells(),
                           "launch_shapes": {kk: [v["block"], v["max_blocks"], v["variant"]] for kk, v in shapes.items()},
                           "time_min": float(times.min()), "time_max": float(times.max())}
+        if precision == 1:
+            # the same steps as one cooperative launch (RG_STEP_PERSISTENT)
+            h.set_step_mode(richgpu.STEP_PERSISTENT)
+            h.run(1)
+            with torch.cuda.stream(stream):
+                e0.record()
+            h.run(steps)
+            with torch.cuda.stream(stream):
+                e1.record()
+            torch.cuda.synchronize()
+            res[precision]["persistent_ms_per_step"] = e0.elapsed_time(e1) / steps
         h.close()
     return res, mesh, gen_s
 
@@ -921,12 +932,14 @@ def batch_block(steps=20, warmup=3, problems=512, tune=True, cpu=True):
             "steps": steps, "warmup": max(warmup, 3), "value": n / (res[1]["ms_per_step"] * 1e-3), "unit": UNIT,
             "ms_per_step": res[1]["ms_per_step"], "dtype": "f32+f64",
             "graph_value": n / (res[1]["graph_ms_per_step"] * 1e-3),
+            "persistent_value": n / (res[1]["persistent_ms_per_step"] * 1e-3),
             "l1_density_vs_fp64": float(np.abs(c32[:, 0] - c64[:, 0]).sum() / np.abs(c64[:, 0]).sum()),
             "fp32mixed": res[1], "fp64": {"value": n / (res[0]["ms_per_step"] * 1e-3), **res[0]},
             "roofline": batch_roofline(res, mesh),
             "cpu_baseline": batch_cpu_baseline(problems) if cpu else None,
             "generation_s": gen_s, "gpu_launches_per_step": 4,
-            "launch": "one launch per phase for all problems, per-problem dt; graph of one step replayed"}
+            "launch": "one launch per phase for all problems, per-problem dt; graph of one step replayed; "
+                      "persistent: the whole run in one cooperative launch (RG_STEP_PERSISTENT)"}
 
 
 def run_batch(args, world, rank, local_rank):
@@ -968,8 +981,9 @@ def run_batch(args, world, rank, local_rank):
         from torch.distributed import ReduceOp
         l1 = reduce(l1, ReduceOp.MAX)
         for r in res.values():
-            for key in ("ms_per_step", "graph_ms_per_step"):
-                r[key] = reduce(r[key], ReduceOp.MAX)
+            for key in ("ms_per_step", "graph_ms_per_step", "persistent_ms_per_step"):
+                if key in r:
+                    r[key] = reduce(r[key], ReduceOp.MAX)
     n = int(reduce(float(mesh.n_cells), dist.ReduceOp.SUM if dist is not None else None))
     n_faces = int(reduce(float(mesh.n_faces), dist.ReduceOp.SUM if dist is not None else None))
     if rank != 0:
@@ -990,6 +1004,7 @@ def run_batch(args, world, rank, local_rank):
             "fp32mixed": {k: v for k, v in res[1].items()},
             "fp64": {"value": n / (res[0]["ms_per_step"] * 1e-3), **res[0]},
             "graph_value_fp32mixed": n / (res[1]["graph_ms_per_step"] * 1e-3),
+            "persistent_value_fp32mixed": n / (res[1]["persistent_ms_per_step"] * 1e-3),
             "cpu_baseline": cpu, "gpu_launches": 4 * args.steps}
     print(json.dumps(line), flush=True)
     if dist is not None:

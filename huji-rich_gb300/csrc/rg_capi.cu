@@ -481,6 +481,36 @@ rg_status enqueue_step(rg_handle* h, int step, cudaEvent_t* ev = nullptr) {
   return RG_OK;
 }
 
+// The persistent form takes a batch on the FP32-mixed path, second order,
+// hdsim::TimeAdvance, without tracers, stickers or rule tables.
+bool persistent_ok(const rg_handle* h) {
+  return h->mixed && h->n_problems > 0 && h->cfg.order == 2 && !h->heun && !tracers_on(h) && h->n_rules == 0;
+}
+
+// rg_run of a batch as one cooperative launch (RG_STEP_PERSISTENT)
+rg_status run_persistent(rg_handle* h, int32_t n_steps, double* dt_out) {
+  if (!persistent_ok(h)) return invalid(h, -20, h->step_mode);
+  RG_TRY(reset_status(h, h->d_status, h->stream));
+  if (n_steps > 0) {
+    RG_CUDA(h, h->barrier.ensure(sizeof(rg::GridBarrier)));
+    RG_CUDA(h, h->dt_trace.ensure(sizeof(double) * static_cast<size_t>(n_steps)));
+    rg::MixedArgs a = mixed_args(h);
+    double* trace = static_cast<double*>(h->dt_trace.p);
+    RG_CUDA(h, rg::launch_run32_persistent(a, n_steps, 0, static_cast<rg::GridBarrier*>(h->barrier.p), 0, trace,
+                                           h->stream, nullptr));
+    if (dt_out) {
+      RG_CUDA(h, h->host_dts.ensure(sizeof(double) * static_cast<size_t>(n_steps)));
+      RG_CUDA(h, cudaMemcpyAsync(h->host_dts.p, trace, sizeof(double) * static_cast<size_t>(n_steps),
+                                 cudaMemcpyDeviceToHost, h->stream));
+    }
+  }
+  h->dt_next_ready = false;
+  h->have_fluxes = false;
+  const rg_status st = collect(h, h->d_status, h->stream);
+  if (dt_out && n_steps > 0) std::memcpy(dt_out, h->host_dts.p, sizeof(double) * static_cast<size_t>(n_steps));
+  return st;
+}
+
 }  // namespace
 
 namespace rgh {
@@ -594,6 +624,7 @@ const char* rg_status_string(rg_status s) {
     case RG_ERR_HLLC_WAVE_SPEEDS: return "Invalid wave speeds in hllc solver";
     case RG_ERR_SINGULAR_MATRIX: return "Singular matrix";
     case RG_ERR_TOO_MANY_NEIGHBORS: return "Cell has too many neighbors";
+    case RG_ERR_TIMEOUT: return "a device-side wait timed out";
   }
   return "unknown status";
 }
@@ -664,6 +695,8 @@ rg_status rg_destroy(rg_handle* h) {
   h->lag_ev.release();
   h->pv.release();
   h->flag_buf.release();
+  h->barrier.release();
+  h->dt_trace.release();
   h->cells.release();
   h->ext.release();
   h->ev.release();
@@ -1184,6 +1217,7 @@ rg_status rg_run(rg_handle* h, int32_t n_steps, double* dt_out) {
   if (n_steps < 0) return RG_ERR_INVALID_ARGUMENT;
   if (rg_status st = mesh_error(h)) return st;
   h->last = rg_error{};
+  if (h->step_mode == RG_STEP_PERSISTENT) return run_persistent(h, n_steps, dt_out);
   RG_TRY(reset_status(h, h->d_status, h->stream));
   if (dt_out) RG_CUDA(h, h->host_dts.ensure(sizeof(double) * static_cast<size_t>(std::max(n_steps, 1))));
   double* hd = static_cast<double*>(h->host_dts.p);
@@ -1196,6 +1230,26 @@ rg_status rg_run(rg_handle* h, int32_t n_steps, double* dt_out) {
   rg_status st = collect(h, h->d_status, h->stream);
   if (dt_out) std::memcpy(dt_out, hd, sizeof(double) * static_cast<size_t>(n_steps));
   return st;
+}
+
+rg_status rg_set_step_mode(rg_handle* h, int32_t mode) {
+  if (!h) return RG_ERR_INVALID_ARGUMENT;
+  h->last = rg_error{};
+  if (mode != RG_STEP_PER_PHASE && mode != RG_STEP_PERSISTENT) return invalid(h, 0, mode);
+  if (mode == RG_STEP_PERSISTENT && !persistent_ok(h)) return invalid(h, 1, mode);
+  h->step_mode = mode;
+  return RG_OK;
+}
+
+rg_status rg_grid_barrier_check(rg_handle* h, int32_t missing_blocks) {
+  if (!h || missing_blocks < 0) return RG_ERR_INVALID_ARGUMENT;
+  h->last = rg_error{};
+  RG_CUDA(h, cudaSetDevice(h->cfg.device));
+  RG_CUDA(h, h->barrier.ensure(sizeof(rg::GridBarrier)));
+  RG_TRY(reset_status(h, h->d_status, h->stream));
+  RG_CUDA(h, rg::launch_barrier_check(static_cast<rg::GridBarrier*>(h->barrier.p), missing_blocks, h->d_status,
+                                      h->stream));
+  return collect(h, h->d_status, h->stream);
 }
 
 rg_status rg_set_problems(rg_handle* h, int32_t P, const int32_t* offsets, const double* gamma) {
@@ -1269,6 +1323,7 @@ rg_status rg_run_graph(rg_handle* h, int32_t n_steps) {
   if (rg_status st = mesh_error(h)) return st;
   h->last = rg_error{};
   if (n_steps == 0) return RG_OK;
+  if (h->step_mode == RG_STEP_PERSISTENT) return run_persistent(h, n_steps, nullptr);
   RG_TRY(reset_status(h, h->d_status, h->stream));
   if (fusable(h) && !h->dt_next_ready) {
     // one step with its own CFL pass; the captured step is the fused form,

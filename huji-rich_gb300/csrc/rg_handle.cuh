@@ -171,6 +171,10 @@ struct rg_handle {
   // batch of independent problems (n_problems == 0: one problem)
   int n_problems = 0;
   rgh::DevBuf cell_problem, problem_offsets, gamma_p, gamma32_p, inv_gm1_32_p, dtmin_p, time_p, dt_p;
+  // RG_STEP_PERSISTENT: rg_run / rg_run_graph of a batch in one cooperative
+  // launch (its grid barrier and problem 0's dt per step)
+  int step_mode = 0;
+  rgh::DevBuf barrier, dt_trace;
   // CUDA graph of one fused step
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;

@@ -313,6 +313,54 @@ __device__ __forceinline__ void problem_min(unsigned long long* mins, int proble
 }
 #endif
 
+// Grid barrier of a cooperative launch (every block resident): an arrival
+// counter and a generation word, zeroed before the launch.
+struct GridBarrier {
+  unsigned int count;
+  unsigned int gen;
+};
+// waits of one barrier: __nanosleep(500) each, about 1 s in all
+constexpr unsigned int kBarrierSpins = 1u << 21;
+
+#ifdef __CUDACC__
+// All blocks of the grid meet here (expected: the blocks that arrive, the
+// grid's size).  The last to arrive resets the counter and advances the
+// generation; the others wait for the generation to move, at most
+// kBarrierSpins sleeps, after which the block records RG_ERR_TIMEOUT (phase
+// 7, the block) and the barrier returns false: the caller returns, so the
+// launch ends with the error instead of waiting on.  gen is the block's copy
+// of the generation (thread 0's is the one used); ok is a __shared__ word.
+__device__ inline bool grid_sync(GridBarrier* gb, unsigned int& gen, unsigned int expected, int& ok, DevStatus* st,
+                                 int step) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int good = 1;
+    __threadfence();
+    const unsigned int arrived = atomicAdd(&gb->count, 1u) + 1u;
+    if (arrived == expected) {
+      atomicExch(&gb->count, 0u);
+      __threadfence();
+      atomicAdd(&gb->gen, 1u);
+    } else {
+      unsigned int spins = 0;
+      while (*reinterpret_cast<volatile unsigned int*>(&gb->gen) == gen) {
+        if (++spins > kBarrierSpins) {
+          good = 0;
+          record_error(st, step, RG_ERR_TIMEOUT, 7, blockIdx.x, static_cast<double>(arrived));
+          break;
+        }
+        __nanosleep(500);
+      }
+    }
+    __threadfence();
+    gen += 1u;
+    ok = good;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+#endif
+
 struct GeomArgs {
   MeshDev mesh;
   int order;

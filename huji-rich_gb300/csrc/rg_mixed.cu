@@ -310,6 +310,27 @@ __device__ __forceinline__ bool skipped32(const MixedArgs& a, int p) {
 
 // SimpleCFL (simple_cfl.cpp:28-47, 58-71) in FP32.  max_e (c+|v-w_e|)/R is
 // (c + sqrt(max_e |v-w_e|^2))/R: the bound is monotone in |v-w|.
+// cell t's bound 1 / max_e((c + |v - w_e|) / R)
+template <bool kBatch>
+__device__ __forceinline__ float cfl32_cell(const MixedArgs& a, int t) {
+  const MeshDev& m = a.mesh;
+  const float4 c = a.cells32[t];
+  const float cs = sqrtf(gamma32<kBatch>(a, t) * c.y / c.x);
+  float q = 0.0f;
+  const int b = m.cell_off[t], e1 = m.cell_off[t + 1];
+  if (a.ev_zero) {
+    if (e1 > b) q = fmaxf(q, fmaf(c.z, c.z, c.w * c.w));
+  } else {
+    for (int k = b; k < e1; ++k) {
+      const float2 w = a.ev32[m.cell_faces[k]];
+      const float dx = c.z - w.x, dy = c.w - w.y;
+      q = fmaxf(q, fmaf(dx, dx, dy * dy));
+    }
+  }
+  const float res = (cs + sqrtf(q)) / a.g32.width[t];
+  return 1.0f / res;
+}
+
 template <bool kBatch>
 __global__ void __launch_bounds__(kMaxBlock) k_cfl32(MixedArgs a, int fill_ghosts) {
   const MeshDev& m = a.mesh;
@@ -320,21 +341,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_cfl32(MixedArgs a, int fill_ghost
     const int t = base + threadIdx.x;
     float x = __int_as_float(0x7f800000);
     if (t < m.n) {
-      const float4 c = a.cells32[t];
-      const float cs = sqrtf(gamma32<kBatch>(a, t) * c.y / c.x);
-      float q = 0.0f;
-      const int b = m.cell_off[t], e1 = m.cell_off[t + 1];
-      if (a.ev_zero) {
-        if (e1 > b) q = fmaxf(q, fmaf(c.z, c.z, c.w * c.w));
-      } else {
-        for (int k = b; k < e1; ++k) {
-          const float2 w = a.ev32[m.cell_faces[k]];
-          const float dx = c.z - w.x, dy = c.w - w.y;
-          q = fmaxf(q, fmaf(dx, dx, dy * dy));
-        }
-      }
-      const float res = (cs + sqrtf(q)) / a.g32.width[t];
-      x = 1.0f / res;
+      x = cfl32_cell<kBatch>(a, t);
     } else if (t < total) {
       fill_ghost32(a, t - m.n);
     }
@@ -1051,6 +1058,59 @@ __global__ void __launch_bounds__(kMinBlocks ? kCappedBlock : kMaxBlock, kMinBlo
   if (!kBatch && a.cfl_next) grid_min_times(a.status, bits, a.cfl, &a.status->dt_next, &a.status->dt_next32);
 }
 
+// The batch run as one persistent launch (cooperative: every block is
+// resident).  Each step runs the per-phase kernels' items in their order --
+// CFL (each problem's minimum), slopes, faces (scaled by the problem's dt),
+// each problem's dt and time, the cell update -- with a grid barrier between
+// phases, so every cell and face gets the same operations on the same inputs
+// as with one launch per phase (bit-identical results).  dt_trace[k] keeps
+// problem 0's dt of step k.
+__global__ void __launch_bounds__(kPersistBlock, 4)
+    k_run32_persistent(MixedArgs a, int n_steps, int step0, GridBarrier* gb, int missing, double* dt_trace) {
+  __shared__ unsigned int s_gen;
+  __shared__ int s_ok;
+  if (threadIdx.x == 0) s_gen = *reinterpret_cast<volatile unsigned int*>(&gb->gen);
+  __syncthreads();
+  unsigned int gen = s_gen;
+  const unsigned int expected = gridDim.x + static_cast<unsigned int>(missing);
+  const MeshDev& m = a.mesh;
+  const int t0 = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+  for (int k = 0; k < n_steps; ++k) {
+    a.step = step0 + k < 0x1fff ? step0 + k : 0x1fff;
+    // CFL: each problem's minimum bound (k_cfl32's batch branch)
+    for (int base = blockIdx.x * blockDim.x; base < m.n; base += stride) {
+      const int t = base + threadIdx.x;
+      const float x = t < m.n ? cfl32_cell<true>(a, t) : __int_as_float(0x7f800000);
+      problem_min(a.dtmin_p, t < m.n ? a.cell_problem[t] : -1,
+                  static_cast<unsigned long long>(__double_as_longlong(widen_exact(x))));
+    }
+    if (!grid_sync(gb, gen, expected, s_ok, a.status, a.step)) return;
+    for (int i = t0; i < m.n; i += stride) k_slopes32_item<true, 1>(a, i);
+    if (!grid_sync(gb, gen, expected, s_ok, a.status, a.step)) return;
+    for (int e = t0; e < m.e; e += stride) k_faces32_lgi_item<true, true>(a, e);
+    if (!grid_sync(gb, gen, expected, s_ok, a.status, a.step)) return;
+    // each problem's dt and time (k_update_mixed's batch branch), the update
+    for (int p = t0; p < a.n_problems; p += stride) {
+      const double dt = a.cfl * __longlong_as_double(static_cast<long long>(a.dtmin_p[p]));
+      a.dt_p[p] = dt;
+      a.time_p[p] += dt;
+      a.dtmin_p[p] = kInfBits;
+      if (p == 0 && dt_trace) dt_trace[k] = dt;
+    }
+    for (int i = t0; i < m.n; i += stride) k_update_mixed_item<true>(a, i, 0, 1, 1);
+    if (!grid_sync(gb, gen, expected, s_ok, a.status, a.step)) return;
+  }
+}
+
+__global__ void __launch_bounds__(kPersistBlock) k_barrier_check(GridBarrier* gb, int missing, DevStatus* st) {
+  __shared__ unsigned int s_gen;
+  __shared__ int s_ok;
+  if (threadIdx.x == 0) s_gen = *reinterpret_cast<volatile unsigned int*>(&gb->gen);
+  __syncthreads();
+  unsigned int gen = s_gen;
+  grid_sync(gb, gen, gridDim.x + static_cast<unsigned int>(missing), s_ok, st, 0);
+}
+
 inline int blocks(int n) { return (n + kBlock - 1) / kBlock; }
 
 }  // namespace
@@ -1067,6 +1127,40 @@ cudaError_t launch_geom32_direct(const GeomArgs& ga, const MixedGeomArgs& a, cud
   const int work = a.n > a.g ? a.n : a.g;
   if (work > 0) k_geom_cells32<<<blocks(work), kBlock, 0, s>>>(ga, a);
   return cudaGetLastError();
+}
+
+cudaError_t launch_run32_persistent(const MixedArgs& a, int n_steps, int step0, GridBarrier* gb, int missing,
+                                   double* dt_trace, cudaStream_t s, int* grid_out) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_run32_persistent, kPersistBlock, 0);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorCooperativeLaunchTooLarge;
+  // every block resident; no more blocks than the largest phase has items for
+  const int work = a.mesh.e > a.mesh.n ? a.mesh.e : a.mesh.n;
+  int grid = per_sm * sms;
+  const int need = (work + kPersistBlock - 1) / kPersistBlock;
+  if (need < grid) grid = need > 0 ? need : 1;
+  if (grid_out) *grid_out = grid;
+  e = cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s);
+  if (e != cudaSuccess) return e;
+  MixedArgs ac = a;
+  void* args[] = {&ac, &n_steps, &step0, &gb, &missing, &dt_trace};
+  return cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(k_run32_persistent), dim3(grid),
+                                     dim3(kPersistBlock), args, 0, s);
+}
+
+cudaError_t launch_barrier_check(GridBarrier* gb, int missing, DevStatus* st, cudaStream_t s) {
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s);
+  if (e != cudaSuccess) return e;
+  void* args[] = {&gb, &missing, &st};
+  return cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(k_barrier_check), dim3(2 * sms),
+                                     dim3(kPersistBlock), args, 0, s);
 }
 
 cudaError_t launch_cells_to32(const double* c64, float4* c32, int n, cudaStream_t s) {

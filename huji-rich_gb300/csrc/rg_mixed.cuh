@@ -122,5 +122,14 @@ cudaError_t launch_ghost_fill32(const MixedArgs& a, cudaStream_t s);
 cudaError_t launch_slopes32(const MixedArgs& a, cudaStream_t s);
 cudaError_t launch_faces32(const MixedArgs& a, cudaStream_t s, bool scaled);
 cudaError_t launch_update_mixed(const MixedArgs& a, cudaStream_t s, bool from_unscaled, bool extensive, bool cells);
+// n_steps batch steps (hdsim::TimeAdvance, second order) in one cooperative
+// launch with grid barriers between the phases; missing > 0 makes the first
+// barrier expect that many blocks more than run (its wait then runs out:
+// RG_ERR_TIMEOUT).  dt_trace (n_steps, or null) receives problem 0's dts.
+constexpr int kPersistBlock = 256;
+cudaError_t launch_run32_persistent(const MixedArgs& a, int n_steps, int step0, GridBarrier* gb, int missing,
+                                   double* dt_trace, cudaStream_t s, int* grid_out);
+// grid_sync once, in a cooperative launch of two blocks per SM
+cudaError_t launch_barrier_check(GridBarrier* gb, int missing, DevStatus* st, cudaStream_t s);
 
 }  // namespace rg

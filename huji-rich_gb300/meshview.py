@@ -45,7 +45,7 @@ STATUS_NAMES = {0: "RG_OK", 1: "RG_ERR_INVALID_ARGUMENT", 2: "RG_ERR_CUDA", 3: "
                 4: "RG_ERR_OUT_OF_MEMORY", 10: "RG_ERR_NEGATIVE_DENSITY",
                 11: "RG_ERR_NEGATIVE_ENERGY", 12: "RG_ERR_HLLC_NAN",
                 13: "RG_ERR_HLLC_WAVE_SPEEDS", 14: "RG_ERR_SINGULAR_MATRIX",
-                15: "RG_ERR_TOO_MANY_NEIGHBORS"}
+                15: "RG_ERR_TOO_MANY_NEIGHBORS", 16: "RG_ERR_TIMEOUT"}
 
 # Messages of the reference's UniversalError for each physical failure.
 REFERENCE_MESSAGES = {10: "Negative density", 11: "Negative thermal energy",

@@ -34,9 +34,11 @@ EXPORTS = ("rg_default_config", "rg_create", "rg_destroy", "rg_status_string", "
            "rg_get_tracer_fluxes", "rg_get_tracer_slopes", "rg_set_outer_box", "rg_set_point_motion",
            "rg_point_velocities", "rg_apply_fix", "rg_get_edge_velocities", "rg_get_geometry",
            "rg_advance_begin", "rg_set_physical_geometry", "rg_set_tracer_fluxes", "rg_set_flux_rules",
-           "rg_set_lagrangian_updater", "rg_get_lagrangian_faces", "rg_set_lagrangian_faces")
+           "rg_set_lagrangian_updater", "rg_get_lagrangian_faces", "rg_set_lagrangian_faces",
+           "rg_set_step_mode", "rg_grid_barrier_check")
 
 MESH_DEVICE_GEOMETRY = 2  # RG_MESH_DEVICE_GEOMETRY
+STEP_PER_PHASE, STEP_PERSISTENT = 0, 1  # rg_step_mode
 
 KERNELS = ("cfl", "slopes", "faces", "update")
 
@@ -123,6 +125,8 @@ def load(path=LIB_PATH):
     lib.rg_set_problems.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), dp]
     lib.rg_get_problem_times.argtypes = [vp, dp, dp]
     lib.rg_run_graph.argtypes = [vp, C.c_int32]
+    lib.rg_set_step_mode.argtypes = [vp, C.c_int32]
+    lib.rg_grid_barrier_check.argtypes = [vp, C.c_int32]
     lib.rg_step_fwd.argtypes = [vp, C.c_int32, C.c_double, C.c_int32]
     lib.rg_step_bwd.argtypes = [vp, dp, dp]
     lib.rg_step_tlm.argtypes = [vp, C.c_int32, C.c_double, dp, dp]
@@ -455,6 +459,16 @@ class Handle:
 
     def run_graph(self, n_steps):
         self._check(self.lib.rg_run_graph(self.h, n_steps))
+
+    def set_step_mode(self, mode):
+        """STEP_PER_PHASE (0) or STEP_PERSISTENT (1): a batch run in one
+        cooperative launch."""
+        self._check(self.lib.rg_set_step_mode(self.h, mode))
+
+    def grid_barrier_check(self, missing_blocks=0):
+        """The persistent form's grid barrier alone, expecting missing_blocks
+        more blocks than run (RG_ERR_TIMEOUT after its bounded wait)."""
+        self._check(self.lib.rg_grid_barrier_check(self.h, missing_blocks))
 
     def step_async(self):
         self._check(self.lib.rg_step_async(self.h))

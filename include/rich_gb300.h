@@ -56,7 +56,10 @@ typedef enum rg_status {
   RG_ERR_HLLC_NAN = 12,          /* hllc.cpp:102-103 "Hllc::Solved entered with nan" */
   RG_ERR_HLLC_WAVE_SPEEDS = 13,  /* hllc.cpp:142-148 "Invalid wave speeds in hllc solver" */
   RG_ERR_SINGULAR_MATRIX = 14,   /* LinearGaussImproved.cpp:111-119 "Singular matrix" */
-  RG_ERR_TOO_MANY_NEIGHBORS = 15 /* LinearGaussImproved.cpp:73-79 "Cell has too many neighbors" */
+  RG_ERR_TOO_MANY_NEIGHBORS = 15, /* LinearGaussImproved.cpp:73-79 "Cell has too many neighbors" */
+  RG_ERR_TIMEOUT = 16             /* a device-side wait gave up (the persistent batch run's grid
+                                     barrier, rg_set_step_mode); the launch ended, the context
+                                     stays usable */
 } rg_status;
 
 /* First failure of the last call.  index is a cell index for density,
@@ -292,6 +295,24 @@ rg_status rg_get_problem_times(rg_handle* h, double* time_out, double* dt_last_o
  * synchronisation at the end.  Same results as rg_run; a failure is reported
  * with step 0 in its key. */
 rg_status rg_run_graph(rg_handle* h, int32_t n_steps);
+
+/* How rg_run / rg_run_graph run a batch (no reference counterpart).
+ * RG_STEP_PER_PHASE (default): one launch per phase of each step.
+ * RG_STEP_PERSISTENT: the whole run in one cooperative launch, every block
+ * resident, the phases of each step (CFL, slopes, faces, each problem's dt
+ * and time, update) separated by a grid barrier; results bit-identical to
+ * RG_STEP_PER_PHASE, and rg_run's dt_out is problem 0's dt per step.  Taken
+ * by a batch (rg_set_problems) on the FP32-mixed path, second order,
+ * hdsim::TimeAdvance, without tracers, stickers or flux rules; anything else
+ * returns RG_ERR_INVALID_ARGUMENT, here or at the run.  A barrier wait that
+ * runs out (about 1 s) ends the launch with RG_ERR_TIMEOUT. */
+typedef enum { RG_STEP_PER_PHASE = 0, RG_STEP_PERSISTENT = 1 } rg_step_mode;
+rg_status rg_set_step_mode(rg_handle* h, int32_t mode);
+/* Runs the persistent form's grid barrier once on its own, in a cooperative
+ * launch, expecting missing_blocks more blocks than it launches: RG_OK for 0,
+ * RG_ERR_TIMEOUT (after the barrier's bounded wait) otherwise.  For testing
+ * the timeout path; the handle stays usable. */
+rg_status rg_grid_barrier_check(rg_handle* h, int32_t missing_blocks);
 
 /* The CUDA stream (cudaStream_t) all kernels of the handle run on, for
  * callers that order their own work with the handle's (no reference

@@ -1,5 +1,6 @@
 """Batched form: independent problems of uneven size in one handle, each with
-its own gamma and SimpleCFL dt, advanced by one launch per phase.  Every
+its own gamma and SimpleCFL dt, advanced by one launch per phase or (FP32-mixed,
+RG_STEP_PERSISTENT) by one cooperative launch for the whole run.  Every
 problem of a batch must evolve exactly as it does alone (FP64: bit-for-bit,
 and the same for the FP32-mixed path, whose kernels are per cell and per
 face too), and a CUDA-graph replay must equal rg_run."""
@@ -188,3 +189,72 @@ def test_batch_with_tracers_equals_problems_alone(heun):
             exact(be[a:b], h.get_extensives())
             exact(bt[a:b], h.get_tracers())
             exact(bte[a:b], h.get_extensive_tracers())
+
+
+def batch_handle(mesh, off, gam, cells, ext, precision=1, heun=0):
+    h = richgpu.Handle(gamma=1.4, order=2, ghost_kind=0, precision=precision, device=0, time_integrator=heun)
+    h.upload_mesh(mesh)
+    h.set_problems(off, gam)
+    h.set_cells(cells)
+    h.set_extensives(ext)
+    h.set_edge_velocities(np.zeros((mesh.n_faces, 2)))
+    return h
+
+
+@pytest.mark.parametrize("seed,n", [(5, 12), (7, 40)])
+def test_persistent_run_equals_per_phase_run(seed, n):
+    """RG_STEP_PERSISTENT (the batch run in one cooperative launch, grid
+    barriers between the phases) gives the per-phase launches' cells,
+    extensives, problem times and dts bit for bit."""
+    mesh, off, gam, cells, _ = synthetic.riemann_batch(n, seed=seed, min_cells=64, max_cells=2500)
+    ext = init_ext(mesh, cells, off, gam)
+    out = []
+    for mode in (richgpu.STEP_PER_PHASE, richgpu.STEP_PERSISTENT):
+        with batch_handle(mesh, off, gam, cells, ext) as h:
+            h.set_step_mode(mode)
+            dts = list(h.run(9))
+            h.run_graph(4)
+            dts += list(h.run(3))
+            out.append((h.get_cells(), h.get_extensives(), np.array(dts)) + h.problem_times())
+    for a, b in zip(out[0], out[1]):
+        exact(a, b)
+
+
+def test_persistent_mode_where_it_applies():
+    mesh, off, gam, cells, _ = small_batch()
+    ext = init_ext(mesh, cells, off, gam)
+    with batch_handle(mesh, off, gam, cells, ext, precision=0) as h:
+        with pytest.raises(richgpu.RichError):
+            h.set_step_mode(richgpu.STEP_PERSISTENT)        # FP64 batches run one launch per phase
+    with batch_handle(mesh, off, gam, cells, ext, heun=1) as h:
+        with pytest.raises(richgpu.RichError):
+            h.set_step_mode(richgpu.STEP_PERSISTENT)        # TimeAdvance only
+    with batch_handle(mesh, off, gam, cells, ext) as h:
+        with pytest.raises(richgpu.RichError):
+            h.set_step_mode(2)
+        h.set_step_mode(richgpu.STEP_PERSISTENT)
+        h.set_tracer_config(0, n_stickers=1)
+        with pytest.raises(richgpu.RichError) as ei:
+            h.run(1)                                        # no stickers or tracers in the persistent form
+        assert ei.value.status == 1
+        h.set_tracer_config(0)
+        h.run(2)
+        h.set_step_mode(richgpu.STEP_PER_PHASE)
+        h.run(1)
+
+
+def test_grid_barrier_wait_runs_out_and_the_handle_stays_usable():
+    """The persistent form's barrier with a block that never arrives: the
+    bounded wait ends the launch with RG_ERR_TIMEOUT (about a second), and
+    the next launches run normally."""
+    mesh, off, gam, cells, _ = small_batch()
+    ext = init_ext(mesh, cells, off, gam)
+    with batch_handle(mesh, off, gam, cells, ext) as h:
+        h.grid_barrier_check(0)
+        with pytest.raises(richgpu.RichError) as ei:
+            h.grid_barrier_check(1)
+        assert ei.value.status == 16 and ei.value.phase == 7
+        h.grid_barrier_check(0)
+        h.set_step_mode(richgpu.STEP_PERSISTENT)
+        h.run(3)
+        assert np.all(np.isfinite(h.get_cells()))
