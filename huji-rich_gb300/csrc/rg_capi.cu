@@ -865,6 +865,11 @@ rg_status rg_upload_mesh(rg_handle* h, const rg_mesh_view* v, uint32_t flags) {
   if (!ext_keep) h->have_ext = false;
   RG_CUDA(h, h->ext.ensure(32 * static_cast<size_t>(n)));
   if (h->ev.bytes < 16 * static_cast<size_t>(e)) h->have_ev = false;
+  if (h->ev64_pending) {
+    // the FP32-mixed device motion's face velocities belong to the old mesh
+    h->ev64_pending = false;
+    h->have_ev = false;
+  }
   RG_CUDA(h, h->ev.ensure(16 * static_cast<size_t>(std::max(e, 1))));
   RG_CUDA(h, h->slopes.ensure(64 * static_cast<size_t>(n)));
   RG_CUDA(h, h->fluxes.ensure(32 * static_cast<size_t>(std::max(e, 1))));
@@ -984,6 +989,7 @@ rg_status rg_get_extensives(rg_handle* h, double* ext) {
 
 rg_status rg_set_edge_velocities(rg_handle* h, const double* ev) {
   if (!h || !ev) return RG_ERR_INVALID_ARGUMENT;
+  h->ev64_pending = false;
   h->dt_next_ready = false;
   if (h->active < 0) return require(h, false, false, false, false);
   RG_CUDA(h, cudaMemcpyAsync(h->ev.p, ev, 16 * static_cast<size_t>(active_slot(h)->e),

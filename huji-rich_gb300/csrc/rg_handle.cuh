@@ -200,6 +200,9 @@ struct rg_handle {
   bool external_state = false;
   // every face velocity last set is +-0 (checked on the device when set)
   bool ev_zero = false;
+  // FP32-mixed device motion wrote only the FP32 face velocities: the FP64
+  // ones are formed from the point velocities when read back
+  bool ev64_pending = false;
   rgh::DevBuf flag_buf;
   // differentiation: checkpoints, recomputation buffers, reverse adjacency
   rg_adjoint_state* adj = nullptr;

@@ -243,6 +243,36 @@ __global__ void __launch_bounds__(kMoBlock) k_edge_velocities(StepArgs a, Motion
   mo.ev[e] = w;
 }
 
+// The same face velocities for an FP32-mixed handle, straight into its FP32
+// copy: the coordinate differences in FP64, each rounded once (x_R - x_L, and
+// the face centroid's offset from the points' midpoint as
+// ((v0 - x_L) + (v1 - x_R)) / 2), the rest in FP32 (|x_R - x_L| from the
+// FP64 geometry).  The FP64 face velocities are formed when they are read
+// back (rg_get_edge_velocities).
+__global__ void __launch_bounds__(kMoBlock) k_edge_velocities32(StepArgs a, MotionArgs mo, float2* ev32) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const MeshDev& m = a.mesh;
+  if (e >= m.e) return;
+  const int2 fc = m.face_cells[e];
+  const int oa = fc.x < m.n ? fc.x : m.ghost_source[fc.x - m.n];
+  const int ob = fc.y < m.n ? fc.y : m.ghost_source[fc.y - m.n];
+  float2 w = make_float2(0.0f, 0.0f);
+  if (mo.edges == RG_EDGES_PERIODIC || oa != ob) {
+    const double2 wl = mo.pv[oa], wr = mo.pv[ob];
+    const double2 rl = m.points[fc.x], rr = m.points[fc.y];
+    const dbl4 v = m.face_vertices[e];
+    const float dx = narrow(rr.x - rl.x), dy = narrow(rr.y - rl.y);
+    const float ox = 0.5f * (narrow(v.x - rl.x) + narrow(v.z - rr.x));
+    const float oy = 0.5f * (narrow(v.y - rl.y) + narrow(v.w - rr.y));
+    const float lx = narrow(wl.x), ly = narrow(wl.y), rx = narrow(wr.x), ry = narrow(wr.y);
+    const float sp = (lx - rx) * ox + (ly - ry) * oy;
+    const float ab = narrow(a.geom.dab[e]);
+    const float q = sp / (ab * ab);
+    w = make_float2(0.5f * (lx + rx) + dx * q, 0.5f * (ly + ry) + dy * q);
+  }
+  ev32[e] = w;
+}
+
 inline int mo_blocks(int n) { return (n + kMoBlock - 1) / kMoBlock; }
 
 }  // namespace
@@ -276,6 +306,11 @@ cudaError_t launch_apply_fix(const StepArgs& a, const MotionArgs& mo, cudaStream
 
 cudaError_t launch_edge_velocities(const StepArgs& a, const MotionArgs& mo, cudaStream_t s) {
   if (a.mesh.e > 0) k_edge_velocities<<<mo_blocks(a.mesh.e), kMoBlock, 0, s>>>(a, mo);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_edge_velocities32(const StepArgs& a, const MotionArgs& mo, float2* ev32, cudaStream_t s) {
+  if (a.mesh.e > 0) k_edge_velocities32<<<mo_blocks(a.mesh.e), kMoBlock, 0, s>>>(a, mo, ev32);
   return cudaGetLastError();
 }
 

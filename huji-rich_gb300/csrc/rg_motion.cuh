@@ -26,5 +26,7 @@ cudaError_t launch_cyl_geometry(const MeshDev& m, double* xarea, double* cd_volu
 cudaError_t launch_point_velocities(const StepArgs& a, const MotionArgs& mo, cudaStream_t s);
 cudaError_t launch_apply_fix(const StepArgs& a, const MotionArgs& mo, cudaStream_t s);
 cudaError_t launch_edge_velocities(const StepArgs& a, const MotionArgs& mo, cudaStream_t s);
+// FP32-mixed handles: the face velocities into their FP32 copy only
+cudaError_t launch_edge_velocities32(const StepArgs& a, const MotionArgs& mo, float2* ev32, cudaStream_t s);
 
 }  // namespace rg

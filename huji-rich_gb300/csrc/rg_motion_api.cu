@@ -2,8 +2,9 @@
 // (include/rich_gb300.h, "Point motion on the device"): hdsim::TimeAdvance's
 // first half (hdsim2d.cpp:149-195) enqueued on the handle's stream, the
 // kernels in rg_motion.cu.  Point motion reads FP64 cell records; on the
-// FP32-mixed path they are widened from the FP32 primitives first and the
-// face velocities narrowed for the FP32 kernels afterwards.
+// FP32-mixed path they are widened from the FP32 primitives first, and the
+// face velocities are written straight into their FP32 copy (the FP64 ones
+// are formed when read back).
 #include <cuda_runtime.h>
 
 #include "rg_handle.cuh"
@@ -37,20 +38,24 @@ rg_status widen_cells(rg_handle* h) {
 }
 
 // face velocities from the point velocities, as the handle's edge velocities
+// (an FP32-mixed handle: the FP32 copy; the FP64 one on read-back)
 rg_status edges_from_points(rg_handle* h, const rg::StepArgs& a, const rg::MotionArgs& mo) {
   MeshSlot* s = active_slot(h);
+  h->ev64_pending = false;
   if (h->motion.kind == RG_MOTION_EULERIAN) {
     // every face velocity is +0 (CalcFaceVelocity of zero velocities): the
     // kernels read none
     RG_CUDA(h, cudaMemsetAsync(h->ev.p, 0, 16 * static_cast<size_t>(s->e), h->stream));
+    if (h->mixed) RG_CUDA(h, cudaMemsetAsync(h->ev32.p, 0, 8 * static_cast<size_t>(s->e), h->stream));
     h->ev_zero = true;
+  } else if (h->mixed) {
+    RG_CUDA(h, rg::launch_edge_velocities32(a, mo, static_cast<float2*>(h->ev32.p), h->stream));
+    h->ev64_pending = true;
+    h->ev_zero = false;
   } else {
     RG_CUDA(h, rg::launch_edge_velocities(a, mo, h->stream));
     h->ev_zero = false;
   }
-  if (h->mixed)
-    RG_CUDA(h, rg::launch_vec2_to32(static_cast<const double*>(h->ev.p), static_cast<float2*>(h->ev32.p), s->e,
-                                    h->stream));
   h->have_ev = true;
   h->dt_next_ready = false;
   return RG_OK;
@@ -124,6 +129,11 @@ rg_status rg_apply_fix(rg_handle* h, double dt, double* pv_out) {
 rg_status rg_get_edge_velocities(rg_handle* h, double* ev) {
   if (rg_status st = require(h, false, false, true, false)) return st;
   if (!ev) return RG_ERR_INVALID_ARGUMENT;
+  if (h->ev64_pending) {
+    // the FP64 face velocities of the last device motion (FP32-mixed)
+    RG_CUDA(h, rg::launch_edge_velocities(step_args(h), motion_args(h), h->stream));
+    h->ev64_pending = false;
+  }
   RG_CUDA(h, cudaMemcpyAsync(ev, h->ev.p, 16 * static_cast<size_t>(active_slot(h)->e), cudaMemcpyDeviceToHost,
                              h->stream));
   RG_CUDA(h, cudaStreamSynchronize(h->stream));

@@ -142,6 +142,17 @@ def test_direct_fp32_geometry_against_rounded_fp64_geometry():
     (s0, c0, e0), (s1, c1, e1) = out
     exact(s0[0][1], s1[0][1])
     exact(s0[0][2], s1[0][2])
+    # the first dt reads the FP32 face velocities (formed from FP64
+    # coordinate differences) and FP32 cells: an FP64 handle's dt to FP32
+    # rounding
+    with richgpu.Handle(gamma=5 / 3, order=2, ghost_kind=0, device=0) as h:
+        h.set_outer_box(-1.0, 1.0, -1.0, 1.0)
+        h.upload_mesh(mesh, flags=richgpu.MESH_DEVICE_GEOMETRY)
+        h.set_point_motion(kind=2, edges=0, chi=0.15, eta=0.02)
+        h.set_cells(cells)
+        h.set_extensives(ext)
+        dt64, _ = h.advance_begin()
+    assert abs(s0[0][0] - dt64) <= 1e-6 * dt64
     for k in range(4):
         assert abs(s0[k][0] - s1[k][0]) <= 1e-6 * s1[k][0]
     l1 = np.abs(c0[:, 0] - c1[:, 0]).sum() / np.abs(c1[:, 0]).sum()
