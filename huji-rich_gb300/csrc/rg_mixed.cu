@@ -161,6 +161,13 @@ __global__ void __launch_bounds__(kBlock) k_geom_faces32(GeomArgs ga, MixedGeomA
   a.frec[2 * e + 1] = dm;
 }
 
+// Two passes over a warp's 32 consecutive cells.  The entry pass writes
+// their CSR entries one entry per lane (coalesced stores: the neighbour
+// word, the {stencil vector, centroid offset} record and the signed face
+// index), the entry's cell found by a binary search over the lanes' offsets.
+// The cell pass sums each cell's entries in order (the boundary slope's
+// sums, or the naive slope's matrix and its inverse), re-reading the face
+// records from cache.
 __global__ void __launch_bounds__(kBlock) k_geom_cells32(GeomArgs ga, MixedGeomArgs a) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const MeshDev& m = ga.mesh;
@@ -169,8 +176,46 @@ __global__ void __launch_bounds__(kBlock) k_geom_cells32(GeomArgs ga, MixedGeomA
     const double2 u = a.g64.ghost_unit[t];
     a.ghost_unit[t] = make_float2(narrow(u.x), narrow(u.y));
   }
+  const int lane = threadIdx.x & 31;
+  const int c0 = t - lane;  // the warp's first cell
+  if (c0 < m.n) {
+    const unsigned full = 0xffffffffu;
+    const int my_off = m.cell_off[c0 + lane < m.n ? c0 + lane : m.n];
+    const int last = m.cell_off[c0 + 32 < m.n ? c0 + 32 : m.n];
+    const int base = __shfl_sync(full, my_off, 0);
+    for (int k0 = base; k0 < last; k0 += 32) {
+      const int k = k0 + lane;
+      // the entry's cell: the last lane j with cell_off[c0 + j] <= k
+      int j = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const int o = __shfl_sync(full, my_off, j + step);
+        if (o <= k) j += step;
+      }
+      if (k < last) {
+        const int i = c0 + j;
+        const int e = __ldg(m.cell_faces + k);
+        const float4 r0 = __ldg(a.frec + 2 * e), r1 = __ldg(a.frec + 2 * e + 1);
+        const int f0 = __float_as_int(r0.z), f1 = __float_as_int(r0.w);
+        const bool first = f0 == i;
+        const int other = first ? f1 : f0;
+        const float dmx = first ? r1.x : r1.z, dmy = first ? r1.y : r1.w;
+        if (ga.cflags[i] & kCellBoundarySlope) {
+          const bool mirror = orig_of(m, f0) == orig_of(m, f1);
+          ga.nbr[k] = static_cast<uint32_t>(other) | (mirror ? kNbrMirror : 0u) | (first ? kNbrFirst : 0u);
+          const double2 cci = m.cms[i], co = m.cms[other];
+          a.ent[k] = make_float4(narrow(co.x - cci.x), narrow(co.y - cci.y), dmx, dmy);
+        } else {
+          ga.nbr[k] = static_cast<uint32_t>(other) | (first ? kNbrFirst : 0u);
+          const float rx = first ? r0.x : -r0.x, ry = first ? r0.y : -r0.y;
+          a.ent[k] = make_float4(rx * 0.5f, ry * 0.5f, dmx, dmy);
+        }
+        a.fsign[k] = e | (first ? static_cast<int>(0x80000000u) : 0);
+      }
+    }
+  }
   if (t >= m.n) return;
-  const int i = ga.cell_order ? ga.cell_order[t] : t;
+  const int i = t;
   const double width = root(quot(m.volume[i], kPi));
   ga.width[i] = width;
   a.width[i] = narrow(width);
@@ -182,16 +227,10 @@ __global__ void __launch_bounds__(kBlock) k_geom_cells32(GeomArgs ga, MixedGeomA
     float sxsy = 0, sy2 = 0, sx2 = 0;
     for (int k = 0; k < nn; ++k) {
       const int e = __ldg(m.cell_faces + b + k);
-      const float4 r0 = __ldg(a.frec + 2 * e), r1 = __ldg(a.frec + 2 * e + 1);
+      const float4 r0 = __ldg(a.frec + 2 * e);
       const int f0 = __float_as_int(r0.z), f1 = __float_as_int(r0.w);
-      const bool first = f0 == i;
-      const int other = first ? f1 : f0;
-      const bool mirror = orig_of(m, f0) == orig_of(m, f1);
-      ga.nbr[b + k] = static_cast<uint32_t>(other) | (mirror ? kNbrMirror : 0u) | (first ? kNbrFirst : 0u);
-      const double2 co = m.cms[other];
+      const double2 co = m.cms[f0 == i ? f1 : f0];
       const float dx = narrow(co.x - cci.x), dy = narrow(co.y - cci.y);
-      a.ent[b + k] = make_float4(dx, dy, first ? r1.x : r1.z, first ? r1.y : r1.w);
-      a.fsign[b + k] = e | (first ? static_cast<int>(0x80000000u) : 0);
       sxsy += dy * dx;
       sx2 += dx * dx;
       sy2 += dy * dy;
@@ -199,16 +238,16 @@ __global__ void __launch_bounds__(kBlock) k_geom_cells32(GeomArgs ga, MixedGeomA
     a.minv[i] = make_float4(sxsy, sx2, sy2, sxsy * sxsy - sx2 * sy2);
     return;
   }
-  const bool too_many = nn > kMaxNaiveNeighbours;
-  if (too_many) record_error(ga.status, 0, RG_ERR_TOO_MANY_NEIGHBORS, 2, i, nn);
+  if (nn > kMaxNaiveNeighbours) {
+    record_error(ga.status, 0, RG_ERR_TOO_MANY_NEIGHBORS, 2, i, nn);
+    a.minv[i] = make_float4(0, 0, 0, 0);
+    return;
+  }
   float m0 = 0, m1 = 0, m2 = 0, m3 = 0;
-#pragma unroll 2
   for (int k = 0; k < nn; ++k) {
     const int e = __ldg(m.cell_faces + b + k);
     const float4 r0 = __ldg(a.frec + 2 * e), r1 = __ldg(a.frec + 2 * e + 1);
-    const int f0 = __float_as_int(r0.z), f1 = __float_as_int(r0.w);
-    const bool first = f0 == i;
-    ga.nbr[b + k] = static_cast<uint32_t>(first ? f1 : f0) | (first ? kNbrFirst : 0u);
+    const bool first = __float_as_int(r0.z) == i;
     // -r_ij for the second neighbour; c_ij = centroid - (cm_a + cm_b) / 2
     const float rx = first ? r0.x : -r0.x, ry = first ? r0.y : -r0.y;
     const float cx = 0.5f * (r1.x + r1.z), cy = 0.5f * (r1.y + r1.w);
@@ -216,12 +255,6 @@ __global__ void __launch_bounds__(kBlock) k_geom_cells32(GeomArgs ga, MixedGeomA
     m1 -= cy * rx;
     m2 -= cx * ry;
     m3 -= cy * ry;
-    a.ent[b + k] = make_float4(rx * 0.5f, ry * 0.5f, first ? r1.x : r1.z, first ? r1.y : r1.w);
-    a.fsign[b + k] = e | (first ? static_cast<int>(0x80000000u) : 0);
-  }
-  if (too_many) {
-    a.minv[i] = make_float4(0, 0, 0, 0);
-    return;
   }
   const float vol = narrow(m.volume[i]);
   m0 += vol;
