@@ -381,10 +381,17 @@ rg_status rg_point_velocities(rg_handle* h, double* point_velocities_out);
 /* PointMotion::ApplyFix with dt on the current point velocities, then the face
  * velocities again */
 rg_status rg_apply_fix(rg_handle* h, double dt, double* point_velocities_out);
+/* The handle's face velocities (n_faces*2).  On an FP32-mixed handle the
+ * device motion forms only their FP32 copy, which the FP32 passes read; this
+ * call forms the FP64 ones from the same point velocities first.  After a
+ * new mesh is uploaded, face velocities of the old mesh's motion are gone
+ * (RG_ERR_NOT_READY until the next motion or rg_set_edge_velocities). */
 rg_status rg_get_edge_velocities(rg_handle* h, double* edge_velocities_out);
 /* the mesh geometry in use (computed on the device or uploaded); cd_area:
  * CacheData's face areas (n_faces) of the PhysicalGeometry.  Any pointer may
- * be NULL. */
+ * be NULL.  On an FP32-mixed handle without tracers the upload forms only
+ * the FP32 face geometry; asking for cd_area forms the FP64 geometry (once
+ * per mesh) and rounds the FP32 copies from it. */
 rg_status rg_get_geometry(rg_handle* h, double* volume, double* cm_xy, double* cd_volume, double* cd_area);
 
 /* PhysicalGeometry (physical_geometry.hpp): SlabSymmetry (the default) or
