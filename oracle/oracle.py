@@ -426,6 +426,48 @@ def run_tr(mesh, cells, ext, tr, tr_ext, ev, gamma, steps, ts, cfl_number=0.3, o
     return cells, ext, tr, tr_ext, np.array(dts)
 
 
+def cas_flux_tr(mesh, cells, tr, ev, gamma, order, lp, rules, ts, lagrangian=False):
+    """(fluxes, tracer fluxes[, ws_, edge_vel_]) of the condition/action flux
+    calculators with tracers; the stickers come from ts."""
+    E = mesh.n_faces
+    fl, tfl = np.zeros((E, 4)), np.zeros((E, max(ts.n, 1)))
+    ws, lev = np.zeros(E), np.zeros(E)
+    arr, nr = _rules(rules)
+    err, tc = RoError(), ts.c()
+    _check(_setup_tr().ro_cas_flux_tr(C.byref(mesh.view()), _d(_f64(cells)), _d(_f64(tr)), _d(_f64(ev)),
+                                      C.c_double(gamma), C.c_int(order), C.byref(lp), C.byref(tc), arr, C.c_int(nr),
+                                      tc.stickers, _d(fl), _d(tfl), _d(ws), _d(lev), C.byref(err)), err)
+    return (fl, tfl[:, :ts.n], ws, lev) if lagrangian else (fl, tfl[:, :ts.n])
+
+
+def lagrangian_update_tr(mesh, ws, lag_ev, dt, ext, tr_ext):
+    """LagrangianExtensiveUpdater's factor on the extensives and the extensive
+    tracers (already updated by SimpleExtensiveUpdater)."""
+    ext, tr_ext = _f64(ext).copy(), _f64(tr_ext).copy()
+    _setup_tr().ro_lagrangian_update_tr(C.byref(mesh.view()), _d(_f64(ws)), _d(_f64(lag_ev)), C.c_double(dt), None,
+                                        _d(ext), _d(tr_ext), C.c_int(tr_ext.shape[1]))
+    return ext, tr_ext
+
+
+def run_cas_tr(mesh, cells, ext, tr, tr_ext, ev, gamma, steps, order, lp, rules, ts, cfl_number=0.3,
+               lagrangian_update=False):
+    """hdsim::TimeAdvance steps with a condition/action flux calculator and
+    tracers on a fixed mesh; returns (cells, ext, tracers, extensive tracers, dts)."""
+    cells, ext = _f64(cells).copy(), _f64(ext).copy()
+    tr, tr_ext = _f64(tr).copy(), _f64(tr_ext).copy()
+    arr, nr = _rules(rules)
+    L = _setup_tr()
+    dts = []
+    for _ in range(steps):
+        dt, err, tc = C.c_double(), RoError(), ts.c()
+        _check(L.ro_step_cas_tr(C.byref(mesh.view()), _d(cells), _d(ext), _d(tr), _d(tr_ext), _d(_f64(ev)),
+                                C.c_double(gamma), C.c_double(cfl_number), C.c_int(order), C.byref(lp), arr,
+                                C.c_int(nr), C.byref(tc), C.c_int(1 if lagrangian_update else 0), C.byref(dt),
+                                C.byref(err)), err)
+        dts.append(dt.value)
+    return cells, ext, tr, tr_ext, np.array(dts)
+
+
 # ---------------------------------------------------------------- 3D first-order path
 
 def _setup3():

@@ -1268,14 +1268,35 @@ static v2 wall_normal(const rg_mesh_view* m, int e, int aux, v2 p) {
   return vnormalize(remove_parallel(w, p));
 }
 
-int ro_cas_flux(const rg_mesh_view* m, const double* cells, const double* ev, double g, int order,
-                const ro_lgi_params* lp, const ro_flux_rule* rules, int n_rules, const uint32_t* st,
-                double* fluxes, double* lag_ws, double* lag_ev, ro_error* err) {
+/* the tracer flux of one condition/action face: Mass times the tracers of
+ * the cell (tcell, n_cells*nt) or LinearGaussImproved face value (tip, the
+ * face's 2*nt) of the side the action takes, as the reference's
+ * conserved_to_extensive forms it: tracers * Mass */
+static void cas_tracer_flux(int nt, double mass, int first, int face_value, const double* tr, int ca, int cb,
+                            const double* tip, double* out) {
+  for (int j = 0; j < nt; ++j) {
+    const double q = face_value ? tip[first ? j : nt + j] : tr[(size_t)(first ? ca : cb) * nt + j];
+    out[j] = q * mass;
+  }
+}
+
+int ro_cas_flux_tr(const rg_mesh_view* m, const double* cells, const double* tr, const double* ev, double g,
+                   int order, const ro_lgi_params* lp, const ro_tracers* t, const ro_flux_rule* rules, int n_rules,
+                   const uint32_t* st, double* fluxes, double* tfluxes, double* lag_ws, double* lag_ev,
+                   ro_error* err) {
+  const int nt = (t && tr && tfluxes) ? t->n : 0;
+  const size_t E = (size_t)(m->n_faces > 0 ? m->n_faces : 1);
   double* ip = NULL;
+  double* tip = NULL;
   int rc = 0;
   if (order == 2) {
-    ip = (double*)malloc(sizeof(double) * 8 * (size_t)(m->n_faces > 0 ? m->n_faces : 1));
-    rc = ro_lgi(m, cells, g, lp, NULL, ip, err);
+    ip = (double*)malloc(sizeof(double) * 8 * E);
+    if (nt > 0) {
+      tip = (double*)malloc(sizeof(double) * 2 * (size_t)nt * E);
+      rc = ro_lgi_tr(m, cells, tr, g, lp, t, NULL, ip, NULL, tip, err);
+    } else {
+      rc = ro_lgi(m, cells, g, lp, NULL, ip, err);
+    }
   }
   for (int e = 0; e < m->n_faces && !rc; ++e) {
     const int a = fc0(m, e), b = fc1(m, e);
@@ -1323,6 +1344,10 @@ int ro_cas_flux(const rg_mesh_view* m, const double* cells, const double* ev, do
       put_flux(fluxes + 4 * e, c);
       if (lag_ws) lag_ws[e] = lag ? energy : 0;
       if (lag_ev) lag_ev[e] = speed;
+      /* convert_conserved_to_extensive (:29-40): the upwind face value */
+      if (nt > 0)
+        cas_tracer_flux(nt, c.m, c.m > 0, 1, tr, orig(m, a), orig(m, b), tip + (size_t)e * 2 * nt,
+                        tfluxes + (size_t)e * nt);
       continue;
     }
     if (action == 0 || action == 3) {
@@ -1343,10 +1368,51 @@ int ro_cas_flux(const rg_mesh_view* m, const double* cells, const double* ev, do
       l = rr = to_prim(g, aux ? c0 : c1);
     }
     rc = rotate_solve_rotate_back(l, rr, v, n, p, &c, e, err);
-    if (!rc) put_flux(fluxes + 4 * e, c);
+    if (rc) break;
+    put_flux(fluxes + 4 * e, c);
+    if (nt > 0) {
+      /* RegularFlux: the upwind cell (condition_action_sequence.cpp:110-114);
+       * RegularFlux2: the upwind face value (condition_action_sequence_2.cpp:156);
+       * RigidWallFlux, FreeFlowFlux: the aux side's cell (:178, :221);
+       * RigidWallFlux2: the aux side's face value (condition_action_sequence_2.cpp:221) */
+      const int regular = action == 0 || action == 3, face_value = action == 3 || action == 4;
+      cas_tracer_flux(nt, c.m, regular ? c.m > 0 : aux, face_value, tr, orig(m, a), orig(m, b),
+                      tip ? tip + (size_t)e * 2 * nt : NULL, tfluxes + (size_t)e * nt);
+    }
   }
   free(ip);
+  free(tip);
   return rc;
+}
+
+int ro_cas_flux(const rg_mesh_view* m, const double* cells, const double* ev, double g, int order,
+                const ro_lgi_params* lp, const ro_flux_rule* rules, int n_rules, const uint32_t* st,
+                double* fluxes, double* lag_ws, double* lag_ev, ro_error* err) {
+  return ro_cas_flux_tr(m, cells, NULL, ev, g, order, lp, NULL, rules, n_rules, st, fluxes, NULL, lag_ws, lag_ev,
+                        err);
+}
+
+void ro_lagrangian_update_tr(const rg_mesh_view* m, const double* ws, const double* ev, double dt,
+                             const double* areas, double* ext, double* tr_ext, int nt) {
+  for (int i = 0; i < m->n_cells; ++i) {
+    double dv = 0, dvw = 0;
+    for (int k = m->cell_face_offset[i]; k < m->cell_face_offset[i + 1]; ++k) {
+      const int e = m->cell_faces[k];
+      const double area = areas ? areas[e] : edge_length(m, e);
+      if (fc0(m, e) == i) {
+        dv += area * dt * ev[e];
+        dvw += area * dt * ws[e];
+      } else {
+        dv -= area * dt * ev[e];
+        dvw -= area * dt * ws[e];
+      }
+    }
+    const double V = m->cd_volume[i];
+    const double a = (V + dv) / (V + dv + dvw);
+    /* Extensive::operator*= (extensive.cpp:98-107): every component and tracer */
+    for (int c = 0; c < 4; ++c) ext[4 * i + c] *= a;
+    for (int j = 0; j < nt; ++j) tr_ext[(size_t)i * nt + j] *= a;
+  }
 }
 
 void ro_lagrangian_update(const rg_mesh_view* m, const double* ws, const double* ev, double dt,
@@ -1398,6 +1464,39 @@ int ro_step_cas(const rg_mesh_view* m, double* cells, double* ext, const double*
   free(ws);
   free(lev);
   free(old);
+  if (dt_out) *dt_out = dt;
+  return rc;
+}
+
+int ro_step_cas_tr(const rg_mesh_view* m, double* cells, double* ext, double* tr, double* tr_ext, const double* ev,
+                   double g, double cfl, int order, const ro_lgi_params* lp, const ro_flux_rule* rules, int n_rules,
+                   const ro_tracers* t, int lagrangian_update, double* dt_out, ro_error* err) {
+  double dt;
+  int rc = ro_cfl(m, cells, ev, g, cfl, &dt, err);
+  if (rc) return rc;
+  const int nt = t ? t->n : 0;
+  const size_t N = (size_t)m->n_cells;
+  const size_t E = (size_t)(m->n_faces > 0 ? m->n_faces : 1);
+  double* fl = (double*)malloc(sizeof(double) * 4 * E);
+  double* tfl = (double*)malloc(sizeof(double) * E * (nt > 0 ? nt : 1));
+  double* ws = (double*)calloc(E, sizeof(double));
+  double* lev = (double*)calloc(E, sizeof(double));
+  double* old = (double*)malloc(sizeof(double) * 4 * N);
+  double* old_tr = (double*)malloc(sizeof(double) * N * (nt > 0 ? nt : 1));
+  memcpy(old, cells, sizeof(double) * 4 * N);
+  if (nt > 0) memcpy(old_tr, tr, sizeof(double) * N * nt);
+  rc = ro_cas_flux_tr(m, cells, tr, ev, g, order, lp, t, rules, n_rules, t ? t->stickers : NULL, fl, tfl, ws, lev,
+                      err);
+  if (!rc) rc = ro_extensive_update(m, fl, dt, ext, err);
+  if (!rc) ro_extensive_update_tr(m, tfl, nt, dt, tr_ext);
+  if (!rc && lagrangian_update) ro_lagrangian_update_tr(m, ws, lev, dt, NULL, ext, tr_ext, nt);
+  if (!rc) rc = ro_cell_update_tr(m, ext, tr_ext, old, old_tr, g, t, cells, tr, err);
+  free(fl);
+  free(tfl);
+  free(ws);
+  free(lev);
+  free(old);
+  free(old_tr);
   if (dt_out) *dt_out = dt;
   return rc;
 }

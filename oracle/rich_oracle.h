@@ -127,6 +127,15 @@ typedef struct ro_flux_rule {
 int ro_cas_flux(const rg_mesh_view* m, const double* cells, const double* ev, double gamma, int order,
                 const ro_lgi_params* lp, const ro_flux_rule* rules, int n_rules, const uint32_t* stickers,
                 double* fluxes, double* lag_ws, double* lag_ev, ro_error* err);
+/* The same with tracers (t->n of them in tr, n_cells*n): tfluxes (n_faces*n)
+ * receives each face's Mass times the tracers of the side its action takes,
+ * the cell (RegularFlux: upwind; RigidWallFlux, FreeFlowFlux: the aux side)
+ * or LinearGaussImproved's face value (RegularFlux2, LagrangianFlux: upwind;
+ * RigidWallFlux2: the aux side), as conserved_to_extensive forms it. */
+int ro_cas_flux_tr(const rg_mesh_view* m, const double* cells, const double* tr, const double* ev, double gamma,
+                   int order, const ro_lgi_params* lp, const ro_tracers* t, const ro_flux_rule* rules, int n_rules,
+                   const uint32_t* stickers, double* fluxes, double* tfluxes, double* lag_ws, double* lag_ev,
+                   ro_error* err);
 /* LagrangianExtensiveUpdater (LagrangianExtensiveUpdater.cpp:8-80) after the
  * base update: per cell dV = sum area*dt*edge_vel and dv_ws = sum area*dt*ws
  * over its faces (+ as the first neighbour, - as the second, in face order),
@@ -134,12 +143,20 @@ int ro_cas_flux(const rg_mesh_view* m, const double* cells, const double* ev, do
  * volume; areas NULL = the edge lengths (SlabSymmetry) */
 void ro_lagrangian_update(const rg_mesh_view* m, const double* lag_ws, const double* lag_ev, double dt,
                           const double* areas, double* ext);
+/* the same factor on the nt extensive tracers too (Extensive::operator*=) */
+void ro_lagrangian_update_tr(const rg_mesh_view* m, const double* lag_ws, const double* lag_ev, double dt,
+                             const double* areas, double* ext, double* tr_ext, int nt);
 /* hdsim::TimeAdvance with a condition/action flux calculator on a fixed
  * mesh; cells with a bit of frozen_mask keep their state (SkipUpdate);
  * lagrangian_update: LagrangianExtensiveUpdater around SimpleExtensiveUpdater */
 int ro_step_cas(const rg_mesh_view* m, double* cells, double* ext, const double* ev, double gamma, double cfl,
                 int order, const ro_lgi_params* lp, const ro_flux_rule* rules, int n_rules, const uint32_t* stickers,
                 uint32_t frozen_mask, int lagrangian_update, double* dt_out, ro_error* err);
+/* ro_step_cas with tracers: the stickers, the calc_tracers mask and the
+ * SkipUpdate sticker come from t */
+int ro_step_cas_tr(const rg_mesh_view* m, double* cells, double* ext, double* tr, double* tr_ext, const double* ev,
+                   double gamma, double cfl, int order, const ro_lgi_params* lp, const ro_flux_rule* rules,
+                   int n_rules, const ro_tracers* t, int lagrangian_update, double* dt_out, ro_error* err);
 
 /* CylindricalSymmetry (physical_geometry.cpp:62-110) about the axis through
  * origin along direction (normalised as Axis does): CacheData's face areas

@@ -17,7 +17,9 @@ import os
 import numpy as np
 import pytest
 
+import oracle
 import richgpu
+import synthetic
 from conftest import GOLDEN, load_golden, set_geometry
 from test_oracle_golden import accumulate, exact
 
@@ -118,3 +120,61 @@ def test_graph_steps_equal_plain_steps(name):
             out.append((h.get_extensive_tracers(), h.get_tracers()))
     exact(out[0][0], out[1][0])
     exact(out[0][1], out[1][1])
+
+
+def tracer_field(mesh, seed):
+    rng = np.random.default_rng(seed)
+    xy = mesh.point_xy[:mesh.n_cells]
+    a = xy[:, 0] + (xy[:, 1] > 0.45) * 0.5
+    z = (np.hypot(xy[:, 0] - 0.3, xy[:, 1] - 0.3) < 0.2).astype(float) + 0.01 * rng.random(mesh.n_cells)
+    return np.stack([a, z], axis=1)
+
+
+# rule tables: CAS2 rigid walls + obstacle faces (RigidWallFlux2) + bulk
+# RegularFlux2; an outflow Ratchet with a CAS first-order wall list; and
+# LagrangianFlux on every face with LagrangianExtensiveUpdater
+LARGE_RULES = {
+    "walls_obstacle": ([[1, 0, -1, 4, 0], [1, 2, 0, 4, 0], [1, 1, -1, 3, 0]], True, False),
+    "ratchet": ([[0, 2, 0, 1, 0], [1, 0, -1, 5, 0], [1, 1, -1, 3, 0]], True, False),
+    "lagrangian": ([[1, 1, -1, 6, 0, 1], [1, 0, -1, 6, 0, 2]], False, True),
+}
+
+
+@pytest.mark.parametrize("case", sorted(LARGE_RULES))
+def test_large_runs_vs_oracle(case):
+    """A 160^2 rigid box with tracers {"A" in calc_tracers, "Z"} under each
+    rule table: 10 fused steps equal the oracle's (ro_step_cas_tr, pinned to
+    the reference's fixtures) bit for bit, tracers included."""
+    rules, obstacle, lag = LARGE_RULES[case]
+    mesh = synthetic.lattice_mesh(160, 160, (0.0, 1.0, 0.0, 1.0), "rigid", seed=27)
+    cells = synthetic.bumps_cells(mesh, seed=27)
+    n = mesh.n_cells
+    xy = mesh.point_xy[:n]
+    st = ((np.hypot(xy[:, 0] - 0.4, xy[:, 1] - 0.55) < 0.12) if obstacle else np.zeros(n, bool)).astype(np.uint32)
+    cells[st == 1, 2:] = 0.0
+    tr = tracer_field(mesh, 27)
+    ext = oracle.init_extensives(mesh, cells, 5 / 3)
+    tr_ext = oracle.init_extensives_tr(mesh, cells, tr)
+    ev = np.zeros((mesh.n_faces, 2))
+    lp = oracle.lgi_params(ghost_kind=0)
+    ts = oracle.TracerSetup(2, limited=0b01, frozen_sticker=0 if obstacle else -1, stickers=st)
+    oc, oe, otr, otr_ext, odts = oracle.run_cas_tr(mesh, cells, ext, tr, tr_ext, ev, 5 / 3, 10, 2, lp, rules, ts,
+                                                   lagrangian_update=lag)
+    with richgpu.Handle(gamma=5 / 3, order=2, ghost_kind=0, device=0) as h:
+        h.upload_mesh(mesh)
+        h.set_tracer_config(2, limited=[0], n_stickers=1, frozen_sticker=0 if obstacle else -1)
+        h.set_stickers(st)
+        h.set_flux_rules(rules)
+        if lag:
+            h.set_lagrangian_updater(True)
+        h.set_cells(cells)
+        h.set_tracers(tr)
+        h.set_extensives(ext)
+        h.set_extensive_tracers(tr_ext)
+        h.set_edge_velocities(ev)
+        exact(h.run(10), odts)
+        exact(h.get_cells(), oc)
+        exact(h.get_extensives(), oe)
+        exact(h.get_tracers(), otr)
+        exact(h.get_extensive_tracers(), otr_ext)
+    assert np.count_nonzero(otr_ext - tr_ext) > n // 10
