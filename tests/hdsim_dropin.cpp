@@ -50,6 +50,10 @@
 //   tracers   the sedov case with tracers {"A", "Entropy", "Z"} and stickers
 //             {"frozen", "skip"} (LinearGaussImproved's calc_tracers {"A"}
 //             and skip_key "skip"; HasSticker("frozen") + SkipUpdate)
+//   cas       the sedov case with ConditionActionSequence2 {(IsBoundaryEdge,
+//             RigidWallFlux2), (IsBulkEdge, RegularFlux2)} as the flux
+//             calculator (the GPU set: the same rule table) and tracers
+//             {"A", "Z"} ("A" in calc_tracers); FP64 only
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -67,6 +71,8 @@
 #include "rich_gpu_adapters.hpp"
 #include "source/newtonian/common/hllc.hpp"
 #include "source/newtonian/common/ideal_gas.hpp"
+#include "source/newtonian/two_dimensional/condition_action_sequence.hpp"
+#include "source/newtonian/two_dimensional/condition_action_sequence_2.hpp"
 #include "source/newtonian/two_dimensional/geometric_outer_boundaries/PeriodicBox.hpp"
 #include "source/newtonian/two_dimensional/geometric_outer_boundaries/SquareBox.hpp"
 #include "source/newtonian/two_dimensional/ghost_point_generators/PeriodicGhostGenerator.hpp"
@@ -205,6 +211,10 @@ struct Sim {
   ZeroForce force;
   std::unique_ptr<GhostPointGenerator> ghosts;
   std::unique_ptr<LinearGaussImproved> sr;
+  // the cas case's conditions and actions (ConditionActionSequence2 keeps
+  // pointers to them)
+  std::unique_ptr<ConditionActionSequence::Condition> c_bnd, c_bulk;
+  std::unique_ptr<ConditionActionSequence2::Action2> a_wall, a_reg;
   // stock plugins
   std::unique_ptr<SimpleCFL> s_tsf;
   std::unique_ptr<FluxCalculator> s_fc;
@@ -242,11 +252,13 @@ double g_perturb = 0;
 std::unique_ptr<Sim> make_sim(const std::string& which, int n, Set set) {
   std::unique_ptr<Sim> s(new Sim);
   const bool tracers = which == "tracers";
+  const bool cas = which == "cas";
   g_entropy = tracers ? 1 : -1;  // sorted names {"A", "Entropy", "Z"}
-  const std::string base = tracers ? "sedov" : which;
+  const std::string base = tracers || cas ? "sedov" : which;
   const TracerStickerNames tsn = tracers ? TracerStickerNames({"A", "Entropy", "Z"}, {"frozen", "skip"})
+                                 : cas   ? TracerStickerNames({"A", "Z"}, {})
                                          : TracerStickerNames();
-  const vector<string> calc_tracers = tracers ? vector<string>{"A"} : vector<string>();
+  const vector<string> calc_tracers = tracers || cas ? vector<string>{"A"} : vector<string>();
   const string skip_key = tracers ? "skip" : "";
   vector<pair<const SimpleCellUpdater::Condition*, const SimpleCellUpdater::Action*> > seq;
   if (tracers) seq.push_back({new HasSticker("frozen"), new SkipUpdate()});
@@ -287,7 +299,18 @@ std::unique_ptr<Sim> make_sim(const std::string& which, int n, Set set) {
     s->evc.reset(new StationaryBox());
     s->ghosts.reset(new RigidWallGenerator());
     s->sr.reset(new LinearGaussImproved(*s->eos, *s->ghosts, true, 0.2, 0.5, 0.7, calc_tracers, skip_key));
-    s->s_fc.reset(new ModularFluxCalculator(*s->sr, s->rs));
+    if (cas) {
+      s->c_bnd.reset(new IsBoundaryEdge());
+      s->c_bulk.reset(new IsBulkEdge());
+      s->a_wall.reset(new RigidWallFlux2(s->rs));
+      s->a_reg.reset(new RegularFlux2(s->rs));
+      const vector<pair<const ConditionActionSequence::Condition*, const ConditionActionSequence::Action*> > seq1;
+      const vector<pair<const ConditionActionSequence::Condition*, const ConditionActionSequence2::Action2*> > seq2 = {
+          {s->c_bnd.get(), s->a_wall.get()}, {s->c_bulk.get(), s->a_reg.get()}};
+      s->s_fc.reset(new ConditionActionSequence2(seq1, seq2, *s->sr));
+    } else {
+      s->s_fc.reset(new ModularFluxCalculator(*s->sr, s->rs));
+    }
     cfg.order = 2;
     cfg.ghost_kind = RG_GHOST_RIGID_WALL;
     const double rdep = std::max(0.02, 1.5 * 2.0 / n);
@@ -299,6 +322,11 @@ std::unique_ptr<Sim> make_sim(const std::string& which, int n, Set set) {
       ic[i].density = 1;
       ic[i].pressure = abs(s->tess->GetMeshPoint(static_cast<int>(i))) < rdep ? (gamma - 1) / vin : 1e-6;
     }
+    if (cas)
+      for (size_t i = 0; i < ic.size(); ++i) {
+        const Vector2D r = s->tess->GetMeshPoint(static_cast<int>(i));
+        ic[i].tracers = {r.x + (r.y > 0.1 ? 0.5 : 0.0), abs(r) < 0.3 ? 1.0 : 0.0};
+      }
     if (tracers)
       for (size_t i = 0; i < ic.size(); ++i) {
         const Vector2D r = s->tess->GetMeshPoint(static_cast<int>(i));
@@ -357,6 +385,12 @@ std::unique_ptr<Sim> make_sim(const std::string& which, int n, Set set) {
   if (set != kStock) {
     s->ctx.reset(new rich_gb300::GpuContext(cfg, spec));
     if (g_device_geometry) s->ctx->set_outer_boundary(*s->outer);
+    if (cas) {
+      if (set == kGpu32) throw std::runtime_error("the cas case runs the FP64 plugins only");
+      // {sequence, condition, sticker, action, ratchet_in, massflux}
+      s->ctx->set_flux_rules({{1, RG_COND_BOUNDARY_EDGE, -1, RG_ACT_RIGID_WALL2, 0, 0},
+                              {1, RG_COND_BULK_EDGE, -1, RG_ACT_REGULAR2, 0, 0}});
+    }
     s->g_tsf.reset(new rich_gb300::GpuCFL(*s->ctx));
     s->g_fc.reset(new rich_gb300::GpuFluxCalculator(*s->ctx));
     s->g_eu.reset(new rich_gb300::GpuExtensiveUpdater(*s->ctx));

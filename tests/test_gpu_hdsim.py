@@ -52,6 +52,10 @@ def run_driver(*args, timeout=900, exe=DRIVER):
     # "Entropy" tracer, p * pow(d, -gamma), within 1e-15 relative: libm's pow
     # against the device's)
     ("tracers", 64, 60, "device"),
+    # Sedov 64^2 with RoundCells and ConditionActionSequence2 (rigid-wall and
+    # regular face-value fluxes; the GPU set: the same rule table) carrying
+    # tracers {"A", "Z"}
+    ("cas", 64, 60, "device"),
 ])
 def test_hdsim_with_gpu_plugins_equals_hdsim_with_reference_plugins(case, n, steps, geometry):
     extra = ["hostgeom"] if geometry == "hostgeom" else []
