@@ -62,3 +62,22 @@ def test_hdsim_run(name):
     exact(cells, g["run_cells"])
     exact(tr_ext, g["tr_run_ext"])
     exact(tr, g["tr_run_cells"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_unit_tracers_carry_the_mass_flux(name):
+    """Tracers that are 1 everywhere move the mass flux across every face,
+    whichever side each action takes: exactly from cell values (first
+    order); from LinearGaussImproved's face values to rounding (the naive
+    slope of a constant is a sum of stencil vectors that cancels only to
+    rounding)."""
+    g = case(name)
+    m = g["mesh"]
+    ones = np.ones((m.n_cells, 2))
+    fl, tfl = oracle.cas_flux_tr(m, g["cells0"], ones, g["ev_flux"], g["gamma"], g["order"], g["lp"],
+                                 g["flux_rules"], g["ts"])
+    for j in range(2):
+        if g["order"] == 1:
+            exact(tfl[:, j], fl[:, 0])
+        else:
+            np.testing.assert_allclose(tfl[:, j], fl[:, 0], rtol=1e-12, atol=1e-15 * np.abs(fl[:, 0]).max())
