@@ -52,3 +52,42 @@ def test_fixture_regenerates_bitwise(name, spec, sub):
         a, b = got[k], want[k]
         assert a.shape == b.shape and a.dtype == b.dtype, k
         assert a.tobytes() == b.tobytes(), k
+
+
+REF_DUMP3D = os.path.join(SCRATCH, "ref_dump3d")
+
+
+@pytest.mark.skipif(not os.path.exists(REF_DUMP3D), reason="ref_dump3d not built here")
+@pytest.mark.parametrize("name", sorted(make_golden.CASES3D))
+def test_3d_fixture_regenerates_bitwise(name):
+    case, nx, ny, nz, run = make_golden.CASES3D[name]
+    with tempfile.TemporaryDirectory(dir=SCRATCH) as d:
+        subprocess.run([REF_DUMP3D, case, d, str(nx), str(ny), str(nz), str(run)], check=True, capture_output=True,
+                       timeout=600)
+        got = {os.path.basename(f)[:-4]: np.load(f) for f in glob.glob(os.path.join(d, "*.npy"))}
+    want = np.load(os.path.join(GOLDEN, "3d", name + ".npz"))
+    keys = set(want.files) - ADDED
+    assert keys == set(got), sorted(keys ^ set(got))
+    for k in sorted(keys):
+        assert got[k].tobytes() == want[k].tobytes() and got[k].shape == want[k].shape, k
+
+
+@pytest.mark.parametrize("name", sorted(make_golden.MESH_PINS))
+def test_mesh_pin_regenerates_bitwise(name):
+    """The reference's VoronoiMesh of synthetic.lattice_mesh's points, packed
+    by ref_dump, as tests/golden/mesh/ holds it."""
+    sys.path.insert(0, os.path.join(ROOT, "huji-rich_gb300"))
+    import synthetic
+    nx, ny, box, boundary, seed = make_golden.MESH_PINS[name]
+    px, py = synthetic.jittered_points(nx, ny, *box, seed)
+    with tempfile.TemporaryDirectory(dir=SCRATCH) as d:
+        np.stack([px.ravel(), py.ravel()], 1).astype("<f8").tofile(os.path.join(d, "points.f64"))
+        np.array(box, dtype="<f8").tofile(os.path.join(d, "box.f64"))
+        subprocess.run([REF_DUMP, "mesh_" + boundary, d, str(nx), str(ny), "0", "0"], check=True,
+                       capture_output=True, timeout=600)
+        got = {os.path.basename(f)[:-4]: np.load(f) for f in glob.glob(os.path.join(d, "*.npy"))}
+    want = np.load(os.path.join(GOLDEN, "mesh", name + ".npz"))
+    keys = set(want.files) - {"case_params", "box"}
+    assert keys == set(got), sorted(keys ^ set(got))
+    for k in sorted(keys):
+        assert got[k].tobytes() == want[k].tobytes() and got[k].shape == want[k].shape, k
